@@ -1,0 +1,219 @@
+"""GB300-native implicit Rosenbrock transport stage of ASAM (All Scale Atmospheric Model).
+
+Python host mirror of the reference's Fortran seams for this path, on top of
+the C-ABI in ``include/asam_gb300.h``.  Method names follow the reference:
+
+=====================  =======================================================
+``Fcn``                FcnMet advection terms (ADVECT/Function_Mod.f90:989)
+``DivCompute``         ADVECT/Advection_Mod.f90:2901
+``Jac``                JacMeteo -> JacAdvectionCompute + JacScaleCompute
+                       (ADVECT/Function_Mod.f90:1508, 1782)
+``MatVecMet``          MODULE/SpMatrix4CellPar_Mod.f90:70
+``PSolve``             MODULE/SpMatrix4CellPar_Mod.f90:86
+``BiCGStabMetSp``      MODULE/SpMatrix4CellPar_Mod.f90:245 (MaxIter/Tol in-out)
+``Ros3MetC``           ADVECT/Int_Mod.f90:1059 (fixed dt)
+``TotalScalar``        ADVECT/Diagnostic_Mod.f90:13
+``ExchangeCell``       MODULE/Vector4CellPar_Mod.f90:752
+``Solve_1D``           MULTI/TriDiagT_Mod.f90:135 (batched over columns)
+``MatVecT_1D``         MULTI/TriDiagT_Mod.f90:113 (batched over columns)
+=====================  =======================================================
+
+Fields are numpy arrays in the Fortran layout (ix fastest): a state is
+``(ncomp, nz+2, ny+2, nx+2)`` float64, C-contiguous.  All compute runs in the
+CUDA library; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import ASAM_BREAKDOWN, ASAM_NOT_CONVERGED, ASAM_OK, AsamConfig, AsamError, check, ptr
+
+METHODS = {"Ros3AMF": 0, "RosRK32": 1, "RosEul": 2, "Ros3P": 3, "Ros3Pw": 4, "RosRK3": 5, "RosTVD": 6,
+           "RosRK4": 7}
+PRECISIONS = {"fp64": 0, "fp32_refined": 1}
+
+__all__ = ["TransportBlock", "Solve_1D", "MatVecT_1D", "ros_coeffs", "METHODS", "PRECISIONS", "AsamError"]
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def ros_coeffs(method: str | int):
+    """InitRos3MetC coefficient tables (ADVECT/Int_Mod.f90:78-261): (nStage, beta0, alpha, beta, gamma1)."""
+    lib = _lib.load()
+    m = METHODS[method] if isinstance(method, str) else int(method)
+    b0 = C.c_double()
+    al = np.zeros(16)
+    be = np.zeros(16)
+    gm = np.zeros(5)
+    n = lib.asam_ros_coeffs(m, C.byref(b0), al.ctypes.data_as(_lib._D), be.ctypes.data_as(_lib._D),
+                            gm.ctypes.data_as(_lib._D))
+    if n <= 0:
+        raise ValueError(f"unknown Rosenbrock method {method!r}")
+    return n, b0.value, al.reshape(4, 4), be.reshape(4, 4), gm
+
+
+class TransportBlock:
+    """One ASAM block (``Floor(ib)``) resident on the GPU: geometry, face velocities,
+    the 7-diagonal stage matrix and the Krylov work space."""
+
+    def __init__(self, geo, ncomp: int, rho_pos: int = 0, method: str = "RosRK3", bicgstab_tol: float = 1e-6,
+                 bicgstab_maxiter: int = 30, gs_iter: int = 5, precision: str = "fp64"):
+        self.lib = _lib.load()
+        g = geo.grid
+        self.grid = g
+        self.ncomp = ncomp
+        self.cfg = AsamConfig(g.nx, g.ny, g.nz, int(g.periodic_x), int(g.periodic_y), int(g.periodic_z), ncomp,
+                              rho_pos, METHODS[method], bicgstab_maxiter, bicgstab_tol, gs_iter,
+                              PRECISIONS[precision])
+        self._geo = [_f64(geo.volc), _f64(geo.fu), _f64(geo.fv), _f64(geo.fw)]
+        h = C.c_void_p()
+        check(self.lib.asam_create(C.byref(self.cfg), *(ptr(a) for a in self._geo), C.byref(h)), "asam_create")
+        self.h = h
+        self.nstage = ros_coeffs(method)[0]
+
+    # -- lifetime -------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.asam_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def state_shape(self):
+        g = self.grid
+        return (self.ncomp, g.nz + 2, g.ny + 2, g.nx + 2)
+
+    def _state(self, c) -> np.ndarray:
+        a = _f64(c)
+        if a.size != self.ncomp * self.grid.npad:
+            raise ValueError(f"state must have {self.ncomp}*npad elements")
+        return a
+
+    def set_stream(self, stream_handle: int | None):
+        check(self.lib.asam_set_stream(self.h, stream_handle or None), "asam_set_stream")
+
+    def state_device_ptr(self) -> int:
+        p = C.c_void_p()
+        check(self.lib.asam_state_device_ptr(self.h, C.byref(p)), "asam_state_device_ptr")
+        return p.value
+
+    def synchronize(self):
+        check(self.lib.asam_synchronize(self.h), "asam_synchronize")
+
+    # -- reference seams ------------------------------------------------------------
+    def set_velocity(self, uf, vf, wf):
+        self._vel = [_f64(uf), _f64(vf), _f64(wf)]
+        check(self.lib.asam_set_velocity(self.h, *(ptr(a) for a in self._vel)), "asam_set_velocity")
+
+    def ExchangeCell(self, c: np.ndarray, ncomp: int | None = None) -> np.ndarray:
+        a = _f64(c).copy()
+        n = ncomp if ncomp is not None else a.size // self.grid.npad
+        check(self.lib.asam_exchange_cell(self.h, n, ptr(a)), "asam_exchange_cell")
+        return a
+
+    def Fcn(self, c: np.ndarray) -> np.ndarray:
+        a = self._state(c)
+        f = np.empty_like(a)
+        check(self.lib.asam_fcn(self.h, ptr(a), ptr(f)), "asam_fcn")
+        return f
+
+    def DivCompute(self, rhs: np.ndarray) -> np.ndarray:
+        a = _f64(rhs).copy()
+        check(self.lib.asam_div(self.h, ptr(a)), "asam_div")
+        return a
+
+    def Jac(self, c: np.ndarray, dt: float):
+        a = self._state(c)
+        check(self.lib.asam_jac(self.h, ptr(a), float(dt)), "asam_jac")
+
+    def jac_matrix(self) -> np.ndarray:
+        val = np.empty((7, self.grid.npad))
+        check(self.lib.asam_get_jac(self.h, ptr(val)), "asam_get_jac")
+        return val
+
+    def set_jac_matrix(self, val: np.ndarray):
+        v = _f64(val)
+        check(self.lib.asam_set_jac(self.h, ptr(v)), "asam_set_jac")
+
+    def MatVecMet(self, x: np.ndarray) -> np.ndarray:
+        a = self._state(x)
+        y = np.empty_like(a)
+        check(self.lib.asam_matvec(self.h, ptr(a), ptr(y)), "asam_matvec")
+        return y
+
+    def PSolve(self, x: np.ndarray) -> np.ndarray:
+        a = self._state(x)
+        y = np.empty_like(a)
+        check(self.lib.asam_psolve(self.h, ptr(a), ptr(y)), "asam_psolve")
+        return y
+
+    def BiCGStabMetSp(self, x: np.ndarray, b: np.ndarray, MaxIter: int, Tol: float):
+        """Solve A x = b in place of x; returns (MaxIter, Tol) with the reference's
+        sentinels (negative: converged at the half step; 2*Iter: limit hit)."""
+        if not (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous):
+            raise TypeError("x must be a C-contiguous float64 array (updated in place)")
+        bb = self._state(b)
+        it = C.c_int(int(MaxIter))
+        tol = C.c_double(float(Tol))
+        st = self.lib.asam_bicgstab(self.h, ptr(x), ptr(bb), C.byref(it), C.byref(tol))
+        check(st, "asam_bicgstab", allow=(ASAM_OK, ASAM_NOT_CONVERGED, ASAM_BREAKDOWN))
+        return it.value, tol.value
+
+    def Ros3MetC(self, c: np.ndarray, dt: float):
+        """One fixed-dt Rosenbrock step of state c (updated in place).  Returns the
+        per-stage BiCGStab (MaxIter, Tol) outputs."""
+        if not (isinstance(c, np.ndarray) and c.dtype == np.float64 and c.flags.c_contiguous):
+            raise TypeError("c must be a C-contiguous float64 array (updated in place)")
+        iters = (C.c_int * 4)()
+        resid = (C.c_double * 4)()
+        st = self.lib.asam_ros_step(self.h, ptr(c), float(dt), iters, resid)
+        check(st, "asam_ros_step", allow=(ASAM_OK, ASAM_NOT_CONVERGED, ASAM_BREAKDOWN))
+        return [iters[i] for i in range(self.nstage)], [resid[i] for i in range(self.nstage)]
+
+    def ros_step_device(self, dptr: int, dt: float):
+        """Rosenbrock step on a device-resident state (no host copies)."""
+        iters = (C.c_int * 4)()
+        resid = (C.c_double * 4)()
+        st = self.lib.asam_ros_step(self.h, C.c_void_p(dptr), float(dt), iters, resid)
+        check(st, "asam_ros_step", allow=(ASAM_OK, ASAM_NOT_CONVERGED, ASAM_BREAKDOWN))
+        return [iters[i] for i in range(self.nstage)], [resid[i] for i in range(self.nstage)]
+
+    def TotalScalar(self, c: np.ndarray, comp: int = 0) -> float:
+        a = self._state(c)
+        out = C.c_double()
+        check(self.lib.asam_total_scalar(self.h, ptr(a), int(comp), C.byref(out)), "asam_total_scalar")
+        return out.value
+
+
+def Solve_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Thomas solve of a batch of columns: d,b (ncol,n1); u,l (ncol,n1-1)."""
+    lib = _lib.load()
+    d, u, l, x = _f64(d), _f64(u), _f64(l), _f64(b).copy()
+    ncol, n1 = d.shape
+    check(lib.asam_tri_solve(ncol, n1, ptr(d), ptr(u), ptr(l), ptr(x)), "asam_tri_solve")
+    return x
+
+
+def MatVecT_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, x: np.ndarray) -> np.ndarray:
+    lib = _lib.load()
+    d, u, l, xx = _f64(d), _f64(u), _f64(l), _f64(x)
+    ncol, n1 = d.shape
+    y = np.empty_like(xx)
+    check(lib.asam_tri_matvec(ncol, n1, ptr(d), ptr(u), ptr(l), ptr(xx), ptr(y)), "asam_tri_matvec")
+    return y

@@ -1,0 +1,108 @@
+"""ctypes binding of libasam_gb300.so (the C-ABI declared in include/asam_gb300.h).
+
+The library is built in-tree by :func:`asam_gb300.build.build_library`.  There
+is no CPU fallback: if the library or a CUDA device is missing, the calls
+raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libasam_gb300.so"
+
+STATUS = {
+    0: "ASAM_OK",
+    1: "ASAM_NOT_CONVERGED",
+    2: "ASAM_BREAKDOWN",
+    3: "ASAM_NAN_DETECTED",
+    4: "ASAM_BAD_ARG",
+    5: "ASAM_CUDA_ERROR",
+    6: "ASAM_NO_DEVICE",
+}
+ASAM_OK, ASAM_NOT_CONVERGED, ASAM_BREAKDOWN = 0, 1, 2
+
+
+class AsamConfig(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("periodic_x", C.c_int), ("periodic_y", C.c_int), ("periodic_z", C.c_int),
+        ("ncomp", C.c_int), ("rho_pos", C.c_int), ("method", C.c_int),
+        ("bicgstab_maxiter", C.c_int), ("bicgstab_tol", C.c_double), ("gs_iter", C.c_int),
+        ("precision", C.c_int),
+    ]
+
+
+# (name, restype, argtypes) of every exported entry point of include/asam_gb300.h
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_V = C.c_void_p
+SIGNATURES = [
+    ("asam_create", C.c_int, [C.POINTER(AsamConfig), _V, _V, _V, _V, C.POINTER(C.c_void_p)]),
+    ("asam_destroy", C.c_int, [_V]),
+    ("asam_set_stream", C.c_int, [_V, _V]),
+    ("asam_state_device_ptr", C.c_int, [_V, C.POINTER(C.c_void_p)]),
+    ("asam_synchronize", C.c_int, [_V]),
+    ("asam_set_velocity", C.c_int, [_V, _V, _V, _V]),
+    ("asam_exchange_cell", C.c_int, [_V, C.c_int, _V]),
+    ("asam_fcn", C.c_int, [_V, _V, _V]),
+    ("asam_div", C.c_int, [_V, _V]),
+    ("asam_jac", C.c_int, [_V, _V, C.c_double]),
+    ("asam_get_jac", C.c_int, [_V, _V]),
+    ("asam_set_jac", C.c_int, [_V, _V]),
+    ("asam_matvec", C.c_int, [_V, _V, _V]),
+    ("asam_psolve", C.c_int, [_V, _V, _V]),
+    ("asam_bicgstab", C.c_int, [_V, _V, _V, _I, _D]),
+    ("asam_ros_step", C.c_int, [_V, _V, C.c_double, _I, _D]),
+    ("asam_total_scalar", C.c_int, [_V, _V, C.c_int, _D]),
+    ("asam_tri_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
+    ("asam_tri_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
+    ("asam_ros_coeffs", C.c_int, [C.c_int, _D, _D, _D, _D]),
+    ("asam_npad", C.c_longlong, [C.POINTER(AsamConfig)]),
+    ("asam_probe_fp64_fma", C.c_int, [C.c_int, _D]),
+    ("asam_launch_count", C.c_longlong, []),
+    ("asam_last_error", C.c_char_p, []),
+]
+
+_lib = None
+
+
+def load(path: Path | str | None = None) -> C.CDLL:
+    """Load the library (once).  Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with asam_gb300.build.build_library() "
+                           "(there is no CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class AsamError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        lib = load()
+        msg = lib.asam_last_error().decode(errors="replace")
+        super().__init__(f"{where}: {STATUS.get(status, status)} {msg}")
+        self.status = status
+
+
+def check(status: int, where: str, allow=(ASAM_OK,)) -> int:
+    if status not in allow:
+        raise AsamError(status, where)
+    return status
+
+
+def ptr(a: np.ndarray) -> int:
+    """Address of a C-contiguous float64 array."""
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous float64 numpy array")
+    return a.ctypes.data

@@ -1,0 +1,121 @@
+// Shared definitions of the GB300 transport-stage library.
+//
+// Memory layout in HBM is the Fortran layout of ASAM, so a Fortran caller can
+// hand its arrays over without reshuffling:
+//   cell fields   c(ix0:ix1+1, iy0:iy1+1, iz0:iz1+1)  (MODULE/Vector4Cell_Mod.f90:913-926)
+//                 padded (i,j,k) -> i + NX*(j + NY*k), NX=nx+2, NY=ny+2
+//   face areas    FU(ix0-1:ix1+1, iy0+1:iy1, iz0+1:iz1) etc. (MODULE/Domain_Mod.f90:447-449)
+//   volumes       VolC(ix0:ix1+1, iy0:iy1+1, iz0:iz1+1)     (MODULE/Domain_Mod.f90:460)
+//   face velocity uF(ix0:ix1, iy0+1:iy1, iz0+1:iz1) etc.   (MODULE/VelocityFace_Mod.f90:211-213)
+//   DIA matrix    Val(m,7) column-major, offsets -NXY,-NX,-1,0,1,NX,NXY
+//                 (MODULE/Vector4Cell_Mod.f90:1020-1036)
+// Several components are stored back to back: comp ic at c + ic*npad.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace asam {
+
+constexpr double kEps = 1.0e-30;  // Eps of CG/Kind_Mod_gf.f90
+constexpr int kMaxComp = 16;
+
+struct Dims {
+  int nx, ny, nz;        // interior cells
+  int per_x, per_y, per_z;  // 1 = periodic side pair (block is its own neighbour), 0 = closed wall
+  __host__ __device__ int NX() const { return nx + 2; }
+  __host__ __device__ int NY() const { return ny + 2; }
+  __host__ __device__ int NZ() const { return nz + 2; }
+  __host__ __device__ size_t npad() const { return (size_t)(nx + 2) * (ny + 2) * (nz + 2); }
+  __host__ __device__ size_t P(int i, int j, int k) const {
+    return (size_t)i + (size_t)(nx + 2) * ((size_t)j + (size_t)(ny + 2) * (size_t)k);
+  }
+  // native Fortran extents of the face arrays
+  __host__ __device__ size_t FU(int i, int j, int k) const {
+    return (size_t)(i + 1) + (size_t)(nx + 3) * ((size_t)(j - 1) + (size_t)ny * (size_t)(k - 1));
+  }
+  __host__ __device__ size_t FV(int i, int j, int k) const {
+    return (size_t)(i - 1) + (size_t)nx * ((size_t)(j + 1) + (size_t)(ny + 3) * (size_t)(k - 1));
+  }
+  __host__ __device__ size_t FW(int i, int j, int k) const {
+    return (size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)(k + 1));
+  }
+  __host__ __device__ size_t UF(int i, int j, int k) const {
+    return (size_t)i + (size_t)(nx + 1) * ((size_t)(j - 1) + (size_t)ny * (size_t)(k - 1));
+  }
+  __host__ __device__ size_t VF(int i, int j, int k) const {
+    return (size_t)(i - 1) + (size_t)nx * ((size_t)j + (size_t)(ny + 1) * (size_t)(k - 1));
+  }
+  __host__ __device__ size_t WF(int i, int j, int k) const {
+    return (size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)k);
+  }
+  size_t n_fu() const { return (size_t)(nx + 3) * ny * nz; }
+  size_t n_fv() const { return (size_t)nx * (ny + 3) * nz; }
+  size_t n_fw() const { return (size_t)nx * ny * (nz + 3); }
+  size_t n_uf() const { return (size_t)(nx + 1) * ny * nz; }
+  size_t n_vf() const { return (size_t)nx * (ny + 1) * nz; }
+  size_t n_wf() const { return (size_t)nx * ny * (nz + 1); }
+};
+
+// Geometry and prescribed face velocities resident on the device.
+template <typename T>
+struct GeomT {
+  const T* volc;
+  const T* fu;
+  const T* fv;
+  const T* fw;
+  const T* uf;
+  const T* vf;
+  const T* wf;
+};
+
+// Krylov scalars that stay on the device between kernels.
+struct KrylovScalars {
+  double rho, rho_old, alpha, beta, omega;
+  double rnorm, rnorm0, tol;
+  double dot_a, dot_b;
+  int done;       // 0 running; 1 converged at half step; 2 converged; 3 breakdown
+  int iter;
+};
+
+// What a reduction's final kernel does with the sum (Krylov recurrences of
+// BiCGStabMet_Vec4CellSp, MODULE/SpMatrix4CellPar_Mod.f90:283-338).
+enum ScalarOp {
+  OP_STORE_A = 0,     // dot_a = sum
+  OP_STORE_B = 1,     // dot_b = sum
+  OP_RNORM0 = 2,      // rnorm0 = sqrt(sum)
+  OP_RHO = 3,         // rho_old = rho; rho = sum; breakdown flag if rho == 0
+  OP_ALPHA = 4,       // alpha = rho / sum
+  OP_RNORM_HALF = 5,  // rnorm = sqrt(sum); converged-at-half-step flag
+  OP_OMEGA = 6,       // omega = dot_a / sum   (dot_a = (t,r), sum = (t,t))
+  OP_RNORM_FULL = 7,  // rnorm = sqrt(sum); converged flag
+};
+// Which device scalar scales an update.
+enum ScalarSel { SEL_ALPHA = 0, SEL_OMEGA = 1, SEL_BETA = 2 };
+
+// Error codes of the C-ABI (mirrored in include/asam_gb300.h).
+enum Status {
+  kOk = 0,
+  kNotConverged = 1,
+  kBreakdown = 2,
+  kNanDetected = 3,
+  kBadArg = 4,
+  kCudaError = 5,
+  kNoDevice = 6,
+};
+
+}  // namespace asam
+
+#define ASAM_CUDA_OK(expr)                                   \
+  do {                                                       \
+    cudaError_t _e = (expr);                                 \
+    if (_e != cudaSuccess) {                                 \
+      asam::set_last_error(cudaGetErrorString(_e), __FILE__, __LINE__); \
+      return asam::kCudaError;                               \
+    }                                                        \
+  } while (0)
+
+namespace asam {
+void set_last_error(const char* msg, const char* file, int line);
+inline int grid_for(size_t n, int block) { return (int)((n + block - 1) / block); }
+}  // namespace asam

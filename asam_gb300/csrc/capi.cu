@@ -1,0 +1,874 @@
+// C-ABI of the GB300 transport-stage library: context, staging of host
+// pointers, and the host-side drivers of BiCGStab, the preconditioner and the
+// Rosenbrock stage.  The drivers keep every Krylov scalar on the device; the
+// host only reads the convergence flag twice per iteration.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "asam_common.cuh"
+#include "asam_gb300.h"
+#include "launch.h"
+
+#include <atomic>
+
+namespace asam {
+static std::atomic<long long> g_launches{0};
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+static thread_local std::string g_last_error;
+void set_last_error(const char* msg, const char* file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s (%s:%d)", msg, file, line);
+  g_last_error = buf;
+}
+}  // namespace asam
+
+using namespace asam;
+
+namespace {
+
+template <typename T>
+struct Work {
+  T *r = nullptr, *rt = nullptr, *rh = nullptr, *p = nullptr, *ph = nullptr, *t = nullptr, *v = nullptr;
+  T *bbuf = nullptr, *tbuf = nullptr;
+};
+
+template <typename T>
+cudaError_t alloc_work(Work<T>& w, size_t len) {
+  T** ptrs[] = {&w.r, &w.rt, &w.rh, &w.p, &w.ph, &w.t, &w.v, &w.bbuf, &w.tbuf};
+  for (T** q : ptrs) {
+    cudaError_t e = cudaMalloc((void**)q, len * sizeof(T));
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+template <typename T>
+void free_work(Work<T>& w) {
+  T* ptrs[] = {w.r, w.rt, w.rh, w.p, w.ph, w.t, w.v, w.bbuf, w.tbuf};
+  for (T* q : ptrs)
+    if (q) cudaFree(q);
+  w = Work<T>();
+}
+
+// Host restatement of InitRos3MetC's coefficient tables (ADVECT/Int_Mod.f90:78-261).
+int ros_coeffs(int method, double* beta0_out, double alpha[16], double beta[16], double gamma1[5]) {
+  double a[4][4] = {{0}}, b[4][4] = {{0}}, gm[5] = {0};
+  double beta0 = 0;
+  int nStage = 0;
+  auto scale_all = [&]() {
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) {
+        a[i][j] *= beta0;
+        b[i][j] *= beta0;
+      }
+  };
+  switch (method) {
+    case ASAM_ROS3AMF:
+      nStage = 2;
+      beta0 = (double)(0.5f + sqrtf(3.0f) / 6.0f);  // single-precision literals in the Fortran
+      a[0][0] = 2.0 / 3.0;
+      a[1][0] = 5.0 / 4.0;
+      a[1][1] = 3.0 / 4.0;
+      b[1][0] = -4.0 / 3.0;
+      gm[1] = 0.666666666666667;
+      gm[2] = 1.0;
+      break;
+    case ASAM_ROSRK32: {
+      nStage = 3;
+      double theta = 1.0 / 3.0 * atan(sqrt(2.0) / 4.0);
+      beta0 = 1.0 - 0.5 * sqrt(2.0) * cos(theta) + 0.5 * sqrt(6.0) * sin(theta);
+      double g32 = 0.5 - 3.0 * beta0;
+      double g31 = -(6.0 * beta0 * beta0 * beta0 - 12.0 * beta0 * beta0 + 6.0 * (1.0 + g32) * beta0 + 2.0 * g32 * g32 - 0.5) /
+                   (1.0 + 2.0 * g32);
+      double g21 = -(3.0 * beta0 + g31 + g32);
+      double tt[3][3] = {{1.0, 0, 0}, {-g21 / beta0, 1.0, 0}, {-g31 / beta0 + g32 * g21 / (beta0 * beta0), -g32 / beta0, 1.0}};
+      double al[3][3] = {{0.5, 0, 0}, {0.5, 0.5, 0}, {1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0}};
+      double be[3][3] = {{0, 0, 0}, {g21 / beta0, 0, 0}, {g31 / beta0, g32 / beta0, 0}};
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double s = 0.0, s2 = 0.0;
+          for (int k = 0; k < 3; ++k) {
+            s = s + al[i][k] * tt[k][j];
+            s2 = s2 + be[i][k] * tt[k][j];
+          }
+          a[i][j] = s;
+          b[i][j] = s2;
+        }
+      gm[2] = 1.0;
+      break;
+    }
+    case ASAM_ROSEUL:
+      beta0 = 1.0;
+      nStage = 1;
+      a[0][0] = 1.0;
+      gm[1] = 1.0;
+      break;
+    case ASAM_ROS3P:
+      nStage = 3;
+      beta0 = 7.886751345948129e-1;
+      a[0][0] = 1.267949192431123;
+      a[1][0] = 1.267949192431123;
+      a[2][0] = 2.0;
+      a[2][1] = 5.773502691896258e-1;
+      a[2][2] = 4.226497308103742e-1;
+      b[1][0] = -1.607695154586736;
+      b[2][0] = -3.464101615137755;
+      b[2][1] = -1.732050807568877;
+      scale_all();
+      break;
+    case ASAM_ROS3PW:
+      nStage = 3;
+      beta0 = 7.88675134594812865529e-01;
+      a[0][0] = 2.0;
+      a[1][0] = 6.33974596215561403412e-01;
+      a[2][0] = 1.63397459621556140341e+00;
+      a[2][1] = 2.94228634059947813384e-01;
+      a[2][2] = 1.07179676972449078320e+00;
+      b[1][0] = -2.53589838486224561365e+00;
+      b[2][0] = -1.62740473580835520728e+00;
+      b[2][1] = -2.74519052838329002952e-01;
+      scale_all();
+      break;
+    case ASAM_ROSRK3:
+      nStage = 3;
+      beta0 = 1.0;
+      a[0][0] = 1.0 / (3.0 * beta0);
+      a[1][0] = (-1.0 + 12.0 * pow(beta0, 2.0)) / (18.0 * pow(beta0, 2.0) * (-1.0 + 4.0 * beta0));
+      a[1][1] = 1.0 / (2.0 * beta0);
+      a[2][0] = (1.0 - 3.0 * beta0 * (7.0 + 16.0 * beta0 * (-2.0 + 3.0 * beta0))) / (36.0 * pow(beta0, 3.0) * (-1.0 + 4.0 * beta0));
+      a[2][1] = (-1.0 + 12.0 * beta0) / (4.0 * pow(beta0, 2.0));
+      a[2][2] = 1.0 / beta0;
+      b[1][0] = (1.0 - 12.0 * pow(beta0, 2.0)) / (pow(beta0, 2.0) * (-9.0 + 36.0 * beta0));
+      b[2][0] = (-1.0 + 3.0 * beta0 * (7.0 + 16.0 * beta0 * (-2.0 + 3.0 * beta0))) / (36. * pow(beta0, 3.0) * (-1.0 + 4.0 * beta0));
+      b[2][1] = (0.250 - 3.0 * beta0) / pow(beta0, 2.0);
+      scale_all();
+      gm[1] = 1.0 / 3.0;
+      gm[2] = 1.0 / 2.0;
+      gm[3] = 1.0;
+      break;
+    case ASAM_ROSTVD:
+      nStage = 3;
+      beta0 = 0.5;
+      a[0][0] = 1.0 / beta0;
+      a[1][0] = (1.0 + beta0 * (-9.0 + 16.0 * beta0)) / (4. * pow(beta0, 2.0) * (-1.0 + 4.0 * beta0));
+      a[1][1] = 1.0 / (4.0 * beta0);
+      a[2][0] = (1.0 + beta0 * (-3.0 + 2.0 * beta0 * (-17.0 + 44.0 * beta0))) / (12. * pow(beta0, 3.0) * (-1.0 + 4.0 * beta0));
+      a[2][1] = (1.0 + 6.0 * beta0) / (12.0 * pow(beta0, 2.0));
+      a[2][2] = 2.0 / (3. * beta0);
+      b[1][0] = pow(beta0, -2.0) - 4.0 / beta0 + 4.0 / (-1.0 + 4.0 * beta0);
+      b[2][0] = (-1.0 + beta0 * (5.0 + 8.0 * (2.0 - 7.0 * beta0) * beta0)) / (8.0 * pow(beta0, 3.0) * (-1.0 + 4.0 * beta0));
+      b[2][1] = -(1.0 + 4.0 * beta0) / (8. * pow(beta0, 2.0));
+      scale_all();
+      break;
+    case ASAM_ROSRK4:
+      nStage = 4;
+      beta0 = 1.0 / 4.0;
+      a[0][0] = 2.0;
+      a[1][0] = 2.0;
+      a[1][1] = 2.0;
+      a[2][0] = 6.0;
+      a[2][1] = 10.0;
+      a[2][2] = 4.0;
+      a[3][0] = 14.0 / 3.0;
+      a[3][1] = 20.0 / 3.0;
+      a[3][2] = 4.0 / 3.0;
+      a[3][3] = 2.0 / 3.0;
+      b[1][0] = -4.0;
+      b[2][0] = -6.0;
+      b[2][1] = -10.0;
+      b[3][0] = -4.0;
+      b[3][1] = -12.0;
+      scale_all();
+      break;
+    default:
+      return 0;
+  }
+  *beta0_out = beta0;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      alpha[i * 4 + j] = a[i][j];
+      beta[i * 4 + j] = b[i][j];
+    }
+  for (int i = 0; i < 5; ++i) gamma1[i] = gm[i];
+  return nStage;
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+struct asam_ctx {
+  asam_config cfg;
+  Dims d;
+  Launch L;
+  cudaStream_t own_stream = nullptr;
+  size_t npad = 0, len = 0;
+  int nstage = 0;
+  double beta0 = 0, alpha[16], beta[16], gamma1[5];
+  // geometry + velocities (device)
+  double *volc = nullptr, *fu = nullptr, *fv = nullptr, *fw = nullptr, *uf = nullptr, *vf = nullptr, *wf = nullptr;
+  // stage storage
+  double *c = nullptr, *cold = nullptr, *rhs = nullptr, *incr = nullptr, *phi = nullptr;
+  double *gx = nullptr, *gy = nullptr, *gz = nullptr;
+  double* val = nullptr;
+  float* val32 = nullptr;
+  Work<double> w64;
+  Work<float> w32;
+  float *x32 = nullptr, *b32 = nullptr;
+  double* dcorr = nullptr;
+  KrylovScalars* sc = nullptr;
+  KrylovScalars* sc_host = nullptr;
+  double* partial = nullptr;
+  double* red_out = nullptr;
+  double* red_host = nullptr;
+  double *stage_a = nullptr, *stage_b = nullptr;
+  bool jac_ready = false;
+
+  GeomT<double> geom() const { return GeomT<double>{volc, fu, fv, fw, uf, vf, wf}; }
+};
+
+namespace {
+
+#define CK(expr) ASAM_CUDA_OK(expr)
+
+int check_launch() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+    return kCudaError;
+  }
+  return kOk;
+}
+
+int read_scalars(asam_ctx* h) {
+  CK(cudaMemcpyAsync(h->sc_host, h->sc, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->L.stream));
+  CK(cudaStreamSynchronize(h->L.stream));
+  return kOk;
+}
+
+int reduce_to_host(asam_ctx* h, double* out) {
+  CK(cudaMemcpyAsync(h->red_host, h->red_out, sizeof(double), cudaMemcpyDeviceToHost, h->L.stream));
+  CK(cudaStreamSynchronize(h->L.stream));
+  *out = *h->red_host;
+  return kOk;
+}
+
+// PSolve_Vec4CellSp: copy, exchange, 1+IterG Gauss-Seidel sweeps, zero halo, exchange.
+template <typename T>
+void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w) {
+  const Launch& L = h->L;
+  const Dims& d = h->d;
+  const int nc = h->cfg.ncomp;
+  cudaMemcpyAsync(w.bbuf, in, h->len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream);
+  launch_exchange_cell(L, d, nc, w.bbuf);
+  launch_gs_lower(L, d, nc, val, w.bbuf, out);
+  for (int s = 0; s < h->cfg.gs_iter; ++s) {
+    launch_gs_upper(L, d, nc, val, w.bbuf, out, w.tbuf);
+    launch_gs_lower(L, d, nc, val, w.tbuf, out);
+  }
+  launch_zero_halo(L, d, nc, out);
+  launch_exchange_cell(L, d, nc, out);
+}
+
+// BiCGStabMet_Vec4CellSp (MODULE/SpMatrix4CellPar_Mod.f90:245-348) on the device.
+template <typename T>
+int bicgstab_dev(asam_ctx* h, const T* val, T* x, const T* b, int* maxiter, double* tol, Work<T>& w) {
+  const Launch& L = h->L;
+  const Dims& d = h->d;
+  const int nc = h->cfg.ncomp;
+  const size_t len = h->len;
+  memset(h->sc_host, 0, sizeof(KrylovScalars));
+  h->sc_host->tol = *tol;
+  CK(cudaMemcpyAsync(h->sc, h->sc_host, sizeof(KrylovScalars), cudaMemcpyHostToDevice, L.stream));
+  launch_matvec(L, d, nc, val, x, w.r, 0);
+  launch_xpay_host(L, len, b, (T)-1, w.r);
+  CK(cudaMemcpyAsync(w.rt, w.r, len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream));
+  launch_dot(L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM0, nullptr);
+  const int MaxIter = *maxiter;
+  for (int it = 1; it <= MaxIter; ++it) {
+    launch_dot(L, d, nc, w.rt, w.r, h->partial, h->sc, OP_RHO, nullptr);
+    if (it == 1) {
+      CK(cudaMemcpyAsync(w.p, w.r, len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream));
+    } else {
+      launch_beta(L, h->sc);
+      launch_pupdate(L, len, h->sc, w.r, w.v, w.p);
+    }
+    psolve_dev<T>(h, val, w.p, w.ph, w);
+    launch_matvec(L, d, nc, val, w.ph, w.v, 0);
+    launch_dot(L, d, nc, w.rt, w.v, h->partial, h->sc, OP_ALPHA, nullptr);
+    launch_axpy_sc(L, len, h->sc, SEL_ALPHA, -1.0, w.v, w.r);
+    launch_dot(L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM_HALF, nullptr);
+    int rc = check_launch();
+    if (rc) return rc;
+    rc = read_scalars(h);
+    if (rc) return rc;
+    if (h->sc_host->done == 3) {
+      *maxiter = it;
+      *tol = 0.0;
+      return h->sc_host->rnorm0 > 0.0 ? kBreakdown : kOk;
+    }
+    if (h->sc_host->done == 1) {
+      launch_xupdate(L, len, h->sc, 0, w.ph, (const T*)nullptr, x);
+      *maxiter = -it;
+      *tol = h->sc_host->rnorm;
+      return check_launch();
+    }
+    psolve_dev<T>(h, val, w.r, w.rh, w);
+    launch_matvec(L, d, nc, val, w.rh, w.t, 0);
+    launch_dot(L, d, nc, w.t, w.r, h->partial, h->sc, OP_STORE_A, nullptr);
+    launch_dot(L, d, nc, w.t, w.t, h->partial, h->sc, OP_OMEGA, nullptr);
+    launch_xupdate(L, len, h->sc, 1, w.ph, w.rh, x);
+    launch_axpy_sc(L, len, h->sc, SEL_OMEGA, -1.0, w.t, w.r);
+    launch_dot(L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM_FULL, nullptr);
+    rc = check_launch();
+    if (rc) return rc;
+    rc = read_scalars(h);
+    if (rc) return rc;
+    if (h->sc_host->done == 2) {
+      *maxiter = it;
+      *tol = h->sc_host->rnorm;
+      return kOk;
+    }
+    if (it == MaxIter) {
+      *maxiter = 2 * it;
+      *tol = h->sc_host->rnorm;
+      return kNotConverged;
+    }
+  }
+  *tol = 0.0;
+  return kOk;
+}
+
+// FP32-refined solve: outer FP64 iterative refinement, FP32 inner BiCGStab
+// with the FP32 Gauss-Seidel preconditioner, FP64 residual recomputation and
+// the reference's stopping test ||r|| <= Tol*||r0|| on the FP64 residual.
+int bicgstab_refined(asam_ctx* h, double* x, const double* b, int* maxiter, double* tol) {
+  const Launch& L = h->L;
+  const Dims& d = h->d;
+  const int nc = h->cfg.ncomp;
+  const size_t len = h->len;
+  double* r = h->w64.r;
+  launch_matvec(L, d, nc, h->val, x, r, 0);
+  launch_xpay_host(L, len, b, -1.0, r);
+  launch_dot(L, d, nc, r, r, h->partial, h->sc, OP_STORE_A, h->red_out);
+  double rr0 = 0;
+  int rc = reduce_to_host(h, &rr0);
+  if (rc) return rc;
+  const double rnorm0 = sqrt(rr0);
+  const double target = *tol * rnorm0;
+  if (rnorm0 == 0.0) {
+    *maxiter = 1;
+    *tol = 0.0;
+    return kOk;
+  }
+  double rnorm = rnorm0;
+  int total_inner = 0;
+  const int max_outer = 8;
+  for (int outer = 0; outer < max_outer; ++outer) {
+    launch_convert_f64_to_f32(L, len, r, h->b32);
+    CK(cudaMemsetAsync(h->x32, 0, len * sizeof(float), L.stream));
+    int it = h->cfg.bicgstab_maxiter;
+    double tin = 0.5 * target / rnorm;
+    if (tin < 1e-6) tin = 1e-6;
+    if (tin > 1e-2) tin = 1e-2;
+    rc = bicgstab_dev<float>(h, h->val32, h->x32, h->b32, &it, &tin, h->w32);
+    if (rc != kOk && rc != kNotConverged) return rc;
+    total_inner += it < 0 ? -it : (it > h->cfg.bicgstab_maxiter ? it / 2 : it);
+    launch_convert_f32_to_f64(L, len, h->x32, h->dcorr);
+    launch_axpy_host(L, len, 1.0, h->dcorr, x);
+    launch_matvec(L, d, nc, h->val, x, r, 0);
+    launch_xpay_host(L, len, b, -1.0, r);
+    launch_dot(L, d, nc, r, r, h->partial, h->sc, OP_STORE_A, h->red_out);
+    double rr = 0;
+    rc = reduce_to_host(h, &rr);
+    if (rc) return rc;
+    rnorm = sqrt(rr);
+    if (rnorm <= target) {
+      *maxiter = total_inner;
+      *tol = rnorm;
+      return kOk;
+    }
+  }
+  *maxiter = 2 * total_inner;
+  *tol = rnorm;
+  return kNotConverged;
+}
+
+int fcn_dev(asam_ctx* h, const double* c, double* f) {
+  const Launch& L = h->L;
+  launch_phi(L, h->d, h->cfg.ncomp, h->cfg.rho_pos, c, h->phi);
+  launch_face_flux(L, h->d, h->geom(), h->cfg.ncomp, h->phi, h->gx, h->gy, h->gz);
+  launch_flux_gather(L, h->d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz, f);
+  return check_launch();
+}
+
+int jac_dev(asam_ctx* h, const double* c, double dt) {
+  const double* rho = c + (size_t)h->cfg.rho_pos * h->npad;
+  launch_jac(h->L, h->d, h->geom(), rho, h->beta0 * dt, h->val);
+  if (h->cfg.precision == ASAM_PREC_FP32_REFINED) launch_convert_f64_to_f32(h->L, 7 * h->npad, h->val, h->val32);
+  h->jac_ready = true;
+  return check_launch();
+}
+
+int solve_dev(asam_ctx* h, double* x, const double* b, int* maxiter, double* tol) {
+  if (h->cfg.precision == ASAM_PREC_FP32_REFINED) return bicgstab_refined(h, x, b, maxiter, tol);
+  return bicgstab_dev<double>(h, h->val, x, b, maxiter, tol, h->w64);
+}
+
+// Ros3MetC + StageRos, transport part (ADVECT/Int_Mod.f90:263-374, 1059-1122).
+int ros_step_dev(asam_ctx* h, double* c, double dt, int* iters, double* resid) {
+  const Launch& L = h->L;
+  const Dims& d = h->d;
+  const int nc = h->cfg.ncomp;
+  const size_t len = h->len;
+  int status = kOk;
+  CK(cudaMemcpyAsync(h->cold, c, len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+  for (int is = 0; is < h->nstage; ++is) {
+    launch_exchange_cell(L, d, nc, c);
+    if (is == 0) {
+      int rc = jac_dev(h, c, dt);
+      if (rc) return rc;
+    }
+    int rc = fcn_dev(h, c, h->rhs);
+    if (rc) return rc;
+    launch_scale_host(L, len, dt, h->rhs);
+    for (int js = 0; js < is; ++js) launch_axpy_host(L, len, h->beta[is * 4 + js], h->incr + (size_t)js * len, h->rhs);
+    double* x = h->incr + (size_t)is * len;
+    CK(cudaMemsetAsync(x, 0, len * sizeof(double), L.stream));
+    int it = h->cfg.bicgstab_maxiter;
+    double tol = h->cfg.bicgstab_tol;
+    rc = solve_dev(h, x, h->rhs, &it, &tol);
+    if (rc != kOk && rc != kNotConverged && rc != kBreakdown) return rc;
+    if (rc != kOk && status == kOk) status = rc;
+    if (iters) iters[is] = it;
+    if (resid) resid[is] = tol;
+    launch_exchange_cell(L, d, nc, x);
+    launch_exchange_cell(L, d, nc, x);
+    CK(cudaMemcpyAsync(c, h->cold, len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+    for (int js = 0; js <= is; ++js) launch_axpy_host(L, len, h->alpha[is * 4 + js], h->incr + (size_t)js * len, c);
+  }
+  int rc = check_launch();
+  return rc ? rc : status;
+}
+
+// Staging of a caller pointer: device pointers are used in place, host
+// pointers are copied through the context's staging buffers.
+struct InArg {
+  const double* dev;
+};
+int stage_in(asam_ctx* h, const double* p, size_t n, double* buf, const double** dev) {
+  if (is_device_ptr(p)) {
+    *dev = p;
+    return kOk;
+  }
+  CK(cudaMemcpyAsync(buf, p, n * sizeof(double), cudaMemcpyHostToDevice, h->L.stream));
+  *dev = buf;
+  return kOk;
+}
+int stage_out_begin(asam_ctx* h, double* p, size_t n, double* buf, double** dev, bool copy_in) {
+  if (is_device_ptr(p)) {
+    *dev = p;
+    return kOk;
+  }
+  if (copy_in) CK(cudaMemcpyAsync(buf, p, n * sizeof(double), cudaMemcpyHostToDevice, h->L.stream));
+  *dev = buf;
+  return kOk;
+}
+int stage_out_end(asam_ctx* h, double* p, size_t n, double* dev) {
+  if (dev != p) {
+    CK(cudaMemcpyAsync(p, dev, n * sizeof(double), cudaMemcpyDeviceToHost, h->L.stream));
+    CK(cudaStreamSynchronize(h->L.stream));
+  }
+  return kOk;
+}
+
+int validate(const asam_config* c) {
+  if (!c) return kBadArg;
+  if (c->nx < 1 || c->ny < 1 || c->nz < 1) return kBadArg;
+  if (c->ncomp < 1 || c->ncomp > kMaxComp) return kBadArg;
+  if (c->rho_pos < 0 || c->rho_pos >= c->ncomp) return kBadArg;
+  if (c->bicgstab_maxiter < 1 || c->gs_iter < 0) return kBadArg;
+  if (c->precision != ASAM_PREC_FP64 && c->precision != ASAM_PREC_FP32_REFINED) return kBadArg;
+  return kOk;
+}
+
+}  // namespace
+
+// Scalar FP64 FMA throughput probe: 8 independent chains per thread.
+__global__ void k_probe_fp64(int iters, double seed, double* out) {
+  double a[8];
+  for (int q = 0; q < 8; ++q) a[q] = seed + q + threadIdx.x;
+  const double m = 0.999999, c = 1e-7;
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] = __fma_rn(a[q], m, c);
+  double s = 0;
+  for (int q = 0; q < 8; ++q) s += a[q];
+  if (s == 12345.678) out[0] = s;  // keeps the chains alive
+}
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int asam_probe_fp64_fma(int iters, double* gflops) {
+  if (iters < 1 || !gflops) return kBadArg;
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double* out;
+  CK(cudaMalloc((void**)&out, sizeof(double)));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int blocks = sms * 8, threads = 256;
+  k_probe_fp64<<<blocks, threads>>>(iters / 10 + 1, 1.0, out);  // warm-up
+  CK(cudaEventRecord(e0));
+  k_probe_fp64<<<blocks, threads>>>(iters, 1.0, out);
+  CK(cudaEventRecord(e1));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  *gflops = 2.0 * 8.0 * (double)iters * blocks * threads / (ms * 1e-3) / 1e9;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  return check_launch();
+}
+
+const char* asam_last_error(void) { return g_last_error.c_str(); }
+
+long long asam_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+long long asam_npad(const asam_config* cfg) {
+  if (!cfg) return -1;
+  return (long long)(cfg->nx + 2) * (cfg->ny + 2) * (cfg->nz + 2);
+}
+
+int asam_ros_coeffs(int method, double* beta0, double* alpha, double* beta, double* gamma1) {
+  return ros_coeffs(method, beta0, alpha, beta, gamma1);
+}
+
+int asam_destroy(asam_ctx* h) {
+  if (!h) return kOk;
+  double* dptrs[] = {h->volc, h->fu, h->fv, h->fw, h->uf, h->vf, h->wf, h->c, h->cold, h->rhs, h->incr, h->phi,
+                     h->gx, h->gy, h->gz, h->val, h->dcorr, h->partial, h->red_out, h->stage_a, h->stage_b};
+  for (double* p : dptrs)
+    if (p) cudaFree(p);
+  if (h->val32) cudaFree(h->val32);
+  if (h->x32) cudaFree(h->x32);
+  if (h->b32) cudaFree(h->b32);
+  if (h->sc) cudaFree(h->sc);
+  if (h->sc_host) cudaFreeHost(h->sc_host);
+  if (h->red_host) cudaFreeHost(h->red_host);
+  free_work(h->w64);
+  free_work(h->w32);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+  return kOk;
+}
+
+int asam_create(const asam_config* cfg, const double* volc, const double* fu, const double* fv, const double* fw,
+                asam_ctx** out) {
+  if (!out || validate(cfg) != kOk || !volc || !fu || !fv || !fw) {
+    set_last_error("invalid configuration or null geometry", __FILE__, __LINE__);
+    return kBadArg;
+  }
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_last_error("no CUDA device", __FILE__, __LINE__);
+    return kNoDevice;
+  }
+  asam_ctx* h = new asam_ctx();
+  h->cfg = *cfg;
+  h->d = Dims{cfg->nx, cfg->ny, cfg->nz, cfg->periodic_x ? 1 : 0, cfg->periodic_y ? 1 : 0, cfg->periodic_z ? 1 : 0};
+  h->npad = h->d.npad();
+  h->len = h->npad * (size_t)cfg->ncomp;
+  h->nstage = ros_coeffs(cfg->method, &h->beta0, h->alpha, h->beta, h->gamma1);
+  if (h->nstage <= 0) {
+    delete h;
+    set_last_error("unknown Rosenbrock method", __FILE__, __LINE__);
+    return kBadArg;
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&h->L.sm_count, cudaDevAttrMultiProcessorCount, dev);
+  auto fail = [&](cudaError_t e) {
+    set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+    asam_destroy(h);
+    return (int)kCudaError;
+  };
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  h->L.stream = h->own_stream;
+  const Dims& d = h->d;
+  struct A {
+    double** p;
+    size_t n;
+  } allocs[] = {{&h->volc, h->npad},      {&h->fu, d.n_fu()},        {&h->fv, d.n_fv()},        {&h->fw, d.n_fw()},
+                {&h->uf, d.n_uf()},       {&h->vf, d.n_vf()},        {&h->wf, d.n_wf()},        {&h->c, h->len},
+                {&h->cold, h->len},       {&h->rhs, h->len},         {&h->incr, h->len * h->nstage},
+                {&h->phi, h->len},        {&h->gx, d.n_uf() * cfg->ncomp}, {&h->gy, d.n_vf() * cfg->ncomp},
+                {&h->gz, d.n_wf() * cfg->ncomp}, {&h->val, 7 * h->npad}, {&h->partial, (size_t)kRedGrid},
+                {&h->red_out, 1},         {&h->stage_a, h->len},     {&h->stage_b, h->len}};
+  for (auto& a : allocs)
+    if ((e = cudaMalloc((void**)a.p, a.n * sizeof(double))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc((void**)&h->sc, sizeof(KrylovScalars))) != cudaSuccess) return fail(e);
+  if ((e = cudaMallocHost((void**)&h->sc_host, sizeof(KrylovScalars))) != cudaSuccess) return fail(e);
+  if ((e = cudaMallocHost((void**)&h->red_host, sizeof(double))) != cudaSuccess) return fail(e);
+  if ((e = alloc_work(h->w64, h->len)) != cudaSuccess) return fail(e);
+  if (cfg->precision == ASAM_PREC_FP32_REFINED) {
+    if ((e = alloc_work(h->w32, h->len)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&h->val32, 7 * h->npad * sizeof(float))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&h->x32, h->len * sizeof(float))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&h->b32, h->len * sizeof(float))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&h->dcorr, h->len * sizeof(double))) != cudaSuccess) return fail(e);
+  }
+  struct C {
+    double* dst;
+    const double* src;
+    size_t n;
+  } copies[] = {{h->volc, volc, h->npad}, {h->fu, fu, d.n_fu()}, {h->fv, fv, d.n_fv()}, {h->fw, fw, d.n_fw()}};
+  for (auto& c : copies)
+    if ((e = cudaMemcpy(c.dst, c.src, c.n * sizeof(double), cudaMemcpyDefault)) != cudaSuccess) return fail(e);
+  double* zero[] = {h->uf, h->vf, h->wf};
+  size_t nz[] = {d.n_uf(), d.n_vf(), d.n_wf()};
+  for (int q = 0; q < 3; ++q)
+    if ((e = cudaMemset(zero[q], 0, nz[q] * sizeof(double))) != cudaSuccess) return fail(e);
+  if ((e = cudaMemset(h->c, 0, h->len * sizeof(double))) != cudaSuccess) return fail(e);
+  *out = h;
+  return kOk;
+}
+
+int asam_set_stream(asam_ctx* h, void* stream) {
+  if (!h) return kBadArg;
+  h->L.stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return kOk;
+}
+
+int asam_state_device_ptr(asam_ctx* h, double** dptr) {
+  if (!h || !dptr) return kBadArg;
+  *dptr = h->c;
+  return kOk;
+}
+
+int asam_synchronize(asam_ctx* h) {
+  if (!h) return kBadArg;
+  CK(cudaStreamSynchronize(h->L.stream));
+  return kOk;
+}
+
+int asam_set_velocity(asam_ctx* h, const double* uf, const double* vf, const double* wf) {
+  if (!h || !uf || !vf || !wf) return kBadArg;
+  const Dims& d = h->d;
+  CK(cudaMemcpyAsync(h->uf, uf, d.n_uf() * sizeof(double), cudaMemcpyDefault, h->L.stream));
+  CK(cudaMemcpyAsync(h->vf, vf, d.n_vf() * sizeof(double), cudaMemcpyDefault, h->L.stream));
+  CK(cudaMemcpyAsync(h->wf, wf, d.n_wf() * sizeof(double), cudaMemcpyDefault, h->L.stream));
+  CK(cudaStreamSynchronize(h->L.stream));
+  return kOk;
+}
+
+int asam_exchange_cell(asam_ctx* h, int ncomp, double* c) {
+  if (!h || !c || ncomp < 1 || ncomp > h->cfg.ncomp) return kBadArg;
+  double* dc;
+  size_t n = h->npad * (size_t)ncomp;
+  int rc = stage_out_begin(h, c, n, h->stage_a, &dc, true);
+  if (rc) return rc;
+  launch_exchange_cell(h->L, h->d, ncomp, dc);
+  rc = check_launch();
+  if (rc) return rc;
+  return stage_out_end(h, c, n, dc);
+}
+
+int asam_fcn(asam_ctx* h, const double* c, double* f) {
+  if (!h || !c || !f) return kBadArg;
+  const double* dc;
+  double* df;
+  int rc = stage_in(h, c, h->len, h->stage_a, &dc);
+  if (rc) return rc;
+  rc = stage_out_begin(h, f, h->len, h->stage_b, &df, false);
+  if (rc) return rc;
+  rc = fcn_dev(h, dc, df);
+  if (rc) return rc;
+  return stage_out_end(h, f, h->len, df);
+}
+
+int asam_div(asam_ctx* h, double* rhs) {
+  if (!h || !rhs) return kBadArg;
+  double* dr;
+  int rc = stage_out_begin(h, rhs, h->npad, h->stage_a, &dr, true);
+  if (rc) return rc;
+  launch_div(h->L, h->d, h->geom(), dr);
+  rc = check_launch();
+  if (rc) return rc;
+  return stage_out_end(h, rhs, h->npad, dr);
+}
+
+int asam_jac(asam_ctx* h, const double* c, double dt) {
+  if (!h || !c) return kBadArg;
+  const double* dc;
+  int rc = stage_in(h, c, h->len, h->stage_a, &dc);
+  if (rc) return rc;
+  rc = jac_dev(h, dc, dt);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->L.stream));
+  return kOk;
+}
+
+int asam_get_jac(asam_ctx* h, double* val) {
+  if (!h || !val) return kBadArg;
+  CK(cudaMemcpyAsync(val, h->val, 7 * h->npad * sizeof(double), cudaMemcpyDefault, h->L.stream));
+  CK(cudaStreamSynchronize(h->L.stream));
+  return kOk;
+}
+
+int asam_set_jac(asam_ctx* h, const double* val) {
+  if (!h || !val) return kBadArg;
+  CK(cudaMemcpyAsync(h->val, val, 7 * h->npad * sizeof(double), cudaMemcpyDefault, h->L.stream));
+  if (h->cfg.precision == ASAM_PREC_FP32_REFINED) launch_convert_f64_to_f32(h->L, 7 * h->npad, h->val, h->val32);
+  CK(cudaStreamSynchronize(h->L.stream));
+  h->jac_ready = true;
+  return check_launch();
+}
+
+int asam_matvec(asam_ctx* h, const double* x, double* y) {
+  if (!h || !x || !y) return kBadArg;
+  const double* dx;
+  double* dy;
+  int rc = stage_in(h, x, h->len, h->stage_a, &dx);
+  if (rc) return rc;
+  rc = stage_out_begin(h, y, h->len, h->stage_b, &dy, false);
+  if (rc) return rc;
+  launch_matvec(h->L, h->d, h->cfg.ncomp, h->val, dx, dy, 0);
+  rc = check_launch();
+  if (rc) return rc;
+  return stage_out_end(h, y, h->len, dy);
+}
+
+int asam_psolve(asam_ctx* h, const double* x, double* px) {
+  if (!h || !x || !px) return kBadArg;
+  const double* dx;
+  double* dp;
+  int rc = stage_in(h, x, h->len, h->stage_a, &dx);
+  if (rc) return rc;
+  rc = stage_out_begin(h, px, h->len, h->stage_b, &dp, false);
+  if (rc) return rc;
+  psolve_dev<double>(h, h->val, dx, dp, h->w64);
+  rc = check_launch();
+  if (rc) return rc;
+  return stage_out_end(h, px, h->len, dp);
+}
+
+int asam_bicgstab(asam_ctx* h, double* x, const double* b, int* maxiter, double* tol) {
+  if (!h || !x || !b || !maxiter || !tol || *maxiter < 1) return kBadArg;
+  const double* db;
+  double* dx;
+  int rc = stage_in(h, b, h->len, h->stage_a, &db);
+  if (rc) return rc;
+  rc = stage_out_begin(h, x, h->len, h->stage_b, &dx, true);
+  if (rc) return rc;
+  int st = solve_dev(h, dx, db, maxiter, tol);
+  if (st != kOk && st != kNotConverged && st != kBreakdown) return st;
+  rc = stage_out_end(h, x, h->len, dx);
+  return rc ? rc : st;
+}
+
+int asam_ros_step(asam_ctx* h, double* c, double dt, int* iters, double* resid) {
+  if (!h || !c) return kBadArg;
+  double* dc;
+  int rc = stage_out_begin(h, c, h->len, h->c, &dc, true);
+  if (rc) return rc;
+  int st = ros_step_dev(h, dc, dt, iters, resid);
+  if (st != kOk && st != kNotConverged && st != kBreakdown) return st;
+  rc = stage_out_end(h, c, h->len, dc);
+  return rc ? rc : st;
+}
+
+int asam_total_scalar(asam_ctx* h, const double* c, int comp, double* out) {
+  if (!h || !c || !out || comp < 0 || comp >= h->cfg.ncomp) return kBadArg;
+  const double* dc;
+  int rc = stage_in(h, c, h->len, h->stage_a, &dc);
+  if (rc) return rc;
+  launch_mass(h->L, h->d, dc + (size_t)comp * h->npad, h->volc, h->partial, h->red_out);
+  rc = check_launch();
+  if (rc) return rc;
+  return reduce_to_host(h, out);
+}
+
+int asam_tri_solve(int ncol, int n1, const double* d, const double* u, const double* l, double* b) {
+  if (ncol < 1 || n1 < 1 || !d || !b || (n1 > 1 && (!u || !l))) return kBadArg;
+  size_t nd = (size_t)ncol * n1, no = (size_t)ncol * (n1 - 1);
+  double *dd, *du = nullptr, *dl = nullptr, *db, *dw;
+  CK(cudaMalloc((void**)&dd, nd * sizeof(double)));
+  CK(cudaMalloc((void**)&db, nd * sizeof(double)));
+  CK(cudaMalloc((void**)&dw, nd * sizeof(double)));
+  if (no) {
+    CK(cudaMalloc((void**)&du, no * sizeof(double)));
+    CK(cudaMalloc((void**)&dl, no * sizeof(double)));
+    CK(cudaMemcpy(du, u, no * sizeof(double), cudaMemcpyDefault));
+    CK(cudaMemcpy(dl, l, no * sizeof(double), cudaMemcpyDefault));
+  }
+  CK(cudaMemcpy(dd, d, nd * sizeof(double), cudaMemcpyDefault));
+  CK(cudaMemcpy(db, b, nd * sizeof(double), cudaMemcpyDefault));
+  Launch L{0, 1};
+  launch_tri_solve(L, ncol, n1, dd, du, dl, db, dw);
+  int rc = check_launch();
+  if (!rc) {
+    cudaError_t e = cudaMemcpy(b, db, nd * sizeof(double), cudaMemcpyDefault);
+    if (e != cudaSuccess) {
+      set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+      rc = kCudaError;
+    }
+  }
+  cudaFree(dd);
+  cudaFree(db);
+  cudaFree(dw);
+  if (du) cudaFree(du);
+  if (dl) cudaFree(dl);
+  return rc;
+}
+
+int asam_tri_matvec(int ncol, int n1, const double* d, const double* u, const double* l, const double* x, double* y) {
+  if (ncol < 1 || n1 < 1 || !d || !x || !y || (n1 > 1 && (!u || !l))) return kBadArg;
+  size_t nd = (size_t)ncol * n1, no = (size_t)ncol * (n1 - 1);
+  double *dd, *du = nullptr, *dl = nullptr, *dx, *dy;
+  CK(cudaMalloc((void**)&dd, nd * sizeof(double)));
+  CK(cudaMalloc((void**)&dx, nd * sizeof(double)));
+  CK(cudaMalloc((void**)&dy, nd * sizeof(double)));
+  if (no) {
+    CK(cudaMalloc((void**)&du, no * sizeof(double)));
+    CK(cudaMalloc((void**)&dl, no * sizeof(double)));
+    CK(cudaMemcpy(du, u, no * sizeof(double), cudaMemcpyDefault));
+    CK(cudaMemcpy(dl, l, no * sizeof(double), cudaMemcpyDefault));
+  }
+  CK(cudaMemcpy(dd, d, nd * sizeof(double), cudaMemcpyDefault));
+  CK(cudaMemcpy(dx, x, nd * sizeof(double), cudaMemcpyDefault));
+  Launch L{0, 1};
+  launch_tri_matvec(L, ncol, n1, dd, du, dl, dx, dy);
+  int rc = check_launch();
+  if (!rc) {
+    cudaError_t e = cudaMemcpy(y, dy, nd * sizeof(double), cudaMemcpyDefault);
+    if (e != cudaSuccess) {
+      set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+      rc = kCudaError;
+    }
+  }
+  cudaFree(dd);
+  cudaFree(dx);
+  cudaFree(dy);
+  if (du) cudaFree(du);
+  if (dl) cudaFree(dl);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,36 @@
+// FP64 kernels, compiled with -fmad=false: every product and sum is rounded
+// separately, as in the reference Fortran built without FMA contraction.
+#include "launchers_impl.cuh"
+
+ASAM_DEFINE_LAUNCHERS(double, double)
+
+namespace {
+__global__ void k_cvt_d2f(size_t len, const double* __restrict__ x, float* __restrict__ y) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
+    y[q] = (float)x[q];
+}
+__global__ void k_cvt_f2d(size_t len, const float* __restrict__ x, double* __restrict__ y) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
+    y[q] = (double)x[q];
+}
+}  // namespace
+
+namespace asam {
+void launch_beta(const Launch& L, KrylovScalars* sc) {
+  k_beta<<<1, 1, 0, L.stream>>>(sc);
+  count_launches(1);
+}
+void launch_mass(const Launch& L, const Dims& d, const double* c, const double* volc, double* partial, double* out) {
+  k_mass_partial<<<RED_GRID, RED_BLOCK, 0, L.stream>>>(d, c, volc, partial);
+  k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, RED_GRID, nullptr, -1, out);
+  count_launches(2);
+}
+void launch_convert_f64_to_f32(const Launch& L, size_t len, const double* x, float* y) {
+  k_cvt_d2f<<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, x, y);
+  count_launches(1);
+}
+void launch_convert_f32_to_f64(const Launch& L, size_t len, const float* x, double* y) {
+  k_cvt_f2d<<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, x, y);
+  count_launches(1);
+}
+}  // namespace asam

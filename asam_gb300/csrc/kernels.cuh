@@ -1,0 +1,774 @@
+// Templated CUDA kernels of the transport stage.  Included by k64.cu (FP64,
+// compiled with -fmad=false so every product and sum is rounded exactly as in
+// the reference Fortran) and by k32.cu (FP32 inner solver of the refined mode).
+// Everything here lives in an anonymous namespace: each translation unit gets
+// its own copy, and the launch wrappers of launch.h are the only exports.
+#pragma once
+#include "asam_common.cuh"
+#include "launch.h"
+
+namespace {
+
+using asam::Dims;
+
+template <typename T>
+__device__ __forceinline__ T eps_t() {
+  return (T)1.0e-30;
+}
+
+// ---------------------------------------------------------------------------
+// Limiter and stencil coefficients: ADVECT/Advection_Mod.f90:2118-2134
+// (k1F, k2F, PhiLim with MethAdv='Koren').
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T k1f(T hL, T hC, T hR) {
+  const T e = eps_t<T>();
+  return (hC / (hC + hR + e)) * ((hL + hC) / (hL + hC + hR + e));
+}
+template <typename T>
+__device__ __forceinline__ T k2f(T hL, T hC, T hR) {
+  const T e = eps_t<T>();
+  return (hC / (hL + hC + e)) * (hR / (hL + hC + hR + e));
+}
+template <typename T>
+__device__ __forceinline__ T koren(T r, T k1, T k2) {
+  T a = k1 * r + k2;
+  T m = a < (T)1 ? a : (T)1;
+  m = r < m ? r : m;
+  return (T)0 > m ? (T)0 : m;
+}
+
+// Outflow flux of the upwind cell C through one of its faces, as computed
+// inside the triple loop of ADVECT/Advection_Mod.f90:854-974.
+//   right=true : flux through the right face (velocity > 0), ":885-894"
+//   right=false: flux through the left face (velocity < 0), ":875-884"
+// pL,pC,pR: c/(Rho+Eps) of the cells left/centre/right of C along the axis,
+// VL..VR volumes, FL/FR the left/right face areas of C, vblend: x-axis only.
+template <typename T>
+__device__ __forceinline__ T upwind_flux(T cL, T cC, T cR, T VL, T VC, T VR, T FL, T FR, T vel, bool right,
+                                         bool vblend) {
+  const T e = eps_t<T>();
+  if (vblend) {
+    if (VL < VC) cL = ((VC - VL) * cC + VL * cL) / VC;
+    if (VR < VC) cR = ((VC - VR) * cC + VR * cR) / VC;
+  }
+  if (FL < FR) cL = ((FR - FL) * cC + FL * cL) / FR;
+  if (FR < FL) cR = ((FL - FR) * cC + FR * cR) / FL;
+  const T half = (T)0.5;
+  if (!right) {
+    T k1 = k1f(VR, VC, VL);
+    T k2 = k2f(VR, VC, VL);
+    T cDiff = cR - cC;
+    T r = (cC - cL + e) / (cDiff + e);
+    return half * (fabs(vel) - vel) * FL * (cC + FR / (FR + e) * (koren(r, k1, k2) * (cC - cR)));
+  } else {
+    T k1 = k1f(VL, VC, VR);
+    T k2 = k2f(VL, VC, VR);
+    T cDiff = cC - cL;
+    T r = (cR - cC + e) / (cDiff + e);
+    return half * (fabs(vel) + vel) * FR * (cC + FL / (FL + e) * (koren(r, k1, k2) * (cC - cL)));
+  }
+}
+
+using asam::GeomT;
+
+// phi = c/(Rho+Eps) over the padded box, all components
+template <typename T>
+__global__ void k_phi(Dims d, int ncomp, int rho_pos, const T* __restrict__ c, T* __restrict__ phi) {
+  const size_t n = d.npad();
+  const T e = eps_t<T>();
+  const T* rho = c + (size_t)rho_pos * n;
+  for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
+    T rp = rho[P] + e;
+    for (int ic = 0; ic < ncomp; ++ic) phi[ic * n + P] = c[ic * n + P] / rp;
+  }
+}
+
+// Face fluxes.  axis 0: x faces (i in [0,nx], j,k interior) stored at UF(i,j,k);
+// axis 1: y faces at VF; axis 2: z faces at WF.  g[ic*nface + face] holds the
+// flux computed by the reference's loop for the upwind interior cell of the
+// face (zero when the upwind cell is a halo cell or the velocity is zero).
+template <typename T, int AXIS>
+__global__ void k_face_flux(Dims d, GeomT<T> g, int ncomp, const T* __restrict__ phi, T* __restrict__ gout) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int ex = AXIS == 0 ? nx + 1 : nx;
+  const int ey = AXIS == 1 ? ny + 1 : ny;
+  const int ez = AXIS == 2 ? nz + 1 : nz;
+  const size_t nface = (size_t)ex * ey * ez;
+  const size_t n = d.npad();
+  for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < nface; f += (size_t)gridDim.x * blockDim.x) {
+    int a = (int)(f % ex);
+    size_t rest = f / ex;
+    int b = (int)(rest % ey);
+    int cc = (int)(rest / ey);
+    // face lies between padded cells L=(i,j,k) and R=(i,j,k)+e_axis
+    int i, j, k;
+    T vel;
+    if (AXIS == 0) {
+      i = a; j = b + 1; k = cc + 1;
+      vel = g.uf[d.UF(i, j, k)];
+    } else if (AXIS == 1) {
+      i = a + 1; j = b; k = cc + 1;
+      vel = g.vf[d.VF(i, j, k)];
+    } else {
+      i = a + 1; j = b + 1; k = cc;
+      vel = g.wf[d.WF(i, j, k)];
+    }
+    const int s = AXIS == 0 ? i : (AXIS == 1 ? j : k);
+    const int smax = AXIS == 0 ? nx : (AXIS == 1 ? ny : nz);
+    bool right;
+    int ci, cj, ck;
+    if (vel > (T)0 && s >= 1) {
+      right = true;  // upwind cell = L
+      ci = i; cj = j; ck = k;
+    } else if (vel < (T)0 && s + 1 <= smax) {
+      right = false;  // upwind cell = R
+      ci = i + (AXIS == 0); cj = j + (AXIS == 1); ck = k + (AXIS == 2);
+    } else {
+      for (int ic = 0; ic < ncomp; ++ic) gout[ic * nface + f] = (T)0;
+      continue;
+    }
+    const size_t PC = d.P(ci, cj, ck);
+    const size_t stride = AXIS == 0 ? 1 : (AXIS == 1 ? (size_t)d.NX() : (size_t)d.NX() * d.NY());
+    const size_t PL = PC - stride, PR = PC + stride;
+    T FL, FR;
+    if (AXIS == 0) {
+      FR = g.fu[d.FU(ci, cj, ck)];
+      FL = g.fu[d.FU(ci - 1, cj, ck)];
+    } else if (AXIS == 1) {
+      FR = g.fv[d.FV(ci, cj, ck)];
+      FL = g.fv[d.FV(ci, cj - 1, ck)];
+    } else {
+      FR = g.fw[d.FW(ci, cj, ck)];
+      FL = g.fw[d.FW(ci, cj, ck - 1)];
+    }
+    const T VL = g.volc[PL], VC = g.volc[PC], VR = g.volc[PR];
+    for (int ic = 0; ic < ncomp; ++ic) {
+      const T* ph = phi + ic * n;
+      gout[ic * nface + f] = upwind_flux<T>(ph[PL], ph[PC], ph[PR], VL, VC, VR, FL, FR, vel, right, AXIS == 0);
+    }
+  }
+}
+
+// Gather of the face fluxes into the cell right-hand side in the exact order
+// in which the reference's scatter loop touches f(ix,iy,iz), then the
+// zero-volume mask (:1045-1051), the periodic ExchangeFlux (neighbour order
+// W,E,S,N,B,T) and AdvectionScale (:2888-2898).  One thread per padded cell.
+template <typename T>
+__global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict__ gx, const T* __restrict__ gy,
+                              const T* __restrict__ gz, T* __restrict__ f) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
+  const size_t n = d.npad();
+  const size_t nfx = (size_t)(nx + 1) * ny * nz, nfy = (size_t)nx * (ny + 1) * nz, nfz = (size_t)nx * ny * (nz + 1);
+  const T e = eps_t<T>();
+  for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(P % NX);
+    const int j = (int)((P / NX) % NY);
+    const int k = (int)(P / ((size_t)NX * NY));
+    const T V = g.volc[P];
+    const bool ii = i >= 1 && i <= nx, jj = j >= 1 && j <= ny, kk = k >= 1 && k <= nz;
+    if (ii && jj && kk) {
+      const size_t fxL = d.UF(i - 1, j, k), fxR = d.UF(i, j, k);
+      const size_t fyL = d.VF(i, j - 1, k), fyR = d.VF(i, j, k);
+      const size_t fzL = d.WF(i, j, k - 1), fzR = d.WF(i, j, k);
+      const T uL = g.uf[fxL], uR = g.uf[fxR];
+      const T vL = g.vf[fyL], vR = g.vf[fyR];
+      const T wL = g.wf[fzL], wR = g.wf[fzR];
+      // periodic exchange sources (masked halo values of the opposite side)
+      const bool exW = d.per_x && i == 1, exE = d.per_x && i == nx;
+      const bool exS = d.per_y && j == 1, exN = d.per_y && j == ny;
+      const bool exB = d.per_z && k == 1, exT = d.per_z && k == nz;
+      for (int ic = 0; ic < ncomp; ++ic) {
+        const T* GX = gx + ic * nfx;
+        const T* GY = gy + ic * nfy;
+        const T* GZ = gz + ic * nfz;
+        T a = (T)0;
+        if (wL > (T)0) a = a + GZ[fzL];  // FluxZR of the cell below
+        if (vL > (T)0) a = a + GY[fyL];  // FluxYR of the cell south
+        if (uL > (T)0) a = a + GX[fxL];  // FluxXR of the cell west
+        if (uL < (T)0) a = a - GX[fxL];  // own x-left
+        if (uR > (T)0) a = a - GX[fxR];  // own x-right
+        if (vL < (T)0) a = a - GY[fyL];
+        if (vR > (T)0) a = a - GY[fyR];
+        if (wL < (T)0) a = a - GZ[fzL];
+        if (wR > (T)0) a = a - GZ[fzR];
+        if (uR < (T)0) a = a + GX[fxR];  // FluxXL of the cell east
+        if (vR < (T)0) a = a + GY[fyR];
+        if (wR < (T)0) a = a + GZ[fzR];
+        a = a * V / (V + e);
+        if (exW) {
+          const size_t PH = d.P(nx + 1, j, k), fh = d.UF(nx, j, k);
+          T h = g.uf[fh] > (T)0 ? GX[fh] : (T)0;
+          T VH = g.volc[PH];
+          a = a + h * VH / (VH + e);
+        }
+        if (exE) {
+          const size_t PH = d.P(0, j, k), fh = d.UF(0, j, k);
+          T h = g.uf[fh] < (T)0 ? GX[fh] : (T)0;
+          T VH = g.volc[PH];
+          a = a + h * VH / (VH + e);
+        }
+        if (exS) {
+          const size_t PH = d.P(i, ny + 1, k), fh = d.VF(i, ny, k);
+          T h = g.vf[fh] > (T)0 ? GY[fh] : (T)0;
+          T VH = g.volc[PH];
+          a = a + h * VH / (VH + e);
+        }
+        if (exN) {
+          const size_t PH = d.P(i, 0, k), fh = d.VF(i, 0, k);
+          T h = g.vf[fh] < (T)0 ? GY[fh] : (T)0;
+          T VH = g.volc[PH];
+          a = a + h * VH / (VH + e);
+        }
+        if (exB) {
+          const size_t PH = d.P(i, j, nz + 1), fh = d.WF(i, j, nz);
+          T h = g.wf[fh] > (T)0 ? GZ[fh] : (T)0;
+          T VH = g.volc[PH];
+          a = a + h * VH / (VH + e);
+        }
+        if (exT) {
+          const size_t PH = d.P(i, j, 0), fh = d.WF(i, j, 0);
+          T h = g.wf[fh] < (T)0 ? GZ[fh] : (T)0;
+          T VH = g.volc[PH];
+          a = a + h * VH / (VH + e);
+        }
+        f[ic * n + P] = a / (V + e);
+      }
+    } else {
+      // halo cell: only the face-halo cells next to the interior receive a flux
+      int axis = -1;
+      size_t fidx = 0;
+      bool take_pos = false;
+      if (jj && kk && (i == 0 || i == NX - 1)) {
+        axis = 0;
+        fidx = d.UF(i == 0 ? 0 : nx, j, k);
+        take_pos = i != 0;
+      } else if (ii && kk && (j == 0 || j == NY - 1)) {
+        axis = 1;
+        fidx = d.VF(i, j == 0 ? 0 : ny, k);
+        take_pos = j != 0;
+      } else if (ii && jj && (k == 0 || k == NZ - 1)) {
+        axis = 2;
+        fidx = d.WF(i, j, k == 0 ? 0 : nz);
+        take_pos = k != 0;
+      }
+      T vel = (T)0;
+      if (axis == 0) vel = g.uf[fidx];
+      if (axis == 1) vel = g.vf[fidx];
+      if (axis == 2) vel = g.wf[fidx];
+      const bool has = axis >= 0 && (take_pos ? vel > (T)0 : vel < (T)0);
+      for (int ic = 0; ic < ncomp; ++ic) {
+        T a = (T)0;
+        if (has) {
+          if (axis == 0) a = a + gx[ic * nfx + fidx];
+          if (axis == 1) a = a + gy[ic * nfy + fidx];
+          if (axis == 2) a = a + gz[ic * nfz + fidx];
+        }
+        a = a * V / (V + e);
+        f[ic * n + P] = a / (V + e);
+      }
+    }
+  }
+}
+
+// DivCompute, ADVECT/Advection_Mod.f90:2901-2916 (rhs accumulated)
+template <typename T>
+__global__ void k_div(Dims d, GeomT<T> g, T* __restrict__ rhs) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const size_t n = (size_t)nx * ny * nz;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(q % nx) + 1;
+    int j = (int)((q / nx) % ny) + 1;
+    int k = (int)(q / ((size_t)nx * ny)) + 1;
+    size_t P = d.P(i, j, k);
+    rhs[P] = rhs[P] - (g.uf[d.UF(i, j, k)] * g.fu[d.FU(i, j, k)] - g.uf[d.UF(i - 1, j, k)] * g.fu[d.FU(i - 1, j, k)] +
+                       g.vf[d.VF(i, j, k)] * g.fv[d.FV(i, j, k)] - g.vf[d.VF(i, j - 1, k)] * g.fv[d.FV(i, j - 1, k)] +
+                       g.wf[d.WF(i, j, k)] * g.fw[d.FW(i, j, k)] - g.wf[d.WF(i, j, k - 1)] * g.fw[d.FW(i, j, k - 1)]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Jacobian: JacAdvectionCompute (ADVECT/Advection_Mod.f90:2220-2872) followed by
+// JacScaleCompute (ADVECT/Function_Mod.f90:1782-1862), one thread per padded
+// cell computing its column of the 7-diagonal matrix in the reference's
+// accumulation order.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T jac_term(T vel, bool plus, T F, T Vden, T rho) {
+  // Half*(ABS(u)+/-u)*F/V/(Rho+Eps)
+  const T half = (T)0.5;
+  T s = plus ? (fabs(vel) + vel) : (fabs(vel) - vel);
+  return half * s * F / Vden / (rho + eps_t<T>());
+}
+
+template <typename T>
+__global__ void k_jac(Dims d, GeomT<T> g, const T* __restrict__ rho, T bdt, T* __restrict__ val) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int NX = d.NX(), NY = d.NY();
+  const size_t n = d.npad();
+  const T e = eps_t<T>();
+  const size_t sx = 1, sy = (size_t)NX, sz = (size_t)NX * NY;
+  for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(P % NX);
+    const int j = (int)((P / NX) % NY);
+    const int k = (int)(P / ((size_t)NX * NY));
+    const bool ii = i >= 1 && i <= nx, jj = j >= 1 && j <= ny, kk = k >= 1 && k <= nz;
+    const T rP = rho[P];
+    const T VP = g.volc[P] + e;
+    T v[7] = {(T)0, (T)0, (T)0, (T)0, (T)0, (T)0, (T)0};
+    // face activity: interior faces, plus boundary faces of periodic sides
+    auto actx = [&](int fi) { return jj && kk && fi >= 0 && fi <= nx && ((fi >= 1 && fi <= nx - 1) || d.per_x); };
+    auto acty = [&](int fj) { return ii && kk && fj >= 0 && fj <= ny && ((fj >= 1 && fj <= ny - 1) || d.per_y); };
+    auto actz = [&](int fk) { return ii && jj && fk >= 0 && fk <= nz && ((fk >= 1 && fk <= nz - 1) || d.per_z); };
+    // off-diagonals (each a single term)
+    if (actx(i)) v[2] = v[2] + jac_term(g.uf[d.UF(i, j, k)], true, g.fu[d.FU(i, j, k)], g.volc[P + sx] + e, rP);
+    if (actx(i - 1))
+      v[4] = v[4] + jac_term(g.uf[d.UF(i - 1, j, k)], false, g.fu[d.FU(i - 1, j, k)], g.volc[P - sx] + e, rP);
+    if (acty(j)) v[1] = v[1] + jac_term(g.vf[d.VF(i, j, k)], true, g.fv[d.FV(i, j, k)], g.volc[P + sy] + e, rP);
+    if (acty(j - 1))
+      v[5] = v[5] + jac_term(g.vf[d.VF(i, j - 1, k)], false, g.fv[d.FV(i, j - 1, k)], g.volc[P - sy] + e, rP);
+    if (actz(k)) v[0] = v[0] + jac_term(g.wf[d.WF(i, j, k)], true, g.fw[d.FW(i, j, k)], g.volc[P + sz] + e, rP);
+    if (actz(k - 1))
+      v[6] = v[6] + jac_term(g.wf[d.WF(i, j, k - 1)], false, g.fw[d.FW(i, j, k - 1)], g.volc[P - sz] + e, rP);
+    // diagonal: interior loops x, y, z (face left of P then face right of P)
+    T dg = (T)0;
+    if (jj && kk && i - 1 >= 1 && i - 1 <= nx - 1)
+      dg = dg - jac_term(g.uf[d.UF(i - 1, j, k)], false, g.fu[d.FU(i - 1, j, k)], VP, rP);
+    if (jj && kk && i >= 1 && i <= nx - 1) dg = dg - jac_term(g.uf[d.UF(i, j, k)], true, g.fu[d.FU(i, j, k)], VP, rP);
+    if (ii && kk && j - 1 >= 1 && j - 1 <= ny - 1)
+      dg = dg - jac_term(g.vf[d.VF(i, j - 1, k)], false, g.fv[d.FV(i, j - 1, k)], VP, rP);
+    if (ii && kk && j >= 1 && j <= ny - 1) dg = dg - jac_term(g.vf[d.VF(i, j, k)], true, g.fv[d.FV(i, j, k)], VP, rP);
+    if (ii && jj && k - 1 >= 1 && k - 1 <= nz - 1)
+      dg = dg - jac_term(g.wf[d.WF(i, j, k - 1)], false, g.fw[d.FW(i, j, k - 1)], VP, rP);
+    if (ii && jj && k >= 1 && k <= nz - 1) dg = dg - jac_term(g.wf[d.WF(i, j, k)], true, g.fw[d.FW(i, j, k)], VP, rP);
+    // neighbour branches W, E, S, N, B, T of a periodic block
+    if (d.per_x && jj && kk) {
+      if (i == 0) dg = dg - jac_term(g.uf[d.UF(0, j, k)], true, g.fu[d.FU(0, j, k)], VP, rP);
+      if (i == 1) dg = dg - jac_term(g.uf[d.UF(0, j, k)], false, g.fu[d.FU(0, j, k)], VP, rP);
+      if (i == nx) dg = dg - jac_term(g.uf[d.UF(nx, j, k)], true, g.fu[d.FU(nx, j, k)], VP, rP);
+      if (i == nx + 1) dg = dg - jac_term(g.uf[d.UF(nx, j, k)], false, g.fu[d.FU(nx, j, k)], VP, rP);
+    }
+    if (d.per_y && ii && kk) {
+      if (j == 0) dg = dg - jac_term(g.vf[d.VF(i, 0, k)], true, g.fv[d.FV(i, 0, k)], VP, rP);
+      if (j == 1) dg = dg - jac_term(g.vf[d.VF(i, 0, k)], false, g.fv[d.FV(i, 0, k)], VP, rP);
+      if (j == ny) dg = dg - jac_term(g.vf[d.VF(i, ny, k)], true, g.fv[d.FV(i, ny, k)], VP, rP);
+      if (j == ny + 1) dg = dg - jac_term(g.vf[d.VF(i, ny, k)], false, g.fv[d.FV(i, ny, k)], VP, rP);
+    }
+    if (d.per_z && ii && jj) {
+      if (k == 0) dg = dg - jac_term(g.wf[d.WF(i, j, 0)], true, g.fw[d.FW(i, j, 0)], VP, rP);
+      if (k == 1) dg = dg - jac_term(g.wf[d.WF(i, j, 0)], false, g.fw[d.FW(i, j, 0)], VP, rP);
+      if (k == nz) dg = dg - jac_term(g.wf[d.WF(i, j, nz)], true, g.fw[d.FW(i, j, nz)], VP, rP);
+      if (k == nz + 1) dg = dg - jac_term(g.wf[d.WF(i, j, nz)], false, g.fw[d.FW(i, j, nz)], VP, rP);
+    }
+    // JacScaleCompute fold of the face-halo rows (:1791-1856)
+    if (jj && kk && i == 0) dg = dg - v[2];
+    if (jj && kk && i == nx + 1) dg = dg - v[4];
+    if (ii && kk && j == 0) dg = dg - v[1];
+    if (ii && kk && j == ny + 1) dg = dg - v[5];
+    if (ii && jj && k == 0) dg = dg - v[0];
+    if (ii && jj && k == nz + 1) dg = dg - v[6];
+    // scale to I - beta0*dt*J (:1857-1862)
+    val[3 * n + P] = (T)1 - bdt * dg;
+    val[0 * n + P] = -(bdt * v[0]);
+    val[1 * n + P] = -(bdt * v[1]);
+    val[2 * n + P] = -(bdt * v[2]);
+    val[4 * n + P] = -(bdt * v[4]);
+    val[5 * n + P] = -(bdt * v[5]);
+    val[6 * n + P] = -(bdt * v[6]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stage operator: MatVecMet_Vec4CellSp (MODULE/SpMatrix4CellPar_Mod.f90:70-84):
+// y = T*x (SpAVec_SpDiag, CG/MatSpDiag_Mod.f90:87-108, row sums in diagonal
+// order), then y = -1*x + y, y = x + y (identity source block).
+// ---------------------------------------------------------------------------
+template <typename TM, typename T>
+__global__ void k_matvec(Dims d, int ncomp, const TM* __restrict__ val, const T* __restrict__ x, T* __restrict__ y,
+                         int plain_spmv) {
+  const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
+  const size_t n = d.npad();
+  const size_t sy = (size_t)NX, sz = (size_t)NX * NY;
+  for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(P % NX);
+    const int j = (int)((P / NX) % NY);
+    const int k = (int)(P / sz);
+    const T v0 = k > 0 ? (T)val[0 * n + P - sz] : (T)0;
+    const T v1 = j > 0 ? (T)val[1 * n + P - sy] : (T)0;
+    const T v2 = i > 0 ? (T)val[2 * n + P - 1] : (T)0;
+    const T v3 = (T)val[3 * n + P];
+    const T v4 = i < NX - 1 ? (T)val[4 * n + P + 1] : (T)0;
+    const T v5 = j < NY - 1 ? (T)val[5 * n + P + sy] : (T)0;
+    const T v6 = k < NZ - 1 ? (T)val[6 * n + P + sz] : (T)0;
+    for (int ic = 0; ic < ncomp; ++ic) {
+      const T* xa = x + ic * n;
+      T s = (T)0;
+      if (k > 0) s = s + v0 * xa[P - sz];
+      if (j > 0) s = s + v1 * xa[P - sy];
+      if (i > 0) s = s + v2 * xa[P - 1];
+      s = s + v3 * xa[P];
+      if (i < NX - 1) s = s + v4 * xa[P + 1];
+      if (j < NY - 1) s = s + v5 * xa[P + sy];
+      if (k < NZ - 1) s = s + v6 * xa[P + sz];
+      if (!plain_spmv) {
+        const T xp = xa[P];
+        s = (T)(-1) * xp + s;
+        s = xp + s;
+      }
+      y[ic * n + P] = s;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Gauss-Seidel preconditioner GaussSeidel_SpDiag (CG/MatSpDiag_Mod.f90:191-235),
+// restated as: sweep 0 solves (L+D)x=b; sweeps 1..IterG solve
+// (L+D)x_new = b - U*x_old.  Row r of the column-oriented storage receives
+//   U part: columns r+1, r+NX, r+NXY (in that order),
+//   L part: columns r-NXY, r-NX, r-1 (in that order), then the division.
+// ---------------------------------------------------------------------------
+template <typename TM, typename T>
+__global__ void k_gs_upper(Dims d, int ncomp, const TM* __restrict__ val, const T* __restrict__ b,
+                           const T* __restrict__ x, T* __restrict__ t) {
+  const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
+  const size_t n = d.npad();
+  const size_t sy = (size_t)NX, sz = (size_t)NX * NY;
+  for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(P % NX);
+    const int j = (int)((P / NX) % NY);
+    const int k = (int)(P / sz);
+    const bool hx = i < NX - 1, hy = j < NY - 1, hz = k < NZ - 1;
+    const T v4 = hx ? (T)val[4 * n + P + 1] : (T)0;
+    const T v5 = hy ? (T)val[5 * n + P + sy] : (T)0;
+    const T v6 = hz ? (T)val[6 * n + P + sz] : (T)0;
+    for (int ic = 0; ic < ncomp; ++ic) {
+      const T* xa = x + ic * n;
+      T s = b[ic * n + P];
+      if (hx) s = s - v4 * xa[P + 1];
+      if (hy) s = s - v5 * xa[P + sy];
+      if (hz) s = s - v6 * xa[P + sz];
+      t[ic * n + P] = s;
+    }
+  }
+}
+
+// Lower solve over one level of tiles.  The padded box is cut into tiles of
+// GS_TX x GS_TY x GS_TZ cells; tile (I,J,K) depends only on tiles (I-1,J,K),
+// (I,J-1,K), (I,J,K-1), so all tiles with I+J+K = level are independent.
+// Inside a tile the cells are visited by hyperplanes a+b+c = l: each thread
+// owns one (b,c) line of one component and walks it in x, so the x-neighbour
+// is in a register and the y/z-neighbours were written at an earlier
+// hyperplane (same block, ordered by __syncthreads) or an earlier launch.
+constexpr int GS_TX = 32;
+constexpr int GS_TY = 4;
+constexpr int GS_TZ = 4;
+
+template <typename TM, typename T>
+__global__ void k_gs_lower_level(Dims d, int ncomp, const TM* __restrict__ val, const T* __restrict__ t, T* x,
+                                 int level, int ntx, int nty, int ntz) {
+  // enumerate tiles of this level: blockIdx.x -> (J,K) pair, I = level-J-K
+  const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
+  const size_t n = d.npad();
+  const size_t sy = (size_t)NX, sz = (size_t)NX * NY;
+  const int pair = blockIdx.x;
+  const int J = pair % nty;
+  const int K = pair / nty;
+  const int I = level - J - K;
+  if (I < 0 || I >= ntx || K >= ntz) return;
+  const int lb = threadIdx.x % (GS_TY * GS_TZ);
+  const int ic = threadIdx.x / (GS_TY * GS_TZ);
+  const int tb = lb % GS_TY, tc = lb / GS_TY;
+  const int j = J * GS_TY + tb, k = K * GS_TZ + tc;
+  const bool line_ok = ic < ncomp && j < NY && k < NZ;
+  const int i0 = I * GS_TX;
+  T xprev = (T)0;
+  const T* ta = t + (size_t)ic * n;
+  T* xa = x + (size_t)ic * n;
+  const int nlev = GS_TX + GS_TY + GS_TZ - 2;
+  for (int l = 0; l < nlev; ++l) {
+    const int a = l - tb - tc;
+    const int i = i0 + a;
+    if (line_ok && a >= 0 && a < GS_TX && i < NX) {
+      const size_t P = (size_t)i + sy * (size_t)j + sz * (size_t)k;
+      T s = ta[P];
+      if (k > 0) s = s - (T)val[0 * n + P - sz] * xa[P - sz];
+      if (j > 0) s = s - (T)val[1 * n + P - sy] * xa[P - sy];
+      if (i > 0) {
+        const T xl = a > 0 ? xprev : xa[P - 1];
+        s = s - (T)val[2 * n + P - 1] * xl;
+      }
+      s = s / (T)val[3 * n + P];
+      xa[P] = s;
+      xprev = s;
+    }
+    __syncthreads();
+  }
+}
+
+// zero the whole halo layer (PSolveSp, MODULE/Vector4Cell_Mod.f90:732-737)
+template <typename T>
+__global__ void k_zero_halo(Dims d, int ncomp, T* __restrict__ x) {
+  const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
+  const size_t n = d.npad();
+  for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(P % NX);
+    const int j = (int)((P / NX) % NY);
+    const int k = (int)(P / ((size_t)NX * NY));
+    if (i == 0 || i == NX - 1 || j == 0 || j == NY - 1 || k == 0 || k == NZ - 1)
+      for (int ic = 0; ic < ncomp; ++ic) x[ic * n + P] = (T)0;
+  }
+}
+
+// periodic halo fill (ExchangeCell of a single periodic block)
+template <typename T>
+__global__ void k_exchange_cell(Dims d, int ncomp, T* __restrict__ c) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const size_t n = d.npad();
+  const size_t nxf = d.per_x ? (size_t)ny * nz : 0;
+  const size_t nyf = d.per_y ? (size_t)nx * nz : 0;
+  const size_t nzf = d.per_z ? (size_t)nx * ny : 0;
+  const size_t tot = nxf + nyf + nzf;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
+    size_t lo, hi_src, lo_src, hi;
+    if (q < nxf) {
+      int j = (int)(q % ny) + 1, k = (int)(q / ny) + 1;
+      lo = d.P(0, j, k); lo_src = d.P(nx, j, k); hi = d.P(nx + 1, j, k); hi_src = d.P(1, j, k);
+    } else if (q < nxf + nyf) {
+      size_t r = q - nxf;
+      int i = (int)(r % nx) + 1, k = (int)(r / nx) + 1;
+      lo = d.P(i, 0, k); lo_src = d.P(i, ny, k); hi = d.P(i, ny + 1, k); hi_src = d.P(i, 1, k);
+    } else {
+      size_t r = q - nxf - nyf;
+      int i = (int)(r % nx) + 1, j = (int)(r / nx) + 1;
+      lo = d.P(i, j, 0); lo_src = d.P(i, j, nz); hi = d.P(i, j, nz + 1); hi_src = d.P(i, j, 1);
+    }
+    for (int ic = 0; ic < ncomp; ++ic) {
+      T* a = c + ic * n;
+      a[lo] = a[lo_src];
+      a[hi] = a[hi_src];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Interior dot products (Dot_VectorCell, MODULE/Vector4Cell_Mod.f90:1120-1132),
+// deterministic two-stage reduction; accumulation in double.
+// ---------------------------------------------------------------------------
+constexpr int RED_BLOCK = 256;
+constexpr int RED_GRID = 1024;
+
+template <typename T>
+__global__ void k_dot_partial(Dims d, int ncomp, const T* __restrict__ x, const T* __restrict__ y,
+                              double* __restrict__ partial) {
+  const int nx = d.nx, ny = d.ny;
+  const size_t nint = (size_t)nx * ny * d.nz;
+  const size_t n = d.npad();
+  double s = 0.0;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nint; q += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(q % nx) + 1;
+    int j = (int)((q / nx) % ny) + 1;
+    int k = (int)(q / ((size_t)nx * ny)) + 1;
+    size_t P = d.P(i, j, k);
+    for (int ic = 0; ic < ncomp; ++ic) s += (double)x[ic * n + P] * (double)y[ic * n + P];
+  }
+  __shared__ double sh[RED_BLOCK];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = RED_BLOCK / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__device__ __forceinline__ double block_sum_partials(const double* partial, int npart) {
+  __shared__ double sh[RED_BLOCK];
+  double s = 0.0;
+  for (int q = threadIdx.x; q < npart; q += blockDim.x) s += partial[q];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = RED_BLOCK / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  return sh[0];
+}
+
+// final reduction + the scalar recurrences of BiCGStabMet_Vec4CellSp
+// (MODULE/SpMatrix4CellPar_Mod.f90:283-338); op (asam::ScalarOp) selects what
+// the dot product is.
+using namespace asam;
+
+__global__ void k_dot_final(const double* __restrict__ partial, int npart, asam::KrylovScalars* sc, int op,
+                            double* out) {
+  double s = block_sum_partials(partial, npart);
+  if (threadIdx.x != 0) return;
+  if (out) *out = s;
+  switch (op) {
+    case OP_STORE_A: sc->dot_a = s; break;
+    case OP_STORE_B: sc->dot_b = s; break;
+    case OP_RNORM0: sc->rnorm0 = sqrt(s); break;
+    case OP_RHO:
+      sc->rho_old = sc->rho;
+      sc->rho = s;
+      if (s == 0.0 && sc->done == 0) sc->done = 3;
+      break;
+    case OP_ALPHA: sc->alpha = sc->rho / s; break;
+    case OP_RNORM_HALF:
+      sc->rnorm = sqrt(s);
+      if (sc->done == 0 && sc->rnorm <= sc->tol * sc->rnorm0) sc->done = 1;
+      break;
+    case OP_OMEGA: sc->omega = sc->dot_a / s; break;
+    case OP_RNORM_FULL:
+      sc->rnorm = sqrt(s);
+      if (sc->done == 0 && sc->rnorm <= sc->tol * sc->rnorm0) sc->done = 2;
+      break;
+  }
+}
+
+// beta = (rho/rho_old)*(alpha/omega), computed on the device
+__global__ void k_beta(asam::KrylovScalars* sc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) sc->beta = (sc->rho / sc->rho_old) * (sc->alpha / sc->omega);
+}
+
+// Vector updates over the whole padded arrays.  The coefficient comes from
+// the scalar block (sel) times sign, and an Axpy with a zero coefficient is
+// skipped as in Axpy_VectorCell (MODULE/Vector4Cell_Mod.f90:1237-1250).
+__device__ __forceinline__ double pick(const asam::KrylovScalars* sc, int sel) {
+  return sel == SEL_ALPHA ? sc->alpha : (sel == SEL_OMEGA ? sc->omega : sc->beta);
+}
+
+template <typename T>
+__global__ void k_axpy_sc(size_t len, const asam::KrylovScalars* sc, int sel, double sign, const T* __restrict__ x,
+                          T* __restrict__ y) {
+  const T a = (T)(sign * pick(sc, sel));
+  if (a == (T)0) return;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
+    y[q] = a * x[q] + y[q];
+}
+
+// p = beta*(p - omega*v) + r in the reference's two steps:
+// Axpy(-omega,v,p) then Xpay(r,beta,p)
+template <typename T>
+__global__ void k_pupdate(size_t len, const asam::KrylovScalars* sc, const T* __restrict__ r, const T* __restrict__ v,
+                          T* __restrict__ p) {
+  const T mo = (T)(-sc->omega);
+  const T be = (T)sc->beta;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x) {
+    T pp = p[q];
+    if (mo != (T)0) pp = mo * v[q] + pp;
+    p[q] = be * pp + r[q];
+  }
+}
+
+// x = x + alpha*ph (+ omega*rh), the two Axpy calls of :322-323
+template <typename T>
+__global__ void k_xupdate(size_t len, const asam::KrylovScalars* sc, int with_omega, const T* __restrict__ ph,
+                          const T* __restrict__ rh, T* __restrict__ x) {
+  const T al = (T)sc->alpha;
+  const T om = (T)sc->omega;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x) {
+    T xx = x[q];
+    if (al != (T)0) xx = al * ph[q] + xx;
+    if (with_omega && om != (T)0) xx = om * rh[q] + xx;
+    x[q] = xx;
+  }
+}
+
+// y = a*x + y with a host coefficient (skipped when a == 0)
+template <typename T>
+__global__ void k_axpy_host(size_t len, T a, const T* __restrict__ x, T* __restrict__ y) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
+    y[q] = a * x[q] + y[q];
+}
+// y = a*y + x
+template <typename T>
+__global__ void k_xpay_host(size_t len, const T* __restrict__ x, T a, T* __restrict__ y) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
+    y[q] = a * y[q] + x[q];
+}
+template <typename T>
+__global__ void k_scale_host(size_t len, T a, T* __restrict__ y) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
+    y[q] = a * y[q];
+}
+
+// ---------------------------------------------------------------------------
+// Batched Thomas solve / tridiagonal product on vertical columns:
+// MULTI/TriDiagT_Mod.f90:135-155 Solve_1D and :113-133 MatVecT_1D.
+// One thread per column; columns are contiguous (col*n1 + i).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_tri_solve(int ncol, int n1, const T* __restrict__ dd, const T* __restrict__ uu,
+                            const T* __restrict__ ll, T* __restrict__ bb, T* __restrict__ ww) {
+  int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const T* d = dd + (size_t)col * n1;
+  const T* u = uu + (size_t)col * (n1 - 1);
+  const T* l = ll + (size_t)col * (n1 - 1);
+  T* b = bb + (size_t)col * n1;
+  T* w = ww + (size_t)col * n1;
+  T t = d[0];
+  T bprev = b[0] / t;
+  b[0] = bprev;
+  for (int i = 1; i < n1; ++i) {
+    T wi = u[i - 1] / t;
+    w[i - 1] = wi;
+    t = d[i] - l[i - 1] * wi;
+    bprev = (b[i] - l[i - 1] * bprev) / t;
+    b[i] = bprev;
+  }
+  for (int i = n1 - 2; i >= 0; --i) {
+    bprev = b[i] - w[i] * bprev;
+    b[i] = bprev;
+  }
+}
+
+template <typename T>
+__global__ void k_tri_matvec(int ncol, int n1, const T* __restrict__ dd, const T* __restrict__ uu,
+                             const T* __restrict__ ll, const T* __restrict__ xx, T* __restrict__ yy) {
+  size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (q >= (size_t)ncol * n1) return;
+  int col = (int)(q / n1), i = (int)(q % n1);
+  const T* d = dd + (size_t)col * n1;
+  const T* u = uu + (size_t)col * (n1 - 1);
+  const T* l = ll + (size_t)col * (n1 - 1);
+  const T* x = xx + (size_t)col * n1;
+  T y;
+  if (n1 == 1) {
+    y = d[0] * x[0];
+  } else if (i == 0) {
+    y = d[0] * x[0] + u[0] * x[1];
+  } else if (i == n1 - 1) {
+    y = l[n1 - 2] * x[n1 - 2] + d[n1 - 1] * x[n1 - 1];
+  } else {
+    y = l[i - 1] * x[i - 1] + d[i] * x[i] + u[i] * x[i + 1];
+  }
+  yy[q] = y;
+}
+
+// TotalScalar partials: sum(c*VolB) over the interior (ADVECT/Diagnostic_Mod.f90:13-31)
+__global__ void k_mass_partial(Dims d, const double* __restrict__ c, const double* __restrict__ volc,
+                               double* __restrict__ partial) {
+  const int nx = d.nx, ny = d.ny;
+  const size_t nint = (size_t)nx * ny * d.nz;
+  double s = 0.0;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nint; q += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(q % nx) + 1;
+    int j = (int)((q / nx) % ny) + 1;
+    int k = (int)(q / ((size_t)nx * ny)) + 1;
+    size_t P = d.P(i, j, k);
+    s += c[P] * volc[P];
+  }
+  __shared__ double sh[RED_BLOCK];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = RED_BLOCK / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+}  // namespace

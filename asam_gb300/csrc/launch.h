@@ -1,0 +1,50 @@
+// Host-side launch wrappers of the transport-stage kernels.  Each function is
+// defined twice: in k64.cu for double (exact FP64 rounding, no FMA
+// contraction) and in k32.cu for float (inner solver of the refined mode).
+#pragma once
+#include "asam_common.cuh"
+
+namespace asam {
+
+struct Launch {
+  cudaStream_t stream;
+  int sm_count;
+};
+
+#define ASAM_DECLARE_LAUNCHERS(T, TM)                                                                            \
+  void launch_phi(const Launch&, const Dims&, int ncomp, int rho_pos, const T* c, T* phi);                      \
+  void launch_face_flux(const Launch&, const Dims&, const GeomT<T>&, int ncomp, const T* phi, T* gx, T* gy,      \
+                        T* gz);                                                                                  \
+  void launch_flux_gather(const Launch&, const Dims&, const GeomT<T>&, int ncomp, const T* gx, const T* gy,      \
+                          const T* gz, T* f);                                                                    \
+  void launch_div(const Launch&, const Dims&, const GeomT<T>&, T* rhs);                                          \
+  void launch_jac(const Launch&, const Dims&, const GeomT<T>&, const T* rho, T bdt, T* val);                     \
+  void launch_matvec(const Launch&, const Dims&, int ncomp, const TM* val, const T* x, T* y, int plain_spmv);    \
+  void launch_gs_upper(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, const T* x, T* t);      \
+  void launch_gs_lower(const Launch&, const Dims&, int ncomp, const TM* val, const T* t, T* x);                  \
+  void launch_zero_halo(const Launch&, const Dims&, int ncomp, T* x);                                           \
+  void launch_exchange_cell(const Launch&, const Dims&, int ncomp, T* c);                                       \
+  void launch_dot(const Launch&, const Dims&, int ncomp, const T* x, const T* y, double* partial,               \
+                  KrylovScalars* sc, int op, double* out);                                                       \
+  void launch_axpy_sc(const Launch&, size_t len, const KrylovScalars* sc, int sel, double sign, const T* x,      \
+                      T* y);                                                                                     \
+  void launch_pupdate(const Launch&, size_t len, const KrylovScalars* sc, const T* r, const T* v, T* p);         \
+  void launch_xupdate(const Launch&, size_t len, const KrylovScalars* sc, int with_omega, const T* ph,          \
+                      const T* rh, T* x);                                                                        \
+  void launch_axpy_host(const Launch&, size_t len, T a, const T* x, T* y);                                      \
+  void launch_xpay_host(const Launch&, size_t len, const T* x, T a, T* y);                                      \
+  void launch_scale_host(const Launch&, size_t len, T a, T* y);                                                 \
+  void launch_tri_solve(const Launch&, int ncol, int n1, const T* d, const T* u, const T* l, T* b, T* w);        \
+  void launch_tri_matvec(const Launch&, int ncol, int n1, const T* d, const T* u, const T* l, const T* x, T* y);
+
+ASAM_DECLARE_LAUNCHERS(double, double)
+ASAM_DECLARE_LAUNCHERS(float, float)
+
+void launch_beta(const Launch&, KrylovScalars* sc);
+void launch_mass(const Launch&, const Dims&, const double* c, const double* volc, double* partial, double* out);
+void launch_convert_f64_to_f32(const Launch&, size_t len, const double* x, float* y);
+void launch_convert_f32_to_f64(const Launch&, size_t len, const float* x, double* y);
+
+constexpr int kRedGrid = 1024;  // number of partial sums of the reductions
+
+}  // namespace asam

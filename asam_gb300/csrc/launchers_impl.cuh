@@ -1,0 +1,100 @@
+// Definitions of the launch wrappers declared in launch.h for one scalar type.
+// Included once per precision translation unit after kernels.cuh.
+#pragma once
+#include "kernels.cuh"
+
+namespace asam {
+void count_launches(long long n);
+}
+namespace {
+constexpr int kBlock = 256;
+inline int gs_grid(const asam::Launch& L, size_t n) {
+  size_t g = (n + kBlock - 1) / kBlock;
+  size_t cap = (size_t)L.sm_count * 16;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+}  // namespace
+
+#define ASAM_DEFINE_LAUNCHERS(T, TM)                                                                               \
+  namespace asam {                                                                                                 \
+  void launch_phi(const Launch& L, const Dims& d, int ncomp, int rho_pos, const T* c, T* phi) {                   \
+    k_phi<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, rho_pos, c, phi); count_launches(1);                            \
+  }                                                                                                                \
+  void launch_face_flux(const Launch& L, const Dims& d, const GeomT<T>& g, int ncomp, const T* phi, T* gx, T* gy,  \
+                        T* gz) {                                                                                   \
+    k_face_flux<T, 0><<<gs_grid(L, d.n_uf()), kBlock, 0, L.stream>>>(d, g, ncomp, phi, gx); count_launches(1);                        \
+    k_face_flux<T, 1><<<gs_grid(L, d.n_vf()), kBlock, 0, L.stream>>>(d, g, ncomp, phi, gy); count_launches(1);                        \
+    k_face_flux<T, 2><<<gs_grid(L, d.n_wf()), kBlock, 0, L.stream>>>(d, g, ncomp, phi, gz); count_launches(1);                        \
+  }                                                                                                                \
+  void launch_flux_gather(const Launch& L, const Dims& d, const GeomT<T>& g, int ncomp, const T* gx, const T* gy,  \
+                          const T* gz, T* f) {                                                                     \
+    k_flux_gather<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, f); count_launches(1);                   \
+  }                                                                                                                \
+  void launch_div(const Launch& L, const Dims& d, const GeomT<T>& g, T* rhs) {                                     \
+    k_div<T><<<gs_grid(L, (size_t)d.nx * d.ny * d.nz), kBlock, 0, L.stream>>>(d, g, rhs); count_launches(1);                          \
+  }                                                                                                                \
+  void launch_jac(const Launch& L, const Dims& d, const GeomT<T>& g, const T* rho, T bdt, T* val) {                \
+    k_jac<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, rho, bdt, val); count_launches(1);                                  \
+  }                                                                                                                \
+  void launch_matvec(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* x, T* y, int plain) {      \
+    k_matvec<TM, T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, val, x, y, plain); count_launches(1);                    \
+  }                                                                                                                \
+  void launch_gs_upper(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* b, const T* x, T* t) {   \
+    k_gs_upper<TM, T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, val, b, x, t); count_launches(1);                      \
+  }                                                                                                                \
+  void launch_gs_lower(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* t, T* x) {               \
+    const int ntx = (d.NX() + GS_TX - 1) / GS_TX;                                                                  \
+    const int nty = (d.NY() + GS_TY - 1) / GS_TY;                                                                  \
+    const int ntz = (d.NZ() + GS_TZ - 1) / GS_TZ;                                                                  \
+    const int nlev = ntx + nty + ntz - 2;                                                                          \
+    const int threads = GS_TY * GS_TZ * ncomp;                                                                     \
+    for (int lev = 0; lev < nlev; ++lev) {                                                                         \
+      k_gs_lower_level<TM, T><<<nty * ntz, threads, 0, L.stream>>>(d, ncomp, val, t, x, lev, ntx, nty, ntz); count_launches(1);       \
+    }                                                                                                              \
+  }                                                                                                                \
+  void launch_zero_halo(const Launch& L, const Dims& d, int ncomp, T* x) {                                         \
+    k_zero_halo<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, x); count_launches(1);                                    \
+  }                                                                                                                \
+  void launch_exchange_cell(const Launch& L, const Dims& d, int ncomp, T* c) {                                     \
+    size_t tot = (d.per_x ? (size_t)d.ny * d.nz : 0) + (d.per_y ? (size_t)d.nx * d.nz : 0) +                       \
+                 (d.per_z ? (size_t)d.nx * d.ny : 0);                                                              \
+    if (tot == 0) return;                                                                                          \
+    k_exchange_cell<T><<<gs_grid(L, tot), kBlock, 0, L.stream>>>(d, ncomp, c); count_launches(1);                                     \
+  }                                                                                                                \
+  void launch_dot(const Launch& L, const Dims& d, int ncomp, const T* x, const T* y, double* partial,              \
+                  KrylovScalars* sc, int op, double* out) {                                                        \
+    k_dot_partial<T><<<RED_GRID, RED_BLOCK, 0, L.stream>>>(d, ncomp, x, y, partial); count_launches(1);                               \
+    k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, RED_GRID, sc, op, out); count_launches(1);                                    \
+  }                                                                                                                \
+  void launch_axpy_sc(const Launch& L, size_t len, const KrylovScalars* sc, int sel, double sign, const T* x,       \
+                      T* y) {                                                                                      \
+    k_axpy_sc<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, sc, sel, sign, x, y); count_launches(1);                              \
+  }                                                                                                                \
+  void launch_pupdate(const Launch& L, size_t len, const KrylovScalars* sc, const T* r, const T* v, T* p) {         \
+    k_pupdate<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, sc, r, v, p); count_launches(1);                                      \
+  }                                                                                                                \
+  void launch_xupdate(const Launch& L, size_t len, const KrylovScalars* sc, int with_omega, const T* ph,           \
+                      const T* rh, T* x) {                                                                         \
+    k_xupdate<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, sc, with_omega, ph, rh, x); count_launches(1);                        \
+  }                                                                                                                \
+  void launch_axpy_host(const Launch& L, size_t len, T a, const T* x, T* y) {                                      \
+    if (a == (T)0) return;                                                                                         \
+    k_axpy_host<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, a, x, y); count_launches(1);                                        \
+  }                                                                                                                \
+  void launch_xpay_host(const Launch& L, size_t len, const T* x, T a, T* y) {                                      \
+    k_xpay_host<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, x, a, y); count_launches(1);                                        \
+  }                                                                                                                \
+  void launch_scale_host(const Launch& L, size_t len, T a, T* y) {                                                 \
+    k_scale_host<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, a, y); count_launches(1);                                          \
+  }                                                                                                                \
+  void launch_tri_solve(const Launch& L, int ncol, int n1, const T* dd, const T* uu, const T* ll, T* bb, T* ww) {  \
+    k_tri_solve<T><<<(ncol + 127) / 128, 128, 0, L.stream>>>(ncol, n1, dd, uu, ll, bb, ww); count_launches(1);                        \
+  }                                                                                                                \
+  void launch_tri_matvec(const Launch& L, int ncol, int n1, const T* dd, const T* uu, const T* ll, const T* xx,    \
+                         T* yy) {                                                                                  \
+    size_t tot = (size_t)ncol * n1;                                                                                \
+    k_tri_matvec<T><<<(unsigned)((tot + 255) / 256), 256, 0, L.stream>>>(ncol, n1, dd, uu, ll, xx, yy); count_launches(1);            \
+  }                                                                                                                \
+  }

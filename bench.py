@@ -1,0 +1,374 @@
+"""Benchmark of the GB300 Rosenbrock transport step.
+
+Workload (default): the 256x256x128 cut-cell configuration -- Gaussian hill
+h=1 km, half-width 5 km, Gaussian-correlated roughness (sigma 50 m, 2 km),
+dz 50->400 m, snapping + small-cell merge, N=0.01 1/s, u=10 m/s, moist,
+one tracer; 10 cell components (Rho, six LR momentum components, Rho*theta,
+Rho*qv, Rho*tracer); RosRK3 (3 stages), dt = 2 s, BiCGStab tolerance 1e-10,
+6-sweep Gauss-Seidel preconditioner.  Seeded synthetic fields stand in for
+the reference's (unpublished) decks.
+
+One step = one Ros3MetC call: per stage ExchangeCell, (stage 1) the 7-diagonal
+Jacobian, the flux RHS of all components, the stage combinations and a full
+BiCGStab solve, then the state update.  The metric is Mcell-steps/s (interior
+cells x steps / s).
+
+Arms:
+  (default)          ours: FP64 drop-in path (value), plus the FP32-refined path
+  --impl reference   the reference's CPU path (the oracle restatement of the
+                     Fortran; the Fortran itself has no compiler here), one
+                     process per host core on independent blocks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mcell-steps/s"
+BYTES_PER_CELL_FLUX = lambda ncomp: 64 + 16 * ncomp  # noqa: E731  algorithmic bytes per interior cell
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--nx", type=int, default=256)
+    p.add_argument("--ny", type=int, default=256)
+    p.add_argument("--nz", type=int, default=128)
+    p.add_argument("--dt", type=float, default=2.0)
+    p.add_argument("--tol", type=float, default=1e-10)
+    p.add_argument("--no-refined", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample", type=int, default=48, help="edge of the oracle's CPU sample window")
+    return p.parse_args()
+
+
+def workload(nx, ny, nz, seed=2):
+    from asam_gb300 import geometry as G
+
+    return G.hill_case(nx, ny, nz, seed=seed)
+
+
+def workload_config(a):
+    return {"workload": f"cut-cell Gaussian hill {a.nx}x{a.ny}x{a.nz}, 10 components, RosRK3 dt={a.dt}s, "
+                        f"BiCGStab tol {a.tol:g}, 6-sweep GS preconditioner",
+            "nx": a.nx, "ny": a.ny, "nz": a.nz, "ncomp": 10, "method": "RosRK3", "dt": a.dt,
+            "bicgstab_tol": a.tol, "l2": "inputs larger than L2 (state 0.7 GB, matrix 0.5 GB)",
+            "parallelism": "replicas" if a.gpus > 1 else "single GPU"}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle restatement of the reference Fortran), one block per process
+# ---------------------------------------------------------------------------
+def _cpu_worker(args):
+    edge, nz, dt, tol, steps, seed = args
+    import oracle
+    from asam_gb300 import METHODS
+
+    geo, vel, st = workload(edge, edge, nz, seed=seed)
+    o = oracle.Oracle(geo)
+    c = st.c.copy()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.ros_step(c, vel, dt, method=METHODS["RosRK3"], tol=tol)
+    return time.perf_counter() - t0, edge * edge * nz * steps
+
+
+def cpu_baseline(edge, nz, dt, tol, steps, procs):
+    ctx = mp.get_context("spawn")
+    jobs = [(edge, nz, dt, tol, steps, 2 + i) for i in range(procs)]
+    t0 = time.perf_counter()
+    if procs == 1:
+        res = [_cpu_worker(jobs[0])]
+    else:
+        with ctx.Pool(procs) as pool:
+            res = pool.map(_cpu_worker, jobs)
+    wall = time.perf_counter() - t0
+    cells = sum(r[1] for r in res)
+    slowest = max(r[0] for r in res)
+    return cells / slowest / 1e6, wall
+
+
+def cpu_model():
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.tmp = None
+
+    def __enter__(self):
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.tmp,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.tmp.flush()
+        rows = [r.split(",") for r in Path(self.tmp.name).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.tmp.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def run_reference(a, rank):
+    """--impl reference: the reference's CPU path (oracle port) on all host cores."""
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    edge = max(8, a.cpu_sample // 2)
+    value, wall = cpu_baseline(edge, a.nz, a.dt, a.tol, a.steps, procs)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators)",
+            "config": workload_config(a),
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": procs, "kind": "port",
+                             "sample": f"{procs} independent {edge}x{edge}x{a.nz} blocks of the same generator, "
+                                       f"{a.steps} steps each (MPI-over-blocks model), oracle restatement of the "
+                                       f"Fortran, {cpu_model()}"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def time_region(torch, stream, fn, n):
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s.record(stream)
+    for _ in range(n):
+        fn()
+    e.record(stream)
+    torch.cuda.synchronize()
+    return s.elapsed_time(e)
+
+
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        run_reference(a, rank)
+        return
+
+    # CPU baseline first (before any GPU call), rank 0, N=1 only
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        edge = a.cpu_sample
+        value, wall = cpu_baseline(edge, a.nz, a.dt, a.tol, 1, 1)
+        cpu = {"value": value, "unit": METRIC, "cores": 1, "kind": "port",
+               "sample": f"one {edge}x{edge}x{a.nz} window of the same generator, 1 step, single-threaded oracle "
+                         f"restatement of the Fortran ({wall:.1f} s), {cpu_model()}"}
+
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import asam_gb300
+    from asam_gb300 import _lib
+
+    lib = _lib.load()
+    geo, vel, st = workload(a.nx, a.ny, a.nz)
+    ncomp = st.c.shape[0]
+    ncell = a.nx * a.ny * a.nz
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    results = {}
+    gpu_launches = {}
+    for prec in (["fp64"] + ([] if a.no_refined else ["fp32_refined"])):
+        blk = asam_gb300.TransportBlock(geo, ncomp, method="RosRK3", bicgstab_tol=a.tol, bicgstab_maxiter=30,
+                                        precision=prec)
+        blk.set_velocity(*vel)
+        blk.set_stream(stream.cuda_stream)
+        dptr = blk.state_device_ptr()
+        host0 = torch.from_numpy(st.c.reshape(-1).copy())
+        dstate = torch.empty(st.c.size, dtype=torch.float64, device="cuda")
+        dstate.copy_(host0)
+        ctypes_dptr = C.c_void_p(dstate.data_ptr())
+        iters_all = []
+
+        def step():
+            iters = (C.c_int * 4)()
+            resid = (C.c_double * 4)()
+            rc = lib.asam_ros_step(blk.h, ctypes_dptr, a.dt, iters, resid)
+            _lib.check(rc, "asam_ros_step", allow=(0, 1, 2))
+            iters_all.append([iters[i] for i in range(blk.nstage)])
+
+        for _ in range(a.warmup):
+            step()
+        barrier()
+        iters_all.clear()
+        n0 = lib.asam_launch_count()
+        with ClockSampler(local) as clk:
+            ms = time_region(torch, stream, step, a.steps)
+        barrier()
+        gpu_launches[prec] = lib.asam_launch_count() - n0
+        ms = max_over_ranks(ms)
+        final = dstate.cpu().numpy().copy()
+
+        # end to end through the public API with pinned host buffers
+        pinned = torch.empty(st.c.size, dtype=torch.float64).pin_memory()
+        pinned.copy_(host0)
+        hptr = C.c_void_p(pinned.data_ptr())
+
+        def step_e2e():
+            iters = (C.c_int * 4)()
+            resid = (C.c_double * 4)()
+            _lib.check(lib.asam_ros_step(blk.h, hptr, a.dt, iters, resid), "asam_ros_step", allow=(0, 1, 2))
+
+        step_e2e()
+        barrier()
+        t0 = time.perf_counter()
+        ms_e2e = time_region(torch, stream, step_e2e, a.steps)
+        wall_e2e = (time.perf_counter() - t0) * 1e3
+        ms_e2e = max_over_ranks(max(ms_e2e, wall_e2e))
+
+        # dominant kernels, timed alone with CUDA events on the same stream
+        f_out = torch.empty_like(dstate)
+        kt = {}
+        nrep = 5
+        kt["flux_rhs_ms"] = time_region(torch, stream, lambda: _lib.check(
+            lib.asam_fcn(blk.h, ctypes_dptr, C.c_void_p(f_out.data_ptr())), "asam_fcn"), nrep) / nrep
+        kt["psolve_ms"] = time_region(torch, stream, lambda: _lib.check(
+            lib.asam_psolve(blk.h, C.c_void_p(f_out.data_ptr()), ctypes_dptr), "asam_psolve"), nrep) / nrep
+        dstate.copy_(torch.from_numpy(final.reshape(-1)))
+        kt["matvec_ms"] = time_region(torch, stream, lambda: _lib.check(
+            lib.asam_matvec(blk.h, ctypes_dptr, C.c_void_p(f_out.data_ptr())), "asam_matvec"), nrep) / nrep
+        results[prec] = {"ms": ms, "ms_e2e": ms_e2e, "final": final, "iters": iters_all, "clocks": clk.summary(),
+                         "kernels": kt}
+        blk.close()
+        del dstate, f_out, pinned
+        torch.cuda.empty_cache()
+
+    gf = C.c_double()
+    lib.asam_probe_fp64_fma(20000, C.byref(gf))
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    r64 = results["fp64"]
+    ms_step = r64["ms"] / a.steps
+    value = world * ncell * a.steps / (r64["ms"] * 1e-3) / 1e6
+    e2e = world * ncell * a.steps / (r64["ms_e2e"] * 1e-3) / 1e6
+    flux_bytes = ncell * BYTES_PER_CELL_FLUX(ncomp)
+    flux_gbs = flux_bytes / (r64["kernels"]["flux_rhs_ms"] * 1e-3) / 1e9
+    nbytes_state = st.c.size * 8
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded cut-cell generators)", "config": workload_config(a),
+        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": nbytes_state, "d2h_bytes_per_step": nbytes_state},
+        "roofline": {"kernel": "flux RHS (asam_fcn: phi + face fluxes + gather)", "bound": "hbm",
+                     "achieved": flux_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": flux_gbs / hbm_peak,
+                     "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
+                     "algorithmic_bytes_per_launch": flux_bytes,
+                     "fp64_fma_peak_gflops_probe": gf.value},
+        "kernels_ms": r64["kernels"],
+        "krylov_iterations": r64["iters"],
+        "clocks": r64["clocks"],
+        "gpu_launches": gpu_launches["fp64"],
+    }
+    if "fp32_refined" in results:
+        rr = results["fp32_refined"]
+        ref = r64["final"].reshape(st.c.shape)
+        got = rr["final"].reshape(st.c.shape)
+        errs = []
+        for i in range(ncomp):
+            den = max(float(np.abs(ref[i]).max()), 1e-300)
+            d = np.abs(got[i] - ref[i])
+            errs.append({"field": st.names[i], "max_rel": float(d.max() / den),
+                         "rms_rel": float(np.sqrt(np.mean(d ** 2)) / den)})
+        line["fp32_refined"] = {"value": world * ncell * a.steps / (rr["ms"] * 1e-3) / 1e6,
+                                "ms_per_step": rr["ms"] / a.steps,
+                                "speedup_vs_fp64": r64["ms"] / rr["ms"],
+                                "max_rel_err_vs_fp64": max(e["max_rel"] for e in errs), "fields": errs,
+                                "krylov_iterations": rr["iters"], "kernels_ms": rr["kernels"],
+                                "gpu_launches": gpu_launches["fp32_refined"],
+                                "clocks": rr["clocks"]}
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

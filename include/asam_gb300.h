@@ -1,0 +1,160 @@
+/*
+ * asam_gb300 -- C-ABI of the GB300 (sm_103a) implementation of ASAM's implicit
+ * Rosenbrock transport stage.
+ *
+ * Every entry point takes plain pointers and sizes.  Field pointers may point
+ * to host memory (staged through the context's device buffers) or to device
+ * memory (used in place); the library tells them apart itself.  Layouts are
+ * the Fortran layouts of ASAM (ix fastest):
+ *   cell field   (nx+2)*(ny+2)*(nz+2) doubles, c(ix0:ix1+1,iy0:iy1+1,iz0:iz1+1)
+ *   state        ncomp such fields back to back (component ic at ic*npad)
+ *   FU (nx+3)*ny*nz, FV nx*(ny+3)*nz, FW nx*ny*(nz+3)   (WeiFU/WeiFV/WeiFW)
+ *   uF (nx+1)*ny*nz, vF nx*(ny+1)*nz, wF nx*ny*(nz+1)   (VelocityFace_T)
+ *   VolC (nx+2)*(ny+2)*(nz+2)
+ *   DIA matrix 7*npad doubles, Val(m,7) column-major
+ * All calls return an asam_status; asam_last_error() describes the last
+ * failure.  A context is not thread-safe; its work runs on one CUDA stream.
+ */
+#ifndef ASAM_GB300_H
+#define ASAM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  ASAM_OK = 0,
+  ASAM_NOT_CONVERGED = 1, /* Krylov iteration limit hit (reference: MaxIter=2*Iter) */
+  ASAM_BREAKDOWN = 2,     /* rho == 0 in BiCGStab */
+  ASAM_NAN_DETECTED = 3,
+  ASAM_BAD_ARG = 4,
+  ASAM_CUDA_ERROR = 5,
+  ASAM_NO_DEVICE = 6
+} asam_status;
+
+typedef enum {
+  ASAM_PREC_FP64 = 0,        /* plain FP64, reference operation order (drop-in) */
+  ASAM_PREC_FP32_REFINED = 1 /* FP32 inner BiCGStab + preconditioner inside FP64 refinement */
+} asam_precision;
+
+/* Rosenbrock methods of ADVECT/Int_Mod.f90:96-234 (InitRos3MetC). */
+typedef enum {
+  ASAM_ROS3AMF = 0,
+  ASAM_ROSRK32 = 1,
+  ASAM_ROSEUL = 2,
+  ASAM_ROS3P = 3,
+  ASAM_ROS3PW = 4,
+  ASAM_ROSRK3 = 5,
+  ASAM_ROSTVD = 6,
+  ASAM_ROSRK4 = 7
+} asam_method;
+
+typedef struct {
+  int nx, ny, nz;                          /* interior cells of the block */
+  int periodic_x, periodic_y, periodic_z;  /* 1: side pair is periodic ('iw'/'ie' self-neighbour); 0: closed wall */
+  int ncomp;                               /* cell components of VecMet (Vector4Cell_T%Vec) */
+  int rho_pos;                             /* 0-based index of the density component (RhoPos-1) */
+  int method;                              /* asam_method (Control_Mod Method) */
+  int bicgstab_maxiter;                    /* BiCGStabMaxIter (Control_Mod.f90:581, default 30) */
+  double bicgstab_tol;                     /* BiCGStabTol (Control_Mod.f90:580, default 1e-6) */
+  int gs_iter;                             /* IterG (CG/MatSpDiag_Mod.f90:14, default 5) */
+  int precision;                           /* asam_precision */
+} asam_config;
+
+typedef struct asam_ctx asam_ctx;
+
+/* Create a context for one block: uploads the cut-cell geometry (face areas
+ * and volumes of MODULE/Domain_Mod.f90:447-460, read by
+ * INIT/ReadWeights_Mod.f90:408) and allocates the stage work space
+ * (replaces InitRos3MetC's allocations, ADVECT/Int_Mod.f90:235-257, and
+ * Allocate_Jac, CHEMIE/Chemie_Mod.f90:294-345). */
+int asam_create(const asam_config *cfg, const double *volc, const double *fu, const double *fv, const double *fw,
+                asam_ctx **out);
+int asam_destroy(asam_ctx *ctx);
+
+/* Run the context's work on this CUDA stream (cudaStream_t); NULL = own stream. */
+int asam_set_stream(asam_ctx *ctx, void *stream);
+/* Device pointer of the context's resident state buffer (ncomp*npad doubles). */
+int asam_state_device_ptr(asam_ctx *ctx, double **dptr);
+/* Block until the context's stream is idle. */
+int asam_synchronize(asam_ctx *ctx);
+
+/* Face velocities uF, vF, wF (VelocityFace_T, MODULE/VelocityFace_Mod.f90:211-213). */
+int asam_set_velocity(asam_ctx *ctx, const double *uf, const double *vf, const double *wf);
+
+/* Periodic halo fill of ncomp fields: ExchangeCell
+ * (MODULE/Vector4CellPar_Mod.f90:752, RandCopyCell_VecCell :611-659). */
+int asam_exchange_cell(asam_ctx *ctx, int ncomp, double *c);
+
+/* Advection right-hand side of all components: the FcnMet advection terms
+ * (ADVECT/Function_Mod.f90:1032-1099, 1312-1345): AdvectionComputeP
+ * (ADVECT/Advection_Mod.f90:737-1054), ExchangeFlux, AdvectionScale.
+ * c: state with current halos; f: output. */
+int asam_fcn(asam_ctx *ctx, const double *c, double *f);
+
+/* Face-flux divergence, DivCompute (ADVECT/Advection_Mod.f90:2901-2916):
+ * rhs(interior) -= sum F*u.  One field. */
+int asam_div(asam_ctx *ctx, double *rhs);
+
+/* Transport Jacobian into the context's DIA matrix: JacAdvectionCompute
+ * (ADVECT/Advection_Mod.f90:2220-2872) + JacScaleCompute
+ * (ADVECT/Function_Mod.f90:1782-1939), A = I - beta0*dt*J.  c: state (the
+ * density component is used). */
+int asam_jac(asam_ctx *ctx, const double *c, double dt);
+/* Copy the context's DIA matrix out (7*npad doubles) / in. */
+int asam_get_jac(asam_ctx *ctx, double *val);
+int asam_set_jac(asam_ctx *ctx, const double *val);
+
+/* Stage operator y = A x: MatVecMet_Vec4CellSp
+ * (MODULE/SpMatrix4CellPar_Mod.f90:70-84). */
+int asam_matvec(asam_ctx *ctx, const double *x, double *y);
+
+/* Transport preconditioner px = P^-1 x: PSolve_Vec4CellSp
+ * (MODULE/SpMatrix4CellPar_Mod.f90:86-102; GaussSeidel_SpDiag,
+ * CG/MatSpDiag_Mod.f90:191-235). */
+int asam_psolve(asam_ctx *ctx, const double *x, double *px);
+
+/* BiCGStabMetSp: BiCGStabMet_Vec4CellSp (MODULE/SpMatrix4CellPar_Mod.f90:245-348).
+ * x in/out (initial guess), b right-hand side.  maxiter/tol in/out with the
+ * reference's conventions: on return *maxiter = -Iter (converged at the half
+ * step), Iter (converged), 2*Iter (limit hit); *tol = final residual norm. */
+int asam_bicgstab(asam_ctx *ctx, double *x, const double *b, int *maxiter, double *tol);
+
+/* One Rosenbrock step with fixed dt (Ros3MetC with ErrControl=.FALSE.,
+ * ADVECT/Int_Mod.f90:1059-1122, stages StageRos :263-374, transport part with
+ * prescribed steady face velocities).  c: state in/out.  iters/resid: per
+ * stage BiCGStab iteration count / residual (may be NULL, else >= nStage). */
+int asam_ros_step(asam_ctx *ctx, double *c, double dt, int *iters, double *resid);
+
+/* Global mass of one component: TotalScalar (ADVECT/Diagnostic_Mod.f90:13-31). */
+int asam_total_scalar(asam_ctx *ctx, const double *c, int comp, double *out);
+
+/* Batched vertical-column tridiagonal solve, Solve_1D (Thomas,
+ * MULTI/TriDiagT_Mod.f90:135-155), over ncol independent columns of length n1:
+ * d[col*n1+i], u[col*(n1-1)+i], l[col*(n1-1)+i]; b overwritten by the solution. */
+int asam_tri_solve(int ncol, int n1, const double *d, const double *u, const double *l, double *b);
+/* y = T x for the same column batch, MatVecT_1D (MULTI/TriDiagT_Mod.f90:113-133). */
+int asam_tri_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x, double *y);
+
+/* Rosenbrock coefficients of InitRos3MetC (ADVECT/Int_Mod.f90:78-261):
+ * alpha/beta 4x4 row-major, gamma1[5].  Returns nStage (0 = unknown method). */
+int asam_ros_coeffs(int method, double *beta0, double *alpha, double *beta, double *gamma1);
+
+/* Diagnostic: scalar FP64 FMA throughput of the current device in GFLOP/s
+ * (no reference counterpart; used for the FP64 roofline of the benchmark). */
+int asam_probe_fp64_fma(int iters, double *gflops);
+
+/* Sizes of the padded cell field for a configuration. */
+long long asam_npad(const asam_config *cfg);
+
+/* Number of CUDA kernels this library has launched since it was loaded
+ * (diagnostic; no reference counterpart). */
+long long asam_launch_count(void);
+
+/* Text of the last error (thread-local). */
+const char *asam_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ASAM_GB300_H */

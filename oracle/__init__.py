@@ -1,0 +1,191 @@
+"""CPU oracle of the ASAM transport stage -- TEST INFRASTRUCTURE ONLY.
+
+ctypes binding of ``oracle/asam_oracle.c``, a loop-for-loop C restatement of
+the reference Fortran (see that file's header for the routines and
+conventions).  Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline
+leg of ``bench.py`` may use it, and only as the checker.  Parity with the
+Fortran binary itself is unpinned (no Fortran compiler is available); the
+restatement is checked against analytic known answers and an independent
+Python restatement in ``tests/``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "_build" / "libasam_oracle.so"
+
+
+class OraGeom(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("per_x", C.c_int), ("per_y", C.c_int),
+                ("per_z", C.c_int), ("volc", C.c_void_p), ("fu", C.c_void_p), ("fv", C.c_void_p),
+                ("fw", C.c_void_p)]
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            import sys
+            sys.path.insert(0, str(_HERE.parent))
+            from asam_gb300.build import build_oracle
+            build_oracle()
+        lib = C.CDLL(str(LIB_PATH))
+        G = C.POINTER(OraGeom)
+        V, I, D = C.c_void_p, C.c_int, C.c_double
+        sig = {
+            "ora_exchange_cell": (None, [G, I, V]),
+            "ora_exchange_flux": (None, [G, I, V]),
+            "ora_fcn": (None, [G, I, I, V, V, V, V, V]),
+            "ora_div": (None, [G, V, V, V, V]),
+            "ora_jac": (None, [G, V, V, V, V, D, D, V]),
+            "ora_spmv": (None, [G, V, V, V]),
+            "ora_gauss_seidel": (None, [G, V, V, V, I]),
+            "ora_psolve": (None, [G, I, V, V, V, I]),
+            "ora_matvec": (None, [G, I, V, V, V]),
+            "ora_dot": (D, [G, I, V, V]),
+            "ora_bicgstab": (None, [G, I, V, V, V, C.POINTER(C.c_int), C.POINTER(C.c_double), I]),
+            "ora_ros_coeffs": (I, [I, C.POINTER(C.c_double), V, V, V]),
+            "ora_ros_step": (I, [G, I, I, V, V, V, V, D, I, D, I, I, V, V]),
+            "ora_total_scalar": (D, [G, V]),
+            "ora_tri_solve": (None, [I, I, V, V, V, V]),
+            "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _p(a: np.ndarray) -> int:
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data
+
+
+class Oracle:
+    """Oracle bound to one geometry (keeps the arrays alive)."""
+
+    def __init__(self, geo):
+        self.lib = load()
+        g = geo.grid
+        self.grid = g
+        self._keep = [np.ascontiguousarray(x, dtype=np.float64) for x in (geo.volc, geo.fu, geo.fv, geo.fw)]
+        self.g = OraGeom(g.nx, g.ny, g.nz, int(g.periodic_x), int(g.periodic_y), int(g.periodic_z),
+                         *(a.ctypes.data for a in self._keep))
+        self.gp = C.byref(self.g)
+        self.npad = g.npad
+
+    def exchange_cell(self, c):
+        a = np.ascontiguousarray(c, dtype=np.float64).copy()
+        self.lib.ora_exchange_cell(self.gp, a.size // self.npad, _p(a))
+        return a
+
+    def fcn(self, c, vel, rho_pos=0):
+        a = np.ascontiguousarray(c, dtype=np.float64)
+        f = np.empty_like(a)
+        uf, vf, wf = (np.ascontiguousarray(v, dtype=np.float64) for v in vel)
+        self.lib.ora_fcn(self.gp, a.size // self.npad, rho_pos, _p(a), _p(uf), _p(vf), _p(wf), _p(f))
+        return f
+
+    def div(self, rhs, vel):
+        a = np.ascontiguousarray(rhs, dtype=np.float64).copy()
+        uf, vf, wf = (np.ascontiguousarray(v, dtype=np.float64) for v in vel)
+        self.lib.ora_div(self.gp, _p(uf), _p(vf), _p(wf), _p(a))
+        return a
+
+    def jac(self, rho, vel, beta0, dt):
+        r = np.ascontiguousarray(rho, dtype=np.float64)
+        uf, vf, wf = (np.ascontiguousarray(v, dtype=np.float64) for v in vel)
+        val = np.empty((7, self.npad))
+        self.lib.ora_jac(self.gp, _p(r), _p(uf), _p(vf), _p(wf), float(beta0), float(dt), _p(val))
+        return val
+
+    def spmv(self, val, x):
+        v = np.ascontiguousarray(val, dtype=np.float64)
+        xx = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(self.npad)
+        self.lib.ora_spmv(self.gp, _p(v), _p(xx), _p(y))
+        return y
+
+    def gauss_seidel(self, val, b, iterg=5):
+        v = np.ascontiguousarray(val, dtype=np.float64)
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.empty(self.npad)
+        self.lib.ora_gauss_seidel(self.gp, _p(v), _p(bb), _p(x), iterg)
+        return x
+
+    def psolve(self, val, x, iterg=5):
+        v = np.ascontiguousarray(val, dtype=np.float64)
+        xx = np.ascontiguousarray(x, dtype=np.float64)
+        px = np.empty_like(xx)
+        self.lib.ora_psolve(self.gp, xx.size // self.npad, _p(v), _p(xx), _p(px), iterg)
+        return px
+
+    def matvec(self, val, x):
+        v = np.ascontiguousarray(val, dtype=np.float64)
+        xx = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(xx)
+        self.lib.ora_matvec(self.gp, xx.size // self.npad, _p(v), _p(xx), _p(y))
+        return y
+
+    def dot(self, x, y):
+        xx = np.ascontiguousarray(x, dtype=np.float64)
+        yy = np.ascontiguousarray(y, dtype=np.float64)
+        return self.lib.ora_dot(self.gp, xx.size // self.npad, _p(xx), _p(yy))
+
+    def bicgstab(self, val, x, b, maxiter, tol, iterg=5):
+        """x updated in place; returns (MaxIter, Tol) with the reference's sentinels."""
+        v = np.ascontiguousarray(val, dtype=np.float64)
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        it = C.c_int(maxiter)
+        tl = C.c_double(tol)
+        self.lib.ora_bicgstab(self.gp, x.size // self.npad, _p(v), _p(x), _p(bb), C.byref(it), C.byref(tl), iterg)
+        return it.value, tl.value
+
+    def ros_step(self, c, vel, dt, method=5, tol=1e-6, maxiter=30, iterg=5, rho_pos=0):
+        """c updated in place; returns (iters, resid) per stage."""
+        uf, vf, wf = (np.ascontiguousarray(v, dtype=np.float64) for v in vel)
+        iters = np.zeros(4, dtype=np.int32)
+        resid = np.zeros(4)
+        n = self.lib.ora_ros_step(self.gp, c.size // self.npad, rho_pos, _p(c), _p(uf), _p(vf), _p(wf), float(dt),
+                                  int(method), float(tol), int(maxiter), int(iterg), iters.ctypes.data,
+                                  resid.ctypes.data)
+        return list(iters[:n]), list(resid[:n])
+
+    def total_scalar(self, c):
+        a = np.ascontiguousarray(c, dtype=np.float64)
+        return self.lib.ora_total_scalar(self.gp, _p(a))
+
+
+def ros_coeffs(method: int):
+    lib = load()
+    b0 = C.c_double()
+    al, be, gm = np.zeros(16), np.zeros(16), np.zeros(5)
+    n = lib.ora_ros_coeffs(int(method), C.byref(b0), al.ctypes.data, be.ctypes.data, gm.ctypes.data)
+    return n, b0.value, al.reshape(4, 4), be.reshape(4, 4), gm
+
+
+def tri_solve(d, u, l, b):
+    lib = load()
+    d, u, l = (np.ascontiguousarray(a, dtype=np.float64) for a in (d, u, l))
+    x = np.ascontiguousarray(b, dtype=np.float64).copy()
+    ncol, n1 = d.shape
+    lib.ora_tri_solve(ncol, n1, _p(d), _p(u), _p(l), _p(x))
+    return x
+
+
+def tri_matvec(d, u, l, x):
+    lib = load()
+    d, u, l, xx = (np.ascontiguousarray(a, dtype=np.float64) for a in (d, u, l, x))
+    ncol, n1 = d.shape
+    y = np.empty_like(xx)
+    lib.ora_tri_matvec(ncol, n1, _p(d), _p(u), _p(l), _p(xx), _p(y))
+    return y

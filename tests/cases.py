@@ -1,0 +1,57 @@
+"""Small seeded cases shared by the tests (sizes the oracle finishes in seconds)."""
+from __future__ import annotations
+
+import functools
+
+import numpy as np
+
+from asam_gb300 import geometry as G
+
+
+def _flat(nx, ny, nz, u0=10.0, v0=0.0, per_x=True, per_y=True, seed=1):
+    grid = G.Grid(nx, ny, nz, 100.0, 100.0, G.uniform_levels(nz, 100.0), per_x, per_y, False)
+    geo = G.cut_cell_geometry(grid, None, snap=0.0, merge=0.0)
+    vel = G.face_velocity(geo, u0, v0)
+    if not per_x:
+        vel[0][:, :, 0] = 0.0
+        vel[0][:, :, -1] = 0.0
+    if not per_y:
+        vel[1][:, 0, :] = 0.0
+        vel[1][:, -1, :] = 0.0
+    st = G.initial_state(geo, *vel, theta0=300.0, bubble_amp=2.0, bubble_radius=400.0, bubble_z=500.0, noise=0.01,
+                         seed=seed)
+    return geo, vel, st
+
+
+def _hill(nx, ny, nz, u0=10.0, v0=0.0, seed=2, height=600.0, halfwidth=800.0):
+    grid = G.Grid(nx, ny, nz, 200.0, 200.0, G.stretched_levels(nz, 50.0, 400.0))
+    h = G.gaussian_hill_terrain(grid, height, halfwidth, 50.0, 600.0, seed=seed)
+    geo = G.cut_cell_geometry(grid, h, snap=0.01, merge=0.1)
+    vel = G.face_velocity(geo, u0, v0)
+    st = G.initial_state(geo, *vel, theta0=300.0, n_bv=0.01, moist=True, tracer=True, seed=seed + 7)
+    return geo, vel, st
+
+
+CASES = {
+    "bubble_12x10x8": lambda: _flat(12, 10, 8),
+    "hill_24x20x16": lambda: _hill(24, 20, 16),
+    "hill_odd_13x7x9_reverse": lambda: _hill(13, 7, 9, u0=-7.0, v0=4.0, seed=5),
+    "flat_walls_9x6x5": lambda: _flat(9, 6, 5, u0=3.0, v0=-2.0, per_x=False, per_y=False),
+    "column_1x1x12": lambda: _flat(1, 1, 12, u0=2.0, v0=1.0),
+    "slab_1x9x6": lambda: _hill(1, 9, 6, u0=5.0, v0=-3.0, seed=9),
+}
+
+
+@functools.lru_cache(maxsize=None)
+def get(name: str):
+    return CASES[name]()
+
+
+def relerr(a: np.ndarray, b: np.ndarray) -> float:
+    """max |a-b| / max |b| (field-normwise), with a floor for all-zero fields."""
+    den = max(float(np.max(np.abs(b))), 1e-300)
+    return float(np.max(np.abs(a - b))) / den
+
+
+def field_relerr(a: np.ndarray, b: np.ndarray) -> list[float]:
+    return [relerr(a[i], b[i]) for i in range(a.shape[0])]

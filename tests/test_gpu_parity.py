@@ -1,0 +1,210 @@
+"""Parity of the CUDA library (through the C-ABI) with the CPU oracle.
+
+Bit-exact where the kernel restates the reference's operation order
+(flux RHS, Jacobian, stage operator, preconditioner, Thomas); the Krylov
+solves and the Rosenbrock step differ only by the summation order of the dot
+products and are held to 1e-12 relative per field (the drop-in tolerance),
+with BiCGStab iteration counts equal or within one.
+"""
+import numpy as np
+import pytest
+
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12  # relative, per prognostic field
+REFINED_TOL = 1e-10  # FP32-refined vs FP64 oracle
+
+ALL = list(cases.CASES)
+
+
+@pytest.fixture(scope="module")
+def env(built_lib):
+    import asam_gb300
+    import oracle
+
+    return asam_gb300, oracle
+
+
+def _block(env, name, **kw):
+    asam, _ = env
+    geo, vel, st = cases.get(name)
+    blk = asam.TransportBlock(geo, ncomp=st.c.shape[0], rho_pos=st.rho_pos, **kw)
+    blk.set_velocity(*vel)
+    return blk
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_exchange_cell_bitwise(env, name):
+    _, oracle = env
+    geo, vel, st = cases.get(name)
+    with _block(env, name) as blk:
+        got = blk.ExchangeCell(st.c)
+    ref = oracle.Oracle(geo).exchange_cell(st.c)
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_fcn_bitwise(env, name):
+    _, oracle = env
+    geo, vel, st = cases.get(name)
+    o = oracle.Oracle(geo)
+    c = o.exchange_cell(st.c)
+    ref = o.fcn(c, vel, st.rho_pos)
+    with _block(env, name) as blk:
+        got = blk.Fcn(c)
+    assert np.isfinite(got).all()
+    diff = np.argwhere(got != ref)
+    assert diff.size == 0, f"{len(diff)} mismatches, first {diff[:3].tolist()} max rel {cases.relerr(got, ref):.3e}"
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_div_bitwise(env, name):
+    _, oracle = env
+    geo, vel, st = cases.get(name)
+    rhs = np.ascontiguousarray(st.c[0])
+    ref = oracle.Oracle(geo).div(rhs, vel)
+    with _block(env, name) as blk:
+        got = blk.DivCompute(rhs)
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_jac_bitwise(env, name):
+    asam, oracle = env
+    geo, vel, st = cases.get(name)
+    o = oracle.Oracle(geo)
+    c = o.exchange_cell(st.c)
+    n, beta0, *_ = asam.ros_coeffs("Ros3Pw")
+    ref = o.jac(c[st.rho_pos], vel, beta0, 2.0)
+    with _block(env, name, method="Ros3Pw") as blk:
+        blk.Jac(c, 2.0)
+        got = blk.jac_matrix()
+    for d in range(7):
+        assert np.array_equal(got[d], ref[d]), f"diagonal {d}: max rel {cases.relerr(got[d], ref[d]):.3e}"
+
+
+def _system(env, name, dt=2.0):
+    asam, oracle = env
+    geo, vel, st = cases.get(name)
+    o = oracle.Oracle(geo)
+    c = o.exchange_cell(st.c)
+    n, beta0, *_ = asam.ros_coeffs("RosRK3")
+    val = o.jac(c[st.rho_pos], vel, beta0, dt)
+    b = dt * o.fcn(c, vel, st.rho_pos)
+    return o, c, val, b
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_matvec_bitwise(env, name):
+    o, c, val, b = _system(env, name)
+    ref = o.matvec(val, c)
+    with _block(env, name) as blk:
+        blk.set_jac_matrix(val)
+        got = blk.MatVecMet(c)
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_psolve_bitwise(env, name):
+    o, c, val, b = _system(env, name)
+    ref = o.psolve(val, b)
+    with _block(env, name) as blk:
+        blk.set_jac_matrix(val)
+        got = blk.PSolve(b)
+    diff = np.argwhere(got != ref)
+    assert diff.size == 0, f"{len(diff)} mismatches, first {diff[:3].tolist()} max rel {cases.relerr(got, ref):.3e}"
+
+
+@pytest.mark.parametrize("name", ALL)
+@pytest.mark.parametrize("tol", [1e-6, 1e-10])
+def test_bicgstab(env, name, tol):
+    o, c, val, b = _system(env, name, dt=20.0)
+    xr = np.zeros_like(b)
+    it_r, tol_r = o.bicgstab(val, xr, b, 30, tol)
+    with _block(env, name) as blk:
+        blk.set_jac_matrix(val)
+        xg = np.zeros_like(b)
+        it_g, tol_g = blk.BiCGStabMetSp(xg, b, 30, tol)
+    assert abs(abs(it_g) - abs(it_r)) <= 1, (it_g, it_r)
+    if it_g == it_r:
+        errs = cases.field_relerr(xg, xr)
+        assert max(errs) <= FP64_TOL, errs
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_ros_step_fp64(env, name):
+    asam, oracle = env
+    geo, vel, st = cases.get(name)
+    o = oracle.Oracle(geo)
+    cr = st.c.copy()
+    cg = st.c.copy()
+    with _block(env, name, method="RosRK3", bicgstab_tol=1e-10) as blk:
+        for step in range(3):
+            it_r, _ = o.ros_step(cr, vel, 2.0, method=asam.METHODS["RosRK3"], tol=1e-10)
+            it_g, _ = blk.Ros3MetC(cg, 2.0)
+            for a, b in zip(it_g, it_r):
+                assert abs(abs(a) - abs(b)) <= 1, (step, it_g, it_r)
+            errs = cases.field_relerr(cg, cr)
+            assert max(errs) <= FP64_TOL, (step, errs)
+
+
+@pytest.mark.parametrize("method", ["Ros3AMF", "RosRK32", "RosEul", "Ros3P", "Ros3Pw", "RosTVD", "RosRK4"])
+def test_ros_methods(env, method):
+    asam, oracle = env
+    name = "hill_24x20x16"
+    geo, vel, st = cases.get(name)
+    o = oracle.Oracle(geo)
+    cr, cg = st.c.copy(), st.c.copy()
+    o.ros_step(cr, vel, 5.0, method=asam.METHODS[method], tol=1e-10)
+    with _block(env, name, method=method, bicgstab_tol=1e-10) as blk:
+        blk.Ros3MetC(cg, 5.0)
+    assert max(cases.field_relerr(cg, cr)) <= FP64_TOL
+
+
+def test_ros_coeffs_match_oracle(env):
+    asam, oracle = env
+    for m, mid in asam.METHODS.items():
+        a = asam.ros_coeffs(m)
+        b = oracle.ros_coeffs(mid)
+        assert a[0] == b[0] and a[1] == b[1]
+        assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3]) and np.array_equal(a[4], b[4])
+
+
+@pytest.mark.parametrize("name", ["hill_24x20x16", "hill_odd_13x7x9_reverse"])
+def test_ros_step_refined(env, name):
+    asam, oracle = env
+    geo, vel, st = cases.get(name)
+    o = oracle.Oracle(geo)
+    cr, cg = st.c.copy(), st.c.copy()
+    with _block(env, name, method="RosRK3", bicgstab_tol=1e-12, precision="fp32_refined") as blk:
+        for _ in range(2):
+            o.ros_step(cr, vel, 4.0, method=asam.METHODS["RosRK3"], tol=1e-12)
+            blk.Ros3MetC(cg, 4.0)
+    errs = cases.field_relerr(cg, cr)
+    assert max(errs) <= REFINED_TOL, errs
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_total_scalar(env, name):
+    _, oracle = env
+    geo, vel, st = cases.get(name)
+    ref = oracle.Oracle(geo).total_scalar(np.ascontiguousarray(st.c[0]))
+    with _block(env, name) as blk:
+        got = blk.TotalScalar(st.c, 0)
+    assert abs(got - ref) <= 1e-13 * abs(ref)
+
+
+@pytest.mark.parametrize("ncol,n1", [(1, 1), (7, 2), (33, 64), (1000, 128)])
+def test_thomas_bitwise(env, ncol, n1):
+    asam, oracle = env
+    rng = np.random.default_rng(ncol * 1000 + n1)
+    d = 4.0 + rng.random((ncol, n1))
+    u = rng.standard_normal((ncol, max(n1 - 1, 0)))
+    l = rng.standard_normal((ncol, max(n1 - 1, 0)))
+    b = rng.standard_normal((ncol, n1))
+    ref = oracle.tri_solve(d, u, l, b)
+    got = asam.Solve_1D(d, u, l, b)
+    assert np.array_equal(got, ref)
+    assert np.array_equal(asam.MatVecT_1D(d, u, l, b), oracle.tri_matvec(d, u, l, b))
