@@ -106,6 +106,7 @@ class TransportBlock:
         return a
 
     def set_stream(self, stream_handle: int | None):
+        """cudaStream_t as an integer; 0/None selects the legacy default stream."""
         check(self.lib.asam_set_stream(self.h, stream_handle or None), "asam_set_stream")
 
     def state_device_ptr(self) -> int:

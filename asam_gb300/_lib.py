@@ -63,6 +63,7 @@ SIGNATURES = [
     ("asam_npad", C.c_longlong, [C.POINTER(AsamConfig)]),
     ("asam_probe_fp64_fma", C.c_int, [C.c_int, _D]),
     ("asam_launch_count", C.c_longlong, []),
+    ("asam_probe_div", C.c_int, [C.c_longlong, C.c_longlong, C.c_int, C.POINTER(C.c_longlong)]),
     ("asam_last_error", C.c_char_p, []),
 ]
 

@@ -219,6 +219,9 @@ struct asam_ctx {
   // stage storage
   double *c = nullptr, *cold = nullptr, *rhs = nullptr, *incr = nullptr, *phi = nullptr;
   double *gx = nullptr, *gy = nullptr, *gz = nullptr;
+  double *coef_x = nullptr, *coef_y = nullptr, *coef_z = nullptr;  // per-face flux coefficients
+  unsigned char *mask_x = nullptr, *mask_y = nullptr, *mask_z = nullptr;
+  double* rvol = nullptr;  // 1/(VolC+Eps)
   double* val = nullptr;
   float* val32 = nullptr;
   Work<double> w64;
@@ -262,7 +265,8 @@ int reduce_to_host(asam_ctx* h, double* out) {
   return kOk;
 }
 
-// PSolve_Vec4CellSp: copy, exchange, 1+IterG Gauss-Seidel sweeps, zero halo, exchange.
+// PSolve_Vec4CellSp: copy, exchange, 1+IterG Gauss-Seidel sweeps (one
+// pipelined wavefront), zero halo, exchange.
 template <typename T>
 void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w) {
   const Launch& L = h->L;
@@ -270,11 +274,7 @@ void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w) {
   const int nc = h->cfg.ncomp;
   cudaMemcpyAsync(w.bbuf, in, h->len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream);
   launch_exchange_cell(L, d, nc, w.bbuf);
-  launch_gs_lower(L, d, nc, val, w.bbuf, out);
-  for (int s = 0; s < h->cfg.gs_iter; ++s) {
-    launch_gs_upper(L, d, nc, val, w.bbuf, out, w.tbuf);
-    launch_gs_lower(L, d, nc, val, w.tbuf, out);
-  }
+  launch_gs_sweeps(L, d, nc, val, w.bbuf, out, w.tbuf, 1 + h->cfg.gs_iter);
   launch_zero_halo(L, d, nc, out);
   launch_exchange_cell(L, d, nc, out);
 }
@@ -406,15 +406,16 @@ int bicgstab_refined(asam_ctx* h, double* x, const double* b, int* maxiter, doub
 int fcn_dev(asam_ctx* h, const double* c, double* f) {
   const Launch& L = h->L;
   launch_phi(L, h->d, h->cfg.ncomp, h->cfg.rho_pos, c, h->phi);
-  launch_face_flux(L, h->d, h->geom(), h->cfg.ncomp, h->phi, h->gx, h->gy, h->gz);
-  launch_flux_gather(L, h->d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz, f);
+  launch_face_flux(L, h->d, h->geom(), h->cfg.ncomp, h->coef_x, h->coef_y, h->coef_z, h->mask_x, h->mask_y,
+                   h->mask_z, h->phi, h->gx, h->gy, h->gz);
+  launch_flux_gather(L, h->d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz, h->rvol, f);
   return check_launch();
 }
 
 int jac_dev(asam_ctx* h, const double* c, double dt) {
   const double* rho = c + (size_t)h->cfg.rho_pos * h->npad;
   launch_jac(h->L, h->d, h->geom(), rho, h->beta0 * dt, h->val);
-  if (h->cfg.precision == ASAM_PREC_FP32_REFINED) launch_convert_f64_to_f32(h->L, 7 * h->npad, h->val, h->val32);
+  if (h->cfg.precision == ASAM_PREC_FP32_REFINED) launch_convert_f64_to_f32(h->L, 8 * h->npad, h->val, h->val32);
   h->jac_ready = true;
   return check_launch();
 }
@@ -516,8 +517,57 @@ __global__ void k_probe_fp64(int iters, double seed, double* out) {
   if (s == 12345.678) out[0] = s;  // keeps the chains alive
 }
 
+// Check of the FMA-corrected quotient (kernels.cuh div_rn) against the IEEE
+// quotient on pseudo-random operands spanning many binades.
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long x) {
+  x += 0x9e3779b97f4a7c15ULL;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebULL;
+  return x ^ (x >> 31);
+}
+__device__ __forceinline__ double rand_double(unsigned long long h, int span) {
+  // mantissa from the hash, exponent in [-span, span], random sign
+  const double m = 1.0 + (double)(h >> 12) * 0x1.0p-52;
+  const int e = (int)((h >> 3) % (unsigned long long)(2 * span + 1)) - span;
+  return ((h & 1) ? -1.0 : 1.0) * ldexp(m, e);
+}
+__global__ void k_probe_div(unsigned long long n, unsigned long long seed, int span, unsigned long long* bad) {
+  unsigned long long cnt = 0;
+  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
+       q += (unsigned long long)gridDim.x * blockDim.x) {
+    const double x = rand_double(splitmix(seed ^ (2 * q)), span);
+    const double dd = rand_double(splitmix(seed ^ (2 * q + 1)), span);
+    const double r = 1.0 / dd;
+    const double q0 = __dmul_rn(x, r);
+    const double e = __fma_rn(-q0, dd, x);
+    const double qq = __fma_rn(e, r, q0);
+    if (qq != x / dd) ++cnt;
+  }
+  if (cnt) atomicAdd(bad, cnt);
+}
+
 // ---------------------------------------------------------------------------
 extern "C" {
+
+int asam_probe_div(long long n, long long seed, int span, long long* mismatches) {
+  if (n < 1 || !mismatches || span < 0 || span > 500) return kBadArg;
+  unsigned long long* d;
+  CK(cudaMalloc((void**)&d, sizeof(unsigned long long)));
+  CK(cudaMemset(d, 0, sizeof(unsigned long long)));
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  k_probe_div<<<sms * 8, 256>>>((unsigned long long)n, (unsigned long long)seed, span, d);
+  unsigned long long h = 0;
+  cudaError_t e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+    return kCudaError;
+  }
+  *mismatches = (long long)h;
+  return check_launch();
+}
 
 int asam_probe_fp64_fma(int iters, double* gflops) {
   if (iters < 1 || !gflops) return kBadArg;
@@ -559,8 +609,13 @@ int asam_ros_coeffs(int method, double* beta0, double* alpha, double* beta, doub
 
 int asam_destroy(asam_ctx* h) {
   if (!h) return kOk;
-  double* dptrs[] = {h->volc, h->fu, h->fv, h->fw, h->uf, h->vf, h->wf, h->c, h->cold, h->rhs, h->incr, h->phi,
-                     h->gx, h->gy, h->gz, h->val, h->dcorr, h->partial, h->red_out, h->stage_a, h->stage_b};
+  double* dptrs[] = {h->volc, h->fu,     h->fv,     h->fw,     h->uf,     h->vf,      h->wf,      h->c,
+                     h->cold, h->rhs,    h->incr,   h->phi,    h->gx,     h->gy,      h->gz,      h->val,
+                     h->dcorr, h->partial, h->red_out, h->stage_a, h->stage_b, h->coef_x, h->coef_y, h->coef_z,
+                     h->rvol};
+  unsigned char* bptrs[] = {h->mask_x, h->mask_y, h->mask_z};
+  for (unsigned char* p : bptrs)
+    if (p) cudaFree(p);
   for (double* p : dptrs)
     if (p) cudaFree(p);
   if (h->val32) cudaFree(h->val32);
@@ -619,17 +674,22 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
                 {&h->uf, d.n_uf()},       {&h->vf, d.n_vf()},        {&h->wf, d.n_wf()},        {&h->c, h->len},
                 {&h->cold, h->len},       {&h->rhs, h->len},         {&h->incr, h->len * h->nstage},
                 {&h->phi, h->len},        {&h->gx, d.n_uf() * cfg->ncomp}, {&h->gy, d.n_vf() * cfg->ncomp},
-                {&h->gz, d.n_wf() * cfg->ncomp}, {&h->val, 7 * h->npad}, {&h->partial, (size_t)kRedGrid},
-                {&h->red_out, 1},         {&h->stage_a, h->len},     {&h->stage_b, h->len}};
+                {&h->gz, d.n_wf() * cfg->ncomp}, {&h->val, 8 * h->npad}, {&h->partial, (size_t)kRedGrid},
+                {&h->red_out, 1},         {&h->stage_a, h->len},     {&h->stage_b, h->len},
+                {&h->coef_x, 4 * d.n_uf()}, {&h->coef_y, 4 * d.n_vf()}, {&h->coef_z, 4 * d.n_wf()},
+                {&h->rvol, h->npad}};
   for (auto& a : allocs)
     if ((e = cudaMalloc((void**)a.p, a.n * sizeof(double))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc((void**)&h->mask_x, d.n_uf())) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc((void**)&h->mask_y, d.n_vf())) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc((void**)&h->mask_z, d.n_wf())) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc((void**)&h->sc, sizeof(KrylovScalars))) != cudaSuccess) return fail(e);
   if ((e = cudaMallocHost((void**)&h->sc_host, sizeof(KrylovScalars))) != cudaSuccess) return fail(e);
   if ((e = cudaMallocHost((void**)&h->red_host, sizeof(double))) != cudaSuccess) return fail(e);
   if ((e = alloc_work(h->w64, h->len)) != cudaSuccess) return fail(e);
   if (cfg->precision == ASAM_PREC_FP32_REFINED) {
     if ((e = alloc_work(h->w32, h->len)) != cudaSuccess) return fail(e);
-    if ((e = cudaMalloc((void**)&h->val32, 7 * h->npad * sizeof(float))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&h->val32, 8 * h->npad * sizeof(float))) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&h->x32, h->len * sizeof(float))) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&h->b32, h->len * sizeof(float))) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&h->dcorr, h->len * sizeof(double))) != cudaSuccess) return fail(e);
@@ -646,13 +706,17 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
   for (int q = 0; q < 3; ++q)
     if ((e = cudaMemset(zero[q], 0, nz[q] * sizeof(double))) != cudaSuccess) return fail(e);
   if ((e = cudaMemset(h->c, 0, h->len * sizeof(double))) != cudaSuccess) return fail(e);
+  launch_recip_eps(h->L, h->npad, h->volc, h->rvol);
+  launch_face_coef(h->L, d, h->geom(), h->coef_x, h->coef_y, h->coef_z, h->mask_x, h->mask_y, h->mask_z);
+  if ((e = cudaStreamSynchronize(h->L.stream)) != cudaSuccess) return fail(e);
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
   *out = h;
   return kOk;
 }
 
 int asam_set_stream(asam_ctx* h, void* stream) {
   if (!h) return kBadArg;
-  h->L.stream = stream ? (cudaStream_t)stream : h->own_stream;
+  h->L.stream = (cudaStream_t)stream;  // NULL: the legacy default stream
   return kOk;
 }
 
@@ -674,8 +738,9 @@ int asam_set_velocity(asam_ctx* h, const double* uf, const double* vf, const dou
   CK(cudaMemcpyAsync(h->uf, uf, d.n_uf() * sizeof(double), cudaMemcpyDefault, h->L.stream));
   CK(cudaMemcpyAsync(h->vf, vf, d.n_vf() * sizeof(double), cudaMemcpyDefault, h->L.stream));
   CK(cudaMemcpyAsync(h->wf, wf, d.n_wf() * sizeof(double), cudaMemcpyDefault, h->L.stream));
+  launch_face_coef(h->L, d, h->geom(), h->coef_x, h->coef_y, h->coef_z, h->mask_x, h->mask_y, h->mask_z);
   CK(cudaStreamSynchronize(h->L.stream));
-  return kOk;
+  return check_launch();
 }
 
 int asam_exchange_cell(asam_ctx* h, int ncomp, double* c) {
@@ -735,7 +800,8 @@ int asam_get_jac(asam_ctx* h, double* val) {
 int asam_set_jac(asam_ctx* h, const double* val) {
   if (!h || !val) return kBadArg;
   CK(cudaMemcpyAsync(h->val, val, 7 * h->npad * sizeof(double), cudaMemcpyDefault, h->L.stream));
-  if (h->cfg.precision == ASAM_PREC_FP32_REFINED) launch_convert_f64_to_f32(h->L, 7 * h->npad, h->val, h->val32);
+  launch_recip_diag(h->L, h->npad, h->val);
+  if (h->cfg.precision == ASAM_PREC_FP32_REFINED) launch_convert_f64_to_f32(h->L, 8 * h->npad, h->val, h->val32);
   CK(cudaStreamSynchronize(h->L.stream));
   h->jac_ready = true;
   return check_launch();

@@ -13,6 +13,11 @@ __global__ void k_cvt_f2d(size_t len, const float* __restrict__ x, double* __res
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
     y[q] = (double)x[q];
 }
+// slot 7 of the DIA storage: 1/diagonal (IEEE division)
+__global__ void k_recip_diag(size_t n, double* __restrict__ val) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    val[7 * n + q] = 1.0 / val[3 * n + q];
+}
 }  // namespace
 
 namespace asam {
@@ -24,6 +29,10 @@ void launch_mass(const Launch& L, const Dims& d, const double* c, const double* 
   k_mass_partial<<<RED_GRID, RED_BLOCK, 0, L.stream>>>(d, c, volc, partial);
   k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, RED_GRID, nullptr, -1, out);
   count_launches(2);
+}
+void launch_recip_diag(const Launch& L, size_t npad, double* val) {
+  k_recip_diag<<<gs_grid(L, npad), kBlock, 0, L.stream>>>(npad, val);
+  count_launches(1);
 }
 void launch_convert_f64_to_f32(const Launch& L, size_t len, const double* x, float* y) {
   k_cvt_d2f<<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, x, y);

@@ -16,6 +16,22 @@ __device__ __forceinline__ T eps_t() {
   return (T)1.0e-30;
 }
 
+// Correctly rounded quotient x/d from a precomputed rinv = RN(1/d), by one
+// FMA correction step (Markstein, "Computation of elementary functions on the
+// IBM RISC System/6000 processor", IBM J. Res. Dev. 34, 1990): q0 = RN(x*rinv),
+// e = x - q0*d (exact with an FMA), q = RN(q0 + e*rinv).  Agreement with the
+// IEEE quotient is checked on the device by asam_probe_div.
+__device__ __forceinline__ double div_rn(double x, double d, double rinv) {
+  const double q0 = __dmul_rn(x, rinv);
+  const double e = __fma_rn(-q0, d, x);
+  return __fma_rn(e, rinv, q0);
+}
+__device__ __forceinline__ float div_rn(float x, float d, float rinv) {
+  const float q0 = __fmul_rn(x, rinv);
+  const float e = __fmaf_rn(-q0, d, x);
+  return __fmaf_rn(e, rinv, q0);
+}
+
 // ---------------------------------------------------------------------------
 // Limiter and stencil coefficients: ADVECT/Advection_Mod.f90:2118-2134
 // (k1F, k2F, PhiLim with MethAdv='Koren').
@@ -38,70 +54,44 @@ __device__ __forceinline__ T koren(T r, T k1, T k2) {
   return (T)0 > m ? (T)0 : m;
 }
 
-// Outflow flux of the upwind cell C through one of its faces, as computed
-// inside the triple loop of ADVECT/Advection_Mod.f90:854-974.
-//   right=true : flux through the right face (velocity > 0), ":885-894"
-//   right=false: flux through the left face (velocity < 0), ":875-884"
-// pL,pC,pR: c/(Rho+Eps) of the cells left/centre/right of C along the axis,
-// VL..VR volumes, FL/FR the left/right face areas of C, vblend: x-axis only.
-template <typename T>
-__device__ __forceinline__ T upwind_flux(T cL, T cC, T cR, T VL, T VC, T VR, T FL, T FR, T vel, bool right,
-                                         bool vblend) {
-  const T e = eps_t<T>();
-  if (vblend) {
-    if (VL < VC) cL = ((VC - VL) * cC + VL * cL) / VC;
-    if (VR < VC) cR = ((VC - VR) * cC + VR * cR) / VC;
-  }
-  if (FL < FR) cL = ((FR - FL) * cC + FL * cL) / FR;
-  if (FR < FL) cR = ((FL - FR) * cC + FR * cR) / FL;
-  const T half = (T)0.5;
-  if (!right) {
-    T k1 = k1f(VR, VC, VL);
-    T k2 = k2f(VR, VC, VL);
-    T cDiff = cR - cC;
-    T r = (cC - cL + e) / (cDiff + e);
-    return half * (fabs(vel) - vel) * FL * (cC + FR / (FR + e) * (koren(r, k1, k2) * (cC - cR)));
-  } else {
-    T k1 = k1f(VL, VC, VR);
-    T k2 = k2f(VL, VC, VR);
-    T cDiff = cC - cL;
-    T r = (cR - cC + e) / (cDiff + e);
-    return half * (fabs(vel) + vel) * FR * (cC + FL / (FL + e) * (koren(r, k1, k2) * (cC - cL)));
-  }
-}
-
 using asam::GeomT;
 
-// phi = c/(Rho+Eps) over the padded box, all components
+// phi = c/(Rho+Eps) over the padded box, all components.  One IEEE
+// reciprocal of Rho+Eps per cell, then the correctly rounded quotient per
+// component (div_rn), identical to the reference's c/(Rho+Eps).
 template <typename T>
 __global__ void k_phi(Dims d, int ncomp, int rho_pos, const T* __restrict__ c, T* __restrict__ phi) {
   const size_t n = d.npad();
   const T e = eps_t<T>();
   const T* rho = c + (size_t)rho_pos * n;
   for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
-    T rp = rho[P] + e;
-    for (int ic = 0; ic < ncomp; ++ic) phi[ic * n + P] = c[ic * n + P] / rp;
+    const T rp = rho[P] + e;
+    const T rr = (T)1 / rp;
+    for (int ic = 0; ic < ncomp; ++ic) phi[ic * n + P] = div_rn(c[ic * n + P], rp, rr);
   }
 }
 
-// Face fluxes.  axis 0: x faces (i in [0,nx], j,k interior) stored at UF(i,j,k);
-// axis 1: y faces at VF; axis 2: z faces at WF.  g[ic*nface + face] holds the
-// flux computed by the reference's loop for the upwind interior cell of the
-// face (zero when the upwind cell is a halo cell or the velocity is zero).
+// Per-face coefficients of the flux (geometry and face velocity only, so
+// they are computed once when the velocities are set):
+//   coef[0] = +/- Half*(ABS(u)+/-u)*F  (sign: + upwind cell left of the face,
+//             - upwind cell right of it, 0 no flux in the reference's loop)
+//   coef[1] = F_other/(F_other+Eps), coef[2] = k1, coef[3] = k2 of the upwind cell
+//   mask bits: 1 VL<VC, 2 VR<VC (x only), 4 FL<FR, 8 FR<FL (blends of :868-871)
+// with the upwind cell's VL, VC, VR, FL, FR as in ADVECT/Advection_Mod.f90:854-974.
 template <typename T, int AXIS>
-__global__ void k_face_flux(Dims d, GeomT<T> g, int ncomp, const T* __restrict__ phi, T* __restrict__ gout) {
+__global__ void k_face_coef(Dims d, GeomT<T> g, T* __restrict__ coef, unsigned char* __restrict__ mask) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int ex = AXIS == 0 ? nx + 1 : nx;
   const int ey = AXIS == 1 ? ny + 1 : ny;
   const int ez = AXIS == 2 ? nz + 1 : nz;
   const size_t nface = (size_t)ex * ey * ez;
-  const size_t n = d.npad();
+  const T e = eps_t<T>();
+  const T half = (T)0.5;
   for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < nface; f += (size_t)gridDim.x * blockDim.x) {
-    int a = (int)(f % ex);
-    size_t rest = f / ex;
-    int b = (int)(rest % ey);
-    int cc = (int)(rest / ey);
-    // face lies between padded cells L=(i,j,k) and R=(i,j,k)+e_axis
+    const int a = (int)(f % ex);
+    const size_t rest = f / ex;
+    const int b = (int)(rest % ey);
+    const int cc = (int)(rest / ey);
     int i, j, k;
     T vel;
     if (AXIS == 0) {
@@ -116,36 +106,127 @@ __global__ void k_face_flux(Dims d, GeomT<T> g, int ncomp, const T* __restrict__
     }
     const int s = AXIS == 0 ? i : (AXIS == 1 ? j : k);
     const int smax = AXIS == 0 ? nx : (AXIS == 1 ? ny : nz);
-    bool right;
-    int ci, cj, ck;
-    if (vel > (T)0 && s >= 1) {
-      right = true;  // upwind cell = L
-      ci = i; cj = j; ck = k;
-    } else if (vel < (T)0 && s + 1 <= smax) {
-      right = false;  // upwind cell = R
-      ci = i + (AXIS == 0); cj = j + (AXIS == 1); ck = k + (AXIS == 2);
-    } else {
+    int orient = 0;
+    if (vel > (T)0 && s >= 1) orient = 1;           // upwind = left cell, its right face
+    else if (vel < (T)0 && s + 1 <= smax) orient = -1;  // upwind = right cell, its left face
+    T c0 = (T)0, c1 = (T)0, c2 = (T)0, c3 = (T)0;
+    unsigned char m = 0;
+    if (orient != 0) {
+      const int ci = i + (orient < 0 && AXIS == 0), cj = j + (orient < 0 && AXIS == 1),
+                ck = k + (orient < 0 && AXIS == 2);
+      const size_t PC = d.P(ci, cj, ck);
+      const size_t stride = AXIS == 0 ? 1 : (AXIS == 1 ? (size_t)d.NX() : (size_t)d.NX() * d.NY());
+      T FL, FR;
+      if (AXIS == 0) {
+        FR = g.fu[d.FU(ci, cj, ck)];
+        FL = g.fu[d.FU(ci - 1, cj, ck)];
+      } else if (AXIS == 1) {
+        FR = g.fv[d.FV(ci, cj, ck)];
+        FL = g.fv[d.FV(ci, cj - 1, ck)];
+      } else {
+        FR = g.fw[d.FW(ci, cj, ck)];
+        FL = g.fw[d.FW(ci, cj, ck - 1)];
+      }
+      const T VL = g.volc[PC - stride], VC = g.volc[PC], VR = g.volc[PC + stride];
+      if (orient > 0) {
+        c0 = half * (fabs(vel) + vel) * FR;
+        c1 = FL / (FL + e);
+        c2 = k1f(VL, VC, VR);
+        c3 = k2f(VL, VC, VR);
+      } else {
+        c0 = -(half * (fabs(vel) - vel) * FL);
+        c1 = FR / (FR + e);
+        c2 = k1f(VR, VC, VL);
+        c3 = k2f(VR, VC, VL);
+      }
+      if (AXIS == 0 && VL < VC) m |= 1;
+      if (AXIS == 0 && VR < VC) m |= 2;
+      if (FL < FR) m |= 4;
+      if (FR < FL) m |= 8;
+    }
+    coef[0 * nface + f] = c0;
+    coef[1 * nface + f] = c1;
+    coef[2 * nface + f] = c2;
+    coef[3 * nface + f] = c3;
+    mask[f] = m;
+  }
+}
+
+// Face fluxes.  axis 0: x faces (i in [0,nx], j,k interior) stored at UF(i,j,k);
+// axis 1: y faces at VF; axis 2: z faces at WF.  gout[ic*nface + face] holds the
+// flux the reference's loop computes for the upwind interior cell of the face
+// (zero when the upwind cell is a halo cell or the velocity is zero):
+//   Half*(ABS(u)+-u)*F*(cC + Fo/(Fo+Eps)*PhiLim(r,k1,k2,...))   (:875-894)
+template <typename T, int AXIS>
+__global__ void k_face_flux(Dims d, GeomT<T> g, int ncomp, const T* __restrict__ coef,
+                            const unsigned char* __restrict__ mask, const T* __restrict__ phi,
+                            T* __restrict__ gout) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int ex = AXIS == 0 ? nx + 1 : nx;
+  const int ey = AXIS == 1 ? ny + 1 : ny;
+  const int ez = AXIS == 2 ? nz + 1 : nz;
+  const size_t nface = (size_t)ex * ey * ez;
+  const size_t n = d.npad();
+  const T e = eps_t<T>();
+  for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < nface; f += (size_t)gridDim.x * blockDim.x) {
+    const T pref_s = coef[f];
+    if (pref_s == (T)0) {
       for (int ic = 0; ic < ncomp; ++ic) gout[ic * nface + f] = (T)0;
       continue;
+    }
+    const bool right = pref_s > (T)0;
+    const T pref = right ? pref_s : -pref_s;
+    const T ratio = coef[nface + f], k1 = coef[2 * nface + f], k2 = coef[3 * nface + f];
+    const unsigned char m = mask[f];
+    const int a = (int)(f % ex);
+    const size_t rest = f / ex;
+    const int b = (int)(rest % ey);
+    const int cc = (int)(rest / ey);
+    int ci, cj, ck;
+    if (AXIS == 0) {
+      ci = a + !right; cj = b + 1; ck = cc + 1;
+    } else if (AXIS == 1) {
+      ci = a + 1; cj = b + !right; ck = cc + 1;
+    } else {
+      ci = a + 1; cj = b + 1; ck = cc + !right;
     }
     const size_t PC = d.P(ci, cj, ck);
     const size_t stride = AXIS == 0 ? 1 : (AXIS == 1 ? (size_t)d.NX() : (size_t)d.NX() * d.NY());
     const size_t PL = PC - stride, PR = PC + stride;
-    T FL, FR;
-    if (AXIS == 0) {
-      FR = g.fu[d.FU(ci, cj, ck)];
-      FL = g.fu[d.FU(ci - 1, cj, ck)];
-    } else if (AXIS == 1) {
-      FR = g.fv[d.FV(ci, cj, ck)];
-      FL = g.fv[d.FV(ci, cj - 1, ck)];
-    } else {
-      FR = g.fw[d.FW(ci, cj, ck)];
-      FL = g.fw[d.FW(ci, cj, ck - 1)];
+    T VL = (T)0, VC = (T)0, VR = (T)0, FL = (T)0, FR = (T)0;
+    if (m) {  // cut-cell blends (rare): geometry of the upwind cell
+      VL = g.volc[PL];
+      VC = g.volc[PC];
+      VR = g.volc[PR];
+      if (AXIS == 0) {
+        FR = g.fu[d.FU(ci, cj, ck)];
+        FL = g.fu[d.FU(ci - 1, cj, ck)];
+      } else if (AXIS == 1) {
+        FR = g.fv[d.FV(ci, cj, ck)];
+        FL = g.fv[d.FV(ci, cj - 1, ck)];
+      } else {
+        FR = g.fw[d.FW(ci, cj, ck)];
+        FL = g.fw[d.FW(ci, cj, ck - 1)];
+      }
     }
-    const T VL = g.volc[PL], VC = g.volc[PC], VR = g.volc[PR];
     for (int ic = 0; ic < ncomp; ++ic) {
       const T* ph = phi + ic * n;
-      gout[ic * nface + f] = upwind_flux<T>(ph[PL], ph[PC], ph[PR], VL, VC, VR, FL, FR, vel, right, AXIS == 0);
+      T cL = ph[PL], cC = ph[PC], cR = ph[PR];
+      if (m) {
+        if (m & 1) cL = ((VC - VL) * cC + VL * cL) / VC;
+        if (m & 2) cR = ((VC - VR) * cC + VR * cR) / VC;
+        if (m & 4) cL = ((FR - FL) * cC + FL * cL) / FR;
+        if (m & 8) cR = ((FL - FR) * cC + FR * cR) / FL;
+      }
+      T flux;
+      if (right) {
+        const T r = (cR - cC + e) / ((cC - cL) + e);
+        flux = pref * (cC + ratio * (koren(r, k1, k2) * (cC - cL)));
+      } else {
+        const T r = (cC - cL + e) / ((cR - cC) + e);
+        flux = pref * (cC + ratio * (koren(r, k1, k2) * (cC - cR)));
+      }
+      gout[ic * nface + f] = flux;
     }
   }
 }
@@ -156,7 +237,7 @@ __global__ void k_face_flux(Dims d, GeomT<T> g, int ncomp, const T* __restrict__
 // W,E,S,N,B,T) and AdvectionScale (:2888-2898).  One thread per padded cell.
 template <typename T>
 __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict__ gx, const T* __restrict__ gy,
-                              const T* __restrict__ gz, T* __restrict__ f) {
+                              const T* __restrict__ gz, const T* __restrict__ rvol, T* __restrict__ f) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
   const size_t n = d.npad();
@@ -167,6 +248,7 @@ __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict
     const int j = (int)((P / NX) % NY);
     const int k = (int)(P / ((size_t)NX * NY));
     const T V = g.volc[P];
+    const T Ve = V + e, rV = rvol[P];
     const bool ii = i >= 1 && i <= nx, jj = j >= 1 && j <= ny, kk = k >= 1 && k <= nz;
     if (ii && jj && kk) {
       const size_t fxL = d.UF(i - 1, j, k), fxR = d.UF(i, j, k);
@@ -196,44 +278,44 @@ __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict
         if (uR < (T)0) a = a + GX[fxR];  // FluxXL of the cell east
         if (vR < (T)0) a = a + GY[fyR];
         if (wR < (T)0) a = a + GZ[fzR];
-        a = a * V / (V + e);
+        a = div_rn(a * V, Ve, rV);
         if (exW) {
           const size_t PH = d.P(nx + 1, j, k), fh = d.UF(nx, j, k);
           T h = g.uf[fh] > (T)0 ? GX[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + h * VH / (VH + e);
+          a = a + div_rn(h * VH, VH + e, rvol[PH]);
         }
         if (exE) {
           const size_t PH = d.P(0, j, k), fh = d.UF(0, j, k);
           T h = g.uf[fh] < (T)0 ? GX[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + h * VH / (VH + e);
+          a = a + div_rn(h * VH, VH + e, rvol[PH]);
         }
         if (exS) {
           const size_t PH = d.P(i, ny + 1, k), fh = d.VF(i, ny, k);
           T h = g.vf[fh] > (T)0 ? GY[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + h * VH / (VH + e);
+          a = a + div_rn(h * VH, VH + e, rvol[PH]);
         }
         if (exN) {
           const size_t PH = d.P(i, 0, k), fh = d.VF(i, 0, k);
           T h = g.vf[fh] < (T)0 ? GY[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + h * VH / (VH + e);
+          a = a + div_rn(h * VH, VH + e, rvol[PH]);
         }
         if (exB) {
           const size_t PH = d.P(i, j, nz + 1), fh = d.WF(i, j, nz);
           T h = g.wf[fh] > (T)0 ? GZ[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + h * VH / (VH + e);
+          a = a + div_rn(h * VH, VH + e, rvol[PH]);
         }
         if (exT) {
           const size_t PH = d.P(i, j, 0), fh = d.WF(i, j, 0);
           T h = g.wf[fh] < (T)0 ? GZ[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + h * VH / (VH + e);
+          a = a + div_rn(h * VH, VH + e, rvol[PH]);
         }
-        f[ic * n + P] = a / (V + e);
+        f[ic * n + P] = div_rn(a, Ve, rV);
       }
     } else {
       // halo cell: only the face-halo cells next to the interior receive a flux
@@ -265,11 +347,18 @@ __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict
           if (axis == 1) a = a + gy[ic * nfy + fidx];
           if (axis == 2) a = a + gz[ic * nfz + fidx];
         }
-        a = a * V / (V + e);
-        f[ic * n + P] = a / (V + e);
+        a = div_rn(a * V, Ve, rV);
+        f[ic * n + P] = div_rn(a, Ve, rV);
       }
     }
   }
+}
+
+// rv = 1/(v + Eps) over n values (IEEE division)
+template <typename T>
+__global__ void k_recip_eps(size_t len, const T* __restrict__ v, T* __restrict__ rv) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
+    rv[q] = (T)1 / (v[q] + eps_t<T>());
 }
 
 // DivCompute, ADVECT/Advection_Mod.f90:2901-2916 (rhs accumulated)
@@ -368,8 +457,11 @@ __global__ void k_jac(Dims d, GeomT<T> g, const T* __restrict__ rho, T bdt, T* _
     if (ii && kk && j == ny + 1) dg = dg - v[5];
     if (ii && jj && k == 0) dg = dg - v[0];
     if (ii && jj && k == nz + 1) dg = dg - v[6];
-    // scale to I - beta0*dt*J (:1857-1862)
-    val[3 * n + P] = (T)1 - bdt * dg;
+    // scale to I - beta0*dt*J (:1857-1862); slot 7 holds 1/diagonal for the
+    // correctly rounded divisions of the Gauss-Seidel sweeps
+    const T diag = (T)1 - bdt * dg;
+    val[3 * n + P] = diag;
+    val[7 * n + P] = (T)1 / diag;
     val[0 * n + P] = -(bdt * v[0]);
     val[1 * n + P] = -(bdt * v[1]);
     val[2 * n + P] = -(bdt * v[2]);
@@ -427,80 +519,74 @@ __global__ void k_matvec(Dims d, int ncomp, const TM* __restrict__ val, const T*
 // (L+D)x_new = b - U*x_old.  Row r of the column-oriented storage receives
 //   U part: columns r+1, r+NX, r+NXY (in that order),
 //   L part: columns r-NXY, r-NX, r-1 (in that order), then the division.
+// The padded box is cut into tiles of GS_TX x GS_TY x GS_TZ cells; tile
+// (I,J,K) depends only on tiles (I-1,J,K), (I,J-1,K), (I,J,K-1) in the lower
+// solve, so all tiles with I+J+K = level are independent.  Inside a tile the
+// cells are visited by hyperplanes a+b+c = l: each thread owns one (b,c) line
+// of one component and walks it in x, so the x-neighbour is in a register and
+// the y/z-neighbours were written at an earlier hyperplane (same block,
+// ordered by __syncthreads) or by an earlier launch.
 // ---------------------------------------------------------------------------
-template <typename TM, typename T>
-__global__ void k_gs_upper(Dims d, int ncomp, const TM* __restrict__ val, const T* __restrict__ b,
-                           const T* __restrict__ x, T* __restrict__ t) {
-  const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
-  const size_t n = d.npad();
-  const size_t sy = (size_t)NX, sz = (size_t)NX * NY;
-  for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(P % NX);
-    const int j = (int)((P / NX) % NY);
-    const int k = (int)(P / sz);
-    const bool hx = i < NX - 1, hy = j < NY - 1, hz = k < NZ - 1;
-    const T v4 = hx ? (T)val[4 * n + P + 1] : (T)0;
-    const T v5 = hy ? (T)val[5 * n + P + sy] : (T)0;
-    const T v6 = hz ? (T)val[6 * n + P + sz] : (T)0;
-    for (int ic = 0; ic < ncomp; ++ic) {
-      const T* xa = x + ic * n;
-      T s = b[ic * n + P];
-      if (hx) s = s - v4 * xa[P + 1];
-      if (hy) s = s - v5 * xa[P + sy];
-      if (hz) s = s - v6 * xa[P + sz];
-      t[ic * n + P] = s;
-    }
-  }
-}
-
-// Lower solve over one level of tiles.  The padded box is cut into tiles of
-// GS_TX x GS_TY x GS_TZ cells; tile (I,J,K) depends only on tiles (I-1,J,K),
-// (I,J-1,K), (I,J,K-1), so all tiles with I+J+K = level are independent.
-// Inside a tile the cells are visited by hyperplanes a+b+c = l: each thread
-// owns one (b,c) line of one component and walks it in x, so the x-neighbour
-// is in a register and the y/z-neighbours were written at an earlier
-// hyperplane (same block, ordered by __syncthreads) or an earlier launch.
 constexpr int GS_TX = 32;
 constexpr int GS_TY = 4;
 constexpr int GS_TZ = 4;
 
+// All 1+IterG sweeps of GaussSeidel_SpDiag in one pipelined wavefront.
+// Sweep s solves (L+D) x^s = b - U x^{s-1} (x^{-1} = 0, i.e. no U part in
+// sweep 0) and trails sweep s-1 by two tile levels: its U-neighbour tiles
+// (I+1,J,K), (I,J+1,K), (I,J,K+1) hold x^{s-1} from the previous launch, so one
+// launch (index tau) runs tile level tau-2s of every sweep s.  x^s lives in
+// buffer s%2 relative to the last sweep (the last sweep writes `out`); within
+// one launch the tile levels read and written in each buffer are disjoint.
+// Per cell the operation order is the reference's: b, U part (columns r+1,
+// r+NX, r+NXY), L part (columns r-NXY, r-NX, r-1), division.
 template <typename TM, typename T>
-__global__ void k_gs_lower_level(Dims d, int ncomp, const TM* __restrict__ val, const T* __restrict__ t, T* x,
-                                 int level, int ntx, int nty, int ntz) {
-  // enumerate tiles of this level: blockIdx.x -> (J,K) pair, I = level-J-K
+__global__ void __launch_bounds__(256) k_gs_pipe(Dims d, int ncomp, const TM* __restrict__ val,
+                                                 const T* __restrict__ b, T* buf_last, T* buf_other, int tau,
+                                                 int nsweep, int ntx, int nty, int ntz, int nlev) {
+  const int s = blockIdx.z;
+  const int L = tau - 2 * s;
+  if (L < 0 || L >= nlev) return;
+  const int K = blockIdx.y;
+  const int Jlo = max(0, L - K - (ntx - 1));
+  const int J = Jlo + (int)blockIdx.x;
+  const int I = L - J - K;
+  if (J >= nty || I < 0 || I >= ntx) return;  // uniform over the block
   const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
   const size_t n = d.npad();
   const size_t sy = (size_t)NX, sz = (size_t)NX * NY;
-  const int pair = blockIdx.x;
-  const int J = pair % nty;
-  const int K = pair / nty;
-  const int I = level - J - K;
-  if (I < 0 || I >= ntx || K >= ntz) return;
+  const bool last_parity = ((nsweep - 1 - s) & 1) == 0;
+  T* xn_all = last_parity ? buf_last : buf_other;        // x^s
+  const T* xo_all = last_parity ? buf_other : buf_last;  // x^{s-1}
   const int lb = threadIdx.x % (GS_TY * GS_TZ);
   const int ic = threadIdx.x / (GS_TY * GS_TZ);
   const int tb = lb % GS_TY, tc = lb / GS_TY;
   const int j = J * GS_TY + tb, k = K * GS_TZ + tc;
   const bool line_ok = ic < ncomp && j < NY && k < NZ;
+  const size_t off = (size_t)(line_ok ? ic : 0) * n;
+  const T* bb = b + off;
+  T* xn = xn_all + off;
+  const T* xo = xo_all + off;
   const int i0 = I * GS_TX;
   T xprev = (T)0;
-  const T* ta = t + (size_t)ic * n;
-  T* xa = x + (size_t)ic * n;
-  const int nlev = GS_TX + GS_TY + GS_TZ - 2;
-  for (int l = 0; l < nlev; ++l) {
+  const int nlev_in = GS_TX + GS_TY + GS_TZ - 2;
+  for (int l = 0; l < nlev_in; ++l) {
     const int a = l - tb - tc;
     const int i = i0 + a;
     if (line_ok && a >= 0 && a < GS_TX && i < NX) {
       const size_t P = (size_t)i + sy * (size_t)j + sz * (size_t)k;
-      T s = ta[P];
-      if (k > 0) s = s - (T)val[0 * n + P - sz] * xa[P - sz];
-      if (j > 0) s = s - (T)val[1 * n + P - sy] * xa[P - sy];
-      if (i > 0) {
-        const T xl = a > 0 ? xprev : xa[P - 1];
-        s = s - (T)val[2 * n + P - 1] * xl;
+      T t = bb[P];
+      if (s > 0) {
+        if (i < NX - 1) t = t - (T)val[4 * n + P + 1] * xo[P + 1];
+        if (j < NY - 1) t = t - (T)val[5 * n + P + sy] * xo[P + sy];
+        if (k < NZ - 1) t = t - (T)val[6 * n + P + sz] * xo[P + sz];
       }
-      s = s / (T)val[3 * n + P];
-      xa[P] = s;
-      xprev = s;
+      if (k > 0) t = t - (T)val[0 * n + P - sz] * xn[P - sz];
+      if (j > 0) t = t - (T)val[1 * n + P - sy] * xn[P - sy];
+      if (i > 0) t = t - (T)val[2 * n + P - 1] * (a > 0 ? xprev : xn[P - 1]);
+      t = div_rn(t, (T)val[3 * n + P], (T)val[7 * n + P]);
+      xn[P] = t;
+      xprev = t;
     }
     __syncthreads();
   }

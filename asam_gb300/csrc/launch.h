@@ -13,15 +13,19 @@ struct Launch {
 
 #define ASAM_DECLARE_LAUNCHERS(T, TM)                                                                            \
   void launch_phi(const Launch&, const Dims&, int ncomp, int rho_pos, const T* c, T* phi);                      \
-  void launch_face_flux(const Launch&, const Dims&, const GeomT<T>&, int ncomp, const T* phi, T* gx, T* gy,      \
-                        T* gz);                                                                                  \
+  void launch_face_coef(const Launch&, const Dims&, const GeomT<T>&, T* coef_x, T* coef_y, T* coef_z,           \
+                        unsigned char* mask_x, unsigned char* mask_y, unsigned char* mask_z);                    \
+  void launch_face_flux(const Launch&, const Dims&, const GeomT<T>&, int ncomp, const T* coef_x, const T* coef_y, \
+                        const T* coef_z, const unsigned char* mask_x, const unsigned char* mask_y,               \
+                        const unsigned char* mask_z, const T* phi, T* gx, T* gy, T* gz);                         \
   void launch_flux_gather(const Launch&, const Dims&, const GeomT<T>&, int ncomp, const T* gx, const T* gy,      \
-                          const T* gz, T* f);                                                                    \
+                          const T* gz, const T* rvol, T* f);                                                     \
+  void launch_recip_eps(const Launch&, size_t len, const T* v, T* rv);                                          \
   void launch_div(const Launch&, const Dims&, const GeomT<T>&, T* rhs);                                          \
   void launch_jac(const Launch&, const Dims&, const GeomT<T>&, const T* rho, T bdt, T* val);                     \
   void launch_matvec(const Launch&, const Dims&, int ncomp, const TM* val, const T* x, T* y, int plain_spmv);    \
-  void launch_gs_upper(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, const T* x, T* t);      \
-  void launch_gs_lower(const Launch&, const Dims&, int ncomp, const TM* val, const T* t, T* x);                  \
+  void launch_gs_sweeps(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, T* out, T* work,       \
+                        int nsweep);                                                                             \
   void launch_zero_halo(const Launch&, const Dims&, int ncomp, T* x);                                           \
   void launch_exchange_cell(const Launch&, const Dims&, int ncomp, T* c);                                       \
   void launch_dot(const Launch&, const Dims&, int ncomp, const T* x, const T* y, double* partial,               \
@@ -41,6 +45,7 @@ ASAM_DECLARE_LAUNCHERS(double, double)
 ASAM_DECLARE_LAUNCHERS(float, float)
 
 void launch_beta(const Launch&, KrylovScalars* sc);
+void launch_recip_diag(const Launch&, size_t npad, double* val);
 void launch_mass(const Launch&, const Dims&, const double* c, const double* volc, double* partial, double* out);
 void launch_convert_f64_to_f32(const Launch&, size_t len, const double* x, float* y);
 void launch_convert_f32_to_f64(const Launch&, size_t len, const float* x, double* y);

@@ -22,15 +22,29 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
   void launch_phi(const Launch& L, const Dims& d, int ncomp, int rho_pos, const T* c, T* phi) {                   \
     k_phi<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, rho_pos, c, phi); count_launches(1);                            \
   }                                                                                                                \
-  void launch_face_flux(const Launch& L, const Dims& d, const GeomT<T>& g, int ncomp, const T* phi, T* gx, T* gy,  \
-                        T* gz) {                                                                                   \
-    k_face_flux<T, 0><<<gs_grid(L, d.n_uf()), kBlock, 0, L.stream>>>(d, g, ncomp, phi, gx); count_launches(1);                        \
-    k_face_flux<T, 1><<<gs_grid(L, d.n_vf()), kBlock, 0, L.stream>>>(d, g, ncomp, phi, gy); count_launches(1);                        \
-    k_face_flux<T, 2><<<gs_grid(L, d.n_wf()), kBlock, 0, L.stream>>>(d, g, ncomp, phi, gz); count_launches(1);                        \
+  void launch_face_coef(const Launch& L, const Dims& d, const GeomT<T>& g, T* cx, T* cy, T* cz, unsigned char* mx,  \
+                        unsigned char* my, unsigned char* mz) {                                                    \
+    k_face_coef<T, 0><<<gs_grid(L, d.n_uf()), kBlock, 0, L.stream>>>(d, g, cx, mx);                               \
+    k_face_coef<T, 1><<<gs_grid(L, d.n_vf()), kBlock, 0, L.stream>>>(d, g, cy, my);                               \
+    k_face_coef<T, 2><<<gs_grid(L, d.n_wf()), kBlock, 0, L.stream>>>(d, g, cz, mz);                               \
+    count_launches(3);                                                                                             \
+  }                                                                                                                \
+  void launch_face_flux(const Launch& L, const Dims& d, const GeomT<T>& g, int ncomp, const T* cx, const T* cy,    \
+                        const T* cz, const unsigned char* mx, const unsigned char* my, const unsigned char* mz,    \
+                        const T* phi, T* gx, T* gy, T* gz) {                                                       \
+    k_face_flux<T, 0><<<gs_grid(L, d.n_uf()), kBlock, 0, L.stream>>>(d, g, ncomp, cx, mx, phi, gx);               \
+    k_face_flux<T, 1><<<gs_grid(L, d.n_vf()), kBlock, 0, L.stream>>>(d, g, ncomp, cy, my, phi, gy);               \
+    k_face_flux<T, 2><<<gs_grid(L, d.n_wf()), kBlock, 0, L.stream>>>(d, g, ncomp, cz, mz, phi, gz);               \
+    count_launches(3);                                                                                             \
   }                                                                                                                \
   void launch_flux_gather(const Launch& L, const Dims& d, const GeomT<T>& g, int ncomp, const T* gx, const T* gy,  \
-                          const T* gz, T* f) {                                                                     \
-    k_flux_gather<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, f); count_launches(1);                   \
+                          const T* gz, const T* rvol, T* f) {                                                      \
+    k_flux_gather<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f);             \
+    count_launches(1);                                                                                             \
+  }                                                                                                                \
+  void launch_recip_eps(const Launch& L, size_t len, const T* v, T* rv) {                                          \
+    k_recip_eps<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, v, rv);                                          \
+    count_launches(1);                                                                                             \
   }                                                                                                                \
   void launch_div(const Launch& L, const Dims& d, const GeomT<T>& g, T* rhs) {                                     \
     k_div<T><<<gs_grid(L, (size_t)d.nx * d.ny * d.nz), kBlock, 0, L.stream>>>(d, g, rhs); count_launches(1);                          \
@@ -41,17 +55,18 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
   void launch_matvec(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* x, T* y, int plain) {      \
     k_matvec<TM, T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, val, x, y, plain); count_launches(1);                    \
   }                                                                                                                \
-  void launch_gs_upper(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* b, const T* x, T* t) {   \
-    k_gs_upper<TM, T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, val, b, x, t); count_launches(1);                      \
-  }                                                                                                                \
-  void launch_gs_lower(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* t, T* x) {               \
+  void launch_gs_sweeps(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* b, T* out, T* work,     \
+                        int nsweep) {                                                                              \
     const int ntx = (d.NX() + GS_TX - 1) / GS_TX;                                                                  \
     const int nty = (d.NY() + GS_TY - 1) / GS_TY;                                                                  \
     const int ntz = (d.NZ() + GS_TZ - 1) / GS_TZ;                                                                  \
     const int nlev = ntx + nty + ntz - 2;                                                                          \
     const int threads = GS_TY * GS_TZ * ncomp;                                                                     \
-    for (int lev = 0; lev < nlev; ++lev) {                                                                         \
-      k_gs_lower_level<TM, T><<<nty * ntz, threads, 0, L.stream>>>(d, ncomp, val, t, x, lev, ntx, nty, ntz); count_launches(1);       \
+    const dim3 grid(ntx, ntz, nsweep);                                                                             \
+    for (int tau = 0; tau < nlev + 2 * (nsweep - 1); ++tau) {                                                      \
+      k_gs_pipe<TM, T><<<grid, threads, 0, L.stream>>>(d, ncomp, val, b, out, work, tau, nsweep, ntx, nty, ntz,    \
+                                                       nlev);                                                      \
+      count_launches(1);                                                                                           \
     }                                                                                                              \
   }                                                                                                                \
   void launch_zero_halo(const Launch& L, const Dims& d, int ncomp, T* x) {                                         \

@@ -72,7 +72,8 @@ int asam_create(const asam_config *cfg, const double *volc, const double *fu, co
                 asam_ctx **out);
 int asam_destroy(asam_ctx *ctx);
 
-/* Run the context's work on this CUDA stream (cudaStream_t); NULL = own stream. */
+/* Run the context's work on this CUDA stream (cudaStream_t); NULL = the legacy
+ * default stream.  Until this is called the context uses a stream of its own. */
 int asam_set_stream(asam_ctx *ctx, void *stream);
 /* Device pointer of the context's resident state buffer (ncomp*npad doubles). */
 int asam_state_device_ptr(asam_ctx *ctx, double **dptr);
@@ -143,6 +144,12 @@ int asam_ros_coeffs(int method, double *beta0, double *alpha, double *beta, doub
 /* Diagnostic: scalar FP64 FMA throughput of the current device in GFLOP/s
  * (no reference counterpart; used for the FP64 roofline of the benchmark). */
 int asam_probe_fp64_fma(int iters, double *gflops);
+
+/* Diagnostic: count operand pairs (n pseudo-random pairs, exponents within
+ * +-span binades) where the library's FMA-corrected quotient from a
+ * precomputed reciprocal differs from the IEEE quotient (no reference
+ * counterpart; guards the bit-exact FP64 path). */
+int asam_probe_div(long long n, long long seed, int span, long long *mismatches);
 
 /* Sizes of the padded cell field for a configuration. */
 long long asam_npad(const asam_config *cfg);

@@ -1,0 +1,208 @@
+"""Independent numpy restatement of the transport-stage operators (test-only).
+
+Written in gather form (face fluxes first, then each cell sums its faces in
+the order the reference's scatter loop touches it), so it shares no code and
+no loop structure with the C oracle, yet follows the same floating-point
+operation order -- agreement with the oracle is therefore expected to be
+bit-exact.  Sources: ADVECT/Advection_Mod.f90:737-1054 (AdvectionComputeP),
+:2106-2134 (hLF..PhiLim), :2220-2872 (JacAdvectionCompute),
+ADVECT/Function_Mod.f90:1782-1862 (JacScaleCompute),
+CG/MatSpDiag_Mod.f90:87-235 (SpAVec, GaussSeidel).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+EPS = 1e-30
+
+
+def _k1(hL, hC, hR):
+    return (hC / (hC + hR + EPS)) * ((hL + hC) / (hL + hC + hR + EPS))
+
+
+def _k2(hL, hC, hR):
+    return (hC / (hL + hC + EPS)) * (hR / (hL + hC + hR + EPS))
+
+
+def _koren(r, k1, k2):
+    a = k1 * r + k2
+    m = np.where(a < 1.0, a, 1.0)
+    m = np.where(r < m, r, m)
+    return np.where(0.0 > m, 0.0, m)
+
+
+def _upwind(cL, cC, cR, VL, VC, VR, FL, FR, vel, right, vblend):
+    with np.errstate(divide="ignore", invalid="ignore"):
+        if vblend:
+            cL = np.where(VL < VC, ((VC - VL) * cC + VL * cL) / VC, cL)
+            cR = np.where(VR < VC, ((VC - VR) * cC + VR * cR) / VC, cR)
+        cL = np.where(FL < FR, ((FR - FL) * cC + FL * cL) / FR, cL)
+        cR = np.where(FR < FL, ((FL - FR) * cC + FR * cR) / FL, cR)
+        if not right:
+            k1 = _k1(VR, VC, VL)
+            k2 = _k2(VR, VC, VL)
+            r = (cC - cL + EPS) / ((cR - cC) + EPS)
+            return 0.5 * (np.abs(vel) - vel) * FL * (cC + FR / (FR + EPS) * (_koren(r, k1, k2) * (cC - cR)))
+        k1 = _k1(VL, VC, VR)
+        k2 = _k2(VL, VC, VR)
+        r = (cR - cC + EPS) / ((cC - cL) + EPS)
+        return 0.5 * (np.abs(vel) + vel) * FR * (cC + FL / (FL + EPS) * (_koren(r, k1, k2) * (cC - cL)))
+
+
+def face_fluxes(geo, phi, vel):
+    """Upwind-cell flux of every x/y/z face for one component field phi (padded, k,j,i)."""
+    g = geo.grid
+    nx, ny, nz = g.nx, g.ny, g.nz
+    V = geo.volc
+    uf, vf, wf = vel
+    out = []
+    # x faces i=0..nx between padded cells i,i+1 (j,k interior)
+    J, K = slice(1, ny + 1), slice(1, nz + 1)
+    gx = np.zeros((nz, ny, nx + 1))
+    for i in range(nx + 1):
+        u = uf[:, :, i]
+        res = np.zeros((nz, ny))
+        if i >= 1:  # upwind = cell i (right face of i)
+            c = i
+            val = _upwind(phi[K, J, c - 1], phi[K, J, c], phi[K, J, c + 1], V[K, J, c - 1], V[K, J, c], V[K, J, c + 1],
+                          geo.fu[:, :, c], geo.fu[:, :, c + 1], u, True, True)
+            res = np.where(u > 0, val, res)
+        if i + 1 <= nx:  # upwind = cell i+1 (left face of i+1)
+            c = i + 1
+            val = _upwind(phi[K, J, c - 1], phi[K, J, c], phi[K, J, c + 1], V[K, J, c - 1], V[K, J, c], V[K, J, c + 1],
+                          geo.fu[:, :, c], geo.fu[:, :, c + 1], u, False, True)
+            res = np.where(u < 0, val, res)
+        gx[:, :, i] = res
+    out.append(gx)
+    I = slice(1, nx + 1)
+    gy = np.zeros((nz, ny + 1, nx))
+    for j in range(ny + 1):
+        v = vf[:, j, :]
+        res = np.zeros((nz, nx))
+        if j >= 1:
+            c = j
+            val = _upwind(phi[K, c - 1, I], phi[K, c, I], phi[K, c + 1, I], V[K, c - 1, I], V[K, c, I], V[K, c + 1, I],
+                          geo.fv[:, c, :], geo.fv[:, c + 1, :], v, True, False)
+            res = np.where(v > 0, val, res)
+        if j + 1 <= ny:
+            c = j + 1
+            val = _upwind(phi[K, c - 1, I], phi[K, c, I], phi[K, c + 1, I], V[K, c - 1, I], V[K, c, I], V[K, c + 1, I],
+                          geo.fv[:, c, :], geo.fv[:, c + 1, :], v, False, False)
+            res = np.where(v < 0, val, res)
+        gy[:, j, :] = res
+    out.append(gy)
+    gz = np.zeros((nz + 1, ny, nx))
+    for k in range(nz + 1):
+        w = wf[k]
+        res = np.zeros((ny, nx))
+        if k >= 1:
+            c = k
+            val = _upwind(phi[c - 1, J, I], phi[c, J, I], phi[c + 1, J, I], V[c - 1, J, I], V[c, J, I], V[c + 1, J, I],
+                          geo.fw[c], geo.fw[c + 1], w, True, False)
+            res = np.where(w > 0, val, res)
+        if k + 1 <= nz:
+            c = k + 1
+            val = _upwind(phi[c - 1, J, I], phi[c, J, I], phi[c + 1, J, I], V[c - 1, J, I], V[c, J, I], V[c + 1, J, I],
+                          geo.fw[c], geo.fw[c + 1], w, False, False)
+            res = np.where(w < 0, val, res)
+        gz[k] = res
+    out.append(gz)
+    return out
+
+
+def fcn(geo, c, vel, rho_pos=0):
+    """FcnMet advection terms of all components (gather form)."""
+    g = geo.grid
+    nx, ny, nz = g.nx, g.ny, g.nz
+    V = geo.volc
+    uf, vf, wf = vel
+    rho = c[rho_pos]
+    out = np.zeros_like(c)
+    for ic in range(c.shape[0]):
+        phi = c[ic] / (rho + EPS)
+        gx, gy, gz = face_fluxes(geo, phi, vel)
+        f = np.zeros_like(phi)
+        a = np.zeros((nz, ny, nx))
+        uL, uR = uf[:, :, :-1], uf[:, :, 1:]
+        vL, vR = vf[:, :-1, :], vf[:, 1:, :]
+        wL, wR = wf[:-1], wf[1:]
+        GxL, GxR = gx[:, :, :-1], gx[:, :, 1:]
+        GyL, GyR = gy[:, :-1, :], gy[:, 1:, :]
+        GzL, GzR = gz[:-1], gz[1:]
+        for cond, term, sign in ((wL > 0, GzL, 1), (vL > 0, GyL, 1), (uL > 0, GxL, 1), (uL < 0, GxL, -1),
+                                 (uR > 0, GxR, -1), (vL < 0, GyL, -1), (vR > 0, GyR, -1), (wL < 0, GzL, -1),
+                                 (wR > 0, GzR, -1), (uR < 0, GxR, 1), (vR < 0, GyR, 1), (wR < 0, GzR, 1)):
+            a = np.where(cond, a + term if sign > 0 else a - term, a)
+        f[1:nz + 1, 1:ny + 1, 1:nx + 1] = a
+        # halo cells next to the interior
+        f[1:nz + 1, 1:ny + 1, 0] = np.where(uf[:, :, 0] < 0, gx[:, :, 0], 0.0)
+        f[1:nz + 1, 1:ny + 1, nx + 1] = np.where(uf[:, :, nx] > 0, gx[:, :, nx], 0.0)
+        f[1:nz + 1, 0, 1:nx + 1] = np.where(vf[:, 0, :] < 0, gy[:, 0, :], 0.0)
+        f[1:nz + 1, ny + 1, 1:nx + 1] = np.where(vf[:, ny, :] > 0, gy[:, ny, :], 0.0)
+        f[0, 1:ny + 1, 1:nx + 1] = np.where(wf[0] < 0, gz[0], 0.0)
+        f[nz + 1, 1:ny + 1, 1:nx + 1] = np.where(wf[nz] > 0, gz[nz], 0.0)
+        f = f * V / (V + EPS)
+        if g.periodic_x:
+            f[1:nz + 1, 1:ny + 1, 1] = f[1:nz + 1, 1:ny + 1, 1] + f[1:nz + 1, 1:ny + 1, nx + 1]
+            f[1:nz + 1, 1:ny + 1, nx] = f[1:nz + 1, 1:ny + 1, nx] + f[1:nz + 1, 1:ny + 1, 0]
+        if g.periodic_y:
+            f[1:nz + 1, 1, 1:nx + 1] = f[1:nz + 1, 1, 1:nx + 1] + f[1:nz + 1, ny + 1, 1:nx + 1]
+            f[1:nz + 1, ny, 1:nx + 1] = f[1:nz + 1, ny, 1:nx + 1] + f[1:nz + 1, 0, 1:nx + 1]
+        out[ic] = f / (V + EPS)
+    return out
+
+
+def upwind_rhs(geo, c, vel, rho):
+    """First-order upwind advection RHS (what the Jacobian linearises): per
+    interior cell sum of inflow u*F*c_up/rho_up minus outflow u*F*c/rho, over V."""
+    g = geo.grid
+    nx, ny, nz = g.nx, g.ny, g.nz
+    V = geo.volc
+    uf, vf, wf = vel
+    phi = c / (rho + EPS)
+    out = np.zeros_like(c)
+    I, J, K = slice(1, nx + 1), slice(1, ny + 1), slice(1, nz + 1)
+    acc = np.zeros((nz, ny, nx))
+    fu = geo.fu[:, :, 1:nx + 2]
+    fv = geo.fv[:, 1:ny + 2, :]
+    fw = geo.fw[1:nz + 2]
+    # flux through each face, positive in +axis direction (upwind value)
+    px = np.where(uf > 0, uf * fu * phi[K, J, 0:nx + 1], uf * fu * phi[K, J, 1:nx + 2])
+    py = np.where(vf > 0, vf * fv * phi[K, 0:ny + 1, I], vf * fv * phi[K, 1:ny + 2, I])
+    pz = np.where(wf > 0, wf * fw * phi[0:nz + 1, J, I], wf * fw * phi[1:nz + 2, J, I])
+    if not g.periodic_x:
+        px[:, :, 0] = 0
+        px[:, :, nx] = 0
+    if not g.periodic_y:
+        py[:, 0, :] = 0
+        py[:, ny, :] = 0
+    pz[0] = 0
+    pz[nz] = 0
+    acc = (px[:, :, :-1] - px[:, :, 1:]) + (py[:, :-1, :] - py[:, 1:, :]) + (pz[:-1] - pz[1:])
+    out[K, J, I] = acc / (V[K, J, I] + EPS)
+    return out
+
+
+def dia_scipy(val, grid):
+    """The column-oriented DIA matrix as scipy.sparse (A[col-shift, col] = Val(col, d))."""
+    import scipy.sparse as sp
+
+    NX, NY = grid.nx + 2, grid.ny + 2
+    n = grid.npad
+    shifts = [-NX * NY, -NX, -1, 0, 1, NX, NX * NY]
+    # scipy dia: A[i, i+k] = data[d, i+k]  ->  offset k = shift
+    return sp.dia_matrix((np.asarray(val), shifts), shape=(n, n)).tocsr()
+
+
+def gauss_seidel(val, grid, b, iterg=5):
+    """x = (L+D)^-1 b, then IterG sweeps x = (L+D)^-1 (b - U x) (scipy triangular solves)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+
+    A = dia_scipy(val, grid)
+    L = sp.tril(A, 0).tocsr()
+    U = sp.triu(A, 1).tocsr()
+    x = spl.spsolve_triangular(L, b, lower=True)
+    for _ in range(iterg):
+        x = spl.spsolve_triangular(L, b - U @ x, lower=True)
+    return x

@@ -208,3 +208,18 @@ def test_thomas_bitwise(env, ncol, n1):
     got = asam.Solve_1D(d, u, l, b)
     assert np.array_equal(got, ref)
     assert np.array_equal(asam.MatVecT_1D(d, u, l, b), oracle.tri_matvec(d, u, l, b))
+
+
+@pytest.mark.parametrize("span", [4, 30, 120])
+def test_corrected_division_matches_ieee(env, span):
+    """The FMA-corrected quotient from a precomputed reciprocal (used for the
+    divisions by VolC+Eps, Rho+Eps and the Gauss-Seidel diagonal) equals the
+    IEEE quotient on 2e7 random operand pairs."""
+    import ctypes as C
+
+    from asam_gb300 import _lib
+
+    lib = _lib.load()
+    bad = C.c_longlong(-1)
+    _lib.check(lib.asam_probe_div(20_000_000, 1000 + span, span, C.byref(bad)), "asam_probe_div")
+    assert bad.value == 0
