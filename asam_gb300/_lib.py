@@ -59,6 +59,7 @@ SIGNATURES = [
     ("asam_total_scalar", C.c_int, [_V, _V, C.c_int, _D]),
     ("asam_tri_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
+    ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_ros_coeffs", C.c_int, [C.c_int, _D, _D, _D, _D]),
     ("asam_npad", C.c_longlong, [C.POINTER(AsamConfig)]),
     ("asam_probe_fp64_fma", C.c_int, [C.c_int, _D]),

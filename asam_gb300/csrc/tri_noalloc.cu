@@ -1,0 +1,104 @@
+// Batched vertical-column Thomas solve that allocates nothing.
+//
+// asam_tri_solve (capi.cu) allocates device buffers for its inputs and for
+// the elimination factors w of Solve_1D on every call.  Some callers cannot
+// let a library allocate device memory: a host model that hands out all
+// device memory from its own pool at start-up, and a caller that overlaps this
+// solve with work on other streams (cudaMalloc and cudaFree synchronise the
+// device, which would serialise that work).  For them this entry point takes
+// device pointers for every input and output and keeps w in a fixed-size
+// array that lives in the library's device image.
+//
+// Compiled with -fmad=false like k64.cu, so the solution is bit-identical to
+// asam_tri_solve's.
+#include <mutex>
+
+#include "kernels.cuh"
+
+namespace asam {
+void set_last_error(const char* msg, const char* file, int line);
+void count_launches(long long n);
+}  // namespace asam
+
+namespace {
+
+// Elimination factors of the column solve.  Every GPU that loads the library
+// holds this array (32 MiB) until the process exits.  All calls share it: it
+// keeps the previous call's contents, which is harmless because the Thomas
+// forward sweep writes each w before the backward sweep reads it (nothing has
+// to start at zero).  Calls that overlap on the GPU (two streams at once) race
+// on it.
+constexpr long long kTriNoAllocMax = 1LL << 22;  // ncol*n1 doubles
+static __device__ __align__(256) double g_tri_scratch[kTriNoAllocMax];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+double* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host-side symbol is only a stand-in and must not be passed
+// to a kernel).
+int scratch_on_current_device(double** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    asam::set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+    return asam::kCudaError;
+  }
+  if (dev < 0 || dev >= kMaxDevices) {
+    asam::set_last_error("device ordinal out of range for the no-alloc scratch table", __FILE__, __LINE__);
+    return asam::kBadArg;
+  }
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_tri_scratch);
+    if (e != cudaSuccess) {
+      asam::set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+      return asam::kCudaError;
+    }
+    g_scratch_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_scratch_ptr[dev];
+  return asam::kOk;
+}
+
+bool on_device(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+extern "C" int asam_tri_solve_noalloc(int ncol, int n1, const double* d, const double* u, const double* l, double* b,
+                                      void* stream) {
+  if (ncol < 1 || n1 < 1 || !d || !b || (n1 > 1 && (!u || !l))) {
+    asam::set_last_error("asam_tri_solve_noalloc: bad sizes or null pointer", __FILE__, __LINE__);
+    return asam::kBadArg;
+  }
+  if ((long long)ncol * n1 > kTriNoAllocMax) {
+    asam::set_last_error(
+        "asam_tri_solve_noalloc: ncol*n1 exceeds the fixed scratch of 4194304 values; use asam_tri_solve",
+        __FILE__, __LINE__);
+    return asam::kBadArg;
+  }
+  if (!on_device(d) || !on_device(b) || (n1 > 1 && (!on_device(u) || !on_device(l)))) {
+    asam::set_last_error("asam_tri_solve_noalloc: d, u, l and b must be device pointers", __FILE__, __LINE__);
+    return asam::kBadArg;
+  }
+  double* w = nullptr;
+  int rc = scratch_on_current_device(&w);
+  if (rc) return rc;
+  k_tri_solve<double><<<(ncol + 127) / 128, 128, 0, (cudaStream_t)stream>>>(ncol, n1, d, u, l, b, w);
+  asam::count_launches(1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    asam::set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+    return asam::kCudaError;
+  }
+  return asam::kOk;
+}

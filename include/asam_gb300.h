@@ -134,6 +134,18 @@ int asam_total_scalar(asam_ctx *ctx, const double *c, int comp, double *out);
  * MULTI/TriDiagT_Mod.f90:135-155), over ncol independent columns of length n1:
  * d[col*n1+i], u[col*(n1-1)+i], l[col*(n1-1)+i]; b overwritten by the solution. */
 int asam_tri_solve(int ncol, int n1, const double *d, const double *u, const double *l, double *b);
+/* Same solve without any allocation (no counterpart in the reference).  For
+ * callers that cannot let a library allocate device memory: a host model
+ * that owns all device memory through its own pool, or one that overlaps this
+ * solve with other streams (cudaMalloc/cudaFree synchronise the device).  d,
+ * u, l and b must be device pointers; the work runs on `stream` (NULL = legacy
+ * default stream) and is not waited for.  The elimination factors go to a
+ * fixed 32 MiB array inside the library, so ncol*n1 may not exceed 4194304
+ * (ASAM_BAD_ARG otherwise).  The first call on a device looks the array's
+ * device address up; make that first call before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race. */
+int asam_tri_solve_noalloc(int ncol, int n1, const double *d, const double *u, const double *l, double *b,
+                           void *stream);
 /* y = T x for the same column batch, MatVecT_1D (MULTI/TriDiagT_Mod.f90:113-133). */
 int asam_tri_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x, double *y);
 
