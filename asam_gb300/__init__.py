@@ -34,6 +34,7 @@ from ._lib import ASAM_BREAKDOWN, ASAM_NOT_CONVERGED, ASAM_OK, AsamConfig, AsamE
 METHODS = {"Ros3AMF": 0, "RosRK32": 1, "RosEul": 2, "Ros3P": 3, "Ros3Pw": 4, "RosRK3": 5, "RosTVD": 6,
            "RosRK4": 7}
 PRECISIONS = {"fp64": 0, "fp32_refined": 1}
+INNER_PRECONDS = {"gauss_seidel": 0, "line": 1}
 
 __all__ = ["TransportBlock", "Solve_1D", "MatVecT_1D", "ros_coeffs", "METHODS", "PRECISIONS", "AsamError"]
 
@@ -62,14 +63,15 @@ class TransportBlock:
     the 7-diagonal stage matrix and the Krylov work space."""
 
     def __init__(self, geo, ncomp: int, rho_pos: int = 0, method: str = "RosRK3", bicgstab_tol: float = 1e-6,
-                 bicgstab_maxiter: int = 30, gs_iter: int = 5, precision: str = "fp64"):
+                 bicgstab_maxiter: int = 30, gs_iter: int = 5, precision: str = "fp64",
+                 inner_precond: str = "gauss_seidel"):
         self.lib = _lib.load()
         g = geo.grid
         self.grid = g
         self.ncomp = ncomp
         self.cfg = AsamConfig(g.nx, g.ny, g.nz, int(g.periodic_x), int(g.periodic_y), int(g.periodic_z), ncomp,
                               rho_pos, METHODS[method], bicgstab_maxiter, bicgstab_tol, gs_iter,
-                              PRECISIONS[precision])
+                              PRECISIONS[precision], INNER_PRECONDS[inner_precond])
         self._geo = [_f64(geo.volc), _f64(geo.fu), _f64(geo.fv), _f64(geo.fw)]
         h = C.c_void_p()
         check(self.lib.asam_create(C.byref(self.cfg), *(ptr(a) for a in self._geo), C.byref(h)), "asam_create")

@@ -31,7 +31,7 @@ class AsamConfig(C.Structure):
         ("periodic_x", C.c_int), ("periodic_y", C.c_int), ("periodic_z", C.c_int),
         ("ncomp", C.c_int), ("rho_pos", C.c_int), ("method", C.c_int),
         ("bicgstab_maxiter", C.c_int), ("bicgstab_tol", C.c_double), ("gs_iter", C.c_int),
-        ("precision", C.c_int),
+        ("precision", C.c_int), ("inner_precond", C.c_int),
     ]
 
 
@@ -57,6 +57,13 @@ SIGNATURES = [
     ("asam_bicgstab", C.c_int, [_V, _V, _V, _I, _D]),
     ("asam_ros_step", C.c_int, [_V, _V, C.c_double, _I, _D]),
     ("asam_total_scalar", C.c_int, [_V, _V, C.c_int, _D]),
+    ("asam_fcn_tlm", C.c_int, [_V, _V, C.c_int, _V, _V]),
+    ("asam_fcn_adj", C.c_int, [_V, _V, C.c_int, _V, _V]),
+    ("asam_matvec_adj", C.c_int, [_V, _V, _V]),
+    ("asam_bicgstab_adj", C.c_int, [_V, _V, _V, _I, _D]),
+    ("asam_ros_step_tlm", C.c_int, [_V, _V, C.c_int, _V, _V, C.c_double, C.c_double]),
+    ("asam_ros_step_adj", C.c_int, [_V, _V, C.c_int, _V, _V, C.c_double, C.c_double]),
+    ("asam_tracer_gradient", C.c_int, [_V, _V, C.c_int, C.c_int, C.c_double, C.c_int, _V, C.c_double, _D, _V]),
     ("asam_tri_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),

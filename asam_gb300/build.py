@@ -1,12 +1,13 @@
 """Build recipe of the CUDA library (sm_103a) and of the CPU oracle.
 
-The library is four translation units compiled in parallel by nvcc and
+The library is five translation units compiled in parallel by nvcc and
 linked into ``asam_gb300/libasam_gb300.so``:
 
 * ``k64.cu``  FP64 kernels with ``-fmad=false`` (reference rounding, no FMA)
 * ``k32.cu``  FP32 kernels of the refined mode
 * ``capi.cu`` context, drivers and the ``extern "C"`` entry points
 * ``tri_noalloc.cu`` the column solve that allocates nothing
+* ``adjoint.cu`` tangent-linear and adjoint of the transport stage
 
 The oracle (``oracle/asam_oracle.c``) is a test-only checker compiled by gcc
 into ``oracle/_build/libasam_oracle.so``.
@@ -35,6 +36,7 @@ UNITS = {
     "k32.cu": [],
     "capi.cu": [],
     "tri_noalloc.cu": ["-fmad=false"],
+    "adjoint.cu": ["-fmad=false"],
 }
 
 

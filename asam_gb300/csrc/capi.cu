@@ -7,9 +7,7 @@
 #include <cstring>
 #include <string>
 
-#include "asam_common.cuh"
-#include "asam_gb300.h"
-#include "launch.h"
+#include "context.h"
 
 #include <atomic>
 
@@ -27,29 +25,6 @@ void set_last_error(const char* msg, const char* file, int line) {
 using namespace asam;
 
 namespace {
-
-template <typename T>
-struct Work {
-  T *r = nullptr, *rt = nullptr, *rh = nullptr, *p = nullptr, *ph = nullptr, *t = nullptr, *v = nullptr;
-  T *bbuf = nullptr, *tbuf = nullptr;
-};
-
-template <typename T>
-cudaError_t alloc_work(Work<T>& w, size_t len) {
-  T** ptrs[] = {&w.r, &w.rt, &w.rh, &w.p, &w.ph, &w.t, &w.v, &w.bbuf, &w.tbuf};
-  for (T** q : ptrs) {
-    cudaError_t e = cudaMalloc((void**)q, len * sizeof(T));
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
-}
-template <typename T>
-void free_work(Work<T>& w) {
-  T* ptrs[] = {w.r, w.rt, w.rh, w.p, w.ph, w.t, w.v, w.bbuf, w.tbuf};
-  for (T* q : ptrs)
-    if (q) cudaFree(q);
-  w = Work<T>();
-}
 
 // Host restatement of InitRos3MetC's coefficient tables (ADVECT/Int_Mod.f90:78-261).
 int ros_coeffs(int method, double* beta0_out, double alpha[16], double beta[16], double gamma1[5]) {
@@ -194,6 +169,9 @@ int ros_coeffs(int method, double* beta0_out, double alpha[16], double beta[16],
   return nStage;
 }
 
+}  // namespace
+
+namespace asam {
 bool is_device_ptr(const void* p) {
   if (!p) return false;
   cudaPointerAttributes a;
@@ -204,44 +182,10 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-}  // namespace
+}  // namespace asam
 
-struct asam_ctx {
-  asam_config cfg;
-  Dims d;
-  Launch L;
-  cudaStream_t own_stream = nullptr;
-  size_t npad = 0, len = 0;
-  int nstage = 0;
-  double beta0 = 0, alpha[16], beta[16], gamma1[5];
-  // geometry + velocities (device)
-  double *volc = nullptr, *fu = nullptr, *fv = nullptr, *fw = nullptr, *uf = nullptr, *vf = nullptr, *wf = nullptr;
-  // stage storage
-  double *c = nullptr, *cold = nullptr, *rhs = nullptr, *incr = nullptr, *phi = nullptr;
-  double *gx = nullptr, *gy = nullptr, *gz = nullptr;
-  double *coef_x = nullptr, *coef_y = nullptr, *coef_z = nullptr;  // per-face flux coefficients
-  unsigned char *mask_x = nullptr, *mask_y = nullptr, *mask_z = nullptr;
-  double* rvol = nullptr;  // 1/(VolC+Eps)
-  double* val = nullptr;
-  float* val32 = nullptr;
-  Work<double> w64;
-  Work<float> w32;
-  float *x32 = nullptr, *b32 = nullptr;
-  double* dcorr = nullptr;
-  KrylovScalars* sc = nullptr;
-  KrylovScalars* sc_host = nullptr;
-  double* partial = nullptr;
-  double* red_out = nullptr;
-  double* red_host = nullptr;
-  double *stage_a = nullptr, *stage_b = nullptr;
-  bool jac_ready = false;
 
-  GeomT<double> geom() const { return GeomT<double>{volc, fu, fv, fw, uf, vf, wf}; }
-};
-
-namespace {
-
-#define CK(expr) ASAM_CUDA_OK(expr)
+namespace asam {
 
 int check_launch() {
   cudaError_t e = cudaGetLastError();
@@ -266,7 +210,8 @@ int reduce_to_host(asam_ctx* h, double* out) {
 }
 
 // PSolve_Vec4CellSp: copy, exchange, 1+IterG Gauss-Seidel sweeps (one
-// pipelined wavefront), zero halo, exchange.
+// pipelined wavefront), zero halo, exchange.  The FP32 inner solver of the
+// refined mode may use the vertical-column line solve instead of the sweeps.
 template <typename T>
 void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w) {
   const Launch& L = h->L;
@@ -274,14 +219,18 @@ void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w) {
   const int nc = h->cfg.ncomp;
   cudaMemcpyAsync(w.bbuf, in, h->len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream);
   launch_exchange_cell(L, d, nc, w.bbuf);
-  launch_gs_sweeps(L, d, nc, val, w.bbuf, out, w.tbuf, 1 + h->cfg.gs_iter);
+  if (sizeof(T) == sizeof(float) && h->cfg.inner_precond == 1)
+    launch_line_psolve(L, d, nc, val, w.bbuf, out, w.tbuf);
+  else
+    launch_gs_sweeps(L, d, nc, val, w.bbuf, out, w.tbuf, 1 + h->cfg.gs_iter);
   launch_zero_halo(L, d, nc, out);
   launch_exchange_cell(L, d, nc, out);
 }
 
 // BiCGStabMet_Vec4CellSp (MODULE/SpMatrix4CellPar_Mod.f90:245-348) on the device.
 template <typename T>
-int bicgstab_dev(asam_ctx* h, const T* val, T* x, const T* b, int* maxiter, double* tol, Work<T>& w) {
+int bicgstab_dev(asam_ctx* h, const T* val, T* x, const T* b, int* maxiter, double* tol, Work<T>& w,
+                 bool x_is_zero) {
   const Launch& L = h->L;
   const Dims& d = h->d;
   const int nc = h->cfg.ncomp;
@@ -289,8 +238,12 @@ int bicgstab_dev(asam_ctx* h, const T* val, T* x, const T* b, int* maxiter, doub
   memset(h->sc_host, 0, sizeof(KrylovScalars));
   h->sc_host->tol = *tol;
   CK(cudaMemcpyAsync(h->sc, h->sc_host, sizeof(KrylovScalars), cudaMemcpyHostToDevice, L.stream));
-  launch_matvec(L, d, nc, val, x, w.r, 0);
-  launch_xpay_host(L, len, b, (T)-1, w.r);
+  if (x_is_zero) {  // r = b - A*0 = b exactly
+    CK(cudaMemcpyAsync(w.r, b, len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream));
+  } else {
+    launch_matvec(L, d, nc, val, x, w.r, 0);
+    launch_xpay_host(L, len, b, (T)-1, w.r);
+  }
   CK(cudaMemcpyAsync(w.rt, w.r, len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream));
   launch_dot(L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM0, nullptr);
   const int MaxIter = *maxiter;
@@ -351,14 +304,18 @@ int bicgstab_dev(asam_ctx* h, const T* val, T* x, const T* b, int* maxiter, doub
 // FP32-refined solve: outer FP64 iterative refinement, FP32 inner BiCGStab
 // with the FP32 Gauss-Seidel preconditioner, FP64 residual recomputation and
 // the reference's stopping test ||r|| <= Tol*||r0|| on the FP64 residual.
-int bicgstab_refined(asam_ctx* h, double* x, const double* b, int* maxiter, double* tol) {
+int bicgstab_refined(asam_ctx* h, double* x, const double* b, int* maxiter, double* tol, bool x_is_zero) {
   const Launch& L = h->L;
   const Dims& d = h->d;
   const int nc = h->cfg.ncomp;
   const size_t len = h->len;
   double* r = h->w64.r;
-  launch_matvec(L, d, nc, h->val, x, r, 0);
-  launch_xpay_host(L, len, b, -1.0, r);
+  if (x_is_zero) {  // r = b - A*0 = b
+    CK(cudaMemcpyAsync(r, b, len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+  } else {
+    launch_matvec(L, d, nc, h->val, x, r, 0);
+    launch_xpay_host(L, len, b, -1.0, r);
+  }
   launch_dot(L, d, nc, r, r, h->partial, h->sc, OP_STORE_A, h->red_out);
   double rr0 = 0;
   int rc = reduce_to_host(h, &rr0);
@@ -380,7 +337,7 @@ int bicgstab_refined(asam_ctx* h, double* x, const double* b, int* maxiter, doub
     double tin = 0.5 * target / rnorm;
     if (tin < 1e-6) tin = 1e-6;
     if (tin > 1e-2) tin = 1e-2;
-    rc = bicgstab_dev<float>(h, h->val32, h->x32, h->b32, &it, &tin, h->w32);
+    rc = bicgstab_dev<float>(h, h->val32, h->x32, h->b32, &it, &tin, h->w32, true);
     if (rc != kOk && rc != kNotConverged) return rc;
     total_inner += it < 0 ? -it : (it > h->cfg.bicgstab_maxiter ? it / 2 : it);
     launch_convert_f32_to_f64(L, len, h->x32, h->dcorr);
@@ -420,9 +377,9 @@ int jac_dev(asam_ctx* h, const double* c, double dt) {
   return check_launch();
 }
 
-int solve_dev(asam_ctx* h, double* x, const double* b, int* maxiter, double* tol) {
-  if (h->cfg.precision == ASAM_PREC_FP32_REFINED) return bicgstab_refined(h, x, b, maxiter, tol);
-  return bicgstab_dev<double>(h, h->val, x, b, maxiter, tol, h->w64);
+int solve_dev(asam_ctx* h, double* x, const double* b, int* maxiter, double* tol, bool x_is_zero) {
+  if (h->cfg.precision == ASAM_PREC_FP32_REFINED) return bicgstab_refined(h, x, b, maxiter, tol, x_is_zero);
+  return bicgstab_dev<double>(h, h->val, x, b, maxiter, tol, h->w64, x_is_zero);
 }
 
 // Ros3MetC + StageRos, transport part (ADVECT/Int_Mod.f90:263-374, 1059-1122).
@@ -447,7 +404,7 @@ int ros_step_dev(asam_ctx* h, double* c, double dt, int* iters, double* resid) {
     CK(cudaMemsetAsync(x, 0, len * sizeof(double), L.stream));
     int it = h->cfg.bicgstab_maxiter;
     double tol = h->cfg.bicgstab_tol;
-    rc = solve_dev(h, x, h->rhs, &it, &tol);
+    rc = solve_dev(h, x, h->rhs, &it, &tol, true);
     if (rc != kOk && rc != kNotConverged && rc != kBreakdown) return rc;
     if (rc != kOk && status == kOk) status = rc;
     if (iters) iters[is] = it;
@@ -463,9 +420,6 @@ int ros_step_dev(asam_ctx* h, double* c, double dt, int* iters, double* resid) {
 
 // Staging of a caller pointer: device pointers are used in place, host
 // pointers are copied through the context's staging buffers.
-struct InArg {
-  const double* dev;
-};
 int stage_in(asam_ctx* h, const double* p, size_t n, double* buf, const double** dev) {
   if (is_device_ptr(p)) {
     *dev = p;
@@ -492,6 +446,15 @@ int stage_out_end(asam_ctx* h, double* p, size_t n, double* dev) {
   return kOk;
 }
 
+template void psolve_dev<double>(asam_ctx*, const double*, const double*, double*, Work<double>&);
+template void psolve_dev<float>(asam_ctx*, const float*, const float*, float*, Work<float>&);
+template int bicgstab_dev<double>(asam_ctx*, const double*, double*, const double*, int*, double*, Work<double>&,
+                                  bool);
+template int bicgstab_dev<float>(asam_ctx*, const float*, float*, const float*, int*, double*, Work<float>&, bool);
+
+}  // namespace asam
+
+namespace {
 int validate(const asam_config* c) {
   if (!c) return kBadArg;
   if (c->nx < 1 || c->ny < 1 || c->nz < 1) return kBadArg;
@@ -499,6 +462,7 @@ int validate(const asam_config* c) {
   if (c->rho_pos < 0 || c->rho_pos >= c->ncomp) return kBadArg;
   if (c->bicgstab_maxiter < 1 || c->gs_iter < 0) return kBadArg;
   if (c->precision != ASAM_PREC_FP64 && c->precision != ASAM_PREC_FP32_REFINED) return kBadArg;
+  if (c->inner_precond != 0 && c->inner_precond != 1) return kBadArg;
   return kOk;
 }
 
@@ -843,7 +807,7 @@ int asam_bicgstab(asam_ctx* h, double* x, const double* b, int* maxiter, double*
   if (rc) return rc;
   rc = stage_out_begin(h, x, h->len, h->stage_b, &dx, true);
   if (rc) return rc;
-  int st = solve_dev(h, dx, db, maxiter, tol);
+  int st = solve_dev(h, dx, db, maxiter, tol, false);
   if (st != kOk && st != kNotConverged && st != kBreakdown) return st;
   rc = stage_out_end(h, x, h->len, dx);
   return rc ? rc : st;

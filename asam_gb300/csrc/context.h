@@ -1,0 +1,95 @@
+// Context of one block on the device and the internal host drivers shared by
+// the C-ABI translation units (capi.cu, adjoint.cu).
+#pragma once
+#include "asam_common.cuh"
+#include "asam_gb300.h"
+#include "launch.h"
+
+namespace asam {
+
+template <typename T>
+struct Work {
+  T *r = nullptr, *rt = nullptr, *rh = nullptr, *p = nullptr, *ph = nullptr, *t = nullptr, *v = nullptr;
+  T *bbuf = nullptr, *tbuf = nullptr;
+};
+
+template <typename T>
+inline cudaError_t alloc_work(Work<T>& w, size_t len) {
+  T** ptrs[] = {&w.r, &w.rt, &w.rh, &w.p, &w.ph, &w.t, &w.v, &w.bbuf, &w.tbuf};
+  for (T** q : ptrs) {
+    cudaError_t e = cudaMalloc((void**)q, len * sizeof(T));
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+template <typename T>
+inline void free_work(Work<T>& w) {
+  T* ptrs[] = {w.r, w.rt, w.rh, w.p, w.ph, w.t, w.v, w.bbuf, w.tbuf};
+  for (T* q : ptrs)
+    if (q) cudaFree(q);
+  w = Work<T>();
+}
+
+}  // namespace asam
+
+struct asam_ctx {
+  using Launch = asam::Launch;
+  using Dims = asam::Dims;
+  template <typename T> using Work = asam::Work<T>;
+  template <typename T> using GeomT = asam::GeomT<T>;
+  using KrylovScalars = asam::KrylovScalars;
+  asam_config cfg;
+  Dims d;
+  Launch L;
+  cudaStream_t own_stream = nullptr;
+  size_t npad = 0, len = 0;
+  int nstage = 0;
+  double beta0 = 0, alpha[16], beta[16], gamma1[5];
+  // geometry + velocities (device)
+  double *volc = nullptr, *fu = nullptr, *fv = nullptr, *fw = nullptr, *uf = nullptr, *vf = nullptr, *wf = nullptr;
+  // stage storage
+  double *c = nullptr, *cold = nullptr, *rhs = nullptr, *incr = nullptr, *phi = nullptr;
+  double *gx = nullptr, *gy = nullptr, *gz = nullptr;
+  double *coef_x = nullptr, *coef_y = nullptr, *coef_z = nullptr;  // per-face flux coefficients
+  unsigned char *mask_x = nullptr, *mask_y = nullptr, *mask_z = nullptr;
+  double* rvol = nullptr;  // 1/(VolC+Eps)
+  double* val = nullptr;
+  float* val32 = nullptr;
+  Work<double> w64;
+  Work<float> w32;
+  float *x32 = nullptr, *b32 = nullptr;
+  double* dcorr = nullptr;
+  KrylovScalars* sc = nullptr;
+  KrylovScalars* sc_host = nullptr;
+  double* partial = nullptr;
+  double* red_out = nullptr;
+  double* red_host = nullptr;
+  double *stage_a = nullptr, *stage_b = nullptr;
+  bool jac_ready = false;
+
+  GeomT<double> geom() const { return GeomT<double>{volc, fu, fv, fw, uf, vf, wf}; }
+};
+
+namespace asam {
+
+void count_launches(long long n);
+int check_launch();
+int read_scalars(asam_ctx* h);
+int reduce_to_host(asam_ctx* h, double* out);
+bool is_device_ptr(const void* p);
+template <typename T>
+void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w);
+template <typename T>
+int bicgstab_dev(asam_ctx* h, const T* val, T* x, const T* b, int* maxiter, double* tol, Work<T>& w,
+                 bool x_is_zero);
+int fcn_dev(asam_ctx* h, const double* c, double* f);
+int jac_dev(asam_ctx* h, const double* c, double dt);
+int solve_dev(asam_ctx* h, double* x, const double* b, int* maxiter, double* tol, bool x_is_zero);
+int ros_step_dev(asam_ctx* h, double* c, double dt, int* iters, double* resid);
+int stage_in(asam_ctx* h, const double* p, size_t n, double* buf, const double** dev);
+int stage_out_begin(asam_ctx* h, double* p, size_t n, double* buf, double** dev, bool copy_in);
+int stage_out_end(asam_ctx* h, double* p, size_t n, double* dev);
+
+}  // namespace asam
+
+#define CK(expr) ASAM_CUDA_OK(expr)

@@ -10,6 +10,7 @@
 namespace {
 
 using asam::Dims;
+using asam::kMaxComp;
 
 template <typename T>
 __device__ __forceinline__ T eps_t() {
@@ -523,9 +524,10 @@ __global__ void k_matvec(Dims d, int ncomp, const TM* __restrict__ val, const T*
 // (I,J,K) depends only on tiles (I-1,J,K), (I,J-1,K), (I,J,K-1) in the lower
 // solve, so all tiles with I+J+K = level are independent.  Inside a tile the
 // cells are visited by hyperplanes a+b+c = l: each thread owns one (b,c) line
-// of one component and walks it in x, so the x-neighbour is in a register and
-// the y/z-neighbours were written at an earlier hyperplane (same block,
-// ordered by __syncthreads) or by an earlier launch.
+// of one component and walks it in x, so the x-neighbour is in a register;
+// the 16 lines of a component sit in one warp, so the y/z-neighbours computed
+// at the previous hyperplane arrive by warp shuffle, and neighbours in the
+// previous tiles come from an earlier launch.
 // ---------------------------------------------------------------------------
 constexpr int GS_TX = 32;
 constexpr int GS_TY = 4;
@@ -540,10 +542,14 @@ constexpr int GS_TZ = 4;
 // one launch the tile levels read and written in each buffer are disjoint.
 // Per cell the operation order is the reference's: b, U part (columns r+1,
 // r+NX, r+NXY), L part (columns r-NXY, r-NX, r-1), division.
+// Variant for the FP64 pipe (occupancy matters more than latency): each
+// thread prefetches the next cell's operands into registers one hyperplane
+// ahead; no shared memory, so many tiles fit on an SM.
 template <typename TM, typename T>
-__global__ void __launch_bounds__(256) k_gs_pipe(Dims d, int ncomp, const TM* __restrict__ val,
-                                                 const T* __restrict__ b, T* buf_last, T* buf_other, int tau,
-                                                 int nsweep, int ntx, int nty, int ntz, int nlev) {
+__global__ void __launch_bounds__(256) k_gs_pipe_reg(Dims d, int ncomp, const TM* __restrict__ val,
+                                                     const T* __restrict__ b, T* buf_last, T* buf_other, int tau,
+                                                     int nsweep, int ntx, int nty, int ntz, int nlev) {
+  static_assert(GS_TY * GS_TZ == 16, "one component's tile lines fill half a warp");
   const int s = blockIdx.z;
   const int L = tau - 2 * s;
   if (L < 0 || L >= nlev) return;
@@ -558,6 +564,8 @@ __global__ void __launch_bounds__(256) k_gs_pipe(Dims d, int ncomp, const TM* __
   const bool last_parity = ((nsweep - 1 - s) & 1) == 0;
   T* xn_all = last_parity ? buf_last : buf_other;        // x^s
   const T* xo_all = last_parity ? buf_other : buf_last;  // x^{s-1}
+  // lane = tb + GS_TY*tc + 16*(ic&1): the y-neighbour line is lane-1 and the
+  // z-neighbour line lane-GS_TY, both in this warp
   const int lb = threadIdx.x % (GS_TY * GS_TZ);
   const int ic = threadIdx.x / (GS_TY * GS_TZ);
   const int tb = lb % GS_TY, tc = lb / GS_TY;
@@ -568,27 +576,236 @@ __global__ void __launch_bounds__(256) k_gs_pipe(Dims d, int ncomp, const TM* __
   T* xn = xn_all + off;
   const T* xo = xo_all + off;
   const int i0 = I * GS_TX;
-  T xprev = (T)0;
+  const size_t rowP = sy * (size_t)j + sz * (size_t)k;
+  const bool up = s > 0;
+
+  // operands of one cell that do not depend on this sweep's current results
+  struct Cell {
+    T bb, u4, u5, u6, xo4, xo5, xo6, l0, l1, l2, dg, rd, xz, xy, xx;
+  };
+  auto load = [&](int a, Cell& c) {
+    const int i = i0 + a;
+    const size_t P = (size_t)i + rowP;
+    c.bb = bb[P];
+    c.u4 = c.u5 = c.u6 = c.xo4 = c.xo5 = c.xo6 = (T)0;
+    if (up) {
+      if (i < NX - 1) { c.u4 = (T)val[4 * n + P + 1]; c.xo4 = xo[P + 1]; }
+      if (j < NY - 1) { c.u5 = (T)val[5 * n + P + sy]; c.xo5 = xo[P + sy]; }
+      if (k < NZ - 1) { c.u6 = (T)val[6 * n + P + sz]; c.xo6 = xo[P + sz]; }
+    }
+    c.l0 = k > 0 ? (T)val[0 * n + P - sz] : (T)0;
+    c.l1 = j > 0 ? (T)val[1 * n + P - sy] : (T)0;
+    c.l2 = i > 0 ? (T)val[2 * n + P - 1] : (T)0;
+    c.dg = (T)val[3 * n + P];
+    c.rd = (T)val[7 * n + P];
+    // neighbours in the previous tiles (written by an earlier launch)
+    c.xz = (tc == 0 && k > 0) ? xn[P - sz] : (T)0;
+    c.xy = (tb == 0 && j > 0) ? xn[P - sy] : (T)0;
+    c.xx = (a == 0 && i > 0) ? xn[P - 1] : (T)0;
+  };
+
+  const int amax = min(GS_TX, NX - i0);  // cells of this line inside the box
+  Cell cur, nxt;
+  if (line_ok && amax > 0) load(0, nxt);
+  T last = (T)0;
+  const unsigned full = 0xffffffffu;
   const int nlev_in = GS_TX + GS_TY + GS_TZ - 2;
   for (int l = 0; l < nlev_in; ++l) {
+    const T from_y = __shfl_up_sync(full, last, 1);
+    const T from_z = __shfl_up_sync(full, last, GS_TY);
     const int a = l - tb - tc;
-    const int i = i0 + a;
-    if (line_ok && a >= 0 && a < GS_TX && i < NX) {
-      const size_t P = (size_t)i + sy * (size_t)j + sz * (size_t)k;
-      T t = bb[P];
-      if (s > 0) {
+    if (line_ok && a >= 0 && a < amax) {
+      cur = nxt;
+      if (a + 1 < amax) load(a + 1, nxt);
+      const int i = i0 + a;
+      T t = cur.bb;
+      if (up) {
+        if (i < NX - 1) t = t - cur.u4 * cur.xo4;
+        if (j < NY - 1) t = t - cur.u5 * cur.xo5;
+        if (k < NZ - 1) t = t - cur.u6 * cur.xo6;
+      }
+      if (k > 0) t = t - cur.l0 * (tc > 0 ? from_z : cur.xz);
+      if (j > 0) t = t - cur.l1 * (tb > 0 ? from_y : cur.xy);
+      if (i > 0) t = t - cur.l2 * (a > 0 ? last : cur.xx);
+      t = div_rn(t, cur.dg, cur.rd);
+      xn[(size_t)i + rowP] = t;
+      last = t;
+    }
+  }
+}
+
+// Shared-memory layout of one tile of k_gs_pipe_smem (in units of T):
+//   ts [ncomp][TZ][TY][TX]  b - U x^{s-1}   (computed in the prologue)
+//   ls [5][TZ][TY][TX]      lower-part coefficients for columns r-NXY, r-NX, r-1,
+//                           the diagonal and its reciprocal
+//   zb [ncomp][TY][TX]      x^s of the cells below the tile's bottom plane
+//   yb [ncomp][TZ][TX]      x^s of the cells south of the tile's first row
+//   xb [ncomp][TZ][TY]      x^s of the cells west of the tile's first column
+constexpr int GS_TILE = GS_TX * GS_TY * GS_TZ;
+inline size_t gs_smem_elems(int ncomp) {
+  return (size_t)ncomp * (GS_TILE + GS_TY * GS_TX + GS_TZ * GS_TX + GS_TZ * GS_TY) + 5 * (size_t)GS_TILE;
+}
+
+// Variant for latency-bound precisions (FP32): the tile's operands are staged
+// in shared memory by a coalesced prologue, the wavefront reads only shared
+// memory and registers.
+template <typename TM, typename T>
+__global__ void __launch_bounds__(256) k_gs_pipe_smem(Dims d, int ncomp, const TM* __restrict__ val,
+                                                      const T* __restrict__ b, T* buf_last, T* buf_other, int tau,
+                                                      int nsweep, int ntx, int nty, int ntz, int nlev) {
+  static_assert(GS_TY * GS_TZ == 16, "one component's tile lines fill half a warp");
+  const int s = blockIdx.z;
+  const int L = tau - 2 * s;
+  if (L < 0 || L >= nlev) return;
+  const int K = blockIdx.y;
+  const int Jlo = max(0, L - K - (ntx - 1));
+  const int J = Jlo + (int)blockIdx.x;
+  const int I = L - J - K;
+  if (J >= nty || I < 0 || I >= ntx) return;  // uniform over the block
+  const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
+  const size_t n = d.npad();
+  const size_t sy = (size_t)NX, sz = (size_t)NX * NY;
+  const bool last_parity = ((nsweep - 1 - s) & 1) == 0;
+  T* xn_all = last_parity ? buf_last : buf_other;        // x^s
+  const T* xo_all = last_parity ? buf_other : buf_last;  // x^{s-1}
+  const bool up = s > 0;
+  const int i0 = I * GS_TX, j0 = J * GS_TY, k0 = K * GS_TZ;
+
+  extern __shared__ __align__(16) unsigned char gs_smem_raw[];
+  T* ts = reinterpret_cast<T*>(gs_smem_raw);
+  T* ls = ts + (size_t)ncomp * GS_TILE;
+  T* zb = ls + 5 * (size_t)GS_TILE;
+  T* yb = zb + (size_t)ncomp * GS_TY * GS_TX;
+  T* xb = yb + (size_t)ncomp * GS_TZ * GS_TX;
+
+  // ---- prologue: coalesced loads of everything that does not depend on this
+  // sweep's new values (consecutive threads take consecutive x)
+  for (int q = threadIdx.x; q < GS_TILE; q += blockDim.x) {
+    const int a = q % GS_TX, tb = (q / GS_TX) % GS_TY, tc = q / (GS_TX * GS_TY);
+    const int i = i0 + a, j = j0 + tb, k = k0 + tc;
+    if (i < NX && j < NY && k < NZ) {
+      const size_t P = (size_t)i + sy * j + sz * k;
+      ls[0 * GS_TILE + q] = k > 0 ? (T)val[0 * n + P - sz] : (T)0;
+      ls[1 * GS_TILE + q] = j > 0 ? (T)val[1 * n + P - sy] : (T)0;
+      ls[2 * GS_TILE + q] = i > 0 ? (T)val[2 * n + P - 1] : (T)0;
+      ls[3 * GS_TILE + q] = (T)val[3 * n + P];
+      ls[4 * GS_TILE + q] = (T)val[7 * n + P];
+    }
+  }
+  for (int q = threadIdx.x; q < ncomp * GS_TILE; q += blockDim.x) {
+    const int ic = q / GS_TILE, c = q % GS_TILE;
+    const int a = c % GS_TX, tb = (c / GS_TX) % GS_TY, tc = c / (GS_TX * GS_TY);
+    const int i = i0 + a, j = j0 + tb, k = k0 + tc;
+    if (i < NX && j < NY && k < NZ) {
+      const size_t P = (size_t)i + sy * j + sz * k;
+      const T* xo = xo_all + (size_t)ic * n;
+      T t = b[(size_t)ic * n + P];
+      if (up) {
         if (i < NX - 1) t = t - (T)val[4 * n + P + 1] * xo[P + 1];
         if (j < NY - 1) t = t - (T)val[5 * n + P + sy] * xo[P + sy];
         if (k < NZ - 1) t = t - (T)val[6 * n + P + sz] * xo[P + sz];
       }
-      if (k > 0) t = t - (T)val[0 * n + P - sz] * xn[P - sz];
-      if (j > 0) t = t - (T)val[1 * n + P - sy] * xn[P - sy];
-      if (i > 0) t = t - (T)val[2 * n + P - 1] * (a > 0 ? xprev : xn[P - 1]);
-      t = div_rn(t, (T)val[3 * n + P], (T)val[7 * n + P]);
-      xn[P] = t;
-      xprev = t;
+      ts[q] = t;
     }
-    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < ncomp * GS_TY * GS_TX; q += blockDim.x) {  // plane below
+    const int ic = q / (GS_TY * GS_TX), c = q % (GS_TY * GS_TX);
+    const int a = c % GS_TX, tb = c / GS_TX;
+    const int i = i0 + a, j = j0 + tb, k = k0;
+    zb[q] = (k > 0 && i < NX && j < NY) ? xn_all[(size_t)ic * n + (size_t)i + sy * j + sz * (k - 1)] : (T)0;
+  }
+  for (int q = threadIdx.x; q < ncomp * GS_TZ * GS_TX; q += blockDim.x) {  // row to the south
+    const int ic = q / (GS_TZ * GS_TX), c = q % (GS_TZ * GS_TX);
+    const int a = c % GS_TX, tc = c / GS_TX;
+    const int i = i0 + a, j = j0, k = k0 + tc;
+    yb[q] = (j > 0 && i < NX && k < NZ) ? xn_all[(size_t)ic * n + (size_t)i + sy * (j - 1) + sz * k] : (T)0;
+  }
+  for (int q = threadIdx.x; q < ncomp * GS_TZ * GS_TY; q += blockDim.x) {  // column to the west
+    const int ic = q / (GS_TZ * GS_TY), c = q % (GS_TZ * GS_TY);
+    const int tb = c % GS_TY, tc = c / GS_TY;
+    const int i = i0, j = j0 + tb, k = k0 + tc;
+    xb[q] = (i > 0 && j < NY && k < NZ) ? xn_all[(size_t)ic * n + (size_t)(i - 1) + sy * j + sz * k] : (T)0;
+  }
+  __syncthreads();
+
+  // ---- wavefront over the tile's hyperplanes.  lane = tb + GS_TY*tc + 16*(ic&1):
+  // the y-neighbour line is lane-1 and the z-neighbour line lane-GS_TY.
+  const int lb = threadIdx.x % (GS_TY * GS_TZ);
+  const int ic = threadIdx.x / (GS_TY * GS_TZ);
+  const int tb = lb % GS_TY, tc = lb / GS_TY;
+  const int j = j0 + tb, k = k0 + tc;
+  const bool line_ok = ic < ncomp && j < NY && k < NZ;
+  const int icc = line_ok ? ic : 0;
+  T* xn = xn_all + (size_t)icc * n;
+  const size_t rowP = sy * (size_t)j + sz * (size_t)k;
+  const int amax = min(GS_TX, NX - i0);
+  const T* tl = ts + (size_t)icc * GS_TILE + (tc * GS_TY + tb) * GS_TX;
+  const int lq = (tc * GS_TY + tb) * GS_TX;
+  T last = line_ok ? xb[(icc * GS_TZ + tc) * GS_TY + tb] : (T)0;  // x-neighbour of cell 0
+  const unsigned full = 0xffffffffu;
+  const int nlev_in = GS_TX + GS_TY + GS_TZ - 2;
+  for (int l = 0; l < nlev_in; ++l) {
+    const T from_y = __shfl_up_sync(full, last, 1);
+    const T from_z = __shfl_up_sync(full, last, GS_TY);
+    const int a = l - tb - tc;
+    if (line_ok && a >= 0 && a < amax) {
+      const int i = i0 + a;
+      const int q = lq + a;
+      T t = tl[a];
+      if (k > 0) t = t - ls[0 * GS_TILE + q] * (tc > 0 ? from_z : zb[(icc * GS_TY + tb) * GS_TX + a]);
+      if (j > 0) t = t - ls[1 * GS_TILE + q] * (tb > 0 ? from_y : yb[(icc * GS_TZ + tc) * GS_TX + a]);
+      if (i > 0) t = t - ls[2 * GS_TILE + q] * last;
+      t = div_rn(t, ls[3 * GS_TILE + q], ls[4 * GS_TILE + q]);
+      xn[(size_t)i + rowP] = t;
+      last = t;
+    }
+  }
+}
+
+// Vertical-column line preconditioner of the refined mode's inner solver:
+// x = Tz^{-1} b with Tz the z-tridiagonal part of the stage matrix (diagonal,
+// column r-NXY of row r and column r+NXY of row r), solved by the Thomas
+// algorithm along each padded column.  One thread per (i,j) column handles
+// all components: the elimination factors depend on the matrix only and are
+// kept in `w` (one value per cell).  Consecutive threads take consecutive i,
+// so every k-plane access is coalesced.
+template <typename TM, typename T>
+__global__ void k_line_psolve(Dims d, int ncomp, const TM* __restrict__ val, const T* __restrict__ b,
+                              T* __restrict__ x, T* __restrict__ w) {
+  const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
+  const size_t n = d.npad();
+  const size_t sz = (size_t)NX * NY;
+  const size_t ncols = (size_t)NX * NY;
+  for (size_t col = blockIdx.x * (size_t)blockDim.x + threadIdx.x; col < ncols;
+       col += (size_t)gridDim.x * blockDim.x) {
+    T g[kMaxComp];
+    // forward elimination
+    T wprev = (T)0;
+    for (int k = 0; k < NZ; ++k) {
+      const size_t P = col + sz * (size_t)k;
+      const T a = k > 0 ? (T)val[0 * n + P - sz] : (T)0;
+      const T c = k < NZ - 1 ? (T)val[6 * n + P + sz] : (T)0;
+      const T den = (T)val[3 * n + P] - a * wprev;
+      const T rden = (T)1 / den;
+      const T wk = c * rden;
+      w[P] = wk;
+      for (int ic = 0; ic < ncomp; ++ic) {
+        const T gk = (b[ic * n + P] - a * (k > 0 ? g[ic] : (T)0)) * rden;
+        g[ic] = gk;
+        x[ic * n + P] = gk;
+      }
+      wprev = wk;
+    }
+    // back substitution
+    for (int k = NZ - 2; k >= 0; --k) {
+      const size_t P = col + sz * (size_t)k;
+      const T wk = w[P];
+      for (int ic = 0; ic < ncomp; ++ic) {
+        const T xk = x[ic * n + P] - wk * g[ic];
+        g[ic] = xk;
+        x[ic * n + P] = xk;
+      }
+    }
   }
 }
 

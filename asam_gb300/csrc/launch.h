@@ -26,6 +26,7 @@ struct Launch {
   void launch_matvec(const Launch&, const Dims&, int ncomp, const TM* val, const T* x, T* y, int plain_spmv);    \
   void launch_gs_sweeps(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, T* out, T* work,       \
                         int nsweep);                                                                             \
+  void launch_line_psolve(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, T* x, T* w);         \
   void launch_zero_halo(const Launch&, const Dims&, int ncomp, T* x);                                           \
   void launch_exchange_cell(const Launch&, const Dims&, int ncomp, T* c);                                       \
   void launch_dot(const Launch&, const Dims&, int ncomp, const T* x, const T* y, double* partial,               \

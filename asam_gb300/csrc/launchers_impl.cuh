@@ -61,13 +61,29 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
     const int nty = (d.NY() + GS_TY - 1) / GS_TY;                                                                  \
     const int ntz = (d.NZ() + GS_TZ - 1) / GS_TZ;                                                                  \
     const int nlev = ntx + nty + ntz - 2;                                                                          \
-    const int threads = GS_TY * GS_TZ * ncomp;                                                                     \
+    const int threads = (GS_TY * GS_TZ * ncomp + 31) / 32 * 32; /* whole warps: the sweep shuffles */             \
     const dim3 grid(ntx, ntz, nsweep);                                                                             \
+    const bool staged = sizeof(T) == sizeof(float);                                                               \
+    const size_t smem = staged ? gs_smem_elems(ncomp) * sizeof(T) : 0;                                             \
+    static size_t smem_set = 0;                                                                                    \
+    if (smem > smem_set) {                                                                                         \
+      cudaFuncSetAttribute(k_gs_pipe_smem<TM, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
+      smem_set = smem;                                                                                             \
+    }                                                                                                              \
     for (int tau = 0; tau < nlev + 2 * (nsweep - 1); ++tau) {                                                      \
-      k_gs_pipe<TM, T><<<grid, threads, 0, L.stream>>>(d, ncomp, val, b, out, work, tau, nsweep, ntx, nty, ntz,    \
-                                                       nlev);                                                      \
+      if (staged)                                                                                                  \
+        k_gs_pipe_smem<TM, T><<<grid, threads, smem, L.stream>>>(d, ncomp, val, b, out, work, tau, nsweep, ntx,   \
+                                                                 nty, ntz, nlev);                                  \
+      else                                                                                                         \
+        k_gs_pipe_reg<TM, T><<<grid, threads, 0, L.stream>>>(d, ncomp, val, b, out, work, tau, nsweep, ntx, nty,  \
+                                                             ntz, nlev);                                           \
       count_launches(1);                                                                                           \
     }                                                                                                              \
+  }                                                                                                                \
+  void launch_line_psolve(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* b, T* x, T* w) {      \
+    const size_t ncols = (size_t)d.NX() * d.NY();                                                                  \
+    k_line_psolve<TM, T><<<(unsigned)((ncols + 127) / 128), 128, 0, L.stream>>>(d, ncomp, val, b, x, w);           \
+    count_launches(1);                                                                                             \
   }                                                                                                                \
   void launch_zero_halo(const Launch& L, const Dims& d, int ncomp, T* x) {                                         \
     k_zero_halo<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, x); count_launches(1);                                    \

@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--no-refined", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample", type=int, default=48, help="edge of the oracle's CPU sample window")
+    p.add_argument("--inner", default="gauss_seidel", choices=["gauss_seidel", "line"],
+                   help="preconditioner of the FP32 inner solver of the refined path")
     return p.parse_args()
 
 
@@ -253,7 +255,7 @@ def main():
     gpu_launches = {}
     for prec in (["fp64"] + ([] if a.no_refined else ["fp32_refined"])):
         blk = asam_gb300.TransportBlock(geo, ncomp, method="RosRK3", bicgstab_tol=a.tol, bicgstab_maxiter=30,
-                                        precision=prec)
+                                        precision=prec, inner_precond=a.inner)
         blk.set_velocity(*vel)
         blk.set_stream(stream.cuda_stream)
         dptr = blk.state_device_ptr()
@@ -327,6 +329,18 @@ def main():
     ms_step = r64["ms"] / a.steps
     value = world * ncell * a.steps / (r64["ms"] * 1e-3) / 1e6
     e2e = world * ncell * a.steps / (r64["ms_e2e"] * 1e-3) / 1e6
+    npad = (a.nx + 2) * (a.ny + 2) * (a.nz + 2)
+    nsweep = 6
+    # dominant kernel of the FP64 step: the Gauss-Seidel wavefront (one PSolve call =
+    # nlev + 10 launches of k_gs_pipe); algorithmic bytes per padded cell and sweep:
+    # the 8 matrix slots (64 B) + b, x_old and x_new of every component (24 B each)
+    gs_bytes = npad * nsweep * (64 + 24 * ncomp)
+    # FP64 instructions per cell, component and sweep: 6 products + 6 differences
+    # (upper and lower part) + 3 for the corrected division
+    gs_dp = npad * nsweep * ncomp * 15
+    ps_s = r64["kernels"]["psolve_ms"] * 1e-3
+    gs_gbs = gs_bytes / ps_s / 1e9
+    fp64_peak_inst = gf.value / 2.0  # DFMA instructions per ns = GFLOP/s / 2
     flux_bytes = ncell * BYTES_PER_CELL_FLUX(ncomp)
     flux_gbs = flux_bytes / (r64["kernels"]["flux_rhs_ms"] * 1e-3) / 1e9
     nbytes_state = st.c.size * 8
@@ -335,11 +349,17 @@ def main():
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded cut-cell generators)", "config": workload_config(a),
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": nbytes_state, "d2h_bytes_per_step": nbytes_state},
-        "roofline": {"kernel": "flux RHS (asam_fcn: phi + face fluxes + gather)", "bound": "hbm",
-                     "achieved": flux_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": flux_gbs / hbm_peak,
+        "roofline": {"kernel": "k_gs_pipe (one PSolve: 1+IterG Gauss-Seidel sweeps)", "bound": "hbm",
+                     "achieved": gs_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gs_gbs / hbm_peak,
                      "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
-                     "algorithmic_bytes_per_launch": flux_bytes,
-                     "fp64_fma_peak_gflops_probe": gf.value},
+                     "algorithmic_bytes_per_call": gs_bytes,
+                     "fp64_pipe": {"achieved_ginst_s": gs_dp / ps_s / 1e9, "peak_ginst_s": fp64_peak_inst,
+                                   "frac": gs_dp / ps_s / 1e9 / fp64_peak_inst,
+                                   "peak_source": "asam_probe_fp64_fma (measured live)"},
+                     "note": "FP64 kernels on GB300 are bounded by the FP64 pipe (ridge 0.16 flop/B)"},
+        "flux_roofline": {"achieved": flux_gbs, "unit": "GB/s", "frac": flux_gbs / hbm_peak,
+                          "algorithmic_bytes_per_call": flux_bytes},
+        "fp64_fma_peak_gflops_probe": gf.value,
         "kernels_ms": r64["kernels"],
         "krylov_iterations": r64["iters"],
         "clocks": r64["clocks"],
@@ -359,6 +379,7 @@ def main():
                                 "ms_per_step": rr["ms"] / a.steps,
                                 "speedup_vs_fp64": r64["ms"] / rr["ms"],
                                 "max_rel_err_vs_fp64": max(e["max_rel"] for e in errs), "fields": errs,
+                                "inner_preconditioner": a.inner,
                                 "krylov_iterations": rr["iters"], "kernels_ms": rr["kernels"],
                                 "gpu_launches": gpu_launches["fp32_refined"],
                                 "clocks": rr["clocks"]}

@@ -59,6 +59,9 @@ typedef struct {
   double bicgstab_tol;                     /* BiCGStabTol (Control_Mod.f90:580, default 1e-6) */
   int gs_iter;                             /* IterG (CG/MatSpDiag_Mod.f90:14, default 5) */
   int precision;                           /* asam_precision */
+  int inner_precond;                       /* refined mode's FP32 inner preconditioner:
+                                              0 = the Gauss-Seidel sweeps of the FP64 path,
+                                              1 = vertical-column line solve (Thomas along z) */
 } asam_config;
 
 typedef struct asam_ctx asam_ctx;
@@ -126,6 +129,38 @@ int asam_bicgstab(asam_ctx *ctx, double *x, const double *b, int *maxiter, doubl
  * prescribed steady face velocities).  c: state in/out.  iters/resid: per
  * stage BiCGStab iteration count / residual (may be NULL, else >= nStage). */
 int asam_ros_step(asam_ctx *ctx, double *c, double dt, int *iters, double *resid);
+
+/* ---- tangent-linear / adjoint pair of the transport stage ------------------
+ * For one passive component `comp` of the state (not the density), with the
+ * density and the face velocities held fixed.  The flux operator is piecewise
+ * linear in the component (Koren limiter branches); the tangent-linear model
+ * freezes the branches of the state it is linearised around.  These have no
+ * counterpart in the reference, which has no adjoint. */
+/* df = F'(c) dc for the FcnMet advection terms of component comp (single padded fields). */
+int asam_fcn_tlm(asam_ctx *ctx, const double *c, int comp, const double *dc, double *df);
+/* lc = F'(c)^T lf, the exact transpose of asam_fcn_tlm. */
+int asam_fcn_adj(asam_ctx *ctx, const double *c, int comp, const double *lf, double *lc);
+/* y = A^T x for the context's DIA matrix (one padded field): a gather from the
+ * column-oriented storage of SpAVec_SpDiag (CG/MatSpDiag_Mod.f90:87-108). */
+int asam_matvec_adj(asam_ctx *ctx, const double *x, double *y);
+/* Solve A_per^T x = b for the periodic interior system transposed (adjoint of
+ * the stage solve), BiCGStab with a diagonal preconditioner.  maxiter/tol in:
+ * limit and relative tolerance; maxiter out: iterations used. */
+int asam_bicgstab_adj(asam_ctx *ctx, double *x, const double *b, int *maxiter, double *tol);
+/* Tangent-linear / adjoint of one Rosenbrock step (asam_ros_step) of component
+ * comp around state c; du/lam are interior perturbations (padded fields, halos
+ * ignored).  tol: relative tolerance of the stage solves. */
+int asam_ros_step_tlm(asam_ctx *ctx, const double *c, int comp, const double *du, double *du_out, double dt,
+                      double tol);
+int asam_ros_step_adj(asam_ctx *ctx, const double *c, int comp, const double *lam, double *lam_out, double dt,
+                      double tol);
+/* Gradient of J = sum over the box of (c_comp/Rho)^2 * VolC after nsteps steps
+ * with respect to the initial component field (interior of a padded field).
+ * box = {i0,i1,j0,j1,k0,k1}, 1-based interior indices, inclusive.  The forward
+ * states are checkpointed every ckpt_every steps and recomputed in the reverse
+ * sweep: memory (nsteps/ckpt_every + ckpt_every + nStage + 1) states. */
+int asam_tracer_gradient(asam_ctx *ctx, const double *c0, int comp, int nsteps, double dt, int ckpt_every,
+                         const int *box, double tol, double *J, double *grad);
 
 /* Global mass of one component: TotalScalar (ADVECT/Diagnostic_Mod.f90:13-31). */
 int asam_total_scalar(asam_ctx *ctx, const double *c, int comp, double *out);

@@ -172,13 +172,15 @@ def test_ros_coeffs_match_oracle(env):
         assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3]) and np.array_equal(a[4], b[4])
 
 
-@pytest.mark.parametrize("name", ["hill_24x20x16", "hill_odd_13x7x9_reverse"])
-def test_ros_step_refined(env, name):
+@pytest.mark.parametrize("inner", ["line", "gauss_seidel"])
+@pytest.mark.parametrize("name", ["hill_24x20x16", "hill_odd_13x7x9_reverse", "flat_walls_9x6x5"])
+def test_ros_step_refined(env, name, inner):
     asam, oracle = env
     geo, vel, st = cases.get(name)
     o = oracle.Oracle(geo)
     cr, cg = st.c.copy(), st.c.copy()
-    with _block(env, name, method="RosRK3", bicgstab_tol=1e-12, precision="fp32_refined") as blk:
+    with _block(env, name, method="RosRK3", bicgstab_tol=1e-12, precision="fp32_refined",
+                inner_precond=inner) as blk:
         for _ in range(2):
             o.ros_step(cr, vel, 4.0, method=asam.METHODS["RosRK3"], tol=1e-12)
             blk.Ros3MetC(cg, 4.0)
