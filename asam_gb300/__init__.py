@@ -64,14 +64,14 @@ class TransportBlock:
 
     def __init__(self, geo, ncomp: int, rho_pos: int = 0, method: str = "RosRK3", bicgstab_tol: float = 1e-6,
                  bicgstab_maxiter: int = 30, gs_iter: int = 5, precision: str = "fp64",
-                 inner_precond: str = "gauss_seidel"):
+                 inner_precond: str = "gauss_seidel", inner_gs_iter: int = 1):
         self.lib = _lib.load()
         g = geo.grid
         self.grid = g
         self.ncomp = ncomp
         self.cfg = AsamConfig(g.nx, g.ny, g.nz, int(g.periodic_x), int(g.periodic_y), int(g.periodic_z), ncomp,
                               rho_pos, METHODS[method], bicgstab_maxiter, bicgstab_tol, gs_iter,
-                              PRECISIONS[precision], INNER_PRECONDS[inner_precond])
+                              PRECISIONS[precision], INNER_PRECONDS[inner_precond], inner_gs_iter)
         self._geo = [_f64(geo.volc), _f64(geo.fu), _f64(geo.fv), _f64(geo.fw)]
         h = C.c_void_p()
         check(self.lib.asam_create(C.byref(self.cfg), *(ptr(a) for a in self._geo), C.byref(h)), "asam_create")

@@ -31,7 +31,7 @@ class AsamConfig(C.Structure):
         ("periodic_x", C.c_int), ("periodic_y", C.c_int), ("periodic_z", C.c_int),
         ("ncomp", C.c_int), ("rho_pos", C.c_int), ("method", C.c_int),
         ("bicgstab_maxiter", C.c_int), ("bicgstab_tol", C.c_double), ("gs_iter", C.c_int),
-        ("precision", C.c_int), ("inner_precond", C.c_int),
+        ("precision", C.c_int), ("inner_precond", C.c_int), ("inner_gs_iter", C.c_int),
     ]
 
 

@@ -864,9 +864,14 @@ int asam_tracer_gradient(asam_ctx* h, const double* c0, int comp, int nsteps, do
   if ((rc = dev_copy_in(h, c0, len, &dc0, o.p)) || (rc = dev_out(h, grad, n, &dgrad, o))) return rc;
   AdjScratch sc;
   if ((rc = sc.alloc(h))) return rc;
-  // checkpoints every ckpt_every steps: (nsteps/k + 1) states, plus k states of one segment
+  // checkpoints every ckpt_every steps (nsteps/k states); in the reverse sweep
+  // one segment of k steps is recomputed once from its checkpoint with the
+  // stage states of every step recorded (k*nStage states, plus two for the
+  // running state), so each step costs one forward recomputation, the rebuild
+  // of its stage matrix and its adjoint
   const int nck = (nsteps + ckpt_every - 1) / ckpt_every;
-  std::vector<double*> ckpt(nck, nullptr), seg(ckpt_every, nullptr);
+  const int ns = h->nstage;
+  std::vector<double*> ckpt(nck, nullptr), recbuf((size_t)ckpt_every * ns + 2, nullptr);
   struct Free {
     std::vector<double*>* a;
     ~Free() {
@@ -874,9 +879,16 @@ int asam_tracer_gradient(asam_ctx* h, const double* c0, int comp, int nsteps, do
         if (p) cudaFree(p);
     }
   };
-  Free f1{&ckpt}, f2{&seg};
+  Free f1{&ckpt}, f2{&recbuf};
   for (auto& p : ckpt) CK(cudaMalloc((void**)&p, len * sizeof(double)));
-  for (auto& p : seg) CK(cudaMalloc((void**)&p, len * sizeof(double)));
+  for (auto& p : recbuf) CK(cudaMalloc((void**)&p, len * sizeof(double)));
+  // rec[m]: stage states of step s0+m, then the state after the step (one of
+  // two alternating buffers)
+  std::vector<std::vector<double*>> rec(ckpt_every, std::vector<double*>(ns + 1, nullptr));
+  for (int m = 0; m < ckpt_every; ++m) {
+    for (int is = 0; is < ns; ++is) rec[m][is] = recbuf[(size_t)m * ns + is];
+    rec[m][ns] = recbuf[(size_t)ckpt_every * ns + (m & 1)];
+  }
   struct TolGuard {
     asam_ctx* h;
     double saved;
@@ -902,22 +914,19 @@ int asam_tracer_gradient(asam_ctx* h, const double* c0, int comp, int nsteps, do
   k_sum_partials<<<1, RED_BLOCK, 0, L.stream>>>(h->partial, RED_GRID, h->red_out);
   count_launches(2);
   if ((rc = reduce_to_host(h, J))) return rc;
-  // reverse sweep over segments, recomputing each segment from its checkpoint
+  // reverse sweep over segments
   double* lam_next = dgrad;
   for (int sgi = nck - 1; sgi >= 0; --sgi) {
     const int s0 = sgi * ckpt_every;
     const int s1 = std::min(nsteps, s0 + ckpt_every);
-    CK(cudaMemcpyAsync(seg[0], ckpt[sgi], len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
-    for (int s = s0 + 1; s < s1; ++s) {
-      CK(cudaMemcpyAsync(seg[s - s0], seg[s - s0 - 1], len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
-      int it[4];
-      double rs[4];
-      rc = ros_step_dev(h, seg[s - s0], dt, it, rs);
-      if (rc != kOk && rc != kNotConverged) return rc;
+    const double* src = ckpt[sgi];
+    for (int s = s0; s < s1; ++s) {
+      if ((rc = forward_record(h, src, dt, tol, rec[s - s0]))) return rc;
+      src = rec[s - s0][ns];
     }
     for (int s = s1 - 1; s >= s0; --s) {
-      if ((rc = forward_record(h, seg[s - s0], dt, tol, sc.stage))) return rc;
-      if ((rc = step_adj(h, sc.w, sc.stage, comp, lam, lam_next, dt, tol, sc.k))) return rc;
+      if ((rc = jac_dev(h, rec[s - s0][0], dt))) return rc;  // the step's stage matrix
+      if ((rc = step_adj(h, sc.w, rec[s - s0], comp, lam, lam_next, dt, tol, sc.k))) return rc;
       CK(cudaMemcpyAsync(lam, lam_next, n * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
     }
   }

@@ -219,10 +219,11 @@ void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w) {
   const int nc = h->cfg.ncomp;
   cudaMemcpyAsync(w.bbuf, in, h->len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream);
   launch_exchange_cell(L, d, nc, w.bbuf);
-  if (sizeof(T) == sizeof(float) && h->cfg.inner_precond == 1)
+  const bool inner = sizeof(T) == sizeof(float);  // FP32 inner solver of the refined mode
+  if (inner && h->cfg.inner_precond == 1)
     launch_line_psolve(L, d, nc, val, w.bbuf, out, w.tbuf);
   else
-    launch_gs_sweeps(L, d, nc, val, w.bbuf, out, w.tbuf, 1 + h->cfg.gs_iter);
+    launch_gs_sweeps(L, d, nc, val, w.bbuf, out, w.tbuf, 1 + (inner ? h->cfg.inner_gs_iter : h->cfg.gs_iter));
   launch_zero_halo(L, d, nc, out);
   launch_exchange_cell(L, d, nc, out);
 }
@@ -463,6 +464,7 @@ int validate(const asam_config* c) {
   if (c->bicgstab_maxiter < 1 || c->gs_iter < 0) return kBadArg;
   if (c->precision != ASAM_PREC_FP64 && c->precision != ASAM_PREC_FP32_REFINED) return kBadArg;
   if (c->inner_precond != 0 && c->inner_precond != 1) return kBadArg;
+  if (c->inner_gs_iter < 0) return kBadArg;
   return kOk;
 }
 

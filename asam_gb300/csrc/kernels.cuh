@@ -543,8 +543,8 @@ constexpr int GS_TZ = 4;
 // Per cell the operation order is the reference's: b, U part (columns r+1,
 // r+NX, r+NXY), L part (columns r-NXY, r-NX, r-1), division.
 // Variant for the FP64 pipe (occupancy matters more than latency): each
-// thread prefetches the next cell's operands into registers one hyperplane
-// ahead; no shared memory, so many tiles fit on an SM.
+// thread prefetches its next two cells' operands into registers, two
+// hyperplanes ahead; no shared memory, so many tiles fit on an SM.
 template <typename TM, typename T>
 __global__ void __launch_bounds__(256) k_gs_pipe_reg(Dims d, int ncomp, const TM* __restrict__ val,
                                                      const T* __restrict__ b, T* buf_last, T* buf_other, int tau,
@@ -605,8 +605,9 @@ __global__ void __launch_bounds__(256) k_gs_pipe_reg(Dims d, int ncomp, const TM
   };
 
   const int amax = min(GS_TX, NX - i0);  // cells of this line inside the box
-  Cell cur, nxt;
+  Cell cur, nxt, nxt2;  // operands of cells a, a+1, a+2
   if (line_ok && amax > 0) load(0, nxt);
+  if (line_ok && amax > 1) load(1, nxt2);
   T last = (T)0;
   const unsigned full = 0xffffffffu;
   const int nlev_in = GS_TX + GS_TY + GS_TZ - 2;
@@ -616,7 +617,8 @@ __global__ void __launch_bounds__(256) k_gs_pipe_reg(Dims d, int ncomp, const TM
     const int a = l - tb - tc;
     if (line_ok && a >= 0 && a < amax) {
       cur = nxt;
-      if (a + 1 < amax) load(a + 1, nxt);
+      nxt = nxt2;
+      if (a + 2 < amax) load(a + 2, nxt2);
       const int i = i0 + a;
       T t = cur.bb;
       if (up) {
@@ -635,25 +637,47 @@ __global__ void __launch_bounds__(256) k_gs_pipe_reg(Dims d, int ncomp, const TM
 }
 
 // Shared-memory layout of one tile of k_gs_pipe_smem (in units of T):
-//   ts [ncomp][TZ][TY][TX]  b - U x^{s-1}   (computed in the prologue)
-//   ls [5][TZ][TY][TX]      lower-part coefficients for columns r-NXY, r-NX, r-1,
-//                           the diagonal and its reciprocal
-//   zb [ncomp][TY][TX]      x^s of the cells below the tile's bottom plane
-//   yb [ncomp][TZ][TX]      x^s of the cells south of the tile's first row
-//   xb [ncomp][TZ][TY]      x^s of the cells west of the tile's first column
+//   ts [ncomp][TZ][TY][TX]       b, then b - U x^{s-1}
+//   ls [8][TZ][TY][TX]           lower-part coefficients for columns r-NXY, r-NX,
+//                                r-1, the diagonal, its reciprocal, and the
+//                                upper-part coefficients for columns r+1, r+NX, r+NXY
+//   xs [ncomp][TZ+1][TY+1][TX+1] x^{s-1} on the tile grown by one cell in +x,
+//                                +y and +z (the upper-part neighbours)
+//   zb [ncomp][TY][TX]           x^s of the cells below the tile's bottom plane
+//   yb [ncomp][TZ][TX]           x^s of the cells south of the tile's first row
+//   xb [ncomp][TZ][TY]           x^s of the cells west of the tile's first column
 constexpr int GS_TILE = GS_TX * GS_TY * GS_TZ;
+constexpr int GS_BX = GS_TX + 1, GS_BY = GS_TY + 1, GS_BZ = GS_TZ + 1;
+constexpr int GS_BOX = GS_BX * GS_BY * GS_BZ;
 inline size_t gs_smem_elems(int ncomp) {
-  return (size_t)ncomp * (GS_TILE + GS_TY * GS_TX + GS_TZ * GS_TX + GS_TZ * GS_TY) + 5 * (size_t)GS_TILE;
+  return (size_t)ncomp * (GS_TILE + GS_BOX + GS_TY * GS_TX + GS_TZ * GS_TX + GS_TZ * GS_TY) + 8 * (size_t)GS_TILE;
 }
 
-// Variant for latency-bound precisions (FP32): the tile's operands are staged
-// in shared memory by a coalesced prologue, the wavefront reads only shared
-// memory and registers.
+// Asynchronous global->shared copy of one element (cp.async, no register
+// staging); when `pred` is false nothing is read and the element is zeroed.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem, bool pred) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "cp.async element of 4 or 8 bytes");
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  const unsigned src_size = pred ? (unsigned)sizeof(T) : 0u;
+  if constexpr (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_size) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_size) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Variant for latency-bound precisions (FP32): every operand of the tile that
+// does not depend on this sweep's new values is copied to shared memory by
+// cp.async in one batch (one memory round trip per launch instead of one per
+// load), b - U x^{s-1} is formed there, and the wavefront then reads only
+// shared memory and registers.
 template <typename TM, typename T>
 __global__ void __launch_bounds__(256) k_gs_pipe_smem(Dims d, int ncomp, const TM* __restrict__ val,
                                                       const T* __restrict__ b, T* buf_last, T* buf_other, int tau,
                                                       int nsweep, int ntx, int nty, int ntz, int nlev) {
   static_assert(GS_TY * GS_TZ == 16, "one component's tile lines fill half a warp");
+  static_assert(sizeof(TM) == sizeof(T), "coefficients are copied as they are stored");
   const int s = blockIdx.z;
   const int L = tau - 2 * s;
   if (L < 0 || L >= nlev) return;
@@ -674,59 +698,90 @@ __global__ void __launch_bounds__(256) k_gs_pipe_smem(Dims d, int ncomp, const T
   extern __shared__ __align__(16) unsigned char gs_smem_raw[];
   T* ts = reinterpret_cast<T*>(gs_smem_raw);
   T* ls = ts + (size_t)ncomp * GS_TILE;
-  T* zb = ls + 5 * (size_t)GS_TILE;
+  T* xs = ls + 8 * (size_t)GS_TILE;
+  T* zb = xs + (size_t)ncomp * GS_BOX;
   T* yb = zb + (size_t)ncomp * GS_TY * GS_TX;
   T* xb = yb + (size_t)ncomp * GS_TZ * GS_TX;
+  const TM* vbase = reinterpret_cast<const TM*>(val);
 
-  // ---- prologue: coalesced loads of everything that does not depend on this
-  // sweep's new values (consecutive threads take consecutive x)
-  for (int q = threadIdx.x; q < GS_TILE; q += blockDim.x) {
-    const int a = q % GS_TX, tb = (q / GS_TX) % GS_TY, tc = q / (GS_TX * GS_TY);
+  // ---- prologue, phase 1: issue every copy of the tile (consecutive threads
+  // take consecutive x, so each warp's copies are coalesced)
+  for (int c = threadIdx.x; c < GS_TILE; c += blockDim.x) {
+    const int a = c % GS_TX, tb = (c / GS_TX) % GS_TY, tc = c / (GS_TX * GS_TY);
     const int i = i0 + a, j = j0 + tb, k = k0 + tc;
-    if (i < NX && j < NY && k < NZ) {
-      const size_t P = (size_t)i + sy * j + sz * k;
-      ls[0 * GS_TILE + q] = k > 0 ? (T)val[0 * n + P - sz] : (T)0;
-      ls[1 * GS_TILE + q] = j > 0 ? (T)val[1 * n + P - sy] : (T)0;
-      ls[2 * GS_TILE + q] = i > 0 ? (T)val[2 * n + P - 1] : (T)0;
-      ls[3 * GS_TILE + q] = (T)val[3 * n + P];
-      ls[4 * GS_TILE + q] = (T)val[7 * n + P];
-    }
+    const bool in = i < NX && j < NY && k < NZ;
+    const size_t P = in ? (size_t)i + sy * j + sz * k : 0;
+    const bool p0 = in && k > 0, p1 = in && j > 0, p2 = in && i > 0;
+    const bool p5 = in && up && i < NX - 1, p6 = in && up && j < NY - 1, p7 = in && up && k < NZ - 1;
+    cp_async_elem(reinterpret_cast<TM*>(ls) + 0 * GS_TILE + c, p0 ? vbase + 0 * n + P - sz : vbase, p0);
+    cp_async_elem(reinterpret_cast<TM*>(ls) + 1 * GS_TILE + c, p1 ? vbase + 1 * n + P - sy : vbase, p1);
+    cp_async_elem(reinterpret_cast<TM*>(ls) + 2 * GS_TILE + c, p2 ? vbase + 2 * n + P - 1 : vbase, p2);
+    cp_async_elem(reinterpret_cast<TM*>(ls) + 3 * GS_TILE + c, vbase + 3 * n + P, in);
+    cp_async_elem(reinterpret_cast<TM*>(ls) + 4 * GS_TILE + c, vbase + 7 * n + P, in);
+    cp_async_elem(reinterpret_cast<TM*>(ls) + 5 * GS_TILE + c, p5 ? vbase + 4 * n + P + 1 : vbase, p5);
+    cp_async_elem(reinterpret_cast<TM*>(ls) + 6 * GS_TILE + c, p6 ? vbase + 5 * n + P + sy : vbase, p6);
+    cp_async_elem(reinterpret_cast<TM*>(ls) + 7 * GS_TILE + c, p7 ? vbase + 6 * n + P + sz : vbase, p7);
   }
-  for (int q = threadIdx.x; q < ncomp * GS_TILE; q += blockDim.x) {
+  for (int q = threadIdx.x; q < ncomp * GS_TILE; q += blockDim.x) {  // b
     const int ic = q / GS_TILE, c = q % GS_TILE;
     const int a = c % GS_TX, tb = (c / GS_TX) % GS_TY, tc = c / (GS_TX * GS_TY);
     const int i = i0 + a, j = j0 + tb, k = k0 + tc;
-    if (i < NX && j < NY && k < NZ) {
-      const size_t P = (size_t)i + sy * j + sz * k;
-      const T* xo = xo_all + (size_t)ic * n;
-      T t = b[(size_t)ic * n + P];
-      if (up) {
-        if (i < NX - 1) t = t - (T)val[4 * n + P + 1] * xo[P + 1];
-        if (j < NY - 1) t = t - (T)val[5 * n + P + sy] * xo[P + sy];
-        if (k < NZ - 1) t = t - (T)val[6 * n + P + sz] * xo[P + sz];
-      }
-      ts[q] = t;
+    const bool in = i < NX && j < NY && k < NZ;
+    cp_async_elem(ts + q, in ? b + (size_t)ic * n + (size_t)i + sy * j + sz * k : b, in);
+  }
+  if (up) {
+    for (int q = threadIdx.x; q < ncomp * GS_BOX; q += blockDim.x) {  // x^{s-1} on the grown tile
+      const int ic = q / GS_BOX, r = q % GS_BOX;
+      const int a = r % GS_BX, tb = (r / GS_BX) % GS_BY, tc = r / (GS_BX * GS_BY);
+      const int i = i0 + a, j = j0 + tb, k = k0 + tc;
+      // the edges and the corner of the grown part are never read (and may be
+      // written by sweep s-1 during this launch): skip them
+      const int grown = (a == GS_TX) + (tb == GS_TY) + (tc == GS_TZ);
+      const bool in = grown <= 1 && i < NX && j < NY && k < NZ;
+      cp_async_elem(xs + q, in ? xo_all + (size_t)ic * n + (size_t)i + sy * j + sz * k : xo_all, in);
     }
   }
   for (int q = threadIdx.x; q < ncomp * GS_TY * GS_TX; q += blockDim.x) {  // plane below
     const int ic = q / (GS_TY * GS_TX), c = q % (GS_TY * GS_TX);
     const int a = c % GS_TX, tb = c / GS_TX;
     const int i = i0 + a, j = j0 + tb, k = k0;
-    zb[q] = (k > 0 && i < NX && j < NY) ? xn_all[(size_t)ic * n + (size_t)i + sy * j + sz * (k - 1)] : (T)0;
+    const bool in = k > 0 && i < NX && j < NY;
+    cp_async_elem(zb + q, in ? xn_all + (size_t)ic * n + (size_t)i + sy * j + sz * (k - 1) : xn_all, in);
   }
   for (int q = threadIdx.x; q < ncomp * GS_TZ * GS_TX; q += blockDim.x) {  // row to the south
     const int ic = q / (GS_TZ * GS_TX), c = q % (GS_TZ * GS_TX);
     const int a = c % GS_TX, tc = c / GS_TX;
     const int i = i0 + a, j = j0, k = k0 + tc;
-    yb[q] = (j > 0 && i < NX && k < NZ) ? xn_all[(size_t)ic * n + (size_t)i + sy * (j - 1) + sz * k] : (T)0;
+    const bool in = j > 0 && i < NX && k < NZ;
+    cp_async_elem(yb + q, in ? xn_all + (size_t)ic * n + (size_t)i + sy * (j - 1) + sz * k : xn_all, in);
   }
   for (int q = threadIdx.x; q < ncomp * GS_TZ * GS_TY; q += blockDim.x) {  // column to the west
     const int ic = q / (GS_TZ * GS_TY), c = q % (GS_TZ * GS_TY);
     const int tb = c % GS_TY, tc = c / GS_TY;
     const int i = i0, j = j0 + tb, k = k0 + tc;
-    xb[q] = (i > 0 && j < NY && k < NZ) ? xn_all[(size_t)ic * n + (size_t)(i - 1) + sy * j + sz * k] : (T)0;
+    const bool in = i > 0 && j < NY && k < NZ;
+    cp_async_elem(xb + q, in ? xn_all + (size_t)ic * n + (size_t)(i - 1) + sy * j + sz * k : xn_all, in);
   }
+  cp_async_wait_all();
   __syncthreads();
+
+  // ---- prologue, phase 2: t = b - U x^{s-1} in the reference's column order
+  if (up) {
+    for (int q = threadIdx.x; q < ncomp * GS_TILE; q += blockDim.x) {
+      const int ic = q / GS_TILE, c = q % GS_TILE;
+      const int a = c % GS_TX, tb = (c / GS_TX) % GS_TY, tc = c / (GS_TX * GS_TY);
+      const int i = i0 + a, j = j0 + tb, k = k0 + tc;
+      if (i < NX && j < NY && k < NZ) {
+        const T* xq = xs + (size_t)ic * GS_BOX + (tc * GS_BY + tb) * GS_BX + a;
+        T t = ts[q];
+        if (i < NX - 1) t = t - ls[5 * GS_TILE + c] * xq[1];
+        if (j < NY - 1) t = t - ls[6 * GS_TILE + c] * xq[GS_BX];
+        if (k < NZ - 1) t = t - ls[7 * GS_TILE + c] * xq[GS_BX * GS_BY];
+        ts[q] = t;
+      }
+    }
+    __syncthreads();
+  }
 
   // ---- wavefront over the tile's hyperplanes.  lane = tb + GS_TY*tc + 16*(ic&1):
   // the y-neighbour line is lane-1 and the z-neighbour line lane-GS_TY.
@@ -856,27 +911,74 @@ __global__ void k_exchange_cell(Dims d, int ncomp, T* __restrict__ c) {
 
 // ---------------------------------------------------------------------------
 // Interior dot products (Dot_VectorCell, MODULE/Vector4Cell_Mod.f90:1120-1132),
-// deterministic two-stage reduction; accumulation in double.
+// deterministic two-stage reduction.
 // ---------------------------------------------------------------------------
 constexpr int RED_BLOCK = 256;
 constexpr int RED_GRID = 1024;
 
+// Per-thread accumulator of a dot product.  FP64 operands accumulate in FP64.
+// FP32 operands use the compensated Dot2 scheme of Ogita, Rump and Oishi
+// ("Accurate sum and dot product", SIAM J. Sci. Comput. 26 (2005)): the
+// rounding error of each product (recovered exactly by an FMA) and of each
+// running sum (Knuth's TwoSum) is carried in a second float, so a thread's
+// partial is as accurate as if accumulated in twice the working precision,
+// at FP32-pipe cost; the partials are then summed in FP64.
+template <typename T>
+struct DotAcc;
+template <>
+struct DotAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x, double y) { s += x * y; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct DotAcc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x, float y) {
+    const float p = __fmul_rn(x, y);
+    const float pe = __fmaf_rn(x, y, -p);  // x*y - p exactly
+    const float t = __fadd_rn(hi, p);
+    const float bp = __fsub_rn(t, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(p, bp));  // hi + p - t exactly
+    hi = t;
+    lo = __fadd_rn(lo, __fadd_rn(e, pe));
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// One warp per interior x-row of one component at a time (lanes along x, so
+// every load is coalesced and no per-element index division is needed).
 template <typename T>
 __global__ void k_dot_partial(Dims d, int ncomp, const T* __restrict__ x, const T* __restrict__ y,
                               double* __restrict__ partial) {
   const int nx = d.nx, ny = d.ny;
-  const size_t nint = (size_t)nx * ny * d.nz;
+  const long long rows_c = (long long)ny * d.nz;
+  const long long nrow = rows_c * ncomp;
   const size_t n = d.npad();
-  double s = 0.0;
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nint; q += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(q % nx) + 1;
-    int j = (int)((q / nx) % ny) + 1;
-    int k = (int)(q / ((size_t)nx * ny)) + 1;
-    size_t P = d.P(i, j, k);
-    for (int ic = 0; ic < ncomp; ++ic) s += (double)x[ic * n + P] * (double)y[ic * n + P];
+  const size_t sy = (size_t)d.NX(), sz = (size_t)d.NX() * d.NY();
+  const int lane = threadIdx.x & 31;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  DotAcc<T> acc;
+  for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < nrow; r += nw) {
+    const int ic = (int)(r / rows_c);
+    const int jk = (int)(r - ic * rows_c);
+    const int j = jk % ny + 1, k = jk / ny + 1;
+    const size_t base = (size_t)ic * n + 1 + sy * j + sz * k;
+    const T* xr = x + base;
+    const T* yr = y + base;
+    int i = lane;
+    for (; i + 96 < nx; i += 128) {
+      const T x0 = xr[i], x1 = xr[i + 32], x2 = xr[i + 64], x3 = xr[i + 96];
+      const T y0 = yr[i], y1 = yr[i + 32], y2 = yr[i + 64], y3 = yr[i + 96];
+      acc.add(x0, y0);
+      acc.add(x1, y1);
+      acc.add(x2, y2);
+      acc.add(x3, y3);
+    }
+    for (; i < nx; i += 32) acc.add(xr[i], yr[i]);
   }
   __shared__ double sh[RED_BLOCK];
-  sh[threadIdx.x] = s;
+  sh[threadIdx.x] = acc.value();
   __syncthreads();
   for (int w = RED_BLOCK / 2; w > 0; w >>= 1) {
     if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];

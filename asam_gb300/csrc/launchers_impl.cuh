@@ -66,7 +66,7 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
     const bool staged = sizeof(T) == sizeof(float);                                                               \
     const size_t smem = staged ? gs_smem_elems(ncomp) * sizeof(T) : 0;                                             \
     static size_t smem_set = 0;                                                                                    \
-    if (smem > smem_set) {                                                                                         \
+    if (staged && smem > smem_set) {                                                                              \
       cudaFuncSetAttribute(k_gs_pipe_smem<TM, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
       smem_set = smem;                                                                                             \
     }                                                                                                              \

@@ -51,10 +51,18 @@ def parse():
     p.add_argument("--dt", type=float, default=2.0)
     p.add_argument("--tol", type=float, default=1e-10)
     p.add_argument("--no-refined", action="store_true")
+    p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--adj-grid", default="128,128,64", help="nx,ny,nz of the adjoint-cost workload")
+    p.add_argument("--adj-steps", type=int, default=40)
+    p.add_argument("--adj-ckpt", type=int, default=8)
+    p.add_argument("--precision", default="both", choices=["both", "fp64", "fp32_refined"],
+                   help="which variants to run (profiling runs take one)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample", type=int, default=48, help="edge of the oracle's CPU sample window")
     p.add_argument("--inner", default="gauss_seidel", choices=["gauss_seidel", "line"],
                    help="preconditioner of the FP32 inner solver of the refined path")
+    p.add_argument("--inner-gs-iter", type=int, default=1,
+                   help="IterG of the refined path's FP32 inner Gauss-Seidel (the FP64 path keeps 5)")
     return p.parse_args()
 
 
@@ -186,6 +194,79 @@ def run_reference(a, rank):
     print(json.dumps(line), flush=True)
 
 
+def adjoint_cost(a, lib, torch, stream):
+    """Cost of the checkpointed gradient against the forward run it differentiates.
+
+    Workload: cut-cell Gaussian hill h=800 m, half-width 4 km on the adjoint grid
+    (default 128x128x64), Rho, Rho*theta and a passive tracer, RosRK3 dt=2 s,
+    adj_steps steps, checkpoints every adj_ckpt steps, J = sum over a 16x16x8 box
+    of (tracer mixing ratio)^2 V at the final time; everything device-resident.
+    """
+    import ctypes as C
+
+    import asam_gb300
+    from asam_gb300 import _lib
+    from asam_gb300 import geometry as G
+
+    nx, ny, nz = (int(v) for v in a.adj_grid.split(","))
+    geo, vel, st = G.hill_case(nx, ny, nz, seed=5, height=800.0, halfwidth=4000.0, moist=False, momentum=False,
+                               tracer=True)
+    ncomp = st.c.shape[0]
+    comp = ncomp - 1
+    tol = a.tol
+    blk = asam_gb300.TransportBlock(geo, ncomp, method="RosRK3", bicgstab_tol=tol, bicgstab_maxiter=200)
+    blk.set_velocity(*vel)
+    blk.set_stream(stream.cuda_stream)
+    c0 = torch.from_numpy(st.c.reshape(-1).copy()).cuda()
+    cur = c0.clone()
+    npad = geo.grid.npad
+    grad = torch.empty(npad, dtype=torch.float64, device="cuda")
+    lam = torch.zeros(npad, dtype=torch.float64, device="cuda")
+    lam_out = torch.empty_like(lam)
+    i0 = max(1, int(0.3 * nx) + 1)
+    j0 = max(1, ny // 2 - 7)
+    k0 = max(1, nz // 8)
+    box = (C.c_int * 6)(i0, min(nx, i0 + 15), j0, min(ny, j0 + 15), k0, min(nz, k0 + 7))
+    lamv = lam.view(nz + 2, ny + 2, nx + 2)
+    lamv[k0:k0 + 8, j0:j0 + 16, i0:i0 + 16] = 1.0
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+
+    def fwd():
+        iters = (C.c_int * 4)()
+        resid = (C.c_double * 4)()
+        _lib.check(lib.asam_ros_step(blk.h, p(cur), a.dt, iters, resid), "asam_ros_step", allow=(0, 1, 2))
+
+    J = C.c_double()
+
+    def gradient(nsteps):
+        _lib.check(lib.asam_tracer_gradient(blk.h, p(c0), comp, nsteps, a.dt, a.adj_ckpt, box, tol, C.byref(J),
+                                            p(grad)), "asam_tracer_gradient", allow=(0, 1))
+
+    def adj_step():
+        _lib.check(lib.asam_ros_step_adj(blk.h, p(c0), comp, p(lam), p(lam_out), a.dt, tol), "asam_ros_step_adj",
+                   allow=(0, 1))
+
+    fwd()
+    cur.copy_(c0)
+    ms_fwd = time_region(torch, stream, fwd, a.adj_steps)
+    gradient(a.adj_ckpt)
+    ms_grad = time_region(torch, stream, lambda: gradient(a.adj_steps), 1)
+    cur.copy_(c0)
+    ms_fwd1 = time_region(torch, stream, fwd, 3) / 3
+    adj_step()
+    ms_adj1 = time_region(torch, stream, adj_step, 3) / 3
+    blk.close()
+    return {"workload": f"cut-cell Gaussian hill h=800 m, half-width 4 km, {nx}x{ny}x{nz}, {ncomp} components "
+                        f"(Rho, Rho*theta, Rho*tracer), RosRK3 dt={a.dt}s, {a.adj_steps} steps, checkpoint every "
+                        f"{a.adj_ckpt}, J over a 16x16x8 box, BiCGStab tol {tol:g}",
+            "forward_ms": ms_fwd, "gradient_ms": ms_grad, "gradient_over_forward": ms_grad / ms_fwd,
+            "forward_step_ms": ms_fwd1, "adjoint_step_ms": ms_adj1,
+            "adjoint_step_over_forward_step": ms_adj1 / ms_fwd1,
+            "note": "adjoint step = asam_ros_step_adj: the step's forward recomputation with stage states plus its "
+                    "transpose; gradient = forward sweep with checkpoints + per step one recomputation, the stage "
+                    "matrix rebuild and the adjoint step", "J": J.value}
+
+
 def time_region(torch, stream, fn, n):
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -253,9 +334,12 @@ def main():
 
     results = {}
     gpu_launches = {}
-    for prec in (["fp64"] + ([] if a.no_refined else ["fp32_refined"])):
+    precs = ["fp64"] + ([] if a.no_refined else ["fp32_refined"])
+    if a.precision != "both":
+        precs = [a.precision]
+    for prec in precs:
         blk = asam_gb300.TransportBlock(geo, ncomp, method="RosRK3", bicgstab_tol=a.tol, bicgstab_maxiter=30,
-                                        precision=prec, inner_precond=a.inner)
+                                        precision=prec, inner_precond=a.inner, inner_gs_iter=a.inner_gs_iter)
         blk.set_velocity(*vel)
         blk.set_stream(stream.cuda_stream)
         dptr = blk.state_device_ptr()
@@ -318,6 +402,17 @@ def main():
         del dstate, f_out, pinned
         torch.cuda.empty_cache()
 
+    adj = None
+    if not a.no_adjoint and world == 1:
+        adj = adjoint_cost(a, lib, torch, stream)
+    if "fp64" not in results:  # a profiling run of one variant: no comparison line
+        rr = results[precs[0]]
+        if rank == 0:
+            print(json.dumps({"variant": precs[0], "ms_per_step": rr["ms"] / a.steps, "kernels_ms": rr["kernels"],
+                              "krylov_iterations": rr["iters"], "gpu_launches": gpu_launches[precs[0]]}), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     gf = C.c_double()
     lib.asam_probe_fp64_fma(20000, C.byref(gf))
     peaks = {}
@@ -379,10 +474,12 @@ def main():
                                 "ms_per_step": rr["ms"] / a.steps,
                                 "speedup_vs_fp64": r64["ms"] / rr["ms"],
                                 "max_rel_err_vs_fp64": max(e["max_rel"] for e in errs), "fields": errs,
-                                "inner_preconditioner": a.inner,
+                                "inner_preconditioner": a.inner, "inner_gs_iter": a.inner_gs_iter,
                                 "krylov_iterations": rr["iters"], "kernels_ms": rr["kernels"],
                                 "gpu_launches": gpu_launches["fp32_refined"],
                                 "clocks": rr["clocks"]}
+    if adj is not None:
+        line["adjoint"] = adj
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if rank == 0:

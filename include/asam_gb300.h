@@ -62,6 +62,8 @@ typedef struct {
   int inner_precond;                       /* refined mode's FP32 inner preconditioner:
                                               0 = the Gauss-Seidel sweeps of the FP64 path,
                                               1 = vertical-column line solve (Thomas along z) */
+  int inner_gs_iter;                       /* refined mode: IterG of the FP32 inner Gauss-Seidel
+                                              (1+inner_gs_iter sweeps; the FP64 path keeps gs_iter) */
 } asam_config;
 
 typedef struct asam_ctx asam_ctx;
@@ -157,8 +159,11 @@ int asam_ros_step_adj(asam_ctx *ctx, const double *c, int comp, const double *la
 /* Gradient of J = sum over the box of (c_comp/Rho)^2 * VolC after nsteps steps
  * with respect to the initial component field (interior of a padded field).
  * box = {i0,i1,j0,j1,k0,k1}, 1-based interior indices, inclusive.  The forward
- * states are checkpointed every ckpt_every steps and recomputed in the reverse
- * sweep: memory (nsteps/ckpt_every + ckpt_every + nStage + 1) states. */
+ * states are checkpointed every ckpt_every steps; the reverse sweep recomputes
+ * each segment once from its checkpoint, recording the stage states of its
+ * steps: memory (nsteps/ckpt_every + ckpt_every*nStage + nStage + 3) states;
+ * cost one forward sweep plus, per step, one forward recomputation and one
+ * adjoint step. */
 int asam_tracer_gradient(asam_ctx *ctx, const double *c0, int comp, int nsteps, double dt, int ckpt_every,
                          const int *box, double tol, double *J, double *grad);
 
