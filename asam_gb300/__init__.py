@@ -34,7 +34,8 @@ from ._lib import ASAM_BREAKDOWN, ASAM_NOT_CONVERGED, ASAM_OK, AsamConfig, AsamE
 METHODS = {"Ros3AMF": 0, "RosRK32": 1, "RosEul": 2, "Ros3P": 3, "Ros3Pw": 4, "RosRK3": 5, "RosTVD": 6,
            "RosRK4": 7}
 PRECISIONS = {"fp64": 0, "fp32_refined": 1}
-INNER_PRECONDS = {"gauss_seidel": 0, "line": 1}
+INNER_PRECONDS = {"gauss_seidel": 0, "line": 1, "xline": 2, "yline": 3}
+GS_SCHEDULES = {"persistent": 0, "levels": 1}
 
 __all__ = ["TransportBlock", "Solve_1D", "MatVecT_1D", "ros_coeffs", "METHODS", "PRECISIONS", "AsamError"]
 
@@ -64,14 +65,16 @@ class TransportBlock:
 
     def __init__(self, geo, ncomp: int, rho_pos: int = 0, method: str = "RosRK3", bicgstab_tol: float = 1e-6,
                  bicgstab_maxiter: int = 30, gs_iter: int = 5, precision: str = "fp64",
-                 inner_precond: str = "gauss_seidel", inner_gs_iter: int = 1):
+                 inner_precond: str = "gauss_seidel", inner_gs_iter: int = 1, gs_schedule: str = "persistent",
+                 gs_group: int = 0):
         self.lib = _lib.load()
         g = geo.grid
         self.grid = g
         self.ncomp = ncomp
         self.cfg = AsamConfig(g.nx, g.ny, g.nz, int(g.periodic_x), int(g.periodic_y), int(g.periodic_z), ncomp,
                               rho_pos, METHODS[method], bicgstab_maxiter, bicgstab_tol, gs_iter,
-                              PRECISIONS[precision], INNER_PRECONDS[inner_precond], inner_gs_iter)
+                              PRECISIONS[precision], INNER_PRECONDS[inner_precond], inner_gs_iter,
+                              GS_SCHEDULES[gs_schedule], gs_group)
         self._geo = [_f64(geo.volc), _f64(geo.fu), _f64(geo.fv), _f64(geo.fw)]
         h = C.c_void_p()
         check(self.lib.asam_create(C.byref(self.cfg), *(ptr(a) for a in self._geo), C.byref(h)), "asam_create")
@@ -166,6 +169,26 @@ class TransportBlock:
         check(self.lib.asam_psolve(self.h, ptr(a), ptr(y)), "asam_psolve")
         return y
 
+    def autotune(self, c, dt: float) -> dict:
+        """Pick the refined inner-solver settings for this block (asam_autotune).
+        c: host state array or device pointer (int)."""
+        choice = (C.c_int * 4)()
+        ms = C.c_double()
+        p = C.c_void_p(c) if isinstance(c, int) else ptr(self._state(c))
+        check(self.lib.asam_autotune(self.h, p, float(dt), choice, C.byref(ms)), "asam_autotune")
+        names = {v: k for k, v in INNER_PRECONDS.items()}
+        scheds = {v: k for k, v in GS_SCHEDULES.items()}
+        return {"inner_precond": names[choice[0]], "inner_gs_iter": choice[1], "gs_schedule": scheds[choice[2]],
+                "gs_group": choice[3], "stage_solve_ms": ms.value}
+
+    def inner_psolve(self, x: np.ndarray) -> np.ndarray:
+        """The refined mode's FP32 inner preconditioner applied to x (no reference
+        counterpart; for tests and measurement)."""
+        a = self._state(x)
+        y = np.empty_like(a)
+        check(self.lib.asam_inner_psolve(self.h, ptr(a), ptr(y)), "asam_inner_psolve")
+        return y
+
     def BiCGStabMetSp(self, x: np.ndarray, b: np.ndarray, MaxIter: int, Tol: float):
         """Solve A x = b in place of x; returns (MaxIter, Tol) with the reference's
         sentinels (negative: converged at the half step; 2*Iter: limit hit)."""
@@ -202,6 +225,65 @@ class TransportBlock:
         out = C.c_double()
         check(self.lib.asam_total_scalar(self.h, ptr(a), int(comp), C.byref(out)), "asam_total_scalar")
         return out.value
+
+
+class Batch:
+    """Independent blocks advanced together on one GPU (asam_batch_*): each member
+    keeps its own geometry, wind, configuration and stream; the members' steps
+    run concurrently."""
+
+    def __init__(self, blocks, nthreads: int = 0):
+        self.lib = _lib.load()
+        self.blocks = list(blocks)
+        arr = (C.c_void_p * len(self.blocks))(*[b.h.value for b in self.blocks])
+        h = C.c_void_p()
+        check(self.lib.asam_batch_create(len(self.blocks), arr, int(nthreads), C.byref(h)), "asam_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.asam_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def ros_step(self, states, dt, nsteps: int = 1):
+        """Advance every member nsteps steps.  states: per member a C-contiguous
+        float64 host array (updated in place) or a device pointer (int); dt: one
+        value or one per member.  Returns (iters[m][step][stage], status[m])."""
+        n = len(self.blocks)
+        if len(states) != n:
+            raise ValueError(f"expected {n} states")
+        ptrs = []
+        for b, c in zip(self.blocks, states):
+            if isinstance(c, int):
+                ptrs.append(c)
+            else:
+                if not (isinstance(c, np.ndarray) and c.dtype == np.float64 and c.flags.c_contiguous):
+                    raise TypeError("states must be C-contiguous float64 arrays (updated in place) or device pointers")
+                b._state(c)
+                ptrs.append(c.ctypes.data)
+        parr = (C.c_void_p * n)(*ptrs)
+        dts = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,)))
+        iters = np.zeros((n, nsteps, 4), dtype=np.int32)
+        resid = np.zeros((n, nsteps, 4), dtype=np.float64)
+        status = np.zeros(n, dtype=np.int32)
+        rc = self.lib.asam_batch_ros_step(self.h, parr, dts.ctypes.data_as(_lib._D), int(nsteps),
+                                          iters.ctypes.data_as(_lib._I), resid.ctypes.data_as(_lib._D),
+                                          status.ctypes.data_as(_lib._I))
+        check(rc, "asam_batch_ros_step", allow=(ASAM_OK, ASAM_NOT_CONVERGED, ASAM_BREAKDOWN))
+        its = [[list(iters[m, s, :b.nstage]) for s in range(nsteps)] for m, b in enumerate(self.blocks)]
+        return its, status
 
 
 def Solve_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, b: np.ndarray) -> np.ndarray:

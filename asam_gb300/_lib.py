@@ -32,6 +32,7 @@ class AsamConfig(C.Structure):
         ("ncomp", C.c_int), ("rho_pos", C.c_int), ("method", C.c_int),
         ("bicgstab_maxiter", C.c_int), ("bicgstab_tol", C.c_double), ("gs_iter", C.c_int),
         ("precision", C.c_int), ("inner_precond", C.c_int), ("inner_gs_iter", C.c_int),
+        ("gs_schedule", C.c_int), ("gs_group", C.c_int),
     ]
 
 
@@ -54,6 +55,7 @@ SIGNATURES = [
     ("asam_set_jac", C.c_int, [_V, _V]),
     ("asam_matvec", C.c_int, [_V, _V, _V]),
     ("asam_psolve", C.c_int, [_V, _V, _V]),
+    ("asam_inner_psolve", C.c_int, [_V, _V, _V]),
     ("asam_bicgstab", C.c_int, [_V, _V, _V, _I, _D]),
     ("asam_ros_step", C.c_int, [_V, _V, C.c_double, _I, _D]),
     ("asam_total_scalar", C.c_int, [_V, _V, C.c_int, _D]),
@@ -68,6 +70,10 @@ SIGNATURES = [
     ("asam_tri_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_ros_coeffs", C.c_int, [C.c_int, _D, _D, _D, _D]),
+    ("asam_autotune", C.c_int, [_V, _V, C.c_double, _I, _D]),
+    ("asam_batch_create", C.c_int, [C.c_int, _V, C.c_int, C.POINTER(C.c_void_p)]),
+    ("asam_batch_destroy", C.c_int, [_V]),
+    ("asam_batch_ros_step", C.c_int, [_V, _V, _D, C.c_int, _I, _D, _I]),
     ("asam_npad", C.c_longlong, [C.POINTER(AsamConfig)]),
     ("asam_probe_fp64_fma", C.c_int, [C.c_int, _D]),
     ("asam_launch_count", C.c_longlong, []),

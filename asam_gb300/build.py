@@ -37,6 +37,8 @@ UNITS = {
     "capi.cu": [],
     "tri_noalloc.cu": ["-fmad=false"],
     "adjoint.cu": ["-fmad=false"],
+    "batch.cu": [],
+    "tune.cu": [],
 }
 
 

@@ -76,6 +76,22 @@ struct KrylovScalars {
   double dot_a, dot_b;
   int done;       // 0 running; 1 converged at half step; 2 converged; 3 breakdown
   int iter;
+  int gs_err;     // set by the persistent Gauss-Seidel schedule when a wait gave up
+};
+
+// Schedule of the persistent Gauss-Seidel wavefront (k_gs_persist): tickets
+// (I, J, K, sweep) in pipelined-level order, per-tile completion counters
+// (base + last completed sweep + 1; base grows by the sweep count every
+// launch, so counters never need clearing), the ticket counter (zeroed before
+// each launch) and the error flag.
+struct GsTileSched {
+  const int4* order;
+  int nticket;
+  int* flags;
+  int* counter;
+  int* err;
+  int base;
+  int group;  // components per CTA
 };
 
 // What a reduction's final kernel does with the sum (Krylov recurrences of

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 #include <string>
 
 #include "context.h"
@@ -199,6 +200,10 @@ int check_launch() {
 int read_scalars(asam_ctx* h) {
   CK(cudaMemcpyAsync(h->sc_host, h->sc, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->L.stream));
   CK(cudaStreamSynchronize(h->L.stream));
+  if (h->sc_host->gs_err) {
+    set_last_error("persistent Gauss-Seidel schedule: a dependency wait gave up", __FILE__, __LINE__);
+    return kCudaError;
+  }
   return kOk;
 }
 
@@ -207,6 +212,63 @@ int reduce_to_host(asam_ctx* h, double* out) {
   CK(cudaStreamSynchronize(h->L.stream));
   *out = *h->red_host;
   return kOk;
+}
+
+// Tiles of the Gauss-Seidel wavefront (32 x 4 x 4 cells of the padded box) and
+// component groups of its FP32 variants (two components per CTA).
+static int gs_tile_count(const Dims& d) {
+  return ((d.NX() + 31) / 32) * ((d.NY() + 3) / 4) * ((d.NZ() + 3) / 4);
+}
+static int gs_ngroups_host(int ncomp, int group) { return (ncomp + group - 1) / group; }
+
+// Components per CTA of the FP32 Gauss-Seidel (asam_config.gs_group; 0 picks
+// the library default).
+static int gs_group_of(const asam_config& c) {
+  const int g = c.gs_group > 0 ? c.gs_group : 5;
+  return g < c.ncomp ? g : c.ncomp;
+}
+
+// Ticket table of the persistent schedule: (I, J, K, sweep*ngroups + group)
+// ordered by level + 2*sweep, so that every dependency of a ticket has a
+// smaller ticket.
+int gs_schedule_init(asam_ctx* h, int nsweep) {
+  const Dims& d = h->d;
+  const int ntx = (d.NX() + 31) / 32, nty = (d.NY() + 3) / 4, ntz = (d.NZ() + 3) / 4;
+  const int nlev = ntx + nty + ntz - 2;
+  const int ngroups = gs_ngroups_host(h->cfg.ncomp, gs_group_of(h->cfg));
+  std::vector<int4> order;
+  order.reserve((size_t)ntx * nty * ntz * nsweep * ngroups);
+  for (int tau = 0; tau < nlev + 2 * (nsweep - 1); ++tau)
+    for (int s = 0; s < nsweep; ++s) {
+      const int L = tau - 2 * s;
+      if (L < 0 || L >= nlev) continue;
+      for (int K = 0; K < ntz; ++K)
+        for (int J = 0; J < nty; ++J) {
+          const int I = L - J - K;
+          if (I < 0 || I >= ntx) continue;
+          for (int g = 0; g < ngroups; ++g) order.push_back(make_int4(I, J, K, s * ngroups + g));
+        }
+    }
+  gs_schedule_free(h);
+  h->gs_nticket = (int)order.size();
+  h->gs_nflags = (size_t)gs_tile_count(d) * ngroups;
+  CK(cudaMalloc((void**)&h->gs_order, order.size() * sizeof(int4)));
+  CK(cudaMalloc((void**)&h->gs_flags, h->gs_nflags * sizeof(int)));
+  CK(cudaMalloc((void**)&h->gs_counter, sizeof(int)));
+  CK(cudaMemcpy(h->gs_order, order.data(), order.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  CK(cudaMemset(h->gs_flags, 0, h->gs_nflags * sizeof(int)));
+  h->gs_base = 0;
+  return kOk;
+}
+
+void gs_schedule_free(asam_ctx* h) {
+  if (h->gs_order) cudaFree(h->gs_order);
+  if (h->gs_flags) cudaFree(h->gs_flags);
+  if (h->gs_counter) cudaFree(h->gs_counter);
+  h->gs_order = nullptr;
+  h->gs_flags = nullptr;
+  h->gs_counter = nullptr;
+  h->gs_nticket = 0;
 }
 
 // PSolve_Vec4CellSp: copy, exchange, 1+IterG Gauss-Seidel sweeps (one
@@ -220,10 +282,22 @@ void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w) {
   cudaMemcpyAsync(w.bbuf, in, h->len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream);
   launch_exchange_cell(L, d, nc, w.bbuf);
   const bool inner = sizeof(T) == sizeof(float);  // FP32 inner solver of the refined mode
-  if (inner && h->cfg.inner_precond == 1)
-    launch_line_psolve(L, d, nc, val, w.bbuf, out, w.tbuf);
-  else
-    launch_gs_sweeps(L, d, nc, val, w.bbuf, out, w.tbuf, 1 + (inner ? h->cfg.inner_gs_iter : h->cfg.gs_iter));
+  const int nsweep = 1 + (inner ? h->cfg.inner_gs_iter : h->cfg.gs_iter);
+  if (inner && h->cfg.inner_precond != 0) {  // 1: z lines, 2: x lines, 3: y lines
+    const int axis = h->cfg.inner_precond == 1 ? 2 : h->cfg.inner_precond == 2 ? 0 : 1;
+    launch_line_psolve(L, d, nc, val, w.bbuf, out, w.tbuf, axis);
+  } else if (inner && h->gs_order) {
+    const GsTileSched sch{h->gs_order,   h->gs_nticket,  h->gs_flags,          h->gs_counter,
+                          &h->sc->gs_err, h->gs_base,     gs_group_of(h->cfg)};
+    launch_gs_persist(L, d, nc, val, w.bbuf, out, w.tbuf, nsweep, sch);
+    h->gs_base += nsweep;
+    if (h->gs_base > (1 << 30)) {  // counters are compared against base + sweep: restart from zero
+      cudaMemsetAsync(h->gs_flags, 0, h->gs_nflags * sizeof(int), L.stream);
+      h->gs_base = 0;
+    }
+  } else {
+    launch_gs_sweeps(L, d, nc, val, w.bbuf, out, w.tbuf, nsweep, gs_group_of(h->cfg));
+  }
   launch_zero_halo(L, d, nc, out);
   launch_exchange_cell(L, d, nc, out);
 }
@@ -463,8 +537,10 @@ int validate(const asam_config* c) {
   if (c->rho_pos < 0 || c->rho_pos >= c->ncomp) return kBadArg;
   if (c->bicgstab_maxiter < 1 || c->gs_iter < 0) return kBadArg;
   if (c->precision != ASAM_PREC_FP64 && c->precision != ASAM_PREC_FP32_REFINED) return kBadArg;
-  if (c->inner_precond != 0 && c->inner_precond != 1) return kBadArg;
+  if (c->inner_precond < 0 || c->inner_precond > 3) return kBadArg;
   if (c->inner_gs_iter < 0) return kBadArg;
+  if (c->gs_schedule != 0 && c->gs_schedule != 1) return kBadArg;
+  if (c->gs_group < 0 || c->gs_group > 16) return kBadArg;
   return kOk;
 }
 
@@ -592,6 +668,7 @@ int asam_destroy(asam_ctx* h) {
   if (h->red_host) cudaFreeHost(h->red_host);
   free_work(h->w64);
   free_work(h->w32);
+  gs_schedule_free(h);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return kOk;
@@ -624,6 +701,7 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&h->L.sm_count, cudaDevAttrMultiProcessorCount, dev);
+  h->device = dev;
   auto fail = [&](cudaError_t e) {
     set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
     asam_destroy(h);
@@ -659,6 +737,10 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
     if ((e = cudaMalloc((void**)&h->x32, h->len * sizeof(float))) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&h->b32, h->len * sizeof(float))) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&h->dcorr, h->len * sizeof(double))) != cudaSuccess) return fail(e);
+    if (cfg->inner_precond == 0 && cfg->gs_schedule == 0 && gs_schedule_init(h, 1 + cfg->inner_gs_iter) != kOk) {
+      asam_destroy(h);
+      return (int)kCudaError;
+    }
   }
   struct C {
     double* dst;
@@ -798,6 +880,27 @@ int asam_psolve(asam_ctx* h, const double* x, double* px) {
   psolve_dev<double>(h, h->val, dx, dp, h->w64);
   rc = check_launch();
   if (rc) return rc;
+  return stage_out_end(h, px, h->len, dp);
+}
+
+int asam_inner_psolve(asam_ctx* h, const double* x, double* px) {
+  if (!h || !x || !px) return kBadArg;
+  if (h->cfg.precision != ASAM_PREC_FP32_REFINED) {
+    set_last_error("the FP32 inner preconditioner exists in the refined precision only", __FILE__, __LINE__);
+    return kBadArg;
+  }
+  const Launch& L = h->L;
+  const double* dx;
+  double* dp;
+  int rc = stage_in(h, x, h->len, h->stage_a, &dx);
+  if (rc) return rc;
+  rc = stage_out_begin(h, px, h->len, h->stage_b, &dp, false);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(&h->sc->gs_err, 0, sizeof(int), L.stream));
+  launch_convert_f64_to_f32(L, h->len, dx, h->b32);
+  psolve_dev<float>(h, h->val32, h->b32, h->x32, h->w32);
+  launch_convert_f32_to_f64(L, h->len, h->x32, dp);
+  if ((rc = check_launch()) || (rc = read_scalars(h))) return rc;
   return stage_out_end(h, px, h->len, dp);
 }
 

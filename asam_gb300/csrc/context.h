@@ -41,6 +41,7 @@ struct asam_ctx {
   asam_config cfg;
   Dims d;
   Launch L;
+  int device = 0;
   cudaStream_t own_stream = nullptr;
   size_t npad = 0, len = 0;
   int nstage = 0;
@@ -66,6 +67,13 @@ struct asam_ctx {
   double* red_host = nullptr;
   double *stage_a = nullptr, *stage_b = nullptr;
   bool jac_ready = false;
+  // persistent Gauss-Seidel schedule of the FP32 inner sweeps
+  int4* gs_order = nullptr;
+  int gs_nticket = 0;
+  int* gs_flags = nullptr;  // one completion counter per tile and component group
+  size_t gs_nflags = 0;
+  int* gs_counter = nullptr;
+  int gs_base = 0;
 
   GeomT<double> geom() const { return GeomT<double>{volc, fu, fv, fw, uf, vf, wf}; }
 };
@@ -73,6 +81,7 @@ struct asam_ctx {
 namespace asam {
 
 void count_launches(long long n);
+void set_last_error(const char* msg, const char* file, int line);
 int check_launch();
 int read_scalars(asam_ctx* h);
 int reduce_to_host(asam_ctx* h, double* out);
@@ -89,6 +98,8 @@ int ros_step_dev(asam_ctx* h, double* c, double dt, int* iters, double* resid);
 int stage_in(asam_ctx* h, const double* p, size_t n, double* buf, const double** dev);
 int stage_out_begin(asam_ctx* h, double* p, size_t n, double* buf, double** dev, bool copy_in);
 int stage_out_end(asam_ctx* h, double* p, size_t n, double* dev);
+int gs_schedule_init(asam_ctx* h, int nsweep);
+void gs_schedule_free(asam_ctx* h);
 
 }  // namespace asam
 

@@ -11,6 +11,7 @@ namespace {
 
 using asam::Dims;
 using asam::kMaxComp;
+using asam::GsTileSched;
 
 template <typename T>
 __device__ __forceinline__ T eps_t() {
@@ -667,18 +668,203 @@ __device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem, bool pred)
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// Variant for latency-bound precisions (FP32): every operand of the tile that
-// does not depend on this sweep's new values is copied to shared memory by
-// cp.async in one batch (one memory round trip per launch instead of one per
-// load), b - U x^{s-1} is formed there, and the wavefront then reads only
-// shared memory and registers.
+// One tile of one sweep with its operands staged in shared memory (the FP32
+// variants): every operand that does not depend on this sweep's new values is
+// copied by cp.async in one batch (one memory round trip instead of one per
+// load), b - U x^{s-1} is formed in shared memory, and the wavefront then reads
+// only shared memory and registers.  The copies are issued in two groups so
+// that a scheduler can wait for the tile's dependencies in between: the
+// coefficients and b never change during the sweeps; x^{s-1} and the x^s halo
+// are written by other tiles.
 template <typename TM, typename T>
-__global__ void __launch_bounds__(256) k_gs_pipe_smem(Dims d, int ncomp, const TM* __restrict__ val,
+struct GsTile {
+  static_assert(sizeof(TM) == sizeof(T), "coefficients are copied as they are stored");
+  int ncomp, NX, NY, NZ;
+  size_t n, sy, sz;
+  const TM* val;
+  const T* b;
+  T* xn_all;        // x^s
+  const T* xo_all;  // x^{s-1}
+  bool up;
+  int i0, j0, k0;
+  T *ts, *ls, *xs, *zb, *yb, *xb;
+
+  // components c0 .. c0+ncomp_-1 of the fields (the sweeps of different
+  // components are independent: one matrix, no coupling)
+  __device__ GsTile(const Dims& d, int c0, int ncomp_, const TM* val_, const T* b_, T* buf_last, T* buf_other,
+                    int nsweep, int I, int J, int K, int s, unsigned char* smem)
+      : ncomp(ncomp_), NX(d.NX()), NY(d.NY()), NZ(d.NZ()), n(d.npad()), sy((size_t)d.NX()),
+        sz((size_t)d.NX() * d.NY()), val(val_), b(b_ + (size_t)c0 * d.npad()), up(s > 0), i0(I * GS_TX),
+        j0(J * GS_TY), k0(K * GS_TZ) {
+    const bool last_parity = ((nsweep - 1 - s) & 1) == 0;
+    xn_all = (last_parity ? buf_last : buf_other) + (size_t)c0 * n;
+    xo_all = (last_parity ? buf_other : buf_last) + (size_t)c0 * n;
+    ts = reinterpret_cast<T*>(smem);
+    ls = ts + (size_t)ncomp * GS_TILE;
+    xs = ls + 8 * (size_t)GS_TILE;
+    zb = xs + (size_t)ncomp * GS_BOX;
+    yb = zb + (size_t)ncomp * GS_TY * GS_TX;
+    xb = yb + (size_t)ncomp * GS_TZ * GS_TX;
+  }
+
+  // The copies are issued per x-row of the tile: warp w takes rows w, w+nwarp,
+  // ...; lane a copies cell i0+a of the row (coalesced, one address per lane).
+  // group 1: the eight coefficient slots and b
+  __device__ void issue_fixed() const {
+    TM* lsm = reinterpret_cast<TM*>(ls);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int i = i0 + lane;
+    constexpr int ROWS = GS_TY * GS_TZ;
+    for (int r = warp; r < 8 * ROWS; r += nwarp) {
+      const int m = r / ROWS, line = r % ROWS;
+      const int j = j0 + line % GS_TY, k = k0 + line / GS_TY;
+      const bool in = i < NX && j < NY && k < NZ;
+      const size_t P = in ? (size_t)i + sy * j + sz * k : 0;
+      // slot m of the shared tile: (matrix column, cell offset, condition)
+      const TM* src = val;
+      bool p = false;
+      switch (m) {
+        case 0: p = in && k > 0; src = val + 0 * n + P - sz; break;
+        case 1: p = in && j > 0; src = val + 1 * n + P - sy; break;
+        case 2: p = in && i > 0; src = val + 2 * n + P - 1; break;
+        case 3: p = in; src = val + 3 * n + P; break;
+        case 4: p = in; src = val + 7 * n + P; break;
+        case 5: p = in && up && i < NX - 1; src = val + 4 * n + P + 1; break;
+        case 6: p = in && up && j < NY - 1; src = val + 5 * n + P + sy; break;
+        default: p = in && up && k < NZ - 1; src = val + 6 * n + P + sz; break;
+      }
+      cp_async_elem(lsm + m * GS_TILE + line * GS_TX + lane, p ? src : val, p);
+    }
+    for (int r = warp; r < ncomp * ROWS; r += nwarp) {
+      const int ic = r / ROWS, line = r % ROWS;
+      const int j = j0 + line % GS_TY, k = k0 + line / GS_TY;
+      const bool in = i < NX && j < NY && k < NZ;
+      cp_async_elem(ts + r * GS_TX + lane, in ? b + (size_t)ic * n + (size_t)i + sy * j + sz * k : b, in);
+    }
+  }
+
+  // group 2: x^{s-1} on the tile grown by one cell in +x, +y, +z (the edges
+  // and the corner of the grown part are never read, and may be written by
+  // sweep s-1 meanwhile: they are skipped), and the x^s faces of the three
+  // lower neighbour tiles
+  __device__ void issue_neighbours() const {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int i = i0 + lane;
+    if (up) {
+      constexpr int BROWS = GS_BY * GS_BZ;
+      for (int r = warp; r < ncomp * BROWS; r += nwarp) {
+        const int ic = r / BROWS, line = r % BROWS;
+        const int tb = line % GS_BY, tc = line / GS_BY;
+        if (tb == GS_TY && tc == GS_TZ) continue;  // edge of the grown part: never read
+        const int j = j0 + tb, k = k0 + tc;
+        const bool row = j < NY && k < NZ;
+        const T* src = xo_all + (size_t)ic * n + sy * j + sz * k;
+        T* dst = xs + (size_t)ic * GS_BOX + line * GS_BX;
+        cp_async_elem(dst + lane, row && i < NX ? src + i : xo_all, row && i < NX);
+        if (lane == 0 && tb < GS_TY && tc < GS_TZ) {  // the +x cell of the row
+          const bool p = row && i0 + GS_TX < NX;
+          cp_async_elem(dst + GS_TX, p ? src + i0 + GS_TX : xo_all, p);
+        }
+      }
+    }
+    for (int r = warp; r < ncomp * GS_TY; r += nwarp) {  // plane below: rows tb
+      const int ic = r / GS_TY, tb = r % GS_TY;
+      const int j = j0 + tb, k = k0;
+      const bool in = k > 0 && i < NX && j < NY;
+      cp_async_elem(zb + r * GS_TX + lane, in ? xn_all + (size_t)ic * n + (size_t)i + sy * j + sz * (k - 1) : xn_all,
+                    in);
+    }
+    for (int r = warp; r < ncomp * GS_TZ; r += nwarp) {  // row to the south: rows tc
+      const int ic = r / GS_TZ, tc = r % GS_TZ;
+      const int j = j0, k = k0 + tc;
+      const bool in = j > 0 && i < NX && k < NZ;
+      cp_async_elem(yb + r * GS_TX + lane, in ? xn_all + (size_t)ic * n + (size_t)i + sy * (j - 1) + sz * k : xn_all,
+                    in);
+    }
+    for (int q = threadIdx.x; q < ncomp * GS_TZ * GS_TY; q += blockDim.x) {  // column to the west
+      const int ic = q / (GS_TZ * GS_TY), c = q % (GS_TZ * GS_TY);
+      const int tb = c % GS_TY, tc = c / GS_TY;
+      const int j = j0 + tb, k = k0 + tc;
+      const bool in = i0 > 0 && j < NY && k < NZ;
+      cp_async_elem(xb + q, in ? xn_all + (size_t)ic * n + (size_t)(i0 - 1) + sy * j + sz * k : xn_all, in);
+    }
+  }
+
+  // waits for both groups, forms b - U x^{s-1}, runs the wavefront and stores x^s
+  __device__ void compute() const {
+    cp_async_wait_all();
+    __syncthreads();
+    if (up) {  // b - U x^{s-1} in the reference's column order, one x-row per warp
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+      const int i = i0 + lane;
+      constexpr int ROWS = GS_TY * GS_TZ;
+      for (int r = warp; r < ncomp * ROWS; r += nwarp) {
+        const int ic = r / ROWS, line = r % ROWS;
+        const int tb = line % GS_TY, tc = line / GS_TY;
+        const int j = j0 + tb, k = k0 + tc;
+        if (i < NX && j < NY && k < NZ) {
+          const int c = line * GS_TX + lane;
+          const T* xq = xs + (size_t)ic * GS_BOX + (tc * GS_BY + tb) * GS_BX + lane;
+          T t = ts[r * GS_TX + lane];
+          if (i < NX - 1) t = t - ls[5 * GS_TILE + c] * xq[1];
+          if (j < NY - 1) t = t - ls[6 * GS_TILE + c] * xq[GS_BX];
+          if (k < NZ - 1) t = t - ls[7 * GS_TILE + c] * xq[GS_BX * GS_BY];
+          ts[r * GS_TX + lane] = t;
+        }
+      }
+      __syncthreads();
+    }
+    // wavefront over the tile's hyperplanes.  lane = tb + GS_TY*tc + 16*(ic&1):
+    // the y-neighbour line is lane-1 and the z-neighbour line lane-GS_TY.
+    const int lb = threadIdx.x % (GS_TY * GS_TZ);
+    const int ic = threadIdx.x / (GS_TY * GS_TZ);
+    const int tb = lb % GS_TY, tc = lb / GS_TY;
+    const int j = j0 + tb, k = k0 + tc;
+    const bool line_ok = ic < ncomp && j < NY && k < NZ;
+    const int icc = line_ok ? ic : 0;
+    T* xn = xn_all + (size_t)icc * n;
+    const size_t rowP = sy * (size_t)j + sz * (size_t)k;
+    const int amax = min(GS_TX, NX - i0);
+    const T* tl = ts + (size_t)icc * GS_TILE + (tc * GS_TY + tb) * GS_TX;
+    const int lq = (tc * GS_TY + tb) * GS_TX;
+    T last = line_ok ? xb[(icc * GS_TZ + tc) * GS_TY + tb] : (T)0;  // x-neighbour of cell 0
+    const unsigned full = 0xffffffffu;
+    const int nlev_in = GS_TX + GS_TY + GS_TZ - 2;
+    for (int l = 0; l < nlev_in; ++l) {
+      const T from_y = __shfl_up_sync(full, last, 1);
+      const T from_z = __shfl_up_sync(full, last, GS_TY);
+      const int a = l - tb - tc;
+      if (line_ok && a >= 0 && a < amax) {
+        const int i = i0 + a;
+        const int q = lq + a;
+        T t = tl[a];
+        if (k > 0) t = t - ls[0 * GS_TILE + q] * (tc > 0 ? from_z : zb[(icc * GS_TY + tb) * GS_TX + a]);
+        if (j > 0) t = t - ls[1 * GS_TILE + q] * (tb > 0 ? from_y : yb[(icc * GS_TZ + tc) * GS_TX + a]);
+        if (i > 0) t = t - ls[2 * GS_TILE + q] * last;
+        t = div_rn(t, ls[3 * GS_TILE + q], ls[4 * GS_TILE + q]);
+        xn[(size_t)i + rowP] = t;
+        last = t;
+      }
+    }
+  }
+};
+
+// The shared-memory variants run `group` components per CTA (16 tile lines
+// per component, whole warps): the sweeps of different components are
+// independent wavefronts, so smaller groups give more, smaller CTAs (more per
+// SM, shorter copy phases) at the price of copying the tile's coefficients
+// once per group.
+__host__ __device__ inline int gs_ngroups(int ncomp, int group) { return (ncomp + group - 1) / group; }
+
+// Level-synchronous schedule: launch tau runs tile level tau-2s of every sweep
+// s and component group g (blockIdx.z = s*ngroups + g).
+template <typename TM, typename T>
+__global__ void __launch_bounds__(256) k_gs_pipe_smem(Dims d, int ncomp, int group, const TM* __restrict__ val,
                                                       const T* __restrict__ b, T* buf_last, T* buf_other, int tau,
                                                       int nsweep, int ntx, int nty, int ntz, int nlev) {
   static_assert(GS_TY * GS_TZ == 16, "one component's tile lines fill half a warp");
-  static_assert(sizeof(TM) == sizeof(T), "coefficients are copied as they are stored");
-  const int s = blockIdx.z;
+  const int ngroups = gs_ngroups(ncomp, group);
+  const int s = blockIdx.z / ngroups, g = blockIdx.z % ngroups;
   const int L = tau - 2 * s;
   if (L < 0 || L >= nlev) return;
   const int K = blockIdx.y;
@@ -686,160 +872,139 @@ __global__ void __launch_bounds__(256) k_gs_pipe_smem(Dims d, int ncomp, const T
   const int J = Jlo + (int)blockIdx.x;
   const int I = L - J - K;
   if (J >= nty || I < 0 || I >= ntx) return;  // uniform over the block
-  const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
-  const size_t n = d.npad();
-  const size_t sy = (size_t)NX, sz = (size_t)NX * NY;
-  const bool last_parity = ((nsweep - 1 - s) & 1) == 0;
-  T* xn_all = last_parity ? buf_last : buf_other;        // x^s
-  const T* xo_all = last_parity ? buf_other : buf_last;  // x^{s-1}
-  const bool up = s > 0;
-  const int i0 = I * GS_TX, j0 = J * GS_TY, k0 = K * GS_TZ;
-
   extern __shared__ __align__(16) unsigned char gs_smem_raw[];
-  T* ts = reinterpret_cast<T*>(gs_smem_raw);
-  T* ls = ts + (size_t)ncomp * GS_TILE;
-  T* xs = ls + 8 * (size_t)GS_TILE;
-  T* zb = xs + (size_t)ncomp * GS_BOX;
-  T* yb = zb + (size_t)ncomp * GS_TY * GS_TX;
-  T* xb = yb + (size_t)ncomp * GS_TZ * GS_TX;
-  const TM* vbase = reinterpret_cast<const TM*>(val);
+  const int c0 = g * group;
+  const GsTile<TM, T> tile(d, c0, min(group, ncomp - c0), val, b, buf_last, buf_other, nsweep, I, J, K, s,
+                           gs_smem_raw);
+  tile.issue_fixed();
+  tile.issue_neighbours();
+  tile.compute();
+}
 
-  // ---- prologue, phase 1: issue every copy of the tile (consecutive threads
-  // take consecutive x, so each warp's copies are coalesced)
-  for (int c = threadIdx.x; c < GS_TILE; c += blockDim.x) {
-    const int a = c % GS_TX, tb = (c / GS_TX) % GS_TY, tc = c / (GS_TX * GS_TY);
-    const int i = i0 + a, j = j0 + tb, k = k0 + tc;
-    const bool in = i < NX && j < NY && k < NZ;
-    const size_t P = in ? (size_t)i + sy * j + sz * k : 0;
-    const bool p0 = in && k > 0, p1 = in && j > 0, p2 = in && i > 0;
-    const bool p5 = in && up && i < NX - 1, p6 = in && up && j < NY - 1, p7 = in && up && k < NZ - 1;
-    cp_async_elem(reinterpret_cast<TM*>(ls) + 0 * GS_TILE + c, p0 ? vbase + 0 * n + P - sz : vbase, p0);
-    cp_async_elem(reinterpret_cast<TM*>(ls) + 1 * GS_TILE + c, p1 ? vbase + 1 * n + P - sy : vbase, p1);
-    cp_async_elem(reinterpret_cast<TM*>(ls) + 2 * GS_TILE + c, p2 ? vbase + 2 * n + P - 1 : vbase, p2);
-    cp_async_elem(reinterpret_cast<TM*>(ls) + 3 * GS_TILE + c, vbase + 3 * n + P, in);
-    cp_async_elem(reinterpret_cast<TM*>(ls) + 4 * GS_TILE + c, vbase + 7 * n + P, in);
-    cp_async_elem(reinterpret_cast<TM*>(ls) + 5 * GS_TILE + c, p5 ? vbase + 4 * n + P + 1 : vbase, p5);
-    cp_async_elem(reinterpret_cast<TM*>(ls) + 6 * GS_TILE + c, p6 ? vbase + 5 * n + P + sy : vbase, p6);
-    cp_async_elem(reinterpret_cast<TM*>(ls) + 7 * GS_TILE + c, p7 ? vbase + 6 * n + P + sz : vbase, p7);
-  }
-  for (int q = threadIdx.x; q < ncomp * GS_TILE; q += blockDim.x) {  // b
-    const int ic = q / GS_TILE, c = q % GS_TILE;
-    const int a = c % GS_TX, tb = (c / GS_TX) % GS_TY, tc = c / (GS_TX * GS_TY);
-    const int i = i0 + a, j = j0 + tb, k = k0 + tc;
-    const bool in = i < NX && j < NY && k < NZ;
-    cp_async_elem(ts + q, in ? b + (size_t)ic * n + (size_t)i + sy * j + sz * k : b, in);
-  }
-  if (up) {
-    for (int q = threadIdx.x; q < ncomp * GS_BOX; q += blockDim.x) {  // x^{s-1} on the grown tile
-      const int ic = q / GS_BOX, r = q % GS_BOX;
-      const int a = r % GS_BX, tb = (r / GS_BX) % GS_BY, tc = r / (GS_BX * GS_BY);
-      const int i = i0 + a, j = j0 + tb, k = k0 + tc;
-      // the edges and the corner of the grown part are never read (and may be
-      // written by sweep s-1 during this launch): skip them
-      const int grown = (a == GS_TX) + (tb == GS_TY) + (tc == GS_TZ);
-      const bool in = grown <= 1 && i < NX && j < NY && k < NZ;
-      cp_async_elem(xs + q, in ? xo_all + (size_t)ic * n + (size_t)i + sy * j + sz * k : xo_all, in);
-    }
-  }
-  for (int q = threadIdx.x; q < ncomp * GS_TY * GS_TX; q += blockDim.x) {  // plane below
-    const int ic = q / (GS_TY * GS_TX), c = q % (GS_TY * GS_TX);
-    const int a = c % GS_TX, tb = c / GS_TX;
-    const int i = i0 + a, j = j0 + tb, k = k0;
-    const bool in = k > 0 && i < NX && j < NY;
-    cp_async_elem(zb + q, in ? xn_all + (size_t)ic * n + (size_t)i + sy * j + sz * (k - 1) : xn_all, in);
-  }
-  for (int q = threadIdx.x; q < ncomp * GS_TZ * GS_TX; q += blockDim.x) {  // row to the south
-    const int ic = q / (GS_TZ * GS_TX), c = q % (GS_TZ * GS_TX);
-    const int a = c % GS_TX, tc = c / GS_TX;
-    const int i = i0 + a, j = j0, k = k0 + tc;
-    const bool in = j > 0 && i < NX && k < NZ;
-    cp_async_elem(yb + q, in ? xn_all + (size_t)ic * n + (size_t)i + sy * (j - 1) + sz * k : xn_all, in);
-  }
-  for (int q = threadIdx.x; q < ncomp * GS_TZ * GS_TY; q += blockDim.x) {  // column to the west
-    const int ic = q / (GS_TZ * GS_TY), c = q % (GS_TZ * GS_TY);
-    const int tb = c % GS_TY, tc = c / GS_TY;
-    const int i = i0, j = j0 + tb, k = k0 + tc;
-    const bool in = i > 0 && j < NY && k < NZ;
-    cp_async_elem(xb + q, in ? xn_all + (size_t)ic * n + (size_t)(i - 1) + sy * j + sz * k : xn_all, in);
-  }
-  cp_async_wait_all();
-  __syncthreads();
+// ---------------------------------------------------------------------------
+// Persistent schedule of the same sweeps: one launch, CTAs take tickets
+// (tile, sweep, component group) from an atomic counter in pipelined-level
+// order (level + 2*sweep, the launch index of the level-synchronous schedule)
+// and wait for the tickets their tile depends on through per-(tile, group)
+// completion counters:
+//   sweep s of tile (I,J,K) needs sweep s of (I-1,J,K), (I,J-1,K), (I,J,K-1)
+//   (lower part) and, for s > 0, sweep s-1 of the tile itself and of
+//   (I+1,J,K), (I,J+1,K), (I,J,K+1) (upper part, x^{s-1}), same group.
+// Every dependency has a smaller ticket, and a CTA only takes a ticket while
+// it runs, so the smallest unfinished ticket can always proceed: no deadlock
+// whatever the number of resident CTAs.  The buffer reuse (x^s overwrites
+// x^{s-2}) is safe by the same chain: every reader of x^{s-2} of a tile is a
+// dependency, direct or transitive, of its sweep s.
+// Waits are bounded: a CTA that gives up sets the error flag, lets its own
+// copies in flight land and returns; the other CTAs see the flag and return.
+// ---------------------------------------------------------------------------
+constexpr int kGsSpinLimit = 1 << 21;
 
-  // ---- prologue, phase 2: t = b - U x^{s-1} in the reference's column order
-  if (up) {
-    for (int q = threadIdx.x; q < ncomp * GS_TILE; q += blockDim.x) {
-      const int ic = q / GS_TILE, c = q % GS_TILE;
-      const int a = c % GS_TX, tb = (c / GS_TX) % GS_TY, tc = c / (GS_TX * GS_TY);
-      const int i = i0 + a, j = j0 + tb, k = k0 + tc;
-      if (i < NX && j < NY && k < NZ) {
-        const T* xq = xs + (size_t)ic * GS_BOX + (tc * GS_BY + tb) * GS_BX + a;
-        T t = ts[q];
-        if (i < NX - 1) t = t - ls[5 * GS_TILE + c] * xq[1];
-        if (j < NY - 1) t = t - ls[6 * GS_TILE + c] * xq[GS_BX];
-        if (k < NZ - 1) t = t - ls[7 * GS_TILE + c] * xq[GS_BX * GS_BY];
-        ts[q] = t;
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ bool gs_wait_flag(const int* f, int target, const int* err) {
+  for (int it = 0; it < kGsSpinLimit; ++it) {
+    if (ld_acquire(f) >= target) return true;
+    if (*(volatile const int*)err) return false;
+    __nanosleep(32);
+  }
+  return false;
+}
+
+template <typename TM, typename T>
+__global__ void __launch_bounds__(256) k_gs_persist(Dims d, int ncomp, const TM* __restrict__ val,
+                                                    const T* __restrict__ b, T* buf_last, T* buf_other, int nsweep,
+                                                    int ntx, int nty, int ntz, GsTileSched sch) {
+  static_assert(GS_TY * GS_TZ == 16, "one component's tile lines fill half a warp");
+  extern __shared__ __align__(16) unsigned char gs_smem_raw[];
+  __shared__ int s_ticket, s_ok;
+  const int group = sch.group;
+  const int ngroups = gs_ngroups(ncomp, group);
+  for (;;) {
+    if (threadIdx.x == 0) s_ticket = *(volatile const int*)sch.err ? sch.nticket : atomicAdd(sch.counter, 1);
+    __syncthreads();
+    const int tk = s_ticket;
+    if (tk >= sch.nticket) return;  // uniform over the block
+    const int4 e = sch.order[tk];
+    const int I = e.x, J = e.y, K = e.z, s = e.w / ngroups, g = e.w % ngroups;
+    const int c0 = g * group;
+    const GsTile<TM, T> tile(d, c0, min(group, ncomp - c0), val, b, buf_last, buf_other, nsweep, I, J, K, s,
+                             gs_smem_raw);
+    tile.issue_fixed();
+    if (threadIdx.x == 0) {
+      const int* f = sch.flags;
+      const int now = sch.base + s + 1, prev = sch.base + s;  // sweep s done, sweep s-1 done
+      const int id = ((K * nty + J) * ntx + I) * ngroups + g;
+      const int sx = ngroups, sy_ = ntx * ngroups, sz_ = ntx * nty * ngroups;
+      bool ok = true;
+      if (I > 0) ok = ok && gs_wait_flag(f + id - sx, now, sch.err);
+      if (J > 0) ok = ok && gs_wait_flag(f + id - sy_, now, sch.err);
+      if (K > 0) ok = ok && gs_wait_flag(f + id - sz_, now, sch.err);
+      if (s > 0) {
+        ok = ok && gs_wait_flag(f + id, prev, sch.err);
+        if (I + 1 < ntx) ok = ok && gs_wait_flag(f + id + sx, prev, sch.err);
+        if (J + 1 < nty) ok = ok && gs_wait_flag(f + id + sy_, prev, sch.err);
+        if (K + 1 < ntz) ok = ok && gs_wait_flag(f + id + sz_, prev, sch.err);
       }
+      if (!ok) atomicExch(sch.err, 1);
+      s_ok = ok;
     }
     __syncthreads();
-  }
-
-  // ---- wavefront over the tile's hyperplanes.  lane = tb + GS_TY*tc + 16*(ic&1):
-  // the y-neighbour line is lane-1 and the z-neighbour line lane-GS_TY.
-  const int lb = threadIdx.x % (GS_TY * GS_TZ);
-  const int ic = threadIdx.x / (GS_TY * GS_TZ);
-  const int tb = lb % GS_TY, tc = lb / GS_TY;
-  const int j = j0 + tb, k = k0 + tc;
-  const bool line_ok = ic < ncomp && j < NY && k < NZ;
-  const int icc = line_ok ? ic : 0;
-  T* xn = xn_all + (size_t)icc * n;
-  const size_t rowP = sy * (size_t)j + sz * (size_t)k;
-  const int amax = min(GS_TX, NX - i0);
-  const T* tl = ts + (size_t)icc * GS_TILE + (tc * GS_TY + tb) * GS_TX;
-  const int lq = (tc * GS_TY + tb) * GS_TX;
-  T last = line_ok ? xb[(icc * GS_TZ + tc) * GS_TY + tb] : (T)0;  // x-neighbour of cell 0
-  const unsigned full = 0xffffffffu;
-  const int nlev_in = GS_TX + GS_TY + GS_TZ - 2;
-  for (int l = 0; l < nlev_in; ++l) {
-    const T from_y = __shfl_up_sync(full, last, 1);
-    const T from_z = __shfl_up_sync(full, last, GS_TY);
-    const int a = l - tb - tc;
-    if (line_ok && a >= 0 && a < amax) {
-      const int i = i0 + a;
-      const int q = lq + a;
-      T t = tl[a];
-      if (k > 0) t = t - ls[0 * GS_TILE + q] * (tc > 0 ? from_z : zb[(icc * GS_TY + tb) * GS_TX + a]);
-      if (j > 0) t = t - ls[1 * GS_TILE + q] * (tb > 0 ? from_y : yb[(icc * GS_TZ + tc) * GS_TX + a]);
-      if (i > 0) t = t - ls[2 * GS_TILE + q] * last;
-      t = div_rn(t, ls[3 * GS_TILE + q], ls[4 * GS_TILE + q]);
-      xn[(size_t)i + rowP] = t;
-      last = t;
+    if (!s_ok) {  // give up: let this CTA's copies land, then leave
+      cp_async_wait_all();
+      return;
     }
+    __threadfence();
+    tile.issue_neighbours();
+    tile.compute();
+    // publish: every thread's stores are ordered before the counter update
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0)
+      st_release(sch.flags + ((K * nty + J) * ntx + I) * ngroups + g, sch.base + s + 1);
   }
 }
 
-// Vertical-column line preconditioner of the refined mode's inner solver:
-// x = Tz^{-1} b with Tz the z-tridiagonal part of the stage matrix (diagonal,
-// column r-NXY of row r and column r+NXY of row r), solved by the Thomas
-// algorithm along each padded column.  One thread per (i,j) column handles
-// all components: the elimination factors depend on the matrix only and are
-// kept in `w` (one value per cell).  Consecutive threads take consecutive i,
-// so every k-plane access is coalesced.
+// Line preconditioners of the refined mode's inner solver: x = T^{-1} b with
+// T the tridiagonal part of the stage matrix along one axis (the diagonal and
+// the couplings to the two neighbours on the axis), solved by the Thomas
+// algorithm along every padded line of that axis; the other couplings are
+// dropped (block Jacobi over lines).  Along the wind the dropped part is small
+// and one application is nearly an exact inverse.
+//
+// y and z lines: one thread per line handles all components (the elimination
+// factors depend on the matrix only and are kept in `w`, one value per cell);
+// consecutive threads take consecutive i, so every access is coalesced.
+// axis 1: lines along y (columns (i,k)); axis 2: along z (columns (i,j)).
 template <typename TM, typename T>
-__global__ void k_line_psolve(Dims d, int ncomp, const TM* __restrict__ val, const T* __restrict__ b,
+__global__ void k_line_psolve(Dims d, int ncomp, int axis, const TM* __restrict__ val, const T* __restrict__ b,
                               T* __restrict__ x, T* __restrict__ w) {
   const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
   const size_t n = d.npad();
-  const size_t sz = (size_t)NX * NY;
-  const size_t ncols = (size_t)NX * NY;
+  const size_t sy = (size_t)NX, sz = (size_t)NX * NY;
+  const bool alz = axis == 2;
+  const size_t st = alz ? sz : sy;          // stride along the line
+  const int len = alz ? NZ : NY;            // cells on the line
+  const int lo = alz ? 0 : 1, hi = alz ? 6 : 5;  // matrix slots of the two neighbours
+  const size_t ncols = (size_t)NX * (alz ? NY : NZ);
   for (size_t col = blockIdx.x * (size_t)blockDim.x + threadIdx.x; col < ncols;
        col += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = col % NX, o = col / NX;
+    const size_t P0 = i + (alz ? sy * o : sz * o);
     T g[kMaxComp];
     // forward elimination
     T wprev = (T)0;
-    for (int k = 0; k < NZ; ++k) {
-      const size_t P = col + sz * (size_t)k;
-      const T a = k > 0 ? (T)val[0 * n + P - sz] : (T)0;
-      const T c = k < NZ - 1 ? (T)val[6 * n + P + sz] : (T)0;
+    for (int k = 0; k < len; ++k) {
+      const size_t P = P0 + st * (size_t)k;
+      const T a = k > 0 ? (T)val[lo * n + P - st] : (T)0;
+      const T c = k < len - 1 ? (T)val[hi * n + P + st] : (T)0;
       const T den = (T)val[3 * n + P] - a * wprev;
       const T rden = (T)1 / den;
       const T wk = c * rden;
@@ -852,8 +1017,8 @@ __global__ void k_line_psolve(Dims d, int ncomp, const TM* __restrict__ val, con
       wprev = wk;
     }
     // back substitution
-    for (int k = NZ - 2; k >= 0; --k) {
-      const size_t P = col + sz * (size_t)k;
+    for (int k = len - 2; k >= 0; --k) {
+      const size_t P = P0 + st * (size_t)k;
       const T wk = w[P];
       for (int ic = 0; ic < ncomp; ++ic) {
         const T xk = x[ic * n + P] - wk * g[ic];
@@ -861,6 +1026,113 @@ __global__ void k_line_psolve(Dims d, int ncomp, const TM* __restrict__ val, con
         x[ic * n + P] = xk;
       }
     }
+  }
+}
+
+// x lines (the memory-contiguous axis): the padded rows of the box are
+// consecutive, so 32 consecutive rows form one contiguous 32 x NX block.  A
+// warp takes 32 rows of one component and walks them in chunks of 32 columns:
+// each chunk of every operand is loaded row by row (lanes along x, coalesced)
+// into a shared 32 x 33 tile, lane q then runs the Thomas recurrence of row q
+// through the chunk from the tile (conflict-free: row pitch 33), and results
+// leave through the tile the same way.  Forward elimination writes the factors
+// w (per component, in `w`) and the partial solution (in x); back
+// substitution walks the chunks in reverse.  One warp per (32 rows, component)
+// gives many independent warps; the factors are recomputed per component.
+template <typename T>
+__host__ __device__ constexpr int xl_warps() {  // warps per CTA: four 32 x 33 tiles per warp within 48 KB
+  return sizeof(T) == 4 ? 2 : 1;
+}
+template <typename TM, typename T>
+__global__ void __launch_bounds__(32 * xl_warps<T>()) k_xline_psolve(Dims d, int ncomp, const TM* __restrict__ val,
+                                                                    const T* __restrict__ b, T* __restrict__ x,
+                                                                    T* __restrict__ w) {
+  constexpr int XL_WARPS = xl_warps<T>();
+  __shared__ T tile[XL_WARPS][4][32][33];  // a, c (then w), d, b (then g, then x)
+  const int NX = d.NX();
+  const size_t n = d.npad();
+  const int nrows = d.NY() * d.NZ();
+  const int ngrp = (nrows + 31) / 32;
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  const long long task = (long long)blockIdx.x * XL_WARPS + wq;  // (row group, component)
+  if (task >= (long long)ngrp * ncomp) return;                   // whole warp
+  const int ic = (int)(task % ncomp), grp = (int)(task / ncomp);
+  const int r0 = grp * 32;
+  const int nr = min(32, nrows - r0);
+  T(*ta)[33] = tile[wq][0];
+  T(*tc)[33] = tile[wq][1];
+  T(*td)[33] = tile[wq][2];
+  T(*tb)[33] = tile[wq][3];
+  const TM* v2 = val + 2 * n;
+  const TM* v3 = val + 3 * n;
+  const TM* v4 = val + 4 * n;
+  const T* bc = b + (size_t)ic * n;
+  T* xc = x + (size_t)ic * n;
+  T* wc = w + (size_t)ic * n;
+  const int nch = (NX + 31) / 32;
+  // chunk loads: every row of the chunk at once by cp.async (one memory round
+  // trip per chunk; out-of-box elements are zero-filled)
+  auto load = [&](T(*t)[33], const auto* src, int ch, int shift, bool lo_ok, bool hi_ok) {
+    const int i = ch * 32 + lane;
+    for (int q = 0; q < nr; ++q) {
+      const size_t P = (size_t)(r0 + q) * NX + i;
+      const bool in = i < NX && (lo_ok || i > 0) && (hi_ok || i < NX - 1);
+      cp_async_elem(&t[q][lane], in ? src + P + shift : src, in);
+    }
+  };
+  T wprev = (T)0, gprev = (T)0;
+  for (int ch = 0; ch < nch; ++ch) {
+    load(ta, v2, ch, -1, false, true);
+    load(tc, v4, ch, +1, true, false);
+    load(td, v3, ch, 0, true, true);
+    load(tb, bc, ch, 0, true, true);
+    cp_async_wait_all();
+    __syncwarp();
+    if (lane < nr) {
+      const int m = min(32, NX - ch * 32);
+      for (int k = 0; k < m; ++k) {
+        const T a = ta[lane][k];
+        const T rden = (T)1 / (td[lane][k] - a * wprev);
+        const T wk = tc[lane][k] * rden;
+        const T gk = (tb[lane][k] - a * gprev) * rden;
+        tc[lane][k] = wk;
+        tb[lane][k] = gk;
+        wprev = wk;
+        gprev = gk;
+      }
+    }
+    __syncwarp();
+    const int i = ch * 32 + lane;
+    for (int q = 0; q < nr; ++q) {
+      const size_t P = (size_t)(r0 + q) * NX + i;
+      if (i < NX) {
+        wc[P] = tc[q][lane];
+        xc[P] = tb[q][lane];
+      }
+    }
+    __syncwarp();
+  }
+  T xnext = (T)0;
+  for (int ch = nch - 1; ch >= 0; --ch) {
+    load(tc, static_cast<const T*>(wc), ch, 0, true, true);
+    load(tb, static_cast<const T*>(xc), ch, 0, true, true);
+    cp_async_wait_all();
+    __syncwarp();
+    if (lane < nr) {
+      const int m = min(32, NX - ch * 32);
+      for (int k = m - 1; k >= 0; --k) {
+        const T xk = (ch == nch - 1 && k == m - 1) ? tb[lane][k] : tb[lane][k] - tc[lane][k] * xnext;
+        tb[lane][k] = xk;
+        xnext = xk;
+      }
+    }
+    __syncwarp();
+    const int i = ch * 32 + lane;
+    for (int q = 0; q < nr; ++q) {
+      const size_t P = (size_t)(r0 + q) * NX + i;
+      if (i < NX) xc[P] = tb[q][lane];
+    }
+    __syncwarp();
   }
 }
 

@@ -25,8 +25,11 @@ struct Launch {
   void launch_jac(const Launch&, const Dims&, const GeomT<T>&, const T* rho, T bdt, T* val);                     \
   void launch_matvec(const Launch&, const Dims&, int ncomp, const TM* val, const T* x, T* y, int plain_spmv);    \
   void launch_gs_sweeps(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, T* out, T* work,       \
-                        int nsweep);                                                                             \
-  void launch_line_psolve(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, T* x, T* w);         \
+                        int nsweep, int group);                                                                  \
+  void launch_gs_persist(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, T* out, T* work,      \
+                         int nsweep, const GsTileSched& sch);                                                    \
+  void launch_line_psolve(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, T* x, T* w,         \
+                          int axis);                                                                             \
   void launch_zero_halo(const Launch&, const Dims&, int ncomp, T* x);                                           \
   void launch_exchange_cell(const Launch&, const Dims&, int ncomp, T* c);                                       \
   void launch_dot(const Launch&, const Dims&, int ncomp, const T* x, const T* y, double* partial,               \

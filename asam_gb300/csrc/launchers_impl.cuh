@@ -56,33 +56,64 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
     k_matvec<TM, T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, val, x, y, plain); count_launches(1);                    \
   }                                                                                                                \
   void launch_gs_sweeps(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* b, T* out, T* work,     \
-                        int nsweep) {                                                                              \
+                        int nsweep, int group) {                                                                   \
     const int ntx = (d.NX() + GS_TX - 1) / GS_TX;                                                                  \
     const int nty = (d.NY() + GS_TY - 1) / GS_TY;                                                                  \
     const int ntz = (d.NZ() + GS_TZ - 1) / GS_TZ;                                                                  \
     const int nlev = ntx + nty + ntz - 2;                                                                          \
-    const int threads = (GS_TY * GS_TZ * ncomp + 31) / 32 * 32; /* whole warps: the sweep shuffles */             \
-    const dim3 grid(ntx, ntz, nsweep);                                                                             \
     const bool staged = sizeof(T) == sizeof(float);                                                               \
-    const size_t smem = staged ? gs_smem_elems(ncomp) * sizeof(T) : 0;                                             \
-    static size_t smem_set = 0;                                                                                    \
-    if (staged && smem > smem_set) {                                                                              \
+    /* whole warps (the sweep shuffles); the staged variant runs one component group per CTA */                 \
+    const int threads = (GS_TY * GS_TZ * (staged ? group : ncomp) + 31) / 32 * 32;                                \
+    const dim3 grid(ntx, ntz, nsweep * (staged ? gs_ngroups(ncomp, group) : 1));                                   \
+    const size_t smem = staged ? gs_smem_elems(group) * sizeof(T) : 0;                                             \
+    thread_local size_t smem_set = 0;                                                                              \
+    if (staged && smem > smem_set) {                                                                               \
       cudaFuncSetAttribute(k_gs_pipe_smem<TM, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
       smem_set = smem;                                                                                             \
     }                                                                                                              \
     for (int tau = 0; tau < nlev + 2 * (nsweep - 1); ++tau) {                                                      \
       if (staged)                                                                                                  \
-        k_gs_pipe_smem<TM, T><<<grid, threads, smem, L.stream>>>(d, ncomp, val, b, out, work, tau, nsweep, ntx,   \
-                                                                 nty, ntz, nlev);                                  \
+        k_gs_pipe_smem<TM, T><<<grid, threads, smem, L.stream>>>(d, ncomp, group, val, b, out, work, tau, nsweep,  \
+                                                                 ntx, nty, ntz, nlev);                             \
       else                                                                                                         \
         k_gs_pipe_reg<TM, T><<<grid, threads, 0, L.stream>>>(d, ncomp, val, b, out, work, tau, nsweep, ntx, nty,  \
                                                              ntz, nlev);                                           \
       count_launches(1);                                                                                           \
     }                                                                                                              \
   }                                                                                                                \
-  void launch_line_psolve(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* b, T* x, T* w) {      \
-    const size_t ncols = (size_t)d.NX() * d.NY();                                                                  \
-    k_line_psolve<TM, T><<<(unsigned)((ncols + 127) / 128), 128, 0, L.stream>>>(d, ncomp, val, b, x, w);           \
+  void launch_gs_persist(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* b, T* out, T* work,    \
+                         int nsweep, const GsTileSched& sch) {                                                     \
+    const int ntx = (d.NX() + GS_TX - 1) / GS_TX;                                                                  \
+    const int nty = (d.NY() + GS_TY - 1) / GS_TY;                                                                  \
+    const int ntz = (d.NZ() + GS_TZ - 1) / GS_TZ;                                                                  \
+    const int threads = (GS_TY * GS_TZ * sch.group + 31) / 32 * 32;                                                \
+    const size_t smem = gs_smem_elems(sch.group) * sizeof(T);                                                      \
+    /* per host thread: the attribute and the occupancy of the last shared-memory size */                       \
+    thread_local size_t smem_set = 0;                                                                              \
+    thread_local int per_sm = 0;                                                                                   \
+    if (smem != smem_set) { /* smem determines threads */                                                         \
+      cudaFuncSetAttribute(k_gs_persist<TM, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);           \
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gs_persist<TM, T>, threads, smem);                  \
+      if (per_sm < 1) per_sm = 1;                                                                                  \
+      smem_set = smem;                                                                                             \
+    }                                                                                                              \
+    int grid = per_sm * L.sm_count;                                                                                \
+    if (grid > sch.nticket) grid = sch.nticket;                                                                    \
+    cudaMemsetAsync(sch.counter, 0, sizeof(int), L.stream);                                                        \
+    k_gs_persist<TM, T><<<grid, threads, smem, L.stream>>>(d, ncomp, val, b, out, work, nsweep, ntx, nty, ntz,    \
+                                                            sch);                                                  \
+    count_launches(1);                                                                                             \
+  }                                                                                                                \
+  void launch_line_psolve(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* b, T* x, T* w,       \
+                          int axis) {                                                                              \
+    if (axis == 0) {                                                                                               \
+      const long long tasks = (long long)((d.NY() * d.NZ() + 31) / 32) * ncomp;                                   \
+      const int wpb = xl_warps<T>();                                                                               \
+      k_xline_psolve<TM, T><<<(unsigned)((tasks + wpb - 1) / wpb), 32 * wpb, 0, L.stream>>>(d, ncomp, val, b, x, w); \
+    } else {                                                                                                       \
+      const size_t ncols = (size_t)d.NX() * (axis == 2 ? d.NY() : d.NZ());                                         \
+      k_line_psolve<TM, T><<<(unsigned)((ncols + 127) / 128), 128, 0, L.stream>>>(d, ncomp, axis, val, b, x, w);   \
+    }                                                                                                              \
     count_launches(1);                                                                                             \
   }                                                                                                                \
   void launch_zero_halo(const Launch& L, const Dims& d, int ncomp, T* x) {                                         \

@@ -52,6 +52,10 @@ def parse():
     p.add_argument("--tol", type=float, default=1e-10)
     p.add_argument("--no-refined", action="store_true")
     p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--batch-members", type=int, default=48)
+    p.add_argument("--batch-steps", type=int, default=20)
+    p.add_argument("--batch-threads", type=int, default=0, help="host threads driving the members (0: one each)")
     p.add_argument("--adj-grid", default="128,128,64", help="nx,ny,nz of the adjoint-cost workload")
     p.add_argument("--adj-steps", type=int, default=40)
     p.add_argument("--adj-ckpt", type=int, default=8)
@@ -59,7 +63,8 @@ def parse():
                    help="which variants to run (profiling runs take one)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample", type=int, default=48, help="edge of the oracle's CPU sample window")
-    p.add_argument("--inner", default="gauss_seidel", choices=["gauss_seidel", "line"],
+    p.add_argument("--no-autotune", action="store_true", help="keep --inner/--inner-gs-iter instead of autotuning")
+    p.add_argument("--inner", default="gauss_seidel", choices=["gauss_seidel", "line", "xline", "yline"],
                    help="preconditioner of the FP32 inner solver of the refined path")
     p.add_argument("--inner-gs-iter", type=int, default=1,
                    help="IterG of the refined path's FP32 inner Gauss-Seidel (the FP64 path keeps 5)")
@@ -267,6 +272,70 @@ def adjoint_cost(a, lib, torch, stream):
                     "matrix rebuild and the adjoint step", "J": J.value}
 
 
+def batch_members(n, seed=4):
+    """Ensemble of independent cut-cell domains: sizes between 64x64x48 and
+    192x160x96, Gaussian hill 0-1.5 km high with half-width 2-8 km, u 5-15 m/s,
+    N 0.008-0.012 1/s, all drawn from the seed."""
+    import numpy as np
+
+    from asam_gb300 import geometry as G
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for m in range(n):
+        nx, ny, nz = int(rng.integers(64, 193)), int(rng.integers(64, 161)), int(rng.integers(48, 97))
+        height, halfwidth = float(rng.uniform(0.0, 1500.0)), float(rng.uniform(2000.0, 8000.0))
+        u0, nbv = float(rng.uniform(5.0, 15.0)), float(rng.uniform(0.008, 0.012))
+        out.append(G.hill_case(nx, ny, nz, seed=seed * 1000 + m, height=height, halfwidth=halfwidth, u0=u0, n_bv=nbv))
+    return out
+
+
+def batch_bench(a, torch, members):
+    """Batched ensemble: all members advanced batch_steps RosRK3 steps (dt=2 s)
+    in one asam_batch_ros_step call, device-resident states; FP64 and refined."""
+    import asam_gb300
+
+    cells = sum(g.grid.nx * g.grid.ny * g.grid.nz for g, _, _ in members)
+    res = {"workload": f"{len(members)} independent cut-cell domains (64x64x48 to 192x160x96, hill 0-1.5 km, "
+                       f"half-width 2-8 km, u 5-15 m/s, N 0.008-0.012), {cells / 1e6:.1f} M cells in total, "
+                       f"{members[0][2].c.shape[0]} components, RosRK3 dt=2 s, {a.batch_steps} steps, "
+                       f"BiCGStab tol {a.tol:g}", "cells": cells, "steps": a.batch_steps}
+    for prec in ("fp64", "fp32_refined"):
+        blocks, dev = [], []
+        t_tune, choices = 0.0, {}
+        for geo, vel, st in members:
+            b = asam_gb300.TransportBlock(geo, st.c.shape[0], method="RosRK3", bicgstab_tol=a.tol,
+                                          bicgstab_maxiter=30, precision=prec, inner_gs_iter=a.inner_gs_iter)
+            b.set_velocity(*vel)
+            if prec == "fp32_refined" and not a.no_autotune:  # each member picks its own inner solver
+                t0 = time.perf_counter()
+                ch = b.autotune(st.c, 2.0)
+                t_tune += time.perf_counter() - t0
+                key = f"{ch['inner_precond']}/iterg{ch['inner_gs_iter']}/{ch['gs_schedule']}/g{ch['gs_group']}"
+                choices[key] = choices.get(key, 0) + 1
+            blocks.append(b)
+            dev.append(torch.from_numpy(st.c.reshape(-1).copy()).cuda())
+        torch.cuda.synchronize()
+        ptrs = [t.data_ptr() for t in dev]
+        with asam_gb300.Batch(blocks, nthreads=a.batch_threads) as batch:
+            batch.ros_step(ptrs, 2.0, nsteps=1)  # warm-up
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            its, status = batch.ros_step(ptrs, 2.0, nsteps=a.batch_steps)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        for b in blocks:
+            b.close()
+        del dev
+        torch.cuda.empty_cache()
+        res[prec] = {"value": cells * a.batch_steps / wall / 1e6, "unit": METRIC, "seconds": wall,
+                     "members_not_ok": int((status != 0).sum())}
+        if choices:
+            res[prec]["autotuned"] = {"settings": choices, "tuning_seconds": t_tune}
+    res["speedup_refined_vs_fp64"] = res["fp32_refined"]["value"] / res["fp64"]["value"]
+    return res
+
+
 def time_region(torch, stream, fn, n):
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -342,6 +411,11 @@ def main():
                                         precision=prec, inner_precond=a.inner, inner_gs_iter=a.inner_gs_iter)
         blk.set_velocity(*vel)
         blk.set_stream(stream.cuda_stream)
+        tuned = None
+        if prec == "fp32_refined" and not a.no_autotune:
+            t0 = time.perf_counter()
+            tuned = blk.autotune(st.c, a.dt)
+            tuned["tuning_seconds"] = time.perf_counter() - t0
         dptr = blk.state_device_ptr()
         host0 = torch.from_numpy(st.c.reshape(-1).copy())
         dstate = torch.empty(st.c.size, dtype=torch.float64, device="cuda")
@@ -396,8 +470,12 @@ def main():
         dstate.copy_(torch.from_numpy(final.reshape(-1)))
         kt["matvec_ms"] = time_region(torch, stream, lambda: _lib.check(
             lib.asam_matvec(blk.h, ctypes_dptr, C.c_void_p(f_out.data_ptr())), "asam_matvec"), nrep) / nrep
+        if prec == "fp32_refined":
+            kt["inner_psolve_ms"] = time_region(torch, stream, lambda: _lib.check(
+                lib.asam_inner_psolve(blk.h, ctypes_dptr, C.c_void_p(f_out.data_ptr())), "asam_inner_psolve"),
+                nrep) / nrep
         results[prec] = {"ms": ms, "ms_e2e": ms_e2e, "final": final, "iters": iters_all, "clocks": clk.summary(),
-                         "kernels": kt}
+                         "kernels": kt, "tuned": tuned}
         blk.close()
         del dstate, f_out, pinned
         torch.cuda.empty_cache()
@@ -405,6 +483,9 @@ def main():
     adj = None
     if not a.no_adjoint and world == 1:
         adj = adjoint_cost(a, lib, torch, stream)
+    bat = None
+    if not a.no_batch and world == 1:
+        bat = batch_bench(a, torch, batch_members(a.batch_members))
     if "fp64" not in results:  # a profiling run of one variant: no comparison line
         rr = results[precs[0]]
         if rank == 0:
@@ -470,16 +551,41 @@ def main():
             d = np.abs(got[i] - ref[i])
             errs.append({"field": st.names[i], "max_rel": float(d.max() / den),
                          "rms_rel": float(np.sqrt(np.mean(d ** 2)) / den)})
+        # dominant kernel of the refined step: the FP32 Gauss-Seidel wavefront; algorithmic
+        # bytes per padded cell and sweep: the 8 matrix slots (32 B) + b, x_old, x_new of
+        # every component (12 B each); the timed call adds two conversion passes
+        # (FP64 in -> FP32 -> FP64 out: 20 B per value), counted too
+        inner = (rr["tuned"] or {}).get("inner_precond", a.inner)
+        if inner == "gauss_seidel":
+            nsw32 = 1 + (rr["tuned"] or {}).get("inner_gs_iter", a.inner_gs_iter)
+            gs32_bytes = npad * nsw32 * (32 + 12 * ncomp) + npad * ncomp * 2 * 12
+            kname = (f"k_gs_persist<float> (one FP32 inner PSolve: {nsw32} sweeps, persistent tile schedule, "
+                     "with its FP64<->FP32 conversions)")
+        else:
+            # line solve: the 3 matrix slots of the axis (12 B) + w (4 B write, 4 B read) per cell, b, g (write,
+            # read) and x per component (16 B), plus the two conversion passes (12 B per value each)
+            gs32_bytes = npad * (20 + 16 * ncomp) + npad * ncomp * 2 * 12
+            kname = f"k_{'xline' if inner == 'xline' else 'line'}_psolve<float> (one FP32 inner PSolve: {inner} " \
+                    "Thomas, with its FP64<->FP32 conversions)"
+        gs32_s = rr["kernels"]["inner_psolve_ms"] * 1e-3
+        line["roofline_refined"] = {
+            "kernel": kname, "bound": "hbm",
+            "achieved": gs32_bytes / gs32_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
+            "frac": gs32_bytes / gs32_s / 1e9 / hbm_peak, "traffic": None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)", "algorithmic_bytes_per_call": gs32_bytes}
         line["fp32_refined"] = {"value": world * ncell * a.steps / (rr["ms"] * 1e-3) / 1e6,
                                 "ms_per_step": rr["ms"] / a.steps,
                                 "speedup_vs_fp64": r64["ms"] / rr["ms"],
                                 "max_rel_err_vs_fp64": max(e["max_rel"] for e in errs), "fields": errs,
-                                "inner_preconditioner": a.inner, "inner_gs_iter": a.inner_gs_iter,
+                                "inner_solver": rr["tuned"] or {"inner_precond": a.inner,
+                                                                "inner_gs_iter": a.inner_gs_iter},
                                 "krylov_iterations": rr["iters"], "kernels_ms": rr["kernels"],
                                 "gpu_launches": gpu_launches["fp32_refined"],
                                 "clocks": rr["clocks"]}
     if adj is not None:
         line["adjoint"] = adj
+    if bat is not None:
+        line["batch"] = bat
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if rank == 0:

@@ -61,9 +61,16 @@ typedef struct {
   int precision;                           /* asam_precision */
   int inner_precond;                       /* refined mode's FP32 inner preconditioner:
                                               0 = the Gauss-Seidel sweeps of the FP64 path,
-                                              1 = vertical-column line solve (Thomas along z) */
+                                              1, 2, 3 = line solves (Thomas along z, x, y: the
+                                              tridiagonal part of the stage matrix on that axis) */
   int inner_gs_iter;                       /* refined mode: IterG of the FP32 inner Gauss-Seidel
                                               (1+inner_gs_iter sweeps; the FP64 path keeps gs_iter) */
+  int gs_schedule;                         /* refined mode, schedule of the FP32 inner sweeps (same
+                                              results either way): 0 = one persistent launch, CTAs
+                                              take tiles in wavefront order and wait for their
+                                              neighbours (bounded waits); 1 = one launch per tile level */
+  int gs_group;                            /* refined mode: components per CTA of the FP32 inner
+                                              Gauss-Seidel (1..16; 0 = library default) */
 } asam_config;
 
 typedef struct asam_ctx asam_ctx;
@@ -119,6 +126,11 @@ int asam_matvec(asam_ctx *ctx, const double *x, double *y);
  * (MODULE/SpMatrix4CellPar_Mod.f90:86-102; GaussSeidel_SpDiag,
  * CG/MatSpDiag_Mod.f90:191-235). */
 int asam_psolve(asam_ctx *ctx, const double *x, double *px);
+/* No reference counterpart: the refined mode's FP32 inner preconditioner
+ * (x rounded to FP32, 1+inner_gs_iter Gauss-Seidel sweeps in the configured
+ * schedule or the column line solve, halo handling as PSolve, result widened
+ * to FP64), for tests and measurement.  Refined precision only. */
+int asam_inner_psolve(asam_ctx *ctx, const double *x, double *px);
 
 /* BiCGStabMetSp: BiCGStabMet_Vec4CellSp (MODULE/SpMatrix4CellPar_Mod.f90:245-348).
  * x in/out (initial guess), b right-hand side.  maxiter/tol in/out with the
@@ -188,6 +200,35 @@ int asam_tri_solve_noalloc(int ncol, int n1, const double *d, const double *u, c
                            void *stream);
 /* y = T x for the same column batch, MatVecT_1D (MULTI/TriDiagT_Mod.f90:113-133). */
 int asam_tri_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x, double *y);
+
+/* Batched ensemble (no single reference routine: ASAM advances the blocks of
+ * one process in turn, DO ibLoc=1,nbLoc, inside Ros3MetC; here the blocks are
+ * independent domains).  A batch groups existing contexts, each with its own
+ * geometry, wind, configuration and CUDA stream; asam_batch_ros_step advances
+ * every member by nsteps Rosenbrock steps of its own dt, members running
+ * concurrently on the GPU, driven by up to nthreads host threads (0: one per
+ * member, at most 64), largest members first.  states[m] is member m's state
+ * (device or host pointer, as asam_ros_step).  iters/resid (optional, NULL
+ * allowed): nmember*nsteps*4 entries, as asam_ros_step per step; status
+ * (optional): nmember entries.  Returns the first failure's status if any
+ * member failed (asam_last_error names it), else NOT_CONVERGED/BREAKDOWN if
+ * any member reported it, else OK.  A context may belong to several batches
+ * but must not be used elsewhere while a batch call runs. */
+/* No reference counterpart: picks the refined mode's inner-solver settings
+ * (inner_precond, inner_gs_iter, gs_schedule, gs_group) for this block by
+ * timing complete refined solves of its first Rosenbrock stage at state c
+ * (host or device) and step dt, one setting at a time; keeps the fastest in
+ * the context and returns it in choice[4] (that order) with its solve time in
+ * *best_ms (may be NULL).  The settings change speed only: every candidate
+ * solves to the configured tolerance.  FP64 contexts have nothing to choose
+ * and return their configuration. */
+int asam_autotune(asam_ctx *ctx, const double *c, double dt, int *choice, double *best_ms);
+
+typedef struct asam_batch asam_batch;
+int asam_batch_create(int nmember, asam_ctx *const *members, int nthreads, asam_batch **out);
+int asam_batch_destroy(asam_batch *batch);
+int asam_batch_ros_step(asam_batch *batch, double *const *states, const double *dt, int nsteps, int *iters,
+                        double *resid, int *status);
 
 /* Rosenbrock coefficients of InitRos3MetC (ADVECT/Int_Mod.f90:78-261):
  * alpha/beta 4x4 row-major, gamma1[5].  Returns nStage (0 = unknown method). */

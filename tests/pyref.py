@@ -206,3 +206,23 @@ def gauss_seidel(val, grid, b, iterg=5):
     for _ in range(iterg):
         x = spl.spsolve_triangular(L, b - U @ x, lower=True)
     return x
+
+
+def line_solve(val, grid, b, axis):
+    """x = T^-1 b with T the tridiagonal part of the stage matrix along one axis
+    (0: x, 1: y, 2: z): the diagonal and the couplings to the two neighbours on
+    that axis inside the padded box, every line solved on its own."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+
+    NX, NY, NZ = grid.nx + 2, grid.ny + 2, grid.nz + 2
+    A = dia_scipy(val, grid).tocoo()
+    st = [1, NX, NX * NY][axis]
+    length = [NX, NY, NZ][axis]
+    d = A.col - A.row
+    pos = lambda r: (r // st) % length  # noqa: E731  index of a cell along the axis
+    keep = (d == 0) | (((d == st) | (d == -st)) & (np.abs(pos(A.col) - pos(A.row)) == 1))
+    T = sp.csc_matrix((A.data[keep], (A.row[keep], A.col[keep])), shape=A.shape)
+    lu = spl.splu(T)
+    bb = np.asarray(b, dtype=np.float64).reshape(-1, grid.npad)
+    return np.stack([lu.solve(r) for r in bb]).reshape(np.shape(b))

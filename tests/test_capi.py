@@ -54,5 +54,5 @@ def test_npad(built_lib):
     from asam_gb300 import _lib
 
     lib = _lib.load()
-    cfg = _lib.AsamConfig(10, 20, 30, 1, 1, 0, 3, 0, 5, 30, 1e-6, 5, 0, 1, 1)
+    cfg = _lib.AsamConfig(10, 20, 30, 1, 1, 0, 3, 0, 5, 30, 1e-6, 5, 0, 1, 1, 0, 0)
     assert lib.asam_npad(cfg) == 12 * 22 * 32

@@ -1,0 +1,82 @@
+"""Batched ensemble (asam_batch_*): members of different sizes, orography and
+wind advanced together give exactly what each member gives alone."""
+import numpy as np
+import pytest
+
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+MEMBERS = ["hill_24x20x16", "hill_odd_13x7x9_reverse", "flat_walls_9x6x5", "column_1x1x12", "slab_1x9x6",
+           "bubble_12x10x8"]
+
+
+@pytest.fixture(scope="module")
+def asam(built_lib):
+    import asam_gb300
+
+    return asam_gb300
+
+
+def _blocks(asam, **kw):
+    out = []
+    for name in MEMBERS:
+        geo, vel, st = cases.get(name)
+        b = asam.TransportBlock(geo, ncomp=st.c.shape[0], rho_pos=st.rho_pos, method="RosRK3", **kw)
+        b.set_velocity(*vel)
+        out.append((b, st))
+    return out
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
+@pytest.mark.parametrize("nthreads", [1, 0])
+def test_batch_matches_members_alone(asam, precision, nthreads):
+    kw = dict(bicgstab_tol=1e-10, precision=precision)
+    dts = [2.0, 3.0, 1.5, 2.5, 2.0, 4.0]
+    alone = []
+    for (b, st), dt in zip(_blocks(asam, **kw), dts):
+        c = st.c.copy()
+        its = [b.Ros3MetC(c, dt)[0] for _ in range(3)]
+        alone.append((c, its))
+        b.close()
+    members = _blocks(asam, **kw)
+    states = [st.c.copy() for _, st in members]
+    with asam.Batch([b for b, _ in members], nthreads=nthreads) as batch:
+        its, status = batch.ros_step(states, dts, nsteps=3)
+    for b, _ in members:
+        b.close()
+    # statuses carry the members' own BiCGStab outcomes (the one-column member
+    # reaches the iteration limit alone too); the iteration sentinels must match
+    assert all(int(x) in (0, 1) for x in status), status
+    for m, (c_ref, its_ref) in enumerate(alone):
+        assert np.array_equal(states[m], c_ref), MEMBERS[m]
+        assert [list(map(int, s)) for s in its[m]] == its_ref, MEMBERS[m]
+
+
+def test_batch_device_states(asam):
+    import torch
+
+    members = _blocks(asam, bicgstab_tol=1e-10)
+    host = [st.c.copy() for _, st in members]
+    dev = [torch.from_numpy(st.c.reshape(-1).copy()).cuda() for _, st in members]
+    torch.cuda.synchronize()  # the members' streams do not wait for torch's
+    with asam.Batch([b for b, _ in members]) as batch:
+        batch.ros_step(host, 2.0, nsteps=2)
+        batch.ros_step([t.data_ptr() for t in dev], 2.0, nsteps=2)
+    torch.cuda.synchronize()
+    for h, d in zip(host, dev):
+        assert np.array_equal(h.reshape(-1), d.cpu().numpy())
+    for b, _ in members:
+        b.close()
+
+
+def test_batch_rejects_bad_arguments(asam):
+    members = _blocks(asam)
+    b0 = members[0][0]
+    with pytest.raises(Exception):
+        asam.Batch([b0, b0])  # one context twice
+    with asam.Batch([b for b, _ in members]) as batch:
+        with pytest.raises(ValueError):
+            batch.ros_step([members[0][1].c.copy()], 2.0)
+    for b, _ in members:
+        b.close()

@@ -172,7 +172,84 @@ def test_ros_coeffs_match_oracle(env):
         assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3]) and np.array_equal(a[4], b[4])
 
 
-@pytest.mark.parametrize("inner", ["line", "gauss_seidel"])
+@pytest.mark.parametrize("iterg", [0, 1, 3])
+@pytest.mark.parametrize("name", ALL)
+def test_inner_psolve_fp32(env, name, iterg):
+    """FP32 inner Gauss-Seidel: the persistent and the level-by-level schedule
+    give the same bits (same arithmetic, only the order of the tiles differs),
+    repeated calls reproduce them, and the result is the FP64 oracle's to FP32
+    accuracy."""
+    o, c, val, b = _system(env, name)
+    ref = o.psolve(val, b, iterg=iterg)
+    got = {}
+    for sched in ("persistent", "levels"):
+        with _block(env, name, precision="fp32_refined", inner_gs_iter=iterg, gs_schedule=sched) as blk:
+            blk.set_jac_matrix(val)
+            got[sched] = blk.inner_psolve(b)
+            for _ in range(2):
+                assert np.array_equal(blk.inner_psolve(b), got[sched])
+    assert np.array_equal(got["persistent"], got["levels"])
+    errs = cases.field_relerr(got["persistent"], ref)
+    assert max(errs) <= 2e-5, errs
+
+
+@pytest.mark.parametrize("precond,axis", [("line", 2), ("xline", 0), ("yline", 1)])
+@pytest.mark.parametrize("name", ALL)
+def test_inner_line_psolve_fp32(env, name, precond, axis):
+    """FP32 line preconditioners against scipy's solve of the tridiagonal part of
+    the stage matrix along the axis, with PSolve's halo handling."""
+    import tests.pyref as pyref
+
+    o, c, val, b = _system(env, name)
+    geo = cases.get(name)[0]
+    g = geo.grid
+    bx = o.exchange_cell(b)
+    x = pyref.line_solve(val, g, bx, axis).reshape(b.shape)
+    x[:, [0, -1], :, :] = 0
+    x[:, :, [0, -1], :] = 0
+    x[:, :, :, [0, -1]] = 0
+    ref = o.exchange_cell(x)
+    with _block(env, name, precision="fp32_refined", inner_precond=precond) as blk:
+        blk.set_jac_matrix(val)
+        got = blk.inner_psolve(b)
+    errs = cases.field_relerr(got, ref)
+    assert max(errs) <= 2e-5, errs
+
+
+@pytest.mark.parametrize("name", ["hill_24x20x16", "hill_odd_13x7x9_reverse"])
+def test_refined_step_schedules_identical(env, name):
+    geo, vel, st = cases.get(name)
+    out = {}
+    for sched in ("persistent", "levels"):
+        c = st.c.copy()
+        with _block(env, name, method="RosRK3", bicgstab_tol=1e-12, precision="fp32_refined",
+                    gs_schedule=sched) as blk:
+            its = [blk.Ros3MetC(c, 4.0)[0] for _ in range(2)]
+        out[sched] = (c, its)
+    assert np.array_equal(out["persistent"][0], out["levels"][0])
+    assert out["persistent"][1] == out["levels"][1]
+
+
+@pytest.mark.parametrize("name", ["hill_24x20x16", "bubble_12x10x8"])
+def test_autotuned_refined_step(env, name):
+    """The autotuner only picks among settings that solve to the tolerance: the
+    tuned refined step still matches the FP64 oracle."""
+    asam, oracle = env
+    geo, vel, st = cases.get(name)
+    o = oracle.Oracle(geo)
+    cr, cg = st.c.copy(), st.c.copy()
+    with _block(env, name, method="RosRK3", bicgstab_tol=1e-12, precision="fp32_refined") as blk:
+        choice = blk.autotune(st.c, 4.0)
+        assert choice["inner_precond"] in asam.INNER_PRECONDS and 0 <= choice["inner_gs_iter"] <= 3
+        assert 1 <= choice["gs_group"] <= st.c.shape[0] and choice["stage_solve_ms"] > 0
+        for _ in range(2):
+            o.ros_step(cr, vel, 4.0, method=asam.METHODS["RosRK3"], tol=1e-12)
+            blk.Ros3MetC(cg, 4.0)
+    errs = cases.field_relerr(cg, cr)
+    assert max(errs) <= REFINED_TOL, (choice, errs)
+
+
+@pytest.mark.parametrize("inner", ["line", "xline", "yline", "gauss_seidel"])
 @pytest.mark.parametrize("name", ["hill_24x20x16", "hill_odd_13x7x9_reverse", "flat_walls_9x6x5"])
 def test_ros_step_refined(env, name, inner):
     asam, oracle = env
