@@ -110,6 +110,11 @@ class TransportBlock:
             raise ValueError(f"state must have {self.ncomp}*npad elements")
         return a
 
+    def set_graphs(self, on: bool):
+        """Capture the BiCGStab half-iterations as CUDA graphs (default) or launch
+        every kernel individually; the results are the same."""
+        check(self.lib.asam_set_graphs(self.h, int(bool(on))), "asam_set_graphs")
+
     def set_stream(self, stream_handle: int | None):
         """cudaStream_t as an integer; 0/None selects the legacy default stream."""
         check(self.lib.asam_set_stream(self.h, stream_handle or None), "asam_set_stream")

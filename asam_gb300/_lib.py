@@ -44,6 +44,7 @@ SIGNATURES = [
     ("asam_create", C.c_int, [C.POINTER(AsamConfig), _V, _V, _V, _V, C.POINTER(C.c_void_p)]),
     ("asam_destroy", C.c_int, [_V]),
     ("asam_set_stream", C.c_int, [_V, _V]),
+    ("asam_set_graphs", C.c_int, [_V, C.c_int]),
     ("asam_state_device_ptr", C.c_int, [_V, C.POINTER(C.c_void_p)]),
     ("asam_synchronize", C.c_int, [_V]),
     ("asam_set_velocity", C.c_int, [_V, _V, _V, _V]),

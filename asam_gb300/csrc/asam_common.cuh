@@ -49,6 +49,21 @@ struct Dims {
   __host__ __device__ size_t WF(int i, int j, int k) const {
     return (size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)k);
   }
+  // (i, j, k) of padded cell P; 32-bit division whenever the box allows it
+  __host__ __device__ void ijk(size_t P, int& i, int& j, int& k) const {
+    const unsigned NXu = (unsigned)(nx + 2), NYu = (unsigned)(ny + 2);
+    if (P < (size_t)0xffffffffu) {
+      const unsigned p = (unsigned)P, r = p / NXu;
+      i = (int)(p - r * NXu);
+      k = (int)(r / NYu);
+      j = (int)(r - (unsigned)k * NYu);
+    } else {
+      const size_t r = P / NXu;
+      i = (int)(P - r * NXu);
+      k = (int)(r / NYu);
+      j = (int)(r - (size_t)k * NYu);
+    }
+  }
   size_t n_fu() const { return (size_t)(nx + 3) * ny * nz; }
   size_t n_fv() const { return (size_t)nx * (ny + 3) * nz; }
   size_t n_fw() const { return (size_t)nx * ny * (nz + 3); }
@@ -81,16 +96,18 @@ struct KrylovScalars {
 
 // Schedule of the persistent Gauss-Seidel wavefront (k_gs_persist): tickets
 // (I, J, K, sweep) in pipelined-level order, per-tile completion counters
-// (base + last completed sweep + 1; base grows by the sweep count every
-// launch, so counters never need clearing), the ticket counter (zeroed before
-// each launch) and the error flag.
+// (base + last completed sweep + 1, compared in wrap-around arithmetic), the
+// epoch base in device memory (advanced by the sweep count after every call
+// by a kernel of the same stream, so a captured call replays correctly and
+// the counters never need clearing), the ticket counter (zeroed before each
+// call) and the error flag.
 struct GsTileSched {
   const int4* order;
   int nticket;
   int* flags;
   int* counter;
   int* err;
-  int base;
+  unsigned* base;
   int group;  // components per CTA
 };
 

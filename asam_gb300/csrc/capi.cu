@@ -14,7 +14,12 @@
 
 namespace asam {
 static std::atomic<long long> g_launches{0};
-void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+static thread_local long long t_launches = 0;  // this thread's share (capture bookkeeping)
+void count_launches(long long n) {
+  g_launches.fetch_add(n, std::memory_order_relaxed);
+  t_launches += n;
+}
+long long thread_launches() { return t_launches; }
 static thread_local std::string g_last_error;
 void set_last_error(const char* msg, const char* file, int line) {
   char buf[512];
@@ -254,14 +259,15 @@ int gs_schedule_init(asam_ctx* h, int nsweep) {
   h->gs_nflags = (size_t)gs_tile_count(d) * ngroups;
   CK(cudaMalloc((void**)&h->gs_order, order.size() * sizeof(int4)));
   CK(cudaMalloc((void**)&h->gs_flags, h->gs_nflags * sizeof(int)));
-  CK(cudaMalloc((void**)&h->gs_counter, sizeof(int)));
+  CK(cudaMalloc((void**)&h->gs_counter, 2 * sizeof(int)));
   CK(cudaMemcpy(h->gs_order, order.data(), order.size() * sizeof(int4), cudaMemcpyHostToDevice));
   CK(cudaMemset(h->gs_flags, 0, h->gs_nflags * sizeof(int)));
-  h->gs_base = 0;
+  CK(cudaMemset(h->gs_counter, 0, 2 * sizeof(int)));
   return kOk;
 }
 
 void gs_schedule_free(asam_ctx* h) {
+  graphs_reset(h);
   if (h->gs_order) cudaFree(h->gs_order);
   if (h->gs_flags) cudaFree(h->gs_flags);
   if (h->gs_counter) cudaFree(h->gs_counter);
@@ -285,21 +291,77 @@ void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w) {
   const int nsweep = 1 + (inner ? h->cfg.inner_gs_iter : h->cfg.gs_iter);
   if (inner && h->cfg.inner_precond != 0) {  // 1: z lines, 2: x lines, 3: y lines
     const int axis = h->cfg.inner_precond == 1 ? 2 : h->cfg.inner_precond == 2 ? 0 : 1;
-    launch_line_psolve(L, d, nc, val, w.bbuf, out, w.tbuf, axis);
+    launch_line_psolve(L, d, nc, val, w.bbuf, out, w.tbuf, axis, (const T*)h->xl_w, (const T*)h->xl_r);
   } else if (inner && h->gs_order) {
-    const GsTileSched sch{h->gs_order,   h->gs_nticket,  h->gs_flags,          h->gs_counter,
-                          &h->sc->gs_err, h->gs_base,     gs_group_of(h->cfg)};
+    const GsTileSched sch{h->gs_order,     h->gs_nticket, h->gs_flags,         h->gs_counter,
+                          &h->sc->gs_err, reinterpret_cast<unsigned*>(h->gs_counter + 1), gs_group_of(h->cfg)};
     launch_gs_persist(L, d, nc, val, w.bbuf, out, w.tbuf, nsweep, sch);
-    h->gs_base += nsweep;
-    if (h->gs_base > (1 << 30)) {  // counters are compared against base + sweep: restart from zero
-      cudaMemsetAsync(h->gs_flags, 0, h->gs_nflags * sizeof(int), L.stream);
-      h->gs_base = 0;
-    }
   } else {
     launch_gs_sweeps(L, d, nc, val, w.bbuf, out, w.tbuf, nsweep, gs_group_of(h->cfg));
   }
   launch_zero_halo(L, d, nc, out);
   launch_exchange_cell(L, d, nc, out);
+}
+
+// CUDA graphs of the two half-iterations of BiCGStab, per context and
+// precision: [0] first half of iteration 1, [1] first half of later
+// iterations, [2] second half.  A half runs eagerly the first time (so that
+// every one-time setting of its kernels is done outside a capture), is
+// captured the second time, and is replayed from then on.  The bodies touch
+// only the context's own buffers; the caller's x is updated outside them.
+void graphs_reset(asam_ctx* h) {
+  for (auto& kg : h->kg) {
+    for (int q = 0; q < 3; ++q) {
+      if (kg.exec[q]) cudaGraphExecDestroy(kg.exec[q]);
+      kg.exec[q] = nullptr;
+      kg.warm[q] = false;
+      kg.n[q] = 0;
+    }
+  }
+}
+
+template <typename Body>
+static int run_half(asam_ctx* h, int prec, int q, Body&& body) {
+  KrylovGraphs& kg = h->kg[prec];
+  const Launch& L = h->L;
+  if (!h->use_graphs || L.stream == nullptr) {  // the legacy default stream cannot be captured
+    body();
+    return check_launch();
+  }
+  if (!kg.exec[q]) {
+    if (!kg.warm[q]) {
+      kg.warm[q] = true;
+      body();
+      return check_launch();
+    }
+    const long long t0 = thread_launches();
+    CK(cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal));
+    body();
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(L.stream, &g);
+    const long long nl = thread_launches() - t0;
+    count_launches(-nl);  // captured, not run
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&kg.exec[q], g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      kg.exec[q] = nullptr;
+      set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+      return kCudaError;
+    }
+    kg.n[q] = nl;
+  }
+  CK(cudaGraphLaunch(kg.exec[q], L.stream));
+  count_launches(kg.n[q]);
+  return kOk;
+}
+
+// x-line factors of the current stage matrix for the FP32 inner line solve
+// (outside any captured half-iteration: they change with the matrix only)
+static void prepare_inner(asam_ctx* h) {
+  if (h->cfg.inner_precond == 2 && !h->xline_ready) {
+    launch_xline_factor(h->L, h->d, h->val32, h->xl_w, h->xl_r);
+    h->xline_ready = true;
+  }
 }
 
 // BiCGStabMet_Vec4CellSp (MODULE/SpMatrix4CellPar_Mod.f90:245-348) on the device.
@@ -321,11 +383,12 @@ int bicgstab_dev(asam_ctx* h, const T* val, T* x, const T* b, int* maxiter, doub
   }
   CK(cudaMemcpyAsync(w.rt, w.r, len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream));
   launch_dot(L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM0, nullptr);
-  const int MaxIter = *maxiter;
-  for (int it = 1; it <= MaxIter; ++it) {
+  if (sizeof(T) == sizeof(float)) prepare_inner(h);
+  const int prec = sizeof(T) == sizeof(float) ? 1 : 0;
+  auto half1 = [&](bool first) {
     launch_dot(L, d, nc, w.rt, w.r, h->partial, h->sc, OP_RHO, nullptr);
-    if (it == 1) {
-      CK(cudaMemcpyAsync(w.p, w.r, len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream));
+    if (first) {
+      cudaMemcpyAsync(w.p, w.r, len * sizeof(T), cudaMemcpyDeviceToDevice, L.stream);
     } else {
       launch_beta(L, h->sc);
       launch_pupdate(L, len, h->sc, w.r, w.v, w.p);
@@ -335,7 +398,20 @@ int bicgstab_dev(asam_ctx* h, const T* val, T* x, const T* b, int* maxiter, doub
     launch_dot(L, d, nc, w.rt, w.v, h->partial, h->sc, OP_ALPHA, nullptr);
     launch_axpy_sc(L, len, h->sc, SEL_ALPHA, -1.0, w.v, w.r);
     launch_dot(L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM_HALF, nullptr);
-    int rc = check_launch();
+  };
+  // second half without the update of x (launched after it: x is the
+  // caller's array, and nothing in the half reads alpha/omega after it)
+  auto half2 = [&]() {
+    psolve_dev<T>(h, val, w.r, w.rh, w);
+    launch_matvec(L, d, nc, val, w.rh, w.t, 0);
+    launch_dot(L, d, nc, w.t, w.r, h->partial, h->sc, OP_STORE_A, nullptr);
+    launch_dot(L, d, nc, w.t, w.t, h->partial, h->sc, OP_OMEGA, nullptr);
+    launch_axpy_sc(L, len, h->sc, SEL_OMEGA, -1.0, w.t, w.r);
+    launch_dot(L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM_FULL, nullptr);
+  };
+  const int MaxIter = *maxiter;
+  for (int it = 1; it <= MaxIter; ++it) {
+    int rc = run_half(h, prec, it == 1 ? 0 : 1, [&] { half1(it == 1); });
     if (rc) return rc;
     rc = read_scalars(h);
     if (rc) return rc;
@@ -350,13 +426,8 @@ int bicgstab_dev(asam_ctx* h, const T* val, T* x, const T* b, int* maxiter, doub
       *tol = h->sc_host->rnorm;
       return check_launch();
     }
-    psolve_dev<T>(h, val, w.r, w.rh, w);
-    launch_matvec(L, d, nc, val, w.rh, w.t, 0);
-    launch_dot(L, d, nc, w.t, w.r, h->partial, h->sc, OP_STORE_A, nullptr);
-    launch_dot(L, d, nc, w.t, w.t, h->partial, h->sc, OP_OMEGA, nullptr);
+    if ((rc = run_half(h, prec, 2, half2))) return rc;
     launch_xupdate(L, len, h->sc, 1, w.ph, w.rh, x);
-    launch_axpy_sc(L, len, h->sc, SEL_OMEGA, -1.0, w.t, w.r);
-    launch_dot(L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM_FULL, nullptr);
     rc = check_launch();
     if (rc) return rc;
     rc = read_scalars(h);
@@ -415,11 +486,8 @@ int bicgstab_refined(asam_ctx* h, double* x, const double* b, int* maxiter, doub
     rc = bicgstab_dev<float>(h, h->val32, h->x32, h->b32, &it, &tin, h->w32, true);
     if (rc != kOk && rc != kNotConverged) return rc;
     total_inner += it < 0 ? -it : (it > h->cfg.bicgstab_maxiter ? it / 2 : it);
-    launch_convert_f32_to_f64(L, len, h->x32, h->dcorr);
-    launch_axpy_host(L, len, 1.0, h->dcorr, x);
-    launch_matvec(L, d, nc, h->val, x, r, 0);
-    launch_xpay_host(L, len, b, -1.0, r);
-    launch_dot(L, d, nc, r, r, h->partial, h->sc, OP_STORE_A, h->red_out);
+    launch_add_f32_to_f64(L, len, h->x32, x);                                    // x += correction
+    launch_resid_dot(L, d, nc, h->val, x, b, r, h->partial, h->sc, OP_STORE_A, h->red_out);  // r, r.r
     double rr = 0;
     rc = reduce_to_host(h, &rr);
     if (rc) return rc;
@@ -449,6 +517,7 @@ int jac_dev(asam_ctx* h, const double* c, double dt) {
   launch_jac(h->L, h->d, h->geom(), rho, h->beta0 * dt, h->val);
   if (h->cfg.precision == ASAM_PREC_FP32_REFINED) launch_convert_f64_to_f32(h->L, 8 * h->npad, h->val, h->val32);
   h->jac_ready = true;
+  h->xline_ready = false;
   return check_launch();
 }
 
@@ -653,7 +722,7 @@ int asam_destroy(asam_ctx* h) {
   if (!h) return kOk;
   double* dptrs[] = {h->volc, h->fu,     h->fv,     h->fw,     h->uf,     h->vf,      h->wf,      h->c,
                      h->cold, h->rhs,    h->incr,   h->phi,    h->gx,     h->gy,      h->gz,      h->val,
-                     h->dcorr, h->partial, h->red_out, h->stage_a, h->stage_b, h->coef_x, h->coef_y, h->coef_z,
+                     h->partial, h->red_out, h->stage_a, h->stage_b, h->coef_x, h->coef_y, h->coef_z,
                      h->rvol};
   unsigned char* bptrs[] = {h->mask_x, h->mask_y, h->mask_z};
   for (unsigned char* p : bptrs)
@@ -661,6 +730,8 @@ int asam_destroy(asam_ctx* h) {
   for (double* p : dptrs)
     if (p) cudaFree(p);
   if (h->val32) cudaFree(h->val32);
+  if (h->xl_w) cudaFree(h->xl_w);
+  if (h->xl_r) cudaFree(h->xl_r);
   if (h->x32) cudaFree(h->x32);
   if (h->b32) cudaFree(h->b32);
   if (h->sc) cudaFree(h->sc);
@@ -668,7 +739,7 @@ int asam_destroy(asam_ctx* h) {
   if (h->red_host) cudaFreeHost(h->red_host);
   free_work(h->w64);
   free_work(h->w32);
-  gs_schedule_free(h);
+  gs_schedule_free(h);  // and the graphs
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return kOk;
@@ -736,7 +807,8 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
     if ((e = cudaMalloc((void**)&h->val32, 8 * h->npad * sizeof(float))) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&h->x32, h->len * sizeof(float))) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&h->b32, h->len * sizeof(float))) != cudaSuccess) return fail(e);
-    if ((e = cudaMalloc((void**)&h->dcorr, h->len * sizeof(double))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&h->xl_w, h->npad * sizeof(float))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&h->xl_r, h->npad * sizeof(float))) != cudaSuccess) return fail(e);
     if (cfg->inner_precond == 0 && cfg->gs_schedule == 0 && gs_schedule_init(h, 1 + cfg->inner_gs_iter) != kOk) {
       asam_destroy(h);
       return (int)kCudaError;
@@ -759,6 +831,13 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
   if ((e = cudaStreamSynchronize(h->L.stream)) != cudaSuccess) return fail(e);
   if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
   *out = h;
+  return kOk;
+}
+
+int asam_set_graphs(asam_ctx* h, int on) {
+  if (!h) return kBadArg;
+  graphs_reset(h);
+  h->use_graphs = on != 0;
   return kOk;
 }
 
@@ -852,6 +931,7 @@ int asam_set_jac(asam_ctx* h, const double* val) {
   if (h->cfg.precision == ASAM_PREC_FP32_REFINED) launch_convert_f64_to_f32(h->L, 8 * h->npad, h->val, h->val32);
   CK(cudaStreamSynchronize(h->L.stream));
   h->jac_ready = true;
+  h->xline_ready = false;
   return check_launch();
 }
 
@@ -897,6 +977,7 @@ int asam_inner_psolve(asam_ctx* h, const double* x, double* px) {
   rc = stage_out_begin(h, px, h->len, h->stage_b, &dp, false);
   if (rc) return rc;
   CK(cudaMemsetAsync(&h->sc->gs_err, 0, sizeof(int), L.stream));
+  prepare_inner(h);
   launch_convert_f64_to_f32(L, h->len, dx, h->b32);
   psolve_dev<float>(h, h->val32, h->b32, h->x32, h->w32);
   launch_convert_f32_to_f64(L, h->len, h->x32, dp);

@@ -32,6 +32,13 @@ inline void free_work(Work<T>& w) {
 
 }  // namespace asam
 
+// CUDA graphs of the BiCGStab half-iterations of one precision
+struct KrylovGraphs {
+  cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
+  bool warm[3] = {false, false, false};
+  long long n[3] = {0, 0, 0};  // kernel launches per replay
+};
+
 struct asam_ctx {
   using Launch = asam::Launch;
   using Dims = asam::Dims;
@@ -59,7 +66,6 @@ struct asam_ctx {
   Work<double> w64;
   Work<float> w32;
   float *x32 = nullptr, *b32 = nullptr;
-  double* dcorr = nullptr;
   KrylovScalars* sc = nullptr;
   KrylovScalars* sc_host = nullptr;
   double* partial = nullptr;
@@ -67,13 +73,18 @@ struct asam_ctx {
   double* red_host = nullptr;
   double *stage_a = nullptr, *stage_b = nullptr;
   bool jac_ready = false;
+  KrylovGraphs kg[2];     // [0] FP64, [1] FP32 inner solver
+  bool use_graphs = true;  // capture the half-iterations (when the stream allows it)
+  // x-line factors of the FP32 inner line solve (w and 1/den per cell), valid
+  // for the current stage matrix while xline_ready is set
+  float *xl_w = nullptr, *xl_r = nullptr;
+  bool xline_ready = false;
   // persistent Gauss-Seidel schedule of the FP32 inner sweeps
   int4* gs_order = nullptr;
   int gs_nticket = 0;
   int* gs_flags = nullptr;  // one completion counter per tile and component group
   size_t gs_nflags = 0;
-  int* gs_counter = nullptr;
-  int gs_base = 0;
+  int* gs_counter = nullptr;  // [0] ticket counter; [1] epoch base (unsigned)
 
   GeomT<double> geom() const { return GeomT<double>{volc, fu, fv, fw, uf, vf, wf}; }
 };
@@ -100,6 +111,8 @@ int stage_out_begin(asam_ctx* h, double* p, size_t n, double* buf, double** dev,
 int stage_out_end(asam_ctx* h, double* p, size_t n, double* dev);
 int gs_schedule_init(asam_ctx* h, int nsweep);
 void gs_schedule_free(asam_ctx* h);
+void graphs_reset(asam_ctx* h);
+long long thread_launches();
 
 }  // namespace asam
 

@@ -13,6 +13,11 @@ __global__ void k_cvt_f2d(size_t len, const float* __restrict__ x, double* __res
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
     y[q] = (double)x[q];
 }
+// y += x widened to FP64 (the refinement's correction, one pass)
+__global__ void k_add_f2d(size_t len, const float* __restrict__ x, double* __restrict__ y) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
+    y[q] = y[q] + (double)x[q];
+}
 // slot 7 of the DIA storage: 1/diagonal (IEEE division)
 __global__ void k_recip_diag(size_t n, double* __restrict__ val) {
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
@@ -37,6 +42,16 @@ void launch_recip_diag(const Launch& L, size_t npad, double* val) {
 void launch_convert_f64_to_f32(const Launch& L, size_t len, const double* x, float* y) {
   k_cvt_d2f<<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, x, y);
   count_launches(1);
+}
+void launch_add_f32_to_f64(const Launch& L, size_t len, const float* x, double* y) {
+  k_add_f2d<<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, x, y);
+  count_launches(1);
+}
+void launch_resid_dot(const Launch& L, const Dims& d, int ncomp, const double* val, const double* x, const double* b,
+                      double* r, double* partial, KrylovScalars* sc, int op, double* out) {
+  k_resid_dot<double><<<RED_GRID, RED_BLOCK, 0, L.stream>>>(d, ncomp, val, x, b, r, partial);
+  k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, RED_GRID, sc, op, out);
+  count_launches(2);
 }
 void launch_convert_f32_to_f64(const Launch& L, size_t len, const float* x, double* y) {
   k_cvt_f2d<<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, x, y);

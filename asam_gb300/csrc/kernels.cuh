@@ -485,9 +485,8 @@ __global__ void k_matvec(Dims d, int ncomp, const TM* __restrict__ val, const T*
   const size_t n = d.npad();
   const size_t sy = (size_t)NX, sz = (size_t)NX * NY;
   for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(P % NX);
-    const int j = (int)((P / NX) % NY);
-    const int k = (int)(P / sz);
+    int i, j, k;
+    d.ijk(P, i, j, k);
     const T v0 = k > 0 ? (T)val[0 * n + P - sz] : (T)0;
     const T v1 = j > 0 ? (T)val[1 * n + P - sy] : (T)0;
     const T v2 = i > 0 ? (T)val[2 * n + P - 1] : (T)0;
@@ -909,9 +908,10 @@ __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
-__device__ bool gs_wait_flag(const int* f, int target, const int* err) {
+// counter reached target, in wrap-around (serial number) arithmetic
+__device__ bool gs_wait_flag(const int* f, unsigned target, const int* err) {
   for (int it = 0; it < kGsSpinLimit; ++it) {
-    if (ld_acquire(f) >= target) return true;
+    if ((int)((unsigned)ld_acquire(f) - target) >= 0) return true;
     if (*(volatile const int*)err) return false;
     __nanosleep(32);
   }
@@ -927,6 +927,7 @@ __global__ void __launch_bounds__(256) k_gs_persist(Dims d, int ncomp, const TM*
   __shared__ int s_ticket, s_ok;
   const int group = sch.group;
   const int ngroups = gs_ngroups(ncomp, group);
+  const unsigned base = *sch.base;  // advanced by k_gs_advance after this launch
   for (;;) {
     if (threadIdx.x == 0) s_ticket = *(volatile const int*)sch.err ? sch.nticket : atomicAdd(sch.counter, 1);
     __syncthreads();
@@ -940,7 +941,7 @@ __global__ void __launch_bounds__(256) k_gs_persist(Dims d, int ncomp, const TM*
     tile.issue_fixed();
     if (threadIdx.x == 0) {
       const int* f = sch.flags;
-      const int now = sch.base + s + 1, prev = sch.base + s;  // sweep s done, sweep s-1 done
+      const unsigned now = base + s + 1, prev = base + s;  // sweep s done, sweep s-1 done
       const int id = ((K * nty + J) * ntx + I) * ngroups + g;
       const int sx = ngroups, sy_ = ntx * ngroups, sz_ = ntx * nty * ngroups;
       bool ok = true;
@@ -968,8 +969,13 @@ __global__ void __launch_bounds__(256) k_gs_persist(Dims d, int ncomp, const TM*
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0)
-      st_release(sch.flags + ((K * nty + J) * ntx + I) * ngroups + g, sch.base + s + 1);
+      st_release(sch.flags + ((K * nty + J) * ntx + I) * ngroups + g, (int)(base + s + 1));
   }
+}
+
+// next epoch of the persistent schedule's completion counters
+__global__ void k_gs_advance(unsigned* base, int nsweep) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *base += (unsigned)nsweep;
 }
 
 // Line preconditioners of the refined mode's inner solver: x = T^{-1} b with
@@ -1031,107 +1037,132 @@ __global__ void k_line_psolve(Dims d, int ncomp, int axis, const TM* __restrict_
 
 // x lines (the memory-contiguous axis): the padded rows of the box are
 // consecutive, so 32 consecutive rows form one contiguous 32 x NX block.  A
-// warp takes 32 rows of one component and walks them in chunks of 32 columns:
-// each chunk of every operand is loaded row by row (lanes along x, coalesced)
-// into a shared 32 x 33 tile, lane q then runs the Thomas recurrence of row q
-// through the chunk from the tile (conflict-free: row pitch 33), and results
-// leave through the tile the same way.  Forward elimination writes the factors
-// w (per component, in `w`) and the partial solution (in x); back
-// substitution walks the chunks in reverse.  One warp per (32 rows, component)
-// gives many independent warps; the factors are recomputed per component.
+// warp takes 32 rows and walks them in chunks of 32 columns: each chunk of
+// every operand is copied row by row (lanes along x, coalesced, cp.async, one
+// memory round trip per chunk) into a shared 32 x 33 tile, lane q then runs
+// the recurrence of row q through the chunk from the tile (conflict-free: row
+// pitch 33), and results leave through the tile the same way.
+// The elimination factors depend on the matrix only, so they are computed
+// once per stage matrix (k_xline_factor: w_i = c_i/den_i and 1/den_i with
+// den_i = d_i - a_i w_{i-1}); every application (k_xline_solve, one warp per
+// 32 rows and component) then runs g_i = (b_i - a_i g_{i-1})/den_i forward
+// and x_i = g_i - w_i x_{i+1} backward.
 template <typename T>
-__host__ __device__ constexpr int xl_warps() {  // warps per CTA: four 32 x 33 tiles per warp within 48 KB
-  return sizeof(T) == 4 ? 2 : 1;
+__host__ __device__ constexpr int xl_warps() {  // warps per CTA: three 32 x 33 tiles per warp within 48 KB
+  return sizeof(T) == 4 ? 3 : 1;
 }
+
+template <typename T>
+__device__ __forceinline__ void xl_load(T (*t)[33], const T* src, int r0, int nr, int NX, int ch, int lane,
+                                        int shift, bool lo_ok, bool hi_ok) {
+  const int i = ch * 32 + lane;
+  for (int q = 0; q < nr; ++q) {
+    const size_t P = (size_t)(r0 + q) * NX + i;
+    const bool in = i < NX && (lo_ok || i > 0) && (hi_ok || i < NX - 1);
+    cp_async_elem(&t[q][lane], in ? src + P + shift : src, in);
+  }
+}
+template <typename T>
+__device__ __forceinline__ void xl_store(T (*t)[33], T* dst, int r0, int nr, int NX, int ch, int lane) {
+  const int i = ch * 32 + lane;
+  if (i < NX)
+    for (int q = 0; q < nr; ++q) dst[(size_t)(r0 + q) * NX + i] = t[q][lane];
+}
+
 template <typename TM, typename T>
-__global__ void __launch_bounds__(32 * xl_warps<T>()) k_xline_psolve(Dims d, int ncomp, const TM* __restrict__ val,
-                                                                    const T* __restrict__ b, T* __restrict__ x,
-                                                                    T* __restrict__ w) {
-  constexpr int XL_WARPS = xl_warps<T>();
-  __shared__ T tile[XL_WARPS][4][32][33];  // a, c (then w), d, b (then g, then x)
+__global__ void __launch_bounds__(32 * xl_warps<T>()) k_xline_factor(Dims d, const TM* __restrict__ val,
+                                                                    T* __restrict__ fw, T* __restrict__ fr) {
+  constexpr int XW = xl_warps<T>();
+  __shared__ T tile[XW][3][32][33];  // a, c (then w), d (then 1/den)
   const int NX = d.NX();
   const size_t n = d.npad();
   const int nrows = d.NY() * d.NZ();
-  const int ngrp = (nrows + 31) / 32;
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
-  const long long task = (long long)blockIdx.x * XL_WARPS + wq;  // (row group, component)
-  if (task >= (long long)ngrp * ncomp) return;                   // whole warp
-  const int ic = (int)(task % ncomp), grp = (int)(task / ncomp);
-  const int r0 = grp * 32;
-  const int nr = min(32, nrows - r0);
+  const int grp = blockIdx.x * XW + wq;
+  if (grp * 32 >= nrows) return;  // whole warp
+  const int r0 = grp * 32, nr = min(32, nrows - r0);
   T(*ta)[33] = tile[wq][0];
   T(*tc)[33] = tile[wq][1];
   T(*td)[33] = tile[wq][2];
-  T(*tb)[33] = tile[wq][3];
-  const TM* v2 = val + 2 * n;
-  const TM* v3 = val + 3 * n;
-  const TM* v4 = val + 4 * n;
-  const T* bc = b + (size_t)ic * n;
-  T* xc = x + (size_t)ic * n;
-  T* wc = w + (size_t)ic * n;
   const int nch = (NX + 31) / 32;
-  // chunk loads: every row of the chunk at once by cp.async (one memory round
-  // trip per chunk; out-of-box elements are zero-filled)
-  auto load = [&](T(*t)[33], const auto* src, int ch, int shift, bool lo_ok, bool hi_ok) {
-    const int i = ch * 32 + lane;
-    for (int q = 0; q < nr; ++q) {
-      const size_t P = (size_t)(r0 + q) * NX + i;
-      const bool in = i < NX && (lo_ok || i > 0) && (hi_ok || i < NX - 1);
-      cp_async_elem(&t[q][lane], in ? src + P + shift : src, in);
-    }
-  };
-  T wprev = (T)0, gprev = (T)0;
+  T wprev = (T)0;
   for (int ch = 0; ch < nch; ++ch) {
-    load(ta, v2, ch, -1, false, true);
-    load(tc, v4, ch, +1, true, false);
-    load(td, v3, ch, 0, true, true);
-    load(tb, bc, ch, 0, true, true);
+    xl_load(ta, val + 2 * n, r0, nr, NX, ch, lane, -1, false, true);
+    xl_load(tc, val + 4 * n, r0, nr, NX, ch, lane, +1, true, false);
+    xl_load(td, val + 3 * n, r0, nr, NX, ch, lane, 0, true, true);
     cp_async_wait_all();
     __syncwarp();
     if (lane < nr) {
       const int m = min(32, NX - ch * 32);
       for (int k = 0; k < m; ++k) {
-        const T a = ta[lane][k];
-        const T rden = (T)1 / (td[lane][k] - a * wprev);
-        const T wk = tc[lane][k] * rden;
-        const T gk = (tb[lane][k] - a * gprev) * rden;
-        tc[lane][k] = wk;
-        tb[lane][k] = gk;
-        wprev = wk;
-        gprev = gk;
+        const T rden = (T)1 / (td[lane][k] - ta[lane][k] * wprev);
+        wprev = tc[lane][k] * rden;
+        tc[lane][k] = wprev;
+        td[lane][k] = rden;
       }
     }
     __syncwarp();
-    const int i = ch * 32 + lane;
-    for (int q = 0; q < nr; ++q) {
-      const size_t P = (size_t)(r0 + q) * NX + i;
-      if (i < NX) {
-        wc[P] = tc[q][lane];
-        xc[P] = tb[q][lane];
+    xl_store(tc, fw, r0, nr, NX, ch, lane);
+    xl_store(td, fr, r0, nr, NX, ch, lane);
+    __syncwarp();
+  }
+}
+
+template <typename TM, typename T>
+__global__ void __launch_bounds__(32 * xl_warps<T>()) k_xline_solve(Dims d, int ncomp, const TM* __restrict__ val,
+                                                                   const T* __restrict__ fw,
+                                                                   const T* __restrict__ fr, const T* __restrict__ b,
+                                                                   T* __restrict__ x) {
+  constexpr int XW = xl_warps<T>();
+  __shared__ T tile[XW][3][32][33];  // forward: a, 1/den, b (then g); backward: w, g (then x)
+  const int NX = d.NX();
+  const size_t n = d.npad();
+  const int nrows = d.NY() * d.NZ();
+  const int ngrp = (nrows + 31) / 32;
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  const long long task = (long long)blockIdx.x * XW + wq;  // (row group, component), component fastest
+  if (task >= (long long)ngrp * ncomp) return;             // whole warp
+  const int ic = (int)(task % ncomp), grp = (int)(task / ncomp);
+  const int r0 = grp * 32, nr = min(32, nrows - r0);
+  T(*t0)[33] = tile[wq][0];
+  T(*t1)[33] = tile[wq][1];
+  T(*t2)[33] = tile[wq][2];
+  const T* bc = b + (size_t)ic * n;
+  T* xc = x + (size_t)ic * n;
+  const int nch = (NX + 31) / 32;
+  T gprev = (T)0;
+  for (int ch = 0; ch < nch; ++ch) {
+    xl_load(t0, val + 2 * n, r0, nr, NX, ch, lane, -1, false, true);
+    xl_load(t1, fr, r0, nr, NX, ch, lane, 0, true, true);
+    xl_load(t2, bc, r0, nr, NX, ch, lane, 0, true, true);
+    cp_async_wait_all();
+    __syncwarp();
+    if (lane < nr) {
+      const int m = min(32, NX - ch * 32);
+      for (int k = 0; k < m; ++k) {
+        gprev = (t2[lane][k] - t0[lane][k] * gprev) * t1[lane][k];
+        t2[lane][k] = gprev;
       }
     }
+    __syncwarp();
+    xl_store(t2, xc, r0, nr, NX, ch, lane);
     __syncwarp();
   }
   T xnext = (T)0;
   for (int ch = nch - 1; ch >= 0; --ch) {
-    load(tc, static_cast<const T*>(wc), ch, 0, true, true);
-    load(tb, static_cast<const T*>(xc), ch, 0, true, true);
+    xl_load(t0, fw, r0, nr, NX, ch, lane, 0, true, true);
+    xl_load(t1, static_cast<const T*>(xc), r0, nr, NX, ch, lane, 0, true, true);
     cp_async_wait_all();
     __syncwarp();
     if (lane < nr) {
       const int m = min(32, NX - ch * 32);
       for (int k = m - 1; k >= 0; --k) {
-        const T xk = (ch == nch - 1 && k == m - 1) ? tb[lane][k] : tb[lane][k] - tc[lane][k] * xnext;
-        tb[lane][k] = xk;
-        xnext = xk;
+        xnext = (ch == nch - 1 && k == m - 1) ? t1[lane][k] : t1[lane][k] - t0[lane][k] * xnext;
+        t1[lane][k] = xnext;
       }
     }
     __syncwarp();
-    const int i = ch * 32 + lane;
-    for (int q = 0; q < nr; ++q) {
-      const size_t P = (size_t)(r0 + q) * NX + i;
-      if (i < NX) xc[P] = tb[q][lane];
-    }
+    xl_store(t1, xc, r0, nr, NX, ch, lane);
     __syncwarp();
   }
 }
@@ -1423,6 +1454,55 @@ __global__ void k_tri_matvec(int ncol, int n1, const T* __restrict__ dd, const T
     y = l[i - 1] * x[i - 1] + d[i] * x[i] + u[i] * x[i + 1];
   }
   yy[q] = y;
+}
+
+// Residual of the refinement loop in one pass: r = b + (-1)*MatVecMet(x) (the
+// rounding of the separate MatVecMet and Xpay passes), with the per-block
+// partial sums of r.r over the interior cells for a following k_dot_final.
+template <typename T>
+__global__ void k_resid_dot(Dims d, int ncomp, const T* __restrict__ val, const T* __restrict__ x,
+                            const T* __restrict__ b, T* __restrict__ r, double* __restrict__ partial) {
+  const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
+  const size_t n = d.npad();
+  const size_t sy = (size_t)NX, sz = (size_t)NX * NY;
+  double acc = 0.0;
+  for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    d.ijk(P, i, j, k);
+    const bool interior = i > 0 && i < NX - 1 && j > 0 && j < NY - 1 && k > 0 && k < NZ - 1;
+    const T v0 = k > 0 ? val[0 * n + P - sz] : (T)0;
+    const T v1 = j > 0 ? val[1 * n + P - sy] : (T)0;
+    const T v2 = i > 0 ? val[2 * n + P - 1] : (T)0;
+    const T v3 = val[3 * n + P];
+    const T v4 = i < NX - 1 ? val[4 * n + P + 1] : (T)0;
+    const T v5 = j < NY - 1 ? val[5 * n + P + sy] : (T)0;
+    const T v6 = k < NZ - 1 ? val[6 * n + P + sz] : (T)0;
+    for (int ic = 0; ic < ncomp; ++ic) {
+      const T* xa = x + ic * n;
+      T s = (T)0;
+      if (k > 0) s = s + v0 * xa[P - sz];
+      if (j > 0) s = s + v1 * xa[P - sy];
+      if (i > 0) s = s + v2 * xa[P - 1];
+      s = s + v3 * xa[P];
+      if (i < NX - 1) s = s + v4 * xa[P + 1];
+      if (j < NY - 1) s = s + v5 * xa[P + sy];
+      if (k < NZ - 1) s = s + v6 * xa[P + sz];
+      const T xp = xa[P];
+      s = (T)(-1) * xp + s;
+      s = xp + s;
+      const T rv = b[ic * n + P] + (T)(-1) * s;
+      r[ic * n + P] = rv;
+      if (interior) acc += (double)rv * (double)rv;
+    }
+  }
+  __shared__ double sh[RED_BLOCK];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = RED_BLOCK / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
 }
 
 // TotalScalar partials: sum(c*VolB) over the interior (ADVECT/Diagnostic_Mod.f90:13-31)

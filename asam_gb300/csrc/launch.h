@@ -29,7 +29,8 @@ struct Launch {
   void launch_gs_persist(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, T* out, T* work,      \
                          int nsweep, const GsTileSched& sch);                                                    \
   void launch_line_psolve(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, T* x, T* w,         \
-                          int axis);                                                                             \
+                          int axis, const T* fw, const T* fr);                                                   \
+  void launch_xline_factor(const Launch&, const Dims&, const TM* val, T* fw, T* fr);                            \
   void launch_zero_halo(const Launch&, const Dims&, int ncomp, T* x);                                           \
   void launch_exchange_cell(const Launch&, const Dims&, int ncomp, T* c);                                       \
   void launch_dot(const Launch&, const Dims&, int ncomp, const T* x, const T* y, double* partial,               \
@@ -53,6 +54,9 @@ void launch_recip_diag(const Launch&, size_t npad, double* val);
 void launch_mass(const Launch&, const Dims&, const double* c, const double* volc, double* partial, double* out);
 void launch_convert_f64_to_f32(const Launch&, size_t len, const double* x, float* y);
 void launch_convert_f32_to_f64(const Launch&, size_t len, const float* x, double* y);
+void launch_add_f32_to_f64(const Launch&, size_t len, const float* x, double* y);
+void launch_resid_dot(const Launch&, const Dims&, int ncomp, const double* val, const double* x, const double* b,
+                      double* r, double* partial, KrylovScalars* sc, int op, double* out);
 
 constexpr int kRedGrid = 1024;  // number of partial sums of the reductions
 

@@ -102,18 +102,26 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
     cudaMemsetAsync(sch.counter, 0, sizeof(int), L.stream);                                                        \
     k_gs_persist<TM, T><<<grid, threads, smem, L.stream>>>(d, ncomp, val, b, out, work, nsweep, ntx, nty, ntz,    \
                                                             sch);                                                  \
-    count_launches(1);                                                                                             \
+    k_gs_advance<<<1, 32, 0, L.stream>>>(sch.base, nsweep);                                                        \
+    count_launches(2);                                                                                             \
   }                                                                                                                \
   void launch_line_psolve(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* b, T* x, T* w,       \
-                          int axis) {                                                                              \
+                          int axis, const T* fw, const T* fr) {                                                    \
     if (axis == 0) {                                                                                               \
-      const long long tasks = (long long)((d.NY() * d.NZ() + 31) / 32) * ncomp;                                   \
       const int wpb = xl_warps<T>();                                                                               \
-      k_xline_psolve<TM, T><<<(unsigned)((tasks + wpb - 1) / wpb), 32 * wpb, 0, L.stream>>>(d, ncomp, val, b, x, w); \
+      const long long tasks = (long long)((d.NY() * d.NZ() + 31) / 32) * ncomp;                                   \
+      k_xline_solve<TM, T><<<(unsigned)((tasks + wpb - 1) / wpb), 32 * wpb, 0, L.stream>>>(d, ncomp, val, fw, fr,  \
+                                                                                             b, x);                \
     } else {                                                                                                       \
       const size_t ncols = (size_t)d.NX() * (axis == 2 ? d.NY() : d.NZ());                                         \
       k_line_psolve<TM, T><<<(unsigned)((ncols + 127) / 128), 128, 0, L.stream>>>(d, ncomp, axis, val, b, x, w);   \
     }                                                                                                              \
+    count_launches(1);                                                                                             \
+  }                                                                                                                \
+  void launch_xline_factor(const Launch& L, const Dims& d, const TM* val, T* fw, T* fr) {                          \
+    const int wpb = xl_warps<T>();                                                                                 \
+    const long long groups = (d.NY() * d.NZ() + 31) / 32;                                                         \
+    k_xline_factor<TM, T><<<(unsigned)((groups + wpb - 1) / wpb), 32 * wpb, 0, L.stream>>>(d, val, fw, fr);        \
     count_launches(1);                                                                                             \
   }                                                                                                                \
   void launch_zero_halo(const Launch& L, const Dims& d, int ncomp, T* x) {                                         \

@@ -38,9 +38,10 @@ int install(asam_ctx* h, const Setting& s) {
   return kOk;
 }
 
-// time of one refined solve of the stage system (after one untimed solve)
+// time of one refined solve of the stage system (after two untimed solves:
+// the first runs every half-iteration eagerly, the second captures its graph)
 int time_solve(asam_ctx* h, const double* rhs, double* x, cudaEvent_t e0, cudaEvent_t e1, double* ms) {
-  for (int rep = 0; rep < 2; ++rep) {
+  for (int rep = 0; rep < 3; ++rep) {
     CK(cudaMemsetAsync(x, 0, h->len * sizeof(double), h->L.stream));
     int it = h->cfg.bicgstab_maxiter;
     double tol = h->cfg.bicgstab_tol;

@@ -1,12 +1,14 @@
 """Benchmark of the GB300 Rosenbrock transport step.
 
-Workload (default): the 256x256x128 cut-cell configuration -- Gaussian hill
-h=1 km, half-width 5 km, Gaussian-correlated roughness (sigma 50 m, 2 km),
-dz 50->400 m, snapping + small-cell merge, N=0.01 1/s, u=10 m/s, moist,
-one tracer; 10 cell components (Rho, six LR momentum components, Rho*theta,
+Workload (default): the 512x512x128 cut-cell configuration on which the
+FP32-refined vs FP64 comparison is stated -- Gaussian hill h=1 km, half-width
+5 km, Gaussian-correlated roughness (sigma 50 m, 2 km), dx=dy=200 m,
+dz 50->400 m, snapping + small-cell merge, N=0.01 1/s, u=10 m/s, moist, one
+tracer; 10 cell components (Rho, six LR momentum components, Rho*theta,
 Rho*qv, Rho*tracer); RosRK3 (3 stages), dt = 2 s, BiCGStab tolerance 1e-10,
-6-sweep Gauss-Seidel preconditioner.  Seeded synthetic fields stand in for
-the reference's (unpublished) decks.
+6-sweep Gauss-Seidel preconditioner on the FP64 path.  --nx 256 --ny 256 gives
+the 256x256x128 plain-FP64 configuration.  Seeded synthetic fields stand in
+for the reference's (unpublished) decks.
 
 One step = one Ros3MetC call: per stage ExchangeCell, (stage 1) the 7-diagonal
 Jacobian, the flux RHS of all components, the stage combinations and a full
@@ -15,6 +17,8 @@ cells x steps / s).
 
 Arms:
   (default)          ours: FP64 drop-in path (value), plus the FP32-refined path
+                     (autotuned), the adjoint cost (128x128x64 hill, 40 steps)
+                     and the 48-domain batched ensemble
   --impl reference   the reference's CPU path (the oracle restatement of the
                      Fortran; the Fortran itself has no compiler here), one
                      process per host core on independent blocks.
@@ -45,8 +49,8 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--nx", type=int, default=256)
-    p.add_argument("--ny", type=int, default=256)
+    p.add_argument("--nx", type=int, default=512)
+    p.add_argument("--ny", type=int, default=512)
     p.add_argument("--nz", type=int, default=128)
     p.add_argument("--dt", type=float, default=2.0)
     p.add_argument("--tol", type=float, default=1e-10)
@@ -81,7 +85,9 @@ def workload_config(a):
     return {"workload": f"cut-cell Gaussian hill {a.nx}x{a.ny}x{a.nz}, 10 components, RosRK3 dt={a.dt}s, "
                         f"BiCGStab tol {a.tol:g}, 6-sweep GS preconditioner",
             "nx": a.nx, "ny": a.ny, "nz": a.nz, "ncomp": 10, "method": "RosRK3", "dt": a.dt,
-            "bicgstab_tol": a.tol, "l2": "inputs larger than L2 (state 0.7 GB, matrix 0.5 GB)",
+            "bicgstab_tol": a.tol,
+            "l2": f"inputs larger than L2 (state {10 * 8 * (a.nx + 2) * (a.ny + 2) * (a.nz + 2) / 1e9:.2f} GB, "
+                  f"matrix {8 * 8 * (a.nx + 2) * (a.ny + 2) * (a.nz + 2) / 1e9:.2f} GB)",
             "parallelism": "replicas" if a.gpus > 1 else "single GPU"}
 
 
@@ -387,7 +393,10 @@ def main():
     geo, vel, st = workload(a.nx, a.ny, a.nz)
     ncomp = st.c.shape[0]
     ncell = a.nx * a.ny * a.nz
-    stream = torch.cuda.current_stream()
+    # one non-default stream for torch and the library alike (the library
+    # captures its Krylov half-iterations as CUDA graphs on it)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
 
     def barrier():
         torch.cuda.synchronize()
@@ -562,11 +571,12 @@ def main():
             kname = (f"k_gs_persist<float> (one FP32 inner PSolve: {nsw32} sweeps, persistent tile schedule, "
                      "with its FP64<->FP32 conversions)")
         else:
-            # line solve: the 3 matrix slots of the axis (12 B) + w (4 B write, 4 B read) per cell, b, g (write,
-            # read) and x per component (16 B), plus the two conversion passes (12 B per value each)
-            gs32_bytes = npad * (20 + 16 * ncomp) + npad * ncomp * 2 * 12
-            kname = f"k_{'xline' if inner == 'xline' else 'line'}_psolve<float> (one FP32 inner PSolve: {inner} " \
-                    "Thomas, with its FP64<->FP32 conversions)"
+            # line solve of one call: the per-matrix factors (sub-diagonal, 1/den, w: 12 B per cell), per
+            # component b in, g out and back, x out (16 B), PSolve's copy of the input (8 B), and the two
+            # conversion passes of the call (FP64 -> FP32 in, FP32 -> FP64 out: 12 B per value each)
+            gs32_bytes = npad * (12 + ncomp * (16 + 8 + 24))
+            kname = (f"{'k_xline_solve' if inner == 'xline' else 'k_line_psolve'}<float> (one FP32 inner PSolve: "
+                     f"{inner} Thomas, with its copy and FP64<->FP32 conversions)")
         gs32_s = rr["kernels"]["inner_psolve_ms"] * 1e-3
         line["roofline_refined"] = {
             "kernel": kname, "bound": "hbm",

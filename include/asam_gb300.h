@@ -84,6 +84,12 @@ int asam_create(const asam_config *cfg, const double *volc, const double *fu, co
                 asam_ctx **out);
 int asam_destroy(asam_ctx *ctx);
 
+/* No reference counterpart: capture of the BiCGStab half-iterations as CUDA
+ * graphs, replayed on later iterations and solves (on by default; results are
+ * identical either way; never on the legacy default stream, which cannot be
+ * captured).  on = 0 launches every kernel individually. */
+int asam_set_graphs(asam_ctx *ctx, int on);
+
 /* Run the context's work on this CUDA stream (cudaStream_t); NULL = the legacy
  * default stream.  Until this is called the context uses a stream of its own. */
 int asam_set_stream(asam_ctx *ctx, void *stream);

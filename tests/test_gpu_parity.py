@@ -216,6 +216,25 @@ def test_inner_line_psolve_fp32(env, name, precond, axis):
     assert max(errs) <= 2e-5, errs
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
+@pytest.mark.parametrize("name", ["hill_24x20x16", "flat_walls_9x6x5"])
+def test_graph_captured_iterations_identical(env, name, precision):
+    """BiCGStab half-iterations replayed from CUDA graphs give the bits of the
+    individually launched kernels, over several steps (capture on the second
+    use of each half, replays after)."""
+    geo, vel, st = cases.get(name)
+    out = {}
+    for graphs in (True, False):
+        c = st.c.copy()
+        with _block(env, name, method="RosRK3", bicgstab_tol=1e-12, precision=precision,
+                    inner_precond="xline" if precision == "fp32_refined" else "gauss_seidel") as blk:
+            blk.set_graphs(graphs)
+            its = [blk.Ros3MetC(c, 3.0)[0] for _ in range(4)]
+        out[graphs] = (c, its)
+    assert np.array_equal(out[True][0], out[False][0])
+    assert out[True][1] == out[False][1]
+
+
 @pytest.mark.parametrize("name", ["hill_24x20x16", "hill_odd_13x7x9_reverse"])
 def test_refined_step_schedules_identical(env, name):
     geo, vel, st = cases.get(name)
