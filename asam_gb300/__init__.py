@@ -175,16 +175,17 @@ class TransportBlock:
         return y
 
     def autotune(self, c, dt: float) -> dict:
-        """Pick the refined inner-solver settings for this block (asam_autotune).
-        c: host state array or device pointer (int)."""
-        choice = (C.c_int * 4)()
+        """Pick this block's solver settings (asam_autotune): the refined mode's
+        inner solver and, for either precision, the CUDA-graph replay of the
+        Krylov iterations.  c: host state array or device pointer (int)."""
+        choice = (C.c_int * 5)()
         ms = C.c_double()
         p = C.c_void_p(c) if isinstance(c, int) else ptr(self._state(c))
         check(self.lib.asam_autotune(self.h, p, float(dt), choice, C.byref(ms)), "asam_autotune")
         names = {v: k for k, v in INNER_PRECONDS.items()}
         scheds = {v: k for k, v in GS_SCHEDULES.items()}
         return {"inner_precond": names[choice[0]], "inner_gs_iter": choice[1], "gs_schedule": scheds[choice[2]],
-                "gs_group": choice[3], "stage_solve_ms": ms.value}
+                "gs_group": choice[3], "graphs": bool(choice[4]), "stage_solve_ms": ms.value}
 
     def inner_psolve(self, x: np.ndarray) -> np.ndarray:
         """The refined mode's FP32 inner preconditioner applied to x (no reference
@@ -224,6 +225,14 @@ class TransportBlock:
         st = self.lib.asam_ros_step(self.h, C.c_void_p(dptr), float(dt), iters, resid)
         check(st, "asam_ros_step", allow=(ASAM_OK, ASAM_NOT_CONVERGED, ASAM_BREAKDOWN))
         return [iters[i] for i in range(self.nstage)], [resid[i] for i in range(self.nstage)]
+
+    def state_dot(self, c) -> float:
+        """DOT(VecMet,VecMet) over all components (the driver's NaN check);
+        raises AsamError (ASAM_NAN_DETECTED) when it is NaN."""
+        a = self._state(c)
+        out = C.c_double()
+        check(self.lib.asam_state_dot(self.h, ptr(a), C.byref(out)), "asam_state_dot")
+        return out.value
 
     def TotalScalar(self, c: np.ndarray, comp: int = 0) -> float:
         a = self._state(c)

@@ -67,11 +67,14 @@ SIGNATURES = [
     ("asam_ros_step_tlm", C.c_int, [_V, _V, C.c_int, _V, _V, C.c_double, C.c_double]),
     ("asam_ros_step_adj", C.c_int, [_V, _V, C.c_int, _V, _V, C.c_double, C.c_double]),
     ("asam_tracer_gradient", C.c_int, [_V, _V, C.c_int, C.c_int, C.c_double, C.c_int, _V, C.c_double, _D, _V]),
+    ("asam_tracer_wind_gradient", C.c_int,
+     [_V, _V, C.c_int, C.c_int, C.c_double, C.c_int, _V, C.c_double, _D, _V, _V, _V, _V, _V]),
     ("asam_tri_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_ros_coeffs", C.c_int, [C.c_int, _D, _D, _D, _D]),
     ("asam_autotune", C.c_int, [_V, _V, C.c_double, _I, _D]),
+    ("asam_state_dot", C.c_int, [_V, _V, _D]),
     ("asam_batch_create", C.c_int, [C.c_int, _V, C.c_int, C.POINTER(C.c_void_p)]),
     ("asam_batch_destroy", C.c_int, [_V]),
     ("asam_batch_ros_step", C.c_int, [_V, _V, _D, C.c_int, _I, _D, _I]),

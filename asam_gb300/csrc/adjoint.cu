@@ -399,6 +399,187 @@ __global__ void k_objective(Dims d, const double* __restrict__ c, const double* 
 }
 
 // ---------------------------------------------------------------------------
+// Wind and density derivatives (coupled density-component adjoint).
+//
+// Stage operator: A = I - bdt*J with every entry of column P of J a sum of
+// jac_term(u_f, ., F, V, Rho_P) = Half*(|u_f| +/- u_f)*F/V/(Rho_P+Eps) terms
+// (k_jac), each depending on one face velocity u_f (homogeneous of degree 1
+// on either side of u_f = 0) and on Rho_P only through 1/(Rho_P+Eps):
+//   d term/d u_f = term/u_f,  d term/d Rho_P = -term/(Rho_P+Eps).
+// For the stage solve A k = b the adjoint contribution of dA is
+//   -lb^T dA k = bdt * sum_terms sigma * d(term) * lb(row) * k(P)
+// (sigma the term's sign in J(row, P)), summed over the components.  Faces
+// with u_f = 0 are not differentiable (the upwind side switches) and get 0.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double jac_term_d(double vel, bool plus, double F, double Vden, double rho) {
+  const double s = plus ? (fabs(vel) + vel) : (fabs(vel) - vel);
+  return 0.5 * s * F / Vden / (rho + 1.0e-30);
+}
+
+// k (exchanged) and lb (zero halos) hold nc fields each, `stride` apart.
+__global__ void k_jac_adj(Dims d, GeomT<double> g, const double* __restrict__ rho, double bdt, int nc,
+                          size_t stride, const double* __restrict__ lb, const double* __restrict__ kk_,
+                          double* __restrict__ gu, double* __restrict__ gv, double* __restrict__ gw,
+                          double* __restrict__ grho) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int NX = d.NX(), NY = d.NY();
+  const size_t n = d.npad();
+  const double e = 1.0e-30;
+  const size_t sx = 1, sy = (size_t)NX, sz = (size_t)NX * NY;
+  for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    d.ijk(P, i, j, k);
+    const bool ii = i >= 1 && i <= nx, jj = j >= 1 && j <= ny, kk = k >= 1 && k <= nz;
+    const double rP = rho[P];
+    const double VP = g.volc[P] + e;
+    // w(row) = sum over components of lb(row) * k(P)
+    auto wrow = [&](size_t row) {
+      double s = 0.0;
+      for (int m = 0; m < nc; ++m) s += lb[m * stride + row] * kk_[m * stride + P];
+      return s;
+    };
+    double drho = 0.0;
+    // one term of J(row, P) with sign sigma, velocity u (array a at index f)
+    auto term = [&](double* ga, size_t fidx, double u, bool plus, double F, double Vden, size_t row, double sigma) {
+      const double t = jac_term_d(u, plus, F, Vden, rP);
+      if (t == 0.0) return;
+      const double c = bdt * sigma * t * wrow(row);
+      if (u != 0.0) atomicAdd(ga + fidx, c / u);
+      drho += -c / (rP + e);
+    };
+    auto actx = [&](int fi) { return jj && kk && fi >= 0 && fi <= nx && ((fi >= 1 && fi <= nx - 1) || d.per_x); };
+    auto acty = [&](int fj) { return ii && kk && fj >= 0 && fj <= ny && ((fj >= 1 && fj <= ny - 1) || d.per_y); };
+    auto actz = [&](int fk) { return ii && jj && fk >= 0 && fk <= nz && ((fk >= 1 && fk <= nz - 1) || d.per_z); };
+    // off-diagonals: slot 2 -> row P+1, 4 -> P-1, 1 -> P+NX, 5 -> P-NX, 0 -> P+NXY, 6 -> P-NXY;
+    // the face-halo rows fold the same term into the diagonal with sign -1
+    if (actx(i)) {
+      const size_t f = d.UF(i, j, k);
+      term(gu, f, g.uf[f], true, g.fu[d.FU(i, j, k)], g.volc[P + sx] + e, P + sx, 1.0);
+      if (i == 0) term(gu, f, g.uf[f], true, g.fu[d.FU(i, j, k)], g.volc[P + sx] + e, P, -1.0);
+    }
+    if (actx(i - 1)) {
+      const size_t f = d.UF(i - 1, j, k);
+      term(gu, f, g.uf[f], false, g.fu[d.FU(i - 1, j, k)], g.volc[P - sx] + e, P - sx, 1.0);
+      if (i == nx + 1) term(gu, f, g.uf[f], false, g.fu[d.FU(i - 1, j, k)], g.volc[P - sx] + e, P, -1.0);
+    }
+    if (acty(j)) {
+      const size_t f = d.VF(i, j, k);
+      term(gv, f, g.vf[f], true, g.fv[d.FV(i, j, k)], g.volc[P + sy] + e, P + sy, 1.0);
+      if (j == 0) term(gv, f, g.vf[f], true, g.fv[d.FV(i, j, k)], g.volc[P + sy] + e, P, -1.0);
+    }
+    if (acty(j - 1)) {
+      const size_t f = d.VF(i, j - 1, k);
+      term(gv, f, g.vf[f], false, g.fv[d.FV(i, j - 1, k)], g.volc[P - sy] + e, P - sy, 1.0);
+      if (j == ny + 1) term(gv, f, g.vf[f], false, g.fv[d.FV(i, j - 1, k)], g.volc[P - sy] + e, P, -1.0);
+    }
+    if (actz(k)) {
+      const size_t f = d.WF(i, j, k);
+      term(gw, f, g.wf[f], true, g.fw[d.FW(i, j, k)], g.volc[P + sz] + e, P + sz, 1.0);
+      if (k == 0) term(gw, f, g.wf[f], true, g.fw[d.FW(i, j, k)], g.volc[P + sz] + e, P, -1.0);
+    }
+    if (actz(k - 1)) {
+      const size_t f = d.WF(i, j, k - 1);
+      term(gw, f, g.wf[f], false, g.fw[d.FW(i, j, k - 1)], g.volc[P - sz] + e, P - sz, 1.0);
+      if (k == nz + 1) term(gw, f, g.wf[f], false, g.fw[d.FW(i, j, k - 1)], g.volc[P - sz] + e, P, -1.0);
+    }
+    // diagonal terms (sign -1 in J(P, P)), the interior loops and the periodic branches of k_jac
+    if (jj && kk && i - 1 >= 1 && i - 1 <= nx - 1) {
+      const size_t f = d.UF(i - 1, j, k);
+      term(gu, f, g.uf[f], false, g.fu[d.FU(i - 1, j, k)], VP, P, -1.0);
+    }
+    if (jj && kk && i >= 1 && i <= nx - 1) {
+      const size_t f = d.UF(i, j, k);
+      term(gu, f, g.uf[f], true, g.fu[d.FU(i, j, k)], VP, P, -1.0);
+    }
+    if (ii && kk && j - 1 >= 1 && j - 1 <= ny - 1) {
+      const size_t f = d.VF(i, j - 1, k);
+      term(gv, f, g.vf[f], false, g.fv[d.FV(i, j - 1, k)], VP, P, -1.0);
+    }
+    if (ii && kk && j >= 1 && j <= ny - 1) {
+      const size_t f = d.VF(i, j, k);
+      term(gv, f, g.vf[f], true, g.fv[d.FV(i, j, k)], VP, P, -1.0);
+    }
+    if (ii && jj && k - 1 >= 1 && k - 1 <= nz - 1) {
+      const size_t f = d.WF(i, j, k - 1);
+      term(gw, f, g.wf[f], false, g.fw[d.FW(i, j, k - 1)], VP, P, -1.0);
+    }
+    if (ii && jj && k >= 1 && k <= nz - 1) {
+      const size_t f = d.WF(i, j, k);
+      term(gw, f, g.wf[f], true, g.fw[d.FW(i, j, k)], VP, P, -1.0);
+    }
+    if (d.per_x && jj && kk) {
+      if (i == 0) term(gu, d.UF(0, j, k), g.uf[d.UF(0, j, k)], true, g.fu[d.FU(0, j, k)], VP, P, -1.0);
+      if (i == 1) term(gu, d.UF(0, j, k), g.uf[d.UF(0, j, k)], false, g.fu[d.FU(0, j, k)], VP, P, -1.0);
+      if (i == nx) term(gu, d.UF(nx, j, k), g.uf[d.UF(nx, j, k)], true, g.fu[d.FU(nx, j, k)], VP, P, -1.0);
+      if (i == nx + 1) term(gu, d.UF(nx, j, k), g.uf[d.UF(nx, j, k)], false, g.fu[d.FU(nx, j, k)], VP, P, -1.0);
+    }
+    if (d.per_y && ii && kk) {
+      if (j == 0) term(gv, d.VF(i, 0, k), g.vf[d.VF(i, 0, k)], true, g.fv[d.FV(i, 0, k)], VP, P, -1.0);
+      if (j == 1) term(gv, d.VF(i, 0, k), g.vf[d.VF(i, 0, k)], false, g.fv[d.FV(i, 0, k)], VP, P, -1.0);
+      if (j == ny) term(gv, d.VF(i, ny, k), g.vf[d.VF(i, ny, k)], true, g.fv[d.FV(i, ny, k)], VP, P, -1.0);
+      if (j == ny + 1) term(gv, d.VF(i, ny, k), g.vf[d.VF(i, ny, k)], false, g.fv[d.FV(i, ny, k)], VP, P, -1.0);
+    }
+    if (d.per_z && ii && jj) {
+      if (k == 0) term(gw, d.WF(i, j, 0), g.wf[d.WF(i, j, 0)], true, g.fw[d.FW(i, j, 0)], VP, P, -1.0);
+      if (k == 1) term(gw, d.WF(i, j, 0), g.wf[d.WF(i, j, 0)], false, g.fw[d.FW(i, j, 0)], VP, P, -1.0);
+      if (k == nz) term(gw, d.WF(i, j, nz), g.wf[d.WF(i, j, nz)], true, g.fw[d.FW(i, j, nz)], VP, P, -1.0);
+      if (k == nz + 1) term(gw, d.WF(i, j, nz), g.wf[d.WF(i, j, nz)], false, g.fw[d.FW(i, j, nz)], VP, P, -1.0);
+    }
+    grho[P] += drho;
+  }
+}
+
+// Wind part of the flux adjoint: the stored face flux g = |u| F recon (the
+// upwind reconstruction) gives dg/du = g/u on faces with u != 0, so
+// gface += scale * lg * g / u with lg the face adjoint of the gather transpose.
+__global__ void k_wind_flux_T(size_t nface, const double* __restrict__ vel, const double* __restrict__ lg,
+                              const double* __restrict__ gfl, double scale, double* __restrict__ gface) {
+  for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < nface; f += (size_t)gridDim.x * blockDim.x) {
+    const double u = vel[f];
+    if (u != 0.0) gface[f] += scale * lg[f] * gfl[f] / u;
+  }
+}
+
+// density part of a component's flux adjoint: phi = c/(Rho+Eps) gives
+// d phi/d Rho = -phi/(Rho+Eps), so lr = -phi * lc with lc = lphi/(Rho+Eps)
+__global__ void k_rho_from_phi(size_t n, const double* __restrict__ phi, const double* __restrict__ lc,
+                               double* __restrict__ lr) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    lr[q] = -phi[q] * lc[q];
+}
+
+// J = sum_box (c/(Rho+Eps))^2 V, dJ/dc = 2 q V/(Rho+Eps), dJ/dRho = -2 q^2 V/(Rho+Eps)
+__global__ void k_objective2(Dims d, const double* __restrict__ c, const double* __restrict__ rho,
+                             const double* __restrict__ volc, int i0, int i1, int j0, int j1, int k0, int k1,
+                             double* __restrict__ gc, double* __restrict__ gr, double* __restrict__ partial) {
+  const int nx = d.nx, ny = d.ny;
+  const size_t nint = (size_t)nx * ny * d.nz;
+  double s = 0.0;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nint; q += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % nx) + 1, j = (int)((q / nx) % ny) + 1, k = (int)(q / ((size_t)nx * ny)) + 1;
+    const size_t P = d.P(i, j, k);
+    double a = 0.0, b = 0.0;
+    if (i >= i0 && i <= i1 && j >= j0 && j <= j1 && k >= k0 && k <= k1) {
+      const double r = rho[P] + 1.0e-30;
+      const double qv = c[P] / r;
+      s += qv * qv * volc[P];
+      a = 2.0 * qv * volc[P] / r;
+      b = -2.0 * qv * qv * volc[P] / r;
+    }
+    gc[P] = a;
+    gr[P] = b;
+  }
+  __shared__ double sh[RED_BLOCK];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = RED_BLOCK / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 struct AdjWork {
@@ -687,6 +868,133 @@ int step_adj(asam_ctx* h, AdjWork& w, const std::vector<double*>& stage_states, 
   return check_launch();
 }
 
+// Coupled adjoint step of (Rho, component comp) with the face velocities as
+// parameters: (lr, lc) adjoints of the step's end state (interior) ->
+// (lr_out, lc_out) adjoints of its start state; the wind gradient of the step
+// is added to (gu, gv, gw).  Needs the stage states of the step
+// (stage_states[0..nS-1], halos current), its increments in h->incr
+// (exchanged) and its stage matrix in h->val.  Density enters through the
+// mixing ratio of the component's flux and through the stage matrix; its own
+// flux does not depend on it (phi_Rho = Rho/(Rho+Eps) = 1 in FP64).
+struct CoupledWork {
+  double *lkc[4], *lkr[4];  // adjoints of the increments
+  double *lbc, *lbr, *luc, *lur, *accc, *accr, *grho, *lrp;
+  std::vector<double*> own;
+  int alloc(asam_ctx* h) {
+    const size_t n = h->npad;
+    for (int q = 0; q < 4; ++q) {
+      lkc[q] = lkr[q] = nullptr;
+    }
+    double** ptrs[] = {&lbc, &lbr, &luc, &lur, &accc, &accr, &grho, &lrp};
+    for (double** q : ptrs) {
+      CK(cudaMalloc((void**)q, n * sizeof(double)));
+      own.push_back(*q);
+    }
+    for (int q = 0; q < h->nstage; ++q) {
+      CK(cudaMalloc((void**)&lkc[q], n * sizeof(double)));
+      own.push_back(lkc[q]);
+      CK(cudaMalloc((void**)&lkr[q], n * sizeof(double)));
+      own.push_back(lkr[q]);
+    }
+    return kOk;
+  }
+  ~CoupledWork() {
+    for (double* q : own) cudaFree(q);
+  }
+};
+
+// kr[is], kc[is]: the step's increments of Rho and of the component (exchanged)
+int step_adj_coupled(asam_ctx* h, AdjWork& w, CoupledWork& cw, const std::vector<double*>& stage_states, int comp,
+                     const double* const* kr, const double* const* kc, const double* lr_in, const double* lc_in,
+                     double* lr_out, double* lc_out, double dt, double tol, double* gu, double* gv, double* gw) {
+  const Launch& L = h->L;
+  const Dims& d = h->d;
+  const size_t n = h->npad;
+  const int ns = h->nstage;
+  const int rp = h->cfg.rho_pos;
+  const double bdt = h->beta0 * dt;
+  const int gn = grid_of(L, n);
+  const size_t nint = (size_t)d.nx * d.ny * d.nz;
+  CK(cudaMemcpyAsync(cw.accc, lc_in, n * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+  CK(cudaMemcpyAsync(cw.accr, lr_in, n * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+  k_zero_halo1<<<gn, kB, 0, L.stream>>>(d, cw.accc);
+  k_zero_halo1<<<gn, kB, 0, L.stream>>>(d, cw.accr);
+  count_launches(2);
+  for (int j = 0; j < ns; ++j) {
+    CK(cudaMemsetAsync(cw.lkc[j], 0, n * sizeof(double), L.stream));
+    CK(cudaMemsetAsync(cw.lkr[j], 0, n * sizeof(double), L.stream));
+    axpby(h, h->alpha[(ns - 1) * 4 + j], cw.accc, 1.0, cw.lkc[j]);
+    axpby(h, h->alpha[(ns - 1) * 4 + j], cw.accr, 1.0, cw.lkr[j]);
+  }
+  CK(cudaMemsetAsync(cw.grho, 0, n * sizeof(double), L.stream));
+  const double* rho0 = stage_states[0] + (size_t)rp * n;
+  for (int is = ns - 1; is >= 0; --is) {
+    // stage solve A k = b: lb = A_per^-T lk for both components
+    int rc = bicgstab_T(h, w, cw.lbc, cw.lkc[is], 400, tol, nullptr);
+    if (rc != kOk && rc != kNotConverged) return rc;
+    rc = bicgstab_T(h, w, cw.lbr, cw.lkr[is], 400, tol, nullptr);
+    if (rc != kOk && rc != kNotConverged) return rc;
+    k_zero_halo1<<<gn, kB, 0, L.stream>>>(d, cw.lbc);
+    k_zero_halo1<<<gn, kB, 0, L.stream>>>(d, cw.lbr);
+    count_launches(2);
+    // the stage matrix's dependence on the wind and on Rho_0: lb of (Rho, comp)
+    // against the increments k_is of (Rho, comp)
+    k_jac_adj<<<gn, kB, 0, L.stream>>>(d, h->geom(), rho0, bdt, 1, 0, cw.lbr, kr[is], gu, gv, gw, cw.grho);
+    k_jac_adj<<<gn, kB, 0, L.stream>>>(d, h->geom(), rho0, bdt, 1, 0, cw.lbc, kc[is], gu, gv, gw, cw.grho);
+    count_launches(2);
+    for (int js = 0; js < is; ++js) {
+      axpby(h, h->beta[is * 4 + js], cw.lbc, 1.0, cw.lkc[js]);
+      axpby(h, h->beta[is * 4 + js], cw.lbr, 1.0, cw.lkr[js]);
+    }
+    // flux RHS b = dt R F(E y): forward face fluxes at the stage state
+    if ((rc = fcn_dev(h, stage_states[is], h->rhs))) return rc;
+    const double* rho_s = stage_states[is] + (size_t)rp * n;
+    // component: lc = F_c'^T lb (w.gx/gy/gz: face adjoints), wind and density parts
+    flux_dcoef(h, w, stage_states[is], comp);
+    flux_adj(h, w, rho_s, cw.lbc, cw.luc);
+    k_wind_flux_T<<<grid_of(L, d.n_uf()), kB, 0, L.stream>>>(d.n_uf(), h->uf, w.gx, h->gx + (size_t)comp * d.n_uf(),
+                                                             dt, gu);
+    k_wind_flux_T<<<grid_of(L, d.n_vf()), kB, 0, L.stream>>>(d.n_vf(), h->vf, w.gy, h->gy + (size_t)comp * d.n_vf(),
+                                                             dt, gv);
+    k_wind_flux_T<<<grid_of(L, d.n_wf()), kB, 0, L.stream>>>(d.n_wf(), h->wf, w.gz, h->gz + (size_t)comp * d.n_wf(),
+                                                             dt, gw);
+    k_rho_from_phi<<<gn, kB, 0, L.stream>>>(n, w.phi, cw.luc, cw.lur);
+    count_launches(4);
+    // Rho: its flux depends on the wind only
+    k_gather_T<0><<<grid_of(L, d.n_uf()), kB, 0, L.stream>>>(d, h->geom(), h->rvol, cw.lbr, w.gx);
+    k_gather_T<1><<<grid_of(L, d.n_vf()), kB, 0, L.stream>>>(d, h->geom(), h->rvol, cw.lbr, w.gy);
+    k_gather_T<2><<<grid_of(L, d.n_wf()), kB, 0, L.stream>>>(d, h->geom(), h->rvol, cw.lbr, w.gz);
+    k_wind_flux_T<<<grid_of(L, d.n_uf()), kB, 0, L.stream>>>(d.n_uf(), h->uf, w.gx, h->gx + (size_t)rp * d.n_uf(),
+                                                             dt, gu);
+    k_wind_flux_T<<<grid_of(L, d.n_vf()), kB, 0, L.stream>>>(d.n_vf(), h->vf, w.gy, h->gy + (size_t)rp * d.n_vf(),
+                                                             dt, gv);
+    k_wind_flux_T<<<grid_of(L, d.n_wf()), kB, 0, L.stream>>>(d.n_wf(), h->wf, w.gz, h->gz + (size_t)rp * d.n_wf(),
+                                                             dt, gw);
+    count_launches(6);
+    // stage state y = u0 + sum alpha k: lu = dt E^T Z (lc, lr)
+    double* lus[2] = {cw.luc, cw.lur};
+    for (double* lu : lus) {
+      k_exchange_T<<<grid_of(L, nint), kB, 0, L.stream>>>(d, lu);
+      k_zero_halo1<<<gn, kB, 0, L.stream>>>(d, lu);
+      count_launches(2);
+    }
+    axpby(h, dt, cw.luc, 1.0, cw.accc);
+    axpby(h, dt, cw.lur, 1.0, cw.accr);
+    for (int js = 0; js < is; ++js) {
+      axpby(h, dt * h->alpha[(is - 1) * 4 + js], cw.luc, 1.0, cw.lkc[js]);
+      axpby(h, dt * h->alpha[(is - 1) * 4 + js], cw.lur, 1.0, cw.lkr[js]);
+    }
+  }
+  // Rho_0 of the stage matrix is the exchanged start state: E^T, then add
+  k_exchange_T<<<grid_of(L, nint), kB, 0, L.stream>>>(d, cw.grho);
+  k_zero_halo1<<<gn, kB, 0, L.stream>>>(d, cw.grho);
+  count_launches(2);
+  axpby(h, 1.0, cw.grho, 1.0, cw.accr);
+  CK(cudaMemcpyAsync(lc_out, cw.accc, n * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+  CK(cudaMemcpyAsync(lr_out, cw.accr, n * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+  return check_launch();
+}
+
 struct AdjScratch {
   AdjWork w;
   std::vector<double*> stage;  // nstage+1 full states
@@ -934,6 +1242,121 @@ int asam_tracer_gradient(asam_ctx* h, const double* c0, int comp, int nsteps, do
   rc = check_launch();
   if (rc) return rc;
   return dev_out_finish(h, grad, n, dgrad);
+}
+
+int asam_tracer_wind_gradient(asam_ctx* h, const double* c0, int comp, int nsteps, double dt, int ckpt_every,
+                              const int* box, double tol, double* J, double* grad_c, double* grad_rho,
+                              double* grad_uf, double* grad_vf, double* grad_wf) {
+  if (!h || !c0 || !box || !J || !grad_c || !grad_rho || !grad_uf || !grad_vf || !grad_wf || !valid_comp(h, comp) ||
+      nsteps < 1 || ckpt_every < 1)
+    return kBadArg;
+  const Launch& L = h->L;
+  const Dims& d = h->d;
+  const size_t len = h->len, n = h->npad;
+  const int rp = h->cfg.rho_pos;
+  Owned o;
+  double *dc0, *dgc, *dgr, *dgu, *dgv, *dgw;
+  int rc;
+  if ((rc = dev_copy_in(h, c0, len, &dc0, o.p)) || (rc = dev_out(h, grad_c, n, &dgc, o)) ||
+      (rc = dev_out(h, grad_rho, n, &dgr, o)) || (rc = dev_out(h, grad_uf, d.n_uf(), &dgu, o)) ||
+      (rc = dev_out(h, grad_vf, d.n_vf(), &dgv, o)) || (rc = dev_out(h, grad_wf, d.n_wf(), &dgw, o)))
+    return rc;
+  AdjScratch sc;
+  if ((rc = sc.alloc(h))) return rc;
+  CoupledWork cw;
+  if ((rc = cw.alloc(h))) return rc;
+  const int nck = (nsteps + ckpt_every - 1) / ckpt_every;
+  const int ns = h->nstage;
+  std::vector<double*> ckpt(nck, nullptr), recbuf((size_t)ckpt_every * ns + 2, nullptr);
+  double *lr = nullptr, *lr2 = nullptr, *lc2 = nullptr;
+  struct Free {
+    std::vector<double*>* a;
+    ~Free() {
+      for (auto p : *a)
+        if (p) cudaFree(p);
+    }
+  };
+  std::vector<double*> extra;
+  // increments of Rho and of the component for every stage of every step of a
+  // segment: [(m*ns + is)*2 + 0 | 1]
+  std::vector<double*> incs((size_t)ckpt_every * ns * 2, nullptr);
+  Free f1{&ckpt}, f2{&recbuf}, f3{&extra}, f4{&incs};
+  for (auto& p : ckpt) CK(cudaMalloc((void**)&p, len * sizeof(double)));
+  for (auto& p : recbuf) CK(cudaMalloc((void**)&p, len * sizeof(double)));
+  for (auto& p : incs) CK(cudaMalloc((void**)&p, n * sizeof(double)));
+  for (double** q : {&lr, &lr2, &lc2}) {
+    CK(cudaMalloc((void**)q, n * sizeof(double)));
+    extra.push_back(*q);
+  }
+  std::vector<std::vector<double*>> rec(ckpt_every, std::vector<double*>(ns + 1, nullptr));
+  for (int m = 0; m < ckpt_every; ++m) {
+    for (int is = 0; is < ns; ++is) rec[m][is] = recbuf[(size_t)m * ns + is];
+    rec[m][ns] = recbuf[(size_t)ckpt_every * ns + (m & 1)];
+  }
+  struct TolGuard {
+    asam_ctx* h;
+    double saved;
+    ~TolGuard() { h->cfg.bicgstab_tol = saved; }
+  } tg{h, h->cfg.bicgstab_tol};
+  h->cfg.bicgstab_tol = tol;
+  double* cur = h->c;
+  CK(cudaMemcpyAsync(cur, dc0, len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+  for (int s = 0; s < nsteps; ++s) {
+    if (s % ckpt_every == 0)
+      CK(cudaMemcpyAsync(ckpt[s / ckpt_every], cur, len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+    int it[4];
+    double rs[4];
+    rc = ros_step_dev(h, cur, dt, it, rs);
+    if (rc != kOk && rc != kNotConverged) return rc;
+  }
+  launch_exchange_cell(L, d, h->cfg.ncomp, cur);
+  double* lc = sc.w.lam;
+  k_objective2<<<RED_GRID, RED_BLOCK, 0, L.stream>>>(d, cur + (size_t)comp * n, cur + (size_t)rp * n, h->volc, box[0],
+                                                     box[1], box[2], box[3], box[4], box[5], lc, lr, h->partial);
+  k_sum_partials<<<1, RED_BLOCK, 0, L.stream>>>(h->partial, RED_GRID, h->red_out);
+  count_launches(2);
+  if ((rc = reduce_to_host(h, J))) return rc;
+  CK(cudaMemsetAsync(dgu, 0, d.n_uf() * sizeof(double), L.stream));
+  CK(cudaMemsetAsync(dgv, 0, d.n_vf() * sizeof(double), L.stream));
+  CK(cudaMemsetAsync(dgw, 0, d.n_wf() * sizeof(double), L.stream));
+  for (int sgi = nck - 1; sgi >= 0; --sgi) {
+    const int s0 = sgi * ckpt_every;
+    const int s1 = std::min(nsteps, s0 + ckpt_every);
+    const double* src = ckpt[sgi];
+    for (int s = s0; s < s1; ++s) {
+      const int m = s - s0;
+      if ((rc = forward_record(h, src, dt, tol, rec[m]))) return rc;
+      for (int is = 0; is < ns; ++is) {
+        const double* k = h->incr + (size_t)is * len;
+        CK(cudaMemcpyAsync(incs[((size_t)m * ns + is) * 2], k + (size_t)rp * n, n * sizeof(double),
+                           cudaMemcpyDeviceToDevice, L.stream));
+        CK(cudaMemcpyAsync(incs[((size_t)m * ns + is) * 2 + 1], k + (size_t)comp * n, n * sizeof(double),
+                           cudaMemcpyDeviceToDevice, L.stream));
+      }
+      src = rec[m][ns];
+    }
+    for (int s = s1 - 1; s >= s0; --s) {
+      const int m = s - s0;
+      if ((rc = jac_dev(h, rec[m][0], dt))) return rc;  // the step's stage matrix
+      double* kr[4];
+      double* kc[4];
+      for (int is = 0; is < ns; ++is) {
+        kr[is] = incs[((size_t)m * ns + is) * 2];
+        kc[is] = incs[((size_t)m * ns + is) * 2 + 1];
+      }
+      if ((rc = step_adj_coupled(h, sc.w, cw, rec[m], comp, kr, kc, lr, lc, lr2, lc2, dt, tol, dgu, dgv, dgw)))
+        return rc;
+      CK(cudaMemcpyAsync(lc, lc2, n * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+      CK(cudaMemcpyAsync(lr, lr2, n * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+    }
+  }
+  CK(cudaMemcpyAsync(dgc, lc, n * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+  CK(cudaMemcpyAsync(dgr, lr, n * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+  if ((rc = check_launch())) return rc;
+  if ((rc = dev_out_finish(h, grad_c, n, dgc)) || (rc = dev_out_finish(h, grad_rho, n, dgr)) ||
+      (rc = dev_out_finish(h, grad_uf, d.n_uf(), dgu)) || (rc = dev_out_finish(h, grad_vf, d.n_vf(), dgv)))
+    return rc;
+  return dev_out_finish(h, grad_wf, d.n_wf(), dgw);
 }
 
 }  // extern "C"

@@ -209,6 +209,12 @@ int read_scalars(asam_ctx* h) {
     set_last_error("persistent Gauss-Seidel schedule: a dependency wait gave up", __FILE__, __LINE__);
     return kCudaError;
   }
+  // a NaN in the residual norms means a NaN in the system (the reference's
+  // driver stops on ISNAN(DOT(VecMet,VecMet)), ADVECT/MainProg.f90:975-980)
+  if (std::isnan(h->sc_host->rnorm) || std::isnan(h->sc_host->rnorm0)) {
+    set_last_error("NaN in the stage system", __FILE__, __LINE__);
+    return kNanDetected;
+  }
   return kOk;
 }
 
@@ -466,6 +472,10 @@ int bicgstab_refined(asam_ctx* h, double* x, const double* b, int* maxiter, doub
   double rr0 = 0;
   int rc = reduce_to_host(h, &rr0);
   if (rc) return rc;
+  if (std::isnan(rr0)) {
+    set_last_error("NaN in the stage system", __FILE__, __LINE__);
+    return kNanDetected;
+  }
   const double rnorm0 = sqrt(rr0);
   const double target = *tol * rnorm0;
   if (rnorm0 == 0.0) {
@@ -491,6 +501,10 @@ int bicgstab_refined(asam_ctx* h, double* x, const double* b, int* maxiter, doub
     double rr = 0;
     rc = reduce_to_host(h, &rr);
     if (rc) return rc;
+    if (std::isnan(rr)) {
+      set_last_error("NaN in the stage system", __FILE__, __LINE__);
+      return kNanDetected;
+    }
     rnorm = sqrt(rr);
     if (rnorm <= target) {
       *maxiter = total_inner;
@@ -1008,6 +1022,21 @@ int asam_ros_step(asam_ctx* h, double* c, double dt, int* iters, double* resid) 
   if (st != kOk && st != kNotConverged && st != kBreakdown) return st;
   rc = stage_out_end(h, c, h->len, dc);
   return rc ? rc : st;
+}
+
+int asam_state_dot(asam_ctx* h, const double* c, double* out) {
+  if (!h || !c || !out) return kBadArg;
+  const double* dc;
+  int rc = stage_in(h, c, h->len, h->stage_a, &dc);
+  if (rc) return rc;
+  launch_dot(h->L, h->d, h->cfg.ncomp, dc, dc, h->partial, h->sc, OP_STORE_B, h->red_out);
+  if ((rc = check_launch())) return rc;
+  if ((rc = reduce_to_host(h, out))) return rc;
+  if (std::isnan(*out)) {
+    set_last_error("NaN in the state", __FILE__, __LINE__);
+    return kNanDetected;
+  }
+  return kOk;
 }
 
 int asam_total_scalar(asam_ctx* h, const double* c, int comp, double* out) {

@@ -10,7 +10,9 @@
 // each preconditioner needs).  The tuner times complete refined stage solves
 // of the block's own first stage (its Jacobian and flux RHS at the given
 // state) and keeps the fastest setting, searching one setting at a time
-// (component group, then sweeps, then schedule, then preconditioner).
+// (component group, then sweeps, then schedule, then preconditioner, then
+// the CUDA-graph capture of the iterations; an FP64 context only has the
+// last to choose).
 #include <algorithm>
 #include <vector>
 
@@ -21,7 +23,7 @@ using namespace asam;
 namespace {
 
 struct Setting {
-  int inner_precond, inner_gs_iter, gs_schedule, gs_group;
+  int inner_precond, inner_gs_iter, gs_schedule, gs_group, graphs;
 };
 
 void apply(asam_ctx* h, const Setting& s) {
@@ -29,10 +31,13 @@ void apply(asam_ctx* h, const Setting& s) {
   h->cfg.inner_gs_iter = s.inner_gs_iter;
   h->cfg.gs_schedule = s.gs_schedule;
   h->cfg.gs_group = s.gs_group;
+  h->use_graphs = s.graphs != 0;
 }
 
 int install(asam_ctx* h, const Setting& s) {
   apply(h, s);
+  graphs_reset(h);
+  if (h->cfg.precision != ASAM_PREC_FP32_REFINED) return kOk;
   if (s.inner_precond == 0 && s.gs_schedule == 0) return gs_schedule_init(h, 1 + s.inner_gs_iter);
   gs_schedule_free(h);
   return kOk;
@@ -65,15 +70,9 @@ int time_solve(asam_ctx* h, const double* rhs, double* x, cudaEvent_t e0, cudaEv
 
 extern "C" int asam_autotune(asam_ctx* h, const double* c, double dt, int* choice, double* best_ms) {
   if (!h || !c || !choice) return kBadArg;
-  const Setting start{h->cfg.inner_precond, h->cfg.inner_gs_iter, h->cfg.gs_schedule, h->cfg.gs_group};
-  if (h->cfg.precision != ASAM_PREC_FP32_REFINED) {  // the FP64 path has nothing to choose
-    choice[0] = start.inner_precond;
-    choice[1] = start.inner_gs_iter;
-    choice[2] = start.gs_schedule;
-    choice[3] = start.gs_group;
-    if (best_ms) *best_ms = 0.0;
-    return kOk;
-  }
+  const Setting start{h->cfg.inner_precond, h->cfg.inner_gs_iter, h->cfg.gs_schedule, h->cfg.gs_group,
+                      h->use_graphs ? 1 : 0};
+  const bool refined = h->cfg.precision == ASAM_PREC_FP32_REFINED;
   const Launch& L = h->L;
   const double* dc;
   int rc = stage_in(h, c, h->len, h->stage_a, &dc);
@@ -96,9 +95,12 @@ extern "C" int asam_autotune(asam_ctx* h, const double* c, double dt, int* choic
     }
   } ev{e0, e1};
   Setting best = start;
-  best.inner_precond = 0;
-  best.gs_schedule = 0;
-  if (best.gs_group <= 0) best.gs_group = 5;
+  if (refined) {
+    best.inner_precond = 0;
+    best.gs_schedule = 0;
+    if (best.gs_group <= 0) best.gs_group = 5;
+  }
+  best.graphs = 1;
   double best_t = 1e30;
   auto trial = [&](const Setting& s) -> int {
     int r = install(h, s);
@@ -112,8 +114,14 @@ extern "C" int asam_autotune(asam_ctx* h, const double* c, double dt, int* choic
     return kOk;
   };
   const int nc = h->cfg.ncomp;
+  if (!refined) {  // the FP64 path: only the graph capture of its iterations to choose
+    if ((rc = trial(best))) return rc;
+    Setting s = best;
+    s.graphs = 0;
+    if ((rc = trial(s))) return rc;
+  }
   // 1. components per CTA
-  {
+  if (refined) {
     std::vector<int> groups;
     for (int g : {1, 2, 4, 5, 8, nc})
       if (g >= 1 && g <= nc && g <= 16 && std::find(groups.begin(), groups.end(), g) == groups.end())
@@ -125,7 +133,7 @@ extern "C" int asam_autotune(asam_ctx* h, const double* c, double dt, int* choic
     }
   }
   // 2. inner sweeps
-  {
+  if (refined) {
     Setting s = best;
     for (int it : {0, 1, 2, 3}) {
       if (it == best.inner_gs_iter) continue;
@@ -134,24 +142,31 @@ extern "C" int asam_autotune(asam_ctx* h, const double* c, double dt, int* choic
     }
   }
   // 3. schedule
-  {
+  if (refined) {
     Setting s = best;
     s.gs_schedule = 1;
     if ((rc = trial(s))) return rc;
   }
   // 4. preconditioner: the line solves along z, x and y
-  {
+  if (refined) {
     Setting s = best;
     for (int p : {1, 2, 3}) {
       s.inner_precond = p;
       if ((rc = trial(s))) return rc;
     }
   }
+  // 5. graph capture of the iterations
+  if (refined) {
+    Setting s = best;
+    s.graphs = 0;
+    if ((rc = trial(s))) return rc;
+  }
   if ((rc = install(h, best))) return rc;
   choice[0] = best.inner_precond;
   choice[1] = best.inner_gs_iter;
   choice[2] = best.gs_schedule;
   choice[3] = best.gs_group;
+  choice[4] = best.graphs;
   if (best_ms) *best_ms = best_t;
   return check_launch();
 }

@@ -215,6 +215,8 @@ def adjoint_cost(a, lib, torch, stream):
     """
     import ctypes as C
 
+    import numpy as np
+
     import asam_gb300
     from asam_gb300 import _lib
     from asam_gb300 import geometry as G
@@ -257,11 +259,24 @@ def adjoint_cost(a, lib, torch, stream):
         _lib.check(lib.asam_ros_step_adj(blk.h, p(c0), comp, p(lam), p(lam_out), a.dt, tol), "asam_ros_step_adj",
                    allow=(0, 1))
 
+    uf, vf, wf = (np.ascontiguousarray(v, dtype=np.float64) for v in vel)
+    gr = torch.empty(npad, dtype=torch.float64, device="cuda")
+    gu = torch.empty(uf.size, dtype=torch.float64, device="cuda")
+    gv = torch.empty(vf.size, dtype=torch.float64, device="cuda")
+    gw = torch.empty(wf.size, dtype=torch.float64, device="cuda")
+
+    def wind_gradient(nsteps):
+        _lib.check(lib.asam_tracer_wind_gradient(blk.h, p(c0), comp, nsteps, a.dt, a.adj_ckpt, box, tol, C.byref(J),
+                                                 p(grad), p(gr), p(gu), p(gv), p(gw)), "asam_tracer_wind_gradient",
+                   allow=(0, 1))
+
     fwd()
     cur.copy_(c0)
     ms_fwd = time_region(torch, stream, fwd, a.adj_steps)
     gradient(a.adj_ckpt)
     ms_grad = time_region(torch, stream, lambda: gradient(a.adj_steps), 1)
+    wind_gradient(a.adj_ckpt)
+    ms_wgrad = time_region(torch, stream, lambda: wind_gradient(a.adj_steps), 1)
     cur.copy_(c0)
     ms_fwd1 = time_region(torch, stream, fwd, 3) / 3
     adj_step()
@@ -271,11 +286,15 @@ def adjoint_cost(a, lib, torch, stream):
                         f"(Rho, Rho*theta, Rho*tracer), RosRK3 dt={a.dt}s, {a.adj_steps} steps, checkpoint every "
                         f"{a.adj_ckpt}, J over a 16x16x8 box, BiCGStab tol {tol:g}",
             "forward_ms": ms_fwd, "gradient_ms": ms_grad, "gradient_over_forward": ms_grad / ms_fwd,
+            "tracer_and_wind_gradient_ms": ms_wgrad, "tracer_and_wind_gradient_over_forward": ms_wgrad / ms_fwd,
             "forward_step_ms": ms_fwd1, "adjoint_step_ms": ms_adj1,
             "adjoint_step_over_forward_step": ms_adj1 / ms_fwd1,
             "note": "adjoint step = asam_ros_step_adj: the step's forward recomputation with stage states plus its "
                     "transpose; gradient = forward sweep with checkpoints + per step one recomputation, the stage "
-                    "matrix rebuild and the adjoint step", "J": J.value}
+                    "matrix rebuild and the adjoint step (tracer only, density and wind fixed); tracer-and-wind "
+                    "gradient = the coupled density-tracer adjoint with the face mass fluxes as parameters (one "
+                    "recomputation per step, the increments of Rho and the tracer stored per segment)",
+            "J": J.value}
 
 
 def batch_members(n, seed=4):
@@ -313,11 +332,12 @@ def batch_bench(a, torch, members):
             b = asam_gb300.TransportBlock(geo, st.c.shape[0], method="RosRK3", bicgstab_tol=a.tol,
                                           bicgstab_maxiter=30, precision=prec, inner_gs_iter=a.inner_gs_iter)
             b.set_velocity(*vel)
-            if prec == "fp32_refined" and not a.no_autotune:  # each member picks its own inner solver
+            if not a.no_autotune:  # each member picks its own solver settings
                 t0 = time.perf_counter()
                 ch = b.autotune(st.c, 2.0)
                 t_tune += time.perf_counter() - t0
-                key = f"{ch['inner_precond']}/iterg{ch['inner_gs_iter']}/{ch['gs_schedule']}/g{ch['gs_group']}"
+                key = (f"{ch['inner_precond']}/iterg{ch['inner_gs_iter']}/{ch['gs_schedule']}/g{ch['gs_group']}"
+                       if prec == "fp32_refined" else "fp64") + ("/graphs" if ch["graphs"] else "")
                 choices[key] = choices.get(key, 0) + 1
             blocks.append(b)
             dev.append(torch.from_numpy(st.c.reshape(-1).copy()).cuda())
@@ -421,7 +441,7 @@ def main():
         blk.set_velocity(*vel)
         blk.set_stream(stream.cuda_stream)
         tuned = None
-        if prec == "fp32_refined" and not a.no_autotune:
+        if not a.no_autotune:
             t0 = time.perf_counter()
             tuned = blk.autotune(st.c, a.dt)
             tuned["tuning_seconds"] = time.perf_counter() - t0
@@ -547,6 +567,7 @@ def main():
         "fp64_fma_peak_gflops_probe": gf.value,
         "kernels_ms": r64["kernels"],
         "krylov_iterations": r64["iters"],
+        "solver_settings": r64["tuned"],
         "clocks": r64["clocks"],
         "gpu_launches": gpu_launches["fp64"],
     }

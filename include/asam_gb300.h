@@ -184,6 +184,19 @@ int asam_ros_step_adj(asam_ctx *ctx, const double *c, int comp, const double *la
  * adjoint step. */
 int asam_tracer_gradient(asam_ctx *ctx, const double *c0, int comp, int nsteps, double dt, int ckpt_every,
                          const int *box, double tol, double *J, double *grad);
+/* The same objective's gradient with respect to the initial component field
+ * (grad_c), the initial density (grad_rho; padded fields) and the steady face
+ * mass fluxes (grad_uf/vf/wf, the extents of asam_set_velocity), with the
+ * density evolving with the wind: the reverse sweep runs the coupled
+ * density-component adjoint (the component's flux depends on the density
+ * through the mixing ratio, the stage matrix on the density and the wind).
+ * Faces with zero velocity are not differentiable (the upwind side switches
+ * there) and get 0.  Cost per step: one forward recomputation (segments are
+ * recorded with the stage increments of Rho and the component) and the
+ * coupled adjoint step. */
+int asam_tracer_wind_gradient(asam_ctx *ctx, const double *c0, int comp, int nsteps, double dt, int ckpt_every,
+                              const int *box, double tol, double *J, double *grad_c, double *grad_rho,
+                              double *grad_uf, double *grad_vf, double *grad_wf);
 
 /* Global mass of one component: TotalScalar (ADVECT/Diagnostic_Mod.f90:13-31). */
 int asam_total_scalar(asam_ctx *ctx, const double *c, int comp, double *out);
@@ -207,6 +220,14 @@ int asam_tri_solve_noalloc(int ncol, int n1, const double *d, const double *u, c
 /* y = T x for the same column batch, MatVecT_1D (MULTI/TriDiagT_Mod.f90:113-133). */
 int asam_tri_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x, double *y);
 
+/* DOT(VecMet,VecMet): the interior dot product of the state with itself over
+ * all components (Dot_VecCell, MODULE/Vector4CellPar_Mod.f90:84-102), which the
+ * reference's driver checks for NaN after every step
+ * (ADVECT/MainProg.f90:975-980); returns ASAM_NAN_DETECTED when it is NaN.
+ * asam_ros_step and the solves return ASAM_NAN_DETECTED as soon as a
+ * residual norm is NaN. */
+int asam_state_dot(asam_ctx *ctx, const double *c, double *out);
+
 /* Batched ensemble (no single reference routine: ASAM advances the blocks of
  * one process in turn, DO ibLoc=1,nbLoc, inside Ros3MetC; here the blocks are
  * independent domains).  A batch groups existing contexts, each with its own
@@ -220,14 +241,14 @@ int asam_tri_matvec(int ncol, int n1, const double *d, const double *u, const do
  * member failed (asam_last_error names it), else NOT_CONVERGED/BREAKDOWN if
  * any member reported it, else OK.  A context may belong to several batches
  * but must not be used elsewhere while a batch call runs. */
-/* No reference counterpart: picks the refined mode's inner-solver settings
- * (inner_precond, inner_gs_iter, gs_schedule, gs_group) for this block by
- * timing complete refined solves of its first Rosenbrock stage at state c
- * (host or device) and step dt, one setting at a time; keeps the fastest in
- * the context and returns it in choice[4] (that order) with its solve time in
- * *best_ms (may be NULL).  The settings change speed only: every candidate
- * solves to the configured tolerance.  FP64 contexts have nothing to choose
- * and return their configuration. */
+/* No reference counterpart: picks the block's solver settings (inner_precond,
+ * inner_gs_iter, gs_schedule, gs_group of the refined mode, and whether the
+ * BiCGStab half-iterations are replayed from CUDA graphs) by timing complete
+ * solves of its first Rosenbrock stage at state c (host or device) and step
+ * dt, one setting at a time; keeps the fastest in the context and returns it
+ * in choice[5] (that order) with its solve time in *best_ms (may be NULL).
+ * The settings change speed only: every candidate solves to the configured
+ * tolerance.  An FP64 context only chooses the graph capture. */
 int asam_autotune(asam_ctx *ctx, const double *c, double dt, int *choice, double *best_ms);
 
 typedef struct asam_batch asam_batch;

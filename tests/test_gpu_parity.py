@@ -321,3 +321,27 @@ def test_corrected_division_matches_ieee(env, span):
     bad = C.c_longlong(-1)
     _lib.check(lib.asam_probe_div(20_000_000, 1000 + span, span, C.byref(bad)), "asam_probe_div")
     assert bad.value == 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
+def test_nan_detected(env, precision):
+    """A NaN in the state stops the step with ASAM_NAN_DETECTED (the reference's
+    driver stops on ISNAN(DOT(VecMet,VecMet))); the context stays usable."""
+    asam, _ = env
+    from asam_gb300 import _lib
+
+    name = "hill_24x20x16"
+    geo, vel, st = cases.get(name)
+    with _block(env, name, method="RosRK3", bicgstab_tol=1e-10, precision=precision) as blk:
+        bad = st.c.copy()
+        bad[-1, 5, 6, 7] = np.nan
+        with pytest.raises(_lib.AsamError) as err:
+            blk.state_dot(bad)
+        assert err.value.status == 3
+        with pytest.raises(_lib.AsamError) as err:
+            blk.Ros3MetC(bad, 2.0)
+        assert err.value.status == 3
+        good = st.c.copy()
+        blk.Ros3MetC(good, 2.0)
+        assert np.isfinite(good).all()
+        assert blk.state_dot(good) > 0
