@@ -34,6 +34,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = {
     "k64.cu": ["-fmad=false"],
     "k32.cu": [],
+    "k64fma.cu": [],
     "capi.cu": [],
     "tri_noalloc.cu": ["-fmad=false"],
     "adjoint.cu": ["-fmad=false"],

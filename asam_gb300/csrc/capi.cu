@@ -209,9 +209,11 @@ int read_scalars(asam_ctx* h) {
     set_last_error("persistent Gauss-Seidel schedule: a dependency wait gave up", __FILE__, __LINE__);
     return kCudaError;
   }
-  // a NaN in the residual norms means a NaN in the system (the reference's
-  // driver stops on ISNAN(DOT(VecMet,VecMet)), ADVECT/MainProg.f90:975-980)
-  if (std::isnan(h->sc_host->rnorm) || std::isnan(h->sc_host->rnorm0)) {
+  // a NaN in the residual norms of a running iteration means a NaN in the
+  // system (the reference's driver stops on ISNAN(DOT(VecMet,VecMet)),
+  // ADVECT/MainProg.f90:975-980); after a breakdown (rho = 0, done = 3) the
+  // norms are 0/0 by construction and the breakdown exit is taken instead
+  if (std::isnan(h->sc_host->rnorm0) || (h->sc_host->done != 3 && std::isnan(h->sc_host->rnorm))) {
     set_last_error("NaN in the stage system", __FILE__, __LINE__);
     return kNanDetected;
   }
@@ -487,17 +489,20 @@ int bicgstab_refined(asam_ctx* h, double* x, const double* b, int* maxiter, doub
   int total_inner = 0;
   const int max_outer = 8;
   for (int outer = 0; outer < max_outer; ++outer) {
-    launch_convert_f64_to_f32(L, len, r, h->b32);
+    // the inner system is A d = r/|r| (unit scale in FP32); x += |r| d
+    launch_convert_f64_to_f32_scaled(L, len, r, 1.0 / rnorm, h->b32);
     CK(cudaMemsetAsync(h->x32, 0, len * sizeof(float), L.stream));
     int it = h->cfg.bicgstab_maxiter;
     double tin = 0.5 * target / rnorm;
     if (tin < 1e-6) tin = 1e-6;
     if (tin > 1e-2) tin = 1e-2;
     rc = bicgstab_dev<float>(h, h->val32, h->x32, h->b32, &it, &tin, h->w32, true);
-    if (rc != kOk && rc != kNotConverged) return rc;
+    // an inner breakdown or iteration limit still leaves a usable correction:
+    // the outer FP64 residual decides
+    if (rc != kOk && rc != kNotConverged && rc != kBreakdown) return rc;
     total_inner += it < 0 ? -it : (it > h->cfg.bicgstab_maxiter ? it / 2 : it);
-    launch_add_f32_to_f64(L, len, h->x32, x);                                    // x += correction
-    launch_resid_dot(L, d, nc, h->val, x, b, r, h->partial, h->sc, OP_STORE_A, h->red_out);  // r, r.r
+    launch_add_f32_to_f64(L, len, h->x32, rnorm, x);                             // x += |r| * correction
+    asam_fma::launch_resid_dot(L, d, nc, h->val, x, b, r, h->partial, h->sc, OP_STORE_A, h->red_out);  // r, r.r
     double rr = 0;
     rc = reduce_to_host(h, &rr);
     if (rc) return rc;
@@ -519,6 +524,11 @@ int bicgstab_refined(asam_ctx* h, double* x, const double* b, int* maxiter, doub
 
 int fcn_dev(asam_ctx* h, const double* c, double* f) {
   const Launch& L = h->L;
+  if (h->cfg.precision == ASAM_PREC_FP32_REFINED) {  // contracted FP64 (the refined mode's 1e-10 contract)
+    asam_fma::launch_fcn(L, h->d, h->geom(), h->cfg.ncomp, h->cfg.rho_pos, c, h->coef_x, h->coef_y, h->coef_z,
+                         h->mask_x, h->mask_y, h->mask_z, h->phi, h->gx, h->gy, h->gz, h->rvol, f);
+    return check_launch();
+  }
   launch_phi(L, h->d, h->cfg.ncomp, h->cfg.rho_pos, c, h->phi);
   launch_face_flux(L, h->d, h->geom(), h->cfg.ncomp, h->coef_x, h->coef_y, h->coef_z, h->mask_x, h->mask_y,
                    h->mask_z, h->phi, h->gx, h->gy, h->gz);
@@ -528,7 +538,10 @@ int fcn_dev(asam_ctx* h, const double* c, double* f) {
 
 int jac_dev(asam_ctx* h, const double* c, double dt) {
   const double* rho = c + (size_t)h->cfg.rho_pos * h->npad;
-  launch_jac(h->L, h->d, h->geom(), rho, h->beta0 * dt, h->val);
+  if (h->cfg.precision == ASAM_PREC_FP32_REFINED)
+    asam_fma::launch_jac(h->L, h->d, h->geom(), rho, h->beta0 * dt, h->val);
+  else
+    launch_jac(h->L, h->d, h->geom(), rho, h->beta0 * dt, h->val);
   if (h->cfg.precision == ASAM_PREC_FP32_REFINED) launch_convert_f64_to_f32(h->L, 8 * h->npad, h->val, h->val32);
   h->jac_ready = true;
   h->xline_ready = false;

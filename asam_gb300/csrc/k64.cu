@@ -13,10 +13,16 @@ __global__ void k_cvt_f2d(size_t len, const float* __restrict__ x, double* __res
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
     y[q] = (double)x[q];
 }
-// y += x widened to FP64 (the refinement's correction, one pass)
-__global__ void k_add_f2d(size_t len, const float* __restrict__ x, double* __restrict__ y) {
+// y += s * x widened to FP64 (the refinement's correction, one pass)
+__global__ void k_add_f2d(size_t len, const float* __restrict__ x, double s, double* __restrict__ y) {
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
-    y[q] = y[q] + (double)x[q];
+    y[q] = y[q] + s * (double)x[q];
+}
+// y = (float)(s * x): the residual handed to the FP32 inner solver, scaled to
+// unit norm so that neither tiny nor huge residuals leave the FP32 range
+__global__ void k_cvt_d2f_scaled(size_t len, const double* __restrict__ x, double s, float* __restrict__ y) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
+    y[q] = (float)(s * x[q]);
 }
 // slot 7 of the DIA storage: 1/diagonal (IEEE division)
 __global__ void k_recip_diag(size_t n, double* __restrict__ val) {
@@ -43,8 +49,12 @@ void launch_convert_f64_to_f32(const Launch& L, size_t len, const double* x, flo
   k_cvt_d2f<<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, x, y);
   count_launches(1);
 }
-void launch_add_f32_to_f64(const Launch& L, size_t len, const float* x, double* y) {
-  k_add_f2d<<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, x, y);
+void launch_add_f32_to_f64(const Launch& L, size_t len, const float* x, double s, double* y) {
+  k_add_f2d<<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, x, s, y);
+  count_launches(1);
+}
+void launch_convert_f64_to_f32_scaled(const Launch& L, size_t len, const double* x, double s, float* y) {
+  k_cvt_d2f_scaled<<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, x, s, y);
   count_launches(1);
 }
 void launch_resid_dot(const Launch& L, const Dims& d, int ncomp, const double* val, const double* x, const double* b,

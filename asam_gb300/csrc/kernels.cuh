@@ -1148,6 +1148,7 @@ __global__ void __launch_bounds__(32 * xl_warps<T>()) k_xline_solve(Dims d, int 
     xl_store(t2, xc, r0, nr, NX, ch, lane);
     __syncwarp();
   }
+  __threadfence_block();  // the partial solution is re-read by this warp's copies below
   T xnext = (T)0;
   for (int ch = nch - 1; ch >= 0; --ch) {
     xl_load(t0, fw, r0, nr, NX, ch, lane, 0, true, true);

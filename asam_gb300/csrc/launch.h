@@ -54,10 +54,23 @@ void launch_recip_diag(const Launch&, size_t npad, double* val);
 void launch_mass(const Launch&, const Dims&, const double* c, const double* volc, double* partial, double* out);
 void launch_convert_f64_to_f32(const Launch&, size_t len, const double* x, float* y);
 void launch_convert_f32_to_f64(const Launch&, size_t len, const float* x, double* y);
-void launch_add_f32_to_f64(const Launch&, size_t len, const float* x, double* y);
+void launch_add_f32_to_f64(const Launch&, size_t len, const float* x, double s, double* y);
+void launch_convert_f64_to_f32_scaled(const Launch&, size_t len, const double* x, double s, float* y);
 void launch_resid_dot(const Launch&, const Dims&, int ncomp, const double* val, const double* x, const double* b,
                       double* r, double* partial, KrylovScalars* sc, int op, double* out);
 
 constexpr int kRedGrid = 1024;  // number of partial sums of the reductions
 
 }  // namespace asam
+
+// FP64 launchers of the refined mode with FMA contraction (k64fma.cu)
+namespace asam_fma {
+void launch_fcn(const asam::Launch&, const asam::Dims&, const asam::GeomT<double>& g, int ncomp, int rho_pos,
+                const double* c, const double* cx, const double* cy, const double* cz, const unsigned char* mx,
+                const unsigned char* my, const unsigned char* mz, double* phi, double* gx, double* gy, double* gz,
+                const double* rvol, double* f);
+void launch_jac(const asam::Launch&, const asam::Dims&, const asam::GeomT<double>&, const double* rho, double bdt,
+                double* val);
+void launch_resid_dot(const asam::Launch&, const asam::Dims&, int ncomp, const double* val, const double* x,
+                      const double* b, double* r, double* partial, asam::KrylovScalars* sc, int op, double* out);
+}  // namespace asam_fma

@@ -53,7 +53,8 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
     k_jac<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, rho, bdt, val); count_launches(1);                                  \
   }                                                                                                                \
   void launch_matvec(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* x, T* y, int plain) {      \
-    k_matvec<TM, T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, val, x, y, plain); count_launches(1);                    \
+    k_matvec<TM, T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, val, x, y, plain);                    \
+    count_launches(1);                                                                                             \
   }                                                                                                                \
   void launch_gs_sweeps(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* b, T* out, T* work,     \
                         int nsweep, int group) {                                                                   \

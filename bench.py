@@ -362,6 +362,27 @@ def batch_bench(a, torch, members):
     return res
 
 
+# ---------------------------------------------------------------------------
+# replicas (N > 1): one independent block per rank, no data-path collective;
+# the timed region's maximum over ranks and the whole-job aggregate
+# ---------------------------------------------------------------------------
+def reduce_max(dist, x, device):
+    """Maximum of x over the ranks (x itself without a process group)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(world, units_per_rank, steps, ms_max):
+    """Whole-job rate in M units per second: every rank processed units_per_rank
+    per step, the job took the slowest rank's time."""
+    return world * units_per_rank * steps / (ms_max * 1e-3) / 1e6
+
+
 def time_region(torch, stream, fn, n):
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -424,11 +445,7 @@ def main():
             dist.barrier()
 
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(dist, x, "cuda")
 
     results = {}
     gpu_launches = {}
@@ -532,8 +549,8 @@ def main():
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     r64 = results["fp64"]
     ms_step = r64["ms"] / a.steps
-    value = world * ncell * a.steps / (r64["ms"] * 1e-3) / 1e6
-    e2e = world * ncell * a.steps / (r64["ms_e2e"] * 1e-3) / 1e6
+    value = aggregate_rate(world, ncell, a.steps, r64["ms"])
+    e2e = aggregate_rate(world, ncell, a.steps, r64["ms_e2e"])
     npad = (a.nx + 2) * (a.ny + 2) * (a.nz + 2)
     nsweep = 6
     # dominant kernel of the FP64 step: the Gauss-Seidel wavefront (one PSolve call =
