@@ -110,10 +110,11 @@ class TransportBlock:
             raise ValueError(f"state must have {self.ncomp}*npad elements")
         return a
 
-    def set_graphs(self, on: bool):
-        """Capture the BiCGStab half-iterations as CUDA graphs (default) or launch
-        every kernel individually; the results are the same."""
-        check(self.lib.asam_set_graphs(self.h, int(bool(on))), "asam_set_graphs")
+    def set_graphs(self, mode):
+        """0/False: launch every kernel; 1/True (default): replay the BiCGStab
+        half-iterations from CUDA graphs; 2: FP64 steps as one device-driven
+        graph (WHILE nodes for the Krylov loops).  The results are the same."""
+        check(self.lib.asam_set_graphs(self.h, int(mode)), "asam_set_graphs")
 
     def set_stream(self, stream_handle: int | None):
         """cudaStream_t as an integer; 0/None selects the legacy default stream."""

@@ -40,6 +40,7 @@ UNITS = {
     "adjoint.cu": ["-fmad=false"],
     "batch.cu": [],
     "tune.cu": [],
+    "step_graph.cu": ["-fmad=false"],
 }
 
 

@@ -92,6 +92,11 @@ struct KrylovScalars {
   int done;       // 0 running; 1 converged at half step; 2 converged; 3 breakdown
   int iter;
   int gs_err;     // set by the persistent Gauss-Seidel schedule when a wait gave up
+  // device-driven iteration (CUDA-graph WHILE loop): limit and the reference's
+  // MaxIter/Tol outputs, written by the loop's condition kernel
+  int maxiter;
+  int out_iters;
+  double out_tol;
 };
 
 // Schedule of the persistent Gauss-Seidel wavefront (k_gs_persist): tickets

@@ -318,6 +318,7 @@ void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w) {
 // captured the second time, and is replayed from then on.  The bodies touch
 // only the context's own buffers; the caller's x is updated outside them.
 void graphs_reset(asam_ctx* h) {
+  step_graph_free(h);
   for (auto& kg : h->kg) {
     for (int q = 0; q < 3; ++q) {
       if (kg.exec[q]) cudaGraphExecDestroy(kg.exec[q]);
@@ -555,6 +556,8 @@ int solve_dev(asam_ctx* h, double* x, const double* b, int* maxiter, double* tol
 
 // Ros3MetC + StageRos, transport part (ADVECT/Int_Mod.f90:263-374, 1059-1122).
 int ros_step_dev(asam_ctx* h, double* c, double dt, int* iters, double* resid) {
+  if (h->step_graphs && h->cfg.precision == ASAM_PREC_FP64 && h->L.stream != nullptr)
+    return ros_step_graph(h, c, dt, iters, resid);  // the whole step as one device-driven graph
   const Launch& L = h->L;
   const Dims& d = h->d;
   const int nc = h->cfg.ncomp;
@@ -767,6 +770,10 @@ int asam_destroy(asam_ctx* h) {
   free_work(h->w64);
   free_work(h->w32);
   gs_schedule_free(h);  // and the graphs
+  for (auto st : h->cap_stream)
+    if (st) cudaStreamDestroy(st);
+  if (h->stage_sc) cudaFree(h->stage_sc);
+  if (h->stage_sc_host) cudaFreeHost(h->stage_sc_host);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return kOk;
@@ -862,9 +869,10 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
 }
 
 int asam_set_graphs(asam_ctx* h, int on) {
-  if (!h) return kBadArg;
+  if (!h || on < 0 || on > 2) return kBadArg;
   graphs_reset(h);
   h->use_graphs = on != 0;
+  h->step_graphs = on == 2;
   return kOk;
 }
 

@@ -75,6 +75,16 @@ struct asam_ctx {
   bool jac_ready = false;
   KrylovGraphs kg[2];     // [0] FP64, [1] FP32 inner solver
   bool use_graphs = true;  // capture the half-iterations (when the stream allows it)
+  // device-driven whole-step graphs (FP64): every BiCGStab loop is a graph
+  // WHILE node, so a Rosenbrock step is one graph launch and one host read
+  bool step_graphs = false;
+  cudaGraphExec_t step_exec = nullptr;
+  const double* step_c = nullptr;  // state, step and tolerance the graph was captured for
+  double step_dt = 0.0, step_tol = 0.0;
+  long long step_n_fixed = 0, step_n_h1 = 0, step_n_h2 = 0;  // kernels outside / per pass of the loops
+  cudaStream_t cap_stream[2] = {nullptr, nullptr};  // capture streams of the loop bodies
+  KrylovScalars* stage_sc = nullptr;                // scalars of each stage's solve (4)
+  KrylovScalars* stage_sc_host = nullptr;
   // x-line factors of the FP32 inner line solve (w and 1/den per cell), valid
   // for the current stage matrix while xline_ready is set
   float *xl_w = nullptr, *xl_r = nullptr;
@@ -112,6 +122,8 @@ int stage_out_end(asam_ctx* h, double* p, size_t n, double* dev);
 int gs_schedule_init(asam_ctx* h, int nsweep);
 void gs_schedule_free(asam_ctx* h);
 void graphs_reset(asam_ctx* h);
+int ros_step_graph(asam_ctx* h, double* c, double dt, int* iters, double* resid);
+void step_graph_free(asam_ctx* h);
 long long thread_launches();
 
 }  // namespace asam

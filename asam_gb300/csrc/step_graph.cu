@@ -1,0 +1,309 @@
+// Device-driven Rosenbrock step (FP64): the whole step -- stages, Jacobian,
+// flux RHS and every BiCGStab solve -- is one CUDA graph, and the BiCGStab
+// iteration loop is a graph WHILE node whose condition a kernel sets from the
+// device-resident Krylov scalars (converged, broken down, or the iteration
+// limit reached: the loop always ends).  The second half of an iteration is an
+// IF node that runs only while nothing has ended the solve.  The host launches
+// the step once and reads the per-stage MaxIter/Tol outputs once.
+//
+// The kernels and their order are those of the host-driven solver
+// (bicgstab_dev, capi.cu), so the results are bit-identical; only the exit
+// decisions move from the host to a condition kernel.
+#include <cmath>
+
+#include "context.h"
+#include "kernels.cuh"
+
+using namespace asam;
+
+namespace {
+
+__global__ void k_ks_init(KrylovScalars* sc, double tol, int maxiter) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  KrylovScalars z = {};
+  z.tol = tol;
+  z.maxiter = maxiter;
+  *sc = z;
+}
+
+// p = r on the first iteration, else beta = (rho/rho_old)*(alpha/omega) and
+// p = beta*(p - omega*v) + r (the operations of k_beta + k_pupdate)
+__global__ void k_pupdate_auto(size_t len, KrylovScalars* sc, const double* __restrict__ r,
+                               const double* __restrict__ v, double* __restrict__ p) {
+  const bool first = sc->iter == 0;
+  const double be = (sc->rho / sc->rho_old) * (sc->alpha / sc->omega);
+  const double mo = -sc->omega;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x) {
+    if (first) {
+      p[q] = r[q];
+    } else {
+      double pp = p[q];
+      if (mo != 0.0) pp = mo * v[q] + pp;
+      p[q] = be * pp + r[q];
+    }
+  }
+}
+
+// the half-step exit's update x += alpha*ph, when the first half converged
+__global__ void k_xupdate_half(size_t len, const KrylovScalars* sc, const double* __restrict__ ph,
+                               double* __restrict__ x) {
+  if (sc->done != 1) return;
+  const double al = sc->alpha;
+  if (al == 0.0) return;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
+    x[q] = al * ph[q] + x[q];
+}
+
+__global__ void k_cond_running(cudaGraphConditionalHandle hnd, const KrylovScalars* sc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(hnd, sc->done == 0 ? 1u : 0u);
+}
+
+// end of an iteration: count it, write the reference's outputs, continue?
+__global__ void k_cond_next(cudaGraphConditionalHandle hnd, KrylovScalars* sc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int it = sc->iter + 1;
+  sc->iter = it;
+  const int done = sc->done;
+  if (done == 1) {
+    sc->out_iters = -it;
+    sc->out_tol = sc->rnorm;
+  } else if (done == 2) {
+    sc->out_iters = it;
+    sc->out_tol = sc->rnorm;
+  } else if (done == 3) {
+    sc->out_iters = it;
+    sc->out_tol = 0.0;
+  } else {
+    sc->out_iters = 2 * it;  // the limit's sentinel, replaced if the loop goes on
+    sc->out_tol = sc->rnorm;
+  }
+  cudaGraphSetConditional(hnd, (done == 0 && it < sc->maxiter) ? 1u : 0u);
+}
+
+constexpr int kB = 256;
+inline int grid_of(const Launch& L, size_t n) {
+  size_t g = (n + kB - 1) / kB, cap = (size_t)L.sm_count * 16;
+  return (int)(g > cap ? cap : (g < 1 ? 1 : g));
+}
+
+// A conditional handle of the graph being captured on stream s.
+int make_handle(cudaStream_t s, unsigned dflt, cudaGraphConditionalHandle* hnd) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr));
+  if (st != cudaStreamCaptureStatusActive || !g) return kCudaError;
+  CK(cudaGraphConditionalHandleCreate(hnd, g, dflt, cudaGraphCondAssignDefault));
+  return kOk;
+}
+
+// Adds a conditional node with handle hnd after the current capture position of
+// stream s and starts capturing its body on stream body_s.
+int begin_conditional(cudaStream_t s, cudaStream_t body_s, cudaGraphConditionalNodeType type,
+                      cudaGraphConditionalHandle hnd) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &ndeps));
+  if (st != cudaStreamCaptureStatusActive || !g) return kCudaError;
+  cudaGraphNodeParams prm = {};
+  prm.type = cudaGraphNodeTypeConditional;
+  prm.conditional.handle = hnd;
+  prm.conditional.type = type;
+  prm.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &prm));
+  cudaGraph_t body = prm.conditional.phGraph_out[0];
+  CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  CK(cudaStreamBeginCaptureToGraph(body_s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  return kOk;
+}
+
+int end_conditional(cudaStream_t body_s) {
+  cudaGraph_t body = nullptr;
+  CK(cudaStreamEndCapture(body_s, &body));
+  return kOk;
+}
+
+// kernels per pass of the loop body (first half) and of the IF body (second
+// half), counted while recording, to report how many kernels a step launched
+struct BodyCounts {
+  long long h1 = 0, h2 = 0;
+};
+
+// Records one device-driven BiCGStab solve of A x = b (x = 0 on entry) into
+// the capture of h->L.stream; its outputs land in h->sc.  The bodies are
+// recorded on the context's two capture streams (h->L.stream is switched to
+// them while their kernels are emitted).
+int record_solve(asam_ctx* h, double* x, const double* b, int maxiter, double tol, BodyCounts* bc) {
+  const Dims& d = h->d;
+  const int nc = h->cfg.ncomp;
+  const size_t len = h->len;
+  Work<double>& w = h->w64;
+  const double* val = h->val;
+  const cudaStream_t s0 = h->L.stream, s1 = h->cap_stream[0], s2 = h->cap_stream[1];
+  k_ks_init<<<1, 1, 0, s0>>>(h->sc, tol, maxiter);
+  count_launches(1);
+  CK(cudaMemcpyAsync(w.r, b, len * sizeof(double), cudaMemcpyDeviceToDevice, s0));
+  CK(cudaMemcpyAsync(w.rt, w.r, len * sizeof(double), cudaMemcpyDeviceToDevice, s0));
+  launch_dot(h->L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM0, nullptr);
+  // WHILE: one iteration per pass; the host-driven solver always enters it
+  cudaGraphConditionalHandle wh, ih;
+  int rc;
+  if ((rc = make_handle(s0, 1u, &wh)) || (rc = begin_conditional(s0, s1, cudaGraphCondTypeWhile, wh))) return rc;
+  h->L.stream = s1;
+  const long long n1 = thread_launches();
+  launch_dot(h->L, d, nc, w.rt, w.r, h->partial, h->sc, OP_RHO, nullptr);
+  k_pupdate_auto<<<grid_of(h->L, len), kB, 0, s1>>>(len, h->sc, w.r, w.v, w.p);
+  count_launches(1);
+  psolve_dev<double>(h, val, w.p, w.ph, w);
+  launch_matvec(h->L, d, nc, val, w.ph, w.v, 0);
+  launch_dot(h->L, d, nc, w.rt, w.v, h->partial, h->sc, OP_ALPHA, nullptr);
+  launch_axpy_sc(h->L, len, h->sc, SEL_ALPHA, -1.0, w.v, w.r);
+  launch_dot(h->L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM_HALF, nullptr);
+  k_xupdate_half<<<grid_of(h->L, len), kB, 0, s1>>>(len, h->sc, w.ph, x);
+  count_launches(1);
+  // IF nothing ended the solve: the second half
+  if ((rc = make_handle(s1, 0u, &ih))) return rc;
+  k_cond_running<<<1, 1, 0, s1>>>(ih, h->sc);
+  count_launches(1);
+  if ((rc = begin_conditional(s1, s2, cudaGraphCondTypeIf, ih))) return rc;
+  h->L.stream = s2;
+  const long long n2 = thread_launches();
+  psolve_dev<double>(h, val, w.r, w.rh, w);
+  launch_matvec(h->L, d, nc, val, w.rh, w.t, 0);
+  launch_dot(h->L, d, nc, w.t, w.r, h->partial, h->sc, OP_STORE_A, nullptr);
+  launch_dot(h->L, d, nc, w.t, w.t, h->partial, h->sc, OP_OMEGA, nullptr);
+  launch_axpy_sc(h->L, len, h->sc, SEL_OMEGA, -1.0, w.t, w.r);
+  launch_dot(h->L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM_FULL, nullptr);
+  launch_xupdate(h->L, len, h->sc, 1, w.ph, w.rh, x);
+  bc->h2 = thread_launches() - n2;
+  if ((rc = end_conditional(s2))) return rc;
+  h->L.stream = s1;
+  k_cond_next<<<1, 1, 0, s1>>>(wh, h->sc);
+  count_launches(1);
+  bc->h1 = thread_launches() - n1 - bc->h2;
+  if ((rc = end_conditional(s1))) return rc;
+  h->L.stream = s0;
+  return check_launch();
+}
+
+// Records the whole step (ros_step_dev's operations with device-driven solves).
+int record_step(asam_ctx* h, double* c, double dt, BodyCounts* bc) {
+  const Launch& L = h->L;
+  const Dims& d = h->d;
+  const int nc = h->cfg.ncomp;
+  const size_t len = h->len;
+  CK(cudaMemcpyAsync(h->cold, c, len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+  for (int is = 0; is < h->nstage; ++is) {
+    launch_exchange_cell(L, d, nc, c);
+    int rc;
+    if (is == 0 && (rc = jac_dev(h, c, dt))) return rc;
+    if ((rc = fcn_dev(h, c, h->rhs))) return rc;
+    launch_scale_host(L, len, dt, h->rhs);
+    for (int js = 0; js < is; ++js) launch_axpy_host(L, len, h->beta[is * 4 + js], h->incr + (size_t)js * len, h->rhs);
+    double* x = h->incr + (size_t)is * len;
+    CK(cudaMemsetAsync(x, 0, len * sizeof(double), L.stream));
+    if ((rc = record_solve(h, x, h->rhs, h->cfg.bicgstab_maxiter, h->cfg.bicgstab_tol, bc))) return rc;
+    CK(cudaMemcpyAsync(h->stage_sc + is, h->sc, sizeof(KrylovScalars), cudaMemcpyDeviceToDevice, L.stream));
+    launch_exchange_cell(L, d, nc, x);
+    launch_exchange_cell(L, d, nc, x);
+    CK(cudaMemcpyAsync(c, h->cold, len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
+    for (int js = 0; js <= is; ++js) launch_axpy_host(L, len, h->alpha[is * 4 + js], h->incr + (size_t)js * len, c);
+  }
+  return check_launch();
+}
+
+// after a failed recording: end the captures still open on the body streams
+void abandon_bodies(asam_ctx* h) {
+  for (cudaStream_t s : h->cap_stream) {
+    cudaStreamCaptureStatus st;
+    if (s && cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(s, &g);
+    }
+  }
+  cudaGetLastError();
+}
+
+}  // namespace
+
+namespace asam {
+
+void step_graph_free(asam_ctx* h) {
+  if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
+  h->step_exec = nullptr;
+  h->step_c = nullptr;
+}
+
+// One Rosenbrock step as one graph launch (captured on first use for this
+// state pointer, step size and tolerance); the per-stage BiCGStab outputs are
+// read once.
+int ros_step_graph(asam_ctx* h, double* c, double dt, int* iters, double* resid) {
+  if (!h->stage_sc) {
+    CK(cudaMalloc((void**)&h->stage_sc, 4 * sizeof(KrylovScalars)));
+    CK(cudaMallocHost((void**)&h->stage_sc_host, 4 * sizeof(KrylovScalars)));
+    for (auto& s : h->cap_stream) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  }
+  const cudaStream_t s0 = h->L.stream;
+  if (!h->step_exec || h->step_c != c || h->step_dt != dt || h->step_tol != h->cfg.bicgstab_tol) {
+    step_graph_free(h);
+    const long long t0 = thread_launches();
+    CK(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+    BodyCounts bc;
+    const int rc = record_step(h, c, dt, &bc);
+    h->L.stream = s0;
+    if (rc) abandon_bodies(h);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s0, &g);
+    const long long nrec = thread_launches() - t0;
+    count_launches(-nrec);  // recorded, not run
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    h->step_n_h1 = bc.h1;
+    h->step_n_h2 = bc.h2;
+    h->step_n_fixed = nrec - h->nstage * (bc.h1 + bc.h2);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&h->step_exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      h->step_exec = nullptr;
+      set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+      return kCudaError;
+    }
+    h->step_c = c;
+    h->step_dt = dt;
+    h->step_tol = h->cfg.bicgstab_tol;
+  }
+  CK(cudaGraphLaunch(h->step_exec, s0));
+  CK(cudaMemcpyAsync(h->stage_sc_host, h->stage_sc, h->nstage * sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s0));
+  CK(cudaStreamSynchronize(s0));
+  int status = kOk;
+  long long ran = h->step_n_fixed;  // kernels the graph ran: fixed part + loop passes
+  for (int is = 0; is < h->nstage; ++is) {
+    const KrylovScalars& k = h->stage_sc_host[is];
+    const int passes = k.iter;                                           // first halves
+    const int seconds = (k.done == 1 || k.done == 3) ? passes - 1 : passes;  // second halves
+    ran += passes * h->step_n_h1 + (seconds > 0 ? seconds : 0) * h->step_n_h2;
+    if (k.gs_err) {
+      set_last_error("persistent Gauss-Seidel schedule: a dependency wait gave up", __FILE__, __LINE__);
+      return kCudaError;
+    }
+    if (std::isnan(k.rnorm0) || (k.done != 3 && std::isnan(k.rnorm))) {
+      set_last_error("NaN in the stage system", __FILE__, __LINE__);
+      return kNanDetected;
+    }
+    if (iters) iters[is] = k.out_iters;
+    if (resid) resid[is] = k.out_tol;
+    int st = kOk;
+    if (k.done == 3 && k.rnorm0 > 0.0) st = kBreakdown;
+    if (k.done == 0) st = kNotConverged;
+    if (st != kOk && status == kOk) status = st;
+  }
+  count_launches(ran);
+  const int rc = check_launch();
+  return rc ? rc : status;
+}
+
+}  // namespace asam

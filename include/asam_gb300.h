@@ -84,10 +84,16 @@ int asam_create(const asam_config *cfg, const double *volc, const double *fu, co
                 asam_ctx **out);
 int asam_destroy(asam_ctx *ctx);
 
-/* No reference counterpart: capture of the BiCGStab half-iterations as CUDA
- * graphs, replayed on later iterations and solves (on by default; results are
- * identical either way; never on the legacy default stream, which cannot be
- * captured).  on = 0 launches every kernel individually. */
+/* No reference counterpart: how the Krylov iterations are launched (results
+ * are identical in every mode; graphs are never used on the legacy default
+ * stream, which cannot be captured):
+ *   0 every kernel launched individually, the host takes the exit decisions;
+ *   1 (default) the BiCGStab half-iterations are captured as CUDA graphs and
+ *     replayed, the host takes the exit decisions;
+ *   2 FP64 contexts: the whole Rosenbrock step is one CUDA graph in which each
+ *     BiCGStab loop is a graph WHILE node driven by a condition kernel
+ *     (bounded by MaxIter), so a step is one launch and one host read;
+ *     refined contexts behave as 1. */
 int asam_set_graphs(asam_ctx *ctx, int on);
 
 /* Run the context's work on this CUDA stream (cudaStream_t); NULL = the legacy

@@ -219,20 +219,21 @@ def test_inner_line_psolve_fp32(env, name, precond, axis):
 @pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
 @pytest.mark.parametrize("name", ["hill_24x20x16", "flat_walls_9x6x5"])
 def test_graph_captured_iterations_identical(env, name, precision):
-    """BiCGStab half-iterations replayed from CUDA graphs give the bits of the
-    individually launched kernels, over several steps (capture on the second
-    use of each half, replays after)."""
+    """BiCGStab half-iterations replayed from CUDA graphs, and (FP64) whole steps
+    run as one graph whose Krylov loops are WHILE nodes, give the bits and the
+    iteration counts of the individually launched kernels, over several steps."""
     geo, vel, st = cases.get(name)
     out = {}
-    for graphs in (True, False):
+    for mode in (1, 0, 2):  # 2: the whole FP64 step as one graph with WHILE/IF nodes
         c = st.c.copy()
         with _block(env, name, method="RosRK3", bicgstab_tol=1e-12, precision=precision,
                     inner_precond="xline" if precision == "fp32_refined" else "gauss_seidel") as blk:
-            blk.set_graphs(graphs)
+            blk.set_graphs(mode)
             its = [blk.Ros3MetC(c, 3.0)[0] for _ in range(4)]
-        out[graphs] = (c, its)
-    assert np.array_equal(out[True][0], out[False][0])
-    assert out[True][1] == out[False][1]
+        out[mode] = (c, its)
+    for mode in (1, 2):
+        assert np.array_equal(out[mode][0], out[0][0]), mode
+        assert out[mode][1] == out[0][1], (mode, out[mode][1], out[0][1])
 
 
 @pytest.mark.parametrize("name", ["hill_24x20x16", "hill_odd_13x7x9_reverse"])
