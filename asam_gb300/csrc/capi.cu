@@ -540,9 +540,9 @@ int fcn_dev(asam_ctx* h, const double* c, double* f) {
 int jac_dev(asam_ctx* h, const double* c, double dt) {
   const double* rho = c + (size_t)h->cfg.rho_pos * h->npad;
   if (h->cfg.precision == ASAM_PREC_FP32_REFINED)
-    asam_fma::launch_jac(h->L, h->d, h->geom(), rho, h->beta0 * dt, h->val);
+    asam_fma::launch_jac(h->L, h->d, h->geom(), rho, h->rvol, h->beta0 * dt, h->val);
   else
-    launch_jac(h->L, h->d, h->geom(), rho, h->beta0 * dt, h->val);
+    launch_jac(h->L, h->d, h->geom(), rho, h->rvol, h->beta0 * dt, h->val);
   if (h->cfg.precision == ASAM_PREC_FP32_REFINED) launch_convert_f64_to_f32(h->L, 8 * h->npad, h->val, h->val32);
   h->jac_ready = true;
   h->xline_ready = false;

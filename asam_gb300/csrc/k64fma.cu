@@ -24,8 +24,9 @@ void launch_fcn(const Launch& L, const Dims& d, const GeomT<double>& g, int ncom
   count_launches(5);
 }
 
-void launch_jac(const Launch& L, const Dims& d, const GeomT<double>& g, const double* rho, double bdt, double* val) {
-  k_jac<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, rho, bdt, val);
+void launch_jac(const Launch& L, const Dims& d, const GeomT<double>& g, const double* rho, const double* rvol,
+                double bdt, double* val) {
+  k_jac<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, rho, rvol, bdt, val);
   count_launches(1);
 }
 

@@ -385,16 +385,19 @@ __global__ void k_div(Dims d, GeomT<T> g, T* __restrict__ rhs) {
 // cell computing its column of the 7-diagonal matrix in the reference's
 // accumulation order.
 // ---------------------------------------------------------------------------
+// Half*(ABS(u)+/-u)*F/V/(Rho+Eps), both divisions correctly rounded from the
+// precomputed reciprocals of V (= VolC+Eps of that cell: rvol) and of
+// Rho+Eps (one per column), so the result is the reference's expression
 template <typename T>
-__device__ __forceinline__ T jac_term(T vel, bool plus, T F, T Vden, T rho) {
-  // Half*(ABS(u)+/-u)*F/V/(Rho+Eps)
+__device__ __forceinline__ T jac_term(T vel, bool plus, T F, T Vden, T rVden, T rhoe, T rrhoe) {
   const T half = (T)0.5;
   T s = plus ? (fabs(vel) + vel) : (fabs(vel) - vel);
-  return half * s * F / Vden / (rho + eps_t<T>());
+  return div_rn(div_rn(half * s * F, Vden, rVden), rhoe, rrhoe);
 }
 
 template <typename T>
-__global__ void k_jac(Dims d, GeomT<T> g, const T* __restrict__ rho, T bdt, T* __restrict__ val) {
+__global__ void k_jac(Dims d, GeomT<T> g, const T* __restrict__ rho, const T* __restrict__ rvol, T bdt,
+                      T* __restrict__ val) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int NX = d.NX(), NY = d.NY();
   const size_t n = d.npad();
@@ -406,51 +409,52 @@ __global__ void k_jac(Dims d, GeomT<T> g, const T* __restrict__ rho, T bdt, T* _
     const int k = (int)(P / ((size_t)NX * NY));
     const bool ii = i >= 1 && i <= nx, jj = j >= 1 && j <= ny, kk = k >= 1 && k <= nz;
     const T rP = rho[P];
-    const T VP = g.volc[P] + e;
+    const T rPe = rP + e, rrP = (T)1 / rPe;
+    const T VP = g.volc[P] + e, rVP = rvol[P];
     T v[7] = {(T)0, (T)0, (T)0, (T)0, (T)0, (T)0, (T)0};
     // face activity: interior faces, plus boundary faces of periodic sides
     auto actx = [&](int fi) { return jj && kk && fi >= 0 && fi <= nx && ((fi >= 1 && fi <= nx - 1) || d.per_x); };
     auto acty = [&](int fj) { return ii && kk && fj >= 0 && fj <= ny && ((fj >= 1 && fj <= ny - 1) || d.per_y); };
     auto actz = [&](int fk) { return ii && jj && fk >= 0 && fk <= nz && ((fk >= 1 && fk <= nz - 1) || d.per_z); };
     // off-diagonals (each a single term)
-    if (actx(i)) v[2] = v[2] + jac_term(g.uf[d.UF(i, j, k)], true, g.fu[d.FU(i, j, k)], g.volc[P + sx] + e, rP);
+    if (actx(i)) v[2] = v[2] + jac_term(g.uf[d.UF(i, j, k)], true, g.fu[d.FU(i, j, k)], g.volc[P + sx] + e, rvol[P + sx], rPe, rrP);
     if (actx(i - 1))
-      v[4] = v[4] + jac_term(g.uf[d.UF(i - 1, j, k)], false, g.fu[d.FU(i - 1, j, k)], g.volc[P - sx] + e, rP);
-    if (acty(j)) v[1] = v[1] + jac_term(g.vf[d.VF(i, j, k)], true, g.fv[d.FV(i, j, k)], g.volc[P + sy] + e, rP);
+      v[4] = v[4] + jac_term(g.uf[d.UF(i - 1, j, k)], false, g.fu[d.FU(i - 1, j, k)], g.volc[P - sx] + e, rvol[P - sx], rPe, rrP);
+    if (acty(j)) v[1] = v[1] + jac_term(g.vf[d.VF(i, j, k)], true, g.fv[d.FV(i, j, k)], g.volc[P + sy] + e, rvol[P + sy], rPe, rrP);
     if (acty(j - 1))
-      v[5] = v[5] + jac_term(g.vf[d.VF(i, j - 1, k)], false, g.fv[d.FV(i, j - 1, k)], g.volc[P - sy] + e, rP);
-    if (actz(k)) v[0] = v[0] + jac_term(g.wf[d.WF(i, j, k)], true, g.fw[d.FW(i, j, k)], g.volc[P + sz] + e, rP);
+      v[5] = v[5] + jac_term(g.vf[d.VF(i, j - 1, k)], false, g.fv[d.FV(i, j - 1, k)], g.volc[P - sy] + e, rvol[P - sy], rPe, rrP);
+    if (actz(k)) v[0] = v[0] + jac_term(g.wf[d.WF(i, j, k)], true, g.fw[d.FW(i, j, k)], g.volc[P + sz] + e, rvol[P + sz], rPe, rrP);
     if (actz(k - 1))
-      v[6] = v[6] + jac_term(g.wf[d.WF(i, j, k - 1)], false, g.fw[d.FW(i, j, k - 1)], g.volc[P - sz] + e, rP);
+      v[6] = v[6] + jac_term(g.wf[d.WF(i, j, k - 1)], false, g.fw[d.FW(i, j, k - 1)], g.volc[P - sz] + e, rvol[P - sz], rPe, rrP);
     // diagonal: interior loops x, y, z (face left of P then face right of P)
     T dg = (T)0;
     if (jj && kk && i - 1 >= 1 && i - 1 <= nx - 1)
-      dg = dg - jac_term(g.uf[d.UF(i - 1, j, k)], false, g.fu[d.FU(i - 1, j, k)], VP, rP);
-    if (jj && kk && i >= 1 && i <= nx - 1) dg = dg - jac_term(g.uf[d.UF(i, j, k)], true, g.fu[d.FU(i, j, k)], VP, rP);
+      dg = dg - jac_term(g.uf[d.UF(i - 1, j, k)], false, g.fu[d.FU(i - 1, j, k)], VP, rVP, rPe, rrP);
+    if (jj && kk && i >= 1 && i <= nx - 1) dg = dg - jac_term(g.uf[d.UF(i, j, k)], true, g.fu[d.FU(i, j, k)], VP, rVP, rPe, rrP);
     if (ii && kk && j - 1 >= 1 && j - 1 <= ny - 1)
-      dg = dg - jac_term(g.vf[d.VF(i, j - 1, k)], false, g.fv[d.FV(i, j - 1, k)], VP, rP);
-    if (ii && kk && j >= 1 && j <= ny - 1) dg = dg - jac_term(g.vf[d.VF(i, j, k)], true, g.fv[d.FV(i, j, k)], VP, rP);
+      dg = dg - jac_term(g.vf[d.VF(i, j - 1, k)], false, g.fv[d.FV(i, j - 1, k)], VP, rVP, rPe, rrP);
+    if (ii && kk && j >= 1 && j <= ny - 1) dg = dg - jac_term(g.vf[d.VF(i, j, k)], true, g.fv[d.FV(i, j, k)], VP, rVP, rPe, rrP);
     if (ii && jj && k - 1 >= 1 && k - 1 <= nz - 1)
-      dg = dg - jac_term(g.wf[d.WF(i, j, k - 1)], false, g.fw[d.FW(i, j, k - 1)], VP, rP);
-    if (ii && jj && k >= 1 && k <= nz - 1) dg = dg - jac_term(g.wf[d.WF(i, j, k)], true, g.fw[d.FW(i, j, k)], VP, rP);
+      dg = dg - jac_term(g.wf[d.WF(i, j, k - 1)], false, g.fw[d.FW(i, j, k - 1)], VP, rVP, rPe, rrP);
+    if (ii && jj && k >= 1 && k <= nz - 1) dg = dg - jac_term(g.wf[d.WF(i, j, k)], true, g.fw[d.FW(i, j, k)], VP, rVP, rPe, rrP);
     // neighbour branches W, E, S, N, B, T of a periodic block
     if (d.per_x && jj && kk) {
-      if (i == 0) dg = dg - jac_term(g.uf[d.UF(0, j, k)], true, g.fu[d.FU(0, j, k)], VP, rP);
-      if (i == 1) dg = dg - jac_term(g.uf[d.UF(0, j, k)], false, g.fu[d.FU(0, j, k)], VP, rP);
-      if (i == nx) dg = dg - jac_term(g.uf[d.UF(nx, j, k)], true, g.fu[d.FU(nx, j, k)], VP, rP);
-      if (i == nx + 1) dg = dg - jac_term(g.uf[d.UF(nx, j, k)], false, g.fu[d.FU(nx, j, k)], VP, rP);
+      if (i == 0) dg = dg - jac_term(g.uf[d.UF(0, j, k)], true, g.fu[d.FU(0, j, k)], VP, rVP, rPe, rrP);
+      if (i == 1) dg = dg - jac_term(g.uf[d.UF(0, j, k)], false, g.fu[d.FU(0, j, k)], VP, rVP, rPe, rrP);
+      if (i == nx) dg = dg - jac_term(g.uf[d.UF(nx, j, k)], true, g.fu[d.FU(nx, j, k)], VP, rVP, rPe, rrP);
+      if (i == nx + 1) dg = dg - jac_term(g.uf[d.UF(nx, j, k)], false, g.fu[d.FU(nx, j, k)], VP, rVP, rPe, rrP);
     }
     if (d.per_y && ii && kk) {
-      if (j == 0) dg = dg - jac_term(g.vf[d.VF(i, 0, k)], true, g.fv[d.FV(i, 0, k)], VP, rP);
-      if (j == 1) dg = dg - jac_term(g.vf[d.VF(i, 0, k)], false, g.fv[d.FV(i, 0, k)], VP, rP);
-      if (j == ny) dg = dg - jac_term(g.vf[d.VF(i, ny, k)], true, g.fv[d.FV(i, ny, k)], VP, rP);
-      if (j == ny + 1) dg = dg - jac_term(g.vf[d.VF(i, ny, k)], false, g.fv[d.FV(i, ny, k)], VP, rP);
+      if (j == 0) dg = dg - jac_term(g.vf[d.VF(i, 0, k)], true, g.fv[d.FV(i, 0, k)], VP, rVP, rPe, rrP);
+      if (j == 1) dg = dg - jac_term(g.vf[d.VF(i, 0, k)], false, g.fv[d.FV(i, 0, k)], VP, rVP, rPe, rrP);
+      if (j == ny) dg = dg - jac_term(g.vf[d.VF(i, ny, k)], true, g.fv[d.FV(i, ny, k)], VP, rVP, rPe, rrP);
+      if (j == ny + 1) dg = dg - jac_term(g.vf[d.VF(i, ny, k)], false, g.fv[d.FV(i, ny, k)], VP, rVP, rPe, rrP);
     }
     if (d.per_z && ii && jj) {
-      if (k == 0) dg = dg - jac_term(g.wf[d.WF(i, j, 0)], true, g.fw[d.FW(i, j, 0)], VP, rP);
-      if (k == 1) dg = dg - jac_term(g.wf[d.WF(i, j, 0)], false, g.fw[d.FW(i, j, 0)], VP, rP);
-      if (k == nz) dg = dg - jac_term(g.wf[d.WF(i, j, nz)], true, g.fw[d.FW(i, j, nz)], VP, rP);
-      if (k == nz + 1) dg = dg - jac_term(g.wf[d.WF(i, j, nz)], false, g.fw[d.FW(i, j, nz)], VP, rP);
+      if (k == 0) dg = dg - jac_term(g.wf[d.WF(i, j, 0)], true, g.fw[d.FW(i, j, 0)], VP, rVP, rPe, rrP);
+      if (k == 1) dg = dg - jac_term(g.wf[d.WF(i, j, 0)], false, g.fw[d.FW(i, j, 0)], VP, rVP, rPe, rrP);
+      if (k == nz) dg = dg - jac_term(g.wf[d.WF(i, j, nz)], true, g.fw[d.FW(i, j, nz)], VP, rVP, rPe, rrP);
+      if (k == nz + 1) dg = dg - jac_term(g.wf[d.WF(i, j, nz)], false, g.fw[d.FW(i, j, nz)], VP, rVP, rPe, rrP);
     }
     // JacScaleCompute fold of the face-halo rows (:1791-1856)
     if (jj && kk && i == 0) dg = dg - v[2];

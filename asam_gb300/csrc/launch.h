@@ -22,7 +22,7 @@ struct Launch {
                           const T* gz, const T* rvol, T* f);                                                     \
   void launch_recip_eps(const Launch&, size_t len, const T* v, T* rv);                                          \
   void launch_div(const Launch&, const Dims&, const GeomT<T>&, T* rhs);                                          \
-  void launch_jac(const Launch&, const Dims&, const GeomT<T>&, const T* rho, T bdt, T* val);                     \
+  void launch_jac(const Launch&, const Dims&, const GeomT<T>&, const T* rho, const T* rvol, T bdt, T* val);     \
   void launch_matvec(const Launch&, const Dims&, int ncomp, const TM* val, const T* x, T* y, int plain_spmv);    \
   void launch_gs_sweeps(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, T* out, T* work,       \
                         int nsweep, int group);                                                                  \
@@ -69,8 +69,8 @@ void launch_fcn(const asam::Launch&, const asam::Dims&, const asam::GeomT<double
                 const double* c, const double* cx, const double* cy, const double* cz, const unsigned char* mx,
                 const unsigned char* my, const unsigned char* mz, double* phi, double* gx, double* gy, double* gz,
                 const double* rvol, double* f);
-void launch_jac(const asam::Launch&, const asam::Dims&, const asam::GeomT<double>&, const double* rho, double bdt,
-                double* val);
+void launch_jac(const asam::Launch&, const asam::Dims&, const asam::GeomT<double>&, const double* rho,
+                const double* rvol, double bdt, double* val);
 void launch_resid_dot(const asam::Launch&, const asam::Dims&, int ncomp, const double* val, const double* x,
                       const double* b, double* r, double* partial, asam::KrylovScalars* sc, int op, double* out);
 }  // namespace asam_fma

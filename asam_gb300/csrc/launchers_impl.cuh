@@ -49,8 +49,9 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
   void launch_div(const Launch& L, const Dims& d, const GeomT<T>& g, T* rhs) {                                     \
     k_div<T><<<gs_grid(L, (size_t)d.nx * d.ny * d.nz), kBlock, 0, L.stream>>>(d, g, rhs); count_launches(1);                          \
   }                                                                                                                \
-  void launch_jac(const Launch& L, const Dims& d, const GeomT<T>& g, const T* rho, T bdt, T* val) {                \
-    k_jac<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, rho, bdt, val); count_launches(1);                                  \
+  void launch_jac(const Launch& L, const Dims& d, const GeomT<T>& g, const T* rho, const T* rvol, T bdt,         \
+                  T* val) {                                                                                        \
+    k_jac<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, rho, rvol, bdt, val); count_launches(1);       \
   }                                                                                                                \
   void launch_matvec(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* x, T* y, int plain) {      \
     k_matvec<TM, T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, val, x, y, plain);                    \
