@@ -14,6 +14,12 @@ the C-ABI in ``include/asam_gb300.h``.  Method names follow the reference:
 ``Ros3MetC``           ADVECT/Int_Mod.f90:1059 (fixed dt)
 ``TotalScalar``        ADVECT/Diagnostic_Mod.f90:13
 ``ExchangeCell``       MODULE/Vector4CellPar_Mod.f90:752
+``JacAccGrav``         pressure-Laplacian hierarchy, LaplTFullCompute
+                       (MULTI/JacAccGrav_Mod.f90:1056)
+``MatVecP``            MULTI/JacAccGrav_Mod.f90:531 (MatVecP_Tri)
+``VCycleCG``           MULTI/JacAccGrav_Mod.f90:4466 (one Solve_3D)
+``SolveSound``         SOLU/Iter_Mod.f90:9 (FGMRES, MatVec1, PSolve1)
+``ProjectVelFace``     ADVECT/IntSub_Mod.f90:25
 ``Solve_1D``           MULTI/TriDiagT_Mod.f90:135 (batched over columns)
 ``MatVecT_1D``         MULTI/TriDiagT_Mod.f90:113 (batched over columns)
 =====================  =======================================================
@@ -29,7 +35,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import ASAM_BREAKDOWN, ASAM_NOT_CONVERGED, ASAM_OK, AsamConfig, AsamError, check, ptr
+from ._lib import ASAM_BREAKDOWN, ASAM_NOT_CONVERGED, ASAM_OK, AsamConfig, AsamError, AsamProjConfig, check, ptr
 
 METHODS = {"Ros3AMF": 0, "RosRK32": 1, "RosEul": 2, "Ros3P": 3, "Ros3Pw": 4, "RosRK3": 5, "RosTVD": 6,
            "RosRK4": 7}
@@ -240,6 +246,89 @@ class TransportBlock:
         out = C.c_double()
         check(self.lib.asam_total_scalar(self.h, ptr(a), int(comp), C.byref(out)), "asam_total_scalar")
         return out.value
+
+    # ---- pressure projection (closed blocks) -------------------------------
+    def proj_setup(self, dx, dy, dz, metr=None, ref_level: int = 4, gauss_iter2: int = 1, gauss_iter3: int = 1,
+                   mult_iter2: int = 1, mult_iter3: int = 1, step_gmres: int = 10, max_restart: int = 10,
+                   tol: float = 1e-6, fac_anela: float = 1.0):
+        """Projection set-up: cell widths dx[nx], dy[ny], dz[nz]; metr the six
+        metric arrays MetrXY, MetrXZ, MetrYX, MetrYZ, MetrZX, MetrZY back to
+        back (None: Cartesian).  Defaults are Control_Mod's."""
+        g = self.grid
+        self._pdx, self._pdy, self._pdz = _f64(dx), _f64(dy), _f64(dz)
+        if self._pdx.size != g.nx or self._pdy.size != g.ny or self._pdz.size != g.nz:
+            raise ValueError("dx, dy, dz must have nx, ny, nz entries")
+        self._pmetr = None if metr is None else _f64(metr)
+        if self._pmetr is not None and self._pmetr.size != 2 * (g.nx + g.ny + g.nz):
+            raise ValueError("metr must hold 2*(nx+ny+nz) values")
+        self.pcfg = AsamProjConfig(ref_level, gauss_iter2, gauss_iter3, mult_iter2, mult_iter3, step_gmres, max_restart,
+                                   tol, fac_anela)
+        check(self.lib.asam_proj_setup(self.h, C.byref(self.pcfg), ptr(self._pdx), ptr(self._pdy), ptr(self._pdz),
+                                       None if self._pmetr is None else ptr(self._pmetr)), "asam_proj_setup")
+
+    def proj_weights(self, dtu, dtv, dtw, duu, duv, duw, dut, dtt):
+        """Sound weights (WeightDiagCompute): face arrays with uF/vF/wF extents,
+        DUT and DTT interior (nz, ny, nx)."""
+        arrs = [_f64(a) for a in (dtu, dtv, dtw, duu, duv, duw, dut, dtt)]
+        check(self.lib.asam_proj_weights(self.h, *[ptr(a) for a in arrs]), "asam_proj_weights")
+
+    def JacAccGrav(self, beta0: float, dtp: float):
+        """Assemble the tridiagonal pressure-Laplacian hierarchy (LaplTFullCompute)."""
+        check(self.lib.asam_lapl_compute(self.h, float(beta0), float(dtp)), "asam_lapl_compute")
+
+    def lapl_array(self, level3: int, level2: int, which: int) -> np.ndarray:
+        """One assembled array in the reversed order (see asam_lapl_get)."""
+        n = self.lib.asam_lapl_get(self.h, level3, level2, which, None)
+        if n < 0:
+            raise ValueError("no such level/array")
+        out = np.empty(n)
+        if self.lib.asam_lapl_get(self.h, level3, level2, which, ptr(out)) != n:
+            raise AsamError(4, "asam_lapl_get")
+        return out
+
+    def MatVecP(self, x) -> np.ndarray:
+        a = _f64(x)
+        y = np.empty_like(a)
+        check(self.lib.asam_lapl_matvec(self.h, ptr(a), ptr(y)), "asam_lapl_matvec")
+        return y
+
+    def VCycleCG(self, b) -> np.ndarray:
+        a = _f64(b)
+        x = np.empty_like(a)
+        check(self.lib.asam_lapl_vcycle(self.h, ptr(a), ptr(x)), "asam_lapl_vcycle")
+        return x
+
+    def SolveSound(self, x: np.ndarray, b, MaxIter: int | None = None, Tol: float | None = None):
+        """FGMRES on the pressure, x updated in place; returns (inner steps,
+        relative residual estimate)."""
+        if not (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous):
+            raise TypeError("x must be a C-contiguous float64 array (updated in place)")
+        bb = _f64(b)
+        it = C.c_int(int(self.pcfg.max_restart if MaxIter is None else MaxIter))
+        tol = C.c_double(float(self.pcfg.tol if Tol is None else Tol))
+        st = self.lib.asam_solve_sound(self.h, ptr(x), ptr(bb), C.byref(it), C.byref(tol))
+        check(st, "asam_solve_sound", allow=(ASAM_OK, ASAM_NOT_CONVERGED))
+        return it.value, tol.value
+
+    def ProjectVelFace(self, uf: np.ndarray, vf: np.ndarray, wf: np.ndarray, incr: np.ndarray, state=None,
+                       th_pos: int = -1, rho_pos: int = -1, scalars=()):
+        """Project the face-velocity increments uf/vf/wf (updated in place) and
+        update the cell increments incr (in place).  Returns (pressure,
+        inner steps, relative residual)."""
+        for a in (uf, vf, wf, incr):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+                raise TypeError("uf, vf, wf, incr must be C-contiguous float64 arrays (updated in place)")
+        st_arr = None if state is None else self._state(state)
+        sc = (C.c_int * max(1, len(scalars)))(*scalars)
+        g = self.grid
+        p = np.empty((g.nz, g.ny, g.nx))
+        steps = C.c_int()
+        res = C.c_double()
+        st = self.lib.asam_project_vel_face(self.h, ptr(uf), ptr(vf), ptr(wf), ptr(incr),
+                                            None if st_arr is None else ptr(st_arr), int(th_pos), int(rho_pos), sc,
+                                            len(scalars), ptr(p), C.byref(steps), C.byref(res))
+        check(st, "asam_project_vel_face", allow=(ASAM_OK, ASAM_NOT_CONVERGED))
+        return p, steps.value, res.value
 
 
 class Batch:

@@ -36,6 +36,14 @@ class AsamConfig(C.Structure):
     ]
 
 
+class AsamProjConfig(C.Structure):
+    _fields_ = [
+        ("ref_level", C.c_int), ("gauss_iter2", C.c_int), ("gauss_iter3", C.c_int),
+        ("mult_iter2", C.c_int), ("mult_iter3", C.c_int), ("step_gmres", C.c_int),
+        ("max_restart", C.c_int), ("tol", C.c_double), ("fac_anela", C.c_double),
+    ]
+
+
 # (name, restype, argtypes) of every exported entry point of include/asam_gb300.h
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
@@ -72,6 +80,15 @@ SIGNATURES = [
     ("asam_tri_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
+    ("asam_proj_setup", C.c_int, [_V, C.POINTER(AsamProjConfig), _V, _V, _V, _V]),
+    ("asam_proj_weights", C.c_int, [_V, _V, _V, _V, _V, _V, _V, _V, _V]),
+    ("asam_lapl_compute", C.c_int, [_V, C.c_double, C.c_double]),
+    ("asam_lapl_get", C.c_long, [_V, C.c_int, C.c_int, C.c_int, _V]),
+    ("asam_lapl_matvec", C.c_int, [_V, _V, _V]),
+    ("asam_lapl_vcycle", C.c_int, [_V, _V, _V]),
+    ("asam_solve_sound", C.c_int, [_V, _V, _V, _I, _D]),
+    ("asam_project_vel_face", C.c_int, [_V, _V, _V, _V, _V, _V, C.c_int, C.c_int, _I, C.c_int, _V, _I, _D]),
+    ("asam_proj_vcycles", C.c_longlong, [_V]),
     ("asam_ros_coeffs", C.c_int, [C.c_int, _D, _D, _D, _D]),
     ("asam_autotune", C.c_int, [_V, _V, C.c_double, _I, _D]),
     ("asam_state_dot", C.c_int, [_V, _V, _D]),

@@ -8,9 +8,11 @@ linked into ``asam_gb300/libasam_gb300.so``:
 * ``capi.cu`` context, drivers and the ``extern "C"`` entry points
 * ``tri_noalloc.cu`` the column solve that allocates nothing
 * ``adjoint.cu`` tangent-linear and adjoint of the transport stage
+* ``proj.cu`` pressure projection: Laplacian hierarchy, multigrid, FGMRES
 
-The oracle (``oracle/asam_oracle.c``) is a test-only checker compiled by gcc
-into ``oracle/_build/libasam_oracle.so``.
+The oracle (``oracle/asam_oracle.c`` for the transport stage,
+``oracle/asam_proj.c`` for the pressure projection) is a test-only checker
+compiled by gcc into ``oracle/_build/libasam_oracle.so``.
 """
 from __future__ import annotations
 
@@ -27,7 +29,7 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libasam_gb300.so"
-ORACLE_SRC = ROOT / "oracle" / "asam_oracle.c"
+ORACLE_SRC = [ROOT / "oracle" / "asam_oracle.c", ROOT / "oracle" / "asam_proj.c"]
 ORACLE_LIB = ROOT / "oracle" / "_build" / "libasam_oracle.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -41,6 +43,7 @@ UNITS = {
     "batch.cu": [],
     "tune.cu": [],
     "step_graph.cu": ["-fmad=false"],
+    "proj.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
 }
 
 
@@ -96,12 +99,12 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
 
 def build_oracle(force: bool = False) -> Path:
     """Compile the CPU oracle (test infrastructure) with gcc."""
-    if not force and not _stale(ORACLE_LIB, [ORACLE_SRC]):
+    if not force and not _stale(ORACLE_LIB, ORACLE_SRC):
         return ORACLE_LIB
     ORACLE_LIB.parent.mkdir(exist_ok=True)
     tmp = ORACLE_LIB.with_suffix(".so.tmp")
     cmd = ["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-           str(ORACLE_SRC), "-o", str(tmp), "-lm"]
+           *map(str, ORACLE_SRC), "-o", str(tmp), "-lm"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"gcc failed for the oracle:\n{res.stderr}")

@@ -269,8 +269,8 @@ int gs_schedule_init(asam_ctx* h, int nsweep) {
   CK(cudaMalloc((void**)&h->gs_flags, h->gs_nflags * sizeof(int)));
   CK(cudaMalloc((void**)&h->gs_counter, 2 * sizeof(int)));
   CK(cudaMemcpy(h->gs_order, order.data(), order.size() * sizeof(int4), cudaMemcpyHostToDevice));
-  CK(cudaMemset(h->gs_flags, 0, h->gs_nflags * sizeof(int)));
-  CK(cudaMemset(h->gs_counter, 0, 2 * sizeof(int)));
+  CK(cudaMemsetAsync(h->gs_flags, 0, h->gs_nflags * sizeof(int), h->L.stream));
+  CK(cudaMemsetAsync(h->gs_counter, 0, 2 * sizeof(int), h->L.stream));
   return kOk;
 }
 
@@ -770,6 +770,7 @@ int asam_destroy(asam_ctx* h) {
   free_work(h->w64);
   free_work(h->w32);
   gs_schedule_free(h);  // and the graphs
+  proj_free(h);
   for (auto st : h->cap_stream)
     if (st) cudaStreamDestroy(st);
   if (h->stage_sc) cudaFree(h->stage_sc);
@@ -858,8 +859,8 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
   double* zero[] = {h->uf, h->vf, h->wf};
   size_t nz[] = {d.n_uf(), d.n_vf(), d.n_wf()};
   for (int q = 0; q < 3; ++q)
-    if ((e = cudaMemset(zero[q], 0, nz[q] * sizeof(double))) != cudaSuccess) return fail(e);
-  if ((e = cudaMemset(h->c, 0, h->len * sizeof(double))) != cudaSuccess) return fail(e);
+    if ((e = cudaMemsetAsync(zero[q], 0, nz[q] * sizeof(double), h->L.stream)) != cudaSuccess) return fail(e);
+  if ((e = cudaMemsetAsync(h->c, 0, h->len * sizeof(double), h->L.stream)) != cudaSuccess) return fail(e);
   launch_recip_eps(h->L, h->npad, h->volc, h->rvol);
   launch_face_coef(h->L, d, h->geom(), h->coef_x, h->coef_y, h->coef_z, h->mask_x, h->mask_y, h->mask_z);
   if ((e = cudaStreamSynchronize(h->L.stream)) != cudaSuccess) return fail(e);

@@ -30,6 +30,8 @@ inline void free_work(Work<T>& w) {
   w = Work<T>();
 }
 
+struct ProjState;
+
 }  // namespace asam
 
 // CUDA graphs of the BiCGStab half-iterations of one precision
@@ -96,6 +98,8 @@ struct asam_ctx {
   size_t gs_nflags = 0;
   int* gs_counter = nullptr;  // [0] ticket counter; [1] epoch base (unsigned)
 
+  asam::ProjState* proj = nullptr;  // pressure projection (proj.cu), set up on demand
+
   GeomT<double> geom() const { return GeomT<double>{volc, fu, fv, fw, uf, vf, wf}; }
 };
 
@@ -125,6 +129,7 @@ void graphs_reset(asam_ctx* h);
 int ros_step_graph(asam_ctx* h, double* c, double dt, int* iters, double* resid);
 void step_graph_free(asam_ctx* h);
 long long thread_launches();
+void proj_free(asam_ctx* h);
 
 }  // namespace asam
 

@@ -1,0 +1,1522 @@
+// Pressure projection (sound solve) of one block on the device:
+//   * assembly of the tridiagonal pressure-Laplacian hierarchy
+//     (MULTI/JacAccGrav_Mod.f90:1056-1310 LaplTFullCompute with the
+//     coarsening helpers :709-903 and MULTI/TriDiagT_Mod.f90 ComputeFull_1D/2D/3D),
+//   * its operator MatVecT_3D (TriDiagT_Mod.f90:885-917, MatVecP_Tri),
+//   * the semi-coarsening multigrid V-cycle Solve_3D (TriDiagT_Mod.f90:1009-1085)
+//     with plane -> x-line -> z-column (Thomas) relaxation,
+//   * FGMRES(StepGMRES) with MatVec1/PSolve1 (SOLU/Iter_Mod.f90:121-199,
+//     MATRIX/MatVec_Mod.f90:184-258, MATRIX/PreCond_Mod.f90:1555-1571),
+//   * Rhs/DivergenceS and UpdateVelocity (MATRIX/Rhs_Mod.f90:41-78, 110-187, 589-952).
+//
+// Scope: a block whose six sides are outer boundaries without boundary
+// pressure unknowns (closed box); the PressureVelocity vector is then the
+// pressure alone, SetFactorN gives 0 boundary factors, the Schur step of
+// PSolve1 leaves the pressure unchanged and PSolve1 reduces to
+// PressurePre(-x) (the first PressurePre of PSolve1 only feeds the face
+// unknowns, so it is not run).
+//
+// Data layout.  The hierarchy lives in the reference's reversed index space
+// (n1,n2,n3) = (z,x,y) (MULTI/Reverse_Mod.f90 with xOrder=2,yOrder=3,zOrder=1).
+// A level with c1 rows (z), c2 lines (x) and m3 planes (y) stores entry
+// (i,j,k) at k*ps + i*w + (j&1)*h + (j>>1), h = ceil(c2/2), w = 2h, ps = c1*w:
+// within a plane row the even lines come first, then the odd ones, so the
+// threads that relax the lines of one parity read consecutive addresses.
+//
+// Smoother ordering.  The reference relaxes planes and lines in lexicographic
+// order, a chain with no parallelism.  Here planes (then lines inside a plane)
+// of one parity are relaxed concurrently -- the zebra ordering of the same
+// smoother: every plane right-hand side, line right-hand side and Thomas solve
+// uses the reference's arithmetic and operation order; only the order of the
+// relaxations differs.  One CTA owns one plane and runs that plane's whole 2D
+// multigrid with block barriers, so a half-sweep over all planes of one
+// parity is a single launch.  FP64 without FMA contraction (-fmad=false);
+// divisions by the Thomas pivots use the correctly rounded div_rn with
+// precomputed reciprocals, so every value equals the oracle's zebra run bit
+// for bit.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "context.h"
+#include "kernels.cuh"
+
+namespace asam {
+
+namespace prj {
+
+constexpr int kMaxLev = 8;
+constexpr int kPlaneBlock = 256;
+constexpr int kRedGrid = 1024;
+constexpr int kRedBlock = 256;
+constexpr double kTiny = 1.0e-40;  // initial diagonal of Allocate_1D (TriDiagT_Mod.f90:99)
+
+struct Lev2 {
+  int c1, c2, h, w, m3;
+  size_t ps;
+  double *d, *uz, *lz, *fw, *ft, *frt, *ux, *lx, *res;
+  double *x, *b;  // own vectors of the coarse plane levels (nullptr on the 3D level's own planes)
+};
+
+struct Lev3 {
+  int m1, m2, m3, nl;
+  Lev2 pl[kMaxLev];
+  double *u3, *l3, *x, *b, *res, *t;
+};
+
+// Input fields of one level in the natural reversed layout (1-based logical
+// indices): F1(0:n1,1:n2,1:n3), F2(1:n1,0:n2,1:n3), F3(1:n1,1:n2,0:n3),
+// cell arrays (1:n1,1:n2,1:n3).
+struct Fields {
+  int n1, n2, n3;
+  double *F1, *T1, *U1, *F2, *T2, *U2, *F3, *T3, *U3, *vol, *dut;
+  double *d1, *d2, *d3, *m12, *m13, *m21, *m23, *m31, *m32;
+  __host__ __device__ size_t i1(int i, int j, int k) const {
+    return (size_t)i + (size_t)(n1 + 1) * ((size_t)(j - 1) + (size_t)n2 * (size_t)(k - 1));
+  }
+  __host__ __device__ size_t i2(int i, int j, int k) const {
+    return (size_t)(i - 1) + (size_t)n1 * ((size_t)j + (size_t)(n2 + 1) * (size_t)(k - 1));
+  }
+  __host__ __device__ size_t i3(int i, int j, int k) const {
+    return (size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * (size_t)k);
+  }
+  __host__ __device__ size_t ic(int i, int j, int k) const {
+    return (size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * (size_t)(k - 1));
+  }
+};
+
+struct Facs {
+  double f1l, f1r, f2l, f2r, f3l, f3r;
+};
+
+__host__ __device__ inline size_t slot(int w, int h, int i, int j) {
+  return (size_t)i * w + (size_t)(j & 1) * h + (size_t)(j >> 1);
+}
+
+// line index j of a padded position pos in a plane row (-1: padding)
+__device__ inline int line_of(int pos, int h, int c2) {
+  const int j = pos < h ? 2 * pos : 2 * (pos - h) + 1;
+  return j < c2 ? j : -1;
+}
+
+// ---------------------------------------------------------------------------
+// Assembly
+// ---------------------------------------------------------------------------
+
+// ReverseWeight / Reverse of the fine fields (Reverse_Mod.f90:330-360, 565-575)
+__global__ void k_fine_fields(Dims d, const double* __restrict__ fu, const double* __restrict__ fv,
+                              const double* __restrict__ fw, const double* __restrict__ volc,
+                              const double* __restrict__ dtu, const double* __restrict__ dtv,
+                              const double* __restrict__ dtw, const double* __restrict__ duu,
+                              const double* __restrict__ duv, const double* __restrict__ duw,
+                              const double* __restrict__ dut, Fields g) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const size_t n = (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(e % (nx + 1));
+    const size_t r = e / (nx + 1);
+    const int y = (int)(r % (ny + 1));
+    const int z = (int)(r / (ny + 1));
+    if (x >= 1 && y >= 1) {  // F1 = FW(x,y,z), z = 0..nz
+      const size_t q = g.i1(z, x, y);
+      g.F1[q] = fw[d.FW(x, y, z)];
+      g.T1[q] = dtw[d.WF(x, y, z)];
+      g.U1[q] = duw[d.WF(x, y, z)];
+    }
+    if (y >= 1 && z >= 1) {  // F2 = FU(x,y,z), x = 0..nx
+      const size_t q = g.i2(z, x, y);
+      g.F2[q] = fu[d.FU(x, y, z)];
+      g.T2[q] = dtu[d.UF(x, y, z)];
+      g.U2[q] = duu[d.UF(x, y, z)];
+    }
+    if (x >= 1 && z >= 1) {  // F3 = FV(x,y,z), y = 0..ny
+      const size_t q = g.i3(z, x, y);
+      g.F3[q] = fv[d.FV(x, y, z)];
+      g.T3[q] = dtv[d.VF(x, y, z)];
+      g.U3[q] = duv[d.VF(x, y, z)];
+    }
+    if (x >= 1 && y >= 1 && z >= 1) {
+      const size_t q = g.ic(z, x, y);
+      g.vol[q] = volc[d.P(x, y, z)];
+      g.dut[q] = dut[(size_t)(x - 1) + (size_t)nx * ((size_t)(y - 1) + (size_t)ny * (size_t)(z - 1))];
+    }
+  }
+}
+
+// ReverseIncr / ReverseMetr (Reverse_Mod.f90:362-541): d1=dz, d2=dx, d3=dy,
+// Metr12=MetrZX, Metr13=MetrZY, Metr21=MetrXZ, Metr23=MetrXY, Metr31=MetrYZ, Metr32=MetrYX
+__global__ void k_fine_1d(int nx, int ny, int nz, const double* dx, const double* dy, const double* dz,
+                          const double* metr, Fields g) {
+  const double* mxy = metr;
+  const double* mxz = metr + ny;
+  const double* myx = metr + ny + nz;
+  const double* myz = metr + ny + nz + nx;
+  const double* mzx = metr + ny + 2 * nz + nx;
+  const double* mzy = metr + ny + 2 * nz + 2 * nx;
+  for (int q = threadIdx.x; q < nz; q += blockDim.x) {
+    g.d1[q] = dz[q];
+    g.m21[q] = mxz[q];
+    g.m31[q] = myz[q];
+  }
+  for (int q = threadIdx.x; q < nx; q += blockDim.x) {
+    g.d2[q] = dx[q];
+    g.m12[q] = mzx[q];
+    g.m32[q] = myx[q];
+  }
+  for (int q = threadIdx.x; q < ny; q += blockDim.x) {
+    g.d3[q] = dy[q];
+    g.m13[q] = mzy[q];
+    g.m23[q] = mxy[q];
+  }
+}
+
+__device__ inline int blo(int c, int s) { return (c - 1) * (s + 1) + 1; }
+__device__ inline int bhi(int c, int s, int n) { return min(c * (s + 1), n); }
+
+// FaceCoarse + CFaceCoarse (JacAccGrav_Mod.f90:804-903): every coarse face sums
+// its fine faces in the reference's loop order; then the face-weighted DTU
+// and DUU averages.
+__global__ void k_coarse_faces(Fields g, Fields c, int s1, int s2, int s3) {
+  const int n = g.n1, m = g.n2, l = g.n3;
+  const int nC = c.n1, mC = c.n2, lC = c.n3;
+  const size_t n1f = (size_t)(nC + 1) * mC * lC, n2f = (size_t)nC * (mC + 1) * lC, n3f = (size_t)nC * mC * (lC + 1);
+  const size_t tot = n1f + n2f + n3f;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    double F = 0.0, TF = 0.0, UF = 0.0;
+    if (e < n1f) {
+      const int iC = (int)(e % (nC + 1));
+      const size_t r = e / (nC + 1);
+      const int jC = (int)(r % mC) + 1, kC = (int)(r / mC) + 1;
+      const int i = min((s1 + 1) * iC, n);
+      for (int j = blo(jC, s2); j <= bhi(jC, s2, m); ++j)
+        for (int k = blo(kC, s3); k <= bhi(kC, s3, l); ++k) {
+          const size_t q = g.i1(i, j, k);
+          const double f = g.F1[q];
+          F = F + f;
+          TF = TF + g.T1[q] * f;
+          UF = UF + g.U1[q] * f;
+        }
+      const size_t qc = c.i1(iC, jC, kC);
+      c.F1[qc] = F;
+      c.T1[qc] = TF / (F + asam::kEps);
+      c.U1[qc] = UF / (F + asam::kEps);
+    } else if (e < n1f + n2f) {
+      const size_t ee = e - n1f;
+      const int iC = (int)(ee % nC) + 1;
+      const size_t r = ee / nC;
+      const int jC = (int)(r % (mC + 1)), kC = (int)(r / (mC + 1)) + 1;
+      const int j = min((s2 + 1) * jC, m);
+      for (int i = blo(iC, s1); i <= bhi(iC, s1, n); ++i)
+        for (int k = blo(kC, s3); k <= bhi(kC, s3, l); ++k) {
+          const size_t q = g.i2(i, j, k);
+          const double f = g.F2[q];
+          F = F + f;
+          TF = TF + g.T2[q] * f;
+          UF = UF + g.U2[q] * f;
+        }
+      const size_t qc = c.i2(iC, jC, kC);
+      c.F2[qc] = F;
+      c.T2[qc] = TF / (F + asam::kEps);
+      c.U2[qc] = UF / (F + asam::kEps);
+    } else {
+      const size_t ee = e - n1f - n2f;
+      const int iC = (int)(ee % nC) + 1;
+      const size_t r = ee / nC;
+      const int jC = (int)(r % mC) + 1, kC = (int)(r / mC);
+      const int k = min((s3 + 1) * kC, l);
+      for (int i = blo(iC, s1); i <= bhi(iC, s1, n); ++i)
+        for (int j = blo(jC, s2); j <= bhi(jC, s2, m); ++j) {
+          const size_t q = g.i3(i, j, k);
+          const double f = g.F3[q];
+          F = F + f;
+          TF = TF + g.T3[q] * f;
+          UF = UF + g.U3[q] * f;
+        }
+      const size_t qc = c.i3(iC, jC, kC);
+      c.F3[qc] = F;
+      c.T3[qc] = TF / (F + asam::kEps);
+      c.U3[qc] = UF / (F + asam::kEps);
+    }
+  }
+}
+
+// VolCoarse + CVolCoarse (JacAccGrav_Mod.f90:724-745, 784-802)
+__global__ void k_coarse_cells(Fields g, Fields c, int s1, int s2, int s3) {
+  const size_t tot = (size_t)c.n1 * c.n2 * c.n3;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const int iC = (int)(e % c.n1) + 1;
+    const size_t r = e / c.n1;
+    const int jC = (int)(r % c.n2) + 1, kC = (int)(r / c.n2) + 1;
+    double V = 0.0, DV = 0.0;
+    for (int i = blo(iC, s1); i <= bhi(iC, s1, g.n1); ++i)
+      for (int j = blo(jC, s2); j <= bhi(jC, s2, g.n2); ++j)
+        for (int k = blo(kC, s3); k <= bhi(kC, s3, g.n3); ++k) {
+          const size_t q = g.ic(i, j, k);
+          V = V + g.vol[q];
+          DV = DV + g.dut[q] * g.vol[q];
+        }
+    const size_t qc = c.ic(iC, jC, kC);
+    c.vol[qc] = V;
+    c.dut[qc] = DV / (V + asam::kEps);
+  }
+}
+
+// IncrCoarse + CIncrCoarse (JacAccGrav_Mod.f90:747-782), one thread
+__global__ void k_coarse_1d(Fields g, Fields c, int s1, int s2, int s3) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  auto incr = [](const double* d, int n, double* dc, int nc, int s) {
+    for (int i = 0; i < nc; ++i) dc[i] = 0.0;
+    for (int i = 1; i <= n; ++i) dc[(i + s) / (s + 1) - 1] = dc[(i + s) / (s + 1) - 1] + d[i - 1];
+  };
+  auto cincr = [](const double* C, const double* d, int n, double* CC, const double* dc, int nc, int s) {
+    for (int i = 0; i < nc; ++i) CC[i] = 0.0;
+    for (int i = 1; i <= n; ++i) CC[(i + s) / (s + 1) - 1] = CC[(i + s) / (s + 1) - 1] + d[i - 1] * C[i - 1];
+    for (int i = 0; i < nc; ++i) CC[i] = CC[i] / dc[i];
+  };
+  incr(g.d1, g.n1, c.d1, c.n1, s1);
+  incr(g.d2, g.n2, c.d2, c.n2, s2);
+  incr(g.d3, g.n3, c.d3, c.n3, s3);
+  cincr(g.m12, g.d2, g.n2, c.m12, c.d2, c.n2, s2);
+  cincr(g.m13, g.d3, g.n3, c.m13, c.d3, c.n3, s3);
+  cincr(g.m21, g.d1, g.n1, c.m21, c.d1, c.n1, s1);
+  cincr(g.m23, g.d3, g.n3, c.m23, c.d3, c.n3, s3);
+  cincr(g.m31, g.d1, g.n1, c.m31, c.d1, c.n1, s1);
+  cincr(g.m32, g.d2, g.n2, c.m32, c.d2, c.n2, s2);
+}
+
+// ComputeFull_1D/2D/3D (TriDiagT_Mod.f90:62-90, 330-403, 790-883) for every
+// cell of a level: the diagonal accumulates, in the reference's order, 1e-40,
+// the two z terms, FacAnela*Vol, the two x terms and the two y terms; u/l are
+// the negated coupling terms.  full = 1: the 3D level's own planes (y terms
+// without DUU3 except the low boundary term, and the y couplings u3/l3);
+// full = 0: a coarse plane level (DUU3 in every y term).
+__global__ void k_assemble(Fields c, Lev2 P, double* __restrict__ u3, double* __restrict__ l3, int full, double bd2,
+                           Facs fc, double fac_anela) {
+  const int n1 = c.n1, n2 = c.n2, n3 = c.n3;
+  const size_t tot = (size_t)n1 * n2 * n3;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n1) + 1;
+    const size_t r = e / n1;
+    const int j = (int)(r % n2) + 1, k = (int)(r / n2) + 1;
+    const double M1 = c.m12[j - 1], M2 = c.m13[k - 1];
+    const double M21 = c.m21[i - 1], M23 = c.m23[k - 1];
+    const double M31 = c.m31[i - 1], M32 = c.m32[j - 1];
+    auto DUT = [&](int ii, int jj, int kk) { return c.dut[c.ic(ii, jj, kk)]; };
+    // face f (0-based) separates 1-based cells f and f+1
+    auto zt = [&](int f, int cell) {
+      const size_t q = c.i1(f, j, k);
+      return bd2 * 2.0 * c.F1[q] * c.T1[q] * c.U1[q] * DUT(cell, j, k) / ((c.d1[f - 1] + c.d1[f]) * M1 * M2);
+    };
+    auto xt = [&](int f, int col) {
+      const size_t q = c.i2(i, f, k);
+      return bd2 * 2.0 * c.F2[q] * c.T2[q] * c.U2[q] * DUT(i, col, k) / ((c.d2[f - 1] + c.d2[f]) * M21 * M23);
+    };
+    auto yt = [&](int f, int pl, bool with_u) {
+      const size_t q = c.i3(i, j, f);
+      const double den = (c.d3[f - 1] + c.d3[f]) * M31 * M32;
+      return with_u ? bd2 * 2.0 * c.F3[q] * c.T3[q] * c.U3[q] * DUT(i, j, pl) / den
+                    : bd2 * 2.0 * c.F3[q] * c.T3[q] * DUT(i, j, pl) / den;
+    };
+    double dg = kTiny;
+    {
+      const size_t q0 = c.i1(0, j, k), qn = c.i1(n1, j, k);
+      const double fl = bd2 * fc.f1l * c.F1[q0] * c.T1[q0] * c.U1[q0] * DUT(1, j, k) / (c.d1[0] * M1 * M2);
+      const double fr = bd2 * fc.f1r * c.F1[qn] * c.T1[qn] * c.U1[qn] * DUT(n1, j, k) / (c.d1[n1 - 1] * M1 * M2);
+      dg = dg + (i == 1 ? fl : zt(i - 1, i));
+      dg = dg + (i == n1 ? fr : zt(i, i));
+    }
+    dg = dg + fac_anela * c.vol[c.ic(i, j, k)];
+    {
+      const size_t q0 = c.i2(i, 0, k), qn = c.i2(i, n2, k);
+      const double fl = bd2 * fc.f2l * c.F2[q0] * c.T2[q0] * c.U2[q0] * DUT(i, 1, k) / (c.d2[0] * M21 * M23);
+      const double fr = bd2 * fc.f2r * c.F2[qn] * c.T2[qn] * c.U2[qn] * DUT(i, n2, k) / (c.d2[n2 - 1] * M21 * M23);
+      dg = dg + (j == 1 ? fl : xt(j - 1, j));
+      dg = dg + (j == n2 ? fr : xt(j, j));
+    }
+    {
+      const size_t q0 = c.i3(i, j, 0), qn = c.i3(i, j, n3);
+      const double fl = bd2 * fc.f3l * c.F3[q0] * c.T3[q0] * c.U3[q0] * DUT(i, j, 1) / (c.d3[0] * M31 * M32);
+      const double fr = full ? bd2 * fc.f3r * c.F3[qn] * c.T3[qn] * DUT(i, j, n3) / (c.d3[n3 - 1] * M31 * M32)
+                             : bd2 * fc.f3r * c.F3[qn] * c.T3[qn] * c.U3[qn] * DUT(i, j, n3) / (c.d3[n3 - 1] * M31 * M32);
+      dg = dg + (k == 1 ? fl : yt(k - 1, k, !full));
+      dg = dg + (k == n3 ? fr : yt(k, k, !full));
+    }
+    const size_t s = (size_t)(k - 1) * P.ps + slot(P.w, P.h, i - 1, j - 1);
+    P.d[s] = dg;
+    P.uz[s] = i < n1 ? -zt(i, i + 1) : 0.0;
+    P.lz[s] = i < n1 ? -zt(i, i) : 0.0;
+    P.ux[s] = j < n2 ? -xt(j, j + 1) : 0.0;
+    P.lx[s] = j < n2 ? -xt(j, j) : 0.0;
+    if (full) {
+      u3[s] = k < n3 ? -yt(k, k + 1, false) : 0.0;
+      l3[s] = k < n3 ? -yt(k, k, false) : 0.0;
+    }
+  }
+}
+
+// Thomas factors of every column (the t and w of Solve_1D, which depend on
+// the matrix only): ft = t_i, frt = 1/t_i, fw = u_i/t_i
+__global__ void k_factor(Lev2 P) {
+  const size_t ncol = (size_t)P.m3 * P.c2;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < ncol; e += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(e % P.c2), k = (int)(e / P.c2);
+    const size_t base = (size_t)k * P.ps + slot(P.w, P.h, 0, j);
+    double t = P.d[base];
+    P.ft[base] = t;
+    P.frt[base] = 1.0 / t;
+    for (int i = 1; i < P.c1; ++i) {
+      const size_t q = base + (size_t)i * P.w, qm = q - P.w;
+      const double wv = P.uz[qm] / t;
+      P.fw[qm] = wv;
+      t = P.d[q] - P.lz[qm] * wv;
+      P.ft[q] = t;
+      P.frt[q] = 1.0 / t;
+    }
+    P.fw[base + (size_t)(P.c1 - 1) * P.w] = 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Operator and multigrid
+// ---------------------------------------------------------------------------
+
+// MatVecT_2D at entry (i,j) of a plane (TriDiagT_Mod.f90:113-133, 405-431);
+// x is the plane's vector, mo the plane's offset in the matrix arrays
+__device__ inline double matvec2_at(const Lev2& P, size_t mo, const double* __restrict__ x, size_t s, int i, int j) {
+  const int c1 = P.c1, c2 = P.c2, w = P.w;
+  const double* d = P.d + mo;
+  const double* uz = P.uz + mo;
+  const double* lz = P.lz + mo;
+  double y;
+  if (c1 > 1) {
+    if (i == 0)
+      y = d[s] * x[s] + uz[s] * x[s + w];
+    else if (i < c1 - 1)
+      y = lz[s - w] * x[s - w] + d[s] * x[s] + uz[s] * x[s + w];
+    else
+      y = lz[s - w] * x[s - w] + d[s] * x[s];
+  } else {
+    y = d[s] * x[s];
+  }
+  if (c2 > 1) {
+    const size_t row = (size_t)i * w;
+    const double* ux = P.ux + mo;
+    const double* lx = P.lx + mo;
+    if (j == 0) {
+      const size_t sr = row + slot(0, P.h, 0, j + 1);
+      y = y + ux[s] * x[sr];
+    } else if (j < c2 - 1) {
+      const size_t sl = row + slot(0, P.h, 0, j - 1), sr = row + slot(0, P.h, 0, j + 1);
+      y = y + lx[sl] * x[sl] + ux[s] * x[sr];
+    } else {
+      const size_t sl = row + slot(0, P.h, 0, j - 1);
+      y = y + lx[sl] * x[sl];
+    }
+  }
+  return y;
+}
+
+// One zebra half-sweep over the x-lines of parity c of one plane: the line
+// right-hand side in the forward or backward operation order of
+// GaussSeidel_2D, then Solve_1D with the precomputed factors.  Rows are
+// handled in chunks of kChunk: every load of a chunk is issued before its
+// recurrence runs, so a thread keeps several rows of loads in flight.
+constexpr int kChunk = 4;
+
+__device__ __noinline__ void line_half(const Lev2& P, size_t mo, const double* __restrict__ b, double* __restrict__ x, int c,
+                          int fwd) {
+  const int c1 = P.c1, c2 = P.c2, h = P.h, w = P.w;
+  const double* __restrict__ lx = P.lx + mo;
+  const double* __restrict__ ux = P.ux + mo;
+  const double* __restrict__ lz = P.lz + mo;
+  const double* __restrict__ ft = P.ft + mo;
+  const double* __restrict__ frt = P.frt + mo;
+  const double* __restrict__ fw = P.fw + mo;
+  const int nl = (c2 - c + 1) / 2;
+  for (int q = threadIdx.x; q < nl; q += blockDim.x) {
+    const int j = 2 * q + c;
+    const size_t col = (size_t)c * h + q;
+    const bool hasL = j > 0, hasR = j < c2 - 1;
+    const size_t colL = hasL ? (size_t)(1 - c) * h + ((j - 1) >> 1) : col;
+    const size_t colR = hasR ? (size_t)(1 - c) * h + ((j + 1) >> 1) : col;
+    double prev = 0.0;
+    for (int i0 = 0; i0 < c1; i0 += kChunk) {
+      double t[kChunk], l[kChunk], pv[kChunk], rp[kChunk];
+#pragma unroll
+      for (int r = 0; r < kChunk; ++r) {
+        const int i = i0 + r;
+        if (i < c1) {
+          const size_t o = (size_t)i * w;
+          double v = b[col + o];
+          const double xl = x[colL + o], xr = x[colR + o];
+          const double cl = hasL ? lx[colL + o] : 0.0, cr = hasR ? ux[col + o] : 0.0;
+          if (fwd) {
+            if (hasL) v = v - cl * xl;
+            if (hasR) v = v - cr * xr;
+          } else {
+            if (hasR) v = v - cr * xr;
+            if (hasL) v = v - cl * xl;
+          }
+          t[r] = v;
+          l[r] = i > 0 ? lz[col + o - w] : 0.0;
+          pv[r] = ft[col + o];
+          rp[r] = frt[col + o];
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kChunk; ++r) {
+        const int i = i0 + r;
+        if (i < c1) {
+          double v = t[r];
+          if (i > 0) v = v - l[r] * prev;
+          const double y = div_rn(v, pv[r], rp[r]);
+          x[col + (size_t)i * w] = y;
+          prev = y;
+        }
+      }
+    }
+    // back substitution b(i) = b(i) - w(i)*b(i+1), rows c1-2 .. 0
+    for (int i0 = c1 - 2; i0 >= 0; i0 -= kChunk) {
+      double xv[kChunk], wv[kChunk];
+#pragma unroll
+      for (int r = 0; r < kChunk; ++r) {
+        const int i = i0 - r;
+        if (i >= 0) {
+          const size_t o = (size_t)i * w;
+          xv[r] = x[col + o];
+          wv[r] = fw[col + o];
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kChunk; ++r) {
+        const int i = i0 - r;
+        if (i >= 0) {
+          const double v = xv[r] - wv[r] * prev;
+          x[col + (size_t)i * w] = v;
+          prev = v;
+        }
+      }
+    }
+  }
+}
+
+__device__ void gs2d(const Lev2& P, size_t mo, const double* b, double* x, int gi) {
+  if (P.c2 > 1) {
+    for (int it = 0; it < gi; ++it) {
+      line_half(P, mo, b, x, 0, 1);
+      __syncthreads();
+      line_half(P, mo, b, x, 1, 1);
+      __syncthreads();
+      line_half(P, mo, b, x, 1, 0);
+      __syncthreads();
+      line_half(P, mo, b, x, 0, 0);
+      __syncthreads();
+    }
+  } else {
+    line_half(P, mo, b, x, 0, 1);
+    __syncthreads();
+  }
+}
+
+// Multigrid_2D (TriDiagT_Mod.f90:490-551) on plane k of a 3D level, inside one CTA
+__device__ void mg2d(const Lev3& A, int k, double* x0, const double* b0, int gi2) {
+  const int nl = A.nl;
+  int gi = 1;
+  int lv = 0;
+  for (;;) {
+    const Lev2& P = A.pl[lv];
+    double* x = lv == 0 ? x0 : P.x + (size_t)k * P.ps;
+    const double* b = lv == 0 ? b0 : P.b + (size_t)k * P.ps;
+    const size_t mo = (size_t)k * P.ps;
+    gs2d(P, mo, b, x, gi);
+    gi += gi2;
+    if (lv + 1 < nl) {
+      double* res = P.res + (size_t)k * P.ps;
+      const size_t np = P.ps;
+      for (size_t s = threadIdx.x; s < np; s += blockDim.x) {
+        const int i = (int)(s / P.w), j = line_of((int)(s % P.w), P.h, P.c2);
+        if (j < 0) continue;
+        res[s] = b[s] - matvec2_at(P, mo, x, s, i, j);
+      }
+      __syncthreads();
+      const Lev2& Q = A.pl[lv + 1];
+      double* bq = Q.b + (size_t)k * Q.ps;
+      double* xq = Q.x + (size_t)k * Q.ps;
+      for (size_t s = threadIdx.x; s < Q.ps; s += blockDim.x) {
+        const int a = (int)(s / Q.w), bb = line_of((int)(s % Q.w), Q.h, Q.c2);
+        if (bb < 0) continue;
+        double v = 0.0;
+        for (int i1 = 2 * a; i1 <= 2 * a + 1 && i1 < P.c1; ++i1)
+          for (int i2 = 2 * bb; i2 <= 2 * bb + 1 && i2 < P.c2; ++i2) v = v + res[slot(P.w, P.h, i1, i2)];
+        bq[s] = v;
+        xq[s] = 0.0;
+      }
+      __syncthreads();
+      ++lv;
+    } else {
+      gi -= gi2;
+      break;
+    }
+  }
+  for (;;) {
+    const Lev2& P = A.pl[lv];
+    double* x = lv == 0 ? x0 : P.x + (size_t)k * P.ps;
+    const double* b = lv == 0 ? b0 : P.b + (size_t)k * P.ps;
+    gs2d(P, (size_t)k * P.ps, b, x, gi);
+    gi -= gi2;
+    if (lv > 0) {
+      const Lev2& F = A.pl[lv - 1];
+      double* xf = lv - 1 == 0 ? x0 : F.x + (size_t)k * F.ps;
+      for (size_t s = threadIdx.x; s < F.ps; s += blockDim.x) {
+        const int i = (int)(s / F.w), j = line_of((int)(s % F.w), F.h, F.c2);
+        if (j < 0) continue;
+        xf[s] = xf[s] + x[slot(P.w, P.h, i >> 1, j >> 1)];
+      }
+      __syncthreads();
+      --lv;
+    } else {
+      break;
+    }
+  }
+}
+
+// One zebra half-sweep of GaussSeidel_3D over the planes of parity `color` of
+// 3D level L: each CTA forms its plane's right-hand side (forward or backward
+// operation order of the reference) and runs Solve_2D on it.
+__global__ void __launch_bounds__(kPlaneBlock, 2) k_plane_half(const Lev3* __restrict__ lvs, int L, int color, int fwd,
+                                                             int mult_iter2, int gi2) {
+  __shared__ Lev3 A;
+  if (threadIdx.x == 0) A = lvs[L];
+  __syncthreads();
+  const Lev2& P0 = A.pl[0];
+  for (int q = blockIdx.x;; q += gridDim.x) {
+    const int k = 2 * q + color;
+    if (k >= A.m3) break;
+    const size_t off = (size_t)k * P0.ps, ps = P0.ps;
+    for (size_t s = threadIdx.x; s < ps; s += blockDim.x) {
+      if (line_of((int)(s % P0.w), P0.h, P0.c2) < 0) continue;
+      const size_t e = off + s;
+      double v = A.b[e];
+      if (fwd) {
+        if (k > 0) v = v - A.l3[e - ps] * A.x[e - ps];
+        if (k < A.m3 - 1) v = v - A.u3[e] * A.x[e + ps];
+      } else {
+        if (k < A.m3 - 1) v = v - A.u3[e] * A.x[e + ps];
+        if (k > 0) v = v - A.l3[e - ps] * A.x[e - ps];
+      }
+      A.t[e] = v;
+    }
+    __syncthreads();
+    for (int it = 0; it < mult_iter2; ++it) mg2d(A, k, A.x + off, A.t + off, gi2);
+    __syncthreads();
+  }
+}
+
+// MatVecT_3D at every entry of level L: mode 0 res = b - A x; mode 1 y = -(A x)
+// (MatVecFull's sign); mode 2 y = A x.
+__global__ void k_matvec3(const Lev3* __restrict__ lvs, int L, const double* __restrict__ x, const double* __restrict__ b,
+                          double* __restrict__ y, int mode) {
+  const Lev3& A = lvs[L];
+  const Lev2& P = A.pl[0];
+  const size_t tot = (size_t)A.m3 * P.ps, ps = P.ps;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t s = e % ps;
+    const int k = (int)(e / ps);
+    const int i = (int)(s / P.w), j = line_of((int)(s % P.w), P.h, P.c2);
+    if (j < 0) continue;
+    double v = matvec2_at(P, (size_t)k * ps, x + (size_t)k * ps, s, i, j);
+    if (A.m3 > 1) {
+      if (k == 0)
+        v = v + A.u3[e] * x[e + ps];
+      else if (k < A.m3 - 1)
+        v = v + A.l3[e - ps] * x[e - ps] + A.u3[e] * x[e + ps];
+      else
+        v = v + A.l3[e - ps] * x[e - ps];
+    }
+    y[e] = mode == 0 ? b[e] - v : (mode == 1 ? -v : v);
+  }
+}
+
+// RestrictT_3D (level L residual -> level L+1 right-hand side), zero x of L+1
+__global__ void k_restrict3(const Lev3* __restrict__ lvs, int L) {
+  const Lev3& A = lvs[L];
+  const Lev3& C = lvs[L + 1];
+  const Lev2& P = A.pl[0];
+  const Lev2& Q = C.pl[0];
+  const size_t tot = (size_t)C.m3 * Q.ps;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t s = e % Q.ps;
+    const int kc = (int)(e / Q.ps);
+    const int a = (int)(s / Q.w), bb = line_of((int)(s % Q.w), Q.h, Q.c2);
+    if (bb < 0) continue;
+    double v = 0.0;
+    for (int i1 = 2 * a; i1 <= 2 * a + 1 && i1 < P.c1; ++i1)
+      for (int i2 = 2 * bb; i2 <= 2 * bb + 1 && i2 < P.c2; ++i2)
+        for (int i3 = 2 * kc; i3 <= 2 * kc + 1 && i3 < A.m3; ++i3) v = v + A.res[(size_t)i3 * P.ps + slot(P.w, P.h, i1, i2)];
+    C.b[e] = v;
+    C.x[e] = 0.0;
+  }
+}
+
+// ProlongateT_3D + x = x + Res (level L+1 -> level L)
+__global__ void k_prolong3(const Lev3* __restrict__ lvs, int L) {
+  const Lev3& A = lvs[L];
+  const Lev3& C = lvs[L + 1];
+  const Lev2& P = A.pl[0];
+  const Lev2& Q = C.pl[0];
+  const size_t tot = (size_t)A.m3 * P.ps;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t s = e % P.ps;
+    const int k = (int)(e / P.ps);
+    const int i = (int)(s / P.w), j = line_of((int)(s % P.w), P.h, P.c2);
+    if (j < 0) continue;
+    A.x[e] = A.x[e] + C.x[(size_t)(k >> 1) * Q.ps + slot(Q.w, Q.h, i >> 1, j >> 1)];
+  }
+}
+
+// natural (x,y,z) interior <-> level-0 layout (z,x,y)
+__global__ void k_to_layout(Lev2 P, int nx, int ny, int nz, const double* __restrict__ nat, double* __restrict__ lay,
+                            double scale) {
+  const size_t tot = (size_t)nx * ny * nz;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(e % nx);
+    const size_t r = e / nx;
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    const double v = nat[e];
+    lay[(size_t)y * P.ps + slot(P.w, P.h, z, x)] = scale == 1.0 ? v : scale * v;
+  }
+}
+__global__ void k_from_layout(Lev2 P, int nx, int ny, int nz, const double* __restrict__ lay, double* __restrict__ nat) {
+  const size_t tot = (size_t)nx * ny * nz;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(e % nx);
+    const size_t r = e / nx;
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    nat[e] = lay[(size_t)y * P.ps + slot(P.w, P.h, z, x)];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FGMRES vector kernels (padding entries of the layout stay 0)
+// ---------------------------------------------------------------------------
+__global__ void k_pdot_partial(const double* __restrict__ a, const double* __restrict__ b, size_t n,
+                               double* __restrict__ partial) {
+  __shared__ double sh[kRedBlock];
+  double s = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    s = s + a[e] * b[e];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+// out = sum (mode 0) or sqrt(sum) (mode 1)
+__global__ void k_pdot_final(const double* __restrict__ partial, int n, double* out, int mode) {
+  __shared__ double sh[kRedBlock];
+  double s = 0.0;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) s = s + partial[e];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = mode == 1 ? sqrt(sh[0]) : sh[0];
+}
+// y = (-*h)*x + y   (DAXPY with the Gram-Schmidt coefficient held on the device)
+__global__ void k_axpy_negdev(double* __restrict__ y, const double* __restrict__ x, const double* h, size_t n) {
+  const double a = -*h;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    y[e] = a * x[e] + y[e];
+}
+// v = (1/*h)*v   (DSCALE(One/H(i+1,i)))
+__global__ void k_scale_recipdev(double* __restrict__ v, const double* h, size_t n) {
+  const double a = 1.0 / *h;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) v[e] = a * v[e];
+}
+// y = a*x + y (host scalar)
+__global__ void k_axpy(double* __restrict__ y, const double* __restrict__ x, double a, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    y[e] = a * x[e] + y[e];
+}
+// y = x + a*y (DXPBY)
+__global__ void k_xpby(const double* __restrict__ x, double a, double* __restrict__ y, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    y[e] = x[e] + a * y[e];
+}
+// v = a*v
+__global__ void k_scale(double* __restrict__ v, double a, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) v[e] = a * v[e];
+}
+// y = -x
+__global__ void k_neg(double* __restrict__ y, const double* __restrict__ x, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) y[e] = -x[e];
+}
+
+// ---------------------------------------------------------------------------
+// Rhs / UpdateVelocity (MATRIX/Rhs_Mod.f90)
+// ---------------------------------------------------------------------------
+struct Wts {
+  double *dtu, *dtv, *dtw, *duu, *duv, *duw, *dut, *dtt;
+  double *dx, *dy, *dz, *metr;
+};
+
+// Rhs with DivergenceS: b = beta0*dtP*div (- VolB*incr_th), written in the level-0 layout
+__global__ void k_rhs(Dims d, GeomT<double> g, Wts wt, const double* __restrict__ u, const double* __restrict__ v,
+                      const double* __restrict__ w, const double* __restrict__ incr_th, double bdt, int anela,
+                      Lev2 P, double* __restrict__ b) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const size_t tot = (size_t)nx * ny * nz;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % nx) + 1;
+    const size_t r = e / nx;
+    const int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
+    const double div = (-(g.fu[d.FU(i - 1, j, k)] * wt.dtu[d.UF(i - 1, j, k)] * u[d.UF(i - 1, j, k)]) +
+                        g.fu[d.FU(i, j, k)] * wt.dtu[d.UF(i, j, k)] * u[d.UF(i, j, k)] -
+                        g.fv[d.FV(i, j - 1, k)] * wt.dtv[d.VF(i, j - 1, k)] * v[d.VF(i, j - 1, k)] +
+                        g.fv[d.FV(i, j, k)] * wt.dtv[d.VF(i, j, k)] * v[d.VF(i, j, k)] -
+                        g.fw[d.FW(i, j, k - 1)] * wt.dtw[d.WF(i, j, k - 1)] * w[d.WF(i, j, k - 1)] +
+                        g.fw[d.FW(i, j, k)] * wt.dtw[d.WF(i, j, k)] * w[d.WF(i, j, k)]) *
+                       wt.dtt[e];
+    double val = bdt * div;
+    if (incr_th && anela) val = val - g.volc[d.P(i, j, k)] * incr_th[d.P(i, j, k)];
+    b[(size_t)(j - 1) * P.ps + slot(P.w, P.h, k - 1, i - 1)] = val;
+  }
+}
+
+// UpdateVelocity, GradFull + MultiTriT: p = p*DUT, the boundary-face terms
+// (0 - 0/(...) without face unknowns) and u = utilde - grad p on interior faces
+__global__ void k_update_vel(Dims d, GeomT<double> g, Wts wt, double* __restrict__ p, double* __restrict__ u,
+                             double* __restrict__ v, double* __restrict__ w, double beta0, double dtp) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const double* mxy = wt.metr;
+  const double* mxz = wt.metr + ny;
+  const double* myx = wt.metr + ny + nz;
+  const double* myz = wt.metr + ny + nz + nx;
+  const double* mzx = wt.metr + ny + 2 * nz + nx;
+  const double* mzy = wt.metr + ny + 2 * nz + 2 * nx;
+  auto C = [&](int i, int j, int k) { return (size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)(k - 1)); };
+  auto pd = [&](int i, int j, int k) { const size_t q = C(i, j, k); return p[q] * wt.dut[q]; };
+  const size_t nu = (size_t)(nx + 1) * ny * nz, nv = (size_t)nx * (ny + 1) * nz, nw = (size_t)nx * ny * (nz + 1);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nu + nv + nw; e += (size_t)gridDim.x * blockDim.x) {
+    if (e < nu) {
+      const int i = (int)(e % (nx + 1));
+      const size_t r = e / (nx + 1);
+      const int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
+      if (i == 0 || i == nx) {
+        const double t = 0.0 - 0.0 / (0.5 * wt.dx[i == 0 ? 0 : nx - 1] * mxy[j - 1] * mxz[k - 1]);
+        u[e] = u[e] + t;
+      }
+      if (i >= 1 && i <= nx - 1) {
+        const double t = 2.0 * beta0 * dtp * wt.duu[e] * (pd(i + 1, j, k) - pd(i, j, k)) /
+                         ((wt.dx[i] + wt.dx[i - 1]) * mxy[j - 1] * mxz[k - 1]);
+        u[e] = u[e] - t;
+      }
+    } else if (e < nu + nv) {
+      const size_t ee = e - nu;
+      const int i = (int)(ee % nx) + 1;
+      const size_t r = ee / nx;
+      const int j = (int)(r % (ny + 1)), k = (int)(r / (ny + 1)) + 1;
+      if (j == 0 || j == ny) {
+        const double t = 0.0 - 0.0 / (0.5 * wt.dy[j == 0 ? 0 : ny - 1] * myx[i - 1] * myz[k - 1]);
+        v[ee] = v[ee] + t;
+      }
+      if (j >= 1 && j <= ny - 1) {
+        const double t = 2.0 * beta0 * dtp * wt.duv[ee] * (pd(i, j + 1, k) - pd(i, j, k)) /
+                         ((wt.dy[j] + wt.dy[j - 1]) * myx[i - 1] * myz[k - 1]);
+        v[ee] = v[ee] - t;
+      }
+    } else {
+      const size_t ee = e - nu - nv;
+      const int i = (int)(ee % nx) + 1;
+      const size_t r = ee / nx;
+      const int j = (int)(r % ny) + 1, k = (int)(r / ny);
+      const double fwv = g.fw[d.FW(i, j, k)];
+      if (k == 0) {
+        const double t = 0.0 - 0.0 / (0.5 * wt.dz[0] * mzx[i - 1] * mzy[j - 1]);
+        w[ee] = w[ee] + t;
+      } else if (k == nz) {
+        const double t = 0.0 - 0.0 / (0.5 * wt.dz[nz - 1] * mzx[i - 1] * mzy[j - 1]);
+        w[ee] = w[ee] + fwv / (fwv + asam::kEps) * t;
+      }
+      if (k >= 1 && k <= nz - 1) {
+        const double t = 2.0 * beta0 * dtp * wt.duw[ee] * (pd(i, j, k + 1) - pd(i, j, k)) / (wt.dz[k] + wt.dz[k - 1]);
+        w[ee] = w[ee] - fwv / (fwv + asam::kEps) * t;
+      }
+    }
+  }
+}
+
+// p = p*DUT (the pressure the reference leaves in x after UpdateVelocity)
+__global__ void k_scale_dut(double* __restrict__ p, const double* __restrict__ dut, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) p[e] = p[e] * dut[e];
+}
+
+// ThPos / RhoPos increments and DivScalar of the other listed components
+// (Rhs_Mod.f90:834-871, 915-950), all from the projected face velocities
+__global__ void k_update_incr(Dims d, GeomT<double> g, Wts wt, const double* __restrict__ u, const double* __restrict__ v,
+                              const double* __restrict__ w, double* __restrict__ incr, const double* __restrict__ state,
+                              int th_pos, int rho_pos, const int* __restrict__ scal, int nscal, double beta0, double dtp) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const size_t npad = d.npad();
+  const size_t tot = (size_t)nx * ny * nz;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % nx) + 1;
+    const size_t r = e / nx;
+    const int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
+    const size_t P = d.P(i, j, k);
+    const double vC = g.volc[P];
+    const double fuR = g.fu[d.FU(i, j, k)], fuL = g.fu[d.FU(i - 1, j, k)];
+    const double fvR = g.fv[d.FV(i, j, k)], fvL = g.fv[d.FV(i, j - 1, k)];
+    const double fwR = g.fw[d.FW(i, j, k)], fwL = g.fw[d.FW(i, j, k - 1)];
+    const double uR = u[d.UF(i, j, k)], uL = u[d.UF(i - 1, j, k)];
+    const double vR = v[d.VF(i, j, k)], vL = v[d.VF(i, j - 1, k)];
+    const double wR = w[d.WF(i, j, k)], wL = w[d.WF(i, j, k - 1)];
+    if (th_pos >= 0) {
+      const double s = fuR * wt.dtu[d.UF(i, j, k)] * uR - fuL * wt.dtu[d.UF(i - 1, j, k)] * uL +
+                       fvR * wt.dtv[d.VF(i, j, k)] * vR - fvL * wt.dtv[d.VF(i, j - 1, k)] * vL +
+                       fwR * wt.dtw[d.WF(i, j, k)] * wR - fwL * wt.dtw[d.WF(i, j, k - 1)] * wL;
+      double* c = incr + (size_t)th_pos * npad;
+      c[P] = c[P] - dtp * beta0 * wt.dtt[e] * s / (vC + asam::kEps);
+    }
+    if (rho_pos >= 0) {
+      const double s = fuR * uR - fuL * uL + fvR * vR - fvL * vL + fwR * wR - fwL * wL;
+      double* c = incr + (size_t)rho_pos * npad;
+      c[P] = c[P] - dtp * beta0 * s / (vC + asam::kEps);
+    }
+    if (nscal > 0) {
+      const double* rho = state + (size_t)rho_pos * npad;
+      const size_t sx = 1, sy = (size_t)d.NX(), sz = (size_t)d.NX() * d.NY();
+      const double vW = g.volc[P - sx], vE = g.volc[P + sx], vS = g.volc[P - sy], vN = g.volc[P + sy];
+      const double vB = g.volc[P - sz], vT = g.volc[P + sz];
+      for (int q = 0; q < nscal; ++q) {
+        const double* cc = state + (size_t)scal[q] * npad;
+        double* cd = incr + (size_t)scal[q] * npad;
+        const double qC = vC * cc[P] / (rho[P] + asam::kEps);
+        const double s = fuR * uR * (qC + vE * cc[P + sx] / (rho[P + sx] + asam::kEps)) / (vC + vE + asam::kEps) -
+                         fuL * uL * (qC + vW * cc[P - sx] / (rho[P - sx] + asam::kEps)) / (vC + vW + asam::kEps) +
+                         fvR * vR * (qC + vN * cc[P + sy] / (rho[P + sy] + asam::kEps)) / (vC + vN + asam::kEps) -
+                         fvL * vL * (qC + vS * cc[P - sy] / (rho[P - sy] + asam::kEps)) / (vC + vS + asam::kEps) +
+                         fwR * wR * (qC + vT * cc[P + sz] / (rho[P + sz] + asam::kEps)) / (vC + vT + asam::kEps) -
+                         fwL * wL * (qC + vB * cc[P - sz] / (rho[P - sz] + asam::kEps)) / (vC + vB + asam::kEps);
+        cd[P] = cd[P] - dtp * beta0 * s / (vC + asam::kEps);
+      }
+    }
+  }
+}
+
+}  // namespace prj
+
+using namespace prj;
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct ProjState {
+  asam_proj_config cfg{};
+  cudaStream_t st = nullptr;  // the context's stream at the current call
+  int R = 0;
+  Wts wt{};
+  bool weights = false, assembled = false;
+  double beta0 = 0.0, dtp = 0.0;
+  std::vector<Lev3> lv;
+  Lev3* d_lv = nullptr;
+  Fields g{}, c{};
+  std::vector<void*> allocs;
+  // FGMRES storage (level-0 layout)
+  std::vector<double*> v, z;
+  double *H = nullptr, *partial = nullptr, *scal_h = nullptr;
+  double *tmp = nullptr, *xn = nullptr, *bn = nullptr, *xl = nullptr, *bl = nullptr;
+  double *stage_u = nullptr, *stage_v = nullptr, *stage_w = nullptr;
+  int* d_scal = nullptr;
+  int nscal_cap = 0;
+  long long vcycles = 0;
+};
+
+namespace prj {
+
+int grid_of(size_t n) {
+  size_t g = (n + 255) / 256;
+  if (g > 152 * 16) g = 152 * 16;
+  return (int)(g ? g : 1);
+}
+
+// allocate and zero on the context's stream, so the zeroing is ordered before
+// every later upload and kernel on that stream
+template <typename T>
+int palloc(ProjState* s, T** p, size_t n) {
+  void* q = nullptr;
+  CK(cudaMalloc(&q, (n ? n : 1) * sizeof(T)));
+  CK(cudaMemsetAsync(q, 0, (n ? n : 1) * sizeof(T), s->st));
+  s->allocs.push_back(q);
+  *p = (T*)q;
+  return kOk;
+}
+
+int alloc_fields(ProjState* s, Fields& f, int n1, int n2, int n3) {
+  f.n1 = n1;
+  f.n2 = n2;
+  f.n3 = n3;
+  const size_t s1 = (size_t)(n1 + 1) * n2 * n3, s2 = (size_t)n1 * (n2 + 1) * n3, s3 = (size_t)n1 * n2 * (n3 + 1);
+  const size_t sc = (size_t)n1 * n2 * n3;
+  struct {
+    double** p;
+    size_t n;
+  } a[] = {{&f.F1, s1}, {&f.T1, s1}, {&f.U1, s1}, {&f.F2, s2}, {&f.T2, s2}, {&f.U2, s2}, {&f.F3, s3},
+           {&f.T3, s3}, {&f.U3, s3}, {&f.vol, sc}, {&f.dut, sc}, {&f.d1, (size_t)n1}, {&f.d2, (size_t)n2},
+           {&f.d3, (size_t)n3}, {&f.m12, (size_t)n2}, {&f.m13, (size_t)n3}, {&f.m21, (size_t)n1}, {&f.m23, (size_t)n3},
+           {&f.m31, (size_t)n1}, {&f.m32, (size_t)n2}};
+  for (auto& q : a)
+    if (int rc = palloc(s, q.p, q.n)) return rc;
+  return kOk;
+}
+
+int alloc_lev2(ProjState* s, Lev2& P, int c1, int c2, int m3, bool own_vectors) {
+  P.c1 = c1;
+  P.c2 = c2;
+  P.h = (c2 + 1) / 2;
+  P.w = 2 * P.h;
+  P.m3 = m3;
+  P.ps = (size_t)c1 * P.w;
+  const size_t n = P.ps * m3;
+  double** arr[] = {&P.d, &P.uz, &P.lz, &P.fw, &P.ft, &P.frt, &P.ux, &P.lx, &P.res};
+  for (double** q : arr)
+    if (int rc = palloc(s, q, n)) return rc;
+  P.x = P.b = nullptr;
+  if (own_vectors) {
+    if (int rc = palloc(s, &P.x, n)) return rc;
+    if (int rc = palloc(s, &P.b, n)) return rc;
+  }
+  return kOk;
+}
+
+size_t len0(const ProjState* s) { return (size_t)s->lv[0].m3 * s->lv[0].pl[0].ps; }
+
+}  // namespace prj
+
+void proj_free(asam_ctx* h) {
+  ProjState* s = h->proj;
+  if (!s) return;
+  for (void* p : s->allocs) cudaFree(p);
+  if (s->scal_h) cudaFreeHost(s->scal_h);
+  delete s;
+  h->proj = nullptr;
+}
+
+namespace prj {
+
+int proj_build(asam_ctx* h) {
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const int n1 = d.nz, n2 = d.nx, n3 = d.ny;
+  const int R = s->R;
+  s->lv.assign(R, Lev3{});
+  for (int L = 0; L < R; ++L) {
+    const int sh = (1 << L) - 1;
+    Lev3& A = s->lv[L];
+    A.m1 = (n1 + sh) / (sh + 1);
+    A.m2 = (n2 + sh) / (sh + 1);
+    A.m3 = (n3 + sh) / (sh + 1);
+    A.nl = R - L;
+    for (int L2 = L; L2 < R; ++L2) {
+      const int s2 = (1 << L2) - 1;
+      if (int rc = alloc_lev2(s, A.pl[L2 - L], (n1 + s2) / (s2 + 1), (n2 + s2) / (s2 + 1), A.m3, L2 > L)) return rc;
+    }
+    const size_t n = A.pl[0].ps * A.m3;
+    double** arr[] = {&A.u3, &A.l3, &A.x, &A.b, &A.res, &A.t};
+    for (double** q : arr)
+      if (int rc = palloc(s, q, n)) return rc;
+  }
+  if (int rc = palloc(s, &s->d_lv, (size_t)R)) return rc;
+  CK(cudaMemcpyAsync(s->d_lv, s->lv.data(), sizeof(Lev3) * R, cudaMemcpyHostToDevice, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  if (int rc = alloc_fields(s, s->g, n1, n2, n3)) return rc;
+  if (int rc = alloc_fields(s, s->c, n1, n2, n3)) return rc;
+  // FGMRES storage
+  const int step = s->cfg.step_gmres;
+  const size_t n = len0(s);
+  s->v.assign(step + 1, nullptr);
+  s->z.assign(step, nullptr);
+  for (auto& p : s->v)
+    if (int rc = palloc(s, &p, n)) return rc;
+  for (auto& p : s->z)
+    if (int rc = palloc(s, &p, n)) return rc;
+  if (int rc = palloc(s, &s->H, (size_t)(step + 1) * (step + 1))) return rc;
+  if (int rc = palloc(s, &s->partial, (size_t)kRedGrid)) return rc;
+  if (int rc = palloc(s, &s->tmp, n)) return rc;
+  if (int rc = palloc(s, &s->xl, n)) return rc;
+  if (int rc = palloc(s, &s->bl, n)) return rc;
+  const size_t nc = (size_t)d.nx * d.ny * d.nz;
+  if (int rc = palloc(s, &s->xn, nc)) return rc;
+  if (int rc = palloc(s, &s->bn, nc)) return rc;
+  CK(cudaMallocHost((void**)&s->scal_h, sizeof(double) * (step + 2)));
+  return kOk;
+}
+
+// Solve_3D from a zero start on level 0 (VCycleCG's MatrixT branch): lv[0].b
+// holds the right-hand side, the result is left in lv[0].x
+void vcycle_dev(asam_ctx* h) {
+  ProjState* s = h->proj;
+  const cudaStream_t st = h->L.stream;
+  const int R = s->R;
+  const int gi2 = s->cfg.gauss_iter2, gi3 = s->cfg.gauss_iter3;
+  const int mi2 = s->cfg.mult_iter2;
+  long long nl = 0;
+  cudaMemsetAsync(s->lv[0].x, 0, sizeof(double) * len0(s), st);
+  auto gs3 = [&](int L, int gi) {
+    const Lev3& A = s->lv[L];
+    auto half = [&](int c, int fwd) {
+      const int np = (A.m3 - c + 1) / 2;
+      if (np <= 0) return;
+      k_plane_half<<<np, kPlaneBlock, 0, st>>>(s->d_lv, L, c, fwd, mi2, gi2);
+      ++nl;
+    };
+    if (A.m3 > 1) {
+      for (int it = 0; it < gi; ++it) {
+        half(0, 1);
+        half(1, 1);
+        half(1, 0);
+        half(0, 0);
+      }
+    } else {
+      half(0, 1);
+    }
+  };
+  for (int it = 0; it < s->cfg.mult_iter3; ++it) {
+    int gi = 1, L = 0;
+    for (;;) {
+      gs3(L, gi);
+      gi += gi3;
+      if (L + 1 < R) {
+        const Lev3& A = s->lv[L];
+        const size_t n = A.pl[0].ps * A.m3;
+        k_matvec3<<<grid_of(n), 256, 0, st>>>(s->d_lv, L, A.x, A.b, A.res, 0);
+        const size_t nc = s->lv[L + 1].pl[0].ps * s->lv[L + 1].m3;
+        k_restrict3<<<grid_of(nc), 256, 0, st>>>(s->d_lv, L);
+        nl += 2;
+        ++L;
+      } else {
+        gi -= gi3;
+        break;
+      }
+    }
+    for (;;) {
+      gs3(L, gi);
+      gi -= gi3;
+      if (L > 0) {
+        --L;
+        const size_t n = s->lv[L].pl[0].ps * s->lv[L].m3;
+        k_prolong3<<<grid_of(n), 256, 0, st>>>(s->d_lv, L);
+        ++nl;
+      } else {
+        break;
+      }
+    }
+  }
+  count_launches(nl);
+  ++s->vcycles;
+}
+
+int dot_dev(asam_ctx* h, const double* a, const double* b, double* out, int mode) {
+  ProjState* s = h->proj;
+  const size_t n = len0(s);
+  k_pdot_partial<<<kRedGrid, kRedBlock, 0, h->L.stream>>>(a, b, n, s->partial);
+  k_pdot_final<<<1, kRedBlock, 0, h->L.stream>>>(s->partial, kRedGrid, out, mode);
+  count_launches(2);
+  return kOk;
+}
+
+// y = MatVec1(x) = -(A x) on level 0
+void matvec1_dev(asam_ctx* h, const double* x, double* y) {
+  ProjState* s = h->proj;
+  const size_t n = len0(s);
+  k_matvec3<<<grid_of(n), 256, 0, h->L.stream>>>(s->d_lv, 0, x, nullptr, y, 1);
+  count_launches(1);
+}
+
+// z = PSolve1(v) = PressurePre(-v) (no boundary face unknowns)
+void psolve1_dev(asam_ctx* h, const double* v, double* z) {
+  ProjState* s = h->proj;
+  const size_t n = len0(s);
+  k_neg<<<grid_of(n), 256, 0, h->L.stream>>>(s->lv[0].b, v, n);
+  count_launches(1);
+  vcycle_dev(h);
+  cudaMemcpyAsync(z, s->lv[0].x, n * sizeof(double), cudaMemcpyDeviceToDevice, h->L.stream);
+}
+
+// FGMRES (SOLU/Iter_Mod.f90:121-199) on level-0 vectors x (in/out), b
+int fgmres_dev(asam_ctx* h, double* x, const double* b, int maxiter, double tol, int* steps_out, double* rho_out,
+               double* rho0_out) {
+  ProjState* s = h->proj;
+  const cudaStream_t st = h->L.stream;
+  const int step = s->cfg.step_gmres;
+  const size_t n = len0(s);
+  const int g = grid_of(n);
+  std::vector<double> Hh((size_t)(step + 1) * step, 0.0), c(step), sn(step), bh(step + 1), y(step);
+  auto HH = [&](int i, int j) -> double& { return Hh[(size_t)(i - 1) + (size_t)(step + 1) * (j - 1)]; };
+  double rho = 0.0, rho0 = 0.0;
+  int steps = 0;
+  double* hd = s->H;  // device slots: column i of H at hd + (step+1)*(i-1)
+  for (int iter = 1; iter <= maxiter; ++iter) {
+    matvec1_dev(h, x, s->v[0]);
+    k_xpby<<<g, 256, 0, st>>>(b, -1.0, s->v[0], n);
+    count_launches(1);
+    dot_dev(h, s->v[0], s->v[0], hd, 1);
+    CK(cudaMemcpyAsync(s->scal_h, hd, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const double beta = s->scal_h[0];
+    if (std::isnan(beta)) return kNanDetected;
+    if (iter == 1) rho0 = beta;
+    if (beta <= 0.0) break;
+    k_scale<<<g, 256, 0, st>>>(s->v[0], 1.0 / beta, n);
+    count_launches(1);
+    bh[0] = beta * 1.0;
+    int nr = step;
+    for (int i = 1; i <= step; ++i) {
+      psolve1_dev(h, s->v[i - 1], s->z[i - 1]);
+      matvec1_dev(h, s->z[i - 1], s->v[i]);
+      ++steps;
+      double* col = hd + (size_t)(step + 1) * (i - 1);
+      for (int k = 1; k <= i; ++k) {
+        dot_dev(h, s->v[k - 1], s->v[i], col + (k - 1), 0);
+        k_axpy_negdev<<<g, 256, 0, st>>>(s->v[i], s->v[k - 1], col + (k - 1), n);
+        count_launches(1);
+      }
+      dot_dev(h, s->v[i], s->v[i], col + i, 1);
+      k_scale_recipdev<<<g, 256, 0, st>>>(s->v[i], col + i, n);
+      count_launches(1);
+      CK(cudaMemcpyAsync(s->scal_h, col, sizeof(double) * (i + 1), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      for (int k = 1; k <= i + 1; ++k) HH(k, i) = s->scal_h[k - 1];
+      for (int k = 2; k <= i; ++k) {
+        const double temp = c[k - 2] * HH(k - 1, i) + sn[k - 2] * HH(k, i);
+        HH(k, i) = -sn[k - 2] * HH(k - 1, i) + c[k - 2] * HH(k, i);
+        HH(k - 1, i) = temp;
+      }
+      const double delta = std::sqrt(HH(i, i) * HH(i, i) + HH(i + 1, i) * HH(i + 1, i));
+      c[i - 1] = HH(i, i) / delta;
+      sn[i - 1] = HH(i + 1, i) / delta;
+      HH(i, i) = c[i - 1] * HH(i, i) + sn[i - 1] * HH(i + 1, i);
+      bh[i] = -sn[i - 1] * bh[i - 1];
+      bh[i - 1] = c[i - 1] * bh[i - 1];
+      rho = std::fabs(bh[i]);
+      if (std::isnan(rho)) return kNanDetected;
+      if (rho <= tol * rho0) {
+        nr = i;
+        break;
+      }
+      nr = step;
+    }
+    y[nr - 1] = bh[nr - 1] / HH(nr, nr);
+    for (int k = nr - 1; k >= 1; --k) {
+      y[k - 1] = bh[k - 1];
+      for (int i = k + 1; i <= nr; ++i) y[k - 1] = y[k - 1] - HH(k, i) * y[i - 1];
+      y[k - 1] = y[k - 1] / HH(k, k);
+    }
+    for (int i = 1; i <= nr; ++i) k_axpy<<<g, 256, 0, st>>>(x, s->z[i - 1], y[i - 1], n);
+    count_launches(nr);
+    if (rho <= tol * rho0) break;
+  }
+  if (steps_out) *steps_out = steps;
+  if (rho_out) *rho_out = rho;
+  if (rho0_out) *rho0_out = rho0;
+  return check_launch();
+}
+
+int need_assembled(asam_ctx* h) {
+  if (!h || !h->proj) {
+    set_last_error("projection not set up (asam_proj_setup)", __FILE__, __LINE__);
+    return kBadArg;
+  }
+  if (!h->proj->assembled) {
+    set_last_error("pressure Laplacian not assembled (asam_lapl_compute)", __FILE__, __LINE__);
+    return kBadArg;
+  }
+  return kOk;
+}
+
+// copy n doubles from host or device pointer p into device buffer dst
+int copy_in(asam_ctx* h, double* dst, const double* p, size_t n) {
+  CK(cudaMemcpyAsync(dst, p, n * sizeof(double), cudaMemcpyDefault, h->L.stream));
+  return kOk;
+}
+
+}  // namespace prj
+}  // namespace asam
+
+using namespace asam;
+using namespace asam::prj;
+
+extern "C" {
+
+int asam_proj_setup(asam_ctx* h, const asam_proj_config* cfg, const double* dx, const double* dy, const double* dz,
+                    const double* metr) {
+  if (!h || !cfg || !dx || !dy || !dz) return kBadArg;
+  if (cfg->ref_level < 1 || cfg->ref_level > kMaxLev || cfg->gauss_iter2 < 0 || cfg->gauss_iter3 < 0 ||
+      cfg->mult_iter2 < 1 || cfg->mult_iter3 < 1 || cfg->step_gmres < 1 || cfg->step_gmres > 64 ||
+      cfg->max_restart < 1) {
+    set_last_error("asam_proj_setup: configuration out of range", __FILE__, __LINE__);
+    return kBadArg;
+  }
+  if (h->d.per_x || h->d.per_y || h->d.per_z) {
+    set_last_error("asam_proj_setup: the projection covers closed blocks only (no periodic sides)", __FILE__, __LINE__);
+    return kBadArg;
+  }
+  proj_free(h);
+  ProjState* s = new ProjState();
+  h->proj = s;
+  s->st = h->L.stream;
+  s->cfg = *cfg;
+  s->R = cfg->ref_level;
+  const Dims& d = h->d;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  int rc = kOk;
+  Wts& w = s->wt;
+  const size_t nc = (size_t)nx * ny * nz;
+  struct {
+    double** p;
+    size_t n;
+  } a[] = {{&w.dtu, d.n_uf()}, {&w.dtv, d.n_vf()}, {&w.dtw, d.n_wf()}, {&w.duu, d.n_uf()},
+           {&w.duv, d.n_vf()}, {&w.duw, d.n_wf()}, {&w.dut, nc},       {&w.dtt, nc},
+           {&w.dx, (size_t)nx}, {&w.dy, (size_t)ny}, {&w.dz, (size_t)nz}, {&w.metr, (size_t)2 * (nx + ny + nz)}};
+  for (auto& q : a)
+    if ((rc = palloc(s, q.p, q.n))) return rc;
+  if ((rc = copy_in(h, w.dx, dx, nx)) || (rc = copy_in(h, w.dy, dy, ny)) || (rc = copy_in(h, w.dz, dz, nz))) return rc;
+  if (metr) {
+    if ((rc = copy_in(h, w.metr, metr, (size_t)2 * (nx + ny + nz)))) return rc;
+  } else {
+    std::vector<double> ones((size_t)2 * (nx + ny + nz), 1.0);
+    CK(cudaMemcpyAsync(w.metr, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice, h->L.stream));
+    CK(cudaStreamSynchronize(h->L.stream));
+  }
+  if ((rc = proj_build(h))) return rc;
+  CK(cudaStreamSynchronize(h->L.stream));
+  return kOk;
+}
+
+int asam_proj_weights(asam_ctx* h, const double* dtu, const double* dtv, const double* dtw, const double* duu,
+                      const double* duv, const double* duw, const double* dut, const double* dtt) {
+  if (!h || !h->proj || !dtu || !dtv || !dtw || !duu || !duv || !duw || !dut || !dtt) return kBadArg;
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const size_t nc = (size_t)d.nx * d.ny * d.nz;
+  int rc;
+  if ((rc = copy_in(h, s->wt.dtu, dtu, d.n_uf())) || (rc = copy_in(h, s->wt.dtv, dtv, d.n_vf())) ||
+      (rc = copy_in(h, s->wt.dtw, dtw, d.n_wf())) || (rc = copy_in(h, s->wt.duu, duu, d.n_uf())) ||
+      (rc = copy_in(h, s->wt.duv, duv, d.n_vf())) || (rc = copy_in(h, s->wt.duw, duw, d.n_wf())) ||
+      (rc = copy_in(h, s->wt.dut, dut, nc)) || (rc = copy_in(h, s->wt.dtt, dtt, nc)))
+    return rc;
+  CK(cudaStreamSynchronize(h->L.stream));
+  s->weights = true;
+  s->assembled = false;
+  return kOk;
+}
+
+int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
+  if (!h || !h->proj || !h->proj->weights) {
+    set_last_error("asam_lapl_compute: call asam_proj_setup and asam_proj_weights first", __FILE__, __LINE__);
+    return kBadArg;
+  }
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const cudaStream_t st = h->L.stream;
+  s->beta0 = beta0;
+  s->dtp = dtp;
+  const double bd = beta0 * dtp, bd2 = bd * bd;
+  const Facs fc{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // SetFactorN
+  const double fa = s->cfg.fac_anela;
+  k_fine_fields<<<grid_of((size_t)(d.nx + 1) * (d.ny + 1) * (d.nz + 1)), 256, 0, st>>>(
+      d, h->fu, h->fv, h->fw, h->volc, s->wt.dtu, s->wt.dtv, s->wt.dtw, s->wt.duu, s->wt.duv, s->wt.duw, s->wt.dut, s->g);
+  k_fine_1d<<<1, 256, 0, st>>>(d.nx, d.ny, d.nz, s->wt.dx, s->wt.dy, s->wt.dz, s->wt.metr, s->g);
+  long long nl = 2;
+  const int n1 = d.nz, n2 = d.nx, n3 = d.ny;
+  for (int L = 0; L < s->R; ++L) {
+    Lev3& A = s->lv[L];
+    const int sh3 = (1 << L) - 1;
+    for (int L2 = L; L2 < s->R; ++L2) {
+      const int sh = (1 << L2) - 1;
+      Fields c = s->c;
+      c.n1 = (n1 + sh) / (sh + 1);
+      c.n2 = (n2 + sh) / (sh + 1);
+      c.n3 = (n3 + sh3) / (sh3 + 1);
+      const size_t nf = (size_t)(c.n1 + 1) * c.n2 * c.n3 + (size_t)c.n1 * (c.n2 + 1) * c.n3 + (size_t)c.n1 * c.n2 * (c.n3 + 1);
+      const size_t ncell = (size_t)c.n1 * c.n2 * c.n3;
+      k_coarse_faces<<<grid_of(nf), 256, 0, st>>>(s->g, c, sh, sh, sh3);
+      k_coarse_cells<<<grid_of(ncell), 256, 0, st>>>(s->g, c, sh, sh, sh3);
+      k_coarse_1d<<<1, 32, 0, st>>>(s->g, c, sh, sh, sh3);
+      Lev2& P = A.pl[L2 - L];
+      const bool full = L2 == L;
+      k_assemble<<<grid_of(ncell), 256, 0, st>>>(c, P, full ? A.u3 : nullptr, full ? A.l3 : nullptr, full ? 1 : 0, bd2, fc, fa);
+      k_factor<<<grid_of((size_t)P.m3 * P.c2), 256, 0, st>>>(P);
+      nl += 5;
+    }
+  }
+  count_launches(nl);
+  CK(cudaStreamSynchronize(st));
+  int rc = check_launch();
+  if (!rc) s->assembled = true;
+  return rc;
+}
+
+long asam_lapl_get(asam_ctx* h, int level3, int level2, int which, double* out) {
+  if (need_assembled(h)) return -1;
+  ProjState* s = h->proj;
+  if (level3 < 0 || level3 >= s->R || level2 < level3 || level2 >= s->R || which < 0 || which > 6) return -1;
+  if (which >= 5 && level2 != level3) return -1;
+  const Lev3& A = s->lv[level3];
+  const Lev2& P = A.pl[level2 - level3];
+  const double* src[] = {P.d, P.uz, P.lz, P.ux, P.lx, A.u3, A.l3};
+  const size_t n = P.ps * P.m3;
+  const long cnt = (long)P.c1 * P.c2 * P.m3;
+  if (!out) return cnt;
+  std::vector<double> buf(n);
+  if (cudaStreamSynchronize(h->L.stream) != cudaSuccess) return -1;
+  if (cudaMemcpy(buf.data(), src[which], n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  long q = 0;
+  for (int k = 0; k < P.m3; ++k)
+    for (int j = 0; j < P.c2; ++j)
+      for (int i = 0; i < P.c1; ++i) out[q++] = buf[(size_t)k * P.ps + slot(P.w, P.h, i, j)];
+  return cnt;
+}
+
+int asam_lapl_matvec(asam_ctx* h, const double* x, double* y) {
+  if (int rc = need_assembled(h)) return rc;
+  if (!x || !y) return kBadArg;
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const size_t nc = (size_t)d.nx * d.ny * d.nz, n = len0(s);
+  const cudaStream_t st = h->L.stream;
+  const Lev2& P0 = s->lv[0].pl[0];
+  int rc;
+  if ((rc = copy_in(h, s->xn, x, nc))) return rc;
+  k_to_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->xn, s->tmp, 1.0);
+  k_matvec3<<<grid_of(n), 256, 0, st>>>(s->d_lv, 0, s->tmp, nullptr, s->v[0], 2);
+  k_from_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->v[0], s->bn);
+  count_launches(3);
+  CK(cudaMemcpyAsync(y, s->bn, nc * sizeof(double), cudaMemcpyDefault, st));
+  CK(cudaStreamSynchronize(st));
+  return check_launch();
+}
+
+int asam_lapl_vcycle(asam_ctx* h, const double* b, double* x) {
+  if (int rc = need_assembled(h)) return rc;
+  if (!x || !b) return kBadArg;
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const size_t nc = (size_t)d.nx * d.ny * d.nz;
+  const cudaStream_t st = h->L.stream;
+  const Lev2& P0 = s->lv[0].pl[0];
+  int rc;
+  if ((rc = copy_in(h, s->bn, b, nc))) return rc;
+  k_to_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->bn, s->lv[0].b, 1.0);
+  count_launches(1);
+  vcycle_dev(h);
+  k_from_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->lv[0].x, s->xn);
+  count_launches(1);
+  CK(cudaMemcpyAsync(x, s->xn, nc * sizeof(double), cudaMemcpyDefault, st));
+  CK(cudaStreamSynchronize(st));
+  return check_launch();
+}
+
+int asam_solve_sound(asam_ctx* h, double* x, const double* b, int* maxiter, double* tol) {
+  if (int rc = need_assembled(h)) return rc;
+  if (!x || !b || !maxiter || !tol || *maxiter < 1) return kBadArg;
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const size_t nc = (size_t)d.nx * d.ny * d.nz;
+  const cudaStream_t st = h->L.stream;
+  const Lev2& P0 = s->lv[0].pl[0];
+  int rc;
+  if ((rc = copy_in(h, s->bn, b, nc)) || (rc = copy_in(h, s->xn, x, nc))) return rc;
+  k_to_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->bn, s->bl, 1.0);
+  k_to_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->xn, s->xl, 1.0);
+  count_launches(2);
+  int steps = 0;
+  double rho = 0.0, rho0 = 0.0;
+  rc = fgmres_dev(h, s->xl, s->bl, *maxiter, *tol, &steps, &rho, &rho0);
+  if (rc && rc != kNotConverged) return rc;
+  k_from_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->xl, s->xn);
+  count_launches(1);
+  CK(cudaMemcpyAsync(x, s->xn, nc * sizeof(double), cudaMemcpyDefault, st));
+  CK(cudaStreamSynchronize(st));
+  if ((rc = check_launch())) return rc;
+  const double lim = *tol * rho0;
+  *maxiter = steps;
+  *tol = rho0 > 0.0 ? rho / rho0 : 0.0;
+  return rho0 > 0.0 && rho > lim ? kNotConverged : kOk;
+}
+
+int asam_project_vel_face(asam_ctx* h, double* uf, double* vf, double* wf, double* incr, const double* state,
+                          int th_pos, int rho_pos, const int* scalars, int nscalar, double* pressure, int* steps,
+                          double* resid) {
+  if (int rc = need_assembled(h)) return rc;
+  const int ncomp = h->cfg.ncomp;
+  if (!uf || !vf || !wf || !incr || th_pos >= ncomp || rho_pos >= ncomp || nscalar < 0 ||
+      (nscalar > 0 && (!scalars || !state || rho_pos < 0)))
+    return kBadArg;
+  for (int q = 0; q < nscalar; ++q)
+    if (scalars[q] < 0 || scalars[q] >= ncomp) return kBadArg;
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const size_t nc = (size_t)d.nx * d.ny * d.nz, len = (size_t)ncomp * h->npad;
+  const cudaStream_t st = h->L.stream;
+  s->st = st;
+  const Lev2& P0 = s->lv[0].pl[0];
+  int rc;
+  if (!s->stage_u) {
+    if ((rc = palloc(s, &s->stage_u, d.n_uf())) || (rc = palloc(s, &s->stage_v, d.n_vf())) ||
+        (rc = palloc(s, &s->stage_w, d.n_wf())))
+      return rc;
+  }
+  if (nscalar > s->nscal_cap) {
+    if ((rc = palloc(s, &s->d_scal, (size_t)nscalar))) return rc;
+    s->nscal_cap = nscalar;
+  }
+  if (nscalar > 0) CK(cudaMemcpyAsync(s->d_scal, scalars, sizeof(int) * nscalar, cudaMemcpyHostToDevice, st));
+  double *du, *dv, *dw, *di;
+  const double* ds = nullptr;
+  du = is_device_ptr(uf) ? uf : s->stage_u;
+  dv = is_device_ptr(vf) ? vf : s->stage_v;
+  dw = is_device_ptr(wf) ? wf : s->stage_w;
+  if (du != uf) CK(cudaMemcpyAsync(du, uf, d.n_uf() * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (dv != vf) CK(cudaMemcpyAsync(dv, vf, d.n_vf() * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (dw != wf) CK(cudaMemcpyAsync(dw, wf, d.n_wf() * sizeof(double), cudaMemcpyHostToDevice, st));
+  if ((rc = stage_out_begin(h, incr, len, h->stage_a, &di, true))) return rc;
+  if (state) {
+    if ((rc = stage_in(h, state, len, h->stage_b, &ds))) return rc;
+  }
+  // Rhs
+  k_rhs<<<grid_of(nc), 256, 0, st>>>(d, h->geom(), s->wt, du, dv, dw, th_pos >= 0 ? di + (size_t)th_pos * h->npad : nullptr,
+                                      s->beta0 * s->dtp, s->cfg.fac_anela >= 1.0 ? 1 : 0, P0, s->bl);
+  CK(cudaMemsetAsync(s->xl, 0, sizeof(double) * len0(s), st));
+  count_launches(1);
+  int nsteps = 0;
+  double rho = 0.0, rho0 = 0.0;
+  rc = fgmres_dev(h, s->xl, s->bl, s->cfg.max_restart, s->cfg.tol, &nsteps, &rho, &rho0);
+  if (rc) return rc;
+  // UpdateVelocity
+  k_from_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->xl, s->xn);
+  k_update_vel<<<grid_of(d.n_uf() + d.n_vf() + d.n_wf()), 256, 0, st>>>(d, h->geom(), s->wt, s->xn, du, dv, dw, s->beta0,
+                                                                         s->dtp);
+  k_update_incr<<<grid_of(nc), 256, 0, st>>>(d, h->geom(), s->wt, du, dv, dw, di, ds, th_pos, rho_pos, s->d_scal, nscalar,
+                                             s->beta0, s->dtp);
+  k_scale_dut<<<grid_of(nc), 256, 0, st>>>(s->xn, s->wt.dut, nc);
+  count_launches(4);
+  if (du != uf) CK(cudaMemcpyAsync(uf, du, d.n_uf() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (dv != vf) CK(cudaMemcpyAsync(vf, dv, d.n_vf() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (dw != wf) CK(cudaMemcpyAsync(wf, dw, d.n_wf() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (pressure) CK(cudaMemcpyAsync(pressure, s->xn, nc * sizeof(double), cudaMemcpyDefault, st));
+  if ((rc = stage_out_end(h, incr, len, di))) return rc;
+  CK(cudaStreamSynchronize(st));
+  if ((rc = check_launch())) return rc;
+  if (steps) *steps = nsteps;
+  if (resid) *resid = rho0 > 0.0 ? rho / rho0 : 0.0;
+  return rho0 > 0.0 && rho > s->cfg.tol * rho0 ? kNotConverged : kOk;
+}
+
+long long asam_proj_vcycles(asam_ctx* h) { return h && h->proj ? h->proj->vcycles : 0; }
+
+}  // extern "C"

@@ -222,6 +222,73 @@ def _fill_halo_xy(a: np.ndarray, grid: Grid) -> None:
         a[:, ny + 1, :] = a[:, 1, :]
 
 
+def close_dead_faces(geo: Geometry) -> Geometry:
+    """Close every face of an interior cell with zero volume (in place).
+
+    Snapping the terrain onto a level can leave the face that lies on the
+    ground surface open (h == zf) above a cell of zero volume.  The transport
+    never carries flux through it, but the pressure projection would couple
+    the live cell above to a cell with no volume; a consistent cut-cell
+    geometry has all faces of a zero-volume cell closed.
+    """
+    g = geo.grid
+    nx, ny, nz = g.nx, g.ny, g.nz
+    dead = geo.volc[1:nz + 1, 1:ny + 1, 1:nx + 1] <= 0.0
+    k, j, i = np.nonzero(dead)
+    geo.fu[k, j, i + 1] = 0.0      # west face of interior cell i+1 (FU index i)
+    geo.fu[k, j, i + 2] = 0.0      # east face
+    geo.fv[k, j + 1, i] = 0.0
+    geo.fv[k, j + 2, i] = 0.0
+    geo.fw[k + 1, j, i] = 0.0
+    geo.fw[k + 2, j, i] = 0.0
+    geo.info["dead_cells_closed"] = int(dead.sum())
+    return geo
+
+
+def closed_hill_case(nx: int, ny: int, nz: int, seed: int = 4, height: float = 600.0, halfwidth: float = 800.0,
+                     dx: float = 200.0) -> Geometry:
+    """Cut-cell Gaussian hill with roughness in a closed box (walls on all six
+    sides), stretched levels 50 -> 400 m, snapping and merging; the faces of
+    zero-volume cells closed.  The block of the pressure projection."""
+    grid = Grid(nx, ny, nz, dx, dx, stretched_levels(nz, 50.0, 400.0), False, False, False)
+    h = gaussian_hill_terrain(grid, height, halfwidth, 50.0, 600.0, seed=seed)
+    return close_dead_faces(cut_cell_geometry(grid, h, snap=0.01, merge=0.1))
+
+
+def projection_inputs(geo: Geometry, seed: int = 3, amp: float = 1.0):
+    """Seeded inputs of the pressure projection of a closed block: the sound
+    weights of WeightDiagCompute (DTU ~ potential temperature at the faces
+    ~300 K, DUT ~ dp/d(rho theta) ~400, DUU = F/(F+Eps), DTT = 1), the cell
+    widths, and a face-velocity increment of amplitude amp that vanishes on the
+    walls.  Returns (weights, dx, dy, dz, (u, v, w)); weights in the order
+    DTU, DTV, DTW, DUU, DUV, DUW, DUT, DTT with uF/vF/wF extents and interior
+    cell shapes (nz, ny, nx)."""
+    g = geo.grid
+    nx, ny, nz = g.nx, g.ny, g.nz
+    rng = np.random.default_rng(seed)
+    fu = geo.fu[:, :, 1:nx + 2]
+    fv = geo.fv[:, 1:ny + 2, :]
+    fw = geo.fw[1:nz + 2]
+    eps = 1.0e-30
+    duu, duv, duw = fu / (fu + eps), fv / (fv + eps), fw / (fw + eps)
+    dtu = 300.0 + 5.0 * rng.standard_normal(fu.shape)
+    dtv = 300.0 + 5.0 * rng.standard_normal(fv.shape)
+    dtw = 300.0 + 5.0 * rng.standard_normal(fw.shape)
+    dut = 400.0 + 10.0 * rng.standard_normal((nz, ny, nx))
+    dtt = np.ones((nz, ny, nx))
+    weights = [np.ascontiguousarray(a) for a in (dtu, dtv, dtw, duu, duv, duw, dut, dtt)]
+    dx = np.full(nx, g.dx)
+    dy = np.full(ny, g.dy)
+    dz = np.asarray(g.dz, dtype=np.float64).copy()
+    u = amp * rng.standard_normal(fu.shape) * (fu > 0)
+    v = amp * rng.standard_normal(fv.shape) * (fv > 0)
+    w = amp * rng.standard_normal(fw.shape) * (fw > 0)
+    u[:, :, 0] = u[:, :, nx] = 0.0
+    v[:, 0, :] = v[:, ny, :] = 0.0
+    w[0] = w[nz] = 0.0
+    return weights, dx, dy, dz, tuple(np.ascontiguousarray(a) for a in (u, v, w))
+
+
 def face_velocity(geo: Geometry, u0: float, v0: float = 0.0) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     """Prescribed steady face velocities with zero discrete divergence in flux form.
 

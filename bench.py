@@ -17,8 +17,9 @@ cells x steps / s).
 
 Arms:
   (default)          ours: FP64 drop-in path (value), plus the FP32-refined path
-                     (autotuned), the adjoint cost (128x128x64 hill, 40 steps)
-                     and the 48-domain batched ensemble
+                     (autotuned), the adjoint cost (128x128x64 hill, 40 steps),
+                     the 48-domain batched ensemble and the pressure projection
+                     (ProjectVelFace) of a closed block on the bench grid
   --impl reference   the reference's CPU path (the oracle restatement of the
                      Fortran; the Fortran itself has no compiler here), one
                      process per host core on independent blocks.
@@ -57,6 +58,7 @@ def parse():
     p.add_argument("--no-refined", action="store_true")
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--no-projection", action="store_true")
     p.add_argument("--batch-members", type=int, default=48)
     p.add_argument("--batch-steps", type=int, default=20)
     p.add_argument("--batch-threads", type=int, default=0, help="host threads driving the members (0: one each)")
@@ -297,6 +299,136 @@ def adjoint_cost(a, lib, torch, stream):
             "J": J.value}
 
 
+PROJ_BETA0 = 0.435866521508459  # beta0 of RosRK3 (the projection's beta0*dtP)
+
+
+def vcycle_bytes(n1, n2, n3, R, gi2=1, gi3=1):
+    """Algorithmic bytes of one multigrid V-cycle (Solve_3D, zebra order) on the
+    (z,x,y) = (n1,n2,n3) hierarchy with R levels, counted from its schedule:
+    per line-solve element 96 B (rhs b, the two neighbour-line x, the two x
+    couplings, the z sub-diagonal, the pivot and its reciprocal, x written;
+    the back substitution reads x and w and writes x), per plane right-hand
+    side element 48 B, per residual element 64 B (plane) / 88 B (3D), per
+    restriction fine element 8 B and coarse element 16 B, per prolongation fine
+    element 16 B and coarse element 8 B, plus the two layout passes (16 B per
+    cell each) of the call."""
+    cd = lambda n, L: (n + (1 << L) - 1) >> L  # noqa: E731
+
+    def mg2d(dims):
+        t = 0
+        nq = len(dims)
+        for q, (c1, c2) in enumerate(dims):
+            n = c1 * c2
+            t += (2 * (q * gi2 + 1) * 2 * n * 96) if c2 > 1 else 2 * n * 96
+            if q + 1 < nq:
+                nc = dims[q + 1][0] * dims[q + 1][1]
+                t += n * 64 + n * 8 + nc * 16 + n * 16 + nc * 8
+        return t
+
+    total = 2 * 16 * n1 * n2 * n3
+    for L in range(R):
+        m1, m2, m3 = cd(n1, L), cd(n2, L), cd(n3, L)
+        dims = [(cd(n1, L2), cd(n2, L2)) for L2 in range(L, R)]
+        plane = m1 * m2 * 48 + mg2d(dims)
+        gi = L * gi3 + 1
+        total += (2 * gi * 2 * m3 * plane) if m3 > 1 else 2 * plane
+        if L + 1 < R:
+            n = m1 * m2 * m3
+            nc = cd(n1, L + 1) * cd(n2, L + 1) * cd(n3, L + 1)
+            total += n * 88 + n * 8 + nc * 16 + n * 16 + nc * 8
+    return total
+
+
+def projection_bench(a, torch, stream, hbm_peak):
+    """Pressure projection (ProjectVelFace: Rhs, FGMRES(10) on MatVec1 with the
+    multigrid-preconditioned PSolve1, UpdateVelocity) of a closed-box cut-cell
+    hill on the bench grid (h=600 m, half-width 800 m plus roughness, dx=dy=200 m,
+    dz 50->400 m, RefLevel 4), seeded sound weights and face-velocity
+    increments, dtP = dt, beta0 of RosRK3; device-resident fields.  The CPU
+    baseline is the oracle (reference lexicographic smoother) on a 64x64x32
+    block of the same generator, single-threaded."""
+    import ctypes as C
+
+    import numpy as np
+
+    import asam_gb300
+    import oracle
+    from asam_gb300 import geometry as G
+
+    nx, ny, nz = a.nx, a.ny, a.nz
+    ncell = nx * ny * nz
+    # CPU baseline (reference ordering) on a small block
+    cgeo = G.closed_hill_case(64, 64, 32, seed=9)
+    cW, cdx, cdy, cdz, (cu, cv, cw) = G.projection_inputs(cgeo, seed=21)
+    t0 = time.perf_counter()
+    op = oracle.OracleProj(cgeo, cdx, cdy, cdz, cW, zebra=0)
+    op.lapl_compute(PROJ_BETA0, a.dt)
+    b = op.rhs(cu, cv, cw)
+    x = np.zeros_like(b)
+    csteps, _, _ = op.fgmres(x, b)
+    op.update(x, cu.copy(), cv.copy(), cw.copy())
+    cpu_s = time.perf_counter() - t0
+    op.close()
+
+    geo = G.closed_hill_case(nx, ny, nz, seed=9)
+    W, dx, dy, dz, (u, v, w) = G.projection_inputs(geo, seed=21)
+    blk = asam_gb300.TransportBlock(geo, 3, rho_pos=0)
+    blk.set_stream(stream.cuda_stream)
+    blk.proj_setup(dx, dy, dz)
+    blk.proj_weights(*W)
+    lib = blk.lib
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    assemble_ms = time_region(torch, stream, lambda: blk.JacAccGrav(PROJ_BETA0, a.dt), 2) / 2
+    du0, dv0, dw0 = (torch.from_numpy(q).cuda() for q in (u, v, w))
+    du, dv, dw = du0.clone(), dv0.clone(), dw0.clone()
+    incr = torch.zeros((3,) + geo.grid.pshape, dtype=torch.float64, device="cuda")
+    steps, res = C.c_int(), C.c_double()
+
+    def project():
+        du.copy_(du0)
+        dv.copy_(dv0)
+        dw.copy_(dw0)
+        rc = lib.asam_project_vel_face(blk.h, P(du), P(dv), P(dw), P(incr), None, 1, 0, None, 0, None,
+                                       C.byref(steps), C.byref(res))
+        if rc not in (0, 1):
+            raise RuntimeError(f"asam_project_vel_face: {rc}")
+
+    for _ in range(2):
+        project()
+    n_rep = 3
+    l0 = lib.asam_launch_count()
+    v0 = lib.asam_proj_vcycles(blk.h)
+    proj_ms = time_region(torch, stream, project, n_rep) / n_rep
+    launches = (lib.asam_launch_count() - l0) // n_rep
+    vcyc = (lib.asam_proj_vcycles(blk.h) - v0) // n_rep
+    bb = torch.randn(nz, ny, nx, dtype=torch.float64, device="cuda")
+    xx = torch.zeros_like(bb)
+    vc_ms = time_region(torch, stream, lambda: lib.asam_lapl_vcycle(blk.h, P(bb), P(xx)), 3) / 3
+    yy = torch.zeros_like(bb)
+    lib.asam_lapl_matvec(blk.h, P(xx), P(yy))
+    red = float(torch.linalg.norm(bb - yy) / torch.linalg.norm(bb))
+    vb = vcycle_bytes(nz, nx, ny, 4)
+    gbs = vb / (vc_ms * 1e-3) / 1e9
+    blk.close()
+    return {
+        "workload": f"closed-box cut-cell hill {nx}x{ny}x{nz} (h=600 m, half-width 800 m, roughness 50 m / 600 m, "
+                    f"dx=dy=200 m, dz 50->400 m), RefLevel 4, FGMRES(10) QMRTol 1e-6, dtP={a.dt} s, "
+                    "seeded sound weights and velocity increments",
+        "metric": "Mcell-projections/s", "value": ncell / (proj_ms * 1e-3) / 1e6, "ms_per_projection": proj_ms,
+        "fgmres_steps": steps.value, "fgmres_rel_residual": res.value, "vcycles_per_projection": vcyc,
+        "assemble_ms": assemble_ms, "vcycle_ms": vc_ms, "vcycle_residual_reduction": red,
+        "gpu_launches_per_projection": launches,
+        "roofline": {"kernel": "one V-cycle (k_plane_half zebra plane/line relaxations + 3D residual, restriction, "
+                               "prolongation)", "bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": gbs / hbm_peak, "algorithmic_bytes_per_call": vb, "traffic": None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+        "cpu_baseline": {"value": 64 * 64 * 32 / cpu_s / 1e6, "unit": "Mcell-projections/s", "cores": 1,
+                         "kind": "port", "sample": f"64x64x32 block of the same generator, oracle restatement with the "
+                                                   f"reference's lexicographic smoother, {csteps} FGMRES steps "
+                                                   f"({cpu_s:.1f} s)"},
+    }
+
+
 def batch_members(n, seed=4):
     """Ensemble of independent cut-cell domains: sizes between 64x64x48 and
     192x160x96, Gaussian hill 0-1.5 km high with half-width 2-8 km, u 5-15 m/s,
@@ -532,6 +664,11 @@ def main():
     bat = None
     if not a.no_batch and world == 1:
         bat = batch_bench(a, torch, batch_members(a.batch_members))
+    proj = None
+    if not a.no_projection and world == 1:
+        pk0 = ROOT / "MEASURED_PEAKS.json"
+        hp = json.loads(pk0.read_text()).get("hbm_gbs", 6800.0) if pk0.exists() else 6800.0
+        proj = projection_bench(a, torch, stream, hp)
     if "fp64" not in results:  # a profiling run of one variant: no comparison line
         rr = results[precs[0]]
         if rank == 0:
@@ -634,6 +771,8 @@ def main():
         line["adjoint"] = adj
     if bat is not None:
         line["batch"] = bat
+    if proj is not None:
+        line["projection"] = proj
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if rank == 0:

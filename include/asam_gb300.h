@@ -226,6 +226,73 @@ int asam_tri_solve_noalloc(int ncol, int n1, const double *d, const double *u, c
 /* y = T x for the same column batch, MatVecT_1D (MULTI/TriDiagT_Mod.f90:113-133). */
 int asam_tri_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x, double *y);
 
+/* ---- Pressure projection (sound solve) of a closed block --------------------
+ * ProjectVelFace (ADVECT/IntSub_Mod.f90:25-71) with MultiTriT, GradFull and
+ * MethSound='FGMRES': Rhs (MATRIX/Rhs_Mod.f90:110-187), FGMRES(StepGMRES)
+ * (SOLU/Iter_Mod.f90:121-199) on MatVec1 = MatVecFull (MATRIX/MatVec_Mod.f90:184)
+ * preconditioned by PSolve1 (MATRIX/PreCond_Mod.f90:1555), whose pressure
+ * block is the semi-coarsening multigrid Solve_3D (MULTI/TriDiagT_Mod.f90:1073)
+ * on the tridiagonal Laplacian hierarchy of LaplTFullCompute
+ * (MULTI/JacAccGrav_Mod.f90:1056), then UpdateVelocity (Rhs_Mod.f90:589).
+ * Scope: blocks whose six sides are closed outer boundaries (no periodic
+ * sides, no boundary pressure unknowns), default orders (z,x,y) and
+ * coarsening factors 2.  The multigrid relaxes planes and x-lines of one
+ * parity concurrently (zebra order of the reference's plane/line
+ * Gauss-Seidel; each relaxation is the reference's arithmetic).
+ * Interior cell fields below are nx*ny*nz doubles, x fastest (p(1,ix0+1:ix1,..)).
+ */
+typedef struct {
+  int ref_level;   /* RefLevel of the block (grid input; 4 for generated blocks) */
+  int gauss_iter2; /* GaussIter2 (Control_Mod.f90:55, default 1) */
+  int gauss_iter3; /* GaussIter3 (default 1) */
+  int mult_iter2;  /* MultIter2 (default 1) */
+  int mult_iter3;  /* MultIter3 (default 1) */
+  int step_gmres;  /* StepGMRES (Control_Mod.f90:66, default 10) */
+  int max_restart; /* QMRMaxIter (Control_Mod.f90:583, default 10) */
+  double tol;      /* QMRTol (Control_Mod.f90:582, default 1e-6) */
+  double fac_anela;/* FacAnela (MODULE/Physics_Mod.f90:117, 1 = compressible) */
+} asam_proj_config;
+
+/* Set up the projection of a context: dx[nx], dy[ny], dz[nz] cell widths and
+ * metr = MetrXY[ny], MetrXZ[nz], MetrYX[nx], MetrYZ[nz], MetrZX[nx], MetrZY[ny]
+ * back to back (NULL: all 1, Cartesian).  Allocates the hierarchy. */
+int asam_proj_setup(asam_ctx *ctx, const asam_proj_config *cfg, const double *dx, const double *dy, const double *dz,
+                    const double *metr);
+/* Sound weights of WeightDiagCompute (MULTI/JacAccGrav_Mod.f90:4152-4391):
+ * DTU/DUU with uF extents, DTV/DUV vF, DTW/DUW wF; DUT and DTT interior. */
+int asam_proj_weights(asam_ctx *ctx, const double *dtu, const double *dtv, const double *dtw, const double *duu,
+                      const double *duv, const double *duw, const double *dut, const double *dtt);
+/* LaplTFullCompute with the Neumann factors of SetFactorN
+ * (MULTI/JacAccGrav_Mod.f90:1056-1310, MULTI/Reverse_Mod.f90:225-292) for
+ * beta0 and dtP = dt (ADVECT/Int_Mod.f90:293-295). */
+int asam_lapl_compute(asam_ctx *ctx, double beta0, double dtp);
+/* Export one assembled array of 3D level level3 and plane level level2
+ * (>= level3) in the reversed order (z fastest, then x, then y):
+ * which 0 diagonal, 1/2 z couplings u/l, 3/4 x couplings, 5/6 y couplings
+ * (level2 == level3 only); entries past the last row/line/plane are 0.
+ * Returns the count (out may be NULL), -1 on error.  Diagnostic. */
+long asam_lapl_get(asam_ctx *ctx, int level3, int level2, int which, double *out);
+/* y = A x, MatVecP_Tri (MULTI/JacAccGrav_Mod.f90:531-545). */
+int asam_lapl_matvec(asam_ctx *ctx, const double *x, double *y);
+/* x = one Solve_3D from x=0 (VCycleCG, MULTI/JacAccGrav_Mod.f90:4466-4517). */
+int asam_lapl_vcycle(asam_ctx *ctx, const double *b, double *x);
+/* SolveSound / FGMRES (SOLU/Iter_Mod.f90:9-199): x in/out (start value),
+ * *maxiter in: restarts (QMRMaxIter), out: inner steps taken; *tol in:
+ * relative tolerance, out: final residual estimate / initial residual.
+ * ASAM_NOT_CONVERGED when the tolerance was not reached. */
+int asam_solve_sound(asam_ctx *ctx, double *x, const double *b, int *maxiter, double *tol);
+/* ProjectVelFace for one stage (ADVECT/IntSub_Mod.f90:25-71): uf/vf/wf the
+ * face-velocity increments (updated), incr the cell increments of all
+ * components (ncomp*npad, updated: th_pos, rho_pos and the listed scalars
+ * via DivScalar), state the old state (needed when nscalar > 0); th_pos /
+ * rho_pos 0-based or -1; pressure (nullable) receives x*DUT; steps and
+ * resid (nullable) the FGMRES inner steps and relative residual. */
+int asam_project_vel_face(asam_ctx *ctx, double *uf, double *vf, double *wf, double *incr, const double *state,
+                          int th_pos, int rho_pos, const int *scalars, int nscalar, double *pressure, int *steps,
+                          double *resid);
+/* Number of multigrid V-cycles run by this context's projection (diagnostic). */
+long long asam_proj_vcycles(asam_ctx *ctx);
+
 /* DOT(VecMet,VecMet): the interior dot product of the state with itself over
  * all components (Dot_VecCell, MODULE/Vector4CellPar_Mod.f90:84-102), which the
  * reference's driver checks for NaN after every step

@@ -57,6 +57,20 @@ def load() -> C.CDLL:
             "ora_tri_solve": (None, [I, I, V, V, V, V]),
             "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
         }
+        sig.update({
+            "ora_proj_create": (V, [C.POINTER(C.c_int), C.POINTER(C.c_double)] + [V] * 16),
+            "ora_proj_destroy": (None, [V]),
+            "ora_proj_set_zebra": (None, [V, I]),
+            "ora_lapl_compute": (None, [V, D, D]),
+            "ora_lapl_get": (C.c_long, [V, I, I, I, V]),
+            "ora_lapl_matvec": (None, [V, V, V]),
+            "ora_lapl_vcycle": (None, [V, V, V]),
+            "ora_psolve1": (None, [V, V, V]),
+            "ora_matvec1": (None, [V, V, V]),
+            "ora_fgmres": (I, [V, V, V, I, D, I, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+            "ora_proj_rhs": (None, [V, V, V, V, V, V]),
+            "ora_proj_update": (None, [V, V, V, V, V, V, V, I, V, V, V]),
+        })
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
             f.restype = res
@@ -189,3 +203,92 @@ def tri_matvec(d, u, l, x):
     y = np.empty_like(xx)
     lib.ora_tri_matvec(ncol, n1, _p(d), _p(u), _p(l), _p(xx), _p(y))
     return y
+
+
+class OracleProj:
+    """Oracle of the pressure projection of one closed block (oracle/asam_proj.c).
+
+    Arrays use the same Fortran layouts as the library: faces with uF/vF/wF
+    extents, interior cell fields (nz, ny, nx), padded state fields."""
+
+    def __init__(self, geo, dx, dy, dz, weights, metr=None, ref_level=4, gauss_iter2=1, gauss_iter3=1, mult_iter2=1,
+                 mult_iter3=1, zebra=1, fac_anela=1.0):
+        self.lib = load()
+        g = geo.grid
+        self.grid = g
+        n = 2 * (g.nx + g.ny + g.nz)
+        metr = np.ones(n) if metr is None else metr
+        self._keep = [np.ascontiguousarray(a, dtype=np.float64) for a in
+                      (geo.fu, geo.fv, geo.fw, geo.volc, *weights, dx, dy, dz, metr)]
+        ip = (C.c_int * 9)(g.nx, g.ny, g.nz, ref_level, gauss_iter2, gauss_iter3, mult_iter2, mult_iter3, zebra)
+        dp = (C.c_double * 1)(fac_anela)
+        self.h = self.lib.ora_proj_create(ip, dp, *[_p(a) for a in self._keep])
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ora_proj_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_zebra(self, on: bool):
+        self.lib.ora_proj_set_zebra(self.h, int(on))
+
+    def lapl_compute(self, beta0, dtp):
+        self.lib.ora_lapl_compute(self.h, beta0, dtp)
+
+    def lapl_get(self, level3, level2, which):
+        n = self.lib.ora_lapl_get(self.h, level3, level2, which, None)
+        out = np.empty(n)
+        self.lib.ora_lapl_get(self.h, level3, level2, which, _p(out))
+        return out
+
+    def _cell(self):
+        g = self.grid
+        return np.empty((g.nz, g.ny, g.nx))
+
+    def matvec(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = self._cell()
+        self.lib.ora_lapl_matvec(self.h, _p(x), _p(y))
+        return y
+
+    def vcycle(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = self._cell()
+        self.lib.ora_lapl_vcycle(self.h, _p(b), _p(x))
+        return x
+
+    def psolve1(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        b = self._cell()
+        self.lib.ora_psolve1(self.h, _p(x), _p(b))
+        return b
+
+    def matvec1(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        b = self._cell()
+        self.lib.ora_matvec1(self.h, _p(x), _p(b))
+        return b
+
+    def fgmres(self, x, b, maxiter=10, tol=1e-6, step=10):
+        """x updated in place; returns (inner steps, rho, rho0)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        rho, rho0 = C.c_double(), C.c_double()
+        steps = self.lib.ora_fgmres(self.h, _p(x), _p(b), maxiter, tol, step, C.byref(rho), C.byref(rho0))
+        return steps, rho.value, rho0.value
+
+    def rhs(self, u, v, w, incr_th=None):
+        b = self._cell()
+        self.lib.ora_proj_rhs(self.h, _p(u), _p(v), _p(w), None if incr_th is None else _p(incr_th), _p(b))
+        return b
+
+    def update(self, x, u, v, w, incr_th=None, incr_rho=None, incr_c=(), c=(), rho=None):
+        """UpdateVelocity in place (x becomes x*DUT)."""
+        nc = len(incr_c)
+        pi = (C.c_void_p * max(1, nc))(*[_p(a) for a in incr_c])
+        pc = (C.c_void_p * max(1, nc))(*[_p(a) for a in c])
+        self.lib.ora_proj_update(self.h, _p(x), _p(u), _p(v), _p(w), None if incr_th is None else _p(incr_th),
+                                 None if incr_rho is None else _p(incr_rho), nc, pi, pc,
+                                 None if rho is None else _p(rho))

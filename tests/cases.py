@@ -32,6 +32,28 @@ def _hill(nx, ny, nz, u0=10.0, v0=0.0, seed=2, height=600.0, halfwidth=800.0):
     return geo, vel, st
 
 
+def _hill_closed(nx, ny, nz, seed=4, height=600.0, halfwidth=800.0):
+    return G.closed_hill_case(nx, ny, nz, seed=seed, height=height, halfwidth=halfwidth)
+
+
+def _flat_closed(nx, ny, nz):
+    grid = G.Grid(nx, ny, nz, 100.0, 100.0, G.uniform_levels(nz, 100.0), False, False, False)
+    return G.cut_cell_geometry(grid, None, snap=0.0, merge=0.0)
+
+
+def proj_inputs(geo, seed=3, amp=1.0):
+    return G.projection_inputs(geo, seed=seed, amp=amp)
+
+
+PROJ_CASES = {
+    "proj_hill_24x20x16": lambda: _hill_closed(24, 20, 16),
+    "proj_hill_odd_13x7x9": lambda: _hill_closed(13, 7, 9, seed=6),
+    "proj_flat_16x12x10": lambda: _flat_closed(16, 12, 10),
+    "proj_column_1x1x12": lambda: _flat_closed(1, 1, 12),
+    "proj_slab_9x1x6": lambda: _flat_closed(9, 1, 6),
+}
+
+
 CASES = {
     "bubble_12x10x8": lambda: _flat(12, 10, 8),
     "hill_24x20x16": lambda: _hill(24, 20, 16),
@@ -44,7 +66,7 @@ CASES = {
 
 @functools.lru_cache(maxsize=None)
 def get(name: str):
-    return CASES[name]()
+    return CASES[name]() if name in CASES else PROJ_CASES[name]()
 
 
 def relerr(a: np.ndarray, b: np.ndarray) -> float:

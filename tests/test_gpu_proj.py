@@ -1,0 +1,157 @@
+"""GPU parity of the pressure projection against the oracle (oracle/asam_proj.c).
+
+Bit-exact: every array of the assembled Laplacian hierarchy (all 3D levels and
+their plane levels), the operator MatVecP_Tri and one multigrid V-cycle in the
+zebra ordering.  Within the Krylov tolerance (the dot products are reduced in
+a different order): FGMRES and the whole ProjectVelFace.  The reference's
+lexicographic ordering (oracle) and the GPU's zebra ordering agree to the
+Krylov tolerance.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from asam_gb300 import AsamError, TransportBlock
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+BETA0, DTP = 0.435866521508459, 2.0
+PROJ = ["proj_hill_24x20x16", "proj_hill_odd_13x7x9", "proj_flat_16x12x10", "proj_column_1x1x12", "proj_slab_9x1x6"]
+REF_LEVEL = 4
+
+
+def _pair(name, zebra=1, ref_level=REF_LEVEL):
+    geo = cases.get(name)
+    W, dx, dy, dz, vel = cases.proj_inputs(geo)
+    blk = TransportBlock(geo, ncomp=3, rho_pos=0)
+    blk.proj_setup(dx, dy, dz, ref_level=ref_level)
+    blk.proj_weights(*W)
+    blk.JacAccGrav(BETA0, DTP)
+    o = oracle.OracleProj(geo, dx, dy, dz, W, zebra=zebra, ref_level=ref_level)
+    o.lapl_compute(BETA0, DTP)
+    return geo, W, vel, blk, o
+
+
+@pytest.mark.parametrize("name", PROJ)
+def test_hierarchy_bitwise(name):
+    geo, W, vel, blk, o = _pair(name)
+    with blk:
+        for L3 in range(REF_LEVEL):
+            for L2 in range(L3, REF_LEVEL):
+                for which in range(7 if L2 == L3 else 5):
+                    np.testing.assert_array_equal(blk.lapl_array(L3, L2, which), o.lapl_get(L3, L2, which),
+                                                  err_msg=f"level {L3}/{L2} array {which}")
+
+
+@pytest.mark.parametrize("name", PROJ)
+def test_matvec_and_vcycle_bitwise(name):
+    geo, W, vel, blk, o = _pair(name)
+    g = geo.grid
+    rng = np.random.default_rng(11)
+    with blk:
+        for _ in range(2):
+            x = rng.standard_normal((g.nz, g.ny, g.nx))
+            np.testing.assert_array_equal(blk.MatVecP(x), o.matvec(x))
+            b = rng.standard_normal((g.nz, g.ny, g.nx))
+            np.testing.assert_array_equal(blk.VCycleCG(b), o.vcycle(b))
+
+
+@pytest.mark.parametrize("name", PROJ)
+def test_solve_sound_matches_oracle(name):
+    geo, W, (u, v, w), blk, o = _pair(name)
+    with blk:
+        b = o.rhs(u, v, w)
+        x_ref = np.zeros_like(b)
+        steps_ref, rho, rho0 = o.fgmres(x_ref, b, maxiter=10, tol=1e-6, step=10)
+        x = np.zeros_like(b)
+        steps, rel = blk.SolveSound(x, b, MaxIter=10, Tol=1e-6)
+        assert abs(steps - steps_ref) <= 1
+        assert rel <= 1e-6
+        scale = max(np.max(np.abs(x_ref)), 1e-300)
+        # same Krylov subspace: the iterates differ by the rounding of the dots
+        tol = 1e-9 if steps == steps_ref else 1e-5
+        assert np.max(np.abs(x - x_ref)) <= tol * scale
+
+
+def _state(geo, ncomp, seed):
+    g = geo.grid
+    rng = np.random.default_rng(seed)
+    st = np.empty((ncomp,) + g.pshape)
+    st[0] = 1.0 + 0.1 * rng.random(g.pshape)
+    st[1] = st[0] * (300.0 + rng.random(g.pshape))
+    st[2] = st[0] * rng.random(g.pshape)
+    return st
+
+
+@pytest.mark.parametrize("name", ["proj_hill_24x20x16", "proj_hill_odd_13x7x9", "proj_flat_16x12x10", "proj_slab_9x1x6"])
+def test_project_vel_face_matches_oracle(name):
+    geo, W, (u, v, w), blk, o = _pair(name)
+    g = geo.grid
+    rng = np.random.default_rng(13)
+    state = _state(geo, 3, 17)
+    incr = rng.standard_normal((3,) + g.pshape)
+    with blk:
+        u1, v1, w1, incr1 = u.copy(), v.copy(), w.copy(), incr.copy()
+        p, steps, rel = blk.ProjectVelFace(u1, v1, w1, incr1, state, th_pos=1, rho_pos=0, scalars=[2])
+        u2, v2, w2, incr2 = u.copy(), v.copy(), w.copy(), incr.copy()
+        b = o.rhs(u2, v2, w2, incr_th=incr2[1])
+        x = np.zeros_like(b)
+        o.fgmres(x, b, maxiter=10, tol=1e-6, step=10)
+        o.update(x, u2, v2, w2, incr_th=incr2[1], incr_rho=incr2[0], incr_c=[incr2[2]], c=[state[2]], rho=state[0])
+        assert rel <= 1e-6
+        for got, ref in ((u1, u2), (v1, v2), (w1, w2), (incr1, incr2), (p, x)):
+            scale = max(np.max(np.abs(ref)), 1e-300)
+            assert np.max(np.abs(got - ref)) <= 1e-8 * scale
+
+
+@pytest.mark.parametrize("name", ["proj_hill_24x20x16", "proj_flat_16x12x10"])
+def test_zebra_vs_reference_ordering(name):
+    geo, W, (u, v, w), blk, o = _pair(name, zebra=0)
+    with blk:
+        b = o.rhs(u, v, w)
+        x_ref = np.zeros_like(b)
+        o.fgmres(x_ref, b, maxiter=20, tol=1e-12, step=10)
+        x = np.zeros_like(b)
+        blk.SolveSound(x, b, MaxIter=20, Tol=1e-12)
+        live = geo.volc[1:-1, 1:-1, 1:-1] > 0
+        assert np.max(np.abs(x - x_ref)[live]) <= 1e-9 * np.max(np.abs(x_ref)[live])
+
+
+def test_larger_block_converges():
+    geo = cases._hill_closed(96, 80, 48, seed=9)
+    W, dx, dy, dz, (u, v, w) = cases.proj_inputs(geo, seed=21)
+    g = geo.grid
+    with TransportBlock(geo, ncomp=3, rho_pos=0) as blk:
+        blk.proj_setup(dx, dy, dz)
+        blk.proj_weights(*W)
+        blk.JacAccGrav(BETA0, DTP)
+        rng = np.random.default_rng(3)
+        b = rng.standard_normal((g.nz, g.ny, g.nx))
+        x = blk.VCycleCG(b)
+        assert np.linalg.norm(b - blk.MatVecP(x)) / np.linalg.norm(b) < 0.05
+        x = np.zeros_like(b)
+        steps, rel = blk.SolveSound(x, b)
+        assert rel <= 1e-6 and steps <= 60
+        true = np.linalg.norm(b + blk.MatVecP(x)) / np.linalg.norm(b)  # MatVec1 = -A
+        assert true <= 2e-6
+
+
+def test_bad_calls_raise():
+    geo = cases.get("proj_flat_16x12x10")
+    W, dx, dy, dz, _ = cases.proj_inputs(geo)
+    with TransportBlock(geo, ncomp=3, rho_pos=0) as blk:
+        with pytest.raises(AsamError):
+            blk.JacAccGrav(BETA0, DTP)  # no set-up
+        blk.proj_setup(dx, dy, dz)
+        with pytest.raises(AsamError):
+            blk.JacAccGrav(BETA0, DTP)  # no weights
+        with pytest.raises(AsamError):
+            blk.proj_setup(dx, dy, dz, ref_level=0)
+    per = cases.get("bubble_12x10x8")[0]
+    with TransportBlock(per, ncomp=3, rho_pos=0) as blk:
+        g = per.grid
+        with pytest.raises(AsamError):
+            blk.proj_setup(np.full(g.nx, g.dx), np.full(g.ny, g.dy), g.dz)
