@@ -272,6 +272,23 @@ class TransportBlock:
         arrs = [_f64(a) for a in (dtu, dtv, dtw, duu, duv, duw, dut, dtt)]
         check(self.lib.asam_proj_weights(self.h, *[ptr(a) for a in arrs]), "asam_proj_weights")
 
+    def WeightDiagCompute(self, state, tabs, th_pos: int, rho_pos: int, rv_pos: int = -1, rc_pos: int = -1,
+                          rr_pos: int = -1):
+        """Sound weights of ThetaKind='Density' from the state and the absolute
+        temperature (padded), computed on the device."""
+        st = self._state(state)
+        t = _f64(tabs)
+        check(self.lib.asam_proj_weights_density(self.h, ptr(st), th_pos, rho_pos, rv_pos, rc_pos, rr_pos, ptr(t)),
+              "asam_proj_weights_density")
+
+    def proj_weight(self, which: int) -> np.ndarray:
+        n = self.lib.asam_proj_get_weights(self.h, which, None)
+        if n < 0:
+            raise ValueError("no weights")
+        out = np.empty(n)
+        self.lib.asam_proj_get_weights(self.h, which, ptr(out))
+        return out
+
     def JacAccGrav(self, beta0: float, dtp: float):
         """Assemble the tridiagonal pressure-Laplacian hierarchy (LaplTFullCompute)."""
         check(self.lib.asam_lapl_compute(self.h, float(beta0), float(dtp)), "asam_lapl_compute")

@@ -82,6 +82,8 @@ SIGNATURES = [
     ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_proj_setup", C.c_int, [_V, C.POINTER(AsamProjConfig), _V, _V, _V, _V]),
     ("asam_proj_weights", C.c_int, [_V, _V, _V, _V, _V, _V, _V, _V, _V]),
+    ("asam_proj_weights_density", C.c_int, [_V, _V, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _V]),
+    ("asam_proj_get_weights", C.c_long, [_V, C.c_int, _V]),
     ("asam_lapl_compute", C.c_int, [_V, C.c_double, C.c_double]),
     ("asam_lapl_get", C.c_long, [_V, C.c_int, C.c_int, C.c_int, _V]),
     ("asam_lapl_matvec", C.c_int, [_V, _V, _V]),

@@ -64,24 +64,27 @@ struct Lev3 {
   double *u3, *l3, *x, *b, *res, *t;
 };
 
-// Input fields of one level in the natural reversed layout (1-based logical
-// indices): F1(0:n1,1:n2,1:n3), F2(1:n1,0:n2,1:n3), F3(1:n1,1:n2,0:n3),
-// cell arrays (1:n1,1:n2,1:n3).
+// Input fields of one level in the reversed index space with 1-based logical
+// indices F1(0:n1,1:n2,1:n3), F2(1:n1,0:n2,1:n3), F3(1:n1,1:n2,0:n3) and cell
+// arrays (1:n1,1:n2,1:n3).  In memory the x index (n2) runs fastest, then z
+// (n1), then y (n3) -- the order of the Fortran inputs, so reading them and
+// writing the level layout are both coalesced.  Every coarse sum follows the
+// reference's loop order whatever the memory order.
 struct Fields {
   int n1, n2, n3;
   double *F1, *T1, *U1, *F2, *T2, *U2, *F3, *T3, *U3, *vol, *dut;
   double *d1, *d2, *d3, *m12, *m13, *m21, *m23, *m31, *m32;
   __host__ __device__ size_t i1(int i, int j, int k) const {
-    return (size_t)i + (size_t)(n1 + 1) * ((size_t)(j - 1) + (size_t)n2 * (size_t)(k - 1));
+    return (size_t)(j - 1) + (size_t)n2 * ((size_t)i + (size_t)(n1 + 1) * (size_t)(k - 1));
   }
   __host__ __device__ size_t i2(int i, int j, int k) const {
-    return (size_t)(i - 1) + (size_t)n1 * ((size_t)j + (size_t)(n2 + 1) * (size_t)(k - 1));
+    return (size_t)j + (size_t)(n2 + 1) * ((size_t)(i - 1) + (size_t)n1 * (size_t)(k - 1));
   }
   __host__ __device__ size_t i3(int i, int j, int k) const {
-    return (size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * (size_t)k);
+    return (size_t)(j - 1) + (size_t)n2 * ((size_t)(i - 1) + (size_t)n1 * (size_t)k);
   }
   __host__ __device__ size_t ic(int i, int j, int k) const {
-    return (size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * (size_t)(k - 1));
+    return (size_t)(j - 1) + (size_t)n2 * ((size_t)(i - 1) + (size_t)n1 * (size_t)(k - 1));
   }
 };
 
@@ -111,12 +114,12 @@ __global__ void k_fine_fields(Dims d, const double* __restrict__ fu, const doubl
                               const double* __restrict__ duv, const double* __restrict__ duw,
                               const double* __restrict__ dut, Fields g) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
-  const size_t n = (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+  const size_t n = (size_t)(nx + 1) * (nz + 1) * (ny + 1);
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     const int x = (int)(e % (nx + 1));
     const size_t r = e / (nx + 1);
-    const int y = (int)(r % (ny + 1));
-    const int z = (int)(r / (ny + 1));
+    const int z = (int)(r % (nz + 1));
+    const int y = (int)(r / (nz + 1));
     if (x >= 1 && y >= 1) {  // F1 = FW(x,y,z), z = 0..nz
       const size_t q = g.i1(z, x, y);
       g.F1[q] = fw[d.FW(x, y, z)];
@@ -184,9 +187,9 @@ __global__ void k_coarse_faces(Fields g, Fields c, int s1, int s2, int s3) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
     double F = 0.0, TF = 0.0, UF = 0.0;
     if (e < n1f) {
-      const int iC = (int)(e % (nC + 1));
-      const size_t r = e / (nC + 1);
-      const int jC = (int)(r % mC) + 1, kC = (int)(r / mC) + 1;
+      const int jC = (int)(e % mC) + 1;
+      const size_t r = e / mC;
+      const int iC = (int)(r % (nC + 1)), kC = (int)(r / (nC + 1)) + 1;
       const int i = min((s1 + 1) * iC, n);
       for (int j = blo(jC, s2); j <= bhi(jC, s2, m); ++j)
         for (int k = blo(kC, s3); k <= bhi(kC, s3, l); ++k) {
@@ -202,9 +205,9 @@ __global__ void k_coarse_faces(Fields g, Fields c, int s1, int s2, int s3) {
       c.U1[qc] = UF / (F + asam::kEps);
     } else if (e < n1f + n2f) {
       const size_t ee = e - n1f;
-      const int iC = (int)(ee % nC) + 1;
-      const size_t r = ee / nC;
-      const int jC = (int)(r % (mC + 1)), kC = (int)(r / (mC + 1)) + 1;
+      const int jC = (int)(ee % (mC + 1));
+      const size_t r = ee / (mC + 1);
+      const int iC = (int)(r % nC) + 1, kC = (int)(r / nC) + 1;
       const int j = min((s2 + 1) * jC, m);
       for (int i = blo(iC, s1); i <= bhi(iC, s1, n); ++i)
         for (int k = blo(kC, s3); k <= bhi(kC, s3, l); ++k) {
@@ -220,9 +223,9 @@ __global__ void k_coarse_faces(Fields g, Fields c, int s1, int s2, int s3) {
       c.U2[qc] = UF / (F + asam::kEps);
     } else {
       const size_t ee = e - n1f - n2f;
-      const int iC = (int)(ee % nC) + 1;
-      const size_t r = ee / nC;
-      const int jC = (int)(r % mC) + 1, kC = (int)(r / mC);
+      const int jC = (int)(ee % mC) + 1;
+      const size_t r = ee / mC;
+      const int iC = (int)(r % nC) + 1, kC = (int)(r / nC);
       const int k = min((s3 + 1) * kC, l);
       for (int i = blo(iC, s1); i <= bhi(iC, s1, n); ++i)
         for (int j = blo(jC, s2); j <= bhi(jC, s2, m); ++j) {
@@ -244,9 +247,9 @@ __global__ void k_coarse_faces(Fields g, Fields c, int s1, int s2, int s3) {
 __global__ void k_coarse_cells(Fields g, Fields c, int s1, int s2, int s3) {
   const size_t tot = (size_t)c.n1 * c.n2 * c.n3;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
-    const int iC = (int)(e % c.n1) + 1;
-    const size_t r = e / c.n1;
-    const int jC = (int)(r % c.n2) + 1, kC = (int)(r / c.n2) + 1;
+    const int jC = (int)(e % c.n2) + 1;
+    const size_t r = e / c.n2;
+    const int iC = (int)(r % c.n1) + 1, kC = (int)(r / c.n1) + 1;
     double V = 0.0, DV = 0.0;
     for (int i = blo(iC, s1); i <= bhi(iC, s1, g.n1); ++i)
       for (int j = blo(jC, s2); j <= bhi(jC, s2, g.n2); ++j)
@@ -261,27 +264,43 @@ __global__ void k_coarse_cells(Fields g, Fields c, int s1, int s2, int s3) {
   }
 }
 
-// IncrCoarse + CIncrCoarse (JacAccGrav_Mod.f90:747-782), one thread
+// IncrCoarse + CIncrCoarse (JacAccGrav_Mod.f90:747-782), one block: every
+// coarse entry sums its fine entries in increasing order (the reference's
+// loop order), the increments first
+__device__ inline void incr_entry(const double* d, int n, double* dc, int ic, int s) {
+  double v = 0.0;
+  for (int i = ic * (s + 1) + 1; i <= min((ic + 1) * (s + 1), n); ++i) v = v + d[i - 1];
+  dc[ic] = v;
+}
+__device__ inline void cincr_entry(const double* C, const double* d, int n, double* CC, const double* dc, int ic, int s) {
+  double v = 0.0;
+  for (int i = ic * (s + 1) + 1; i <= min((ic + 1) * (s + 1), n); ++i) v = v + d[i - 1] * C[i - 1];
+  CC[ic] = v / dc[ic];
+}
 __global__ void k_coarse_1d(Fields g, Fields c, int s1, int s2, int s3) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  auto incr = [](const double* d, int n, double* dc, int nc, int s) {
-    for (int i = 0; i < nc; ++i) dc[i] = 0.0;
-    for (int i = 1; i <= n; ++i) dc[(i + s) / (s + 1) - 1] = dc[(i + s) / (s + 1) - 1] + d[i - 1];
-  };
-  auto cincr = [](const double* C, const double* d, int n, double* CC, const double* dc, int nc, int s) {
-    for (int i = 0; i < nc; ++i) CC[i] = 0.0;
-    for (int i = 1; i <= n; ++i) CC[(i + s) / (s + 1) - 1] = CC[(i + s) / (s + 1) - 1] + d[i - 1] * C[i - 1];
-    for (int i = 0; i < nc; ++i) CC[i] = CC[i] / dc[i];
-  };
-  incr(g.d1, g.n1, c.d1, c.n1, s1);
-  incr(g.d2, g.n2, c.d2, c.n2, s2);
-  incr(g.d3, g.n3, c.d3, c.n3, s3);
-  cincr(g.m12, g.d2, g.n2, c.m12, c.d2, c.n2, s2);
-  cincr(g.m13, g.d3, g.n3, c.m13, c.d3, c.n3, s3);
-  cincr(g.m21, g.d1, g.n1, c.m21, c.d1, c.n1, s1);
-  cincr(g.m23, g.d3, g.n3, c.m23, c.d3, c.n3, s3);
-  cincr(g.m31, g.d1, g.n1, c.m31, c.d1, c.n1, s1);
-  cincr(g.m32, g.d2, g.n2, c.m32, c.d2, c.n2, s2);
+  for (int q = threadIdx.x; q < c.n1 + c.n2 + c.n3; q += blockDim.x) {
+    if (q < c.n1)
+      incr_entry(g.d1, g.n1, c.d1, q, s1);
+    else if (q < c.n1 + c.n2)
+      incr_entry(g.d2, g.n2, c.d2, q - c.n1, s2);
+    else
+      incr_entry(g.d3, g.n3, c.d3, q - c.n1 - c.n2, s3);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < 2 * (c.n1 + c.n2 + c.n3); q += blockDim.x) {
+    int r = q;
+    if (r < c.n2) { cincr_entry(g.m12, g.d2, g.n2, c.m12, c.d2, r, s2); continue; }
+    r -= c.n2;
+    if (r < c.n3) { cincr_entry(g.m13, g.d3, g.n3, c.m13, c.d3, r, s3); continue; }
+    r -= c.n3;
+    if (r < c.n1) { cincr_entry(g.m21, g.d1, g.n1, c.m21, c.d1, r, s1); continue; }
+    r -= c.n1;
+    if (r < c.n3) { cincr_entry(g.m23, g.d3, g.n3, c.m23, c.d3, r, s3); continue; }
+    r -= c.n3;
+    if (r < c.n1) { cincr_entry(g.m31, g.d1, g.n1, c.m31, c.d1, r, s1); continue; }
+    r -= c.n1;
+    cincr_entry(g.m32, g.d2, g.n2, c.m32, c.d2, r, s2);
+  }
 }
 
 // ComputeFull_1D/2D/3D (TriDiagT_Mod.f90:62-90, 330-403, 790-883) for every
@@ -295,9 +314,9 @@ __global__ void k_assemble(Fields c, Lev2 P, double* __restrict__ u3, double* __
   const int n1 = c.n1, n2 = c.n2, n3 = c.n3;
   const size_t tot = (size_t)n1 * n2 * n3;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(e % n1) + 1;
-    const size_t r = e / n1;
-    const int j = (int)(r % n2) + 1, k = (int)(r / n2) + 1;
+    const int j = (int)(e % n2) + 1;
+    const size_t r = e / n2;
+    const int i = (int)(r % n1) + 1, k = (int)(r / n1) + 1;
     const double M1 = c.m12[j - 1], M2 = c.m13[k - 1];
     const double M21 = c.m21[i - 1], M23 = c.m23[k - 1];
     const double M31 = c.m31[i - 1], M32 = c.m32[j - 1];
@@ -908,6 +927,68 @@ __global__ void k_update_incr(Dims d, GeomT<double> g, Wts wt, const double* __r
   }
 }
 
+// WeightDiagCompute, ThetaKind='Density' (MULTI/JacAccGrav_Mod.f90:4259-4282)
+// with CellToFaceRhoWeight (:3254-3702) on a closed block: DUT and DTT per
+// cell, the face potential temperature DTU/DTV/DTW (volume-weighted between
+// the two cells, one-sided on the walls), DUU/DUV/DUW = F/(F+Eps).
+// Constants of MODULE/Parameter_Mod.f90:21-29.
+constexpr double kCpd = 1004.0, kCvd = 717.0, kRd = kCpd - kCvd, kCpv = 1885.0, kRv = 461.0, kCpl = 4186.0;
+
+__global__ void k_weights_density(Dims d, GeomT<double> g, Wts wt, const double* __restrict__ rth,
+                                  const double* __restrict__ rho, const double* __restrict__ rv,
+                                  const double* __restrict__ rc, const double* __restrict__ rr,
+                                  const double* __restrict__ tabs) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const size_t nc = (size_t)nx * ny * nz, nu = (size_t)(nx + 1) * ny * nz, nv = (size_t)nx * (ny + 1) * nz,
+               nw = (size_t)nx * ny * (nz + 1);
+  const size_t tot = nc + nu + nv + nw;
+  auto th = [&](size_t P) { return rth[P] / (rho[P] + asam::kEps); };
+  auto face = [&](size_t P, size_t Q) {
+    const double* V = g.volc;
+    return (V[P] * rth[P] / (rho[P] + asam::kEps) + V[Q] * rth[Q] / (rho[Q] + asam::kEps)) / (V[P] + V[Q] + asam::kEps);
+  };
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    if (e < nc) {
+      const int i = (int)(e % nx) + 1;
+      const size_t r = e / nx;
+      const int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
+      const size_t P = d.P(i, j, k);
+      const double rvl = rv ? rv[P] : 0.0;
+      const double rll = (rc ? rc[P] : 0.0) + (rr ? rr[P] : 0.0);
+      const double rd = rho[P] - rvl - rll + asam::kEps;
+      const double rm = kRd + kRv * rvl / rd;
+      const double cpml = kCpd + kCpv * rvl / rd + kCpl * rll / rd;
+      const double kap = rm / cpml;
+      wt.dut[e] = tabs[P] / (rth[P] + asam::kEps) * (rd * kRd + rvl * kRv) / (1.0 - kap);
+      wt.dtt[e] = 1.0;
+    } else if (e < nc + nu) {
+      const size_t q = e - nc;
+      const int i = (int)(q % (nx + 1));
+      const size_t r = q / (nx + 1);
+      const int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
+      wt.dtu[q] = i == 0 ? th(d.P(1, j, k)) : (i == nx ? th(d.P(nx, j, k)) : face(d.P(i, j, k), d.P(i + 1, j, k)));
+      const double f = g.fu[d.FU(i, j, k)];
+      wt.duu[q] = f / (f + asam::kEps);
+    } else if (e < nc + nu + nv) {
+      const size_t q = e - nc - nu;
+      const int i = (int)(q % nx) + 1;
+      const size_t r = q / nx;
+      const int j = (int)(r % (ny + 1)), k = (int)(r / (ny + 1)) + 1;
+      wt.dtv[q] = j == 0 ? th(d.P(i, 1, k)) : (j == ny ? th(d.P(i, ny, k)) : face(d.P(i, j, k), d.P(i, j + 1, k)));
+      const double f = g.fv[d.FV(i, j, k)];
+      wt.duv[q] = f / (f + asam::kEps);
+    } else {
+      const size_t q = e - nc - nu - nv;
+      const int i = (int)(q % nx) + 1;
+      const size_t r = q / nx;
+      const int j = (int)(r % ny) + 1, k = (int)(r / ny);
+      wt.dtw[q] = k == 0 ? th(d.P(i, j, 1)) : (k == nz ? th(d.P(i, j, nz)) : face(d.P(i, j, k), d.P(i, j, k + 1)));
+      const double f = g.fw[d.FW(i, j, k)];
+      wt.duw[q] = f / (f + asam::kEps);
+    }
+  }
+}
+
 }  // namespace prj
 
 using namespace prj;
@@ -930,7 +1011,7 @@ struct ProjState {
   std::vector<double*> v, z;
   double *H = nullptr, *partial = nullptr, *scal_h = nullptr;
   double *tmp = nullptr, *xn = nullptr, *bn = nullptr, *xl = nullptr, *bl = nullptr;
-  double *stage_u = nullptr, *stage_v = nullptr, *stage_w = nullptr;
+  double *stage_u = nullptr, *stage_v = nullptr, *stage_w = nullptr, *tabs = nullptr;
   int* d_scal = nullptr;
   int nscal_cap = 0;
   long long vcycles = 0;
@@ -1315,6 +1396,50 @@ int asam_proj_weights(asam_ctx* h, const double* dtu, const double* dtv, const d
   return kOk;
 }
 
+int asam_proj_weights_density(asam_ctx* h, const double* state, int th_pos, int rho_pos, int rv_pos, int rc_pos,
+                              int rr_pos, const double* tabs) {
+  if (!h || !h->proj || !state || !tabs) return kBadArg;
+  const int nc = h->cfg.ncomp;
+  auto bad = [&](int p, bool opt) { return opt ? (p < -1 || p >= nc) : (p < 0 || p >= nc); };
+  if (bad(th_pos, false) || bad(rho_pos, false) || bad(rv_pos, true) || bad(rc_pos, true) || bad(rr_pos, true))
+    return kBadArg;
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const cudaStream_t st = h->L.stream;
+  s->st = st;
+  const size_t len = (size_t)nc * h->npad;
+  const double* ds;
+  int rc;
+  if ((rc = stage_in(h, state, len, h->stage_a, &ds))) return rc;
+  if (!s->tabs) {
+    if ((rc = palloc(s, &s->tabs, h->npad))) return rc;
+  }
+  if ((rc = copy_in(h, s->tabs, tabs, h->npad))) return rc;
+  auto comp = [&](int p) { return p >= 0 ? ds + (size_t)p * h->npad : nullptr; };
+  const size_t tot = (size_t)d.nx * d.ny * d.nz + d.n_uf() + d.n_vf() + d.n_wf();
+  k_weights_density<<<grid_of(tot), 256, 0, st>>>(d, h->geom(), s->wt, comp(th_pos), comp(rho_pos), comp(rv_pos),
+                                                   comp(rc_pos), comp(rr_pos), s->tabs);
+  count_launches(1);
+  CK(cudaStreamSynchronize(st));
+  if ((rc = check_launch())) return rc;
+  s->weights = true;
+  s->assembled = false;
+  return kOk;
+}
+
+long asam_proj_get_weights(asam_ctx* h, int which, double* out) {
+  if (!h || !h->proj || which < 0 || which > 7) return -1;
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const size_t nc = (size_t)d.nx * d.ny * d.nz;
+  const double* src[] = {s->wt.dtu, s->wt.dtv, s->wt.dtw, s->wt.duu, s->wt.duv, s->wt.duw, s->wt.dut, s->wt.dtt};
+  const size_t n[] = {d.n_uf(), d.n_vf(), d.n_wf(), d.n_uf(), d.n_vf(), d.n_wf(), nc, nc};
+  if (!out) return (long)n[which];
+  if (cudaStreamSynchronize(h->L.stream) != cudaSuccess) return -1;
+  if (cudaMemcpy(out, src[which], n[which] * sizeof(double), cudaMemcpyDefault) != cudaSuccess) return -1;
+  return (long)n[which];
+}
+
 int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
   if (!h || !h->proj || !h->proj->weights) {
     set_last_error("asam_lapl_compute: call asam_proj_setup and asam_proj_weights first", __FILE__, __LINE__);
@@ -1328,7 +1453,7 @@ int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
   const double bd = beta0 * dtp, bd2 = bd * bd;
   const Facs fc{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // SetFactorN
   const double fa = s->cfg.fac_anela;
-  k_fine_fields<<<grid_of((size_t)(d.nx + 1) * (d.ny + 1) * (d.nz + 1)), 256, 0, st>>>(
+  k_fine_fields<<<grid_of((size_t)(d.nx + 1) * (d.nz + 1) * (d.ny + 1)), 256, 0, st>>>(
       d, h->fu, h->fv, h->fw, h->volc, s->wt.dtu, s->wt.dtv, s->wt.dtw, s->wt.duu, s->wt.duv, s->wt.duw, s->wt.dut, s->g);
   k_fine_1d<<<1, 256, 0, st>>>(d.nx, d.ny, d.nz, s->wt.dx, s->wt.dy, s->wt.dz, s->wt.metr, s->g);
   long long nl = 2;
@@ -1346,7 +1471,7 @@ int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
       const size_t ncell = (size_t)c.n1 * c.n2 * c.n3;
       k_coarse_faces<<<grid_of(nf), 256, 0, st>>>(s->g, c, sh, sh, sh3);
       k_coarse_cells<<<grid_of(ncell), 256, 0, st>>>(s->g, c, sh, sh, sh3);
-      k_coarse_1d<<<1, 32, 0, st>>>(s->g, c, sh, sh, sh3);
+      k_coarse_1d<<<1, 256, 0, st>>>(s->g, c, sh, sh, sh3);
       Lev2& P = A.pl[L2 - L];
       const bool full = L2 == L;
       k_assemble<<<grid_of(ncell), 256, 0, st>>>(c, P, full ? A.u3 : nullptr, full ? A.l3 : nullptr, full ? 1 : 0, bd2, fc, fa);

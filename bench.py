@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--no-projection", action="store_true")
+    p.add_argument("--projection-only", action="store_true",
+                   help="only the projection section (profiling); prints its JSON object")
     p.add_argument("--batch-members", type=int, default=48)
     p.add_argument("--batch-steps", type=int, default=20)
     p.add_argument("--batch-threads", type=int, default=0, help="host threads driving the members (0: one each)")
@@ -357,18 +359,9 @@ def projection_bench(a, torch, stream, hbm_peak):
 
     nx, ny, nz = a.nx, a.ny, a.nz
     ncell = nx * ny * nz
-    # CPU baseline (reference ordering) on a small block
-    cgeo = G.closed_hill_case(64, 64, 32, seed=9)
-    cW, cdx, cdy, cdz, (cu, cv, cw) = G.projection_inputs(cgeo, seed=21)
-    t0 = time.perf_counter()
-    op = oracle.OracleProj(cgeo, cdx, cdy, cdz, cW, zebra=0)
-    op.lapl_compute(PROJ_BETA0, a.dt)
-    b = op.rhs(cu, cv, cw)
-    x = np.zeros_like(b)
-    csteps, _, _ = op.fgmres(x, b)
-    op.update(x, cu.copy(), cv.copy(), cw.copy())
-    cpu_s = time.perf_counter() - t0
-    op.close()
+    cpu_base = None
+    if not a.no_cpu_baseline:
+        cpu_base = _projection_cpu_baseline(a)
 
     geo = G.closed_hill_case(nx, ny, nz, seed=9)
     W, dx, dy, dz, (u, v, w) = G.projection_inputs(geo, seed=21)
@@ -422,11 +415,33 @@ def projection_bench(a, torch, stream, hbm_peak):
                                "prolongation)", "bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": gbs / hbm_peak, "algorithmic_bytes_per_call": vb, "traffic": None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
-        "cpu_baseline": {"value": 64 * 64 * 32 / cpu_s / 1e6, "unit": "Mcell-projections/s", "cores": 1,
-                         "kind": "port", "sample": f"64x64x32 block of the same generator, oracle restatement with the "
-                                                   f"reference's lexicographic smoother, {csteps} FGMRES steps "
-                                                   f"({cpu_s:.1f} s)"},
+        "cpu_baseline": cpu_base,
     }
+
+
+def _projection_cpu_baseline(a):
+    """The oracle (reference lexicographic smoother) projecting a 64x64x32
+    closed block of the same generator on one host core."""
+    import numpy as np
+
+    import oracle
+    from asam_gb300 import geometry as G
+
+    cgeo = G.closed_hill_case(64, 64, 32, seed=9)
+    cW, cdx, cdy, cdz, (cu, cv, cw) = G.projection_inputs(cgeo, seed=21)
+    t0 = time.perf_counter()
+    op = oracle.OracleProj(cgeo, cdx, cdy, cdz, cW, zebra=0)
+    op.lapl_compute(PROJ_BETA0, a.dt)
+    b = op.rhs(cu, cv, cw)
+    x = np.zeros_like(b)
+    csteps, _, _ = op.fgmres(x, b)
+    op.update(x, cu.copy(), cv.copy(), cw.copy())
+    cpu_s = time.perf_counter() - t0
+    op.close()
+
+    return {"value": 64 * 64 * 32 / cpu_s / 1e6, "unit": "Mcell-projections/s", "cores": 1, "kind": "port",
+            "sample": f"64x64x32 block of the same generator, oracle restatement with the reference's "
+                      f"lexicographic smoother, {csteps} FGMRES steps ({cpu_s:.1f} s)"}
 
 
 def batch_members(n, seed=4):
@@ -535,6 +550,18 @@ def main():
         run_reference(a, rank)
         return
 
+    if a.projection_only:
+        import torch
+
+        import __graft_entry__
+
+        __graft_entry__.build()
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        pk0 = ROOT / "MEASURED_PEAKS.json"
+        hp = json.loads(pk0.read_text()).get("hbm_gbs", 6800.0) if pk0.exists() else 6800.0
+        print(json.dumps(projection_bench(a, torch, stream, hp)), flush=True)
+        return
     # CPU baseline first (before any GPU call), rank 0, N=1 only
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:

@@ -262,6 +262,18 @@ int asam_proj_setup(asam_ctx *ctx, const asam_proj_config *cfg, const double *dx
  * DTU/DUU with uF extents, DTV/DUV vF, DTW/DUW wF; DUT and DTT interior. */
 int asam_proj_weights(asam_ctx *ctx, const double *dtu, const double *dtv, const double *dtw, const double *duu,
                       const double *duv, const double *duw, const double *dut, const double *dtt);
+/* The sound weights computed on the device instead, for ThetaKind='Density'
+ * (WeightDiagCompute, MULTI/JacAccGrav_Mod.f90:4259-4282, with
+ * CellToFaceRhoWeight :3254-3702 on a closed block): state holds rho theta
+ * (th_pos), the density (rho_pos) and optionally vapour, cloud and rain water
+ * (rv_pos, rc_pos, rr_pos; -1 = absent); tabs is the padded absolute
+ * temperature (TAbsCell).  The reference points its vapour at the cloud-water
+ * component (JacAccGrav_Mod.f90:313); pass rv_pos = rc_pos to reproduce that. */
+int asam_proj_weights_density(asam_ctx *ctx, const double *state, int th_pos, int rho_pos, int rv_pos, int rc_pos,
+                              int rr_pos, const double *tabs);
+/* Copy one weight array to out (which: 0 DTU, 1 DTV, 2 DTW, 3 DUU, 4 DUV,
+ * 5 DUW, 6 DUT, 7 DTT); returns its length, -1 on error.  Diagnostic. */
+long asam_proj_get_weights(asam_ctx *ctx, int which, double *out);
 /* LaplTFullCompute with the Neumann factors of SetFactorN
  * (MULTI/JacAccGrav_Mod.f90:1056-1310, MULTI/Reverse_Mod.f90:225-292) for
  * beta0 and dtP = dt (ADVECT/Int_Mod.f90:293-295). */

@@ -70,6 +70,8 @@ def load() -> C.CDLL:
             "ora_fgmres": (I, [V, V, V, I, D, I, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "ora_proj_rhs": (None, [V, V, V, V, V, V]),
             "ora_proj_update": (None, [V, V, V, V, V, V, V, I, V, V, V]),
+            "ora_weights_density": (None, [V] * 15),
+            "ora_proj_set_weights": (None, [V] * 9),
         })
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -292,3 +294,17 @@ class OracleProj:
         self.lib.ora_proj_update(self.h, _p(x), _p(u), _p(v), _p(w), None if incr_th is None else _p(incr_th),
                                  None if incr_rho is None else _p(incr_rho), nc, pi, pc,
                                  None if rho is None else _p(rho))
+
+    def weights_density(self, rth, rho, rv, rc, rr, t):
+        """Density-kind sound weights (padded inputs; None for absent water);
+        returns [DTU, DTV, DTW, DUU, DUV, DUW, DUT, DTT] and installs them."""
+        g = self.grid
+        nx, ny, nz = g.nx, g.ny, g.nz
+        out = [np.empty((nz, ny, nx + 1)), np.empty((nz, ny + 1, nx)), np.empty((nz + 1, ny, nx)),
+               np.empty((nz, ny, nx + 1)), np.empty((nz, ny + 1, nx)), np.empty((nz + 1, ny, nx)),
+               np.empty((nz, ny, nx)), np.empty((nz, ny, nx))]
+        keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (rth, rho, rv, rc, rr, t)]
+        ptrs = [None if a is None else _p(a) for a in keep]
+        self.lib.ora_weights_density(self.h, *ptrs, *[_p(a) for a in out])
+        self.lib.ora_proj_set_weights(self.h, *[_p(a) for a in out])
+        return out

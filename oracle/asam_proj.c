@@ -1376,3 +1376,111 @@ void ora_proj_update(void* hv, double* x, double* u, double* v, double* w, doubl
 #undef WI
 #undef CI
 #undef PI
+
+/* WeightDiagCompute, ThetaKind='Density' branch (MULTI/JacAccGrav_Mod.f90:
+ * 4259-4282) with CellToFaceRhoWeight (:3254-3702) for a closed block
+ * (outer walls, no inflow): DUT per cell, DTU/DTV/DTW the volume-weighted
+ * face values of theta = (rho theta)/(rho+Eps) (one-sided on the walls),
+ * DUU/DUV/DUW = F/(F+Eps), DTT = 1.  Inputs are padded fields: rth = rho
+ * theta, rho, rv (RhoV, may be NULL), rl (RhoL + RhoR summed by the caller:
+ * rc and rr, each may be NULL), t = absolute temperature.  Outputs with the
+ * library's weight layouts. */
+#define CP_D 1004.0
+#define CV_D 717.0
+#define R_D (CP_D - CV_D)
+#define CP_V 1885.0
+#define R_V 461.0
+#define CP_L 4186.0
+void ora_weights_density(void* hv, const double* rth, const double* rho, const double* rv, const double* rc,
+                         const double* rr, const double* t, double* dtu, double* dtv, double* dtw, double* duu,
+                         double* duv, double* duw, double* dut, double* dtt) {
+  Proj* h = (Proj*)hv;
+  const int nx = h->par.nx, ny = h->par.ny, nz = h->par.nz;
+  const double* V = h->volp;
+#define PI(i, j, k) ((size_t)(i) + (size_t)(nx + 2) * ((size_t)(j) + (size_t)(ny + 2) * (k)))
+#define UI(i, j, k) ((size_t)(i) + (size_t)(nx + 1) * ((size_t)((j) - 1) + (size_t)ny * ((k) - 1)))
+#define VI(i, j, k) ((size_t)((i) - 1) + (size_t)nx * ((size_t)(j) + (size_t)(ny + 1) * ((k) - 1)))
+#define WI(i, j, k) ((size_t)((i) - 1) + (size_t)nx * ((size_t)((j) - 1) + (size_t)ny * (k)))
+#define CI(i, j, k) ((size_t)((i) - 1) + (size_t)nx * ((size_t)((j) - 1) + (size_t)ny * ((k) - 1)))
+#define TH(P) (rth[P] / (rho[P] + EPS))
+#define FACE(P, Q) ((V[P] * rth[P] / (rho[P] + EPS) + V[Q] * rth[Q] / (rho[Q] + EPS)) / (V[P] + V[Q] + EPS))
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const size_t P = PI(i, j, k);
+        const double rvl = rv ? rv[P] : 0.0;
+        const double rll = (rc ? rc[P] : 0.0) + (rr ? rr[P] : 0.0);
+        const double rd = rho[P] - rvl - rll + EPS;
+        const double rm = R_D + R_V * rvl / rd;
+        const double cpml = CP_D + CP_V * rvl / rd + CP_L * rll / rd;
+        const double kap = rm / cpml;
+        dut[CI(i, j, k)] = t[P] / (rth[P] + EPS) * (rd * R_D + rvl * R_V) / (1.0 - kap);
+        dtt[CI(i, j, k)] = 1.0;
+      }
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 0; i <= nx; ++i) {
+        double v;
+        if (i == 0)
+          v = TH(PI(1, j, k));
+        else if (i == nx)
+          v = TH(PI(nx, j, k));
+        else
+          v = FACE(PI(i, j, k), PI(i + 1, j, k));
+        dtu[UI(i, j, k)] = v;
+        const double f = h->fu[UI(i, j, k)];
+        duu[UI(i, j, k)] = f / (f + EPS);
+      }
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 0; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        double v;
+        if (j == 0)
+          v = TH(PI(i, 1, k));
+        else if (j == ny)
+          v = TH(PI(i, ny, k));
+        else
+          v = FACE(PI(i, j, k), PI(i, j + 1, k));
+        dtv[VI(i, j, k)] = v;
+        const double f = h->fv[VI(i, j, k)];
+        duv[VI(i, j, k)] = f / (f + EPS);
+      }
+  for (int k = 0; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        double v;
+        if (k == 0)
+          v = TH(PI(i, j, 1));
+        else if (k == nz)
+          v = TH(PI(i, j, nz));
+        else
+          v = FACE(PI(i, j, k), PI(i, j, k + 1));
+        dtw[WI(i, j, k)] = v;
+        const double f = h->fw[WI(i, j, k)];
+        duw[WI(i, j, k)] = f / (f + EPS);
+      }
+#undef PI
+#undef UI
+#undef VI
+#undef WI
+#undef CI
+#undef TH
+#undef FACE
+}
+
+/* Replace the oracle's weights (after ora_weights_density) */
+void ora_proj_set_weights(void* hv, const double* dtu, const double* dtv, const double* dtw, const double* duu,
+                          const double* duv, const double* duw, const double* dut, const double* dtt) {
+  Proj* h = (Proj*)hv;
+  const int nx = h->par.nx, ny = h->par.ny, nz = h->par.nz;
+  const size_t nu = (size_t)(nx + 1) * ny * nz, nv = (size_t)nx * (ny + 1) * nz, nw = (size_t)nx * ny * (nz + 1);
+  const size_t nc = (size_t)nx * ny * nz;
+  memcpy(h->dtu, dtu, nu * sizeof(double));
+  memcpy(h->duu, duu, nu * sizeof(double));
+  memcpy(h->dtv, dtv, nv * sizeof(double));
+  memcpy(h->duv, duv, nv * sizeof(double));
+  memcpy(h->dtw, dtw, nw * sizeof(double));
+  memcpy(h->duw, duw, nw * sizeof(double));
+  memcpy(h->dut, dut, nc * sizeof(double));
+  memcpy(h->dtt, dtt, nc * sizeof(double));
+}

@@ -155,3 +155,30 @@ def test_bad_calls_raise():
         g = per.grid
         with pytest.raises(AsamError):
             blk.proj_setup(np.full(g.nx, g.dx), np.full(g.ny, g.dy), g.dz)
+
+
+@pytest.mark.parametrize("name", ["proj_hill_24x20x16", "proj_hill_odd_13x7x9"])
+def test_density_weights_and_hierarchy_bitwise(name):
+    geo = cases.get(name)
+    g = geo.grid
+    W, dx, dy, dz, _ = cases.proj_inputs(geo)
+    rng = np.random.default_rng(31)
+    rho = 1.0 + 0.1 * rng.random(g.pshape)
+    rth = rho * (300.0 + 5.0 * rng.random(g.pshape))
+    rv = 0.01 * rho * rng.random(g.pshape)
+    rc = 0.001 * rho * rng.random(g.pshape)
+    t = 290.0 + 10.0 * rng.random(g.pshape)
+    state = np.ascontiguousarray(np.stack([rho, rth, rv, rc]))
+    o = oracle.OracleProj(geo, dx, dy, dz, W, zebra=1)
+    ref = o.weights_density(rth, rho, rv, rc, None, t)
+    o.lapl_compute(BETA0, DTP)
+    with TransportBlock(geo, ncomp=4, rho_pos=0) as blk:
+        blk.proj_setup(dx, dy, dz)
+        blk.WeightDiagCompute(state, t, th_pos=1, rho_pos=0, rv_pos=2, rc_pos=3)
+        for which in range(8):
+            np.testing.assert_array_equal(blk.proj_weight(which), ref[which].ravel(), err_msg=f"weight {which}")
+        blk.JacAccGrav(BETA0, DTP)
+        for L3 in range(REF_LEVEL):
+            for L2 in range(L3, REF_LEVEL):
+                for which in range(7 if L2 == L3 else 5):
+                    np.testing.assert_array_equal(blk.lapl_array(L3, L2, which), o.lapl_get(L3, L2, which))

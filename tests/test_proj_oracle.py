@@ -174,3 +174,43 @@ def test_orderings_agree_to_krylov_tolerance(name):
         sols.append(xs)
     live = cases.get(name).volc[1:-1, 1:-1, 1:-1] > 0
     assert np.max(np.abs(sols[0] - sols[1])[live]) <= 1e-9 * np.max(np.abs(sols[0])[live])
+
+
+def _moist_state(geo, seed=31):
+    g = geo.grid
+    rng = np.random.default_rng(seed)
+    rho = 1.0 + 0.1 * rng.random(g.pshape)
+    rth = rho * (300.0 + 5.0 * rng.random(g.pshape))
+    rv = 0.01 * rho * rng.random(g.pshape)
+    rc = 0.001 * rho * rng.random(g.pshape)
+    t = 290.0 + 10.0 * rng.random(g.pshape)
+    return rth, rho, rv, rc, t
+
+
+@pytest.mark.parametrize("name", ["proj_hill_odd_13x7x9", "proj_flat_16x12x10"])
+def test_density_weights_formula(name):
+    """WeightDiagCompute 'Density' (JacAccGrav_Mod.f90:4259-4282) and the
+    interior/wall faces of CellToFaceRhoWeight, restated in numpy."""
+    geo, W, dx, dy, dz, _, o = _make(name)
+    g = geo.grid
+    rth, rho, rv, rc, t = _moist_state(geo)
+    dtu, dtv, dtw, duu, duv, duw, dut, dtt = o.weights_density(rth, rho, rv, rc, None, t)
+    eps = 1.0e-30
+    Rd, Rv, Cpd, Cpv, Cpl = 1004.0 - 717.0, 461.0, 1004.0, 1885.0, 4186.0
+    I = (slice(1, -1),) * 3
+    rvl, rll = rv[I], rc[I] + 0.0
+    rd = rho[I] - rvl - rll + eps
+    kap = (Rd + Rv * rvl / rd) / (Cpd + Cpv * rvl / rd + Cpl * rll / rd)
+    np.testing.assert_array_equal(dut, t[I] / (rth[I] + eps) * (rd * Rd + rvl * Rv) / (1.0 - kap))
+    np.testing.assert_array_equal(dtt, np.ones_like(dtt))
+    th = rth / (rho + eps)
+    V = geo.volc
+    vt = V * rth / (rho + eps)
+    ex = (vt[1:-1, 1:-1, 1:-2] + vt[1:-1, 1:-1, 2:-1]) / (V[1:-1, 1:-1, 1:-2] + V[1:-1, 1:-1, 2:-1] + eps)
+    np.testing.assert_array_equal(dtu[:, :, 1:-1], ex)
+    np.testing.assert_array_equal(dtu[:, :, 0], th[1:-1, 1:-1, 1])
+    np.testing.assert_array_equal(dtu[:, :, -1], th[1:-1, 1:-1, -2])
+    ez = (vt[1:-2, 1:-1, 1:-1] + vt[2:-1, 1:-1, 1:-1]) / (V[1:-2, 1:-1, 1:-1] + V[2:-1, 1:-1, 1:-1] + eps)
+    np.testing.assert_array_equal(dtw[1:-1], ez)
+    fu = geo.fu[:, :, 1:g.nx + 2]
+    np.testing.assert_array_equal(duu, fu / (fu + eps))
