@@ -18,7 +18,7 @@ import numpy as np
 import pytest
 
 import oracle
-from tests import cases
+from tests import cases, pyref
 
 BETA0, DTP = 0.435866521508459, 2.0
 PROJ = ["proj_hill_24x20x16", "proj_hill_odd_13x7x9", "proj_flat_16x12x10", "proj_column_1x1x12", "proj_slab_9x1x6"]
@@ -33,85 +33,7 @@ def _make(name, zebra=1, **kw):
 
 
 def _level0_numpy(geo, W, dx, dy, dz):
-    """Independent restatement of the level-0 assembly (shift 0, Cartesian
-    metric, Neumann factors 0) in the reversed order (z fastest, then x, then y).
-    Arrays are indexed [y, x, z]."""
-    g = geo.grid
-    nx, ny, nz = g.nx, g.ny, g.nz
-    eps = 1.0e-30
-    dtu, dtv, dtw, duu, duv, duw, dut, _ = W
-    rv = lambda a: np.ascontiguousarray(np.transpose(a, (1, 2, 0)))  # [z,y,x] -> [y,x,z]
-    F1, T1, U1 = rv(geo.fw[1:nz + 2]), rv(dtw), rv(duw)
-    F2, T2, U2 = rv(geo.fu[:, :, 1:nx + 2]), rv(dtu), rv(duu)
-    F3, T3, U3 = rv(geo.fv[:, 1:ny + 2, :]), rv(dtv), rv(duv)
-    # CFaceCoarse with shift 0
-    T1, U1 = (T1 * F1) / (F1 + eps), (U1 * F1) / (F1 + eps)
-    T2, U2 = (T2 * F2) / (F2 + eps), (U2 * F2) / (F2 + eps)
-    T3, U3 = (T3 * F3) / (F3 + eps), (U3 * F3) / (F3 + eps)
-    vol = rv(geo.volc[1:-1, 1:-1, 1:-1])
-    vol = 0.0 + vol
-    D = (rv(dut) * vol) / (vol + eps)
-    bd = BETA0 * DTP
-    bd2 = bd * bd
-    one = 1.0
-    d = np.full((ny, nx, nz), 1.0e-40)
-    z = np.zeros_like(d)
-    # z terms: face f (1..nz-1) between cells f-1, f (0-based)
-    dzc = 0.0 + np.asarray(dz)
-    if nz > 1:
-        den = (dzc[:-1] + dzc[1:]) * one * one
-        base = bd2 * 2.0 * F1[:, :, 1:nz] * T1[:, :, 1:nz] * U1[:, :, 1:nz]
-        below = base * D[:, :, 1:] / den   # cell f, face below
-        above = base * D[:, :, :-1] / den  # cell f-1, face above
-        first = np.concatenate([bd2 * 0.0 * F1[:, :, :1] * T1[:, :, :1] * U1[:, :, :1] * D[:, :, :1] / (dzc[0] * one * one),
-                                below], axis=2)
-        second = np.concatenate([above, bd2 * 0.0 * F1[:, :, nz:] * T1[:, :, nz:] * U1[:, :, nz:] * D[:, :, -1:] /
-                                 (dzc[-1] * one * one)], axis=2)
-        uz = np.concatenate([-(base * D[:, :, 1:] / den), z[:, :, :1]], axis=2)
-        lz = np.concatenate([-(base * D[:, :, :-1] / den), z[:, :, :1]], axis=2)
-    else:
-        first = bd2 * 0.0 * F1[:, :, :1] * T1[:, :, :1] * U1[:, :, :1] * D / (dzc[0] * one * one)
-        second = bd2 * 0.0 * F1[:, :, 1:] * T1[:, :, 1:] * U1[:, :, 1:] * D / (dzc[0] * one * one)
-        uz = lz = z.copy()
-    d = d + first
-    d = d + second
-    d = d + 1.0 * vol
-    # x terms: face f (1..nx-1) between columns f-1, f
-    dxc = 0.0 + np.asarray(dx)
-    if nx > 1:
-        den = ((dxc[:-1] + dxc[1:]) * one)[None, :, None] * one
-        base = bd2 * 2.0 * F2[:, 1:nx] * T2[:, 1:nx] * U2[:, 1:nx]
-        first = np.concatenate([bd2 * 0.0 * F2[:, :1] * T2[:, :1] * U2[:, :1] * D[:, :1] / (dxc[0] * one * one),
-                                base * D[:, 1:] / den], axis=1)
-        second = np.concatenate([base * D[:, :-1] / den,
-                                 bd2 * 0.0 * F2[:, nx:] * T2[:, nx:] * U2[:, nx:] * D[:, -1:] / (dxc[-1] * one * one)],
-                                axis=1)
-        ux = np.concatenate([-(base * D[:, 1:] / den), z[:, :1]], axis=1)
-        lx = np.concatenate([-(base * D[:, :-1] / den), z[:, :1]], axis=1)
-    else:
-        first = bd2 * 0.0 * F2[:, :1] * T2[:, :1] * U2[:, :1] * D / (dxc[0] * one * one)
-        second = bd2 * 0.0 * F2[:, 1:] * T2[:, 1:] * U2[:, 1:] * D / (dxc[0] * one * one)
-        ux = lx = z.copy()
-    d = d + first
-    d = d + second
-    # y terms (no DUU3 in the couplings, the interior diagonal terms and the high boundary term)
-    dyc = 0.0 + np.asarray(dy)
-    if ny > 1:
-        den = ((dyc[:-1] + dyc[1:]) * one)[:, None, None] * one
-        base = bd2 * 2.0 * F3[1:ny] * T3[1:ny]
-        first = np.concatenate([bd2 * 0.0 * F3[:1] * T3[:1] * U3[:1] * D[:1] / (dyc[0] * one * one),
-                                base * D[1:] / den], axis=0)
-        second = np.concatenate([base * D[:-1] / den, bd2 * 0.0 * F3[ny:] * T3[ny:] * D[-1:] / (dyc[-1] * one * one)],
-                                axis=0)
-        u3 = np.concatenate([-(base * D[1:] / den), z[:1]], axis=0)
-        l3 = np.concatenate([-(base * D[:-1] / den), z[:1]], axis=0)
-    else:
-        first = bd2 * 0.0 * F3[:1] * T3[:1] * U3[:1] * D / (dyc[0] * one * one)
-        second = bd2 * 0.0 * F3[1:] * T3[1:] * D / (dyc[0] * one * one)
-        u3 = l3 = z.copy()
-    d = d + first
-    d = d + second
-    return [a.ravel() for a in (d, uz, lz, ux, lx, u3, l3)]
+    return pyref.lapl_level0(geo, W, dx, dy, dz, BETA0, DTP)
 
 
 @pytest.mark.parametrize("name", PROJ)
