@@ -49,6 +49,7 @@ constexpr int kMaxLev = 8;
 constexpr int kPlaneBlock = 256;
 constexpr int kRedGrid = 1024;
 constexpr int kRedBlock = 256;
+constexpr size_t kRingBytes = (size_t)4 * 8 * kPlaneBlock * sizeof(double);  // kRing * kFields * block
 constexpr double kTiny = 1.0e-40;  // initial diagonal of Allocate_1D (TriDiagT_Mod.f90:99)
 
 struct Lev2 {
@@ -437,13 +438,23 @@ __device__ inline double matvec2_at(const Lev2& P, size_t mo, const double* __re
 
 // One zebra half-sweep over the x-lines of parity c of one plane: the line
 // right-hand side in the forward or backward operation order of
-// GaussSeidel_2D, then Solve_1D with the precomputed factors.  Rows are
-// handled in chunks of kChunk: every load of a chunk is issued before its
-// recurrence runs, so a thread keeps several rows of loads in flight.
-constexpr int kChunk = 4;
+// GaussSeidel_2D, then Solve_1D with the precomputed factors.  The forward
+// elimination streams the eight inputs of each row (b, the two neighbour
+// lines, their couplings, the sub-diagonal of the previous row, the pivot
+// and its reciprocal) through a per-thread ring of kRing rows in shared
+// memory with cp.async, kAhead rows ahead of the recurrence; the copies read
+// only the other parity's lines and the matrix, never this thread's column.
+// The back substitution loads x and w four rows ahead in two register sets.
+constexpr int kRing = 4;
+constexpr int kAhead = 3;
+constexpr int kFields = 8;
+
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 __device__ __noinline__ void line_half(const Lev2& P, size_t mo, const double* __restrict__ b, double* __restrict__ x, int c,
-                          int fwd) {
+                                       int fwd, double* __restrict__ ring) {
   const int c1 = P.c1, c2 = P.c2, h = P.h, w = P.w;
   const double* __restrict__ lx = P.lx + mo;
   const double* __restrict__ ux = P.ux + mo;
@@ -452,93 +463,102 @@ __device__ __noinline__ void line_half(const Lev2& P, size_t mo, const double* _
   const double* __restrict__ frt = P.frt + mo;
   const double* __restrict__ fw = P.fw + mo;
   const int nl = (c2 - c + 1) / 2;
-  for (int q = threadIdx.x; q < nl; q += blockDim.x) {
+  const int bd = blockDim.x, tid = threadIdx.x;
+  for (int q = tid; q < nl; q += bd) {
     const int j = 2 * q + c;
     const size_t col = (size_t)c * h + q;
     const bool hasL = j > 0, hasR = j < c2 - 1;
     const size_t colL = hasL ? (size_t)(1 - c) * h + ((j - 1) >> 1) : col;
     const size_t colR = hasR ? (size_t)(1 - c) * h + ((j + 1) >> 1) : col;
+    auto issue = [&](int i) {
+      double* sl = ring + (size_t)(i % kRing) * kFields * bd + tid;
+      const bool ok = i < c1;
+      const size_t o = (size_t)(ok ? i : 0) * w;
+      const size_t om = i > 0 && ok ? o - w : o;
+      cp_async_elem(sl + 0 * bd, b + col + o, ok);
+      cp_async_elem(sl + 1 * bd, x + colL + o, ok && hasL);
+      cp_async_elem(sl + 2 * bd, x + colR + o, ok && hasR);
+      cp_async_elem(sl + 3 * bd, lx + colL + o, ok && hasL);
+      cp_async_elem(sl + 4 * bd, ux + col + o, ok && hasR);
+      cp_async_elem(sl + 5 * bd, lz + col + om, ok && i > 0);
+      cp_async_elem(sl + 6 * bd, ft + col + o, ok);
+      cp_async_elem(sl + 7 * bd, frt + col + o, ok);
+      cp_commit();
+    };
+    for (int r = 0; r < kAhead; ++r) issue(r);
     double prev = 0.0;
-    for (int i0 = 0; i0 < c1; i0 += kChunk) {
-      double t[kChunk], l[kChunk], pv[kChunk], rp[kChunk];
-#pragma unroll
-      for (int r = 0; r < kChunk; ++r) {
-        const int i = i0 + r;
-        if (i < c1) {
-          const size_t o = (size_t)i * w;
-          double v = b[col + o];
-          const double xl = x[colL + o], xr = x[colR + o];
-          const double cl = hasL ? lx[colL + o] : 0.0, cr = hasR ? ux[col + o] : 0.0;
-          if (fwd) {
-            if (hasL) v = v - cl * xl;
-            if (hasR) v = v - cr * xr;
-          } else {
-            if (hasR) v = v - cr * xr;
-            if (hasL) v = v - cl * xl;
-          }
-          t[r] = v;
-          l[r] = i > 0 ? lz[col + o - w] : 0.0;
-          pv[r] = ft[col + o];
-          rp[r] = frt[col + o];
-        }
+    for (int i = 0; i < c1; ++i) {
+      issue(i + kAhead);
+      cp_wait<kAhead>();
+      const double* sl = ring + (size_t)(i % kRing) * kFields * bd + tid;
+      double t = sl[0];
+      if (fwd) {
+        if (hasL) t = t - sl[3 * bd] * sl[1 * bd];
+        if (hasR) t = t - sl[4 * bd] * sl[2 * bd];
+      } else {
+        if (hasR) t = t - sl[4 * bd] * sl[2 * bd];
+        if (hasL) t = t - sl[3 * bd] * sl[1 * bd];
       }
-#pragma unroll
-      for (int r = 0; r < kChunk; ++r) {
-        const int i = i0 + r;
-        if (i < c1) {
-          double v = t[r];
-          if (i > 0) v = v - l[r] * prev;
-          const double y = div_rn(v, pv[r], rp[r]);
-          x[col + (size_t)i * w] = y;
-          prev = y;
-        }
-      }
+      if (i > 0) t = t - sl[5 * bd] * prev;
+      const double y = div_rn(t, sl[6 * bd], sl[7 * bd]);
+      x[col + (size_t)i * w] = y;
+      prev = y;
     }
+    cp_wait<0>();
     // back substitution b(i) = b(i) - w(i)*b(i+1), rows c1-2 .. 0
-    for (int i0 = c1 - 2; i0 >= 0; i0 -= kChunk) {
-      double xv[kChunk], wv[kChunk];
+    const int nb = c1 - 1;
+    double xa[4], wa[4], xb[4], wb[4];
+    auto load4 = [&](double* xs, double* ws, int r0) {
 #pragma unroll
-      for (int r = 0; r < kChunk; ++r) {
-        const int i = i0 - r;
+      for (int r = 0; r < 4; ++r) {
+        const int i = c1 - 2 - (r0 + r);
         if (i >= 0) {
-          const size_t o = (size_t)i * w;
-          xv[r] = x[col + o];
-          wv[r] = fw[col + o];
+          xs[r] = x[col + (size_t)i * w];
+          ws[r] = fw[col + (size_t)i * w];
         }
       }
+    };
+    auto solve4 = [&](const double* xs, const double* ws, int r0) {
 #pragma unroll
-      for (int r = 0; r < kChunk; ++r) {
-        const int i = i0 - r;
+      for (int r = 0; r < 4; ++r) {
+        const int i = c1 - 2 - (r0 + r);
         if (i >= 0) {
-          const double v = xv[r] - wv[r] * prev;
+          const double v = xs[r] - ws[r] * prev;
           x[col + (size_t)i * w] = v;
           prev = v;
         }
       }
+    };
+    if (nb > 0) load4(xa, wa, 0);
+    for (int r0 = 0; r0 < nb; r0 += 8) {
+      load4(xb, wb, r0 + 4);
+      solve4(xa, wa, r0);
+      load4(xa, wa, r0 + 8);
+      solve4(xb, wb, r0 + 4);
     }
   }
 }
 
-__device__ void gs2d(const Lev2& P, size_t mo, const double* b, double* x, int gi) {
+__device__ void gs2d(const Lev2& P, size_t mo, const double* b, double* x, int gi, double* ring) {
   if (P.c2 > 1) {
     for (int it = 0; it < gi; ++it) {
-      line_half(P, mo, b, x, 0, 1);
+      line_half(P, mo, b, x, 0, 1, ring);
       __syncthreads();
-      line_half(P, mo, b, x, 1, 1);
+      line_half(P, mo, b, x, 1, 1, ring);
       __syncthreads();
-      line_half(P, mo, b, x, 1, 0);
+      line_half(P, mo, b, x, 1, 0, ring);
       __syncthreads();
-      line_half(P, mo, b, x, 0, 0);
+      line_half(P, mo, b, x, 0, 0, ring);
       __syncthreads();
     }
   } else {
-    line_half(P, mo, b, x, 0, 1);
+    line_half(P, mo, b, x, 0, 1, ring);
     __syncthreads();
   }
 }
 
 // Multigrid_2D (TriDiagT_Mod.f90:490-551) on plane k of a 3D level, inside one CTA
-__device__ void mg2d(const Lev3& A, int k, double* x0, const double* b0, int gi2) {
+__device__ void mg2d(const Lev3& A, int k, double* x0, const double* b0, int gi2, double* ring) {
   const int nl = A.nl;
   int gi = 1;
   int lv = 0;
@@ -547,7 +567,7 @@ __device__ void mg2d(const Lev3& A, int k, double* x0, const double* b0, int gi2
     double* x = lv == 0 ? x0 : P.x + (size_t)k * P.ps;
     const double* b = lv == 0 ? b0 : P.b + (size_t)k * P.ps;
     const size_t mo = (size_t)k * P.ps;
-    gs2d(P, mo, b, x, gi);
+    gs2d(P, mo, b, x, gi, ring);
     gi += gi2;
     if (lv + 1 < nl) {
       double* res = P.res + (size_t)k * P.ps;
@@ -581,7 +601,7 @@ __device__ void mg2d(const Lev3& A, int k, double* x0, const double* b0, int gi2
     const Lev2& P = A.pl[lv];
     double* x = lv == 0 ? x0 : P.x + (size_t)k * P.ps;
     const double* b = lv == 0 ? b0 : P.b + (size_t)k * P.ps;
-    gs2d(P, (size_t)k * P.ps, b, x, gi);
+    gs2d(P, (size_t)k * P.ps, b, x, gi, ring);
     gi -= gi2;
     if (lv > 0) {
       const Lev2& F = A.pl[lv - 1];
@@ -605,6 +625,7 @@ __device__ void mg2d(const Lev3& A, int k, double* x0, const double* b0, int gi2
 __global__ void __launch_bounds__(kPlaneBlock, 2) k_plane_half(const Lev3* __restrict__ lvs, int L, int color, int fwd,
                                                              int mult_iter2, int gi2) {
   __shared__ Lev3 A;
+  extern __shared__ double ring[];  // kRing * kFields * blockDim doubles
   if (threadIdx.x == 0) A = lvs[L];
   __syncthreads();
   const Lev2& P0 = A.pl[0];
@@ -626,7 +647,7 @@ __global__ void __launch_bounds__(kPlaneBlock, 2) k_plane_half(const Lev3* __res
       A.t[e] = v;
     }
     __syncthreads();
-    for (int it = 0; it < mult_iter2; ++it) mg2d(A, k, A.x + off, A.t + off, gi2);
+    for (int it = 0; it < mult_iter2; ++it) mg2d(A, k, A.x + off, A.t + off, gi2, ring);
     __syncthreads();
   }
 }
@@ -1111,6 +1132,7 @@ int proj_build(asam_ctx* h) {
     for (double** q : arr)
       if (int rc = palloc(s, q, n)) return rc;
   }
+  CK(cudaFuncSetAttribute(k_plane_half, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
   if (int rc = palloc(s, &s->d_lv, (size_t)R)) return rc;
   CK(cudaMemcpyAsync(s->d_lv, s->lv.data(), sizeof(Lev3) * R, cudaMemcpyHostToDevice, s->st));
   CK(cudaStreamSynchronize(s->st));
@@ -1152,7 +1174,7 @@ void vcycle_dev(asam_ctx* h) {
     auto half = [&](int c, int fwd) {
       const int np = (A.m3 - c + 1) / 2;
       if (np <= 0) return;
-      k_plane_half<<<np, kPlaneBlock, 0, st>>>(s->d_lv, L, c, fwd, mi2, gi2);
+      k_plane_half<<<np, kPlaneBlock, kRingBytes, st>>>(s->d_lv, L, c, fwd, mi2, gi2);
       ++nl;
     };
     if (A.m3 > 1) {
