@@ -14,12 +14,18 @@ the C-ABI in ``include/asam_gb300.h``.  Method names follow the reference:
 ``Ros3MetC``           ADVECT/Int_Mod.f90:1059 (fixed dt)
 ``TotalScalar``        ADVECT/Diagnostic_Mod.f90:13
 ``ExchangeCell``       MODULE/Vector4CellPar_Mod.f90:752
+``BoundaryCondition``  ADVECT/BoundaryCondition_Mod.f90:1143 (outer-wall halos)
 ``JacAccGrav``         pressure-Laplacian hierarchy, LaplTFullCompute
                        (MULTI/JacAccGrav_Mod.f90:1056)
 ``MatVecP``            MULTI/JacAccGrav_Mod.f90:531 (MatVecP_Tri)
 ``VCycleCG``           MULTI/JacAccGrav_Mod.f90:4466 (one Solve_3D)
 ``SolveSound``         SOLU/Iter_Mod.f90:9 (FGMRES, MatVec1, PSolve1)
 ``ProjectVelFace``     ADVECT/IntSub_Mod.f90:25
+``VelocityFaceToCellLR``  ADVECT/VelocityCellFace_Mod.f90:72
+``VelocityCellToFaceLR``  ADVECT/VelocityCellFace_Mod.f90:27
+``AbsTPreCompute``     AbsTCompute + PreCompute (ADVECT/Diagnostic_Mod.f90:593, 710)
+``FcnMet``             FcnMet with PGradComputeC and buoyancy (ADVECT/Function_Mod.f90:989)
+``Ros3MetC_dyn``       Ros3MetC + StageRos with prognostic momentum (ADVECT/Int_Mod.f90:263)
 ``Solve_1D``           MULTI/TriDiagT_Mod.f90:135 (batched over columns)
 ``MatVecT_1D``         MULTI/TriDiagT_Mod.f90:113 (batched over columns)
 =====================  =======================================================
@@ -35,7 +41,8 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import ASAM_BREAKDOWN, ASAM_NOT_CONVERGED, ASAM_OK, AsamConfig, AsamError, AsamProjConfig, check, ptr
+from ._lib import (ASAM_BREAKDOWN, ASAM_NOT_CONVERGED, ASAM_OK, AsamConfig, AsamDynConfig, AsamError, AsamProjConfig,
+                   check, ptr)
 
 METHODS = {"Ros3AMF": 0, "RosRK32": 1, "RosEul": 2, "Ros3P": 3, "Ros3Pw": 4, "RosRK3": 5, "RosTVD": 6,
            "RosRK4": 7}
@@ -143,6 +150,21 @@ class TransportBlock:
         a = _f64(c).copy()
         n = ncomp if ncomp is not None else a.size // self.grid.npad
         check(self.lib.asam_exchange_cell(self.h, n, ptr(a)), "asam_exchange_cell")
+        return a
+
+    def set_boundary(self, kinds):
+        """Halo rule of the outer walls, applied to the state at the start of
+        every stage (BoundaryCondition / BoundaryVelocity, ADVECT/Int_Mod.f90:
+        283-287): (ncomp, 6) ints, sides W,E,S,N,B,T, 0 none, 1 ZeroGrad,
+        2 ZeroValue.  A new block has ZeroGrad everywhere."""
+        k = np.ascontiguousarray(kinds, dtype=np.int32).reshape(-1)
+        if k.size != 6 * self.ncomp:
+            raise ValueError("kinds must have 6 entries per component")
+        check(self.lib.asam_set_boundary(self.h, k.ctypes.data_as(C.POINTER(C.c_int))), "asam_set_boundary")
+
+    def BoundaryCondition(self, c: np.ndarray) -> np.ndarray:
+        a = self._state(c).copy()
+        check(self.lib.asam_boundary_condition(self.h, ptr(a)), "asam_boundary_condition")
         return a
 
     def Fcn(self, c: np.ndarray) -> np.ndarray:
@@ -346,6 +368,77 @@ class TransportBlock:
                                             len(scalars), ptr(p), C.byref(steps), C.byref(res))
         check(st, "asam_project_vel_face", allow=(ASAM_OK, ASAM_NOT_CONVERGED))
         return p, steps.value, res.value
+
+    # -- dynamical-core stage (momentum branch of StageRos) -------------------------
+    def dyn_setup(self, th_pos: int, mom_pos, rv_pos: int = -1, rc_pos: int = -1, rr_pos: int = -1,
+                  ri_pos: int = -1, pgradient: bool = True, buoyancy: bool = True, free_slip: bool = True,
+                  wall_no_slip: bool = False, grav: float = 9.81, bound_cells=None, scalars=()):
+        """asam_dyn_setup: component positions (0-based, -1 absent), the
+        physics switches, the BoundCell list ((n,3) 1-based interior cells)
+        and the DivScalar components of ProjectVelFace.  Needs proj_setup."""
+        self.dcfg = AsamDynConfig(int(th_pos), int(rv_pos), int(rc_pos), int(rr_pos), int(ri_pos),
+                                  (C.c_int * 6)(*[int(q) for q in mom_pos]), int(bool(pgradient)),
+                                  int(bool(buoyancy)), int(bool(free_slip)), int(bool(wall_no_slip)), float(grav))
+        bc = np.zeros((0, 3), dtype=np.int32) if bound_cells is None else np.ascontiguousarray(bound_cells,
+                                                                                              dtype=np.int32)
+        self._bound = bc.reshape(-1, 3)
+        sc = (C.c_int * max(1, len(scalars)))(*scalars)
+        check(self.lib.asam_dyn_setup(self.h, C.byref(self.dcfg), self._bound.ctypes.data_as(_lib._I),
+                                      len(self._bound), sc, len(scalars)), "asam_dyn_setup")
+
+    def VelocityFaceToCellLR(self, uf, vf, wf, c) -> np.ndarray:
+        a = self._state(c).copy()
+        u, v, w = _f64(uf), _f64(vf), _f64(wf)
+        check(self.lib.asam_face_to_cell(self.h, ptr(u), ptr(v), ptr(w), ptr(a)), "asam_face_to_cell")
+        return a
+
+    def VelocityCellToFaceLR(self, c):
+        a = self._state(c)
+        g = self.grid
+        u = np.empty((g.nz, g.ny, g.nx + 1))
+        v = np.empty((g.nz, g.ny + 1, g.nx))
+        w = np.empty((g.nz + 1, g.ny, g.nx))
+        check(self.lib.asam_cell_to_face(self.h, ptr(a), ptr(u), ptr(v), ptr(w)), "asam_cell_to_face")
+        return u, v, w
+
+    def AbsTPreCompute(self, c):
+        """AbsTCompute ('Density') and PreCompute: (TAbsCell, PreCell), padded."""
+        a = self._state(c)
+        t = np.empty(self.grid.pshape)
+        p = np.empty(self.grid.pshape)
+        check(self.lib.asam_thermo(self.h, ptr(a), ptr(t), ptr(p)), "asam_thermo")
+        return t, p
+
+    def FcnMet(self, c, pre) -> np.ndarray:
+        """FcnMet of the dynamical stage: advection, pressure gradient, scale, buoyancy."""
+        a = self._state(c)
+        pp = _f64(pre)
+        f = np.empty_like(a)
+        check(self.lib.asam_fcn_dyn(self.h, ptr(a), ptr(pp), ptr(f)), "asam_fcn_dyn")
+        return f
+
+    def Ros3MetC_dyn(self, c: np.ndarray, dt: float):
+        """One Rosenbrock step of the dynamical core: c (in place) and the
+        block's face velocities advance.  Returns (BiCGStab (iters, resid),
+        FGMRES (steps, relative residual)) per stage."""
+        if not (isinstance(c, np.ndarray) and c.dtype == np.float64 and c.flags.c_contiguous):
+            raise TypeError("c must be a C-contiguous float64 array (updated in place)")
+        it = (C.c_int * 4)()
+        rs = (C.c_double * 4)()
+        ps = (C.c_int * 4)()
+        pr = (C.c_double * 4)()
+        st = self.lib.asam_ros_step_dyn(self.h, ptr(c), float(dt), it, rs, ps, pr)
+        check(st, "asam_ros_step_dyn", allow=(ASAM_OK, ASAM_NOT_CONVERGED, ASAM_BREAKDOWN))
+        n = self.nstage
+        return (list(it[:n]), list(rs[:n])), (list(ps[:n]), list(pr[:n]))
+
+    def get_velocity(self):
+        g = self.grid
+        u = np.empty((g.nz, g.ny, g.nx + 1))
+        v = np.empty((g.nz, g.ny + 1, g.nx))
+        w = np.empty((g.nz + 1, g.ny, g.nx))
+        check(self.lib.asam_get_velocity(self.h, ptr(u), ptr(v), ptr(w)), "asam_get_velocity")
+        return u, v, w
 
 
 class Batch:

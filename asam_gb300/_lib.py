@@ -44,6 +44,14 @@ class AsamProjConfig(C.Structure):
     ]
 
 
+class AsamDynConfig(C.Structure):
+    _fields_ = [
+        ("th_pos", C.c_int), ("rv_pos", C.c_int), ("rc_pos", C.c_int), ("rr_pos", C.c_int), ("ri_pos", C.c_int),
+        ("mom_pos", C.c_int * 6), ("pgradient", C.c_int), ("buoyancy", C.c_int), ("free_slip", C.c_int),
+        ("wall_no_slip", C.c_int), ("grav", C.c_double),
+    ]
+
+
 # (name, restype, argtypes) of every exported entry point of include/asam_gb300.h
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
@@ -57,6 +65,8 @@ SIGNATURES = [
     ("asam_synchronize", C.c_int, [_V]),
     ("asam_set_velocity", C.c_int, [_V, _V, _V, _V]),
     ("asam_exchange_cell", C.c_int, [_V, C.c_int, _V]),
+    ("asam_set_boundary", C.c_int, [_V, C.POINTER(C.c_int)]),
+    ("asam_boundary_condition", C.c_int, [_V, _V]),
     ("asam_fcn", C.c_int, [_V, _V, _V]),
     ("asam_div", C.c_int, [_V, _V]),
     ("asam_jac", C.c_int, [_V, _V, C.c_double]),
@@ -91,6 +101,13 @@ SIGNATURES = [
     ("asam_solve_sound", C.c_int, [_V, _V, _V, _I, _D]),
     ("asam_project_vel_face", C.c_int, [_V, _V, _V, _V, _V, _V, C.c_int, C.c_int, _I, C.c_int, _V, _I, _D]),
     ("asam_proj_vcycles", C.c_longlong, [_V]),
+    ("asam_dyn_setup", C.c_int, [_V, C.POINTER(AsamDynConfig), _I, C.c_int, _I, C.c_int]),
+    ("asam_face_to_cell", C.c_int, [_V, _V, _V, _V, _V]),
+    ("asam_cell_to_face", C.c_int, [_V, _V, _V, _V, _V]),
+    ("asam_thermo", C.c_int, [_V, _V, _V, _V]),
+    ("asam_fcn_dyn", C.c_int, [_V, _V, _V, _V]),
+    ("asam_ros_step_dyn", C.c_int, [_V, _V, C.c_double, _I, _D, _I, _D]),
+    ("asam_get_velocity", C.c_int, [_V, _V, _V, _V]),
     ("asam_ros_coeffs", C.c_int, [C.c_int, _D, _D, _D, _D]),
     ("asam_autotune", C.c_int, [_V, _V, C.c_double, _I, _D]),
     ("asam_state_dot", C.c_int, [_V, _V, _D]),

@@ -1,6 +1,6 @@
 """Build recipe of the CUDA library (sm_103a) and of the CPU oracle.
 
-The library is five translation units compiled in parallel by nvcc and
+The library is a set of translation units compiled in parallel by nvcc and
 linked into ``asam_gb300/libasam_gb300.so``:
 
 * ``k64.cu``  FP64 kernels with ``-fmad=false`` (reference rounding, no FMA)
@@ -9,9 +9,13 @@ linked into ``asam_gb300/libasam_gb300.so``:
 * ``tri_noalloc.cu`` the column solve that allocates nothing
 * ``adjoint.cu`` tangent-linear and adjoint of the transport stage
 * ``proj.cu`` pressure projection: Laplacian hierarchy, multigrid, FGMRES
+* ``dyn.cu`` dynamical-core stage: momentum sources, face/cell velocities,
+  thermodynamics and the stage driver around the transport solve and the
+  projection
 
 The oracle (``oracle/asam_oracle.c`` for the transport stage,
-``oracle/asam_proj.c`` for the pressure projection) is a test-only checker
+``oracle/asam_proj.c`` for the pressure projection, ``oracle/asam_dyn.c`` for
+the dynamical-core stage) is a test-only checker
 compiled by gcc into ``oracle/_build/libasam_oracle.so``.
 """
 from __future__ import annotations
@@ -29,7 +33,8 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libasam_gb300.so"
-ORACLE_SRC = [ROOT / "oracle" / "asam_oracle.c", ROOT / "oracle" / "asam_proj.c"]
+ORACLE_SRC = [ROOT / "oracle" / "asam_oracle.c", ROOT / "oracle" / "asam_proj.c", ROOT / "oracle" / "asam_dyn.c"]
+ORACLE_DEPS = ORACLE_SRC + [ROOT / "oracle" / "asam_oracle.h"]
 ORACLE_LIB = ROOT / "oracle" / "_build" / "libasam_oracle.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -44,6 +49,7 @@ UNITS = {
     "tune.cu": [],
     "step_graph.cu": ["-fmad=false"],
     "proj.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    "dyn.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
 }
 
 
@@ -99,7 +105,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
 
 def build_oracle(force: bool = False) -> Path:
     """Compile the CPU oracle (test infrastructure) with gcc."""
-    if not force and not _stale(ORACLE_LIB, ORACLE_SRC):
+    if not force and not _stale(ORACLE_LIB, ORACLE_DEPS):
         return ORACLE_LIB
     ORACLE_LIB.parent.mkdir(exist_ok=True)
     tmp = ORACLE_LIB.with_suffix(".so.tmp")

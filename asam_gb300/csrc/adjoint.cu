@@ -668,6 +668,18 @@ void axpby(asam_ctx* h, double a, const double* x, double b, double* y) {
   count_launches(1);
 }
 
+// Transpose of the halo derivation of a state field of component comp at the
+// start of a stage: the periodic ExchangeCell and the outer-wall rule
+// (k_bound_cond); both read interior cells only and write disjoint halos, so
+// their transposes add independently.  The halo layer is left to the caller.
+void state_halo_T(asam_ctx* h, int comp, double* x) {
+  const Launch& L = h->L;
+  const size_t nint = (size_t)h->d.nx * h->d.ny * h->d.nz;
+  k_exchange_T<<<grid_of(L, nint), kB, 0, L.stream>>>(h->d, x);
+  k_bound_cond_T<double><<<grid_of(L, nint), kB, 0, L.stream>>>(h->d, comp, h->bc, x);
+  count_launches(2);
+}
+
 // y = A_per^T x = E^T A^T Z x  (x: interior values, halos ignored; y: zero halos)
 void matvec_per_T(asam_ctx* h, AdjWork& w, const double* x, double* y) {
   const Launch& L = h->L;
@@ -777,6 +789,7 @@ int forward_record(asam_ctx* h, const double* c, double dt, double tol, std::vec
   const int nc = h->cfg.ncomp;
   for (int is = 0; is < h->nstage; ++is) {
     launch_exchange_cell(L, d, nc, cur);
+    launch_bound_cond(L, d, nc, 0, h->bc, cur);
     CK(cudaMemcpyAsync(stage_states[is], cur, len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
     if (is == 0) {
       int rc = jac_dev(h, cur, dt);
@@ -813,6 +826,7 @@ int step_tlm(asam_ctx* h, AdjWork& w, const std::vector<double*>& stage_states, 
     for (int js = 0; js < is; ++js) axpby(h, h->alpha[(is - 1) * 4 + js], dk[js], 1.0, ui);
     k_zero_halo1<<<grid_of(L, n), kB, 0, L.stream>>>(h->d, ui);
     launch_exchange_cell(L, h->d, 1, ui);
+    launch_bound_cond(L, h->d, 1, comp, h->bc, ui);
     flux_dcoef(h, w, stage_states[is], comp);
     flux_tlm(h, w, rho, ui, bi);
     k_axpby<<<grid_of(L, n), kB, 0, L.stream>>>(n, 0.0, bi, dt, bi);
@@ -859,9 +873,9 @@ int step_adj(asam_ctx* h, AdjWork& w, const std::vector<double*>& stage_states, 
     k_zero_halo1<<<grid_of(L, n), kB, 0, L.stream>>>(h->d, lb);
     flux_dcoef(h, w, stage_states[is], comp);
     flux_adj(h, w, rho, lb, lu);
-    k_exchange_T<<<grid_of(L, (size_t)h->d.nx * h->d.ny * h->d.nz), kB, 0, L.stream>>>(h->d, lu);
+    state_halo_T(h, comp, lu);
     k_zero_halo1<<<grid_of(L, n), kB, 0, L.stream>>>(h->d, lu);
-    count_launches(3);
+    count_launches(1);
     axpby(h, dt, lu, 1.0, acc);
     for (int js = 0; js < is; ++js) axpby(h, dt * h->alpha[(is - 1) * 4 + js], lu, 1.0, lk[js]);
   }
@@ -973,10 +987,11 @@ int step_adj_coupled(asam_ctx* h, AdjWork& w, CoupledWork& cw, const std::vector
     count_launches(6);
     // stage state y = u0 + sum alpha k: lu = dt E^T Z (lc, lr)
     double* lus[2] = {cw.luc, cw.lur};
-    for (double* lu : lus) {
-      k_exchange_T<<<grid_of(L, nint), kB, 0, L.stream>>>(d, lu);
-      k_zero_halo1<<<gn, kB, 0, L.stream>>>(d, lu);
-      count_launches(2);
+    const int lcomp[2] = {comp, rp};
+    for (int q = 0; q < 2; ++q) {
+      state_halo_T(h, lcomp[q], lus[q]);
+      k_zero_halo1<<<gn, kB, 0, L.stream>>>(d, lus[q]);
+      count_launches(1);
     }
     axpby(h, dt, cw.luc, 1.0, cw.accc);
     axpby(h, dt, cw.lur, 1.0, cw.accr);
@@ -986,9 +1001,9 @@ int step_adj_coupled(asam_ctx* h, AdjWork& w, CoupledWork& cw, const std::vector
     }
   }
   // Rho_0 of the stage matrix is the exchanged start state: E^T, then add
-  k_exchange_T<<<grid_of(L, nint), kB, 0, L.stream>>>(d, cw.grho);
+  state_halo_T(h, rp, cw.grho);
   k_zero_halo1<<<gn, kB, 0, L.stream>>>(d, cw.grho);
-  count_launches(2);
+  count_launches(1);
   axpby(h, 1.0, cw.grho, 1.0, cw.accr);
   CK(cudaMemcpyAsync(lc_out, cw.accc, n * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
   CK(cudaMemcpyAsync(lr_out, cw.accr, n * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));

@@ -64,12 +64,12 @@ struct Dims {
       j = (int)(r - (size_t)k * NYu);
     }
   }
-  size_t n_fu() const { return (size_t)(nx + 3) * ny * nz; }
-  size_t n_fv() const { return (size_t)nx * (ny + 3) * nz; }
-  size_t n_fw() const { return (size_t)nx * ny * (nz + 3); }
-  size_t n_uf() const { return (size_t)(nx + 1) * ny * nz; }
-  size_t n_vf() const { return (size_t)nx * (ny + 1) * nz; }
-  size_t n_wf() const { return (size_t)nx * ny * (nz + 1); }
+  __host__ __device__ size_t n_fu() const { return (size_t)(nx + 3) * ny * nz; }
+  __host__ __device__ size_t n_fv() const { return (size_t)nx * (ny + 3) * nz; }
+  __host__ __device__ size_t n_fw() const { return (size_t)nx * ny * (nz + 3); }
+  __host__ __device__ size_t n_uf() const { return (size_t)(nx + 1) * ny * nz; }
+  __host__ __device__ size_t n_vf() const { return (size_t)nx * (ny + 1) * nz; }
+  __host__ __device__ size_t n_wf() const { return (size_t)nx * ny * (nz + 1); }
 };
 
 // Geometry and prescribed face velocities resident on the device.
@@ -82,6 +82,21 @@ struct GeomT {
   const T* uf;
   const T* vf;
   const T* wf;
+};
+
+// Halo rule of each component on each side that is not periodic (the outer
+// walls 'ow'...'ot' of a block): BoundaryCompute
+// (ADVECT/BoundaryCondition_Mod.f90:70-346) for the scalars and
+// BoundaryVelocityCellCompute (:424-970) for the momentum components.  Sides
+// in the order W, E, S, N, B, T; only the face halo cells (tangential interior
+// ranges) are set, like the reference's loops.
+enum BcKind : signed char {
+  kBcNone = 0,       // halo left as it is
+  kBcZeroGrad = 1,   // halo = adjacent interior cell
+  kBcZeroValue = 2,  // halo = -adjacent interior cell
+};
+struct BcKinds {
+  signed char k[kMaxComp][6];
 };
 
 // Krylov scalars that stay on the device between kernels.

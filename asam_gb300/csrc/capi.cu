@@ -566,6 +566,7 @@ int ros_step_dev(asam_ctx* h, double* c, double dt, int* iters, double* resid) {
   CK(cudaMemcpyAsync(h->cold, c, len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
   for (int is = 0; is < h->nstage; ++is) {
     launch_exchange_cell(L, d, nc, c);
+    launch_bound_cond(L, d, nc, 0, h->bc, c);
     if (is == 0) {
       int rc = jac_dev(h, c, dt);
       if (rc) return rc;
@@ -771,6 +772,7 @@ int asam_destroy(asam_ctx* h) {
   free_work(h->w32);
   gs_schedule_free(h);  // and the graphs
   proj_free(h);
+  dyn_free(h);
   for (auto st : h->cap_stream)
     if (st) cudaStreamDestroy(st);
   if (h->stage_sc) cudaFree(h->stage_sc);
@@ -799,6 +801,8 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
   h->npad = h->d.npad();
   h->len = h->npad * (size_t)cfg->ncomp;
   h->nstage = ros_coeffs(cfg->method, &h->beta0, h->alpha, h->beta, h->gamma1);
+  for (int ic = 0; ic < kMaxComp; ++ic)
+    for (int sd = 0; sd < 6; ++sd) h->bc.k[ic][sd] = kBcZeroGrad;
   if (h->nstage <= 0) {
     delete h;
     set_last_error("unknown Rosenbrock method", __FILE__, __LINE__);
@@ -916,6 +920,27 @@ int asam_exchange_cell(asam_ctx* h, int ncomp, double* c) {
   rc = check_launch();
   if (rc) return rc;
   return stage_out_end(h, c, n, dc);
+}
+
+int asam_set_boundary(asam_ctx* h, const int* kinds) {
+  if (!h || !kinds) return kBadArg;
+  for (int q = 0; q < 6 * h->cfg.ncomp; ++q)
+    if (kinds[q] < ASAM_BC_NONE || kinds[q] > ASAM_BC_ZERO_VALUE) return kBadArg;
+  for (int ic = 0; ic < h->cfg.ncomp; ++ic)
+    for (int sd = 0; sd < 6; ++sd) h->bc.k[ic][sd] = (signed char)kinds[6 * ic + sd];
+  graphs_reset(h);  // a captured step holds the old rule
+  return kOk;
+}
+
+int asam_boundary_condition(asam_ctx* h, double* c) {
+  if (!h || !c) return kBadArg;
+  double* dc;
+  int rc = stage_out_begin(h, c, h->len, h->stage_a, &dc, true);
+  if (rc) return rc;
+  launch_bound_cond(h->L, h->d, h->cfg.ncomp, 0, h->bc, dc);
+  rc = check_launch();
+  if (rc) return rc;
+  return stage_out_end(h, c, h->len, dc);
 }
 
 int asam_fcn(asam_ctx* h, const double* c, double* f) {

@@ -31,6 +31,7 @@ inline void free_work(Work<T>& w) {
 }
 
 struct ProjState;
+struct DynState;
 
 }  // namespace asam
 
@@ -99,6 +100,10 @@ struct asam_ctx {
   int* gs_counter = nullptr;  // [0] ticket counter; [1] epoch base (unsigned)
 
   asam::ProjState* proj = nullptr;  // pressure projection (proj.cu), set up on demand
+  asam::DynState* dyn = nullptr;    // dynamical-core stage (dyn.cu), set up on demand
+  // halo rule of each component on the outer walls, applied to the state at
+  // the start of every stage (default ZeroGrad, BoundaryCond_Mod.f90:240-247)
+  asam::BcKinds bc{};
 
   GeomT<double> geom() const { return GeomT<double>{volc, fu, fv, fw, uf, vf, wf}; }
 };
@@ -130,6 +135,12 @@ int ros_step_graph(asam_ctx* h, double* c, double dt, int* iters, double* resid)
 void step_graph_free(asam_ctx* h);
 long long thread_launches();
 void proj_free(asam_ctx* h);
+// device arrays of the projection's grid (valid after asam_proj_setup)
+struct ProjGrid {
+  const double *dx, *dy, *dz, *mxy, *myx;
+};
+bool proj_grid(asam_ctx* h, ProjGrid* out);
+void dyn_free(asam_ctx* h);
 
 }  // namespace asam
 

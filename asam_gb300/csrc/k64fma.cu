@@ -20,7 +20,7 @@ void launch_fcn(const Launch& L, const Dims& d, const GeomT<double>& g, int ncom
   k_face_flux<double, 0><<<gs_grid(L, d.n_uf()), kBlock, 0, L.stream>>>(d, g, ncomp, cx, mx, phi, gx);
   k_face_flux<double, 1><<<gs_grid(L, d.n_vf()), kBlock, 0, L.stream>>>(d, g, ncomp, cy, my, phi, gy);
   k_face_flux<double, 2><<<gs_grid(L, d.n_wf()), kBlock, 0, L.stream>>>(d, g, ncomp, cz, mz, phi, gz);
-  k_flux_gather<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f);
+  k_flux_gather<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f, MomSrc<double>{});
   count_launches(5);
 }
 

@@ -233,13 +233,66 @@ __global__ void k_face_flux(Dims d, GeomT<T> g, int ncomp, const T* __restrict__
   }
 }
 
+// Momentum sources of the dynamical stage of a closed block, added by FcnMet
+// to the six LR momentum components (ADVECT/Function_Mod.f90:1267-1297,
+// 1389-1393): the pressure gradient before AdvectionScale and the buoyancy
+// after it.
+template <typename T>
+struct MomSrc {
+  const T* p;    // PreCell, padded
+  const T* rho;  // density component of the state, padded
+  const T *dx, *dy, *dz;  // widths of the interior cells
+  const T *mxy, *myx;     // MetrXY(iy), MetrYX(ix)
+  int pos[6];             // uL, uR, vL, vR, wL, wR components (-1: none)
+  int pgrad, buoy;        // PGradient, Buoyancy
+  T grav;                 // Grav
+};
+
+// Grad of PGradComputeCFull (ADVECT/PressureGrad_Mod.f90:252-276) on the
+// interior face between padded cells (i,j,k) and their +1 neighbour along
+// axis, with DUU = F/(F+Eps) of IniJacAccGrav (MULTI/JacAccGrav_Mod.f90:297):
+//   DUU*F/(F+Eps)*(p(+1)-p)/(Metr*(d(+1)+d+Eps)), evaluated left to right.
+template <typename T>
+__device__ __forceinline__ T pgrad_face(const Dims& d, const GeomT<T>& g, const MomSrc<T>& ms, int axis, int i, int j,
+                                        int k) {
+  const T e = eps_t<T>();
+  if (axis == 0) {
+    const T F = g.fu[d.FU(i, j, k)];
+    const T du = F / (F + e);
+    return du * F / (F + e) * (ms.p[d.P(i + 1, j, k)] - ms.p[d.P(i, j, k)]) /
+           (ms.mxy[j - 1] * (ms.dx[i] + ms.dx[i - 1] + e));
+  }
+  if (axis == 1) {
+    const T F = g.fv[d.FV(i, j, k)];
+    const T du = F / (F + e);
+    return du * F / (F + e) * (ms.p[d.P(i, j + 1, k)] - ms.p[d.P(i, j, k)]) /
+           (ms.myx[i - 1] * (ms.dy[j] + ms.dy[j - 1] + e));
+  }
+  const T F = g.fw[d.FW(i, j, k)];
+  const T du = F / (F + e);
+  return du * F / (F + e) * (ms.p[d.P(i, j, k + 1)] - ms.p[d.P(i, j, k)]) / (ms.dz[k] + ms.dz[k - 1] + e);
+}
+
+// RhoLoc of AuftriebDryComputeLRFull (ADVECT/Buoyancy_Mod.f90:51-63) on the
+// face between levels k and k+1.
+template <typename T>
+__device__ __forceinline__ T buoy_rho_face(const Dims& d, const GeomT<T>& g, const MomSrc<T>& ms, int i, int j,
+                                           int k) {
+  const T e = eps_t<T>();
+  const T F = g.fw[d.FW(i, j, k)];
+  return F / (F + e) * (ms.dz[k - 1] * ms.rho[d.P(i, j, k)] + ms.dz[k] * ms.rho[d.P(i, j, k + 1)]) /
+         (ms.dz[k - 1] + ms.dz[k] + e);
+}
+
 // Gather of the face fluxes into the cell right-hand side in the exact order
 // in which the reference's scatter loop touches f(ix,iy,iz), then the
 // zero-volume mask (:1045-1051), the periodic ExchangeFlux (neighbour order
 // W,E,S,N,B,T) and AdvectionScale (:2888-2898).  One thread per padded cell.
-template <typename T>
+// kMom adds the momentum sources of ms (closed blocks).
+template <typename T, bool kMom = false>
 __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict__ gx, const T* __restrict__ gy,
-                              const T* __restrict__ gz, const T* __restrict__ rvol, T* __restrict__ f) {
+                              const T* __restrict__ gz, const T* __restrict__ rvol, T* __restrict__ f,
+                              MomSrc<T> ms) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
   const size_t n = d.npad();
@@ -281,6 +334,20 @@ __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict
         if (vR < (T)0) a = a + GY[fyR];
         if (wR < (T)0) a = a + GZ[fzR];
         a = div_rn(a * V, Ve, rV);
+        if (kMom && ms.pgrad) {  // uRhsL(ix+1) - Two*VolC(ix+1)*Grad, uRhsR(ix) - Two*VolC(ix)*Grad
+          int axis = -1, lo = 0;
+          if (ic == ms.pos[0] && i >= 2) axis = 0, lo = 1;
+          else if (ic == ms.pos[1] && i <= nx - 1) axis = 0;
+          else if (ic == ms.pos[2] && j >= 2) axis = 1, lo = 1;
+          else if (ic == ms.pos[3] && j <= ny - 1) axis = 1;
+          else if (ic == ms.pos[4] && k >= 2) axis = 2, lo = 1;
+          else if (ic == ms.pos[5] && k <= nz - 1) axis = 2;
+          if (axis >= 0) {
+            const T gr = pgrad_face(d, g, ms, axis, i - (axis == 0 ? lo : 0), j - (axis == 1 ? lo : 0),
+                                    k - (axis == 2 ? lo : 0));
+            a = a - (T)2 * V * gr;
+          }
+        }
         if (exW) {
           const size_t PH = d.P(nx + 1, j, k), fh = d.UF(nx, j, k);
           T h = g.uf[fh] > (T)0 ? GX[fh] : (T)0;
@@ -317,7 +384,12 @@ __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict
           T VH = g.volc[PH];
           a = a + div_rn(h * VH, VH + e, rvol[PH]);
         }
-        f[ic * n + P] = div_rn(a, Ve, rV);
+        T fv = div_rn(a, Ve, rV);
+        if (kMom && ms.buoy) {  // fL(iz+1) - RhoLoc*Grav, fR(iz) - RhoLoc*Grav
+          if (ic == ms.pos[4] && k >= 2) fv = fv - buoy_rho_face(d, g, ms, i, j, k - 1) * ms.grav;
+          else if (ic == ms.pos[5] && k <= nz - 1) fv = fv - buoy_rho_face(d, g, ms, i, j, k) * ms.grav;
+        }
+        f[ic * n + P] = fv;
       }
     } else {
       // halo cell: only the face-halo cells next to the interior receive a flux
@@ -1214,6 +1286,73 @@ __global__ void k_exchange_cell(Dims d, int ncomp, T* __restrict__ c) {
       a[lo] = a[lo_src];
       a[hi] = a[hi_src];
     }
+  }
+}
+
+// Halo rule of the outer walls (BoundaryCondition / BoundaryVelocity at the
+// start of a stage, ADVECT/Int_Mod.f90:283-287): every face halo cell of a
+// side that is not periodic takes the adjacent interior value (ZeroGrad) or
+// its negative (ZeroValue).  comp0 is the first component's index in bc.
+template <typename T>
+__global__ void k_bound_cond(Dims d, int ncomp, int comp0, asam::BcKinds bc, T* __restrict__ c) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const size_t n = d.npad();
+  const size_t nxf = d.per_x ? 0 : (size_t)ny * nz;
+  const size_t nyf = d.per_y ? 0 : (size_t)nx * nz;
+  const size_t nzf = d.per_z ? 0 : (size_t)nx * ny;
+  const size_t tot = nxf + nyf + nzf;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
+    size_t lo, lo_src, hi, hi_src;
+    int side;  // W/E = 0, S/N = 2, B/T = 4
+    if (q < nxf) {
+      int j = (int)(q % ny) + 1, k = (int)(q / ny) + 1;
+      lo = d.P(0, j, k); lo_src = d.P(1, j, k); hi = d.P(nx + 1, j, k); hi_src = d.P(nx, j, k);
+      side = 0;
+    } else if (q < nxf + nyf) {
+      size_t r = q - nxf;
+      int i = (int)(r % nx) + 1, k = (int)(r / nx) + 1;
+      lo = d.P(i, 0, k); lo_src = d.P(i, 1, k); hi = d.P(i, ny + 1, k); hi_src = d.P(i, ny, k);
+      side = 2;
+    } else {
+      size_t r = q - nxf - nyf;
+      int i = (int)(r % nx) + 1, j = (int)(r / nx) + 1;
+      lo = d.P(i, j, 0); lo_src = d.P(i, j, 1); hi = d.P(i, j, nz + 1); hi_src = d.P(i, j, nz);
+      side = 4;
+    }
+    for (int ic = 0; ic < ncomp; ++ic) {
+      T* a = c + ic * n;
+      const signed char kl = bc.k[comp0 + ic][side], kh = bc.k[comp0 + ic][side + 1];
+      if (kl == asam::kBcZeroGrad) a[lo] = a[lo_src];
+      else if (kl == asam::kBcZeroValue) a[lo] = -a[lo_src];
+      if (kh == asam::kBcZeroGrad) a[hi] = a[hi_src];
+      else if (kh == asam::kBcZeroValue) a[hi] = -a[hi_src];
+    }
+  }
+}
+
+// Transpose of k_bound_cond for one field of component comp: every interior
+// cell next to a wall adds the halo cells that were derived from it (with
+// the rule's sign) and those halo cells become 0.  Each halo cell has exactly
+// one source cell, so the gather needs no atomics.
+template <typename T>
+__global__ void k_bound_cond_T(Dims d, int comp, asam::BcKinds bc, T* __restrict__ x) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const size_t nint = (size_t)nx * ny * nz;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nint; q += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % nx) + 1, j = (int)((q / nx) % ny) + 1, k = (int)(q / ((size_t)nx * ny)) + 1;
+    const bool on[6] = {!d.per_x && i == 1, !d.per_x && i == nx, !d.per_y && j == 1,
+                        !d.per_y && j == ny, !d.per_z && k == 1, !d.per_z && k == nz};
+    T add = (T)0;
+    for (int s = 0; s < 6; ++s) {
+      if (!on[s]) continue;
+      const signed char kind = bc.k[comp][s];
+      if (kind != asam::kBcZeroGrad && kind != asam::kBcZeroValue) continue;
+      const size_t H = s == 0 ? d.P(0, j, k) : s == 1 ? d.P(nx + 1, j, k) : s == 2 ? d.P(i, 0, k)
+                     : s == 3 ? d.P(i, ny + 1, k) : s == 4 ? d.P(i, j, 0) : d.P(i, j, nz + 1);
+      add = kind == asam::kBcZeroGrad ? add + x[H] : add - x[H];
+      x[H] = (T)0;
+    }
+    if (add != (T)0) x[d.P(i, j, k)] += add;
   }
 }
 

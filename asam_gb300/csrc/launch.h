@@ -33,6 +33,7 @@ struct Launch {
   void launch_xline_factor(const Launch&, const Dims&, const TM* val, T* fw, T* fr);                            \
   void launch_zero_halo(const Launch&, const Dims&, int ncomp, T* x);                                           \
   void launch_exchange_cell(const Launch&, const Dims&, int ncomp, T* c);                                       \
+  void launch_bound_cond(const Launch&, const Dims&, int ncomp, int comp0, const BcKinds& bc, T* c);            \
   void launch_dot(const Launch&, const Dims&, int ncomp, const T* x, const T* y, double* partial,               \
                   KrylovScalars* sc, int op, double* out);                                                       \
   void launch_axpy_sc(const Launch&, size_t len, const KrylovScalars* sc, int sel, double sign, const T* x,      \

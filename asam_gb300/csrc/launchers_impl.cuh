@@ -39,7 +39,7 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
   }                                                                                                                \
   void launch_flux_gather(const Launch& L, const Dims& d, const GeomT<T>& g, int ncomp, const T* gx, const T* gy,  \
                           const T* gz, const T* rvol, T* f) {                                                      \
-    k_flux_gather<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f);             \
+    k_flux_gather<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f, MomSrc<T>{}); \
     count_launches(1);                                                                                             \
   }                                                                                                                \
   void launch_recip_eps(const Launch& L, size_t len, const T* v, T* rv) {                                          \
@@ -134,6 +134,15 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
                  (d.per_z ? (size_t)d.nx * d.ny : 0);                                                              \
     if (tot == 0) return;                                                                                          \
     k_exchange_cell<T><<<gs_grid(L, tot), kBlock, 0, L.stream>>>(d, ncomp, c); count_launches(1);                                     \
+  }                                                                                                                \
+  void launch_bound_cond(const Launch& L, const Dims& d, int ncomp, int comp0, const BcKinds& bc, T* c) {        \
+    size_t tot = (d.per_x ? 0 : (size_t)d.ny * d.nz) + (d.per_y ? 0 : (size_t)d.nx * d.nz) +                       \
+                 (d.per_z ? 0 : (size_t)d.nx * d.ny);                                                              \
+    bool any = false;                                                                                              \
+    for (int ic = comp0; ic < comp0 + ncomp; ++ic)                                                                 \
+      for (int s = 0; s < 6; ++s) any = any || bc.k[ic][s] != kBcNone;                                            \
+    if (tot == 0 || !any) return;                                                                                  \
+    k_bound_cond<T><<<gs_grid(L, tot), kBlock, 0, L.stream>>>(d, ncomp, comp0, bc, c); count_launches(1);         \
   }                                                                                                                \
   void launch_dot(const Launch& L, const Dims& d, int ncomp, const T* x, const T* y, double* partial,              \
                   KrylovScalars* sc, int op, double* out) {                                                        \

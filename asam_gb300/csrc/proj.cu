@@ -1108,6 +1108,18 @@ void proj_free(asam_ctx* h) {
   h->proj = nullptr;
 }
 
+bool proj_grid(asam_ctx* h, ProjGrid* out) {
+  ProjState* s = h->proj;
+  if (!s) return false;
+  const Dims& d = h->d;
+  out->dx = s->wt.dx;
+  out->dy = s->wt.dy;
+  out->dz = s->wt.dz;
+  out->mxy = s->wt.metr;                    // MetrXY[ny]
+  out->myx = s->wt.metr + d.ny + d.nz;      // MetrYX[nx]
+  return true;
+}
+
 namespace prj {
 
 int proj_build(asam_ctx* h) {

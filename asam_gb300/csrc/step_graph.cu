@@ -197,6 +197,7 @@ int record_step(asam_ctx* h, double* c, double dt, BodyCounts* bc) {
   CK(cudaMemcpyAsync(h->cold, c, len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
   for (int is = 0; is < h->nstage; ++is) {
     launch_exchange_cell(L, d, nc, c);
+    launch_bound_cond(L, d, nc, 0, h->bc, c);
     int rc;
     if (is == 0 && (rc = jac_dev(h, c, dt))) return rc;
     if ((rc = fcn_dev(h, c, h->rhs))) return rc;

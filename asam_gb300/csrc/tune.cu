@@ -81,6 +81,7 @@ extern "C" int asam_autotune(asam_ctx* h, const double* c, double dt, int* choic
   double* cs = h->stage_b;
   CK(cudaMemcpyAsync(cs, dc, h->len * sizeof(double), cudaMemcpyDeviceToDevice, L.stream));
   launch_exchange_cell(L, h->d, h->cfg.ncomp, cs);
+  launch_bound_cond(L, h->d, h->cfg.ncomp, 0, h->bc, cs);
   if ((rc = jac_dev(h, cs, dt)) || (rc = fcn_dev(h, cs, h->rhs))) return rc;
   launch_scale_host(L, h->len, dt, h->rhs);
   double* x = h->incr;

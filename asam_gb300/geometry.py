@@ -289,6 +289,72 @@ def projection_inputs(geo: Geometry, seed: int = 3, amp: float = 1.0):
     return weights, dx, dy, dz, tuple(np.ascontiguousarray(a) for a in (u, v, w))
 
 
+def boundary_cells(geo: Geometry) -> np.ndarray:
+    """BoundCell list of a cut-cell geometry: the live interior cells that hold
+    a piece of the terrain surface, i.e. whose opposite face areas differ along
+    some axis (the surface closes the difference).  (n, 3) int32 of 1-based
+    (ix, iy, iz), x fastest."""
+    g = geo.grid
+    nx, ny, nz = g.nx, g.ny, g.nz
+    vol = geo.volc[1:nz + 1, 1:ny + 1, 1:nx + 1]
+    dif = ((geo.fu[:, :, 1:nx + 1] != geo.fu[:, :, 2:nx + 2]) | (geo.fv[:, 1:ny + 1, :] != geo.fv[:, 2:ny + 2, :]) |
+           (geo.fw[1:nz + 1] != geo.fw[2:nz + 2]))
+    k, j, i = np.nonzero((vol > 0) & dif)
+    return np.ascontiguousarray(np.stack([i + 1, j + 1, k + 1], axis=1).astype(np.int32).reshape(-1, 3))
+
+
+def closed_face_velocity(geo: Geometry, amp: float, seed: int = 0) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Seeded smooth face velocities of a closed block: amplitude amp, zero on
+    the six walls and on closed faces.  uF (nz, ny, nx+1), vF (nz, ny+1, nx),
+    wF (nz+1, ny, nx)."""
+    g = geo.grid
+    nx, ny, nz = g.nx, g.ny, g.nz
+    rng = np.random.default_rng(seed)
+
+    def smooth(shape):
+        a = rng.standard_normal(shape)
+        for ax in range(3):
+            a = (a + np.roll(a, 1, axis=ax) + np.roll(a, -1, axis=ax)) / 3.0
+        return a / max(float(np.std(a)), 1e-300)
+
+    fu = geo.fu[:, :, 1:nx + 2]
+    fv = geo.fv[:, 1:ny + 2, :]
+    fw = geo.fw[1:nz + 2]
+    u = amp * smooth(fu.shape) * (fu > 0)
+    v = amp * smooth(fv.shape) * (fv > 0)
+    w = 0.3 * amp * smooth(fw.shape) * (fw > 0)
+    u[:, :, 0] = u[:, :, nx] = 0.0
+    v[:, 0, :] = v[:, ny, :] = 0.0
+    w[0] = w[nz] = 0.0
+    return tuple(np.ascontiguousarray(a) for a in (u, v, w))
+
+
+def dyn_case(nx: int, ny: int, nz: int, seed: int = 5, hill: bool = True, moist: bool = False,
+             tracer: bool = False, amp: float = 1.0, bubble: float = 2.0):
+    """Closed block for the dynamical core: a cut-cell hill (or flat ground)
+    in a box with six walls, a stratified (N=0.01) state with a warm bubble,
+    seeded face velocities of amplitude amp that vanish on the walls.
+    Returns (geo, (uF, vF, wF), state, positions, (dx, dy, dz), boundary cells);
+    positions maps rho, mom (uL,uR,vL,vR,wL,wR), th, qv, tracer to components."""
+    if hill:
+        geo = closed_hill_case(nx, ny, nz, seed=seed)
+    else:
+        grid = Grid(nx, ny, nz, 200.0, 200.0, stretched_levels(nz, 50.0, 400.0), False, False, False)
+        geo = cut_cell_geometry(grid, None, snap=0.0, merge=0.0)
+    g = geo.grid
+    vel = closed_face_velocity(geo, amp, seed=seed + 1)
+    st = initial_state(geo, *vel, theta0=300.0, n_bv=0.01, bubble_amp=bubble, bubble_radius=600.0,
+                       bubble_z=min(1000.0, 0.3 * float(g.zP[-1])), moist=moist, tracer=tracer, momentum=True,
+                       seed=seed + 2)
+    pos = {"rho": 0, "mom": [1, 2, 3, 4, 5, 6], "th": 7}
+    if moist:
+        pos["qv"] = 8
+    if tracer:
+        pos["tracer"] = 8 + int(moist)
+    widths = (np.full(g.nx, g.dx), np.full(g.ny, g.dy), np.asarray(g.dz, dtype=np.float64).copy())
+    return geo, vel, st, pos, widths, boundary_cells(geo)
+
+
 def face_velocity(geo: Geometry, u0: float, v0: float = 0.0) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     """Prescribed steady face velocities with zero discrete divergence in flux form.
 

@@ -111,6 +111,20 @@ int asam_set_velocity(asam_ctx *ctx, const double *uf, const double *vf, const d
  * (MODULE/Vector4CellPar_Mod.f90:752, RandCopyCell_VecCell :611-659). */
 int asam_exchange_cell(asam_ctx *ctx, int ncomp, double *c);
 
+/* Halo rule of the outer walls (sides that are not periodic), applied to the
+ * state at the start of every Rosenbrock stage like BoundaryCondition and
+ * BoundaryVelocity (ADVECT/Int_Mod.f90:283-287; BoundaryCompute
+ * ADVECT/BoundaryCondition_Mod.f90:70-346 and BoundaryVelocityCellCompute
+ * :424-970 for the kinds below).  kinds[6*ic + side], sides W,E,S,N,B,T.
+ * The default of a new context is ZeroGrad everywhere, the reference's
+ * default BCMetVec (MODULE/BoundaryCond_Mod.f90:240-247).  A closed box with
+ * free-slip walls (BCVel='FreeSlip') has ZeroValue for the momentum
+ * components normal to a wall (:292-294 and the other sides). */
+enum { ASAM_BC_NONE = 0, ASAM_BC_ZERO_GRAD = 1, ASAM_BC_ZERO_VALUE = 2 };
+int asam_set_boundary(asam_ctx *ctx, const int *kinds);
+/* Apply the halo rule to a state (ncomp padded fields) once. */
+int asam_boundary_condition(asam_ctx *ctx, double *c);
+
 /* Advection right-hand side of all components: the FcnMet advection terms
  * (ADVECT/Function_Mod.f90:1032-1099, 1312-1345): AdvectionComputeP
  * (ADVECT/Advection_Mod.f90:737-1054), ExchangeFlux, AdvectionScale.
@@ -304,6 +318,63 @@ int asam_project_vel_face(asam_ctx *ctx, double *uf, double *vf, double *wf, dou
                           double *resid);
 /* Number of multigrid V-cycles run by this context's projection (diagnostic). */
 long long asam_proj_vcycles(asam_ctx *ctx);
+
+/* ---------------------------------------------------------------------------
+ * Dynamical-core stage of a closed block: the momentum branch (uPosL>0) of
+ * StageRos (ADVECT/Int_Mod.f90:263-374) around the transport solve and the
+ * pressure projection.  Needs asam_proj_setup first.  The state holds the
+ * six LR momentum components (Rho times the face velocity left/right of the
+ * cell) besides Rho, rho theta and the moisture/tracer components; the face
+ * velocities VelF are the context's (asam_set_velocity), advanced by
+ * asam_ros_step_dyn.  Component positions are 0-based, -1 = absent (the
+ * reference's zero component).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int th_pos;       /* ThPos: rho theta */
+  int rv_pos;       /* RhoVPos */
+  int rc_pos;       /* RhoCPos */
+  int rr_pos;       /* RhoRPos */
+  int ri_pos;       /* RhoIPos */
+  int mom_pos[6];   /* uPosL, uPosR, vPosL, vPosR, wPosL, wPosR */
+  int pgradient;    /* PGradient (MODULE/Physics_Mod.f90:107) */
+  int buoyancy;     /* Buoyancy (:129) */
+  int free_slip;    /* FreeSlip (:189, default 1): ShiftVel1 at the boundary cells, else ShiftNoSlip */
+  int wall_no_slip; /* BCVel of the six walls: 0 'FreeSlip', 1 'NoSlip' (MODULE/BoundaryCond_Mod.f90:292-299) */
+  double grav;      /* Grav (9.81) */
+} asam_dyn_config;
+/* Configure the stage: bound_cells = BoundCell list, (ix,iy,iz) triples of
+ * interior cells (1-based) that hold a piece of the terrain surface;
+ * scalars = the components that ProjectVelFace corrects with DivScalar
+ * (MATRIX/Rhs_Mod.f90:883-889: 1..uPosL-1 without ThPos and RhoPos).
+ * Sets the walls' halo rule of the momentum components from wall_no_slip
+ * (the BCVel -> BCMetVec derivation, MODULE/BoundaryCond_Mod.f90:279-390). */
+int asam_dyn_setup(asam_ctx *ctx, const asam_dyn_config *cfg, const int *bound_cells, int nbound,
+                   const int *scalars, int nscalar);
+/* VelocityFaceToCellLR (ADVECT/VelocityCellFace_Mod.f90:72-95, 541-654): the
+ * momentum components of c (ncomp*npad, in/out) from face values uf/vf/wf,
+ * with the boundary-cell shift, then ExchangeCell. */
+int asam_face_to_cell(asam_ctx *ctx, const double *uf, const double *vf, const double *wf, double *c);
+/* VelocityCellToFaceLR (:27-52, 1369-1894): face values from the momentum
+ * components of c; outer walls take the adjacent cell value where the normal
+ * component's halo rule is ZeroGrad, 0 otherwise. */
+int asam_cell_to_face(asam_ctx *ctx, const double *c, double *uf, double *vf, double *wf);
+/* AbsTCompute ThetaKind='Density' and PreCompute (ADVECT/Diagnostic_Mod.f90:
+ * 593-615, 710-865) over the padded box: tabs and pre (npad each, nullable). */
+int asam_thermo(asam_ctx *ctx, const double *c, double *tabs, double *pre);
+/* FcnMet of the dynamical stage (ADVECT/Function_Mod.f90:989-1506): the
+ * advection of every component with the context's face velocities, the
+ * pressure gradient PGradComputeCFull (ADVECT/PressureGrad_Mod.f90:245-276)
+ * from pre, AdvectionScale and the buoyancy AuftriebDryComputeLRFull
+ * (ADVECT/Buoyancy_Mod.f90:43-63). */
+int asam_fcn_dyn(asam_ctx *ctx, const double *c, const double *pre, double *f);
+/* One Rosenbrock step of the dynamical core (Ros3MetC + StageRos,
+ * ADVECT/Int_Mod.f90:1059-1122, 263-374): c (in/out), the context's VelF
+ * advanced.  Per stage: iters/resid the BiCGStab MaxIter/Tol outputs,
+ * psteps/presid the FGMRES inner steps and relative residual (nullable). */
+int asam_ros_step_dyn(asam_ctx *ctx, double *c, double dt, int *iters, double *resid, int *psteps,
+                      double *presid);
+/* Read the context's face velocities VelF. */
+int asam_get_velocity(asam_ctx *ctx, double *uf, double *vf, double *wf);
 
 /* DOT(VecMet,VecMet): the interior dot product of the state with itself over
  * all components (Dot_VecCell, MODULE/Vector4CellPar_Mod.f90:84-102), which the

@@ -22,7 +22,7 @@ LIB_PATH = _HERE / "_build" / "libasam_oracle.so"
 class OraGeom(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("per_x", C.c_int), ("per_y", C.c_int),
                 ("per_z", C.c_int), ("volc", C.c_void_p), ("fu", C.c_void_p), ("fv", C.c_void_p),
-                ("fw", C.c_void_p)]
+                ("fw", C.c_void_p), ("bc", C.c_void_p)]
 
 
 _lib = None
@@ -42,6 +42,7 @@ def load() -> C.CDLL:
         sig = {
             "ora_exchange_cell": (None, [G, I, V]),
             "ora_exchange_flux": (None, [G, I, V]),
+            "ora_bound_cond": (None, [G, I, I, V]),
             "ora_fcn": (None, [G, I, I, V, V, V, V, V]),
             "ora_div": (None, [G, V, V, V, V]),
             "ora_jac": (None, [G, V, V, V, V, D, D, V]),
@@ -73,6 +74,13 @@ def load() -> C.CDLL:
             "ora_weights_density": (None, [V] * 15),
             "ora_proj_set_weights": (None, [V] * 9),
         })
+        sig.update({
+            "ora_face_to_cell": (None, [G, I, V, V, V, V, V, I, I, V]),
+            "ora_cell_to_face": (None, [G, V, V, V, V, V]),
+            "ora_thermo": (None, [G, V, V, V, V, V, V, V, V]),
+            "ora_fcn_dyn": (None, [G, I, I, V, I, I, D, V, V, V, V, V, V, V, V, V, V, V]),
+            "ora_ros_step_dyn": (I, [G, V, V, V, V, V, V, V, V, V, V, V, V, V, I, V, I, D, V, V, V, V]),
+        })
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
             f.restype = res
@@ -89,19 +97,35 @@ def _p(a: np.ndarray) -> int:
 class Oracle:
     """Oracle bound to one geometry (keeps the arrays alive)."""
 
-    def __init__(self, geo):
+    def __init__(self, geo, bc=None):
         self.lib = load()
         g = geo.grid
         self.grid = g
         self._keep = [np.ascontiguousarray(x, dtype=np.float64) for x in (geo.volc, geo.fu, geo.fv, geo.fw)]
         self.g = OraGeom(g.nx, g.ny, g.nz, int(g.periodic_x), int(g.periodic_y), int(g.periodic_z),
-                         *(a.ctypes.data for a in self._keep))
+                         *(a.ctypes.data for a in self._keep), None)
         self.gp = C.byref(self.g)
         self.npad = g.npad
+        self.set_boundary(bc)
+
+    def set_boundary(self, kinds):
+        """Halo rule of the outer walls, (ncomp, 6) ints W,E,S,N,B,T (0 none,
+        1 ZeroGrad, 2 ZeroValue); None = ZeroGrad everywhere."""
+        if kinds is None:
+            self._bc = None
+            self.g.bc = None
+        else:
+            self._bc = np.ascontiguousarray(kinds, dtype=np.int32).reshape(-1)
+            self.g.bc = self._bc.ctypes.data
 
     def exchange_cell(self, c):
         a = np.ascontiguousarray(c, dtype=np.float64).copy()
         self.lib.ora_exchange_cell(self.gp, a.size // self.npad, _p(a))
+        return a
+
+    def bound_cond(self, c, comp0=0):
+        a = np.ascontiguousarray(c, dtype=np.float64).copy()
+        self.lib.ora_bound_cond(self.gp, a.size // self.npad, int(comp0), _p(a))
         return a
 
     def fcn(self, c, vel, rho_pos=0):
@@ -175,6 +199,82 @@ class Oracle:
                                   int(method), float(tol), int(maxiter), int(iterg), iters.ctypes.data,
                                   resid.ctypes.data)
         return list(iters[:n]), list(resid[:n])
+
+    # -- dynamical-core stage (oracle/asam_dyn.c) ------------------------------
+    def face_to_cell(self, pos, vel, c, bound=None, free_slip=True):
+        a = np.ascontiguousarray(c, dtype=np.float64).copy()
+        uf, vf, wf = (np.ascontiguousarray(v, dtype=np.float64) for v in vel)
+        pp = np.ascontiguousarray(pos, dtype=np.int32)
+        bd = np.zeros((0, 3), np.int32) if bound is None else np.ascontiguousarray(bound, dtype=np.int32)
+        self.lib.ora_face_to_cell(self.gp, a.size // self.npad, pp.ctypes.data, _p(uf), _p(vf), _p(wf),
+                                  bd.ctypes.data, len(bd.reshape(-1, 3)), int(bool(free_slip)), _p(a))
+        return a
+
+    def cell_to_face(self, pos, c):
+        g = self.grid
+        a = np.ascontiguousarray(c, dtype=np.float64)
+        pp = np.ascontiguousarray(pos, dtype=np.int32)
+        u = np.empty((g.nz, g.ny, g.nx + 1))
+        v = np.empty((g.nz, g.ny + 1, g.nx))
+        w = np.empty((g.nz + 1, g.ny, g.nx))
+        self.lib.ora_cell_to_face(self.gp, pp.ctypes.data, _p(a), _p(u), _p(v), _p(w))
+        return u, v, w
+
+    def thermo(self, c, rho_pos, th_pos, rv_pos=-1, rc_pos=-1, rr_pos=-1, ri_pos=-1):
+        a = np.ascontiguousarray(c, dtype=np.float64)
+        n = self.npad
+        comp = lambda q: None if q < 0 else a.ctypes.data + 8 * n * q
+        t = np.empty(self.grid.pshape)
+        p = np.empty(self.grid.pshape)
+        self.lib.ora_thermo(self.gp, comp(rho_pos), comp(th_pos), comp(rv_pos), comp(rc_pos), comp(rr_pos),
+                            comp(ri_pos), _p(t), _p(p))
+        return t, p
+
+    def fcn_dyn(self, c, vel, pre, pos, dx, dy, dz, mxy=None, myx=None, rho_pos=0, pgrad=True, buoy=True,
+                grav=9.81):
+        g = self.grid
+        a = np.ascontiguousarray(c, dtype=np.float64)
+        f = np.empty_like(a)
+        uf, vf, wf = (np.ascontiguousarray(v, dtype=np.float64) for v in vel)
+        pr = np.ascontiguousarray(pre, dtype=np.float64)
+        pp = np.ascontiguousarray(pos, dtype=np.int32)
+        mxy = np.ones(g.ny) if mxy is None else np.ascontiguousarray(mxy, dtype=np.float64)
+        myx = np.ones(g.nx) if myx is None else np.ascontiguousarray(myx, dtype=np.float64)
+        dx, dy, dz = (np.ascontiguousarray(q, dtype=np.float64) for q in (dx, dy, dz))
+        self.lib.ora_fcn_dyn(self.gp, a.size // self.npad, int(rho_pos), pp.ctypes.data, int(bool(pgrad)),
+                             int(bool(buoy)), float(grav), _p(a), _p(uf), _p(vf), _p(wf), _p(pr), _p(dx), _p(dy),
+                             _p(dz), _p(mxy), _p(myx), _p(f))
+        return f
+
+    def ros_step_dyn(self, proj, c, vel, dt, *, rho_pos, th_pos, pos, dx, dy, dz, rv_pos=-1, rc_pos=-1, rr_pos=-1,
+                     ri_pos=-1, pgrad=True, buoy=True, free_slip=True, method=5, bicg_tol=1e-6, bicg_maxiter=30,
+                     iterg=5, proj_maxiter=10, proj_step=10, proj_tol=1e-6, grav=9.81, bound=None, scalars=(),
+                     mxy=None, myx=None):
+        """One step of the dynamical core; c and vel (uf, vf, wf arrays) updated
+        in place.  proj: an OracleProj of this block.  Returns per stage
+        (iters, resid, fgmres steps, fgmres relative residual)."""
+        g = self.grid
+        uf, vf, wf = vel
+        for a in (c, uf, vf, wf):
+            assert a.dtype == np.float64 and a.flags.c_contiguous
+        ip = np.array([c.size // self.npad, rho_pos, th_pos, rv_pos, rc_pos, rr_pos, ri_pos, *pos, int(bool(pgrad)),
+                       int(bool(buoy)), int(bool(free_slip)), method, bicg_maxiter, iterg, proj_maxiter, proj_step],
+                      dtype=np.int32)
+        dp = np.array([grav, bicg_tol, proj_tol])
+        mxy = np.ones(g.ny) if mxy is None else np.ascontiguousarray(mxy, dtype=np.float64)
+        myx = np.ones(g.nx) if myx is None else np.ascontiguousarray(myx, dtype=np.float64)
+        dx, dy, dz = (np.ascontiguousarray(q, dtype=np.float64) for q in (dx, dy, dz))
+        bd = np.zeros((0, 3), np.int32) if bound is None else np.ascontiguousarray(bound, dtype=np.int32)
+        sc = np.ascontiguousarray(list(scalars) or [0], dtype=np.int32)
+        it = np.zeros(4, np.int32)
+        rs = np.zeros(4)
+        ps = np.zeros(4, np.int32)
+        pr = np.zeros(4)
+        n = self.lib.ora_ros_step_dyn(self.gp, proj.h, ip.ctypes.data, dp.ctypes.data, _p(c), _p(uf), _p(vf), _p(wf),
+                                      _p(dx), _p(dy), _p(dz), _p(mxy), _p(myx), bd.ctypes.data,
+                                      len(bd.reshape(-1, 3)), sc.ctypes.data, len(scalars), float(dt),
+                                      it.ctypes.data, rs.ctypes.data, ps.ctypes.data, pr.ctypes.data)
+        return list(it[:n]), list(rs[:n]), list(ps[:n]), list(pr[:n])
 
     def total_scalar(self, c):
         a = np.ascontiguousarray(c, dtype=np.float64)

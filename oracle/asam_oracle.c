@@ -26,8 +26,10 @@
  *   MODULE/Vector4Cell_Mod.f90:1030-1036.
  *
  * Boundary handling covered: periodic sides ('iw'/'ie'/'is'/'in' neighbours
- * that are the block itself) and closed walls (no neighbour).  Outflow and
- * refined-neighbour branches are not restated.
+ * that are the block itself) and closed walls (outer sides 'ow'...'ot' with
+ * zero normal face velocity), whose halo cells the stage driver sets with the
+ * ZeroGrad / ZeroValue rules of BoundaryCondition.  Inflow ('Function'),
+ * 'MeanValue' and refined-neighbour branches are not restated.
  *
  * Build with -O2 -ffp-contract=off (no FMA contraction, like gfortran on
  * x86-64 without -march).
@@ -37,26 +39,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-#define EPS 1.0e-30 /* CG/Kind_Mod_gf.f90 Eps */
-#define HALF 0.5
-
-typedef struct {
-  int nx, ny, nz;
-  int per_x, per_y, per_z; /* 1 = periodic side pair, 0 = closed walls */
-  const double *volc, *fu, *fv, *fw;
-} ora_geom;
-
-#define NXP(g) ((g)->nx + 2)
-#define NYP(g) ((g)->ny + 2)
-#define NZP(g) ((g)->nz + 2)
-#define NPAD(g) ((size_t)NXP(g) * NYP(g) * NZP(g))
-#define PIDX(g, i, j, k) ((size_t)(i) + (size_t)NXP(g) * ((size_t)(j) + (size_t)NYP(g) * (size_t)(k)))
-#define FUI(g, i, j, k) ((size_t)((i) + 1) + (size_t)((g)->nx + 3) * ((size_t)((j)-1) + (size_t)(g)->ny * (size_t)((k)-1)))
-#define FVI(g, i, j, k) ((size_t)((i)-1) + (size_t)(g)->nx * ((size_t)((j) + 1) + (size_t)((g)->ny + 3) * (size_t)((k)-1)))
-#define FWI(g, i, j, k) ((size_t)((i)-1) + (size_t)(g)->nx * ((size_t)((j)-1) + (size_t)(g)->ny * (size_t)((k) + 1)))
-#define UFI(g, i, j, k) ((size_t)(i) + (size_t)((g)->nx + 1) * ((size_t)((j)-1) + (size_t)(g)->ny * (size_t)((k)-1)))
-#define VFI(g, i, j, k) ((size_t)((i)-1) + (size_t)(g)->nx * ((size_t)(j) + (size_t)((g)->ny + 1) * (size_t)((k)-1)))
-#define WFI(g, i, j, k) ((size_t)((i)-1) + (size_t)(g)->nx * ((size_t)((j)-1) + (size_t)(g)->ny * (size_t)(k)))
+#include "asam_oracle.h"
 
 /* ------------------------------------------------------------------ */
 /* Halo exchange for a single periodic block:                          */
@@ -86,6 +69,45 @@ void ora_exchange_cell(const ora_geom *g, int ncomp, double *c) {
         for (int i = 1; i <= nx; ++i) {
           a[PIDX(g, i, j, 0)] = a[PIDX(g, i, j, nz)];
           a[PIDX(g, i, j, nz + 1)] = a[PIDX(g, i, j, 1)];
+        }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Halo rule of the outer walls at the start of a stage, BoundaryCondition /
+ * BoundaryCompute (ADVECT/BoundaryCondition_Mod.f90:1143-1221, 70-346) and
+ * BoundaryVelocityCellCompute (:424-970) for the ZeroGrad and ZeroValue
+ * kinds: face halos of the non-periodic sides, tangential interior ranges.
+ * comp0 is the index of the first of the ncomp fields in g->bc. */
+/* ------------------------------------------------------------------ */
+static int bc_kind(const ora_geom *g, int ic, int side) { return g->bc ? g->bc[6 * ic + side] : 1; }
+static void bc_set(double *a, size_t h, size_t src, int kind) {
+  if (kind == 1) a[h] = a[src];
+  else if (kind == 2) a[h] = -a[src];
+}
+void ora_bound_cond(const ora_geom *g, int ncomp, int comp0, double *c) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const size_t n = NPAD(g);
+  for (int ic = 0; ic < ncomp; ++ic) {
+    double *a = c + ic * n;
+    const int q = comp0 + ic;
+    if (!g->per_x)
+      for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j) {
+          bc_set(a, PIDX(g, 0, j, k), PIDX(g, 1, j, k), bc_kind(g, q, 0));
+          bc_set(a, PIDX(g, nx + 1, j, k), PIDX(g, nx, j, k), bc_kind(g, q, 1));
+        }
+    if (!g->per_y)
+      for (int k = 1; k <= nz; ++k)
+        for (int i = 1; i <= nx; ++i) {
+          bc_set(a, PIDX(g, i, 0, k), PIDX(g, i, 1, k), bc_kind(g, q, 2));
+          bc_set(a, PIDX(g, i, ny + 1, k), PIDX(g, i, ny, k), bc_kind(g, q, 3));
+        }
+    if (!g->per_z)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          bc_set(a, PIDX(g, i, j, 0), PIDX(g, i, j, 1), bc_kind(g, q, 4));
+          bc_set(a, PIDX(g, i, j, nz + 1), PIDX(g, i, j, nz), bc_kind(g, q, 5));
         }
   }
 }
@@ -269,6 +291,12 @@ void ora_exchange_flux(const ora_geom *g, int ncomp, double *f) {
  *   (ADVECT/Advection_Mod.f90:2888-2898).
  * c: ncomp padded fields; comp rho_pos is the density.  f: output (zeroed here). */
 /* ------------------------------------------------------------------ */
+/* AdvectionComputeP of one component (accumulates into f, unscaled). */
+void ora_advection(const ora_geom *g, const double *c, const double *rho, const double *uf, const double *vf,
+                   const double *wf, double *f) {
+  advection_compute_p(g, c, rho, uf, vf, wf, f);
+}
+
 void ora_fcn(const ora_geom *g, int ncomp, int rho_pos, const double *c, const double *uf,
              const double *vf, const double *wf, double *f) {
   const size_t n = NPAD(g);
@@ -724,6 +752,7 @@ int ora_ros_step(const ora_geom *g, int ncomp, int rho_pos, double *c, const dou
   memcpy(cold, c, sizeof(double) * len);
   for (int is = 0; is < nStage; ++is) {
     ora_exchange_cell(g, ncomp, c);
+    ora_bound_cond(g, ncomp, 0, c); /* StageRos :287 BoundaryCondition */
     if (is == 0) ora_jac(g, c + (size_t)rho_pos * n, uf, vf, wf, beta0, dt, val);
     ora_fcn(g, ncomp, rho_pos, c, uf, vf, wf, rhs);
     for (size_t i = 0; i < len; ++i) rhs[i] = dt * rhs[i]; /* ScaleV */

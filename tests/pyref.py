@@ -310,3 +310,90 @@ def lapl_level0(geo, W, dx, dy, dz, beta0, dtp):
     d = d + first
     d = d + second
     return [a.ravel() for a in (d, uz, lz, ux, lx, u3, l3)]
+
+
+# ---------------------------------------------------------------------------
+# Dynamical-core pieces (numpy, vectorised; independent of oracle/asam_dyn.c)
+# ---------------------------------------------------------------------------
+CPD, CVD, CPV, RV, CPL, CPI, P0 = 1004.0, 717.0, 1885.0, 461.0, 4186.0, 2110.0, 1.0e5
+RD = CPD - CVD
+
+
+def bound_cond(c, kinds, periodic=(False, False, False)):
+    """BoundaryCompute ZeroGrad/ZeroValue on the face halos of the non-periodic
+    sides (ADVECT/BoundaryCondition_Mod.f90:70-346); c (ncomp, NZ, NY, NX)."""
+    out = c.copy()
+    sgn = {1: 1.0, 2: -1.0}
+    for ic in range(c.shape[0]):
+        a = out[ic]
+        k = kinds[ic]
+        if not periodic[0]:
+            if k[0] in sgn:
+                a[1:-1, 1:-1, 0] = sgn[k[0]] * a[1:-1, 1:-1, 1]
+            if k[1] in sgn:
+                a[1:-1, 1:-1, -1] = sgn[k[1]] * a[1:-1, 1:-1, -2]
+        if not periodic[1]:
+            if k[2] in sgn:
+                a[1:-1, 0, 1:-1] = sgn[k[2]] * a[1:-1, 1, 1:-1]
+            if k[3] in sgn:
+                a[1:-1, -1, 1:-1] = sgn[k[3]] * a[1:-1, -2, 1:-1]
+        if not periodic[2]:
+            if k[4] in sgn:
+                a[0, 1:-1, 1:-1] = sgn[k[4]] * a[1, 1:-1, 1:-1]
+            if k[5] in sgn:
+                a[-1, 1:-1, 1:-1] = sgn[k[5]] * a[-2, 1:-1, 1:-1]
+    return out
+
+
+def thermo(rho, rth, rv=None, rc=None, rr=None, ri=None):
+    """AbsTCompute 'Density' and PreCompute default branch
+    (ADVECT/Diagnostic_Mod.f90:602-615, 805-811), element-wise."""
+    z = np.zeros_like(rho)
+    rv = z if rv is None else rv
+    rl, rrr = (z if rc is None else rc), (z if rr is None else rr)
+    ri = z if ri is None else ri
+    rll = rl + rrr
+    rd = rho - rv - rll - ri + EPS
+    rm = RD * rd + RV * rv + EPS
+    cpml = CPD * rd + CPV * rv + CPL * rll + CPI * ri + EPS
+    kap = rm / cpml
+    with np.errstate(invalid="ignore"):
+        t = np.power(RD * rth / np.power(P0, kap), 1.0 / (1.0 - kap)) / rm + EPS
+    p = (RD * (rho - rl - rrr) + (RV - RD) * rv) * t
+    return t, p
+
+
+def momentum_sources(geo, p, rho, dx, dy, dz, grav=9.81):
+    """Pressure gradient (ADVECT/PressureGrad_Mod.f90:252-276, before
+    AdvectionScale: -2 VolC Grad per LR component) and buoyancy
+    (ADVECT/Buoyancy_Mod.f90:51-63, after the scale: -RhoLoc Grav) on the
+    interior cells of a closed block.  Returns (pg[6], bu[2]) as (nz, ny, nx)
+    arrays in the order uL, uR, vL, vR, wL, wR and wL, wR."""
+    g = geo.grid
+    nx, ny, nz = g.nx, g.ny, g.nz
+    V = geo.volc[1:nz + 1, 1:ny + 1, 1:nx + 1]
+    P = p
+    pg = [np.zeros((nz, ny, nx)) for _ in range(6)]
+    # x faces between interior cells i and i+1 (i = 1..nx-1): native FU index i+1
+    F = geo.fu[:, :, 2:nx + 1]
+    gx = F / (F + EPS) * F / (F + EPS) * (P[1:-1, 1:-1, 2:nx + 1] - P[1:-1, 1:-1, 1:nx]) / (
+        1.0 * (dx[1:] + dx[:-1] + EPS))
+    pg[0][:, :, 1:] = -2.0 * V[:, :, 1:] * gx
+    pg[1][:, :, :-1] = -2.0 * V[:, :, :-1] * gx
+    F = geo.fv[:, 2:ny + 1, :]
+    gy = F / (F + EPS) * F / (F + EPS) * (P[1:-1, 2:ny + 1, 1:-1] - P[1:-1, 1:ny, 1:-1]) / (
+        1.0 * (dy[1:] + dy[:-1] + EPS))[None, :, None]
+    pg[2][:, 1:, :] = -2.0 * V[:, 1:, :] * gy
+    pg[3][:, :-1, :] = -2.0 * V[:, :-1, :] * gy
+    F = geo.fw[2:nz + 1]
+    gz = F / (F + EPS) * F / (F + EPS) * (P[2:nz + 1, 1:-1, 1:-1] - P[1:nz, 1:-1, 1:-1]) / (
+        dz[1:] + dz[:-1] + EPS)[:, None, None]
+    pg[4][1:] = -2.0 * V[1:] * gz
+    pg[5][:-1] = -2.0 * V[:-1] * gz
+    R = rho[1:-1, 1:-1, 1:-1]
+    rl = F / (F + EPS) * (dz[:-1, None, None] * R[:-1] + dz[1:, None, None] * R[1:]) / (
+        dz[:-1] + dz[1:] + EPS)[:, None, None]
+    bu = [np.zeros((nz, ny, nx)) for _ in range(2)]
+    bu[0][1:] = -rl * grav
+    bu[1][:-1] = -rl * grav
+    return pg, bu
