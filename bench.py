@@ -18,8 +18,11 @@ cells x steps / s).
 Arms:
   (default)          ours: FP64 drop-in path (value), plus the FP32-refined path
                      (autotuned), the adjoint cost (128x128x64 hill, 40 steps),
-                     the 48-domain batched ensemble and the pressure projection
-                     (ProjectVelFace) of a closed block on the bench grid
+                     the 48-domain batched ensemble, the pressure projection
+                     (ProjectVelFace) of a closed block on the bench grid and
+                     the Rosenbrock step of the dynamical core (prognostic
+                     momentum, pressure gradient, buoyancy, projection) on
+                     the same closed block
   --impl reference   the reference's CPU path (the oracle restatement of the
                      Fortran; the Fortran itself has no compiler here), one
                      process per host core on independent blocks.
@@ -59,6 +62,9 @@ def parse():
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--no-projection", action="store_true")
+    p.add_argument("--no-dyn", action="store_true", help="skip the dynamical-core step")
+    p.add_argument("--dyn-only", action="store_true",
+                   help="only the dynamical-core section (profiling); prints its JSON object")
     p.add_argument("--projection-only", action="store_true",
                    help="only the projection section (profiling); prints its JSON object")
     p.add_argument("--batch-members", type=int, default=48)
@@ -444,6 +450,88 @@ def _projection_cpu_baseline(a):
                       f"lexicographic smoother, {csteps} FGMRES steps ({cpu_s:.1f} s)"}
 
 
+def _dyn_kinds(ncomp, mom):
+    """Closed box with free-slip walls: the momentum component normal to a wall
+    is ZeroValue there, everything else ZeroGrad."""
+    k = [[1] * 6 for _ in range(ncomp)]
+    for q, p in enumerate(mom):
+        for sd in range(6):
+            k[p][sd] = 2 if q // 2 == sd // 2 else 1
+    return k
+
+
+def dyn_bench(a, torch, stream):
+    """Rosenbrock step of the dynamical core (asam_ros_step_dyn: per stage the
+    face->cell velocities, thermodynamics, FcnMet with pressure gradient and
+    buoyancy, the transport BiCGStab, cell->face, ProjectVelFace; the
+    Jacobian and the Laplacian hierarchy at the first stage) on a closed-box
+    cut-cell hill of the bench grid with a warm bubble, moisture and a tracer;
+    device-resident state.  The CPU baseline is the oracle on a 64x64x32
+    block of the same generator, single-threaded."""
+    import ctypes as C
+
+    import numpy as np
+
+    import asam_gb300
+    import oracle
+    from asam_gb300 import geometry as G
+
+    nx, ny, nz = a.nx, a.ny, a.nz
+    geo, vel, st, pos, (dx, dy, dz), bc = G.dyn_case(nx, ny, nz, seed=11, moist=True, tracer=True)
+    nc = st.c.shape[0]
+    blk = asam_gb300.TransportBlock(geo, nc, rho_pos=0, method="RosRK3", bicgstab_tol=a.tol)
+    blk.set_stream(stream.cuda_stream)
+    blk.set_velocity(*vel)
+    blk.proj_setup(dx, dy, dz)
+    blk.dyn_setup(pos["th"], pos["mom"], rv_pos=pos["qv"], bound_cells=bc, scalars=[pos["qv"], pos["tracer"]])
+    lib = blk.lib
+    c = torch.from_numpy(st.c).cuda()
+    it = (C.c_int * 4)()
+    rs = (C.c_double * 4)()
+    ps = (C.c_int * 4)()
+    pr = (C.c_double * 4)()
+
+    def step():
+        rc = lib.asam_ros_step_dyn(blk.h, C.c_void_p(c.data_ptr()), a.dt, it, rs, ps, pr)
+        if rc not in (0, 1, 2):
+            raise RuntimeError(f"asam_ros_step_dyn: {rc}")
+
+    step()  # warm-up
+    n_rep = 2
+    l0 = lib.asam_launch_count()
+    ms = time_region(torch, stream, step, n_rep) / n_rep
+    launches = (lib.asam_launch_count() - l0) // n_rep
+    vol = torch.from_numpy(geo.volc).cuda()
+    mass = float((c[0] * vol)[1:-1, 1:-1, 1:-1].sum())
+    mass0 = float(np.sum((st.c[0] * geo.volc)[1:-1, 1:-1, 1:-1]))
+    blk.close()
+    cpu = None
+    if not a.no_cpu_baseline:
+        cgeo, cvel, cst, cpos, (cdx, cdy, cdz), cbc = G.dyn_case(64, 64, 32, seed=11, moist=True, tracer=True)
+        o = oracle.Oracle(cgeo, bc=_dyn_kinds(cst.c.shape[0], cpos["mom"]))
+        op = oracle.OracleProj(cgeo, cdx, cdy, cdz, G.projection_inputs(cgeo)[0], zebra=0)
+        cc = cst.c.copy()
+        cu = [q.copy() for q in cvel]
+        t0 = time.perf_counter()
+        o.ros_step_dyn(op, cc, cu, a.dt, rho_pos=0, th_pos=cpos["th"], pos=cpos["mom"], dx=cdx, dy=cdy, dz=cdz,
+                       rv_pos=cpos["qv"], bound=cbc, scalars=[cpos["qv"], cpos["tracer"]], bicg_tol=a.tol)
+        cpu_s = time.perf_counter() - t0
+        op.close()
+        cpu = {"value": 64 * 64 * 32 / cpu_s / 1e6, "unit": "Mcell-steps/s", "cores": 1, "kind": "port",
+               "sample": f"one step of a 64x64x32 block of the same generator, oracle restatement with the "
+                         f"reference's lexicographic smoother ({cpu_s:.2f} s)"}
+    return {
+        "workload": f"dynamical core, closed-box cut-cell hill {nx}x{ny}x{nz} (h=600 m, half-width 800 m, "
+                    f"roughness, dx=dy=200 m, dz 50->400 m), N=0.01 1/s, 2 K warm bubble, moisture and a tracer "
+                    f"({nc} components), {len(bc)} boundary cells, free-slip walls, RosRK3 dt={a.dt} s, "
+                    f"BiCGStab tol {a.tol}, FGMRES(10) QMRTol 1e-6",
+        "metric": "Mcell-steps/s", "value": nx * ny * nz / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+        "bicgstab_iterations": list(it[:3]), "fgmres_steps": list(ps[:3]),
+        "fgmres_rel_residual": list(pr[:3]), "gpu_launches_per_step": launches,
+        "mass_rel_change": (mass - mass0) / mass0, "cpu_baseline": cpu,
+    }
+
+
 def batch_members(n, seed=4):
     """Ensemble of independent cut-cell domains: sizes between 64x64x48 and
     192x160x96, Gaussian hill 0-1.5 km high with half-width 2-8 km, u 5-15 m/s,
@@ -561,6 +649,16 @@ def main():
         pk0 = ROOT / "MEASURED_PEAKS.json"
         hp = json.loads(pk0.read_text()).get("hbm_gbs", 6800.0) if pk0.exists() else 6800.0
         print(json.dumps(projection_bench(a, torch, stream, hp)), flush=True)
+        return
+    if a.dyn_only:
+        import torch
+
+        import __graft_entry__
+
+        __graft_entry__.build()
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        print(json.dumps(dyn_bench(a, torch, stream)), flush=True)
         return
     # CPU baseline first (before any GPU call), rank 0, N=1 only
     cpu = None
@@ -696,6 +794,9 @@ def main():
         pk0 = ROOT / "MEASURED_PEAKS.json"
         hp = json.loads(pk0.read_text()).get("hbm_gbs", 6800.0) if pk0.exists() else 6800.0
         proj = projection_bench(a, torch, stream, hp)
+    dyn = None
+    if not a.no_dyn and world == 1:
+        dyn = dyn_bench(a, torch, stream)
     if "fp64" not in results:  # a profiling run of one variant: no comparison line
         rr = results[precs[0]]
         if rank == 0:
@@ -800,6 +901,8 @@ def main():
         line["batch"] = bat
     if proj is not None:
         line["projection"] = proj
+    if dyn is not None:
+        line["dyn"] = dyn
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if rank == 0:
