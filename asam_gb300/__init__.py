@@ -288,6 +288,13 @@ class TransportBlock:
         check(self.lib.asam_proj_setup(self.h, C.byref(self.pcfg), ptr(self._pdx), ptr(self._pdy), ptr(self._pdz),
                                        None if self._pmetr is None else ptr(self._pmetr)), "asam_proj_setup")
 
+    def proj_set_precision(self, prec):
+        """Precision of the FGMRES preconditioner's V-cycle: "fp64" (the
+        reference's arithmetic), "fp32" (rounded copy of the hierarchy), or
+        None (follow the block's precision)."""
+        code = {None: -1, "fp64": 0, "fp32": 1}[prec]
+        check(self.lib.asam_proj_set_precision(self.h, code), "asam_proj_set_precision")
+
     def proj_weights(self, dtu, dtv, dtw, duu, duv, duw, dut, dtt):
         """Sound weights (WeightDiagCompute): face arrays with uF/vF/wF extents,
         DUT and DTT interior (nz, ny, nx)."""

@@ -52,18 +52,25 @@ constexpr int kRedBlock = 256;
 constexpr size_t kRingBytes = (size_t)4 * 8 * kPlaneBlock * sizeof(double);  // kRing * kFields * block
 constexpr double kTiny = 1.0e-40;  // initial diagonal of Allocate_1D (TriDiagT_Mod.f90:99)
 
-struct Lev2 {
+// One plane level of a 3D level (all its planes); T = double for the
+// reference arithmetic, float for the single-precision copy of the multigrid
+// that preconditions FGMRES in the refined mode.
+template <typename T>
+struct Lev2T {
   int c1, c2, h, w, m3;
   size_t ps;
-  double *d, *uz, *lz, *fw, *ft, *frt, *ux, *lx, *res;
-  double *x, *b;  // own vectors of the coarse plane levels (nullptr on the 3D level's own planes)
+  T *d, *uz, *lz, *fw, *ft, *frt, *ux, *lx, *res;
+  T *x, *b;  // own vectors of the coarse plane levels (nullptr on the 3D level's own planes)
 };
+using Lev2 = Lev2T<double>;
 
-struct Lev3 {
+template <typename T>
+struct Lev3T {
   int m1, m2, m3, nl;
-  Lev2 pl[kMaxLev];
-  double *u3, *l3, *x, *b, *res, *t;
+  Lev2T<T> pl[kMaxLev];
+  T *u3, *l3, *x, *b, *res, *t;
 };
+using Lev3 = Lev3T<double>;
 
 // Input fields of one level in the reversed index space with 1-based logical
 // indices F1(0:n1,1:n2,1:n3), F2(1:n1,0:n2,1:n3), F3(1:n1,1:n2,0:n3) and cell
@@ -402,12 +409,13 @@ __global__ void k_factor(Lev2 P) {
 
 // MatVecT_2D at entry (i,j) of a plane (TriDiagT_Mod.f90:113-133, 405-431);
 // x is the plane's vector, mo the plane's offset in the matrix arrays
-__device__ inline double matvec2_at(const Lev2& P, size_t mo, const double* __restrict__ x, size_t s, int i, int j) {
+template <typename T>
+__device__ inline T matvec2_at(const Lev2T<T>& P, size_t mo, const T* __restrict__ x, size_t s, int i, int j) {
   const int c1 = P.c1, c2 = P.c2, w = P.w;
-  const double* d = P.d + mo;
-  const double* uz = P.uz + mo;
-  const double* lz = P.lz + mo;
-  double y;
+  const T* d = P.d + mo;
+  const T* uz = P.uz + mo;
+  const T* lz = P.lz + mo;
+  T y;
   if (c1 > 1) {
     if (i == 0)
       y = d[s] * x[s] + uz[s] * x[s + w];
@@ -420,8 +428,8 @@ __device__ inline double matvec2_at(const Lev2& P, size_t mo, const double* __re
   }
   if (c2 > 1) {
     const size_t row = (size_t)i * w;
-    const double* ux = P.ux + mo;
-    const double* lx = P.lx + mo;
+    const T* ux = P.ux + mo;
+    const T* lx = P.lx + mo;
     if (j == 0) {
       const size_t sr = row + slot(0, P.h, 0, j + 1);
       y = y + ux[s] * x[sr];
@@ -453,15 +461,16 @@ __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_grou
 template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-__device__ __noinline__ void line_half(const Lev2& P, size_t mo, const double* __restrict__ b, double* __restrict__ x, int c,
-                                       int fwd, double* __restrict__ ring) {
+template <typename T>
+__device__ __noinline__ void line_half(const Lev2T<T>& P, size_t mo, const T* __restrict__ b, T* __restrict__ x, int c,
+                                       int fwd, T* __restrict__ ring) {
   const int c1 = P.c1, c2 = P.c2, h = P.h, w = P.w;
-  const double* __restrict__ lx = P.lx + mo;
-  const double* __restrict__ ux = P.ux + mo;
-  const double* __restrict__ lz = P.lz + mo;
-  const double* __restrict__ ft = P.ft + mo;
-  const double* __restrict__ frt = P.frt + mo;
-  const double* __restrict__ fw = P.fw + mo;
+  const T* __restrict__ lx = P.lx + mo;
+  const T* __restrict__ ux = P.ux + mo;
+  const T* __restrict__ lz = P.lz + mo;
+  const T* __restrict__ ft = P.ft + mo;
+  const T* __restrict__ frt = P.frt + mo;
+  const T* __restrict__ fw = P.fw + mo;
   const int nl = (c2 - c + 1) / 2;
   const int bd = blockDim.x, tid = threadIdx.x;
   for (int q = tid; q < nl; q += bd) {
@@ -471,7 +480,7 @@ __device__ __noinline__ void line_half(const Lev2& P, size_t mo, const double* _
     const size_t colL = hasL ? (size_t)(1 - c) * h + ((j - 1) >> 1) : col;
     const size_t colR = hasR ? (size_t)(1 - c) * h + ((j + 1) >> 1) : col;
     auto issue = [&](int i) {
-      double* sl = ring + (size_t)(i % kRing) * kFields * bd + tid;
+      T* sl = ring + (size_t)(i % kRing) * kFields * bd + tid;
       const bool ok = i < c1;
       const size_t o = (size_t)(ok ? i : 0) * w;
       const size_t om = i > 0 && ok ? o - w : o;
@@ -486,12 +495,12 @@ __device__ __noinline__ void line_half(const Lev2& P, size_t mo, const double* _
       cp_commit();
     };
     for (int r = 0; r < kAhead; ++r) issue(r);
-    double prev = 0.0;
+    T prev = (T)0;
     for (int i = 0; i < c1; ++i) {
       issue(i + kAhead);
       cp_wait<kAhead>();
-      const double* sl = ring + (size_t)(i % kRing) * kFields * bd + tid;
-      double t = sl[0];
+      const T* sl = ring + (size_t)(i % kRing) * kFields * bd + tid;
+      T t = sl[0];
       if (fwd) {
         if (hasL) t = t - sl[3 * bd] * sl[1 * bd];
         if (hasR) t = t - sl[4 * bd] * sl[2 * bd];
@@ -500,15 +509,15 @@ __device__ __noinline__ void line_half(const Lev2& P, size_t mo, const double* _
         if (hasL) t = t - sl[3 * bd] * sl[1 * bd];
       }
       if (i > 0) t = t - sl[5 * bd] * prev;
-      const double y = div_rn(t, sl[6 * bd], sl[7 * bd]);
+      const T y = div_rn(t, sl[6 * bd], sl[7 * bd]);
       x[col + (size_t)i * w] = y;
       prev = y;
     }
     cp_wait<0>();
     // back substitution b(i) = b(i) - w(i)*b(i+1), rows c1-2 .. 0
     const int nb = c1 - 1;
-    double xa[4], wa[4], xb[4], wb[4];
-    auto load4 = [&](double* xs, double* ws, int r0) {
+    T xa[4], wa[4], xb[4], wb[4];
+    auto load4 = [&](T* xs, T* ws, int r0) {
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const int i = c1 - 2 - (r0 + r);
@@ -518,12 +527,12 @@ __device__ __noinline__ void line_half(const Lev2& P, size_t mo, const double* _
         }
       }
     };
-    auto solve4 = [&](const double* xs, const double* ws, int r0) {
+    auto solve4 = [&](const T* xs, const T* ws, int r0) {
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const int i = c1 - 2 - (r0 + r);
         if (i >= 0) {
-          const double v = xs[r] - ws[r] * prev;
+          const T v = xs[r] - ws[r] * prev;
           x[col + (size_t)i * w] = v;
           prev = v;
         }
@@ -539,7 +548,8 @@ __device__ __noinline__ void line_half(const Lev2& P, size_t mo, const double* _
   }
 }
 
-__device__ void gs2d(const Lev2& P, size_t mo, const double* b, double* x, int gi, double* ring) {
+template <typename T>
+__device__ void gs2d(const Lev2T<T>& P, size_t mo, const T* b, T* x, int gi, T* ring) {
   if (P.c2 > 1) {
     for (int it = 0; it < gi; ++it) {
       line_half(P, mo, b, x, 0, 1, ring);
@@ -558,19 +568,20 @@ __device__ void gs2d(const Lev2& P, size_t mo, const double* b, double* x, int g
 }
 
 // Multigrid_2D (TriDiagT_Mod.f90:490-551) on plane k of a 3D level, inside one CTA
-__device__ void mg2d(const Lev3& A, int k, double* x0, const double* b0, int gi2, double* ring) {
+template <typename T>
+__device__ void mg2d(const Lev3T<T>& A, int k, T* x0, const T* b0, int gi2, T* ring) {
   const int nl = A.nl;
   int gi = 1;
   int lv = 0;
   for (;;) {
-    const Lev2& P = A.pl[lv];
-    double* x = lv == 0 ? x0 : P.x + (size_t)k * P.ps;
-    const double* b = lv == 0 ? b0 : P.b + (size_t)k * P.ps;
+    const Lev2T<T>& P = A.pl[lv];
+    T* x = lv == 0 ? x0 : P.x + (size_t)k * P.ps;
+    const T* b = lv == 0 ? b0 : P.b + (size_t)k * P.ps;
     const size_t mo = (size_t)k * P.ps;
     gs2d(P, mo, b, x, gi, ring);
     gi += gi2;
     if (lv + 1 < nl) {
-      double* res = P.res + (size_t)k * P.ps;
+      T* res = P.res + (size_t)k * P.ps;
       const size_t np = P.ps;
       for (size_t s = threadIdx.x; s < np; s += blockDim.x) {
         const int i = (int)(s / P.w), j = line_of((int)(s % P.w), P.h, P.c2);
@@ -578,17 +589,17 @@ __device__ void mg2d(const Lev3& A, int k, double* x0, const double* b0, int gi2
         res[s] = b[s] - matvec2_at(P, mo, x, s, i, j);
       }
       __syncthreads();
-      const Lev2& Q = A.pl[lv + 1];
-      double* bq = Q.b + (size_t)k * Q.ps;
-      double* xq = Q.x + (size_t)k * Q.ps;
+      const Lev2T<T>& Q = A.pl[lv + 1];
+      T* bq = Q.b + (size_t)k * Q.ps;
+      T* xq = Q.x + (size_t)k * Q.ps;
       for (size_t s = threadIdx.x; s < Q.ps; s += blockDim.x) {
         const int a = (int)(s / Q.w), bb = line_of((int)(s % Q.w), Q.h, Q.c2);
         if (bb < 0) continue;
-        double v = 0.0;
+        T v = (T)0;
         for (int i1 = 2 * a; i1 <= 2 * a + 1 && i1 < P.c1; ++i1)
           for (int i2 = 2 * bb; i2 <= 2 * bb + 1 && i2 < P.c2; ++i2) v = v + res[slot(P.w, P.h, i1, i2)];
         bq[s] = v;
-        xq[s] = 0.0;
+        xq[s] = (T)0;
       }
       __syncthreads();
       ++lv;
@@ -598,14 +609,14 @@ __device__ void mg2d(const Lev3& A, int k, double* x0, const double* b0, int gi2
     }
   }
   for (;;) {
-    const Lev2& P = A.pl[lv];
-    double* x = lv == 0 ? x0 : P.x + (size_t)k * P.ps;
-    const double* b = lv == 0 ? b0 : P.b + (size_t)k * P.ps;
+    const Lev2T<T>& P = A.pl[lv];
+    T* x = lv == 0 ? x0 : P.x + (size_t)k * P.ps;
+    const T* b = lv == 0 ? b0 : P.b + (size_t)k * P.ps;
     gs2d(P, (size_t)k * P.ps, b, x, gi, ring);
     gi -= gi2;
     if (lv > 0) {
-      const Lev2& F = A.pl[lv - 1];
-      double* xf = lv - 1 == 0 ? x0 : F.x + (size_t)k * F.ps;
+      const Lev2T<T>& F = A.pl[lv - 1];
+      T* xf = lv - 1 == 0 ? x0 : F.x + (size_t)k * F.ps;
       for (size_t s = threadIdx.x; s < F.ps; s += blockDim.x) {
         const int i = (int)(s / F.w), j = line_of((int)(s % F.w), F.h, F.c2);
         if (j < 0) continue;
@@ -622,13 +633,15 @@ __device__ void mg2d(const Lev3& A, int k, double* x0, const double* b0, int gi2
 // One zebra half-sweep of GaussSeidel_3D over the planes of parity `color` of
 // 3D level L: each CTA forms its plane's right-hand side (forward or backward
 // operation order of the reference) and runs Solve_2D on it.
-__global__ void __launch_bounds__(kPlaneBlock, 2) k_plane_half(const Lev3* __restrict__ lvs, int L, int color, int fwd,
+template <typename T>
+__global__ void __launch_bounds__(kPlaneBlock, 2) k_plane_half(const Lev3T<T>* __restrict__ lvs, int L, int color, int fwd,
                                                              int mult_iter2, int gi2) {
-  __shared__ Lev3 A;
-  extern __shared__ double ring[];  // kRing * kFields * blockDim doubles
+  __shared__ Lev3T<T> A;
+  extern __shared__ __align__(16) unsigned char ring_raw[];  // kRing * kFields * blockDim values of T
+  T* ring = reinterpret_cast<T*>(ring_raw);
   if (threadIdx.x == 0) A = lvs[L];
   __syncthreads();
-  const Lev2& P0 = A.pl[0];
+  const Lev2T<T>& P0 = A.pl[0];
   for (int q = blockIdx.x;; q += gridDim.x) {
     const int k = 2 * q + color;
     if (k >= A.m3) break;
@@ -636,7 +649,7 @@ __global__ void __launch_bounds__(kPlaneBlock, 2) k_plane_half(const Lev3* __res
     for (size_t s = threadIdx.x; s < ps; s += blockDim.x) {
       if (line_of((int)(s % P0.w), P0.h, P0.c2) < 0) continue;
       const size_t e = off + s;
-      double v = A.b[e];
+      T v = A.b[e];
       if (fwd) {
         if (k > 0) v = v - A.l3[e - ps] * A.x[e - ps];
         if (k < A.m3 - 1) v = v - A.u3[e] * A.x[e + ps];
@@ -654,17 +667,18 @@ __global__ void __launch_bounds__(kPlaneBlock, 2) k_plane_half(const Lev3* __res
 
 // MatVecT_3D at every entry of level L: mode 0 res = b - A x; mode 1 y = -(A x)
 // (MatVecFull's sign); mode 2 y = A x.
-__global__ void k_matvec3(const Lev3* __restrict__ lvs, int L, const double* __restrict__ x, const double* __restrict__ b,
-                          double* __restrict__ y, int mode) {
-  const Lev3& A = lvs[L];
-  const Lev2& P = A.pl[0];
+template <typename T>
+__global__ void k_matvec3(const Lev3T<T>* __restrict__ lvs, int L, const T* __restrict__ x, const T* __restrict__ b,
+                          T* __restrict__ y, int mode) {
+  const Lev3T<T>& A = lvs[L];
+  const Lev2T<T>& P = A.pl[0];
   const size_t tot = (size_t)A.m3 * P.ps, ps = P.ps;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
     const size_t s = e % ps;
     const int k = (int)(e / ps);
     const int i = (int)(s / P.w), j = line_of((int)(s % P.w), P.h, P.c2);
     if (j < 0) continue;
-    double v = matvec2_at(P, (size_t)k * ps, x + (size_t)k * ps, s, i, j);
+    T v = matvec2_at(P, (size_t)k * ps, x + (size_t)k * ps, s, i, j);
     if (A.m3 > 1) {
       if (k == 0)
         v = v + A.u3[e] * x[e + ps];
@@ -678,32 +692,34 @@ __global__ void k_matvec3(const Lev3* __restrict__ lvs, int L, const double* __r
 }
 
 // RestrictT_3D (level L residual -> level L+1 right-hand side), zero x of L+1
-__global__ void k_restrict3(const Lev3* __restrict__ lvs, int L) {
-  const Lev3& A = lvs[L];
-  const Lev3& C = lvs[L + 1];
-  const Lev2& P = A.pl[0];
-  const Lev2& Q = C.pl[0];
+template <typename T>
+__global__ void k_restrict3(const Lev3T<T>* __restrict__ lvs, int L) {
+  const Lev3T<T>& A = lvs[L];
+  const Lev3T<T>& C = lvs[L + 1];
+  const Lev2T<T>& P = A.pl[0];
+  const Lev2T<T>& Q = C.pl[0];
   const size_t tot = (size_t)C.m3 * Q.ps;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
     const size_t s = e % Q.ps;
     const int kc = (int)(e / Q.ps);
     const int a = (int)(s / Q.w), bb = line_of((int)(s % Q.w), Q.h, Q.c2);
     if (bb < 0) continue;
-    double v = 0.0;
+    T v = (T)0;
     for (int i1 = 2 * a; i1 <= 2 * a + 1 && i1 < P.c1; ++i1)
       for (int i2 = 2 * bb; i2 <= 2 * bb + 1 && i2 < P.c2; ++i2)
         for (int i3 = 2 * kc; i3 <= 2 * kc + 1 && i3 < A.m3; ++i3) v = v + A.res[(size_t)i3 * P.ps + slot(P.w, P.h, i1, i2)];
     C.b[e] = v;
-    C.x[e] = 0.0;
+    C.x[e] = (T)0;
   }
 }
 
 // ProlongateT_3D + x = x + Res (level L+1 -> level L)
-__global__ void k_prolong3(const Lev3* __restrict__ lvs, int L) {
-  const Lev3& A = lvs[L];
-  const Lev3& C = lvs[L + 1];
-  const Lev2& P = A.pl[0];
-  const Lev2& Q = C.pl[0];
+template <typename T>
+__global__ void k_prolong3(const Lev3T<T>* __restrict__ lvs, int L) {
+  const Lev3T<T>& A = lvs[L];
+  const Lev3T<T>& C = lvs[L + 1];
+  const Lev2T<T>& P = A.pl[0];
+  const Lev2T<T>& Q = C.pl[0];
   const size_t tot = (size_t)A.m3 * P.ps;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
     const size_t s = e % P.ps;
@@ -1036,6 +1052,13 @@ struct ProjState {
   int* d_scal = nullptr;
   int nscal_cap = 0;
   long long vcycles = 0;
+  // single-precision copy of the multigrid hierarchy: FGMRES is flexible (it
+  // keeps the preconditioned vectors), so a V-cycle in FP32 preconditions the
+  // FP64 iteration without touching its residual test
+  std::vector<prj::Lev3T<float>> lv32;
+  prj::Lev3T<float>* d_lv32 = nullptr;
+  int mg_prec = -1;  // -1: follow the context's precision, 0: FP64, 1: FP32
+  bool lv32_ready = false;
 };
 
 namespace prj {
@@ -1144,7 +1167,8 @@ int proj_build(asam_ctx* h) {
     for (double** q : arr)
       if (int rc = palloc(s, q, n)) return rc;
   }
-  CK(cudaFuncSetAttribute(k_plane_half, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
+  CK(cudaFuncSetAttribute(k_plane_half<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
+  CK(cudaFuncSetAttribute(k_plane_half<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
   if (int rc = palloc(s, &s->d_lv, (size_t)R)) return rc;
   CK(cudaMemcpyAsync(s->d_lv, s->lv.data(), sizeof(Lev3) * R, cudaMemcpyHostToDevice, s->st));
   CK(cudaStreamSynchronize(s->st));
@@ -1173,20 +1197,22 @@ int proj_build(asam_ctx* h) {
 
 // Solve_3D from a zero start on level 0 (VCycleCG's MatrixT branch): lv[0].b
 // holds the right-hand side, the result is left in lv[0].x
-void vcycle_dev(asam_ctx* h) {
+template <typename T>
+void vcycle_run(asam_ctx* h, std::vector<Lev3T<T>>& lv, Lev3T<T>* d_lv) {
   ProjState* s = h->proj;
   const cudaStream_t st = h->L.stream;
   const int R = s->R;
   const int gi2 = s->cfg.gauss_iter2, gi3 = s->cfg.gauss_iter3;
   const int mi2 = s->cfg.mult_iter2;
+  const size_t ring = kRingBytes / sizeof(double) * sizeof(T);
   long long nl = 0;
-  cudaMemsetAsync(s->lv[0].x, 0, sizeof(double) * len0(s), st);
+  cudaMemsetAsync(lv[0].x, 0, sizeof(T) * len0(s), st);
   auto gs3 = [&](int L, int gi) {
-    const Lev3& A = s->lv[L];
+    const Lev3T<T>& A = lv[L];
     auto half = [&](int c, int fwd) {
       const int np = (A.m3 - c + 1) / 2;
       if (np <= 0) return;
-      k_plane_half<<<np, kPlaneBlock, kRingBytes, st>>>(s->d_lv, L, c, fwd, mi2, gi2);
+      k_plane_half<T><<<np, kPlaneBlock, ring, st>>>(d_lv, L, c, fwd, mi2, gi2);
       ++nl;
     };
     if (A.m3 > 1) {
@@ -1206,11 +1232,11 @@ void vcycle_dev(asam_ctx* h) {
       gs3(L, gi);
       gi += gi3;
       if (L + 1 < R) {
-        const Lev3& A = s->lv[L];
+        const Lev3T<T>& A = lv[L];
         const size_t n = A.pl[0].ps * A.m3;
-        k_matvec3<<<grid_of(n), 256, 0, st>>>(s->d_lv, L, A.x, A.b, A.res, 0);
-        const size_t nc = s->lv[L + 1].pl[0].ps * s->lv[L + 1].m3;
-        k_restrict3<<<grid_of(nc), 256, 0, st>>>(s->d_lv, L);
+        k_matvec3<T><<<grid_of(n), 256, 0, st>>>(d_lv, L, A.x, A.b, A.res, 0);
+        const size_t nc = lv[L + 1].pl[0].ps * lv[L + 1].m3;
+        k_restrict3<T><<<grid_of(nc), 256, 0, st>>>(d_lv, L);
         nl += 2;
         ++L;
       } else {
@@ -1223,8 +1249,8 @@ void vcycle_dev(asam_ctx* h) {
       gi -= gi3;
       if (L > 0) {
         --L;
-        const size_t n = s->lv[L].pl[0].ps * s->lv[L].m3;
-        k_prolong3<<<grid_of(n), 256, 0, st>>>(s->d_lv, L);
+        const size_t n = lv[L].pl[0].ps * lv[L].m3;
+        k_prolong3<T><<<grid_of(n), 256, 0, st>>>(d_lv, L);
         ++nl;
       } else {
         break;
@@ -1233,6 +1259,126 @@ void vcycle_dev(asam_ctx* h) {
   }
   count_launches(nl);
   ++s->vcycles;
+}
+
+bool use_mg32(const asam_ctx* h) {
+  const ProjState* s = h->proj;
+  return s->mg_prec == 1 || (s->mg_prec < 0 && h->cfg.precision == ASAM_PREC_FP32_REFINED);
+}
+
+__global__ void k_cvt_to_f32(const double* __restrict__ a, float* __restrict__ b, size_t n, double sign) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    b[e] = (float)(sign * a[e]);
+}
+// Thomas pivots and their reciprocals in FP32.  A cell without volume has
+// the pivot 1e-40 (Allocate_1D's initial diagonal), below FP32's normal range
+// and with a reciprocal beyond it; its couplings and right-hand side are 0,
+// so the FP32 copy solves that row with the pivot 1 instead, which leaves it 0.
+__global__ void k_cvt_pivot(const double* __restrict__ ft, const double* __restrict__ frt, float* __restrict__ ft32,
+                            float* __restrict__ frt32, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const double p = ft[e];
+    const bool ok = fabs(p) >= 1.0e-30 && fabs(frt[e]) <= 1.0e30;
+    ft32[e] = ok ? (float)p : 1.0f;
+    frt32[e] = ok ? (float)frt[e] : 1.0f;
+  }
+}
+__global__ void k_cvt_to_f64(const float* __restrict__ a, double* __restrict__ b, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    b[e] = (double)a[e];
+}
+
+// the FP32 hierarchy with the shapes of the FP64 one (allocated once)
+int alloc_lev32(ProjState* s) {
+  if (s->d_lv32) return kOk;
+  const int R = s->R;
+  s->lv32.assign(R, Lev3T<float>{});
+  for (int L = 0; L < R; ++L) {
+    const Lev3& A = s->lv[L];
+    Lev3T<float>& B = s->lv32[L];
+    B.m1 = A.m1;
+    B.m2 = A.m2;
+    B.m3 = A.m3;
+    B.nl = A.nl;
+    for (int q = 0; q < A.nl; ++q) {
+      const Lev2& P = A.pl[q];
+      Lev2T<float>& Q = B.pl[q];
+      Q.c1 = P.c1;
+      Q.c2 = P.c2;
+      Q.h = P.h;
+      Q.w = P.w;
+      Q.m3 = P.m3;
+      Q.ps = P.ps;
+      const size_t n = P.ps * P.m3;
+      float** arr[] = {&Q.d, &Q.uz, &Q.lz, &Q.fw, &Q.ft, &Q.frt, &Q.ux, &Q.lx, &Q.res};
+      for (float** r : arr)
+        if (int rc = palloc(s, r, n)) return rc;
+      Q.x = Q.b = nullptr;
+      if (P.x) {
+        if (int rc = palloc(s, &Q.x, n)) return rc;
+        if (int rc = palloc(s, &Q.b, n)) return rc;
+      }
+    }
+    const size_t n = A.pl[0].ps * A.m3;
+    float** arr[] = {&B.u3, &B.l3, &B.x, &B.b, &B.res, &B.t};
+    for (float** r : arr)
+      if (int rc = palloc(s, r, n)) return rc;
+  }
+  if (int rc = palloc(s, &s->d_lv32, (size_t)R)) return rc;
+  CK(cudaMemcpyAsync(s->d_lv32, s->lv32.data(), sizeof(Lev3T<float>) * R, cudaMemcpyHostToDevice, s->st));
+  return kOk;
+}
+
+// round the assembled FP64 hierarchy (matrix and Thomas factors) to FP32
+int convert_lev32(asam_ctx* h) {
+  ProjState* s = h->proj;
+  if (int rc = alloc_lev32(s)) return rc;
+  const cudaStream_t st = h->L.stream;
+  long long nl = 0;
+  for (int L = 0; L < s->R; ++L) {
+    const Lev3& A = s->lv[L];
+    const Lev3T<float>& B = s->lv32[L];
+    for (int q = 0; q < A.nl; ++q) {
+      const Lev2& P = A.pl[q];
+      const Lev2T<float>& Q = B.pl[q];
+      const size_t n = P.ps * P.m3;
+      const double* src[] = {P.d, P.uz, P.lz, P.fw, P.ux, P.lx};
+      float* dst[] = {Q.d, Q.uz, Q.lz, Q.fw, Q.ux, Q.lx};
+      for (int a = 0; a < 6; ++a, ++nl) k_cvt_to_f32<<<grid_of(n), 256, 0, st>>>(src[a], dst[a], n, 1.0);
+      k_cvt_pivot<<<grid_of(n), 256, 0, st>>>(P.ft, P.frt, Q.ft, Q.frt, n);
+      ++nl;
+    }
+    const size_t n = A.pl[0].ps * A.m3;
+    k_cvt_to_f32<<<grid_of(n), 256, 0, st>>>(A.u3, B.u3, n, 1.0);
+    k_cvt_to_f32<<<grid_of(n), 256, 0, st>>>(A.l3, B.l3, n, 1.0);
+    nl += 2;
+  }
+  count_launches(nl);
+  s->lv32_ready = true;
+  return kOk;
+}
+
+// Solve_3D in the selected precision: b (level-0 layout, FP64) scaled by
+// sign -> x (FP64)
+void vcycle_any(asam_ctx* h, const double* b, double sign, double* x) {
+  ProjState* s = h->proj;
+  const size_t n = len0(s);
+  const cudaStream_t st = h->L.stream;
+  if (use_mg32(h) && s->lv32_ready) {
+    k_cvt_to_f32<<<grid_of(n), 256, 0, st>>>(b, s->lv32[0].b, n, sign);
+    vcycle_run<float>(h, s->lv32, s->d_lv32);
+    k_cvt_to_f64<<<grid_of(n), 256, 0, st>>>(s->lv32[0].x, x, n);
+    count_launches(2);
+    return;
+  }
+  if (sign == 1.0) {
+    if (b != s->lv[0].b) cudaMemcpyAsync(s->lv[0].b, b, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+  } else {
+    k_neg<<<grid_of(n), 256, 0, st>>>(s->lv[0].b, b, n);
+    count_launches(1);
+  }
+  vcycle_run<double>(h, s->lv, s->d_lv);
+  if (x != s->lv[0].x) cudaMemcpyAsync(x, s->lv[0].x, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
 }
 
 int dot_dev(asam_ctx* h, const double* a, const double* b, double* out, int mode) {
@@ -1248,19 +1394,12 @@ int dot_dev(asam_ctx* h, const double* a, const double* b, double* out, int mode
 void matvec1_dev(asam_ctx* h, const double* x, double* y) {
   ProjState* s = h->proj;
   const size_t n = len0(s);
-  k_matvec3<<<grid_of(n), 256, 0, h->L.stream>>>(s->d_lv, 0, x, nullptr, y, 1);
+  k_matvec3<double><<<grid_of(n), 256, 0, h->L.stream>>>(s->d_lv, 0, x, nullptr, y, 1);
   count_launches(1);
 }
 
 // z = PSolve1(v) = PressurePre(-v) (no boundary face unknowns)
-void psolve1_dev(asam_ctx* h, const double* v, double* z) {
-  ProjState* s = h->proj;
-  const size_t n = len0(s);
-  k_neg<<<grid_of(n), 256, 0, h->L.stream>>>(s->lv[0].b, v, n);
-  count_launches(1);
-  vcycle_dev(h);
-  cudaMemcpyAsync(z, s->lv[0].x, n * sizeof(double), cudaMemcpyDeviceToDevice, h->L.stream);
-}
+void psolve1_dev(asam_ctx* h, const double* v, double* z) { vcycle_any(h, v, -1.0, z); }
 
 // FGMRES (SOLU/Iter_Mod.f90:121-199) on level-0 vectors x (in/out), b
 int fgmres_dev(asam_ctx* h, double* x, const double* b, int maxiter, double tol, int* steps_out, double* rho_out,
@@ -1482,6 +1621,7 @@ int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
   ProjState* s = h->proj;
   const Dims& d = h->d;
   const cudaStream_t st = h->L.stream;
+  s->st = st;
   s->beta0 = beta0;
   s->dtp = dtp;
   const double bd = beta0 * dtp, bd2 = bd * bd;
@@ -1514,10 +1654,27 @@ int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
     }
   }
   count_launches(nl);
+  s->lv32_ready = false;
+  if (use_mg32(h)) {
+    if (int rc = convert_lev32(h)) return rc;
+  }
   CK(cudaStreamSynchronize(st));
   int rc = check_launch();
   if (!rc) s->assembled = true;
   return rc;
+}
+
+int asam_proj_set_precision(asam_ctx* h, int prec) {
+  if (!h || !h->proj || prec < -1 || prec > 1) return kBadArg;
+  ProjState* s = h->proj;
+  s->mg_prec = prec;
+  if (s->assembled && use_mg32(h) && !s->lv32_ready) {
+    s->st = h->L.stream;
+    if (int rc = convert_lev32(h)) return rc;
+    CK(cudaStreamSynchronize(h->L.stream));
+    return check_launch();
+  }
+  return kOk;
 }
 
 long asam_lapl_get(asam_ctx* h, int level3, int level2, int which, double* out) {
@@ -1552,7 +1709,7 @@ int asam_lapl_matvec(asam_ctx* h, const double* x, double* y) {
   int rc;
   if ((rc = copy_in(h, s->xn, x, nc))) return rc;
   k_to_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->xn, s->tmp, 1.0);
-  k_matvec3<<<grid_of(n), 256, 0, st>>>(s->d_lv, 0, s->tmp, nullptr, s->v[0], 2);
+  k_matvec3<double><<<grid_of(n), 256, 0, st>>>(s->d_lv, 0, s->tmp, nullptr, s->v[0], 2);
   k_from_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->v[0], s->bn);
   count_launches(3);
   CK(cudaMemcpyAsync(y, s->bn, nc * sizeof(double), cudaMemcpyDefault, st));
@@ -1572,7 +1729,7 @@ int asam_lapl_vcycle(asam_ctx* h, const double* b, double* x) {
   if ((rc = copy_in(h, s->bn, b, nc))) return rc;
   k_to_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->bn, s->lv[0].b, 1.0);
   count_launches(1);
-  vcycle_dev(h);
+  vcycle_any(h, s->lv[0].b, 1.0, s->lv[0].x);
   k_from_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->lv[0].x, s->xn);
   count_launches(1);
   CK(cudaMemcpyAsync(x, s->xn, nc * sizeof(double), cudaMemcpyDefault, st));

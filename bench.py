@@ -408,19 +408,34 @@ def projection_bench(a, torch, stream, hbm_peak):
     red = float(torch.linalg.norm(bb - yy) / torch.linalg.norm(bb))
     vb = vcycle_bytes(nz, nx, ny, 4)
     gbs = vb / (vc_ms * 1e-3) / 1e9
+    steps64, res64 = steps.value, res.value
+    # the same with the FP32 copy of the multigrid preconditioning FGMRES
+    blk.proj_set_precision("fp32")
+    for _ in range(2):
+        project()
+    proj32_ms = time_region(torch, stream, project, n_rep) / n_rep
+    steps32, res32 = steps.value, res.value
+    vc32_ms = time_region(torch, stream, lambda: lib.asam_lapl_vcycle(blk.h, P(bb), P(xx)), 3) / 3
+    gbs32 = vb / 2 / (vc32_ms * 1e-3) / 1e9
     blk.close()
     return {
         "workload": f"closed-box cut-cell hill {nx}x{ny}x{nz} (h=600 m, half-width 800 m, roughness 50 m / 600 m, "
                     f"dx=dy=200 m, dz 50->400 m), RefLevel 4, FGMRES(10) QMRTol 1e-6, dtP={a.dt} s, "
                     "seeded sound weights and velocity increments",
         "metric": "Mcell-projections/s", "value": ncell / (proj_ms * 1e-3) / 1e6, "ms_per_projection": proj_ms,
-        "fgmres_steps": steps.value, "fgmres_rel_residual": res.value, "vcycles_per_projection": vcyc,
+        "fgmres_steps": steps64, "fgmres_rel_residual": res64, "vcycles_per_projection": vcyc,
         "assemble_ms": assemble_ms, "vcycle_ms": vc_ms, "vcycle_residual_reduction": red,
         "gpu_launches_per_projection": launches,
         "roofline": {"kernel": "one V-cycle (k_plane_half zebra plane/line relaxations + 3D residual, restriction, "
                                "prolongation)", "bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": gbs / hbm_peak, "algorithmic_bytes_per_call": vb, "traffic": None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+        "fp32_multigrid": {"ms_per_projection": proj32_ms, "value": ncell / (proj32_ms * 1e-3) / 1e6,
+                           "speedup_vs_fp64_multigrid": proj_ms / proj32_ms, "fgmres_steps": steps32,
+                           "fgmres_rel_residual": res32, "vcycle_ms": vc32_ms,
+                           "roofline": {"bound": "hbm", "achieved": gbs32, "peak": hbm_peak, "unit": "GB/s",
+                                        "frac": gbs32 / hbm_peak, "algorithmic_bytes_per_call": vb // 2,
+                                        "traffic": None}},
         "cpu_baseline": cpu_base,
     }
 
@@ -466,8 +481,10 @@ def dyn_bench(a, torch, stream):
     buoyancy, the transport BiCGStab, cell->face, ProjectVelFace; the
     Jacobian and the Laplacian hierarchy at the first stage) on a closed-box
     cut-cell hill of the bench grid with a warm bubble, moisture and a tracer;
-    device-resident state.  The CPU baseline is the oracle on a 64x64x32
-    block of the same generator, single-threaded."""
+    device-resident state.  Run with the FP64 transport solve and with the
+    FP32-refined one (x-line inner preconditioner); the two end states are
+    compared.  The CPU baseline is the oracle on a 64x64x32 block of the same
+    generator, single-threaded."""
     import ctypes as C
 
     import numpy as np
@@ -479,32 +496,40 @@ def dyn_bench(a, torch, stream):
     nx, ny, nz = a.nx, a.ny, a.nz
     geo, vel, st, pos, (dx, dy, dz), bc = G.dyn_case(nx, ny, nz, seed=11, moist=True, tracer=True)
     nc = st.c.shape[0]
-    blk = asam_gb300.TransportBlock(geo, nc, rho_pos=0, method="RosRK3", bicgstab_tol=a.tol)
-    blk.set_stream(stream.cuda_stream)
-    blk.set_velocity(*vel)
-    blk.proj_setup(dx, dy, dz)
-    blk.dyn_setup(pos["th"], pos["mom"], rv_pos=pos["qv"], bound_cells=bc, scalars=[pos["qv"], pos["tracer"]])
-    lib = blk.lib
-    c = torch.from_numpy(st.c).cuda()
-    it = (C.c_int * 4)()
-    rs = (C.c_double * 4)()
-    ps = (C.c_int * 4)()
-    pr = (C.c_double * 4)()
 
-    def step():
-        rc = lib.asam_ros_step_dyn(blk.h, C.c_void_p(c.data_ptr()), a.dt, it, rs, ps, pr)
-        if rc not in (0, 1, 2):
-            raise RuntimeError(f"asam_ros_step_dyn: {rc}")
+    def run(prec):
+        kw = {"inner_precond": "xline"} if prec == "fp32_refined" else {}
+        blk = asam_gb300.TransportBlock(geo, nc, rho_pos=0, method="RosRK3", bicgstab_tol=a.tol, precision=prec, **kw)
+        blk.set_stream(stream.cuda_stream)
+        blk.set_velocity(*vel)
+        blk.proj_setup(dx, dy, dz)
+        blk.dyn_setup(pos["th"], pos["mom"], rv_pos=pos["qv"], bound_cells=bc, scalars=[pos["qv"], pos["tracer"]])
+        lib = blk.lib
+        c = torch.from_numpy(st.c).cuda()
+        it = (C.c_int * 4)()
+        rs = (C.c_double * 4)()
+        ps = (C.c_int * 4)()
+        pr = (C.c_double * 4)()
 
-    step()  # warm-up
-    n_rep = 2
-    l0 = lib.asam_launch_count()
-    ms = time_region(torch, stream, step, n_rep) / n_rep
-    launches = (lib.asam_launch_count() - l0) // n_rep
+        def step():
+            rc = lib.asam_ros_step_dyn(blk.h, C.c_void_p(c.data_ptr()), a.dt, it, rs, ps, pr)
+            if rc not in (0, 1, 2):
+                raise RuntimeError(f"asam_ros_step_dyn: {rc}")
+
+        step()  # warm-up
+        n_rep = 2
+        l0 = lib.asam_launch_count()
+        ms = time_region(torch, stream, step, n_rep) / n_rep
+        launches = (lib.asam_launch_count() - l0) // n_rep
+        blk.close()
+        return ms, launches, c, list(it[:3]), list(ps[:3]), list(pr[:3])
+
+    ms, launches, c, its, pss, prs = run("fp64")
+    ms_r, _, c_r, its_r, _, _ = run("fp32_refined")
+    err = float(max(((c_r[q] - c[q]).abs().max() / c[q].abs().max().clamp_min(1e-300)).item() for q in range(nc)))
     vol = torch.from_numpy(geo.volc).cuda()
     mass = float((c[0] * vol)[1:-1, 1:-1, 1:-1].sum())
     mass0 = float(np.sum((st.c[0] * geo.volc)[1:-1, 1:-1, 1:-1]))
-    blk.close()
     cpu = None
     if not a.no_cpu_baseline:
         cgeo, cvel, cst, cpos, (cdx, cdy, cdz), cbc = G.dyn_case(64, 64, 32, seed=11, moist=True, tracer=True)
@@ -526,9 +551,12 @@ def dyn_bench(a, torch, stream):
                     f"({nc} components), {len(bc)} boundary cells, free-slip walls, RosRK3 dt={a.dt} s, "
                     f"BiCGStab tol {a.tol}, FGMRES(10) QMRTol 1e-6",
         "metric": "Mcell-steps/s", "value": nx * ny * nz / (ms * 1e-3) / 1e6, "ms_per_step": ms,
-        "bicgstab_iterations": list(it[:3]), "fgmres_steps": list(ps[:3]),
-        "fgmres_rel_residual": list(pr[:3]), "gpu_launches_per_step": launches,
-        "mass_rel_change": (mass - mass0) / mass0, "cpu_baseline": cpu,
+        "bicgstab_iterations": its, "fgmres_steps": pss, "fgmres_rel_residual": prs,
+        "gpu_launches_per_step": launches, "mass_rel_change": (mass - mass0) / mass0,
+        "fp32_refined": {"value": nx * ny * nz / (ms_r * 1e-3) / 1e6, "ms_per_step": ms_r,
+                         "speedup_vs_fp64": ms / ms_r, "bicgstab_iterations": its_r,
+                         "max_rel_err_vs_fp64_after_3_steps": err},
+        "cpu_baseline": cpu,
     }
 
 

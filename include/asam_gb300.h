@@ -316,6 +316,13 @@ int asam_solve_sound(asam_ctx *ctx, double *x, const double *b, int *maxiter, do
 int asam_project_vel_face(asam_ctx *ctx, double *uf, double *vf, double *wf, double *incr, const double *state,
                           int th_pos, int rho_pos, const int *scalars, int nscalar, double *pressure, int *steps,
                           double *resid);
+/* Precision of the multigrid V-cycle that preconditions FGMRES (PSolve1):
+ * 0 FP64 (the reference's arithmetic, bit-exact), 1 FP32 (a rounded copy of
+ * the hierarchy; FGMRES is flexible, so the FP64 Arnoldi relation and its
+ * residual test are unchanged and the tolerance is met as before), -1 (the
+ * default) FP32 when the context runs ASAM_PREC_FP32_REFINED, else FP64.
+ * No reference counterpart.  asam_lapl_vcycle follows the same choice. */
+int asam_proj_set_precision(asam_ctx *ctx, int prec);
 /* Number of multigrid V-cycles run by this context's projection (diagnostic). */
 long long asam_proj_vcycles(asam_ctx *ctx);
 

@@ -158,6 +158,28 @@ def test_ros_step_dyn_matches_oracle(built_lib, name):
     assert abs(m1 - m0) <= 1e-13 * m0
 
 
+def test_ros_step_dyn_refined(built_lib):
+    """The dynamical step with the FP32-refined transport solve stays within
+    the step tolerance of the FP64 oracle."""
+    name = "dyn_hill_13x9x10"
+    geo, vel, st, pos, (dx, dy, dz), bc = _case(name)
+    nc = st.c.shape[0]
+    o = oracle.Oracle(geo, bc=_kinds(nc, pos["mom"]))
+    pr = oracle.OracleProj(geo, dx, dy, dz, G.projection_inputs(geo)[0], zebra=1)
+    sc = [pos[k] for k in ("qv", "tracer") if k in pos]
+    cr, cg = st.c.copy(), st.c.copy()
+    ur = [a.copy() for a in vel]
+    with _block(name, bicgstab_tol=1e-10, proj_tol=1e-10, proj_restarts=20, precision="fp32_refined",
+                inner_precond="xline") as blk:
+        for step in range(2):
+            o.ros_step_dyn(pr, cr, ur, 2.0, rho_pos=0, th_pos=pos["th"], pos=pos["mom"], dx=dx, dy=dy, dz=dz,
+                           rv_pos=pos["qv"], bound=bc, scalars=sc, bicg_tol=1e-10, proj_tol=1e-10, proj_maxiter=20)
+            blk.Ros3MetC_dyn(cg, 2.0)
+            assert max(cases.field_relerr(cg, cr)) <= STEP_TOL, step
+            for a, b in zip(blk.get_velocity(), ur):
+                assert cases.relerr(a, b) <= STEP_TOL
+
+
 def test_dyn_bad_calls(built_lib):
     geo, vel, st, pos, (dx, dy, dz), bc = _case("dyn_flat_10x8x7")
     with TransportBlock(geo, ncomp=st.c.shape[0], rho_pos=0) as blk:

@@ -182,3 +182,31 @@ def test_density_weights_and_hierarchy_bitwise(name):
             for L2 in range(L3, REF_LEVEL):
                 for which in range(7 if L2 == L3 else 5):
                     np.testing.assert_array_equal(blk.lapl_array(L3, L2, which), o.lapl_get(L3, L2, which))
+
+
+@pytest.mark.parametrize("name", ["proj_hill_24x20x16", "proj_hill_odd_13x7x9", "proj_column_1x1x12"])
+def test_fp32_multigrid_preconditioner(name):
+    """The FP32 copy of the hierarchy: one V-cycle agrees with the FP64 one to
+    FP32 accuracy, and FGMRES preconditioned by it reaches the same tolerance
+    (the FP64 Arnoldi relation is unchanged) and the oracle's solution."""
+    geo, W, (u, v, w), blk, o = _pair(name)
+    g = geo.grid
+    rng = np.random.default_rng(17)
+    live = geo.volc[1:-1, 1:-1, 1:-1] > 0
+    with blk:
+        # cells without volume have a zero right-hand side in the projection
+        b = rng.standard_normal((g.nz, g.ny, g.nx)) * live
+        x64 = blk.VCycleCG(b)
+        blk.proj_set_precision("fp32")
+        x32 = blk.VCycleCG(b)
+        assert np.all(np.isfinite(x32))
+        assert np.max(np.abs(x32 - x64)[live]) <= 1e-5 * np.max(np.abs(x64)[live])
+        rhs = o.rhs(u, v, w)
+        xr = np.zeros_like(rhs)
+        o.fgmres(xr, rhs, maxiter=20, tol=1e-10, step=10)
+        x = np.zeros_like(rhs)
+        steps, rel = blk.SolveSound(x, rhs, MaxIter=20, Tol=1e-10)
+        assert rel <= 1e-10
+        assert np.max(np.abs(x - xr)) <= 1e-8 * max(np.max(np.abs(xr)), 1e-300)
+        blk.proj_set_precision("fp64")
+        np.testing.assert_array_equal(blk.VCycleCG(b), x64)
