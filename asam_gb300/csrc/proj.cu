@@ -49,7 +49,7 @@ constexpr int kMaxLev = 8;
 constexpr int kPlaneBlock = 256;
 constexpr int kRedGrid = 1024;
 constexpr int kRedBlock = 256;
-constexpr size_t kRingBytes = (size_t)4 * 8 * kPlaneBlock * sizeof(double);  // kRing * kFields * block
+constexpr size_t kRingBytes = (size_t)4 * 8 * kPlaneBlock * sizeof(double);  // ring rows * fields * block, 64 KB
 constexpr double kTiny = 1.0e-40;  // initial diagonal of Allocate_1D (TriDiagT_Mod.f90:99)
 
 // One plane level of a 3D level (all its planes); T = double for the
@@ -453,8 +453,16 @@ __device__ inline T matvec2_at(const Lev2T<T>& P, size_t mo, const T* __restrict
 // memory with cp.async, kAhead rows ahead of the recurrence; the copies read
 // only the other parity's lines and the matrix, never this thread's column.
 // The back substitution loads x and w four rows ahead in two register sets.
-constexpr int kRing = 4;
-constexpr int kAhead = 3;
+// Ring depth by value type: the same 64 KB per CTA hold 4 FP64 rows or 8 FP32
+// rows, so the FP32 copy keeps twice as many rows in flight.
+template <typename T>
+struct RingCfg {
+  static constexpr int ring = 4, ahead = 3;
+};
+template <>
+struct RingCfg<float> {
+  static constexpr int ring = 8, ahead = 7;
+};
 constexpr int kFields = 8;
 
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
@@ -471,6 +479,7 @@ __device__ __noinline__ void line_half(const Lev2T<T>& P, size_t mo, const T* __
   const T* __restrict__ ft = P.ft + mo;
   const T* __restrict__ frt = P.frt + mo;
   const T* __restrict__ fw = P.fw + mo;
+  constexpr int kRing = RingCfg<T>::ring, kAhead = RingCfg<T>::ahead;
   const int nl = (c2 - c + 1) / 2;
   const int bd = blockDim.x, tid = threadIdx.x;
   for (int q = tid; q < nl; q += bd) {
@@ -1204,7 +1213,7 @@ void vcycle_run(asam_ctx* h, std::vector<Lev3T<T>>& lv, Lev3T<T>* d_lv) {
   const int R = s->R;
   const int gi2 = s->cfg.gauss_iter2, gi3 = s->cfg.gauss_iter3;
   const int mi2 = s->cfg.mult_iter2;
-  const size_t ring = kRingBytes / sizeof(double) * sizeof(T);
+  const size_t ring = (size_t)RingCfg<T>::ring * kFields * kPlaneBlock * sizeof(T);
   long long nl = 0;
   cudaMemsetAsync(lv[0].x, 0, sizeof(T) * len0(s), st);
   auto gs3 = [&](int L, int gi) {

@@ -44,6 +44,12 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Mcell-steps/s"
+# DRAM bytes of one PSolve per padded cell, measured with ncu on the 256x256x64
+# workload (profiles/traffic_psolve_256x256x64.md), 10 components: the FP64
+# Gauss-Seidel call and the refined mode's FP32 x-line call (without the
+# once-per-matrix factors); scaled to a launch of the bench grid by padded cells
+TRAFFIC_PSOLVE_FP64_PER_PCELL = 11553.6e6 / 4393224
+TRAFFIC_PSOLVE_XLINE_PER_PCELL = (1622.97e6 - 55.0e6) / 4393224
 BYTES_PER_CELL_FLUX = lambda ncomp: 64 + 16 * ncomp  # noqa: E731  algorithmic bytes per interior cell
 
 
@@ -65,6 +71,9 @@ def parse():
     p.add_argument("--no-dyn", action="store_true", help="skip the dynamical-core step")
     p.add_argument("--dyn-only", action="store_true",
                    help="only the dynamical-core section (profiling); prints its JSON object")
+    p.add_argument("--probe", choices=["psolve", "inner_psolve"],
+                   help="profiling: build the workload, compute its stage matrix, run exactly one PSolve "
+                        "(FP64 Gauss-Seidel) or one FP32 inner PSolve (x-line) and exit")
     p.add_argument("--projection-only", action="store_true",
                    help="only the projection section (profiling); prints its JSON object")
     p.add_argument("--batch-members", type=int, default=48)
@@ -678,6 +687,34 @@ def main():
         hp = json.loads(pk0.read_text()).get("hbm_gbs", 6800.0) if pk0.exists() else 6800.0
         print(json.dumps(projection_bench(a, torch, stream, hp)), flush=True)
         return
+    if a.probe:
+        import ctypes as C
+
+        import torch
+
+        import __graft_entry__
+        import asam_gb300
+
+        __graft_entry__.build()
+        geo, vel, st = workload(a.nx, a.ny, a.nz)
+        refined = a.probe == "inner_psolve"
+        blk = asam_gb300.TransportBlock(geo, st.c.shape[0], method="RosRK3", bicgstab_tol=a.tol,
+                                        precision="fp32_refined" if refined else "fp64",
+                                        inner_precond="xline" if refined else "gauss_seidel")
+        blk.set_velocity(*vel)
+        c = torch.from_numpy(st.c).cuda()
+        out = torch.empty_like(c)
+        P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+        blk.lib.asam_jac(blk.h, P(c), a.dt)
+        fn = blk.lib.asam_inner_psolve if refined else blk.lib.asam_psolve
+        torch.cuda.synchronize()
+        n0 = blk.lib.asam_launch_count()
+        rc = fn(blk.h, P(c), P(out))
+        torch.cuda.synchronize()
+        print(json.dumps({"probe": a.probe, "rc": rc, "launches": blk.lib.asam_launch_count() - n0,
+                          "npad": (a.nx + 2) * (a.ny + 2) * (a.nz + 2), "ncomp": st.c.shape[0]}), flush=True)
+        blk.close()
+        return
     if a.dyn_only:
         import torch
 
@@ -866,7 +903,10 @@ def main():
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": nbytes_state, "d2h_bytes_per_step": nbytes_state},
         "roofline": {"kernel": "k_gs_pipe (one PSolve: 1+IterG Gauss-Seidel sweeps)", "bound": "hbm",
                      "achieved": gs_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gs_gbs / hbm_peak,
-                     "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
+                     "traffic": TRAFFIC_PSOLVE_FP64_PER_PCELL * npad if ncomp == 10 else None,
+                     "traffic_source": "ncu dram__bytes_read.sum+dram__bytes_write.sum of one PSolve at 256x256x64, "
+                                       "scaled by padded cells (profiles/traffic_psolve_256x256x64.md)",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
                      "algorithmic_bytes_per_call": gs_bytes,
                      "fp64_pipe": {"achieved_ginst_s": gs_dp / ps_s / 1e9, "peak_ginst_s": fp64_peak_inst,
                                    "frac": gs_dp / ps_s / 1e9 / fp64_peak_inst,
@@ -912,7 +952,10 @@ def main():
         line["roofline_refined"] = {
             "kernel": kname, "bound": "hbm",
             "achieved": gs32_bytes / gs32_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
-            "frac": gs32_bytes / gs32_s / 1e9 / hbm_peak, "traffic": None,
+            "frac": gs32_bytes / gs32_s / 1e9 / hbm_peak,
+            "traffic": TRAFFIC_PSOLVE_XLINE_PER_PCELL * npad if (inner == "xline" and ncomp == 10) else None,
+            "traffic_source": "ncu dram__bytes_read.sum+dram__bytes_write.sum of one x-line inner PSolve at "
+                              "256x256x64, scaled by padded cells (profiles/traffic_psolve_256x256x64.md)",
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)", "algorithmic_bytes_per_call": gs32_bytes}
         line["fp32_refined"] = {"value": world * ncell * a.steps / (rr["ms"] * 1e-3) / 1e6,
                                 "ms_per_step": rr["ms"] / a.steps,
