@@ -84,6 +84,21 @@ struct GeomT {
   const T* wf;
 };
 
+// Momentum sources of the dynamical stage of a closed block, added by FcnMet
+// to the six LR momentum components (ADVECT/Function_Mod.f90:1267-1297,
+// 1389-1393): the pressure gradient before AdvectionScale and the buoyancy
+// after it.
+template <typename T>
+struct MomSrc {
+  const T* p;    // PreCell, padded
+  const T* rho;  // density component of the state, padded
+  const T *dx, *dy, *dz;  // widths of the interior cells
+  const T *mxy, *myx;     // MetrXY(iy), MetrYX(ix)
+  int pos[6];             // uL, uR, vL, vR, wL, wR components (-1: none)
+  int pgrad, buoy;        // PGradient, Buoyancy
+  T grav;                 // Grav
+};
+
 // Halo rule of each component on each side that is not periodic (the outer
 // walls 'ow'...'ot' of a block): BoundaryCompute
 // (ADVECT/BoundaryCondition_Mod.f90:70-346) for the scalars and

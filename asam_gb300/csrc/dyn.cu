@@ -13,7 +13,9 @@
 //     the first stage, the transport BiCGStab, ProjectVelFace, the face
 //     velocity update.
 // FP64 without FMA contraction (-fmad=false): every value except the
-// temperature (pow) is the oracle's bit for bit.
+// temperature (pow) is the oracle's bit for bit.  A context in the refined
+// precision takes its flux from the contracted copy (k64fma.cu), like the
+// transport step.
 #include <cmath>
 #include <vector>
 
@@ -263,9 +265,6 @@ void fcn_dyn_dev(asam_ctx* h, const double* c, const double* p, double* f) {
   const DynState* s = h->dyn;
   ProjGrid pg{};
   proj_grid(h, &pg);
-  launch_phi(L, d, h->cfg.ncomp, h->cfg.rho_pos, c, h->phi);
-  launch_face_flux(L, d, h->geom(), h->cfg.ncomp, h->coef_x, h->coef_y, h->coef_z, h->mask_x, h->mask_y, h->mask_z,
-                   h->phi, h->gx, h->gy, h->gz);
   MomSrc<double> ms{};
   ms.p = p;
   ms.rho = c + (size_t)h->cfg.rho_pos * h->npad;
@@ -278,6 +277,14 @@ void fcn_dyn_dev(asam_ctx* h, const double* c, const double* p, double* f) {
   ms.pgrad = s->cfg.pgradient;
   ms.buoy = s->cfg.buoyancy;
   ms.grav = s->cfg.grav;
+  if (h->cfg.precision == ASAM_PREC_FP32_REFINED) {  // contracted FP64, the refined mode's 1e-10 contract
+    asam_fma::launch_fcn_mom(L, d, h->geom(), h->cfg.ncomp, h->cfg.rho_pos, c, h->coef_x, h->coef_y, h->coef_z,
+                             h->mask_x, h->mask_y, h->mask_z, h->phi, h->gx, h->gy, h->gz, h->rvol, f, ms);
+    return;
+  }
+  launch_phi(L, d, h->cfg.ncomp, h->cfg.rho_pos, c, h->phi);
+  launch_face_flux(L, d, h->geom(), h->cfg.ncomp, h->coef_x, h->coef_y, h->coef_z, h->mask_x, h->mask_y, h->mask_z,
+                   h->phi, h->gx, h->gy, h->gz);
   const int grid = grid_of(L, h->npad);
   k_flux_gather<double, true><<<grid, kB, 0, L.stream>>>(d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz, h->rvol, f,
                                                            ms);

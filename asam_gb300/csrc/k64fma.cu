@@ -1,5 +1,6 @@
 // FP64 kernels of the refined mode with FMA contraction allowed: the flux
-// right-hand side, the stage matrix and the refinement residual.  The refined
+// right-hand side (with the momentum sources of the dynamical stage), the
+// stage matrix and the refinement residual.  The refined
 // mode is held to 1e-10 against the FP64 oracle, not to bit parity, so these
 // may fuse multiply-adds (fewer instructions on the scarce FP64 pipe); the
 // drop-in path keeps its own copies compiled without contraction (k64.cu).
@@ -21,6 +22,18 @@ void launch_fcn(const Launch& L, const Dims& d, const GeomT<double>& g, int ncom
   k_face_flux<double, 1><<<gs_grid(L, d.n_vf()), kBlock, 0, L.stream>>>(d, g, ncomp, cy, my, phi, gy);
   k_face_flux<double, 2><<<gs_grid(L, d.n_wf()), kBlock, 0, L.stream>>>(d, g, ncomp, cz, mz, phi, gz);
   k_flux_gather<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f, MomSrc<double>{});
+  count_launches(5);
+}
+
+void launch_fcn_mom(const Launch& L, const Dims& d, const GeomT<double>& g, int ncomp, int rho_pos, const double* c,
+                    const double* cx, const double* cy, const double* cz, const unsigned char* mx,
+                    const unsigned char* my, const unsigned char* mz, double* phi, double* gx, double* gy,
+                    double* gz, const double* rvol, double* f, const asam::MomSrc<double>& ms) {
+  k_phi<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, rho_pos, c, phi);
+  k_face_flux<double, 0><<<gs_grid(L, d.n_uf()), kBlock, 0, L.stream>>>(d, g, ncomp, cx, mx, phi, gx);
+  k_face_flux<double, 1><<<gs_grid(L, d.n_vf()), kBlock, 0, L.stream>>>(d, g, ncomp, cy, my, phi, gy);
+  k_face_flux<double, 2><<<gs_grid(L, d.n_wf()), kBlock, 0, L.stream>>>(d, g, ncomp, cz, mz, phi, gz);
+  k_flux_gather<double, true><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f, ms);
   count_launches(5);
 }
 

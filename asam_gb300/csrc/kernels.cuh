@@ -12,6 +12,7 @@ namespace {
 using asam::Dims;
 using asam::kMaxComp;
 using asam::GsTileSched;
+using asam::MomSrc;
 
 template <typename T>
 __device__ __forceinline__ T eps_t() {
@@ -232,21 +233,6 @@ __global__ void k_face_flux(Dims d, GeomT<T> g, int ncomp, const T* __restrict__
     }
   }
 }
-
-// Momentum sources of the dynamical stage of a closed block, added by FcnMet
-// to the six LR momentum components (ADVECT/Function_Mod.f90:1267-1297,
-// 1389-1393): the pressure gradient before AdvectionScale and the buoyancy
-// after it.
-template <typename T>
-struct MomSrc {
-  const T* p;    // PreCell, padded
-  const T* rho;  // density component of the state, padded
-  const T *dx, *dy, *dz;  // widths of the interior cells
-  const T *mxy, *myx;     // MetrXY(iy), MetrYX(ix)
-  int pos[6];             // uL, uR, vL, vR, wL, wR components (-1: none)
-  int pgrad, buoy;        // PGradient, Buoyancy
-  T grav;                 // Grav
-};
 
 // Grad of PGradComputeCFull (ADVECT/PressureGrad_Mod.f90:252-276) on the
 // interior face between padded cells (i,j,k) and their +1 neighbour along

@@ -70,6 +70,11 @@ void launch_fcn(const asam::Launch&, const asam::Dims&, const asam::GeomT<double
                 const double* c, const double* cx, const double* cy, const double* cz, const unsigned char* mx,
                 const unsigned char* my, const unsigned char* mz, double* phi, double* gx, double* gy, double* gz,
                 const double* rvol, double* f);
+// the same flux with the momentum sources of the dynamical stage
+void launch_fcn_mom(const asam::Launch&, const asam::Dims&, const asam::GeomT<double>& g, int ncomp, int rho_pos,
+                    const double* c, const double* cx, const double* cy, const double* cz, const unsigned char* mx,
+                    const unsigned char* my, const unsigned char* mz, double* phi, double* gx, double* gy, double* gz,
+                    const double* rvol, double* f, const asam::MomSrc<double>& ms);
 void launch_jac(const asam::Launch&, const asam::Dims&, const asam::GeomT<double>&, const double* rho,
                 const double* rvol, double bdt, double* val);
 void launch_resid_dot(const asam::Launch&, const asam::Dims&, int ncomp, const double* val, const double* x,
