@@ -162,6 +162,18 @@ class TransportBlock:
             raise ValueError("kinds must have 6 entries per component")
         check(self.lib.asam_set_boundary(self.h, k.ctypes.data_as(C.POINTER(C.c_int))), "asam_set_boundary")
 
+    def set_diffusion(self, dh, dv=None, jac: bool = True):
+        """Diffusion of every component with coefficients DH, DV (padded cell
+        fields; DV defaults to DH), or None to switch it off; jac adds the
+        diffusion Jacobian to the stage matrix."""
+        if dh is None:
+            self._diff = None
+            check(self.lib.asam_set_diffusion(self.h, None, None, 0), "asam_set_diffusion")
+            return
+        self._diff = (_f64(dh), None if dv is None else _f64(dv))
+        check(self.lib.asam_set_diffusion(self.h, ptr(self._diff[0]), None if dv is None else ptr(self._diff[1]),
+                                          int(bool(jac))), "asam_set_diffusion")
+
     def BoundaryCondition(self, c: np.ndarray) -> np.ndarray:
         a = self._state(c).copy()
         check(self.lib.asam_boundary_condition(self.h, ptr(a)), "asam_boundary_condition")

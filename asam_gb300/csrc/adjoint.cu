@@ -640,7 +640,7 @@ void flux_tlm(asam_ctx* h, AdjWork& w, const double* rho, const double* dc, doub
   k_face_tlm<0><<<grid_of(L, d.n_uf()), kB, 0, L.stream>>>(d, h->coef_x, w.dcx, w.t1, w.gx);
   k_face_tlm<1><<<grid_of(L, d.n_vf()), kB, 0, L.stream>>>(d, h->coef_y, w.dcy, w.t1, w.gy);
   k_face_tlm<2><<<grid_of(L, d.n_wf()), kB, 0, L.stream>>>(d, h->coef_z, w.dcz, w.t1, w.gz);
-  launch_flux_gather(L, d, h->geom(), 1, w.gx, w.gy, w.gz, h->rvol, df);
+  launch_flux_gather(L, d, h->geom(), 1, w.gx, w.gy, w.gz, h->rvol, df, nullptr);
   count_launches(4);
 }
 
@@ -1071,7 +1071,15 @@ int dev_out_finish(asam_ctx* h, double* user, size_t n, double* dev) {
   return kOk;
 }
 
-bool valid_comp(asam_ctx* h, int comp) { return comp >= 0 && comp < h->cfg.ncomp && comp != h->cfg.rho_pos; }
+// the tangent-linear and adjoint flux cover the advection; a context with
+// diffusion (asam_set_diffusion) is refused rather than differentiated wrongly
+bool valid_comp(asam_ctx* h, int comp) {
+  if (h->dkx) {
+    set_last_error("the adjoint covers the advection flux; switch diffusion off first", __FILE__, __LINE__);
+    return false;
+  }
+  return comp >= 0 && comp < h->cfg.ncomp && comp != h->cfg.rho_pos;
+}
 
 }  // namespace
 

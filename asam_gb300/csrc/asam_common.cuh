@@ -99,6 +99,19 @@ struct MomSrc {
   T grav;                 // Grav
 };
 
+// Diffusion of the flux right-hand side (DiffusionCompute,
+// ADVECT/Diffusion_Mod.f90:11-275): per face the coefficient
+// K = DRhoF*F*F/(VL+VR+Eps) (DRhoF the arithmetic face mean DF of the cell
+// coefficients, ADVECT/Operator_Mod.f90:49-53, or on an outer wall the interior
+// cell's), computed once per coefficient field; a face between two cells of
+// the block carries the flux 2K*(phiR-phiL), a face of a periodic side K*(...)
+// from each side.  phi = c/(Rho+Eps) of every component.
+template <typename T>
+struct DiffSrc {
+  const T *kx, *ky, *kz;  // uF, vF, wF extents
+  const T* phi;
+};
+
 // Halo rule of each component on each side that is not periodic (the outer
 // walls 'ow'...'ot' of a block): BoundaryCompute
 // (ADVECT/BoundaryCondition_Mod.f90:70-346) for the scalars and

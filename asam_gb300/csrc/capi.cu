@@ -525,24 +525,28 @@ int bicgstab_refined(asam_ctx* h, double* x, const double* b, int* maxiter, doub
 
 int fcn_dev(asam_ctx* h, const double* c, double* f) {
   const Launch& L = h->L;
+  DiffSrc<double> tmp;
+  const DiffSrc<double>* df = h->diff_src(tmp);
   if (h->cfg.precision == ASAM_PREC_FP32_REFINED) {  // contracted FP64 (the refined mode's 1e-10 contract)
     asam_fma::launch_fcn(L, h->d, h->geom(), h->cfg.ncomp, h->cfg.rho_pos, c, h->coef_x, h->coef_y, h->coef_z,
-                         h->mask_x, h->mask_y, h->mask_z, h->phi, h->gx, h->gy, h->gz, h->rvol, f);
+                         h->mask_x, h->mask_y, h->mask_z, h->phi, h->gx, h->gy, h->gz, h->rvol, f, df);
     return check_launch();
   }
   launch_phi(L, h->d, h->cfg.ncomp, h->cfg.rho_pos, c, h->phi);
   launch_face_flux(L, h->d, h->geom(), h->cfg.ncomp, h->coef_x, h->coef_y, h->coef_z, h->mask_x, h->mask_y,
                    h->mask_z, h->phi, h->gx, h->gy, h->gz);
-  launch_flux_gather(L, h->d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz, h->rvol, f);
+  launch_flux_gather(L, h->d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz, h->rvol, f, df);
   return check_launch();
 }
 
 int jac_dev(asam_ctx* h, const double* c, double dt) {
   const double* rho = c + (size_t)h->cfg.rho_pos * h->npad;
+  const bool jd = h->dkx && h->jac_diff;
+  const double *kx = jd ? h->dkx : nullptr, *ky = jd ? h->dky : nullptr, *kz = jd ? h->dkz : nullptr;
   if (h->cfg.precision == ASAM_PREC_FP32_REFINED)
-    asam_fma::launch_jac(h->L, h->d, h->geom(), rho, h->rvol, h->beta0 * dt, h->val);
+    asam_fma::launch_jac(h->L, h->d, h->geom(), rho, h->rvol, h->beta0 * dt, h->val, kx, ky, kz);
   else
-    launch_jac(h->L, h->d, h->geom(), rho, h->rvol, h->beta0 * dt, h->val);
+    launch_jac(h->L, h->d, h->geom(), rho, h->rvol, h->beta0 * dt, h->val, kx, ky, kz);
   if (h->cfg.precision == ASAM_PREC_FP32_REFINED) launch_convert_f64_to_f32(h->L, 8 * h->npad, h->val, h->val32);
   h->jac_ready = true;
   h->xline_ready = false;
@@ -773,6 +777,9 @@ int asam_destroy(asam_ctx* h) {
   gs_schedule_free(h);  // and the graphs
   proj_free(h);
   dyn_free(h);
+  double* dk[] = {h->dkx, h->dky, h->dkz};
+  for (double* q : dk)
+    if (q) cudaFree(q);
   for (auto st : h->cap_stream)
     if (st) cudaStreamDestroy(st);
   if (h->stage_sc) cudaFree(h->stage_sc);
@@ -930,6 +937,37 @@ int asam_set_boundary(asam_ctx* h, const int* kinds) {
     for (int sd = 0; sd < 6; ++sd) h->bc.k[ic][sd] = (signed char)kinds[6 * ic + sd];
   graphs_reset(h);  // a captured step holds the old rule
   return kOk;
+}
+
+int asam_set_diffusion(asam_ctx* h, const double* dh, const double* dv, int jac) {
+  if (!h) return kBadArg;
+  const Dims& d = h->d;
+  if (!dh) {  // off
+    double* p[] = {h->dkx, h->dky, h->dkz};
+    for (double* q : p)
+      if (q) cudaFree(q);
+    h->dkx = h->dky = h->dkz = nullptr;
+    h->jac_diff = false;
+    h->jac_ready = false;
+    graphs_reset(h);
+    return kOk;
+  }
+  if (!dv) dv = dh;
+  if (!h->dkx) {
+    CK(cudaMalloc((void**)&h->dkx, d.n_uf() * sizeof(double)));
+    CK(cudaMalloc((void**)&h->dky, d.n_vf() * sizeof(double)));
+    CK(cudaMalloc((void**)&h->dkz, d.n_wf() * sizeof(double)));
+  }
+  const double *ddh, *ddv;
+  int rc;
+  if ((rc = stage_in(h, dh, h->npad, h->stage_a, &ddh))) return rc;
+  if ((rc = stage_in(h, dv, h->npad, h->stage_b, &ddv))) return rc;
+  launch_diff_coef(h->L, d, h->geom(), ddh, ddv, h->dkx, h->dky, h->dkz);
+  CK(cudaStreamSynchronize(h->L.stream));
+  h->jac_diff = jac != 0;
+  h->jac_ready = false;
+  graphs_reset(h);  // a captured step holds the old flux
+  return check_launch();
 }
 
 int asam_boundary_condition(asam_ctx* h, double* c) {

@@ -104,6 +104,15 @@ struct asam_ctx {
   // halo rule of each component on the outer walls, applied to the state at
   // the start of every stage (default ZeroGrad, BoundaryCond_Mod.f90:240-247)
   asam::BcKinds bc{};
+  // diffusion (asam_set_diffusion): face coefficients of DiffusionCompute,
+  // nullptr while diffusion is off; jac_diff adds the diffusion Jacobian
+  double *dkx = nullptr, *dky = nullptr, *dkz = nullptr;
+  bool jac_diff = false;
+  const asam::DiffSrc<double>* diff_src(asam::DiffSrc<double>& tmp) const {
+    if (!dkx) return nullptr;
+    tmp = asam::DiffSrc<double>{dkx, dky, dkz, phi};
+    return &tmp;
+  }
 
   GeomT<double> geom() const { return GeomT<double>{volc, fu, fv, fw, uf, vf, wf}; }
 };

@@ -277,17 +277,23 @@ void fcn_dyn_dev(asam_ctx* h, const double* c, const double* p, double* f) {
   ms.pgrad = s->cfg.pgradient;
   ms.buoy = s->cfg.buoyancy;
   ms.grav = s->cfg.grav;
+  DiffSrc<double> tmp;
+  const DiffSrc<double>* df = h->diff_src(tmp);
   if (h->cfg.precision == ASAM_PREC_FP32_REFINED) {  // contracted FP64, the refined mode's 1e-10 contract
     asam_fma::launch_fcn_mom(L, d, h->geom(), h->cfg.ncomp, h->cfg.rho_pos, c, h->coef_x, h->coef_y, h->coef_z,
-                             h->mask_x, h->mask_y, h->mask_z, h->phi, h->gx, h->gy, h->gz, h->rvol, f, ms);
+                             h->mask_x, h->mask_y, h->mask_z, h->phi, h->gx, h->gy, h->gz, h->rvol, f, ms, df);
     return;
   }
   launch_phi(L, d, h->cfg.ncomp, h->cfg.rho_pos, c, h->phi);
   launch_face_flux(L, d, h->geom(), h->cfg.ncomp, h->coef_x, h->coef_y, h->coef_z, h->mask_x, h->mask_y, h->mask_z,
                    h->phi, h->gx, h->gy, h->gz);
   const int grid = grid_of(L, h->npad);
-  k_flux_gather<double, true><<<grid, kB, 0, L.stream>>>(d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz, h->rvol, f,
-                                                           ms);
+  if (df)
+    k_flux_gather<double, true, true><<<grid, kB, 0, L.stream>>>(d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz,
+                                                                 h->rvol, f, ms, *df);
+  else
+    k_flux_gather<double, true><<<grid, kB, 0, L.stream>>>(d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz, h->rvol,
+                                                             f, ms);
   count_launches(1);
 }
 

@@ -16,30 +16,40 @@ using asam::Launch;
 void launch_fcn(const Launch& L, const Dims& d, const GeomT<double>& g, int ncomp, int rho_pos, const double* c,
                 const double* cx, const double* cy, const double* cz, const unsigned char* mx,
                 const unsigned char* my, const unsigned char* mz, double* phi, double* gx, double* gy, double* gz,
-                const double* rvol, double* f) {
+                const double* rvol, double* f, const asam::DiffSrc<double>* df) {
   k_phi<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, rho_pos, c, phi);
   k_face_flux<double, 0><<<gs_grid(L, d.n_uf()), kBlock, 0, L.stream>>>(d, g, ncomp, cx, mx, phi, gx);
   k_face_flux<double, 1><<<gs_grid(L, d.n_vf()), kBlock, 0, L.stream>>>(d, g, ncomp, cy, my, phi, gy);
   k_face_flux<double, 2><<<gs_grid(L, d.n_wf()), kBlock, 0, L.stream>>>(d, g, ncomp, cz, mz, phi, gz);
-  k_flux_gather<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f, MomSrc<double>{});
+  if (df)
+    k_flux_gather<double, false, true><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f,
+                                                                                        MomSrc<double>{}, *df);
+  else
+    k_flux_gather<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f,
+                                                                          MomSrc<double>{});
   count_launches(5);
 }
 
 void launch_fcn_mom(const Launch& L, const Dims& d, const GeomT<double>& g, int ncomp, int rho_pos, const double* c,
                     const double* cx, const double* cy, const double* cz, const unsigned char* mx,
                     const unsigned char* my, const unsigned char* mz, double* phi, double* gx, double* gy,
-                    double* gz, const double* rvol, double* f, const asam::MomSrc<double>& ms) {
+                    double* gz, const double* rvol, double* f, const asam::MomSrc<double>& ms,
+                    const asam::DiffSrc<double>* df) {
   k_phi<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, rho_pos, c, phi);
   k_face_flux<double, 0><<<gs_grid(L, d.n_uf()), kBlock, 0, L.stream>>>(d, g, ncomp, cx, mx, phi, gx);
   k_face_flux<double, 1><<<gs_grid(L, d.n_vf()), kBlock, 0, L.stream>>>(d, g, ncomp, cy, my, phi, gy);
   k_face_flux<double, 2><<<gs_grid(L, d.n_wf()), kBlock, 0, L.stream>>>(d, g, ncomp, cz, mz, phi, gz);
-  k_flux_gather<double, true><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f, ms);
+  if (df)
+    k_flux_gather<double, true, true><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f,
+                                                                                       ms, *df);
+  else
+    k_flux_gather<double, true><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f, ms);
   count_launches(5);
 }
 
 void launch_jac(const Launch& L, const Dims& d, const GeomT<double>& g, const double* rho, const double* rvol,
-                double bdt, double* val) {
-  k_jac<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, rho, rvol, bdt, val);
+                double bdt, double* val, const double* dkx, const double* dky, const double* dkz) {
+  k_jac<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, rho, rvol, bdt, val, dkx, dky, dkz);
   count_launches(1);
 }
 

@@ -13,6 +13,7 @@ using asam::Dims;
 using asam::kMaxComp;
 using asam::GsTileSched;
 using asam::MomSrc;
+using asam::DiffSrc;
 
 template <typename T>
 __device__ __forceinline__ T eps_t() {
@@ -274,11 +275,13 @@ __device__ __forceinline__ T buoy_rho_face(const Dims& d, const GeomT<T>& g, con
 // in which the reference's scatter loop touches f(ix,iy,iz), then the
 // zero-volume mask (:1045-1051), the periodic ExchangeFlux (neighbour order
 // W,E,S,N,B,T) and AdvectionScale (:2888-2898).  One thread per padded cell.
-// kMom adds the momentum sources of ms (closed blocks).
-template <typename T, bool kMom = false>
+// kMom adds the momentum sources of ms (closed blocks); kDiff the diffusion
+// fluxes of df with DiffusionCompute's second zero-volume mask (the halo
+// cells of a periodic side included, before ExchangeFlux reads them).
+template <typename T, bool kMom = false, bool kDiff = false>
 __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict__ gx, const T* __restrict__ gy,
                               const T* __restrict__ gz, const T* __restrict__ rvol, T* __restrict__ f,
-                              MomSrc<T> ms) {
+                              MomSrc<T> ms, DiffSrc<T> df = DiffSrc<T>{}) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
   const size_t n = d.npad();
@@ -320,6 +323,22 @@ __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict
         if (vR < (T)0) a = a + GY[fyR];
         if (wR < (T)0) a = a + GZ[fzR];
         a = div_rn(a * V, Ve, rV);
+        if (kDiff) {  // f(R) - Flux, f(L) + Flux per face, x then y then z; then the mask
+          const T* ph = df.phi + ic * n;
+          const T pc = ph[P];
+          const bool ix0 = i >= 2, ix1 = i <= nx - 1;  // faces i-1 and i between two cells of the block
+          const bool iy0 = j >= 2, iy1 = j <= ny - 1;
+          const bool iz0 = k >= 2, iz1 = k <= nz - 1;
+          const T kxl = df.kx[fxL], kxr = df.kx[fxR], kyl = df.ky[fyL], kyr = df.ky[fyR];
+          const T kzl = df.kz[fzL], kzr = df.kz[fzR];
+          a = a - ((ix0 || !d.per_x) ? (T)2 * kxl : kxl) * (pc - ph[P - 1]);
+          a = a + ((ix1 || !d.per_x) ? (T)2 * kxr : kxr) * (ph[P + 1] - pc);
+          a = a - ((iy0 || !d.per_y) ? (T)2 * kyl : kyl) * (pc - ph[P - (size_t)NX]);
+          a = a + ((iy1 || !d.per_y) ? (T)2 * kyr : kyr) * (ph[P + (size_t)NX] - pc);
+          a = a - ((iz0 || !d.per_z) ? (T)2 * kzl : kzl) * (pc - ph[P - (size_t)NX * NY]);
+          a = a + ((iz1 || !d.per_z) ? (T)2 * kzr : kzr) * (ph[P + (size_t)NX * NY] - pc);
+          a = div_rn(a * V, Ve, rV);
+        }
         if (kMom && ms.pgrad) {  // uRhsL(ix+1) - Two*VolC(ix+1)*Grad, uRhsR(ix) - Two*VolC(ix)*Grad
           int axis = -1, lo = 0;
           if (ic == ms.pos[0] && i >= 2) axis = 0, lo = 1;
@@ -338,37 +357,73 @@ __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict
           const size_t PH = d.P(nx + 1, j, k), fh = d.UF(nx, j, k);
           T h = g.uf[fh] > (T)0 ? GX[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + div_rn(h * VH, VH + e, rvol[PH]);
+          T hv = div_rn(h * VH, VH + e, rvol[PH]);
+          if (kDiff) {  // the halo's diffusion deposit and second mask
+            const T* ph = df.phi + ic * n;
+            hv = hv - df.kx[fh] * (ph[PH] - ph[d.P(nx, j, k)]);
+            hv = div_rn(hv * VH, VH + e, rvol[PH]);
+          }
+          a = a + hv;
         }
         if (exE) {
           const size_t PH = d.P(0, j, k), fh = d.UF(0, j, k);
           T h = g.uf[fh] < (T)0 ? GX[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + div_rn(h * VH, VH + e, rvol[PH]);
+          T hv = div_rn(h * VH, VH + e, rvol[PH]);
+          if (kDiff) {  // the halo's diffusion deposit and second mask
+            const T* ph = df.phi + ic * n;
+            hv = hv + df.kx[fh] * (ph[d.P(1, j, k)] - ph[PH]);
+            hv = div_rn(hv * VH, VH + e, rvol[PH]);
+          }
+          a = a + hv;
         }
         if (exS) {
           const size_t PH = d.P(i, ny + 1, k), fh = d.VF(i, ny, k);
           T h = g.vf[fh] > (T)0 ? GY[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + div_rn(h * VH, VH + e, rvol[PH]);
+          T hv = div_rn(h * VH, VH + e, rvol[PH]);
+          if (kDiff) {  // the halo's diffusion deposit and second mask
+            const T* ph = df.phi + ic * n;
+            hv = hv - df.ky[fh] * (ph[PH] - ph[d.P(i, ny, k)]);
+            hv = div_rn(hv * VH, VH + e, rvol[PH]);
+          }
+          a = a + hv;
         }
         if (exN) {
           const size_t PH = d.P(i, 0, k), fh = d.VF(i, 0, k);
           T h = g.vf[fh] < (T)0 ? GY[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + div_rn(h * VH, VH + e, rvol[PH]);
+          T hv = div_rn(h * VH, VH + e, rvol[PH]);
+          if (kDiff) {  // the halo's diffusion deposit and second mask
+            const T* ph = df.phi + ic * n;
+            hv = hv + df.ky[fh] * (ph[d.P(i, 1, k)] - ph[PH]);
+            hv = div_rn(hv * VH, VH + e, rvol[PH]);
+          }
+          a = a + hv;
         }
         if (exB) {
           const size_t PH = d.P(i, j, nz + 1), fh = d.WF(i, j, nz);
           T h = g.wf[fh] > (T)0 ? GZ[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + div_rn(h * VH, VH + e, rvol[PH]);
+          T hv = div_rn(h * VH, VH + e, rvol[PH]);
+          if (kDiff) {  // the halo's diffusion deposit and second mask
+            const T* ph = df.phi + ic * n;
+            hv = hv - df.kz[fh] * (ph[PH] - ph[d.P(i, j, nz)]);
+            hv = div_rn(hv * VH, VH + e, rvol[PH]);
+          }
+          a = a + hv;
         }
         if (exT) {
           const size_t PH = d.P(i, j, 0), fh = d.WF(i, j, 0);
           T h = g.wf[fh] < (T)0 ? GZ[fh] : (T)0;
           T VH = g.volc[PH];
-          a = a + div_rn(h * VH, VH + e, rvol[PH]);
+          T hv = div_rn(h * VH, VH + e, rvol[PH]);
+          if (kDiff) {  // the halo's diffusion deposit and second mask
+            const T* ph = df.phi + ic * n;
+            hv = hv + df.kz[fh] * (ph[d.P(i, j, 1)] - ph[PH]);
+            hv = div_rn(hv * VH, VH + e, rvol[PH]);
+          }
+          a = a + hv;
         }
         T fv = div_rn(a, Ve, rV);
         if (kMom && ms.buoy) {  // fL(iz+1) - RhoLoc*Grav, fR(iz) - RhoLoc*Grav
@@ -408,9 +463,81 @@ __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict
           if (axis == 2) a = a + gz[ic * nfz + fidx];
         }
         a = div_rn(a * V, Ve, rV);
+        if (kDiff) {  // periodic face halos receive the half flux of their face; every halo is masked again
+          const T* ph = df.phi + ic * n;
+          if (axis == 0 && d.per_x) {
+            if (i == 0) a = a + df.kx[fidx] * (ph[P + 1] - ph[P]);
+            else a = a - df.kx[fidx] * (ph[P] - ph[P - 1]);
+          } else if (axis == 1 && d.per_y) {
+            if (j == 0) a = a + df.ky[fidx] * (ph[P + (size_t)NX] - ph[P]);
+            else a = a - df.ky[fidx] * (ph[P] - ph[P - (size_t)NX]);
+          } else if (axis == 2 && d.per_z) {
+            if (k == 0) a = a + df.kz[fidx] * (ph[P + (size_t)NX * NY] - ph[P]);
+            else a = a - df.kz[fidx] * (ph[P] - ph[P - (size_t)NX * NY]);
+          }
+          a = div_rn(a * V, Ve, rV);
+        }
         f[ic * n + P] = div_rn(a, Ve, rV);
       }
     }
+  }
+}
+
+// Face coefficients of DiffusionCompute: K = DRhoF*F*F/(VL+VR+Eps), DRhoF =
+// DF(D_L, VL, D_R, VR) = (D_L*VR + D_R*VL)/(VL+VR+Eps) on faces between two
+// cells of the block or on a periodic side, the interior cell's D on an
+// outer wall (ADVECT/Diffusion_Mod.f90:24-52 and the matching branches);
+// D = DH on x and y faces, DV on z faces.
+template <typename T>
+__global__ void k_diff_coef(Dims d, GeomT<T> g, const T* __restrict__ dh, const T* __restrict__ dv,
+                            T* __restrict__ kx, T* __restrict__ ky, T* __restrict__ kz) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const size_t nu = d.n_uf(), nv = d.n_vf(), nw = d.n_wf();
+  const T e = eps_t<T>();
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nu + nv + nw; q += (size_t)gridDim.x * blockDim.x) {
+    size_t L, R;
+    T F;
+    bool wall_lo, wall_hi;
+    const T* D;
+    T* out;
+    size_t o;
+    if (q < nu) {
+      const int i = (int)(q % (nx + 1)), j = (int)((q / (nx + 1)) % ny) + 1, k = (int)(q / ((size_t)(nx + 1) * ny)) + 1;
+      L = d.P(i, j, k);
+      R = d.P(i + 1, j, k);
+      F = g.fu[d.FU(i, j, k)];
+      wall_lo = !d.per_x && i == 0;
+      wall_hi = !d.per_x && i == nx;
+      D = dh;
+      out = kx;
+      o = q;
+    } else if (q < nu + nv) {
+      o = q - nu;
+      const int i = (int)(o % nx) + 1, j = (int)((o / nx) % (ny + 1)), k = (int)(o / ((size_t)nx * (ny + 1))) + 1;
+      L = d.P(i, j, k);
+      R = d.P(i, j + 1, k);
+      F = g.fv[d.FV(i, j, k)];
+      wall_lo = !d.per_y && j == 0;
+      wall_hi = !d.per_y && j == ny;
+      D = dh;
+      out = ky;
+    } else {
+      o = q - nu - nv;
+      const int i = (int)(o % nx) + 1, j = (int)((o / nx) % ny) + 1, k = (int)(o / ((size_t)nx * ny));
+      L = d.P(i, j, k);
+      R = d.P(i, j, k + 1);
+      F = g.fw[d.FW(i, j, k)];
+      wall_lo = !d.per_z && k == 0;
+      wall_hi = !d.per_z && k == nz;
+      D = dv;
+      out = kz;
+    }
+    const T VL = g.volc[L], VR = g.volc[R];
+    T DRhoF;
+    if (wall_lo) DRhoF = D[R];
+    else if (wall_hi) DRhoF = D[L];
+    else DRhoF = (D[L] * VR + D[R] * VL) / (VL + VR + e);
+    out[o] = DRhoF * F * F / (VL + VR + e);
   }
 }
 
@@ -455,7 +582,8 @@ __device__ __forceinline__ T jac_term(T vel, bool plus, T F, T Vden, T rVden, T 
 
 template <typename T>
 __global__ void k_jac(Dims d, GeomT<T> g, const T* __restrict__ rho, const T* __restrict__ rvol, T bdt,
-                      T* __restrict__ val) {
+                      T* __restrict__ val, const T* __restrict__ dkx = nullptr, const T* __restrict__ dky = nullptr,
+                      const T* __restrict__ dkz = nullptr) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int NX = d.NX(), NY = d.NY();
   const size_t n = d.npad();
@@ -513,6 +641,43 @@ __global__ void k_jac(Dims d, GeomT<T> g, const T* __restrict__ rho, const T* __
       if (k == 1) dg = dg - jac_term(g.wf[d.WF(i, j, 0)], false, g.fw[d.FW(i, j, 0)], VP, rVP, rPe, rrP);
       if (k == nz) dg = dg - jac_term(g.wf[d.WF(i, j, nz)], true, g.fw[d.FW(i, j, nz)], VP, rVP, rPe, rrP);
       if (k == nz + 1) dg = dg - jac_term(g.wf[d.WF(i, j, nz)], false, g.fw[d.FW(i, j, nz)], VP, rVP, rPe, rrP);
+    }
+    // JacDiffusionCompute (ADVECT/Diffusion_Mod.f90:1504-1708): per face with
+    // a neighbour Temp = 2K; the off-diagonal of each column and its diagonal
+    // (face left of P, then face right of P; x, y, z) get
+    // Temp/(VolC_row+Eps)/(Rho_col+Eps)
+    if (dkx) {
+      auto term = [&](T K, size_t Q) { return div_rn(div_rn((T)2 * K, g.volc[Q] + e, rvol[Q]), rPe, rrP); };
+      if (actx(i - 1)) {
+        const T K = dkx[d.UF(i - 1, j, k)];
+        v[4] = v[4] + term(K, P - sx);
+        dg = dg - term(K, P);
+      }
+      if (actx(i)) {
+        const T K = dkx[d.UF(i, j, k)];
+        v[2] = v[2] + term(K, P + sx);
+        dg = dg - term(K, P);
+      }
+      if (acty(j - 1)) {
+        const T K = dky[d.VF(i, j - 1, k)];
+        v[5] = v[5] + term(K, P - sy);
+        dg = dg - term(K, P);
+      }
+      if (acty(j)) {
+        const T K = dky[d.VF(i, j, k)];
+        v[1] = v[1] + term(K, P + sy);
+        dg = dg - term(K, P);
+      }
+      if (actz(k - 1)) {
+        const T K = dkz[d.WF(i, j, k - 1)];
+        v[6] = v[6] + term(K, P - sz);
+        dg = dg - term(K, P);
+      }
+      if (actz(k)) {
+        const T K = dkz[d.WF(i, j, k)];
+        v[0] = v[0] + term(K, P + sz);
+        dg = dg - term(K, P);
+      }
     }
     // JacScaleCompute fold of the face-halo rows (:1791-1856)
     if (jj && kk && i == 0) dg = dg - v[2];

@@ -19,10 +19,13 @@ struct Launch {
                         const T* coef_z, const unsigned char* mask_x, const unsigned char* mask_y,               \
                         const unsigned char* mask_z, const T* phi, T* gx, T* gy, T* gz);                         \
   void launch_flux_gather(const Launch&, const Dims&, const GeomT<T>&, int ncomp, const T* gx, const T* gy,      \
-                          const T* gz, const T* rvol, T* f);                                                     \
+                          const T* gz, const T* rvol, T* f, const DiffSrc<T>* df);                               \
+  void launch_diff_coef(const Launch&, const Dims&, const GeomT<T>&, const T* dh, const T* dv, T* kx, T* ky,    \
+                        T* kz);                                                                                  \
   void launch_recip_eps(const Launch&, size_t len, const T* v, T* rv);                                          \
   void launch_div(const Launch&, const Dims&, const GeomT<T>&, T* rhs);                                          \
-  void launch_jac(const Launch&, const Dims&, const GeomT<T>&, const T* rho, const T* rvol, T bdt, T* val);     \
+  void launch_jac(const Launch&, const Dims&, const GeomT<T>&, const T* rho, const T* rvol, T bdt, T* val,      \
+                  const T* dkx, const T* dky, const T* dkz);                                                     \
   void launch_matvec(const Launch&, const Dims&, int ncomp, const TM* val, const T* x, T* y, int plain_spmv);    \
   void launch_gs_sweeps(const Launch&, const Dims&, int ncomp, const TM* val, const T* b, T* out, T* work,       \
                         int nsweep, int group);                                                                  \
@@ -69,14 +72,14 @@ namespace asam_fma {
 void launch_fcn(const asam::Launch&, const asam::Dims&, const asam::GeomT<double>& g, int ncomp, int rho_pos,
                 const double* c, const double* cx, const double* cy, const double* cz, const unsigned char* mx,
                 const unsigned char* my, const unsigned char* mz, double* phi, double* gx, double* gy, double* gz,
-                const double* rvol, double* f);
+                const double* rvol, double* f, const asam::DiffSrc<double>* df);
 // the same flux with the momentum sources of the dynamical stage
 void launch_fcn_mom(const asam::Launch&, const asam::Dims&, const asam::GeomT<double>& g, int ncomp, int rho_pos,
                     const double* c, const double* cx, const double* cy, const double* cz, const unsigned char* mx,
                     const unsigned char* my, const unsigned char* mz, double* phi, double* gx, double* gy, double* gz,
-                    const double* rvol, double* f, const asam::MomSrc<double>& ms);
+                    const double* rvol, double* f, const asam::MomSrc<double>& ms, const asam::DiffSrc<double>* df);
 void launch_jac(const asam::Launch&, const asam::Dims&, const asam::GeomT<double>&, const double* rho,
-                const double* rvol, double bdt, double* val);
+                const double* rvol, double bdt, double* val, const double* dkx, const double* dky, const double* dkz);
 void launch_resid_dot(const asam::Launch&, const asam::Dims&, int ncomp, const double* val, const double* x,
                       const double* b, double* r, double* partial, asam::KrylovScalars* sc, int op, double* out);
 }  // namespace asam_fma

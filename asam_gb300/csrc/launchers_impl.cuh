@@ -38,8 +38,18 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
     count_launches(3);                                                                                             \
   }                                                                                                                \
   void launch_flux_gather(const Launch& L, const Dims& d, const GeomT<T>& g, int ncomp, const T* gx, const T* gy,  \
-                          const T* gz, const T* rvol, T* f) {                                                      \
-    k_flux_gather<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f, MomSrc<T>{}); \
+                          const T* gz, const T* rvol, T* f, const DiffSrc<T>* df) {                                \
+    if (df)                                                                                                        \
+      k_flux_gather<T, false, true><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol,  \
+                                                                                   f, MomSrc<T>{}, *df);           \
+    else                                                                                                           \
+      k_flux_gather<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f,            \
+                                                                      MomSrc<T>{});                                \
+    count_launches(1);                                                                                             \
+  }                                                                                                                \
+  void launch_diff_coef(const Launch& L, const Dims& d, const GeomT<T>& g, const T* dh, const T* dv, T* kx, T* ky,  \
+                        T* kz) {                                                                                   \
+    k_diff_coef<T><<<gs_grid(L, d.n_uf() + d.n_vf() + d.n_wf()), kBlock, 0, L.stream>>>(d, g, dh, dv, kx, ky, kz);  \
     count_launches(1);                                                                                             \
   }                                                                                                                \
   void launch_recip_eps(const Launch& L, size_t len, const T* v, T* rv) {                                          \
@@ -50,8 +60,9 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
     k_div<T><<<gs_grid(L, (size_t)d.nx * d.ny * d.nz), kBlock, 0, L.stream>>>(d, g, rhs); count_launches(1);                          \
   }                                                                                                                \
   void launch_jac(const Launch& L, const Dims& d, const GeomT<T>& g, const T* rho, const T* rvol, T bdt,         \
-                  T* val) {                                                                                        \
-    k_jac<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, rho, rvol, bdt, val); count_launches(1);       \
+                  T* val, const T* dkx, const T* dky, const T* dkz) {                                              \
+    k_jac<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, rho, rvol, bdt, val, dkx, dky, dkz);            \
+    count_launches(1);                                                                                             \
   }                                                                                                                \
   void launch_matvec(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* x, T* y, int plain) {      \
     k_matvec<TM, T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, ncomp, val, x, y, plain);                    \

@@ -355,6 +355,21 @@ def dyn_case(nx: int, ny: int, nz: int, seed: int = 5, hill: bool = True, moist:
     return geo, vel, st, pos, widths, boundary_cells(geo)
 
 
+def diffusion_coefficients(geo: Geometry, rho: np.ndarray, kh: float = 50.0, kv: float = 5.0, seed: int = 0,
+                           spread: float = 0.2) -> tuple[np.ndarray, np.ndarray]:
+    """Seeded density-weighted eddy diffusivities (padded cell fields, m^2/s
+    times Rho): horizontal kh and vertical kv decaying with height, with a
+    seeded relative spread; the halos follow the state's density."""
+    g = geo.grid
+    rng = np.random.default_rng(seed)
+    zc = np.concatenate([[0.0], 0.5 * (g.zP[:-1] + g.zP[1:]), [g.zP[-1]]])
+    prof = np.exp(-zc / max(float(g.zP[-1]) * 0.5, 1.0))[:, None, None]
+    noise = 1.0 + spread * rng.uniform(-1.0, 1.0, size=g.pshape)
+    dh = np.ascontiguousarray(rho * kh * prof * noise)
+    dv = np.ascontiguousarray(rho * kv * prof * noise)
+    return dh, dv
+
+
 def face_velocity(geo: Geometry, u0: float, v0: float = 0.0) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     """Prescribed steady face velocities with zero discrete divergence in flux form.
 

@@ -125,6 +125,17 @@ int asam_set_boundary(asam_ctx *ctx, const int *kinds);
 /* Apply the halo rule to a state (ncomp padded fields) once. */
 int asam_boundary_condition(asam_ctx *ctx, double *c);
 
+/* Diffusion of every component (the FcnMet diffusion terms,
+ * ADVECT/Function_Mod.f90:1106-1239, DiffusionCompute
+ * ADVECT/Diffusion_Mod.f90:11-275, with CrossDiff off and Prandtl number 1):
+ * dh, dv the density-weighted horizontal and vertical coefficients (padded
+ * cell fields, the DiffKoeff of the TkeDis/TkeOme models; dv NULL = dh);
+ * jac != 0 also adds JacDiffusionCompute (:1504-1708) to the stage matrix.
+ * dh NULL switches diffusion off.  The face coefficients are computed once
+ * here; call again when the coefficients change.  The adjoint entry points
+ * refuse a context with diffusion. */
+int asam_set_diffusion(asam_ctx *ctx, const double *dh, const double *dv, int jac);
+
 /* Advection right-hand side of all components: the FcnMet advection terms
  * (ADVECT/Function_Mod.f90:1032-1099, 1312-1345): AdvectionComputeP
  * (ADVECT/Advection_Mod.f90:737-1054), ExchangeFlux, AdvectionScale.

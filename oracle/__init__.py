@@ -22,7 +22,8 @@ LIB_PATH = _HERE / "_build" / "libasam_oracle.so"
 class OraGeom(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("per_x", C.c_int), ("per_y", C.c_int),
                 ("per_z", C.c_int), ("volc", C.c_void_p), ("fu", C.c_void_p), ("fv", C.c_void_p),
-                ("fw", C.c_void_p), ("bc", C.c_void_p)]
+                ("fw", C.c_void_p), ("bc", C.c_void_p), ("dh", C.c_void_p), ("dv", C.c_void_p),
+                ("jac_diff", C.c_int)]
 
 
 _lib = None
@@ -43,6 +44,7 @@ def load() -> C.CDLL:
             "ora_exchange_cell": (None, [G, I, V]),
             "ora_exchange_flux": (None, [G, I, V]),
             "ora_bound_cond": (None, [G, I, I, V]),
+            "ora_diffusion": (None, [G, I, I, V, V]),
             "ora_fcn": (None, [G, I, I, V, V, V, V, V]),
             "ora_div": (None, [G, V, V, V, V]),
             "ora_jac": (None, [G, V, V, V, V, D, D, V]),
@@ -103,7 +105,7 @@ class Oracle:
         self.grid = g
         self._keep = [np.ascontiguousarray(x, dtype=np.float64) for x in (geo.volc, geo.fu, geo.fv, geo.fw)]
         self.g = OraGeom(g.nx, g.ny, g.nz, int(g.periodic_x), int(g.periodic_y), int(g.periodic_z),
-                         *(a.ctypes.data for a in self._keep), None)
+                         *(a.ctypes.data for a in self._keep), None, None, None, 0)
         self.gp = C.byref(self.g)
         self.npad = g.npad
         self.set_boundary(bc)
@@ -118,10 +120,31 @@ class Oracle:
             self._bc = np.ascontiguousarray(kinds, dtype=np.int32).reshape(-1)
             self.g.bc = self._bc.ctypes.data
 
+    def set_diffusion(self, dh, dv=None, jac=True):
+        """Diffusion coefficients DH, DV (padded cell fields; DV defaults to
+        DH) or None: no diffusion; jac adds the diffusion Jacobian."""
+        if dh is None:
+            self._diff = None
+            self.g.dh = self.g.dv = None
+            self.g.jac_diff = 0
+            return
+        dh = np.ascontiguousarray(dh, dtype=np.float64)
+        dv = dh if dv is None else np.ascontiguousarray(dv, dtype=np.float64)
+        self._diff = (dh, dv)
+        self.g.dh, self.g.dv = dh.ctypes.data, dv.ctypes.data
+        self.g.jac_diff = int(bool(jac))
+
     def exchange_cell(self, c):
         a = np.ascontiguousarray(c, dtype=np.float64).copy()
         self.lib.ora_exchange_cell(self.gp, a.size // self.npad, _p(a))
         return a
+
+    def diffusion(self, c, rho_pos=0):
+        """The diffusion terms of FcnMet alone (unscaled, masked), every component."""
+        a = np.ascontiguousarray(c, dtype=np.float64)
+        f = np.zeros_like(a)
+        self.lib.ora_diffusion(self.gp, a.size // self.npad, int(rho_pos), _p(a), _p(f))
+        return f
 
     def bound_cond(self, c, comp0=0):
         a = np.ascontiguousarray(c, dtype=np.float64).copy()

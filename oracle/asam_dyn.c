@@ -19,7 +19,8 @@
  *   PGradComputeCFull          ADVECT/PressureGrad_Mod.f90:245-276
  *   AuftriebDryComputeLRFull   ADVECT/Buoyancy_Mod.f90:43-63
  *   FcnMet                     ADVECT/Function_Mod.f90:989-1506 (advection,
- *                              pressure gradient, AdvectionScale, buoyancy)
+ *                              diffusion, pressure gradient, AdvectionScale,
+ *                              buoyancy)
  *   JacAccGrav, ProjectVelFace through the projection oracle (asam_proj.c)
  *
  * The BoundCell list of the grid (cells that hold a piece of the terrain
@@ -262,6 +263,7 @@ void ora_fcn_dyn(const ora_geom *g, int ncomp, int rho_pos, const int *pos, int 
   memset(f, 0, sizeof(double) * n * (size_t)ncomp);
   const double *rho = c + (size_t)rho_pos * n;
   for (int ic = 0; ic < ncomp; ++ic) ora_advection(g, c + ic * n, rho, uf, vf, wf, f + ic * n);
+  ora_diffusion(g, ncomp, rho_pos, c, f); /* Function_Mod.f90:1106-1239 (no-op without coefficients) */
   if (pgrad) {
     double *uRhsL = comp(f, g, pos[0]), *uRhsR = comp(f, g, pos[1]), *vRhsL = comp(f, g, pos[2]);
     double *vRhsR = comp(f, g, pos[3]), *wRhsL = comp(f, g, pos[4]), *wRhsR = comp(f, g, pos[5]);

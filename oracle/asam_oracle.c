@@ -291,6 +291,142 @@ void ora_exchange_flux(const ora_geom *g, int ncomp, double *f) {
  *   (ADVECT/Advection_Mod.f90:2888-2898).
  * c: ncomp padded fields; comp rho_pos is the density.  f: output (zeroed here). */
 /* ------------------------------------------------------------------ */
+/* ------------------------------------------------------------------ */
+/* DiffusionCompute (ADVECT/Diffusion_Mod.f90:11-275) of one component with
+ * DH/DV = g->dh/g->dv and DF the arithmetic face mean
+ * (ADVECT/Operator_Mod.f90:49-53).  Sides that are not outer walls (the
+ * periodic neighbour) carry half the flux from each side, completed by
+ * ExchangeFlux; an outer wall takes the interior cell's coefficient and
+ * updates the interior cell only.  Ends with f = f*VolC/(VolC+Eps) over the
+ * padded box. */
+/* ------------------------------------------------------------------ */
+static double df_mean(double DL, double VL, double DR, double VR) { return (DL * VR + DR * VL) / (VL + VR + EPS); }
+static void diffusion_compute(const ora_geom *g, const double *c, const double *rho, double *f) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const double *V = g->volc, *DH = g->dh, *DV = g->dv;
+  const size_t n = NPAD(g);
+#define CF(P) (c[P] / (rho[P] + EPS))
+  /* x */
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j) {
+      const size_t L = PIDX(g, 0, j, k), R = PIDX(g, 1, j, k);
+      const double FF = g->fu[FUI(g, 0, j, k)], VL = V[L], VR = V[R];
+      if (g->per_x) {
+        const double Flux = df_mean(DH[L], VL, DH[R], VR) * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+        f[L] = f[L] + Flux;
+      } else {
+        const double Flux = 2.0 * DH[R] * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+      }
+    }
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx - 1; ++i) {
+        const size_t L = PIDX(g, i, j, k), R = PIDX(g, i + 1, j, k);
+        const double FF = g->fu[FUI(g, i, j, k)], VL = V[L], VR = V[R];
+        const double Flux = 2.0 * df_mean(DH[L], VL, DH[R], VR) * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+        f[L] = f[L] + Flux;
+      }
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j) {
+      const size_t L = PIDX(g, nx, j, k), R = PIDX(g, nx + 1, j, k);
+      const double FF = g->fu[FUI(g, nx, j, k)], VL = V[L], VR = V[R];
+      if (g->per_x) {
+        const double Flux = df_mean(DH[L], VL, DH[R], VR) * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+        f[L] = f[L] + Flux;
+      } else {
+        const double Flux = 2.0 * DH[L] * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[L] = f[L] + Flux;
+      }
+    }
+  /* y */
+  for (int k = 1; k <= nz; ++k)
+    for (int i = 1; i <= nx; ++i) {
+      const size_t L = PIDX(g, i, 0, k), R = PIDX(g, i, 1, k);
+      const double FF = g->fv[FVI(g, i, 0, k)], VL = V[L], VR = V[R];
+      if (g->per_y) {
+        const double Flux = df_mean(DH[L], VL, DH[R], VR) * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+        f[L] = f[L] + Flux;
+      } else {
+        const double Flux = 2.0 * DH[R] * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+      }
+    }
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny - 1; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const size_t L = PIDX(g, i, j, k), R = PIDX(g, i, j + 1, k);
+        const double FF = g->fv[FVI(g, i, j, k)], VL = V[L], VR = V[R];
+        const double Flux = 2.0 * df_mean(DH[L], VL, DH[R], VR) * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+        f[L] = f[L] + Flux;
+      }
+  for (int k = 1; k <= nz; ++k)
+    for (int i = 1; i <= nx; ++i) {
+      const size_t L = PIDX(g, i, ny, k), R = PIDX(g, i, ny + 1, k);
+      const double FF = g->fv[FVI(g, i, ny, k)], VL = V[L], VR = V[R];
+      if (g->per_y) {
+        const double Flux = df_mean(DH[L], VL, DH[R], VR) * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+        f[L] = f[L] + Flux;
+      } else {
+        const double Flux = 2.0 * DH[L] * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[L] = f[L] + Flux;
+      }
+    }
+  /* z */
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      const size_t L = PIDX(g, i, j, 0), R = PIDX(g, i, j, 1);
+      const double FF = g->fw[FWI(g, i, j, 0)], VL = V[L], VR = V[R];
+      if (g->per_z) {
+        const double Flux = df_mean(DV[L], VL, DV[R], VR) * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+        f[L] = f[L] + Flux;
+      } else {
+        const double Flux = 2.0 * DV[R] * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+      }
+    }
+  for (int k = 1; k <= nz - 1; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const size_t L = PIDX(g, i, j, k), R = PIDX(g, i, j, k + 1);
+        const double FF = g->fw[FWI(g, i, j, k)], VL = V[L], VR = V[R];
+        const double Flux = 2.0 * df_mean(DV[L], VL, DV[R], VR) * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+        f[L] = f[L] + Flux;
+      }
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      const size_t L = PIDX(g, i, j, nz), R = PIDX(g, i, j, nz + 1);
+      const double FF = g->fw[FWI(g, i, j, nz)], VL = V[L], VR = V[R];
+      if (g->per_z) {
+        const double Flux = df_mean(DV[L], VL, DV[R], VR) * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[R] = f[R] - Flux;
+        f[L] = f[L] + Flux;
+      } else {
+        const double Flux = 2.0 * DV[L] * FF * FF / (VL + VR + EPS) * (CF(R) - CF(L));
+        f[L] = f[L] + Flux;
+      }
+    }
+#undef CF
+  for (size_t P = 0; P < n; ++P) f[P] = f[P] * V[P] / (V[P] + EPS);
+}
+
+/* the diffusion terms of FcnMet for every component (Function_Mod.f90:1112-1239;
+ * CrossDiff off, Prandtl number 1, one coefficient pair for all components) */
+void ora_diffusion(const ora_geom *g, int ncomp, int rho_pos, const double *c, double *f) {
+  if (!g->dh) return;
+  const size_t n = NPAD(g);
+  const double *rho = c + (size_t)rho_pos * n;
+  for (int ic = 0; ic < ncomp; ++ic) diffusion_compute(g, c + ic * n, rho, f + ic * n);
+}
+
 /* AdvectionComputeP of one component (accumulates into f, unscaled). */
 void ora_advection(const ora_geom *g, const double *c, const double *rho, const double *uf, const double *vf,
                    const double *wf, double *f) {
@@ -303,6 +439,7 @@ void ora_fcn(const ora_geom *g, int ncomp, int rho_pos, const double *c, const d
   memset(f, 0, sizeof(double) * n * (size_t)ncomp);
   const double *rho = c + (size_t)rho_pos * n;
   for (int ic = 0; ic < ncomp; ++ic) advection_compute_p(g, c + ic * n, rho, uf, vf, wf, f + ic * n);
+  ora_diffusion(g, ncomp, rho_pos, c, f);
   ora_exchange_flux(g, ncomp, f);
   for (int ic = 0; ic < ncomp; ++ic) {
     double *a = f + ic * n;
@@ -336,6 +473,44 @@ static void jac_face(double *val, size_t n, size_t iL, size_t iR, int dUp, int d
   val[3 * n + iL] = val[3 * n + iL] - HALF * (fabs(vel) + vel) * F / VL / (rhoL + EPS);
   val[(size_t)dDn * n + iR] = val[(size_t)dDn * n + iR] + HALF * (fabs(vel) - vel) * F / VL / (rhoR + EPS);
   val[3 * n + iR] = val[3 * n + iR] - HALF * (fabs(vel) - vel) * F / VR / (rhoR + EPS);
+}
+
+/* JacDiffusionCompute (ADVECT/Diffusion_Mod.f90:1504-1708): per face with a
+ * neighbour (interior faces, and the boundary faces of periodic sides; an
+ * outer wall adds nothing) Temp = Two*DF*F*F/(VL+VR+Eps) enters the two
+ * off-diagonals and the two diagonals of the face's cells, divided by the
+ * row cell's VolC+Eps and by the column cell's Rho+Eps.  Slots: off-diagonal
+ * of the left column d_lo (x: 2, y: 1, z: 0), of the right column d_hi. */
+static void jac_diff_face(double *val, size_t n, size_t L, size_t R, int d_lo, int d_hi, double DL, double DR,
+                          double VL, double VR, double FF, const double *rho) {
+  const double Temp = 2.0 * df_mean(DL, VL, DR, VR) * FF * FF / (VL + VR + EPS);
+  val[(size_t)d_lo * n + L] = val[(size_t)d_lo * n + L] + Temp / (VR + EPS) / (rho[L] + EPS);
+  val[3 * n + L] = val[3 * n + L] - Temp / (VL + EPS) / (rho[L] + EPS);
+  val[(size_t)d_hi * n + R] = val[(size_t)d_hi * n + R] + Temp / (VL + EPS) / (rho[R] + EPS);
+  val[3 * n + R] = val[3 * n + R] - Temp / (VR + EPS) / (rho[R] + EPS);
+}
+static void jac_diffusion(const ora_geom *g, const double *rho, double *val) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const size_t n = NPAD(g);
+  const double *V = g->volc, *DH = g->dh, *DV = g->dv;
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = g->per_x ? 0 : 1; i <= (g->per_x ? nx : nx - 1); ++i) {
+        const size_t L = PIDX(g, i, j, k), R = PIDX(g, i + 1, j, k);
+        jac_diff_face(val, n, L, R, 2, 4, DH[L], DH[R], V[L], V[R], g->fu[FUI(g, i, j, k)], rho);
+      }
+  for (int k = 1; k <= nz; ++k)
+    for (int j = g->per_y ? 0 : 1; j <= (g->per_y ? ny : ny - 1); ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const size_t L = PIDX(g, i, j, k), R = PIDX(g, i, j + 1, k);
+        jac_diff_face(val, n, L, R, 1, 5, DH[L], DH[R], V[L], V[R], g->fv[FVI(g, i, j, k)], rho);
+      }
+  for (int k = g->per_z ? 0 : 1; k <= (g->per_z ? nz : nz - 1); ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const size_t L = PIDX(g, i, j, k), R = PIDX(g, i, j, k + 1);
+        jac_diff_face(val, n, L, R, 0, 6, DV[L], DV[R], V[L], V[R], g->fw[FWI(g, i, j, k)], rho);
+      }
 }
 
 void ora_jac(const ora_geom *g, const double *rho, const double *uf, const double *vf, const double *wf,
@@ -401,6 +576,7 @@ void ora_jac(const ora_geom *g, const double *rho, const double *uf, const doubl
         jac_face(val, n, iL, iR, 0, 6, wf[WFI(g, i, j, nz)], g->fw[FWI(g, i, j, nz)], V[iL] + EPS, V[iR] + EPS, rho[iL], rho[iR]);
       }
   }
+  if (g->dh && g->jac_diff) jac_diffusion(g, rho, val);
   /* JacScaleCompute fold (no side is outflow): Function_Mod.f90:1791-1856 */
   for (int k = 1; k <= nz; ++k)
     for (int j = 1; j <= ny; ++j) {

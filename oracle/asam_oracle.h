@@ -18,6 +18,11 @@ typedef struct {
    * 0 none, 1 ZeroGrad, 2 ZeroValue; bc[6*ic + side].  NULL = ZeroGrad
    * everywhere, the default BCMetVec (MODULE/BoundaryCond_Mod.f90:240-247). */
   const int *bc;
+  /* diffusion coefficients (DH horizontal, DV vertical; padded cell fields,
+   * the reference's DiffKoeff) or NULL: no diffusion.  jac_diff: add the
+   * diffusion Jacobian (JacDiffusion) to the stage matrix. */
+  const double *dh, *dv;
+  int jac_diff;
 } ora_geom;
 
 #define NXP(g) ((g)->nx + 2)
@@ -38,6 +43,7 @@ void ora_bound_cond(const ora_geom *g, int ncomp, int comp0, double *c);
 void ora_exchange_flux(const ora_geom *g, int ncomp, double *f);
 void ora_advection(const ora_geom *g, const double *c, const double *rho, const double *uf, const double *vf,
                    const double *wf, double *f);
+void ora_diffusion(const ora_geom *g, int ncomp, int rho_pos, const double *c, double *f);
 void ora_jac(const ora_geom *g, const double *rho, const double *uf, const double *vf, const double *wf,
              double beta0, double dt, double *val);
 void ora_bicgstab(const ora_geom *g, int ncomp, const double *val, double *x, const double *b, int *maxiter,

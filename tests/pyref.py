@@ -397,3 +397,67 @@ def momentum_sources(geo, p, rho, dx, dy, dz, grav=9.81):
     bu[0][1:] = -rl * grav
     bu[1][:-1] = -rl * grav
     return pg, bu
+
+
+def diffusion(geo, c, rho, dh, dv):
+    """DiffusionCompute (ADVECT/Diffusion_Mod.f90:11-275) for one component
+    on the padded box, in gather form: each cell sums its face fluxes in the
+    reference's order (x left, x right, y left, y right, z left, z right),
+    then f*VolC/(VolC+Eps).  Periodic sides carry half a flux from each side
+    (the halo cells receive theirs); walls use the interior coefficient."""
+    g = geo.grid
+    nx, ny, nz = g.nx, g.ny, g.nz
+    V = geo.volc
+    phi = c / (rho + EPS)
+    f = np.zeros_like(c)
+
+    def face(axis):
+        # coefficient arrays of the faces 0..n along axis between padded cells (f, f+1)
+        per = (g.periodic_x, g.periodic_y, g.periodic_z)[axis]
+        D = dv if axis == 2 else dh
+        if axis == 0:
+            F = geo.fu[:, :, 1:nx + 2]
+            sl = lambda a, o: a[1:-1, 1:-1, o:o + nx + 1]
+        elif axis == 1:
+            F = geo.fv[:, 1:ny + 2, :]
+            sl = lambda a, o: a[1:-1, o:o + ny + 1, 1:-1]
+        else:
+            F = geo.fw[1:nz + 2]
+            sl = lambda a, o: a[o:o + nz + 1, 1:-1, 1:-1]
+        VL, VR, DL, DR = sl(V, 0), sl(V, 1), sl(D, 0), sl(D, 1)
+        dfm = (DL * VR + DR * VL) / (VL + VR + EPS)
+        npax = 2 - axis  # numpy axis of the face direction (arrays are (z, y, x))
+        n = F.shape[npax]
+        idx = np.arange(n).reshape([-1 if a == npax else 1 for a in range(3)])
+        if per:
+            DR_ = dfm
+            two = np.where((idx >= 1) & (idx <= n - 2), 2.0, 1.0)
+        else:
+            DR_ = np.where(idx == 0, DR, np.where(idx == n - 1, DL, dfm))
+            two = 2.0
+        flux = two * DR_ * F * F / (VL + VR + EPS) * (sl(phi, 1) - sl(phi, 0))
+        return flux, per
+
+    out = f.copy()
+    I = (slice(1, -1),) * 3
+    fx, px = face(0)
+    fy, py = face(1)
+    fz, pz = face(2)
+    a = out[I]
+    a = a - fx[:, :, :-1]
+    a = a + fx[:, :, 1:]
+    a = a - fy[:, :-1, :]
+    a = a + fy[:, 1:, :]
+    a = a - fz[:-1]
+    a = a + fz[1:]
+    out[I] = a
+    if px:
+        out[1:-1, 1:-1, 0] += fx[:, :, 0]
+        out[1:-1, 1:-1, -1] -= fx[:, :, -1]
+    if py:
+        out[1:-1, 0, 1:-1] += fy[:, 0, :]
+        out[1:-1, -1, 1:-1] -= fy[:, -1, :]
+    if pz:
+        out[0, 1:-1, 1:-1] += fz[0]
+        out[-1, 1:-1, 1:-1] -= fz[-1]
+    return out * V / (V + EPS)
