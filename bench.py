@@ -69,6 +69,9 @@ def parse():
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--no-projection", action="store_true")
     p.add_argument("--no-dyn", action="store_true", help="skip the dynamical-core step")
+    p.add_argument("--no-diffusion", action="store_true", help="skip the diffusion cost")
+    p.add_argument("--diffusion-only", action="store_true",
+                   help="only the diffusion section (profiling); prints its JSON object")
     p.add_argument("--dyn-only", action="store_true",
                    help="only the dynamical-core section (profiling); prints its JSON object")
     p.add_argument("--probe", choices=["psolve", "inner_psolve"],
@@ -569,6 +572,51 @@ def dyn_bench(a, torch, stream):
     }
 
 
+def diffusion_bench(a, torch, stream):
+    """Cost of the diffusion terms on the bench workload (faces of zero-volume
+    cells closed, seeded density-weighted diffusivities 50 / 5 m^2/s decaying
+    with height): the flux right-hand side with and without diffusion, and the
+    FP64 Rosenbrock step with diffusion and its Jacobian."""
+    import copy
+    import ctypes as C
+
+    import asam_gb300
+    from asam_gb300 import geometry as G
+
+    geo, vel, st = workload(a.nx, a.ny, a.nz)
+    geo = G.close_dead_faces(copy.deepcopy(geo))
+    dh, dv = G.diffusion_coefficients(geo, st.c[0], seed=5)
+    blk = asam_gb300.TransportBlock(geo, st.c.shape[0], method="RosRK3", bicgstab_tol=a.tol)
+    blk.set_stream(stream.cuda_stream)
+    blk.set_velocity(*vel)
+    lib = blk.lib
+    c = torch.from_numpy(st.c).cuda()
+    f = torch.empty_like(c)
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    fcn = lambda: lib.asam_fcn(blk.h, P(c), P(f))  # noqa: E731
+    fcn()
+    ms_plain = time_region(torch, stream, fcn, 3) / 3
+    blk.set_diffusion(dh, dv)
+    fcn()
+    ms_diff = time_region(torch, stream, fcn, 3) / 3
+    it = (C.c_int * 4)()
+    rs = (C.c_double * 4)()
+
+    def step():
+        rc = lib.asam_ros_step(blk.h, P(c), a.dt, it, rs)
+        if rc not in (0, 1, 2):
+            raise RuntimeError(f"asam_ros_step: {rc}")
+
+    step()
+    ms_step = time_region(torch, stream, step, 2) / 2
+    blk.close()
+    return {"workload": f"bench grid {a.nx}x{a.ny}x{a.nz}, zero-volume cells' faces closed, DiffKoeff 50/5 m^2/s x Rho "
+                        "decaying with height, +-20 % seeded", "flux_rhs_ms": ms_diff, "flux_rhs_ms_without": ms_plain,
+            "flux_rhs_diffusion_overhead": ms_diff / ms_plain - 1.0, "ms_per_step": ms_step,
+            "value": a.nx * a.ny * a.nz / (ms_step * 1e-3) / 1e6, "metric": METRIC,
+            "krylov_iterations": list(it[:3])}
+
+
 def batch_members(n, seed=4):
     """Ensemble of independent cut-cell domains: sizes between 64x64x48 and
     192x160x96, Gaussian hill 0-1.5 km high with half-width 2-8 km, u 5-15 m/s,
@@ -714,6 +762,16 @@ def main():
         print(json.dumps({"probe": a.probe, "rc": rc, "launches": blk.lib.asam_launch_count() - n0,
                           "npad": (a.nx + 2) * (a.ny + 2) * (a.nz + 2), "ncomp": st.c.shape[0]}), flush=True)
         blk.close()
+        return
+    if a.diffusion_only:
+        import torch
+
+        import __graft_entry__
+
+        __graft_entry__.build()
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        print(json.dumps(diffusion_bench(a, torch, stream)), flush=True)
         return
     if a.dyn_only:
         import torch
@@ -862,6 +920,9 @@ def main():
     dyn = None
     if not a.no_dyn and world == 1:
         dyn = dyn_bench(a, torch, stream)
+    diff = None
+    if not a.no_diffusion and world == 1:
+        diff = diffusion_bench(a, torch, stream)
     if "fp64" not in results:  # a profiling run of one variant: no comparison line
         rr = results[precs[0]]
         if rank == 0:
@@ -974,6 +1035,8 @@ def main():
         line["projection"] = proj
     if dyn is not None:
         line["dyn"] = dyn
+    if diff is not None:
+        line["diffusion"] = diff
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if rank == 0:
