@@ -21,6 +21,7 @@ STATUS = {
     4: "ASAM_BAD_ARG",
     5: "ASAM_CUDA_ERROR",
     6: "ASAM_NO_DEVICE",
+    7: "ASAM_IO_ERROR",
 }
 ASAM_OK, ASAM_NOT_CONVERGED, ASAM_BREAKDOWN = 0, 1, 2
 
@@ -50,6 +51,15 @@ class AsamDynConfig(C.Structure):
         ("mom_pos", C.c_int * 6), ("pgradient", C.c_int), ("buoyancy", C.c_int), ("free_slip", C.c_int),
         ("wall_no_slip", C.c_int), ("grav", C.c_double),
     ]
+
+
+class AsamRestartHeader(C.Structure):
+    _fields_ = [("time", C.c_double), ("gmv_step", C.c_int), ("output_time", C.c_double)]
+
+
+class AsamRestartBlock(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("ncomp", C.c_int), ("nfrac", C.c_int),
+                ("c", C.c_void_p), ("uf", C.c_void_p), ("vf", C.c_void_p), ("wf", C.c_void_p)]
 
 
 # (name, restype, argtypes) of every exported entry point of include/asam_gb300.h
@@ -119,6 +129,10 @@ SIGNATURES = [
     ("asam_npad", C.c_longlong, [C.POINTER(AsamConfig)]),
     ("asam_probe_fp64_fma", C.c_int, [C.c_int, _D]),
     ("asam_launch_count", C.c_longlong, []),
+    ("asam_restart_write", C.c_int, [C.c_char_p, C.POINTER(AsamRestartHeader), C.c_int, C.POINTER(AsamRestartBlock)]),
+    ("asam_restart_read", C.c_int, [C.c_char_p, C.POINTER(AsamRestartHeader), C.c_int, C.POINTER(AsamRestartBlock)]),
+    ("asam_restart_file_name", C.c_int, [C.c_char_p, C.c_int, C.c_char_p, C.c_int]),
+    ("asam_restart_set_max_subrecord", C.c_int, [C.c_longlong]),
     ("asam_probe_div", C.c_int, [C.c_longlong, C.c_longlong, C.c_int, C.POINTER(C.c_longlong)]),
     ("asam_last_error", C.c_char_p, []),
 ]

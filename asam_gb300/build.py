@@ -50,6 +50,7 @@ UNITS = {
     "step_graph.cu": ["-fmad=false"],
     "proj.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "dyn.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    "restart.cu": [],
 }
 
 

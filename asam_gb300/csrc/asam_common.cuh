@@ -183,6 +183,7 @@ enum Status {
   kBadArg = 4,
   kCudaError = 5,
   kNoDevice = 6,
+  kIoError = 7,
 };
 
 }  // namespace asam

@@ -70,6 +70,8 @@ def parse():
     p.add_argument("--no-projection", action="store_true")
     p.add_argument("--no-dyn", action="store_true", help="skip the dynamical-core step")
     p.add_argument("--no-diffusion", action="store_true", help="skip the diffusion cost")
+    p.add_argument("--no-restart", action="store_true", help="skip the restart-file throughput")
+    p.add_argument("--restart-only", action="store_true", help="only the restart section; prints its JSON object")
     p.add_argument("--diffusion-only", action="store_true",
                    help="only the diffusion section (profiling); prints its JSON object")
     p.add_argument("--dyn-only", action="store_true",
@@ -617,6 +619,49 @@ def diffusion_bench(a, torch, stream):
             "krylov_iterations": list(it[:3])}
 
 
+def restart_bench(a, torch):
+    """Restart file of the bench state (WriteRestart / ReadRestart): the
+    device-resident components and face velocities streamed to a file and
+    back through the pinned staging buffers.  Wall-clock timed: the write
+    ends when the file is closed (page cache, no fsync, like the reference's
+    CLOSE); the read follows it."""
+    import numpy as np
+
+    from asam_gb300 import restart as R
+
+    geo, vel, st = workload(a.nx, a.ny, a.nz)
+    g = geo.grid
+    c = torch.from_numpy(st.c).cuda().reshape(st.c.shape[0], -1)
+    veld = [torch.from_numpy(np.ascontiguousarray(v).ravel()).cuda() for v in vel]
+    blk = R.block(g.nx, g.ny, g.nz, c, *veld)
+    c2 = torch.empty_like(c)
+    vel2 = [torch.empty_like(v) for v in veld]
+    blk2 = R.block(g.nx, g.ny, g.nz, c2, *vel2)
+    nbytes = (c.numel() + sum(v.numel() for v in veld)) * 8
+    d = tempfile.mkdtemp(prefix="asam_restart_")
+    path = os.path.join(d, "Hill.0")
+    try:
+        tw, tr = [], []
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            R.write_restart(path, [blk], 100.0, 1, 0.0)
+            tw.append(time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            R.read_restart(path, [blk2])
+            tr.append(time.perf_counter() - t0)
+        ok = bool(torch.equal(c2, c) and all(torch.equal(x, y) for x, y in zip(vel2, veld)))
+        fsize = os.path.getsize(path)
+    finally:
+        if os.path.exists(path):
+            os.remove(path)
+        os.rmdir(d)
+    return {"workload": f"bench state {g.nx}x{g.ny}x{g.nz}, {st.c.shape[0]} components + face velocities, "
+                        "device-resident, one file", "bytes": nbytes, "file_bytes": fsize,
+            "write_s": min(tw), "read_s": min(tr), "write_gbs": nbytes / min(tw) / 1e9,
+            "read_gbs": nbytes / min(tr) / 1e9, "roundtrip_bitwise": ok}
+
+
 def batch_members(n, seed=4):
     """Ensemble of independent cut-cell domains: sizes between 64x64x48 and
     192x160x96, Gaussian hill 0-1.5 km high with half-width 2-8 km, u 5-15 m/s,
@@ -762,6 +807,14 @@ def main():
         print(json.dumps({"probe": a.probe, "rc": rc, "launches": blk.lib.asam_launch_count() - n0,
                           "npad": (a.nx + 2) * (a.ny + 2) * (a.nz + 2), "ncomp": st.c.shape[0]}), flush=True)
         blk.close()
+        return
+    if a.restart_only:
+        import torch
+
+        import __graft_entry__
+
+        __graft_entry__.build()
+        print(json.dumps(restart_bench(a, torch)), flush=True)
         return
     if a.diffusion_only:
         import torch
@@ -923,6 +976,9 @@ def main():
     diff = None
     if not a.no_diffusion and world == 1:
         diff = diffusion_bench(a, torch, stream)
+    rst = None
+    if not a.no_restart and world == 1:
+        rst = restart_bench(a, torch)
     if "fp64" not in results:  # a profiling run of one variant: no comparison line
         rr = results[precs[0]]
         if rank == 0:
@@ -1037,6 +1093,8 @@ def main():
         line["dyn"] = dyn
     if diff is not None:
         line["diffusion"] = diff
+    if rst is not None:
+        line["restart"] = rst
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if rank == 0:

@@ -29,7 +29,8 @@ typedef enum {
   ASAM_NAN_DETECTED = 3,
   ASAM_BAD_ARG = 4,
   ASAM_CUDA_ERROR = 5,
-  ASAM_NO_DEVICE = 6
+  ASAM_NO_DEVICE = 6,
+  ASAM_IO_ERROR = 7 /* restart file cannot be opened, is short, or its records do not fit the blocks */
 } asam_status;
 
 typedef enum {
@@ -444,6 +445,49 @@ int asam_probe_fp64_fma(int iters, double *gflops);
  * precomputed reciprocal differs from the IEEE quotient (no reference
  * counterpart; guards the bit-exact FP64 path). */
 int asam_probe_div(long long n, long long seed, int span, long long *mismatches);
+
+/* ---- Restart files (INIT/Restart_Mod.f90:14-82) --------------------------
+ * The file of one rank as WriteRestart writes it with gfortran: unformatted
+ * sequential records (4-byte length markers, records above the maximum
+ * subrecord length split into subrecords), REAL 8 bytes, INTEGER 4 bytes:
+ * Time, GMVStep, OutputTime, then per block one record per component
+ * (Vec(ib)%Vec(ic)%c, the padded cell array with its nFrac extent) and one
+ * record holding uF, vF, wF.  Every array may live in device or host memory;
+ * device arrays are staged through pinned buffers. */
+typedef struct {
+  double time;        /* Time */
+  int gmv_step;       /* GetGMVStep() / SetGMVStep */
+  double output_time; /* GetOutputTime() / SetOutputTime */
+} asam_restart_header;
+
+typedef struct {
+  int nx, ny, nz; /* interior cells of the block (ix1-ix0, iy1-iy0, iz1-iz0) */
+  int ncomp;      /* UBOUND(Vec(ibLoc)%Vec,1) */
+  int nfrac;      /* 4th extent of each component's c array; 0 or 1 without size classes */
+  double *c;      /* ncomp arrays of (nx+2)(ny+2)(nz+2)*nfrac values back to back */
+  double *uf;     /* uF(ix0:ix1,iy0+1:iy1,iz0+1:iz1) */
+  double *vf;     /* vF(ix0+1:ix1,iy0:iy1,iz0+1:iz1) */
+  double *wf;     /* wF(ix0+1:ix1,iy0+1:iy1,iz0:iz1) */
+} asam_restart_block;
+
+/* WriteRestart (Restart_Mod.f90:14-43) without its RestartTime test: writes
+ * the file unconditionally; the caller schedules.  Waits for all device work
+ * before reading device arrays. */
+int asam_restart_write(const char *path, const asam_restart_header *hdr, int nblock,
+                       const asam_restart_block *blocks);
+
+/* ReadRestart (Restart_Mod.f90:45-81): fills hdr and the blocks' arrays;
+ * ASAM_IO_ERROR when a record's length differs from the block's array. */
+int asam_restart_read(const char *path, asam_restart_header *hdr, int nblock, const asam_restart_block *blocks);
+
+/* The reference's restart file name for a grid file and rank:
+ * 'RESTART/'//TRIM(FileName(1:INDEX(FileName,'.grid')))//ADJUSTL(rank)
+ * (Restart_Mod.f90:24-27).  cap = size of buf in bytes. */
+int asam_restart_file_name(const char *grid_file, int rank, char *buf, int cap);
+
+/* gfortran's -fmax-subrecord-length for files this library writes (default
+ * and maximum 2147483639 bytes); the reader accepts any split. */
+int asam_restart_set_max_subrecord(long long bytes);
 
 /* Sizes of the padded cell field for a configuration. */
 long long asam_npad(const asam_config *cfg);
