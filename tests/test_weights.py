@@ -1,0 +1,156 @@
+"""Cut-cell geometry files (.Weight2): a hand-written file in the layout
+WriteWeightBlk writes (GRID/OutputWeightBlk_Mod.f90:501-670) read to known
+arrays, written and re-read generated geometries bit for bit, block
+selection, the boundary-cell normals of ReadWeights
+(INIT/ReadWeights_Mod.f90:1283-1319) and the refusals.  Host only."""
+import copy
+
+import numpy as np
+import pytest
+
+from asam_gb300 import geometry as G
+from asam_gb300 import weights as W
+from tests import cases
+
+KNOWN = """ Cart
+           1   ! Number of blocks
+ #.... Block           1 .....................................................
+   0.0000000000000000        0.0000000000000000        0.0000000000000000
+           2
+   100.00000000000000
+   100.00000000000000
+           1
+   50.000000000000000
+           2
+   10.000000000000000
+   20.000000000000000
+           2   NrW_FacesYZ
+           0           1           1
+   0.0000000000000000
+           1           1           1
+   2.5D+02
+           1   NrMP_FacesYZ
+           1           1           1
+   100.0  25.0  5.0
+           1   NrW_FacesZX
+           2          -1           2
+   1.0E3
+           0   NrMP_FacesZX
+           1   NrW_FacesXY
+           1           1           0
+   0.0000000000000000
+           0   NrMP_FacesXY
+           2    NrW_Cells
+           1           1           1
+   2.0D4
+           2           1           2
+   1.25E5
+           1      NrB_Cells     3   Struct_Bound     0  Nr_SoilLayers
+           1           1           1
+   50.0 25.0 2.0
+  0.1000000D+00  0.8000000D-01  0.8000000D+00  0.5000000D+02  0.2500000D+02  0.2000000D+01
+"""
+
+
+def test_known_file(tmp_path):
+    p = tmp_path / "known.Weight2"
+    p.write_text(KNOWN)
+    b = W.read_weight2(str(p), expect=(2, 1, 2))
+    g = b.geo
+    assert (g.grid.nx, g.grid.ny, g.grid.nz) == (2, 1, 2)
+    assert g.grid.dx == 100.0 and g.grid.dy == 50.0 and np.array_equal(g.grid.dz, [10.0, 20.0])
+    fu, fv, fw, vol = W.default_weights([100.0, 100.0], [50.0], [10.0, 20.0])
+    fu[0, 0, 1] = 0.0  # FU(0,1,1)
+    fu[0, 0, 2] = 250.0  # FU(1,1,1)
+    fv[1, 0, 1] = 1000.0  # FV(2,-1,2)
+    fw[1, 0, 0] = 0.0  # FW(1,1,0)
+    vol[1, 1, 1] = 2.0e4  # VolC(1,1,1)
+    vol[2, 1, 2] = 1.25e5  # VolC(2,1,2)
+    for got, exp in ((g.fu, fu), (g.fv, fv), (g.fw, fw), (g.volc, vol)):
+        assert np.array_equal(got, exp)
+    # the untouched defaults: full faces, interior volumes, periodic halos
+    assert g.fu[1, 0, 4] == 50.0 * 20.0 and g.fw[3, 0, 1] == 100.0 * 50.0
+    assert g.volc[1, 1, 2] == 100.0 * 50.0 * 10.0 and g.volc[1, 1, 0] == 100.0 * 50.0 * 10.0
+    assert g.volc[0, 1, 1] == 100.0 * 50.0 * 10.0 and g.volc[0, 0, 0] == 1.0
+    mi, mx = b.mid_faces[0]
+    assert mi.tolist() == [[1, 1, 1]] and mx.tolist() == [[100.0, 25.0, 5.0]]
+    bc = b.bound
+    assert bc.ijk.tolist() == [[1, 1, 1]] and bc.xs.tolist() == [[50.0, 25.0, 2.0]]
+    assert np.allclose(bc.surf, [[0.1, 0.08, 0.8, 50.0, 25.0, 2.0]])
+    # normal of cell (1,1,1): FU(1)-FU(0) = 250 - 0, FV(1,1)-FV(1,0) = 0,
+    # FW(1,1,1)-FW(1,1,0) = 5000 - 0
+    n = np.array([250.0, 0.0, 5000.0])
+    fl = np.sqrt((n * n).sum())
+    assert np.allclose(bc.normal[0], n / fl, rtol=0, atol=1e-15) and bc.fl[0] == fl
+    with pytest.raises(ValueError, match="nx"):
+        W.read_weight2(str(p), expect=(3, 1, 2))
+
+
+@pytest.mark.parametrize("name", ["hill_24x20x16", "bubble_12x10x8", "hill_odd_13x7x9_reverse"])
+def test_round_trip_generated(tmp_path, name):
+    geo, _, _ = cases.get(name)
+    p = tmp_path / "case.Weight2"
+    W.write_weight2(str(p), [geo])
+    b = W.read_weight2(str(p), expect=(geo.grid.nx, geo.grid.ny, geo.grid.nz))
+    for a in ("fu", "fv", "fw", "volc"):
+        assert np.array_equal(getattr(b.geo, a), getattr(geo, a)), a
+    assert np.array_equal(b.geo.grid.dz, geo.grid.dz)
+    assert (b.geo.grid.dx, b.geo.grid.dy) == (geo.grid.dx, geo.grid.dy)
+    assert np.array_equal(b.bound.ijk, G.boundary_cells(geo))
+    assert b.bound.surf.shape == (len(b.bound.ijk), 6)
+    norm = np.linalg.norm(b.bound.normal, axis=1)
+    assert np.allclose(norm, 1.0)
+    # the file lists only what differs from the reader's defaults
+    text = p.read_text()
+    assert text.startswith(" Cart\n")
+
+
+def test_two_blocks_and_closed_faces(tmp_path):
+    g0, _, _ = cases.get("hill_24x20x16")
+    g1 = G.close_dead_faces(copy.deepcopy(g0))
+    p = tmp_path / "two.Weight2"
+    W.write_weight2(str(p), [g0, (g1, (2400.0, 0.0, 0.0), None)])
+    b1 = W.read_weight2(str(p), ib=2)
+    assert b1.origin == (2400.0, 0.0, 0.0)
+    for a in ("fu", "fv", "fw", "volc"):
+        assert np.array_equal(getattr(b1.geo, a), getattr(g1, a))
+    b0 = W.read_weight2(str(p), ib=1)
+    assert np.array_equal(b0.geo.fw, g0.fw)
+    with pytest.raises(ValueError):
+        W.read_weight2(str(p), ib=3)
+
+
+def test_walls_change_the_halo_defaults(tmp_path):
+    geo, _, _ = cases.get("hill_24x20x16")
+    p = tmp_path / "w.Weight2"
+    W.write_weight2(str(p), [geo], periodic=(False, False, False))
+    b = W.read_weight2(str(p), periodic=(False, False, False))
+    assert np.array_equal(b.geo.volc, geo.volc)
+    fu, fv, fw, vol = W.default_weights(np.full(3, 2.0), np.full(2, 3.0), np.array([1.0, 4.0]), (False, False, False))
+    assert vol[1, 1, 0] == 2.0 * 3.0 * 1.0 and vol[2, 1, 1] == 2.0 * 3.0 * 4.0 and vol[3, 1, 1] == 2.0 * 3.0 * 4.0
+
+
+def test_list_directed_reader():
+    rd = W._ListReader(["1, 2 3*4.5D0 rest", "7 8", "9 / 10", "11"])
+    assert rd.values(2) == ["1", "2"]  # the rest of the line is dropped
+    assert rd.ints(2) == [7, 8]
+    with pytest.raises(ValueError):
+        rd.values(2)  # '/' ends the read
+    rd = W._ListReader(["2*1.5d+01 x"])
+    assert rd.reals(2) == [15.0, 15.0]
+
+
+def test_refusals(tmp_path):
+    p = tmp_path / "g.Weight2"
+    p.write_text(" Globe\n 1\n")
+    with pytest.raises(NotImplementedError):
+        W.read_weight2(str(p))
+    p.write_text(KNOWN.replace("3   Struct_Bound", "5   Struct_Bound"))
+    with pytest.raises(NotImplementedError):
+        W.read_weight2(str(p))
+    p.write_text(KNOWN.replace("           2          -1           2", "           2          -3           2"))
+    with pytest.raises(ValueError):
+        W.read_weight2(str(p))
+    p.write_text(KNOWN[:400])
+    with pytest.raises(ValueError):
+        W.read_weight2(str(p))
