@@ -528,6 +528,25 @@ def Solve_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, b: np.ndarray) -> np.n
     return x
 
 
+def Solve_TB_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Block Thomas solve of TriDiagTB (2x2 blocks) on a batch of columns:
+    d (ncol,n1,4), u,l (ncol,n1-1,4) with blocks column-major, b (ncol,n1,2)."""
+    lib = _lib.load()
+    d, u, l, x = _f64(d), _f64(u), _f64(l), _f64(b).copy()
+    ncol, n1 = d.shape[:2]
+    check(lib.asam_tri_tb_solve(ncol, n1, ptr(d), ptr(u), ptr(l), ptr(x)), "asam_tri_tb_solve")
+    return x
+
+
+def MatVecTB_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, x: np.ndarray) -> np.ndarray:
+    lib = _lib.load()
+    d, u, l, xx = _f64(d), _f64(u), _f64(l), _f64(x)
+    ncol, n1 = d.shape[:2]
+    y = np.empty_like(xx)
+    check(lib.asam_tri_tb_matvec(ncol, n1, ptr(d), ptr(u), ptr(l), ptr(xx), ptr(y)), "asam_tri_tb_matvec")
+    return y
+
+
 def MatVecT_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, x: np.ndarray) -> np.ndarray:
     lib = _lib.load()
     d, u, l, xx = _f64(d), _f64(u), _f64(l), _f64(x)

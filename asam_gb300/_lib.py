@@ -100,6 +100,8 @@ SIGNATURES = [
      [_V, _V, C.c_int, C.c_int, C.c_double, C.c_int, _V, C.c_double, _D, _V, _V, _V, _V, _V]),
     ("asam_tri_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
+    ("asam_tri_tb_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
+    ("asam_tri_tb_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_proj_setup", C.c_int, [_V, C.POINTER(AsamProjConfig), _V, _V, _V, _V]),
     ("asam_proj_weights", C.c_int, [_V, _V, _V, _V, _V, _V, _V, _V, _V]),

@@ -33,7 +33,8 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libasam_gb300.so"
-ORACLE_SRC = [ROOT / "oracle" / "asam_oracle.c", ROOT / "oracle" / "asam_proj.c", ROOT / "oracle" / "asam_dyn.c"]
+ORACLE_SRC = [ROOT / "oracle" / "asam_oracle.c", ROOT / "oracle" / "asam_proj.c", ROOT / "oracle" / "asam_dyn.c",
+              ROOT / "oracle" / "asam_tritb.c"]
 ORACLE_DEPS = ORACLE_SRC + [ROOT / "oracle" / "asam_oracle.h"]
 ORACLE_LIB = ROOT / "oracle" / "_build" / "libasam_oracle.so"
 
@@ -51,6 +52,7 @@ UNITS = {
     "proj.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "dyn.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "restart.cu": [],
+    "tritb.cu": ["-fmad=false"],
 }
 
 

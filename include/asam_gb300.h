@@ -446,6 +446,18 @@ int asam_probe_fp64_fma(int iters, double *gflops);
  * counterpart; guards the bit-exact FP64 path). */
 int asam_probe_div(long long n, long long seed, int span, long long *mismatches);
 
+/* Batched block-tridiagonal column solve of the density/buoyancy-coupled
+ * line preconditioner (MultiTriTB): Solve_1D of MULTI/TriDiagTB_Mod.f90:143-163,
+ * a Thomas elimination with 2x2 blocks (Div_2, Div_22, Mult_2, Mult_22 of
+ * CG/Matrix_Mod.f90), over ncol independent columns of n1 levels.
+ * d[(col*n1+i)*4 + r+2c] = A%d(r+1,c+1,i+1); u, l[(col*(n1-1)+i)*4 + r+2c];
+ * b[(col*n1+i)*2 + r] overwritten by the solution.  Host or device pointers. */
+int asam_tri_tb_solve(int ncol, int n1, const double *d, const double *u, const double *l, double *b);
+
+/* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141). */
+int asam_tri_tb_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x,
+                       double *y);
+
 /* ---- Restart files (INIT/Restart_Mod.f90:14-82) --------------------------
  * The file of one rank as WriteRestart writes it with gfortran: unformatted
  * sequential records (4-byte length markers, records above the maximum

@@ -58,6 +58,8 @@ def load() -> C.CDLL:
             "ora_ros_step": (I, [G, I, I, V, V, V, V, D, I, D, I, I, V, V]),
             "ora_total_scalar": (D, [G, V]),
             "ora_tri_solve": (None, [I, I, V, V, V, V]),
+            "ora_tri_tb_solve": (None, [I, I, V, V, V, V, V]),
+            "ora_tri_tb_matvec": (None, [I, I, V, V, V, V, V]),
             "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
         }
         sig.update({
@@ -327,6 +329,28 @@ def tri_matvec(d, u, l, x):
     ncol, n1 = d.shape
     y = np.empty_like(xx)
     lib.ora_tri_matvec(ncol, n1, _p(d), _p(u), _p(l), _p(xx), _p(y))
+    return y
+
+
+def tri_tb_solve(d, u, l, b):
+    """Solve_1D of MULTI/TriDiagTB_Mod.f90:143-163 on columns: d (ncol, n1, 4),
+    u/l (ncol, n1-1, 4) with 2x2 blocks column-major, b (ncol, n1, 2)."""
+    lib = load()
+    d, u, l = (np.ascontiguousarray(a, dtype=np.float64) for a in (d, u, l))
+    x = np.ascontiguousarray(b, dtype=np.float64).copy()
+    ncol, n1 = d.shape[:2]
+    w = np.empty(max(n1 - 1, 1) * 4)
+    lib.ora_tri_tb_solve(ncol, n1, _p(d), _p(u), _p(l), _p(x), _p(w))
+    return x
+
+
+def tri_tb_matvec(d, u, l, x):
+    """MatVecTB_1D of MULTI/TriDiagTB_Mod.f90:121-141 on columns."""
+    lib = load()
+    d, u, l, xx = (np.ascontiguousarray(a, dtype=np.float64) for a in (d, u, l, x))
+    ncol, n1 = d.shape[:2]
+    y = np.empty_like(xx)
+    lib.ora_tri_tb_matvec(ncol, n1, _p(d), _p(u), _p(l), _p(xx), _p(y))
     return y
 
 

