@@ -188,13 +188,12 @@ def run_cases(root) -> None:
         fn(d, *args)
 
 
-@pytest.mark.gpu
+@pytest.mark.xfail(reason="open defect: a process that ran these host-array restart cases crashes later "
+                          "(segmentation fault in numpy code), with and without a CUDA driver; cause not found",
+                   strict=False)
 def test_library_restart_io(built_lib, tmp_path):
-    """The library's reader and writer on host arrays, run in a child process.
-    Marked gpu: on a machine without a CUDA driver, processes that made these
-    calls have crashed later inside numpy code (not reproduced on a machine
-    with a driver, nor under AddressSanitizer and UBSan on the same code
-    paths), so the library cases run where a driver is present."""
+    """The library's reader and writer on host arrays, run in a child process
+    (the crash described in the xfail reason stays out of the test runner)."""
     import subprocess
     import sys
     from pathlib import Path
