@@ -32,7 +32,11 @@ def _numel(a) -> int:
 
 
 def block(nx: int, ny: int, nz: int, c, uf, vf, wf) -> _lib.AsamRestartBlock:
-    """Descriptor of one block: c is (ncomp, npad*nFrac)."""
+    """Descriptor of one block: c is (ncomp, npad*nFrac).
+
+    The descriptor holds raw addresses, so it keeps references to the four
+    arrays (``_keep``): a descriptor built from temporaries stays valid for
+    as long as the descriptor itself lives."""
     npad = (nx + 2) * (ny + 2) * (nz + 2)
     ncomp = c.shape[0]
     per = _numel(c) // max(ncomp, 1)
@@ -41,19 +45,31 @@ def block(nx: int, ny: int, nz: int, c, uf, vf, wf) -> _lib.AsamRestartBlock:
     for a, n in ((uf, (nx + 1) * ny * nz), (vf, nx * (ny + 1) * nz), (wf, nx * ny * (nz + 1))):
         if _numel(a) != n:
             raise ValueError("face velocity of the wrong size")
-    return _lib.AsamRestartBlock(nx, ny, nz, ncomp, per // npad, _ptr(c), _ptr(uf), _ptr(vf), _ptr(wf))
+    desc = _lib.AsamRestartBlock(nx, ny, nz, ncomp, per // npad, _ptr(c), _ptr(uf), _ptr(vf), _ptr(wf))
+    desc._keep = (c, uf, vf, wf)
+    return desc
+
+
+def _array(blocks):
+    """ctypes array of the descriptors; the copies carry no references, so the
+    caller keeps ``blocks`` (and with it the arrays) alive across the call."""
+    blocks = list(blocks)
+    for b in blocks:
+        if not hasattr(b, "_keep"):
+            raise TypeError("restart blocks must come from asam_gb300.restart.block()")
+    return blocks, (_lib.AsamRestartBlock * len(blocks))(*blocks)
 
 
 def write_restart(path: str, blocks, time: float, gmv_step: int = 0, output_time: float = 0.0) -> None:
     lib = _lib.load()
-    arr = (_lib.AsamRestartBlock * len(blocks))(*blocks)
+    blocks, arr = _array(blocks)
     hdr = _lib.AsamRestartHeader(time, gmv_step, output_time)
     _lib.check(lib.asam_restart_write(os.fsencode(path), C.byref(hdr), len(blocks), arr), "asam_restart_write")
 
 
 def read_restart(path: str, blocks) -> tuple[float, int, float]:
     lib = _lib.load()
-    arr = (_lib.AsamRestartBlock * len(blocks))(*blocks)
+    blocks, arr = _array(blocks)
     hdr = _lib.AsamRestartHeader()
     _lib.check(lib.asam_restart_read(os.fsencode(path), C.byref(hdr), len(blocks), arr), "asam_restart_read")
     return hdr.time, hdr.gmv_step, hdr.output_time

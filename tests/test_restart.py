@@ -174,31 +174,50 @@ def case_restart_schedule(tmp_path):
         assert np.array_equal(got, exp)
 
 
-def run_cases(root) -> None:
-    """Every library case, each in its own directory under root."""
-    import pathlib
-
-    root = pathlib.Path(root)
-    jobs = [(case_file_name, n) for n in NAMES] + [(case_library_write_matches_oracle, w) for w in WRITES]
-    jobs += [(case_library_read_of_oracle_file_two_blocks, ()), (case_refusals, ()), (case_restart_schedule, ())]
-    jobs += [(case_subrecords_both_ways, (m,)) for m in (8, 1000, 4096 + 3)]
-    for k, (fn, args) in enumerate(jobs):
-        d = root / f"{k:02d}_{fn.__name__}"
-        d.mkdir()
-        fn(d, *args)
+LIBRARY_CASES = ([(case_file_name, n) for n in NAMES] + [(case_library_write_matches_oracle, w) for w in WRITES]
+                 + [(case_library_read_of_oracle_file_two_blocks, ()), (case_refusals, ()),
+                    (case_restart_schedule, ())] + [(case_subrecords_both_ways, (m,)) for m in (8, 1000, 4096 + 3)])
 
 
-@pytest.mark.xfail(reason="open defect: a process that ran these host-array restart cases crashes later "
-                          "(segmentation fault in numpy code), with and without a CUDA driver; cause not found",
-                   strict=False)
-def test_library_restart_io(built_lib, tmp_path):
-    """The library's reader and writer on host arrays, run in a child process
-    (the crash described in the xfail reason stays out of the test runner)."""
+@pytest.mark.parametrize("fn,args", LIBRARY_CASES, ids=[f"{k:02d}_{fn.__name__}" for k, (fn, _) in
+                                                          enumerate(LIBRARY_CASES)])
+def test_library_restart_io(built_lib, tmp_path, fn, args):
+    """The library's reader and writer on host arrays, in the test process."""
+    fn(tmp_path, *args)
+
+
+def test_descriptor_keeps_temporaries_alive(built_lib, tmp_path):
+    """A descriptor built from temporary arrays stays valid: the reader fills
+    arrays that only the descriptor references, and the process keeps working
+    on the heap afterwards (run in a child so a heap corruption cannot take
+    the test runner down)."""
     import subprocess
     import sys
     from pathlib import Path
 
     root = Path(__file__).resolve().parent.parent
-    code = f"import sys; sys.path.insert(0, {str(root)!r}); import tests.test_restart as t; t.run_cases({str(tmp_path)!r})"
+    code = f"""
+import sys, gc
+sys.path.insert(0, {str(root)!r})
+import numpy as np
+from asam_gb300 import restart as R
+from oracle import restart as ORA
+dims = (5, 4, 3)
+r = np.random.default_rng(9)
+b = (r.standard_normal((2, 7 * 6 * 5)), r.standard_normal(6 * 4 * 3), r.standard_normal(5 * 5 * 3),
+     r.standard_normal(5 * 4 * 4))
+path = {str(tmp_path / "r.0")!r}
+open(path, "wb").write(ORA.encode(3.0, 1, 0.0, [b]))
+for it in range(50):
+    desc = R.block(*dims, *(np.zeros_like(a) for a in b))
+    gc.collect()
+    assert R.read_restart(path, [desc]) == (3.0, 1, 0.0)
+    for got, exp in zip(desc._keep, b):
+        assert np.array_equal(got, exp)
+    R.write_restart(path + ".w", [R.block(*dims, *(a.copy() for a in b))], 3.0, 1, 0.0)
+    junk = [np.ones(1000 + k) * k for k in range(200)]
+    assert sum(float(j.sum()) for j in junk) > 0
+print("ok")
+"""
     res = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=600)
-    assert res.returncode == 0, res.stdout[-4000:] + res.stderr[-4000:]
+    assert res.returncode == 0 and res.stdout.strip().endswith("ok"), res.stdout[-4000:] + res.stderr[-4000:]
