@@ -256,11 +256,11 @@ def closed_hill_case(nx: int, ny: int, nz: int, seed: int = 4, height: float = 6
 
 
 def projection_inputs(geo: Geometry, seed: int = 3, amp: float = 1.0):
-    """Seeded inputs of the pressure projection of a closed block: the sound
+    """Seeded inputs of the pressure projection of a block: the sound
     weights of WeightDiagCompute (DTU ~ potential temperature at the faces
     ~300 K, DUT ~ dp/d(rho theta) ~400, DUU = F/(F+Eps), DTT = 1), the cell
     widths, and a face-velocity increment of amplitude amp that vanishes on the
-    walls.  Returns (weights, dx, dy, dz, (u, v, w)); weights in the order
+    walls (a periodic side's two copies of one face get equal values).  Returns (weights, dx, dy, dz, (u, v, w)); weights in the order
     DTU, DTV, DTW, DUU, DUV, DUW, DUT, DTT with uF/vF/wF extents and interior
     cell shapes (nz, ny, nx)."""
     g = geo.grid
@@ -276,16 +276,30 @@ def projection_inputs(geo: Geometry, seed: int = 3, amp: float = 1.0):
     dtw = 300.0 + 5.0 * rng.standard_normal(fw.shape)
     dut = 400.0 + 10.0 * rng.standard_normal((nz, ny, nx))
     dtt = np.ones((nz, ny, nx))
-    weights = [np.ascontiguousarray(a) for a in (dtu, dtv, dtw, duu, duv, duw, dut, dtt)]
     dx = np.full(nx, g.dx)
     dy = np.full(ny, g.dy)
     dz = np.asarray(g.dz, dtype=np.float64).copy()
     u = amp * rng.standard_normal(fu.shape) * (fu > 0)
     v = amp * rng.standard_normal(fv.shape) * (fv > 0)
     w = amp * rng.standard_normal(fw.shape) * (fw > 0)
-    u[:, :, 0] = u[:, :, nx] = 0.0
-    v[:, 0, :] = v[:, ny, :] = 0.0
-    w[0] = w[nz] = 0.0
+    # a periodic side is one face stored twice (first and last): same
+    # velocity and weights on both; a closed side has no normal flow
+    if g.periodic_x:
+        u[:, :, nx] = u[:, :, 0]
+        dtu[:, :, nx] = dtu[:, :, 0]
+    else:
+        u[:, :, 0] = u[:, :, nx] = 0.0
+    if g.periodic_y:
+        v[:, ny, :] = v[:, 0, :]
+        dtv[:, ny, :] = dtv[:, 0, :]
+    else:
+        v[:, 0, :] = v[:, ny, :] = 0.0
+    if g.periodic_z:
+        w[nz] = w[0]
+        dtw[nz] = dtw[0]
+    else:
+        w[0] = w[nz] = 0.0
+    weights = [np.ascontiguousarray(a) for a in (dtu, dtv, dtw, duu, duv, duw, dut, dtt)]
     return weights, dx, dy, dz, tuple(np.ascontiguousarray(a) for a in (u, v, w))
 
 
@@ -304,9 +318,9 @@ def boundary_cells(geo: Geometry) -> np.ndarray:
 
 
 def closed_face_velocity(geo: Geometry, amp: float, seed: int = 0) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
-    """Seeded smooth face velocities of a closed block: amplitude amp, zero on
-    the six walls and on closed faces.  uF (nz, ny, nx+1), vF (nz, ny+1, nx),
-    wF (nz+1, ny, nx)."""
+    """Seeded smooth face velocities of a block: amplitude amp, zero on the
+    walls and on closed faces, equal on the two copies of a periodic side's
+    face.  uF (nz, ny, nx+1), vF (nz, ny+1, nx), wF (nz+1, ny, nx)."""
     g = geo.grid
     nx, ny, nz = g.nx, g.ny, g.nz
     rng = np.random.default_rng(seed)
@@ -323,23 +337,36 @@ def closed_face_velocity(geo: Geometry, amp: float, seed: int = 0) -> tuple[np.n
     u = amp * smooth(fu.shape) * (fu > 0)
     v = amp * smooth(fv.shape) * (fv > 0)
     w = 0.3 * amp * smooth(fw.shape) * (fw > 0)
-    u[:, :, 0] = u[:, :, nx] = 0.0
-    v[:, 0, :] = v[:, ny, :] = 0.0
+    # a periodic side stores one face twice (equal values), a wall has no normal flow
+    if g.periodic_x:
+        u[:, :, nx] = u[:, :, 0]
+    else:
+        u[:, :, 0] = u[:, :, nx] = 0.0
+    if g.periodic_y:
+        v[:, ny, :] = v[:, 0, :]
+    else:
+        v[:, 0, :] = v[:, ny, :] = 0.0
     w[0] = w[nz] = 0.0
     return tuple(np.ascontiguousarray(a) for a in (u, v, w))
 
 
 def dyn_case(nx: int, ny: int, nz: int, seed: int = 5, hill: bool = True, moist: bool = False,
-             tracer: bool = False, amp: float = 1.0, bubble: float = 2.0):
-    """Closed block for the dynamical core: a cut-cell hill (or flat ground)
-    in a box with six walls, a stratified (N=0.01) state with a warm bubble,
-    seeded face velocities of amplitude amp that vanish on the walls.
+             tracer: bool = False, amp: float = 1.0, bubble: float = 2.0, periodic: bool = False):
+    """Block for the dynamical core: a cut-cell hill (or flat ground) in a box
+    with six walls (periodic=True: periodic in x and y, rigid bottom and lid),
+    a stratified (N=0.01) state with a warm bubble, seeded face velocities of
+    amplitude amp that vanish on the walls.
     Returns (geo, (uF, vF, wF), state, positions, (dx, dy, dz), boundary cells);
     positions maps rho, mom (uL,uR,vL,vR,wL,wR), th, qv, tracer to components."""
     if hill:
-        geo = closed_hill_case(nx, ny, nz, seed=seed)
+        if periodic:
+            grid = Grid(nx, ny, nz, 200.0, 200.0, stretched_levels(nz, 50.0, 400.0), True, True, False)
+            h = gaussian_hill_terrain(grid, 600.0, 800.0, 50.0, 600.0, seed=seed)
+            geo = close_dead_faces(cut_cell_geometry(grid, h, snap=0.01, merge=0.1))
+        else:
+            geo = closed_hill_case(nx, ny, nz, seed=seed)
     else:
-        grid = Grid(nx, ny, nz, 200.0, 200.0, stretched_levels(nz, 50.0, 400.0), False, False, False)
+        grid = Grid(nx, ny, nz, 200.0, 200.0, stretched_levels(nz, 50.0, 400.0), periodic, periodic, False)
         geo = cut_cell_geometry(grid, None, snap=0.0, merge=0.0)
     g = geo.grid
     vel = closed_face_velocity(geo, amp, seed=seed + 1)
@@ -497,6 +524,19 @@ def bubble_case(nx: int = 64, ny: int = 64, nz: int = 64, seed: int = 1):
     st = initial_state(geo, uf, vf, wf, theta0=300.0, n_bv=0.0, bubble_amp=2.0, bubble_radius=1000.0,
                        bubble_z=1000.0, noise=0.01, seed=seed)
     return geo, (uf, vf, wf), st
+
+
+def bubble_dyn_case(nx: int = 64, ny: int = 64, nz: int = 64, seed: int = 1):
+    """The warm bubble with prognostic momentum for the dynamical core:
+    bubble_case's grid (periodic x/y, rigid bottom and lid, no orography,
+    dx=dy=dz=100 m), state and u=10 m/s face velocities.  Returns (geo,
+    (uF, vF, wF), state, positions, (dx, dy, dz), boundary cells) like
+    dyn_case; a flat grid has no boundary cells."""
+    geo, vel, st = bubble_case(nx, ny, nz, seed=seed)
+    g = geo.grid
+    pos = {"rho": 0, "mom": [1, 2, 3, 4, 5, 6], "th": 7}
+    widths = (np.full(g.nx, g.dx), np.full(g.ny, g.dy), np.asarray(g.dz, dtype=np.float64).copy())
+    return geo, vel, st, pos, widths, boundary_cells(geo)
 
 
 def hill_case(nx: int = 256, ny: int = 256, nz: int = 128, seed: int = 2, dx: float = 200.0,

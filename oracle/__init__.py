@@ -68,9 +68,14 @@ def load() -> C.CDLL:
             "ora_proj_set_zebra": (None, [V, I]),
             "ora_lapl_compute": (None, [V, D, D]),
             "ora_lapl_get": (C.c_long, [V, I, I, I, V]),
+            "ora_lapl_get_dirichlet": (C.c_long, [V, I, I, I, V]),
             "ora_lapl_matvec": (None, [V, V, V]),
             "ora_lapl_vcycle": (None, [V, V, V]),
             "ora_psolve1": (None, [V, V, V]),
+            "ora_proj_nvec": (C.c_long, [V]),
+            "ora_lapl_vcycle_dirichlet": (I, [V, V, V]),
+            "ora_proj_exchange": (None, [V, V]),
+            "ora_proj_dot2": (D, [V, V, V]),
             "ora_matvec1": (None, [V, V, V]),
             "ora_fgmres": (I, [V, V, V, I, D, I, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "ora_proj_rhs": (None, [V, V, V, V, V, V]),
@@ -355,13 +360,18 @@ def tri_tb_matvec(d, u, l, x):
 
 
 class OracleProj:
-    """Oracle of the pressure projection of one closed block (oracle/asam_proj.c).
+    """Oracle of the pressure projection of one block (oracle/asam_proj.c)
+    whose sides are closed walls or periodic (the grid's periodic_x/y/z).
 
     Arrays use the same Fortran layouts as the library: faces with uF/vF/wF
-    extents, interior cell fields (nz, ny, nx), padded state fields."""
+    extents, interior cell fields (nz, ny, nx), padded state fields.  A block
+    with periodic sides carries boundary face unknowns: its PressureVelocity
+    vectors (rhs, fgmres, psolve1, matvec1, update) are flat arrays of
+    ``nvec`` values, the pressure (x fastest) followed by u_w, u_e, v_s, v_n,
+    w_b, w_t of the periodic sides; a closed block keeps (nz, ny, nx)."""
 
     def __init__(self, geo, dx, dy, dz, weights, metr=None, ref_level=4, gauss_iter2=1, gauss_iter3=1, mult_iter2=1,
-                 mult_iter3=1, zebra=1, fac_anela=1.0):
+                 mult_iter3=1, zebra=1, fac_anela=1.0, prefac2=0.5):
         self.lib = load()
         g = geo.grid
         self.grid = g
@@ -369,9 +379,16 @@ class OracleProj:
         metr = np.ones(n) if metr is None else metr
         self._keep = [np.ascontiguousarray(a, dtype=np.float64) for a in
                       (geo.fu, geo.fv, geo.fw, geo.volc, *weights, dx, dy, dz, metr)]
-        ip = (C.c_int * 9)(g.nx, g.ny, g.nz, ref_level, gauss_iter2, gauss_iter3, mult_iter2, mult_iter3, zebra)
-        dp = (C.c_double * 1)(fac_anela)
+        per = (int(bool(g.periodic_x)), int(bool(g.periodic_y)), int(bool(g.periodic_z)))
+        ip = (C.c_int * 12)(g.nx, g.ny, g.nz, ref_level, gauss_iter2, gauss_iter3, mult_iter2, mult_iter3, zebra,
+                            *per)
+        dp = (C.c_double * 2)(fac_anela, prefac2)
         self.h = self.lib.ora_proj_create(ip, dp, *[_p(a) for a in self._keep])
+        self.nvec = int(self.lib.ora_proj_nvec(self.h))
+        self.nface = self.nvec - g.nx * g.ny * g.nz
+
+    def _pv(self):
+        return self._cell() if self.nface == 0 else np.zeros(self.nvec)
 
     def close(self):
         if getattr(self, "h", None):
@@ -387,10 +404,13 @@ class OracleProj:
     def lapl_compute(self, beta0, dtp):
         self.lib.ora_lapl_compute(self.h, beta0, dtp)
 
-    def lapl_get(self, level3, level2, which):
-        n = self.lib.ora_lapl_get(self.h, level3, level2, which, None)
+    def lapl_get(self, level3, level2, which, dirichlet=False):
+        f = self.lib.ora_lapl_get_dirichlet if dirichlet else self.lib.ora_lapl_get
+        n = f(self.h, level3, level2, which, None)
+        if n < 0:
+            raise ValueError("no such level")
         out = np.empty(n)
-        self.lib.ora_lapl_get(self.h, level3, level2, which, _p(out))
+        f(self.h, level3, level2, which, _p(out))
         return out
 
     def _cell(self):
@@ -409,17 +429,32 @@ class OracleProj:
         self.lib.ora_lapl_vcycle(self.h, _p(b), _p(x))
         return x
 
+    def vcycle_dirichlet(self, b):
+        """One Solve_3D on LaplDirichlet (periodic blocks)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = self._cell()
+        if self.lib.ora_lapl_vcycle_dirichlet(self.h, _p(b), _p(x)) != 0:
+            raise ValueError("no Dirichlet hierarchy: the block has no periodic side")
+        return x
+
     def psolve1(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)
-        b = self._cell()
+        b = self._pv()
         self.lib.ora_psolve1(self.h, _p(x), _p(b))
         return b
 
     def matvec1(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)
-        b = self._cell()
+        b = self._pv()
         self.lib.ora_matvec1(self.h, _p(x), _p(b))
         return b
+
+    def exchange(self, v):
+        """Exchange of the face unknowns in place (u_w = u_w + u_e; u_e = u_w ...)."""
+        self.lib.ora_proj_exchange(self.h, _p(v))
+
+    def dot2(self, x, y):
+        return float(self.lib.ora_proj_dot2(self.h, _p(np.ascontiguousarray(x)), _p(np.ascontiguousarray(y))))
 
     def fgmres(self, x, b, maxiter=10, tol=1e-6, step=10):
         """x updated in place; returns (inner steps, rho, rho0)."""
@@ -429,7 +464,7 @@ class OracleProj:
         return steps, rho.value, rho0.value
 
     def rhs(self, u, v, w, incr_th=None):
-        b = self._cell()
+        b = self._pv()
         self.lib.ora_proj_rhs(self.h, _p(u), _p(v), _p(w), None if incr_th is None else _p(incr_th), _p(b))
         return b
 

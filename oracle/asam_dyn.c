@@ -1,5 +1,6 @@
 /*
- * CPU oracle of the dynamical-core stage of one closed block.
+ * CPU oracle of the dynamical-core stage of one block with closed or
+ * periodic sides.
  *
  * TEST INFRASTRUCTURE ONLY.  The parity tests and the CPU-baseline leg of the
  * benchmark call it as the checker; the CUDA library never links or calls it.
@@ -57,6 +58,7 @@ int ora_fgmres(void *hv, double *x, const double *b, int maxiter, double tol, in
                double *rho0_out);
 void ora_proj_update(void *hv, double *x, double *u, double *v, double *w, double *incr_th, double *incr_rho, int ncs,
                      double *const *incr_c, const double *const *c, const double *rho_pad);
+long ora_proj_nvec(void *hv);
 
 /* positions of the six LR momentum components: uL, uR, vL, vR, wL, wR */
 typedef struct {
@@ -297,6 +299,33 @@ void ora_fcn_dyn(const ora_geom *g, int ncomp, int rho_pos, const int *pos, int 
           wRhsL[PIDX(g, i, j, k + 1)] = wRhsL[PIDX(g, i, j, k + 1)] - 2.0 * V[PIDX(g, i, j, k + 1)] * Grad;
           wRhsR[PIDX(g, i, j, k)] = wRhsR[PIDX(g, i, j, k)] - 2.0 * V[PIDX(g, i, j, k)] * Grad;
         }
+    /* the periodic sides: the neighbour loop of PGradComputeCFull
+     * ('iw'/'ie'/'is'/'in' with equal refinement, PressureGrad_Mod.f90:307-313,
+     * 340-346, 373-379, 406-412): no DUU factor, and the partner cell's width dLoc (the last
+     * cell of the block for 'iw', the first for 'ie', ReadWeights_Mod.f90:
+     * 903-960) in the denominator */
+    if (g->per_x)
+      for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j) {
+          const double FW0 = g->fu[FUI(g, 0, j, k)], FE0 = g->fu[FUI(g, nx, j, k)];
+          const double GW = FW0 / (FW0 + EPS) * (p[PIDX(g, 1, j, k)] - p[PIDX(g, 0, j, k)]) /
+                            (mxy[j - 1] * (dx[0] + dx[nx - 1] + EPS));
+          uRhsL[PIDX(g, 1, j, k)] = uRhsL[PIDX(g, 1, j, k)] - 2.0 * V[PIDX(g, 1, j, k)] * GW;
+          const double GE = FE0 / (FE0 + EPS) * (p[PIDX(g, nx + 1, j, k)] - p[PIDX(g, nx, j, k)]) /
+                            (mxy[j - 1] * (dx[nx - 1] + dx[0] + EPS));
+          uRhsR[PIDX(g, nx, j, k)] = uRhsR[PIDX(g, nx, j, k)] - 2.0 * V[PIDX(g, nx, j, k)] * GE;
+        }
+    if (g->per_y)
+      for (int k = 1; k <= nz; ++k)
+        for (int i = 1; i <= nx; ++i) {
+          const double FS0 = g->fv[FVI(g, i, 0, k)], FN0 = g->fv[FVI(g, i, ny, k)];
+          const double GS = FS0 / (FS0 + EPS) * (p[PIDX(g, i, 1, k)] - p[PIDX(g, i, 0, k)]) /
+                            (myx[i - 1] * (dy[0] + dy[ny - 1] + EPS));
+          vRhsL[PIDX(g, i, 1, k)] = vRhsL[PIDX(g, i, 1, k)] - 2.0 * V[PIDX(g, i, 1, k)] * GS;
+          const double GN = FN0 / (FN0 + EPS) * (p[PIDX(g, i, ny + 1, k)] - p[PIDX(g, i, ny, k)]) /
+                            (myx[i - 1] * (dy[0] + dy[ny - 1] + EPS));
+          vRhsR[PIDX(g, i, ny, k)] = vRhsR[PIDX(g, i, ny, k)] - 2.0 * V[PIDX(g, i, ny, k)] * GN;
+        }
   }
   ora_exchange_flux(g, ncomp, f);
   for (int ic = 0; ic < ncomp; ++ic) {
@@ -318,7 +347,7 @@ void ora_fcn_dyn(const ora_geom *g, int ncomp, int rho_pos, const int *pos, int 
 }
 
 /* ------------------------------------------------------------------ */
-/* One Rosenbrock step of the dynamical core of a closed block
+/* One Rosenbrock step of the dynamical core of one block
  * (Ros3MetC + StageRos with uPosL>0, ADVECT/Int_Mod.f90:1059-1122, 263-374).
  * c: state (ncomp padded fields, in/out); uf, vf, wf: face velocities VelF
  * (in/out).  proj: the projection oracle of this block (ora_proj_create).
@@ -354,7 +383,8 @@ int ora_ros_step_dyn(const ora_geom *g, void *proj, const int *ipar, const doubl
   double *t = (double *)malloc(sizeof(double) * n);
   double *p = (double *)malloc(sizeof(double) * n);
   double *w8 = (double *)malloc(sizeof(double) * (3 * nu + 3 * nv + 3 * nw + 2 * nc));
-  double *xp = (double *)malloc(sizeof(double) * nc), *bp = (double *)malloc(sizeof(double) * nc);
+  const size_t nvec = (size_t)ora_proj_nvec(proj); /* pressure + boundary face unknowns */
+  double *xp = (double *)malloc(sizeof(double) * nvec), *bp = (double *)malloc(sizeof(double) * nvec);
   double **ic_ptr = (double **)malloc(sizeof(double *) * (nscalar > 0 ? nscalar : 1));
   const double **c_ptr = (const double **)malloc(sizeof(double *) * (nscalar > 0 ? nscalar : 1));
   memcpy(cold, c, sizeof(double) * len); /* Copy(VecMet,VecMetOld) */
@@ -398,7 +428,7 @@ int ora_ros_step_dyn(const ora_geom *g, void *proj, const int *ipar, const doubl
     ora_cell_to_face(g, pos, x, fu, fv, fw); /* VelocityCellToFaceLR */
     /* ProjectVelFace(dt, VecIncrF, VecIncrMetC, VecMetOld) */
     ora_proj_rhs(proj, fu, fv, fw, x + (size_t)th_pos * n, bp);
-    memset(xp, 0, sizeof(double) * nc);
+    memset(xp, 0, sizeof(double) * nvec);
     double rr = 0.0, rr0 = 0.0;
     const int steps = ora_fgmres(proj, xp, bp, proj_maxiter, proj_tol, proj_step, &rr, &rr0);
     if (psteps) psteps[is] = steps;

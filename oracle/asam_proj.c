@@ -28,12 +28,31 @@
  *   UpdateVelocity            MATRIX/Rhs_Mod.f90:589-952 (GradFull, MultiTriT)
  *   ProjectVelFace            ADVECT/IntSub_Mod.f90:25-71
  *
- * Scope: one block whose six sides are outer boundaries without boundary
- * pressure unknowns (TypeW='ow' ... with BCP=0, the closed box of the
- * configurations' projection).  The PressureVelocity vector then has no face
- * components (u_w ... w_t are never set), the Schur step of PSolve1 leaves the
- * pressure unchanged, and the Neumann factors of SetFactorN
- * (MULTI/Reverse_Mod.f90:225-292) are 0 on every side.
+ * Scope: one block whose sides are either closed outer boundaries
+ * (TypeW='ow' ... with BCP=0 and a velocity rule other than 'OutFlow') or
+ * periodic, i.e. the block is its own neighbour across the side pair
+ * (nType 'iw'/'ie', 'is'/'in', 'ib'/'it' with equal refinement).  A periodic
+ * side carries the boundary face unknowns u_w ... w_t of PressureVelocity
+ * (MODULE/VecPrVel_Mod.f90:10-18); a closed side has none.  With face
+ * unknowns the routines restated here are
+ *   MatVecFull face terms      MATRIX/MatVec_Mod.f90:184-258
+ *   Exchange / RandCopy / CopyFluxVel (EqualEqual)
+ *                              MODULE/VecPrVel_Mod.f90:809-974,
+ *                              MODULE/Exchange_Mod.f90:769-859
+ *   DOT2                       MODULE/VecPrVel_Mod.f90:112-172
+ *   PSolve1 = PressurePre, b2pBx1Full, Exchange, SchurPreFull, Exchange,
+ *   b1pBTx2Full, PressurePre   MATRIX/PreCond_Mod.f90:1555-1571, 599-844, 20-597
+ *   SetFactorD (Fac=2 on the periodic sides) for the Dirichlet hierarchy
+ *   LaplDirichlet               MULTI/Reverse_Mod.f90:95-213,
+ *                              MULTI/JacAccGrav_Mod.f90:453-469
+ *   UpdateVelocity boundary faces MATRIX/Rhs_Mod.f90:636-660
+ * The Neumann hierarchy LaplNeumann keeps the factors 0 of SetFactorN
+ * (MULTI/Reverse_Mod.f90:215-292) on every side.
+ *
+ * PressureVelocity vectors of this file: the pressure (natural interior
+ * order, nx*ny*nz) followed by the face unknowns of the periodic sides in the
+ * order u_w, u_e (ny*nz each, y fastest), v_s, v_n (nx*nz, x fastest), w_b,
+ * w_t (nx*ny, x fastest); ora_proj_nvec() gives the length.
  *
  * Besides the reference's lexicographic plane/line Gauss-Seidel smoother the
  * file also holds the zebra (two-colour) ordering of the same smoother that the
@@ -95,6 +114,12 @@ typedef struct {
   double *dx, *dy, *dz;
   double *mxy, *mxz, *myx, *myz, *mzx, *mzy;
   double beta0, dtp;
+  /* periodic side pairs (face unknowns) and the Dirichlet hierarchy */
+  int per_x, per_y, per_z;
+  double prefac2;      /* PreFac2 (MODULE/Control_Mod.f90:59, default 0.5) */
+  T3* AD;              /* LaplDirichlet: SetFactorD factors */
+  size_t nvec;         /* length of a PressureVelocity vector */
+  long off[6];         /* offsets of u_w, u_e, v_s, v_n, w_b, w_t (-1: no face unknowns) */
 } Proj;
 
 static double* zalloc(size_t n) { return (double*)calloc(n ? n : 1, sizeof(double)); }
@@ -876,8 +901,26 @@ void* ora_proj_create(const int* ipar, const double* dpar, const double* fu, con
   p->fac_anela = dpar[0];
   /* SetFactorN: all sides Neumann (Fac = 0) */
   p->fac1_l = p->fac1_r = p->fac2_l = p->fac2_r = p->fac3_l = p->fac3_r = 0.0;
+  h->per_x = ipar[9];
+  h->per_y = ipar[10];
+  h->per_z = ipar[11];
+  h->prefac2 = dpar[1];
   const int nx = p->nx, ny = p->ny, nz = p->nz;
   const size_t nc = (size_t)nx * ny * nz;
+  {
+    const int per[3] = {h->per_x, h->per_y, h->per_z};
+    const size_t fsz[3] = {(size_t)ny * nz, (size_t)nx * nz, (size_t)nx * ny};
+    size_t o = nc;
+    for (int side = 0; side < 6; ++side) {
+      if (per[side / 2]) {
+        h->off[side] = (long)o;
+        o += fsz[side / 2];
+      } else {
+        h->off[side] = -1;
+      }
+    }
+    h->nvec = o;
+  }
   h->fu = zalloc((size_t)(nx + 1) * ny * nz);
   h->fv = zalloc((size_t)nx * (ny + 1) * nz);
   h->fw = zalloc((size_t)nx * ny * (nz + 1));
@@ -932,6 +975,7 @@ void ora_proj_destroy(void* hv) {
   Proj* h = (Proj*)hv;
   if (!h) return;
   t3_free(h->A);
+  t3_free(h->AD);
   double* p[] = {h->fu, h->fv, h->fw, h->dtu, h->dtv, h->dtw, h->duu, h->duv, h->duw, h->dut, h->dtt, h->vol, h->volp,
                  h->dx, h->dy, h->dz, h->mxy, h->mxz, h->myx, h->myz, h->mzx, h->mzy};
   for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); ++i) free(p[i]);
@@ -939,6 +983,56 @@ void ora_proj_destroy(void* hv) {
 }
 
 void ora_proj_set_zebra(void* hv, int zebra) { ((Proj*)hv)->par.zebra = zebra; }
+
+/* Length of a PressureVelocity vector: nx*ny*nz plus the face unknowns. */
+long ora_proj_nvec(void* hv) { return (long)((Proj*)hv)->nvec; }
+
+/* The semi-coarsening hierarchy of LaplTFullCompute (all 3D levels, the
+ * plane levels of each) from the reversed fine fields g, with the boundary
+ * factors of p. */
+static T3* build_hierarchy(const PrjPar* p, const Fields* g, double bd2, int n1, int n2, int n3) {
+  const int R = p->ref_level;
+  T3 *top = NULL, *cur3 = NULL;
+  for (int L3 = 0; L3 < R; ++L3) {
+    const int s = (1 << L3) - 1;
+    const int n1C = (n1 + s) / (s + 1), n2C = (n2 + s) / (s + 1), n3C = (n3 + s) / (s + 1);
+    Fields c;
+    fields_alloc(&c, n1C, n2C, n3C);
+    coarsen(g, &c, s, s, s);
+    T3* a = t3_alloc(n3C, n2C, n1C);
+    compute_3d(p, bd2, a->pl, a->u, a->l, n3C, &c, 1);
+    fields_free(&c);
+    if (!cur3) {
+      top = a;
+    } else {
+      cur3->coarse = a;
+      a->fine = cur3;
+    }
+    cur3 = a;
+    /* the coarse plane levels of this 3D level */
+    T2** cur2 = (T2**)calloc(n3C, sizeof(T2*));
+    for (int k = 0; k < n3C; ++k) cur2[k] = a->pl[k];
+    for (int L2 = L3 + 1; L2 < R; ++L2) {
+      const int s2 = (1 << L2) - 1;
+      const int m1 = (n1 + s2) / (s2 + 1), m2 = (n2 + s2) / (s2 + 1);
+      Fields c2;
+      fields_alloc(&c2, m1, m2, n3C);
+      coarsen(g, &c2, s2, s2, s);
+      T2** neu = (T2**)calloc(n3C, sizeof(T2*));
+      for (int k = 0; k < n3C; ++k) {
+        neu[k] = t2_alloc(m2, m1);
+        cur2[k]->coarse = neu[k];
+        neu[k]->fine = cur2[k];
+      }
+      compute_3d(p, bd2, neu, NULL, NULL, n3C, &c2, 0);
+      fields_free(&c2);
+      for (int k = 0; k < n3C; ++k) cur2[k] = neu[k];
+      free(neu);
+    }
+    free(cur2);
+  }
+  return top;
+}
 
 /* LaplTFullCompute (JacAccGrav_Mod.f90:1056-1310) with SetFactorN */
 void ora_lapl_compute(void* hv, double beta0, double dtp) {
@@ -991,45 +1085,19 @@ void ora_lapl_compute(void* hv, double beta0, double dtp) {
   reverse(h, h->dut, g.dut);
   reverse(h, h->vol, g.vol);
 
-  const int R = p->ref_level;
-  T3* cur3 = NULL;
-  for (int L3 = 0; L3 < R; ++L3) {
-    const int s = (1 << L3) - 1;
-    const int n1C = (n1 + s) / (s + 1), n2C = (n2 + s) / (s + 1), n3C = (n3 + s) / (s + 1);
-    Fields c;
-    fields_alloc(&c, n1C, n2C, n3C);
-    coarsen(&g, &c, s, s, s);
-    T3* a = t3_alloc(n3C, n2C, n1C);
-    compute_3d(p, bd2, a->pl, a->u, a->l, n3C, &c, 1);
-    fields_free(&c);
-    if (!cur3) {
-      h->A = a;
-    } else {
-      cur3->coarse = a;
-      a->fine = cur3;
-    }
-    cur3 = a;
-    /* the coarse plane levels of this 3D level */
-    T2** cur2 = (T2**)calloc(n3C, sizeof(T2*));
-    for (int k = 0; k < n3C; ++k) cur2[k] = a->pl[k];
-    for (int L2 = L3 + 1; L2 < R; ++L2) {
-      const int s2 = (1 << L2) - 1;
-      const int m1 = (n1 + s2) / (s2 + 1), m2 = (n2 + s2) / (s2 + 1);
-      Fields c2;
-      fields_alloc(&c2, m1, m2, n3C);
-      coarsen(&g, &c2, s2, s2, s);
-      T2** neu = (T2**)calloc(n3C, sizeof(T2*));
-      for (int k = 0; k < n3C; ++k) {
-        neu[k] = t2_alloc(m2, m1);
-        cur2[k]->coarse = neu[k];
-        neu[k]->fine = cur2[k];
-      }
-      compute_3d(p, bd2, neu, NULL, NULL, n3C, &c2, 0);
-      fields_free(&c2);
-      for (int k = 0; k < n3C; ++k) cur2[k] = neu[k];
-      free(neu);
-    }
-    free(cur2);
+  /* LaplNeumann with SetFactorN (p's factors are 0) */
+  h->A = build_hierarchy(p, &g, bd2, n1, n2, n3);
+  /* LaplDirichlet with SetFactorD: 2 on the periodic sides, 0 on the closed
+   * ones (their velocity rule is not 'OutFlow'); order (z,x,y) -> factors
+   * 1 = bottom/top, 2 = west/east, 3 = south/north */
+  t3_free(h->AD);
+  h->AD = NULL;
+  if (h->per_x || h->per_y || h->per_z) {
+    PrjPar pd = *p;
+    pd.fac1_l = pd.fac1_r = h->per_z ? 2.0 : 0.0;
+    pd.fac2_l = pd.fac2_r = h->per_x ? 2.0 : 0.0;
+    pd.fac3_l = pd.fac3_r = h->per_y ? 2.0 : 0.0;
+    h->AD = build_hierarchy(&pd, &g, bd2, n1, n2, n3);
   }
   fields_free(&g);
 }
@@ -1038,9 +1106,15 @@ void ora_lapl_compute(void* hv, double beta0, double dtp) {
  * then plane): which 0 d, 1 u (z), 2 l (z), 3 u (x), 4 l (x), 5 u (y), 6 l (y);
  * entries past the end of a coupling (last row / line) are 0.  L3 = 3D level,
  * L2 >= L3 = plane level.  Returns the number of values (-1: no such level). */
+static long lapl_get(T3* a, int L3, int L2, int which, double* out);
 long ora_lapl_get(void* hv, int L3, int L2, int which, double* out) {
-  Proj* h = (Proj*)hv;
-  T3* a = h->A;
+  return lapl_get(((Proj*)hv)->A, L3, L2, which, out);
+}
+/* the same for LaplDirichlet (periodic blocks; -1 without one) */
+long ora_lapl_get_dirichlet(void* hv, int L3, int L2, int which, double* out) {
+  return lapl_get(((Proj*)hv)->AD, L3, L2, which, out);
+}
+static long lapl_get(T3* a, int L3, int L2, int which, double* out) {
   for (int q = 0; q < L3 && a; ++q) a = a->coarse;
   if (!a) return -1;
   const int n3 = a->n3;
@@ -1102,56 +1176,324 @@ void ora_lapl_matvec(void* hv, const double* x, double* y) {
   free(yr);
 }
 
-/* VCycleCG, MatrixT branch (JacAccGrav_Mod.f90:4466-4517): x = Solve_3D(A, b)
- * from a zero start. */
+/* VCycleCG, MatrixT branch (JacAccGrav_Mod.f90:4466-4517) on LaplNeumann:
+ * x = Solve_3D(A, b) from a zero start. */
+static void vcycle_on(Proj* h, T3* A, const double* b, double* x);
 void ora_lapl_vcycle(void* hv, const double* b, double* x) {
   Proj* h = (Proj*)hv;
+  vcycle_on(h, h->A, b, x);
+}
+
+/* the same on LaplDirichlet (periodic blocks only; returns -1 otherwise) */
+int ora_lapl_vcycle_dirichlet(void* hv, const double* b, double* x) {
+  Proj* h = (Proj*)hv;
+  if (!h->AD) return -1;
+  vcycle_on(h, h->AD, b, x);
+  return 0;
+}
+
+/* Solve_3D from a zero start on hierarchy A (VCycleCG, MatrixT branch,
+ * JacAccGrav_Mod.f90:4466-4517): x = Solve(A, b), natural interior order. */
+static void vcycle_on(Proj* h, T3* A, const double* b, double* x) {
   const size_t n = (size_t)h->par.nx * h->par.ny * h->par.nz;
   double* r = zalloc(n);
   double* xc = zalloc(n);
   reverse(h, b, r);
-  for (int it = 0; it < h->par.mult_iter3; ++it) multigrid_3d(&h->par, h->A, r, xc);
+  for (int it = 0; it < h->par.mult_iter3; ++it) multigrid_3d(&h->par, A, r, xc);
   reverse_back(h, xc, x);
   free(r);
   free(xc);
 }
 
-/* MatVecFull, MultiTriT branch without boundary face unknowns
- * (MatVec_Mod.f90:184-258): b%p = -(A x%p). */
+/* Index helpers of the interior cells and faces (1-based logical indices). */
+#define PV_C(i, j, k) ((size_t)((i) - 1) + (size_t)nx * ((size_t)((j) - 1) + (size_t)ny * ((k) - 1)))
+#define PV_U(i, j, k) ((size_t)(i) + (size_t)(nx + 1) * ((size_t)((j) - 1) + (size_t)ny * ((k) - 1)))
+#define PV_V(i, j, k) ((size_t)((i) - 1) + (size_t)nx * ((size_t)(j) + (size_t)(ny + 1) * ((k) - 1)))
+#define PV_W(i, j, k) ((size_t)((i) - 1) + (size_t)nx * ((size_t)((j) - 1) + (size_t)ny * (k)))
+#define FX(j, k) ((size_t)((j) - 1) + (size_t)ny * ((k) - 1)) /* u_w, u_e (iy, iz) */
+#define FY(i, k) ((size_t)((i) - 1) + (size_t)nx * ((k) - 1)) /* v_s, v_n (ix, iz) */
+#define FZ(i, j) ((size_t)((i) - 1) + (size_t)nx * ((j) - 1)) /* w_b, w_t (ix, iy) */
+
+/* The pressure term of the boundary face unknowns of one side, as the
+ * reference's array statements:
+ *   p(ix0+1) += beta0*dtP*FU(ix0)*DTU(ix0)*DTT(ix0+1)*u_w, p(ix1) -= ... u_e, ...
+ * (MatVecFull MATRIX/MatVec_Mod.f90:224-255 and b1pBTx2Full
+ * MATRIX/PreCond_Mod.f90:642-665); v holds the face unknowns. */
+static void face_to_p_side(const Proj* h, int side, double* p, const double* v) {
+  const int nx = h->par.nx, ny = h->par.ny, nz = h->par.nz;
+  const double bd = h->beta0 * h->dtp;
+  const long o = h->off[side];
+  if (o < 0) return;
+  switch (side) {
+    case 0:
+      for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j) {
+          const size_t q = PV_U(0, j, k);
+          p[PV_C(1, j, k)] = p[PV_C(1, j, k)] + bd * h->fu[q] * h->dtu[q] * h->dtt[PV_C(1, j, k)] * v[o + FX(j, k)];
+        }
+      break;
+    case 1:
+      for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j) {
+          const size_t q = PV_U(nx, j, k);
+          p[PV_C(nx, j, k)] = p[PV_C(nx, j, k)] - bd * h->fu[q] * h->dtu[q] * h->dtt[PV_C(nx, j, k)] * v[o + FX(j, k)];
+        }
+      break;
+    case 2:
+      for (int k = 1; k <= nz; ++k)
+        for (int i = 1; i <= nx; ++i) {
+          const size_t q = PV_V(i, 0, k);
+          p[PV_C(i, 1, k)] = p[PV_C(i, 1, k)] + bd * h->fv[q] * h->dtv[q] * h->dtt[PV_C(i, 1, k)] * v[o + FY(i, k)];
+        }
+      break;
+    case 3:
+      for (int k = 1; k <= nz; ++k)
+        for (int i = 1; i <= nx; ++i) {
+          const size_t q = PV_V(i, ny, k);
+          p[PV_C(i, ny, k)] = p[PV_C(i, ny, k)] - bd * h->fv[q] * h->dtv[q] * h->dtt[PV_C(i, ny, k)] * v[o + FY(i, k)];
+        }
+      break;
+    case 4:
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          const size_t q = PV_W(i, j, 0);
+          p[PV_C(i, j, 1)] = p[PV_C(i, j, 1)] + bd * h->fw[q] * h->dtw[q] * h->dtt[PV_C(i, j, 1)] * v[o + FZ(i, j)];
+        }
+      break;
+    default:
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          const size_t q = PV_W(i, j, nz);
+          p[PV_C(i, j, nz)] = p[PV_C(i, j, nz)] - bd * h->fw[q] * h->dtw[q] * h->dtt[PV_C(i, j, nz)] * v[o + FZ(i, j)];
+        }
+      break;
+  }
+}
+
+/* all sides in the order W, E, S, N, B, T */
+static void face_to_p(const Proj* h, double* p, const double* v) {
+  for (int side = 0; side < 6; ++side) face_to_p_side(h, side, p, v);
+}
+
+/* The coupling of a boundary face unknown to the pressure of its cell,
+ * beta0*dtP*F*DUT*DUU*p (MatVecFull, b2pBx1Full, SchurPreFull). */
+static double face_cp(const Proj* h, int side, int a, int b, const double* p) {
+  const int nx = h->par.nx, ny = h->par.ny, nz = h->par.nz;
+  const double bd = h->beta0 * h->dtp;
+  size_t q, c;
+  switch (side) {
+    case 0: q = PV_U(0, a, b); c = PV_C(1, a, b); return bd * h->fu[q] * h->dut[c] * h->duu[q] * p[c];
+    case 1: q = PV_U(nx, a, b); c = PV_C(nx, a, b); return bd * h->fu[q] * h->dut[c] * h->duu[q] * p[c];
+    case 2: q = PV_V(a, 0, b); c = PV_C(a, 1, b); return bd * h->fv[q] * h->dut[c] * h->duv[q] * p[c];
+    case 3: q = PV_V(a, ny, b); c = PV_C(a, ny, b); return bd * h->fv[q] * h->dut[c] * h->duv[q] * p[c];
+    case 4: q = PV_W(a, b, 0); c = PV_C(a, b, 1); return bd * h->fw[q] * h->dut[c] * h->duw[q] * p[c];
+    default: q = PV_W(a, b, nz); c = PV_C(a, b, nz); return bd * h->fw[q] * h->dut[c] * h->duw[q] * p[c];
+  }
+  (void)nz;
+}
+
+/* Half-cell factors of a boundary face unknown, in the two operation orders
+ * of the reference: MatVecFull's face equation multiplies
+ * Half*Metr1*Metr2*d (then *F*u), SchurPreFull divides by
+ * 0.5d0*d*Metr1*Metr2 (then *F + Eps); the w faces have no metric factors. */
+static double half_mv(const Proj* h, int side, int a, int b) {
+  const int nx = h->par.nx, ny = h->par.ny, nz = h->par.nz;
+  switch (side) {
+    case 0: return 0.5 * h->mxy[a - 1] * h->mxz[b - 1] * h->dx[0];
+    case 1: return 0.5 * h->mxy[a - 1] * h->mxz[b - 1] * h->dx[nx - 1];
+    case 2: return 0.5 * h->myx[a - 1] * h->myz[b - 1] * h->dy[0];
+    case 3: return 0.5 * h->myx[a - 1] * h->myz[b - 1] * h->dy[ny - 1];
+    case 4: return 0.5 * h->dz[0];
+    default: return 0.5 * h->dz[nz - 1];
+  }
+}
+static double half_sp(const Proj* h, int side, int a, int b) {
+  const int nx = h->par.nx, ny = h->par.ny, nz = h->par.nz;
+  switch (side) {
+    case 0: return 0.5 * h->dx[0] * h->mxy[a - 1] * h->mxz[b - 1];
+    case 1: return 0.5 * h->dx[nx - 1] * h->mxy[a - 1] * h->mxz[b - 1];
+    case 2: return 0.5 * h->dy[0] * h->myx[a - 1] * h->myz[b - 1];
+    case 3: return 0.5 * h->dy[ny - 1] * h->myx[a - 1] * h->myz[b - 1];
+    case 4: return 0.5 * h->dz[0];
+    default: return 0.5 * h->dz[nz - 1];
+  }
+}
+
+/* area of the face of a boundary unknown */
+static double face_area(const Proj* h, int side, int a, int b) {
+  const int nx = h->par.nx, ny = h->par.ny, nz = h->par.nz;
+  switch (side) {
+    case 0: return h->fu[PV_U(0, a, b)];
+    case 1: return h->fu[PV_U(nx, a, b)];
+    case 2: return h->fv[PV_V(a, 0, b)];
+    case 3: return h->fv[PV_V(a, ny, b)];
+    case 4: return h->fw[PV_W(a, b, 0)];
+    default: return h->fw[PV_W(a, b, nz)];
+  }
+  (void)nz;
+}
+
+/* extents (a,b) of the face array of a side: (ny,nz), (nx,nz), (nx,ny) */
+static void face_ext(const Proj* h, int side, int* na, int* nb) {
+  const int nx = h->par.nx, ny = h->par.ny, nz = h->par.nz;
+  *na = side < 2 ? ny : nx;
+  *nb = side < 4 ? nz : ny;
+}
+static size_t face_idx(const Proj* h, int side, int a, int b) {
+  const int na = side < 2 ? h->par.ny : h->par.nx;
+  return (size_t)(a - 1) + (size_t)na * (b - 1);
+}
+
+/* MatVecFull, MultiTriT branch (MatVec_Mod.f90:184-258): b = Zero;
+ * b%p = -(A x%p); then per periodic side (W, E, S, N, B, T) the pressure term
+ * of the face unknown and the face equation
+ *   b%u_w = Half*MetrXY*MetrXZ*dx(ix0+1)*FU(ix0)*x%u_w + beta0*dtP*FU*DUT*DUU*x%p(ix0+1)
+ *   b%u_e = Half*MetrXY*MetrXZ*dx(ix1)*FU(ix1)*x%u_e - beta0*dtP*FU*DUT*DUU*x%p(ix1)
+ * (w faces without the metric factors). */
 static void matvec1(Proj* h, const double* x, double* b) {
   const size_t n = (size_t)h->par.nx * h->par.ny * h->par.nz;
+  for (size_t q = n; q < h->nvec; ++q) b[q] = 0.0;
   ora_lapl_matvec(h, x, b);
   for (size_t q = 0; q < n; ++q) b[q] = -b[q];
+  for (int side = 0; side < 6; ++side) {
+    if (h->off[side] < 0) continue;
+    face_to_p_side(h, side, b, x); /* the array statement before the face loop */
+    int na, nb;
+    face_ext(h, side, &na, &nb);
+    for (int bb = 1; bb <= nb; ++bb)
+      for (int a = 1; a <= na; ++a) {
+        const size_t f = h->off[side] + face_idx(h, side, a, bb);
+        const double m = half_mv(h, side, a, bb) * face_area(h, side, a, bb) * x[f];
+        const double cp = face_cp(h, side, a, bb, x);
+        b[f] = (side & 1) ? m - cp : m + cp;
+      }
+  }
 }
 
-/* PSolve1 (PreCond_Mod.f90:1555-1571) without boundary face unknowns:
- * b=x; PressurePre(b,x); b2pBx1 (face parts only); SchurPre (leaves the
- * pressure unchanged: p saved, Dirichlet solve of the face coupling,
- * p restored); b1pBTx2Full: b%p = -x%p; PressurePre(b,b). */
-static void psolve1(Proj* h, double* b, const double* x) {
+/* Exchange (MODULE/VecPrVel_Mod.f90:855-974) of a block that is its own
+ * neighbour: RandCopy's 'iw' branch (ibLoc<=ibnLoc) with CopyFluxVel
+ * EqualEqual, u_w = u_w + u_e; u_e = u_w (likewise v_s/v_n, w_b/w_t). */
+static void exchange_pv(const Proj* h, double* v) {
+  for (int pair = 0; pair < 3; ++pair) {
+    const long lo = h->off[2 * pair], hi = h->off[2 * pair + 1];
+    if (lo < 0) continue;
+    int na, nb;
+    face_ext(h, 2 * pair, &na, &nb);
+    const size_t m = (size_t)na * nb;
+    for (size_t q = 0; q < m; ++q) {
+      v[lo + q] = v[lo + q] + v[hi + q];
+      v[hi + q] = v[lo + q];
+    }
+  }
+}
+
+/* DOT2 (MODULE/VecPrVel_Mod.f90:112-172): the pressure, then per neighbour
+ * the face unknowns of the east/north/top side only (Refine>=RefineNachbar),
+ * so a shared face is counted once; neighbour order W, E, S, N, B, T. */
+static double dot2(const Proj* h, const double* x, const double* y) {
   const size_t n = (size_t)h->par.nx * h->par.ny * h->par.nz;
-  double* tmp = zalloc(n);
-  memcpy(b, x, sizeof(double) * n);
-  ora_lapl_vcycle(h, x, b);                    /* PressurePre(b,x) */
-  for (size_t q = 0; q < n; ++q) b[q] = -x[q]; /* b1pBTx2Full */
-  memcpy(tmp, b, sizeof(double) * n);
-  ora_lapl_vcycle(h, tmp, b);                  /* PressurePre(b,b) */
-  free(tmp);
-}
-
-static double dot2(const double* x, const double* y, size_t n) {
   double s = 0.0;
   for (size_t q = 0; q < n; ++q) s = s + x[q] * y[q];
+  for (int side = 1; side < 6; side += 2) {
+    if (h->off[side] < 0) continue;
+    int na, nb;
+    face_ext(h, side, &na, &nb);
+    const size_t m = (size_t)na * nb;
+    double t = 0.0;
+    for (size_t q = 0; q < m; ++q) t = t + x[h->off[side] + q] * y[h->off[side] + q];
+    s = s + t;
+  }
   return s;
 }
 
-/* FGMRES (SOLU/Iter_Mod.f90:121-199) with StepGMRES = step.  x in/out, b
- * in.  Returns the number of inner steps taken in total; *rho_out = last
- * residual estimate, *rho0_out = initial residual norm. */
+/* PSolve1 (PreCond_Mod.f90:1555-1571): b=x; PressurePre(b,x); b2pBx1Full;
+ * Exchange; SchurPreFull; Exchange; b1pBTx2Full; PressurePre(b,b).
+ * SchurPreFull saves b%p and restores it at the end, and b1pBTx2Full then
+ * overwrites it with -x%p, so the saved value never matters; without face
+ * unknowns only the last two steps change b. */
+static void psolve1(Proj* h, double* b, const double* x) {
+  const size_t n = (size_t)h->par.nx * h->par.ny * h->par.nz;
+  const double eps = EPS;
+  memcpy(b, x, sizeof(double) * h->nvec);
+  if (h->nvec > n) {
+    vcycle_on(h, h->A, x, b); /* PressurePre(b,x) */
+    /* b2pBx1Full (PreCond_Mod.f90:694-728): b%u_w = x%u_w + beta0*dtP*FU*DUT*DUU*b%p(ix0+1), ... */
+    for (int side = 0; side < 6; ++side) {
+      if (h->off[side] < 0) continue;
+      int na, nb;
+      face_ext(h, side, &na, &nb);
+      for (int bb = 1; bb <= nb; ++bb)
+        for (int a = 1; a <= na; ++a) {
+          const size_t f = h->off[side] + face_idx(h, side, a, bb);
+          const double cp = face_cp(h, side, a, bb, b);
+          b[f] = (side & 1) ? x[f] - cp : x[f] + cp;
+        }
+    }
+    exchange_pv(h, b);
+    /* SchurPreFull (PreCond_Mod.f90:138-216, 303-326, 327-404): the face
+     * unknowns scaled by the half-cell mass into a pressure right-hand side,
+     * one Solve_3D on LaplDirichlet, then the faces from that pressure */
+    double* r = zalloc(n);
+    double* rp = zalloc(n);
+    {
+      const int nx = h->par.nx, ny = h->par.ny, nz = h->par.nz;
+      const double bd = h->beta0 * h->dtp;
+      for (int side = 0; side < 6; ++side) {
+        if (h->off[side] < 0) continue;
+        int na, nb;
+        face_ext(h, side, &na, &nb);
+        for (int bb = 1; bb <= nb; ++bb)
+          for (int a = 1; a <= na; ++a) {
+            const size_t f = h->off[side] + face_idx(h, side, a, bb);
+            const double F = face_area(h, side, a, bb);
+            size_t q, c;
+            double dt;
+            switch (side) {
+              case 0: q = PV_U(0, a, bb); c = PV_C(1, a, bb); dt = h->dtu[q]; break;
+              case 1: q = PV_U(nx, a, bb); c = PV_C(nx, a, bb); dt = h->dtu[q]; break;
+              case 2: q = PV_V(a, 0, bb); c = PV_C(a, 1, bb); dt = h->dtv[q]; break;
+              case 3: q = PV_V(a, ny, bb); c = PV_C(a, ny, bb); dt = h->dtv[q]; break;
+              case 4: q = PV_W(a, bb, 0); c = PV_C(a, bb, 1); dt = h->dtw[q]; break;
+              default: q = PV_W(a, bb, nz); c = PV_C(a, bb, nz); dt = h->dtw[q]; break;
+            }
+            const double t = bd * F * dt * h->dtt[c] * b[f] / (half_sp(h, side, a, bb) * F + eps);
+            r[c] = (side & 1) ? r[c] - t : r[c] + t;
+          }
+      }
+    }
+    vcycle_on(h, h->AD, r, rp);
+    for (int side = 0; side < 6; ++side) {
+      if (h->off[side] < 0) continue;
+      int na, nb;
+      face_ext(h, side, &na, &nb);
+      for (int bb = 1; bb <= nb; ++bb)
+        for (int a = 1; a <= na; ++a) {
+          const size_t f = h->off[side] + face_idx(h, side, a, bb);
+          const double cp = face_cp(h, side, a, bb, rp);
+          const double den = half_sp(h, side, a, bb) * face_area(h, side, a, bb) + eps;
+          b[f] = (side & 1) ? h->prefac2 * (b[f] + cp) / den : h->prefac2 * (b[f] - cp) / den;
+        }
+    }
+    free(r);
+    free(rp);
+    exchange_pv(h, b);
+  }
+  /* b1pBTx2Full (PreCond_Mod.f90:624-665) and PressurePre(b,b) */
+  double* tmp = zalloc(n);
+  for (size_t q = 0; q < n; ++q) tmp[q] = -x[q];
+  face_to_p(h, tmp, b);
+  vcycle_on(h, h->A, tmp, b);
+  free(tmp);
+}
+
+/* FGMRES (SOLU/Iter_Mod.f90:121-199) with StepGMRES = step on
+ * PressureVelocity vectors (ora_proj_nvec).  x in/out, b in.  Returns the
+ * number of inner steps taken in total; *rho_out = last residual estimate,
+ * *rho0_out = initial residual norm. */
 int ora_fgmres(void* hv, double* x, const double* b, int maxiter, double tol, int step, double* rho_out,
                double* rho0_out) {
   Proj* h = (Proj*)hv;
-  const size_t n = (size_t)h->par.nx * h->par.ny * h->par.nz;
+  const size_t n = h->nvec;
   double** v = (double**)calloc(step + 1, sizeof(double*));
   double** z = (double**)calloc(step, sizeof(double*));
   for (int i = 0; i <= step; ++i) v[i] = zalloc(n);
@@ -1167,7 +1509,8 @@ int ora_fgmres(void* hv, double* x, const double* b, int maxiter, double tol, in
   for (int iter = 1; iter <= maxiter; ++iter) {
     matvec1(h, x, v[0]);
     for (size_t q = 0; q < n; ++q) v[0][q] = b[q] + (-1.0) * v[0][q]; /* DXPBY(b,-One,v) */
-    double beta = sqrt(dot2(v[0], v[0], n));
+    exchange_pv(h, v[0]);
+    double beta = sqrt(dot2(h, v[0], v[0]));
     if (iter == 1) rho0 = beta;
     if (beta <= 0.0) break;
     const double sc = 1.0 / beta;
@@ -1177,12 +1520,13 @@ int ora_fgmres(void* hv, double* x, const double* b, int maxiter, double tol, in
     for (int i = 1; i <= step; ++i) {
       psolve1(h, z[i - 1], v[i - 1]);
       matvec1(h, z[i - 1], v[i]);
+      exchange_pv(h, v[i]);
       ++steps;
       for (int k = 1; k <= i; ++k) {
-        HH(k, i) = dot2(v[k - 1], v[i], n);
+        HH(k, i) = dot2(h, v[k - 1], v[i]);
         for (size_t q = 0; q < n; ++q) v[i][q] = (-HH(k, i)) * v[k - 1][q] + v[i][q];
       }
-      HH(i + 1, i) = sqrt(dot2(v[i], v[i], n));
+      HH(i + 1, i) = sqrt(dot2(h, v[i], v[i]));
       const double sh = 1.0 / HH(i + 1, i);
       for (size_t q = 0; q < n; ++q) v[i][q] = sh * v[i][q];
       for (int k = 2; k <= i; ++k) {
@@ -1228,9 +1572,11 @@ int ora_fgmres(void* hv, double* x, const double* b, int maxiter, double tol, in
   return steps;
 }
 
-/* PSolve1 and MatVec1 exposed for the tests */
+/* PSolve1, MatVec1, Exchange and DOT2 on PressureVelocity vectors, exposed for the tests */
 void ora_psolve1(void* hv, const double* x, double* b) { psolve1((Proj*)hv, b, x); }
 void ora_matvec1(void* hv, const double* x, double* b) { matvec1((Proj*)hv, x, b); }
+void ora_proj_exchange(void* hv, double* v) { exchange_pv((Proj*)hv, v); }
+double ora_proj_dot2(void* hv, const double* x, const double* y) { return dot2((Proj*)hv, x, y); }
 
 #define UI(i, j, k) ((size_t)(i) + (size_t)(nx + 1) * ((size_t)((j) - 1) + (size_t)ny * ((k) - 1)))
 #define VI(i, j, k) ((size_t)((i) - 1) + (size_t)nx * ((size_t)(j) + (size_t)(ny + 1) * ((k) - 1)))
@@ -1240,8 +1586,8 @@ void ora_matvec1(void* hv, const double* x, double* b) { matvec1((Proj*)hv, x, b
 
 /* Rhs (Rhs_Mod.f90:110-187) with DivergenceS (:41-78): b = beta0*dtP*div,
  * minus VolB*incr_th in the FacAnela>=1 branch.  u,v,w uF/vF/wF extents;
- * incr_th the padded theta increment (or NULL: no theta term); b natural
- * interior. */
+ * incr_th the padded theta increment (or NULL: no theta term); b a
+ * PressureVelocity vector (ora_proj_nvec entries, face unknowns 0). */
 void ora_proj_rhs(void* hv, const double* u, const double* v, const double* w, const double* incr_th, double* b) {
   Proj* h = (Proj*)hv;
   const int nx = h->par.nx, ny = h->par.ny, nz = h->par.nz;
@@ -1259,14 +1605,18 @@ void ora_proj_rhs(void* hv, const double* u, const double* v, const double* w, c
         if (incr_th && h->par.fac_anela >= 1.0) val = val - h->vol[CI(i, j, k)] * incr_th[PI(i, j, k)];
         b[CI(i, j, k)] = val;
       }
+  /* the face unknowns of b stay Zero (ProjectVelFace: b=Zero; Rhs sets p only) */
+  for (size_t q = (size_t)nx * ny * nz; q < h->nvec; ++q) b[q] = 0.0;
 }
 
-/* UpdateVelocity (Rhs_Mod.f90:589-952) for GradFull + MultiTriT without
- * boundary face unknowns (their Temp terms are 0 - 0/(...)).  x is the
- * solved pressure (natural interior), overwritten with x*DUT like the
- * reference.  u,v,w updated in place; incr_th / incr_rho (padded, may be
- * NULL) updated; ncs scalars (increment + state arrays, padded) get the
- * DivScalar update with rho (padded). */
+/* UpdateVelocity (Rhs_Mod.f90:589-952) for GradFull + MultiTriT.  x is the
+ * solved PressureVelocity vector; its pressure is overwritten with x*DUT
+ * like the reference.  The boundary faces get Temp = x%u_w - b%u_w/(...)
+ * (Rhs_Mod.f90:636-660) with b's face parts 0 (Rhs sets the pressure only):
+ * the face unknown of a periodic side, 0 on a closed side.  u,v,w updated in
+ * place; incr_th / incr_rho (padded, may be NULL) updated; ncs scalars
+ * (increment + state arrays, padded) get the DivScalar update with rho
+ * (padded). */
 void ora_proj_update(void* hv, double* x, double* u, double* v, double* w, double* incr_th, double* incr_rho, int ncs,
                      double* const* incr_c, const double* const* c, const double* rho_pad) {
   Proj* h = (Proj*)hv;
@@ -1274,29 +1624,35 @@ void ora_proj_update(void* hv, double* x, double* u, double* v, double* w, doubl
   const double beta0 = h->beta0, dtp = h->dtp;
   const size_t n = (size_t)nx * ny * nz;
   for (size_t q = 0; q < n; ++q) x[q] = x[q] * h->dut[q];
-  /* boundary faces: Temp = x%u_w - b%u_w/(...) with zero face parts */
+  /* boundary faces: Temp = x%u_w - b%u_w/(...) with zero face parts of b */
+  const long* o = h->off;
+#define FACEX(side, idx) (o[side] >= 0 ? x[o[side] + (idx)] : 0.0)
   for (int k = 1; k <= nz; ++k)
     for (int j = 1; j <= ny; ++j) {
-      double t0 = 0.0 - 0.0 / (0.5 * h->dx[0] * h->mxy[j - 1] * h->mxz[k - 1]);
+      const size_t f = (size_t)(j - 1) + (size_t)ny * (k - 1);
+      double t0 = FACEX(0, f) - 0.0 / (0.5 * h->dx[0] * h->mxy[j - 1] * h->mxz[k - 1]);
       u[UI(0, j, k)] = u[UI(0, j, k)] + t0;
-      double t1 = 0.0 - 0.0 / (0.5 * h->dx[nx - 1] * h->mxy[j - 1] * h->mxz[k - 1]);
+      double t1 = FACEX(1, f) - 0.0 / (0.5 * h->dx[nx - 1] * h->mxy[j - 1] * h->mxz[k - 1]);
       u[UI(nx, j, k)] = u[UI(nx, j, k)] + t1;
     }
   for (int i = 1; i <= nx; ++i)
     for (int k = 1; k <= nz; ++k) {
-      double t0 = 0.0 - 0.0 / (0.5 * h->dy[0] * h->myx[i - 1] * h->myz[k - 1]);
+      const size_t f = (size_t)(i - 1) + (size_t)nx * (k - 1);
+      double t0 = FACEX(2, f) - 0.0 / (0.5 * h->dy[0] * h->myx[i - 1] * h->myz[k - 1]);
       v[VI(i, 0, k)] = v[VI(i, 0, k)] + t0;
-      double t1 = 0.0 - 0.0 / (0.5 * h->dy[ny - 1] * h->myx[i - 1] * h->myz[k - 1]);
+      double t1 = FACEX(3, f) - 0.0 / (0.5 * h->dy[ny - 1] * h->myx[i - 1] * h->myz[k - 1]);
       v[VI(i, ny, k)] = v[VI(i, ny, k)] + t1;
     }
   for (int i = 1; i <= nx; ++i)
     for (int j = 1; j <= ny; ++j) {
-      double t0 = 0.0 - 0.0 / (0.5 * h->dz[0] * h->mzx[i - 1] * h->mzy[j - 1]);
+      const size_t f = (size_t)(i - 1) + (size_t)nx * (j - 1);
+      double t0 = FACEX(4, f) - 0.0 / (0.5 * h->dz[0] * h->mzx[i - 1] * h->mzy[j - 1]);
       w[WI(i, j, 0)] = w[WI(i, j, 0)] + t0;
-      double t1 = 0.0 - 0.0 / (0.5 * h->dz[nz - 1] * h->mzx[i - 1] * h->mzy[j - 1]);
+      double t1 = FACEX(5, f) - 0.0 / (0.5 * h->dz[nz - 1] * h->mzx[i - 1] * h->mzy[j - 1]);
       const double fwt = h->fw[WI(i, j, nz)];
       w[WI(i, j, nz)] = w[WI(i, j, nz)] + fwt / (fwt + EPS) * t1;
     }
+#undef FACEX
   /* interior faces: u = utilde - grad p */
   for (int k = 1; k <= nz; ++k)
     for (int j = 1; j <= ny; ++j)
@@ -1378,9 +1734,10 @@ void ora_proj_update(void* hv, double* x, double* u, double* v, double* w, doubl
 #undef PI
 
 /* WeightDiagCompute, ThetaKind='Density' branch (MULTI/JacAccGrav_Mod.f90:
- * 4259-4282) with CellToFaceRhoWeight (:3254-3702) for a closed block
- * (outer walls, no inflow): DUT per cell, DTU/DTV/DTW the volume-weighted
- * face values of theta = (rho theta)/(rho+Eps) (one-sided on the walls),
+ * 4259-4282) with CellToFaceRhoWeight (:3254-3702) for closed (outer walls,
+ * no inflow) and periodic sides: DUT per cell, DTU/DTV/DTW the volume-weighted
+ * face values of theta = (rho theta)/(rho+Eps) (one-sided on the walls, with
+ * the halo image on a periodic side),
  * DUU/DUV/DUW = F/(F+Eps), DTT = 1.  Inputs are padded fields: rth = rho
  * theta, rho, rv (RhoV, may be NULL), rl (RhoL + RhoR summed by the caller:
  * rc and rr, each may be NULL), t = absolute temperature.  Outputs with the
@@ -1404,6 +1761,10 @@ void ora_weights_density(void* hv, const double* rth, const double* rho, const d
 #define CI(i, j, k) ((size_t)((i) - 1) + (size_t)nx * ((size_t)((j) - 1) + (size_t)ny * ((k) - 1)))
 #define TH(P) (rth[P] / (rho[P] + EPS))
 #define FACE(P, Q) ((V[P] * rth[P] / (rho[P] + EPS) + V[Q] * rth[Q] / (rho[Q] + EPS)) / (V[P] + V[Q] + EPS))
+/* a periodic x or y side ('iw'/'ie'/'is'/'in' branches, equal refinement,
+ * :3313-3321, 3360-3368, 3407-3415, 3454-3462): theta first, then times the
+ * volume, with the halo cell holding the periodic image */
+#define PFACE(P, Q) ((TH(P) * V[P] + TH(Q) * V[Q]) / (V[P] + V[Q] + EPS))
   for (int k = 1; k <= nz; ++k)
     for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
@@ -1422,9 +1783,9 @@ void ora_weights_density(void* hv, const double* rth, const double* rho, const d
       for (int i = 0; i <= nx; ++i) {
         double v;
         if (i == 0)
-          v = TH(PI(1, j, k));
+          v = h->per_x ? PFACE(PI(1, j, k), PI(0, j, k)) : TH(PI(1, j, k));
         else if (i == nx)
-          v = TH(PI(nx, j, k));
+          v = h->per_x ? PFACE(PI(nx + 1, j, k), PI(nx, j, k)) : TH(PI(nx, j, k));
         else
           v = FACE(PI(i, j, k), PI(i + 1, j, k));
         dtu[UI(i, j, k)] = v;
@@ -1436,9 +1797,9 @@ void ora_weights_density(void* hv, const double* rth, const double* rho, const d
       for (int i = 1; i <= nx; ++i) {
         double v;
         if (j == 0)
-          v = TH(PI(i, 1, k));
+          v = h->per_y ? PFACE(PI(i, 1, k), PI(i, 0, k)) : TH(PI(i, 1, k));
         else if (j == ny)
-          v = TH(PI(i, ny, k));
+          v = h->per_y ? PFACE(PI(i, ny + 1, k), PI(i, ny, k)) : TH(PI(i, ny, k));
         else
           v = FACE(PI(i, j, k), PI(i, j + 1, k));
         dtv[VI(i, j, k)] = v;
@@ -1449,10 +1810,10 @@ void ora_weights_density(void* hv, const double* rth, const double* rho, const d
     for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
         double v;
-        if (k == 0)
-          v = TH(PI(i, j, 1));
+        if (k == 0)  /* 'ib'/'it' (:3501-3509, 3548-3556): the interior rounding */
+          v = h->per_z ? FACE(PI(i, j, 1), PI(i, j, 0)) : TH(PI(i, j, 1));
         else if (k == nz)
-          v = TH(PI(i, j, nz));
+          v = h->per_z ? FACE(PI(i, j, nz + 1), PI(i, j, nz)) : TH(PI(i, j, nz));
         else
           v = FACE(PI(i, j, k), PI(i, j, k + 1));
         dtw[WI(i, j, k)] = v;
@@ -1466,6 +1827,7 @@ void ora_weights_density(void* hv, const double* rth, const double* rho, const d
 #undef CI
 #undef TH
 #undef FACE
+#undef PFACE
 }
 
 /* Replace the oracle's weights (after ora_weights_density) */

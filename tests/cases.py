@@ -45,12 +45,34 @@ def proj_inputs(geo, seed=3, amp=1.0):
     return G.projection_inputs(geo, seed=seed, amp=amp)
 
 
+def _hill_periodic(nx, ny, nz, seed=4, per_y=True, height=600.0, halfwidth=800.0):
+    """Cut-cell hill periodic in x (and y), rigid bottom and lid, the faces of
+    zero-volume cells closed: a block with boundary face unknowns."""
+    grid = G.Grid(nx, ny, nz, 200.0, 200.0, G.stretched_levels(nz, 50.0, 400.0), True, per_y, False)
+    h = G.gaussian_hill_terrain(grid, height, halfwidth, 50.0, 600.0, seed=seed)
+    return G.close_dead_faces(G.cut_cell_geometry(grid, h, snap=0.01, merge=0.1))
+
+
+def _flat_periodic(nx, ny, nz):
+    grid = G.Grid(nx, ny, nz, 100.0, 100.0, G.uniform_levels(nz, 100.0), True, True, False)
+    return G.cut_cell_geometry(grid, None, snap=0.0, merge=0.0)
+
+
+PROJ_PERIODIC = {
+    "proj_per_hill_16x12x10": lambda: _hill_periodic(16, 12, 10),
+    "proj_per_x_hill_13x7x9": lambda: _hill_periodic(13, 7, 9, seed=6, per_y=False),
+    "proj_per_flat_12x10x8": lambda: _flat_periodic(12, 10, 8),
+    "proj_per_slab_9x1x6": lambda: _flat_periodic(9, 1, 6),
+}
+
+
 PROJ_CASES = {
     "proj_hill_24x20x16": lambda: _hill_closed(24, 20, 16),
     "proj_hill_odd_13x7x9": lambda: _hill_closed(13, 7, 9, seed=6),
     "proj_flat_16x12x10": lambda: _flat_closed(16, 12, 10),
     "proj_column_1x1x12": lambda: _flat_closed(1, 1, 12),
     "proj_slab_9x1x6": lambda: _flat_closed(9, 1, 6),
+    **PROJ_PERIODIC,
 }
 
 

@@ -228,12 +228,15 @@ def line_solve(val, grid, b, axis):
     return np.stack([lu.solve(r) for r in bb]).reshape(np.shape(b))
 
 
-def lapl_level0(geo, W, dx, dy, dz, beta0, dtp):
+def lapl_level0(geo, W, dx, dy, dz, beta0, dtp, facs=(0.0, 0.0, 0.0)):
     """Level-0 pressure Laplacian of LaplTFullCompute (MULTI/JacAccGrav_Mod.f90:
     1056-1310 with ComputeFull_1D/2D/3D of MULTI/TriDiagT_Mod.f90; shift 0,
-    Cartesian metric, Neumann factors 0), restated in numpy: the arrays d, u/l
-    along z, along x and along y in the reversed order (z fastest, then x,
-    then y), entries past the last row/line/plane 0."""
+    Cartesian metric), restated in numpy: the arrays d, u/l along z, along x
+    and along y in the reversed order (z fastest, then x, then y), entries past
+    the last row/line/plane 0.  facs = the boundary factors (Fac1, Fac2, Fac3)
+    of both ends of the z, x and y axes: 0 for LaplNeumann (SetFactorN), 2 on
+    the periodic axes for LaplDirichlet (SetFactorD)."""
+    f1, f2, f3 = (float(f) for f in facs)
     g = geo.grid
     nx, ny, nz = g.nx, g.ny, g.nz
     eps = 1.0e-30
@@ -261,15 +264,15 @@ def lapl_level0(geo, W, dx, dy, dz, beta0, dtp):
         base = bd2 * 2.0 * F1[:, :, 1:nz] * T1[:, :, 1:nz] * U1[:, :, 1:nz]
         below = base * D[:, :, 1:] / den   # cell f, face below
         above = base * D[:, :, :-1] / den  # cell f-1, face above
-        first = np.concatenate([bd2 * 0.0 * F1[:, :, :1] * T1[:, :, :1] * U1[:, :, :1] * D[:, :, :1] / (dzc[0] * one * one),
+        first = np.concatenate([bd2 * f1 * F1[:, :, :1] * T1[:, :, :1] * U1[:, :, :1] * D[:, :, :1] / (dzc[0] * one * one),
                                 below], axis=2)
-        second = np.concatenate([above, bd2 * 0.0 * F1[:, :, nz:] * T1[:, :, nz:] * U1[:, :, nz:] * D[:, :, -1:] /
+        second = np.concatenate([above, bd2 * f1 * F1[:, :, nz:] * T1[:, :, nz:] * U1[:, :, nz:] * D[:, :, -1:] /
                                  (dzc[-1] * one * one)], axis=2)
         uz = np.concatenate([-(base * D[:, :, 1:] / den), z[:, :, :1]], axis=2)
         lz = np.concatenate([-(base * D[:, :, :-1] / den), z[:, :, :1]], axis=2)
     else:
-        first = bd2 * 0.0 * F1[:, :, :1] * T1[:, :, :1] * U1[:, :, :1] * D / (dzc[0] * one * one)
-        second = bd2 * 0.0 * F1[:, :, 1:] * T1[:, :, 1:] * U1[:, :, 1:] * D / (dzc[0] * one * one)
+        first = bd2 * f1 * F1[:, :, :1] * T1[:, :, :1] * U1[:, :, :1] * D / (dzc[0] * one * one)
+        second = bd2 * f1 * F1[:, :, 1:] * T1[:, :, 1:] * U1[:, :, 1:] * D / (dzc[0] * one * one)
         uz = lz = z.copy()
     d = d + first
     d = d + second
@@ -279,16 +282,16 @@ def lapl_level0(geo, W, dx, dy, dz, beta0, dtp):
     if nx > 1:
         den = ((dxc[:-1] + dxc[1:]) * one)[None, :, None] * one
         base = bd2 * 2.0 * F2[:, 1:nx] * T2[:, 1:nx] * U2[:, 1:nx]
-        first = np.concatenate([bd2 * 0.0 * F2[:, :1] * T2[:, :1] * U2[:, :1] * D[:, :1] / (dxc[0] * one * one),
+        first = np.concatenate([bd2 * f2 * F2[:, :1] * T2[:, :1] * U2[:, :1] * D[:, :1] / (dxc[0] * one * one),
                                 base * D[:, 1:] / den], axis=1)
         second = np.concatenate([base * D[:, :-1] / den,
-                                 bd2 * 0.0 * F2[:, nx:] * T2[:, nx:] * U2[:, nx:] * D[:, -1:] / (dxc[-1] * one * one)],
+                                 bd2 * f2 * F2[:, nx:] * T2[:, nx:] * U2[:, nx:] * D[:, -1:] / (dxc[-1] * one * one)],
                                 axis=1)
         ux = np.concatenate([-(base * D[:, 1:] / den), z[:, :1]], axis=1)
         lx = np.concatenate([-(base * D[:, :-1] / den), z[:, :1]], axis=1)
     else:
-        first = bd2 * 0.0 * F2[:, :1] * T2[:, :1] * U2[:, :1] * D / (dxc[0] * one * one)
-        second = bd2 * 0.0 * F2[:, 1:] * T2[:, 1:] * U2[:, 1:] * D / (dxc[0] * one * one)
+        first = bd2 * f2 * F2[:, :1] * T2[:, :1] * U2[:, :1] * D / (dxc[0] * one * one)
+        second = bd2 * f2 * F2[:, 1:] * T2[:, 1:] * U2[:, 1:] * D / (dxc[0] * one * one)
         ux = lx = z.copy()
     d = d + first
     d = d + second
@@ -297,15 +300,15 @@ def lapl_level0(geo, W, dx, dy, dz, beta0, dtp):
     if ny > 1:
         den = ((dyc[:-1] + dyc[1:]) * one)[:, None, None] * one
         base = bd2 * 2.0 * F3[1:ny] * T3[1:ny]
-        first = np.concatenate([bd2 * 0.0 * F3[:1] * T3[:1] * U3[:1] * D[:1] / (dyc[0] * one * one),
+        first = np.concatenate([bd2 * f3 * F3[:1] * T3[:1] * U3[:1] * D[:1] / (dyc[0] * one * one),
                                 base * D[1:] / den], axis=0)
-        second = np.concatenate([base * D[:-1] / den, bd2 * 0.0 * F3[ny:] * T3[ny:] * D[-1:] / (dyc[-1] * one * one)],
+        second = np.concatenate([base * D[:-1] / den, bd2 * f3 * F3[ny:] * T3[ny:] * D[-1:] / (dyc[-1] * one * one)],
                                 axis=0)
         u3 = np.concatenate([-(base * D[1:] / den), z[:1]], axis=0)
         l3 = np.concatenate([-(base * D[:-1] / den), z[:1]], axis=0)
     else:
-        first = bd2 * 0.0 * F3[:1] * T3[:1] * U3[:1] * D / (dyc[0] * one * one)
-        second = bd2 * 0.0 * F3[1:] * T3[1:] * D / (dyc[0] * one * one)
+        first = bd2 * f3 * F3[:1] * T3[:1] * U3[:1] * D / (dyc[0] * one * one)
+        second = bd2 * f3 * F3[1:] * T3[1:] * D / (dyc[0] * one * one)
         u3 = l3 = z.copy()
     d = d + first
     d = d + second
@@ -367,7 +370,7 @@ def momentum_sources(geo, p, rho, dx, dy, dz, grav=9.81):
     """Pressure gradient (ADVECT/PressureGrad_Mod.f90:252-276, before
     AdvectionScale: -2 VolC Grad per LR component) and buoyancy
     (ADVECT/Buoyancy_Mod.f90:51-63, after the scale: -RhoLoc Grav) on the
-    interior cells of a closed block.  Returns (pg[6], bu[2]) as (nz, ny, nx)
+    interior cells of a block with closed or periodic x/y sides.  Returns (pg[6], bu[2]) as (nz, ny, nx)
     arrays in the order uL, uR, vL, vR, wL, wR and wL, wR."""
     g = geo.grid
     nx, ny, nz = g.nx, g.ny, g.nz
@@ -390,6 +393,22 @@ def momentum_sources(geo, p, rho, dx, dy, dz, grav=9.81):
         dz[1:] + dz[:-1] + EPS)[:, None, None]
     pg[4][1:] = -2.0 * V[1:] * gz
     pg[5][:-1] = -2.0 * V[:-1] * gz
+    # periodic sides: the neighbour loop ('iw'/'ie'/'is'/'in'), no DUU factor,
+    # the partner cell's width in the denominator; p's halos hold the images
+    if g.periodic_x:
+        Fb = geo.fu[:, :, 1]
+        gw = Fb / (Fb + EPS) * (P[1:-1, 1:-1, 1] - P[1:-1, 1:-1, 0]) / (1.0 * (dx[0] + dx[-1] + EPS))
+        pg[0][:, :, 0] = -2.0 * V[:, :, 0] * gw
+        Fb = geo.fu[:, :, nx + 1]
+        ge = Fb / (Fb + EPS) * (P[1:-1, 1:-1, nx + 1] - P[1:-1, 1:-1, nx]) / (1.0 * (dx[-1] + dx[0] + EPS))
+        pg[1][:, :, -1] = -2.0 * V[:, :, -1] * ge
+    if g.periodic_y:
+        Fb = geo.fv[:, 1, :]
+        gs = Fb / (Fb + EPS) * (P[1:-1, 1, 1:-1] - P[1:-1, 0, 1:-1]) / (1.0 * (dy[0] + dy[-1] + EPS))
+        pg[2][:, 0, :] = -2.0 * V[:, 0, :] * gs
+        Fb = geo.fv[:, ny + 1, :]
+        gn = Fb / (Fb + EPS) * (P[1:-1, ny + 1, 1:-1] - P[1:-1, ny, 1:-1]) / (1.0 * (dy[0] + dy[-1] + EPS))
+        pg[3][:, -1, :] = -2.0 * V[:, -1, :] * gn
     R = rho[1:-1, 1:-1, 1:-1]
     rl = F / (F + EPS) * (dz[:-1, None, None] * R[:-1] + dz[1:, None, None] * R[1:]) / (
         dz[:-1] + dz[1:] + EPS)[:, None, None]

@@ -157,3 +157,56 @@ def test_ros_step_dyn_conserves_mass(hill):
     assert abs(m1 - m0) <= 1e-13 * m0
     # walls stay closed
     assert not u[:, :, 0].any() and not u[:, :, -1].any() and not w[0].any() and not w[-1].any()
+
+
+@pytest.fixture(scope="module")
+def per_hill():
+    return G.dyn_case(12, 10, 8, seed=9, moist=True, tracer=True, periodic=True)
+
+
+def test_fcn_dyn_sources_periodic(per_hill):
+    """The pressure gradient of a periodic block also acts across the shared
+    boundary face (PGradComputeCFull's neighbour loop)."""
+    geo, vel, st, pos, (dx, dy, dz), _ = per_hill
+    o = oracle.Oracle(geo)
+    c = o.exchange_cell(st.c)
+    _, p = o.thermo(c, 0, pos["th"], rv_pos=pos["qv"])
+    f0 = o.fcn(c, vel)
+    f = o.fcn_dyn(c, vel, p, pos["mom"], dx, dy, dz)
+    pg, bu = pyref.momentum_sources(geo, p, c[0], dx, dy, dz)
+    assert np.any(pg[0][:, :, 0]) and np.any(pg[3][:, -1, :])
+    I = (slice(1, -1), slice(1, -1), slice(1, -1))
+    V = geo.volc[I]
+    for q, comp in enumerate(pos["mom"]):
+        src = pg[q] / (V + 1e-30) + (bu[q - 4] if q >= 4 else 0.0)
+        d = f[comp][I] - f0[comp][I]
+        scale = np.max(np.abs(src)) + np.max(np.abs(f0[comp][I]))
+        assert np.max(np.abs(d - src)) <= 1e-13 * scale, q
+
+
+def test_ros_step_dyn_periodic_conserves_mass(per_hill):
+    """Two steps of the dynamical core of a periodic block (boundary face
+    unknowns in the projection): mass conserved to rounding, the FGMRES
+    tolerance reached, both copies of a periodic face keep equal velocities."""
+    geo, vel, st, pos, (dx, dy, dz), bc = per_hill
+    nc = st.c.shape[0]
+    o = oracle.Oracle(geo, bc=_kinds(nc, pos["mom"]))
+    W = G.projection_inputs(geo)[0]
+    pr = oracle.OracleProj(geo, dx, dy, dz, W, zebra=1)
+    assert pr.nface > 0
+    c = st.c.copy()
+    u, v, w = (a.copy() for a in vel)
+    V = geo.volc[1:-1, 1:-1, 1:-1]
+    m0 = float(np.sum(c[0][1:-1, 1:-1, 1:-1] * V))
+    for _ in range(2):
+        it, rs, ps, prr = o.ros_step_dyn(pr, c, (u, v, w), 2.0, rho_pos=0, th_pos=pos["th"], pos=pos["mom"], dx=dx,
+                                         dy=dy, dz=dz, rv_pos=pos["qv"], bound=bc,
+                                         scalars=[pos["qv"], pos["tracer"]], bicg_tol=1e-10, proj_tol=1e-10,
+                                         proj_maxiter=40)
+        assert all(r <= 1e-10 for r in prr)
+    assert np.all(np.isfinite(c))
+    m1 = float(np.sum(c[0][1:-1, 1:-1, 1:-1] * V))
+    assert abs(m1 - m0) <= 1e-13 * m0
+    np.testing.assert_array_equal(u[:, :, 0], u[:, :, -1])
+    np.testing.assert_array_equal(v[:, 0, :], v[:, -1, :])
+    assert not w[0].any() and not w[-1].any()
