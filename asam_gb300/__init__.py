@@ -281,13 +281,17 @@ class TransportBlock:
         check(self.lib.asam_total_scalar(self.h, ptr(a), int(comp), C.byref(out)), "asam_total_scalar")
         return out.value
 
-    # ---- pressure projection (closed blocks) -------------------------------
+    # ---- pressure projection (closed or periodic sides) ----------------------
     def proj_setup(self, dx, dy, dz, metr=None, ref_level: int = 4, gauss_iter2: int = 1, gauss_iter3: int = 1,
                    mult_iter2: int = 1, mult_iter3: int = 1, step_gmres: int = 10, max_restart: int = 10,
-                   tol: float = 1e-6, fac_anela: float = 1.0):
+                   tol: float = 1e-6, fac_anela: float = 1.0, prefac2: float = 0.5):
         """Projection set-up: cell widths dx[nx], dy[ny], dz[nz]; metr the six
         metric arrays MetrXY, MetrXZ, MetrYX, MetrYZ, MetrZX, MetrZY back to
-        back (None: Cartesian).  Defaults are Control_Mod's."""
+        back (None: Cartesian).  Defaults are Control_Mod's.  A block with
+        periodic sides carries boundary face unknowns: its PressureVelocity
+        vectors (SolveSound, MatVec1, PSolve1) are flat arrays of
+        ``proj_nvec`` values, the pressure followed by u_w, u_e, v_s, v_n,
+        w_b, w_t of the periodic sides."""
         g = self.grid
         self._pdx, self._pdy, self._pdz = _f64(dx), _f64(dy), _f64(dz)
         if self._pdx.size != g.nx or self._pdy.size != g.ny or self._pdz.size != g.nz:
@@ -296,9 +300,46 @@ class TransportBlock:
         if self._pmetr is not None and self._pmetr.size != 2 * (g.nx + g.ny + g.nz):
             raise ValueError("metr must hold 2*(nx+ny+nz) values")
         self.pcfg = AsamProjConfig(ref_level, gauss_iter2, gauss_iter3, mult_iter2, mult_iter3, step_gmres, max_restart,
-                                   tol, fac_anela)
+                                   tol, fac_anela, prefac2)
         check(self.lib.asam_proj_setup(self.h, C.byref(self.pcfg), ptr(self._pdx), ptr(self._pdy), ptr(self._pdz),
                                        None if self._pmetr is None else ptr(self._pmetr)), "asam_proj_setup")
+        self.proj_nface = int(self.lib.asam_proj_face_count(self.h))
+        self.proj_nvec = g.nx * g.ny * g.nz + self.proj_nface
+
+    def _pv(self, like=None) -> np.ndarray:
+        """An empty PressureVelocity vector ((nz, ny, nx) for a closed block)."""
+        g = self.grid
+        return np.empty((g.nz, g.ny, g.nx)) if self.proj_nface == 0 else np.empty(self.proj_nvec)
+
+    def MatVec1(self, x) -> np.ndarray:
+        """MatVecFull on a PressureVelocity vector (no Exchange)."""
+        a = _f64(x)
+        y = self._pv()
+        check(self.lib.asam_proj_matvec1(self.h, ptr(a), ptr(y)), "asam_proj_matvec1")
+        return y
+
+    def PSolve1(self, x) -> np.ndarray:
+        """PSolve1 (PressurePre, Schur step, PressurePre) on a PressureVelocity vector."""
+        a = _f64(x)
+        y = self._pv()
+        check(self.lib.asam_proj_psolve1(self.h, ptr(a), ptr(y)), "asam_proj_psolve1")
+        return y
+
+    def lapl_array_dirichlet(self, level3: int, level2: int, which: int) -> np.ndarray:
+        """One array of the Dirichlet hierarchy (periodic blocks)."""
+        n = self.lib.asam_lapl_get_dirichlet(self.h, level3, level2, which, None)
+        if n < 0:
+            raise ValueError("no such level/array (or no Dirichlet hierarchy)")
+        out = np.empty(n)
+        if self.lib.asam_lapl_get_dirichlet(self.h, level3, level2, which, ptr(out)) != n:
+            raise AsamError(4, "asam_lapl_get_dirichlet")
+        return out
+
+    def VCycleCG_dirichlet(self, b) -> np.ndarray:
+        a = _f64(b)
+        x = np.empty_like(a)
+        check(self.lib.asam_lapl_vcycle_dirichlet(self.h, ptr(a), ptr(x)), "asam_lapl_vcycle_dirichlet")
+        return x
 
     def proj_set_precision(self, prec):
         """Precision of the FGMRES preconditioner's V-cycle: "fp64" (the
@@ -357,8 +398,8 @@ class TransportBlock:
         return x
 
     def SolveSound(self, x: np.ndarray, b, MaxIter: int | None = None, Tol: float | None = None):
-        """FGMRES on the pressure, x updated in place; returns (inner steps,
-        relative residual estimate)."""
+        """FGMRES on PressureVelocity vectors (the pressure of a closed block),
+        x updated in place; returns (inner steps, relative residual estimate)."""
         if not (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous):
             raise TypeError("x must be a C-contiguous float64 array (updated in place)")
         bb = _f64(b)

@@ -41,7 +41,7 @@ class AsamProjConfig(C.Structure):
     _fields_ = [
         ("ref_level", C.c_int), ("gauss_iter2", C.c_int), ("gauss_iter3", C.c_int),
         ("mult_iter2", C.c_int), ("mult_iter3", C.c_int), ("step_gmres", C.c_int),
-        ("max_restart", C.c_int), ("tol", C.c_double), ("fac_anela", C.c_double),
+        ("max_restart", C.c_int), ("tol", C.c_double), ("fac_anela", C.c_double), ("prefac2", C.c_double),
     ]
 
 
@@ -112,6 +112,11 @@ SIGNATURES = [
     ("asam_lapl_matvec", C.c_int, [_V, _V, _V]),
     ("asam_lapl_vcycle", C.c_int, [_V, _V, _V]),
     ("asam_solve_sound", C.c_int, [_V, _V, _V, _I, _D]),
+    ("asam_proj_face_count", C.c_long, [_V]),
+    ("asam_proj_matvec1", C.c_int, [_V, _V, _V]),
+    ("asam_proj_psolve1", C.c_int, [_V, _V, _V]),
+    ("asam_lapl_get_dirichlet", C.c_long, [_V, C.c_int, C.c_int, C.c_int, _V]),
+    ("asam_lapl_vcycle_dirichlet", C.c_int, [_V, _V, _V]),
     ("asam_project_vel_face", C.c_int, [_V, _V, _V, _V, _V, _V, C.c_int, C.c_int, _I, C.c_int, _V, _I, _D]),
     ("asam_proj_vcycles", C.c_longlong, [_V]),
     ("asam_proj_set_precision", C.c_int, [_V, C.c_int]),

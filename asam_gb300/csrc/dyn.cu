@@ -1,4 +1,5 @@
-// Dynamical-core stage of one closed block on the device: the momentum branch
+// Dynamical-core stage of one block (closed sides, or periodic in x and/or y)
+// on the device: the momentum branch
 // (uPosL>0) of the Rosenbrock stage around the transport solve and the
 // pressure projection.
 //   * VelocityFaceToCellLR (ADVECT/VelocityCellFace_Mod.f90:72-95, 541-654)
@@ -403,6 +404,11 @@ int asam_dyn_setup(asam_ctx* h, const asam_dyn_config* cfg, const int* bound_cel
     return kBadArg;
   if (!h->proj) {
     set_last_error("asam_dyn_setup: call asam_proj_setup first", __FILE__, __LINE__);
+    return kBadArg;
+  }
+  if (h->d.per_z) {  // the buoyancy's 'ib'/'it' neighbour terms are not built
+    set_last_error("asam_dyn_setup: a block periodic in z is not supported by the dynamical core", __FILE__,
+                   __LINE__);
     return kBadArg;
   }
   const int nc = h->cfg.ncomp;

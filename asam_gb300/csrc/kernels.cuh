@@ -260,6 +260,34 @@ __device__ __forceinline__ T pgrad_face(const Dims& d, const GeomT<T>& g, const 
   return du * F / (F + e) * (ms.p[d.P(i, j, k + 1)] - ms.p[d.P(i, j, k)]) / (ms.dz[k] + ms.dz[k - 1] + e);
 }
 
+// Grad of PGradComputeCFull's neighbour loop on a periodic side ('iw', 'ie',
+// 'is', 'in' with equal refinement, ADVECT/PressureGrad_Mod.f90:307-313,
+// 340-346, 373-379, 406-412): no DUU factor, and the width dLoc of the
+// partner cell across the side (the block's own last cell for 'iw', its
+// first for 'ie'); p's halo holds the periodic image.  side 0 W, 1 E, 2 S, 3 N.
+template <typename T>
+__device__ __forceinline__ T pgrad_side(const Dims& d, const GeomT<T>& g, const MomSrc<T>& ms, int side, int i, int j,
+                                        int k) {
+  const T e = eps_t<T>();
+  const int nx = d.nx, ny = d.ny;
+  if (side == 0) {
+    const T F = g.fu[d.FU(0, j, k)];
+    return F / (F + e) * (ms.p[d.P(1, j, k)] - ms.p[d.P(0, j, k)]) / (ms.mxy[j - 1] * (ms.dx[0] + ms.dx[nx - 1] + e));
+  }
+  if (side == 1) {
+    const T F = g.fu[d.FU(nx, j, k)];
+    return F / (F + e) * (ms.p[d.P(nx + 1, j, k)] - ms.p[d.P(nx, j, k)]) /
+           (ms.mxy[j - 1] * (ms.dx[nx - 1] + ms.dx[0] + e));
+  }
+  if (side == 2) {
+    const T F = g.fv[d.FV(i, 0, k)];
+    return F / (F + e) * (ms.p[d.P(i, 1, k)] - ms.p[d.P(i, 0, k)]) / (ms.myx[i - 1] * (ms.dy[0] + ms.dy[ny - 1] + e));
+  }
+  const T F = g.fv[d.FV(i, ny, k)];
+  return F / (F + e) * (ms.p[d.P(i, ny + 1, k)] - ms.p[d.P(i, ny, k)]) /
+         (ms.myx[i - 1] * (ms.dy[0] + ms.dy[ny - 1] + e));
+}
+
 // RhoLoc of AuftriebDryComputeLRFull (ADVECT/Buoyancy_Mod.f90:51-63) on the
 // face between levels k and k+1.
 template <typename T>
@@ -275,7 +303,7 @@ __device__ __forceinline__ T buoy_rho_face(const Dims& d, const GeomT<T>& g, con
 // in which the reference's scatter loop touches f(ix,iy,iz), then the
 // zero-volume mask (:1045-1051), the periodic ExchangeFlux (neighbour order
 // W,E,S,N,B,T) and AdvectionScale (:2888-2898).  One thread per padded cell.
-// kMom adds the momentum sources of ms (closed blocks); kDiff the diffusion
+// kMom adds the momentum sources of ms (closed or periodic x/y sides); kDiff the diffusion
 // fluxes of df with DiffusionCompute's second zero-volume mask (the halo
 // cells of a periodic side included, before ExchangeFlux reads them).
 template <typename T, bool kMom = false, bool kDiff = false>
@@ -351,6 +379,13 @@ __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict
             const T gr = pgrad_face(d, g, ms, axis, i - (axis == 0 ? lo : 0), j - (axis == 1 ? lo : 0),
                                     k - (axis == 2 ? lo : 0));
             a = a - (T)2 * V * gr;
+          } else {  // the shared face of a periodic side
+            int side = -1;
+            if (ic == ms.pos[0] && d.per_x) side = 0;
+            else if (ic == ms.pos[1] && d.per_x) side = 1;
+            else if (ic == ms.pos[2] && d.per_y) side = 2;
+            else if (ic == ms.pos[3] && d.per_y) side = 3;
+            if (side >= 0) a = a - (T)2 * V * pgrad_side(d, g, ms, side, i, j, k);
           }
         }
         if (exW) {

@@ -9,12 +9,28 @@
 //     MATRIX/MatVec_Mod.f90:184-258, MATRIX/PreCond_Mod.f90:1555-1571),
 //   * Rhs/DivergenceS and UpdateVelocity (MATRIX/Rhs_Mod.f90:41-78, 110-187, 589-952).
 //
-// Scope: a block whose six sides are outer boundaries without boundary
-// pressure unknowns (closed box); the PressureVelocity vector is then the
-// pressure alone, SetFactorN gives 0 boundary factors, the Schur step of
-// PSolve1 leaves the pressure unchanged and PSolve1 reduces to
-// PressurePre(-x) (the first PressurePre of PSolve1 only feeds the face
-// unknowns, so it is not run).
+// Scope: a block whose sides are closed outer boundaries (no boundary
+// pressure unknowns) or periodic, i.e. the block is its own neighbour across
+// the side pair (nType 'iw'/'ie' ...).  A periodic side carries the boundary
+// face unknowns u_w ... w_t of PressureVelocity (MODULE/VecPrVel_Mod.f90:10-18):
+// MatVecFull adds their face equations (MATRIX/MatVec_Mod.f90:224-255), every
+// MatVec1 and residual is followed by Exchange (RandCopy with CopyFluxVel
+// EqualEqual: u_w = u_w + u_e; u_e = u_w, MODULE/VecPrVel_Mod.f90:809-852,
+// MODULE/Exchange_Mod.f90:769-800), DOT2 counts a shared face once
+// (MODULE/VecPrVel_Mod.f90:112-172), and PSolve1 runs in full: PressurePre,
+// b2pBx1Full, Exchange, SchurPreFull (one Solve_3D on the Dirichlet hierarchy
+// LaplDirichlet of SetFactorD, Fac=2 on the periodic sides,
+// MULTI/Reverse_Mod.f90:95-213, MATRIX/PreCond_Mod.f90:20-597), Exchange,
+// b1pBTx2Full, PressurePre (MATRIX/PreCond_Mod.f90:599-844, 1555-1571).  A
+// closed block has no face unknowns: the Schur step leaves the pressure
+// unchanged and PSolve1 reduces to PressurePre(-x) (the first PressurePre
+// only feeds the face unknowns, so it is not run).
+//
+// PressureVelocity vectors on the device: the pressure in the level-0 layout
+// (below), then the face unknowns of the periodic sides in the order
+// u_e, v_n, w_t, u_w, v_s, w_b (u: y fastest then z; v: x then z; w: x then y)
+// -- the sides DOT2 counts first, so every dot product runs over one
+// contiguous prefix of the vector.
 //
 // Data layout.  The hierarchy lives in the reference's reversed index space
 // (n1,n2,n3) = (z,x,y) (MULTI/Reverse_Mod.f90 with xOrder=2,yOrder=3,zOrder=1).
@@ -99,6 +115,13 @@ struct Fields {
 struct Facs {
   double f1l, f1r, f2l, f2r, f3l, f3r;
 };
+
+// Offsets of the six face arrays inside a PressureVelocity vector (-1: the
+// side is closed and has none), sides numbered W, E, S, N, B, T.
+struct PvFaces {
+  long long off[6];
+};
+
 
 __host__ __device__ inline size_t slot(int w, int h, int i, int j) {
   return (size_t)i * w + (size_t)(j & 1) * h + (size_t)(j >> 1);
@@ -853,9 +876,12 @@ __global__ void k_rhs(Dims d, GeomT<double> g, Wts wt, const double* __restrict_
 }
 
 // UpdateVelocity, GradFull + MultiTriT: p = p*DUT, the boundary-face terms
-// (0 - 0/(...) without face unknowns) and u = utilde - grad p on interior faces
-__global__ void k_update_vel(Dims d, GeomT<double> g, Wts wt, double* __restrict__ p, double* __restrict__ u,
-                             double* __restrict__ v, double* __restrict__ w, double beta0, double dtp) {
+// Temp = x%u_w - b%u_w/(...) (Rhs_Mod.f90:636-660; b's face parts are 0: the
+// face unknown of a periodic side, 0 on a closed one) and u = utilde - grad p
+// on interior faces.  pv is the solved PressureVelocity vector (its faces at fc).
+__global__ void k_update_vel(Dims d, GeomT<double> g, Wts wt, double* __restrict__ p, const double* __restrict__ pv,
+                             PvFaces fc, double* __restrict__ u, double* __restrict__ v, double* __restrict__ w,
+                             double beta0, double dtp) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const double* mxy = wt.metr;
   const double* mxz = wt.metr + ny;
@@ -872,7 +898,9 @@ __global__ void k_update_vel(Dims d, GeomT<double> g, Wts wt, double* __restrict
       const size_t r = e / (nx + 1);
       const int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
       if (i == 0 || i == nx) {
-        const double t = 0.0 - 0.0 / (0.5 * wt.dx[i == 0 ? 0 : nx - 1] * mxy[j - 1] * mxz[k - 1]);
+        const int side = i == 0 ? 0 : 1;
+        const double xf = fc.off[side] >= 0 ? pv[fc.off[side] + (j - 1) + (size_t)ny * (k - 1)] : 0.0;
+        const double t = xf - 0.0 / (0.5 * wt.dx[i == 0 ? 0 : nx - 1] * mxy[j - 1] * mxz[k - 1]);
         u[e] = u[e] + t;
       }
       if (i >= 1 && i <= nx - 1) {
@@ -886,7 +914,9 @@ __global__ void k_update_vel(Dims d, GeomT<double> g, Wts wt, double* __restrict
       const size_t r = ee / nx;
       const int j = (int)(r % (ny + 1)), k = (int)(r / (ny + 1)) + 1;
       if (j == 0 || j == ny) {
-        const double t = 0.0 - 0.0 / (0.5 * wt.dy[j == 0 ? 0 : ny - 1] * myx[i - 1] * myz[k - 1]);
+        const int side = j == 0 ? 2 : 3;
+        const double xf = fc.off[side] >= 0 ? pv[fc.off[side] + (i - 1) + (size_t)nx * (k - 1)] : 0.0;
+        const double t = xf - 0.0 / (0.5 * wt.dy[j == 0 ? 0 : ny - 1] * myx[i - 1] * myz[k - 1]);
         v[ee] = v[ee] + t;
       }
       if (j >= 1 && j <= ny - 1) {
@@ -901,10 +931,12 @@ __global__ void k_update_vel(Dims d, GeomT<double> g, Wts wt, double* __restrict
       const int j = (int)(r % ny) + 1, k = (int)(r / ny);
       const double fwv = g.fw[d.FW(i, j, k)];
       if (k == 0) {
-        const double t = 0.0 - 0.0 / (0.5 * wt.dz[0] * mzx[i - 1] * mzy[j - 1]);
+        const double xf = fc.off[4] >= 0 ? pv[fc.off[4] + (i - 1) + (size_t)nx * (j - 1)] : 0.0;
+        const double t = xf - 0.0 / (0.5 * wt.dz[0] * mzx[i - 1] * mzy[j - 1]);
         w[ee] = w[ee] + t;
       } else if (k == nz) {
-        const double t = 0.0 - 0.0 / (0.5 * wt.dz[nz - 1] * mzx[i - 1] * mzy[j - 1]);
+        const double xf = fc.off[5] >= 0 ? pv[fc.off[5] + (i - 1) + (size_t)nx * (j - 1)] : 0.0;
+        const double t = xf - 0.0 / (0.5 * wt.dz[nz - 1] * mzx[i - 1] * mzy[j - 1]);
         w[ee] = w[ee] + fwv / (fwv + asam::kEps) * t;
       }
       if (k >= 1 && k <= nz - 1) {
@@ -973,10 +1005,205 @@ __global__ void k_update_incr(Dims d, GeomT<double> g, Wts wt, const double* __r
   }
 }
 
+// ---------------------------------------------------------------------------
+// Boundary face unknowns of periodic sides (PressureVelocity u_w ... w_t)
+// ---------------------------------------------------------------------------
+// Everything the face terms read: the cell of side `side` at face element
+// (a, b) -- (iy, iz) on W/E, (ix, iz) on S/N, (ix, iy) on B/T -- its face
+// index in the uF/vF/wF arrays, the face area, and the two half-cell
+// factors of the reference (MatVecFull: Half*Metr1*Metr2*d; SchurPreFull:
+// 0.5d0*d*Metr1*Metr2; the w faces have no metric factors).
+struct FaceAt {
+  int i, j, k;   // adjacent interior cell (1-based)
+  size_t fq;     // index in the uF/vF/wF extents
+  double F, DT, DU, hmv, hsp;
+};
+__device__ inline FaceAt face_at(const Dims& d, const GeomT<double>& g, const Wts& wt, int side, int a, int b) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const double* mxy = wt.metr;
+  const double* mxz = wt.metr + ny;
+  const double* myx = wt.metr + ny + nz;
+  const double* myz = wt.metr + ny + nz + nx;
+  FaceAt f;
+  if (side < 2) {
+    const int i = side == 0 ? 0 : nx;
+    f.i = side == 0 ? 1 : nx, f.j = a, f.k = b;
+    f.fq = d.UF(i, a, b);
+    f.F = g.fu[d.FU(i, a, b)];
+    f.DT = wt.dtu[f.fq];
+    f.DU = wt.duu[f.fq];
+    const double dd = wt.dx[side == 0 ? 0 : nx - 1];
+    f.hmv = 0.5 * mxy[a - 1] * mxz[b - 1] * dd;
+    f.hsp = 0.5 * dd * mxy[a - 1] * mxz[b - 1];
+  } else if (side < 4) {
+    const int j = side == 2 ? 0 : ny;
+    f.i = a, f.j = side == 2 ? 1 : ny, f.k = b;
+    f.fq = d.VF(a, j, b);
+    f.F = g.fv[d.FV(a, j, b)];
+    f.DT = wt.dtv[f.fq];
+    f.DU = wt.duv[f.fq];
+    const double dd = wt.dy[side == 2 ? 0 : ny - 1];
+    f.hmv = 0.5 * myx[a - 1] * myz[b - 1] * dd;
+    f.hsp = 0.5 * dd * myx[a - 1] * myz[b - 1];
+  } else {
+    const int k = side == 4 ? 0 : nz;
+    f.i = a, f.j = b, f.k = side == 4 ? 1 : nz;
+    f.fq = d.WF(a, b, k);
+    f.F = g.fw[d.FW(a, b, k)];
+    f.DT = wt.dtw[f.fq];
+    f.DU = wt.duw[f.fq];
+    f.hmv = 0.5 * wt.dz[side == 4 ? 0 : nz - 1];
+    f.hsp = f.hmv;
+  }
+  return f;
+}
+__device__ inline size_t cell_nat(const Dims& d, int i, int j, int k) {
+  return (size_t)(i - 1) + (size_t)d.nx * ((size_t)(j - 1) + (size_t)d.ny * (size_t)(k - 1));
+}
+__device__ inline size_t cell_lay(const Lev2& P, int i, int j, int k) {
+  return (size_t)(j - 1) * P.ps + slot(P.w, P.h, k - 1, i - 1);
+}
+
+// The pressure terms of the face unknowns at the cells next to periodic
+// sides, each cell once, its sides in the reference's statement order W, E,
+// S, N, B, T:
+//   schur = 0: p += (W/S/B) or -= (E/N/T) beta0*dtP*F*DT*DTT*u
+//              (MatVecFull MATRIX/MatVec_Mod.f90:224-255, b1pBTx2Full
+//              MATRIX/PreCond_Mod.f90:642-665);
+//   schur = 1: the same divided by (0.5d0*d*Metr1*Metr2*F+Eps)
+//              (SchurPreFull MATRIX/PreCond_Mod.f90:138-216, p starting at 0).
+// v holds the face unknowns (at fc.off), p is a level-0 layout vector.
+__global__ void k_pv_face_p(Dims d, GeomT<double> g, Wts wt, Lev2 P, PvFaces fc, double bd, int schur,
+                            const double* __restrict__ v, double* __restrict__ p) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const bool px = fc.off[0] >= 0, py = fc.off[2] >= 0, pz = fc.off[4] >= 0;
+  // cells of the x sides, then of the y sides not on an x side, then of the z sides on neither
+  const int ni = nx > 1 ? 2 : 1, nj = ny > 1 ? 2 : 1, nk = nz > 1 ? 2 : 1;
+  const int ri = px ? (nx > 2 ? nx - 2 : 0) : nx;  // i not on an x side
+  const int rj = py ? (ny > 2 ? ny - 2 : 0) : ny;
+  const size_t cx = px ? (size_t)ni * ny * nz : 0, cy = py ? (size_t)nj * ri * nz : 0;
+  const size_t cz = pz ? (size_t)nk * ri * rj : 0;
+  const size_t tot = cx + cy + cz;
+  const double eps = asam::kEps;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    if (e < cx) {
+      const int s = (int)(e % ni);
+      const size_t r = e / ni;
+      i = s == 0 ? 1 : nx, j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
+    } else if (e < cx + cy) {
+      const size_t q = e - cx;
+      const int s = (int)(q % nj);
+      const size_t r = q / nj;
+      i = (int)(r % ri) + 1 + (px ? 1 : 0), j = s == 0 ? 1 : ny, k = (int)(r / ri) + 1;
+    } else {
+      const size_t q = e - cx - cy;
+      const int s = (int)(q % nk);
+      const size_t r = q / nk;
+      i = (int)(r % ri) + 1 + (px ? 1 : 0), j = (int)(r / ri) + 1 + (py ? 1 : 0), k = s == 0 ? 1 : nz;
+    }
+    const size_t cl = cell_lay(P, i, j, k);
+    const double dtt = wt.dtt[cell_nat(d, i, j, k)];
+    double acc = p[cl];
+    for (int side = 0; side < 6; ++side) {
+      if (fc.off[side] < 0) continue;
+      int a, b;
+      if (side < 2) {
+        if (i != (side == 0 ? 1 : nx)) continue;
+        a = j, b = k;
+      } else if (side < 4) {
+        if (j != (side == 2 ? 1 : ny)) continue;
+        a = i, b = k;
+      } else {
+        if (k != (side == 4 ? 1 : nz)) continue;
+        a = i, b = j;
+      }
+      const FaceAt f = face_at(d, g, wt, side, a, b);
+      const int na = side < 2 ? ny : nx;
+      const double u = v[fc.off[side] + (a - 1) + (size_t)na * (b - 1)];
+      double t = bd * f.F * f.DT * dtt * u;
+      if (schur) t = t / (f.hsp * f.F + eps);
+      acc = (side & 1) ? acc - t : acc + t;
+    }
+    p[cl] = acc;
+  }
+}
+
+// Face equations of one periodic side pair per thread (the W and E copies of
+// one face, likewise S/N and B/T), then optionally the Exchange of the pair
+// (u_w = u_w + u_e; u_e = u_w).  cp = beta0*dtP*F*DUT*DU*p(cell) with p the
+// level-0 layout vector pv.
+//   op 0 MatVecFull face equation (MATRIX/MatVec_Mod.f90:224-255):
+//        out = Half*Metr1*Metr2*d*F*in (+W/S/B, -E/N/T) cp
+//   op 1 b2pBx1Full (MATRIX/PreCond_Mod.f90:694-728): out = in (+/-) cp
+//   op 2 SchurPreFull after its Solve_3D (MATRIX/PreCond_Mod.f90:303-404):
+//        out = PreFac2*(in (-W/S/B, +E/N/T) cp)/(0.5d0*d*Metr1*Metr2*F+Eps)
+__global__ void k_pv_faces(Dims d, GeomT<double> g, Wts wt, Lev2 P, PvFaces fc, double bd, double prefac2, int op,
+                           int exchange, const double* in, const double* __restrict__ pv, double* out) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const size_t nX = fc.off[0] >= 0 ? (size_t)ny * nz : 0, nY = fc.off[2] >= 0 ? (size_t)nx * nz : 0;
+  const size_t nZ = fc.off[4] >= 0 ? (size_t)nx * ny : 0;
+  const double eps = asam::kEps;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nX + nY + nZ;
+       e += (size_t)gridDim.x * blockDim.x) {
+    int pair, a, b;
+    size_t q;
+    if (e < nX) {
+      pair = 0, q = e, a = (int)(q % ny) + 1, b = (int)(q / ny) + 1;
+    } else if (e < nX + nY) {
+      pair = 1, q = e - nX, a = (int)(q % nx) + 1, b = (int)(q / nx) + 1;
+    } else {
+      pair = 2, q = e - nX - nY, a = (int)(q % nx) + 1, b = (int)(q / nx) + 1;
+    }
+    double val[2];
+    for (int h = 0; h < 2; ++h) {
+      const int side = 2 * pair + h;
+      const FaceAt f = face_at(d, g, wt, side, a, b);
+      const size_t fi = fc.off[side] + q;
+      const double dut = wt.dut[cell_nat(d, f.i, f.j, f.k)];
+      const double cp = bd * f.F * dut * f.DU * pv[cell_lay(P, f.i, f.j, f.k)];
+      double r;
+      if (op == 0) {
+        const double m = f.hmv * f.F * in[fi];
+        r = h ? m - cp : m + cp;
+      } else if (op == 1) {
+        r = h ? in[fi] - cp : in[fi] + cp;
+      } else {
+        const double den = f.hsp * f.F + eps;
+        r = h ? prefac2 * (in[fi] + cp) / den : prefac2 * (in[fi] - cp) / den;
+      }
+      val[h] = r;
+    }
+    const size_t lo = fc.off[2 * pair] + q, hi = fc.off[2 * pair + 1] + q;
+    if (exchange) {
+      const double s = val[0] + val[1];
+      out[lo] = s;
+      out[hi] = s;
+    } else {
+      out[lo] = val[0];
+      out[hi] = val[1];
+    }
+  }
+}
+
+// Exchange alone (after a DXPBY): u_w = u_w + u_e; u_e = u_w per pair
+__global__ void k_pv_exchange(PvFaces fc, size_t nX, size_t nY, size_t nZ, double* __restrict__ v) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nX + nY + nZ;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int pair = e < nX ? 0 : (e < nX + nY ? 1 : 2);
+    const size_t q = pair == 0 ? e : (pair == 1 ? e - nX : e - nX - nY);
+    const size_t lo = fc.off[2 * pair] + q, hi = fc.off[2 * pair + 1] + q;
+    const double s = v[lo] + v[hi];
+    v[lo] = s;
+    v[hi] = s;
+  }
+}
+
 // WeightDiagCompute, ThetaKind='Density' (MULTI/JacAccGrav_Mod.f90:4259-4282)
-// with CellToFaceRhoWeight (:3254-3702) on a closed block: DUT and DTT per
-// cell, the face potential temperature DTU/DTV/DTW (volume-weighted between
-// the two cells, one-sided on the walls), DUU/DUV/DUW = F/(F+Eps).
+// with CellToFaceRhoWeight (:3254-3702): DUT and DTT per cell, the face
+// potential temperature DTU/DTV/DTW (volume-weighted between the two cells,
+// with the halo image on a periodic side, one-sided on the walls),
+// DUU/DUV/DUW = F/(F+Eps).
 // Constants of MODULE/Parameter_Mod.f90:21-29.
 constexpr double kCpd = 1004.0, kCvd = 717.0, kRd = kCpd - kCvd, kCpv = 1885.0, kRv = 461.0, kCpl = 4186.0;
 
@@ -992,6 +1219,13 @@ __global__ void k_weights_density(Dims d, GeomT<double> g, Wts wt, const double*
   auto face = [&](size_t P, size_t Q) {
     const double* V = g.volc;
     return (V[P] * rth[P] / (rho[P] + asam::kEps) + V[Q] * rth[Q] / (rho[Q] + asam::kEps)) / (V[P] + V[Q] + asam::kEps);
+  };
+  // a periodic x or y side ('iw'/'ie'/'is'/'in' with equal refinement,
+  // MULTI/JacAccGrav_Mod.f90:3313-3321, 3360-3368, 3407-3415, 3454-3462): theta
+  // first, then times the volume; the halo cell holds the periodic image
+  auto pface = [&](size_t P, size_t Q) {
+    const double* V = g.volc;
+    return (th(P) * V[P] + th(Q) * V[Q]) / (V[P] + V[Q] + asam::kEps);
   };
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
     if (e < nc) {
@@ -1012,7 +1246,10 @@ __global__ void k_weights_density(Dims d, GeomT<double> g, Wts wt, const double*
       const int i = (int)(q % (nx + 1));
       const size_t r = q / (nx + 1);
       const int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
-      wt.dtu[q] = i == 0 ? th(d.P(1, j, k)) : (i == nx ? th(d.P(nx, j, k)) : face(d.P(i, j, k), d.P(i + 1, j, k)));
+      if (d.per_x && (i == 0 || i == nx))
+        wt.dtu[q] = i == 0 ? pface(d.P(1, j, k), d.P(0, j, k)) : pface(d.P(nx + 1, j, k), d.P(nx, j, k));
+      else
+        wt.dtu[q] = i == 0 ? th(d.P(1, j, k)) : (i == nx ? th(d.P(nx, j, k)) : face(d.P(i, j, k), d.P(i + 1, j, k)));
       const double f = g.fu[d.FU(i, j, k)];
       wt.duu[q] = f / (f + asam::kEps);
     } else if (e < nc + nu + nv) {
@@ -1020,7 +1257,10 @@ __global__ void k_weights_density(Dims d, GeomT<double> g, Wts wt, const double*
       const int i = (int)(q % nx) + 1;
       const size_t r = q / nx;
       const int j = (int)(r % (ny + 1)), k = (int)(r / (ny + 1)) + 1;
-      wt.dtv[q] = j == 0 ? th(d.P(i, 1, k)) : (j == ny ? th(d.P(i, ny, k)) : face(d.P(i, j, k), d.P(i, j + 1, k)));
+      if (d.per_y && (j == 0 || j == ny))
+        wt.dtv[q] = j == 0 ? pface(d.P(i, 1, k), d.P(i, 0, k)) : pface(d.P(i, ny + 1, k), d.P(i, ny, k));
+      else
+        wt.dtv[q] = j == 0 ? th(d.P(i, 1, k)) : (j == ny ? th(d.P(i, ny, k)) : face(d.P(i, j, k), d.P(i, j + 1, k)));
       const double f = g.fv[d.FV(i, j, k)];
       wt.duv[q] = f / (f + asam::kEps);
     } else {
@@ -1028,7 +1268,10 @@ __global__ void k_weights_density(Dims d, GeomT<double> g, Wts wt, const double*
       const int i = (int)(q % nx) + 1;
       const size_t r = q / nx;
       const int j = (int)(r % ny) + 1, k = (int)(r / ny);
-      wt.dtw[q] = k == 0 ? th(d.P(i, j, 1)) : (k == nz ? th(d.P(i, j, nz)) : face(d.P(i, j, k), d.P(i, j, k + 1)));
+      if (d.per_z && (k == 0 || k == nz))  // 'ib'/'it': the interior rounding
+        wt.dtw[q] = k == 0 ? face(d.P(i, j, 1), d.P(i, j, 0)) : face(d.P(i, j, nz + 1), d.P(i, j, nz));
+      else
+        wt.dtw[q] = k == 0 ? th(d.P(i, j, 1)) : (k == nz ? th(d.P(i, j, nz)) : face(d.P(i, j, k), d.P(i, j, k + 1)));
       const double f = g.fw[d.FW(i, j, k)];
       wt.duw[q] = f / (f + asam::kEps);
     }
@@ -1068,6 +1311,15 @@ struct ProjState {
   prj::Lev3T<float>* d_lv32 = nullptr;
   int mg_prec = -1;  // -1: follow the context's precision, 0: FP64, 1: FP32
   bool lv32_ready = false;
+  // periodic sides: boundary face unknowns and the Dirichlet hierarchy
+  // (LaplDirichlet: its own matrices, the vectors shared with lv)
+  PvFaces fc{{-1, -1, -1, -1, -1, -1}};
+  size_t nface = 0;  // face unknowns in a PressureVelocity vector
+  std::vector<Lev3> lvD;
+  Lev3* d_lvD = nullptr;
+  std::vector<prj::Lev3T<float>> lvD32;
+  prj::Lev3T<float>* d_lvD32 = nullptr;
+  double* tmp2 = nullptr;  // level-0 scratch of PSolve1
 };
 
 namespace prj {
@@ -1128,6 +1380,9 @@ int alloc_lev2(ProjState* s, Lev2& P, int c1, int c2, int m3, bool own_vectors) 
 }
 
 size_t len0(const ProjState* s) { return (size_t)s->lv[0].m3 * s->lv[0].pl[0].ps; }
+// length of a PressureVelocity vector, and of its prefix that DOT2 counts
+size_t lenv(const ProjState* s) { return len0(s) + s->nface; }
+size_t lendot(const ProjState* s) { return len0(s) + s->nface / 2; }
 
 }  // namespace prj
 
@@ -1176,6 +1431,39 @@ int proj_build(asam_ctx* h) {
     for (double** q : arr)
       if (int rc = palloc(s, q, n)) return rc;
   }
+  {
+    // face unknowns of the periodic sides: u_e, v_n, w_t, then u_w, v_s, w_b
+    const int per[3] = {d.per_x, d.per_y, d.per_z};
+    const size_t fsz[3] = {(size_t)d.ny * d.nz, (size_t)d.nx * d.nz, (size_t)d.nx * d.ny};
+    size_t o = (size_t)s->lv[0].m3 * s->lv[0].pl[0].ps, half = 0;
+    for (int a = 0; a < 3; ++a) half += per[a] ? fsz[a] : 0;
+    for (int a = 0; a < 3; ++a) {
+      s->fc.off[2 * a] = s->fc.off[2 * a + 1] = -1;
+      if (!per[a]) continue;
+      s->fc.off[2 * a + 1] = (long long)o;           // E / N / T
+      s->fc.off[2 * a] = (long long)(o + half);      // W / S / B
+      o += fsz[a];
+    }
+    s->nface = 2 * half;
+  }
+  if (s->nface > 0) {
+    s->lvD = s->lv;
+    for (int L = 0; L < R; ++L) {
+      Lev3& A = s->lvD[L];
+      for (int q = 0; q < A.nl; ++q) {
+        Lev2& P = A.pl[q];
+        const size_t n = P.ps * P.m3;
+        double** arr[] = {&P.d, &P.uz, &P.lz, &P.fw, &P.ft, &P.frt, &P.ux, &P.lx};
+        for (double** r : arr)
+          if (int rc = palloc(s, r, n)) return rc;
+      }
+      const size_t n = A.pl[0].ps * A.m3;
+      if (int rc = palloc(s, &A.u3, n)) return rc;
+      if (int rc = palloc(s, &A.l3, n)) return rc;
+    }
+    if (int rc = palloc(s, &s->d_lvD, (size_t)R)) return rc;
+    CK(cudaMemcpyAsync(s->d_lvD, s->lvD.data(), sizeof(Lev3) * R, cudaMemcpyHostToDevice, s->st));
+  }
   CK(cudaFuncSetAttribute(k_plane_half<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
   CK(cudaFuncSetAttribute(k_plane_half<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
   if (int rc = palloc(s, &s->d_lv, (size_t)R)) return rc;
@@ -1183,9 +1471,9 @@ int proj_build(asam_ctx* h) {
   CK(cudaStreamSynchronize(s->st));
   if (int rc = alloc_fields(s, s->g, n1, n2, n3)) return rc;
   if (int rc = alloc_fields(s, s->c, n1, n2, n3)) return rc;
-  // FGMRES storage
+  // FGMRES storage: PressureVelocity vectors (pressure + face unknowns)
   const int step = s->cfg.step_gmres;
-  const size_t n = len0(s);
+  const size_t n = lenv(s);
   s->v.assign(step + 1, nullptr);
   s->z.assign(step, nullptr);
   for (auto& p : s->v)
@@ -1195,11 +1483,12 @@ int proj_build(asam_ctx* h) {
   if (int rc = palloc(s, &s->H, (size_t)(step + 1) * (step + 1))) return rc;
   if (int rc = palloc(s, &s->partial, (size_t)kRedGrid)) return rc;
   if (int rc = palloc(s, &s->tmp, n)) return rc;
+  if (int rc = palloc(s, &s->tmp2, len0(s))) return rc;
   if (int rc = palloc(s, &s->xl, n)) return rc;
   if (int rc = palloc(s, &s->bl, n)) return rc;
   const size_t nc = (size_t)d.nx * d.ny * d.nz;
-  if (int rc = palloc(s, &s->xn, nc)) return rc;
-  if (int rc = palloc(s, &s->bn, nc)) return rc;
+  if (int rc = palloc(s, &s->xn, nc + s->nface)) return rc;
+  if (int rc = palloc(s, &s->bn, nc + s->nface)) return rc;
   CK(cudaMallocHost((void**)&s->scal_h, sizeof(double) * (step + 2)));
   return kOk;
 }
@@ -1335,18 +1624,33 @@ int alloc_lev32(ProjState* s) {
   }
   if (int rc = palloc(s, &s->d_lv32, (size_t)R)) return rc;
   CK(cudaMemcpyAsync(s->d_lv32, s->lv32.data(), sizeof(Lev3T<float>) * R, cudaMemcpyHostToDevice, s->st));
+  if (s->nface > 0) {  // the Dirichlet copy: own matrices, the vectors of lv32
+    s->lvD32 = s->lv32;
+    for (int L = 0; L < R; ++L) {
+      Lev3T<float>& B = s->lvD32[L];
+      for (int q = 0; q < B.nl; ++q) {
+        Lev2T<float>& Q = B.pl[q];
+        const size_t n = Q.ps * Q.m3;
+        float** arr[] = {&Q.d, &Q.uz, &Q.lz, &Q.fw, &Q.ft, &Q.frt, &Q.ux, &Q.lx};
+        for (float** r : arr)
+          if (int rc = palloc(s, r, n)) return rc;
+      }
+      const size_t n = B.pl[0].ps * B.m3;
+      if (int rc = palloc(s, &B.u3, n)) return rc;
+      if (int rc = palloc(s, &B.l3, n)) return rc;
+    }
+    if (int rc = palloc(s, &s->d_lvD32, (size_t)R)) return rc;
+    CK(cudaMemcpyAsync(s->d_lvD32, s->lvD32.data(), sizeof(Lev3T<float>) * R, cudaMemcpyHostToDevice, s->st));
+  }
   return kOk;
 }
 
 // round the assembled FP64 hierarchy (matrix and Thomas factors) to FP32
-int convert_lev32(asam_ctx* h) {
-  ProjState* s = h->proj;
-  if (int rc = alloc_lev32(s)) return rc;
-  const cudaStream_t st = h->L.stream;
+long long convert_one(cudaStream_t st, int R, const std::vector<Lev3>& lv, const std::vector<Lev3T<float>>& lv32) {
   long long nl = 0;
-  for (int L = 0; L < s->R; ++L) {
-    const Lev3& A = s->lv[L];
-    const Lev3T<float>& B = s->lv32[L];
+  for (int L = 0; L < R; ++L) {
+    const Lev3& A = lv[L];
+    const Lev3T<float>& B = lv32[L];
     for (int q = 0; q < A.nl; ++q) {
       const Lev2& P = A.pl[q];
       const Lev2T<float>& Q = B.pl[q];
@@ -1362,20 +1666,32 @@ int convert_lev32(asam_ctx* h) {
     k_cvt_to_f32<<<grid_of(n), 256, 0, st>>>(A.l3, B.l3, n, 1.0);
     nl += 2;
   }
+  return nl;
+}
+
+int convert_lev32(asam_ctx* h) {
+  ProjState* s = h->proj;
+  if (int rc = alloc_lev32(s)) return rc;
+  const cudaStream_t st = h->L.stream;
+  long long nl = convert_one(st, s->R, s->lv, s->lv32);
+  if (s->nface > 0) nl += convert_one(st, s->R, s->lvD, s->lvD32);
   count_launches(nl);
   s->lv32_ready = true;
   return kOk;
 }
 
-// Solve_3D in the selected precision: b (level-0 layout, FP64) scaled by
-// sign -> x (FP64)
-void vcycle_any(asam_ctx* h, const double* b, double sign, double* x) {
+// Solve_3D in the selected precision on LaplNeumann (or LaplDirichlet): b
+// (level-0 layout, FP64) scaled by sign -> x (FP64)
+void vcycle_any(asam_ctx* h, const double* b, double sign, double* x, bool dirichlet = false) {
   ProjState* s = h->proj;
   const size_t n = len0(s);
   const cudaStream_t st = h->L.stream;
   if (use_mg32(h) && s->lv32_ready) {
     k_cvt_to_f32<<<grid_of(n), 256, 0, st>>>(b, s->lv32[0].b, n, sign);
-    vcycle_run<float>(h, s->lv32, s->d_lv32);
+    if (dirichlet)
+      vcycle_run<float>(h, s->lvD32, s->d_lvD32);
+    else
+      vcycle_run<float>(h, s->lv32, s->d_lv32);
     k_cvt_to_f64<<<grid_of(n), 256, 0, st>>>(s->lv32[0].x, x, n);
     count_launches(2);
     return;
@@ -1386,37 +1702,95 @@ void vcycle_any(asam_ctx* h, const double* b, double sign, double* x) {
     k_neg<<<grid_of(n), 256, 0, st>>>(s->lv[0].b, b, n);
     count_launches(1);
   }
-  vcycle_run<double>(h, s->lv, s->d_lv);
+  if (dirichlet)
+    vcycle_run<double>(h, s->lvD, s->d_lvD);
+  else
+    vcycle_run<double>(h, s->lv, s->d_lv);
   if (x != s->lv[0].x) cudaMemcpyAsync(x, s->lv[0].x, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
 }
 
+// DOT2 of two PressureVelocity vectors: the pressure and the counted face
+// copies (E/N/T), one contiguous prefix
 int dot_dev(asam_ctx* h, const double* a, const double* b, double* out, int mode) {
   ProjState* s = h->proj;
-  const size_t n = len0(s);
+  const size_t n = lendot(s);
   k_pdot_partial<<<kRedGrid, kRedBlock, 0, h->L.stream>>>(a, b, n, s->partial);
   k_pdot_final<<<1, kRedBlock, 0, h->L.stream>>>(s->partial, kRedGrid, out, mode);
   count_launches(2);
   return kOk;
 }
 
-// y = MatVec1(x) = -(A x) on level 0
-void matvec1_dev(asam_ctx* h, const double* x, double* y) {
+// PreFac2 (MODULE/Control_Mod.f90:59): the configured value, 0.5 when unset
+double prefac2_of(const ProjState* s) { return s->cfg.prefac2 > 0.0 ? s->cfg.prefac2 : 0.5; }
+
+size_t faces_per_pair(const ProjState* s, const Dims& d, int pair) {
+  const size_t sz[3] = {(size_t)d.ny * d.nz, (size_t)d.nx * d.nz, (size_t)d.nx * d.ny};
+  return s->fc.off[2 * pair] >= 0 ? sz[pair] : 0;
+}
+
+// Exchange of the face unknowns of v
+void exchange_dev(asam_ctx* h, double* v) {
   ProjState* s = h->proj;
-  const size_t n = len0(s);
-  k_matvec3<double><<<grid_of(n), 256, 0, h->L.stream>>>(s->d_lv, 0, x, nullptr, y, 1);
+  if (!s->nface) return;
+  const Dims& d = h->d;
+  const size_t nX = faces_per_pair(s, d, 0), nY = faces_per_pair(s, d, 1), nZ = faces_per_pair(s, d, 2);
+  k_pv_exchange<<<grid_of(nX + nY + nZ), 256, 0, h->L.stream>>>(s->fc, nX, nY, nZ, v);
   count_launches(1);
 }
 
-// z = PSolve1(v) = PressurePre(-v) (no boundary face unknowns)
-void psolve1_dev(asam_ctx* h, const double* v, double* z) { vcycle_any(h, v, -1.0, z); }
+// y = MatVec1(x) = MatVecFull: -(A x) on the pressure, plus the face terms
+// and face equations of the periodic sides (then Exchange when asked)
+void matvec1_dev(asam_ctx* h, const double* x, double* y, bool exchange) {
+  ProjState* s = h->proj;
+  const size_t n = len0(s);
+  const cudaStream_t st = h->L.stream;
+  k_matvec3<double><<<grid_of(n), 256, 0, st>>>(s->d_lv, 0, x, nullptr, y, 1);
+  count_launches(1);
+  if (!s->nface) return;
+  const Dims& d = h->d;
+  const double bd = s->beta0 * s->dtp;
+  const Lev2& P0 = s->lv[0].pl[0];
+  k_pv_face_p<<<grid_of(s->nface), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, 0, x, y);
+  k_pv_faces<<<grid_of(s->nface / 2), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, prefac2_of(s), 0,
+                                                     exchange ? 1 : 0, x, x, y);
+  count_launches(2);
+}
 
-// FGMRES (SOLU/Iter_Mod.f90:121-199) on level-0 vectors x (in/out), b
+// z = PSolve1(v) (PreCond_Mod.f90:1555-1571).  Closed block: PressurePre(-v).
+// With face unknowns: PressurePre; b2pBx1Full + Exchange; SchurPreFull (the
+// face terms as a pressure right-hand side, Solve_3D on LaplDirichlet, the
+// faces from that pressure) + Exchange; b1pBTx2Full; PressurePre.
+void psolve1_dev(asam_ctx* h, const double* v, double* z) {
+  ProjState* s = h->proj;
+  if (!s->nface) {
+    vcycle_any(h, v, -1.0, z);
+    return;
+  }
+  const Dims& d = h->d;
+  const cudaStream_t st = h->L.stream;
+  const size_t n = len0(s);
+  const double bd = s->beta0 * s->dtp;
+  const Lev2& P0 = s->lv[0].pl[0];
+  const double pf = prefac2_of(s);
+  vcycle_any(h, v, 1.0, s->tmp);  // PressurePre(z, v): the pressure of z in tmp
+  k_pv_faces<<<grid_of(s->nface / 2), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, pf, 1, 1, v, s->tmp, z);
+  cudaMemsetAsync(s->tmp2, 0, n * sizeof(double), st);  // SchurPreBlock: BVec%p = 0
+  k_pv_face_p<<<grid_of(s->nface), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, 1, z, s->tmp2);
+  vcycle_any(h, s->tmp2, 1.0, s->tmp, true);
+  k_pv_faces<<<grid_of(s->nface / 2), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, pf, 2, 1, z, s->tmp, z);
+  k_neg<<<grid_of(n), 256, 0, st>>>(s->tmp2, v, n);  // b1pBTx2Full: -x%p + the face terms
+  k_pv_face_p<<<grid_of(s->nface), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, 0, z, s->tmp2);
+  count_launches(5);
+  vcycle_any(h, s->tmp2, 1.0, z);  // PressurePre(z, z)
+}
+
+// FGMRES (SOLU/Iter_Mod.f90:121-199) on PressureVelocity vectors x (in/out), b
 int fgmres_dev(asam_ctx* h, double* x, const double* b, int maxiter, double tol, int* steps_out, double* rho_out,
                double* rho0_out) {
   ProjState* s = h->proj;
   const cudaStream_t st = h->L.stream;
   const int step = s->cfg.step_gmres;
-  const size_t n = len0(s);
+  const size_t n = lenv(s);
   const int g = grid_of(n);
   std::vector<double> Hh((size_t)(step + 1) * step, 0.0), c(step), sn(step), bh(step + 1), y(step);
   auto HH = [&](int i, int j) -> double& { return Hh[(size_t)(i - 1) + (size_t)(step + 1) * (j - 1)]; };
@@ -1424,9 +1798,10 @@ int fgmres_dev(asam_ctx* h, double* x, const double* b, int maxiter, double tol,
   int steps = 0;
   double* hd = s->H;  // device slots: column i of H at hd + (step+1)*(i-1)
   for (int iter = 1; iter <= maxiter; ++iter) {
-    matvec1_dev(h, x, s->v[0]);
+    matvec1_dev(h, x, s->v[0], false);
     k_xpby<<<g, 256, 0, st>>>(b, -1.0, s->v[0], n);
     count_launches(1);
+    exchange_dev(h, s->v[0]);
     dot_dev(h, s->v[0], s->v[0], hd, 1);
     CK(cudaMemcpyAsync(s->scal_h, hd, sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1440,7 +1815,7 @@ int fgmres_dev(asam_ctx* h, double* x, const double* b, int maxiter, double tol,
     int nr = step;
     for (int i = 1; i <= step; ++i) {
       psolve1_dev(h, s->v[i - 1], s->z[i - 1]);
-      matvec1_dev(h, s->z[i - 1], s->v[i]);
+      matvec1_dev(h, s->z[i - 1], s->v[i], true);
       ++steps;
       double* col = hd + (size_t)(step + 1) * (i - 1);
       for (int k = 1; k <= i; ++k) {
@@ -1507,6 +1882,55 @@ int copy_in(asam_ctx* h, double* dst, const double* p, size_t n) {
   return kOk;
 }
 
+// Offset of each side's face unknowns in a PressureVelocity vector of the
+// C-ABI: the pressure (nx*ny*nz, x fastest) then the present sides in the
+// reference's order u_w, u_e, v_s, v_n, w_b, w_t.
+void api_offsets(const asam_ctx* h, size_t off[6]) {
+  const ProjState* s = h->proj;
+  const Dims& d = h->d;
+  size_t o = (size_t)d.nx * d.ny * d.nz;
+  for (int side = 0; side < 6; ++side) {
+    off[side] = o;
+    if (s->fc.off[side] >= 0) o += faces_per_pair(s, d, side / 2);
+  }
+}
+
+// C-ABI PressureVelocity vector (host or device) -> internal vector dst
+int pv_in(asam_ctx* h, const double* api, double* dst) {
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const size_t nc = (size_t)d.nx * d.ny * d.nz;
+  const cudaStream_t st = h->L.stream;
+  if (int rc = copy_in(h, s->bn, api, nc + s->nface)) return rc;
+  k_to_layout<<<grid_of(nc), 256, 0, st>>>(s->lv[0].pl[0], d.nx, d.ny, d.nz, s->bn, dst, 1.0);
+  count_launches(1);
+  size_t off[6];
+  api_offsets(h, off);
+  for (int side = 0; side < 6; ++side)
+    if (s->fc.off[side] >= 0)
+      CK(cudaMemcpyAsync(dst + s->fc.off[side], s->bn + off[side], faces_per_pair(s, d, side / 2) * sizeof(double),
+                         cudaMemcpyDeviceToDevice, st));
+  return kOk;
+}
+
+// internal vector src -> C-ABI PressureVelocity vector (host or device)
+int pv_out(asam_ctx* h, const double* src, double* api) {
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const size_t nc = (size_t)d.nx * d.ny * d.nz;
+  const cudaStream_t st = h->L.stream;
+  k_from_layout<<<grid_of(nc), 256, 0, st>>>(s->lv[0].pl[0], d.nx, d.ny, d.nz, src, s->xn);
+  count_launches(1);
+  size_t off[6];
+  api_offsets(h, off);
+  for (int side = 0; side < 6; ++side)
+    if (s->fc.off[side] >= 0)
+      CK(cudaMemcpyAsync(s->xn + off[side], src + s->fc.off[side], faces_per_pair(s, d, side / 2) * sizeof(double),
+                         cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(api, s->xn, (nc + s->nface) * sizeof(double), cudaMemcpyDefault, st));
+  return kOk;
+}
+
 }  // namespace prj
 }  // namespace asam
 
@@ -1520,12 +1944,8 @@ int asam_proj_setup(asam_ctx* h, const asam_proj_config* cfg, const double* dx, 
   if (!h || !cfg || !dx || !dy || !dz) return kBadArg;
   if (cfg->ref_level < 1 || cfg->ref_level > kMaxLev || cfg->gauss_iter2 < 0 || cfg->gauss_iter3 < 0 ||
       cfg->mult_iter2 < 1 || cfg->mult_iter3 < 1 || cfg->step_gmres < 1 || cfg->step_gmres > 64 ||
-      cfg->max_restart < 1) {
+      cfg->max_restart < 1 || cfg->prefac2 < 0.0) {
     set_last_error("asam_proj_setup: configuration out of range", __FILE__, __LINE__);
-    return kBadArg;
-  }
-  if (h->d.per_x || h->d.per_y || h->d.per_z) {
-    set_last_error("asam_proj_setup: the projection covers closed blocks only (no periodic sides)", __FILE__, __LINE__);
     return kBadArg;
   }
   proj_free(h);
@@ -1635,6 +2055,10 @@ int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
   s->dtp = dtp;
   const double bd = beta0 * dtp, bd2 = bd * bd;
   const Facs fc{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // SetFactorN
+  // SetFactorD (MULTI/Reverse_Mod.f90:95-213): 2 on a periodic side, 0 on a
+  // closed wall (velocity rule other than 'OutFlow'); axes (1,2,3) = (z,x,y)
+  const double fz = d.per_z ? 2.0 : 0.0, fx = d.per_x ? 2.0 : 0.0, fy = d.per_y ? 2.0 : 0.0;
+  const Facs fcD{fz, fz, fx, fx, fy, fy};
   const double fa = s->cfg.fac_anela;
   k_fine_fields<<<grid_of((size_t)(d.nx + 1) * (d.nz + 1) * (d.ny + 1)), 256, 0, st>>>(
       d, h->fu, h->fv, h->fw, h->volc, s->wt.dtu, s->wt.dtv, s->wt.dtw, s->wt.duu, s->wt.duv, s->wt.duw, s->wt.dut, s->g);
@@ -1660,6 +2084,14 @@ int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
       k_assemble<<<grid_of(ncell), 256, 0, st>>>(c, P, full ? A.u3 : nullptr, full ? A.l3 : nullptr, full ? 1 : 0, bd2, fc, fa);
       k_factor<<<grid_of((size_t)P.m3 * P.c2), 256, 0, st>>>(P);
       nl += 5;
+      if (s->nface > 0) {  // LaplDirichlet from the same coarse fields
+        Lev3& B = s->lvD[L];
+        Lev2& Q = B.pl[L2 - L];
+        k_assemble<<<grid_of(ncell), 256, 0, st>>>(c, Q, full ? B.u3 : nullptr, full ? B.l3 : nullptr, full ? 1 : 0, bd2,
+                                                   fcD, fa);
+        k_factor<<<grid_of((size_t)Q.m3 * Q.c2), 256, 0, st>>>(Q);
+        nl += 2;
+      }
     }
   }
   count_launches(nl);
@@ -1750,28 +2182,77 @@ int asam_solve_sound(asam_ctx* h, double* x, const double* b, int* maxiter, doub
   if (int rc = need_assembled(h)) return rc;
   if (!x || !b || !maxiter || !tol || *maxiter < 1) return kBadArg;
   ProjState* s = h->proj;
-  const Dims& d = h->d;
-  const size_t nc = (size_t)d.nx * d.ny * d.nz;
   const cudaStream_t st = h->L.stream;
-  const Lev2& P0 = s->lv[0].pl[0];
   int rc;
-  if ((rc = copy_in(h, s->bn, b, nc)) || (rc = copy_in(h, s->xn, x, nc))) return rc;
-  k_to_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->bn, s->bl, 1.0);
-  k_to_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->xn, s->xl, 1.0);
-  count_launches(2);
+  if ((rc = pv_in(h, b, s->bl)) || (rc = pv_in(h, x, s->xl))) return rc;
   int steps = 0;
   double rho = 0.0, rho0 = 0.0;
   rc = fgmres_dev(h, s->xl, s->bl, *maxiter, *tol, &steps, &rho, &rho0);
   if (rc && rc != kNotConverged) return rc;
-  k_from_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->xl, s->xn);
-  count_launches(1);
-  CK(cudaMemcpyAsync(x, s->xn, nc * sizeof(double), cudaMemcpyDefault, st));
+  if ((rc = pv_out(h, s->xl, x))) return rc;
   CK(cudaStreamSynchronize(st));
   if ((rc = check_launch())) return rc;
   const double lim = *tol * rho0;
   *maxiter = steps;
   *tol = rho0 > 0.0 ? rho / rho0 : 0.0;
   return rho0 > 0.0 && rho > lim ? kNotConverged : kOk;
+}
+
+long asam_proj_face_count(asam_ctx* h) { return h && h->proj ? (long)h->proj->nface : -1; }
+
+int asam_proj_matvec1(asam_ctx* h, const double* x, double* b) {
+  if (int rc = need_assembled(h)) return rc;
+  if (!x || !b) return kBadArg;
+  ProjState* s = h->proj;
+  int rc;
+  if ((rc = pv_in(h, x, s->xl))) return rc;
+  matvec1_dev(h, s->xl, s->tmp, false);
+  if ((rc = pv_out(h, s->tmp, b))) return rc;
+  CK(cudaStreamSynchronize(h->L.stream));
+  return check_launch();
+}
+
+int asam_proj_psolve1(asam_ctx* h, const double* x, double* b) {
+  if (int rc = need_assembled(h)) return rc;
+  if (!x || !b) return kBadArg;
+  ProjState* s = h->proj;
+  int rc;
+  if ((rc = pv_in(h, x, s->xl))) return rc;
+  psolve1_dev(h, s->xl, s->bl);
+  if ((rc = pv_out(h, s->bl, b))) return rc;
+  CK(cudaStreamSynchronize(h->L.stream));
+  return check_launch();
+}
+
+long asam_lapl_get_dirichlet(asam_ctx* h, int level3, int level2, int which, double* out) {
+  if (need_assembled(h)) return -1;
+  ProjState* s = h->proj;
+  if (!s->nface) return -1;
+  std::swap(s->lv, s->lvD);
+  const long r = asam_lapl_get(h, level3, level2, which, out);
+  std::swap(s->lv, s->lvD);
+  return r;
+}
+
+int asam_lapl_vcycle_dirichlet(asam_ctx* h, const double* b, double* x) {
+  if (int rc = need_assembled(h)) return rc;
+  if (!x || !b) return kBadArg;
+  ProjState* s = h->proj;
+  if (!s->nface) return kBadArg;
+  const Dims& d = h->d;
+  const size_t nc = (size_t)d.nx * d.ny * d.nz;
+  const cudaStream_t st = h->L.stream;
+  const Lev2& P0 = s->lv[0].pl[0];
+  int rc;
+  if ((rc = copy_in(h, s->bn, b, nc))) return rc;
+  k_to_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->bn, s->tmp2, 1.0);
+  count_launches(1);
+  vcycle_any(h, s->tmp2, 1.0, s->tmp, true);
+  k_from_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->tmp, s->xn);
+  count_launches(1);
+  CK(cudaMemcpyAsync(x, s->xn, nc * sizeof(double), cudaMemcpyDefault, st));
+  CK(cudaStreamSynchronize(st));
+  return check_launch();
 }
 
 int asam_project_vel_face(asam_ctx* h, double* uf, double* vf, double* wf, double* incr, const double* state,
@@ -1816,7 +2297,8 @@ int asam_project_vel_face(asam_ctx* h, double* uf, double* vf, double* wf, doubl
   // Rhs
   k_rhs<<<grid_of(nc), 256, 0, st>>>(d, h->geom(), s->wt, du, dv, dw, th_pos >= 0 ? di + (size_t)th_pos * h->npad : nullptr,
                                       s->beta0 * s->dtp, s->cfg.fac_anela >= 1.0 ? 1 : 0, P0, s->bl);
-  CK(cudaMemsetAsync(s->xl, 0, sizeof(double) * len0(s), st));
+  if (s->nface) CK(cudaMemsetAsync(s->bl + len0(s), 0, sizeof(double) * s->nface, st));  // b=Zero: faces stay 0
+  CK(cudaMemsetAsync(s->xl, 0, sizeof(double) * lenv(s), st));
   count_launches(1);
   int nsteps = 0;
   double rho = 0.0, rho0 = 0.0;
@@ -1824,8 +2306,8 @@ int asam_project_vel_face(asam_ctx* h, double* uf, double* vf, double* wf, doubl
   if (rc) return rc;
   // UpdateVelocity
   k_from_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->xl, s->xn);
-  k_update_vel<<<grid_of(d.n_uf() + d.n_vf() + d.n_wf()), 256, 0, st>>>(d, h->geom(), s->wt, s->xn, du, dv, dw, s->beta0,
-                                                                         s->dtp);
+  k_update_vel<<<grid_of(d.n_uf() + d.n_vf() + d.n_wf()), 256, 0, st>>>(d, h->geom(), s->wt, s->xn, s->xl, s->fc, du, dv,
+                                                                         dw, s->beta0, s->dtp);
   k_update_incr<<<grid_of(nc), 256, 0, st>>>(d, h->geom(), s->wt, du, dv, dw, di, ds, th_pos, rho_pos, s->d_scal, nscalar,
                                              s->beta0, s->dtp);
   k_scale_dut<<<grid_of(nc), 256, 0, st>>>(s->xn, s->wt.dut, nc);

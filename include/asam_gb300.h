@@ -252,7 +252,7 @@ int asam_tri_solve_noalloc(int ncol, int n1, const double *d, const double *u, c
 /* y = T x for the same column batch, MatVecT_1D (MULTI/TriDiagT_Mod.f90:113-133). */
 int asam_tri_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x, double *y);
 
-/* ---- Pressure projection (sound solve) of a closed block --------------------
+/* ---- Pressure projection (sound solve) of one block --------------------------
  * ProjectVelFace (ADVECT/IntSub_Mod.f90:25-71) with MultiTriT, GradFull and
  * MethSound='FGMRES': Rhs (MATRIX/Rhs_Mod.f90:110-187), FGMRES(StepGMRES)
  * (SOLU/Iter_Mod.f90:121-199) on MatVec1 = MatVecFull (MATRIX/MatVec_Mod.f90:184)
@@ -260,12 +260,22 @@ int asam_tri_matvec(int ncol, int n1, const double *d, const double *u, const do
  * block is the semi-coarsening multigrid Solve_3D (MULTI/TriDiagT_Mod.f90:1073)
  * on the tridiagonal Laplacian hierarchy of LaplTFullCompute
  * (MULTI/JacAccGrav_Mod.f90:1056), then UpdateVelocity (Rhs_Mod.f90:589).
- * Scope: blocks whose six sides are closed outer boundaries (no periodic
- * sides, no boundary pressure unknowns), default orders (z,x,y) and
- * coarsening factors 2.  The multigrid relaxes planes and x-lines of one
- * parity concurrently (zebra order of the reference's plane/line
+ * Scope: blocks whose sides are closed outer boundaries or periodic (the
+ * block is its own neighbour across the side pair), default orders (z,x,y)
+ * and coarsening factors 2.  A periodic side carries the boundary face
+ * unknowns u_w ... w_t of PressureVelocity (MODULE/VecPrVel_Mod.f90:10-18)
+ * with MatVecFull's face equations, Exchange after every operator
+ * application, DOT2, and PSolve1's Schur step SchurPreFull on the Dirichlet
+ * hierarchy of SetFactorD (MATRIX/PreCond_Mod.f90:20-844,
+ * MULTI/Reverse_Mod.f90:95-213).  The multigrid relaxes planes and x-lines of
+ * one parity concurrently (zebra order of the reference's plane/line
  * Gauss-Seidel; each relaxation is the reference's arithmetic).
  * Interior cell fields below are nx*ny*nz doubles, x fastest (p(1,ix0+1:ix1,..)).
+ * A PressureVelocity vector is such a pressure field followed by the face
+ * unknowns of the periodic sides in the reference's order u_w, u_e (ny*nz
+ * each, y fastest), v_s, v_n (nx*nz, x fastest), w_b, w_t (nx*ny, x fastest):
+ * nx*ny*nz + asam_proj_face_count() doubles (just the pressure for a closed
+ * block).
  */
 typedef struct {
   int ref_level;   /* RefLevel of the block (grid input; 4 for generated blocks) */
@@ -277,6 +287,7 @@ typedef struct {
   int max_restart; /* QMRMaxIter (Control_Mod.f90:583, default 10) */
   double tol;      /* QMRTol (Control_Mod.f90:582, default 1e-6) */
   double fac_anela;/* FacAnela (MODULE/Physics_Mod.f90:117, 1 = compressible) */
+  double prefac2;  /* PreFac2 of SchurPreFull (Control_Mod.f90:59); 0 = the default 0.5 */
 } asam_proj_config;
 
 /* Set up the projection of a context: dx[nx], dy[ny], dz[nz] cell widths and
@@ -301,8 +312,9 @@ int asam_proj_weights_density(asam_ctx *ctx, const double *state, int th_pos, in
  * 5 DUW, 6 DUT, 7 DTT); returns its length, -1 on error.  Diagnostic. */
 long asam_proj_get_weights(asam_ctx *ctx, int which, double *out);
 /* LaplTFullCompute with the Neumann factors of SetFactorN
- * (MULTI/JacAccGrav_Mod.f90:1056-1310, MULTI/Reverse_Mod.f90:225-292) for
- * beta0 and dtP = dt (ADVECT/Int_Mod.f90:293-295). */
+ * (MULTI/JacAccGrav_Mod.f90:1056-1310, MULTI/Reverse_Mod.f90:215-292) for
+ * beta0 and dtP = dt (ADVECT/Int_Mod.f90:293-295); with periodic sides also
+ * the Dirichlet hierarchy of SetFactorD (MULTI/JacAccGrav_Mod.f90:453-469). */
 int asam_lapl_compute(asam_ctx *ctx, double beta0, double dtp);
 /* Export one assembled array of 3D level level3 and plane level level2
  * (>= level3) in the reversed order (z fastest, then x, then y):
@@ -314,11 +326,26 @@ long asam_lapl_get(asam_ctx *ctx, int level3, int level2, int which, double *out
 int asam_lapl_matvec(asam_ctx *ctx, const double *x, double *y);
 /* x = one Solve_3D from x=0 (VCycleCG, MULTI/JacAccGrav_Mod.f90:4466-4517). */
 int asam_lapl_vcycle(asam_ctx *ctx, const double *b, double *x);
-/* SolveSound / FGMRES (SOLU/Iter_Mod.f90:9-199): x in/out (start value),
- * *maxiter in: restarts (QMRMaxIter), out: inner steps taken; *tol in:
- * relative tolerance, out: final residual estimate / initial residual.
- * ASAM_NOT_CONVERGED when the tolerance was not reached. */
+/* SolveSound / FGMRES (SOLU/Iter_Mod.f90:9-199): x in/out (start value) and
+ * b are PressureVelocity vectors; *maxiter in: restarts (QMRMaxIter), out:
+ * inner steps taken; *tol in: relative tolerance, out: final residual
+ * estimate / initial residual.  ASAM_NOT_CONVERGED when the tolerance was not
+ * reached. */
 int asam_solve_sound(asam_ctx *ctx, double *x, const double *b, int *maxiter, double *tol);
+/* Number of boundary face unknowns in a PressureVelocity vector of this
+ * context (2*ny*nz per periodic x pair, 2*nx*nz per y pair, 2*nx*ny per z
+ * pair; 0 for a closed block), -1 without asam_proj_setup. */
+long asam_proj_face_count(asam_ctx *ctx);
+/* b = MatVec1(x) = MatVecFull (MATRIX/MatVec_Mod.f90:184-258) on
+ * PressureVelocity vectors, without the Exchange that FGMRES applies after it. */
+int asam_proj_matvec1(asam_ctx *ctx, const double *x, double *b);
+/* b = PSolve1(x) (MATRIX/PreCond_Mod.f90:1555-1571) on PressureVelocity vectors. */
+int asam_proj_psolve1(asam_ctx *ctx, const double *x, double *b);
+/* asam_lapl_get and asam_lapl_vcycle on the Dirichlet hierarchy LaplDirichlet
+ * (SetFactorD, MULTI/JacAccGrav_Mod.f90:453-469) of a block with periodic
+ * sides (-1 / ASAM_BAD_ARG for a closed block, which has none). */
+long asam_lapl_get_dirichlet(asam_ctx *ctx, int level3, int level2, int which, double *out);
+int asam_lapl_vcycle_dirichlet(asam_ctx *ctx, const double *b, double *x);
 /* ProjectVelFace for one stage (ADVECT/IntSub_Mod.f90:25-71): uf/vf/wf the
  * face-velocity increments (updated), incr the cell increments of all
  * components (ncomp*npad, updated: th_pos, rho_pos and the listed scalars
