@@ -235,10 +235,18 @@ def close_dead_faces(geo: Geometry) -> Geometry:
     nx, ny, nz = g.nx, g.ny, g.nz
     dead = geo.volc[1:nz + 1, 1:ny + 1, 1:nx + 1] <= 0.0
     k, j, i = np.nonzero(dead)
-    geo.fu[k, j, i + 1] = 0.0      # west face of interior cell i+1 (FU index i)
-    geo.fu[k, j, i + 2] = 0.0      # east face
-    geo.fv[k, j + 1, i] = 0.0
-    geo.fv[k, j + 2, i] = 0.0
+    # native index f+1 of face f (west face of interior cell i+1 has FU index i);
+    # on a periodic axis faces f and f+-n are one face, stored twice
+    for base in (i + 1, i + 2):
+        for shift in ((-nx, 0, nx) if g.periodic_x else (0,)):
+            t = base + shift
+            ok = (t >= 0) & (t <= nx + 2)
+            geo.fu[k[ok], j[ok], t[ok]] = 0.0
+    for base in (j + 1, j + 2):
+        for shift in ((-ny, 0, ny) if g.periodic_y else (0,)):
+            t = base + shift
+            ok = (t >= 0) & (t <= ny + 2)
+            geo.fv[k[ok], t[ok], i[ok]] = 0.0
     geo.fw[k + 1, j, i] = 0.0
     geo.fw[k + 2, j, i] = 0.0
     geo.info["dead_cells_closed"] = int(dead.sum())
@@ -537,6 +545,26 @@ def bubble_dyn_case(nx: int = 64, ny: int = 64, nz: int = 64, seed: int = 1):
     pos = {"rho": 0, "mom": [1, 2, 3, 4, 5, 6], "th": 7}
     widths = (np.full(g.nx, g.dx), np.full(g.ny, g.dy), np.asarray(g.dz, dtype=np.float64).copy())
     return geo, vel, st, pos, widths, boundary_cells(geo)
+
+
+def hill_dyn_case(nx: int = 512, ny: int = 512, nz: int = 128, seed: int = 3, dx: float = 200.0,
+                  height: float = 1000.0, halfwidth: float = 5000.0, u0: float = 10.0, n_bv: float = 0.01):
+    """The cut-cell hill of hill_case for the dynamical core: periodic in x and
+    y, rigid bottom and lid, dx=dy=200 m, dz 50->400 m, Gaussian hill with
+    correlated roughness, snapping and the small-cell merge, the faces of
+    zero-volume cells closed (the pressure system needs them closed);
+    stratified (N), moist, one tracer, u=10 m/s.  Returns (geo, (uF, vF, wF),
+    state, positions, (dx, dy, dz), boundary cells) like dyn_case."""
+    grid = Grid(nx, ny, nz, dx, dx, stretched_levels(nz, 50.0, 400.0))
+    h = gaussian_hill_terrain(grid, height, halfwidth, 50.0, 2000.0, seed=seed)
+    geo = close_dead_faces(cut_cell_geometry(grid, h, snap=0.01, merge=0.1))
+    uf, vf, wf = face_velocity(geo, u0, 0.0)
+    st = initial_state(geo, uf, vf, wf, theta0=300.0, n_bv=n_bv, moist=True, tracer=True, momentum=True, noise=0.0,
+                       seed=seed + 100)
+    g = geo.grid
+    pos = {"rho": 0, "mom": [1, 2, 3, 4, 5, 6], "th": 7, "qv": 8, "tracer": 9}
+    widths = (np.full(g.nx, g.dx), np.full(g.ny, g.dy), np.asarray(g.dz, dtype=np.float64).copy())
+    return geo, (uf, vf, wf), st, pos, widths, boundary_cells(geo)
 
 
 def hill_case(nx: int = 256, ny: int = 256, nz: int = 128, seed: int = 2, dx: float = 200.0,
