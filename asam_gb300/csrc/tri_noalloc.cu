@@ -11,8 +11,6 @@
 //
 // Compiled with -fmad=false like k64.cu, so the solution is bit-identical to
 // asam_tri_solve's.
-#include <mutex>
-
 #include "kernels.cuh"
 
 namespace asam {
@@ -31,45 +29,30 @@ namespace {
 constexpr long long kTriNoAllocMax = 1LL << 22;  // ncol*n1 doubles
 static __device__ __align__(256) double g_tri_scratch[kTriNoAllocMax];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mutex;
-double* g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device, looked up once
-// per device (the host-side symbol is only a stand-in and must not be passed
-// to a kernel).
+// Device address of the scratch array on the current device (the host-side
+// symbol is only a stand-in and must not be passed to a kernel).  Looked up
+// on every call: the lookup is cheap, and a cached address would go stale
+// when the device's primary context is reset or recreated.
 int scratch_on_current_device(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_tri_scratch);
   if (e != cudaSuccess) {
     asam::set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
     return asam::kCudaError;
   }
-  if (dev < 0 || dev >= kMaxDevices) {
-    asam::set_last_error("device ordinal out of range for the no-alloc scratch table", __FILE__, __LINE__);
-    return asam::kBadArg;
-  }
-  std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_tri_scratch);
-    if (e != cudaSuccess) {
-      asam::set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
-      return asam::kCudaError;
-    }
-    g_scratch_ptr[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch_ptr[dev];
+  *out = static_cast<double*>(p);
   return asam::kOk;
 }
 
-bool on_device(const void* p) {
+// A pointer the kernel on the current device may use: device memory of this
+// device, or managed memory.
+bool on_device(const void* p, int dev) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  return (a.type == cudaMemoryTypeDevice && a.device == dev) || a.type == cudaMemoryTypeManaged;
 }
 
 }  // namespace
@@ -86,8 +69,15 @@ extern "C" int asam_tri_solve_noalloc(int ncol, int n1, const double* d, const d
         __FILE__, __LINE__);
     return asam::kBadArg;
   }
-  if (!on_device(d) || !on_device(b) || (n1 > 1 && (!on_device(u) || !on_device(l)))) {
-    asam::set_last_error("asam_tri_solve_noalloc: d, u, l and b must be device pointers", __FILE__, __LINE__);
+  int dev = 0;
+  cudaError_t de = cudaGetDevice(&dev);
+  if (de != cudaSuccess) {
+    asam::set_last_error(cudaGetErrorString(de), __FILE__, __LINE__);
+    return asam::kCudaError;
+  }
+  if (!on_device(d, dev) || !on_device(b, dev) || (n1 > 1 && (!on_device(u, dev) || !on_device(l, dev)))) {
+    asam::set_last_error("asam_tri_solve_noalloc: d, u, l and b must be device pointers of the current device",
+                         __FILE__, __LINE__);
     return asam::kBadArg;
   }
   double* w = nullptr;

@@ -241,12 +241,13 @@ int asam_tri_solve(int ncol, int n1, const double *d, const double *u, const dou
  * callers that cannot let a library allocate device memory: a host model
  * that owns all device memory through its own pool, or one that overlaps this
  * solve with other streams (cudaMalloc/cudaFree synchronise the device).  d,
- * u, l and b must be device pointers; the work runs on `stream` (NULL = legacy
- * default stream) and is not waited for.  The elimination factors go to a
- * fixed 32 MiB array inside the library, so ncol*n1 may not exceed 4194304
- * (ASAM_BAD_ARG otherwise).  The first call on a device looks the array's
- * device address up; make that first call before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race. */
+ * u, l and b must be device pointers of the current device (or managed
+ * memory); the work runs on `stream` (NULL = legacy default stream) and is not
+ * waited for.  The elimination factors go to a fixed 32 MiB array inside the
+ * library, so ncol*n1 may not exceed 4194304 (ASAM_BAD_ARG otherwise).  Every
+ * call looks the array's device address up on the current device (so a reset
+ * device is handled); make the first call on a device before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
 int asam_tri_solve_noalloc(int ncol, int n1, const double *d, const double *u, const double *l, double *b,
                            void *stream);
 /* y = T x for the same column batch, MatVecT_1D (MULTI/TriDiagT_Mod.f90:113-133). */

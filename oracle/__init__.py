@@ -54,6 +54,7 @@ def load() -> C.CDLL:
             "ora_matvec": (None, [G, I, V, V, V]),
             "ora_dot": (D, [G, I, V, V]),
             "ora_bicgstab": (None, [G, I, V, V, V, C.POINTER(C.c_int), C.POINTER(C.c_double), I]),
+            "ora_bicgstab_halfsteps": (None, [G, I, V, V, V, I, I]),
             "ora_ros_coeffs": (I, [I, C.POINTER(C.c_double), V, V, V]),
             "ora_ros_step": (I, [G, I, I, V, V, V, V, D, I, D, I, I, V, V]),
             "ora_total_scalar": (D, [G, V]),
@@ -219,6 +220,13 @@ class Oracle:
         tl = C.c_double(tol)
         self.lib.ora_bicgstab(self.gp, x.size // self.npad, _p(v), _p(x), _p(bb), C.byref(it), C.byref(tl), iterg)
         return it.value, tl.value
+
+    def bicgstab_halfsteps(self, val, x, b, nhalf, iterg=5):
+        """x updated in place by exactly nhalf BiCGStab half-steps (a run whose
+        exit lands there: MaxIter -k leaves after 2k-1, +k after 2k)."""
+        v = np.ascontiguousarray(val, dtype=np.float64)
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        self.lib.ora_bicgstab_halfsteps(self.gp, x.size // self.npad, _p(v), _p(x), _p(bb), int(nhalf), iterg)
 
     def ros_step(self, c, vel, dt, method=5, tol=1e-6, maxiter=30, iterg=5, rho_pos=0):
         """c updated in place; returns (iters, resid) per stage."""

@@ -745,8 +745,24 @@ static void xpay(size_t len, const double *x, double alpha, double *y) {
  * x: in/out (initial guess), b: rhs.  *maxiter and *tol in/out with the
  * reference's conventions (negative = converged at the half step, 2*Iter =
  * iteration limit hit; tol returns the final residual norm). */
+/* stop_half > 0 (tests only): leave after exactly that many half-steps, the
+ * way the solver leaves when the tolerance is met there (the comparison of a
+ * GPU run whose iteration count differs by one from the tolerance-driven
+ * run); 0: the reference's exits only. */
+static void bicgstab_core(const ora_geom *g, int ncomp, const double *val, double *x, const double *b, int *maxiter,
+                          double *tol, int iterg, int stop_half);
 void ora_bicgstab(const ora_geom *g, int ncomp, const double *val, double *x, const double *b, int *maxiter,
                   double *tol, int iterg) {
+  bicgstab_core(g, ncomp, val, x, b, maxiter, tol, iterg, 0);
+}
+void ora_bicgstab_halfsteps(const ora_geom *g, int ncomp, const double *val, double *x, const double *b, int nhalf,
+                            int iterg) {
+  int maxiter = (nhalf + 1) / 2;
+  double tol = 0.0;
+  bicgstab_core(g, ncomp, val, x, b, &maxiter, &tol, iterg, nhalf);
+}
+static void bicgstab_core(const ora_geom *g, int ncomp, const double *val, double *x, const double *b, int *maxiter,
+                          double *tol, int iterg, int stop_half) {
   const size_t len = NPAD(g) * (size_t)ncomp;
   double *r = (double *)calloc(len, sizeof(double));
   double *rt = (double *)calloc(len, sizeof(double));
@@ -782,7 +798,7 @@ void ora_bicgstab(const ora_geom *g, int ncomp, const double *val, double *x, co
     alpha = rho / ora_dot(g, ncomp, rt, v);
     axpy(len, -alpha, v, r);
     rNorm = sqrt(ora_dot(g, ncomp, r, r));
-    if (rNorm <= Tol * rNorm0) {
+    if (rNorm <= Tol * rNorm0 || stop_half == 2 * Iter - 1) {
       axpy(len, alpha, ph, x);
       *maxiter = -Iter;
       *tol = rNorm;
@@ -795,7 +811,7 @@ void ora_bicgstab(const ora_geom *g, int ncomp, const double *val, double *x, co
     axpy(len, omega, rh, x);
     axpy(len, -omega, t, r);
     rNorm = sqrt(ora_dot(g, ncomp, r, r));
-    if (rNorm <= Tol * rNorm0) {
+    if (rNorm <= Tol * rNorm0 || stop_half == 2 * Iter) {
       *maxiter = Iter;
       *tol = rNorm;
       goto done;

@@ -99,3 +99,19 @@ def relerr(a: np.ndarray, b: np.ndarray) -> float:
 
 def field_relerr(a: np.ndarray, b: np.ndarray) -> list[float]:
     return [relerr(a[i], b[i]) for i in range(a.shape[0])]
+
+
+def state_relerr(a: np.ndarray, b: np.ndarray, mom=()) -> list[float]:
+    """Per-field max |a-b| relative to the field's largest magnitude, except
+    that the six LR momentum components (indices `mom`) are the Cartesian
+    components of one vector field and are measured against the largest
+    magnitude among them: a component that is nearly zero everywhere (the
+    cross-wind v of a flow along x) would otherwise turn rounding-level
+    differences of the Krylov solves into large relative numbers."""
+    mom = list(mom)
+    vscale = max((float(np.max(np.abs(b[q]))) for q in mom), default=0.0)
+    out = []
+    for i in range(a.shape[0]):
+        den = vscale if i in mom else float(np.max(np.abs(b[i])))
+        out.append(float(np.max(np.abs(a[i] - b[i]))) / max(den, 1e-300))
+    return out

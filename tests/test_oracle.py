@@ -207,3 +207,23 @@ def test_ros_coefficients(oracle_mod):
     assert list(gm[:4]) == [0.0, 1.0 / 3.0, 0.5, 1.0]
     n, b0, *_ = oracle_mod.ros_coeffs(0)
     assert n == 2 and b0 == float(np.float32(0.5) + np.sqrt(np.float32(3.0)) / np.float32(6.0))
+
+
+def test_bicgstab_halfsteps_reproduces_exits():
+    """The oracle's fixed half-step count reproduces the tolerance-driven exits
+    bit for bit (the comparison of runs whose counts differ by one)."""
+    import oracle
+    from tests import cases as CS
+
+    geo, vel, st = CS.get("hill_24x20x16")
+    o = oracle.Oracle(geo)
+    c = o.exchange_cell(st.c)
+    val = o.jac(c[0], vel, 0.435866521508459, 20.0)
+    b = np.random.default_rng(3).standard_normal(st.c.shape)
+    for tol in (1e-4, 1e-8, 1e-12):
+        x1 = np.zeros_like(b)
+        it, _ = o.bicgstab(val, x1, b, 30, tol)
+        half = 2 * (-it) - 1 if it < 0 else (it if it > 30 else 2 * it)
+        x2 = np.zeros_like(b)
+        o.bicgstab_halfsteps(val, x2, b, half)
+        assert np.array_equal(x1, x2), (tol, it)
