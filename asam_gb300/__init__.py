@@ -348,6 +348,14 @@ class TransportBlock:
         code = {None: -1, "fp64": 0, "fp32": 1}[prec]
         check(self.lib.asam_proj_set_precision(self.h, code), "asam_proj_set_precision")
 
+    def proj_set_preconditioner(self, kind):
+        """FGMRES preconditioner of a block with periodic x/y sides: "psolve1"
+        (the reference's PSolve1), "periodic" (one V-cycle on the periodic
+        Laplacian, face unknowns eliminated), or None (periodic for refined
+        contexts, else PSolve1).  Takes effect at the next JacAccGrav."""
+        code = {None: -1, "psolve1": 0, "periodic": 1}[kind]
+        check(self.lib.asam_proj_set_preconditioner(self.h, code), "asam_proj_set_preconditioner")
+
     def proj_weights(self, dtu, dtv, dtw, duu, duv, duw, dut, dtt):
         """Sound weights (WeightDiagCompute): face arrays with uF/vF/wF extents,
         DUT and DTT interior (nz, ny, nx)."""

@@ -77,6 +77,10 @@ struct Lev2T {
   size_t ps;
   T *d, *uz, *lz, *fw, *ft, *frt, *ux, *lx, *res;
   T *x, *b;  // own vectors of the coarse plane levels (nullptr on the 3D level's own planes)
+  // periodic-Laplacian hierarchy only (nullptr otherwise): the couplings
+  // across the periodic x side, between line 0 and line c2-1 of row i of
+  // plane k at [k*c1 + i]: wxl in the row of line 0, wxh in the row of line c2-1
+  T *wxl, *wxh;
 };
 using Lev2 = Lev2T<double>;
 
@@ -85,6 +89,10 @@ struct Lev3T {
   int m1, m2, m3, nl;
   Lev2T<T> pl[kMaxLev];
   T *u3, *l3, *x, *b, *res, *t;
+  // periodic-Laplacian hierarchy only: couplings across the periodic y side
+  // between plane 0 and plane m3-1 (one plane layout): wyl in the rows of
+  // plane 0, wyh in the rows of plane m3-1
+  T *wyl, *wyh;
 };
 using Lev3 = Lev3T<double>;
 
@@ -404,6 +412,40 @@ __global__ void k_assemble(Fields c, Lev2 P, double* __restrict__ u3, double* __
   }
 }
 
+// The couplings across the periodic sides of one level of the periodic-
+// Laplacian hierarchy (the refined mode's FGMRES preconditioner on blocks
+// with periodic sides): the interior-face terms of ComputeFull_2D/3D
+// (MULTI/TriDiagT_Mod.f90:330-403, 790-883) applied to the shared face between
+// the last and the first line (x) or plane (y), coefficient
+// -(beta0*dtP)^2*2*F*DT*DU*DUT(column)/((d(first)+d(last))*Metr); the y
+// couplings of a 3D level carry no DU, like its interior ones.  Its
+// diagonal terms come from k_assemble with boundary factor 1 on those sides.
+__global__ void k_assemble_wrap(Fields c, Lev2 P, double* __restrict__ wyl, double* __restrict__ wyh, int full,
+                                int per_x, int per_y, double bd2) {
+  const int n1 = c.n1, n2 = c.n2, n3 = c.n3;
+  const size_t nxw = per_x ? (size_t)n1 * n3 : 0, nyw = (per_y && full) ? (size_t)n1 * n2 : 0;
+  auto DUT = [&](int ii, int jj, int kk) { return c.dut[c.ic(ii, jj, kk)]; };
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nxw + nyw; e += (size_t)gridDim.x * blockDim.x) {
+    if (e < nxw) {
+      const int i = (int)(e % n1) + 1, k = (int)(e / n1) + 1;
+      const size_t q = c.i2(i, 0, k);
+      const double den = (c.d2[0] + c.d2[n2 - 1]) * c.m21[i - 1] * c.m23[k - 1];
+      const double base = bd2 * 2.0 * c.F2[q] * c.T2[q] * c.U2[q];
+      P.wxl[(size_t)(k - 1) * n1 + (i - 1)] = -(base * DUT(i, n2, k) / den);
+      P.wxh[(size_t)(k - 1) * n1 + (i - 1)] = -(base * DUT(i, 1, k) / den);
+    } else {
+      const size_t r = e - nxw;
+      const int i = (int)(r % n1) + 1, j = (int)(r / n1) + 1;
+      const size_t q = c.i3(i, j, 0);
+      const double den = (c.d3[0] + c.d3[n3 - 1]) * c.m31[i - 1] * c.m32[j - 1];
+      const double base = bd2 * 2.0 * c.F3[q] * c.T3[q];
+      const size_t s = slot(P.w, P.h, i - 1, j - 1);
+      wyl[s] = -(base * DUT(i, j, n3) / den);
+      wyh[s] = -(base * DUT(i, j, 1) / den);
+    }
+  }
+}
+
 // Thomas factors of every column (the t and w of Solve_1D, which depend on
 // the matrix only): ft = t_i, frt = 1/t_i, fw = u_i/t_i
 __global__ void k_factor(Lev2 P) {
@@ -432,7 +474,7 @@ __global__ void k_factor(Lev2 P) {
 
 // MatVecT_2D at entry (i,j) of a plane (TriDiagT_Mod.f90:113-133, 405-431);
 // x is the plane's vector, mo the plane's offset in the matrix arrays
-template <typename T>
+template <typename T, bool kWrap = false>
 __device__ inline T matvec2_at(const Lev2T<T>& P, size_t mo, const T* __restrict__ x, size_t s, int i, int j) {
   const int c1 = P.c1, c2 = P.c2, w = P.w;
   const T* d = P.d + mo;
@@ -464,6 +506,11 @@ __device__ inline T matvec2_at(const Lev2T<T>& P, size_t mo, const T* __restrict
       y = y + lx[sl] * x[sl];
     }
   }
+  if (kWrap && P.wxl) {  // periodic-Laplacian hierarchy: the coupling across the periodic x side
+    const size_t k = mo / P.ps, row = (size_t)i * w;
+    if (j == 0) y = y + P.wxl[k * c1 + i] * x[row + slot(0, P.h, 0, c2 - 1)];
+    if (j == c2 - 1) y = y + P.wxh[k * c1 + i] * x[row];
+  }
   return y;
 }
 
@@ -492,7 +539,7 @@ __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_grou
 template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-template <typename T>
+template <typename T, bool kWrap = false>
 __device__ __noinline__ void line_half(const Lev2T<T>& P, size_t mo, const T* __restrict__ b, T* __restrict__ x, int c,
                                        int fwd, T* __restrict__ ring) {
   const int c1 = P.c1, c2 = P.c2, h = P.h, w = P.w;
@@ -511,6 +558,10 @@ __device__ __noinline__ void line_half(const Lev2T<T>& P, size_t mo, const T* __
     const bool hasL = j > 0, hasR = j < c2 - 1;
     const size_t colL = hasL ? (size_t)(1 - c) * h + ((j - 1) >> 1) : col;
     const size_t colR = hasR ? (size_t)(1 - c) * h + ((j + 1) >> 1) : col;
+    // the periodic wrap couples lines 0 and c2-1; used only when they have
+    // different parities (no line reads a line of its own half-sweep)
+    const bool wrap = kWrap && P.wxl && c2 >= 2 && ((c2 - 1) & 1) && (j == 0 || j == c2 - 1);
+    const size_t wk = (mo / P.ps) * (size_t)c1, colW = slot(0, h, 0, c2 - 1);
     auto issue = [&](int i) {
       T* sl = ring + (size_t)(i % kRing) * kFields * bd + tid;
       const bool ok = i < c1;
@@ -539,6 +590,11 @@ __device__ __noinline__ void line_half(const Lev2T<T>& P, size_t mo, const T* __
       } else {
         if (hasR) t = t - sl[4 * bd] * sl[2 * bd];
         if (hasL) t = t - sl[3 * bd] * sl[1 * bd];
+      }
+      if (kWrap && wrap) {  // periodic-Laplacian hierarchy: the line across the periodic x side
+        const size_t ri = (size_t)i * w;
+        if (j == 0) t = t - P.wxl[wk + i] * x[ri + colW];
+        if (j == c2 - 1) t = t - P.wxh[wk + i] * x[ri];
       }
       if (i > 0) t = t - sl[5 * bd] * prev;
       const T y = div_rn(t, sl[6 * bd], sl[7 * bd]);
@@ -580,27 +636,27 @@ __device__ __noinline__ void line_half(const Lev2T<T>& P, size_t mo, const T* __
   }
 }
 
-template <typename T>
+template <typename T, bool kWrap = false>
 __device__ void gs2d(const Lev2T<T>& P, size_t mo, const T* b, T* x, int gi, T* ring) {
   if (P.c2 > 1) {
     for (int it = 0; it < gi; ++it) {
-      line_half(P, mo, b, x, 0, 1, ring);
+      line_half<T, kWrap>(P, mo, b, x, 0, 1, ring);
       __syncthreads();
-      line_half(P, mo, b, x, 1, 1, ring);
+      line_half<T, kWrap>(P, mo, b, x, 1, 1, ring);
       __syncthreads();
-      line_half(P, mo, b, x, 1, 0, ring);
+      line_half<T, kWrap>(P, mo, b, x, 1, 0, ring);
       __syncthreads();
-      line_half(P, mo, b, x, 0, 0, ring);
+      line_half<T, kWrap>(P, mo, b, x, 0, 0, ring);
       __syncthreads();
     }
   } else {
-    line_half(P, mo, b, x, 0, 1, ring);
+    line_half<T, kWrap>(P, mo, b, x, 0, 1, ring);
     __syncthreads();
   }
 }
 
 // Multigrid_2D (TriDiagT_Mod.f90:490-551) on plane k of a 3D level, inside one CTA
-template <typename T>
+template <typename T, bool kWrap = false>
 __device__ void mg2d(const Lev3T<T>& A, int k, T* x0, const T* b0, int gi2, T* ring) {
   const int nl = A.nl;
   int gi = 1;
@@ -610,7 +666,7 @@ __device__ void mg2d(const Lev3T<T>& A, int k, T* x0, const T* b0, int gi2, T* r
     T* x = lv == 0 ? x0 : P.x + (size_t)k * P.ps;
     const T* b = lv == 0 ? b0 : P.b + (size_t)k * P.ps;
     const size_t mo = (size_t)k * P.ps;
-    gs2d(P, mo, b, x, gi, ring);
+    gs2d<T, kWrap>(P, mo, b, x, gi, ring);
     gi += gi2;
     if (lv + 1 < nl) {
       T* res = P.res + (size_t)k * P.ps;
@@ -618,7 +674,7 @@ __device__ void mg2d(const Lev3T<T>& A, int k, T* x0, const T* b0, int gi2, T* r
       for (size_t s = threadIdx.x; s < np; s += blockDim.x) {
         const int i = (int)(s / P.w), j = line_of((int)(s % P.w), P.h, P.c2);
         if (j < 0) continue;
-        res[s] = b[s] - matvec2_at(P, mo, x, s, i, j);
+        res[s] = b[s] - matvec2_at<T, kWrap>(P, mo, x, s, i, j);
       }
       __syncthreads();
       const Lev2T<T>& Q = A.pl[lv + 1];
@@ -644,7 +700,7 @@ __device__ void mg2d(const Lev3T<T>& A, int k, T* x0, const T* b0, int gi2, T* r
     const Lev2T<T>& P = A.pl[lv];
     T* x = lv == 0 ? x0 : P.x + (size_t)k * P.ps;
     const T* b = lv == 0 ? b0 : P.b + (size_t)k * P.ps;
-    gs2d(P, (size_t)k * P.ps, b, x, gi, ring);
+    gs2d<T, kWrap>(P, (size_t)k * P.ps, b, x, gi, ring);
     gi -= gi2;
     if (lv > 0) {
       const Lev2T<T>& F = A.pl[lv - 1];
@@ -665,7 +721,7 @@ __device__ void mg2d(const Lev3T<T>& A, int k, T* x0, const T* b0, int gi2, T* r
 // One zebra half-sweep of GaussSeidel_3D over the planes of parity `color` of
 // 3D level L: each CTA forms its plane's right-hand side (forward or backward
 // operation order of the reference) and runs Solve_2D on it.
-template <typename T>
+template <typename T, bool kWrap = false>
 __global__ void __launch_bounds__(kPlaneBlock, 2) k_plane_half(const Lev3T<T>* __restrict__ lvs, int L, int color, int fwd,
                                                              int mult_iter2, int gi2) {
   __shared__ Lev3T<T> A;
@@ -689,17 +745,23 @@ __global__ void __launch_bounds__(kPlaneBlock, 2) k_plane_half(const Lev3T<T>* _
         if (k < A.m3 - 1) v = v - A.u3[e] * A.x[e + ps];
         if (k > 0) v = v - A.l3[e - ps] * A.x[e - ps];
       }
+      // periodic-Laplacian hierarchy: the plane across the periodic y side
+      // (only when planes 0 and m3-1 have different parities)
+      if (kWrap && A.wyl && A.m3 >= 2 && ((A.m3 - 1) & 1)) {
+        if (k == 0) v = v - A.wyl[s] * A.x[(size_t)(A.m3 - 1) * ps + s];
+        if (k == A.m3 - 1) v = v - A.wyh[s] * A.x[s];
+      }
       A.t[e] = v;
     }
     __syncthreads();
-    for (int it = 0; it < mult_iter2; ++it) mg2d(A, k, A.x + off, A.t + off, gi2, ring);
+    for (int it = 0; it < mult_iter2; ++it) mg2d<T, kWrap>(A, k, A.x + off, A.t + off, gi2, ring);
     __syncthreads();
   }
 }
 
 // MatVecT_3D at every entry of level L: mode 0 res = b - A x; mode 1 y = -(A x)
 // (MatVecFull's sign); mode 2 y = A x.
-template <typename T>
+template <typename T, bool kWrap = false>
 __global__ void k_matvec3(const Lev3T<T>* __restrict__ lvs, int L, const T* __restrict__ x, const T* __restrict__ b,
                           T* __restrict__ y, int mode) {
   const Lev3T<T>& A = lvs[L];
@@ -710,7 +772,7 @@ __global__ void k_matvec3(const Lev3T<T>* __restrict__ lvs, int L, const T* __re
     const int k = (int)(e / ps);
     const int i = (int)(s / P.w), j = line_of((int)(s % P.w), P.h, P.c2);
     if (j < 0) continue;
-    T v = matvec2_at(P, (size_t)k * ps, x + (size_t)k * ps, s, i, j);
+    T v = matvec2_at<T, kWrap>(P, (size_t)k * ps, x + (size_t)k * ps, s, i, j);
     if (A.m3 > 1) {
       if (k == 0)
         v = v + A.u3[e] * x[e + ps];
@@ -718,6 +780,10 @@ __global__ void k_matvec3(const Lev3T<T>* __restrict__ lvs, int L, const T* __re
         v = v + A.l3[e - ps] * x[e - ps] + A.u3[e] * x[e + ps];
       else
         v = v + A.l3[e - ps] * x[e - ps];
+    }
+    if (kWrap && A.wyl) {  // periodic-Laplacian hierarchy: across the periodic y side
+      if (k == 0) v = v + A.wyl[s] * x[(size_t)(A.m3 - 1) * ps + s];
+      if (k == A.m3 - 1) v = v + A.wyh[s] * x[s];
     }
     y[e] = mode == 0 ? b[e] - v : (mode == 1 ? -v : v);
   }
@@ -1071,7 +1137,10 @@ __device__ inline size_t cell_lay(const Lev2& P, int i, int j, int k) {
 //              (MatVecFull MATRIX/MatVec_Mod.f90:224-255, b1pBTx2Full
 //              MATRIX/PreCond_Mod.f90:642-665);
 //   schur = 1: the same divided by (0.5d0*d*Metr1*Metr2*F+Eps)
-//              (SchurPreFull MATRIX/PreCond_Mod.f90:138-216, p starting at 0).
+//              (SchurPreFull MATRIX/PreCond_Mod.f90:138-216, p starting at 0);
+//   schur = 2: with the opposite signs, divided by the whole mass of the
+//              shared face (both halves): the right-hand side of the
+//              periodic-Laplacian preconditioner (face unknowns eliminated).
 // v holds the face unknowns (at fc.off), p is a level-0 layout vector.
 __global__ void k_pv_face_p(Dims d, GeomT<double> g, Wts wt, Lev2 P, PvFaces fc, double bd, int schur,
                             const double* __restrict__ v, double* __restrict__ p) {
@@ -1122,8 +1191,14 @@ __global__ void k_pv_face_p(Dims d, GeomT<double> g, Wts wt, Lev2 P, PvFaces fc,
       const int na = side < 2 ? ny : nx;
       const double u = v[fc.off[side] + (a - 1) + (size_t)na * (b - 1)];
       double t = bd * f.F * f.DT * dtt * u;
-      if (schur) t = t / (f.hsp * f.F + eps);
-      acc = (side & 1) ? acc - t : acc + t;
+      if (schur == 1) t = t / (f.hsp * f.F + eps);
+      if (schur == 2) {  // the face unknown eliminated with the pair's whole mass
+        const FaceAt o = face_at(d, g, wt, side ^ 1, a, b);
+        t = t / (f.hmv * f.F + o.hmv * o.F + eps);
+        acc = (side & 1) ? acc + t : acc - t;
+      } else {
+        acc = (side & 1) ? acc - t : acc + t;
+      }
     }
     p[cl] = acc;
   }
@@ -1138,6 +1213,9 @@ __global__ void k_pv_face_p(Dims d, GeomT<double> g, Wts wt, Lev2 P, PvFaces fc,
 //   op 1 b2pBx1Full (MATRIX/PreCond_Mod.f90:694-728): out = in (+/-) cp
 //   op 2 SchurPreFull after its Solve_3D (MATRIX/PreCond_Mod.f90:303-404):
 //        out = PreFac2*(in (-W/S/B, +E/N/T) cp)/(0.5d0*d*Metr1*Metr2*F+Eps)
+//   op 3 the periodic-Laplacian preconditioner's face unknowns:
+//        out = (in - cp_W + cp_E) / (whole mass of the shared face + Eps),
+//        written to both copies (in holds equal copies after Exchange)
 __global__ void k_pv_faces(Dims d, GeomT<double> g, Wts wt, Lev2 P, PvFaces fc, double bd, double prefac2, int op,
                            int exchange, const double* in, const double* __restrict__ pv, double* out) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
@@ -1155,7 +1233,7 @@ __global__ void k_pv_faces(Dims d, GeomT<double> g, Wts wt, Lev2 P, PvFaces fc, 
     } else {
       pair = 2, q = e - nX - nY, a = (int)(q % nx) + 1, b = (int)(q / nx) + 1;
     }
-    double val[2];
+    double val[2], mass = 0.0;
     for (int h = 0; h < 2; ++h) {
       const int side = 2 * pair + h;
       const FaceAt f = face_at(d, g, wt, side, a, b);
@@ -1168,11 +1246,21 @@ __global__ void k_pv_faces(Dims d, GeomT<double> g, Wts wt, Lev2 P, PvFaces fc, 
         r = h ? m - cp : m + cp;
       } else if (op == 1) {
         r = h ? in[fi] - cp : in[fi] + cp;
-      } else {
+      } else if (op == 2) {
         const double den = f.hsp * f.F + eps;
         r = h ? prefac2 * (in[fi] + cp) / den : prefac2 * (in[fi] - cp) / den;
+      } else {  // op 3: the cp terms of both halves, combined below
+        r = h ? cp : -cp;
+        mass = mass + f.hmv * f.F;
       }
       val[h] = r;
+    }
+    if (op == 3) {  // u = (v - cp_W + cp_E) / (whole mass), both copies
+      const size_t lo = fc.off[2 * pair] + q, hi = fc.off[2 * pair + 1] + q;
+      const double u = (in[lo] + val[0] + val[1]) / (mass + eps);
+      out[lo] = u;
+      out[hi] = u;
+      continue;
     }
     const size_t lo = fc.off[2 * pair] + q, hi = fc.off[2 * pair + 1] + q;
     if (exchange) {
@@ -1320,6 +1408,15 @@ struct ProjState {
   std::vector<prj::Lev3T<float>> lvD32;
   prj::Lev3T<float>* d_lvD32 = nullptr;
   double* tmp2 = nullptr;  // level-0 scratch of PSolve1
+  // the periodic-Laplacian preconditioner (face unknowns eliminated, one
+  // V-cycle on the Laplacian with the couplings across the periodic sides):
+  // -1 follow the precision (refined contexts), 0 PSolve1, 1 periodic
+  int pre_kind = -1;
+  std::vector<Lev3> lvP;
+  Lev3* d_lvP = nullptr;
+  std::vector<prj::Lev3T<float>> lvP32;
+  prj::Lev3T<float>* d_lvP32 = nullptr;
+  bool lvP_ready = false, lvP32_ready = false, lvD_ready = false;
 };
 
 namespace prj {
@@ -1466,6 +1563,8 @@ int proj_build(asam_ctx* h) {
   }
   CK(cudaFuncSetAttribute(k_plane_half<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
   CK(cudaFuncSetAttribute(k_plane_half<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
+  CK(cudaFuncSetAttribute(k_plane_half<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
+  CK(cudaFuncSetAttribute(k_plane_half<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
   if (int rc = palloc(s, &s->d_lv, (size_t)R)) return rc;
   CK(cudaMemcpyAsync(s->d_lv, s->lv.data(), sizeof(Lev3) * R, cudaMemcpyHostToDevice, s->st));
   CK(cudaStreamSynchronize(s->st));
@@ -1495,7 +1594,7 @@ int proj_build(asam_ctx* h) {
 
 // Solve_3D from a zero start on level 0 (VCycleCG's MatrixT branch): lv[0].b
 // holds the right-hand side, the result is left in lv[0].x
-template <typename T>
+template <typename T, bool kWrap = false>
 void vcycle_run(asam_ctx* h, std::vector<Lev3T<T>>& lv, Lev3T<T>* d_lv) {
   ProjState* s = h->proj;
   const cudaStream_t st = h->L.stream;
@@ -1510,7 +1609,7 @@ void vcycle_run(asam_ctx* h, std::vector<Lev3T<T>>& lv, Lev3T<T>* d_lv) {
     auto half = [&](int c, int fwd) {
       const int np = (A.m3 - c + 1) / 2;
       if (np <= 0) return;
-      k_plane_half<T><<<np, kPlaneBlock, ring, st>>>(d_lv, L, c, fwd, mi2, gi2);
+      k_plane_half<T, kWrap><<<np, kPlaneBlock, ring, st>>>(d_lv, L, c, fwd, mi2, gi2);
       ++nl;
     };
     if (A.m3 > 1) {
@@ -1532,7 +1631,7 @@ void vcycle_run(asam_ctx* h, std::vector<Lev3T<T>>& lv, Lev3T<T>* d_lv) {
       if (L + 1 < R) {
         const Lev3T<T>& A = lv[L];
         const size_t n = A.pl[0].ps * A.m3;
-        k_matvec3<T><<<grid_of(n), 256, 0, st>>>(d_lv, L, A.x, A.b, A.res, 0);
+        k_matvec3<T, kWrap><<<grid_of(n), 256, 0, st>>>(d_lv, L, A.x, A.b, A.res, 0);
         const size_t nc = lv[L + 1].pl[0].ps * lv[L + 1].m3;
         k_restrict3<T><<<grid_of(nc), 256, 0, st>>>(d_lv, L);
         nl += 2;
@@ -1562,6 +1661,47 @@ void vcycle_run(asam_ctx* h, std::vector<Lev3T<T>>& lv, Lev3T<T>* d_lv) {
 bool use_mg32(const asam_ctx* h) {
   const ProjState* s = h->proj;
   return s->mg_prec == 1 || (s->mg_prec < 0 && h->cfg.precision == ASAM_PREC_FP32_REFINED);
+}
+
+// FGMRES preconditioned by the periodic-Laplacian multigrid instead of the
+// reference's PSolve1: blocks with face unknowns of periodic x/y sides only
+bool use_per(const asam_ctx* h) {
+  const ProjState* s = h->proj;
+  if (!s->nface || h->d.per_z) return false;
+  return s->pre_kind == 1 || (s->pre_kind < 0 && h->cfg.precision == ASAM_PREC_FP32_REFINED);
+}
+
+// the periodic-Laplacian hierarchy: its own matrices and couplings across the
+// periodic sides, the vectors of lv (FP64) / lv32 (FP32)
+int alloc_levP(ProjState* s, const Dims& d) {
+  if (s->d_lvP) return kOk;
+  const int R = s->R;
+  s->lvP = s->lv;
+  for (int L = 0; L < R; ++L) {
+    Lev3& A = s->lvP[L];
+    for (int q = 0; q < A.nl; ++q) {
+      Lev2& P = A.pl[q];
+      const size_t n = P.ps * P.m3;
+      double** arr[] = {&P.d, &P.uz, &P.lz, &P.fw, &P.ft, &P.frt, &P.ux, &P.lx};
+      for (double** r : arr)
+        if (int rc = palloc(s, r, n)) return rc;
+      if (d.per_x) {
+        if (int rc = palloc(s, &P.wxl, (size_t)P.c1 * P.m3)) return rc;
+        if (int rc = palloc(s, &P.wxh, (size_t)P.c1 * P.m3)) return rc;
+      }
+    }
+    const size_t n = A.pl[0].ps * A.m3;
+    if (int rc = palloc(s, &A.u3, n)) return rc;
+    if (int rc = palloc(s, &A.l3, n)) return rc;
+    if (d.per_y) {
+      if (int rc = palloc(s, &A.wyl, A.pl[0].ps)) return rc;
+      if (int rc = palloc(s, &A.wyh, A.pl[0].ps)) return rc;
+    }
+  }
+  if (int rc = palloc(s, &s->d_lvP, (size_t)R)) return rc;
+  CK(cudaMemcpyAsync(s->d_lvP, s->lvP.data(), sizeof(Lev3) * R, cudaMemcpyHostToDevice, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return kOk;
 }
 
 __global__ void k_cvt_to_f32(const double* __restrict__ a, float* __restrict__ b, size_t n, double sign) {
@@ -1680,16 +1820,76 @@ int convert_lev32(asam_ctx* h) {
   return kOk;
 }
 
+// the FP32 copy of the periodic-Laplacian hierarchy (matrices, factors and
+// couplings across the periodic sides; the vectors of lv32)
+int convert_levP32(asam_ctx* h) {
+  ProjState* s = h->proj;
+  if (int rc = alloc_lev32(s)) return rc;
+  const cudaStream_t st = h->L.stream;
+  const int R = s->R;
+  if (!s->d_lvP32) {
+    s->lvP32 = s->lv32;
+    for (int L = 0; L < R; ++L) {
+      Lev3T<float>& B = s->lvP32[L];
+      const Lev3& A = s->lvP[L];
+      for (int q = 0; q < B.nl; ++q) {
+        Lev2T<float>& Q = B.pl[q];
+        const size_t n = Q.ps * Q.m3;
+        float** arr[] = {&Q.d, &Q.uz, &Q.lz, &Q.fw, &Q.ft, &Q.frt, &Q.ux, &Q.lx};
+        for (float** r : arr)
+          if (int rc = palloc(s, r, n)) return rc;
+        if (A.pl[q].wxl) {
+          if (int rc = palloc(s, &Q.wxl, (size_t)Q.c1 * Q.m3)) return rc;
+          if (int rc = palloc(s, &Q.wxh, (size_t)Q.c1 * Q.m3)) return rc;
+        }
+      }
+      const size_t n = B.pl[0].ps * B.m3;
+      if (int rc = palloc(s, &B.u3, n)) return rc;
+      if (int rc = palloc(s, &B.l3, n)) return rc;
+      if (A.wyl) {
+        if (int rc = palloc(s, &B.wyl, B.pl[0].ps)) return rc;
+        if (int rc = palloc(s, &B.wyh, B.pl[0].ps)) return rc;
+      }
+    }
+    if (int rc = palloc(s, &s->d_lvP32, (size_t)R)) return rc;
+    CK(cudaMemcpyAsync(s->d_lvP32, s->lvP32.data(), sizeof(Lev3T<float>) * R, cudaMemcpyHostToDevice, st));
+  }
+  long long nl = convert_one(st, R, s->lvP, s->lvP32);
+  for (int L = 0; L < R; ++L) {
+    const Lev3& A = s->lvP[L];
+    const Lev3T<float>& B = s->lvP32[L];
+    for (int q = 0; q < A.nl; ++q)
+      if (A.pl[q].wxl) {
+        const size_t n = (size_t)A.pl[q].c1 * A.pl[q].m3;
+        k_cvt_to_f32<<<grid_of(n), 256, 0, st>>>(A.pl[q].wxl, B.pl[q].wxl, n, 1.0);
+        k_cvt_to_f32<<<grid_of(n), 256, 0, st>>>(A.pl[q].wxh, B.pl[q].wxh, n, 1.0);
+        nl += 2;
+      }
+    if (A.wyl) {
+      k_cvt_to_f32<<<grid_of(A.pl[0].ps), 256, 0, st>>>(A.wyl, B.wyl, A.pl[0].ps, 1.0);
+      k_cvt_to_f32<<<grid_of(A.pl[0].ps), 256, 0, st>>>(A.wyh, B.wyh, A.pl[0].ps, 1.0);
+      nl += 2;
+    }
+  }
+  count_launches(nl);
+  s->lvP32_ready = true;
+  return kOk;
+}
+
 // Solve_3D in the selected precision on LaplNeumann (or LaplDirichlet): b
 // (level-0 layout, FP64) scaled by sign -> x (FP64)
-void vcycle_any(asam_ctx* h, const double* b, double sign, double* x, bool dirichlet = false) {
+// which hierarchy a V-cycle runs on
+enum { kHierNeumann = 0, kHierDirichlet = 1, kHierPeriodic = 2 };
+void vcycle_any(asam_ctx* h, const double* b, double sign, double* x, int which = kHierNeumann) {
   ProjState* s = h->proj;
   const size_t n = len0(s);
   const cudaStream_t st = h->L.stream;
-  if (use_mg32(h) && s->lv32_ready) {
+  if (use_mg32(h) && s->lv32_ready && (which != kHierPeriodic || s->lvP32_ready)) {
     k_cvt_to_f32<<<grid_of(n), 256, 0, st>>>(b, s->lv32[0].b, n, sign);
-    if (dirichlet)
+    if (which == kHierDirichlet)
       vcycle_run<float>(h, s->lvD32, s->d_lvD32);
+    else if (which == kHierPeriodic)
+      vcycle_run<float, true>(h, s->lvP32, s->d_lvP32);
     else
       vcycle_run<float>(h, s->lv32, s->d_lv32);
     k_cvt_to_f64<<<grid_of(n), 256, 0, st>>>(s->lv32[0].x, x, n);
@@ -1702,8 +1902,10 @@ void vcycle_any(asam_ctx* h, const double* b, double sign, double* x, bool diric
     k_neg<<<grid_of(n), 256, 0, st>>>(s->lv[0].b, b, n);
     count_launches(1);
   }
-  if (dirichlet)
+  if (which == kHierDirichlet)
     vcycle_run<double>(h, s->lvD, s->d_lvD);
+  else if (which == kHierPeriodic)
+    vcycle_run<double, true>(h, s->lvP, s->d_lvP);
   else
     vcycle_run<double>(h, s->lv, s->d_lv);
   if (x != s->lv[0].x) cudaMemcpyAsync(x, s->lv[0].x, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
@@ -1760,10 +1962,15 @@ void matvec1_dev(asam_ctx* h, const double* x, double* y, bool exchange) {
 // With face unknowns: PressurePre; b2pBx1Full + Exchange; SchurPreFull (the
 // face terms as a pressure right-hand side, Solve_3D on LaplDirichlet, the
 // faces from that pressure) + Exchange; b1pBTx2Full; PressurePre.
+void psolve_per_dev(asam_ctx* h, const double* v, double* z);
 void psolve1_dev(asam_ctx* h, const double* v, double* z) {
   ProjState* s = h->proj;
   if (!s->nface) {
     vcycle_any(h, v, -1.0, z);
+    return;
+  }
+  if (use_per(h) && s->lvP_ready) {
+    psolve_per_dev(h, v, z);
     return;
   }
   const Dims& d = h->d;
@@ -1776,12 +1983,39 @@ void psolve1_dev(asam_ctx* h, const double* v, double* z) {
   k_pv_faces<<<grid_of(s->nface / 2), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, pf, 1, 1, v, s->tmp, z);
   cudaMemsetAsync(s->tmp2, 0, n * sizeof(double), st);  // SchurPreBlock: BVec%p = 0
   k_pv_face_p<<<grid_of(s->nface), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, 1, z, s->tmp2);
-  vcycle_any(h, s->tmp2, 1.0, s->tmp, true);
+  vcycle_any(h, s->tmp2, 1.0, s->tmp, kHierDirichlet);
   k_pv_faces<<<grid_of(s->nface / 2), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, pf, 2, 1, z, s->tmp, z);
   k_neg<<<grid_of(n), 256, 0, st>>>(s->tmp2, v, n);  // b1pBTx2Full: -x%p + the face terms
   k_pv_face_p<<<grid_of(s->nface), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, 0, z, s->tmp2);
   count_launches(5);
   vcycle_any(h, s->tmp2, 1.0, z);  // PressurePre(z, z)
+}
+
+// The refined mode's preconditioner on a block with periodic x/y sides (no
+// reference counterpart; FGMRES is flexible, so any preconditioner leaves its
+// FP64 Arnoldi relation and residual test unchanged): the face unknowns of
+// the PressureVelocity system are eliminated exactly -- the Schur complement
+// on the pressure is the Laplacian with the shared face treated as an
+// interior face -- and that periodic Laplacian is solved by one V-cycle of
+// the same multigrid whose plane and line relaxations also couple across the
+// periodic sides.  One V-cycle per FGMRES step instead of PSolve1's three.
+//   rhs' = v_p - b_W v_u/M at the first cell + b_E v_u/M at the last
+//   p    = L_per^-1 (-rhs')
+//   u    = (v_u - cp_W(p) + cp_E(p))/M on both copies of the face
+// (b = beta0*dtP*F*DT*DTT, cp = beta0*dtP*F*DUT*DU*p, M the face's whole mass).
+void psolve_per_dev(asam_ctx* h, const double* v, double* z) {
+  ProjState* s = h->proj;
+  const Dims& d = h->d;
+  const cudaStream_t st = h->L.stream;
+  const size_t n = len0(s);
+  const double bd = s->beta0 * s->dtp;
+  const Lev2& P0 = s->lv[0].pl[0];
+  cudaMemcpyAsync(s->tmp2, v, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+  k_pv_face_p<<<grid_of(s->nface), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, 2, v, s->tmp2);
+  count_launches(1);
+  vcycle_any(h, s->tmp2, -1.0, z, kHierPeriodic);
+  k_pv_faces<<<grid_of(s->nface / 2), 256, 0, st>>>(d, h->geom(), s->wt, P0, s->fc, bd, 0.0, 3, 1, v, z, z);
+  count_launches(1);
 }
 
 // FGMRES (SOLU/Iter_Mod.f90:121-199) on PressureVelocity vectors x (in/out), b
@@ -2059,6 +2293,15 @@ int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
   // closed wall (velocity rule other than 'OutFlow'); axes (1,2,3) = (z,x,y)
   const double fz = d.per_z ? 2.0 : 0.0, fx = d.per_x ? 2.0 : 0.0, fy = d.per_y ? 2.0 : 0.0;
   const Facs fcD{fz, fz, fx, fx, fy, fy};
+  // the periodic Laplacian: the diagonal term of the shared face is the
+  // interior-face term 2*F*../(d(first)+d(last)), i.e. the boundary term with
+  // factor 2*d(first)/(d(first)+d(last)) -- 1 on the uniform horizontal grids
+  // of the configurations (taken as 1: the hierarchy only preconditions)
+  const bool per = use_per(h);
+  const Facs fcP{0.0, 0.0, d.per_x ? 1.0 : 0.0, d.per_x ? 1.0 : 0.0, d.per_y ? 1.0 : 0.0, d.per_y ? 1.0 : 0.0};
+  if (per) {
+    if (int rc = alloc_levP(s, d)) return rc;
+  }
   const double fa = s->cfg.fac_anela;
   k_fine_fields<<<grid_of((size_t)(d.nx + 1) * (d.nz + 1) * (d.ny + 1)), 256, 0, st>>>(
       d, h->fu, h->fv, h->fw, h->volc, s->wt.dtu, s->wt.dtv, s->wt.dtw, s->wt.duu, s->wt.duv, s->wt.duw, s->wt.dut, s->g);
@@ -2084,7 +2327,7 @@ int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
       k_assemble<<<grid_of(ncell), 256, 0, st>>>(c, P, full ? A.u3 : nullptr, full ? A.l3 : nullptr, full ? 1 : 0, bd2, fc, fa);
       k_factor<<<grid_of((size_t)P.m3 * P.c2), 256, 0, st>>>(P);
       nl += 5;
-      if (s->nface > 0) {  // LaplDirichlet from the same coarse fields
+      if (s->nface > 0 && !per) {  // LaplDirichlet from the same coarse fields
         Lev3& B = s->lvD[L];
         Lev2& Q = B.pl[L2 - L];
         k_assemble<<<grid_of(ncell), 256, 0, st>>>(c, Q, full ? B.u3 : nullptr, full ? B.l3 : nullptr, full ? 1 : 0, bd2,
@@ -2092,17 +2335,44 @@ int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
         k_factor<<<grid_of((size_t)Q.m3 * Q.c2), 256, 0, st>>>(Q);
         nl += 2;
       }
+      if (per) {  // the periodic Laplacian of the refined mode's preconditioner
+        Lev3& B = s->lvP[L];
+        Lev2& Q = B.pl[L2 - L];
+        k_assemble<<<grid_of(ncell), 256, 0, st>>>(c, Q, full ? B.u3 : nullptr, full ? B.l3 : nullptr, full ? 1 : 0, bd2,
+                                                   fcP, fa);
+        const size_t nw = (size_t)c.n1 * (c.n3 + (full ? c.n2 : 0));
+        k_assemble_wrap<<<grid_of(nw), 256, 0, st>>>(c, Q, full ? B.wyl : nullptr, full ? B.wyh : nullptr, full ? 1 : 0,
+                                                     d.per_x, d.per_y, bd2);
+        k_factor<<<grid_of((size_t)Q.m3 * Q.c2), 256, 0, st>>>(Q);
+        nl += 3;
+      }
     }
   }
   count_launches(nl);
   s->lv32_ready = false;
+  s->lvP32_ready = false;
+  s->lvP_ready = per;
+  s->lvD_ready = s->nface > 0 && !per;
   if (use_mg32(h)) {
     if (int rc = convert_lev32(h)) return rc;
+    if (per) {
+      if (int rc = convert_levP32(h)) return rc;
+    }
   }
   CK(cudaStreamSynchronize(st));
   int rc = check_launch();
   if (!rc) s->assembled = true;
   return rc;
+}
+
+int asam_proj_set_preconditioner(asam_ctx* h, int kind) {
+  if (!h || !h->proj || kind < -1 || kind > 1) return kBadArg;
+  ProjState* s = h->proj;
+  if (s->pre_kind != kind) {
+    s->pre_kind = kind;
+    s->assembled = false;  // the next asam_lapl_compute assembles what it needs
+  }
+  return kOk;
 }
 
 int asam_proj_set_precision(asam_ctx* h, int prec) {
@@ -2112,6 +2382,9 @@ int asam_proj_set_precision(asam_ctx* h, int prec) {
   if (s->assembled && use_mg32(h) && !s->lv32_ready) {
     s->st = h->L.stream;
     if (int rc = convert_lev32(h)) return rc;
+    if (s->lvP_ready) {
+      if (int rc = convert_levP32(h)) return rc;
+    }
     CK(cudaStreamSynchronize(h->L.stream));
     return check_launch();
   }
@@ -2227,7 +2500,7 @@ int asam_proj_psolve1(asam_ctx* h, const double* x, double* b) {
 long asam_lapl_get_dirichlet(asam_ctx* h, int level3, int level2, int which, double* out) {
   if (need_assembled(h)) return -1;
   ProjState* s = h->proj;
-  if (!s->nface) return -1;
+  if (!s->nface || !s->lvD_ready) return -1;
   std::swap(s->lv, s->lvD);
   const long r = asam_lapl_get(h, level3, level2, which, out);
   std::swap(s->lv, s->lvD);
@@ -2238,7 +2511,7 @@ int asam_lapl_vcycle_dirichlet(asam_ctx* h, const double* b, double* x) {
   if (int rc = need_assembled(h)) return rc;
   if (!x || !b) return kBadArg;
   ProjState* s = h->proj;
-  if (!s->nface) return kBadArg;
+  if (!s->nface || !s->lvD_ready) return kBadArg;
   const Dims& d = h->d;
   const size_t nc = (size_t)d.nx * d.ny * d.nz;
   const cudaStream_t st = h->L.stream;
@@ -2247,7 +2520,7 @@ int asam_lapl_vcycle_dirichlet(asam_ctx* h, const double* b, double* x) {
   if ((rc = copy_in(h, s->bn, b, nc))) return rc;
   k_to_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->bn, s->tmp2, 1.0);
   count_launches(1);
-  vcycle_any(h, s->tmp2, 1.0, s->tmp, true);
+  vcycle_any(h, s->tmp2, 1.0, s->tmp, kHierDirichlet);
   k_from_layout<<<grid_of(nc), 256, 0, st>>>(P0, d.nx, d.ny, d.nz, s->tmp, s->xn);
   count_launches(1);
   CK(cudaMemcpyAsync(x, s->xn, nc * sizeof(double), cudaMemcpyDefault, st));

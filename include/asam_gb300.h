@@ -363,6 +363,14 @@ int asam_project_vel_face(asam_ctx *ctx, double *uf, double *vf, double *wf, dou
  * default) FP32 when the context runs ASAM_PREC_FP32_REFINED, else FP64.
  * No reference counterpart.  asam_lapl_vcycle follows the same choice. */
 int asam_proj_set_precision(asam_ctx *ctx, int prec);
+/* FGMRES preconditioner of a block with periodic x/y sides: 0 PSolve1 (the
+ * reference's, three V-cycles per step), 1 the periodic Laplacian (the face
+ * unknowns eliminated exactly, the Schur complement on the pressure solved by
+ * one V-cycle of a hierarchy whose relaxations couple across the periodic
+ * sides), -1 (the default) 1 when the context runs ASAM_PREC_FP32_REFINED,
+ * else 0.  FGMRES is flexible, so the tolerance is met either way.  Takes
+ * effect at the next asam_lapl_compute.  No reference counterpart. */
+int asam_proj_set_preconditioner(asam_ctx *ctx, int kind);
 /* Number of multigrid V-cycles run by this context's projection (diagnostic). */
 long long asam_proj_vcycles(asam_ctx *ctx);
 

@@ -329,3 +329,43 @@ def test_periodic_project_vel_face_matches_oracle(name):
             np.testing.assert_array_equal(u1[:, :, 0], u1[:, :, -1])
         if g.periodic_y:
             np.testing.assert_array_equal(v1[:, 0, :], v1[:, -1, :])
+
+
+@pytest.mark.parametrize("name", PROJ_PER)
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_periodic_laplacian_preconditioner(name, prec):
+    """The refined mode's preconditioner of a periodic block (no reference
+    counterpart): the face unknowns are eliminated exactly, so the face rows
+    of Exchange(MatVec1(pre(v))) reproduce v's face rows; the pressure rows
+    keep the residual of one V-cycle on the periodic Laplacian, which
+    contracts; FGMRES with it reaches the oracle's solution."""
+    geo, W, (u, v, w), blk, o = _pair(name)
+    g = geo.grid
+    nc = g.nx * g.ny * g.nz
+    rng = np.random.default_rng(21)
+    with blk:
+        blk.proj_set_precision(prec)
+        blk.proj_set_preconditioner("periodic")
+        blk.JacAccGrav(BETA0, DTP)
+        for _ in range(2):
+            # a vector of the operator's range after Exchange, as FGMRES's
+            # Krylov vectors are (zero on the rows of closed faces)
+            x = o.matvec1(rng.standard_normal(o.nvec))
+            o.exchange(x)
+            z = blk.PSolve1(x)
+            r = o.matvec1(z)
+            o.exchange(r)
+            face_tol = 1e-12 if prec == "fp64" else 1e-6
+            np.testing.assert_allclose(r[nc:], x[nc:], rtol=0, atol=face_tol * np.max(np.abs(x[nc:])))
+            assert np.linalg.norm(r[:nc] - x[:nc]) <= 0.5 * np.linalg.norm(x[:nc])
+        b = o.rhs(u, v, w)
+        x_ref = np.zeros_like(b)
+        o.fgmres(x_ref, b, maxiter=40, tol=1e-12, step=10)
+        x = np.zeros_like(b)
+        steps, rel = blk.SolveSound(x, b, MaxIter=40, Tol=1e-12)
+        assert rel <= 1e-12, (steps, rel)
+        assert np.max(np.abs(x - x_ref)) <= 1e-9 * np.max(np.abs(x_ref))
+        blk.proj_set_preconditioner("psolve1")
+        blk.JacAccGrav(BETA0, DTP)
+        if prec == "fp64":  # back to PSolve1: the Dirichlet hierarchy is assembled again
+            np.testing.assert_array_equal(blk.PSolve1(x), o.psolve1(x))
