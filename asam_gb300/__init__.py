@@ -41,7 +41,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import (ASAM_BREAKDOWN, ASAM_NOT_CONVERGED, ASAM_OK, AsamConfig, AsamDynConfig, AsamError, AsamProjConfig,
+from ._lib import (ASAM_BREAKDOWN, ASAM_CUDA_ERROR, ASAM_NOT_CONVERGED, ASAM_OK, AsamConfig, AsamDynConfig, AsamError, AsamProjConfig,
                    check, ptr)
 
 METHODS = {"Ros3AMF": 0, "RosRK32": 1, "RosEul": 2, "Ros3P": 3, "Ros3Pw": 4, "RosRK3": 5, "RosTVD": 6,
@@ -235,6 +235,13 @@ class TransportBlock:
         y = np.empty_like(a)
         check(self.lib.asam_inner_psolve(self.h, ptr(a), ptr(y)), "asam_inner_psolve")
         return y
+
+    def set_wait_limit(self, polls: int):
+        """Polls of one dependency wait of the persistent Gauss-Seidel schedule
+        before its CTA gives up (0: the default); a wait that runs out makes
+        the call raise AsamError (ASAM_CUDA_ERROR) and leaves the context
+        usable.  Diagnostic, no reference counterpart."""
+        check(self.lib.asam_set_wait_limit(self.h, int(polls)), "asam_set_wait_limit")
 
     def BiCGStabMetSp(self, x: np.ndarray, b: np.ndarray, MaxIter: int, Tol: float):
         """Solve A x = b in place of x; returns (MaxIter, Tol) with the reference's

@@ -24,6 +24,7 @@ STATUS = {
     7: "ASAM_IO_ERROR",
 }
 ASAM_OK, ASAM_NOT_CONVERGED, ASAM_BREAKDOWN = 0, 1, 2
+ASAM_CUDA_ERROR = 5
 
 
 class AsamConfig(C.Structure):
@@ -121,6 +122,7 @@ SIGNATURES = [
     ("asam_proj_vcycles", C.c_longlong, [_V]),
     ("asam_proj_set_precision", C.c_int, [_V, C.c_int]),
     ("asam_proj_set_preconditioner", C.c_int, [_V, C.c_int]),
+    ("asam_set_wait_limit", C.c_int, [_V, C.c_int]),
     ("asam_dyn_setup", C.c_int, [_V, C.POINTER(AsamDynConfig), _I, C.c_int, _I, C.c_int]),
     ("asam_face_to_cell", C.c_int, [_V, _V, _V, _V, _V]),
     ("asam_cell_to_face", C.c_int, [_V, _V, _V, _V, _V]),

@@ -149,6 +149,7 @@ struct KrylovScalars {
 // by a kernel of the same stream, so a captured call replays correctly and
 // the counters never need clearing), the ticket counter (zeroed before each
 // call) and the error flag.
+constexpr int kGsSpinLimit = 1 << 21;  // default polls of one dependency wait
 struct GsTileSched {
   const int4* order;
   int nticket;
@@ -157,6 +158,7 @@ struct GsTileSched {
   int* err;
   unsigned* base;
   int group;  // components per CTA
+  int spin;   // polls of one dependency wait before the CTA gives up
 };
 
 // What a reduction's final kernel does with the sum (Krylov recurrences of

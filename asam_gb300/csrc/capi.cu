@@ -301,8 +301,14 @@ void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w) {
     const int axis = h->cfg.inner_precond == 1 ? 2 : h->cfg.inner_precond == 2 ? 0 : 1;
     launch_line_psolve(L, d, nc, val, w.bbuf, out, w.tbuf, axis, (const T*)h->xl_w, (const T*)h->xl_r);
   } else if (inner && h->gs_order) {
-    const GsTileSched sch{h->gs_order,     h->gs_nticket, h->gs_flags,         h->gs_counter,
-                          &h->sc->gs_err, reinterpret_cast<unsigned*>(h->gs_counter + 1), gs_group_of(h->cfg)};
+    const GsTileSched sch{h->gs_order,
+                          h->gs_nticket,
+                          h->gs_flags,
+                          h->gs_counter,
+                          &h->sc->gs_err,
+                          reinterpret_cast<unsigned*>(h->gs_counter + 1),
+                          gs_group_of(h->cfg),
+                          h->gs_spin > 0 ? h->gs_spin : kGsSpinLimit};
     launch_gs_persist(L, d, nc, val, w.bbuf, out, w.tbuf, nsweep, sch);
   } else {
     launch_gs_sweeps(L, d, nc, val, w.bbuf, out, w.tbuf, nsweep, gs_group_of(h->cfg));
@@ -885,6 +891,13 @@ int asam_set_graphs(asam_ctx* h, int on) {
   graphs_reset(h);
   h->use_graphs = on != 0;
   h->step_graphs = on == 2;
+  return kOk;
+}
+
+int asam_set_wait_limit(asam_ctx* h, int polls) {
+  if (!h || polls < 0) return kBadArg;
+  graphs_reset(h);  // captured launches carry the limit
+  h->gs_spin = polls;
   return kOk;
 }
 

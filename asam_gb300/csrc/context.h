@@ -98,6 +98,7 @@ struct asam_ctx {
   int* gs_flags = nullptr;  // one completion counter per tile and component group
   size_t gs_nflags = 0;
   int* gs_counter = nullptr;  // [0] ticket counter; [1] epoch base (unsigned)
+  int gs_spin = 0;            // polls per dependency wait; 0 = the default (2^21)
 
   asam::ProjState* proj = nullptr;  // pressure projection (proj.cu), set up on demand
   asam::DynState* dyn = nullptr;    // dynamical-core stage (dyn.cu), set up on demand

@@ -1159,7 +1159,6 @@ __global__ void __launch_bounds__(256) k_gs_pipe_smem(Dims d, int ncomp, int gro
 // Waits are bounded: a CTA that gives up sets the error flag, lets its own
 // copies in flight land and returns; the other CTAs see the flag and return.
 // ---------------------------------------------------------------------------
-constexpr int kGsSpinLimit = 1 << 21;
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
   int v;
@@ -1171,8 +1170,8 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 }
 
 // counter reached target, in wrap-around (serial number) arithmetic
-__device__ bool gs_wait_flag(const int* f, unsigned target, const int* err) {
-  for (int it = 0; it < kGsSpinLimit; ++it) {
+__device__ bool gs_wait_flag(const int* f, unsigned target, const int* err, int spin) {
+  for (int it = 0; it < spin; ++it) {
     if ((int)((unsigned)ld_acquire(f) - target) >= 0) return true;
     if (*(volatile const int*)err) return false;
     __nanosleep(32);
@@ -1207,14 +1206,14 @@ __global__ void __launch_bounds__(256) k_gs_persist(Dims d, int ncomp, const TM*
       const int id = ((K * nty + J) * ntx + I) * ngroups + g;
       const int sx = ngroups, sy_ = ntx * ngroups, sz_ = ntx * nty * ngroups;
       bool ok = true;
-      if (I > 0) ok = ok && gs_wait_flag(f + id - sx, now, sch.err);
-      if (J > 0) ok = ok && gs_wait_flag(f + id - sy_, now, sch.err);
-      if (K > 0) ok = ok && gs_wait_flag(f + id - sz_, now, sch.err);
+      if (I > 0) ok = ok && gs_wait_flag(f + id - sx, now, sch.err, sch.spin);
+      if (J > 0) ok = ok && gs_wait_flag(f + id - sy_, now, sch.err, sch.spin);
+      if (K > 0) ok = ok && gs_wait_flag(f + id - sz_, now, sch.err, sch.spin);
       if (s > 0) {
-        ok = ok && gs_wait_flag(f + id, prev, sch.err);
-        if (I + 1 < ntx) ok = ok && gs_wait_flag(f + id + sx, prev, sch.err);
-        if (J + 1 < nty) ok = ok && gs_wait_flag(f + id + sy_, prev, sch.err);
-        if (K + 1 < ntz) ok = ok && gs_wait_flag(f + id + sz_, prev, sch.err);
+        ok = ok && gs_wait_flag(f + id, prev, sch.err, sch.spin);
+        if (I + 1 < ntx) ok = ok && gs_wait_flag(f + id + sx, prev, sch.err, sch.spin);
+        if (J + 1 < nty) ok = ok && gs_wait_flag(f + id + sy_, prev, sch.err, sch.spin);
+        if (K + 1 < ntz) ok = ok && gs_wait_flag(f + id + sz_, prev, sch.err, sch.spin);
       }
       if (!ok) atomicExch(sch.err, 1);
       s_ok = ok;
@@ -1760,6 +1759,105 @@ __global__ void k_tri_solve(int ncol, int n1, const T* __restrict__ dd, const T*
   for (int i = n1 - 2; i >= 0; --i) {
     bprev = b[i] - w[i] * bprev;
     b[i] = bprev;
+  }
+}
+
+// The same solve with every global access coalesced.  One warp owns 32
+// consecutive columns; since columns are contiguous, a chunk of kTriRows rows
+// of those columns is 32 runs of kTriRows consecutive values, which the warp
+// copies with consecutive lanes on consecutive addresses of a run (each
+// 32-byte sector read whole by one instruction) into a shared tile
+// [row][column] (pitch 34 doubles: the sixteen lanes of a half-warp
+// touch sixteen different banks in the copy, and the per-column walk reads
+// consecutive words).  Each lane then runs its own column's recurrence over the
+// chunk from the tile, with the reference's operations in its order, and the
+// elimination factors w and the forward values are written back through the
+// tile the same way; the back substitution walks the chunks downwards.
+constexpr int kTriRows = 8;
+constexpr int kTriWarps = 4;  // warps per block, each independent
+constexpr int kTriPitch = 34;
+
+template <typename T>
+__device__ __forceinline__ void tri_tile_load(T (*tile)[kTriPitch], const T* __restrict__ src, int stride, int c0, int ncol,
+                                              int r0, int nrow, int lane) {
+  // element e of the chunk: column e / kTriRows, row e % kTriRows
+#pragma unroll
+  for (int e = lane; e < 32 * kTriRows; e += 32) {
+    const int c = e / kTriRows, r = e % kTriRows;
+    const int row = r0 + r;
+    if (c0 + c < ncol && row >= 0 && row < nrow) tile[r][c] = src[(size_t)(c0 + c) * stride + row];
+  }
+}
+template <typename T>
+__device__ __forceinline__ void tri_tile_store(const T (*tile)[kTriPitch], T* __restrict__ dst, int stride, int c0, int ncol,
+                                               int r0, int nrow, int lane) {
+#pragma unroll
+  for (int e = lane; e < 32 * kTriRows; e += 32) {
+    const int c = e / kTriRows, r = e % kTriRows;
+    const int row = r0 + r;
+    if (c0 + c < ncol && row >= 0 && row < nrow) dst[(size_t)(c0 + c) * stride + row] = tile[r][c];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kTriWarps) k_tri_solve_w(int ncol, int n1, const T* __restrict__ dd,
+                                                                 const T* __restrict__ uu, const T* __restrict__ ll,
+                                                                 T* __restrict__ bb, T* __restrict__ ww) {
+  __shared__ T sh[kTriWarps][4][kTriRows][kTriPitch];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c0 = (blockIdx.x * kTriWarps + warp) * 32;
+  if (c0 >= ncol) return;  // uniform over the warp
+  T(*td)[kTriPitch] = sh[warp][0];
+  T(*tu)[kTriPitch] = sh[warp][1];  // u(i-1) in, w(i-1) out
+  T(*tl)[kTriPitch] = sh[warp][2];  // l(i-1)
+  T(*tb)[kTriPitch] = sh[warp][3];  // b(i) in, forward value out
+  const int m = n1 - 1;      // length of u, l and w's used part
+  const bool live = c0 + lane < ncol;
+  T t = (T)0, g = (T)0;
+  // forward elimination, rows [r0, r0 + kTriRows); u, l and w at rows r0-1 ...
+  for (int r0 = 0; r0 < n1; r0 += kTriRows) {
+    tri_tile_load(td, dd, n1, c0, ncol, r0, n1, lane);
+    tri_tile_load(tb, bb, n1, c0, ncol, r0, n1, lane);
+    tri_tile_load(tu, uu, m, c0, ncol, r0 - 1, m, lane);
+    tri_tile_load(tl, ll, m, c0, ncol, r0 - 1, m, lane);
+    __syncwarp();
+    if (live) {
+      const int nr = min(kTriRows, n1 - r0);
+      for (int r = 0; r < nr; ++r) {
+        const int i = r0 + r;
+        if (i == 0) {
+          t = td[r][lane];
+          g = tb[r][lane] / t;
+        } else {
+          const T wi = tu[r][lane] / t;
+          tu[r][lane] = wi;
+          t = td[r][lane] - tl[r][lane] * wi;
+          g = (tb[r][lane] - tl[r][lane] * g) / t;
+        }
+        tb[r][lane] = g;
+      }
+    }
+    __syncwarp();
+    tri_tile_store(tb, bb, n1, c0, ncol, r0, n1, lane);
+    tri_tile_store(tu, ww, n1, c0, ncol, r0 - 1, m, lane);
+    __syncwarp();
+  }
+  // back substitution x(i) = g(i) - w(i) x(i+1), i = n1-2 ... 0, chunks downwards
+  T x = g;  // x(n1-1) = g(n1-1), already stored
+  for (int r0 = ((m - 1) / kTriRows) * kTriRows; m > 0 && r0 >= 0; r0 -= kTriRows) {
+    tri_tile_load(tb, bb, n1, c0, ncol, r0, m, lane);
+    tri_tile_load(tu, ww, n1, c0, ncol, r0, m, lane);
+    __syncwarp();
+    if (live) {
+      const int nr = min(kTriRows, m - r0);
+      for (int r = nr - 1; r >= 0; --r) {
+        x = tb[r][lane] - tu[r][lane] * x;
+        tb[r][lane] = x;
+      }
+    }
+    __syncwarp();
+    tri_tile_store(tb, bb, n1, c0, ncol, r0, m, lane);
+    __syncwarp();
   }
 }
 

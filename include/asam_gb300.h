@@ -169,6 +169,14 @@ int asam_psolve(asam_ctx *ctx, const double *x, double *px);
  * schedule or the column line solve, halo handling as PSolve, result widened
  * to FP64), for tests and measurement.  Refined precision only. */
 int asam_inner_psolve(asam_ctx *ctx, const double *x, double *px);
+/* No reference counterpart, diagnostic: the polls of one dependency wait of
+ * the persistent Gauss-Seidel schedule before its CTA gives up (0: the
+ * default 2^21, each poll followed by a short sleep).  A wait that gives up
+ * sets an error flag; every CTA then leaves, and the call returns
+ * ASAM_CUDA_ERROR ("a dependency wait gave up") with the context still
+ * usable.  A limit of a few polls makes the waits run out, which is how the
+ * give-up path is tested. */
+int asam_set_wait_limit(asam_ctx *ctx, int polls);
 
 /* BiCGStabMetSp: BiCGStabMet_Vec4CellSp (MODULE/SpMatrix4CellPar_Mod.f90:245-348).
  * x in/out (initial guess), b right-hand side.  maxiter/tol in/out with the
@@ -302,7 +310,7 @@ int asam_proj_weights(asam_ctx *ctx, const double *dtu, const double *dtv, const
                       const double *duv, const double *duw, const double *dut, const double *dtt);
 /* The sound weights computed on the device instead, for ThetaKind='Density'
  * (WeightDiagCompute, MULTI/JacAccGrav_Mod.f90:4259-4282, with
- * CellToFaceRhoWeight :3254-3702 on a closed block): state holds rho theta
+ * CellToFaceRhoWeight :3254-3702 on closed walls and periodic x/y sides): state holds rho theta
  * (th_pos), the density (rho_pos) and optionally vapour, cloud and rain water
  * (rv_pos, rc_pos, rr_pos; -1 = absent); tabs is the padded absolute
  * temperature (TAbsCell).  The reference points its vapour at the cloud-water

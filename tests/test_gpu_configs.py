@@ -14,10 +14,19 @@ cases), through the C-ABI against the oracle:
   snapping, the small-cell merge, stretched levels): 2 transport steps
   (prescribed winds, dt = 2 s, BiCGStab 1e-10) at 1e-12 per field;
 * configuration 2's generator on a 48x48x128 periodic window: 2 full
-  Rosenbrock steps of the dynamical core at 1e-12.
+  Rosenbrock steps of the dynamical core at 1e-12;
+* configuration 5 at its full size (128x128x64 cut-cell hill, h = 800 m,
+  half-width 4 km, a passive tracer, RosRK3 dt = 2 s, 40 steps, checkpoints
+  every 8, J = volume integral of the tracer mixing ratio squared over a
+  16x16x8 box at the final time): the gradient with respect to the initial
+  tracer and the wind against central differences (eps = 1e-6) along 32
+  seeded directions, and the dot-product tests of the stage-solve and step
+  adjoints.
 The step counts are what the single-threaded oracle finishes in a few minutes.
 """
 from __future__ import annotations
+
+import ctypes as C
 
 import numpy as np
 import pytest
@@ -89,3 +98,143 @@ def test_config2_256_transport_steps(built_lib):
 
 def test_config2_window_full_step(built_lib):
     _dyn_parity(G.hill_dyn_case(48, 48, 128, seed=2), 2.0, 2)
+
+
+ADJ_TOL = 1e-14  # Krylov tolerance of every forward and adjoint solve below
+
+
+def _config5():
+    """The adjoint configuration's workload and target box (the bench's)."""
+    geo, vel, st = G.hill_case(128, 128, 64, seed=5, height=800.0, halfwidth=4000.0, moist=False, momentum=False,
+                               tracer=True)
+    g = geo.grid
+    i0 = max(1, int(0.3 * g.nx) + 1)
+    j0 = max(1, g.ny // 2 - 7)
+    k0 = max(1, g.nz // 8)
+    box = (i0, min(g.nx, i0 + 15), j0, min(g.ny, j0 + 15), k0, min(g.nz, k0 + 7))
+    return geo, vel, st, box
+
+
+def _interior(geo, x):
+    return x.reshape(geo.grid.pshape)[1:-1, 1:-1, 1:-1]
+
+
+def _idot(geo, x, y):
+    return float(np.sum(_interior(geo, x) * _interior(geo, y)))
+
+
+def _rand_interior(geo, rng):
+    x = np.zeros(geo.grid.pshape)
+    x[1:-1, 1:-1, 1:-1] = rng.standard_normal(x[1:-1, 1:-1, 1:-1].shape)
+    return x.reshape(-1)
+
+
+def test_config5_adjoint_full_size(built_lib):
+    geo, vel, st, box = _config5()
+    g = geo.grid
+    nc = st.c.shape[0]
+    comp = nc - 1
+    nsteps, dt, ck = 40, 2.0, 8
+    sl = (slice(box[4], box[5] + 1), slice(box[2], box[3] + 1), slice(box[0], box[1] + 1))
+    uf, vf, wf = (np.ascontiguousarray(v, dtype=np.float64) for v in vel)
+    with TransportBlock(geo, ncomp=nc, method="RosRK3", bicgstab_tol=ADJ_TOL, bicgstab_maxiter=400) as blk:
+        lib = blk.lib
+        blk.set_velocity(uf, vf, wf)
+        c = np.ascontiguousarray(st.c, dtype=np.float64).copy()
+        J = C.c_double()
+        gc, gr = np.empty(g.npad), np.empty(g.npad)
+        gu, gv, gw = np.empty(uf.size), np.empty(vf.size), np.empty(wf.size)
+        cbox = (C.c_int * 6)(*box)
+        assert lib.asam_tracer_wind_gradient(blk.h, c.ctypes.data, comp, nsteps, dt, ck, cbox, ADJ_TOL, C.byref(J),
+                                             gc.ctypes.data, gr.ctypes.data, gu.ctypes.data, gv.ctypes.data,
+                                             gw.ctypes.data) == 0
+
+        def objective(state, u, v, w):
+            blk.set_velocity(u, v, w)
+            s = state.copy()
+            for _ in range(nsteps):
+                blk.Ros3MetC(s, dt)
+            s = blk.ExchangeCell(s)
+            q = s[comp] / (s[0] + 1e-30)
+            return float(np.sum(q[sl] ** 2 * geo.volc[sl]))
+
+        j0 = objective(c, uf, vf, wf)
+        assert abs(j0 - J.value) <= 1e-10 * abs(J.value), (j0, J.value)
+        rng = np.random.default_rng(55)
+        eps = 1e-6
+        cmax = float(np.abs(c[comp]).max())
+        rel_c, rel_w = [], []
+        for q in range(32):  # 16 directions in the initial tracer, 16 in the wind
+            cp, cm = c.copy(), c.copy()
+            up, um = [uf, vf, wf], [uf, vf, wf]
+            if q % 2 == 0:
+                dc = (_rand_interior(geo, rng) * cmax).reshape(c[comp].shape)
+                cp[comp] += eps * dc
+                cm[comp] -= eps * dc
+                ad = _idot(geo, gc, dc.reshape(-1))
+            else:  # relative perturbations: a face at rest stays at rest
+                dw = [rng.standard_normal(f.shape) * 1e-2 * f for f in (uf, vf, wf)]
+                up = [f + eps * e for f, e in zip((uf, vf, wf), dw)]
+                um = [f - eps * e for f, e in zip((uf, vf, wf), dw)]
+                ad = sum(float(np.sum(gq * e.reshape(-1))) for gq, e in zip((gu, gv, gw), dw))
+            fd = (objective(cp, *up) - objective(cm, *um)) / (2 * eps)
+            (rel_c if q % 2 == 0 else rel_w).append(abs(fd - ad) / abs(ad))
+        blk.set_velocity(uf, vf, wf)
+        rel_c, rel_w = np.array(rel_c), np.array(rel_w)
+        print("config5 fd rel: tracer max %.3e median %.3e, wind max %.3e median %.3e"
+              % (rel_c.max(), np.median(rel_c), rel_w.max(), np.median(rel_w)))
+        # exact: the tracer gradient against the tangent-linear chain of the
+        # same 40 steps (dot-product identity over the trajectory)
+        states = [c.copy()]
+        for _ in range(nsteps):
+            s1 = states[-1].copy()
+            blk.Ros3MetC(s1, dt)
+            states.append(s1)
+        final = blk.ExchangeCell(states[-1])
+        dJdc = np.zeros(g.pshape)
+        dJdc[sl] = 2.0 * final[comp][sl] / (final[0][sl] + 1e-30) ** 2 * geo.volc[sl]
+        tlm_rel = []
+        for _ in range(4):
+            d = _rand_interior(geo, rng) * cmax
+            dd = d.copy()
+            for st_ in states[:-1]:
+                out = np.empty_like(dd)
+                assert lib.asam_ros_step_tlm(blk.h, st_.ctypes.data, comp, dd.ctypes.data, out.ctypes.data, dt,
+                                             ADJ_TOL) == 0
+                dd = out
+            tl = _idot(geo, dJdc.reshape(-1), dd)
+            ad = _idot(geo, gc, d)
+            tlm_rel.append(abs(tl - ad) / abs(ad))
+        print("config5 tangent-linear chain rel: max %.3e" % max(tlm_rel))
+        # dot-product test of one step's adjoint at the initial state
+        du = _rand_interior(geo, rng) * cmax * 1e-2
+        out = np.empty_like(du)
+        assert lib.asam_ros_step_tlm(blk.h, c.ctypes.data, comp, du.ctypes.data, out.ctypes.data, dt, ADJ_TOL) == 0
+        lam = _rand_interior(geo, rng)
+        lout = np.empty_like(lam)
+        assert lib.asam_ros_step_adj(blk.h, c.ctypes.data, comp, lam.ctypes.data, lout.ctypes.data, dt, ADJ_TOL) == 0
+        lhs, rhs = _idot(geo, out, lam), _idot(geo, du, lout)
+        step_dot = abs(lhs - rhs) / abs(lhs)
+        # dot-product test of the stage solve's adjoint (the step's first stage matrix)
+        blk.Jac(c, dt)
+        b = _rand_interior(geo, rng)
+        y = _rand_interior(geo, rng)
+        B = np.zeros_like(c)
+        B[comp] = b.reshape(c[comp].shape)
+        X = np.zeros_like(c)
+        it_f, _ = blk.BiCGStabMetSp(X, B, 400, 1e-15)
+        x = np.ascontiguousarray(X[comp]).reshape(-1)
+        z = np.zeros_like(y)
+        mi, tl = C.c_int(800), C.c_double(1e-15)
+        assert lib.asam_bicgstab_adj(blk.h, z.ctypes.data, y.ctypes.data, C.byref(mi), C.byref(tl)) in (0, 1)
+        xy, bz = _idot(geo, x, y), _idot(geo, b, z)
+        solve_dot = abs(xy - bz) / abs(xy)
+        print("config5 dot: step %.3e (%r %r) solve %.3e (%r %r, forward %d, adjoint %d iterations)"
+              % (step_dot, lhs, rhs, solve_dot, xy, bz, it_f, mi.value))
+        assert step_dot <= 1e-12, step_dot
+        assert solve_dot <= 1e-12, solve_dot
+        assert max(tlm_rel) <= 1e-10, tlm_rel
+        # central differences: the Koren limiter's kinks inside +-eps limit
+        # their agreement with the exact derivative
+        assert rel_c.max() <= 2e-3 and np.median(rel_c) <= 1e-4, rel_c
+        assert rel_w.max() <= 2e-3 and np.median(rel_w) <= 1e-4, rel_w

@@ -197,6 +197,30 @@ def test_inner_psolve_fp32(env, name, iterg):
     assert max(errs) <= 2e-5, errs
 
 
+def test_persistent_gs_wait_gives_up(env):
+    """The persistent schedule's bounded dependency waits: with a limit of one
+    poll the waits run out (a tile's dependencies are computed by CTAs that
+    started at the same time), every CTA leaves, the call returns
+    ASAM_CUDA_ERROR with the schedule's message instead of hanging or
+    trapping, and the same context afterwards reproduces its earlier result
+    bit for bit (the completion counters need no repair)."""
+    asam, _ = env
+    name = "hill_24x20x16"
+    _, _, val, b = _system(env, name)
+    with _block(env, name, precision="fp32_refined", inner_gs_iter=3, gs_schedule="persistent") as blk:
+        blk.set_jac_matrix(val)
+        want = blk.inner_psolve(b)
+        blk.set_wait_limit(1)
+        with pytest.raises(asam.AsamError) as e:
+            for _ in range(5):
+                blk.inner_psolve(b)
+        assert e.value.status == asam.ASAM_CUDA_ERROR
+        assert "gave up" in str(e.value)
+        blk.set_wait_limit(0)
+        for _ in range(2):
+            assert np.array_equal(blk.inner_psolve(b), want)
+
+
 @pytest.mark.parametrize("precond,axis", [("line", 2), ("xline", 0), ("yline", 1)])
 @pytest.mark.parametrize("name", ALL)
 def test_inner_line_psolve_fp32(env, name, precond, axis):
@@ -299,7 +323,8 @@ def test_total_scalar(env, name):
     assert abs(got - ref) <= 1e-13 * abs(ref)
 
 
-@pytest.mark.parametrize("ncol,n1", [(1, 1), (7, 2), (33, 64), (1000, 128)])
+@pytest.mark.parametrize("ncol,n1", [(1, 1), (7, 2), (31, 9), (32, 8), (33, 64), (65, 17), (100, 1), (5, 130),
+                                     (1000, 128)])
 def test_thomas_bitwise(env, ncol, n1):
     asam, oracle = env
     rng = np.random.default_rng(ncol * 1000 + n1)
