@@ -546,6 +546,13 @@ class Batch:
     def __exit__(self, *exc):
         self.close()
 
+    def set_graph(self, on: bool = True):
+        """One-graph mode (FP64 members with their own streams): a call records
+        the whole run -- nsteps device-driven steps of every member -- as one
+        CUDA graph with one branch per member (kept while the states, step
+        sizes and step count stay the same) and launches it once."""
+        check(self.lib.asam_batch_set_graph(self.h, int(bool(on))), "asam_batch_set_graph")
+
     def ros_step(self, states, dt, nsteps: int = 1):
         """Advance every member nsteps steps.  states: per member a C-contiguous
         float64 host array (updated in place) or a device pointer (int); dt: one

@@ -136,6 +136,7 @@ SIGNATURES = [
     ("asam_batch_create", C.c_int, [C.c_int, _V, C.c_int, C.POINTER(C.c_void_p)]),
     ("asam_batch_destroy", C.c_int, [_V]),
     ("asam_batch_ros_step", C.c_int, [_V, _V, _D, C.c_int, _I, _D, _I]),
+    ("asam_batch_set_graph", C.c_int, [_V, C.c_int]),
     ("asam_npad", C.c_longlong, [C.POINTER(AsamConfig)]),
     ("asam_probe_fp64_fma", C.c_int, [C.c_int, _D]),
     ("asam_launch_count", C.c_longlong, []),

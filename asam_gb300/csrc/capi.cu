@@ -11,6 +11,7 @@
 #include "context.h"
 
 #include <atomic>
+#include <mutex>
 
 namespace asam {
 static std::atomic<long long> g_launches{0};
@@ -409,20 +410,16 @@ int bicgstab_dev(asam_ctx* h, const T* val, T* x, const T* b, int* maxiter, doub
       launch_pupdate(L, len, h->sc, w.r, w.v, w.p);
     }
     psolve_dev<T>(h, val, w.p, w.ph, w);
-    launch_matvec(L, d, nc, val, w.ph, w.v, 0);
-    launch_dot(L, d, nc, w.rt, w.v, h->partial, h->sc, OP_ALPHA, nullptr);
-    launch_axpy_sc(L, len, h->sc, SEL_ALPHA, -1.0, w.v, w.r);
-    launch_dot(L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM_HALF, nullptr);
+    launch_matvec_dot(L, d, nc, val, w.ph, w.v, w.rt, h->partial, h->sc, OP_ALPHA);  // v = A ph, (r~, v)
+    launch_axpy_dot(L, d, nc, h->sc, SEL_ALPHA, -1.0, w.v, w.r, h->partial, OP_RNORM_HALF);  // r -= alpha v, (r, r)
   };
   // second half without the update of x (launched after it: x is the
   // caller's array, and nothing in the half reads alpha/omega after it)
   auto half2 = [&]() {
     psolve_dev<T>(h, val, w.r, w.rh, w);
-    launch_matvec(L, d, nc, val, w.rh, w.t, 0);
-    launch_dot(L, d, nc, w.t, w.r, h->partial, h->sc, OP_STORE_A, nullptr);
-    launch_dot(L, d, nc, w.t, w.t, h->partial, h->sc, OP_OMEGA, nullptr);
-    launch_axpy_sc(L, len, h->sc, SEL_OMEGA, -1.0, w.t, w.r);
-    launch_dot(L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM_FULL, nullptr);
+    // t = A rh with (t, r) and (t, t); r -= omega t with (r, r)
+    launch_matvec_dot2(L, d, nc, val, w.rh, w.t, w.r, h->partial, h->sc, OP_STORE_A, OP_OMEGA);
+    launch_axpy_dot(L, d, nc, h->sc, SEL_OMEGA, -1.0, w.t, w.r, h->partial, OP_RNORM_FULL);
   };
   const int MaxIter = *maxiter;
   for (int it = 1; it <= MaxIter; ++it) {
@@ -654,6 +651,39 @@ int validate(const asam_config* c) {
   return kOk;
 }
 
+// Device workspace of the host-array column entries (asam_tri_solve,
+// asam_tri_matvec), one per device, grown to the largest call and kept until
+// the process exits, so that a call does not pay cudaMalloc/cudaFree (each
+// synchronises the device).  The entries are synchronous and serialised by
+// g_col_mu, so one workspace per device suffices.  A workspace whose memory
+// no longer belongs to the device (the device was reset) is replaced.
+std::mutex g_col_mu;
+std::vector<std::pair<double*, size_t>> g_col_ws;  // per device ordinal
+
+int col_workspace(size_t n, double** out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if ((int)g_col_ws.size() <= dev) g_col_ws.resize(dev + 1, {nullptr, 0});
+  auto& ws = g_col_ws[dev];
+  if (ws.first) {
+    cudaPointerAttributes a;
+    const bool valid = cudaPointerGetAttributes(&a, ws.first) == cudaSuccess && a.type == cudaMemoryTypeDevice &&
+                       a.device == dev;
+    if (!valid) {
+      cudaGetLastError();
+      ws = {nullptr, 0};
+    }
+  }
+  if (ws.second < n) {
+    if (ws.first) cudaFree(ws.first);
+    ws = {nullptr, 0};
+    CK(cudaMalloc((void**)&ws.first, n * sizeof(double)));
+    ws.second = n;
+  }
+  *out = ws.first;
+  return kOk;
+}
+
 }  // namespace
 
 // Scalar FP64 FMA throughput probe: 8 independent chains per thread.
@@ -841,7 +871,7 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
                 {&h->uf, d.n_uf()},       {&h->vf, d.n_vf()},        {&h->wf, d.n_wf()},        {&h->c, h->len},
                 {&h->cold, h->len},       {&h->rhs, h->len},         {&h->incr, h->len * h->nstage},
                 {&h->phi, h->len},        {&h->gx, d.n_uf() * cfg->ncomp}, {&h->gy, d.n_vf() * cfg->ncomp},
-                {&h->gz, d.n_wf() * cfg->ncomp}, {&h->val, 8 * h->npad}, {&h->partial, (size_t)kRedGrid},
+                {&h->gz, d.n_wf() * cfg->ncomp}, {&h->val, 8 * h->npad}, {&h->partial, 2 * (size_t)kRedGrid},
                 {&h->red_out, 1},         {&h->stage_a, h->len},     {&h->stage_b, h->len},
                 {&h->coef_x, 4 * d.n_uf()}, {&h->coef_y, 4 * d.n_vf()}, {&h->coef_z, 4 * d.n_wf()},
                 {&h->rvol, h->npad}};
@@ -1150,14 +1180,13 @@ int asam_total_scalar(asam_ctx* h, const double* c, int comp, double* out) {
 
 int asam_tri_solve(int ncol, int n1, const double* d, const double* u, const double* l, double* b) {
   if (ncol < 1 || n1 < 1 || !d || !b || (n1 > 1 && (!u || !l))) return kBadArg;
-  size_t nd = (size_t)ncol * n1, no = (size_t)ncol * (n1 - 1);
-  double *dd, *du = nullptr, *dl = nullptr, *db, *dw;
-  CK(cudaMalloc((void**)&dd, nd * sizeof(double)));
-  CK(cudaMalloc((void**)&db, nd * sizeof(double)));
-  CK(cudaMalloc((void**)&dw, nd * sizeof(double)));
+  const size_t nd = (size_t)ncol * n1, no = (size_t)ncol * (n1 - 1);
+  std::lock_guard<std::mutex> lock(g_col_mu);
+  double* ws = nullptr;
+  if (int rc = col_workspace(3 * nd + 2 * no, &ws)) return rc;
+  double *dd = ws, *db = ws + nd, *dw = ws + 2 * nd;
+  double *du = no ? ws + 3 * nd : nullptr, *dl = no ? ws + 3 * nd + no : nullptr;
   if (no) {
-    CK(cudaMalloc((void**)&du, no * sizeof(double)));
-    CK(cudaMalloc((void**)&dl, no * sizeof(double)));
     CK(cudaMemcpy(du, u, no * sizeof(double), cudaMemcpyDefault));
     CK(cudaMemcpy(dl, l, no * sizeof(double), cudaMemcpyDefault));
   }
@@ -1165,32 +1194,20 @@ int asam_tri_solve(int ncol, int n1, const double* d, const double* u, const dou
   CK(cudaMemcpy(db, b, nd * sizeof(double), cudaMemcpyDefault));
   Launch L{0, 1};
   launch_tri_solve(L, ncol, n1, dd, du, dl, db, dw);
-  int rc = check_launch();
-  if (!rc) {
-    cudaError_t e = cudaMemcpy(b, db, nd * sizeof(double), cudaMemcpyDefault);
-    if (e != cudaSuccess) {
-      set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
-      rc = kCudaError;
-    }
-  }
-  cudaFree(dd);
-  cudaFree(db);
-  cudaFree(dw);
-  if (du) cudaFree(du);
-  if (dl) cudaFree(dl);
-  return rc;
+  if (int rc = check_launch()) return rc;
+  CK(cudaMemcpy(b, db, nd * sizeof(double), cudaMemcpyDefault));
+  return kOk;
 }
 
 int asam_tri_matvec(int ncol, int n1, const double* d, const double* u, const double* l, const double* x, double* y) {
   if (ncol < 1 || n1 < 1 || !d || !x || !y || (n1 > 1 && (!u || !l))) return kBadArg;
-  size_t nd = (size_t)ncol * n1, no = (size_t)ncol * (n1 - 1);
-  double *dd, *du = nullptr, *dl = nullptr, *dx, *dy;
-  CK(cudaMalloc((void**)&dd, nd * sizeof(double)));
-  CK(cudaMalloc((void**)&dx, nd * sizeof(double)));
-  CK(cudaMalloc((void**)&dy, nd * sizeof(double)));
+  const size_t nd = (size_t)ncol * n1, no = (size_t)ncol * (n1 - 1);
+  std::lock_guard<std::mutex> lock(g_col_mu);
+  double* ws = nullptr;
+  if (int rc = col_workspace(3 * nd + 2 * no, &ws)) return rc;
+  double *dd = ws, *dx = ws + nd, *dy = ws + 2 * nd;
+  double *du = no ? ws + 3 * nd : nullptr, *dl = no ? ws + 3 * nd + no : nullptr;
   if (no) {
-    CK(cudaMalloc((void**)&du, no * sizeof(double)));
-    CK(cudaMalloc((void**)&dl, no * sizeof(double)));
     CK(cudaMemcpy(du, u, no * sizeof(double), cudaMemcpyDefault));
     CK(cudaMemcpy(dl, l, no * sizeof(double), cudaMemcpyDefault));
   }
@@ -1198,20 +1215,9 @@ int asam_tri_matvec(int ncol, int n1, const double* d, const double* u, const do
   CK(cudaMemcpy(dx, x, nd * sizeof(double), cudaMemcpyDefault));
   Launch L{0, 1};
   launch_tri_matvec(L, ncol, n1, dd, du, dl, dx, dy);
-  int rc = check_launch();
-  if (!rc) {
-    cudaError_t e = cudaMemcpy(y, dy, nd * sizeof(double), cudaMemcpyDefault);
-    if (e != cudaSuccess) {
-      set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
-      rc = kCudaError;
-    }
-  }
-  cudaFree(dd);
-  cudaFree(dx);
-  cudaFree(dy);
-  if (du) cudaFree(du);
-  if (dl) cudaFree(dl);
-  return rc;
+  if (int rc = check_launch()) return rc;
+  CK(cudaMemcpy(y, dy, nd * sizeof(double), cudaMemcpyDefault));
+  return kOk;
 }
 
 }  // extern "C"

@@ -143,6 +143,10 @@ void gs_schedule_free(asam_ctx* h);
 void graphs_reset(asam_ctx* h);
 int ros_step_graph(asam_ctx* h, double* c, double dt, int* iters, double* resid);
 void step_graph_free(asam_ctx* h);
+int step_graph_prepare(asam_ctx* h);
+int step_record(asam_ctx* h, double* c, double dt, long long* n_fixed, long long* n_h1, long long* n_h2);
+int step_outputs(const asam_ctx* h, const KrylovScalars* ks, long long n_fixed, long long n_h1, long long n_h2,
+                 int* iters, double* resid, long long* ran);
 long long thread_launches();
 void proj_free(asam_ctx* h);
 // device arrays of the projection's grid (valid after asam_proj_setup)

@@ -1578,6 +1578,25 @@ struct DotAcc<float> {
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
+// Sum of one double per thread over a block of at most RED_BLOCK threads, in a fixed
+// order (warp shuffles, then the warp sums by the first warp): the value is
+// complete in thread 0.  `ws` holds RED_BLOCK/32 doubles of shared memory;
+// the call ends with the block synchronised, so `ws` may be reused.
+__device__ __forceinline__ double block_sum(double v, double* ws) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) ws[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = lane < (int)((blockDim.x + 31) >> 5) ? ws[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  __syncthreads();
+  return v;
+}
+
 // One warp per interior x-row of one component at a time (lanes along x, so
 // every load is coalesced and no per-element index division is needed).
 template <typename T>
@@ -1609,27 +1628,75 @@ __global__ void k_dot_partial(Dims d, int ncomp, const T* __restrict__ x, const 
     }
     for (; i < nx; i += 32) acc.add(xr[i], yr[i]);
   }
-  __shared__ double sh[RED_BLOCK];
-  sh[threadIdx.x] = acc.value();
-  __syncthreads();
-  for (int w = RED_BLOCK / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-    __syncthreads();
+  __shared__ double ws[RED_BLOCK / 32];
+  const double t = block_sum(acc.value(), ws);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+// SpMV fused with the dot products that read its result (BiCGStab's
+// v = A p-hat with (r~, v), and t = A r-hat with (t, r) and (t, t)): y =
+// MatVecMet(x) exactly as k_matvec, and per-block partial sums over the
+// interior cells of (a, y) -- with kTwo, of (y, a) and (y, y) -- for
+// k_dot_final, so the product is not read back.  RED_GRID blocks of
+// RED_BLOCK threads stride over the padded cells.
+template <typename TM, typename T, bool kTwo>
+__global__ void __launch_bounds__(RED_BLOCK) k_matvec_dot(Dims d, int ncomp, const TM* __restrict__ val,
+                                                          const T* __restrict__ x, T* __restrict__ y,
+                                                          const T* __restrict__ a, double* __restrict__ partial,
+                                                          double* __restrict__ partial2) {
+  const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
+  const size_t n = d.npad();
+  const size_t sy = (size_t)NX, sz = (size_t)NX * NY;
+  DotAcc<T> acc, acc2;
+  for (size_t P = blockIdx.x * (size_t)blockDim.x + threadIdx.x; P < n; P += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    d.ijk(P, i, j, k);
+    const bool in = i >= 1 && i <= d.nx && j >= 1 && j <= d.ny && k >= 1 && k <= d.nz;
+    const T v0 = k > 0 ? (T)val[0 * n + P - sz] : (T)0;
+    const T v1 = j > 0 ? (T)val[1 * n + P - sy] : (T)0;
+    const T v2 = i > 0 ? (T)val[2 * n + P - 1] : (T)0;
+    const T v3 = (T)val[3 * n + P];
+    const T v4 = i < NX - 1 ? (T)val[4 * n + P + 1] : (T)0;
+    const T v5 = j < NY - 1 ? (T)val[5 * n + P + sy] : (T)0;
+    const T v6 = k < NZ - 1 ? (T)val[6 * n + P + sz] : (T)0;
+    for (int ic = 0; ic < ncomp; ++ic) {
+      const T* xa = x + ic * n;
+      T s = (T)0;
+      if (k > 0) s = s + v0 * xa[P - sz];
+      if (j > 0) s = s + v1 * xa[P - sy];
+      if (i > 0) s = s + v2 * xa[P - 1];
+      s = s + v3 * xa[P];
+      if (i < NX - 1) s = s + v4 * xa[P + 1];
+      if (j < NY - 1) s = s + v5 * xa[P + sy];
+      if (k < NZ - 1) s = s + v6 * xa[P + sz];
+      const T xp = xa[P];
+      s = (T)(-1) * xp + s;
+      s = xp + s;
+      y[ic * n + P] = s;
+      if (in) {
+        if (kTwo) {
+          acc.add(s, a[ic * n + P]);
+          acc2.add(s, s);
+        } else {
+          acc.add(a[ic * n + P], s);
+        }
+      }
+    }
   }
-  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+  __shared__ double ws[RED_BLOCK / 32];
+  const double t1 = block_sum(acc.value(), ws);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t1;
+  if (kTwo) {
+    const double t2 = block_sum(acc2.value(), ws);
+    if (threadIdx.x == 0) partial2[blockIdx.x] = t2;
+  }
 }
 
 __device__ __forceinline__ double block_sum_partials(const double* partial, int npart) {
-  __shared__ double sh[RED_BLOCK];
+  __shared__ double ws[RED_BLOCK / 32];
   double s = 0.0;
   for (int q = threadIdx.x; q < npart; q += blockDim.x) s += partial[q];
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (int w = RED_BLOCK / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-    __syncthreads();
-  }
-  return sh[0];
+  return block_sum(s, ws);  // complete in thread 0
 }
 
 // final reduction + the scalar recurrences of BiCGStabMet_Vec4CellSp
@@ -1685,6 +1752,42 @@ __global__ void k_axpy_sc(size_t len, const asam::KrylovScalars* sc, int sel, do
     y[q] = a * x[q] + y[q];
 }
 
+// y = y + sign*coef*x (skipped when the coefficient is 0, as k_axpy_sc)
+// fused with the partial sums of (y, y) over the interior cells that the
+// residual norm test reads next.  One warp per padded x-row of one
+// component (every cell updated; the interior rows and cells counted).
+template <typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_axpy_dot(Dims d, int ncomp, const asam::KrylovScalars* sc, int sel,
+                                                        double sign, const T* __restrict__ x, T* __restrict__ y,
+                                                        double* __restrict__ partial) {
+  const T a = (T)(sign * pick(sc, sel));
+  const int NX = d.NX(), NY = d.NY();
+  const long long rows_c = (long long)NY * d.NZ();
+  const long long nrow = rows_c * ncomp;
+  const size_t n = d.npad();
+  const int lane = threadIdx.x & 31;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  DotAcc<T> acc;
+  for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < nrow; r += nw) {
+    const int ic = (int)(r / rows_c);
+    const long long jk = r - ic * rows_c;
+    const int j = (int)(jk % NY), k = (int)(jk / NY);
+    const bool row_in = j >= 1 && j <= d.ny && k >= 1 && k <= d.nz;
+    const size_t base = (size_t)ic * n + (size_t)jk * NX;
+    for (int i = lane; i < NX; i += 32) {
+      T v = y[base + i];
+      if (a != (T)0) {
+        v = a * x[base + i] + v;
+        y[base + i] = v;
+      }
+      if (row_in && i >= 1 && i <= d.nx) acc.add(v, v);
+    }
+  }
+  __shared__ double ws[RED_BLOCK / 32];
+  const double t = block_sum(acc.value(), ws);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
 // p = beta*(p - omega*v) + r in the reference's two steps:
 // Axpy(-omega,v,p) then Xpay(r,beta,p)
 template <typename T>
@@ -1734,35 +1837,9 @@ __global__ void k_scale_host(size_t len, T a, T* __restrict__ y) {
 // ---------------------------------------------------------------------------
 // Batched Thomas solve / tridiagonal product on vertical columns:
 // MULTI/TriDiagT_Mod.f90:135-155 Solve_1D and :113-133 MatVecT_1D.
-// One thread per column; columns are contiguous (col*n1 + i).
+// Columns are contiguous (col*n1 + i).
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void k_tri_solve(int ncol, int n1, const T* __restrict__ dd, const T* __restrict__ uu,
-                            const T* __restrict__ ll, T* __restrict__ bb, T* __restrict__ ww) {
-  int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= ncol) return;
-  const T* d = dd + (size_t)col * n1;
-  const T* u = uu + (size_t)col * (n1 - 1);
-  const T* l = ll + (size_t)col * (n1 - 1);
-  T* b = bb + (size_t)col * n1;
-  T* w = ww + (size_t)col * n1;
-  T t = d[0];
-  T bprev = b[0] / t;
-  b[0] = bprev;
-  for (int i = 1; i < n1; ++i) {
-    T wi = u[i - 1] / t;
-    w[i - 1] = wi;
-    t = d[i] - l[i - 1] * wi;
-    bprev = (b[i] - l[i - 1] * bprev) / t;
-    b[i] = bprev;
-  }
-  for (int i = n1 - 2; i >= 0; --i) {
-    bprev = b[i] - w[i] * bprev;
-    b[i] = bprev;
-  }
-}
-
-// The same solve with every global access coalesced.  One warp owns 32
+// The solve, with every global access coalesced.  One warp owns 32
 // consecutive columns; since columns are contiguous, a chunk of kTriRows rows
 // of those columns is 32 runs of kTriRows consecutive values, which the warp
 // copies with consecutive lanes on consecutive addresses of a run (each

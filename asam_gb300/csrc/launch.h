@@ -41,6 +41,12 @@ struct Launch {
                   KrylovScalars* sc, int op, double* out);                                                       \
   void launch_axpy_sc(const Launch&, size_t len, const KrylovScalars* sc, int sel, double sign, const T* x,      \
                       T* y);                                                                                     \
+  void launch_matvec_dot(const Launch&, const Dims&, int ncomp, const TM* val, const T* x, T* y, const T* a,     \
+                         double* partial, KrylovScalars* sc, int op);                                            \
+  void launch_matvec_dot2(const Launch&, const Dims&, int ncomp, const TM* val, const T* x, T* y, const T* a,    \
+                          double* partial, KrylovScalars* sc, int op1, int op2);                                 \
+  void launch_axpy_dot(const Launch&, const Dims&, int ncomp, KrylovScalars* sc, int sel, double sign,          \
+                       const T* x, T* y, double* partial, int op);                                               \
   void launch_pupdate(const Launch&, size_t len, const KrylovScalars* sc, const T* r, const T* v, T* p);         \
   void launch_xupdate(const Launch&, size_t len, const KrylovScalars* sc, int with_omega, const T* ph,          \
                       const T* rh, T* x);                                                                        \

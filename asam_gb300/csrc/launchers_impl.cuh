@@ -164,6 +164,27 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
                       T* y) {                                                                                      \
     k_axpy_sc<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, sc, sel, sign, x, y); count_launches(1);                              \
   }                                                                                                                \
+  void launch_matvec_dot(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* x, T* y, const T* a,  \
+                         double* partial, KrylovScalars* sc, int op) {                                             \
+    k_matvec_dot<TM, T, false><<<RED_GRID, RED_BLOCK, 0, L.stream>>>(d, ncomp, val, x, y, a, partial, nullptr);    \
+    k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, RED_GRID, sc, op, nullptr);                                \
+    count_launches(2);                                                                                             \
+  }                                                                                                                \
+  /* two dot products of the product: partial holds 2*RED_GRID values; op1 is final first */                      \
+  void launch_matvec_dot2(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* x, T* y, const T* a, \
+                          double* partial, KrylovScalars* sc, int op1, int op2) {                                  \
+    k_matvec_dot<TM, T, true><<<RED_GRID, RED_BLOCK, 0, L.stream>>>(d, ncomp, val, x, y, a, partial,               \
+                                                                   partial + RED_GRID);                            \
+    k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, RED_GRID, sc, op1, nullptr);                               \
+    k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial + RED_GRID, RED_GRID, sc, op2, nullptr);                    \
+    count_launches(3);                                                                                             \
+  }                                                                                                                \
+  void launch_axpy_dot(const Launch& L, const Dims& d, int ncomp, KrylovScalars* sc, int sel, double sign,        \
+                       const T* x, T* y, double* partial, int op) {                                                \
+    k_axpy_dot<T><<<RED_GRID, RED_BLOCK, 0, L.stream>>>(d, ncomp, sc, sel, sign, x, y, partial);                  \
+    k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, RED_GRID, sc, op, nullptr);                                \
+    count_launches(2);                                                                                             \
+  }                                                                                                                \
   void launch_pupdate(const Launch& L, size_t len, const KrylovScalars* sc, const T* r, const T* v, T* p) {         \
     k_pupdate<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, sc, r, v, p); count_launches(1);                                      \
   }                                                                                                                \
@@ -182,7 +203,9 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
     k_scale_host<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, a, y); count_launches(1);                                          \
   }                                                                                                                \
   void launch_tri_solve(const Launch& L, int ncol, int n1, const T* dd, const T* uu, const T* ll, T* bb, T* ww) {  \
-    k_tri_solve<T><<<(ncol + 127) / 128, 128, 0, L.stream>>>(ncol, n1, dd, uu, ll, bb, ww); count_launches(1);                        \
+    k_tri_solve_w<T><<<(ncol + 32 * kTriWarps - 1) / (32 * kTriWarps), 32 * kTriWarps, 0, L.stream>>>(             \
+        ncol, n1, dd, uu, ll, bb, ww);                                                                             \
+    count_launches(1);                                                                                             \
   }                                                                                                                \
   void launch_tri_matvec(const Launch& L, int ncol, int n1, const T* dd, const T* uu, const T* ll, const T* xx,    \
                          T* yy) {                                                                                  \

@@ -558,20 +558,26 @@ __device__ __noinline__ void line_half(const Lev2T<T>& P, size_t mo, const T* __
     const bool hasL = j > 0, hasR = j < c2 - 1;
     const size_t colL = hasL ? (size_t)(1 - c) * h + ((j - 1) >> 1) : col;
     const size_t colR = hasR ? (size_t)(1 - c) * h + ((j + 1) >> 1) : col;
-    // the periodic wrap couples lines 0 and c2-1; used only when they have
-    // different parities (no line reads a line of its own half-sweep)
-    const bool wrap = kWrap && P.wxl && c2 >= 2 && ((c2 - 1) & 1) && (j == 0 || j == c2 - 1);
-    const size_t wk = (mo / P.ps) * (size_t)c1, colW = slot(0, h, 0, c2 - 1);
+    // periodic-Laplacian hierarchy: line 0's left neighbour is line c2-1 and
+    // line c2-1's right neighbour is line 0, across the periodic side; used
+    // only when the two have different parities (no line reads a line of its
+    // own half-sweep).  The wrap neighbour and its coupling take the ring
+    // slots of the missing neighbour, so they stream ahead like the others.
+    const bool wrap = kWrap && P.wxl && c2 >= 2 && ((c2 - 1) & 1);
+    const bool wL = wrap && j == 0, wR = wrap && j == c2 - 1;
+    const bool useL = hasL || wL, useR = hasR || wR;
+    const size_t wk = (mo / P.ps) * (size_t)c1;
+    const size_t xL0 = wL ? slot(0, h, 0, c2 - 1) : colL, xR0 = wR ? slot(0, h, 0, 0) : colR;
     auto issue = [&](int i) {
       T* sl = ring + (size_t)(i % kRing) * kFields * bd + tid;
       const bool ok = i < c1;
-      const size_t o = (size_t)(ok ? i : 0) * w;
+      const size_t io = ok ? (size_t)i : 0, o = io * w;
       const size_t om = i > 0 && ok ? o - w : o;
       cp_async_elem(sl + 0 * bd, b + col + o, ok);
-      cp_async_elem(sl + 1 * bd, x + colL + o, ok && hasL);
-      cp_async_elem(sl + 2 * bd, x + colR + o, ok && hasR);
-      cp_async_elem(sl + 3 * bd, lx + colL + o, ok && hasL);
-      cp_async_elem(sl + 4 * bd, ux + col + o, ok && hasR);
+      cp_async_elem(sl + 1 * bd, x + xL0 + o, ok && useL);
+      cp_async_elem(sl + 2 * bd, x + xR0 + o, ok && useR);
+      cp_async_elem(sl + 3 * bd, wL ? P.wxl + wk + io : lx + colL + o, ok && useL);
+      cp_async_elem(sl + 4 * bd, wR ? P.wxh + wk + io : ux + col + o, ok && useR);
       cp_async_elem(sl + 5 * bd, lz + col + om, ok && i > 0);
       cp_async_elem(sl + 6 * bd, ft + col + o, ok);
       cp_async_elem(sl + 7 * bd, frt + col + o, ok);
@@ -585,16 +591,11 @@ __device__ __noinline__ void line_half(const Lev2T<T>& P, size_t mo, const T* __
       const T* sl = ring + (size_t)(i % kRing) * kFields * bd + tid;
       T t = sl[0];
       if (fwd) {
-        if (hasL) t = t - sl[3 * bd] * sl[1 * bd];
-        if (hasR) t = t - sl[4 * bd] * sl[2 * bd];
+        if (useL) t = t - sl[3 * bd] * sl[1 * bd];
+        if (useR) t = t - sl[4 * bd] * sl[2 * bd];
       } else {
-        if (hasR) t = t - sl[4 * bd] * sl[2 * bd];
-        if (hasL) t = t - sl[3 * bd] * sl[1 * bd];
-      }
-      if (kWrap && wrap) {  // periodic-Laplacian hierarchy: the line across the periodic x side
-        const size_t ri = (size_t)i * w;
-        if (j == 0) t = t - P.wxl[wk + i] * x[ri + colW];
-        if (j == c2 - 1) t = t - P.wxh[wk + i] * x[ri];
+        if (useR) t = t - sl[4 * bd] * sl[2 * bd];
+        if (useL) t = t - sl[3 * bd] * sl[1 * bd];
       }
       if (i > 0) t = t - sl[5 * bd] * prev;
       const T y = div_rn(t, sl[6 * bd], sl[7 * bd]);

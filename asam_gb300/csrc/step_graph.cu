@@ -157,10 +157,8 @@ int record_solve(asam_ctx* h, double* x, const double* b, int maxiter, double to
   k_pupdate_auto<<<grid_of(h->L, len), kB, 0, s1>>>(len, h->sc, w.r, w.v, w.p);
   count_launches(1);
   psolve_dev<double>(h, val, w.p, w.ph, w);
-  launch_matvec(h->L, d, nc, val, w.ph, w.v, 0);
-  launch_dot(h->L, d, nc, w.rt, w.v, h->partial, h->sc, OP_ALPHA, nullptr);
-  launch_axpy_sc(h->L, len, h->sc, SEL_ALPHA, -1.0, w.v, w.r);
-  launch_dot(h->L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM_HALF, nullptr);
+  launch_matvec_dot(h->L, d, nc, val, w.ph, w.v, w.rt, h->partial, h->sc, OP_ALPHA);
+  launch_axpy_dot(h->L, d, nc, h->sc, SEL_ALPHA, -1.0, w.v, w.r, h->partial, OP_RNORM_HALF);
   k_xupdate_half<<<grid_of(h->L, len), kB, 0, s1>>>(len, h->sc, w.ph, x);
   count_launches(1);
   // IF nothing ended the solve: the second half
@@ -171,11 +169,8 @@ int record_solve(asam_ctx* h, double* x, const double* b, int maxiter, double to
   h->L.stream = s2;
   const long long n2 = thread_launches();
   psolve_dev<double>(h, val, w.r, w.rh, w);
-  launch_matvec(h->L, d, nc, val, w.rh, w.t, 0);
-  launch_dot(h->L, d, nc, w.t, w.r, h->partial, h->sc, OP_STORE_A, nullptr);
-  launch_dot(h->L, d, nc, w.t, w.t, h->partial, h->sc, OP_OMEGA, nullptr);
-  launch_axpy_sc(h->L, len, h->sc, SEL_OMEGA, -1.0, w.t, w.r);
-  launch_dot(h->L, d, nc, w.r, w.r, h->partial, h->sc, OP_RNORM_FULL, nullptr);
+  launch_matvec_dot2(h->L, d, nc, val, w.rh, w.t, w.r, h->partial, h->sc, OP_STORE_A, OP_OMEGA);
+  launch_axpy_dot(h->L, d, nc, h->sc, SEL_OMEGA, -1.0, w.t, w.r, h->partial, OP_RNORM_FULL);
   launch_xupdate(h->L, len, h->sc, 1, w.ph, w.rh, x);
   bc->h2 = thread_launches() - n2;
   if ((rc = end_conditional(s2))) return rc;
@@ -237,56 +232,50 @@ void step_graph_free(asam_ctx* h) {
   h->step_c = nullptr;
 }
 
-// One Rosenbrock step as one graph launch (captured on first use for this
-// state pointer, step size and tolerance); the per-stage BiCGStab outputs are
-// read once.
-int ros_step_graph(asam_ctx* h, double* c, double dt, int* iters, double* resid) {
+// The per-context resources of recorded steps: the stage scalars and the two
+// capture streams of the loop bodies.
+int step_graph_prepare(asam_ctx* h) {
   if (!h->stage_sc) {
     CK(cudaMalloc((void**)&h->stage_sc, 4 * sizeof(KrylovScalars)));
     CK(cudaMallocHost((void**)&h->stage_sc_host, 4 * sizeof(KrylovScalars)));
     for (auto& s : h->cap_stream) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   }
+  return kOk;
+}
+
+// Records one device-driven step of h into the capture running on
+// h->L.stream; kernels outside the loops and per pass of each loop body are
+// returned for the launch count.  On failure the body captures are closed.
+int step_record(asam_ctx* h, double* c, double dt, long long* n_fixed, long long* n_h1, long long* n_h2) {
   const cudaStream_t s0 = h->L.stream;
-  if (!h->step_exec || h->step_c != c || h->step_dt != dt || h->step_tol != h->cfg.bicgstab_tol) {
-    step_graph_free(h);
-    const long long t0 = thread_launches();
-    CK(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
-    BodyCounts bc;
-    const int rc = record_step(h, c, dt, &bc);
-    h->L.stream = s0;
-    if (rc) abandon_bodies(h);
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(s0, &g);
-    const long long nrec = thread_launches() - t0;
-    count_launches(-nrec);  // recorded, not run
-    if (rc) {
-      if (g) cudaGraphDestroy(g);
-      return rc;
-    }
-    h->step_n_h1 = bc.h1;
-    h->step_n_h2 = bc.h2;
-    h->step_n_fixed = nrec - h->nstage * (bc.h1 + bc.h2);
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&h->step_exec, g, 0);
-    if (g) cudaGraphDestroy(g);
-    if (e != cudaSuccess) {
-      h->step_exec = nullptr;
-      set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
-      return kCudaError;
-    }
-    h->step_c = c;
-    h->step_dt = dt;
-    h->step_tol = h->cfg.bicgstab_tol;
+  const long long t0 = thread_launches();
+  BodyCounts bc;
+  const int rc = record_step(h, c, dt, &bc);
+  h->L.stream = s0;
+  const long long nrec = thread_launches() - t0;
+  count_launches(-nrec);  // recorded, not run
+  if (rc) {
+    abandon_bodies(h);
+    return rc;
   }
-  CK(cudaGraphLaunch(h->step_exec, s0));
-  CK(cudaMemcpyAsync(h->stage_sc_host, h->stage_sc, h->nstage * sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s0));
-  CK(cudaStreamSynchronize(s0));
+  *n_h1 = bc.h1;
+  *n_h2 = bc.h2;
+  *n_fixed = nrec - h->nstage * (bc.h1 + bc.h2);
+  return kOk;
+}
+
+// Decodes the stage scalars of one recorded step (host copies) into the
+// reference's per-stage MaxIter/Tol outputs and a status; *ran receives the
+// kernels the step ran (fixed part plus the passes of its loops).
+int step_outputs(const asam_ctx* h, const KrylovScalars* ks, long long n_fixed, long long n_h1, long long n_h2,
+                 int* iters, double* resid, long long* ran) {
   int status = kOk;
-  long long ran = h->step_n_fixed;  // kernels the graph ran: fixed part + loop passes
+  long long nr = n_fixed;
   for (int is = 0; is < h->nstage; ++is) {
-    const KrylovScalars& k = h->stage_sc_host[is];
+    const KrylovScalars& k = ks[is];
     const int passes = k.iter;                                           // first halves
     const int seconds = (k.done == 1 || k.done == 3) ? passes - 1 : passes;  // second halves
-    ran += passes * h->step_n_h1 + (seconds > 0 ? seconds : 0) * h->step_n_h2;
+    nr += passes * n_h1 + (seconds > 0 ? seconds : 0) * n_h2;
     if (k.gs_err) {
       set_last_error("persistent Gauss-Seidel schedule: a dependency wait gave up", __FILE__, __LINE__);
       return kCudaError;
@@ -302,6 +291,44 @@ int ros_step_graph(asam_ctx* h, double* c, double dt, int* iters, double* resid)
     if (k.done == 0) st = kNotConverged;
     if (st != kOk && status == kOk) status = st;
   }
+  *ran = nr;
+  return status;
+}
+
+// One Rosenbrock step as one graph launch (captured on first use for this
+// state pointer, step size and tolerance); the per-stage BiCGStab outputs are
+// read once.
+int ros_step_graph(asam_ctx* h, double* c, double dt, int* iters, double* resid) {
+  if (int rc = step_graph_prepare(h)) return rc;
+  const cudaStream_t s0 = h->L.stream;
+  if (!h->step_exec || h->step_c != c || h->step_dt != dt || h->step_tol != h->cfg.bicgstab_tol) {
+    step_graph_free(h);
+    CK(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+    const int rc = step_record(h, c, dt, &h->step_n_fixed, &h->step_n_h1, &h->step_n_h2);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s0, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&h->step_exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      h->step_exec = nullptr;
+      set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+      return kCudaError;
+    }
+    h->step_c = c;
+    h->step_dt = dt;
+    h->step_tol = h->cfg.bicgstab_tol;
+  }
+  CK(cudaGraphLaunch(h->step_exec, s0));
+  CK(cudaMemcpyAsync(h->stage_sc_host, h->stage_sc, h->nstage * sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s0));
+  CK(cudaStreamSynchronize(s0));
+  long long ran = 0;
+  const int status = step_outputs(h, h->stage_sc_host, h->step_n_fixed, h->step_n_h1, h->step_n_h2, iters, resid,
+                                  &ran);
+  if (status == kCudaError || status == kNanDetected) return status;
   count_launches(ran);
   const int rc = check_launch();
   return rc ? rc : status;

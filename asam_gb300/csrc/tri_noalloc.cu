@@ -83,7 +83,8 @@ extern "C" int asam_tri_solve_noalloc(int ncol, int n1, const double* d, const d
   double* w = nullptr;
   int rc = scratch_on_current_device(&w);
   if (rc) return rc;
-  k_tri_solve<double><<<(ncol + 127) / 128, 128, 0, (cudaStream_t)stream>>>(ncol, n1, d, u, l, b, w);
+  k_tri_solve_w<double><<<(ncol + 32 * kTriWarps - 1) / (32 * kTriWarps), 32 * kTriWarps, 0, (cudaStream_t)stream>>>(
+      ncol, n1, d, u, l, b, w);
   asam::count_launches(1);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

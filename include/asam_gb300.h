@@ -243,7 +243,11 @@ int asam_total_scalar(asam_ctx *ctx, const double *c, int comp, double *out);
 
 /* Batched vertical-column tridiagonal solve, Solve_1D (Thomas,
  * MULTI/TriDiagT_Mod.f90:135-155), over ncol independent columns of length n1:
- * d[col*n1+i], u[col*(n1-1)+i], l[col*(n1-1)+i]; b overwritten by the solution. */
+ * d[col*n1+i], u[col*(n1-1)+i], l[col*(n1-1)+i]; b overwritten by the solution.
+ * Host or device arrays; synchronous.  The inputs go through a device
+ * workspace that the library keeps per device, grown to the largest call (a
+ * call allocates only when it is larger than every earlier one); calls are
+ * serialised. */
 int asam_tri_solve(int ncol, int n1, const double *d, const double *u, const double *l, double *b);
 /* Same solve without any allocation (no counterpart in the reference).  For
  * callers that cannot let a library allocate device memory: a host model
@@ -475,6 +479,15 @@ int asam_batch_create(int nmember, asam_ctx *const *members, int nthreads, asam_
 int asam_batch_destroy(asam_batch *batch);
 int asam_batch_ros_step(asam_batch *batch, double *const *states, const double *dt, int nsteps, int *iters,
                         double *resid, int *status);
+/* One-graph mode (on = 1; 0 returns to the host threads): every member must
+ * be an FP64 context with its own stream.  asam_batch_ros_step then records
+ * the whole call -- nsteps device-driven steps of every member, the BiCGStab
+ * loops as graph WHILE/IF nodes with their exit decisions on the device --
+ * into one CUDA graph with one branch per member, launches it once and reads
+ * every member's per-stage outputs once.  The graph is kept while the device
+ * states, step sizes, step count and tolerances stay the same.  Results are
+ * bitwise those of the members run alone.  No reference counterpart. */
+int asam_batch_set_graph(asam_batch *batch, int on);
 
 /* Rosenbrock coefficients of InitRos3MetC (ADVECT/Int_Mod.f90:78-261):
  * alpha/beta 4x4 row-major, gamma1[5].  Returns nStage (0 = unknown method). */

@@ -53,6 +53,47 @@ def test_batch_matches_members_alone(asam, precision, nthreads):
         assert [list(map(int, s)) for s in its[m]] == its_ref, MEMBERS[m]
 
 
+def test_batch_graph_matches_members_alone(asam):
+    """One-graph mode: the whole 3-step run of every FP64 member as one CUDA
+    graph launch gives bitwise the states and iteration counts of each member
+    run alone; a second call replays the graph; refined members are refused."""
+    import torch
+
+    kw = dict(bicgstab_tol=1e-10)
+    dts = [2.0, 3.0, 1.5, 2.5, 2.0, 4.0]
+    alone = []
+    for (b, st), dt in zip(_blocks(asam, **kw), dts):
+        c = st.c.copy()
+        its = [b.Ros3MetC(c, dt)[0] for _ in range(6)]
+        alone.append((c, its))
+        b.close()
+    members = _blocks(asam, **kw)
+    dev = [torch.from_numpy(st.c.reshape(-1).copy()).cuda() for _, st in members]
+    torch.cuda.synchronize()
+    host0 = members[0][1].c.copy()
+    with asam.Batch([b for b, _ in members]) as batch:
+        batch.set_graph(True)
+        its1, status1 = batch.ros_step([t.data_ptr() for t in dev], dts, nsteps=3)
+        its2, status2 = batch.ros_step([t.data_ptr() for t in dev], dts, nsteps=3)  # replay
+        batch.set_graph(False)
+    torch.cuda.synchronize()
+    for b, _ in members:
+        b.close()
+    assert all(int(x) in (0, 1) for x in status1) and all(int(x) in (0, 1) for x in status2)
+    for m, (c_ref, its_ref) in enumerate(alone):
+        got = dev[m].cpu().numpy().reshape(c_ref.shape)
+        assert np.array_equal(got, c_ref), MEMBERS[m]
+        its = [list(map(int, s)) for s in its1[m]] + [list(map(int, s)) for s in its2[m]]
+        assert its == its_ref, MEMBERS[m]
+    refined = _blocks(asam, bicgstab_tol=1e-10, precision="fp32_refined")
+    with asam.Batch([b for b, _ in refined]) as batch:
+        with pytest.raises(asam.AsamError):
+            batch.set_graph(True)
+    for b, _ in refined:
+        b.close()
+    assert np.array_equal(host0, members[0][1].c)
+
+
 def test_batch_device_states(asam):
     import torch
 
