@@ -94,6 +94,7 @@ def parse():
                         "tight tolerance); prints its JSON object")
     p.add_argument("--accuracy-steps", type=int, default=5)
     p.add_argument("--tight-tol", type=float, default=1e-13, help="Krylov tolerance of the tight runs")
+    p.add_argument("--no-tight", action="store_true", help="accuracy study without the tight-tolerance runs")
     p.add_argument("--no-column", action="store_true", help="skip the column-solve line")
     p.add_argument("--column-only", action="store_true", help="only the column-solve line; prints its JSON object")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -817,8 +818,10 @@ def accuracy_study(a, torch, stream, work, lib_mod):
     alone)."""
     names, mom = work[2].names, work[3]["mom"]
     runs = {}
-    for key, prec, tight in (("fp64", "fp64", False), ("refined", "fp32_refined", False),
-                             ("fp64_tight", "fp64", True), ("refined_tight", "fp32_refined", True)):
+    kinds = [("fp64", "fp64", False), ("refined", "fp32_refined", False)]
+    if not a.no_tight:
+        kinds += [("fp64_tight", "fp64", True), ("refined_tight", "fp32_refined", True)]
+    for key, prec, tight in kinds:
         b = copy.copy(a)
         b.warmup, b.steps = 0, a.accuracy_steps
         if tight:
@@ -830,6 +833,8 @@ def accuracy_study(a, torch, stream, work, lib_mod):
                                                for k, r in runs.items()}, "pairs": {}}
     for got, ref in (("refined", "fp64"), ("fp64", "fp64_tight"), ("refined", "fp64_tight"),
                      ("refined_tight", "fp64_tight")):
+        if got not in runs or ref not in runs:
+            continue
         errs = field_errors(names, runs[got]["final"], runs[ref]["final"], mom)
         out["pairs"][f"{got}_vs_{ref}"] = {
             "max_rel": max(e["max_rel"] for e in errs), "max_rel_state": max(e["max_rel_vec"] for e in errs),
@@ -1081,6 +1086,11 @@ def main():
     # plane/line relaxations with the 3D residual, restriction and prolongation),
     # about 90 % of the FP64 step; algorithmic bytes counted from its schedule
     vb = vcycle_bytes(a.nz, a.nx, a.ny, 4)
+    # DRAM bytes of one such V-cycle at 512x512x128 from one ncu capture of
+    # `python bench.py --probe vcycle` (dram__bytes_read.sum +
+    # dram__bytes_write.sum over its 91 launches; one pass, so taken at full
+    # size); ncu cannot run inside the timed program
+    traffic = 101.389e9 if (a.nx, a.ny, a.nz, a.seed) == (512, 512, 128, 3) else None
     vc_s = r64["kernels"]["vcycle_ms"] * 1e-3
     vgbs = vb / vc_s / 1e9
     line = {
@@ -1094,7 +1104,9 @@ def main():
         "roofline": {"kernel": "one multigrid V-cycle (Solve_3D: k_plane_half zebra plane/x-line/z-column "
                                "relaxations, 3D residual, restriction, prolongation) on the Neumann hierarchy",
                      "bound": "hbm", "achieved": vgbs, "peak": hbm_peak, "unit": "GB/s", "frac": vgbs / hbm_peak,
-                     "traffic": None, "algorithmic_bytes_per_call": vb,
+                     "traffic": traffic, "algorithmic_bytes_per_call": vb,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over the 91 launches of one "
+                                       "V-cycle of this workload (bench.py --probe vcycle), one pass",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
                      "vcycles_per_step": r64["vcycles_per_step"],
                      "share_of_step": r64["vcycles_per_step"] * r64["kernels"]["vcycle_ms"] / (ms / a.steps),

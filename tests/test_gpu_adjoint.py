@@ -133,15 +133,17 @@ def test_stage_solve_adjoint_dot_product(env):
     B = np.zeros_like(c)
     B[comp] = b.reshape(c[comp].shape)
     X = np.zeros_like(c)
-    it, tol = blk.BiCGStabMetSp(X, B, 200, 1e-14)
+    # both solves to 1e-15 (the limit may end them one iteration short of it:
+    # status 1 is accepted), so the dot-product identity holds to 1e-12
+    it, tol = blk.BiCGStabMetSp(X, B, 400, 1e-15)
     x = np.ascontiguousarray(X[comp]).reshape(-1)
     z = np.zeros_like(y)
-    mi = C.c_int(400)
-    tl = C.c_double(1e-14)
+    mi = C.c_int(800)
+    tl = C.c_double(1e-15)
     st = lib.asam_bicgstab_adj(blk.h, z.ctypes.data, y.ctypes.data, C.byref(mi), C.byref(tl))
-    assert st == 0
+    assert st in (0, 1)
     lhs, rhs = _idot(geo, x, y), _idot(geo, b, z)
-    assert abs(lhs - rhs) <= 1e-11 * abs(lhs)
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs), (lhs, rhs, it, mi.value)
     blk.close()
 
 
