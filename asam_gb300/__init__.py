@@ -125,8 +125,9 @@ class TransportBlock:
 
     def set_graphs(self, mode):
         """0/False: launch every kernel; 1/True (default): replay the BiCGStab
-        half-iterations from CUDA graphs; 2: FP64 steps as one device-driven
-        graph (WHILE nodes for the Krylov loops).  The results are the same."""
+        half-iterations from CUDA graphs; 2: steps as one device-driven graph
+        (WHILE nodes for the Krylov loops; refined contexts: the FP64
+        refinement as an outer WHILE node).  The results are the same."""
         check(self.lib.asam_set_graphs(self.h, int(mode)), "asam_set_graphs")
 
     def set_stream(self, stream_handle: int | None):
@@ -547,7 +548,7 @@ class Batch:
         self.close()
 
     def set_graph(self, on: bool = True):
-        """One-graph mode (FP64 members with their own streams): a call records
+        """One-graph mode (members with their own streams): a call records
         the whole run -- nsteps device-driven steps of every member -- as one
         CUDA graph with one branch per member (kept while the states, step
         sizes and step count stay the same) and launches it once."""

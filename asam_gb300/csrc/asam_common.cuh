@@ -140,6 +140,10 @@ struct KrylovScalars {
   int maxiter;
   int out_iters;
   double out_tol;
+  // device-driven refined solve (outer FP64 refinement around the FP32
+  // BiCGStab): passes of the inner loop's two halves, summed over the outer
+  // passes (iter counts the outer passes), to count the kernels that ran
+  int passes1, passes2;
 };
 
 // Schedule of the persistent Gauss-Seidel wavefront (k_gs_persist): tickets

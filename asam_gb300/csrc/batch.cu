@@ -42,7 +42,7 @@ struct asam_batch {
   std::vector<KrylovScalars*> hist;  // per member: nsteps x 4 stage scalars (device)
   KrylovScalars* hist_host = nullptr;
   size_t hist_cap = 0;               // steps the history buffers hold
-  std::vector<long long> n_fixed, n_h1, n_h2;  // per member, per recorded step
+  std::vector<long long> n_fixed, n_h1, n_h2, n_outer;  // per member, per recorded step
 };
 
 namespace {
@@ -108,6 +108,7 @@ int graph_record(asam_batch* b, const std::vector<double*>& dc, const double* dt
   b->n_fixed.assign(n, 0);
   b->n_h1.assign(n, 0);
   b->n_h2.assign(n, 0);
+  b->n_outer.assign(n, 0);
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   int rc = kOk;
   cudaError_t e = cudaEventRecord(b->ev[0], b->stream);
@@ -115,7 +116,7 @@ int graph_record(asam_batch* b, const std::vector<double*>& dc, const double* dt
     asam_ctx* h = b->members[m];
     e = cudaStreamWaitEvent(h->L.stream, b->ev[0], 0);  // the member's stream joins the capture
     for (int st = 0; st < nsteps && rc == kOk && e == cudaSuccess; ++st) {
-      rc = step_record(h, dc[m], dt[m], &b->n_fixed[m], &b->n_h1[m], &b->n_h2[m]);
+      rc = step_record(h, dc[m], dt[m], &b->n_fixed[m], &b->n_h1[m], &b->n_h2[m], &b->n_outer[m]);
       if (rc == kOk)
         e = cudaMemcpyAsync(b->hist[m] + (size_t)st * 4, h->stage_sc, 4 * sizeof(KrylovScalars),
                             cudaMemcpyDeviceToDevice, h->L.stream);
@@ -174,7 +175,7 @@ int graph_run(asam_batch* b, double* const* states, const double* dt, int nsteps
       double rs[4] = {0, 0, 0, 0};
       long long r = 0;
       const int st1 = step_outputs(h, b->hist_host + ((size_t)m * nsteps + st) * 4, b->n_fixed[m], b->n_h1[m],
-                                   b->n_h2[m], it, rs, &r);
+                                   b->n_h2[m], b->n_outer[m], it, rs, &r);
       ran += r;
       if (st1 != kOk && st_m == kOk) st_m = st1;
       for (int q = 0; q < 4; ++q) {
@@ -208,9 +209,9 @@ int asam_batch_set_graph(asam_batch* b, int on) {
     return kOk;
   }
   for (asam_ctx* h : b->members)
-    if (h->cfg.precision != ASAM_PREC_FP64 || h->L.stream == nullptr || h->device != b->members[0]->device) {
-      set_last_error("asam_batch_set_graph: every member must be an FP64 context with its own stream on one device",
-                     __FILE__, __LINE__);
+    if (h->L.stream == nullptr || h->device != b->members[0]->device) {
+      set_last_error("asam_batch_set_graph: every member must have its own stream, all on one device", __FILE__,
+                     __LINE__);
       return kBadArg;
     }
   CK(cudaSetDevice(b->members[0]->device));

@@ -373,7 +373,7 @@ static int run_half(asam_ctx* h, int prec, int q, Body&& body) {
 
 // x-line factors of the current stage matrix for the FP32 inner line solve
 // (outside any captured half-iteration: they change with the matrix only)
-static void prepare_inner(asam_ctx* h) {
+void prepare_inner(asam_ctx* h) {
   if (h->cfg.inner_precond == 2 && !h->xline_ready) {
     launch_xline_factor(h->L, h->d, h->val32, h->xl_w, h->xl_r);
     h->xline_ready = true;
@@ -563,7 +563,7 @@ int solve_dev(asam_ctx* h, double* x, const double* b, int* maxiter, double* tol
 
 // Ros3MetC + StageRos, transport part (ADVECT/Int_Mod.f90:263-374, 1059-1122).
 int ros_step_dev(asam_ctx* h, double* c, double dt, int* iters, double* resid) {
-  if (h->step_graphs && h->cfg.precision == ASAM_PREC_FP64 && h->L.stream != nullptr)
+  if (h->step_graphs && h->L.stream != nullptr)
     return ros_step_graph(h, c, dt, iters, resid);  // the whole step as one device-driven graph
   const Launch& L = h->L;
   const Dims& d = h->d;
@@ -819,6 +819,7 @@ int asam_destroy(asam_ctx* h) {
   for (auto st : h->cap_stream)
     if (st) cudaStreamDestroy(st);
   if (h->stage_sc) cudaFree(h->stage_sc);
+  if (h->ref_sc) cudaFree(h->ref_sc);
   if (h->stage_sc_host) cudaFreeHost(h->stage_sc_host);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;

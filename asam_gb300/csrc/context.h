@@ -84,9 +84,10 @@ struct asam_ctx {
   cudaGraphExec_t step_exec = nullptr;
   const double* step_c = nullptr;  // state, step and tolerance the graph was captured for
   double step_dt = 0.0, step_tol = 0.0;
-  long long step_n_fixed = 0, step_n_h1 = 0, step_n_h2 = 0;  // kernels outside / per pass of the loops
-  cudaStream_t cap_stream[2] = {nullptr, nullptr};  // capture streams of the loop bodies
+  long long step_n_fixed = 0, step_n_h1 = 0, step_n_h2 = 0, step_n_outer = 0;  // kernels outside / per pass of the loops
+  cudaStream_t cap_stream[3] = {nullptr, nullptr, nullptr};  // capture streams of the loop bodies
   KrylovScalars* stage_sc = nullptr;                // scalars of each stage's solve (4)
+  KrylovScalars* ref_sc = nullptr;                  // outer scalars of a device-driven refined solve
   KrylovScalars* stage_sc_host = nullptr;
   // x-line factors of the FP32 inner line solve (w and 1/den per cell), valid
   // for the current stage matrix while xline_ready is set
@@ -144,9 +145,11 @@ void graphs_reset(asam_ctx* h);
 int ros_step_graph(asam_ctx* h, double* c, double dt, int* iters, double* resid);
 void step_graph_free(asam_ctx* h);
 int step_graph_prepare(asam_ctx* h);
-int step_record(asam_ctx* h, double* c, double dt, long long* n_fixed, long long* n_h1, long long* n_h2);
+void prepare_inner(asam_ctx* h);
+int step_record(asam_ctx* h, double* c, double dt, long long* n_fixed, long long* n_h1, long long* n_h2,
+                long long* n_outer);
 int step_outputs(const asam_ctx* h, const KrylovScalars* ks, long long n_fixed, long long n_h1, long long n_h2,
-                 int* iters, double* resid, long long* ran);
+                 long long n_outer, int* iters, double* resid, long long* ran);
 long long thread_launches();
 void proj_free(asam_ctx* h);
 // device arrays of the projection's grid (valid after asam_proj_setup)

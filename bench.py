@@ -95,6 +95,7 @@ def parse():
     p.add_argument("--accuracy-steps", type=int, default=5)
     p.add_argument("--tight-tol", type=float, default=1e-13, help="Krylov tolerance of the tight runs")
     p.add_argument("--no-tight", action="store_true", help="accuracy study without the tight-tolerance runs")
+    p.add_argument("--batch-only", action="store_true", help="only the ensemble section; prints its JSON object")
     p.add_argument("--no-column", action="store_true", help="skip the column-solve line")
     p.add_argument("--column-only", action="store_true", help="only the column-solve line; prints its JSON object")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -541,7 +542,9 @@ def batch_members(n, seed=4):
 
 def batch_bench(a, torch, members):
     """Batched ensemble: all members advanced batch_steps RosRK3 steps (dt=2 s)
-    in one asam_batch_ros_step call, device-resident states; FP64 and refined."""
+    in one asam_batch_ros_step call, device-resident states; FP64 and refined,
+    each with host threads driving the members and as one graph launch of
+    the whole run (`one_graph`)."""
     import asam_gb300
 
     cells = sum(g.grid.nx * g.grid.ny * g.grid.nz for g, _, _ in members)
@@ -575,22 +578,21 @@ def batch_bench(a, torch, members):
             its, status = batch.ros_step(ptrs, 2.0, nsteps=a.batch_steps)
             torch.cuda.synchronize()
             wall = time.perf_counter() - t0
-            if prec == "fp64":
-                # the whole run of every member as one graph launch: recorded by
-                # a first call of the same length, replayed by the timed one
-                batch.set_graph(True)
-                t0 = time.perf_counter()
-                batch.ros_step(ptrs, 2.0, nsteps=a.batch_steps)
-                torch.cuda.synchronize()
-                t_rec = time.perf_counter() - t0
-                t0 = time.perf_counter()
-                _, gstatus = batch.ros_step(ptrs, 2.0, nsteps=a.batch_steps)
-                torch.cuda.synchronize()
-                gwall = time.perf_counter() - t0
-                batch.set_graph(False)
-                graph = {"value": cells * a.batch_steps / gwall / 1e6, "unit": METRIC, "seconds": gwall,
-                         "launches_per_call": 1, "record_and_first_run_seconds": t_rec,
-                         "members_not_ok": int((gstatus != 0).sum())}
+            # the whole run of every member as one graph launch: recorded by a
+            # first call of the same length, replayed by the timed one
+            batch.set_graph(True)
+            t0 = time.perf_counter()
+            batch.ros_step(ptrs, 2.0, nsteps=a.batch_steps)
+            torch.cuda.synchronize()
+            t_rec = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            _, gstatus = batch.ros_step(ptrs, 2.0, nsteps=a.batch_steps)
+            torch.cuda.synchronize()
+            gwall = time.perf_counter() - t0
+            batch.set_graph(False)
+            graph = {"value": cells * a.batch_steps / gwall / 1e6, "unit": METRIC, "seconds": gwall,
+                     "launches_per_call": 1, "record_and_first_run_seconds": t_rec,
+                     "members_not_ok": int((gstatus != 0).sum())}
         for b in blocks:
             b.close()
         del dev
@@ -960,7 +962,8 @@ def main():
         pk = ROOT / "MEASURED_PEAKS.json"
         return json.loads(pk.read_text()) if pk.exists() else {}
 
-    if a.restart_only or a.diffusion_only or a.transport_only or a.probe or a.accuracy or a.column_only:
+    if (a.restart_only or a.diffusion_only or a.transport_only or a.probe or a.accuracy or a.column_only
+            or a.batch_only):
         import ctypes as C
 
         import torch
@@ -972,6 +975,8 @@ def main():
         torch.cuda.set_stream(stream)
         if a.restart_only:
             print(json.dumps(restart_bench(a, torch)), flush=True)
+        elif a.batch_only:
+            print(json.dumps(batch_bench(a, torch, batch_members(a.batch_members))), flush=True)
         elif a.column_only:
             print(json.dumps(column_bench(a, torch, stream, peaks().get("hbm_gbs", 6800.0))), flush=True)
         elif a.accuracy:

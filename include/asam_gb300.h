@@ -91,10 +91,12 @@ int asam_destroy(asam_ctx *ctx);
  *   0 every kernel launched individually, the host takes the exit decisions;
  *   1 (default) the BiCGStab half-iterations are captured as CUDA graphs and
  *     replayed, the host takes the exit decisions;
- *   2 FP64 contexts: the whole Rosenbrock step is one CUDA graph in which each
- *     BiCGStab loop is a graph WHILE node driven by a condition kernel
- *     (bounded by MaxIter), so a step is one launch and one host read;
- *     refined contexts behave as 1. */
+ *   2 the whole Rosenbrock step is one CUDA graph in which each BiCGStab
+ *     loop is a graph WHILE node driven by a condition kernel (bounded by
+ *     MaxIter), so a step is one launch and one host read; in a refined
+ *     context the FP64 refinement is an outer WHILE node (bounded by 8
+ *     passes) around the FP32 BiCGStab's loop.  Transport steps
+ *     (asam_ros_step); the dynamical step keeps mode 1. */
 int asam_set_graphs(asam_ctx *ctx, int on);
 
 /* Run the context's work on this CUDA stream (cudaStream_t); NULL = the legacy
@@ -480,7 +482,7 @@ int asam_batch_destroy(asam_batch *batch);
 int asam_batch_ros_step(asam_batch *batch, double *const *states, const double *dt, int nsteps, int *iters,
                         double *resid, int *status);
 /* One-graph mode (on = 1; 0 returns to the host threads): every member must
- * be an FP64 context with its own stream.  asam_batch_ros_step then records
+ * have its own stream (FP64 or refined).  asam_batch_ros_step then records
  * the whole call -- nsteps device-driven steps of every member, the BiCGStab
  * loops as graph WHILE/IF nodes with their exit decisions on the device --
  * into one CUDA graph with one branch per member, launches it once and reads

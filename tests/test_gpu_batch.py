@@ -53,13 +53,15 @@ def test_batch_matches_members_alone(asam, precision, nthreads):
         assert [list(map(int, s)) for s in its[m]] == its_ref, MEMBERS[m]
 
 
-def test_batch_graph_matches_members_alone(asam):
-    """One-graph mode: the whole 3-step run of every FP64 member as one CUDA
-    graph launch gives bitwise the states and iteration counts of each member
-    run alone; a second call replays the graph; refined members are refused."""
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
+def test_batch_graph_matches_members_alone(asam, precision):
+    """One-graph mode: the whole 3-step run of every member as one CUDA graph
+    launch (refined members: the FP64 refinement and the FP32 BiCGStab as
+    nested WHILE nodes) gives bitwise the states and iteration counts of each
+    member run alone; a second call replays the graph."""
     import torch
 
-    kw = dict(bicgstab_tol=1e-10)
+    kw = dict(bicgstab_tol=1e-10, precision=precision)
     dts = [2.0, 3.0, 1.5, 2.5, 2.0, 4.0]
     alone = []
     for (b, st), dt in zip(_blocks(asam, **kw), dts):
@@ -85,12 +87,6 @@ def test_batch_graph_matches_members_alone(asam):
         assert np.array_equal(got, c_ref), MEMBERS[m]
         its = [list(map(int, s)) for s in its1[m]] + [list(map(int, s)) for s in its2[m]]
         assert its == its_ref, MEMBERS[m]
-    refined = _blocks(asam, bicgstab_tol=1e-10, precision="fp32_refined")
-    with asam.Batch([b for b, _ in refined]) as batch:
-        with pytest.raises(asam.AsamError):
-            batch.set_graph(True)
-    for b, _ in refined:
-        b.close()
     assert np.array_equal(host0, members[0][1].c)
 
 

@@ -244,18 +244,21 @@ def test_inner_line_psolve_fp32(env, name, precond, axis):
     assert max(errs) <= 2e-5, errs
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
+@pytest.mark.parametrize("precision,inner", [("fp64", "gauss_seidel"), ("fp32_refined", "xline"),
+                                             ("fp32_refined", "gauss_seidel")])
 @pytest.mark.parametrize("name", ["hill_24x20x16", "flat_walls_9x6x5"])
-def test_graph_captured_iterations_identical(env, name, precision):
-    """BiCGStab half-iterations replayed from CUDA graphs, and (FP64) whole steps
-    run as one graph whose Krylov loops are WHILE nodes, give the bits and the
+def test_graph_captured_iterations_identical(env, name, precision, inner):
+    """BiCGStab half-iterations replayed from CUDA graphs, and whole steps run
+    as one graph whose Krylov loops are WHILE nodes (refined: the FP64
+    refinement as an outer WHILE around the FP32 BiCGStab's loop; with the
+    persistent Gauss-Seidel inner preconditioner too), give the bits and the
     iteration counts of the individually launched kernels, over several steps."""
     geo, vel, st = cases.get(name)
     out = {}
-    for mode in (1, 0, 2):  # 2: the whole FP64 step as one graph with WHILE/IF nodes
+    for mode in (1, 0, 2):  # 2: the whole step as one graph with WHILE/IF nodes
         c = st.c.copy()
         with _block(env, name, method="RosRK3", bicgstab_tol=1e-12, precision=precision,
-                    inner_precond="xline" if precision == "fp32_refined" else "gauss_seidel") as blk:
+                    inner_precond=inner) as blk:
             blk.set_graphs(mode)
             its = [blk.Ros3MetC(c, 3.0)[0] for _ in range(4)]
         out[mode] = (c, its)
