@@ -140,6 +140,12 @@ __global__ void k_ref_check(cudaGraphConditionalHandle hnd, KrylovScalars* so, c
   cudaGraphSetConditional(hnd, (so->done == 0 && pass < kMaxOuter) ? 1u : 0u);
 }
 
+// enter a WHILE loop: its handle's default is applied once per graph launch
+// only, and a loop nested in another runs once per outer pass
+__global__ void k_cond_enter(cudaGraphConditionalHandle hnd) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(hnd, 1u);
+}
+
 __global__ void k_cond_running(cudaGraphConditionalHandle hnd, const KrylovScalars* sc) {
   if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(hnd, sc->done == 0 ? 1u : 0u);
 }
@@ -235,7 +241,10 @@ int record_bicgstab(asam_ctx* h, const T* val, T* x, const T* b, Work<T>& w, Bod
   // WHILE: one iteration per pass; the host-driven solver always enters it
   cudaGraphConditionalHandle wh, ih;
   int rc;
-  if ((rc = make_handle(s0, 1u, &wh)) || (rc = begin_conditional(s0, s1, cudaGraphCondTypeWhile, wh))) return rc;
+  if ((rc = make_handle(s0, 1u, &wh))) return rc;
+  k_cond_enter<<<1, 1, 0, s0>>>(wh);
+  count_launches(1);
+  if ((rc = begin_conditional(s0, s1, cudaGraphCondTypeWhile, wh))) return rc;
   h->L.stream = s1;
   const long long n1 = thread_launches();
   launch_dot(h->L, d, nc, w.rt, w.r, h->partial, h->sc, OP_RHO, nullptr);
