@@ -112,7 +112,10 @@ int graph_record(asam_batch* b, const std::vector<double*>& dc, const double* dt
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   int rc = kOk;
   cudaError_t e = cudaEventRecord(b->ev[0], b->stream);
-  for (int m = 0; m < n && rc == kOk && e == cudaSuccess; ++m) {
+  // branches in decreasing member size, the order the host threads take them:
+  // the longest chains start first
+  for (int q = 0; q < n && rc == kOk && e == cudaSuccess; ++q) {
+    const int m = b->order[q];
     asam_ctx* h = b->members[m];
     e = cudaStreamWaitEvent(h->L.stream, b->ev[0], 0);  // the member's stream joins the capture
     for (int st = 0; st < nsteps && rc == kOk && e == cudaSuccess; ++st) {

@@ -1816,6 +1816,41 @@ __global__ void k_xupdate(size_t len, const asam::KrylovScalars* sc, int with_om
   }
 }
 
+// The device-driven BiCGStab's updates (graph WHILE loop): p = r on the
+// first iteration, else beta = (rho/rho_old)*(alpha/omega) and
+// p = beta*(p - omega*v) + r -- the operations of k_beta + k_pupdate, in the
+// same expressions, compiled in the same translation unit per precision, so
+// the rounding (and any contraction) is theirs; and the half-step exit's
+// x += alpha*ph when the first half converged (k_xupdate's first term).
+template <typename T>
+__global__ void k_pupdate_auto(size_t len, const asam::KrylovScalars* sc, const T* __restrict__ r,
+                               const T* __restrict__ v, T* __restrict__ p) {
+  const bool first = sc->iter == 0;
+  const T be = (T)((sc->rho / sc->rho_old) * (sc->alpha / sc->omega));
+  const T mo = (T)(-sc->omega);
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x) {
+    if (first) {
+      p[q] = r[q];
+    } else {
+      T pp = p[q];
+      if (mo != (T)0) pp = mo * v[q] + pp;
+      p[q] = be * pp + r[q];
+    }
+  }
+}
+template <typename T>
+__global__ void k_xupdate_half(size_t len, const asam::KrylovScalars* sc, const T* __restrict__ ph,
+                               T* __restrict__ x) {
+  if (sc->done != 1) return;
+  const T al = (T)sc->alpha;
+  if (al == (T)0) return;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x) {
+    T xx = x[q];
+    xx = al * ph[q] + xx;
+    x[q] = xx;
+  }
+}
+
 // y = a*x + y with a host coefficient (skipped when a == 0)
 template <typename T>
 __global__ void k_axpy_host(size_t len, T a, const T* __restrict__ x, T* __restrict__ y) {

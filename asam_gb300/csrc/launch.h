@@ -48,6 +48,8 @@ struct Launch {
   void launch_axpy_dot(const Launch&, const Dims&, int ncomp, KrylovScalars* sc, int sel, double sign,          \
                        const T* x, T* y, double* partial, int op);                                               \
   void launch_pupdate(const Launch&, size_t len, const KrylovScalars* sc, const T* r, const T* v, T* p);         \
+  void launch_pupdate_auto(const Launch&, size_t len, const KrylovScalars* sc, const T* r, const T* v, T* p);    \
+  void launch_xupdate_half(const Launch&, size_t len, const KrylovScalars* sc, const T* ph, T* x);              \
   void launch_xupdate(const Launch&, size_t len, const KrylovScalars* sc, int with_omega, const T* ph,          \
                       const T* rh, T* x);                                                                        \
   void launch_axpy_host(const Launch&, size_t len, T a, const T* x, T* y);                                      \

@@ -185,6 +185,12 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
     k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, RED_GRID, sc, op, nullptr);                                \
     count_launches(2);                                                                                             \
   }                                                                                                                \
+  void launch_pupdate_auto(const Launch& L, size_t len, const KrylovScalars* sc, const T* r, const T* v, T* p) {    \
+    k_pupdate_auto<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, sc, r, v, p); count_launches(1);              \
+  }                                                                                                                \
+  void launch_xupdate_half(const Launch& L, size_t len, const KrylovScalars* sc, const T* ph, T* x) {              \
+    k_xupdate_half<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, sc, ph, x); count_launches(1);                \
+  }                                                                                                                \
   void launch_pupdate(const Launch& L, size_t len, const KrylovScalars* sc, const T* r, const T* v, T* p) {         \
     k_pupdate<T><<<gs_grid(L, len), kBlock, 0, L.stream>>>(len, sc, r, v, p); count_launches(1);                                      \
   }                                                                                                                \

@@ -28,33 +28,6 @@ __global__ void k_ks_init(KrylovScalars* sc, double tol, int maxiter) {
 
 // p = r on the first iteration, else beta = (rho/rho_old)*(alpha/omega) and
 // p = beta*(p - omega*v) + r (the operations of k_beta + k_pupdate)
-template <typename T>
-__global__ void k_pupdate_auto(size_t len, KrylovScalars* sc, const T* __restrict__ r, const T* __restrict__ v,
-                               T* __restrict__ p) {
-  const bool first = sc->iter == 0;
-  const T be = (T)((sc->rho / sc->rho_old) * (sc->alpha / sc->omega));
-  const T mo = (T)(-sc->omega);
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x) {
-    if (first) {
-      p[q] = r[q];
-    } else {
-      T pp = p[q];
-      if (mo != (T)0) pp = mo * v[q] + pp;
-      p[q] = be * pp + r[q];
-    }
-  }
-}
-
-// the half-step exit's update x += alpha*ph, when the first half converged
-template <typename T>
-__global__ void k_xupdate_half(size_t len, const KrylovScalars* sc, const T* __restrict__ ph, T* __restrict__ x) {
-  if (sc->done != 1) return;
-  const T al = (T)sc->alpha;
-  if (al == (T)0) return;
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < len; q += (size_t)gridDim.x * blockDim.x)
-    x[q] = al * ph[q] + x[q];
-}
-
 // ---- the refined solve's outer FP64 refinement (bicgstab_refined, capi.cu)
 // as device kernels with the host driver's arithmetic: outer scalars in `so`
 // (rnorm0, rnorm, tol = the target |r0|*Tol, iter = outer passes, out_*),
@@ -248,13 +221,11 @@ int record_bicgstab(asam_ctx* h, const T* val, T* x, const T* b, Work<T>& w, Bod
   h->L.stream = s1;
   const long long n1 = thread_launches();
   launch_dot(h->L, d, nc, w.rt, w.r, h->partial, h->sc, OP_RHO, nullptr);
-  k_pupdate_auto<T><<<grid_of(h->L, len), kB, 0, s1>>>(len, h->sc, w.r, w.v, w.p);
-  count_launches(1);
+  launch_pupdate_auto(h->L, len, h->sc, w.r, w.v, w.p);
   psolve_dev<T>(h, val, w.p, w.ph, w);
   launch_matvec_dot(h->L, d, nc, val, w.ph, w.v, w.rt, h->partial, h->sc, OP_ALPHA);
   launch_axpy_dot(h->L, d, nc, h->sc, SEL_ALPHA, -1.0, w.v, w.r, h->partial, OP_RNORM_HALF);
-  k_xupdate_half<T><<<grid_of(h->L, len), kB, 0, s1>>>(len, h->sc, w.ph, x);
-  count_launches(1);
+  launch_xupdate_half(h->L, len, h->sc, w.ph, x);
   // IF nothing ended the solve: the second half
   if ((rc = make_handle(s1, 0u, &ih))) return rc;
   k_cond_running<<<1, 1, 0, s1>>>(ih, h->sc);
