@@ -238,3 +238,24 @@ def test_config5_adjoint_full_size(built_lib):
         # their agreement with the exact derivative
         assert rel_c.max() <= 2e-3 and np.median(rel_c) <= 1e-4, rel_c
         assert rel_w.max() <= 2e-3 and np.median(rel_w) <= 1e-4, rel_w
+
+
+def test_config2_256_transport_50_steps(built_lib):
+    """Configuration 2's full run on the GPU (256x256x128, 50 transport steps,
+    dt = 2 s, BiCGStab 1e-10), beyond what the oracle finishes in a test: every
+    solve converges, every field stays finite, and the total mass of Rho and of
+    the tracer (TotalScalar) is conserved to round-off over the whole run."""
+    geo, vel, st = G.hill_case(256, 256, 128, seed=2)
+    c = st.c.copy()
+    with TransportBlock(geo, ncomp=c.shape[0], method="RosRK3", bicgstab_tol=1e-10, bicgstab_maxiter=30) as blk:
+        blk.set_velocity(*vel)
+        comps = [0, c.shape[0] - 1]
+        m0 = [blk.TotalScalar(c, q) for q in comps]
+        for step in range(50):
+            its, res = blk.Ros3MetC(c, 2.0)
+            # MaxIter sentinels: -Iter (half step) or Iter <= 30 converged; 2*Iter = 60 not
+            assert all(abs(i) <= 30 for i in its), (step, its, res)
+        m1 = [blk.TotalScalar(c, q) for q in comps]
+    assert np.isfinite(c).all()
+    for a, b in zip(m0, m1):
+        assert abs(b - a) <= 1e-12 * abs(a), (a, b)
