@@ -141,6 +141,28 @@ __device__ inline int line_of(int pos, int h, int c2) {
   return j < c2 ? j : -1;
 }
 
+// Visits the slots s = 0 .. ps-1 of one plane (rows of w slots) with the
+// block's threads in stride order, passing the row i and the position r in
+// the row, which are tracked by increments: one integer division per call
+// instead of one per slot (a division by a run-time value costs some twenty
+// instructions on the GPU).
+template <typename F>
+__device__ __forceinline__ void for_plane(int w, size_t ps, F&& f) {
+  const int bd = blockDim.x;
+  int i = (int)threadIdx.x / w;
+  int r = (int)threadIdx.x - i * w;
+  const int di = bd / w, dr = bd - di * w;
+  for (size_t s = threadIdx.x; s < ps; s += bd) {
+    f(s, i, r);
+    i += di;
+    r += dr;
+    if (r >= w) {
+      r -= w;
+      ++i;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Assembly
 // ---------------------------------------------------------------------------
@@ -475,7 +497,8 @@ __global__ void k_factor(Lev2 P) {
 // MatVecT_2D at entry (i,j) of a plane (TriDiagT_Mod.f90:113-133, 405-431);
 // x is the plane's vector, mo the plane's offset in the matrix arrays
 template <typename T, bool kWrap = false>
-__device__ inline T matvec2_at(const Lev2T<T>& P, size_t mo, const T* __restrict__ x, size_t s, int i, int j) {
+__device__ inline T matvec2_at(const Lev2T<T>& P, size_t mo, const T* __restrict__ x, size_t s, int i, int j,
+                               int k) {
   const int c1 = P.c1, c2 = P.c2, w = P.w;
   const T* d = P.d + mo;
   const T* uz = P.uz + mo;
@@ -506,10 +529,10 @@ __device__ inline T matvec2_at(const Lev2T<T>& P, size_t mo, const T* __restrict
       y = y + lx[sl] * x[sl];
     }
   }
-  if (kWrap && P.wxl) {  // periodic-Laplacian hierarchy: the coupling across the periodic x side
-    const size_t k = mo / P.ps, row = (size_t)i * w;
-    if (j == 0) y = y + P.wxl[k * c1 + i] * x[row + slot(0, P.h, 0, c2 - 1)];
-    if (j == c2 - 1) y = y + P.wxh[k * c1 + i] * x[row];
+  if (kWrap && P.wxl && (j == 0 || j == c2 - 1)) {  // periodic-Laplacian hierarchy: across the periodic x side
+    const size_t row = (size_t)i * w, kc = (size_t)k * c1;
+    if (j == 0) y = y + P.wxl[kc + i] * x[row + slot(0, P.h, 0, c2 - 1)];
+    if (j == c2 - 1) y = y + P.wxh[kc + i] * x[row];
   }
   return y;
 }
@@ -672,24 +695,23 @@ __device__ void mg2d(const Lev3T<T>& A, int k, T* x0, const T* b0, int gi2, T* r
     if (lv + 1 < nl) {
       T* res = P.res + (size_t)k * P.ps;
       const size_t np = P.ps;
-      for (size_t s = threadIdx.x; s < np; s += blockDim.x) {
-        const int i = (int)(s / P.w), j = line_of((int)(s % P.w), P.h, P.c2);
-        if (j < 0) continue;
-        res[s] = b[s] - matvec2_at<T, kWrap>(P, mo, x, s, i, j);
-      }
+      for_plane(P.w, np, [&](size_t s, int i, int r) {
+        const int j = line_of(r, P.h, P.c2);
+        if (j >= 0) res[s] = b[s] - matvec2_at<T, kWrap>(P, mo, x, s, i, j, k);
+      });
       __syncthreads();
       const Lev2T<T>& Q = A.pl[lv + 1];
       T* bq = Q.b + (size_t)k * Q.ps;
       T* xq = Q.x + (size_t)k * Q.ps;
-      for (size_t s = threadIdx.x; s < Q.ps; s += blockDim.x) {
-        const int a = (int)(s / Q.w), bb = line_of((int)(s % Q.w), Q.h, Q.c2);
-        if (bb < 0) continue;
+      for_plane(Q.w, Q.ps, [&](size_t s, int a, int r) {
+        const int bb = line_of(r, Q.h, Q.c2);
+        if (bb < 0) return;
         T v = (T)0;
         for (int i1 = 2 * a; i1 <= 2 * a + 1 && i1 < P.c1; ++i1)
           for (int i2 = 2 * bb; i2 <= 2 * bb + 1 && i2 < P.c2; ++i2) v = v + res[slot(P.w, P.h, i1, i2)];
         bq[s] = v;
         xq[s] = (T)0;
-      }
+      });
       __syncthreads();
       ++lv;
     } else {
@@ -706,11 +728,10 @@ __device__ void mg2d(const Lev3T<T>& A, int k, T* x0, const T* b0, int gi2, T* r
     if (lv > 0) {
       const Lev2T<T>& F = A.pl[lv - 1];
       T* xf = lv - 1 == 0 ? x0 : F.x + (size_t)k * F.ps;
-      for (size_t s = threadIdx.x; s < F.ps; s += blockDim.x) {
-        const int i = (int)(s / F.w), j = line_of((int)(s % F.w), F.h, F.c2);
-        if (j < 0) continue;
-        xf[s] = xf[s] + x[slot(P.w, P.h, i >> 1, j >> 1)];
-      }
+      for_plane(F.w, F.ps, [&](size_t s, int i, int r) {
+        const int j = line_of(r, F.h, F.c2);
+        if (j >= 0) xf[s] = xf[s] + x[slot(P.w, P.h, i >> 1, j >> 1)];
+      });
       __syncthreads();
       --lv;
     } else {
@@ -735,8 +756,8 @@ __global__ void __launch_bounds__(kPlaneBlock, 2) k_plane_half(const Lev3T<T>* _
     const int k = 2 * q + color;
     if (k >= A.m3) break;
     const size_t off = (size_t)k * P0.ps, ps = P0.ps;
-    for (size_t s = threadIdx.x; s < ps; s += blockDim.x) {
-      if (line_of((int)(s % P0.w), P0.h, P0.c2) < 0) continue;
+    for_plane(P0.w, ps, [&](size_t s, int, int r) {
+      if (line_of(r, P0.h, P0.c2) < 0) return;
       const size_t e = off + s;
       T v = A.b[e];
       if (fwd) {
@@ -753,7 +774,7 @@ __global__ void __launch_bounds__(kPlaneBlock, 2) k_plane_half(const Lev3T<T>* _
         if (k == A.m3 - 1) v = v - A.wyh[s] * A.x[s];
       }
       A.t[e] = v;
-    }
+    });
     __syncthreads();
     for (int it = 0; it < mult_iter2; ++it) mg2d<T, kWrap>(A, k, A.x + off, A.t + off, gi2, ring);
     __syncthreads();
@@ -773,7 +794,7 @@ __global__ void k_matvec3(const Lev3T<T>* __restrict__ lvs, int L, const T* __re
     const int k = (int)(e / ps);
     const int i = (int)(s / P.w), j = line_of((int)(s % P.w), P.h, P.c2);
     if (j < 0) continue;
-    T v = matvec2_at<T, kWrap>(P, (size_t)k * ps, x + (size_t)k * ps, s, i, j);
+    T v = matvec2_at<T, kWrap>(P, (size_t)k * ps, x + (size_t)k * ps, s, i, j, k);
     if (A.m3 > 1) {
       if (k == 0)
         v = v + A.u3[e] * x[e + ps];
