@@ -364,6 +364,12 @@ class TransportBlock:
         code = {None: -1, "psolve1": 0, "periodic": 1}[kind]
         check(self.lib.asam_proj_set_preconditioner(self.h, code), "asam_proj_set_preconditioner")
 
+    def proj_set_pre_schedule(self, gauss_iter2: int = 0, gauss_iter3: int = 0):
+        """Sweep growth per level (GaussIter2, GaussIter3) of the periodic
+        preconditioner's V-cycle; 0, 0 (the default) smooths every level once."""
+        check(self.lib.asam_proj_set_pre_schedule(self.h, int(gauss_iter2), int(gauss_iter3)),
+              "asam_proj_set_pre_schedule")
+
     def proj_weights(self, dtu, dtv, dtw, duu, duv, duw, dut, dtt):
         """Sound weights (WeightDiagCompute): face arrays with uF/vF/wF extents,
         DUT and DTT interior (nz, ny, nx)."""

@@ -1434,6 +1434,12 @@ struct ProjState {
   // V-cycle on the Laplacian with the couplings across the periodic sides):
   // -1 follow the precision (refined contexts), 0 PSolve1, 1 periodic
   int pre_kind = -1;
+  // smoothing schedule of the periodic preconditioner's V-cycle (GaussIter2,
+  // GaussIter3 of its hierarchy): one sweep per level by default -- the
+  // reference's growth of the sweeps with the level buys no FGMRES step
+  // there (9/9/8 steps per stage either way at 512x512x128) and costs a fifth
+  // of the refined step
+  int pre_gi2 = 0, pre_gi3 = 0;
   std::vector<Lev3> lvP;
   Lev3* d_lvP = nullptr;
   std::vector<prj::Lev3T<float>> lvP32;
@@ -1617,11 +1623,10 @@ int proj_build(asam_ctx* h) {
 // Solve_3D from a zero start on level 0 (VCycleCG's MatrixT branch): lv[0].b
 // holds the right-hand side, the result is left in lv[0].x
 template <typename T, bool kWrap = false>
-void vcycle_run(asam_ctx* h, std::vector<Lev3T<T>>& lv, Lev3T<T>* d_lv) {
+void vcycle_run(asam_ctx* h, std::vector<Lev3T<T>>& lv, Lev3T<T>* d_lv, int gi2, int gi3) {
   ProjState* s = h->proj;
   const cudaStream_t st = h->L.stream;
   const int R = s->R;
-  const int gi2 = s->cfg.gauss_iter2, gi3 = s->cfg.gauss_iter3;
   const int mi2 = s->cfg.mult_iter2;
   const size_t ring = (size_t)RingCfg<T>::ring * kFields * kPlaneBlock * sizeof(T);
   long long nl = 0;
@@ -1909,11 +1914,11 @@ void vcycle_any(asam_ctx* h, const double* b, double sign, double* x, int which 
   if (use_mg32(h) && s->lv32_ready && (which != kHierPeriodic || s->lvP32_ready)) {
     k_cvt_to_f32<<<grid_of(n), 256, 0, st>>>(b, s->lv32[0].b, n, sign);
     if (which == kHierDirichlet)
-      vcycle_run<float>(h, s->lvD32, s->d_lvD32);
+      vcycle_run<float>(h, s->lvD32, s->d_lvD32, s->cfg.gauss_iter2, s->cfg.gauss_iter3);
     else if (which == kHierPeriodic)
-      vcycle_run<float, true>(h, s->lvP32, s->d_lvP32);
+      vcycle_run<float, true>(h, s->lvP32, s->d_lvP32, s->pre_gi2, s->pre_gi3);
     else
-      vcycle_run<float>(h, s->lv32, s->d_lv32);
+      vcycle_run<float>(h, s->lv32, s->d_lv32, s->cfg.gauss_iter2, s->cfg.gauss_iter3);
     k_cvt_to_f64<<<grid_of(n), 256, 0, st>>>(s->lv32[0].x, x, n);
     count_launches(2);
     return;
@@ -1925,11 +1930,11 @@ void vcycle_any(asam_ctx* h, const double* b, double sign, double* x, int which 
     count_launches(1);
   }
   if (which == kHierDirichlet)
-    vcycle_run<double>(h, s->lvD, s->d_lvD);
+    vcycle_run<double>(h, s->lvD, s->d_lvD, s->cfg.gauss_iter2, s->cfg.gauss_iter3);
   else if (which == kHierPeriodic)
-    vcycle_run<double, true>(h, s->lvP, s->d_lvP);
+    vcycle_run<double, true>(h, s->lvP, s->d_lvP, s->pre_gi2, s->pre_gi3);
   else
-    vcycle_run<double>(h, s->lv, s->d_lv);
+    vcycle_run<double>(h, s->lv, s->d_lv, s->cfg.gauss_iter2, s->cfg.gauss_iter3);
   if (x != s->lv[0].x) cudaMemcpyAsync(x, s->lv[0].x, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
 }
 
@@ -2385,6 +2390,13 @@ int asam_lapl_compute(asam_ctx* h, double beta0, double dtp) {
   int rc = check_launch();
   if (!rc) s->assembled = true;
   return rc;
+}
+
+int asam_proj_set_pre_schedule(asam_ctx* h, int gauss_iter2, int gauss_iter3) {
+  if (!h || !h->proj || gauss_iter2 < 0 || gauss_iter3 < 0) return kBadArg;
+  h->proj->pre_gi2 = gauss_iter2;
+  h->proj->pre_gi3 = gauss_iter3;
+  return kOk;
 }
 
 int asam_proj_set_preconditioner(asam_ctx* h, int kind) {

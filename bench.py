@@ -89,6 +89,8 @@ def parse():
     p.add_argument("--adj-grid", default="128,128,64", help="nx,ny,nz of the adjoint-cost workload")
     p.add_argument("--adj-steps", type=int, default=40)
     p.add_argument("--adj-ckpt", type=int, default=8)
+    p.add_argument("--gauss-iter2", type=int, default=1, help="GaussIter2 of the projection multigrid")
+    p.add_argument("--gauss-iter3", type=int, default=1, help="GaussIter3 of the projection multigrid")
     p.add_argument("--accuracy", action="store_true",
                    help="only the accuracy study of the refined step (FP64 and refined at the configured and at a "
                         "tight tolerance); prints its JSON object")
@@ -658,7 +660,7 @@ def dyn_measure(a, torch, stream, prec, work, lib_mod, e2e=True, kernels=True, c
                                     precision=prec, **kw)
     blk.set_stream(stream.cuda_stream)
     blk.set_velocity(*vel)
-    blk.proj_setup(dx, dy, dz, tol=a.proj_tol, max_restart=20)
+    blk.proj_setup(dx, dy, dz, tol=a.proj_tol, max_restart=20, gauss_iter2=a.gauss_iter2, gauss_iter3=a.gauss_iter3)
     blk.dyn_setup(pos["th"], pos["mom"], rv_pos=pos["qv"], bound_cells=bc, scalars=[pos["qv"], pos["tracer"]])
     lib = blk.lib
     c = torch.from_numpy(st.c.reshape(-1).copy()).cuda()

@@ -385,6 +385,12 @@ int asam_proj_set_precision(asam_ctx *ctx, int prec);
  * else 0.  FGMRES is flexible, so the tolerance is met either way.  Takes
  * effect at the next asam_lapl_compute.  No reference counterpart. */
 int asam_proj_set_preconditioner(asam_ctx *ctx, int kind);
+/* Smoothing schedule of the periodic-Laplacian preconditioner's V-cycle:
+ * GaussIter2 and GaussIter3 of its hierarchy (the sweeps of a level grow by
+ * them from level to level; Control_Mod.f90:55 for the reference's own).
+ * Default 0, 0: one sweep on every level.  No reference counterpart; the
+ * reference's hierarchies keep asam_proj_config's values. */
+int asam_proj_set_pre_schedule(asam_ctx *ctx, int gauss_iter2, int gauss_iter3);
 /* Number of multigrid V-cycles run by this context's projection (diagnostic). */
 long long asam_proj_vcycles(asam_ctx *ctx);
 
