@@ -123,6 +123,7 @@ SIGNATURES = [
     ("asam_proj_set_precision", C.c_int, [_V, C.c_int]),
     ("asam_proj_set_preconditioner", C.c_int, [_V, C.c_int]),
     ("asam_proj_set_pre_schedule", C.c_int, [_V, C.c_int, C.c_int]),
+    ("asam_probe_fp64_chain", C.c_int, [C.c_int, C.c_int, C.c_int, _D]),
     ("asam_set_wait_limit", C.c_int, [_V, C.c_int]),
     ("asam_dyn_setup", C.c_int, [_V, C.POINTER(AsamDynConfig), _I, C.c_int, _I, C.c_int]),
     ("asam_face_to_cell", C.c_int, [_V, _V, _V, _V, _V]),

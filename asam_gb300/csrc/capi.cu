@@ -699,6 +699,21 @@ __global__ void k_probe_fp64(int iters, double seed, double* out) {
   if (s == 12345.678) out[0] = s;  // keeps the chains alive
 }
 
+// Cost of a dependent FP64 chain: the first `lanes` threads of the first
+// `warps` warps of one block each run iters dependent FMAs; the slowest
+// warp's clock64 cycles per FMA go to cyc[0].
+__global__ void k_probe_fp64_chain(int iters, int lanes, int warps, double* out, long long* cyc) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp >= warps || lane >= lanes) return;
+  double x = 1.0 + threadIdx.x * 1e-3;
+  const double m = 0.999999, c = 1e-7;
+  const long long t0 = clock64();
+  for (int i = 0; i < iters; ++i) x = __fma_rn(x, m, c);
+  const long long t1 = clock64();
+  if (x == 12345.0) out[0] = x;  // keeps the chain alive
+  if (lane == 0) atomicMax((unsigned long long*)cyc, (unsigned long long)(t1 - t0));
+}
+
 // Check of the FMA-corrected quotient (kernels.cuh div_rn) against the IEEE
 // quotient on pseudo-random operands spanning many binades.
 __device__ __forceinline__ unsigned long long splitmix(unsigned long long x) {
@@ -748,6 +763,24 @@ int asam_probe_div(long long n, long long seed, int span, long long* mismatches)
     return kCudaError;
   }
   *mismatches = (long long)h;
+  return check_launch();
+}
+
+int asam_probe_fp64_chain(int warps, int lanes, int iters, double* cycles_per_op) {
+  if (warps < 1 || warps > 32 || lanes < 1 || lanes > 32 || iters < 1 || !cycles_per_op) return kBadArg;
+  double* out;
+  long long* cyc;
+  CK(cudaMalloc((void**)&out, sizeof(double)));
+  CK(cudaMalloc((void**)&cyc, sizeof(long long)));
+  long long h = 0;
+  for (int rep = 0; rep < 2; ++rep) {  // the first launch warms up
+    CK(cudaMemset(cyc, 0, sizeof(long long)));
+    k_probe_fp64_chain<<<1, 32 * warps>>>(iters, lanes, warps, out, cyc);
+    CK(cudaMemcpy(&h, cyc, sizeof(h), cudaMemcpyDeviceToHost));
+  }
+  cudaFree(out);
+  cudaFree(cyc);
+  *cycles_per_op = (double)h / iters;
   return check_launch();
 }
 

@@ -78,11 +78,13 @@ def parse():
                    help="only the diffusion section; prints its JSON object")
     p.add_argument("--transport-only", action="store_true",
                    help="only the transport-only step (prescribed winds); prints its JSON object")
-    p.add_argument("--probe", choices=["psolve", "inner_psolve", "vcycle", "vcycle_refined", "step", "step_refined"],
+    p.add_argument("--probe", choices=["psolve", "inner_psolve", "vcycle", "vcycle_refined", "step", "step_refined",
+                                       "fp64_chain"],
                    help="for profiling: one transport PSolve call on the transport workload (psolve, "
                         "inner_psolve); one FGMRES preconditioner call on the headline block (vcycle: the FP64 "
                         "V-cycle; vcycle_refined: the refined mode's FP32 periodic-Laplacian V-cycle); or "
-                        "--warmup + --steps bare dynamical steps of the headline workload (step, step_refined)")
+                        "--warmup + --steps bare dynamical steps of the headline workload (step, step_refined); "
+                        "cycles per dependent FP64 FMA against active lanes and warps on one SM (fp64_chain)")
     p.add_argument("--batch-members", type=int, default=48)
     p.add_argument("--batch-steps", type=int, default=20)
     p.add_argument("--batch-threads", type=int, default=0, help="host threads driving the members (0: one each)")
@@ -996,6 +998,15 @@ def main():
             _lib.load().asam_probe_fp64_fma(20000, C.byref(gf))
             tb = transport_bench(a, torch, stream, peaks().get("hbm_gbs", 6800.0), gf.value / 2.0)
             print(json.dumps(tb), flush=True)
+        elif a.probe == "fp64_chain":
+            from asam_gb300 import _lib
+
+            lib, out = _lib.load(), []
+            for warps, lanes in ((1, 1), (1, 8), (1, 32), (4, 4), (4, 32), (8, 32), (16, 32), (32, 1), (32, 32)):
+                cyc = C.c_double()
+                _lib.check(lib.asam_probe_fp64_chain(warps, lanes, 20000, C.byref(cyc)), "asam_probe_fp64_chain")
+                out.append({"warps": warps, "lanes": lanes, "cycles_per_dependent_fma": cyc.value})
+            print(json.dumps({"probe": a.probe, "results": out}), flush=True)
         elif a.probe in ("vcycle", "vcycle_refined", "step", "step_refined"):
             print(json.dumps(probe_dyn(a, torch, stream)), flush=True)
         else:

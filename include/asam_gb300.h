@@ -501,6 +501,12 @@ int asam_batch_set_graph(asam_batch *batch, int on);
  * alpha/beta 4x4 row-major, gamma1[5].  Returns nStage (0 = unknown method). */
 int asam_ros_coeffs(int method, double *beta0, double *alpha, double *beta, double *gamma1);
 
+/* No reference counterpart, diagnostic: clock cycles per FMA of a dependent
+ * FP64 chain run by the first `lanes` threads of each of `warps` warps of one
+ * block (one SM), the slowest warp's.  Shows that the FP64 unit's cost is per
+ * warp instruction (independent of the active lanes) and shared by the SM's
+ * warps. */
+int asam_probe_fp64_chain(int warps, int lanes, int iters, double *cycles_per_op);
 /* Diagnostic: scalar FP64 FMA throughput of the current device in GFLOP/s
  * (no reference counterpart; used for the FP64 roofline of the benchmark). */
 int asam_probe_fp64_fma(int iters, double *gflops);
