@@ -905,7 +905,7 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
                 {&h->uf, d.n_uf()},       {&h->vf, d.n_vf()},        {&h->wf, d.n_wf()},        {&h->c, h->len},
                 {&h->cold, h->len},       {&h->rhs, h->len},         {&h->incr, h->len * h->nstage},
                 {&h->phi, h->len},        {&h->gx, d.n_uf() * cfg->ncomp}, {&h->gy, d.n_vf() * cfg->ncomp},
-                {&h->gz, d.n_wf() * cfg->ncomp}, {&h->val, 8 * h->npad}, {&h->partial, 2 * (size_t)kRedGrid},
+                {&h->gz, d.n_wf() * cfg->ncomp}, {&h->val, 8 * h->npad}, {&h->partial, 2 * (size_t)kFusedGridMax},
                 {&h->red_out, 1},         {&h->stage_a, h->len},     {&h->stage_b, h->len},
                 {&h->coef_x, 4 * d.n_uf()}, {&h->coef_y, 4 * d.n_vf()}, {&h->coef_z, 4 * d.n_wf()},
                 {&h->rvol, h->npad}};

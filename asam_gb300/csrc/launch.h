@@ -72,6 +72,9 @@ void launch_resid_dot(const Launch&, const Dims&, int ncomp, const double* val, 
                       double* r, double* partial, KrylovScalars* sc, int op, double* out);
 
 constexpr int kRedGrid = 1024;  // number of partial sums of the reductions
+// blocks of the fused SpMV + dot kernels (at most; the matvec's grid, whose
+// every thread keeps many cells' loads in flight), and the partials they need
+constexpr int kFusedGridMax = 4096;
 
 }  // namespace asam
 

@@ -8,6 +8,12 @@ void count_launches(long long n);
 }
 namespace {
 constexpr int kBlock = 256;
+inline int fused_grid(const asam::Launch& L, size_t n) {
+  size_t g = (n + RED_BLOCK - 1) / RED_BLOCK, cap = (size_t)L.sm_count * 16;
+  if (cap > (size_t)asam::kFusedGridMax) cap = asam::kFusedGridMax;
+  if (g > cap) g = cap;
+  return g < 1 ? 1 : (int)g;
+}
 inline int gs_grid(const asam::Launch& L, size_t n) {
   size_t g = (n + kBlock - 1) / kBlock;
   size_t cap = (size_t)L.sm_count * 16;
@@ -166,17 +172,18 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
   }                                                                                                                \
   void launch_matvec_dot(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* x, T* y, const T* a,  \
                          double* partial, KrylovScalars* sc, int op) {                                             \
-    k_matvec_dot<TM, T, false><<<RED_GRID, RED_BLOCK, 0, L.stream>>>(d, ncomp, val, x, y, a, partial, nullptr);    \
-    k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, RED_GRID, sc, op, nullptr);                                \
+    const int g = fused_grid(L, d.npad());                                                                         \
+    k_matvec_dot<TM, T, false><<<g, RED_BLOCK, 0, L.stream>>>(d, ncomp, val, x, y, a, partial, nullptr);           \
+    k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, g, sc, op, nullptr);                                       \
     count_launches(2);                                                                                             \
   }                                                                                                                \
   /* two dot products of the product: partial holds 2*RED_GRID values; op1 is final first */                      \
   void launch_matvec_dot2(const Launch& L, const Dims& d, int ncomp, const TM* val, const T* x, T* y, const T* a, \
                           double* partial, KrylovScalars* sc, int op1, int op2) {                                  \
-    k_matvec_dot<TM, T, true><<<RED_GRID, RED_BLOCK, 0, L.stream>>>(d, ncomp, val, x, y, a, partial,               \
-                                                                   partial + RED_GRID);                            \
-    k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, RED_GRID, sc, op1, nullptr);                               \
-    k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial + RED_GRID, RED_GRID, sc, op2, nullptr);                    \
+    const int g = fused_grid(L, d.npad());                                                                         \
+    k_matvec_dot<TM, T, true><<<g, RED_BLOCK, 0, L.stream>>>(d, ncomp, val, x, y, a, partial, partial + g);        \
+    k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial, g, sc, op1, nullptr);                                      \
+    k_dot_final<<<1, RED_BLOCK, 0, L.stream>>>(partial + g, g, sc, op2, nullptr);                                  \
     count_launches(3);                                                                                             \
   }                                                                                                                \
   void launch_axpy_dot(const Launch& L, const Dims& d, int ncomp, KrylovScalars* sc, int sel, double sign,        \
