@@ -1162,8 +1162,8 @@ def main():
             "vcycles_per_step": rr["vcycles_per_step"], "gpu_launches": rr["launches"], "clocks": rr["clocks"],
             "krylov_iterations": rr["iters"],
             "preconditioner": "FGMRES(10) preconditioned by one FP32 V-cycle on the periodic Laplacian (face "
-                              "unknowns eliminated); transport BiCGStab in FP32 with the x-line preconditioner "
-                              "inside FP64 refinement",
+                              "unknowns eliminated, one sweep per level); transport BiCGStab in FP32 with the "
+                              "x-line preconditioner inside FP64 refinement",
             "max_rel_err_vs_fp64": max(e["max_rel"] for e in errs),
             "max_rel_err_vs_fp64_state": max(e["max_rel_vec"] for e in errs),
             "error_note": "both runs stop their Krylov solves at a relative residual of the configured tolerance; "
