@@ -4,7 +4,9 @@ JacDiffusionCompute, ADVECT/Diffusion_Mod.f90:11-275, 1504-1708).
 Bit-exact: the flux right-hand side with diffusion (every case: periodic
 sides, closed walls, one column, one-cell-wide slab) and the stage matrix with
 the diffusion Jacobian.  The Rosenbrock step with diffusion: 1e-12 per field
-(FP64), 1e-10 (refined); the dynamical step of a closed block: 1e-8.
+(FP64), 1e-10 (refined); the dynamical step of a closed block: 1e-12 per
+field after each step (the momentum components as one vector) and in the
+face velocities.
 """
 from __future__ import annotations
 
@@ -106,8 +108,12 @@ def test_dyn_step_with_diffusion(built_lib):
         blk.set_diffusion(dh, dv)
         blk.proj_setup(dx, dy, dz, tol=1e-10, max_restart=20)
         blk.dyn_setup(pos["th"], pos["mom"], rv_pos=pos["qv"], bound_cells=bc, scalars=sc)
-        for _ in range(2):
+        for step in range(2):
             o.ros_step_dyn(pr, cr, ur, 2.0, rho_pos=0, th_pos=pos["th"], pos=pos["mom"], dx=dx, dy=dy, dz=dz,
                            rv_pos=pos["qv"], bound=bc, scalars=sc, bicg_tol=1e-10, proj_tol=1e-10, proj_maxiter=20)
             blk.Ros3MetC_dyn(cg, 2.0)
-            assert max(cases.field_relerr(cg, cr)) <= 1e-8
+            errs = cases.state_relerr(cg, cr, mom=pos["mom"])
+            assert max(errs) <= 1e-12, (step, errs)
+            vmax = max(float(np.max(np.abs(b))) for b in ur)
+            for a, b in zip(blk.get_velocity(), ur):
+                assert float(np.max(np.abs(a - b))) <= 1e-12 * vmax, step
