@@ -172,12 +172,12 @@ def test_bad_calls_raise():
         with pytest.raises(ValueError):
             blk.lapl_array_dirichlet(0, 0, 0)  # not assembled yet
         with pytest.raises(AsamError):
-            blk.proj_setup(np.full(g.nx, g.dx), np.full(g.ny, g.dy), g.dz, prefac2=-1.0)
-        with pytest.raises(AsamError):
             blk.proj_set_pre_schedule(-1, 0)
         with pytest.raises(KeyError):
             blk.proj_set_preconditioner("jacobi")
         blk.proj_set_pre_schedule(1, 1)  # the reference's growth, accepted
+        with pytest.raises(AsamError):
+            blk.proj_setup(np.full(g.nx, g.dx), np.full(g.ny, g.dy), g.dz, prefac2=-1.0)
     # the dynamical core refuses a block periodic in z (the buoyancy's
     # neighbour terms across a vertical periodic side are not built)
     grid = G.Grid(6, 5, 4, 100.0, 100.0, G.uniform_levels(4, 100.0), True, True, True)
