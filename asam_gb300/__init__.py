@@ -327,7 +327,9 @@ class TransportBlock:
         return y
 
     def PSolve1(self, x) -> np.ndarray:
-        """PSolve1 (PressurePre, Schur step, PressurePre) on a PressureVelocity vector."""
+        """PSolve1 (PressurePre, Schur step, PressurePre) on a PressureVelocity
+        vector -- the context's FGMRES preconditioner, so the periodic-Laplacian
+        one when proj_set_preconditioner (or the refined default) selects it."""
         a = _f64(x)
         y = self._pv()
         check(self.lib.asam_proj_psolve1(self.h, ptr(a), ptr(y)), "asam_proj_psolve1")

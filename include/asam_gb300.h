@@ -354,7 +354,10 @@ long asam_proj_face_count(asam_ctx *ctx);
 /* b = MatVec1(x) = MatVecFull (MATRIX/MatVec_Mod.f90:184-258) on
  * PressureVelocity vectors, without the Exchange that FGMRES applies after it. */
 int asam_proj_matvec1(asam_ctx *ctx, const double *x, double *b);
-/* b = PSolve1(x) (MATRIX/PreCond_Mod.f90:1555-1571) on PressureVelocity vectors. */
+/* b = PSolve1(x) (MATRIX/PreCond_Mod.f90:1555-1571) on PressureVelocity vectors:
+ * the context's FGMRES preconditioner, i.e. the periodic-Laplacian one
+ * instead when asam_proj_set_preconditioner (or the refined default) selects
+ * it. */
 int asam_proj_psolve1(asam_ctx *ctx, const double *x, double *b);
 /* asam_lapl_get and asam_lapl_vcycle on the Dirichlet hierarchy LaplDirichlet
  * (SetFactorD, MULTI/JacAccGrav_Mod.f90:453-469) of a block with periodic
