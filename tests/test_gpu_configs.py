@@ -13,8 +13,9 @@ cases), through the C-ABI against the oracle:
 * configuration 2 at its full size 256x256x128 (cut-cell hill with roughness,
   snapping, the small-cell merge, stretched levels): 2 transport steps
   (prescribed winds, dt = 2 s, BiCGStab 1e-10) at 1e-12 per field;
-* configuration 2's generator on a 48x48x128 periodic window: 2 full
-  Rosenbrock steps of the dynamical core at 1e-12;
+* configuration 2's generator on a 48x48x128 periodic window, and the same
+  window of the headline workload (configuration 3's seed): 2 full Rosenbrock
+  steps of the dynamical core at 1e-12 each;
 * configuration 5 at its full size (128x128x64 cut-cell hill, h = 800 m,
   half-width 4 km, a passive tracer, RosRK3 dt = 2 s, 40 steps, checkpoints
   every 8, J = volume integral of the tracer mixing ratio squared over a
@@ -98,6 +99,13 @@ def test_config2_256_transport_steps(built_lib):
 
 def test_config2_window_full_step(built_lib):
     _dyn_parity(G.hill_dyn_case(48, 48, 128, seed=2), 2.0, 2)
+
+
+def test_config3_window_full_step(built_lib):
+    """The headline workload's generator and seed (the mixed-precision
+    configuration, 512x512x128, seed 3) on a 48x48x128 periodic window: 2 full
+    FP64 dynamical steps at 1e-12 against the oracle."""
+    _dyn_parity(G.hill_dyn_case(48, 48, 128, seed=3), 2.0, 2)
 
 
 ADJ_TOL = 1e-14  # Krylov tolerance of every forward and adjoint solve below
