@@ -14,8 +14,9 @@ the block count:
   ix0-1:ix1+1), ``NrMP_FacesYZ`` then ``ix iy iz`` / ``xS yS zS`` pairs;
   the same for FV (ZX) and FW (XY); ``NrW_Cells`` then ``ix iy iz`` / ``VolC``;
   ``NrB_Cells  Struct_Bound`` then per boundary cell ``ix iy iz`` / ``xS yS zS``
-  / ``zRauh alb ee xFLS yFLS zFLS`` (Struct_Bound 3; 4-6 add soil and land
-  classes).
+  / ``zRauh alb ee xFLS yFLS zFLS`` (Struct_Bound 0-3), followed on the same
+  READ by the soil types of every soil layer (4), the land class (5), or the
+  land class and the soil types (6).
 
 Every weight not listed keeps the reader's Cartesian default
 (ReadWeights_Mod.f90:633-640, 893-940): full faces dy*dz, dx*dz, dx*dy over
@@ -34,6 +35,7 @@ arrays: ``FU(ix,iy,iz)`` = ``fu[iz-1, iy-1, ix+1]``, ``FV(ix,iy,iz)`` =
 Globe and Cyl grids (spherical and cylindrical face and volume formulas) and
 multi-block neighbour halos are not read: the reader refuses them.
 """
+
 from __future__ import annotations
 
 from dataclasses import dataclass, field
@@ -41,6 +43,12 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .geometry import Geometry, Grid, boundary_cells
+
+# roughness length per land class 0..9 (the zrough table of SOIL/SoilData_Mod.f90:104)
+ZROUGH = (0.05, 1.0, 0.15, 1.0, 1.0, 1.0, 0.2, 0.5, 0.03, 0.01)
+LAND_CLASS_DEF = 5       # LandClassDef default (MODULE/Physics_Mod.f90:560)
+NR_SOIL_LAYERS = 7       # Domain%nrsoillayers default (INIT/Grid_Mod.f90:676)
+LAND_CLASS_SEA = 9
 
 
 @dataclass
@@ -53,6 +61,8 @@ class BoundCells:
     xs: np.ndarray  # (n, 3) xS yS zS
     surf: np.ndarray  # (n, 6) zRauh alb ee xFLS yFLS zFLS
     struct_bound: int = 3
+    land_class: np.ndarray = field(default_factory=lambda: np.zeros(0, dtype=np.int32))  # LandClass
+    soil_type: np.ndarray = field(default_factory=lambda: np.zeros((0, 0), dtype=np.int32))  # SoilType(1:nrsoil)
     normal: np.ndarray = field(default_factory=lambda: np.zeros((0, 3)))  # n1 n2 n3
     fl: np.ndarray = field(default_factory=lambda: np.zeros(0))  # FL
     dl: np.ndarray = field(default_factory=lambda: np.zeros(0))  # dL
@@ -170,11 +180,18 @@ def write_weight2(path, blocks, grid_type: str = "Cart", periodic=(True, True, F
         ijk, vals = _entries("volc", geo.volc, ref[3])
         out.append(f" {len(vals)}    NrW_Cells")
         out += _pairs(ijk, vals)
-        out.append(f"{len(bound.ijk):12d}      NrB_Cells{bound.struct_bound:6d}   Struct_Bound{0:6d}  Nr_SoilLayers")
-        for t, xs, s in zip(bound.ijk.tolist(), bound.xs.tolist(), bound.surf.tolist()):
+        sb = bound.struct_bound
+        nsoil = bound.soil_type.shape[1] if sb in (4, 6) else 0
+        out.append(f"{len(bound.ijk):12d}      NrB_Cells{sb:6d}   Struct_Bound{nsoil:6d}  Nr_SoilLayers")
+        for q, (t, xs, s) in enumerate(zip(bound.ijk.tolist(), bound.xs.tolist(), bound.surf.tolist())):
             out.append(" {} {} {}".format(*t))
             out.append(" " + " ".join(_fmt(v) for v in xs))
-            out.append(" " + " ".join(_fmt(v) for v in s))
+            extra = []
+            if sb in (5, 6):
+                extra.append(str(int(bound.land_class[q])))
+            if sb in (4, 6):
+                extra += [str(int(v)) for v in bound.soil_type[q]]
+            out.append(" " + " ".join([_fmt(v) for v in s] + extra))
     with open(path, "w") as f:
         f.write("\n".join(out) + "\n")
 
@@ -246,10 +263,14 @@ class _ListReader:
         return [float(v.replace("D", "E").replace("d", "e")) for v in self.values(n)]
 
 
-def read_weight2(path, ib: int = 1, periodic=(True, True, False), expect=None) -> WeightBlock:
+def read_weight2(path, ib: int = 1, periodic=(True, True, False), expect=None,
+                 nr_soil_layers: int = NR_SOIL_LAYERS, land_class_def: int = LAND_CLASS_DEF,
+                 real_island: bool = False) -> WeightBlock:
     """ReadWeights for block ib (1-based) of a Cartesian file.  expect =
     (nx, ny, nz) checks the extents like the reference's 'Error WeightFile'
-    stops."""
+    stops.  nr_soil_layers (the grid deck's #NrSoilLayers), land_class_def
+    (LandClassDef) and real_island (RealIsland) are the model inputs the
+    boundary cells' land and soil classes depend on."""
     with open(path) as f:
         rd = _ListReader(f.read().splitlines())
     grid_type = rd.values(1)[0].strip("'\"")
@@ -282,20 +303,43 @@ def read_weight2(path, ib: int = 1, periodic=(True, True, False), expect=None) -
     _place("volc", volc, ijk, vals[:, 0])
     head = rd.values(3)
     nbc, sb = int(head[0]), int(head[2])
-    if sb not in (0, 1, 2, 3):
-        raise NotImplementedError(f"Weight2 reader: Struct_Bound {sb} (soil and land classes)")
+    if sb not in range(7):
+        raise NotImplementedError(f"Weight2 reader: Struct_Bound {sb}")
     bi, bx, bs = np.zeros((nbc, 3), dtype=np.int32), np.zeros((nbc, 3)), np.zeros((nbc, 6))
+    land = np.full(nbc, land_class_def, dtype=np.int32)
+    soil = np.zeros((nbc, nr_soil_layers), dtype=np.int32)
+    # ReadWeights_Mod.f90:1236-1279: what follows the six surface values, and
+    # the roughness and land class each Struct_Bound implies
+    ntail = {4: nr_soil_layers, 5: 1, 6: 1 + nr_soil_layers}.get(sb, 0)
     for i in range(nbc):
         bi[i] = rd.ints(3)
         bx[i] = rd.reals(3)
-        bs[i] = rd.reals(6)
+        v = rd.values(6 + ntail)
+        bs[i] = [float(t.replace("D", "E").replace("d", "e")) for t in v[:6]]
+        tail = [int(t) for t in v[6:]]
+        if sb == 4:
+            soil[i] = tail
+            bs[i, 0] = 0.05
+        elif sb == 5:
+            land[i] = LAND_CLASS_SEA  # only the sea class is read
+            bs[i, 0] = ZROUGH[land[i]]
+        elif sb == 6:
+            land[i] = tail[0]
+            soil[i] = tail[1:]
+            bs[i, 0] = ZROUGH[land[i]]
+        else:
+            soil[i, -1] = 5
     nx, ny, nz = dx.size, dy.size, dz.size
+    if real_island:  # a boundary cell with a full volume is an island in the sea
+        vol = volc[bi[:, 2], bi[:, 1], bi[:, 0]]
+        full = vol >= dx[bi[:, 0] - 1] * dy[bi[:, 1] - 1] * dz[bi[:, 2] - 1] * 0.9999
+        land[full] = LAND_CLASS_SEA
     if not (np.all(dx == dx[0]) and np.all(dy == dy[0])):
         raise NotImplementedError("Weight2 reader: the library's grids have uniform dx and dy")
     geo = Geometry(grid=Grid(nx=nx, ny=ny, nz=nz, dx=float(dx[0]), dy=float(dy[0]), dz=dz.copy(),
                              periodic_x=periodic[0], periodic_y=periodic[1], periodic_z=periodic[2]),
                    volc=volc, fu=fu, fv=fv, fw=fw)
-    bound = BoundCells(ijk=bi, xs=bx, surf=bs, struct_bound=sb)
+    bound = BoundCells(ijk=bi, xs=bx, surf=bs, struct_bound=sb, land_class=land, soil_type=soil)
     bound.normal, bound.fl, bound.dl = _normals(geo, dx, dy, dz, bi)
     return WeightBlock(geo=geo, origin=origin, dx=dx, dy=dy, dz=dz, mid_faces=tuple(mids), bound=bound)
 

@@ -145,7 +145,7 @@ def test_refusals(tmp_path):
     p.write_text(" Globe\n 1\n")
     with pytest.raises(NotImplementedError):
         W.read_weight2(str(p))
-    p.write_text(KNOWN.replace("3   Struct_Bound", "5   Struct_Bound"))
+    p.write_text(KNOWN.replace("3   Struct_Bound", "7   Struct_Bound"))
     with pytest.raises(NotImplementedError):
         W.read_weight2(str(p))
     p.write_text(KNOWN.replace("           2          -1           2", "           2          -3           2"))
@@ -154,3 +154,62 @@ def test_refusals(tmp_path):
     p.write_text(KNOWN[:400])
     with pytest.raises(ValueError):
         W.read_weight2(str(p))
+
+
+_SURF = "  0.1000000D+00  0.8000000D-01  0.8000000D+00  0.5000000D+02  0.2500000D+02  0.2000000D+01\n"
+
+
+@pytest.mark.parametrize("sb,tail,land,soil,zrauh", [
+    (3, "", [W.LAND_CLASS_DEF], [0, 0, 5], 0.1),                        # roughness as read, last layer 5
+    (4, " 3 4\n 6\n", [W.LAND_CLASS_DEF], [3, 4, 6], 0.05),            # soil types over two lines
+    (5, " 2\n", [W.LAND_CLASS_SEA], [0, 0, 0], W.ZROUGH[9]),            # any class read becomes sea
+    (6, " 7 1 1 2\n", [7], [1, 1, 2], W.ZROUGH[7]),                     # land class, then the soil types
+])
+def test_soil_and_land_classes(tmp_path, sb, tail, land, soil, zrauh):
+    """Struct_Bound 3-6 (ReadWeights_Mod.f90:1236-1279) with three soil
+    layers: the soil types and the land class follow the six surface values
+    on the same list-directed READ; 4 sets the roughness to 0.05, 5 and 6
+    take it from the land class's roughness length."""
+    text = KNOWN.replace("3   Struct_Bound", f"{sb}   Struct_Bound")
+    if tail:
+        text = text.replace(_SURF, _SURF.rstrip("\n") + tail)
+    p = tmp_path / "k.Weight2"
+    p.write_text(text)
+    bc = W.read_weight2(str(p), nr_soil_layers=3).bound
+    assert bc.struct_bound == sb
+    assert bc.land_class.tolist() == land and bc.soil_type.tolist() == [soil]
+    assert bc.surf[0, 0] == zrauh and bc.surf[0, 1] == 0.08
+
+
+def test_real_island(tmp_path):
+    """With RealIsland a boundary cell of full volume becomes sea (class 9);
+    the known file's cell (1,1,1) has VolC 2e4 < dx*dy*dz = 5e4, so a full
+    volume is written for it first."""
+    p = tmp_path / "k.Weight2"
+    p.write_text(KNOWN)
+    assert W.read_weight2(str(p), real_island=True).bound.land_class.tolist() == [W.LAND_CLASS_DEF]
+    p.write_text(KNOWN.replace("   2.0D4", "   5.0D4"))
+    assert W.read_weight2(str(p), real_island=True).bound.land_class.tolist() == [W.LAND_CLASS_SEA]
+    assert W.read_weight2(str(p)).bound.land_class.tolist() == [W.LAND_CLASS_DEF]
+
+
+@pytest.mark.parametrize("sb", [4, 6])
+def test_soil_classes_round_trip(tmp_path, sb):
+    """The writer's soil and land columns read back as written."""
+    geo = G.close_dead_faces(G.hill_case(8, 6, 5, seed=3)[0])
+    bound = W.surface_data(geo)
+    n = len(bound.ijk)
+    rng = np.random.default_rng(5)
+    bound.struct_bound = sb
+    bound.land_class = rng.integers(0, 10, n).astype(np.int32)
+    bound.soil_type = rng.integers(1, 9, (n, 4)).astype(np.int32)
+    p = tmp_path / "s.Weight2"
+    W.write_weight2(str(p), [(geo, (0.0, 0.0, 0.0), bound)])
+    got = W.read_weight2(str(p), nr_soil_layers=4).bound
+    assert np.array_equal(got.soil_type, bound.soil_type)
+    if sb == 6:
+        assert np.array_equal(got.land_class, bound.land_class)
+        assert np.array_equal(got.surf[:, 0], np.asarray(W.ZROUGH)[bound.land_class])
+    else:
+        assert (got.land_class == W.LAND_CLASS_DEF).all() and (got.surf[:, 0] == 0.05).all()
+    assert np.array_equal(got.surf[:, 1:], bound.surf[:, 1:])
