@@ -22,9 +22,11 @@ STATUS = {
     5: "ASAM_CUDA_ERROR",
     6: "ASAM_NO_DEVICE",
     7: "ASAM_IO_ERROR",
+    8: "ASAM_UNSUPPORTED",
 }
 ASAM_OK, ASAM_NOT_CONVERGED, ASAM_BREAKDOWN = 0, 1, 2
 ASAM_CUDA_ERROR = 5
+ASAM_BAD_ARG, ASAM_IO_ERROR, ASAM_UNSUPPORTED = 4, 7, 8
 
 
 class AsamConfig(C.Structure):
@@ -61,6 +63,22 @@ class AsamRestartHeader(C.Structure):
 class AsamRestartBlock(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("ncomp", C.c_int), ("nfrac", C.c_int),
                 ("c", C.c_void_p), ("uf", C.c_void_p), ("vf", C.c_void_p), ("wf", C.c_void_p)]
+
+
+class AsamWeight2Block(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("origin", C.c_double * 3),
+                ("dx", C.c_void_p), ("dy", C.c_void_p), ("dz", C.c_void_p),
+                ("fu", C.c_void_p), ("fv", C.c_void_p), ("fw", C.c_void_p), ("volc", C.c_void_p),
+                ("nmid", C.c_int * 3), ("mid_ijk", C.c_void_p * 3), ("mid_xs", C.c_void_p * 3),
+                ("nbound", C.c_int), ("struct_bound", C.c_int), ("nsoil", C.c_int),
+                ("bound_ijk", C.c_void_p), ("bound_xs", C.c_void_p), ("bound_surf", C.c_void_p),
+                ("land_class", C.c_void_p), ("soil_type", C.c_void_p),
+                ("normal", C.c_void_p), ("fl", C.c_void_p), ("dl", C.c_void_p)]
+
+
+class AsamWeight2Options(C.Structure):
+    _fields_ = [("periodic", C.c_int * 3), ("nr_soil_layers", C.c_int), ("land_class_def", C.c_int),
+                ("real_island", C.c_int), ("expect", C.c_int * 3)]
 
 
 # (name, restype, argtypes) of every exported entry point of include/asam_gb300.h
@@ -146,6 +164,11 @@ SIGNATURES = [
     ("asam_restart_read", C.c_int, [C.c_char_p, C.POINTER(AsamRestartHeader), C.c_int, C.POINTER(AsamRestartBlock)]),
     ("asam_restart_file_name", C.c_int, [C.c_char_p, C.c_int, C.c_char_p, C.c_int]),
     ("asam_restart_set_max_subrecord", C.c_int, [C.c_longlong]),
+    ("asam_weight2_open", C.c_int, [C.c_char_p, C.c_int, C.POINTER(AsamWeight2Options), C.POINTER(C.c_void_p),
+                                     C.POINTER(AsamWeight2Block)]),
+    ("asam_weight2_fetch", C.c_int, [_V, C.POINTER(AsamWeight2Block)]),
+    ("asam_weight2_close", None, [_V]),
+    ("asam_weight2_write", C.c_int, [C.c_char_p, C.c_int, C.POINTER(AsamWeight2Block), C.POINTER(C.c_int)]),
     ("asam_probe_div", C.c_int, [C.c_longlong, C.c_longlong, C.c_int, C.POINTER(C.c_longlong)]),
     ("asam_last_error", C.c_char_p, []),
 ]

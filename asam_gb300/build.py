@@ -12,6 +12,7 @@ linked into ``asam_gb300/libasam_gb300.so``:
 * ``dyn.cu`` dynamical-core stage: momentum sources, face/cell velocities,
   thermodynamics and the stage driver around the transport solve and the
   projection
+* ``restart.cu`` and ``weight2.cu`` restart and cut-cell geometry files (host)
 
 The oracle (``oracle/asam_oracle.c`` for the transport stage,
 ``oracle/asam_proj.c`` for the pressure projection, ``oracle/asam_dyn.c`` for
@@ -53,6 +54,7 @@ UNITS = {
     "dyn.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "restart.cu": [],
     "tritb.cu": ["-fmad=false"],
+    "weight2.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 
 

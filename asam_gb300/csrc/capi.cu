@@ -2,6 +2,8 @@
 // pointers, and the host-side drivers of BiCGStab, the preconditioner and the
 // Rosenbrock stage.  The drivers keep every Krylov scalar on the device; the
 // host only reads the convergence flag twice per iteration.
+#include <dlfcn.h>
+
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -187,6 +189,18 @@ bool is_device_ptr(const void* p) {
     return false;
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Without a CUDA driver every array is a host array, and the CUDA runtime is
+// not touched at all (the host-only file routines run on machines without a
+// GPU).
+bool device_array(const void* p) {
+  static const bool driver = [] {
+    void* d = dlopen("libcuda.so.1", RTLD_LAZY | RTLD_LOCAL);
+    if (d) dlclose(d);
+    return d != nullptr;
+  }();
+  return p && driver && is_device_ptr(p);
 }
 
 }  // namespace asam

@@ -127,6 +127,7 @@ int check_launch();
 int read_scalars(asam_ctx* h);
 int reduce_to_host(asam_ctx* h, double* out);
 bool is_device_ptr(const void* p);
+bool device_array(const void* p);  // device memory, false without a CUDA driver
 template <typename T>
 void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w);
 template <typename T>

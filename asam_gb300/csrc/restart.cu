@@ -20,8 +20,6 @@
 // contiguous array.  Device arrays move through two pinned staging buffers on
 // a private stream: the copy of one chunk overlaps the file transfer of the
 // other.  Host arrays go to the file directly.
-#include <dlfcn.h>
-
 #include <cerrno>
 #include <cstdint>
 #include <cstdio>
@@ -63,19 +61,7 @@ int arg_fail(const std::string& msg) {
   return ASAM_BAD_ARG;
 }
 
-// Without a CUDA driver every array is a host array, and the CUDA runtime is
-// not touched at all (its initialisation without a driver is not needed for
-// host-only restart files on a machine without a GPU).
-bool driver_present() {
-  static const bool present = [] {
-    void* h = dlopen("libcuda.so.1", RTLD_LAZY | RTLD_LOCAL);
-    if (h) dlclose(h);
-    return h != nullptr;
-  }();
-  return present;
-}
-
-bool on_device(const void* p) { return driver_present() && asam::is_device_ptr(p); }
+bool on_device(const void* p) { return asam::device_array(p); }
 
 struct Stage {
   char* pin[2] = {nullptr, nullptr};

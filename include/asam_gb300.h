@@ -30,7 +30,8 @@ typedef enum {
   ASAM_BAD_ARG = 4,
   ASAM_CUDA_ERROR = 5,
   ASAM_NO_DEVICE = 6,
-  ASAM_IO_ERROR = 7 /* restart file cannot be opened, is short, or its records do not fit the blocks */
+  ASAM_IO_ERROR = 7,   /* a restart or geometry file cannot be opened, is short, or does not fit */
+  ASAM_UNSUPPORTED = 8 /* a file form this library does not read (Globe/Cyl grids, Struct_Bound above 6) */
 } asam_status;
 
 typedef enum {
@@ -574,6 +575,66 @@ int asam_restart_file_name(const char *grid_file, int rank, char *buf, int cap);
 /* gfortran's -fmax-subrecord-length for files this library writes (default
  * and maximum 2147483639 bytes); the reader accepts any split. */
 int asam_restart_set_max_subrecord(long long bytes);
+
+/* ---- Cut-cell geometry files (.Weight2) ----------------------------------
+ * ReadWeights (INIT/ReadWeights_Mod.f90:568-1330) and WriteWeightBlk
+ * (GRID/OutputWeightBlk_Mod.f90:501-670) for Cartesian grids: Fortran
+ * list-directed text holding per block the origin, the cell widths, the face
+ * areas and cell volumes that differ from the reader's Cartesian defaults,
+ * the cut-face midpoints and the boundary cells with their surface data.
+ * Host arrays only (ASAM_BAD_ARG for device memory).  Layouts of the weights
+ * as in the block's fields: FU (nx+3)*ny*nz, FV nx*(ny+3)*nz, FW
+ * nx*ny*(nz+3), VolC (nx+2)*(ny+2)*(nz+2), ix fastest. */
+typedef struct {
+  int nx, ny, nz;        /* interior cells */
+  double origin[3];      /* x0 y0 z0 */
+  double *dx, *dy, *dz;  /* nx, ny, nz cell widths */
+  double *fu, *fv, *fw;  /* face areas (WeiFU/WeiFV/WeiFW) */
+  double *volc;          /* cell volumes */
+  int nmid[3];           /* cut-face midpoints of the YZ, ZX and XY faces */
+  int *mid_ijk[3];       /* 3*nmid[d]: ix iy iz */
+  double *mid_xs[3];     /* 3*nmid[d]: xS yS zS */
+  int nbound;            /* NrB_Cells */
+  int struct_bound;      /* 0-6: what follows the six surface values of a boundary cell */
+  int nsoil;             /* soil layers per boundary cell in soil_type */
+  int *bound_ijk;        /* 3*nbound: ix iy iz (1-based) */
+  double *bound_xs;      /* 3*nbound: xS yS zS */
+  double *bound_surf;    /* 6*nbound: zRauh alb ee xFLS yFLS zFLS */
+  int *land_class;       /* nbound: LandClass */
+  int *soil_type;        /* nbound*nsoil: SoilType(1:nsoil) */
+  double *normal;        /* 3*nbound: n1 n2 n3 (reader output) */
+  double *fl, *dl;       /* nbound each: FL, dL (reader output) */
+} asam_weight2_block;
+
+typedef struct {
+  int periodic[3];    /* 1: the side pair is periodic (the halo volumes' defaults depend on it) */
+  int nr_soil_layers; /* Domain%nrsoillayers (#NrSoilLayers, default 7; at most 57) */
+  int land_class_def; /* LandClassDef (default 5) */
+  int real_island;    /* RealIsland: a boundary cell of full volume becomes sea (class 9) */
+  int expect[3];      /* the caller's nx ny nz ('Error WeightFile' when the file differs); 0 = any */
+} asam_weight2_options;
+
+typedef struct asam_weight2_file asam_weight2_file;
+
+/* ReadWeights for block ib (1-based): parses the file into *out and fills
+ * info's sizes (nx ny nz, origin, nmid, nbound, struct_bound, nsoil; its
+ * pointers are zeroed).  ASAM_IO_ERROR for a file that is short, malformed
+ * or does not fit (an index outside the block, 'Error WeightFile'),
+ * ASAM_UNSUPPORTED for Globe/Cyl grids and Struct_Bound above 6. */
+int asam_weight2_open(const char *path, int ib, const asam_weight2_options *opt, asam_weight2_file **out,
+                      asam_weight2_block *info);
+
+/* Copies the block read by asam_weight2_open into dst's arrays, sized from
+ * its info; a NULL pointer skips that array.  Also the normal, area and wall
+ * distance of each boundary cell (ReadWeights_Mod.f90:1283-1319). */
+int asam_weight2_fetch(const asam_weight2_file *f, const asam_weight2_block *dst);
+
+void asam_weight2_close(asam_weight2_file *f);
+
+/* WriteWeightBlk for nblock blocks: lists the weights that differ from the
+ * reader's defaults for the given periodicity, each as the shortest decimal
+ * that reads back to the same double; the blocks' normal/fl/dl are unused. */
+int asam_weight2_write(const char *path, int nblock, const asam_weight2_block *blocks, const int periodic[3]);
 
 /* Sizes of the padded cell field for a configuration. */
 long long asam_npad(const asam_config *cfg);
