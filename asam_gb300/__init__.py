@@ -157,11 +157,33 @@ class TransportBlock:
         """Halo rule of the outer walls, applied to the state at the start of
         every stage (BoundaryCondition / BoundaryVelocity, ADVECT/Int_Mod.f90:
         283-287): (ncomp, 6) ints, sides W,E,S,N,B,T, 0 none, 1 ZeroGrad,
-        2 ZeroValue.  A new block has ZeroGrad everywhere."""
+        2 ZeroValue, and the open-boundary kinds of BoundaryCompute
+        (ADVECT/BoundaryCondition_Mod.f90:70-346) 3 MeanValue, 4 Function,
+        5 InFlowOutFlow (lateral sides), 6 Extrapolation (bottom and top),
+        whose data come from set_boundary_data first.  A new block has
+        ZeroGrad everywhere."""
         k = np.ascontiguousarray(kinds, dtype=np.int32).reshape(-1)
         if k.size != 6 * self.ncomp:
             raise ValueError("kinds must have 6 entries per component")
         check(self.lib.asam_set_boundary(self.h, k.ctypes.data_as(C.POINTER(C.c_int))), "asam_set_boundary")
+
+    def set_boundary_data(self, mean_profile=None, function_values=None, ambient=None):
+        """Data of the open-boundary kinds: MeanProfile (ncomp, nz), the
+        Function values F at the halo cells and the ambient state VecAmb
+        (ncomp padded fields each); None drops an array."""
+        g = self.grid
+        arrs = []
+        for a, n in ((mean_profile, self.ncomp * g.nz), (function_values, self.ncomp * g.npad),
+                     (ambient, self.ncomp * g.npad)):
+            if a is None:
+                arrs.append(None)
+                continue
+            a = _f64(a).reshape(-1)
+            if a.size != n:
+                raise ValueError(f"boundary data of {a.size} values, expected {n}")
+            arrs.append(a)
+        check(self.lib.asam_set_boundary_data(self.h, *[None if a is None else ptr(a) for a in arrs]),
+              "asam_set_boundary_data")
 
     def set_diffusion(self, dh, dv=None, jac: bool = True):
         """Diffusion of every component with coefficients DH, DV (padded cell

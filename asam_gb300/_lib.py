@@ -95,6 +95,7 @@ SIGNATURES = [
     ("asam_set_velocity", C.c_int, [_V, _V, _V, _V]),
     ("asam_exchange_cell", C.c_int, [_V, C.c_int, _V]),
     ("asam_set_boundary", C.c_int, [_V, C.POINTER(C.c_int)]),
+    ("asam_set_boundary_data", C.c_int, [_V, _V, _V, _V]),
     ("asam_boundary_condition", C.c_int, [_V, _V]),
     ("asam_set_diffusion", C.c_int, [_V, _V, _V, C.c_int]),
     ("asam_fcn", C.c_int, [_V, _V, _V]),

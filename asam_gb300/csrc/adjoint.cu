@@ -1071,11 +1071,16 @@ int dev_out_finish(asam_ctx* h, double* user, size_t n, double* dev) {
   return kOk;
 }
 
-// the tangent-linear and adjoint flux cover the advection; a context with
-// diffusion (asam_set_diffusion) is refused rather than differentiated wrongly
+// the tangent-linear and adjoint flux cover the advection with closed walls; a
+// context with diffusion (asam_set_diffusion) or with open-boundary wall
+// rules is refused rather than differentiated wrongly
 bool valid_comp(asam_ctx* h, int comp) {
   if (h->dkx) {
     set_last_error("the adjoint covers the advection flux; switch diffusion off first", __FILE__, __LINE__);
+    return false;
+  }
+  if (h->bc_open()) {
+    set_last_error("the adjoint covers the ZeroGrad and ZeroValue wall rules only", __FILE__, __LINE__);
     return false;
   }
   return comp >= 0 && comp < h->cfg.ncomp && comp != h->cfg.rho_pos;

@@ -112,19 +112,53 @@ struct DiffSrc {
   const T* phi;
 };
 
+// State read by the inflow through the faces of the outer walls
+// (AdvectionComputeP, ADVECT/Advection_Mod.f90:975-1044): the ncomp padded
+// fields and the density; c == nullptr leaves the inflow and the zeroing of
+// the wall halos out (the linearised operators of the adjoint).
+template <typename T>
+struct WallIn {
+  const T* c = nullptr;
+  const T* rho = nullptr;
+};
+
 // Halo rule of each component on each side that is not periodic (the outer
 // walls 'ow'...'ot' of a block): BoundaryCompute
 // (ADVECT/BoundaryCondition_Mod.f90:70-346) for the scalars and
 // BoundaryVelocityCellCompute (:424-970) for the momentum components.  Sides
 // in the order W, E, S, N, B, T; only the face halo cells (tangential interior
 // ranges) are set, like the reference's loops.
+// The open-boundary kinds of BoundaryCompute take their data from the
+// pointers below (device memory, set with the kinds):
+//   MeanValue      halo = 2*MeanProfile(ic,iz) - interior (:102-107, 194-199,
+//                  282-287: the bottom and top take the first and last level)
+//   Function       halo = 2*F - interior, F the caller's value of the start
+//                  function (times RhoFun for the non-number components) at
+//                  the halo cell (:108-120)
+//   InFlowOutFlow  W/E/S/N: on inflow (the face velocity into the block, zero
+//                  included) halo = Rho(halo)*VecAmb(halo), else the interior
+//                  value (:86-95); no branch on the bottom and top
+//   Extrapolation  B/T: halo = 2*c(iz0+1) - c(iz0+2) (:276-281); no branch on
+//                  the lateral sides
+// A side without the kind's branch leaves its halo as it is, like the
+// reference's IF chains.
 enum BcKind : signed char {
   kBcNone = 0,       // halo left as it is
   kBcZeroGrad = 1,   // halo = adjacent interior cell
   kBcZeroValue = 2,  // halo = -adjacent interior cell
+  kBcMeanValue = 3,
+  kBcFunction = 4,
+  kBcInflowOutflow = 5,
+  kBcExtrapolation = 6,
 };
 struct BcKinds {
   signed char k[kMaxComp][6];
+  const double* mean = nullptr;  // MeanProfile: ncomp x nz, level iz at [ic*nz + iz-1]
+  const double* fval = nullptr;  // Function values: ncomp padded fields (halo cells read)
+  const double* amb = nullptr;   // VecAmb: ncomp padded fields (halo cells read)
+  const double* uf = nullptr;    // face velocities whose sign InFlowOutFlow tests
+  const double* vf = nullptr;
+  int rho = 0;                   // density component (RhoPos)
 };
 
 // Krylov scalars that stay on the device between kernels.

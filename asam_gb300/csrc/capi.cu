@@ -552,7 +552,8 @@ int fcn_dev(asam_ctx* h, const double* c, double* f) {
   launch_phi(L, h->d, h->cfg.ncomp, h->cfg.rho_pos, c, h->phi);
   launch_face_flux(L, h->d, h->geom(), h->cfg.ncomp, h->coef_x, h->coef_y, h->coef_z, h->mask_x, h->mask_y,
                    h->mask_z, h->phi, h->gx, h->gy, h->gz);
-  launch_flux_gather(L, h->d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz, h->rvol, f, df);
+  launch_flux_gather(L, h->d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz, h->rvol, f, df,
+                     WallIn<double>{c, c + (size_t)h->cfg.rho_pos * h->npad});
   return check_launch();
 }
 
@@ -848,6 +849,8 @@ int asam_destroy(asam_ctx* h) {
   for (double* p : dptrs)
     if (p) cudaFree(p);
   if (h->val32) cudaFree(h->val32);
+  for (double* p : {h->bc_mean, h->bc_fval, h->bc_amb})
+    if (p) cudaFree(p);
   if (h->xl_w) cudaFree(h->xl_w);
   if (h->xl_r) cudaFree(h->xl_r);
   if (h->x32) cudaFree(h->x32);
@@ -925,6 +928,9 @@ int asam_create(const asam_config* cfg, const double* volc, const double* fu, co
                 {&h->rvol, h->npad}};
   for (auto& a : allocs)
     if ((e = cudaMalloc((void**)a.p, a.n * sizeof(double))) != cudaSuccess) return fail(e);
+  h->bc.uf = h->uf;  // InFlowOutFlow tests the sign of the context's face velocities
+  h->bc.vf = h->vf;
+  h->bc.rho = cfg->rho_pos;
   if ((e = cudaMalloc((void**)&h->mask_x, d.n_uf())) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc((void**)&h->mask_y, d.n_vf())) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc((void**)&h->mask_z, d.n_wf())) != cudaSuccess) return fail(e);
@@ -1022,11 +1028,61 @@ int asam_exchange_cell(asam_ctx* h, int ncomp, double* c) {
 
 int asam_set_boundary(asam_ctx* h, const int* kinds) {
   if (!h || !kinds) return kBadArg;
-  for (int q = 0; q < 6 * h->cfg.ncomp; ++q)
-    if (kinds[q] < ASAM_BC_NONE || kinds[q] > ASAM_BC_ZERO_VALUE) return kBadArg;
+  bool open = false;
+  for (int q = 0; q < 6 * h->cfg.ncomp; ++q) {
+    if (kinds[q] < ASAM_BC_NONE || kinds[q] > ASAM_BC_EXTRAPOLATION) return kBadArg;
+    const char* missing = kinds[q] == ASAM_BC_MEAN_VALUE && !h->bc_mean ? "MeanValue needs its profile"
+                          : kinds[q] == ASAM_BC_FUNCTION && !h->bc_fval ? "Function needs its halo values"
+                          : kinds[q] == ASAM_BC_INFLOW_OUTFLOW && !h->bc_amb ? "InFlowOutFlow needs the ambient state"
+                                                                              : nullptr;
+    if (missing) {
+      set_last_error((std::string("asam_set_boundary: ") + missing + " (asam_set_boundary_data first)").c_str(),
+                     __FILE__, __LINE__);
+      return kBadArg;
+    }
+    open = open || kinds[q] > ASAM_BC_ZERO_VALUE;
+  }
+  if (open && h->dyn) {
+    set_last_error("asam_set_boundary: the open-boundary kinds are built for the transport stage only", __FILE__,
+                   __LINE__);
+    return kBadArg;
+  }
   for (int ic = 0; ic < h->cfg.ncomp; ++ic)
     for (int sd = 0; sd < 6; ++sd) h->bc.k[ic][sd] = (signed char)kinds[6 * ic + sd];
   graphs_reset(h);  // a captured step holds the old rule
+  return kOk;
+}
+
+int asam_set_boundary_data(asam_ctx* h, const double* mean_profile, const double* function_values,
+                           const double* ambient) {
+  if (!h) return kBadArg;
+  const size_t sizes[3] = {(size_t)h->cfg.ncomp * h->cfg.nz, h->len, h->len};
+  const double* src[3] = {mean_profile, function_values, ambient};
+  double** dst[3] = {&h->bc_mean, &h->bc_fval, &h->bc_amb};
+  const signed char kind[3] = {kBcMeanValue, kBcFunction, kBcInflowOutflow};
+  for (int q = 0; q < 3; ++q) {
+    if (src[q]) continue;
+    for (int ic = 0; ic < h->cfg.ncomp; ++ic)
+      for (int sd = 0; sd < 6; ++sd)
+        if (h->bc.k[ic][sd] == kind[q]) {
+          set_last_error("asam_set_boundary_data: a kind in use needs this array", __FILE__, __LINE__);
+          return kBadArg;
+        }
+  }
+  for (int q = 0; q < 3; ++q) {
+    if (!src[q]) {
+      if (*dst[q]) cudaFree(*dst[q]);
+      *dst[q] = nullptr;
+      continue;
+    }
+    if (!*dst[q]) CK(cudaMalloc((void**)dst[q], sizes[q] * sizeof(double)));
+    CK(cudaMemcpyAsync(*dst[q], src[q], sizes[q] * sizeof(double), cudaMemcpyDefault, h->L.stream));
+  }
+  CK(cudaStreamSynchronize(h->L.stream));
+  h->bc.mean = h->bc_mean;
+  h->bc.fval = h->bc_fval;
+  h->bc.amb = h->bc_amb;
+  graphs_reset(h);  // a captured step holds the old pointers
   return kOk;
 }
 

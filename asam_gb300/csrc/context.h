@@ -106,6 +106,14 @@ struct asam_ctx {
   // halo rule of each component on the outer walls, applied to the state at
   // the start of every stage (default ZeroGrad, BoundaryCond_Mod.f90:240-247)
   asam::BcKinds bc{};
+  // device copies of the open-boundary rules' data (asam_set_boundary_data)
+  double *bc_mean = nullptr, *bc_fval = nullptr, *bc_amb = nullptr;
+  bool bc_open() const {  // a kind beyond ZeroGrad/ZeroValue is set
+    for (int ic = 0; ic < cfg.ncomp; ++ic)
+      for (int sd = 0; sd < 6; ++sd)
+        if (bc.k[ic][sd] > asam::kBcZeroValue) return true;
+    return false;
+  }
   // diffusion (asam_set_diffusion): face coefficients of DiffusionCompute,
   // nullptr while diffusion is off; jac_diff adds the diffusion Jacobian
   double *dkx = nullptr, *dky = nullptr, *dkz = nullptr;

@@ -289,12 +289,13 @@ void fcn_dyn_dev(asam_ctx* h, const double* c, const double* p, double* f) {
   launch_face_flux(L, d, h->geom(), h->cfg.ncomp, h->coef_x, h->coef_y, h->coef_z, h->mask_x, h->mask_y, h->mask_z,
                    h->phi, h->gx, h->gy, h->gz);
   const int grid = grid_of(L, h->npad);
+  const WallIn<double> wl{c, c + (size_t)h->cfg.rho_pos * h->npad};
   if (df)
     k_flux_gather<double, true, true><<<grid, kB, 0, L.stream>>>(d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz,
-                                                                 h->rvol, f, ms, *df);
+                                                                 h->rvol, f, ms, *df, wl);
   else
     k_flux_gather<double, true><<<grid, kB, 0, L.stream>>>(d, h->geom(), h->cfg.ncomp, h->gx, h->gy, h->gz, h->rvol,
-                                                             f, ms);
+                                                             f, ms, DiffSrc<double>{}, wl);
   count_launches(1);
 }
 
@@ -404,6 +405,11 @@ int asam_dyn_setup(asam_ctx* h, const asam_dyn_config* cfg, const int* bound_cel
     return kBadArg;
   if (!h->proj) {
     set_last_error("asam_dyn_setup: call asam_proj_setup first", __FILE__, __LINE__);
+    return kBadArg;
+  }
+  if (h->bc_open()) {  // BoundaryVelocity and the projection of open boundaries are not built
+    set_last_error("asam_dyn_setup: the open-boundary wall rules are built for the transport stage only", __FILE__,
+                   __LINE__);
     return kBadArg;
   }
   if (h->d.per_z) {  // the buoyancy's 'ib'/'it' neighbour terms are not built

@@ -21,12 +21,14 @@ void launch_fcn(const Launch& L, const Dims& d, const GeomT<double>& g, int ncom
   k_face_flux<double, 0><<<gs_grid(L, d.n_uf()), kBlock, 0, L.stream>>>(d, g, ncomp, cx, mx, phi, gx);
   k_face_flux<double, 1><<<gs_grid(L, d.n_vf()), kBlock, 0, L.stream>>>(d, g, ncomp, cy, my, phi, gy);
   k_face_flux<double, 2><<<gs_grid(L, d.n_wf()), kBlock, 0, L.stream>>>(d, g, ncomp, cz, mz, phi, gz);
+  const asam::WallIn<double> wl{c, c + (size_t)rho_pos * d.npad()};
   if (df)
     k_flux_gather<double, false, true><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f,
-                                                                                        MomSrc<double>{}, *df);
+                                                                                        MomSrc<double>{}, *df, wl);
   else
     k_flux_gather<double><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f,
-                                                                          MomSrc<double>{});
+                                                                          MomSrc<double>{}, asam::DiffSrc<double>{},
+                                                                          wl);
   count_launches(5);
 }
 
@@ -39,11 +41,13 @@ void launch_fcn_mom(const Launch& L, const Dims& d, const GeomT<double>& g, int 
   k_face_flux<double, 0><<<gs_grid(L, d.n_uf()), kBlock, 0, L.stream>>>(d, g, ncomp, cx, mx, phi, gx);
   k_face_flux<double, 1><<<gs_grid(L, d.n_vf()), kBlock, 0, L.stream>>>(d, g, ncomp, cy, my, phi, gy);
   k_face_flux<double, 2><<<gs_grid(L, d.n_wf()), kBlock, 0, L.stream>>>(d, g, ncomp, cz, mz, phi, gz);
+  const asam::WallIn<double> wl{c, c + (size_t)rho_pos * d.npad()};
   if (df)
     k_flux_gather<double, true, true><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f,
-                                                                                       ms, *df);
+                                                                                       ms, *df, wl);
   else
-    k_flux_gather<double, true><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f, ms);
+    k_flux_gather<double, true><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f, ms,
+                                                                                asam::DiffSrc<double>{}, wl);
   count_launches(5);
 }
 

@@ -14,6 +14,7 @@ using asam::kMaxComp;
 using asam::GsTileSched;
 using asam::MomSrc;
 using asam::DiffSrc;
+using asam::WallIn;
 
 template <typename T>
 __device__ __forceinline__ T eps_t() {
@@ -300,16 +301,18 @@ __device__ __forceinline__ T buoy_rho_face(const Dims& d, const GeomT<T>& g, con
 }
 
 // Gather of the face fluxes into the cell right-hand side in the exact order
-// in which the reference's scatter loop touches f(ix,iy,iz), then the
-// zero-volume mask (:1045-1051), the periodic ExchangeFlux (neighbour order
-// W,E,S,N,B,T) and AdvectionScale (:2888-2898).  One thread per padded cell.
+// in which the reference's scatter loop touches f(ix,iy,iz), then (wl set)
+// the first-order inflow through the faces of the outer walls from their
+// halo cells and the zeroed wall halos, the zero-volume mask (:1045-1051),
+// the periodic ExchangeFlux (neighbour order W,E,S,N,B,T) and AdvectionScale
+// (:2888-2898).  One thread per padded cell.
 // kMom adds the momentum sources of ms (closed or periodic x/y sides); kDiff the diffusion
 // fluxes of df with DiffusionCompute's second zero-volume mask (the halo
 // cells of a periodic side included, before ExchangeFlux reads them).
 template <typename T, bool kMom = false, bool kDiff = false>
 __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict__ gx, const T* __restrict__ gy,
                               const T* __restrict__ gz, const T* __restrict__ rvol, T* __restrict__ f,
-                              MomSrc<T> ms, DiffSrc<T> df = DiffSrc<T>{}) {
+                              MomSrc<T> ms, DiffSrc<T> df = DiffSrc<T>{}, WallIn<T> wl = WallIn<T>{}) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int NX = d.NX(), NY = d.NY(), NZ = d.NZ();
   const size_t n = d.npad();
@@ -350,6 +353,34 @@ __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict
         if (uR < (T)0) a = a + GX[fxR];  // FluxXL of the cell east
         if (vR < (T)0) a = a + GY[fyR];
         if (wR < (T)0) a = a + GZ[fzR];
+        if (wl.c) {  // inflow through the outer walls' faces, W, E, S, N, B, T (:975-1044)
+          const T* cc = wl.c + ic * n;
+          const T half = (T)0.5;
+          if (!d.per_x && i == 1) {
+            const size_t H = d.P(0, j, k);
+            a = a + half * (fabs(uL) + uL) * cc[H] / (wl.rho[H] + e) * g.fu[d.FU(0, j, k)];
+          }
+          if (!d.per_x && i == nx) {
+            const size_t H = d.P(nx + 1, j, k);
+            a = a + half * (fabs(uR) - uR) * cc[H] / (wl.rho[H] + e) * g.fu[d.FU(nx, j, k)];
+          }
+          if (!d.per_y && j == 1) {
+            const size_t H = d.P(i, 0, k);
+            a = a + half * (fabs(vL) + vL) * cc[H] / (wl.rho[H] + e) * g.fv[d.FV(i, 0, k)];
+          }
+          if (!d.per_y && j == ny) {
+            const size_t H = d.P(i, ny + 1, k);
+            a = a + half * (fabs(vR) - vR) * cc[H] / (wl.rho[H] + e) * g.fv[d.FV(i, ny, k)];
+          }
+          if (!d.per_z && k == 1) {  // the bottom divides by the interior cell's density
+            const size_t H = d.P(i, j, 0);
+            a = a + half * (fabs(wL) + wL) * cc[H] / (wl.rho[P] + e) * g.fw[d.FW(i, j, 0)];
+          }
+          if (!d.per_z && k == nz) {
+            const size_t H = d.P(i, j, nz + 1);
+            a = a + half * (fabs(wR) - wR) * cc[H] / (wl.rho[H] + e) * g.fw[d.FW(i, j, nz)];
+          }
+        }
         a = div_rn(a * V, Ve, rV);
         if (kDiff) {  // f(R) - Flux, f(L) + Flux per face, x then y then z; then the mask
           const T* ph = df.phi + ic * n;
@@ -489,7 +520,9 @@ __global__ void k_flux_gather(Dims d, GeomT<T> g, int ncomp, const T* __restrict
       if (axis == 0) vel = g.uf[fidx];
       if (axis == 1) vel = g.vf[fidx];
       if (axis == 2) vel = g.wf[fidx];
-      const bool has = axis >= 0 && (take_pos ? vel > (T)0 : vel < (T)0);
+      // an outer wall's face halo is zeroed after the inflow (:975-1044)
+      const bool wall = (axis == 0 && !d.per_x) || (axis == 1 && !d.per_y) || (axis == 2 && !d.per_z);
+      const bool has = axis >= 0 && !(wl.c && wall) && (take_pos ? vel > (T)0 : vel < (T)0);
       for (int ic = 0; ic < ncomp; ++ic) {
         T a = (T)0;
         if (has) {
@@ -665,17 +698,31 @@ __global__ void k_jac(Dims d, GeomT<T> g, const T* __restrict__ rho, const T* __
       if (i == nx) dg = dg - jac_term(g.uf[d.UF(nx, j, k)], true, g.fu[d.FU(nx, j, k)], VP, rVP, rPe, rrP);
       if (i == nx + 1) dg = dg - jac_term(g.uf[d.UF(nx, j, k)], false, g.fu[d.FU(nx, j, k)], VP, rVP, rPe, rrP);
     }
+    // outer walls 'ow'/'oe' (ADVECT/Advection_Mod.f90:2390-2410, 2469-2489): the
+    // outflow through the wall face on the interior cell's diagonal
+    if (!d.per_x && jj && kk) {
+      if (i == 1) dg = dg - jac_term(g.uf[d.UF(0, j, k)], false, g.fu[d.FU(0, j, k)], VP, rVP, rPe, rrP);
+      if (i == nx) dg = dg - jac_term(g.uf[d.UF(nx, j, k)], true, g.fu[d.FU(nx, j, k)], VP, rVP, rPe, rrP);
+    }
     if (d.per_y && ii && kk) {
       if (j == 0) dg = dg - jac_term(g.vf[d.VF(i, 0, k)], true, g.fv[d.FV(i, 0, k)], VP, rVP, rPe, rrP);
       if (j == 1) dg = dg - jac_term(g.vf[d.VF(i, 0, k)], false, g.fv[d.FV(i, 0, k)], VP, rVP, rPe, rrP);
       if (j == ny) dg = dg - jac_term(g.vf[d.VF(i, ny, k)], true, g.fv[d.FV(i, ny, k)], VP, rVP, rPe, rrP);
       if (j == ny + 1) dg = dg - jac_term(g.vf[d.VF(i, ny, k)], false, g.fv[d.FV(i, ny, k)], VP, rVP, rPe, rrP);
     }
+    if (!d.per_y && ii && kk) {  // 'os'/'on'
+      if (j == 1) dg = dg - jac_term(g.vf[d.VF(i, 0, k)], false, g.fv[d.FV(i, 0, k)], VP, rVP, rPe, rrP);
+      if (j == ny) dg = dg - jac_term(g.vf[d.VF(i, ny, k)], true, g.fv[d.FV(i, ny, k)], VP, rVP, rPe, rrP);
+    }
     if (d.per_z && ii && jj) {
       if (k == 0) dg = dg - jac_term(g.wf[d.WF(i, j, 0)], true, g.fw[d.FW(i, j, 0)], VP, rVP, rPe, rrP);
       if (k == 1) dg = dg - jac_term(g.wf[d.WF(i, j, 0)], false, g.fw[d.FW(i, j, 0)], VP, rVP, rPe, rrP);
       if (k == nz) dg = dg - jac_term(g.wf[d.WF(i, j, nz)], true, g.fw[d.FW(i, j, nz)], VP, rVP, rPe, rrP);
       if (k == nz + 1) dg = dg - jac_term(g.wf[d.WF(i, j, nz)], false, g.fw[d.FW(i, j, nz)], VP, rVP, rPe, rrP);
+    }
+    if (!d.per_z && ii && jj) {  // 'ob'/'ot'
+      if (k == 1) dg = dg - jac_term(g.wf[d.WF(i, j, 0)], false, g.fw[d.FW(i, j, 0)], VP, rVP, rPe, rrP);
+      if (k == nz) dg = dg - jac_term(g.wf[d.WF(i, j, nz)], true, g.fw[d.FW(i, j, nz)], VP, rVP, rPe, rrP);
     }
     // JacDiffusionCompute (ADVECT/Diffusion_Mod.f90:1504-1708): per face with
     // a neighbour Temp = 2K; the off-diagonal of each column and its diagonal
@@ -1476,8 +1523,33 @@ __global__ void k_exchange_cell(Dims d, int ncomp, T* __restrict__ c) {
 
 // Halo rule of the outer walls (BoundaryCondition / BoundaryVelocity at the
 // start of a stage, ADVECT/Int_Mod.f90:283-287): every face halo cell of a
-// side that is not periodic takes the adjacent interior value (ZeroGrad) or
-// its negative (ZeroValue).  comp0 is the first component's index in bc.
+// side that is not periodic takes the rule of its component and side (the
+// kinds of BcKind).  comp0 is the first component's index in bc; one thread
+// handles one halo location for every component in order, so a density halo
+// that InFlowOutFlow reads is updated before the components after the
+// density, as in the reference's component loop.
+template <typename T>
+__device__ __forceinline__ void bc_apply(const asam::BcKinds& bc, signed char kind, int side, int q, size_t n, T* a,
+                                         const T* rho, size_t h, size_t src, size_t src2, int level, int nz,
+                                         double vel) {
+  switch (kind) {
+    case asam::kBcZeroGrad: a[h] = a[src]; break;
+    case asam::kBcZeroValue: a[h] = -a[src]; break;
+    case asam::kBcMeanValue: a[h] = (T)2 * (T)bc.mean[(size_t)q * nz + (level - 1)] - a[src]; break;
+    case asam::kBcFunction: a[h] = (T)2 * (T)bc.fval[(size_t)q * n + h] - a[src]; break;
+    case asam::kBcInflowOutflow:
+      if (side < 4 && rho) {
+        const bool in = (side & 1) ? vel <= 0.0 : vel >= 0.0;
+        a[h] = in ? rho[h] * (T)bc.amb[(size_t)q * n + h] : a[src];
+      }
+      break;
+    case asam::kBcExtrapolation:
+      if (side >= 4) a[h] = (T)2 * a[src] - a[src2];
+      break;
+    default: break;
+  }
+}
+
 template <typename T>
 __global__ void k_bound_cond(Dims d, int ncomp, int comp0, asam::BcKinds bc, T* __restrict__ c) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
@@ -1486,31 +1558,41 @@ __global__ void k_bound_cond(Dims d, int ncomp, int comp0, asam::BcKinds bc, T* 
   const size_t nyf = d.per_y ? 0 : (size_t)nx * nz;
   const size_t nzf = d.per_z ? 0 : (size_t)nx * ny;
   const size_t tot = nxf + nyf + nzf;
+  const T* rho = comp0 == 0 ? c + (size_t)bc.rho * n : nullptr;  // the density, read by InFlowOutFlow
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
-    size_t lo, lo_src, hi, hi_src;
+    size_t lo, lo_src, lo_src2, hi, hi_src, hi_src2;
     int side;  // W/E = 0, S/N = 2, B/T = 4
+    int lev_lo, lev_hi;
+    double vel_lo = 0.0, vel_hi = 0.0;
     if (q < nxf) {
       int j = (int)(q % ny) + 1, k = (int)(q / ny) + 1;
-      lo = d.P(0, j, k); lo_src = d.P(1, j, k); hi = d.P(nx + 1, j, k); hi_src = d.P(nx, j, k);
+      lo = d.P(0, j, k); lo_src = d.P(1, j, k); lo_src2 = d.P(2, j, k);
+      hi = d.P(nx + 1, j, k); hi_src = d.P(nx, j, k); hi_src2 = d.P(nx - 1, j, k);
       side = 0;
+      lev_lo = lev_hi = k;
+      if (bc.uf) vel_lo = bc.uf[d.UF(0, j, k)], vel_hi = bc.uf[d.UF(nx, j, k)];
     } else if (q < nxf + nyf) {
       size_t r = q - nxf;
       int i = (int)(r % nx) + 1, k = (int)(r / nx) + 1;
-      lo = d.P(i, 0, k); lo_src = d.P(i, 1, k); hi = d.P(i, ny + 1, k); hi_src = d.P(i, ny, k);
+      lo = d.P(i, 0, k); lo_src = d.P(i, 1, k); lo_src2 = d.P(i, 2, k);
+      hi = d.P(i, ny + 1, k); hi_src = d.P(i, ny, k); hi_src2 = d.P(i, ny - 1, k);
       side = 2;
+      lev_lo = lev_hi = k;
+      if (bc.vf) vel_lo = bc.vf[d.VF(i, 0, k)], vel_hi = bc.vf[d.VF(i, ny, k)];
     } else {
       size_t r = q - nxf - nyf;
       int i = (int)(r % nx) + 1, j = (int)(r / nx) + 1;
-      lo = d.P(i, j, 0); lo_src = d.P(i, j, 1); hi = d.P(i, j, nz + 1); hi_src = d.P(i, j, nz);
+      lo = d.P(i, j, 0); lo_src = d.P(i, j, 1); lo_src2 = d.P(i, j, 2);
+      hi = d.P(i, j, nz + 1); hi_src = d.P(i, j, nz); hi_src2 = d.P(i, j, nz - 1);
       side = 4;
+      lev_lo = 1, lev_hi = nz;
     }
     for (int ic = 0; ic < ncomp; ++ic) {
       T* a = c + ic * n;
-      const signed char kl = bc.k[comp0 + ic][side], kh = bc.k[comp0 + ic][side + 1];
-      if (kl == asam::kBcZeroGrad) a[lo] = a[lo_src];
-      else if (kl == asam::kBcZeroValue) a[lo] = -a[lo_src];
-      if (kh == asam::kBcZeroGrad) a[hi] = a[hi_src];
-      else if (kh == asam::kBcZeroValue) a[hi] = -a[hi_src];
+      const int cq = comp0 + ic;
+      const signed char kl = bc.k[cq][side], kh = bc.k[cq][side + 1];
+      if (kl != asam::kBcNone) bc_apply(bc, kl, side, cq, n, a, rho, lo, lo_src, lo_src2, lev_lo, nz, vel_lo);
+      if (kh != asam::kBcNone) bc_apply(bc, kh, side + 1, cq, n, a, rho, hi, hi_src, hi_src2, lev_hi, nz, vel_hi);
     }
   }
 }

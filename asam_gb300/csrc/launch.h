@@ -19,7 +19,8 @@ struct Launch {
                         const T* coef_z, const unsigned char* mask_x, const unsigned char* mask_y,               \
                         const unsigned char* mask_z, const T* phi, T* gx, T* gy, T* gz);                         \
   void launch_flux_gather(const Launch&, const Dims&, const GeomT<T>&, int ncomp, const T* gx, const T* gy,      \
-                          const T* gz, const T* rvol, T* f, const DiffSrc<T>* df);                               \
+                          const T* gz, const T* rvol, T* f, const DiffSrc<T>* df,                                \
+                          const WallIn<T>& wl = WallIn<T>{});                                                    \
   void launch_diff_coef(const Launch&, const Dims&, const GeomT<T>&, const T* dh, const T* dv, T* kx, T* ky,    \
                         T* kz);                                                                                  \
   void launch_recip_eps(const Launch&, size_t len, const T* v, T* rv);                                          \

@@ -44,13 +44,13 @@ inline int gs_grid(const asam::Launch& L, size_t n) {
     count_launches(3);                                                                                             \
   }                                                                                                                \
   void launch_flux_gather(const Launch& L, const Dims& d, const GeomT<T>& g, int ncomp, const T* gx, const T* gy,  \
-                          const T* gz, const T* rvol, T* f, const DiffSrc<T>* df) {                                \
+                          const T* gz, const T* rvol, T* f, const DiffSrc<T>* df, const WallIn<T>& wl) {           \
     if (df)                                                                                                        \
       k_flux_gather<T, false, true><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol,  \
-                                                                                   f, MomSrc<T>{}, *df);           \
+                                                                                   f, MomSrc<T>{}, *df, wl);       \
     else                                                                                                           \
       k_flux_gather<T><<<gs_grid(L, d.npad()), kBlock, 0, L.stream>>>(d, g, ncomp, gx, gy, gz, rvol, f,            \
-                                                                      MomSrc<T>{});                                \
+                                                                      MomSrc<T>{}, DiffSrc<T>{}, wl);              \
     count_launches(1);                                                                                             \
   }                                                                                                                \
   void launch_diff_coef(const Launch& L, const Dims& d, const GeomT<T>& g, const T* dh, const T* dv, T* kx, T* ky,  \

@@ -123,9 +123,41 @@ int asam_exchange_cell(asam_ctx *ctx, int ncomp, double *c);
  * The default of a new context is ZeroGrad everywhere, the reference's
  * default BCMetVec (MODULE/BoundaryCond_Mod.f90:240-247).  A closed box with
  * free-slip walls (BCVel='FreeSlip') has ZeroValue for the momentum
- * components normal to a wall (:292-294 and the other sides). */
-enum { ASAM_BC_NONE = 0, ASAM_BC_ZERO_GRAD = 1, ASAM_BC_ZERO_VALUE = 2 };
+ * components normal to a wall (:292-294 and the other sides).
+ * The open-boundary kinds of BoundaryCompute (transport stage only; their
+ * data from asam_set_boundary_data):
+ *   MEAN_VALUE      halo = 2*MeanProfile(ic,iz) - interior (bottom and top:
+ *                   the profile's first and last level)
+ *   FUNCTION        halo = 2*F - interior, F the value of the case's start
+ *                   function at the halo cell (times RhoFun for all but the
+ *                   number concentrations), as the caller evaluates it
+ *   INFLOW_OUTFLOW  W/E/S/N: where the face velocity points into the block
+ *                   (or is zero) halo = Rho(halo)*VecAmb(halo), else the
+ *                   interior value; the bottom and top keep their halos
+ *   EXTRAPOLATION   B/T: halo = 2*c(iz0+1) - c(iz0+2); the lateral sides keep
+ *                   their halos
+ * Whatever the kinds, a face velocity pointing into the block through an
+ * outer wall carries the halo's value in (the first-order inflow of
+ * AdvectionComputeP, ADVECT/Advection_Mod.f90:975-1044). */
+enum {
+  ASAM_BC_NONE = 0,
+  ASAM_BC_ZERO_GRAD = 1,
+  ASAM_BC_ZERO_VALUE = 2,
+  ASAM_BC_MEAN_VALUE = 3,
+  ASAM_BC_FUNCTION = 4,
+  ASAM_BC_INFLOW_OUTFLOW = 5,
+  ASAM_BC_EXTRAPOLATION = 6
+};
 int asam_set_boundary(asam_ctx *ctx, const int *kinds);
+/* Data of the open-boundary kinds, copied into the context (host or device
+ * pointers; NULL drops an array, refused while a kind uses it): mean_profile
+ * ncomp*nz with level iz of component ic at [ic*nz + iz-1] (MeanProfile,
+ * ADVECT/Diagnostic_Mod.f90:275-314); function_values ncomp padded fields
+ * whose halo cells hold F; ambient ncomp padded fields of VecAmb.  The
+ * values stay until the next call: a time-dependent F is evaluated by the
+ * caller, once per step (the reference evaluates it at each stage's time). */
+int asam_set_boundary_data(asam_ctx *ctx, const double *mean_profile, const double *function_values,
+                           const double *ambient);
 /* Apply the halo rule to a state (ncomp padded fields) once. */
 int asam_boundary_condition(asam_ctx *ctx, double *c);
 

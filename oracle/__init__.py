@@ -23,7 +23,8 @@ class OraGeom(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("per_x", C.c_int), ("per_y", C.c_int),
                 ("per_z", C.c_int), ("volc", C.c_void_p), ("fu", C.c_void_p), ("fv", C.c_void_p),
                 ("fw", C.c_void_p), ("bc", C.c_void_p), ("dh", C.c_void_p), ("dv", C.c_void_p),
-                ("jac_diff", C.c_int)]
+                ("jac_diff", C.c_int), ("bc_mean", C.c_void_p), ("bc_fval", C.c_void_p), ("bc_amb", C.c_void_p),
+                ("bc_uf", C.c_void_p), ("bc_vf", C.c_void_p), ("bc_rho", C.c_int)]
 
 
 _lib = None
@@ -120,13 +121,34 @@ class Oracle:
 
     def set_boundary(self, kinds):
         """Halo rule of the outer walls, (ncomp, 6) ints W,E,S,N,B,T (0 none,
-        1 ZeroGrad, 2 ZeroValue); None = ZeroGrad everywhere."""
+        1 ZeroGrad, 2 ZeroValue, 3 MeanValue, 4 Function, 5 InFlowOutFlow,
+        6 Extrapolation); None = ZeroGrad everywhere."""
         if kinds is None:
             self._bc = None
             self.g.bc = None
         else:
             self._bc = np.ascontiguousarray(kinds, dtype=np.int32).reshape(-1)
             self.g.bc = self._bc.ctypes.data
+
+    def set_boundary_data(self, mean=None, fval=None, amb=None, vel=None, rho_pos=0):
+        """Data of the open-boundary halo rules: MeanProfile (ncomp, nz), the
+        Function values and the ambient state (ncomp padded fields), the face
+        velocities (uF, vF, wF) whose sign InFlowOutFlow tests when bound_cond
+        is called alone (a step uses its own), the density component."""
+        keep = {}
+        for name, a in (("bc_mean", mean), ("bc_fval", fval), ("bc_amb", amb)):
+            if a is None:
+                setattr(self.g, name, None)
+            else:
+                keep[name] = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+                setattr(self.g, name, keep[name].ctypes.data)
+        if vel is None:
+            self.g.bc_uf = self.g.bc_vf = None
+        else:
+            keep["uf"], keep["vf"] = (np.ascontiguousarray(v, dtype=np.float64).reshape(-1) for v in vel[:2])
+            self.g.bc_uf, self.g.bc_vf = keep["uf"].ctypes.data, keep["vf"].ctypes.data
+        self.g.bc_rho = int(rho_pos)
+        self._bc_data = keep
 
     def set_diffusion(self, dh, dv=None, jac=True):
         """Diffusion coefficients DH, DV (padded cell fields; DV defaults to

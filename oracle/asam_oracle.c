@@ -78,38 +78,73 @@ void ora_exchange_cell(const ora_geom *g, int ncomp, double *c) {
  * BoundaryCompute (ADVECT/BoundaryCondition_Mod.f90:1143-1221, 70-346) and
  * BoundaryVelocityCellCompute (:424-970) for the ZeroGrad and ZeroValue
  * kinds: face halos of the non-periodic sides, tangential interior ranges.
+ * Kinds of BoundaryCompute beyond those, per component and side in the order
+ * W, E, S, N, B, T (a side without the kind's branch leaves its halo alone):
+ *   3 MeanValue      halo = 2*MeanProfile(ic,iz) - interior; the bottom and
+ *                    top take the profile's first and last level (:102-107)
+ *   4 Function       halo = 2*F - interior, F the caller's value of Val
+ *                    (RhoFun*Val for the non-number components) at the halo
+ *                    cell (:108-120)
+ *   5 InFlowOutFlow  W/E/S/N only: inflow (uF(ix0) >= 0 on the west,
+ *                    uF(ix1) <= 0 on the east, vF likewise) halo =
+ *                    Rho(halo)*VecAmb(halo), else the interior value (:86-95)
+ *   6 Extrapolation  B/T only: halo = 2*c(iz0+1) - c(iz0+2) (:276-281)
+ * Components are processed in order, so the density halo an InFlowOutFlow
+ * rule reads is already updated for the components after the density.
  * comp0 is the index of the first of the ncomp fields in g->bc. */
 /* ------------------------------------------------------------------ */
 static int bc_kind(const ora_geom *g, int ic, int side) { return g->bc ? g->bc[6 * ic + side] : 1; }
-static void bc_set(double *a, size_t h, size_t src, int kind) {
+typedef struct {
+  const ora_geom *g;
+  const double *uf, *vf, *rho;
+  size_t n;
+  int q; /* component index in g->bc and the data arrays */
+} bc_ctx;
+/* one halo cell h from its interior neighbour src (src2 the next one inward);
+ * side 0-5, level iz of the profile, vel the InFlowOutFlow face velocity */
+static void bc_set(const bc_ctx *x, double *a, size_t h, size_t src, size_t src2, int side, int iz, double vel) {
+  const ora_geom *g = x->g;
+  const int kind = bc_kind(g, x->q, side);
   if (kind == 1) a[h] = a[src];
   else if (kind == 2) a[h] = -a[src];
+  else if (kind == 3) a[h] = 2.0 * g->bc_mean[(size_t)x->q * g->nz + (size_t)(iz - 1)] - a[src];
+  else if (kind == 4) a[h] = 2.0 * g->bc_fval[(size_t)x->q * x->n + h] - a[src];
+  else if (kind == 5 && side < 4) {
+    const int in = (side & 1) ? vel <= 0.0 : vel >= 0.0;
+    a[h] = in ? x->rho[h] * g->bc_amb[(size_t)x->q * x->n + h] : a[src];
+  } else if (kind == 6 && side >= 4) a[h] = 2.0 * a[src] - a[src2];
 }
-void ora_bound_cond(const ora_geom *g, int ncomp, int comp0, double *c) {
+static void bound_cond(const ora_geom *g, int ncomp, int comp0, double *c, const double *uf, const double *vf,
+                       int rho_pos) {
   const int nx = g->nx, ny = g->ny, nz = g->nz;
   const size_t n = NPAD(g);
   for (int ic = 0; ic < ncomp; ++ic) {
     double *a = c + ic * n;
-    const int q = comp0 + ic;
+    bc_ctx x = {g, uf, vf, c + (size_t)(rho_pos - comp0) * n, n, comp0 + ic};
     if (!g->per_x)
       for (int k = 1; k <= nz; ++k)
         for (int j = 1; j <= ny; ++j) {
-          bc_set(a, PIDX(g, 0, j, k), PIDX(g, 1, j, k), bc_kind(g, q, 0));
-          bc_set(a, PIDX(g, nx + 1, j, k), PIDX(g, nx, j, k), bc_kind(g, q, 1));
+          bc_set(&x, a, PIDX(g, 0, j, k), PIDX(g, 1, j, k), PIDX(g, 2, j, k), 0, k, uf ? uf[UFI(g, 0, j, k)] : 0.0);
+          bc_set(&x, a, PIDX(g, nx + 1, j, k), PIDX(g, nx, j, k), PIDX(g, nx - 1, j, k), 1, k,
+                 uf ? uf[UFI(g, nx, j, k)] : 0.0);
         }
     if (!g->per_y)
       for (int k = 1; k <= nz; ++k)
         for (int i = 1; i <= nx; ++i) {
-          bc_set(a, PIDX(g, i, 0, k), PIDX(g, i, 1, k), bc_kind(g, q, 2));
-          bc_set(a, PIDX(g, i, ny + 1, k), PIDX(g, i, ny, k), bc_kind(g, q, 3));
+          bc_set(&x, a, PIDX(g, i, 0, k), PIDX(g, i, 1, k), PIDX(g, i, 2, k), 2, k, vf ? vf[VFI(g, i, 0, k)] : 0.0);
+          bc_set(&x, a, PIDX(g, i, ny + 1, k), PIDX(g, i, ny, k), PIDX(g, i, ny - 1, k), 3, k,
+                 vf ? vf[VFI(g, i, ny, k)] : 0.0);
         }
     if (!g->per_z)
       for (int j = 1; j <= ny; ++j)
         for (int i = 1; i <= nx; ++i) {
-          bc_set(a, PIDX(g, i, j, 0), PIDX(g, i, j, 1), bc_kind(g, q, 4));
-          bc_set(a, PIDX(g, i, j, nz + 1), PIDX(g, i, j, nz), bc_kind(g, q, 5));
+          bc_set(&x, a, PIDX(g, i, j, 0), PIDX(g, i, j, 1), PIDX(g, i, j, 2), 4, 1, 0.0);
+          bc_set(&x, a, PIDX(g, i, j, nz + 1), PIDX(g, i, j, nz), PIDX(g, i, j, nz - 1), 5, nz, 0.0);
         }
   }
+}
+void ora_bound_cond(const ora_geom *g, int ncomp, int comp0, double *c) {
+  bound_cond(g, ncomp, comp0, c, g->bc_uf, g->bc_vf, g->bc_rho);
 }
 
 /* ADVECT/Advection_Mod.f90:2118-2125 k1F / k2F */
@@ -247,6 +282,62 @@ static void advection_compute_p(const ora_geom *g, const double *c, const double
           f[PR] = f[PR] + Flux;
           f[P] = f[P] - Flux;
         }
+      }
+  /* inflow through the faces of the outer walls, first-order upwind from
+   * the halo cell (:975-1044); the bottom divides by the interior density */
+  if (!g->per_x)
+    for (int k = 1; k <= nz; ++k)
+      for (int j = 1; j <= ny; ++j) {
+        size_t H = PIDX(g, 0, j, k);
+        double u = uf[UFI(g, 0, j, k)];
+        double Flux = HALF * (fabs(u) + u) * c[H] / (rho[H] + EPS) * g->fu[FUI(g, 0, j, k)];
+        f[PIDX(g, 1, j, k)] = f[PIDX(g, 1, j, k)] + Flux;
+        f[H] = 0.0;
+      }
+  if (!g->per_x)
+    for (int k = 1; k <= nz; ++k)
+      for (int j = 1; j <= ny; ++j) {
+        size_t H = PIDX(g, nx + 1, j, k);
+        double u = uf[UFI(g, nx, j, k)];
+        double Flux = HALF * (fabs(u) - u) * c[H] / (rho[H] + EPS) * g->fu[FUI(g, nx, j, k)];
+        f[PIDX(g, nx, j, k)] = f[PIDX(g, nx, j, k)] + Flux;
+        f[H] = 0.0;
+      }
+  if (!g->per_y)
+    for (int k = 1; k <= nz; ++k)
+      for (int i = 1; i <= nx; ++i) {
+        size_t H = PIDX(g, i, 0, k);
+        double v = vf[VFI(g, i, 0, k)];
+        double Flux = HALF * (fabs(v) + v) * c[H] / (rho[H] + EPS) * g->fv[FVI(g, i, 0, k)];
+        f[PIDX(g, i, 1, k)] = f[PIDX(g, i, 1, k)] + Flux;
+        f[H] = 0.0;
+      }
+  if (!g->per_y)
+    for (int k = 1; k <= nz; ++k)
+      for (int i = 1; i <= nx; ++i) {
+        size_t H = PIDX(g, i, ny + 1, k);
+        double v = vf[VFI(g, i, ny, k)];
+        double Flux = HALF * (fabs(v) - v) * c[H] / (rho[H] + EPS) * g->fv[FVI(g, i, ny, k)];
+        f[PIDX(g, i, ny, k)] = f[PIDX(g, i, ny, k)] + Flux;
+        f[H] = 0.0;
+      }
+  if (!g->per_z)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        size_t H = PIDX(g, i, j, 0), P = PIDX(g, i, j, 1);
+        double w = wf[WFI(g, i, j, 0)];
+        double Flux = HALF * (fabs(w) + w) * c[H] / (rho[P] + EPS) * g->fw[FWI(g, i, j, 0)];
+        f[P] = f[P] + Flux;
+        f[H] = 0.0;
+      }
+  if (!g->per_z)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        size_t H = PIDX(g, i, j, nz + 1);
+        double w = wf[WFI(g, i, j, nz)];
+        double Flux = HALF * (fabs(w) - w) * c[H] / (rho[H] + EPS) * g->fw[FWI(g, i, j, nz)];
+        f[PIDX(g, i, j, nz)] = f[PIDX(g, i, j, nz)] + Flux;
+        f[H] = 0.0;
       }
   /* zero-volume mask over the padded box, :1045-1051 */
   const size_t n = NPAD(g);
@@ -552,6 +643,20 @@ void ora_jac(const ora_geom *g, const double *rho, const double *uf, const doubl
         jac_face(val, n, iL, iR, 2, 4, uf[UFI(g, nx, j, k)], g->fu[FUI(g, nx, j, k)], V[iL] + EPS, V[iR] + EPS, rho[iL], rho[iR]);
       }
   }
+  else { /* 'ow', 'oe' (:2390-2410 and the east twin): the outflow diagonal of the interior cell */
+    for (int k = 1; k <= nz; ++k)
+      for (int j = 1; j <= ny; ++j) {
+        size_t P = PIDX(g, 1, j, k);
+        double u = uf[UFI(g, 0, j, k)], F = g->fu[FUI(g, 0, j, k)];
+        val[3 * n + P] = val[3 * n + P] - HALF * (fabs(u) - u) * F / (V[P] + EPS) / (rho[P] + EPS);
+      }
+    for (int k = 1; k <= nz; ++k)
+      for (int j = 1; j <= ny; ++j) {
+        size_t P = PIDX(g, nx, j, k);
+        double u = uf[UFI(g, nx, j, k)], F = g->fu[FUI(g, nx, j, k)];
+        val[3 * n + P] = val[3 * n + P] - HALF * (fabs(u) + u) * F / (V[P] + EPS) / (rho[P] + EPS);
+      }
+  }
   if (g->per_y) {
     for (int k = 1; k <= nz; ++k)
       for (int i = 1; i <= nx; ++i) {
@@ -564,6 +669,20 @@ void ora_jac(const ora_geom *g, const double *rho, const double *uf, const doubl
         jac_face(val, n, iL, iR, 1, 5, vf[VFI(g, i, ny, k)], g->fv[FVI(g, i, ny, k)], V[iL] + EPS, V[iR] + EPS, rho[iL], rho[iR]);
       }
   }
+  else { /* 'os', 'on' */
+    for (int k = 1; k <= nz; ++k)
+      for (int i = 1; i <= nx; ++i) {
+        size_t P = PIDX(g, i, 1, k);
+        double v = vf[VFI(g, i, 0, k)], F = g->fv[FVI(g, i, 0, k)];
+        val[3 * n + P] = val[3 * n + P] - HALF * (fabs(v) - v) * F / (V[P] + EPS) / (rho[P] + EPS);
+      }
+    for (int k = 1; k <= nz; ++k)
+      for (int i = 1; i <= nx; ++i) {
+        size_t P = PIDX(g, i, ny, k);
+        double v = vf[VFI(g, i, ny, k)], F = g->fv[FVI(g, i, ny, k)];
+        val[3 * n + P] = val[3 * n + P] - HALF * (fabs(v) + v) * F / (V[P] + EPS) / (rho[P] + EPS);
+      }
+  }
   if (g->per_z) {
     for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
@@ -574,6 +693,20 @@ void ora_jac(const ora_geom *g, const double *rho, const double *uf, const doubl
       for (int i = 1; i <= nx; ++i) {
         size_t iL = PIDX(g, i, j, nz), iR = PIDX(g, i, j, nz + 1);
         jac_face(val, n, iL, iR, 0, 6, wf[WFI(g, i, j, nz)], g->fw[FWI(g, i, j, nz)], V[iL] + EPS, V[iR] + EPS, rho[iL], rho[iR]);
+      }
+  }
+  else { /* 'ob', 'ot' */
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        size_t P = PIDX(g, i, j, 1);
+        double w = wf[WFI(g, i, j, 0)], F = g->fw[FWI(g, i, j, 0)];
+        val[3 * n + P] = val[3 * n + P] - HALF * (fabs(w) - w) * F / (V[P] + EPS) / (rho[P] + EPS);
+      }
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        size_t P = PIDX(g, i, j, nz);
+        double w = wf[WFI(g, i, j, nz)], F = g->fw[FWI(g, i, j, nz)];
+        val[3 * n + P] = val[3 * n + P] - HALF * (fabs(w) + w) * F / (V[P] + EPS) / (rho[P] + EPS);
       }
   }
   if (g->dh && g->jac_diff) jac_diffusion(g, rho, val);
@@ -944,7 +1077,7 @@ int ora_ros_step(const ora_geom *g, int ncomp, int rho_pos, double *c, const dou
   memcpy(cold, c, sizeof(double) * len);
   for (int is = 0; is < nStage; ++is) {
     ora_exchange_cell(g, ncomp, c);
-    ora_bound_cond(g, ncomp, 0, c); /* StageRos :287 BoundaryCondition */
+    bound_cond(g, ncomp, 0, c, uf, vf, rho_pos); /* StageRos :287 BoundaryCondition */
     if (is == 0) ora_jac(g, c + (size_t)rho_pos * n, uf, vf, wf, beta0, dt, val);
     ora_fcn(g, ncomp, rho_pos, c, uf, vf, wf, rhs);
     for (size_t i = 0; i < len; ++i) rhs[i] = dt * rhs[i]; /* ScaleV */

@@ -15,7 +15,8 @@ typedef struct {
   int per_x, per_y, per_z; /* 1 = periodic side pair, 0 = closed walls */
   const double *volc, *fu, *fv, *fw;
   /* halo rule of the outer walls per component and side (W,E,S,N,B,T):
-   * 0 none, 1 ZeroGrad, 2 ZeroValue; bc[6*ic + side].  NULL = ZeroGrad
+   * 0 none, 1 ZeroGrad, 2 ZeroValue, 3 MeanValue, 4 Function,
+   * 5 InFlowOutFlow, 6 Extrapolation; bc[6*ic + side].  NULL = ZeroGrad
    * everywhere, the default BCMetVec (MODULE/BoundaryCond_Mod.f90:240-247). */
   const int *bc;
   /* diffusion coefficients (DH horizontal, DV vertical; padded cell fields,
@@ -23,6 +24,13 @@ typedef struct {
    * diffusion Jacobian (JacDiffusion) to the stage matrix. */
   const double *dh, *dv;
   int jac_diff;
+  /* data of the open-boundary halo rules (kinds 3-6 of bc): MeanProfile
+   * (ncomp*nz, level iz at [ic*nz + iz-1]), the Function values at the halo
+   * cells (ncomp padded fields), the ambient state VecAmb (ncomp padded
+   * fields), the face velocities whose sign InFlowOutFlow tests and the
+   * density component; NULL where the kinds in use need none. */
+  const double *bc_mean, *bc_fval, *bc_amb, *bc_uf, *bc_vf;
+  int bc_rho;
 } ora_geom;
 
 #define NXP(g) ((g)->nx + 2)

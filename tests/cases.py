@@ -32,6 +32,26 @@ def _hill(nx, ny, nz, u0=10.0, v0=0.0, seed=2, height=600.0, halfwidth=800.0):
     return geo, vel, st
 
 
+def _channel(nx, ny, nz, u0=6.0, v0=1.5, seed=11):
+    """Flat block with outer walls on all sides and flow through them: inflow
+    on the west, outflow on the east, and face velocities of both signs on
+    the south/north walls, the ground and the lid (the open boundaries of
+    AdvectionComputeP and the InFlowOutFlow rule)."""
+    grid = G.Grid(nx, ny, nz, 100.0, 100.0, G.uniform_levels(nz, 100.0), False, False, False)
+    geo = G.cut_cell_geometry(grid, None, snap=0.0, merge=0.0)
+    uf, vf, wf = (a.copy() for a in G.face_velocity(geo, u0, v0))
+    rng = np.random.default_rng(seed)
+    uf *= 1.0 + 0.2 * rng.standard_normal(uf.shape)
+    vf[:, 0, :] = 2.0 * rng.standard_normal((nz, nx))
+    vf[:, -1, :] = 2.0 * rng.standard_normal((nz, nx))
+    wf[0] = 0.5 * rng.standard_normal((ny, nx))
+    wf[-1] = 0.5 * rng.standard_normal((ny, nx))
+    vel = (uf, vf, wf)
+    st = G.initial_state(geo, *vel, theta0=300.0, bubble_amp=2.0, bubble_radius=300.0, bubble_z=300.0, noise=0.01,
+                         seed=seed)
+    return geo, vel, st
+
+
 def _hill_closed(nx, ny, nz, seed=4, height=600.0, halfwidth=800.0):
     return G.closed_hill_case(nx, ny, nz, seed=seed, height=height, halfwidth=halfwidth)
 
@@ -77,6 +97,7 @@ PROJ_CASES = {
 
 
 CASES = {
+    "channel_open_10x7x6": lambda: _channel(10, 7, 6),
     "bubble_12x10x8": lambda: _flat(12, 10, 8),
     "hill_24x20x16": lambda: _hill(24, 20, 16),
     "hill_odd_13x7x9_reverse": lambda: _hill(13, 7, 9, u0=-7.0, v0=4.0, seed=5),

@@ -133,14 +133,35 @@ def fcn(geo, c, vel, rho_pos=0):
                                  (uR > 0, GxR, -1), (vL < 0, GyL, -1), (vR > 0, GyR, -1), (wL < 0, GzL, -1),
                                  (wR > 0, GzR, -1), (uR < 0, GxR, 1), (vR < 0, GyR, 1), (wR < 0, GzR, 1)):
             a = np.where(cond, a + term if sign > 0 else a - term, a)
+        # first-order inflow through the faces of the outer walls from the halo
+        # cells, W, E, S, N, B, T (the bottom divides by the interior density)
+        ci = c[ic]
+        if not g.periodic_x:
+            u = uf[:, :, 0]
+            a[:, :, 0] = a[:, :, 0] + 0.5 * (np.abs(u) + u) * ci[1:-1, 1:-1, 0] / (rho[1:-1, 1:-1, 0] + EPS) * geo.fu[:, :, 1]
+            u = uf[:, :, nx]
+            a[:, :, nx - 1] = (a[:, :, nx - 1] + 0.5 * (np.abs(u) - u) * ci[1:-1, 1:-1, nx + 1]
+                               / (rho[1:-1, 1:-1, nx + 1] + EPS) * geo.fu[:, :, nx + 1])
+        if not g.periodic_y:
+            v = vf[:, 0, :]
+            a[:, 0, :] = a[:, 0, :] + 0.5 * (np.abs(v) + v) * ci[1:-1, 0, 1:-1] / (rho[1:-1, 0, 1:-1] + EPS) * geo.fv[:, 1, :]
+            v = vf[:, ny, :]
+            a[:, ny - 1, :] = (a[:, ny - 1, :] + 0.5 * (np.abs(v) - v) * ci[1:-1, ny + 1, 1:-1]
+                               / (rho[1:-1, ny + 1, 1:-1] + EPS) * geo.fv[:, ny + 1, :])
+        if not g.periodic_z:
+            w = wf[0]
+            a[0] = a[0] + 0.5 * (np.abs(w) + w) * ci[0, 1:-1, 1:-1] / (rho[1, 1:-1, 1:-1] + EPS) * geo.fw[1]
+            w = wf[nz]
+            a[nz - 1] = a[nz - 1] + 0.5 * (np.abs(w) - w) * ci[nz + 1, 1:-1, 1:-1] / (rho[nz + 1, 1:-1, 1:-1] + EPS) * geo.fw[nz + 1]
         f[1:nz + 1, 1:ny + 1, 1:nx + 1] = a
-        # halo cells next to the interior
-        f[1:nz + 1, 1:ny + 1, 0] = np.where(uf[:, :, 0] < 0, gx[:, :, 0], 0.0)
-        f[1:nz + 1, 1:ny + 1, nx + 1] = np.where(uf[:, :, nx] > 0, gx[:, :, nx], 0.0)
-        f[1:nz + 1, 0, 1:nx + 1] = np.where(vf[:, 0, :] < 0, gy[:, 0, :], 0.0)
-        f[1:nz + 1, ny + 1, 1:nx + 1] = np.where(vf[:, ny, :] > 0, gy[:, ny, :], 0.0)
-        f[0, 1:ny + 1, 1:nx + 1] = np.where(wf[0] < 0, gz[0], 0.0)
-        f[nz + 1, 1:ny + 1, 1:nx + 1] = np.where(wf[nz] > 0, gz[nz], 0.0)
+        # halo cells next to the interior: the outflow a periodic side hands on;
+        # an outer wall's halo is zeroed
+        f[1:nz + 1, 1:ny + 1, 0] = np.where(uf[:, :, 0] < 0, gx[:, :, 0], 0.0) if g.periodic_x else 0.0
+        f[1:nz + 1, 1:ny + 1, nx + 1] = np.where(uf[:, :, nx] > 0, gx[:, :, nx], 0.0) if g.periodic_x else 0.0
+        f[1:nz + 1, 0, 1:nx + 1] = np.where(vf[:, 0, :] < 0, gy[:, 0, :], 0.0) if g.periodic_y else 0.0
+        f[1:nz + 1, ny + 1, 1:nx + 1] = np.where(vf[:, ny, :] > 0, gy[:, ny, :], 0.0) if g.periodic_y else 0.0
+        f[0, 1:ny + 1, 1:nx + 1] = np.where(wf[0] < 0, gz[0], 0.0) if g.periodic_z else 0.0
+        f[nz + 1, 1:ny + 1, 1:nx + 1] = np.where(wf[nz] > 0, gz[nz], 0.0) if g.periodic_z else 0.0
         f = f * V / (V + EPS)
         if g.periodic_x:
             f[1:nz + 1, 1:ny + 1, 1] = f[1:nz + 1, 1:ny + 1, 1] + f[1:nz + 1, 1:ny + 1, nx + 1]
@@ -170,14 +191,16 @@ def upwind_rhs(geo, c, vel, rho):
     px = np.where(uf > 0, uf * fu * phi[K, J, 0:nx + 1], uf * fu * phi[K, J, 1:nx + 2])
     py = np.where(vf > 0, vf * fv * phi[K, 0:ny + 1, I], vf * fv * phi[K, 1:ny + 2, I])
     pz = np.where(wf > 0, wf * fw * phi[0:nz + 1, J, I], wf * fw * phi[1:nz + 2, J, I])
+    # an outer wall keeps the outflow of the interior cell (the inflow from
+    # the halo does not depend on the interior state)
     if not g.periodic_x:
-        px[:, :, 0] = 0
-        px[:, :, nx] = 0
+        px[:, :, 0] = np.minimum(px[:, :, 0], 0.0)
+        px[:, :, nx] = np.maximum(px[:, :, nx], 0.0)
     if not g.periodic_y:
-        py[:, 0, :] = 0
-        py[:, ny, :] = 0
-    pz[0] = 0
-    pz[nz] = 0
+        py[:, 0, :] = np.minimum(py[:, 0, :], 0.0)
+        py[:, ny, :] = np.maximum(py[:, ny, :], 0.0)
+    pz[0] = np.minimum(pz[0], 0.0)
+    pz[nz] = np.maximum(pz[nz], 0.0)
     acc = (px[:, :, :-1] - px[:, :, 1:]) + (py[:, :-1, :] - py[:, 1:, :]) + (pz[:-1] - pz[1:])
     out[K, J, I] = acc / (V[K, J, I] + EPS)
     return out
@@ -322,29 +345,51 @@ CPD, CVD, CPV, RV, CPL, CPI, P0 = 1004.0, 717.0, 1885.0, 461.0, 4186.0, 2110.0, 
 RD = CPD - CVD
 
 
-def bound_cond(c, kinds, periodic=(False, False, False)):
-    """BoundaryCompute ZeroGrad/ZeroValue on the face halos of the non-periodic
-    sides (ADVECT/BoundaryCondition_Mod.f90:70-346); c (ncomp, NZ, NY, NX)."""
+def bound_cond(c, kinds, periodic=(False, False, False), mean=None, fval=None, amb=None, vel=None, rho_pos=0):
+    """BoundaryCompute on the face halos of the non-periodic sides
+    (ADVECT/BoundaryCondition_Mod.f90:70-346); c (ncomp, NZ, NY, NX).  Kinds
+    1 ZeroGrad, 2 ZeroValue, 3 MeanValue (mean (ncomp, nz)), 4 Function
+    (fval: the halo values F), 5 InFlowOutFlow on the lateral sides (amb: the
+    ambient state, vel: the face velocities), 6 Extrapolation on the bottom
+    and top; components in order."""
     out = c.copy()
-    sgn = {1: 1.0, 2: -1.0}
+    nz = c.shape[1] - 2
     for ic in range(c.shape[0]):
         a = out[ic]
         k = kinds[ic]
+        rho = out[rho_pos]
+        # (side, halo index, interior index, next interior index) per side
+        sides = []
         if not periodic[0]:
-            if k[0] in sgn:
-                a[1:-1, 1:-1, 0] = sgn[k[0]] * a[1:-1, 1:-1, 1]
-            if k[1] in sgn:
-                a[1:-1, 1:-1, -1] = sgn[k[1]] * a[1:-1, 1:-1, -2]
+            sides += [(0, np.s_[1:-1, 1:-1, 0], np.s_[1:-1, 1:-1, 1], np.s_[1:-1, 1:-1, 2]),
+                      (1, np.s_[1:-1, 1:-1, -1], np.s_[1:-1, 1:-1, -2], np.s_[1:-1, 1:-1, -3])]
         if not periodic[1]:
-            if k[2] in sgn:
-                a[1:-1, 0, 1:-1] = sgn[k[2]] * a[1:-1, 1, 1:-1]
-            if k[3] in sgn:
-                a[1:-1, -1, 1:-1] = sgn[k[3]] * a[1:-1, -2, 1:-1]
+            sides += [(2, np.s_[1:-1, 0, 1:-1], np.s_[1:-1, 1, 1:-1], np.s_[1:-1, 2, 1:-1]),
+                      (3, np.s_[1:-1, -1, 1:-1], np.s_[1:-1, -2, 1:-1], np.s_[1:-1, -3, 1:-1])]
         if not periodic[2]:
-            if k[4] in sgn:
-                a[0, 1:-1, 1:-1] = sgn[k[4]] * a[1, 1:-1, 1:-1]
-            if k[5] in sgn:
-                a[-1, 1:-1, 1:-1] = sgn[k[5]] * a[-2, 1:-1, 1:-1]
+            sides += [(4, np.s_[0, 1:-1, 1:-1], np.s_[1, 1:-1, 1:-1], np.s_[2, 1:-1, 1:-1]),
+                      (5, np.s_[-1, 1:-1, 1:-1], np.s_[-2, 1:-1, 1:-1], np.s_[-3, 1:-1, 1:-1])]
+        for side, H, S, S2 in sides:
+            kind = k[side]
+            if kind == 1:
+                a[H] = a[S]
+            elif kind == 2:
+                a[H] = -a[S]
+            elif kind == 3:
+                if side < 4:
+                    prof = mean[ic][:, None]
+                else:
+                    prof = mean[ic][0 if side == 4 else nz - 1]
+                a[H] = 2.0 * prof - a[S]
+            elif kind == 4:
+                a[H] = 2.0 * fval[ic][H] - a[S]
+            elif kind == 5 and side < 4:
+                uf, vf = vel[0], vel[1]
+                u = {0: uf[:, :, 0], 1: uf[:, :, -1], 2: vf[:, 0, :], 3: vf[:, -1, :]}[side]
+                inflow = u <= 0 if side & 1 else u >= 0
+                a[H] = np.where(inflow, rho[H] * amb[ic][H], a[S])
+            elif kind == 6 and side >= 4:
+                a[H] = 2.0 * a[S] - a[S2]
     return out
 
 

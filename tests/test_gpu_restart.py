@@ -88,3 +88,43 @@ def test_large_arrays_through_the_staging_chunks(built_lib, tmp_path, max_sub):
     torch.cuda.synchronize()
     assert torch.equal(c2, c) and torch.equal(uf2, uf) and torch.equal(wf2, wf)
     assert np.array_equal(vf2, host_vf)
+
+
+def test_weight2_refuses_device_arrays(built_lib, tmp_path):
+    """The .Weight2 routines take host arrays: a device array in a block to
+    write or to fill is refused with ASAM_BAD_ARG before any file is made
+    or any array is touched."""
+    import ctypes as C
+
+    torch = pytest.importorskip("torch")
+    from asam_gb300 import _lib
+    from asam_gb300 import weights as W
+
+    geo = cases.get("hill_24x20x16")[0]
+    p = tmp_path / "h.Weight2"
+    W.write_weight2(str(p), [geo])
+    lib = _lib.load()
+    opt = _lib.AsamWeight2Options()
+    opt.periodic[:] = [1, 1, 0]
+    opt.nr_soil_layers, opt.land_class_def = 7, 5
+    info, h = _lib.AsamWeight2Block(), C.c_void_p()
+    assert lib.asam_weight2_open(str(p).encode(), 1, C.byref(opt), C.byref(h), C.byref(info)) == _lib.ASAM_OK
+    try:
+        nx, ny, nz = info.nx, info.ny, info.nz
+        fu = torch.zeros((nz, ny, nx + 3), dtype=torch.float64, device="cuda")
+        dst = _lib.AsamWeight2Block()
+        dst.fu = fu.data_ptr()
+        assert lib.asam_weight2_fetch(h, C.byref(dst)) == _lib.ASAM_BAD_ARG
+        torch.cuda.synchronize()
+        assert not fu.any().item()
+    finally:
+        lib.asam_weight2_close(h)
+    b = W.read_weight2(str(p))
+    keep = []
+    desc = W._describe(b, keep)
+    dz = torch.from_numpy(b.dz).cuda()
+    desc.dz = dz.data_ptr()
+    q = tmp_path / "refused.Weight2"
+    per = (C.c_int * 3)(1, 1, 0)
+    assert lib.asam_weight2_write(str(q).encode(), 1, C.byref(desc), per) == _lib.ASAM_BAD_ARG
+    assert not q.exists()
