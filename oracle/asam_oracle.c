@@ -26,10 +26,12 @@
  *   MODULE/Vector4Cell_Mod.f90:1030-1036.
  *
  * Boundary handling covered: periodic sides ('iw'/'ie'/'is'/'in' neighbours
- * that are the block itself) and closed walls (outer sides 'ow'...'ot' with
- * zero normal face velocity), whose halo cells the stage driver sets with the
- * ZeroGrad / ZeroValue rules of BoundaryCondition.  Inflow ('Function'),
- * 'MeanValue' and refined-neighbour branches are not restated.
+ * that are the block itself) and outer walls ('ow'...'ot'), closed or with
+ * flow through them (the first-order inflow of AdvectionComputeP and the
+ * outflow term of JacAdvectionCompute), whose halo cells the stage driver
+ * sets with the rules of BoundaryCompute (ZeroGrad, ZeroValue, MeanValue,
+ * Function, InFlowOutFlow, Extrapolation).  Refined-neighbour branches are
+ * not restated.
  *
  * Build with -O2 -ffp-contract=off (no FMA contraction, like gfortran on
  * x86-64 without -march).
