@@ -562,9 +562,110 @@ __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_grou
 template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// One half-sweep of the line solves with K lanes per line (FP32 copy only:
+// the refined mode's preconditioner need not reproduce the reference's
+// rounding).  On the coarsest plane levels a half-sweep has a handful of
+// lines, and one thread per line left most of the block waiting at the
+// barrier while a 128-row recurrence ran.  Both recurrences of the factored line system --
+// forward y(i) = (t(i) - lz(i-1)*y(i-1))/ft(i) (the coupling of row i is
+// stored at row i-1), backward x(i) = y(i) - fw(i)*x(i+1) -- are first-order
+// affine recurrences, so each lane composes
+// the affine map of its chunk of rows, a shuffle scan over the K lanes gives
+// every chunk its entry value, and each lane re-runs its chunk with the
+// sequential formulas (a chunked scan).  The line right-hand side t(i) is the
+// one of the sequential sweep, neighbour lines and wrap couplings included.
+template <typename T, bool kWrap>
+__device__ void line_half_lanes(const Lev2T<T>& P, size_t mo, const T* __restrict__ b, T* __restrict__ x, int c,
+                                int fwd, int K) {
+  const int c1 = P.c1, c2 = P.c2, h = P.h, w = P.w;
+  const T* __restrict__ lx = P.lx + mo;
+  const T* __restrict__ ux = P.ux + mo;
+  const T* __restrict__ lz = P.lz + mo;
+  const T* __restrict__ ft = P.ft + mo;
+  const T* __restrict__ frt = P.frt + mo;
+  const T* __restrict__ fw = P.fw + mo;
+  const int nl = (c2 - c + 1) / 2;
+  const int q = threadIdx.x / K, p = threadIdx.x % K;
+  const bool active = q < nl;
+  const int j = 2 * q + c;
+  const size_t col = (size_t)c * h + q;
+  const bool hasL = j > 0, hasR = j < c2 - 1;
+  const size_t colL = hasL ? (size_t)(1 - c) * h + ((j - 1) >> 1) : col;
+  const size_t colR = hasR ? (size_t)(1 - c) * h + ((j + 1) >> 1) : col;
+  const bool wrap = kWrap && P.wxl && c2 >= 2 && ((c2 - 1) & 1);
+  const bool wL = wrap && j == 0, wR = wrap && j == c2 - 1;
+  const bool useL = hasL || wL, useR = hasR || wR;
+  const size_t wk = (mo / P.ps) * (size_t)c1;
+  const size_t xL0 = wL ? slot(0, h, 0, c2 - 1) : colL, xR0 = wR ? slot(0, h, 0, 0) : colR;
+  const int rows = (c1 + K - 1) / K;
+  const int r0 = active ? min(c1, p * rows) : 0, r1 = active ? min(c1, r0 + rows) : 0;
+  auto rhs = [&](int i) {
+    const size_t o = (size_t)i * w;
+    T t = b[col + o];
+    const T xl = useL ? x[xL0 + o] : (T)0, cl = useL ? (wL ? P.wxl[wk + i] : lx[colL + o]) : (T)0;
+    const T xr = useR ? x[xR0 + o] : (T)0, cr = useR ? (wR ? P.wxh[wk + i] : ux[col + o]) : (T)0;
+    if (fwd) {
+      if (useL) t = t - cl * xl;
+      if (useR) t = t - cr * xr;
+    } else {
+      if (useR) t = t - cr * xr;
+      if (useL) t = t - cl * xl;
+    }
+    return t;
+  };
+  // forward: the chunk's map y(r1-1) = A*y(r0-1) + B
+  T A = (T)1, B = (T)0;
+  for (int i = r0; i < r1; ++i) {
+    const T ri = frt[col + (size_t)i * w];
+    const T a = i > 0 ? -(lz[col + (size_t)(i - 1) * w] * ri) : (T)0;  // row i's coupling is stored at row i-1
+    A = a * A;
+    B = a * B + rhs(i) * ri;
+  }
+  for (int off = 1; off < K; off <<= 1) {  // inclusive scan over the lanes, chunk 0 first
+    const T Ap = __shfl_up_sync(0xffffffffu, A, off, K), Bp = __shfl_up_sync(0xffffffffu, B, off, K);
+    if (p >= off) B = A * Bp + B, A = A * Ap;
+  }
+  T prev = __shfl_up_sync(0xffffffffu, B, 1, K);  // y before the chunk (the whole line starts from 0)
+  if (p == 0) prev = (T)0;
+  for (int i = r0; i < r1; ++i) {
+    T t = rhs(i);
+    if (i > 0) t = t - lz[col + (size_t)(i - 1) * w] * prev;
+    const T y = div_rn(t, ft[col + (size_t)i * w], frt[col + (size_t)i * w]);
+    x[col + (size_t)i * w] = y;
+    prev = y;
+  }
+  // backward: the chunk's map x(r0) = A*x(r1) + B (row c1-1 takes y alone)
+  A = (T)1, B = (T)0;
+  for (int i = r1 - 1; i >= r0; --i) {
+    const T a = i < c1 - 1 ? -fw[col + (size_t)i * w] : (T)0;
+    A = a * A;
+    B = a * B + x[col + (size_t)i * w];
+  }
+  for (int off = 1; off < K; off <<= 1) {  // inclusive scan from the last chunk down
+    const T An = __shfl_down_sync(0xffffffffu, A, off, K), Bn = __shfl_down_sync(0xffffffffu, B, off, K);
+    if (p + off < K) B = A * Bn + B, A = A * An;
+  }
+  T next = __shfl_down_sync(0xffffffffu, B, 1, K);  // x after the chunk
+  for (int i = r1 - 1; i >= r0; --i) {
+    const T y = x[col + (size_t)i * w];
+    const T v = i < c1 - 1 ? y - fw[col + (size_t)i * w] * next : y;
+    x[col + (size_t)i * w] = v;
+    next = v;
+  }
+}
+
 template <typename T, bool kWrap = false>
 __device__ __noinline__ void line_half(const Lev2T<T>& P, size_t mo, const T* __restrict__ b, T* __restrict__ x, int c,
                                        int fwd, T* __restrict__ ring) {
+  if constexpr (sizeof(T) == 4) {  // few lines: K lanes per line (the whole block takes part in the shuffles)
+    const int nl = (P.c2 - c + 1) / 2;
+    int K = 1;
+    while (K < 32 && nl * K * 2 <= (int)blockDim.x && K * 4 <= P.c1) K *= 2;
+    if (K >= 8) {  // from 8 lanes up; with 2-4 lanes the prefetched sequential sweep below was faster
+      line_half_lanes<T, kWrap>(P, mo, b, x, c, fwd, K);
+      return;
+    }
+  }
   const int c1 = P.c1, c2 = P.c2, h = P.h, w = P.w;
   const T* __restrict__ lx = P.lx + mo;
   const T* __restrict__ ux = P.ux + mo;
