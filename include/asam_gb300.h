@@ -554,14 +554,17 @@ int asam_probe_fp64_fma(int iters, double *gflops);
 int asam_probe_div(long long n, long long seed, int span, long long *mismatches);
 
 /* Batched block-tridiagonal column solve of the density/buoyancy-coupled
- * line preconditioner (MultiTriTB): Solve_1D of MULTI/TriDiagTB_Mod.f90:143-163,
+ * line preconditioners (MultiTriTB, MultiTriTR): Solve_1D of
+ * MULTI/TriDiagTB_Mod.f90:143-163, which MULTI/TriDiagTR_Mod.f90:155-175
+ * repeats statement for statement,
  * a Thomas elimination with 2x2 blocks (Div_2, Div_22, Mult_2, Mult_22 of
  * CG/Matrix_Mod.f90), over ncol independent columns of n1 levels.
  * d[(col*n1+i)*4 + r+2c] = A%d(r+1,c+1,i+1); u, l[(col*(n1-1)+i)*4 + r+2c];
  * b[(col*n1+i)*2 + r] overwritten by the solution.  Host or device pointers. */
 int asam_tri_tb_solve(int ncol, int n1, const double *d, const double *u, const double *l, double *b);
 
-/* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141). */
+/* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141),
+ * the same as MatVecTR_1D (MULTI/TriDiagTR_Mod.f90:133-153). */
 int asam_tri_tb_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x,
                        double *y);
 
