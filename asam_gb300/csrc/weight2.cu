@@ -34,6 +34,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "context.h"
@@ -70,6 +71,25 @@ class ListReader {
     *s = p_;
     *e = (le > p_ && le[-1] == '\r') ? le - 1 : le;
     p_ = q ? q + 1 : end_;
+    return true;
+  }
+
+  const char* pos() const { return p_; }
+  const char* end() const { return end_; }
+  void seek(const char* p) { p_ = p; }
+
+  // one READ of n values that must all stand on the current line (the
+  // writers' layout); false, without an error text, when they do not
+  bool read_line(Tok* out, int n) {
+    const char* save = p_;
+    const char *s, *e;
+    if (!line(&s, &e)) return false;
+    ListReader one(s, e);
+    std::string err;
+    if (!one.read(out, n, &err)) {
+      p_ = save;
+      return false;
+    }
     return true;
   }
 
@@ -198,38 +218,61 @@ long long locate(int a, int nx, int ny, int nz, long long ix, long long iy, long
   return (k * ey + j) * ex + i;
 }
 
+int host_threads();
+
+// f(k0, k1) over the slices of [0, n) on the host threads
+template <typename F>
+void for_slices(long long n, F f) {
+  const int nth = n >= 16 ? host_threads() : 1;
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nth; ++t) pool.emplace_back(f, n * t / nth, n * (t + 1) / nth);
+  f(0LL, n / nth);
+  for (auto& th : pool) th.join();
+}
+
 // The reader's Cartesian weights before the file's lists are applied
 // (ReadWeights_Mod.f90:633-640, 893-1000); products in the reader's order.
 void default_weights(const std::vector<double>& dx, const std::vector<double>& dy, const std::vector<double>& dz,
                      const int periodic[3], std::vector<double>* fu, std::vector<double>* fv,
                      std::vector<double>* fw, std::vector<double>* volc) {
   const long long nx = (long long)dx.size(), ny = (long long)dy.size(), nz = (long long)dz.size();
+  // every element is written below (the halo edges and corners of VolC = 1)
   fu->resize(size_t((nx + 3) * ny * nz));
   fv->resize(size_t(nx * (ny + 3) * nz));
   fw->resize(size_t(nx * ny * (nz + 3)));
-  volc->assign(size_t((nx + 2) * (ny + 2) * (nz + 2)), 1.0);
-  for (long long k = 0; k < nz; ++k)
-    for (long long j = 0; j < ny; ++j) {
-      const double a = dz[k] * dy[j];
-      double* r = fu->data() + (k * ny + j) * (nx + 3);
-      for (long long i = 0; i < nx + 3; ++i) r[i] = a;
-    }
-  for (long long k = 0; k < nz; ++k)
-    for (long long j = 0; j < ny + 3; ++j) {
-      double* r = fv->data() + (k * (ny + 3) + j) * nx;
-      for (long long i = 0; i < nx; ++i) r[i] = dz[k] * dx[i];
-    }
-  for (long long k = 0; k < nz + 3; ++k)
-    for (long long j = 0; j < ny; ++j) {
-      double* r = fw->data() + (k * ny + j) * nx;
-      for (long long i = 0; i < nx; ++i) r[i] = dy[j] * dx[i];
-    }
+  volc->resize(size_t((nx + 2) * (ny + 2) * (nz + 2)));
+  for_slices(nz, [&](long long k0, long long k1) {
+    for (long long k = k0; k < k1; ++k)
+      for (long long j = 0; j < ny; ++j) {
+        const double a = dz[k] * dy[j];
+        double* r = fu->data() + (k * ny + j) * (nx + 3);
+        for (long long i = 0; i < nx + 3; ++i) r[i] = a;
+      }
+    for (long long k = k0; k < k1; ++k)
+      for (long long j = 0; j < ny + 3; ++j) {
+        double* r = fv->data() + (k * (ny + 3) + j) * nx;
+        for (long long i = 0; i < nx; ++i) r[i] = dz[k] * dx[i];
+      }
+  });
+  for_slices(nz + 3, [&](long long k0, long long k1) {
+    for (long long k = k0; k < k1; ++k)
+      for (long long j = 0; j < ny; ++j) {
+        double* r = fw->data() + (k * ny + j) * nx;
+        for (long long i = 0; i < nx; ++i) r[i] = dy[j] * dx[i];
+      }
+  });
   const long long sx = nx + 2, sy = ny + 2;
   double* v = volc->data();
   auto at = [&](long long k, long long j, long long i) -> double& { return v[(k * sy + j) * sx + i]; };
-  for (long long k = 1; k <= nz; ++k)
-    for (long long j = 1; j <= ny; ++j)
-      for (long long i = 1; i <= nx; ++i) at(k, j, i) = dx[i - 1] * dy[j - 1] * dz[k - 1];
+  for_slices(nz + 2, [&](long long k0, long long k1) {
+    for (long long k = k0; k < k1; ++k) {
+      double* pl = v + k * sy * sx;
+      std::fill(pl, pl + sy * sx, 1.0);
+      if (k < 1 || k > nz) continue;
+      for (long long j = 1; j <= ny; ++j)
+        for (long long i = 1; i <= nx; ++i) at(k, j, i) = dx[i - 1] * dy[j - 1] * dz[k - 1];
+    }
+  });
   const double dxw = periodic[0] ? dx[nx - 1] : dx[0], dxe = periodic[0] ? dx[0] : dx[nx - 1];
   const double dys = periodic[1] ? dy[ny - 1] : dy[0], dyn = periodic[1] ? dy[0] : dy[ny - 1];
   const double dzb = periodic[2] ? dz[nz - 1] : dz[0], dzt = periodic[2] ? dz[0] : dz[nz - 1];
@@ -283,6 +326,74 @@ void normals(Block& B) {
     const double a = m1 * ddx, b = m2 * ddy, c = m3 * ddz;
     B.dl[q] = 0.5 * std::sqrt(a * a + b * b + c * c);
   }
+}
+
+int host_threads() {
+  const unsigned hw = std::thread::hardware_concurrency();
+  return (int)std::max(1u, std::min(hw, 16u));
+}
+
+// The cnt pairs of READs 'ix iy iz' / value after a weight count, parsed by
+// several threads when every READ finds its values on its own line (the
+// layout both writers produce): the 2*cnt lines are cut into chunks at pair
+// boundaries, each thread parses its chunk into (index, value) entries, and
+// the entries are applied in file order (a repeated index keeps the last
+// value, as the sequential READs do).  False leaves the reader where it was
+// and the caller parses the pairs one READ at a time, which also gives the
+// exact error of a malformed pair.
+bool pairs_parallel(ListReader& rd, long long cnt, int a, int nx, int ny, int nz, double* dst) {
+  const int nth = host_threads();
+  if (cnt < (1 << 16) || nth < 2) return false;
+  const char* start = rd.pos();
+  const long long lines = 2 * cnt;
+  const long long per = ((lines / nth) + 1) & ~1LL;  // even: chunks begin at a pair
+  std::vector<const char*> cut{start};
+  ListReader scan(start, rd.end());
+  for (long long L = 0; L < lines; ++L) {
+    const char *s, *e;
+    if (!scan.line(&s, &e)) return false;
+    if ((L + 1) % per == 0 && L + 1 < lines) cut.push_back(scan.pos());
+  }
+  const char* q = scan.pos();
+  cut.push_back(q);
+  const int nch = (int)cut.size() - 1;
+  std::vector<std::vector<std::pair<long long, double>>> got(nch);
+  std::vector<char> ok(nch, 1);
+  auto work = [&](int t) {
+    ListReader r(cut[t], cut[t + 1]);
+    Tok tk[3];
+    auto& out = got[t];
+    out.reserve(size_t(per / 2 + 1));
+    while (r.pos() < cut[t + 1]) {
+      long long v[3];
+      double w;
+      if (!r.read_line(tk, 3) || !to_int(tk[0], &v[0]) || !to_int(tk[1], &v[1]) || !to_int(tk[2], &v[2]) ||
+          !r.read_line(tk, 1) || !to_real(tk[0], &w)) {
+        ok[t] = 0;
+        return;
+      }
+      const long long at = locate(a, nx, ny, nz, v[0], v[1], v[2]);
+      if (at < 0) {
+        ok[t] = 0;
+        return;
+      }
+      out.emplace_back(at, w);
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nch; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+  long long n = 0;
+  for (int t = 0; t < nch; ++t) {
+    if (!ok[t]) return false;
+    n += (long long)got[t].size();
+  }
+  if (n != cnt) return false;
+  for (int t = 0; t < nch; ++t)
+    for (const auto& e : got[t]) dst[e.first] = e.second;
+  rd.seek(q);
+  return true;
 }
 
 int parse(const char* buf, size_t size, int ib, const asam_weight2_options& o, Block& B) {
@@ -343,6 +454,7 @@ int parse(const char* buf, size_t size, int ib, const asam_weight2_options& o, B
     RD(1);
     if (!num_i(0, &cnt) || cnt < 0) return io("bad entry count");
     double* dst = arrs[a]->data();
+    if (pairs_parallel(rd, cnt, a, nx, ny, nz, dst)) return ASAM_OK;
     for (long long q = 0; q < cnt; ++q) {
       long long ix, iy, iz;
       double v;
@@ -444,6 +556,24 @@ int parse(const char* buf, size_t size, int ib, const asam_weight2_options& o, B
 }
 
 // ------------------------------------------------------------ writer
+void put_int(std::string& o, long long v, int width = 0) {
+  char tmp[32];
+  const char* e = std::to_chars(tmp, tmp + sizeof(tmp), v).ptr;
+  for (int pad = width - int(e - tmp); pad > 0; --pad) o.push_back(' ');
+  o.append(tmp, size_t(e - tmp));
+}
+// the shortest decimal that reads back to the same double (to_chars), with
+// a decimal point kept on integral values
+void put_real(std::string& o, double v) {
+  char tmp[40];
+  char* e = std::to_chars(tmp, tmp + sizeof(tmp) - 2, v).ptr;
+  bool plain = true;
+  for (const char* c = tmp; c < e; ++c)
+    if (*c == '.' || *c == 'e' || *c == 'n' || *c == 'i') plain = false;
+  if (plain) *e++ = '.', *e++ = '0';
+  o.append(tmp, size_t(e - tmp));
+}
+
 class Out {
  public:
   explicit Out(FILE* f) : f_(f) { buf_.reserve(kFlush + 4096); }
@@ -454,21 +584,17 @@ class Out {
   void put(const char* s) { put(s, strlen(s)); }
   void put(const std::string& s) { put(s.data(), s.size()); }
   void integer(long long v, int width = 0) {
-    char tmp[32];
-    const char* e = std::to_chars(tmp, tmp + sizeof(tmp), v).ptr;
-    for (int pad = width - int(e - tmp); pad > 0; --pad) buf_.push_back(' ');
-    put(tmp, size_t(e - tmp));
+    put_int(buf_, v, width);
+    if (buf_.size() >= kFlush) flush();
   }
-  // the shortest decimal that reads back to the same double (to_chars), with
-  // a decimal point kept on integral values
   void real(double v) {
-    char tmp[40];
-    char* e = std::to_chars(tmp, tmp + sizeof(tmp) - 2, v).ptr;
-    bool plain = true;
-    for (const char* c = tmp; c < e; ++c)
-      if (*c == '.' || *c == 'e' || *c == 'n' || *c == 'i') plain = false;
-    if (plain) *e++ = '.', *e++ = '0';
-    put(tmp, size_t(e - tmp));
+    put_real(buf_, v);
+    if (buf_.size() >= kFlush) flush();
+  }
+  // a large finished piece: flushed, then written as it is
+  void put_large(const std::string& t) {
+    flush();
+    if (!t.empty() && fwrite(t.data(), 1, t.size(), f_) != t.size()) ok_ = false;
   }
   bool flush() {
     if (!buf_.empty() && fwrite(buf_.data(), 1, buf_.size(), f_) != buf_.size()) ok_ = false;
@@ -534,31 +660,49 @@ void write_block(Out& out, const asam_weight2_block& b, int ib, const int period
   const double* arr[4] = {b.fu, b.fv, b.fw, b.volc};
   static const char* kCount[4] = {"NrW_FacesYZ", "NrW_FacesZX", "NrW_FacesXY", "NrW_Cells"};
   static const char* kMid[3] = {"NrMP_FacesYZ", "NrMP_FacesZX", "NrMP_FacesXY"};
+  // the weights that differ from the defaults, formatted by several threads
+  // over slices of the array and written in index order
   auto entries = [&](int a) {
     long long ex, ey, ez;
     extents(a, b.nx, b.ny, b.nz, &ex, &ey, &ez);
     const double* v = arr[a];
     const double* r = ref[a].data();
     const long long n = ex * ey * ez;
-    long long cnt = 0;
-    for (long long q = 0; q < n; ++q) cnt += v[q] != r[q];
+    const int nth = n >= (1 << 18) ? host_threads() : 1;
+    std::vector<std::string> text(nth);
+    std::vector<long long> cnt(nth, 0);
+    auto work = [&](int t) {
+      const long long q0 = n * t / nth, q1 = n * (t + 1) / nth;
+      std::string& o = text[t];
+      for (long long q = q0; q < q1; ++q) {
+        if (!(v[q] != r[q])) continue;
+        const long long i = q % ex, j = (q / ex) % ey, k = q / (ex * ey);
+        o.push_back(' ');
+        put_int(o, i - kOff[a][0]);
+        o.push_back(' ');
+        put_int(o, j - kOff[a][1]);
+        o.push_back(' ');
+        put_int(o, k - kOff[a][2]);
+        o.append("\n ");
+        put_real(o, v[q]);
+        o.push_back('\n');
+        ++cnt[t];
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nth; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto& th : pool) th.join();
+    long long total = 0;
+    for (long long c : cnt) total += c;
     out.put(" ");
-    out.integer(cnt);
+    out.integer(total);
     out.put(a == kVol ? "    " : "   ");
     out.put(kCount[a]);
     out.put("\n");
-    for (long long q = 0; q < n; ++q) {
-      if (!(v[q] != r[q])) continue;
-      const long long i = q % ex, j = (q / ex) % ey, k = q / (ex * ey);
-      out.put(" ");
-      out.integer(i - kOff[a][0]);
-      out.put(" ");
-      out.integer(j - kOff[a][1]);
-      out.put(" ");
-      out.integer(k - kOff[a][2]);
-      out.put("\n ");
-      out.real(v[q]);
-      out.put("\n");
+    for (auto& t : text) {
+      out.put_large(t);
+      std::string().swap(t);
     }
   };
   for (int a = 0; a < 3; ++a) {
@@ -646,15 +790,21 @@ int asam_weight2_open(const char* path, int ib, const asam_weight2_options* opt,
   FILE* f = fopen(path, "rb");
   if (!f) return fail(ASAM_IO_ERROR, std::string("Weight2: cannot open ") + path);
   std::vector<char> text;
-  char chunk[1 << 16];
+  long sz = -1;
   if (fseek(f, 0, SEEK_END) == 0) {
-    const long sz = ftell(f);
-    if (sz > 0) text.reserve(size_t(sz));
+    sz = ftell(f);
     fseek(f, 0, SEEK_SET);
   }
-  size_t got;
-  while ((got = fread(chunk, 1, sizeof(chunk), f)) > 0) text.insert(text.end(), chunk, chunk + got);
-  const bool bad = ferror(f) != 0;
+  bool bad = false;
+  if (sz >= 0) {  // one read into a buffer of the file's size
+    text.resize(size_t(sz));
+    bad = fread(text.data(), 1, text.size(), f) != text.size();
+  } else {  // not seekable: in chunks
+    char chunk[1 << 16];
+    size_t got;
+    while ((got = fread(chunk, 1, sizeof(chunk), f)) > 0) text.insert(text.end(), chunk, chunk + got);
+    bad = ferror(f) != 0;
+  }
   fclose(f);
   if (bad) return fail(ASAM_IO_ERROR, std::string("Weight2: read error on ") + path);
   asam_weight2_file* h = new asam_weight2_file();

@@ -366,3 +366,34 @@ def test_soil_classes_round_trip(tmp_path, sb):
     else:
         assert (got.land_class == W.LAND_CLASS_DEF).all() and (got.surf[:, 0] == 0.05).all()
     assert np.array_equal(got.surf[:, 1:], bound.surf[:, 1:])
+
+
+def test_large_lists_parallel_paths(tmp_path):
+    """A deck whose weight lists are long enough for the threaded reader and
+    writer (more than 65536 pairs in one list): written and re-read bit for
+    bit, equal to the oracle's reading; a pair spread over two lines in the
+    middle of a long list (the threaded reader's layout assumption broken)
+    and a malformed value there are read exactly as the one-READ-at-a-time
+    reader reads them."""
+    geo = G.close_dead_faces(G.hill_case(96, 96, 24, seed=4)[0])
+    p = tmp_path / "big.Weight2"
+    W.write_weight2(str(p), [geo])
+    text = p.read_text()
+    nfu = int(text.split("NrW_FacesYZ")[0].split()[-1])
+    assert nfu > 65536
+    b = W.read_weight2(str(p))
+    for k in ("fu", "fv", "fw", "volc"):
+        assert np.array_equal(getattr(b.geo, k), getattr(geo, k)), k
+    lines = text.split("\n")
+    head = next(i for i, s in enumerate(lines) if "NrW_FacesYZ" in s)
+    mid = head + 1 + 2 * (nfu // 2)  # an 'ix iy iz' line in the middle of the FU list
+    ix, iy, iz = lines[mid].split()
+    split = lines[:mid] + [f" {ix}", f" {iy} {iz}"] + lines[mid + 1:]
+    q = tmp_path / "split.Weight2"
+    q.write_text("\n".join(split))
+    bq = W.read_weight2(str(q))
+    assert np.array_equal(bq.geo.fu, geo.fu)
+    bad = lines[:mid + 1] + [" 1.0x"] + lines[mid + 2:]
+    q.write_text("\n".join(bad))
+    with pytest.raises(ValueError, match="bad weight"):
+        W.read_weight2(str(q))
