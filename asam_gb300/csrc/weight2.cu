@@ -287,9 +287,9 @@ void default_weights(const std::vector<double>& dx, const std::vector<double>& d
       at(k, ny + 1, i) = dyn * dx[i - 1] * dz[k - 1];
     }
   for (long long j = 1; j <= ny; ++j)
-    for (long long i = 1; i <= nx; ++i) {
-      at(0, j, i) = dzb * dx[i - 1] * dy[j - 1];
-      at(nz + 1, j, i) = dzt * dx[i - 1] * dy[j - 1];
+    for (long long i = 1; i <= nx; ++i) {  // dx(jx)*dy(jy)*dzLoc (ReadWeights_Mod.f90:962-987)
+      at(0, j, i) = dx[i - 1] * dy[j - 1] * dzb;
+      at(nz + 1, j, i) = dx[i - 1] * dy[j - 1] * dzt;
     }
 }
 

@@ -67,8 +67,9 @@ def default_weights(dx, dy, dz, periodic=(True, True, False)):
     volc[1:-1, 1:-1, -1] = dxe * dy[None, :] * dz[:, None]
     volc[1:-1, 0, 1:-1] = dyS * dx[None, :] * dz[:, None]
     volc[1:-1, -1, 1:-1] = dyN * dx[None, :] * dz[:, None]
-    volc[0, 1:-1, 1:-1] = dzb * dx[None, :] * dy[:, None]
-    volc[-1, 1:-1, 1:-1] = dzt * dx[None, :] * dy[:, None]
+    # dx(jx)*dy(jy)*dzLoc: the product of the widths first (ReadWeights_Mod.f90:962-987)
+    volc[0, 1:-1, 1:-1] = dx[None, :] * dy[:, None] * dzb
+    volc[-1, 1:-1, 1:-1] = dx[None, :] * dy[:, None] * dzt
     return fu, fv, fw, volc
 
 

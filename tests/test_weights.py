@@ -397,3 +397,26 @@ def test_large_lists_parallel_paths(tmp_path):
     q.write_text("\n".join(bad))
     with pytest.raises(ValueError, match="bad weight"):
         W.read_weight2(str(q))
+
+
+def test_halo_volume_product_order(tmp_path):
+    """The reader's default halo volumes multiply in its own order
+    (ReadWeights_Mod.f90:905-987): dxLoc*dy*dz on the lateral sides and
+    dx*dy*dzLoc on the bottom and top -- widths chosen so that the other
+    order rounds differently.  A file listing no weights reads to exactly
+    those products, in the library and in the oracle."""
+    dx, dy, dz = 0.1, 0.7, 1.7
+    assert (dx * dy) * dz != (dz * dx) * dy
+    text = " Cart\n 1\n #.... Block 1 ....\n 0.0 0.0 0.0\n 2\n 0.1\n 0.1\n 1\n 0.7\n 2\n 1.7\n 1.7\n" \
+           " 0 NrW_FacesYZ\n 0 NrMP_FacesYZ\n 0 NrW_FacesZX\n 0 NrMP_FacesZX\n 0 NrW_FacesXY\n 0 NrMP_FacesXY\n" \
+           " 0 NrW_Cells\n 0 NrB_Cells 3 Struct_Bound\n"
+    p = tmp_path / "o.Weight2"
+    p.write_text(text)
+    for periodic in ((True, True, False), (False, False, False)):
+        b = W.read_weight2(str(p), periodic=periodic)
+        o = ORA.read(str(p), periodic=periodic)
+        assert np.array_equal(b.geo.volc, o["volc"])
+        v = b.geo.volc
+        assert v[0, 1, 1] == (dx * dy) * dz and v[-1, 1, 1] == (dx * dy) * dz
+        assert v[1, 1, 0] == (dx * dy) * dz and v[1, 0, 1] == (dy * dx) * dz
+        assert v[1, 1, 1] == (dx * dy) * dz
