@@ -38,6 +38,7 @@ struct asam_batch {
   cudaGraphExec_t exec = nullptr;
   std::vector<double*> g_c;          // recorded for these device states ...
   std::vector<double> g_dt, g_tol;   // ... step sizes and tolerances
+  std::vector<unsigned long long> g_gen;  // ... and members' configurations (graph_gen)
   int g_nsteps = 0;
   std::vector<KrylovScalars*> hist;  // per member: nsteps x 4 stage scalars (device)
   KrylovScalars* hist_host = nullptr;
@@ -143,6 +144,8 @@ int graph_record(asam_batch* b, const std::vector<double*>& dc, const double* dt
   b->g_dt.assign(dt, dt + n);
   b->g_tol.resize(n);
   for (int m = 0; m < n; ++m) b->g_tol[m] = b->members[m]->cfg.bicgstab_tol;
+  b->g_gen.assign(n, 0);
+  for (int m = 0; m < n; ++m) b->g_gen[m] = b->members[m]->graph_gen;
   b->g_nsteps = nsteps;
   return kOk;
 }
@@ -159,7 +162,8 @@ int graph_run(asam_batch* b, double* const* states, const double* dt, int nsteps
   }
   bool same = b->exec && b->g_c == dc && b->g_nsteps == nsteps;
   for (int m = 0; same && m < n; ++m)
-    same = b->g_dt[m] == dt[m] && b->g_tol[m] == b->members[m]->cfg.bicgstab_tol;
+    same = b->g_dt[m] == dt[m] && b->g_tol[m] == b->members[m]->cfg.bicgstab_tol &&
+           b->g_gen[m] == b->members[m]->graph_gen;  // wall rules, their data, diffusion, ... unchanged
   if (!same) {
     if (int rc = graph_record(b, dc, dt, nsteps)) return rc;
   }

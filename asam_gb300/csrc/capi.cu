@@ -339,6 +339,7 @@ void psolve_dev(asam_ctx* h, const T* val, const T* in, T* out, Work<T>& w) {
 // captured the second time, and is replayed from then on.  The bodies touch
 // only the context's own buffers; the caller's x is updated outside them.
 void graphs_reset(asam_ctx* h) {
+  ++h->graph_gen;  // graphs recorded elsewhere (an ensemble's) compare it before a replay
   step_graph_free(h);
   for (auto& kg : h->kg) {
     for (int q = 0; q < 3; ++q) {

@@ -77,6 +77,7 @@ struct asam_ctx {
   double *stage_a = nullptr, *stage_b = nullptr;
   bool jac_ready = false;
   KrylovGraphs kg[2];     // [0] FP64, [1] FP32 inner solver
+  unsigned long long graph_gen = 0;  // bumped whenever captured work goes stale (graphs_reset)
   bool use_graphs = true;  // capture the half-iterations (when the stream allows it)
   // device-driven whole-step graphs (FP64): every BiCGStab loop is a graph
   // WHILE node, so a Rosenbrock step is one graph launch and one host read

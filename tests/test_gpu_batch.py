@@ -90,6 +90,46 @@ def test_batch_graph_matches_members_alone(asam, precision):
     assert np.array_equal(host0, members[0][1].c)
 
 
+def test_batch_graph_sees_member_changes(asam):
+    """A member's wall rule changed after the ensemble graph was recorded
+    (flat_walls_9x6x5: ZeroValue for every component on every wall) makes
+    the next call record the graph again: the states equal the members run
+    alone with the old rule for the first call and the new one after."""
+    import torch
+
+    kw = dict(bicgstab_tol=1e-10)
+    dts = [2.0, 3.0, 1.5, 2.5, 2.0, 4.0]
+    m_walls = MEMBERS.index("flat_walls_9x6x5")
+    nc = cases.get("flat_walls_9x6x5")[2].c.shape[0]
+    zero_value = np.full((nc, 6), 2, np.int32)
+    alone = []
+    for m, ((b, st), dt) in enumerate(zip(_blocks(asam, **kw), dts)):
+        c = st.c.copy()
+        b.Ros3MetC(c, dt)
+        if m == m_walls:
+            kept = c.copy()
+            b.Ros3MetC(kept, dt)  # the old rule: what a stale graph would give
+            b.set_boundary(zero_value)
+        b.Ros3MetC(c, dt)
+        if m == m_walls:
+            assert not np.array_equal(c, kept)
+        alone.append(c)
+        b.close()
+    members = _blocks(asam, **kw)
+    dev = [torch.from_numpy(st.c.reshape(-1).copy()).cuda() for _, st in members]
+    torch.cuda.synchronize()
+    with asam.Batch([b for b, _ in members]) as batch:
+        batch.set_graph(True)
+        batch.ros_step([t.data_ptr() for t in dev], dts, nsteps=1)
+        members[m_walls][0].set_boundary(zero_value)
+        batch.ros_step([t.data_ptr() for t in dev], dts, nsteps=1)
+    torch.cuda.synchronize()
+    for b, _ in members:
+        b.close()
+    for m, c_ref in enumerate(alone):
+        assert np.array_equal(dev[m].cpu().numpy().reshape(c_ref.shape), c_ref), MEMBERS[m]
+
+
 def test_batch_device_states(asam):
     import torch
 
