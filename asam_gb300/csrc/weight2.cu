@@ -33,6 +33,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <new>
 #include <string>
 #include <thread>
 #include <vector>
@@ -220,14 +221,29 @@ long long locate(int a, int nx, int ny, int nz, long long ix, long long iy, long
 
 int host_threads();
 
+// work(t) for t = 0..n-1, t >= 1 on their own threads; a thread that cannot
+// be started runs its part here, and every started thread is joined
+template <typename F>
+void run_parts(int n, F work) {
+  std::vector<std::thread> pool;
+  std::vector<int> inline_parts;
+  for (int t = 1; t < n; ++t) {
+    try {
+      pool.emplace_back(work, t);
+    } catch (...) {
+      inline_parts.push_back(t);
+    }
+  }
+  work(0);
+  for (int t : inline_parts) work(t);
+  for (auto& th : pool) th.join();
+}
+
 // f(k0, k1) over the slices of [0, n) on the host threads
 template <typename F>
 void for_slices(long long n, F f) {
   const int nth = n >= 16 ? host_threads() : 1;
-  std::vector<std::thread> pool;
-  for (int t = 1; t < nth; ++t) pool.emplace_back(f, n * t / nth, n * (t + 1) / nth);
-  f(0LL, n / nth);
-  for (auto& th : pool) th.join();
+  run_parts(nth, [&](int t) { f(n * t / nth, n * (t + 1) / nth); });
 }
 
 // The reader's Cartesian weights before the file's lists are applied
@@ -359,7 +375,7 @@ bool pairs_parallel(ListReader& rd, long long cnt, int a, int nx, int ny, int nz
   const int nch = (int)cut.size() - 1;
   std::vector<std::vector<std::pair<long long, double>>> got(nch);
   std::vector<char> ok(nch, 1);
-  auto work = [&](int t) {
+  auto parse_chunk = [&](int t) {
     ListReader r(cut[t], cut[t + 1]);
     Tok tk[3];
     auto& out = got[t];
@@ -380,10 +396,14 @@ bool pairs_parallel(ListReader& rd, long long cnt, int a, int nx, int ny, int nz
       out.emplace_back(at, w);
     }
   };
-  std::vector<std::thread> pool;
-  for (int t = 1; t < nch; ++t) pool.emplace_back(work, t);
-  work(0);
-  for (auto& th : pool) th.join();
+  auto work = [&](int t) noexcept {  // an allocation that fails sends the list to the sequential parse
+    try {
+      parse_chunk(t);
+    } catch (...) {
+      ok[t] = 0;
+    }
+  };
+  run_parts(nch, work);
   long long n = 0;
   for (int t = 0; t < nch; ++t) {
     if (!ok[t]) return false;
@@ -671,7 +691,8 @@ void write_block(Out& out, const asam_weight2_block& b, int ib, const int period
     const int nth = n >= (1 << 18) ? host_threads() : 1;
     std::vector<std::string> text(nth);
     std::vector<long long> cnt(nth, 0);
-    auto work = [&](int t) {
+    std::vector<char> fine(nth, 1);
+    auto format = [&](int t) {
       const long long q0 = n * t / nth, q1 = n * (t + 1) / nth;
       std::string& o = text[t];
       for (long long q = q0; q < q1; ++q) {
@@ -689,10 +710,16 @@ void write_block(Out& out, const asam_weight2_block& b, int ib, const int period
         ++cnt[t];
       }
     };
-    std::vector<std::thread> pool;
-    for (int t = 1; t < nth; ++t) pool.emplace_back(work, t);
-    work(0);
-    for (auto& th : pool) th.join();
+    auto work = [&](int t) noexcept {
+      try {
+        format(t);
+      } catch (...) {
+        fine[t] = 0;
+      }
+    };
+    run_parts(nth, work);
+    for (char f : fine)
+      if (!f) throw std::bad_alloc();
     long long total = 0;
     for (long long c : cnt) total += c;
     out.put(" ");
@@ -796,19 +823,29 @@ int asam_weight2_open(const char* path, int ib, const asam_weight2_options* opt,
     fseek(f, 0, SEEK_SET);
   }
   bool bad = false;
-  if (sz >= 0) {  // one read into a buffer of the file's size
-    text.resize(size_t(sz));
-    bad = fread(text.data(), 1, text.size(), f) != text.size();
-  } else {  // not seekable: in chunks
-    char chunk[1 << 16];
-    size_t got;
-    while ((got = fread(chunk, 1, sizeof(chunk), f)) > 0) text.insert(text.end(), chunk, chunk + got);
-    bad = ferror(f) != 0;
+  try {
+    if (sz >= 0) {  // one read into a buffer of the file's size
+      text.resize(size_t(sz));
+      bad = fread(text.data(), 1, text.size(), f) != text.size();
+    } else {  // not seekable: in chunks
+      char chunk[1 << 16];
+      size_t got;
+      while ((got = fread(chunk, 1, sizeof(chunk), f)) > 0) text.insert(text.end(), chunk, chunk + got);
+      bad = ferror(f) != 0;
+    }
+  } catch (const std::exception&) {
+    bad = true;
   }
   fclose(f);
   if (bad) return fail(ASAM_IO_ERROR, std::string("Weight2: read error on ") + path);
-  asam_weight2_file* h = new asam_weight2_file();
-  const int st = parse(text.data(), text.size(), ib, *opt, h->b);
+  asam_weight2_file* h = nullptr;
+  int st;
+  try {
+    h = new asam_weight2_file();
+    st = parse(text.data(), text.size(), ib, *opt, h->b);
+  } catch (const std::exception& e) {  // out of host memory: nothing crosses the C boundary
+    st = fail(ASAM_IO_ERROR, std::string("Weight2: ") + e.what());
+  }
   if (st != ASAM_OK) {
     delete h;
     return st;
@@ -857,13 +894,16 @@ int asam_weight2_write(const char* path, int nblock, const asam_weight2_block* b
   FILE* f = fopen(path, "wb");
   if (!f) return fail(ASAM_IO_ERROR, std::string("Weight2: cannot create ") + path);
   bool ok;
-  {
+  try {
     Out out(f);
     out.put(" Cart\n ");
     out.integer(nblock);
     out.put("  ! Number of blocks\n");
     for (int ib = 0; ib < nblock; ++ib) write_block(out, blocks[ib], ib + 1, periodic);
     ok = out.flush();
+  } catch (const std::exception& e) {  // out of host memory
+    fclose(f);
+    return fail(ASAM_IO_ERROR, std::string("Weight2: ") + e.what());
   }
   ok = (fclose(f) == 0) && ok;
   if (!ok) return fail(ASAM_IO_ERROR, std::string("Weight2: write error on ") + path);
