@@ -92,16 +92,19 @@ def test_batch_graph_matches_members_alone(asam, precision):
 
 def test_batch_graph_sees_member_changes(asam):
     """A member's wall rule changed after the ensemble graph was recorded
-    (flat_walls_9x6x5: ZeroValue for every component on every wall) makes
-    the next call record the graph again: the states equal the members run
-    alone with the old rule for the first call and the new one after."""
+    (flat_walls_9x6x5: ZeroValue on every wall for every component but the
+    density -- negating the density too would leave every halo's mixing
+    ratio, and so the fluxes, as they were) makes the next call record the
+    graph again: the states equal the members run alone with the old rule
+    for the first call and the new one after."""
     import torch
 
     kw = dict(bicgstab_tol=1e-10)
     dts = [2.0, 3.0, 1.5, 2.5, 2.0, 4.0]
     m_walls = MEMBERS.index("flat_walls_9x6x5")
-    nc = cases.get("flat_walls_9x6x5")[2].c.shape[0]
-    zero_value = np.full((nc, 6), 2, np.int32)
+    st_walls = cases.get("flat_walls_9x6x5")[2]
+    zero_value = np.full((st_walls.c.shape[0], 6), 2, np.int32)
+    zero_value[st_walls.rho_pos] = 1
     alone = []
     for m, ((b, st), dt) in enumerate(zip(_blocks(asam, **kw), dts)):
         c = st.c.copy()
