@@ -632,6 +632,28 @@ def Solve_TB_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, b: np.ndarray) -> n
     return x
 
 
+def Compute_TB_1D(f, fg, vol, dtu, duu, dut, dur=None, beta0_dtp: float = 1.0, fac1_l: float = 0.0,
+                  fac1_r: float = 0.0, grav_comp: float = 0.0, fac_anela: float = 0.0):
+    """Allocate_1D + Compute_1D of TriDiagTB (dur None) or TriDiagTR (dur
+    given) on a batch of columns: faces f, fg, dtu, duu (ncol, n1+1), cells
+    vol, dut, dur (ncol, n1).  Returns d (ncol,n1,4), u, l (ncol,n1-1,4)."""
+    lib = _lib.load()
+    faces = [_f64(a) for a in (f, fg, dtu, duu)]
+    cells = [_f64(a) for a in (vol, dut)] + ([_f64(dur)] if dur is not None else [])
+    ncol, n1 = cells[0].shape
+    if any(a.shape != (ncol, n1 + 1) for a in faces) or any(a.shape != (ncol, n1) for a in cells):
+        raise ValueError("faces (ncol, n1+1), cells (ncol, n1)")
+    d = np.empty((ncol, n1, 4))
+    u = np.empty((ncol, max(n1 - 1, 0), 4))
+    l = np.empty_like(u)
+    co = _lib.AsamTriTbCoefs(beta0_dtp, fac1_l, fac1_r, grav_comp, fac_anela)
+    check(lib.asam_tri_tb_compute(int(dur is not None), ncol, n1, C.byref(co), *[ptr(a) for a in faces[:2]],
+                                  ptr(cells[0]), ptr(faces[2]), ptr(faces[3]), ptr(cells[1]),
+                                  ptr(cells[2]) if dur is not None else None, ptr(d),
+                                  ptr(u) if u.size else None, ptr(l) if l.size else None), "asam_tri_tb_compute")
+    return d, u, l
+
+
 def MatVecTB_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, x: np.ndarray) -> np.ndarray:
     lib = _lib.load()
     d, u, l, xx = _f64(d), _f64(u), _f64(l), _f64(x)

@@ -81,6 +81,11 @@ class AsamWeight2Options(C.Structure):
                 ("real_island", C.c_int), ("expect", C.c_int * 3)]
 
 
+class AsamTriTbCoefs(C.Structure):
+    _fields_ = [("beta0_dtp", C.c_double), ("fac1_l", C.c_double), ("fac1_r", C.c_double),
+                ("grav_comp", C.c_double), ("fac_anela", C.c_double)]
+
+
 # (name, restype, argtypes) of every exported entry point of include/asam_gb300.h
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
@@ -120,6 +125,7 @@ SIGNATURES = [
      [_V, _V, C.c_int, C.c_int, C.c_double, C.c_int, _V, C.c_double, _D, _V, _V, _V, _V, _V]),
     ("asam_tri_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
+    ("asam_tri_tb_compute", C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(AsamTriTbCoefs)] + [_V] * 10),
     ("asam_tri_tb_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_tb_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),

@@ -128,6 +128,85 @@ __global__ void k_tri_tb_matvec(int ncol, int n1, const double* __restrict__ d, 
   st_v(y + q * 2, r);
 }
 
+// Compute_1D (Allocate_1D, then MULTI/TriDiagTB_Mod.f90:32-93; with tr the
+// DUR terms of MULTI/TriDiagTR_Mod.f90:32-105) of one column, statement by
+// statement in the reference's order (the GradFull branches are the same
+// statements).  s = {beta0*dtp, Fac1_L, Fac1_R, GravComp, FacAnela}.
+__global__ void k_tri_tb_compute(int tr, int ncol, int n1, asam_tri_tb_coefs s, const double* __restrict__ f,
+                                 const double* __restrict__ fg, const double* __restrict__ vol,
+                                 const double* __restrict__ dtu, const double* __restrict__ duu,
+                                 const double* __restrict__ dut, const double* __restrict__ dur,
+                                 double* __restrict__ d, double* __restrict__ u, double* __restrict__ l) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const double bd = s.beta0_dtp, fl = s.fac1_l, fr = s.fac1_r, grav = s.grav_comp, anela = s.fac_anela;
+  const double bd2 = bd * bd, half = 0.5, eps = 1.0e-30;
+  const double *F = f + (size_t)col * (n1 + 1), *FG = fg + (size_t)col * (n1 + 1);
+  const double *DTU = dtu + (size_t)col * (n1 + 1), *DUU = duu + (size_t)col * (n1 + 1);
+  const double *V = vol + (size_t)col * n1, *DUT = dut + (size_t)col * n1;
+  const double* DUR = tr ? dur + (size_t)col * n1 : nullptr;
+  double* D = d + (size_t)col * n1 * 4;
+  double *U = u + (size_t)col * (n1 - 1) * 4, *L = l + (size_t)col * (n1 - 1) * 4;
+  auto DD = [&](int r, int c, int i) -> double& { return D[(size_t)i * 4 + r + 2 * c]; };
+  auto UU = [&](int r, int c, int i) -> double& { return U[(size_t)i * 4 + r + 2 * c]; };
+  auto LL = [&](int r, int c, int i) -> double& { return L[(size_t)i * 4 + r + 2 * c]; };
+  for (int i = 0; i < n1; ++i) {
+    DD(0, 0, i) = 1.0e-40;
+    DD(1, 0, i) = 0.0;
+    DD(0, 1, i) = 0.0;
+    DD(1, 1, i) = 1.0e-40;
+  }
+  for (int i = 0; i < n1 - 1; ++i)
+    for (int e = 0; e < 4; ++e) U[(size_t)i * 4 + e] = L[(size_t)i * 4 + e] = 0.0;
+  DD(0, 0, 0) = DD(0, 0, 0) + bd2 * fl * F[0] * DTU[0] * DUU[0] * FG[0] * DUT[0] / (V[0] + eps);
+  if (tr) DD(0, 1, 0) = DD(0, 1, 0) + bd2 * fl * F[0] * DTU[0] * DUU[0] * FG[0] * DUR[0] / (V[0] + eps);
+  DD(1, 0, 0) = DD(1, 0, 0) + bd2 * fl * F[0] * DUU[0] * FG[0] * DUT[0] / (V[0] + eps);
+  if (tr) DD(1, 1, 0) = DD(1, 1, 0) + bd2 * fl * F[0] * DUU[0] * FG[0] * DUR[0] / (V[0] + eps);
+  DD(0, 1, 0) = DD(0, 1, 0) - half * grav * bd2 * fl * F[0] * DTU[0] * V[0] / (V[0] + eps);
+  DD(1, 1, 0) = DD(1, 1, 0) - half * grav * bd2 * fl * F[0] * V[0] / (V[0] + eps);
+  for (int i = 0; i < n1 - 1; ++i) {
+    const int q = i + 1;
+    const double S = V[i] + V[q] + eps;
+    UU(0, 0, i) = -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[q] / S);
+    if (tr) UU(0, 1, i) = -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[q] / S);
+    UU(1, 0, i) = -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[q] / S);
+    if (tr) UU(1, 1, i) = -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[q] / S);
+    LL(0, 0, i) = -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[i] / S);
+    if (tr) LL(0, 1, i) = -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[i] / S);
+    LL(1, 0, i) = -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[i] / S);
+    if (tr) LL(1, 1, i) = -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[i] / S);
+    UU(0, 1, i) = UU(0, 1, i) - grav * bd2 * F[q] * DTU[q] * V[q] / S;
+    UU(1, 1, i) = UU(1, 1, i) - grav * bd2 * F[q] * V[q] / S;
+    LL(0, 1, i) = LL(0, 1, i) + grav * bd2 * F[q] * DTU[q] * V[i] / S;
+    LL(1, 1, i) = LL(1, 1, i) + grav * bd2 * F[q] * V[i] / S;
+    DD(0, 0, i) = DD(0, 0, i) + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[i] / S;
+    if (tr) DD(0, 1, i) = DD(0, 1, i) + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[i] / S;
+    DD(1, 0, i) = DD(1, 0, i) + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[i] / S;
+    if (tr) DD(1, 1, i) = DD(1, 1, i) + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[i] / S;
+    DD(0, 0, q) = DD(0, 0, q) + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[q] / S;
+    if (tr) DD(0, 1, q) = DD(0, 1, q) + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[q] / S;
+    DD(1, 0, q) = DD(1, 0, q) + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[q] / S;
+    if (tr) DD(1, 1, q) = DD(1, 1, q) + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[q] / S;
+    DD(0, 1, i) = DD(0, 1, i) - grav * bd2 * F[q] * DTU[q] * V[i] / S;
+    DD(1, 1, i) = DD(1, 1, i) - grav * bd2 * F[q] * V[i] / S;
+    DD(0, 1, q) = DD(0, 1, q) + grav * bd2 * F[q] * DTU[q] * V[q] / S;
+    DD(1, 1, q) = DD(1, 1, q) + grav * bd2 * F[q] * V[q] / S;
+  }
+  {
+    const int c = n1 - 1, q = n1;
+    DD(0, 0, c) = DD(0, 0, c) + bd2 * fr * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[c] / (V[c] + eps);
+    if (tr) DD(0, 1, c) = DD(0, 1, c) + bd2 * fr * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[c] / (V[c] + eps);
+    DD(1, 0, c) = DD(1, 0, c) + bd2 * fr * F[q] * DUU[q] * FG[q] * DUT[c] / (V[c] + eps);
+    if (tr) DD(1, 1, c) = DD(1, 1, c) + bd2 * fr * F[q] * DUU[q] * FG[q] * DUR[c] / (V[c] + eps);
+    DD(0, 1, c) = DD(0, 1, c) + half * grav * bd2 * fr * F[q] * DTU[q] * V[c] / (V[c] + eps);
+    DD(1, 1, c) = DD(1, 1, c) + half * grav * bd2 * fr * F[q] * V[c] / (V[c] + eps);
+  }
+  for (int i = 0; i < n1; ++i) {
+    DD(0, 0, i) = DD(0, 0, i) + anela * V[i];
+    DD(1, 1, i) = DD(1, 1, i) + V[i];
+  }
+}
+
 struct DevBufs {
   double* p[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   ~DevBufs() {
@@ -151,6 +230,43 @@ constexpr int kTbBlock = 128;
 }  // namespace
 
 extern "C" {
+
+int asam_tri_tb_compute(int variant, int ncol, int n1, const asam_tri_tb_coefs* coefs, const double* f,
+                        const double* fg, const double* vol, const double* dtu, const double* duu, const double* dut,
+                        const double* dur, double* d, double* u, double* l) {
+  if ((variant != 0 && variant != 1) || ncol < 1 || n1 < 1 || !coefs || !f || !fg || !vol || !dtu || !duu ||
+      !dut || (variant == 1 && !dur) || !d || (n1 > 1 && (!u || !l))) {
+    asam::set_last_error("asam_tri_tb_compute: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  const size_t nf = (size_t)ncol * (n1 + 1), nc = (size_t)ncol * n1;
+  const size_t nd = nc * 4, no = (size_t)ncol * (n1 - 1) * 4;
+  // inputs: f, fg, dtu, duu (faces), vol, dut, dur (cells) packed in one buffer
+  DevBufs m;
+  TCU(cudaMalloc((void**)&m.p[0], (4 * nf + 3 * nc) * sizeof(double)));
+  TCU(cudaMalloc((void**)&m.p[1], (nd + 2 * no + 1) * sizeof(double)));
+  double* in = m.p[0];
+  const double* src[7] = {f, fg, dtu, duu, vol, dut, variant == 1 ? dur : vol};
+  const size_t len[7] = {nf, nf, nf, nf, nc, nc, nc};
+  double* dev[7];
+  size_t off = 0;
+  for (int q = 0; q < 7; ++q) {
+    dev[q] = in + off;
+    TCU(cudaMemcpy(dev[q], src[q], len[q] * sizeof(double), cudaMemcpyDefault));
+    off += len[q];
+  }
+  double *dd = m.p[1], *du = dd + nd, *dl = du + no;
+  k_tri_tb_compute<<<(ncol + kTbBlock - 1) / kTbBlock, kTbBlock>>>(variant, ncol, n1, *coefs, dev[0], dev[1], dev[4],
+                                                                   dev[2], dev[3], dev[5], dev[6], dd, du, dl);
+  asam::count_launches(1);
+  TCU(cudaGetLastError());
+  TCU(cudaMemcpy(d, dd, nd * sizeof(double), cudaMemcpyDefault));
+  if (no) {
+    TCU(cudaMemcpy(u, du, no * sizeof(double), cudaMemcpyDefault));
+    TCU(cudaMemcpy(l, dl, no * sizeof(double), cudaMemcpyDefault));
+  }
+  return ASAM_OK;
+}
 
 int asam_tri_tb_solve(int ncol, int n1, const double* d, const double* u, const double* l, double* b) {
   if (ncol < 1 || n1 < 1 || !d || !b || (n1 > 1 && (!u || !l))) {

@@ -563,6 +563,24 @@ int asam_probe_div(long long n, long long seed, int span, long long *mismatches)
  * b[(col*n1+i)*2 + r] overwritten by the solution.  Host or device pointers. */
 int asam_tri_tb_solve(int ncol, int n1, const double *d, const double *u, const double *l, double *b);
 
+/* Assembly of the same columns: Allocate_1D and Compute_1D of
+ * MULTI/TriDiagTB_Mod.f90:32-93 (variant 0) or of MULTI/TriDiagTR_Mod.f90:32-105
+ * (variant 1, the density-weight terms DUR in the second block column too),
+ * in the reference's statement order.  Per column, faces f, fg, dtu, duu
+ * [col*(n1+1) + i] (F, FG, DTU, DUU of faces 1..n1+1), cells vol, dut, dur
+ * [col*n1 + i] (dur only for variant 1); d, u, l as for asam_tri_tb_solve,
+ * overwritten.  Host or device pointers. */
+typedef struct {
+  double beta0_dtp; /* beta0*dtp */
+  double fac1_l;    /* Fac1_L, the weight of the first face (boundary condition of the line) */
+  double fac1_r;    /* Fac1_R, the weight of the last face */
+  double grav_comp; /* GravComp */
+  double fac_anela; /* FacAnela */
+} asam_tri_tb_coefs;
+int asam_tri_tb_compute(int variant, int ncol, int n1, const asam_tri_tb_coefs *coefs, const double *f,
+                        const double *fg, const double *vol, const double *dtu, const double *duu, const double *dut,
+                        const double *dur, double *d, double *u, double *l);
+
 /* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141),
  * the same as MatVecTR_1D (MULTI/TriDiagTR_Mod.f90:133-153). */
 int asam_tri_tb_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x,

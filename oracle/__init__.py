@@ -62,6 +62,7 @@ def load() -> C.CDLL:
             "ora_tri_solve": (None, [I, I, V, V, V, V]),
             "ora_tri_tb_solve": (None, [I, I, V, V, V, V, V]),
             "ora_tri_tb_matvec": (None, [I, I, V, V, V, V, V]),
+            "ora_tri_tb_compute": (None, [I, I, I] + [V] * 11),
             "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
         }
         sig.update({
@@ -387,6 +388,26 @@ def tri_tb_matvec(d, u, l, x):
     y = np.empty_like(xx)
     lib.ora_tri_tb_matvec(ncol, n1, _p(d), _p(u), _p(l), _p(xx), _p(y))
     return y
+
+
+def tri_tb_compute(f, fg, vol, dtu, duu, dut, dur=None, beta0_dtp=1.0, fac1_l=0.0, fac1_r=0.0, grav_comp=0.0,
+                   fac_anela=0.0):
+    """Allocate_1D + Compute_1D of TriDiagTB (dur None, MULTI/TriDiagTB_Mod.f90:32-93)
+    or TriDiagTR (MULTI/TriDiagTR_Mod.f90:32-105) on columns: faces (ncol, n1+1),
+    cells (ncol, n1).  Returns d (ncol, n1, 4), u, l (ncol, n1-1, 4)."""
+    lib = load()
+    faces = [np.ascontiguousarray(a, dtype=np.float64) for a in (f, fg, dtu, duu)]
+    vol, dut = (np.ascontiguousarray(a, dtype=np.float64) for a in (vol, dut))
+    tr = dur is not None
+    durr = np.ascontiguousarray(dur, dtype=np.float64) if tr else vol
+    ncol, n1 = vol.shape
+    s = np.array([beta0_dtp, fac1_l, fac1_r, grav_comp, fac_anela])
+    d = np.empty((ncol, n1, 4))
+    u = np.empty((ncol, max(n1 - 1, 1), 4))
+    l = np.empty_like(u)
+    lib.ora_tri_tb_compute(int(tr), ncol, n1, _p(s), _p(faces[0]), _p(faces[1]), _p(vol), _p(faces[2]),
+                           _p(faces[3]), _p(dut), _p(durr), _p(d), _p(u), _p(l))
+    return d, u[:, :n1 - 1], l[:, :n1 - 1]
 
 
 class OracleProj:

@@ -101,3 +101,91 @@ void ora_tri_tb_matvec(int ncol, int n1, const double *d, const double *u, const
     }
   }
 }
+
+/* Compute_1D of the block-tridiagonal line systems: Allocate_1D (d = 1e-40 on
+ * the diagonal of each block, u = l = 0) then the assembly of
+ * MULTI/TriDiagTB_Mod.f90:32-93 (variant 0) or MULTI/TriDiagTR_Mod.f90:32-105
+ * (variant 1, with the DUR terms of the second block column), statement by
+ * statement; the GradFull and .NOT.GradFull branches of the reference are the
+ * same statements.  s = {beta0*dtp, Fac1_L, Fac1_R, GravComp, FacAnela};
+ * face arrays f, fg, dtu, duu [col*(n1+1) + i], cell arrays vol, dut, dur
+ * [col*n1 + i]; d [col*n1 + i][4], u, l [col*(n1-1) + i][4], blocks
+ * column-major (r + 2c). */
+void ora_tri_tb_compute(int variant, int ncol, int n1, const double *s, const double *f, const double *fg,
+                        const double *vol, const double *dtu, const double *duu, const double *dut,
+                        const double *dur, double *d, double *u, double *l) {
+  const double bd = s[0], fl = s[1], fr = s[2], grav = s[3], anela = s[4];
+  const double bd2 = bd * bd, half = 0.5, eps = 1.0e-30;
+  const int tr = variant == 1;
+  for (int col = 0; col < ncol; ++col) {
+    const double *F = f + (size_t)col * (n1 + 1), *FG = fg + (size_t)col * (n1 + 1);
+    const double *DTU = dtu + (size_t)col * (n1 + 1), *DUU = duu + (size_t)col * (n1 + 1);
+    const double *V = vol + (size_t)col * n1, *DUT = dut + (size_t)col * n1;
+    const double *DUR = tr ? dur + (size_t)col * n1 : 0;
+    double *D = d + (size_t)col * n1 * 4;
+    double *U = u + (size_t)col * (n1 - 1) * 4, *L = l + (size_t)col * (n1 - 1) * 4;
+#define DD(r, c, i) D[(size_t)(i) * 4 + (r) + 2 * (c)]
+#define UU(r, c, i) U[(size_t)(i) * 4 + (r) + 2 * (c)]
+#define LL(r, c, i) L[(size_t)(i) * 4 + (r) + 2 * (c)]
+    for (int i = 0; i < n1; ++i) {
+      DD(0, 0, i) = 1.0e-40;
+      DD(1, 0, i) = 0.0;
+      DD(0, 1, i) = 0.0;
+      DD(1, 1, i) = 1.0e-40;
+    }
+    for (int i = 0; i < n1 - 1; ++i)
+      for (int e = 0; e < 4; ++e) U[(size_t)i * 4 + e] = L[(size_t)i * 4 + e] = 0.0;
+    /* first cell, face 1 */
+    DD(0, 0, 0) = DD(0, 0, 0) + bd2 * fl * F[0] * DTU[0] * DUU[0] * FG[0] * DUT[0] / (V[0] + eps);
+    if (tr) DD(0, 1, 0) = DD(0, 1, 0) + bd2 * fl * F[0] * DTU[0] * DUU[0] * FG[0] * DUR[0] / (V[0] + eps);
+    DD(1, 0, 0) = DD(1, 0, 0) + bd2 * fl * F[0] * DUU[0] * FG[0] * DUT[0] / (V[0] + eps);
+    if (tr) DD(1, 1, 0) = DD(1, 1, 0) + bd2 * fl * F[0] * DUU[0] * FG[0] * DUR[0] / (V[0] + eps);
+    DD(0, 1, 0) = DD(0, 1, 0) - half * grav * bd2 * fl * F[0] * DTU[0] * V[0] / (V[0] + eps);
+    DD(1, 1, 0) = DD(1, 1, 0) - half * grav * bd2 * fl * F[0] * V[0] / (V[0] + eps);
+    for (int i = 0; i < n1 - 1; ++i) { /* face i+1 (0-based) between cells i and i+1 */
+      const int q = i + 1;
+      const double S = V[i] + V[q] + eps;
+      UU(0, 0, i) = -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[q] / S);
+      if (tr) UU(0, 1, i) = -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[q] / S);
+      UU(1, 0, i) = -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[q] / S);
+      if (tr) UU(1, 1, i) = -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[q] / S);
+      LL(0, 0, i) = -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[i] / S);
+      if (tr) LL(0, 1, i) = -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[i] / S);
+      LL(1, 0, i) = -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[i] / S);
+      if (tr) LL(1, 1, i) = -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[i] / S);
+      UU(0, 1, i) = UU(0, 1, i) - grav * bd2 * F[q] * DTU[q] * V[q] / S;
+      UU(1, 1, i) = UU(1, 1, i) - grav * bd2 * F[q] * V[q] / S;
+      LL(0, 1, i) = LL(0, 1, i) + grav * bd2 * F[q] * DTU[q] * V[i] / S;
+      LL(1, 1, i) = LL(1, 1, i) + grav * bd2 * F[q] * V[i] / S;
+      DD(0, 0, i) = DD(0, 0, i) + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[i] / S;
+      if (tr) DD(0, 1, i) = DD(0, 1, i) + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[i] / S;
+      DD(1, 0, i) = DD(1, 0, i) + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[i] / S;
+      if (tr) DD(1, 1, i) = DD(1, 1, i) + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[i] / S;
+      DD(0, 0, q) = DD(0, 0, q) + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[q] / S;
+      if (tr) DD(0, 1, q) = DD(0, 1, q) + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[q] / S;
+      DD(1, 0, q) = DD(1, 0, q) + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[q] / S;
+      if (tr) DD(1, 1, q) = DD(1, 1, q) + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[q] / S;
+      DD(0, 1, i) = DD(0, 1, i) - grav * bd2 * F[q] * DTU[q] * V[i] / S;
+      DD(1, 1, i) = DD(1, 1, i) - grav * bd2 * F[q] * V[i] / S;
+      DD(0, 1, q) = DD(0, 1, q) + grav * bd2 * F[q] * DTU[q] * V[q] / S;
+      DD(1, 1, q) = DD(1, 1, q) + grav * bd2 * F[q] * V[q] / S;
+    }
+    /* last cell, face n1+1 */
+    {
+      const int c = n1 - 1, q = n1;
+      DD(0, 0, c) = DD(0, 0, c) + bd2 * fr * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[c] / (V[c] + eps);
+      if (tr) DD(0, 1, c) = DD(0, 1, c) + bd2 * fr * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[c] / (V[c] + eps);
+      DD(1, 0, c) = DD(1, 0, c) + bd2 * fr * F[q] * DUU[q] * FG[q] * DUT[c] / (V[c] + eps);
+      if (tr) DD(1, 1, c) = DD(1, 1, c) + bd2 * fr * F[q] * DUU[q] * FG[q] * DUR[c] / (V[c] + eps);
+      DD(0, 1, c) = DD(0, 1, c) + half * grav * bd2 * fr * F[q] * DTU[q] * V[c] / (V[c] + eps);
+      DD(1, 1, c) = DD(1, 1, c) + half * grav * bd2 * fr * F[q] * V[c] / (V[c] + eps);
+    }
+    for (int i = 0; i < n1; ++i) {
+      DD(0, 0, i) = DD(0, 0, i) + anela * V[i];
+      DD(1, 1, i) = DD(1, 1, i) + V[i];
+    }
+#undef DD
+#undef UU
+#undef LL
+  }
+}

@@ -1,5 +1,7 @@
 """GPU parity of the TriDiagTB block-Thomas column solve and its product
-(MULTI/TriDiagTB_Mod.f90:121-163) with the oracle: bit-exact on every shape,
+(MULTI/TriDiagTB_Mod.f90:121-163, the same statements as TriDiagTR's) and of
+the columns' assembly Compute_1D of both variants (TriDiagTB_Mod.f90:32-93,
+TriDiagTR_Mod.f90:32-105) with the oracle: bit-exact on every shape,
 including one- and two-level columns and a batch of 32768 columns of 128
 levels (the columns of a 256x128 plane stack of the 512x512x128 grid)."""
 import numpy as np
@@ -29,3 +31,26 @@ def test_tri_tb_bad_args(built_lib):
     lib = _lib.load()
     assert lib.asam_tri_tb_solve(0, 4, None, None, None, None) == 4
     assert lib.asam_tri_tb_matvec(2, 3, None, None, None, None, None) == 4
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("ncol,n1", [(3, 1), (4, 2), (129, 17), (4096, 128)])
+def test_tri_tb_compute_bitwise(built_lib, variant, ncol, n1):
+    """Compute_1D of TriDiagTB / TriDiagTR on the GPU equals the oracle bit
+    for bit, and the assembled columns solve to the oracle's solution of its
+    own assembly bit for bit."""
+    from tests.test_tritb import compute_inputs
+
+    faces, vol, dut, dur, coefs = compute_inputs(ncol, n1, seed=3 * n1 + ncol)
+    dr = dur if variant == "TR" else None
+    got = asam.Compute_TB_1D(*faces[:2], vol, faces[2], faces[3], dut, dr, **coefs)
+    ref = oracle.tri_tb_compute(*faces[:2], vol, faces[2], faces[3], dut, dr, **coefs)
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)
+    b = np.random.default_rng(n1).standard_normal((ncol, n1, 2))
+    assert np.array_equal(asam.Solve_TB_1D(*got, b), oracle.tri_tb_solve(*ref, b))
+    from asam_gb300 import _lib
+
+    lib = _lib.load()
+    co = _lib.AsamTriTbCoefs(1.0, 0.0, 0.0, 0.0, 0.0)
+    assert lib.asam_tri_tb_compute(2, 1, 1, co, None, None, None, None, None, None, None, None, None, None) == 4

@@ -54,3 +54,111 @@ def test_oracle_diagonal_blocks_decouple(built_oracle):
     x1 = (d[..., 3] * b[..., 0] - d[..., 2] * b[..., 1]) / det
     x2 = (-d[..., 1] * b[..., 0] + d[..., 0] * b[..., 1]) / det
     assert np.array_equal(x[..., 0], x1) and np.array_equal(x[..., 1], x2)
+
+
+def compute_inputs(ncol, n1, seed):
+    r = np.random.default_rng(seed)
+    faces = [r.uniform(0.2, 2.0, (ncol, n1 + 1)) for _ in range(4)]  # F, FG, DTU, DUU
+    vol = r.uniform(0.5, 3.0, (ncol, n1))
+    dut = r.uniform(0.1, 1.5, (ncol, n1))
+    dur = r.uniform(-0.5, 0.5, (ncol, n1))
+    coefs = dict(beta0_dtp=r.uniform(0.3, 3.0), fac1_l=2.0, fac1_r=1.0, grav_comp=9.81, fac_anela=0.25)
+    return faces, vol, dut, dur, coefs
+
+
+def numpy_compute(faces, vol, dut, dur, beta0_dtp, fac1_l, fac1_r, grav_comp, fac_anela):
+    """Compute_1D restated with numpy, element by element in the order the
+    reference's statements touch each entry: the first face's terms, the
+    entry's share of face i (as the upper cell of that face), of face i+1 (as
+    the lower cell), the last face's terms, the FacAnela/Vol diagonal."""
+    F, FG, DTU, DUU = faces
+    ncol, n1 = vol.shape
+    tr = dur is not None
+    bd2 = beta0_dtp * beta0_dtp
+    eps, half = 1e-30, 0.5
+    d = np.zeros((ncol, n1, 4))
+    d[:, :, 0] = 1e-40
+    d[:, :, 3] = 1e-40
+    u = np.zeros((ncol, max(n1 - 1, 0), 4))
+    l = np.zeros_like(u)
+    V = vol
+    # first face (column index 0 of the faces), first cell
+    d[:, 0, 0] = d[:, 0, 0] + bd2 * fac1_l * F[:, 0] * DTU[:, 0] * DUU[:, 0] * FG[:, 0] * dut[:, 0] / (V[:, 0] + eps)
+    if tr:
+        d[:, 0, 2] = d[:, 0, 2] + bd2 * fac1_l * F[:, 0] * DTU[:, 0] * DUU[:, 0] * FG[:, 0] * dur[:, 0] / (V[:, 0] + eps)
+    d[:, 0, 1] = d[:, 0, 1] + bd2 * fac1_l * F[:, 0] * DUU[:, 0] * FG[:, 0] * dut[:, 0] / (V[:, 0] + eps)
+    if tr:
+        d[:, 0, 3] = d[:, 0, 3] + bd2 * fac1_l * F[:, 0] * DUU[:, 0] * FG[:, 0] * dur[:, 0] / (V[:, 0] + eps)
+    d[:, 0, 2] = d[:, 0, 2] - half * grav_comp * bd2 * fac1_l * F[:, 0] * DTU[:, 0] * V[:, 0] / (V[:, 0] + eps)
+    d[:, 0, 3] = d[:, 0, 3] - half * grav_comp * bd2 * fac1_l * F[:, 0] * V[:, 0] / (V[:, 0] + eps)
+    for i in range(n1 - 1):  # face i+1 between cells i and i+1, in the reference's loop order
+        q = i + 1
+        S = V[:, i] + V[:, q] + eps
+        a = bd2 * 2.0 * F[:, q] * DTU[:, q] * DUU[:, q] * FG[:, q]
+        b = bd2 * 2.0 * F[:, q] * DUU[:, q] * FG[:, q]
+        u[:, i, 0] = -(a * dut[:, q] / S)
+        u[:, i, 1] = -(b * dut[:, q] / S)
+        l[:, i, 0] = -(a * dut[:, i] / S)
+        l[:, i, 1] = -(b * dut[:, i] / S)
+        if tr:
+            u[:, i, 2] = -(a * dur[:, q] / S)
+            u[:, i, 3] = -(b * dur[:, q] / S)
+            l[:, i, 2] = -(a * dur[:, i] / S)
+            l[:, i, 3] = -(b * dur[:, i] / S)
+        g = grav_comp * bd2 * F[:, q]
+        u[:, i, 2] = u[:, i, 2] - g * DTU[:, q] * V[:, q] / S
+        u[:, i, 3] = u[:, i, 3] - g * V[:, q] / S
+        l[:, i, 2] = l[:, i, 2] + g * DTU[:, q] * V[:, i] / S
+        l[:, i, 3] = l[:, i, 3] + g * V[:, i] / S
+        for c, src in ((i, i), (q, q)):
+            d[:, c, 0] = d[:, c, 0] + a * dut[:, src] / S
+            d[:, c, 1] = d[:, c, 1] + b * dut[:, src] / S
+            if tr:
+                d[:, c, 2] = d[:, c, 2] + a * dur[:, src] / S
+                d[:, c, 3] = d[:, c, 3] + b * dur[:, src] / S
+        d[:, i, 2] = d[:, i, 2] - g * DTU[:, q] * V[:, i] / S
+        d[:, i, 3] = d[:, i, 3] - g * V[:, i] / S
+        d[:, q, 2] = d[:, q, 2] + g * DTU[:, q] * V[:, q] / S
+        d[:, q, 3] = d[:, q, 3] + g * V[:, q] / S
+    c, q = n1 - 1, n1
+    d[:, c, 0] = d[:, c, 0] + bd2 * fac1_r * F[:, q] * DTU[:, q] * DUU[:, q] * FG[:, q] * dut[:, c] / (V[:, c] + eps)
+    if tr:
+        d[:, c, 2] = d[:, c, 2] + bd2 * fac1_r * F[:, q] * DTU[:, q] * DUU[:, q] * FG[:, q] * dur[:, c] / (V[:, c] + eps)
+    d[:, c, 1] = d[:, c, 1] + bd2 * fac1_r * F[:, q] * DUU[:, q] * FG[:, q] * dut[:, c] / (V[:, c] + eps)
+    if tr:
+        d[:, c, 3] = d[:, c, 3] + bd2 * fac1_r * F[:, q] * DUU[:, q] * FG[:, q] * dur[:, c] / (V[:, c] + eps)
+    d[:, c, 2] = d[:, c, 2] + half * grav_comp * bd2 * fac1_r * F[:, q] * DTU[:, q] * V[:, c] / (V[:, c] + eps)
+    d[:, c, 3] = d[:, c, 3] + half * grav_comp * bd2 * fac1_r * F[:, q] * V[:, c] / (V[:, c] + eps)
+    d[:, :, 0] = d[:, :, 0] + fac_anela * V
+    d[:, :, 3] = d[:, :, 3] + V
+    return d, u, l
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("ncol,n1", [(4, 1), (3, 2), (5, 9), (2, 40)])
+def test_oracle_compute_matches_numpy(built_oracle, variant, ncol, n1):
+    """Compute_1D (MULTI/TriDiagTB_Mod.f90:32-93, TriDiagTR_Mod.f90:32-105):
+    the oracle equals the numpy restatement bit for bit."""
+    faces, vol, dut, dur, coefs = compute_inputs(ncol, n1, seed=n1 + (variant == "TR"))
+    dr = dur if variant == "TR" else None
+    got = oracle.tri_tb_compute(*faces[:2], vol, faces[2], faces[3], dut, dr, **coefs)
+    ref = numpy_compute(faces, vol, dut, dr, **coefs)
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)
+
+
+def test_oracle_compute_known_answer(built_oracle):
+    """One cell, no gravity, FacAnela 0: d(1,1) = 1e-40 + the two faces'
+    terms + 0, d(2,2) = 1e-40 + Vol, the other entries 0; the (1,1) block of
+    two cells without boundary faces has the row sums of a difference operator."""
+    F, FG, DTU, DUU = (np.array([[2.0, 3.0]]) for _ in range(4))
+    vol, dut = np.array([[4.0]]), np.array([[0.5]])
+    d, u, l = oracle.tri_tb_compute(F, FG, vol, DTU, DUU, dut, beta0_dtp=1.0, fac1_l=1.0, fac1_r=1.0)
+    assert d[0, 0, 0] == 1e-40 + 2.0 * 2.0 * 2.0 * 2.0 * 0.5 / (4.0 + 1e-30) + 3.0 * 3.0 * 3.0 * 3.0 * 0.5 / (4.0 + 1e-30)
+    # d(2,1): the same terms without DTU
+    assert d[0, 0, 1] == 0.0 + 2.0 * 2.0 * 2.0 * 0.5 / (4.0 + 1e-30) + 3.0 * 3.0 * 3.0 * 0.5 / (4.0 + 1e-30)
+    assert d[0, 0, 3] == 1e-40 + 4.0 and d[0, 0, 2] == 0.0
+    ones = [np.ones((1, 3)) for _ in range(4)]
+    d, u, l = oracle.tri_tb_compute(*ones[:2], np.ones((1, 2)), *ones[2:], np.ones((1, 2)))
+    # (1,1) entries: face between the cells only; d = 1e-40 + 2/(2+eps) each, u = l = -2/(2+eps)
+    assert d[0, :, 0].tolist() == [1e-40 + 1.0, 1e-40 + 1.0] and u[0, 0, 0] == -1.0 and l[0, 0, 0] == -1.0
