@@ -654,6 +654,35 @@ def Compute_TB_1D(f, fg, vol, dtu, duu, dut, dur=None, beta0_dtp: float = 1.0, f
     return d, u, l
 
 
+def Compute_TB_2D(z_faces, x_faces, vol, dut, dur=None, beta0_dtp: float = 1.0, fac1_l: float = 0.0,
+                  fac1_r: float = 0.0, grav_comp: float = 0.0, fac_anela: float = 0.0, fac2_l: float = 0.0,
+                  fac2_r: float = 0.0):
+    """Allocate_2D + Compute_2D of TriDiagTB (dur None) or TriDiagTR on a batch
+    of planes: z_faces = (F1, F1G, DTU1, DUU1) (nplane, n2, n1+1), x_faces =
+    (F2, F2G, DTU2, DUU2) (nplane, n2+1, n1), cells vol, dut, dur (nplane, n2,
+    n1).  Returns d, u1, l1 (the lines) and u2, l2 (between lines)."""
+    lib = _lib.load()
+    zf = [_f64(a) for a in z_faces]
+    xf = [_f64(a) for a in x_faces]
+    cells = [_f64(a) for a in (vol, dut)] + ([_f64(dur)] if dur is not None else [])
+    nplane, n2, n1 = cells[0].shape
+    if (any(a.shape != (nplane, n2, n1 + 1) for a in zf) or any(a.shape != (nplane, n2 + 1, n1) for a in xf)
+            or any(a.shape != (nplane, n2, n1) for a in cells)):
+        raise ValueError("z faces (nplane, n2, n1+1), x faces (nplane, n2+1, n1), cells (nplane, n2, n1)")
+    d = np.empty((nplane, n2, n1, 4))
+    u1 = np.empty((nplane, n2, max(n1 - 1, 0), 4))
+    l1 = np.empty_like(u1)
+    u2 = np.empty((nplane, max(n2 - 1, 0), n1, 4))
+    l2 = np.empty_like(u2)
+    co = _lib.AsamTriTbCoefs(beta0_dtp, fac1_l, fac1_r, grav_comp, fac_anela, fac2_l, fac2_r)
+    opt = lambda a: ptr(a) if a.size else None  # noqa: E731
+    check(lib.asam_tri_tb_compute_2d(int(dur is not None), nplane, n2, n1, C.byref(co), *[ptr(a) for a in zf],
+                                     *[ptr(a) for a in xf], ptr(cells[0]), ptr(cells[1]),
+                                     ptr(cells[2]) if dur is not None else None, ptr(d), opt(u1), opt(l1), opt(u2),
+                                     opt(l2)), "asam_tri_tb_compute_2d")
+    return d, u1, l1, u2, l2
+
+
 def MatVecTB_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, x: np.ndarray) -> np.ndarray:
     lib = _lib.load()
     d, u, l, xx = _f64(d), _f64(u), _f64(l), _f64(x)

@@ -207,6 +207,154 @@ __global__ void k_tri_tb_compute(int tr, int ncol, int n1, asam_tri_tb_coefs s, 
   }
 }
 
+// Compute_2D (MULTI/TriDiagTB_Mod.f90:260-343; TriDiagTR_Mod.f90:273-387) over
+// planes, one thread per element (plane p, line j, level i).  Every entry is
+// a sum whose terms the reference adds in a fixed order: its line's
+// Compute_1D (the first z face, the face below as the upper cell, the face
+// above as the lower cell, the last z face, FacAnela/Vol), then the faces
+// between lines (Fac2_L on line 1, the face to the line before, the face to
+// the line after, Fac2_R on the last line).  The thread adds them in that
+// order, so the entries equal the reference's line-by-line sweep bit for bit
+// while all elements are assembled at once.
+__global__ void k_tri_tb_compute_2d(int tr, int nplane, int n2, int n1, asam_tri_tb_coefs s,
+                                    const double* __restrict__ f1, const double* __restrict__ f1g,
+                                    const double* __restrict__ dtu1, const double* __restrict__ duu1,
+                                    const double* __restrict__ f2, const double* __restrict__ f2g,
+                                    const double* __restrict__ dtu2, const double* __restrict__ duu2,
+                                    const double* __restrict__ vol, const double* __restrict__ dut,
+                                    const double* __restrict__ dur, double* __restrict__ d, double* __restrict__ u1,
+                                    double* __restrict__ l1, double* __restrict__ u2, double* __restrict__ l2) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)nplane * n2 * n1) return;
+  const int i = (int)(e % n1);
+  const size_t line = e / n1;  // p*n2 + j
+  const int j = (int)(line % n2);
+  const size_t p = line / n2;
+  const double bd = s.beta0_dtp, fl = s.fac1_l, fr = s.fac1_r, grav = s.grav_comp, anela = s.fac_anela;
+  const double bd2 = bd * bd, half = 0.5, eps = 1.0e-30;
+  // this line's z faces and cells
+  const double *F = f1 + line * (n1 + 1), *FG = f1g + line * (n1 + 1);
+  const double *DTU = dtu1 + line * (n1 + 1), *DUU = duu1 + line * (n1 + 1);
+  const double *V = vol + line * n1, *DUT = dut + line * n1;
+  const double* DUR = tr ? dur + line * n1 : nullptr;
+  // ---- Compute_1D of the line: entry i
+  double e0 = 1.0e-40, e1 = 0.0, e2 = 0.0, e3 = 1.0e-40;
+  if (i == 0) {
+    e0 = e0 + bd2 * fl * F[0] * DTU[0] * DUU[0] * FG[0] * DUT[0] / (V[0] + eps);
+    if (tr) e2 = e2 + bd2 * fl * F[0] * DTU[0] * DUU[0] * FG[0] * DUR[0] / (V[0] + eps);
+    e1 = e1 + bd2 * fl * F[0] * DUU[0] * FG[0] * DUT[0] / (V[0] + eps);
+    if (tr) e3 = e3 + bd2 * fl * F[0] * DUU[0] * FG[0] * DUR[0] / (V[0] + eps);
+    e2 = e2 - half * grav * bd2 * fl * F[0] * DTU[0] * V[0] / (V[0] + eps);
+    e3 = e3 - half * grav * bd2 * fl * F[0] * V[0] / (V[0] + eps);
+  }
+  if (i > 0) {  // face i, entry i as its upper cell
+    const int q = i, c = i - 1;
+    const double S = V[c] + V[q] + eps;
+    e0 = e0 + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[q] / S;
+    if (tr) e2 = e2 + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[q] / S;
+    e1 = e1 + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[q] / S;
+    if (tr) e3 = e3 + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[q] / S;
+    e2 = e2 + grav * bd2 * F[q] * DTU[q] * V[q] / S;
+    e3 = e3 + grav * bd2 * F[q] * V[q] / S;
+  }
+  if (i < n1 - 1) {  // face i+1, entry i as its lower cell; the couplings of that face
+    const int q = i + 1;
+    const double S = V[i] + V[q] + eps;
+    double* U = u1 + (line * (n1 - 1) + i) * 4;
+    double* L = l1 + (line * (n1 - 1) + i) * 4;
+    U[0] = -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[q] / S);
+    double u12 = tr ? -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[q] / S) : 0.0;
+    U[1] = -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[q] / S);
+    double u22 = tr ? -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[q] / S) : 0.0;
+    L[0] = -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[i] / S);
+    double l12 = tr ? -(bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[i] / S) : 0.0;
+    L[1] = -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[i] / S);
+    double l22 = tr ? -(bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[i] / S) : 0.0;
+    U[2] = u12 - grav * bd2 * F[q] * DTU[q] * V[q] / S;
+    U[3] = u22 - grav * bd2 * F[q] * V[q] / S;
+    L[2] = l12 + grav * bd2 * F[q] * DTU[q] * V[i] / S;
+    L[3] = l22 + grav * bd2 * F[q] * V[i] / S;
+    e0 = e0 + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[i] / S;
+    if (tr) e2 = e2 + bd2 * 2.0 * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[i] / S;
+    e1 = e1 + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUT[i] / S;
+    if (tr) e3 = e3 + bd2 * 2.0 * F[q] * DUU[q] * FG[q] * DUR[i] / S;
+    e2 = e2 - grav * bd2 * F[q] * DTU[q] * V[i] / S;
+    e3 = e3 - grav * bd2 * F[q] * V[i] / S;
+  }
+  if (i == n1 - 1) {
+    const int c = i, q = n1;
+    e0 = e0 + bd2 * fr * F[q] * DTU[q] * DUU[q] * FG[q] * DUT[c] / (V[c] + eps);
+    if (tr) e2 = e2 + bd2 * fr * F[q] * DTU[q] * DUU[q] * FG[q] * DUR[c] / (V[c] + eps);
+    e1 = e1 + bd2 * fr * F[q] * DUU[q] * FG[q] * DUT[c] / (V[c] + eps);
+    if (tr) e3 = e3 + bd2 * fr * F[q] * DUU[q] * FG[q] * DUR[c] / (V[c] + eps);
+    e2 = e2 + half * grav * bd2 * fr * F[q] * DTU[q] * V[c] / (V[c] + eps);
+    e3 = e3 + half * grav * bd2 * fr * F[q] * V[c] / (V[c] + eps);
+  }
+  e0 = e0 + anela * V[i];
+  e3 = e3 + V[i];
+  // ---- the faces between lines: face j (to line j-1) and face j+1 (to line j+1)
+  const double* F2 = f2 + p * (n2 + 1) * n1;
+  const double* F2G = f2g + p * (n2 + 1) * n1;
+  const double* DTU2 = dtu2 + p * (n2 + 1) * n1;
+  const double* DUU2 = duu2 + p * (n2 + 1) * n1;
+  const double* Vp = vol + p * n2 * n1;
+  const double* DUTp = dut + p * n2 * n1;
+  const double* DURp = tr ? dur + p * n2 * n1 : nullptr;
+  auto fc = [&](const double* a, int jf) { return a[(size_t)jf * n1 + i]; };  // face jf of level i
+  auto cl = [&](const double* a, int jc) { return a[(size_t)jc * n1 + i]; };  // cell (i, jc)
+  if (j == 0) {
+    const double a = bd2 * s.fac2_l * fc(F2, 0) * fc(DTU2, 0) * fc(DUU2, 0) * fc(F2G, 0);
+    const double b = bd2 * s.fac2_l * fc(F2, 0) * fc(DUU2, 0) * fc(F2G, 0);
+    const double den = cl(Vp, 0) + eps;
+    e0 = e0 + a * cl(DUTp, 0) / den;
+    if (tr) e2 = e2 + a * cl(DURp, 0) / den;
+    e1 = e1 + b * cl(DUTp, 0) / den;
+    if (tr) e3 = e3 + b * cl(DURp, 0) / den;
+  }
+  if (j > 0) {  // face j, this line as the upper one
+    const int q = j, c = j - 1;
+    const double S = cl(Vp, c) + cl(Vp, q) + eps;
+    const double a = bd2 * 2.0 * fc(F2, q) * fc(DTU2, q) * fc(DUU2, q) * fc(F2G, q);
+    const double b = bd2 * 2.0 * fc(F2, q) * fc(DUU2, q) * fc(F2G, q);
+    e0 = e0 + a * cl(DUTp, q) / S;
+    if (tr) e2 = e2 + a * cl(DURp, q) / S;
+    e1 = e1 + b * cl(DUTp, q) / S;
+    if (tr) e3 = e3 + b * cl(DURp, q) / S;
+  }
+  if (j < n2 - 1) {  // face j+1, this line as the lower one; the couplings between the lines
+    const int q = j + 1;
+    const double S = cl(Vp, j) + cl(Vp, q) + eps;
+    const double a = bd2 * 2.0 * fc(F2, q) * fc(DTU2, q) * fc(DUU2, q) * fc(F2G, q);
+    const double b = bd2 * 2.0 * fc(F2, q) * fc(DUU2, q) * fc(F2G, q);
+    double* U = u2 + ((p * (n2 - 1) + j) * n1 + i) * 4;
+    double* L = l2 + ((p * (n2 - 1) + j) * n1 + i) * 4;
+    U[0] = -(a * cl(DUTp, q) / S);
+    U[2] = tr ? -(a * cl(DURp, q) / S) : 0.0;
+    U[1] = -(b * cl(DUTp, q) / S);
+    U[3] = tr ? -(b * cl(DURp, q) / S) : 0.0;
+    L[0] = -(a * cl(DUTp, j) / S);
+    L[2] = tr ? -(a * cl(DURp, j) / S) : 0.0;
+    L[1] = -(b * cl(DUTp, j) / S);
+    L[3] = tr ? -(b * cl(DURp, j) / S) : 0.0;
+    e0 = e0 + a * cl(DUTp, j) / S;
+    if (tr) e2 = e2 + a * cl(DURp, j) / S;
+    e1 = e1 + b * cl(DUTp, j) / S;
+    if (tr) e3 = e3 + b * cl(DURp, j) / S;
+  }
+  if (j == n2 - 1) {
+    const int q = n2;
+    const double a = bd2 * s.fac2_r * fc(F2, q) * fc(DTU2, q) * fc(DUU2, q) * fc(F2G, q);
+    const double b = bd2 * s.fac2_r * fc(F2, q) * fc(DUU2, q) * fc(F2G, q);
+    const double den = cl(Vp, j) + eps;
+    e0 = e0 + a * cl(DUTp, j) / den;
+    if (tr) e2 = e2 + a * cl(DURp, j) / den;
+    e1 = e1 + b * cl(DUTp, j) / den;
+    if (tr) e3 = e3 + b * cl(DURp, j) / den;
+  }
+  double* D = d + e * 4;
+  D[0] = e0, D[1] = e1, D[2] = e2, D[3] = e3;
+}
+
 struct DevBufs {
   double* p[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   ~DevBufs() {
@@ -264,6 +412,49 @@ int asam_tri_tb_compute(int variant, int ncol, int n1, const asam_tri_tb_coefs* 
   if (no) {
     TCU(cudaMemcpy(u, du, no * sizeof(double), cudaMemcpyDefault));
     TCU(cudaMemcpy(l, dl, no * sizeof(double), cudaMemcpyDefault));
+  }
+  return ASAM_OK;
+}
+
+int asam_tri_tb_compute_2d(int variant, int nplane, int n2, int n1, const asam_tri_tb_coefs* coefs,
+                           const double* f1, const double* f1g, const double* dtu1, const double* duu1,
+                           const double* f2, const double* f2g, const double* dtu2, const double* duu2,
+                           const double* vol, const double* dut, const double* dur, double* d, double* u1,
+                           double* l1, double* u2, double* l2) {
+  if ((variant != 0 && variant != 1) || nplane < 1 || n2 < 1 || n1 < 1 || !coefs || !f1 || !f1g || !dtu1 ||
+      !duu1 || !f2 || !f2g || !dtu2 || !duu2 || !vol || !dut || (variant == 1 && !dur) || !d ||
+      (n1 > 1 && (!u1 || !l1)) || (n2 > 1 && (!u2 || !l2))) {
+    asam::set_last_error("asam_tri_tb_compute_2d: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  const size_t nl = (size_t)nplane * n2, nz = nl * (n1 + 1), nx = (size_t)nplane * (n2 + 1) * n1;
+  const size_t nc = nl * n1, nd = nc * 4, no1 = nl * (n1 - 1) * 4, no2 = (size_t)nplane * (n2 - 1) * n1 * 4;
+  DevBufs m;
+  TCU(cudaMalloc((void**)&m.p[0], (4 * nz + 4 * nx + 3 * nc) * sizeof(double)));
+  TCU(cudaMalloc((void**)&m.p[1], (nd + 2 * no1 + 2 * no2 + 1) * sizeof(double)));
+  const double* src[11] = {f1, f1g, dtu1, duu1, f2, f2g, dtu2, duu2, vol, dut, variant == 1 ? dur : vol};
+  const size_t len[11] = {nz, nz, nz, nz, nx, nx, nx, nx, nc, nc, nc};
+  double* dev[11];
+  size_t off = 0;
+  for (int q = 0; q < 11; ++q) {
+    dev[q] = m.p[0] + off;
+    TCU(cudaMemcpy(dev[q], src[q], len[q] * sizeof(double), cudaMemcpyDefault));
+    off += len[q];
+  }
+  double *dd = m.p[1], *du1 = dd + nd, *dl1 = du1 + no1, *du2 = dl1 + no1, *dl2 = du2 + no2;
+  k_tri_tb_compute_2d<<<(unsigned)((nc + 255) / 256), 256>>>(variant, nplane, n2, n1, *coefs, dev[0], dev[1], dev[2],
+                                                              dev[3], dev[4], dev[5], dev[6], dev[7], dev[8], dev[9],
+                                                              dev[10], dd, du1, dl1, du2, dl2);
+  asam::count_launches(1);
+  TCU(cudaGetLastError());
+  TCU(cudaMemcpy(d, dd, nd * sizeof(double), cudaMemcpyDefault));
+  if (no1) {
+    TCU(cudaMemcpy(u1, du1, no1 * sizeof(double), cudaMemcpyDefault));
+    TCU(cudaMemcpy(l1, dl1, no1 * sizeof(double), cudaMemcpyDefault));
+  }
+  if (no2) {
+    TCU(cudaMemcpy(u2, du2, no2 * sizeof(double), cudaMemcpyDefault));
+    TCU(cudaMemcpy(l2, dl2, no2 * sizeof(double), cudaMemcpyDefault));
   }
   return ASAM_OK;
 }

@@ -576,10 +576,30 @@ typedef struct {
   double fac1_r;    /* Fac1_R, the weight of the last face */
   double grav_comp; /* GravComp */
   double fac_anela; /* FacAnela */
+  double fac2_l;    /* Fac2_L, the weight of the first face between lines (asam_tri_tb_compute_2d) */
+  double fac2_r;    /* Fac2_R, the weight of the last one */
 } asam_tri_tb_coefs;
 int asam_tri_tb_compute(int variant, int ncol, int n1, const asam_tri_tb_coefs *coefs, const double *f,
                         const double *fg, const double *vol, const double *dtu, const double *duu, const double *dut,
                         const double *dur, double *d, double *u, double *l);
+
+/* Assembly of the plane systems: Allocate_2D and Compute_2D of
+ * MULTI/TriDiagTB_Mod.f90:221-343 (variant 0) or MULTI/TriDiagTR_Mod.f90:230-387
+ * (variant 1) on nplane planes of n2 lines of n1 levels.  Per plane p:
+ * z faces f1, f1g, dtu1, duu1 [(p*n2 + j)*(n1+1) + i]; the faces between
+ * lines f2, f2g, dtu2, duu2 [(p*(n2+1) + j)*n1 + i] (F2, F2G, DTU2, DUU2 of
+ * faces 1..n2+1); cells vol, dut, dur [(p*n2 + j)*n1 + i].  Out: the lines'
+ * blocks d [(p*n2 + j)*n1 + i][4] and couplings u1, l1
+ * [(p*n2 + j)*(n1-1) + i][4] (as asam_tri_tb_compute per line), and the
+ * couplings between lines j and j+1, u2, l2 [(p*(n2-1) + j)*n1 + i][4]
+ * (TriDiagTB's are a vector, the first block column; entries 2 and 3 are
+ * 0).  Bit for bit the reference's line-by-line sweep, all elements at once.
+ * Host or device pointers. */
+int asam_tri_tb_compute_2d(int variant, int nplane, int n2, int n1, const asam_tri_tb_coefs *coefs,
+                           const double *f1, const double *f1g, const double *dtu1, const double *duu1,
+                           const double *f2, const double *f2g, const double *dtu2, const double *duu2,
+                           const double *vol, const double *dut, const double *dur, double *d, double *u1,
+                           double *l1, double *u2, double *l2);
 
 /* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141),
  * the same as MatVecTR_1D (MULTI/TriDiagTR_Mod.f90:133-153). */

@@ -63,6 +63,7 @@ def load() -> C.CDLL:
             "ora_tri_tb_solve": (None, [I, I, V, V, V, V, V]),
             "ora_tri_tb_matvec": (None, [I, I, V, V, V, V, V]),
             "ora_tri_tb_compute": (None, [I, I, I] + [V] * 11),
+            "ora_tri_tb_compute_2d": (None, [I, I, I, I] + [V] * 17),
             "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
         }
         sig.update({
@@ -408,6 +409,31 @@ def tri_tb_compute(f, fg, vol, dtu, duu, dut, dur=None, beta0_dtp=1.0, fac1_l=0.
     lib.ora_tri_tb_compute(int(tr), ncol, n1, _p(s), _p(faces[0]), _p(faces[1]), _p(vol), _p(faces[2]),
                            _p(faces[3]), _p(dut), _p(durr), _p(d), _p(u), _p(l))
     return d, u[:, :n1 - 1], l[:, :n1 - 1]
+
+
+def tri_tb_compute_2d(z_faces, x_faces, vol, dut, dur=None, beta0_dtp=1.0, fac1_l=0.0, fac1_r=0.0, grav_comp=0.0,
+                      fac_anela=0.0, fac2_l=0.0, fac2_r=0.0):
+    """Allocate_2D + Compute_2D of TriDiagTB (dur None, MULTI/TriDiagTB_Mod.f90:260-343)
+    or TriDiagTR (MULTI/TriDiagTR_Mod.f90:273-387) on planes: z_faces = (F1, F1G,
+    DTU1, DUU1) each (nplane, n2, n1+1), x_faces = (F2, F2G, DTU2, DUU2) each
+    (nplane, n2+1, n1), cells (nplane, n2, n1).  Returns d (nplane, n2, n1, 4),
+    u1, l1 (nplane, n2, n1-1, 4), u2, l2 (nplane, n2-1, n1, 4)."""
+    lib = load()
+    zf = [np.ascontiguousarray(a, dtype=np.float64) for a in z_faces]
+    xf = [np.ascontiguousarray(a, dtype=np.float64) for a in x_faces]
+    vol, dut = (np.ascontiguousarray(a, dtype=np.float64) for a in (vol, dut))
+    tr = dur is not None
+    durr = np.ascontiguousarray(dur, dtype=np.float64) if tr else vol
+    nplane, n2, n1 = vol.shape
+    s = np.array([beta0_dtp, fac1_l, fac1_r, grav_comp, fac_anela, fac2_l, fac2_r])
+    d = np.empty((nplane, n2, n1, 4))
+    u1 = np.empty((nplane, n2, max(n1 - 1, 1), 4))
+    l1 = np.empty_like(u1)
+    u2 = np.empty((nplane, max(n2 - 1, 1), n1, 4))
+    l2 = np.empty_like(u2)
+    lib.ora_tri_tb_compute_2d(int(tr), nplane, n2, n1, _p(s), *[_p(a) for a in zf], *[_p(a) for a in xf], _p(vol),
+                              _p(dut), _p(durr), _p(d), _p(u1), _p(l1), _p(u2), _p(l2))
+    return d, u1[:, :, :n1 - 1], l1[:, :, :n1 - 1], u2[:, :n2 - 1], l2[:, :n2 - 1]
 
 
 class OracleProj:

@@ -189,3 +189,96 @@ void ora_tri_tb_compute(int variant, int ncol, int n1, const double *s, const do
 #undef LL
   }
 }
+
+/* Compute_2D of the plane systems (MULTI/TriDiagTB_Mod.f90:260-343, variant 0;
+ * MULTI/TriDiagTR_Mod.f90:273-387, variant 1): per plane, line 1's Compute_1D
+ * and its Fac2_L terms, then for every face j+1 between lines j and j+1 the
+ * couplings u2/l2, line j's share, line j+1's Compute_1D and line j+1's share,
+ * finally line n2's Fac2_R terms -- the reference's loops as they stand.
+ * s = {beta0*dtp, Fac1_L, Fac1_R, GravComp, FacAnela, Fac2_L, Fac2_R}.
+ * Per plane p: z faces f1, f1g, dtu1, duu1 [(p*n2 + j)*(n1+1) + i]; faces
+ * between lines f2, f2g, dtu2, duu2 [(p*(n2+1) + j)*n1 + i]; cells vol, dut,
+ * dur [(p*n2 + j)*n1 + i].  Out: d [(p*n2 + j)*n1 + i][4] and u1, l1
+ * [(p*n2 + j)*(n1-1) + i][4] of the lines; u2, l2 [(p*(n2-1) + j)*n1 + i][4]
+ * between lines j and j+1 (TriDiagTB keeps the first block column, entries
+ * 2 and 3 are 0). */
+void ora_tri_tb_compute_2d(int variant, int nplane, int n2, int n1, const double *s, const double *f1,
+                           const double *f1g, const double *dtu1, const double *duu1, const double *f2,
+                           const double *f2g, const double *dtu2, const double *duu2, const double *vol,
+                           const double *dut, const double *dur, double *d, double *u1, double *l1, double *u2,
+                           double *l2) {
+  const double bd = s[0], fac2l = s[5], fac2r = s[6];
+  const double bd2 = bd * bd, eps = 1.0e-30;
+  const int tr = variant == 1;
+  for (int p = 0; p < nplane; ++p) {
+    const size_t lines = (size_t)p * n2;
+    const double *F2 = f2 + (size_t)p * (n2 + 1) * n1, *F2G = f2g + (size_t)p * (n2 + 1) * n1;
+    const double *DTU2 = dtu2 + (size_t)p * (n2 + 1) * n1, *DUU2 = duu2 + (size_t)p * (n2 + 1) * n1;
+    const double *V = vol + lines * n1, *DUT = dut + lines * n1, *DUR = tr ? dur + lines * n1 : 0;
+    double *D = d + lines * n1 * 4;
+    double *U2 = u2 + (size_t)p * (n2 - 1) * n1 * 4, *L2 = l2 + (size_t)p * (n2 - 1) * n1 * 4;
+#define LINE(j)                                                                                                  \
+  ora_tri_tb_compute(variant, 1, n1, s, f1 + (lines + (j)) * (n1 + 1), f1g + (lines + (j)) * (n1 + 1),        \
+                     vol + (lines + (j)) * n1, dtu1 + (lines + (j)) * (n1 + 1), duu1 + (lines + (j)) * (n1 + 1), \
+                     dut + (lines + (j)) * n1, tr ? dur + (lines + (j)) * n1 : 0, d + (lines + (j)) * n1 * 4,    \
+                     u1 + (lines + (j)) * (n1 - 1) * 4, l1 + (lines + (j)) * (n1 - 1) * 4)
+#define DD(i, j, e) D[((size_t)(j) * n1 + (i)) * 4 + (e)]
+#define CELL(a, i, j) a[(size_t)(j) * n1 + (i)]
+#define FACE(a, i, j) a[(size_t)(j) * n1 + (i)]
+    LINE(0);
+    for (int i = 0; i < n1; ++i) {
+      const double a = bd2 * fac2l * FACE(F2, i, 0) * FACE(DTU2, i, 0) * FACE(DUU2, i, 0) * FACE(F2G, i, 0);
+      const double b = bd2 * fac2l * FACE(F2, i, 0) * FACE(DUU2, i, 0) * FACE(F2G, i, 0);
+      const double den = CELL(V, i, 0) + eps;
+      DD(i, 0, 0) = DD(i, 0, 0) + a * CELL(DUT, i, 0) / den;
+      if (tr) DD(i, 0, 2) = DD(i, 0, 2) + a * CELL(DUR, i, 0) / den;
+      DD(i, 0, 1) = DD(i, 0, 1) + b * CELL(DUT, i, 0) / den;
+      if (tr) DD(i, 0, 3) = DD(i, 0, 3) + b * CELL(DUR, i, 0) / den;
+    }
+    for (int j = 0; j < n2 - 1; ++j) {
+      const int q = j + 1;
+      for (int i = 0; i < n1; ++i) {
+        const double S = CELL(V, i, j) + CELL(V, i, q) + eps;
+        const double a = bd2 * 2.0 * FACE(F2, i, q) * FACE(DTU2, i, q) * FACE(DUU2, i, q) * FACE(F2G, i, q);
+        const double b = bd2 * 2.0 * FACE(F2, i, q) * FACE(DUU2, i, q) * FACE(F2G, i, q);
+        double *u = U2 + ((size_t)j * n1 + i) * 4, *l = L2 + ((size_t)j * n1 + i) * 4;
+        u[0] = -(a * CELL(DUT, i, q) / S);
+        u[2] = tr ? -(a * CELL(DUR, i, q) / S) : 0.0;
+        u[1] = -(b * CELL(DUT, i, q) / S);
+        u[3] = tr ? -(b * CELL(DUR, i, q) / S) : 0.0;
+        l[0] = -(a * CELL(DUT, i, j) / S);
+        l[2] = tr ? -(a * CELL(DUR, i, j) / S) : 0.0;
+        l[1] = -(b * CELL(DUT, i, j) / S);
+        l[3] = tr ? -(b * CELL(DUR, i, j) / S) : 0.0;
+        DD(i, j, 0) = DD(i, j, 0) + a * CELL(DUT, i, j) / S;
+        if (tr) DD(i, j, 2) = DD(i, j, 2) + a * CELL(DUR, i, j) / S;
+        DD(i, j, 1) = DD(i, j, 1) + b * CELL(DUT, i, j) / S;
+        if (tr) DD(i, j, 3) = DD(i, j, 3) + b * CELL(DUR, i, j) / S;
+      }
+      LINE(q);
+      for (int i = 0; i < n1; ++i) {
+        const double S = CELL(V, i, j) + CELL(V, i, q) + eps;
+        const double a = bd2 * 2.0 * FACE(F2, i, q) * FACE(DTU2, i, q) * FACE(DUU2, i, q) * FACE(F2G, i, q);
+        const double b = bd2 * 2.0 * FACE(F2, i, q) * FACE(DUU2, i, q) * FACE(F2G, i, q);
+        DD(i, q, 0) = DD(i, q, 0) + a * CELL(DUT, i, q) / S;
+        if (tr) DD(i, q, 2) = DD(i, q, 2) + a * CELL(DUR, i, q) / S;
+        DD(i, q, 1) = DD(i, q, 1) + b * CELL(DUT, i, q) / S;
+        if (tr) DD(i, q, 3) = DD(i, q, 3) + b * CELL(DUR, i, q) / S;
+      }
+    }
+    for (int i = 0; i < n1; ++i) {
+      const int j = n2 - 1, q = n2;
+      const double a = bd2 * fac2r * FACE(F2, i, q) * FACE(DTU2, i, q) * FACE(DUU2, i, q) * FACE(F2G, i, q);
+      const double b = bd2 * fac2r * FACE(F2, i, q) * FACE(DUU2, i, q) * FACE(F2G, i, q);
+      const double den = CELL(V, i, j) + eps;
+      DD(i, j, 0) = DD(i, j, 0) + a * CELL(DUT, i, j) / den;
+      if (tr) DD(i, j, 2) = DD(i, j, 2) + a * CELL(DUR, i, j) / den;
+      DD(i, j, 1) = DD(i, j, 1) + b * CELL(DUT, i, j) / den;
+      if (tr) DD(i, j, 3) = DD(i, j, 3) + b * CELL(DUR, i, j) / den;
+    }
+#undef LINE
+#undef DD
+#undef CELL
+#undef FACE
+  }
+}

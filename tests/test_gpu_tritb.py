@@ -54,3 +54,18 @@ def test_tri_tb_compute_bitwise(built_lib, variant, ncol, n1):
     lib = _lib.load()
     co = _lib.AsamTriTbCoefs(1.0, 0.0, 0.0, 0.0, 0.0)
     assert lib.asam_tri_tb_compute(2, 1, 1, co, None, None, None, None, None, None, None, None, None, None) == 4
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("nplane,n2,n1", [(1, 1, 1), (2, 3, 4), (3, 1, 5), (2, 5, 1), (16, 64, 32), (4, 256, 128)])
+def test_tri_tb_compute_2d_bitwise(built_lib, variant, nplane, n2, n1):
+    """Compute_2D of TriDiagTB / TriDiagTR, every element at once on the GPU,
+    equals the oracle's line-by-line sweep bit for bit."""
+    from tests.test_tritb import compute_inputs_2d
+
+    zf, xf, vol, dut, dur, coefs = compute_inputs_2d(nplane, n2, n1, seed=5 * n2 + n1 + nplane)
+    dr = dur if variant == "TR" else None
+    got = asam.Compute_TB_2D(zf, xf, vol, dut, dr, **coefs)
+    ref = oracle.tri_tb_compute_2d(zf, xf, vol, dut, dr, **coefs)
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)

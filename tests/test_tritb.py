@@ -162,3 +162,98 @@ def test_oracle_compute_known_answer(built_oracle):
     d, u, l = oracle.tri_tb_compute(*ones[:2], np.ones((1, 2)), *ones[2:], np.ones((1, 2)))
     # (1,1) entries: face between the cells only; d = 1e-40 + 2/(2+eps) each, u = l = -2/(2+eps)
     assert d[0, :, 0].tolist() == [1e-40 + 1.0, 1e-40 + 1.0] and u[0, 0, 0] == -1.0 and l[0, 0, 0] == -1.0
+
+
+def compute_inputs_2d(nplane, n2, n1, seed):
+    r = np.random.default_rng(seed)
+    zf = [r.uniform(0.2, 2.0, (nplane, n2, n1 + 1)) for _ in range(4)]  # F1, F1G, DTU1, DUU1
+    xf = [r.uniform(0.2, 2.0, (nplane, n2 + 1, n1)) for _ in range(4)]  # F2, F2G, DTU2, DUU2
+    vol = r.uniform(0.5, 3.0, (nplane, n2, n1))
+    dut = r.uniform(0.1, 1.5, (nplane, n2, n1))
+    dur = r.uniform(-0.5, 0.5, (nplane, n2, n1))
+    coefs = dict(beta0_dtp=r.uniform(0.3, 3.0), fac1_l=2.0, fac1_r=1.0, grav_comp=9.81, fac_anela=0.25, fac2_l=1.0,
+                 fac2_r=2.0)
+    return zf, xf, vol, dut, dur, coefs
+
+
+def numpy_compute_2d(zf, xf, vol, dut, dur, fac2_l, fac2_r, **c1):
+    """Compute_2D restated: every line's Compute_1D (numpy_compute over all
+    lines as columns), then the faces between lines in the order the
+    reference adds them to an entry -- Fac2_L on the first line, the face to
+    the line before, the face to the line after, Fac2_R on the last line."""
+    nplane, n2, n1 = vol.shape
+    tr = dur is not None
+    flat = lambda a: a.reshape(nplane * n2, -1)  # noqa: E731
+    d, u1, l1 = numpy_compute([flat(a) for a in zf], flat(vol), flat(dut), flat(dur) if tr else None, **c1)
+    d = d.reshape(nplane, n2, n1, 4)
+    u1 = u1.reshape(nplane, n2, n1 - 1, 4)
+    l1 = l1.reshape(nplane, n2, n1 - 1, 4)
+    F2, F2G, DTU2, DUU2 = xf
+    bd2 = c1["beta0_dtp"] * c1["beta0_dtp"]
+    eps = 1e-30
+    u2 = np.zeros((nplane, n2 - 1, n1, 4))
+    l2 = np.zeros_like(u2)
+
+    def add(jc, jf, fac, den):
+        a = bd2 * fac * F2[:, jf] * DTU2[:, jf] * DUU2[:, jf] * F2G[:, jf]
+        b = bd2 * fac * F2[:, jf] * DUU2[:, jf] * F2G[:, jf]
+        d[:, jc, :, 0] = d[:, jc, :, 0] + a * dut[:, jc] / den
+        if tr:
+            d[:, jc, :, 2] = d[:, jc, :, 2] + a * dur[:, jc] / den
+        d[:, jc, :, 1] = d[:, jc, :, 1] + b * dut[:, jc] / den
+        if tr:
+            d[:, jc, :, 3] = d[:, jc, :, 3] + b * dur[:, jc] / den
+
+    add(0, 0, fac2_l, vol[:, 0] + eps)
+    for j in range(1, n2):  # face j, line j as the upper one
+        add(j, j, 2.0, vol[:, j - 1] + vol[:, j] + eps)
+    for j in range(n2 - 1):  # face j+1, line j as the lower one, and the couplings
+        q = j + 1
+        S = vol[:, j] + vol[:, q] + eps
+        a = bd2 * 2.0 * F2[:, q] * DTU2[:, q] * DUU2[:, q] * F2G[:, q]
+        b = bd2 * 2.0 * F2[:, q] * DUU2[:, q] * F2G[:, q]
+        u2[:, j, :, 0], u2[:, j, :, 1] = -(a * dut[:, q] / S), -(b * dut[:, q] / S)
+        l2[:, j, :, 0], l2[:, j, :, 1] = -(a * dut[:, j] / S), -(b * dut[:, j] / S)
+        if tr:
+            u2[:, j, :, 2], u2[:, j, :, 3] = -(a * dur[:, q] / S), -(b * dur[:, q] / S)
+            l2[:, j, :, 2], l2[:, j, :, 3] = -(a * dur[:, j] / S), -(b * dur[:, j] / S)
+        add(j, q, 2.0, S)
+    add(n2 - 1, n2, fac2_r, vol[:, n2 - 1] + eps)
+    return d, u1, l1, u2, l2
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("nplane,n2,n1", [(1, 1, 1), (2, 3, 4), (3, 1, 5), (2, 5, 1), (2, 6, 9)])
+def test_oracle_compute_2d_matches_numpy(built_oracle, variant, nplane, n2, n1):
+    """Compute_2D (MULTI/TriDiagTB_Mod.f90:260-343, TriDiagTR_Mod.f90:273-387):
+    the oracle's line-by-line sweep equals the numpy restatement bit for bit;
+    one line per plane without Fac2 terms is Compute_1D of that line."""
+    zf, xf, vol, dut, dur, coefs = compute_inputs_2d(nplane, n2, n1, seed=7 * n2 + n1)
+    dr = dur if variant == "TR" else None
+    got = oracle.tri_tb_compute_2d(zf, xf, vol, dut, dr, **coefs)
+    ref = numpy_compute_2d(zf, xf, vol, dut, dr, **coefs)
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)
+    if n2 == 1:
+        c1 = {k: v for k, v in coefs.items() if k not in ("fac2_l", "fac2_r")}
+        one = oracle.tri_tb_compute_2d(zf, xf, vol, dut, dr, **c1)
+        line = oracle.tri_tb_compute(*[a[:, 0] for a in zf[:2]], vol[:, 0], *[a[:, 0] for a in zf[2:]], dut[:, 0],
+                                     None if dr is None else dr[:, 0], **c1)
+        assert np.array_equal(one[0][:, 0], line[0]) and np.array_equal(one[1][:, 0], line[1])
+
+
+def test_oracle_compute_2d_uniform(built_oracle):
+    """All faces, weights and volumes 1, no boundary faces, no gravity: every
+    face between two cells adds 2/(2+eps) = 1 to both cells' (1,1) entry, so
+    the (1,1) diagonal counts each cell's neighbours."""
+    nplane, n2, n1 = 1, 3, 4
+    zf = [np.ones((nplane, n2, n1 + 1)) for _ in range(4)]
+    xf = [np.ones((nplane, n2 + 1, n1)) for _ in range(4)]
+    d, u1, l1, u2, l2 = oracle.tri_tb_compute_2d(zf, xf, np.ones((nplane, n2, n1)), np.ones((nplane, n2, n1)))
+    nb = np.zeros((n2, n1))
+    nb[:, :-1] += 1
+    nb[:, 1:] += 1
+    nb[:-1, :] += 1
+    nb[1:, :] += 1
+    assert np.array_equal(d[0, :, :, 0], 1e-40 + nb)
+    assert (u1[..., 0] == -1.0).all() and (u2[..., 0] == -1.0).all() and (l2[..., 2] == 0.0).all()
