@@ -683,6 +683,35 @@ def Compute_TB_2D(z_faces, x_faces, vol, dut, dur=None, beta0_dtp: float = 1.0, 
     return d, u1, l1, u2, l2
 
 
+def Compute_TB_3D(z_faces, x_faces, y_faces, vol, dut, dur=None, couple: bool = True, **coefs):
+    """Compute_3D of TriDiagTB (dur None) or TriDiagTR of one level: z_faces
+    (n3, n2, n1+1), x_faces (n3, n2+1, n1), y_faces = (F3, F3G, DTU3, DUU3)
+    (n3+1, n2, n1), cells (n3, n2, n1); coefs the fields of
+    asam_tri_tb_coefs.  couple: the reference's branch with the couplings
+    between planes stored.  Returns d, u1, l1, u2, l2, u3, l3."""
+    lib = _lib.load()
+    zf, xf, yf = ([_f64(a) for a in f] for f in (z_faces, x_faces, y_faces))
+    cells = [_f64(a) for a in (vol, dut)] + ([_f64(dur)] if dur is not None else [])
+    n3, n2, n1 = cells[0].shape
+    if (any(a.shape != (n3, n2, n1 + 1) for a in zf) or any(a.shape != (n3, n2 + 1, n1) for a in xf)
+            or any(a.shape != (n3 + 1, n2, n1) for a in yf) or any(a.shape != (n3, n2, n1) for a in cells)):
+        raise ValueError("z (n3,n2,n1+1), x (n3,n2+1,n1), y faces (n3+1,n2,n1), cells (n3,n2,n1)")
+    d = np.empty((n3, n2, n1, 4))
+    u1 = np.empty((n3, n2, max(n1 - 1, 0), 4))
+    l1 = np.empty_like(u1)
+    u2 = np.empty((n3, max(n2 - 1, 0), n1, 4))
+    l2 = np.empty_like(u2)
+    u3 = np.zeros((max(n3 - 1, 0), n2, n1, 4))
+    l3 = np.zeros_like(u3)
+    co = _lib.AsamTriTbCoefs(**{k: float(v) for k, v in coefs.items()})
+    opt = lambda a: ptr(a) if a.size else None  # noqa: E731
+    check(lib.asam_tri_tb_compute_3d(int(dur is not None), int(bool(couple)), n3, n2, n1, C.byref(co),
+                                     *[ptr(a) for a in zf], *[ptr(a) for a in xf], *[ptr(a) for a in yf],
+                                     ptr(cells[0]), ptr(cells[1]), ptr(cells[2]) if dur is not None else None, ptr(d),
+                                     opt(u1), opt(l1), opt(u2), opt(l2), opt(u3), opt(l3)), "asam_tri_tb_compute_3d")
+    return d, u1, l1, u2, l2, u3, l3
+
+
 def MatVecTB_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, x: np.ndarray) -> np.ndarray:
     lib = _lib.load()
     d, u, l, xx = _f64(d), _f64(u), _f64(l), _f64(x)

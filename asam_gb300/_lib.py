@@ -84,7 +84,7 @@ class AsamWeight2Options(C.Structure):
 class AsamTriTbCoefs(C.Structure):
     _fields_ = [("beta0_dtp", C.c_double), ("fac1_l", C.c_double), ("fac1_r", C.c_double),
                 ("grav_comp", C.c_double), ("fac_anela", C.c_double), ("fac2_l", C.c_double),
-                ("fac2_r", C.c_double)]
+                ("fac2_r", C.c_double), ("fac3_l", C.c_double), ("fac3_r", C.c_double)]
 
 
 # (name, restype, argtypes) of every exported entry point of include/asam_gb300.h
@@ -128,6 +128,8 @@ SIGNATURES = [
     ("asam_tri_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_tri_tb_compute", C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(AsamTriTbCoefs)] + [_V] * 10),
     ("asam_tri_tb_compute_2d", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(AsamTriTbCoefs)] + [_V] * 16),
+    ("asam_tri_tb_compute_3d", C.c_int,
+     [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(AsamTriTbCoefs)] + [_V] * 22),
     ("asam_tri_tb_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_tb_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),

@@ -216,16 +216,18 @@ __global__ void k_tri_tb_compute(int tr, int ncol, int n1, asam_tri_tb_coefs s, 
 // the line after, Fac2_R on the last line).  The thread adds them in that
 // order, so the entries equal the reference's line-by-line sweep bit for bit
 // while all elements are assembled at once.
-__global__ void k_tri_tb_compute_2d(int tr, int nplane, int n2, int n1, asam_tri_tb_coefs s,
-                                    const double* __restrict__ f1, const double* __restrict__ f1g,
-                                    const double* __restrict__ dtu1, const double* __restrict__ duu1,
-                                    const double* __restrict__ f2, const double* __restrict__ f2g,
-                                    const double* __restrict__ dtu2, const double* __restrict__ duu2,
-                                    const double* __restrict__ vol, const double* __restrict__ dut,
-                                    const double* __restrict__ dur, double* __restrict__ d, double* __restrict__ u1,
-                                    double* __restrict__ l1, double* __restrict__ u2, double* __restrict__ l2) {
-  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)nplane * n2 * n1) return;
+struct Plane2D {  // the inputs and couplings of the plane systems (layouts of asam_tri_tb_compute_2d)
+  const double *f1, *f1g, *dtu1, *duu1, *f2, *f2g, *dtu2, *duu2, *vol, *dut, *dur;
+  double *u1, *l1, *u2, *l2;
+};
+
+// entry e = (p*n2 + j)*n1 + i of plane p: its block (out[4]) and, for i < n1-1
+// and j < n2-1, the couplings to the next level and to the next line
+__device__ void element_2d(int tr, int n2, int n1, const asam_tri_tb_coefs& s, const Plane2D& P, size_t e,
+                           double* out) {
+  const double *f1 = P.f1, *f1g = P.f1g, *dtu1 = P.dtu1, *duu1 = P.duu1, *f2 = P.f2, *f2g = P.f2g;
+  const double *dtu2 = P.dtu2, *duu2 = P.duu2, *vol = P.vol, *dut = P.dut, *dur = P.dur;
+  double *u1 = P.u1, *l1 = P.l1, *u2 = P.u2, *l2 = P.l2;
   const int i = (int)(e % n1);
   const size_t line = e / n1;  // p*n2 + j
   const int j = (int)(line % n2);
@@ -351,6 +353,79 @@ __global__ void k_tri_tb_compute_2d(int tr, int nplane, int n2, int n1, asam_tri
     e1 = e1 + b * cl(DUTp, j) / den;
     if (tr) e3 = e3 + b * cl(DURp, j) / den;
   }
+  out[0] = e0, out[1] = e1, out[2] = e2, out[3] = e3;
+}
+
+__global__ void k_tri_tb_compute_2d(int tr, int nplane, int n2, int n1, asam_tri_tb_coefs s, Plane2D P,
+                                    double* __restrict__ d) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)nplane * n2 * n1) return;
+  element_2d(tr, n2, n1, s, P, e, d + e * 4);
+}
+
+// Compute_3D (MULTI/TriDiagTB_Mod.f90:663-780; TriDiagTR_Mod.f90:707-864) of
+// n3 planes coupled through the y faces, one thread per element: the plane's
+// Compute_2D entry (element_2d), then the faces between planes in the
+// reference's order -- Fac3_L on plane 1, the face to the plane before, the
+// face to the plane after, Fac3_R on the last plane.  The reference's two
+// branches differ: with the couplings between planes stored (the level's
+// u/l associated) the interior faces and Fac3_R leave DUU3 out, without them
+// every face term has it; Fac3_L has it in both.
+__global__ void k_tri_tb_compute_3d(int tr, int couple, int n3, int n2, int n1, asam_tri_tb_coefs s, Plane2D P,
+                                    const double* __restrict__ f3, const double* __restrict__ f3g,
+                                    const double* __restrict__ dtu3, const double* __restrict__ duu3,
+                                    double* __restrict__ d, double* __restrict__ u3, double* __restrict__ l3) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t npl = (size_t)n2 * n1;
+  if (e >= (size_t)n3 * npl) return;
+  double v[4];
+  element_2d(tr, n2, n1, s, P, e, v);
+  double e0 = v[0], e1 = v[1], e2 = v[2], e3 = v[3];
+  const size_t r = e % npl;  // (j, i) in the plane
+  const int k = (int)(e / npl);
+  const double bd = s.beta0_dtp, bd2 = bd * bd, eps = 1.0e-30;
+  auto fc = [&](const double* a, int kf) { return a[(size_t)kf * npl + r]; };  // face kf of (i, j)
+  auto cl = [&](const double* a, int kc) { return a[(size_t)kc * npl + r]; };  // cell (i, j, kc)
+  const double* dur = P.dur;
+  auto add = [&](double a, double b, int kc, double den) {
+    e0 = e0 + a * cl(P.dut, kc) / den;
+    if (tr) e2 = e2 + a * cl(dur, kc) / den;
+    e1 = e1 + b * cl(P.dut, kc) / den;
+    if (tr) e3 = e3 + b * cl(dur, kc) / den;
+  };
+  // face weights: a (first block row), b (second); DUU3 as the branch has it
+  auto wa = [&](double fac, int q, bool duu) {
+    return duu ? bd2 * fac * fc(f3, q) * fc(dtu3, q) * fc(duu3, q) * fc(f3g, q)
+               : bd2 * fac * fc(f3, q) * fc(dtu3, q) * fc(f3g, q);
+  };
+  auto wb = [&](double fac, int q, bool duu) {
+    return duu ? bd2 * fac * fc(f3, q) * fc(duu3, q) * fc(f3g, q) : bd2 * fac * fc(f3, q) * fc(f3g, q);
+  };
+  const bool inner_duu = !couple;
+  if (k == 0) add(wa(s.fac3_l, 0, true), wb(s.fac3_l, 0, true), 0, cl(P.vol, 0) + eps);
+  if (k > 0) {  // face k, this plane as the upper one
+    const double S = cl(P.vol, k - 1) + cl(P.vol, k) + eps;
+    add(wa(2.0, k, inner_duu), wb(2.0, k, inner_duu), k, S);
+  }
+  if (k < n3 - 1) {  // face k+1, this plane as the lower one; the couplings between the planes
+    const int q = k + 1;
+    const double S = cl(P.vol, k) + cl(P.vol, q) + eps;
+    const double a = wa(2.0, q, inner_duu), b = wb(2.0, q, inner_duu);
+    if (couple) {
+      double* U = u3 + ((size_t)k * npl + r) * 4;
+      double* L = l3 + ((size_t)k * npl + r) * 4;
+      U[0] = -(a * cl(P.dut, q) / S);
+      U[2] = tr ? -(a * cl(dur, q) / S) : 0.0;
+      U[1] = -(b * cl(P.dut, q) / S);
+      U[3] = tr ? -(b * cl(dur, q) / S) : 0.0;
+      L[0] = -(a * cl(P.dut, k) / S);
+      L[2] = tr ? -(a * cl(dur, k) / S) : 0.0;
+      L[1] = -(b * cl(P.dut, k) / S);
+      L[3] = tr ? -(b * cl(dur, k) / S) : 0.0;
+    }
+    add(a, b, k, S);
+  }
+  if (k == n3 - 1) add(wa(s.fac3_r, n3, inner_duu), wb(s.fac3_r, n3, inner_duu), k, cl(P.vol, k) + eps);
   double* D = d + e * 4;
   D[0] = e0, D[1] = e1, D[2] = e2, D[3] = e3;
 }
@@ -442,9 +517,9 @@ int asam_tri_tb_compute_2d(int variant, int nplane, int n2, int n1, const asam_t
     off += len[q];
   }
   double *dd = m.p[1], *du1 = dd + nd, *dl1 = du1 + no1, *du2 = dl1 + no1, *dl2 = du2 + no2;
-  k_tri_tb_compute_2d<<<(unsigned)((nc + 255) / 256), 256>>>(variant, nplane, n2, n1, *coefs, dev[0], dev[1], dev[2],
-                                                              dev[3], dev[4], dev[5], dev[6], dev[7], dev[8], dev[9],
-                                                              dev[10], dd, du1, dl1, du2, dl2);
+  const Plane2D P{dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], dev[6], dev[7], dev[8], dev[9], dev[10],
+                  du1, dl1, du2, dl2};
+  k_tri_tb_compute_2d<<<(unsigned)((nc + 255) / 256), 256>>>(variant, nplane, n2, n1, *coefs, P, dd);
   asam::count_launches(1);
   TCU(cudaGetLastError());
   TCU(cudaMemcpy(d, dd, nd * sizeof(double), cudaMemcpyDefault));
@@ -456,6 +531,52 @@ int asam_tri_tb_compute_2d(int variant, int nplane, int n2, int n1, const asam_t
     TCU(cudaMemcpy(u2, du2, no2 * sizeof(double), cudaMemcpyDefault));
     TCU(cudaMemcpy(l2, dl2, no2 * sizeof(double), cudaMemcpyDefault));
   }
+  return ASAM_OK;
+}
+
+int asam_tri_tb_compute_3d(int variant, int couple, int n3, int n2, int n1, const asam_tri_tb_coefs* coefs,
+                           const double* f1, const double* f1g, const double* dtu1, const double* duu1,
+                           const double* f2, const double* f2g, const double* dtu2, const double* duu2,
+                           const double* f3, const double* f3g, const double* dtu3, const double* duu3,
+                           const double* vol, const double* dut, const double* dur, double* d, double* u1,
+                           double* l1, double* u2, double* l2, double* u3, double* l3) {
+  if ((variant != 0 && variant != 1) || n3 < 1 || n2 < 1 || n1 < 1 || !coefs || !f1 || !f1g || !dtu1 || !duu1 ||
+      !f2 || !f2g || !dtu2 || !duu2 || !f3 || !f3g || !dtu3 || !duu3 || !vol || !dut || (variant == 1 && !dur) ||
+      !d || (n1 > 1 && (!u1 || !l1)) || (n2 > 1 && (!u2 || !l2)) || (couple && n3 > 1 && (!u3 || !l3))) {
+    asam::set_last_error("asam_tri_tb_compute_3d: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  const size_t npl = (size_t)n2 * n1, nl = (size_t)n3 * n2, nc = (size_t)n3 * npl;
+  const size_t nz = nl * (n1 + 1), nx = (size_t)n3 * (n2 + 1) * n1, ny = (size_t)(n3 + 1) * npl;
+  const size_t nd = nc * 4, no1 = nl * (n1 - 1) * 4, no2 = (size_t)n3 * (n2 - 1) * n1 * 4;
+  const size_t no3 = couple ? (size_t)(n3 - 1) * npl * 4 : 0;
+  DevBufs m;
+  TCU(cudaMalloc((void**)&m.p[0], (4 * nz + 4 * nx + 4 * ny + 3 * nc) * sizeof(double)));
+  TCU(cudaMalloc((void**)&m.p[1], (nd + 2 * no1 + 2 * no2 + 2 * no3 + 1) * sizeof(double)));
+  const double* src[15] = {f1, f1g, dtu1, duu1, f2, f2g, dtu2, duu2, f3, f3g, dtu3, duu3,
+                           vol, dut, variant == 1 ? dur : vol};
+  const size_t len[15] = {nz, nz, nz, nz, nx, nx, nx, nx, ny, ny, ny, ny, nc, nc, nc};
+  double* dev[15];
+  size_t off = 0;
+  for (int q = 0; q < 15; ++q) {
+    dev[q] = m.p[0] + off;
+    TCU(cudaMemcpy(dev[q], src[q], len[q] * sizeof(double), cudaMemcpyDefault));
+    off += len[q];
+  }
+  double *dd = m.p[1], *du1 = dd + nd, *dl1 = du1 + no1, *du2 = dl1 + no1, *dl2 = du2 + no2;
+  double *du3 = dl2 + no2, *dl3 = du3 + no3;
+  const Plane2D P{dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], dev[6], dev[7], dev[12], dev[13], dev[14],
+                  du1, dl1, du2, dl2};
+  k_tri_tb_compute_3d<<<(unsigned)((nc + 255) / 256), 256>>>(variant, couple ? 1 : 0, n3, n2, n1, *coefs, P, dev[8],
+                                                              dev[9], dev[10], dev[11], dd, du3, dl3);
+  asam::count_launches(1);
+  TCU(cudaGetLastError());
+  TCU(cudaMemcpy(d, dd, nd * sizeof(double), cudaMemcpyDefault));
+  double* outs[6] = {u1, l1, u2, l2, u3, l3};
+  const double* ins[6] = {du1, dl1, du2, dl2, du3, dl3};
+  const size_t lens[6] = {no1, no1, no2, no2, no3, no3};
+  for (int q = 0; q < 6; ++q)
+    if (lens[q]) TCU(cudaMemcpy(outs[q], ins[q], lens[q] * sizeof(double), cudaMemcpyDefault));
   return ASAM_OK;
 }
 

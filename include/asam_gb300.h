@@ -578,6 +578,8 @@ typedef struct {
   double fac_anela; /* FacAnela */
   double fac2_l;    /* Fac2_L, the weight of the first face between lines (asam_tri_tb_compute_2d) */
   double fac2_r;    /* Fac2_R, the weight of the last one */
+  double fac3_l;    /* Fac3_L, the weight of the first face between planes (asam_tri_tb_compute_3d) */
+  double fac3_r;    /* Fac3_R, the weight of the last one */
 } asam_tri_tb_coefs;
 int asam_tri_tb_compute(int variant, int ncol, int n1, const asam_tri_tb_coefs *coefs, const double *f,
                         const double *fg, const double *vol, const double *dtu, const double *duu, const double *dut,
@@ -600,6 +602,23 @@ int asam_tri_tb_compute_2d(int variant, int nplane, int n2, int n1, const asam_t
                            const double *f2, const double *f2g, const double *dtu2, const double *duu2,
                            const double *vol, const double *dut, const double *dur, double *d, double *u1,
                            double *l1, double *u2, double *l2);
+
+/* Assembly of a 3D level: Compute_3D of MULTI/TriDiagTB_Mod.f90:663-780
+ * (variant 0) or MULTI/TriDiagTR_Mod.f90:707-864 (variant 1) on n3 planes of
+ * n2 lines of n1 levels coupled through the faces between planes f3, f3g,
+ * dtu3, duu3 [(k*n2 + j)*n1 + i] (faces 1..n3+1); the plane arrays as for
+ * asam_tri_tb_compute_2d with p = k.  couple selects the reference's branch:
+ * 1, the level stores the couplings between planes u3, l3
+ * [(k*n2 + j)*n1 + i][4] (k < n3-1; TriDiagTB's the first block column) and
+ * its interior and last faces leave DUU3 out, as the reference does there;
+ * 0, no couplings (u3, l3 unused) and every face term has DUU3 (the coarse
+ * levels).  The first face has DUU3 in both. */
+int asam_tri_tb_compute_3d(int variant, int couple, int n3, int n2, int n1, const asam_tri_tb_coefs *coefs,
+                           const double *f1, const double *f1g, const double *dtu1, const double *duu1,
+                           const double *f2, const double *f2g, const double *dtu2, const double *duu2,
+                           const double *f3, const double *f3g, const double *dtu3, const double *duu3,
+                           const double *vol, const double *dut, const double *dur, double *d, double *u1,
+                           double *l1, double *u2, double *l2, double *u3, double *l3);
 
 /* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141),
  * the same as MatVecTR_1D (MULTI/TriDiagTR_Mod.f90:133-153). */

@@ -64,6 +64,7 @@ def load() -> C.CDLL:
             "ora_tri_tb_matvec": (None, [I, I, V, V, V, V, V]),
             "ora_tri_tb_compute": (None, [I, I, I] + [V] * 11),
             "ora_tri_tb_compute_2d": (None, [I, I, I, I] + [V] * 17),
+            "ora_tri_tb_compute_3d": (None, [I, I, I, I, I] + [V] * 23),
             "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
         }
         sig.update({
@@ -434,6 +435,35 @@ def tri_tb_compute_2d(z_faces, x_faces, vol, dut, dur=None, beta0_dtp=1.0, fac1_
     lib.ora_tri_tb_compute_2d(int(tr), nplane, n2, n1, _p(s), *[_p(a) for a in zf], *[_p(a) for a in xf], _p(vol),
                               _p(dut), _p(durr), _p(d), _p(u1), _p(l1), _p(u2), _p(l2))
     return d, u1[:, :, :n1 - 1], l1[:, :, :n1 - 1], u2[:, :n2 - 1], l2[:, :n2 - 1]
+
+
+def tri_tb_compute_3d(z_faces, x_faces, y_faces, vol, dut, dur=None, couple=True, beta0_dtp=1.0, fac1_l=0.0,
+                      fac1_r=0.0, grav_comp=0.0, fac_anela=0.0, fac2_l=0.0, fac2_r=0.0, fac3_l=0.0, fac3_r=0.0):
+    """Compute_3D of TriDiagTB (dur None, MULTI/TriDiagTB_Mod.f90:663-780) or
+    TriDiagTR (MULTI/TriDiagTR_Mod.f90:707-864) of one level: z_faces (n3, n2,
+    n1+1), x_faces (n3, n2+1, n1), y_faces = (F3, F3G, DTU3, DUU3) (n3+1, n2,
+    n1), cells (n3, n2, n1).  Returns d, u1, l1, u2, l2, u3, l3 (u3, l3 of
+    shape (n3-1, n2, n1, 4), zero when couple is False)."""
+    lib = load()
+    zf = [np.ascontiguousarray(a, dtype=np.float64) for a in z_faces]
+    xf = [np.ascontiguousarray(a, dtype=np.float64) for a in x_faces]
+    yf = [np.ascontiguousarray(a, dtype=np.float64) for a in y_faces]
+    vol, dut = (np.ascontiguousarray(a, dtype=np.float64) for a in (vol, dut))
+    tr = dur is not None
+    durr = np.ascontiguousarray(dur, dtype=np.float64) if tr else vol
+    n3, n2, n1 = vol.shape
+    s = np.array([beta0_dtp, fac1_l, fac1_r, grav_comp, fac_anela, fac2_l, fac2_r, fac3_l, fac3_r])
+    d = np.empty((n3, n2, n1, 4))
+    u1 = np.empty((n3, n2, max(n1 - 1, 1), 4))
+    l1 = np.empty_like(u1)
+    u2 = np.empty((n3, max(n2 - 1, 1), n1, 4))
+    l2 = np.empty_like(u2)
+    u3 = np.zeros((max(n3 - 1, 1), n2, n1, 4))
+    l3 = np.zeros_like(u3)
+    lib.ora_tri_tb_compute_3d(int(tr), int(bool(couple)), n3, n2, n1, _p(s), *[_p(a) for a in zf],
+                              *[_p(a) for a in xf], *[_p(a) for a in yf], _p(vol), _p(dut), _p(durr), _p(d), _p(u1),
+                              _p(l1), _p(u2), _p(l2), _p(u3), _p(l3))
+    return (d, u1[:, :, :n1 - 1], l1[:, :, :n1 - 1], u2[:, :n2 - 1], l2[:, :n2 - 1], u3[:n3 - 1], l3[:n3 - 1])
 
 
 class OracleProj:

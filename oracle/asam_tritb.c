@@ -282,3 +282,97 @@ void ora_tri_tb_compute_2d(int variant, int nplane, int n2, int n1, const double
 #undef FACE
   }
 }
+
+/* Compute_3D (MULTI/TriDiagTB_Mod.f90:663-780, variant 0; TriDiagTR_Mod.f90:707-864,
+ * variant 1) of one 3D level, the reference's loops as they stand: plane 1's
+ * Compute_2D and Fac3_L terms, then per face k+1 between planes k and k+1 the
+ * couplings, plane k's share, plane k+1's Compute_2D and its share, finally
+ * the last plane's Fac3_R terms.  couple = 1: the branch with the couplings
+ * between planes stored, whose interior and Fac3_R terms have no DUU3;
+ * couple = 0: the branch without them, every face term with DUU3.
+ * s = {beta0*dtp, Fac1_L, Fac1_R, GravComp, FacAnela, Fac2_L, Fac2_R, Fac3_L,
+ * Fac3_R}; faces between planes f3.. [(k*n2 + j)*n1 + i], k = 0..n3; the rest
+ * as ora_tri_tb_compute_2d with p = k; u3, l3 [(k*n2 + j)*n1 + i][4]. */
+void ora_tri_tb_compute_3d(int variant, int couple, int n3, int n2, int n1, const double *s, const double *f1,
+                           const double *f1g, const double *dtu1, const double *duu1, const double *f2,
+                           const double *f2g, const double *dtu2, const double *duu2, const double *f3,
+                           const double *f3g, const double *dtu3, const double *duu3, const double *vol,
+                           const double *dut, const double *dur, double *d, double *u1, double *l1, double *u2,
+                           double *l2, double *u3, double *l3) {
+  const double bd = s[0], fac3l = s[7], fac3r = s[8];
+  const double bd2 = bd * bd, eps = 1.0e-30;
+  const int tr = variant == 1;
+  const size_t npl = (size_t)n2 * n1;
+#define PLANE(k)                                                                                                   \
+  ora_tri_tb_compute_2d(variant, 1, n2, n1, s, f1 + (size_t)(k)*n2 * (n1 + 1), f1g + (size_t)(k)*n2 * (n1 + 1),    \
+                        dtu1 + (size_t)(k)*n2 * (n1 + 1), duu1 + (size_t)(k)*n2 * (n1 + 1),                          \
+                        f2 + (size_t)(k) * (n2 + 1) * n1, f2g + (size_t)(k) * (n2 + 1) * n1,                         \
+                        dtu2 + (size_t)(k) * (n2 + 1) * n1, duu2 + (size_t)(k) * (n2 + 1) * n1, vol + (k)*npl,       \
+                        dut + (k)*npl, tr ? dur + (k)*npl : 0, d + (k)*npl * 4, u1 + (size_t)(k)*n2 * (n1 - 1) * 4, \
+                        l1 + (size_t)(k)*n2 * (n1 - 1) * 4, u2 + (size_t)(k) * (n2 - 1) * n1 * 4,                    \
+                        l2 + (size_t)(k) * (n2 - 1) * n1 * 4)
+#define C3(a, r, k) a[(size_t)(k)*npl + (r)]
+#define D3(r, k, e) d[((size_t)(k)*npl + (r)) * 4 + (e)]
+  PLANE(0);
+  for (size_t r = 0; r < npl; ++r) {
+    const double a = bd2 * fac3l * C3(f3, r, 0) * C3(dtu3, r, 0) * C3(duu3, r, 0) * C3(f3g, r, 0);
+    const double b = bd2 * fac3l * C3(f3, r, 0) * C3(duu3, r, 0) * C3(f3g, r, 0);
+    const double den = C3(vol, r, 0) + eps;
+    D3(r, 0, 0) = D3(r, 0, 0) + a * C3(dut, r, 0) / den;
+    if (tr) D3(r, 0, 2) = D3(r, 0, 2) + a * C3(dur, r, 0) / den;
+    D3(r, 0, 1) = D3(r, 0, 1) + b * C3(dut, r, 0) / den;
+    if (tr) D3(r, 0, 3) = D3(r, 0, 3) + b * C3(dur, r, 0) / den;
+  }
+  for (int k = 0; k < n3 - 1; ++k) {
+    const int q = k + 1;
+    for (size_t r = 0; r < npl; ++r) {
+      const double S = C3(vol, r, k) + C3(vol, r, q) + eps;
+      const double a = couple ? bd2 * 2.0 * C3(f3, r, q) * C3(dtu3, r, q) * C3(f3g, r, q)
+                              : bd2 * 2.0 * C3(f3, r, q) * C3(dtu3, r, q) * C3(duu3, r, q) * C3(f3g, r, q);
+      const double b = couple ? bd2 * 2.0 * C3(f3, r, q) * C3(f3g, r, q)
+                              : bd2 * 2.0 * C3(f3, r, q) * C3(duu3, r, q) * C3(f3g, r, q);
+      if (couple) {
+        double *u = u3 + ((size_t)k * npl + r) * 4, *l = l3 + ((size_t)k * npl + r) * 4;
+        u[0] = -(a * C3(dut, r, q) / S);
+        u[2] = tr ? -(a * C3(dur, r, q) / S) : 0.0;
+        u[1] = -(b * C3(dut, r, q) / S);
+        u[3] = tr ? -(b * C3(dur, r, q) / S) : 0.0;
+        l[0] = -(a * C3(dut, r, k) / S);
+        l[2] = tr ? -(a * C3(dur, r, k) / S) : 0.0;
+        l[1] = -(b * C3(dut, r, k) / S);
+        l[3] = tr ? -(b * C3(dur, r, k) / S) : 0.0;
+      }
+      D3(r, k, 0) = D3(r, k, 0) + a * C3(dut, r, k) / S;
+      if (tr) D3(r, k, 2) = D3(r, k, 2) + a * C3(dur, r, k) / S;
+      D3(r, k, 1) = D3(r, k, 1) + b * C3(dut, r, k) / S;
+      if (tr) D3(r, k, 3) = D3(r, k, 3) + b * C3(dur, r, k) / S;
+    }
+    PLANE(q);
+    for (size_t r = 0; r < npl; ++r) {
+      const double S = C3(vol, r, k) + C3(vol, r, q) + eps;
+      const double a = couple ? bd2 * 2.0 * C3(f3, r, q) * C3(dtu3, r, q) * C3(f3g, r, q)
+                              : bd2 * 2.0 * C3(f3, r, q) * C3(dtu3, r, q) * C3(duu3, r, q) * C3(f3g, r, q);
+      const double b = couple ? bd2 * 2.0 * C3(f3, r, q) * C3(f3g, r, q)
+                              : bd2 * 2.0 * C3(f3, r, q) * C3(duu3, r, q) * C3(f3g, r, q);
+      D3(r, q, 0) = D3(r, q, 0) + a * C3(dut, r, q) / S;
+      if (tr) D3(r, q, 2) = D3(r, q, 2) + a * C3(dur, r, q) / S;
+      D3(r, q, 1) = D3(r, q, 1) + b * C3(dut, r, q) / S;
+      if (tr) D3(r, q, 3) = D3(r, q, 3) + b * C3(dur, r, q) / S;
+    }
+  }
+  for (size_t r = 0; r < npl; ++r) {
+    const int k = n3 - 1, q = n3;
+    const double a = couple ? bd2 * fac3r * C3(f3, r, q) * C3(dtu3, r, q) * C3(f3g, r, q)
+                            : bd2 * fac3r * C3(f3, r, q) * C3(dtu3, r, q) * C3(duu3, r, q) * C3(f3g, r, q);
+    const double b = couple ? bd2 * fac3r * C3(f3, r, q) * C3(f3g, r, q)
+                            : bd2 * fac3r * C3(f3, r, q) * C3(duu3, r, q) * C3(f3g, r, q);
+    const double den = C3(vol, r, k) + eps;
+    D3(r, k, 0) = D3(r, k, 0) + a * C3(dut, r, k) / den;
+    if (tr) D3(r, k, 2) = D3(r, k, 2) + a * C3(dur, r, k) / den;
+    D3(r, k, 1) = D3(r, k, 1) + b * C3(dut, r, k) / den;
+    if (tr) D3(r, k, 3) = D3(r, k, 3) + b * C3(dur, r, k) / den;
+  }
+#undef PLANE
+#undef C3
+#undef D3
+}

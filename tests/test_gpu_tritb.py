@@ -69,3 +69,20 @@ def test_tri_tb_compute_2d_bitwise(built_lib, variant, nplane, n2, n1):
     ref = oracle.tri_tb_compute_2d(zf, xf, vol, dut, dr, **coefs)
     for g, r in zip(got, ref):
         assert np.array_equal(g, r)
+
+
+@pytest.mark.parametrize("couple", [True, False])
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("n3,n2,n1", [(1, 1, 1), (2, 3, 4), (4, 1, 3), (3, 2, 1), (16, 32, 64)])
+def test_tri_tb_compute_3d_bitwise(built_lib, couple, variant, n3, n2, n1):
+    """Compute_3D of TriDiagTB / TriDiagTR, both branches of the reference,
+    every element at once on the GPU, equals the oracle's plane-by-plane
+    sweep bit for bit."""
+    from tests.test_tritb import compute_inputs_3d
+
+    zf, xf, yf, vol, dut, dur, coefs = compute_inputs_3d(n3, n2, n1, seed=13 * n3 + n2 + n1)
+    dr = dur if variant == "TR" else None
+    got = asam.Compute_TB_3D(zf, xf, yf, vol, dut, dr, couple=couple, **coefs)
+    ref = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, dr, couple=couple, **coefs)
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)

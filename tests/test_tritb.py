@@ -257,3 +257,92 @@ def test_oracle_compute_2d_uniform(built_oracle):
     nb[1:, :] += 1
     assert np.array_equal(d[0, :, :, 0], 1e-40 + nb)
     assert (u1[..., 0] == -1.0).all() and (u2[..., 0] == -1.0).all() and (l2[..., 2] == 0.0).all()
+
+
+def compute_inputs_3d(n3, n2, n1, seed):
+    zf, xf, vol, dut, dur, coefs = compute_inputs_2d(n3, n2, n1, seed)
+    r = np.random.default_rng(seed + 1000)
+    yf = [r.uniform(0.2, 2.0, (n3 + 1, n2, n1)) for _ in range(4)]  # F3, F3G, DTU3, DUU3
+    coefs.update(fac3_l=2.0, fac3_r=0.5)
+    return zf, xf, yf, vol, dut, dur, coefs
+
+
+def numpy_compute_3d(zf, xf, yf, vol, dut, dur, couple, fac3_l, fac3_r, **c2):
+    """Compute_3D restated: every plane's Compute_2D (numpy_compute_2d with the
+    planes as the batch), then the faces between planes in the order the
+    reference adds them to an entry, DUU3 in the face terms as the branch
+    has it (always in Fac3_L)."""
+    n3, n2, n1 = vol.shape
+    tr = dur is not None
+    d, u1, l1, u2, l2 = numpy_compute_2d(zf, xf, vol, dut, dur, **c2)
+    F3, F3G, DTU3, DUU3 = yf
+    bd2 = c2["beta0_dtp"] * c2["beta0_dtp"]
+    eps = 1e-30
+    u3 = np.zeros((n3 - 1, n2, n1, 4))
+    l3 = np.zeros_like(u3)
+
+    def w(fac, q, duu):
+        if duu:
+            return (bd2 * fac * F3[q] * DTU3[q] * DUU3[q] * F3G[q], bd2 * fac * F3[q] * DUU3[q] * F3G[q])
+        return bd2 * fac * F3[q] * DTU3[q] * F3G[q], bd2 * fac * F3[q] * F3G[q]
+
+    def add(k, ab, den):
+        a, b = ab
+        d[k, :, :, 0] = d[k, :, :, 0] + a * dut[k] / den
+        if tr:
+            d[k, :, :, 2] = d[k, :, :, 2] + a * dur[k] / den
+        d[k, :, :, 1] = d[k, :, :, 1] + b * dut[k] / den
+        if tr:
+            d[k, :, :, 3] = d[k, :, :, 3] + b * dur[k] / den
+
+    inner = not couple
+    add(0, w(fac3_l, 0, True), vol[0] + eps)
+    for k in range(1, n3):
+        add(k, w(2.0, k, inner), vol[k - 1] + vol[k] + eps)
+    for k in range(n3 - 1):
+        q = k + 1
+        S = vol[k] + vol[q] + eps
+        a, b = w(2.0, q, inner)
+        if couple:
+            u3[k, :, :, 0], u3[k, :, :, 1] = -(a * dut[q] / S), -(b * dut[q] / S)
+            l3[k, :, :, 0], l3[k, :, :, 1] = -(a * dut[k] / S), -(b * dut[k] / S)
+            if tr:
+                u3[k, :, :, 2], u3[k, :, :, 3] = -(a * dur[q] / S), -(b * dur[q] / S)
+                l3[k, :, :, 2], l3[k, :, :, 3] = -(a * dur[k] / S), -(b * dur[k] / S)
+        add(k, (a, b), S)
+    add(n3 - 1, w(fac3_r, n3, inner), vol[n3 - 1] + eps)
+    return d, u1, l1, u2, l2, u3, l3
+
+
+@pytest.mark.parametrize("couple", [True, False])
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("n3,n2,n1", [(1, 1, 1), (2, 3, 4), (4, 1, 3), (3, 2, 1), (5, 4, 6)])
+def test_oracle_compute_3d_matches_numpy(built_oracle, couple, variant, n3, n2, n1):
+    """Compute_3D (MULTI/TriDiagTB_Mod.f90:663-780, TriDiagTR_Mod.f90:707-864),
+    both of the reference's branches: the oracle's plane-by-plane sweep
+    equals the numpy restatement bit for bit; one plane without Fac3 terms
+    is Compute_2D of that plane."""
+    zf, xf, yf, vol, dut, dur, coefs = compute_inputs_3d(n3, n2, n1, seed=11 * n3 + 3 * n2 + n1)
+    dr = dur if variant == "TR" else None
+    got = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, dr, couple=couple, **coefs)
+    ref = numpy_compute_3d(zf, xf, yf, vol, dut, dr, couple, **coefs)
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)
+    if n3 == 1:
+        c2 = {k: v for k, v in coefs.items() if k not in ("fac3_l", "fac3_r")}
+        one = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, dr, couple=couple, **c2)
+        plane = oracle.tri_tb_compute_2d(zf, xf, vol, dut, dr, **c2)
+        assert np.array_equal(one[0], plane[0])
+
+
+def test_oracle_compute_3d_branches_differ_by_duu3(built_oracle):
+    """The two branches agree when DUU3 = 1 and differ otherwise (the
+    interior faces and Fac3_R of the branch with couplings leave DUU3 out)."""
+    zf, xf, yf, vol, dut, dur, coefs = compute_inputs_3d(3, 2, 4, seed=1)
+    a = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, couple=True, **coefs)[0]
+    b = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, couple=False, **coefs)[0]
+    assert not np.array_equal(a, b)
+    yf[3] = np.ones_like(yf[3])
+    a = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, couple=True, **coefs)[0]
+    b = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, couple=False, **coefs)[0]
+    assert np.array_equal(a, b)
