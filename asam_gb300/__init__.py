@@ -712,6 +712,20 @@ def Compute_TB_3D(z_faces, x_faces, y_faces, vol, dut, dur=None, couple: bool = 
     return d, u1, l1, u2, l2, u3, l3
 
 
+def MatVecTB_3D(blocks, x, tr: bool = False) -> np.ndarray:
+    """MatVecTB_2D/3D (MatVecTR_2D/3D with tr) of a level assembled by
+    Compute_TB_3D: blocks = (d, u1, l1, u2, l2, u3, l3), x (n3, n2, n1, 2)."""
+    lib = _lib.load()
+    d = _f64(blocks[0])
+    n3, n2, n1 = d.shape[:3]
+    rest = [_f64(a) for a in blocks[1:]]
+    xx = _f64(x)
+    y = np.empty_like(xx)
+    check(lib.asam_tri_tb_matvec_3d(int(bool(tr)), n3, n2, n1, ptr(d), *[ptr(a) if a.size else None for a in rest],
+                                    ptr(xx), ptr(y)), "asam_tri_tb_matvec_3d")
+    return y
+
+
 def MatVecTB_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, x: np.ndarray) -> np.ndarray:
     lib = _lib.load()
     d, u, l, xx = _f64(d), _f64(u), _f64(l), _f64(x)

@@ -430,6 +430,58 @@ __global__ void k_tri_tb_compute_3d(int tr, int couple, int n3, int n2, int n1, 
   D[0] = e0, D[1] = e1, D[2] = e2, D[3] = e3;
 }
 
+// MatVecTB_2D/3D (MULTI/TriDiagTB_Mod.f90:345-372, 782-816) and MatVecTR_2D/3D
+// (TriDiagTR_Mod.f90:389-416, 866-900) of one level, one thread per element:
+// the line product MatVecTB_1D, then the couplings between lines (line 1:
+// + u x(j+1); inner lines: + l x(j-1), then + u x(j+1); last line: + l x(j-1)),
+// then those between planes the same way.  TriDiagTB's couplings are vectors
+// that multiply the neighbour's first component; TriDiagTR's are 2x2 blocks
+// (Mult_2).
+__device__ __forceinline__ V2 couple_mul(int tr, const double* c, const V2& x) {
+  if (tr) return mult_2(ld_m(c), x);
+  return V2{__dmul_rn(c[0], x.x1), __dmul_rn(c[1], x.x1)};
+}
+
+__global__ void k_tri_tb_matvec_3d(int tr, int n3, int n2, int n1, const double* __restrict__ d,
+                                   const double* __restrict__ u1, const double* __restrict__ l1,
+                                   const double* __restrict__ u2, const double* __restrict__ l2,
+                                   const double* __restrict__ u3, const double* __restrict__ l3,
+                                   const double* __restrict__ x, double* __restrict__ y) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t npl = (size_t)n2 * n1;
+  if (e >= (size_t)n3 * npl) return;
+  const int i = (int)(e % n1);
+  const size_t line = e / n1;
+  const int j = (int)(line % n2);
+  const int k = (int)(line / n2);
+  const double* xl = x + line * n1 * 2;
+  const M2 di = ld_m(d + e * 4);
+  V2 r;  // MatVecTB_1D of the line, entry i
+  if (n1 == 1) {
+    r = mult_2(di, ld_v(xl));
+  } else if (i == 0) {
+    r = add_v(mult_2(di, ld_v(xl)), mult_2(ld_m(u1 + line * (n1 - 1) * 4), ld_v(xl + 2)));
+  } else if (i == n1 - 1) {
+    r = add_v(mult_2(ld_m(l1 + (line * (n1 - 1) + i - 1) * 4), ld_v(xl + (size_t)(i - 1) * 2)),
+              mult_2(di, ld_v(xl + (size_t)i * 2)));
+  } else {
+    r = add_v(add_v(mult_2(ld_m(l1 + (line * (n1 - 1) + i - 1) * 4), ld_v(xl + (size_t)(i - 1) * 2)),
+                    mult_2(di, ld_v(xl + (size_t)i * 2))),
+              mult_2(ld_m(u1 + (line * (n1 - 1) + i) * 4), ld_v(xl + (size_t)(i + 1) * 2)));
+  }
+  if (n2 > 1) {  // between lines of plane k
+    const size_t c0 = (size_t)k * (n2 - 1) * n1;
+    if (j > 0) r = add_v(r, couple_mul(tr, l2 + (c0 + (size_t)(j - 1) * n1 + i) * 4, ld_v(x + (e - n1) * 2)));
+    if (j < n2 - 1) r = add_v(r, couple_mul(tr, u2 + (c0 + (size_t)j * n1 + i) * 4, ld_v(x + (e + n1) * 2)));
+  }
+  if (n3 > 1) {  // between planes
+    const size_t r0 = e % npl;
+    if (k > 0) r = add_v(r, couple_mul(tr, l3 + ((size_t)(k - 1) * npl + r0) * 4, ld_v(x + (e - npl) * 2)));
+    if (k < n3 - 1) r = add_v(r, couple_mul(tr, u3 + ((size_t)k * npl + r0) * 4, ld_v(x + (e + npl) * 2)));
+  }
+  st_v(y + e * 2, r);
+}
+
 struct DevBufs {
   double* p[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   ~DevBufs() {
@@ -577,6 +629,39 @@ int asam_tri_tb_compute_3d(int variant, int couple, int n3, int n2, int n1, cons
   const size_t lens[6] = {no1, no1, no2, no2, no3, no3};
   for (int q = 0; q < 6; ++q)
     if (lens[q]) TCU(cudaMemcpy(outs[q], ins[q], lens[q] * sizeof(double), cudaMemcpyDefault));
+  return ASAM_OK;
+}
+
+int asam_tri_tb_matvec_3d(int variant, int n3, int n2, int n1, const double* d, const double* u1, const double* l1,
+                          const double* u2, const double* l2, const double* u3, const double* l3, const double* x,
+                          double* y) {
+  if ((variant != 0 && variant != 1) || n3 < 1 || n2 < 1 || n1 < 1 || !d || !x || !y || (n1 > 1 && (!u1 || !l1)) ||
+      (n2 > 1 && (!u2 || !l2)) || (n3 > 1 && (!u3 || !l3))) {
+    asam::set_last_error("asam_tri_tb_matvec_3d: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  const size_t npl = (size_t)n2 * n1, nc = (size_t)n3 * npl;
+  const size_t len[8] = {nc * 4, (size_t)n3 * n2 * (n1 - 1) * 4, (size_t)n3 * n2 * (n1 - 1) * 4,
+                         (size_t)n3 * (n2 - 1) * n1 * 4, (size_t)n3 * (n2 - 1) * n1 * 4, (size_t)(n3 - 1) * npl * 4,
+                         (size_t)(n3 - 1) * npl * 4, nc * 2};
+  const double* src[8] = {d, u1, l1, u2, l2, u3, l3, x};
+  size_t tot = nc * 2 + 1;
+  for (size_t q : len) tot += q;
+  DevBufs m;
+  TCU(cudaMalloc((void**)&m.p[0], tot * sizeof(double)));
+  double* dev[8];
+  size_t off = 0;
+  for (int q = 0; q < 8; ++q) {
+    dev[q] = m.p[0] + off;
+    if (len[q]) TCU(cudaMemcpy(dev[q], src[q], len[q] * sizeof(double), cudaMemcpyDefault));
+    off += len[q];
+  }
+  double* dy = m.p[0] + off;
+  k_tri_tb_matvec_3d<<<(unsigned)((nc + 255) / 256), 256>>>(variant, n3, n2, n1, dev[0], dev[1], dev[2], dev[3],
+                                                             dev[4], dev[5], dev[6], dev[7], dy);
+  asam::count_launches(1);
+  TCU(cudaGetLastError());
+  TCU(cudaMemcpy(y, dy, nc * 2 * sizeof(double), cudaMemcpyDefault));
   return ASAM_OK;
 }
 

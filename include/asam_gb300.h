@@ -620,6 +620,16 @@ int asam_tri_tb_compute_3d(int variant, int couple, int n3, int n2, int n1, cons
                            const double *vol, const double *dut, const double *dur, double *d, double *u1,
                            double *l1, double *u2, double *l2, double *u3, double *l3);
 
+/* y = A x on one level of n3 planes of n2 lines of n1 levels: MatVecTB_2D/3D
+ * (MULTI/TriDiagTB_Mod.f90:345-372, 782-816; variant 0: the couplings between
+ * lines and planes are vectors that multiply the neighbour's first
+ * component) or MatVecTR_2D/3D (MULTI/TriDiagTR_Mod.f90:389-416, 866-900;
+ * variant 1: 2x2 blocks), with the layouts of asam_tri_tb_compute_3d (n3 = 1:
+ * a plane, u3/l3 unused; n2 = n3 = 1: a line); x, y [(k*n2 + j)*n1 + i][2]. */
+int asam_tri_tb_matvec_3d(int variant, int n3, int n2, int n1, const double *d, const double *u1, const double *l1,
+                          const double *u2, const double *l2, const double *u3, const double *l3, const double *x,
+                          double *y);
+
 /* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141),
  * the same as MatVecTR_1D (MULTI/TriDiagTR_Mod.f90:133-153). */
 int asam_tri_tb_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x,

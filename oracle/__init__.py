@@ -65,6 +65,7 @@ def load() -> C.CDLL:
             "ora_tri_tb_compute": (None, [I, I, I] + [V] * 11),
             "ora_tri_tb_compute_2d": (None, [I, I, I, I] + [V] * 17),
             "ora_tri_tb_compute_3d": (None, [I, I, I, I, I] + [V] * 23),
+            "ora_tri_tb_matvec_3d": (None, [I, I, I, I] + [V] * 9),
             "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
         }
         sig.update({
@@ -464,6 +465,19 @@ def tri_tb_compute_3d(z_faces, x_faces, y_faces, vol, dut, dur=None, couple=True
                               *[_p(a) for a in xf], *[_p(a) for a in yf], _p(vol), _p(dut), _p(durr), _p(d), _p(u1),
                               _p(l1), _p(u2), _p(l2), _p(u3), _p(l3))
     return (d, u1[:, :, :n1 - 1], l1[:, :, :n1 - 1], u2[:, :n2 - 1], l2[:, :n2 - 1], u3[:n3 - 1], l3[:n3 - 1])
+
+
+def tri_tb_matvec_3d(blocks, x, tr=False):
+    """MatVecTB_2D/3D (or MatVecTR with tr) of a level assembled by
+    tri_tb_compute_3d: blocks = (d, u1, l1, u2, l2, u3, l3), x (n3, n2, n1, 2)."""
+    lib = load()
+    d = np.ascontiguousarray(blocks[0], dtype=np.float64)
+    n3, n2, n1 = d.shape[:3]
+    rest = [np.ascontiguousarray(a, dtype=np.float64) if a.size else np.zeros(4) for a in blocks[1:]]
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(xx)
+    lib.ora_tri_tb_matvec_3d(int(tr), n3, n2, n1, _p(d), *[_p(a) for a in rest], _p(xx), _p(y))
+    return y
 
 
 class OracleProj:

@@ -376,3 +376,75 @@ void ora_tri_tb_compute_3d(int variant, int couple, int n3, int n2, int n1, cons
 #undef C3
 #undef D3
 }
+
+/* MatVecTB_2D / MatVecTR_2D (MULTI/TriDiagTB_Mod.f90:345-372, TriDiagTR_Mod.f90:389-416)
+ * of one plane, as the reference loops: line 1's product and its coupling to
+ * line 2, each inner line's product, + l x(j-1), + u x(j+1), the last line's
+ * product and + l x(n2-1).  TriDiagTB's couplings are vectors times the
+ * neighbour's first component, TriDiagTR's 2x2 blocks (Mult_2). */
+static void couple_add(int tr, const double *c, const double *x, double *y) {
+  double v[2];
+  if (tr) {
+    mult_2(c, x, v);
+  } else {
+    v[0] = c[0] * x[0];
+    v[1] = c[1] * x[0];
+  }
+  y[0] = y[0] + v[0];
+  y[1] = y[1] + v[1];
+}
+static void matvec_2d(int tr, int n2, int n1, const double *d, const double *u1, const double *l1, const double *u2,
+                      const double *l2, const double *x, double *y) {
+#define LINEMV(j)                                                                                               \
+  ora_tri_tb_matvec(1, n1, d + (size_t)(j)*n1 * 4, u1 + (size_t)(j) * (n1 - 1) * 4,                            \
+                    l1 + (size_t)(j) * (n1 - 1) * 4, x + (size_t)(j)*n1 * 2, y + (size_t)(j)*n1 * 2)
+#define XY(a, i, j) (a + ((size_t)(j)*n1 + (i)) * 2)
+#define CP(a, i, j) (a + ((size_t)(j)*n1 + (i)) * 4)
+  LINEMV(0);
+  if (n2 > 1) {
+    for (int i = 0; i < n1; ++i) couple_add(tr, CP(u2, i, 0), XY(x, i, 1), XY(y, i, 0));
+    for (int j = 1; j < n2 - 1; ++j) {
+      LINEMV(j);
+      for (int i = 0; i < n1; ++i) {
+        couple_add(tr, CP(l2, i, j - 1), XY(x, i, j - 1), XY(y, i, j));
+        couple_add(tr, CP(u2, i, j), XY(x, i, j + 1), XY(y, i, j));
+      }
+    }
+    LINEMV(n2 - 1);
+    for (int i = 0; i < n1; ++i) couple_add(tr, CP(l2, i, n2 - 2), XY(x, i, n2 - 2), XY(y, i, n2 - 1));
+  }
+#undef LINEMV
+#undef XY
+#undef CP
+}
+
+/* MatVecTB_3D / MatVecTR_3D (TriDiagTB_Mod.f90:782-816, TriDiagTR_Mod.f90:866-900):
+ * the same over planes with the couplings u3, l3. */
+void ora_tri_tb_matvec_3d(int variant, int n3, int n2, int n1, const double *d, const double *u1, const double *l1,
+                          const double *u2, const double *l2, const double *u3, const double *l3, const double *x,
+                          double *y) {
+  const int tr = variant == 1;
+  const size_t npl = (size_t)n2 * n1;
+#define PLANEMV(k)                                                                                               \
+  matvec_2d(tr, n2, n1, d + (size_t)(k)*npl * 4, u1 + (size_t)(k)*n2 * (n1 - 1) * 4,                           \
+            l1 + (size_t)(k)*n2 * (n1 - 1) * 4, u2 + (size_t)(k) * (n2 - 1) * n1 * 4,                          \
+            l2 + (size_t)(k) * (n2 - 1) * n1 * 4, x + (size_t)(k)*npl * 2, y + (size_t)(k)*npl * 2)
+#define X3(a, r, k) (a + ((size_t)(k)*npl + (r)) * 2)
+#define C3(a, r, k) (a + ((size_t)(k)*npl + (r)) * 4)
+  PLANEMV(0);
+  if (n3 > 1) {
+    for (size_t r = 0; r < npl; ++r) couple_add(tr, C3(u3, r, 0), X3(x, r, 1), X3(y, r, 0));
+    for (int k = 1; k < n3 - 1; ++k) {
+      PLANEMV(k);
+      for (size_t r = 0; r < npl; ++r) {
+        couple_add(tr, C3(l3, r, k - 1), X3(x, r, k - 1), X3(y, r, k));
+        couple_add(tr, C3(u3, r, k), X3(x, r, k + 1), X3(y, r, k));
+      }
+    }
+    PLANEMV(n3 - 1);
+    for (size_t r = 0; r < npl; ++r) couple_add(tr, C3(l3, r, n3 - 2), X3(x, r, n3 - 2), X3(y, r, n3 - 1));
+  }
+#undef PLANEMV
+#undef X3
+#undef C3
+}

@@ -86,3 +86,17 @@ def test_tri_tb_compute_3d_bitwise(built_lib, couple, variant, n3, n2, n1):
     ref = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, dr, couple=couple, **coefs)
     for g, r in zip(got, ref):
         assert np.array_equal(g, r)
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("n3,n2,n1", [(1, 1, 4), (1, 3, 4), (3, 2, 1), (3, 4, 5), (16, 32, 64)])
+def test_tri_tb_matvec_3d_bitwise(built_lib, variant, n3, n2, n1):
+    """The level product MatVecTB/TR_2D/3D on the GPU, one thread per
+    element, equals the oracle's loop nest bit for bit."""
+    from tests.test_tritb import compute_inputs_3d
+
+    zf, xf, yf, vol, dut, dur, coefs = compute_inputs_3d(n3, n2, n1, seed=n3 + 5 * n2 + n1)
+    tr = variant == "TR"
+    blocks = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, dur if tr else None, couple=True, **coefs)
+    x = np.random.default_rng(n2).standard_normal((n3, n2, n1, 2))
+    assert np.array_equal(asam.MatVecTB_3D(blocks, x, tr), oracle.tri_tb_matvec_3d(blocks, x, tr))

@@ -346,3 +346,46 @@ def test_oracle_compute_3d_branches_differ_by_duu3(built_oracle):
     a = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, couple=True, **coefs)[0]
     b = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, couple=False, **coefs)[0]
     assert np.array_equal(a, b)
+
+
+def dense_level(blocks, tr):
+    """The level's operator as a dense matrix: unknown (i, j, k, r) at
+    ((k*n2 + j)*n1 + i)*2 + r; TriDiagTB's couplings between lines and
+    planes act on the neighbour's first component only."""
+    d, u1, l1, u2, l2, u3, l3 = blocks
+    n3, n2, n1 = d.shape[:3]
+    N = 2 * n1 * n2 * n3
+    A = np.zeros((N, N))
+    idx = lambda i, j, k: ((k * n2 + j) * n1 + i) * 2  # noqa: E731
+    blk = lambda v: v.reshape(2, 2, order="F")  # noqa: E731
+    cpl = lambda v: blk(v) if tr else np.array([[v[0], 0.0], [v[1], 0.0]])  # noqa: E731
+    for k in range(n3):
+        for j in range(n2):
+            for i in range(n1):
+                a = idx(i, j, k)
+                A[a:a + 2, a:a + 2] = blk(d[k, j, i])
+                if i + 1 < n1:
+                    A[a:a + 2, idx(i + 1, j, k):idx(i + 1, j, k) + 2] = blk(u1[k, j, i])
+                    A[idx(i + 1, j, k):idx(i + 1, j, k) + 2, a:a + 2] = blk(l1[k, j, i])
+                if j + 1 < n2:
+                    A[a:a + 2, idx(i, j + 1, k):idx(i, j + 1, k) + 2] = cpl(u2[k, j, i])
+                    A[idx(i, j + 1, k):idx(i, j + 1, k) + 2, a:a + 2] = cpl(l2[k, j, i])
+                if k + 1 < n3:
+                    A[a:a + 2, idx(i, j, k + 1):idx(i, j, k + 1) + 2] = cpl(u3[k, j, i])
+                    A[idx(i, j, k + 1):idx(i, j, k + 1) + 2, a:a + 2] = cpl(l3[k, j, i])
+    return A
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("n3,n2,n1", [(1, 1, 4), (1, 3, 4), (3, 2, 1), (3, 4, 5)])
+def test_oracle_level_matvec_against_dense(built_oracle, variant, n3, n2, n1):
+    """MatVecTB_2D/3D and MatVecTR_2D/3D (MULTI/TriDiagTB_Mod.f90:345-372,
+    782-816; TriDiagTR_Mod.f90:389-416, 866-900) of an assembled level equal
+    the dense product of the same operator (1e-13)."""
+    zf, xf, yf, vol, dut, dur, coefs = compute_inputs_3d(n3, n2, n1, seed=3 * n3 + n2 + 7 * n1)
+    tr = variant == "TR"
+    blocks = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, dur if tr else None, couple=True, **coefs)
+    x = np.random.default_rng(n1).standard_normal((n3, n2, n1, 2))
+    y = oracle.tri_tb_matvec_3d(blocks, x, tr)
+    ref = (dense_level(blocks, tr) @ x.reshape(-1)).reshape(x.shape)
+    assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
