@@ -726,6 +726,37 @@ def MatVecTB_3D(blocks, x, tr: bool = False) -> np.ndarray:
     return y
 
 
+def GaussSeidelTB_2D(blocks, b, x0, gauss_iter: int, tr: bool = False) -> np.ndarray:
+    """GaussSeidel_2D of TriDiagTB (TriDiagTR with tr) on planes assembled by
+    Compute_TB_2D: blocks = (d, u1, l1, u2, l2); b, x0 (nplane, n2, n1, 2)."""
+    lib = _lib.load()
+    d = _f64(blocks[0])
+    nplane, n2, n1 = d.shape[:3]
+    rest = [_f64(a) for a in blocks[1:5]]
+    bb, x = _f64(b), _f64(x0).copy()
+    check(lib.asam_tri_tb_gauss_seidel_2d(int(bool(tr)), nplane, n2, n1, ptr(d),
+                                          *[ptr(a) if a.size else None for a in rest], ptr(bb), ptr(x),
+                                          int(gauss_iter)), "asam_tri_tb_gauss_seidel_2d")
+    return x
+
+
+def RestrictTB_2D(res) -> np.ndarray:
+    lib = _lib.load()
+    r = _f64(res)
+    nplane, n2, n1 = r.shape[:3]
+    out = np.empty((nplane, (n2 + 1) // 2, (n1 + 1) // 2, 2))
+    check(lib.asam_tri_tb_restrict_2d(nplane, n2, n1, ptr(r), ptr(out)), "asam_tri_tb_restrict_2d")
+    return out
+
+
+def ProlongateTB_2D(xc, n2: int, n1: int) -> np.ndarray:
+    lib = _lib.load()
+    c = _f64(xc)
+    out = np.empty((c.shape[0], n2, n1, 2))
+    check(lib.asam_tri_tb_prolong_2d(c.shape[0], n2, n1, ptr(c), ptr(out)), "asam_tri_tb_prolong_2d")
+    return out
+
+
 def MatVecTB_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, x: np.ndarray) -> np.ndarray:
     lib = _lib.load()
     d, u, l, xx = _f64(d), _f64(u), _f64(l), _f64(x)

@@ -131,6 +131,9 @@ SIGNATURES = [
     ("asam_tri_tb_compute_3d", C.c_int,
      [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(AsamTriTbCoefs)] + [_V] * 22),
     ("asam_tri_tb_matvec_3d", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int] + [_V] * 9),
+    ("asam_tri_tb_gauss_seidel_2d", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int] + [_V] * 7 + [C.c_int]),
+    ("asam_tri_tb_restrict_2d", C.c_int, [C.c_int, C.c_int, C.c_int, _V, _V]),
+    ("asam_tri_tb_prolong_2d", C.c_int, [C.c_int, C.c_int, C.c_int, _V, _V]),
     ("asam_tri_tb_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_tb_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),

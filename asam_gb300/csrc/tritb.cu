@@ -72,22 +72,17 @@ __device__ __forceinline__ V2 add_v(const V2& a, const V2& b) {
   return V2{__dadd_rn(a.x1, b.x1), __dadd_rn(a.x2, b.x2)};
 }
 
-__global__ void k_tri_tb_solve(int ncol, int n1, const double* __restrict__ d, const double* __restrict__ u,
-                               const double* __restrict__ l, double* __restrict__ b, double* __restrict__ w) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= ncol) return;
-  const double* dc = d + (size_t)col * n1 * 4;
-  const double* uc = u + (size_t)col * (n1 - 1) * 4;
-  const double* lc = l + (size_t)col * (n1 - 1) * 4;
-  double* bc = b + (size_t)col * n1 * 2;
-  const size_t ws = (size_t)ncol;
+// Solve_1D of one column (dc, uc, lc, bc of that column); the factors w of
+// level i at w[(i*4 + e)*ws] (ws the stride between the columns' slots)
+__device__ void solve_col(int n1, const double* __restrict__ dc, const double* __restrict__ uc,
+                          const double* __restrict__ lc, double* __restrict__ bc, double* __restrict__ w, size_t ws) {
   M2 t = ld_m(dc);
   V2 bp = div_2(ld_v(bc), t);
   st_v(bc, bp);
   for (int i = 1; i < n1; ++i) {
     const M2 li = ld_m(lc + (size_t)(i - 1) * 4);
     const M2 wi = div_22(ld_m(uc + (size_t)(i - 1) * 4), t);
-    double* wp = w + (size_t)(i - 1) * 4 * ws + col;
+    double* wp = w + (size_t)(i - 1) * 4 * ws;
     wp[0] = wi.a11;
     wp[ws] = wi.a21;
     wp[2 * ws] = wi.a12;
@@ -97,11 +92,114 @@ __global__ void k_tri_tb_solve(int ncol, int n1, const double* __restrict__ d, c
     st_v(bc + (size_t)i * 2, bp);
   }
   for (int i = n1 - 2; i >= 0; --i) {
-    const double* wp = w + (size_t)i * 4 * ws + col;
+    const double* wp = w + (size_t)i * 4 * ws;
     const M2 wi{wp[0], wp[ws], wp[2 * ws], wp[3 * ws]};
     bp = sub_v(ld_v(bc + (size_t)i * 2), mult_2(wi, bp));
     st_v(bc + (size_t)i * 2, bp);
   }
+}
+
+__global__ void k_tri_tb_solve(int ncol, int n1, const double* __restrict__ d, const double* __restrict__ u,
+                               const double* __restrict__ l, double* __restrict__ b, double* __restrict__ w) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  solve_col(n1, d + (size_t)col * n1 * 4, u + (size_t)col * (n1 - 1) * 4, l + (size_t)col * (n1 - 1) * 4,
+            b + (size_t)col * n1 * 2, w + col, (size_t)ncol);
+}
+
+// GaussSeidel_2D (MULTI/TriDiagTB_Mod.f90:374-418, TriDiagTR_Mod.f90:418-462), one
+// thread per plane: the reference's symmetric line sweep, statement by
+// statement; t and the Thomas factors in slots strided by the plane count.
+__device__ __forceinline__ V2 couple_sub(int tr, const V2& t, const double* c, const V2& x) {
+  if (tr) return sub_v(t, mult_2(ld_m(c), x));
+  return V2{__dsub_rn(t.x1, __dmul_rn(c[0], x.x1)), __dsub_rn(t.x2, __dmul_rn(c[1], x.x1))};
+}
+
+__global__ void k_tri_tb_gs_2d(int tr, int nplane, int n2, int n1, const double* __restrict__ d,
+                               const double* __restrict__ u1, const double* __restrict__ l1,
+                               const double* __restrict__ u2, const double* __restrict__ l2,
+                               const double* __restrict__ b, double* __restrict__ x, int iters,
+                               double* __restrict__ tbuf, double* __restrict__ w) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nplane) return;
+  const size_t L0 = (size_t)p * n2, ws = (size_t)nplane;
+  double* wp = w + p;
+  auto T = [&](int i) -> V2 { return V2{tbuf[((size_t)i * 2) * ws + p], tbuf[((size_t)i * 2 + 1) * ws + p]}; };
+  auto setT = [&](int i, const V2& v) {
+    tbuf[((size_t)i * 2) * ws + p] = v.x1;
+    tbuf[((size_t)i * 2 + 1) * ws + p] = v.x2;
+  };
+  auto XL = [&](int j) { return x + (L0 + j) * n1 * 2; };
+  auto BL = [&](int j) { return b + (L0 + j) * n1 * 2; };
+  auto C2 = [&](const double* a, int i, int j) { return a + (((size_t)p * (n2 - 1) + j) * n1 + i) * 4; };
+  auto solve = [&](int j) {
+    solve_col(n1, d + (L0 + j) * n1 * 4, u1 + (L0 + j) * (n1 - 1) * 4, l1 + (L0 + j) * (n1 - 1) * 4, XL(j), wp, ws);
+  };
+  if (n2 > 1) {
+    for (int it = 0; it < iters; ++it) {
+      for (int i = 0; i < n1; ++i) setT(i, ld_v(BL(0) + 2 * i));
+      for (int j = 0; j < n2 - 1; ++j) {
+        for (int i = 0; i < n1; ++i) st_v(XL(j) + 2 * i, couple_sub(tr, T(i), C2(u2, i, j), ld_v(XL(j + 1) + 2 * i)));
+        solve(j);
+        for (int i = 0; i < n1; ++i) setT(i, couple_sub(tr, ld_v(BL(j + 1) + 2 * i), C2(l2, i, j), ld_v(XL(j) + 2 * i)));
+      }
+      for (int i = 0; i < n1; ++i) st_v(XL(n2 - 1) + 2 * i, T(i));
+      solve(n2 - 1);
+      for (int i = 0; i < n1; ++i)
+        setT(i, couple_sub(tr, ld_v(BL(n2 - 2) + 2 * i), C2(u2, i, n2 - 2), ld_v(XL(n2 - 1) + 2 * i)));
+      for (int j = n2 - 2; j >= 1; --j) {
+        for (int i = 0; i < n1; ++i)
+          st_v(XL(j) + 2 * i, couple_sub(tr, T(i), C2(l2, i, j - 1), ld_v(XL(j - 1) + 2 * i)));
+        solve(j);
+        for (int i = 0; i < n1; ++i)
+          setT(i, couple_sub(tr, ld_v(BL(j - 1) + 2 * i), C2(u2, i, j - 1), ld_v(XL(j) + 2 * i)));
+      }
+    }
+    for (int i = 0; i < n1; ++i) st_v(XL(0) + 2 * i, T(i));
+    solve(0);
+  } else {
+    for (int i = 0; i < n1; ++i) st_v(XL(0) + 2 * i, ld_v(BL(0) + 2 * i));
+    solve(0);
+  }
+}
+
+// RestrictTB_2D (TriDiagTB_Mod.f90:495-525) per coarse entry: the value the
+// reference's overwriting loops leave there
+__global__ void k_tri_tb_restrict_2d(int nplane, int n2, int n1, const double* __restrict__ res,
+                                     double* __restrict__ resc) {
+  const int n1c = (n1 + 1) / 2, n2c = (n2 + 1) / 2;
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)nplane * n2c * n1c) return;
+  const int ic = (int)(e % n1c);
+  const int jc = (int)((e / n1c) % n2c);
+  const size_t p = e / ((size_t)n1c * n2c);
+  const double* R = res + p * n2 * n1 * 2;
+  auto rf = [&](int i, int j) { return ld_v(R + ((size_t)j * n1 + i) * 2); };
+  V2 v;
+  if (jc < n2 / 2) {
+    const int jf = 2 * jc;
+    if (ic < n1 / 2) {
+      const int i = 2 * ic;
+      v = add_v(add_v(add_v(rf(i, jf), rf(i + 1, jf)), rf(i, jf + 1)), rf(i + 1, jf + 1));
+    } else {
+      v = add_v(rf(n1 - 1, jf), rf(n1 - 1, jf + 1));
+    }
+  } else {
+    v = ic < n1 / 2 ? add_v(rf(2 * ic, n2 - 1), rf(2 * ic + 1, n2 - 1)) : rf(n1 - 1, n2 - 1);
+  }
+  st_v(resc + e * 2, v);
+}
+
+// ProlongateTB_2D (TriDiagTB_Mod.f90:527-560): each fine entry its coarse cell's value
+__global__ void k_tri_tb_prolong_2d(int nplane, int n2, int n1, const double* __restrict__ xc,
+                                    double* __restrict__ x) {
+  const int n1c = (n1 + 1) / 2, n2c = (n2 + 1) / 2;
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)nplane * n2 * n1) return;
+  const int i = (int)(e % n1);
+  const int j = (int)((e / n1) % n2);
+  const size_t p = e / ((size_t)n1 * n2);
+  st_v(x + e * 2, ld_v(xc + ((p * n2c + j / 2) * n1c + i / 2) * 2));
 }
 
 __global__ void k_tri_tb_matvec(int ncol, int n1, const double* __restrict__ d, const double* __restrict__ u,
@@ -662,6 +760,71 @@ int asam_tri_tb_matvec_3d(int variant, int n3, int n2, int n1, const double* d, 
   asam::count_launches(1);
   TCU(cudaGetLastError());
   TCU(cudaMemcpy(y, dy, nc * 2 * sizeof(double), cudaMemcpyDefault));
+  return ASAM_OK;
+}
+
+int asam_tri_tb_gauss_seidel_2d(int variant, int nplane, int n2, int n1, const double* d, const double* u1,
+                                const double* l1, const double* u2, const double* l2, const double* b, double* x,
+                                int gauss_iter) {
+  if ((variant != 0 && variant != 1) || nplane < 1 || n2 < 1 || n1 < 1 || !d || !b || !x ||
+      (n1 > 1 && (!u1 || !l1)) || (n2 > 1 && (!u2 || !l2 || gauss_iter < 1))) {
+    asam::set_last_error("asam_tri_tb_gauss_seidel_2d: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  const size_t nl = (size_t)nplane * n2;
+  const size_t len[7] = {nl * n1 * 4, nl * (n1 - 1) * 4, nl * (n1 - 1) * 4, (size_t)nplane * (n2 - 1) * n1 * 4,
+                         (size_t)nplane * (n2 - 1) * n1 * 4, nl * n1 * 2, nl * n1 * 2};
+  const double* src[7] = {d, u1, l1, u2, l2, b, x};
+  const size_t nt = (size_t)nplane * n1 * 2, nw = (size_t)nplane * (n1 > 1 ? n1 - 1 : 1) * 4;
+  size_t tot = nt + nw + 1;
+  for (size_t q : len) tot += q;
+  DevBufs m;
+  TCU(cudaMalloc((void**)&m.p[0], tot * sizeof(double)));
+  double* dev[7];
+  size_t off = 0;
+  for (int q = 0; q < 7; ++q) {
+    dev[q] = m.p[0] + off;
+    if (len[q]) TCU(cudaMemcpy(dev[q], src[q], len[q] * sizeof(double), cudaMemcpyDefault));
+    off += len[q];
+  }
+  double *tb = m.p[0] + off, *wb = tb + nt;
+  k_tri_tb_gs_2d<<<(nplane + 63) / 64, 64>>>(variant, nplane, n2, n1, dev[0], dev[1], dev[2], dev[3], dev[4], dev[5],
+                                             dev[6], gauss_iter, tb, wb);
+  asam::count_launches(1);
+  TCU(cudaGetLastError());
+  TCU(cudaMemcpy(x, dev[6], len[6] * sizeof(double), cudaMemcpyDefault));
+  return ASAM_OK;
+}
+
+int asam_tri_tb_restrict_2d(int nplane, int n2, int n1, const double* res, double* resc) {
+  if (nplane < 1 || n2 < 1 || n1 < 1 || !res || !resc) {
+    asam::set_last_error("asam_tri_tb_restrict_2d: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  const size_t nf = (size_t)nplane * n2 * n1 * 2, nc = (size_t)nplane * ((n2 + 1) / 2) * ((n1 + 1) / 2) * 2;
+  DevBufs m;
+  TCU(cudaMalloc((void**)&m.p[0], (nf + nc) * sizeof(double)));
+  TCU(cudaMemcpy(m.p[0], res, nf * sizeof(double), cudaMemcpyDefault));
+  k_tri_tb_restrict_2d<<<(unsigned)((nc / 2 + 255) / 256), 256>>>(nplane, n2, n1, m.p[0], m.p[0] + nf);
+  asam::count_launches(1);
+  TCU(cudaGetLastError());
+  TCU(cudaMemcpy(resc, m.p[0] + nf, nc * sizeof(double), cudaMemcpyDefault));
+  return ASAM_OK;
+}
+
+int asam_tri_tb_prolong_2d(int nplane, int n2, int n1, const double* xc, double* x) {
+  if (nplane < 1 || n2 < 1 || n1 < 1 || !xc || !x) {
+    asam::set_last_error("asam_tri_tb_prolong_2d: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  const size_t nf = (size_t)nplane * n2 * n1 * 2, nc = (size_t)nplane * ((n2 + 1) / 2) * ((n1 + 1) / 2) * 2;
+  DevBufs m;
+  TCU(cudaMalloc((void**)&m.p[0], (nf + nc) * sizeof(double)));
+  TCU(cudaMemcpy(m.p[0], xc, nc * sizeof(double), cudaMemcpyDefault));
+  k_tri_tb_prolong_2d<<<(unsigned)((nf / 2 + 255) / 256), 256>>>(nplane, n2, n1, m.p[0], m.p[0] + nc);
+  asam::count_launches(1);
+  TCU(cudaGetLastError());
+  TCU(cudaMemcpy(x, m.p[0] + nc, nf * sizeof(double), cudaMemcpyDefault));
   return ASAM_OK;
 }
 

@@ -630,6 +630,24 @@ int asam_tri_tb_matvec_3d(int variant, int n3, int n2, int n1, const double *d, 
                           const double *u2, const double *l2, const double *u3, const double *l3, const double *x,
                           double *y);
 
+/* GaussSeidel_2D of TriDiagTB (variant 0, MULTI/TriDiagTB_Mod.f90:374-418) or
+ * TriDiagTR (variant 1, TriDiagTR_Mod.f90:418-462) on nplane planes assembled
+ * by asam_tri_tb_compute_2d: gauss_iter symmetric line sweeps (lines 1..n2-1
+ * forward, n2..2 backward, each line's right-hand side minus its couplings,
+ * then Solve_1D), then line 1 once more, as the reference; planes in
+ * parallel, each plane's sweep in the reference's order.  b, x
+ * [(p*n2 + j)*n1 + i][2]; x in: the initial guess, out: the result;
+ * gauss_iter >= 1 when n2 > 1. */
+int asam_tri_tb_gauss_seidel_2d(int variant, int nplane, int n2, int n1, const double *d, const double *u1,
+                                const double *l1, const double *u2, const double *l2, const double *b, double *x,
+                                int gauss_iter);
+/* RestrictTB_2D / ProlongateTB_2D (TriDiagTB_Mod.f90:495-560, the same in
+ * TriDiagTR): fine planes n2 x n1, coarse (n2+1)/2 x (n1+1)/2; restriction
+ * sums 2x2 fine entries (an odd last line or level alone) in the reference's
+ * order, prolongation copies each coarse entry to its fine cells. */
+int asam_tri_tb_restrict_2d(int nplane, int n2, int n1, const double *res, double *resc);
+int asam_tri_tb_prolong_2d(int nplane, int n2, int n1, const double *xc, double *x);
+
 /* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141),
  * the same as MatVecTR_1D (MULTI/TriDiagTR_Mod.f90:133-153). */
 int asam_tri_tb_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x,

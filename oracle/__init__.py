@@ -66,6 +66,9 @@ def load() -> C.CDLL:
             "ora_tri_tb_compute_2d": (None, [I, I, I, I] + [V] * 17),
             "ora_tri_tb_compute_3d": (None, [I, I, I, I, I] + [V] * 23),
             "ora_tri_tb_matvec_3d": (None, [I, I, I, I] + [V] * 9),
+            "ora_tri_tb_gauss_seidel_2d": (None, [I, I, I, I] + [V] * 7 + [I]),
+            "ora_tri_tb_restrict_2d": (None, [I, I, I, V, V]),
+            "ora_tri_tb_prolong_2d": (None, [I, I, I, V, V]),
             "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
         }
         sig.update({
@@ -478,6 +481,44 @@ def tri_tb_matvec_3d(blocks, x, tr=False):
     y = np.empty_like(xx)
     lib.ora_tri_tb_matvec_3d(int(tr), n3, n2, n1, _p(d), *[_p(a) for a in rest], _p(xx), _p(y))
     return y
+
+
+def _tb_plane_blocks(blocks):
+    d, u1, l1, u2, l2 = (np.ascontiguousarray(a, dtype=np.float64) for a in blocks[:5])
+    return d, *[a if a.size else np.zeros(4) for a in (u1, l1, u2, l2)]
+
+
+def tri_tb_gauss_seidel_2d(blocks, b, x0, iters, tr=False):
+    """GaussSeidel_2D (MULTI/TriDiagTB_Mod.f90:374-418; TriDiagTR with tr) of
+    planes assembled by tri_tb_compute_2d: blocks = (d, u1, l1, u2, l2),
+    b and the initial guess x0 (nplane, n2, n1, 2)."""
+    lib = load()
+    d, u1, l1, u2, l2 = _tb_plane_blocks(blocks)
+    nplane, n2, n1 = d.shape[:3]
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.ascontiguousarray(x0, dtype=np.float64).copy()
+    lib.ora_tri_tb_gauss_seidel_2d(int(tr), nplane, n2, n1, _p(d), _p(u1), _p(l1), _p(u2), _p(l2), _p(bb), _p(x),
+                                   int(iters))
+    return x
+
+
+def tri_tb_restrict_2d(res):
+    """RestrictTB_2D of planes res (nplane, n2, n1, 2) -> ((n2+1)/2, (n1+1)/2)."""
+    lib = load()
+    r = np.ascontiguousarray(res, dtype=np.float64)
+    nplane, n2, n1 = r.shape[:3]
+    out = np.empty((nplane, (n2 + 1) // 2, (n1 + 1) // 2, 2))
+    lib.ora_tri_tb_restrict_2d(nplane, n2, n1, _p(r), _p(out))
+    return out
+
+
+def tri_tb_prolong_2d(xc, n2, n1):
+    """ProlongateTB_2D of coarse planes xc onto fine planes n2 x n1."""
+    lib = load()
+    c = np.ascontiguousarray(xc, dtype=np.float64)
+    out = np.empty((c.shape[0], n2, n1, 2))
+    lib.ora_tri_tb_prolong_2d(c.shape[0], n2, n1, _p(c), _p(out))
+    return out
 
 
 class OracleProj:

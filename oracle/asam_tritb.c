@@ -448,3 +448,106 @@ void ora_tri_tb_matvec_3d(int variant, int n3, int n2, int n1, const double *d, 
 #undef X3
 #undef C3
 }
+
+/* GaussSeidel_2D (MULTI/TriDiagTB_Mod.f90:374-418, TriDiagTR_Mod.f90:418-462) on
+ * nplane planes: the symmetric line sweep of the reference -- per iteration
+ * lines 1..n2-1 forward, then n2..2 backward, each line's right-hand side
+ * minus its couplings to the neighbour lines and a Solve_1D -- and line 1
+ * once more after the iterations.  x holds the initial guess and is
+ * overwritten; gauss_iter >= 1 when n2 > 1 (the reference reads t
+ * unset otherwise). */
+static void couple_sub(int tr, const double *t, const double *c, const double *x, double *o) {
+  double v[2];
+  if (tr) {
+    mult_2(c, x, v);
+  } else {
+    v[0] = c[0] * x[0];
+    v[1] = c[1] * x[0];
+  }
+  o[0] = t[0] - v[0];
+  o[1] = t[1] - v[1];
+}
+void ora_tri_tb_gauss_seidel_2d(int variant, int nplane, int n2, int n1, const double *d, const double *u1,
+                                const double *l1, const double *u2, const double *l2, const double *b, double *x,
+                                int gauss_iter) {
+  const int tr = variant == 1;
+  double *t = (double *)malloc(sizeof(double) * 2 * (size_t)n1);
+  double *w = (double *)malloc(sizeof(double) * 4 * (size_t)(n1 > 1 ? n1 - 1 : 1));
+  for (int p = 0; p < nplane; ++p) {
+    const size_t L0 = (size_t)p * n2;
+#define XL(j) (x + (L0 + (j)) * n1 * 2)
+#define BL(j) (b + (L0 + (j)) * n1 * 2)
+#define C2(a, i, j) (a + (((size_t)p * (n2 - 1) + (j)) * n1 + (i)) * 4)
+#define SOLVE(j)                                                                                                \
+  ora_tri_tb_solve(1, n1, d + (L0 + (j)) * n1 * 4, u1 + (L0 + (j)) * (n1 - 1) * 4, l1 + (L0 + (j)) * (n1 - 1) * 4, \
+                   XL(j), w)
+    if (n2 > 1) {
+      for (int it = 0; it < gauss_iter; ++it) {
+        memcpy(t, BL(0), sizeof(double) * 2 * (size_t)n1);
+        for (int j = 0; j < n2 - 1; ++j) {
+          for (int i = 0; i < n1; ++i) couple_sub(tr, t + 2 * i, C2(u2, i, j), XL(j + 1) + 2 * i, XL(j) + 2 * i);
+          SOLVE(j);
+          for (int i = 0; i < n1; ++i) couple_sub(tr, BL(j + 1) + 2 * i, C2(l2, i, j), XL(j) + 2 * i, t + 2 * i);
+        }
+        memcpy(XL(n2 - 1), t, sizeof(double) * 2 * (size_t)n1);
+        SOLVE(n2 - 1);
+        for (int i = 0; i < n1; ++i)
+          couple_sub(tr, BL(n2 - 2) + 2 * i, C2(u2, i, n2 - 2), XL(n2 - 1) + 2 * i, t + 2 * i);
+        for (int j = n2 - 2; j >= 1; --j) {
+          for (int i = 0; i < n1; ++i) couple_sub(tr, t + 2 * i, C2(l2, i, j - 1), XL(j - 1) + 2 * i, XL(j) + 2 * i);
+          SOLVE(j);
+          for (int i = 0; i < n1; ++i) couple_sub(tr, BL(j - 1) + 2 * i, C2(u2, i, j - 1), XL(j) + 2 * i, t + 2 * i);
+        }
+      }
+      memcpy(XL(0), t, sizeof(double) * 2 * (size_t)n1);
+      SOLVE(0);
+    } else {
+      memcpy(XL(0), BL(0), sizeof(double) * 2 * (size_t)n1);
+      SOLVE(0);
+    }
+#undef XL
+#undef BL
+#undef C2
+#undef SOLVE
+  }
+  free(t);
+  free(w);
+}
+
+/* RestrictTB_2D / RestrictTR_2D (TriDiagTB_Mod.f90:495-525): the coarse residual of
+ * a plane of n2 x n1 fine entries, (n2+1)/2 x (n1+1)/2, sums of 2x2 fine cells
+ * in the reference's order (an odd last row or line on its own). */
+void ora_tri_tb_restrict_2d(int nplane, int n2, int n1, const double *res, double *resc) {
+  const int n1c = (n1 + 1) / 2, n2c = (n2 + 1) / 2;
+  for (int p = 0; p < nplane; ++p) {
+    const double *R = res + (size_t)p * n2 * n1 * 2;
+    double *C = resc + (size_t)p * n2c * n1c * 2;
+#define RF(i, j, r) R[((size_t)(j)*n1 + (i)) * 2 + (r)]
+#define RC(i, j, r) C[((size_t)(j)*n1c + (i)) * 2 + (r)]
+    for (int r = 0; r < 2; ++r) RC(n1c - 1, n2c - 1, r) = RF(n1 - 1, n2 - 1, r);
+    for (int ic = 0; ic < n1 / 2; ++ic)
+      for (int r = 0; r < 2; ++r) RC(ic, n2c - 1, r) = RF(2 * ic, n2 - 1, r) + RF(2 * ic + 1, n2 - 1, r);
+    for (int jc = 0; jc < n2 / 2; ++jc) {
+      const int jf = 2 * jc;
+      for (int r = 0; r < 2; ++r) RC(n1c - 1, jc, r) = RF(n1 - 1, jf, r) + RF(n1 - 1, jf + 1, r);
+      for (int ic = 0; ic < n1 / 2; ++ic) {
+        const int i = 2 * ic;
+        for (int r = 0; r < 2; ++r)
+          RC(ic, jc, r) = RF(i, jf, r) + RF(i + 1, jf, r) + RF(i, jf + 1, r) + RF(i + 1, jf + 1, r);
+      }
+    }
+#undef RF
+#undef RC
+  }
+}
+
+/* ProlongateTB_2D / ProlongateTR_2D (TriDiagTB_Mod.f90:527-560): every fine entry
+ * takes the value of its coarse cell. */
+void ora_tri_tb_prolong_2d(int nplane, int n2, int n1, const double *xc, double *x) {
+  const int n1c = (n1 + 1) / 2, n2c = (n2 + 1) / 2;
+  for (int p = 0; p < nplane; ++p)
+    for (int j = 0; j < n2; ++j)
+      for (int i = 0; i < n1; ++i)
+        for (int r = 0; r < 2; ++r)
+          x[(((size_t)p * n2 + j) * n1 + i) * 2 + r] = xc[(((size_t)p * n2c + j / 2) * n1c + i / 2) * 2 + r];
+}

@@ -100,3 +100,26 @@ def test_tri_tb_matvec_3d_bitwise(built_lib, variant, n3, n2, n1):
     blocks = oracle.tri_tb_compute_3d(zf, xf, yf, vol, dut, dur if tr else None, couple=True, **coefs)
     x = np.random.default_rng(n2).standard_normal((n3, n2, n1, 2))
     assert np.array_equal(asam.MatVecTB_3D(blocks, x, tr), oracle.tri_tb_matvec_3d(blocks, x, tr))
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("nplane,n2,n1", [(2, 1, 5), (2, 2, 3), (3, 5, 4), (1, 7, 1), (64, 32, 48)])
+def test_tri_tb_gauss_seidel_2d_bitwise(built_lib, variant, nplane, n2, n1):
+    """GaussSeidel_2D on the GPU (planes in parallel, each plane's symmetric
+    line sweep in the reference's order) equals the oracle bit for bit."""
+    from tests.test_tritb import plane_case
+
+    tr = variant == "TR"
+    blocks, b = plane_case(nplane, n2, n1, seed=n2 + 3 * n1 + nplane)
+    x0 = np.random.default_rng(nplane).standard_normal(b.shape)
+    for iters in (1, 3):
+        assert np.array_equal(asam.GaussSeidelTB_2D(blocks, b, x0, iters, tr),
+                              oracle.tri_tb_gauss_seidel_2d(blocks, b, x0, iters, tr))
+
+
+@pytest.mark.parametrize("n2,n1", [(1, 1), (2, 2), (3, 5), (4, 7), (65, 130)])
+def test_tri_tb_restrict_prolong_bitwise(built_lib, n2, n1):
+    res = np.random.default_rng(n1).standard_normal((3, n2, n1, 2))
+    rc = asam.RestrictTB_2D(res)
+    assert np.array_equal(rc, oracle.tri_tb_restrict_2d(res))
+    assert np.array_equal(asam.ProlongateTB_2D(rc, n2, n1), oracle.tri_tb_prolong_2d(rc, n2, n1))

@@ -389,3 +389,62 @@ def test_oracle_level_matvec_against_dense(built_oracle, variant, n3, n2, n1):
     y = oracle.tri_tb_matvec_3d(blocks, x, tr)
     ref = (dense_level(blocks, tr) @ x.reshape(-1)).reshape(x.shape)
     assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+def plane_case(nplane, n2, n1, seed, dominance=6.0):
+    """Diagonally dominant plane systems in the layout of Compute_2D."""
+    r = np.random.default_rng(seed)
+    d, u1, l1, _ = tb_case(nplane * n2, n1, seed=seed, dominance=dominance)
+    d = d.reshape(nplane, n2, n1, 4)
+    u1 = u1.reshape(nplane, n2, n1 - 1, 4)
+    l1 = l1.reshape(nplane, n2, n1 - 1, 4)
+    u2 = r.uniform(-1, 1, (nplane, n2 - 1, n1, 4))
+    l2 = r.uniform(-1, 1, (nplane, n2 - 1, n1, 4))
+    b = r.standard_normal((nplane, n2, n1, 2))
+    return (d, u1, l1, u2, l2), b
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("nplane,n2,n1", [(2, 1, 5), (2, 2, 3), (3, 5, 4), (1, 7, 1)])
+def test_oracle_gauss_seidel_2d_converges(built_oracle, variant, nplane, n2, n1):
+    """GaussSeidel_2D (MULTI/TriDiagTB_Mod.f90:374-418, TriDiagTR_Mod.f90:418-462):
+    the symmetric line sweeps of a diagonally dominant plane converge to the
+    dense solution (TriDiagTB's couplings act on the first component only);
+    one line is Solve_1D of that line, bit for bit."""
+    tr = variant == "TR"
+    blocks, b = plane_case(nplane, n2, n1, seed=n2 * 10 + n1)
+    x = oracle.tri_tb_gauss_seidel_2d(blocks, b, np.zeros_like(b), 40, tr)
+    d, u1, l1, u2, l2 = blocks
+    for p in range(nplane):
+        lvl = (d[p][None], u1[p][None], l1[p][None], u2[p][None], l2[p][None], np.zeros((0, n2, n1, 4)),
+               np.zeros((0, n2, n1, 4)))
+        ref = np.linalg.solve(dense_level(lvl, tr), b[p].reshape(-1)).reshape(n2, n1, 2)
+        assert np.max(np.abs(x[p] - ref)) <= 1e-11 * np.max(np.abs(ref))
+    if n2 == 1:
+        for p in range(nplane):
+            assert np.array_equal(x[p, 0], oracle.tri_tb_solve(d[p], u1[p], l1[p], b[p])[0])
+
+
+@pytest.mark.parametrize("n2,n1", [(1, 1), (2, 2), (3, 5), (4, 7), (5, 4)])
+def test_oracle_restrict_prolong(built_oracle, n2, n1):
+    """RestrictTB_2D / ProlongateTB_2D (MULTI/TriDiagTB_Mod.f90:495-560): the
+    coarse entry sums its 2x2 fine cells in the reference's order (an odd
+    last line or level alone), the prolongation copies it back."""
+    res = np.random.default_rng(n2 + n1).standard_normal((2, n2, n1, 2))
+    got = oracle.tri_tb_restrict_2d(res)
+    n2c, n1c = (n2 + 1) // 2, (n1 + 1) // 2
+    ref = np.zeros((2, n2c, n1c, 2))
+    for jc in range(n2c):
+        for ic in range(n1c):
+            js = [2 * jc] + ([2 * jc + 1] if 2 * jc + 1 < n2 else [])
+            is_ = [2 * ic] + ([2 * ic + 1] if 2 * ic + 1 < n1 else [])
+            acc = None
+            for j in js:  # (i, j), (i+1, j), (i, j+1), (i+1, j+1)
+                for i in is_:
+                    acc = res[:, j, i] if acc is None else acc + res[:, j, i]
+            ref[:, jc, ic] = acc
+    assert np.array_equal(got, ref)
+    back = oracle.tri_tb_prolong_2d(got, n2, n1)
+    for j in range(n2):
+        for i in range(n1):
+            assert np.array_equal(back[:, j, i], got[:, j // 2, i // 2])
