@@ -757,6 +757,23 @@ def ProlongateTB_2D(xc, n2: int, n1: int) -> np.ndarray:
     return out
 
 
+def SolveTB_2D(levels, b, x0, gauss_iter2: int = 1, mult_iter: int = 1, tr: bool = False) -> np.ndarray:
+    """Solve_2D of TriDiagTB (TriDiagTR with tr): mult_iter V-cycles of
+    Multigrid_2D over the plane hierarchy levels = [(d, u1, l1, u2, l2), ...]
+    finest first, each as Compute_TB_2D returns it, level l+1 of ((n2+1)/2,
+    (n1+1)/2); b, x0 (nplane, n2, n1, 2) on the finest level."""
+    lib = _lib.load()
+    keep = [[_f64(a) for a in lv[:5]] for lv in levels]
+    nlev = len(keep)
+    n2s = (C.c_int * nlev)(*[k[0].shape[1] for k in keep])
+    n1s = (C.c_int * nlev)(*[k[0].shape[2] for k in keep])
+    arrs = [(C.c_void_p * nlev)(*[k[j].ctypes.data if k[j].size else None for k in keep]) for j in range(5)]
+    bb, x = _f64(b), _f64(x0).copy()
+    check(lib.asam_tri_tb_multigrid_2d(int(bool(tr)), keep[0][0].shape[0], nlev, n2s, n1s, *arrs, ptr(bb), ptr(x),
+                                       int(gauss_iter2), int(mult_iter)), "asam_tri_tb_multigrid_2d")
+    return x
+
+
 def MatVecTB_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, x: np.ndarray) -> np.ndarray:
     lib = _lib.load()
     d, u, l, xx = _f64(d), _f64(u), _f64(l), _f64(x)

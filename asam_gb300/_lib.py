@@ -134,6 +134,7 @@ SIGNATURES = [
     ("asam_tri_tb_gauss_seidel_2d", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int] + [_V] * 7 + [C.c_int]),
     ("asam_tri_tb_restrict_2d", C.c_int, [C.c_int, C.c_int, C.c_int, _V, _V]),
     ("asam_tri_tb_prolong_2d", C.c_int, [C.c_int, C.c_int, C.c_int, _V, _V]),
+    ("asam_tri_tb_multigrid_2d", C.c_int, [C.c_int, C.c_int, C.c_int, _V, _V] + [_V] * 7 + [C.c_int, C.c_int]),
     ("asam_tri_tb_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_tb_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),

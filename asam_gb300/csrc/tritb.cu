@@ -540,14 +540,14 @@ __device__ __forceinline__ V2 couple_mul(int tr, const double* c, const V2& x) {
   return V2{__dmul_rn(c[0], x.x1), __dmul_rn(c[1], x.x1)};
 }
 
-__global__ void k_tri_tb_matvec_3d(int tr, int n3, int n2, int n1, const double* __restrict__ d,
-                                   const double* __restrict__ u1, const double* __restrict__ l1,
-                                   const double* __restrict__ u2, const double* __restrict__ l2,
-                                   const double* __restrict__ u3, const double* __restrict__ l3,
-                                   const double* __restrict__ x, double* __restrict__ y) {
-  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+// entry e of the level product; planes are coupled only when u3 is given
+// (otherwise n3 counts independent planes)
+__device__ __forceinline__ V2 level_entry(int tr, int n3, int n2, int n1, const double* __restrict__ d,
+                                          const double* __restrict__ u1, const double* __restrict__ l1,
+                                          const double* __restrict__ u2, const double* __restrict__ l2,
+                                          const double* __restrict__ u3, const double* __restrict__ l3,
+                                          const double* __restrict__ x, size_t e) {
   const size_t npl = (size_t)n2 * n1;
-  if (e >= (size_t)n3 * npl) return;
   const int i = (int)(e % n1);
   const size_t line = e / n1;
   const int j = (int)(line % n2);
@@ -572,12 +572,46 @@ __global__ void k_tri_tb_matvec_3d(int tr, int n3, int n2, int n1, const double*
     if (j > 0) r = add_v(r, couple_mul(tr, l2 + (c0 + (size_t)(j - 1) * n1 + i) * 4, ld_v(x + (e - n1) * 2)));
     if (j < n2 - 1) r = add_v(r, couple_mul(tr, u2 + (c0 + (size_t)j * n1 + i) * 4, ld_v(x + (e + n1) * 2)));
   }
-  if (n3 > 1) {  // between planes
+  if (n3 > 1 && u3) {  // between planes
     const size_t r0 = e % npl;
     if (k > 0) r = add_v(r, couple_mul(tr, l3 + ((size_t)(k - 1) * npl + r0) * 4, ld_v(x + (e - npl) * 2)));
     if (k < n3 - 1) r = add_v(r, couple_mul(tr, u3 + ((size_t)k * npl + r0) * 4, ld_v(x + (e + npl) * 2)));
   }
-  st_v(y + e * 2, r);
+  return r;
+}
+
+__global__ void k_tri_tb_matvec_3d(int tr, int n3, int n2, int n1, const double* __restrict__ d,
+                                   const double* __restrict__ u1, const double* __restrict__ l1,
+                                   const double* __restrict__ u2, const double* __restrict__ l2,
+                                   const double* __restrict__ u3, const double* __restrict__ l3,
+                                   const double* __restrict__ x, double* __restrict__ y) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)n3 * n2 * n1) return;
+  st_v(y + e * 2, level_entry(tr, n3, n2, n1, d, u1, l1, u2, l2, u3, l3, x, e));
+}
+
+// Multigrid_2D's residual b - A x of nplane independent planes
+// (MULTI/TriDiagTB_Mod.f90:458-459): the product rounded, then the difference
+__global__ void k_tri_tb_residual_2d(int tr, int nplane, int n2, int n1, const double* __restrict__ d,
+                                     const double* __restrict__ u1, const double* __restrict__ l1,
+                                     const double* __restrict__ u2, const double* __restrict__ l2,
+                                     const double* __restrict__ b, const double* __restrict__ x,
+                                     double* __restrict__ res) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)nplane * n2 * n1) return;
+  st_v(res + e * 2, sub_v(ld_v(b + e * 2), level_entry(tr, nplane, n2, n1, d, u1, l1, u2, l2, nullptr, nullptr, x, e)));
+}
+
+// Multigrid_2D's correction x = x + Prolongate(xc) (MULTI/TriDiagTB_Mod.f90:480-488)
+__global__ void k_tri_tb_prolong_add_2d(int nplane, int n2, int n1, const double* __restrict__ xc,
+                                        double* __restrict__ x) {
+  const int n1c = (n1 + 1) / 2, n2c = (n2 + 1) / 2;
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)nplane * n2 * n1) return;
+  const int i = (int)(e % n1);
+  const int j = (int)((e / n1) % n2);
+  const size_t p = e / ((size_t)n1 * n2);
+  st_v(x + e * 2, add_v(ld_v(x + e * 2), ld_v(xc + ((p * n2c + j / 2) * n1c + i / 2) * 2)));
 }
 
 struct DevBufs {
@@ -793,6 +827,81 @@ int asam_tri_tb_gauss_seidel_2d(int variant, int nplane, int n2, int n1, const d
   asam::count_launches(1);
   TCU(cudaGetLastError());
   TCU(cudaMemcpy(x, dev[6], len[6] * sizeof(double), cudaMemcpyDefault));
+  return ASAM_OK;
+}
+
+int asam_tri_tb_multigrid_2d(int variant, int nplane, int nlev, const int* n2s, const int* n1s,
+                             const double* const* d, const double* const* u1, const double* const* l1,
+                             const double* const* u2, const double* const* l2, const double* b, double* x,
+                             int gauss_iter2, int mult_iter) {
+  bool ok = (variant == 0 || variant == 1) && nplane >= 1 && nlev >= 1 && nlev <= 32 && n2s && n1s && d && u1 &&
+            l1 && u2 && l2 && b && x && gauss_iter2 >= 0 && mult_iter >= 0;
+  for (int l = 0; ok && l < nlev; ++l) {
+    ok = n2s[l] >= 1 && n1s[l] >= 1 && d[l] && (n1s[l] == 1 || (u1[l] && l1[l])) && (n2s[l] == 1 || (u2[l] && l2[l]));
+    if (ok && l > 0) ok = n2s[l] == (n2s[l - 1] + 1) / 2 && n1s[l] == (n1s[l - 1] + 1) / 2;
+  }
+  if (!ok) {
+    asam::set_last_error("asam_tri_tb_multigrid_2d: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  // one allocation: per level the five block arrays, b, x and the residual;
+  // the smoother's scratch sized for the finest level
+  size_t len[32][8], tot = 0;
+  for (int l = 0; l < nlev; ++l) {
+    const size_t nl = (size_t)nplane * n2s[l], n1 = (size_t)n1s[l], n2 = (size_t)n2s[l];
+    const size_t a[8] = {nl * n1 * 4,  nl * (n1 - 1) * 4, nl * (n1 - 1) * 4, nplane * (n2 - 1) * n1 * 4,
+                         nplane * (n2 - 1) * n1 * 4, nl * n1 * 2, nl * n1 * 2, nl * n1 * 2};
+    for (int q = 0; q < 8; ++q) tot += (len[l][q] = a[q]);
+  }
+  const size_t nt = (size_t)nplane * n1s[0] * 2, nw = (size_t)nplane * (n1s[0] > 1 ? n1s[0] - 1 : 1) * 4;
+  DevBufs m;
+  TCU(cudaMalloc((void**)&m.p[0], (tot + nt + nw) * sizeof(double)));
+  double* dev[32][8];
+  size_t off = 0;
+  for (int l = 0; l < nlev; ++l) {
+    const double* src[5] = {d[l], u1[l], l1[l], u2[l], l2[l]};
+    for (int q = 0; q < 8; ++q) {
+      dev[l][q] = m.p[0] + off;
+      if (q < 5 && len[l][q]) TCU(cudaMemcpy(dev[l][q], src[q], len[l][q] * sizeof(double), cudaMemcpyDefault));
+      off += len[l][q];
+    }
+  }
+  double *tb = m.p[0] + off, *wb = tb + nt;
+  TCU(cudaMemcpy(dev[0][5], b, len[0][5] * sizeof(double), cudaMemcpyDefault));
+  TCU(cudaMemcpy(dev[0][6], x, len[0][6] * sizeof(double), cudaMemcpyDefault));
+  long launches = 0;
+  auto grid = [&](int l) { return (unsigned)(((size_t)nplane * n2s[l] * n1s[l] + 255) / 256); };
+#define TB_LEVEL(l) variant, nplane, n2s[l], n1s[l], dev[l][0], dev[l][1], dev[l][2], dev[l][3], dev[l][4]
+  for (int it = 0; it < mult_iter; ++it) {
+    int gi = 1, l = 0;
+    for (;;) {  // Multigrid_2D's way down (MULTI/TriDiagTB_Mod.f90:449-470)
+      k_tri_tb_gs_2d<<<(nplane + 63) / 64, 64>>>(TB_LEVEL(l), dev[l][5], dev[l][6], gi, tb, wb);
+      ++launches;
+      gi += gauss_iter2;
+      if (l + 1 == nlev) {
+        gi -= gauss_iter2;
+        break;
+      }
+      k_tri_tb_residual_2d<<<grid(l), 256>>>(TB_LEVEL(l), dev[l][5], dev[l][6], dev[l][7]);
+      k_tri_tb_restrict_2d<<<grid(l + 1), 256>>>(nplane, n2s[l], n1s[l], dev[l][7], dev[l + 1][5]);
+      TCU(cudaMemsetAsync(dev[l + 1][6], 0, len[l + 1][6] * sizeof(double)));
+      launches += 2;
+      ++l;
+    }
+    for (;;) {  // and up (:471-493)
+      k_tri_tb_gs_2d<<<(nplane + 63) / 64, 64>>>(TB_LEVEL(l), dev[l][5], dev[l][6], gi, tb, wb);
+      ++launches;
+      gi -= gauss_iter2;
+      if (l == 0) break;
+      --l;
+      k_tri_tb_prolong_add_2d<<<grid(l), 256>>>(nplane, n2s[l], n1s[l], dev[l + 1][6], dev[l][6]);
+      ++launches;
+    }
+    TCU(cudaGetLastError());
+  }
+#undef TB_LEVEL
+  asam::count_launches(launches);
+  TCU(cudaMemcpy(x, dev[0][6], len[0][6] * sizeof(double), cudaMemcpyDefault));
   return ASAM_OK;
 }
 

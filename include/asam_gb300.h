@@ -647,6 +647,22 @@ int asam_tri_tb_gauss_seidel_2d(int variant, int nplane, int n2, int n1, const d
  * order, prolongation copies each coarse entry to its fine cells. */
 int asam_tri_tb_restrict_2d(int nplane, int n2, int n1, const double *res, double *resc);
 int asam_tri_tb_prolong_2d(int nplane, int n2, int n1, const double *xc, double *x);
+/* Solve_2D of TriDiagTB (variant 0, MULTI/TriDiagTB_Mod.f90:419-494) or
+ * TriDiagTR (variant 1, TriDiagTR_Mod.f90:463-538): mult_iter (MultIter2)
+ * V-cycles of Multigrid_2D on nplane independent planes over a hierarchy of
+ * nlev levels the caller assembled with asam_tri_tb_compute_2d, finest
+ * first: level l has n2s[l] lines of n1s[l] levels, n2s[l+1] =
+ * (n2s[l]+1)/2 and n1s[l+1] = (n1s[l]+1)/2, its blocks at d[l], u1[l],
+ * l1[l], u2[l], l2[l].  Down: GaussSeidel_2D with GaussIter = 1, then raised
+ * by gauss_iter2 per level, the residual b - A x restricted to the coarser
+ * level's right-hand side with a zero guess; up: GaussSeidel_2D again (the
+ * coarsest twice with the same count), the prolonged coarse guess added to
+ * the finer one.  b, x on the finest level as asam_tri_tb_gauss_seidel_2d;
+ * x in: the initial guess, out: the result.  nlev <= 32. */
+int asam_tri_tb_multigrid_2d(int variant, int nplane, int nlev, const int *n2s, const int *n1s,
+                             const double *const *d, const double *const *u1, const double *const *l1,
+                             const double *const *u2, const double *const *l2, const double *b, double *x,
+                             int gauss_iter2, int mult_iter);
 
 /* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141),
  * the same as MatVecTR_1D (MULTI/TriDiagTR_Mod.f90:133-153). */

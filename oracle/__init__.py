@@ -69,6 +69,7 @@ def load() -> C.CDLL:
             "ora_tri_tb_gauss_seidel_2d": (None, [I, I, I, I] + [V] * 7 + [I]),
             "ora_tri_tb_restrict_2d": (None, [I, I, I, V, V]),
             "ora_tri_tb_prolong_2d": (None, [I, I, I, V, V]),
+            "ora_tri_tb_multigrid_2d": (None, [I, I, I, V, V] + [V] * 7 + [I, I]),
             "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
         }
         sig.update({
@@ -519,6 +520,27 @@ def tri_tb_prolong_2d(xc, n2, n1):
     out = np.empty((c.shape[0], n2, n1, 2))
     lib.ora_tri_tb_prolong_2d(c.shape[0], n2, n1, _p(c), _p(out))
     return out
+
+
+def tri_tb_multigrid_2d(levels, b, x0, gauss_iter2=1, mult_iter=1, tr=False):
+    """Solve_2D of TriDiagTB (MULTI/TriDiagTB_Mod.f90:419-494; TriDiagTR with
+    tr): mult_iter V-cycles of Multigrid_2D over the plane hierarchy levels =
+    [(d, u1, l1, u2, l2), ...] finest first (each as tri_tb_compute_2d returns
+    it, level l+1 of ((n2+1)/2, (n1+1)/2)), b and the guess x0 (nplane, n2,
+    n1, 2) on the finest level."""
+    lib = load()
+    keep = [_tb_plane_blocks(lv) for lv in levels]
+    nlev = len(keep)
+    n2s = (C.c_int * nlev)(*[k[0].shape[1] for k in keep])
+    n1s = (C.c_int * nlev)(*[k[0].shape[2] for k in keep])
+    arrs = [(C.c_void_p * nlev)(*[k[j].ctypes.data for k in keep]) for j in range(5)]
+    nplane = keep[0][0].shape[0]
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.ascontiguousarray(x0, dtype=np.float64).copy()
+    lib.ora_tri_tb_multigrid_2d(int(tr), nplane, nlev, C.cast(n2s, C.c_void_p), C.cast(n1s, C.c_void_p),
+                                *[C.cast(a, C.c_void_p) for a in arrs], _p(bb), _p(x), int(gauss_iter2),
+                                int(mult_iter))
+    return x
 
 
 class OracleProj:

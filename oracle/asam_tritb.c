@@ -551,3 +551,69 @@ void ora_tri_tb_prolong_2d(int nplane, int n2, int n1, const double *xc, double 
         for (int r = 0; r < 2; ++r)
           x[(((size_t)p * n2 + j) * n1 + i) * 2 + r] = xc[(((size_t)p * n2c + j / 2) * n1c + i / 2) * 2 + r];
 }
+
+/* Multigrid_2D (MULTI/TriDiagTB_Mod.f90:433-494, TriDiagTR_Mod.f90:477-538) repeated
+ * mult_iter times (Solve_2D, :419-431) on nplane planes whose hierarchy of
+ * nlev levels the caller assembled (level l: n2s[l] lines of n1s[l] levels,
+ * blocks d[l], u1[l], l1[l], u2[l], l2[l] as ora_tri_tb_compute_2d writes
+ * them; level l+1 has ((n2s[l]+1)/2, (n1s[l]+1)/2)).  Down: GaussSeidel_2D
+ * with GaussIter 1, 1+GaussIter2, ..., the residual b - A x, its
+ * restriction, a zero coarse guess; up: GaussSeidel_2D again (the coarsest
+ * a second time with its count), the prolongation added to the finer guess. */
+static void matvec_planes(int variant, int nplane, int n2, int n1, const double *d, const double *u1,
+                          const double *l1, const double *u2, const double *l2, const double *x, double *y) {
+  for (int p = 0; p < nplane; ++p) {
+    const size_t L = (size_t)p * n2;
+    ora_tri_tb_matvec_3d(variant, 1, n2, n1, d + L * n1 * 4, u1 + L * (n1 - 1) * 4, l1 + L * (n1 - 1) * 4,
+                         u2 + (size_t)p * (n2 - 1) * n1 * 4, l2 + (size_t)p * (n2 - 1) * n1 * 4, 0, 0,
+                         x + L * n1 * 2, y + L * n1 * 2);
+  }
+}
+void ora_tri_tb_multigrid_2d(int variant, int nplane, int nlev, const int *n2s, const int *n1s,
+                             const double *const *d, const double *const *u1, const double *const *l1,
+                             const double *const *u2, const double *const *l2, const double *b, double *x,
+                             int gauss_iter2, int mult_iter) {
+  double *bl[32], *xl[32], *res[32];
+  for (int l = 0; l < nlev; ++l) {
+    const size_t n = (size_t)nplane * n2s[l] * n1s[l] * 2;
+    res[l] = (double *)malloc(sizeof(double) * n);
+    bl[l] = l ? (double *)malloc(sizeof(double) * n) : (double *)b;
+    xl[l] = l ? (double *)malloc(sizeof(double) * n) : x;
+  }
+#define LV(l) variant, nplane, n2s[l], n1s[l], d[l], u1[l], l1[l], u2[l], l2[l]
+  for (int it = 0; it < mult_iter; ++it) {
+    int gi = 1, l = 0;
+    for (;;) {
+      ora_tri_tb_gauss_seidel_2d(LV(l), bl[l], xl[l], gi);
+      gi += gauss_iter2;
+      if (l + 1 < nlev) {
+        const size_t n = (size_t)nplane * n2s[l] * n1s[l] * 2;
+        matvec_planes(LV(l), xl[l], res[l]);
+        for (size_t q = 0; q < n; ++q) res[l][q] = bl[l][q] - res[l][q];
+        ora_tri_tb_restrict_2d(nplane, n2s[l], n1s[l], res[l], bl[l + 1]);
+        memset(xl[l + 1], 0, sizeof(double) * (size_t)nplane * n2s[l + 1] * n1s[l + 1] * 2);
+        ++l;
+      } else {
+        gi -= gauss_iter2;
+        break;
+      }
+    }
+    for (;;) {
+      ora_tri_tb_gauss_seidel_2d(LV(l), bl[l], xl[l], gi);
+      gi -= gauss_iter2;
+      if (l == 0) break;
+      --l;
+      const size_t n = (size_t)nplane * n2s[l] * n1s[l] * 2;
+      ora_tri_tb_prolong_2d(nplane, n2s[l], n1s[l], xl[l + 1], res[l]);
+      for (size_t q = 0; q < n; ++q) xl[l][q] = xl[l][q] + res[l][q];
+    }
+  }
+#undef LV
+  for (int l = 0; l < nlev; ++l) {
+    free(res[l]);
+    if (l) {
+      free(bl[l]);
+      free(xl[l]);
+    }
+  }
+}

@@ -3,7 +3,10 @@
 the columns' assembly Compute_1D of both variants (TriDiagTB_Mod.f90:32-93,
 TriDiagTR_Mod.f90:32-105) with the oracle: bit-exact on every shape,
 including one- and two-level columns and a batch of 32768 columns of 128
-levels (the columns of a 256x128 plane stack of the 512x512x128 grid)."""
+levels (the columns of a 256x128 plane stack of the 512x512x128 grid); the
+planes' and levels' assembly, product, smoother, transfers and V-cycle
+(Compute_2D/3D, MatVecTB_2D/3D, GaussSeidel_2D, RestrictTB_2D,
+ProlongateTB_2D, Multigrid_2D) bit for bit as well."""
 import numpy as np
 import pytest
 
@@ -123,3 +126,49 @@ def test_tri_tb_restrict_prolong_bitwise(built_lib, n2, n1):
     rc = asam.RestrictTB_2D(res)
     assert np.array_equal(rc, oracle.tri_tb_restrict_2d(res))
     assert np.array_equal(asam.ProlongateTB_2D(rc, n2, n1), oracle.tri_tb_prolong_2d(rc, n2, n1))
+
+
+def random_hierarchy(nplane, n2, n1, seed):
+    """Independent diagonally dominant planes on every level (the V-cycle's
+    bits do not need a consistent hierarchy)."""
+    from tests.test_tritb import plane_case
+
+    levels = []
+    while True:
+        blocks, b = plane_case(nplane, n2, n1, seed=seed + len(levels))
+        levels.append(blocks)
+        if len(levels) == 1:
+            b0 = b
+        if n2 == 1 and n1 == 1:
+            return levels, b0
+        n2, n1 = (n2 + 1) // 2, (n1 + 1) // 2
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("nplane,n2,n1,gi2,cycles", [(2, 8, 8, 1, 2), (1, 7, 5, 2, 3), (3, 1, 9, 1, 1), (2, 6, 1, 0, 2),
+                                                      (1, 1, 1, 1, 2), (32, 64, 96, 1, 2)])
+def test_tri_tb_multigrid_2d_bitwise(built_lib, variant, nplane, n2, n1, gi2, cycles):
+    """Solve_2D / Multigrid_2D on the GPU (smoother, residual, restriction
+    and correction as kernels on one stream, the level loop on the host)
+    equals the oracle bit for bit, on Galerkin hierarchies and on a 32-plane
+    stack of 64x96 planes with seven levels."""
+    from tests.test_tritb import plane_hierarchy
+
+    tr = variant == "TR"
+    if nplane * n2 * n1 <= 256:
+        levels, b = plane_hierarchy(nplane, n2, n1, seed=n2 * 7 + n1, tr=tr)
+    else:
+        levels, b = random_hierarchy(nplane, n2, n1, seed=11)
+    x0 = np.random.default_rng(1).standard_normal(b.shape)
+    assert np.array_equal(asam.SolveTB_2D(levels, b, x0, gi2, cycles, tr),
+                          oracle.tri_tb_multigrid_2d(levels, b, x0, gi2, cycles, tr))
+
+
+def test_tri_tb_multigrid_2d_bad_args(built_lib):
+    from asam_gb300._lib import AsamError
+
+    levels, b = random_hierarchy(1, 6, 4, seed=2)
+    with pytest.raises(AsamError):  # a level of the wrong size
+        asam.SolveTB_2D([levels[0], levels[0]], b, b, 1, 1)
+    with pytest.raises(AsamError):
+        asam.SolveTB_2D(levels, b, b, -1, 1)

@@ -448,3 +448,121 @@ def test_oracle_restrict_prolong(built_oracle, n2, n1):
     for j in range(n2):
         for i in range(n1):
             assert np.array_equal(back[:, j, i], got[:, j // 2, i // 2])
+
+
+def galerkin_coarse(blocks, tr):
+    """The coarse plane R A P of a plane level (P copies a coarse entry to
+    its 2x2 fine cells, R sums them): again five blocks, the couplings
+    between coarse lines of TriDiagTB acting on the first component only."""
+    d, u1, l1, u2, l2 = blocks
+    nplane, n2, n1 = d.shape[:3]
+    n2c, n1c = (n2 + 1) // 2, (n1 + 1) // 2
+    out = (np.zeros((nplane, n2c, n1c, 4)), np.zeros((nplane, n2c, max(n1c - 1, 0), 4)),
+           np.zeros((nplane, n2c, max(n1c - 1, 0), 4)), np.zeros((nplane, max(n2c - 1, 0), n1c, 4)),
+           np.zeros((nplane, max(n2c - 1, 0), n1c, 4)))
+    idx = lambda i, j: (j * n1 + i) * 2  # noqa: E731
+    cidx = lambda i, j: (j * n1c + i) * 2  # noqa: E731
+    P = np.zeros((n2 * n1 * 2, n2c * n1c * 2))
+    for j in range(n2):
+        for i in range(n1):
+            P[idx(i, j):idx(i, j) + 2, cidx(i // 2, j // 2):cidx(i // 2, j // 2) + 2] = np.eye(2)
+    z = np.zeros((0, n2, n1, 4))
+    for p in range(nplane):
+        A = dense_level((d[p][None], u1[p][None], l1[p][None], u2[p][None], l2[p][None], z, z), tr)
+        Ac = P.T @ A @ P
+        blk = lambda a, c: Ac[a:a + 2, c:c + 2].reshape(-1, order="F")  # noqa: E731
+        for jc in range(n2c):
+            for ic in range(n1c):
+                a = cidx(ic, jc)
+                out[0][p, jc, ic] = blk(a, a)
+                if ic + 1 < n1c:
+                    out[1][p, jc, ic] = blk(a, cidx(ic + 1, jc))
+                    out[2][p, jc, ic] = blk(cidx(ic + 1, jc), a)
+                if jc + 1 < n2c:
+                    out[3][p, jc, ic] = blk(a, cidx(ic, jc + 1))
+                    out[4][p, jc, ic] = blk(cidx(ic, jc + 1), a)
+        zc = np.zeros((0, n2c, n1c, 4))
+        assert np.allclose(dense_level(tuple(o[p][None] for o in out) + (zc, zc), tr), Ac, atol=1e-12)
+    return out
+
+
+def plane_hierarchy(nplane, n2, n1, seed, tr, dominance=6.0):
+    blocks, b = plane_case(nplane, n2, n1, seed, dominance)
+    levels = [blocks]
+    while levels[-1][0].shape[1] > 1 or levels[-1][0].shape[2] > 1:
+        levels.append(galerkin_coarse(levels[-1], tr))
+    return levels, b
+
+
+def compose_multigrid_2d(levels, b, x, gauss_iter2, mult_iter, tr):
+    """Multigrid_2D (MULTI/TriDiagTB_Mod.f90:433-494) cycle by cycle from the
+    oracle's pinned pieces: the smoother, the level product of each plane, the
+    transfers."""
+    z = lambda n2, n1: np.zeros((0, n2, n1, 4))  # noqa: E731
+    x = x.copy()
+    nlev = len(levels)
+    for _ in range(mult_iter):
+        bl, xl = [b] + [None] * (nlev - 1), [x] + [None] * (nlev - 1)
+        gi, lv = 1, 0
+        while True:
+            xl[lv] = oracle.tri_tb_gauss_seidel_2d(levels[lv], bl[lv], xl[lv], gi, tr)
+            gi += gauss_iter2
+            if lv + 1 == nlev:
+                gi -= gauss_iter2
+                break
+            d = levels[lv][0]
+            n2, n1 = d.shape[1:3]
+            ax = np.stack([oracle.tri_tb_matvec_3d(tuple(a[p][None] for a in levels[lv]) + (z(n2, n1), z(n2, n1)),
+                                                   xl[lv][p][None], tr)[0] for p in range(d.shape[0])])
+            bl[lv + 1] = oracle.tri_tb_restrict_2d(bl[lv] - ax)
+            xl[lv + 1] = np.zeros_like(bl[lv + 1])
+            lv += 1
+        while True:
+            xl[lv] = oracle.tri_tb_gauss_seidel_2d(levels[lv], bl[lv], xl[lv], gi, tr)
+            gi -= gauss_iter2
+            if lv == 0:
+                break
+            lv -= 1
+            n2, n1 = levels[lv][0].shape[1:3]
+            xl[lv] = xl[lv] + oracle.tri_tb_prolong_2d(xl[lv + 1], n2, n1)
+        x = xl[0]
+    return x
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("nplane,n2,n1,gi2,cycles", [(2, 8, 8, 1, 2), (1, 7, 5, 2, 3), (3, 1, 9, 1, 1), (2, 6, 1, 0, 2),
+                                                      (1, 1, 1, 1, 2)])
+def test_oracle_multigrid_2d_composes_pieces(built_oracle, variant, nplane, n2, n1, gi2, cycles):
+    """Solve_2D / Multigrid_2D (MULTI/TriDiagTB_Mod.f90:419-494,
+    TriDiagTR_Mod.f90:463-538) in the oracle equal, bit for bit, the V-cycle
+    composed from the separately pinned smoother, product and transfers: the
+    GaussIter counts (1 growing by GaussIter2 per level, the coarsest twice),
+    the zero coarse guess and the added correction."""
+    tr = variant == "TR"
+    levels, b = plane_hierarchy(nplane, n2, n1, seed=n2 * 7 + n1, tr=tr)
+    x0 = np.random.default_rng(1).standard_normal(b.shape)
+    got = oracle.tri_tb_multigrid_2d(levels, b, x0, gi2, cycles, tr)
+    ref = compose_multigrid_2d(levels, b, x0, gi2, cycles, tr)
+    assert np.array_equal(got, ref)
+    assert np.array_equal(oracle.tri_tb_multigrid_2d(levels, b, x0, gi2, 0, tr), x0)
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+def test_oracle_multigrid_2d_converges(built_oracle, variant):
+    """V-cycles over a Galerkin hierarchy of a weakly dominant plane reach
+    the dense solution, the error falling every cycle."""
+    tr = variant == "TR"
+    n2 = n1 = 16
+    levels, b = plane_hierarchy(2, n2, n1, seed=3, tr=tr, dominance=2.5)
+    z = np.zeros((0, n2, n1, 4))
+    d, u1, l1, u2, l2 = levels[0]
+    refs = [np.linalg.solve(dense_level((d[p][None], u1[p][None], l1[p][None], u2[p][None], l2[p][None], z, z), tr),
+                            b[p].reshape(-1)).reshape(n2, n1, 2) for p in range(2)]
+    ref = np.stack(refs)
+    x = np.zeros_like(b)
+    errs = []
+    for _ in range(12):
+        x = oracle.tri_tb_multigrid_2d(levels, b, x, 1, 1, tr)
+        errs.append(np.max(np.abs(x - ref)) / np.max(np.abs(ref)))
+    assert errs[-1] <= 1e-10, errs
+    assert all(e1 < e0 for e0, e1 in zip(errs, errs[1:]) if e0 > 1e-14), errs
