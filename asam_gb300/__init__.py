@@ -774,6 +774,36 @@ def SolveTB_2D(levels, b, x0, gauss_iter2: int = 1, mult_iter: int = 1, tr: bool
     return x
 
 
+def SolveTB_3D(levels, b, x0, gauss_iter2: int = 1, mult_iter2: int = 1, gauss_iter3: int = 1, mult_iter3: int = 1,
+               tr: bool = False) -> np.ndarray:
+    """Solve_3D of TriDiagTB (TriDiagTR with tr): mult_iter3 V-cycles of
+    Multigrid_3D over levels = [(plane_levels, u3, l3), ...] finest first --
+    plane_levels the hierarchy of the level's planes as SolveTB_2D takes it,
+    u3, l3 (n3-1, n2, n1, 4) as Compute_TB_3D returns them; each plane solved
+    by Solve_2D (gauss_iter2, mult_iter2); b, x0 (n3, n2, n1, 2)."""
+    lib = _lib.load()
+    lv = [([[_f64(a) for a in p[:5]] for p in planes], _f64(u3), _f64(l3)) for planes, u3, l3 in levels]
+    for planes, _, _ in lv:  # the C-ABI derives the plane levels' sizes by halving
+        n3, n2, n1 = planes[0][0].shape[:3]
+        for p in planes:
+            if p[0].shape[:3] != (n3, n2, n1):
+                raise ValueError(f"SolveTB_3D: plane level of shape {p[0].shape[:3]}, expected {(n3, n2, n1)}")
+            n2, n1 = (n2 + 1) // 2, (n1 + 1) // 2
+    flat = [k for planes, _, _ in lv for k in planes]
+    nl = len(lv)
+    ints = lambda v: (C.c_int * len(v))(*v)  # noqa: E731
+    ptrs = lambda arrs: (C.c_void_p * len(arrs))(*[a.ctypes.data if a.size else None for a in arrs])  # noqa: E731
+    bb, x = _f64(b), _f64(x0).copy()
+    check(lib.asam_tri_tb_multigrid_3d(int(bool(tr)), nl, ints([p[0][0].shape[0] for p, _, _ in lv]),
+                                       ints([p[0][0].shape[1] for p, _, _ in lv]),
+                                       ints([p[0][0].shape[2] for p, _, _ in lv]), ints([len(p) for p, _, _ in lv]),
+                                       ptrs([u for _, u, _ in lv]), ptrs([l for _, _, l in lv]),
+                                       *[ptrs([k[j] for k in flat]) for j in range(5)], ptr(bb), ptr(x),
+                                       int(gauss_iter2), int(mult_iter2), int(gauss_iter3), int(mult_iter3)),
+          "asam_tri_tb_multigrid_3d")
+    return x
+
+
 def MatVecTB_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, x: np.ndarray) -> np.ndarray:
     lib = _lib.load()
     d, u, l, xx = _f64(d), _f64(u), _f64(l), _f64(x)

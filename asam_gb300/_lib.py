@@ -135,6 +135,7 @@ SIGNATURES = [
     ("asam_tri_tb_restrict_2d", C.c_int, [C.c_int, C.c_int, C.c_int, _V, _V]),
     ("asam_tri_tb_prolong_2d", C.c_int, [C.c_int, C.c_int, C.c_int, _V, _V]),
     ("asam_tri_tb_multigrid_2d", C.c_int, [C.c_int, C.c_int, C.c_int, _V, _V] + [_V] * 7 + [C.c_int, C.c_int]),
+    ("asam_tri_tb_multigrid_3d", C.c_int, [C.c_int, C.c_int] + [_V] * 4 + [_V] * 9 + [C.c_int] * 4),
     ("asam_tri_tb_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_tb_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),
     ("asam_tri_solve_noalloc", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),

@@ -590,28 +590,71 @@ __global__ void k_tri_tb_matvec_3d(int tr, int n3, int n2, int n1, const double*
   st_v(y + e * 2, level_entry(tr, n3, n2, n1, d, u1, l1, u2, l2, u3, l3, x, e));
 }
 
-// Multigrid_2D's residual b - A x of nplane independent planes
-// (MULTI/TriDiagTB_Mod.f90:458-459): the product rounded, then the difference
-__global__ void k_tri_tb_residual_2d(int tr, int nplane, int n2, int n1, const double* __restrict__ d,
-                                     const double* __restrict__ u1, const double* __restrict__ l1,
-                                     const double* __restrict__ u2, const double* __restrict__ l2,
-                                     const double* __restrict__ b, const double* __restrict__ x,
-                                     double* __restrict__ res) {
+// Multigrid_2D/3D's residual b - A x (MULTI/TriDiagTB_Mod.f90:458-459, 901-902)
+// of n3 planes, coupled by u3, l3 or independent when u3 is null: the
+// product rounded, then the difference
+__global__ void k_tri_tb_residual(int tr, int n3, int n2, int n1, const double* __restrict__ d,
+                                  const double* __restrict__ u1, const double* __restrict__ l1,
+                                  const double* __restrict__ u2, const double* __restrict__ l2,
+                                  const double* __restrict__ u3, const double* __restrict__ l3,
+                                  const double* __restrict__ b, const double* __restrict__ x,
+                                  double* __restrict__ res) {
   const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)nplane * n2 * n1) return;
-  st_v(res + e * 2, sub_v(ld_v(b + e * 2), level_entry(tr, nplane, n2, n1, d, u1, l1, u2, l2, nullptr, nullptr, x, e)));
+  if (e >= (size_t)n3 * n2 * n1) return;
+  st_v(res + e * 2, sub_v(ld_v(b + e * 2), level_entry(tr, n3, n2, n1, d, u1, l1, u2, l2, u3, l3, x, e)));
 }
 
-// Multigrid_2D's correction x = x + Prolongate(xc) (MULTI/TriDiagTB_Mod.f90:480-488)
-__global__ void k_tri_tb_prolong_add_2d(int nplane, int n2, int n1, const double* __restrict__ xc,
-                                        double* __restrict__ x) {
+// Multigrid_2D/3D's correction x = x + Prolongate(xc) (MULTI/TriDiagTB_Mod.f90:
+// 480-488, 924-932): the coarse cell of fine entry (i, j, k) is (i/2, j/2,
+// k/2) on a coarser level, (i/2, j/2, k) for independent planes (halve3 0)
+__global__ void k_tri_tb_prolong_add(int halve3, int n3, int n2, int n1, const double* __restrict__ xc,
+                                     double* __restrict__ x) {
   const int n1c = (n1 + 1) / 2, n2c = (n2 + 1) / 2;
   const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)nplane * n2 * n1) return;
+  if (e >= (size_t)n3 * n2 * n1) return;
   const int i = (int)(e % n1);
   const int j = (int)((e / n1) % n2);
-  const size_t p = e / ((size_t)n1 * n2);
-  st_v(x + e * 2, add_v(ld_v(x + e * 2), ld_v(xc + ((p * n2c + j / 2) * n1c + i / 2) * 2)));
+  const size_t k = e / ((size_t)n1 * n2);
+  const size_t kc = halve3 ? k / 2 : k;
+  st_v(x + e * 2, add_v(ld_v(x + e * 2), ld_v(xc + ((kc * n2c + j / 2) * n1c + i / 2) * 2)));
+}
+
+// RestrictTB_3D (MULTI/TriDiagTB_Mod.f90:954-1026) per coarse entry: the value
+// the reference's overwriting loops leave there -- the fine cells summed
+// along the axes where the entry has two (an odd axis's last cell alone), in
+// the reference's term order (i,j,k), (i+1,j,k), (i,j+1,k), (i,j,k+1),
+// (i+1,j+1,k), (i+1,j,k+1), (i,j+1,k+1), (i+1,j+1,k+1) of the cells present
+__global__ void k_tri_tb_restrict_3d(int n3, int n2, int n1, const double* __restrict__ res,
+                                     double* __restrict__ resc) {
+  const int n1c = (n1 + 1) / 2, n2c = (n2 + 1) / 2, n3c = (n3 + 1) / 2;
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)n3c * n2c * n1c) return;
+  const int ic = (int)(e % n1c);
+  const int jc = (int)((e / n1c) % n2c);
+  const int kc = (int)(e / ((size_t)n1c * n2c));
+  const bool pi = ic < n1 / 2, pj = jc < n2 / 2, pk = kc < n3 / 2;
+  const int i0 = pi ? 2 * ic : n1 - 1, j0 = pj ? 2 * jc : n2 - 1, k0 = pk ? 2 * kc : n3 - 1;
+  constexpr int ord[8] = {0, 1, 2, 4, 3, 5, 6, 7};  // bit 0: i+1, bit 1: j+1, bit 2: k+1
+  V2 v{0.0, 0.0};
+  bool first = true;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int di = ord[q] & 1, dj = (ord[q] >> 1) & 1, dk = (ord[q] >> 2) & 1;
+    if ((di && !pi) || (dj && !pj) || (dk && !pk)) continue;
+    const V2 r = ld_v(res + ((((size_t)(k0 + dk) * n2 + j0 + dj) * n1) + i0 + di) * 2);
+    v = first ? r : add_v(v, r);
+    first = false;
+  }
+  st_v(resc + e * 2, v);
+}
+
+// t - (coupling) x of every entry of a plane (GaussSeidel_3D's right-hand
+// sides, MULTI/TriDiagTB_Mod.f90:830-862); t and o may be the same array
+__global__ void k_tri_tb_couple_sub(int tr, int n, const double* t, const double* __restrict__ c,
+                                    const double* __restrict__ x, double* o) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  st_v(o + (size_t)e * 2, couple_sub(tr, ld_v(t + (size_t)e * 2), c + (size_t)e * 4, ld_v(x + (size_t)e * 2)));
 }
 
 struct DevBufs {
@@ -633,6 +676,163 @@ int cu_fail(cudaError_t e) {
   } while (0)
 
 constexpr int kTbBlock = 128;
+
+// One plane level of a V-cycle on the device: its blocks (all planes), its
+// right-hand side, guess and residual.
+struct PlaneLevel {
+  int n2 = 0, n1 = 0;
+  const double* a[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  double *b = nullptr, *x = nullptr, *res = nullptr;
+};
+// the smoother's per-plane scratch, sized for the finest plane
+struct Scratch {
+  double *t, *w;
+};
+
+size_t plane_block_len(int nplane, int n2, int n1) {
+  return (size_t)nplane * ((size_t)n2 * n1 * 4 + 2 * (size_t)n2 * (n1 - 1) * 4 + 2 * (size_t)(n2 - 1) * n1 * 4);
+}
+size_t plane_vec_len(int nplane, int n2, int n1) { return (size_t)nplane * n2 * n1 * 2; }
+
+// the hierarchy's sizes halve (rounding up) from the finest n2 x n1 and every
+// level's arrays are present
+bool plane_levels_ok(int nlev, const int* n2s, const int* n1s, const double* const* d, const double* const* u1,
+                     const double* const* l1, const double* const* u2, const double* const* l2, int n2, int n1) {
+  if (nlev < 1 || nlev > 32 || !n2s || !n1s || !d || !u1 || !l1 || !u2 || !l2 || n2 < 1 || n1 < 1) return false;
+  for (int l = 0; l < nlev; ++l) {
+    if (n2s[l] != n2 || n1s[l] != n1 || !d[l] || (n1 > 1 && (!u1[l] || !l1[l])) || (n2 > 1 && (!u2[l] || !l2[l])))
+      return false;
+    n2 = (n2 + 1) / 2;
+    n1 = (n1 + 1) / 2;
+  }
+  return true;
+}
+
+// copy a level's five block arrays (host or device) into cur and carve its
+// b, x and residual after them; cur advances past all of it
+cudaError_t stage_plane_level(PlaneLevel& L, int nplane, int n2, int n1, const double* const src[5], double*& cur) {
+  L.n2 = n2;
+  L.n1 = n1;
+  const size_t nl = (size_t)nplane * n2;
+  const size_t len[5] = {nl * n1 * 4, nl * (n1 - 1) * 4, nl * (n1 - 1) * 4, (size_t)nplane * (n2 - 1) * n1 * 4,
+                         (size_t)nplane * (n2 - 1) * n1 * 4};
+  for (int q = 0; q < 5; ++q) {
+    L.a[q] = cur;
+    if (len[q]) {
+      cudaError_t e = cudaMemcpy(cur, src[q], len[q] * sizeof(double), cudaMemcpyDefault);
+      if (e != cudaSuccess) return e;
+    }
+    cur += len[q];
+  }
+  const size_t nv = plane_vec_len(nplane, n2, n1);
+  L.b = cur;
+  L.x = cur + nv;
+  L.res = cur + 2 * nv;
+  cur += 3 * nv;
+  return cudaSuccess;
+}
+
+// Solve_2D: mult_iter V-cycles of Multigrid_2D (MULTI/TriDiagTB_Mod.f90:419-494)
+// on nplane independent planes, from lv[0].b and the guess lv[0].x; the
+// coarse levels' b, x and every residual are work space.  Kernels on the
+// legacy stream, the level loop here.
+cudaError_t plane_cycles(int variant, int nplane, int nlev, PlaneLevel* lv, const Scratch& sc, int gauss_iter2,
+                         int mult_iter, long& launches) {
+  auto grid = [&](const PlaneLevel& L) { return (unsigned)(((size_t)nplane * L.n2 * L.n1 + 255) / 256); };
+#define TB_LEVEL(L) variant, nplane, (L).n2, (L).n1, (L).a[0], (L).a[1], (L).a[2], (L).a[3], (L).a[4]
+  for (int it = 0; it < mult_iter; ++it) {
+    int gi = 1, l = 0;
+    for (;;) {  // the way down (:449-470)
+      k_tri_tb_gs_2d<<<(nplane + 63) / 64, 64>>>(TB_LEVEL(lv[l]), lv[l].b, lv[l].x, gi, sc.t, sc.w);
+      ++launches;
+      gi += gauss_iter2;
+      if (l + 1 == nlev) {
+        gi -= gauss_iter2;
+        break;
+      }
+      k_tri_tb_residual<<<grid(lv[l]), 256>>>(TB_LEVEL(lv[l]), nullptr, nullptr, lv[l].b, lv[l].x, lv[l].res);
+      k_tri_tb_restrict_2d<<<grid(lv[l + 1]), 256>>>(nplane, lv[l].n2, lv[l].n1, lv[l].res, lv[l + 1].b);
+      cudaError_t e = cudaMemsetAsync(lv[l + 1].x, 0, plane_vec_len(nplane, lv[l + 1].n2, lv[l + 1].n1) * sizeof(double));
+      if (e != cudaSuccess) return e;
+      launches += 2;
+      ++l;
+    }
+    for (;;) {  // and up (:471-493)
+      k_tri_tb_gs_2d<<<(nplane + 63) / 64, 64>>>(TB_LEVEL(lv[l]), lv[l].b, lv[l].x, gi, sc.t, sc.w);
+      ++launches;
+      gi -= gauss_iter2;
+      if (l == 0) break;
+      --l;
+      k_tri_tb_prolong_add<<<grid(lv[l]), 256>>>(0, nplane, lv[l].n2, lv[l].n1, lv[l + 1].x, lv[l].x);
+      ++launches;
+    }
+  }
+#undef TB_LEVEL
+  return cudaGetLastError();
+}
+
+// GaussSeidel_3D (MULTI/TriDiagTB_Mod.f90:818-874, TriDiagTR_Mod.f90:902-961) of
+// one level of n3 planes whose plane hierarchy pl[0..nlev2) holds all n3
+// planes (pl[0]'s b and x the level's, its residual free while the level is
+// smoothed, the coarser plane levels' b, x and residual work space): the
+// forward and backward plane sweeps, each plane solved by Solve_2D from the
+// current guess, then plane 1 and plane n3 once more.  t: one plane.
+cudaError_t level_gs(int variant, int n3, const PlaneLevel* pl, int nlev2, const double* u3, const double* l3,
+                     double* t, const Scratch& sc, int gauss_iter, int gauss_iter2, int mult_iter2, long& launches) {
+  const size_t npl = (size_t)pl[0].n2 * pl[0].n1;
+  const double* b = pl[0].b;
+  double* x = pl[0].x;
+  auto solve = [&](int k, const double* rhs) {
+    PlaneLevel one[32];
+    for (int m = 0; m < nlev2; ++m) {
+      const size_t a2 = pl[m].n2, a1 = pl[m].n1;
+      const size_t per[5] = {a2 * a1 * 4, a2 * (a1 - 1) * 4, a2 * (a1 - 1) * 4, (a2 - 1) * a1 * 4, (a2 - 1) * a1 * 4};
+      one[m] = pl[m];
+      for (int q = 0; q < 5; ++q) one[m].a[q] = pl[m].a[q] + (size_t)k * per[q];
+    }
+    one[0].b = const_cast<double*>(rhs);
+    one[0].x = x + (size_t)k * npl * 2;
+    return plane_cycles(variant, 1, nlev2, one, sc, gauss_iter2, mult_iter2, launches);
+  };
+  const unsigned g = (unsigned)((npl + 255) / 256);
+  auto couple = [&](const double* tin, const double* c, const double* xn) {
+    k_tri_tb_couple_sub<<<g, 256>>>(variant, (int)npl, tin, c, xn, t);
+    ++launches;
+  };
+#define TB_CHECK(expr)                       \
+  do {                                       \
+    cudaError_t e_ = (expr);                 \
+    if (e_ != cudaSuccess) return e_;        \
+  } while (0)
+  auto X = [&](int k) { return x + (size_t)k * npl * 2; };
+  auto B = [&](int k) { return b + (size_t)k * npl * 2; };
+  auto U = [&](int k) { return u3 + (size_t)k * npl * 4; };
+  auto Lo = [&](int k) { return l3 + (size_t)k * npl * 4; };
+  if (n3 > 1) {
+    for (int it = 0; it < gauss_iter; ++it) {
+      TB_CHECK(cudaMemcpyAsync(t, b, npl * 2 * sizeof(double), cudaMemcpyDeviceToDevice));
+      for (int k = 0; k < n3 - 1; ++k) {
+        couple(t, U(k), X(k + 1));
+        TB_CHECK(solve(k, t));
+        couple(B(k + 1), Lo(k), X(k));
+      }
+      TB_CHECK(solve(n3 - 1, t));
+      couple(B(n3 - 2), U(n3 - 2), X(n3 - 1));
+      for (int k = n3 - 2; k >= 1; --k) {
+        couple(t, Lo(k - 1), X(k - 1));
+        TB_CHECK(solve(k, t));
+        couple(B(k - 1), U(k - 1), X(k));
+      }
+    }
+    TB_CHECK(solve(0, t));
+    couple(B(n3 - 1), Lo(n3 - 2), X(n3 - 2));
+    TB_CHECK(solve(n3 - 1, t));
+  } else {
+    TB_CHECK(solve(0, b));
+  }
+#undef TB_CHECK
+  return cudaGetLastError();
+}
 
 }  // namespace
 
@@ -834,74 +1034,130 @@ int asam_tri_tb_multigrid_2d(int variant, int nplane, int nlev, const int* n2s, 
                              const double* const* d, const double* const* u1, const double* const* l1,
                              const double* const* u2, const double* const* l2, const double* b, double* x,
                              int gauss_iter2, int mult_iter) {
-  bool ok = (variant == 0 || variant == 1) && nplane >= 1 && nlev >= 1 && nlev <= 32 && n2s && n1s && d && u1 &&
-            l1 && u2 && l2 && b && x && gauss_iter2 >= 0 && mult_iter >= 0;
-  for (int l = 0; ok && l < nlev; ++l) {
-    ok = n2s[l] >= 1 && n1s[l] >= 1 && d[l] && (n1s[l] == 1 || (u1[l] && l1[l])) && (n2s[l] == 1 || (u2[l] && l2[l]));
-    if (ok && l > 0) ok = n2s[l] == (n2s[l - 1] + 1) / 2 && n1s[l] == (n1s[l - 1] + 1) / 2;
-  }
+  bool ok = (variant == 0 || variant == 1) && nplane >= 1 && b && x && gauss_iter2 >= 0 && mult_iter >= 0 &&
+            plane_levels_ok(nlev, n2s, n1s, d, u1, l1, u2, l2, (nlev >= 1 && n2s) ? n2s[0] : 0,
+                            (nlev >= 1 && n1s) ? n1s[0] : 0);
   if (!ok) {
     asam::set_last_error("asam_tri_tb_multigrid_2d: bad argument", __FILE__, __LINE__);
     return ASAM_BAD_ARG;
   }
-  // one allocation: per level the five block arrays, b, x and the residual;
-  // the smoother's scratch sized for the finest level
-  size_t len[32][8], tot = 0;
-  for (int l = 0; l < nlev; ++l) {
-    const size_t nl = (size_t)nplane * n2s[l], n1 = (size_t)n1s[l], n2 = (size_t)n2s[l];
-    const size_t a[8] = {nl * n1 * 4,  nl * (n1 - 1) * 4, nl * (n1 - 1) * 4, nplane * (n2 - 1) * n1 * 4,
-                         nplane * (n2 - 1) * n1 * 4, nl * n1 * 2, nl * n1 * 2, nl * n1 * 2};
-    for (int q = 0; q < 8; ++q) tot += (len[l][q] = a[q]);
-  }
+  // one allocation: the levels' blocks, b, x and the residual of every level
+  size_t tot = 0;
+  for (int l = 0; l < nlev; ++l) tot += plane_block_len(nplane, n2s[l], n1s[l]) + 3 * plane_vec_len(nplane, n2s[l], n1s[l]);
   const size_t nt = (size_t)nplane * n1s[0] * 2, nw = (size_t)nplane * (n1s[0] > 1 ? n1s[0] - 1 : 1) * 4;
   DevBufs m;
   TCU(cudaMalloc((void**)&m.p[0], (tot + nt + nw) * sizeof(double)));
-  double* dev[32][8];
-  size_t off = 0;
+  PlaneLevel lv[32];
+  double* cur = m.p[0];
   for (int l = 0; l < nlev; ++l) {
     const double* src[5] = {d[l], u1[l], l1[l], u2[l], l2[l]};
-    for (int q = 0; q < 8; ++q) {
-      dev[l][q] = m.p[0] + off;
-      if (q < 5 && len[l][q]) TCU(cudaMemcpy(dev[l][q], src[q], len[l][q] * sizeof(double), cudaMemcpyDefault));
-      off += len[l][q];
-    }
+    TCU(stage_plane_level(lv[l], nplane, n2s[l], n1s[l], src, cur));
   }
-  double *tb = m.p[0] + off, *wb = tb + nt;
-  TCU(cudaMemcpy(dev[0][5], b, len[0][5] * sizeof(double), cudaMemcpyDefault));
-  TCU(cudaMemcpy(dev[0][6], x, len[0][6] * sizeof(double), cudaMemcpyDefault));
+  Scratch sc{cur, cur + nt};
+  TCU(cudaMemcpy(lv[0].b, b, plane_vec_len(nplane, n2s[0], n1s[0]) * sizeof(double), cudaMemcpyDefault));
+  TCU(cudaMemcpy(lv[0].x, x, plane_vec_len(nplane, n2s[0], n1s[0]) * sizeof(double), cudaMemcpyDefault));
   long launches = 0;
-  auto grid = [&](int l) { return (unsigned)(((size_t)nplane * n2s[l] * n1s[l] + 255) / 256); };
-#define TB_LEVEL(l) variant, nplane, n2s[l], n1s[l], dev[l][0], dev[l][1], dev[l][2], dev[l][3], dev[l][4]
-  for (int it = 0; it < mult_iter; ++it) {
-    int gi = 1, l = 0;
-    for (;;) {  // Multigrid_2D's way down (MULTI/TriDiagTB_Mod.f90:449-470)
-      k_tri_tb_gs_2d<<<(nplane + 63) / 64, 64>>>(TB_LEVEL(l), dev[l][5], dev[l][6], gi, tb, wb);
-      ++launches;
-      gi += gauss_iter2;
-      if (l + 1 == nlev) {
-        gi -= gauss_iter2;
+  TCU(plane_cycles(variant, nplane, nlev, lv, sc, gauss_iter2, mult_iter, launches));
+  asam::count_launches(launches);
+  TCU(cudaMemcpy(x, lv[0].x, plane_vec_len(nplane, n2s[0], n1s[0]) * sizeof(double), cudaMemcpyDefault));
+  return ASAM_OK;
+}
+
+int asam_tri_tb_multigrid_3d(int variant, int nlev3, const int* n3s, const int* n2s, const int* n1s, const int* nlev2s,
+                             const double* const* u3, const double* const* l3, const double* const* d,
+                             const double* const* u1, const double* const* l1, const double* const* u2,
+                             const double* const* l2, const double* b, double* x, int gauss_iter2, int mult_iter2,
+                             int gauss_iter3, int mult_iter3) {
+  bool ok = (variant == 0 || variant == 1) && nlev3 >= 1 && nlev3 <= 32 && n3s && n2s && n1s && nlev2s && u3 && l3 &&
+            d && u1 && l1 && u2 && l2 && b && x && gauss_iter2 >= 0 && mult_iter2 >= 0 && gauss_iter3 >= 0 &&
+            mult_iter3 >= 0;
+  int p2[32][32], p1[32][32], off[32];
+  for (int L = 0, o = 0; ok && L < nlev3; ++L) {
+    ok = n3s[L] >= 1 && n2s[L] >= 1 && n1s[L] >= 1 && nlev2s[L] >= 1 && nlev2s[L] <= 32 && o + nlev2s[L] <= 1024 &&
+         (n3s[L] == 1 || (u3[L] && l3[L]));
+    if (ok && L > 0)
+      ok = n3s[L] == (n3s[L - 1] + 1) / 2 && n2s[L] == (n2s[L - 1] + 1) / 2 && n1s[L] == (n1s[L - 1] + 1) / 2;
+    if (!ok) break;
+    p2[L][0] = n2s[L];
+    p1[L][0] = n1s[L];
+    for (int m = 1; m < nlev2s[L]; ++m) {
+      p2[L][m] = (p2[L][m - 1] + 1) / 2;
+      p1[L][m] = (p1[L][m - 1] + 1) / 2;
+    }
+    ok = plane_levels_ok(nlev2s[L], p2[L], p1[L], d + o, u1 + o, l1 + o, u2 + o, l2 + o, n2s[L], n1s[L]);
+    off[L] = o;
+    o += nlev2s[L];
+  }
+  if (!ok) {
+    asam::set_last_error("asam_tri_tb_multigrid_3d: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  // one allocation: every level's plane hierarchy (blocks, b, x, residual
+  // for all its planes), its couplings between planes, the smoother's plane
+  // right-hand side and scratch
+  size_t tot = 0;
+  for (int L = 0; L < nlev3; ++L) {
+    for (int m = 0; m < nlev2s[L]; ++m)
+      tot += plane_block_len(n3s[L], p2[L][m], p1[L][m]) + 3 * plane_vec_len(n3s[L], p2[L][m], p1[L][m]);
+    tot += 2 * (size_t)(n3s[L] - 1) * n2s[L] * n1s[L] * 4;
+  }
+  const size_t npl = (size_t)n2s[0] * n1s[0], nt = (size_t)n1s[0] * 2, nw = (size_t)(n1s[0] > 1 ? n1s[0] - 1 : 1) * 4;
+  DevBufs m;
+  TCU(cudaMalloc((void**)&m.p[0], (tot + npl * 2 + nt + nw) * sizeof(double)));
+  static thread_local PlaneLevel pl[32][32];
+  double* cur = m.p[0];
+  double *du3[32], *dl3[32];
+  for (int L = 0; L < nlev3; ++L) {
+    for (int q = 0; q < nlev2s[L]; ++q) {
+      const int o = off[L] + q;
+      const double* src[5] = {d[o], u1[o], l1[o], u2[o], l2[o]};
+      TCU(stage_plane_level(pl[L][q], n3s[L], p2[L][q], p1[L][q], src, cur));
+    }
+    const size_t nc = (size_t)(n3s[L] - 1) * n2s[L] * n1s[L] * 4;
+    du3[L] = nc ? cur : nullptr;
+    dl3[L] = nc ? cur + nc : nullptr;
+    if (nc) {
+      TCU(cudaMemcpy(du3[L], u3[L], nc * sizeof(double), cudaMemcpyDefault));
+      TCU(cudaMemcpy(dl3[L], l3[L], nc * sizeof(double), cudaMemcpyDefault));
+    }
+    cur += 2 * nc;
+  }
+  double* t = cur;
+  Scratch sc{cur + npl * 2, cur + npl * 2 + nt};
+  const size_t nv0 = plane_vec_len(n3s[0], n2s[0], n1s[0]);
+  TCU(cudaMemcpy(pl[0][0].b, b, nv0 * sizeof(double), cudaMemcpyDefault));
+  TCU(cudaMemcpy(pl[0][0].x, x, nv0 * sizeof(double), cudaMemcpyDefault));
+  long launches = 0;
+  auto grid = [&](int L) { return (unsigned)(((size_t)n3s[L] * n2s[L] * n1s[L] + 255) / 256); };
+  for (int it = 0; it < mult_iter3; ++it) {
+    int gi = 1, L = 0;
+    for (;;) {  // Multigrid_3D's way down (MULTI/TriDiagTB_Mod.f90:891-914)
+      TCU(level_gs(variant, n3s[L], pl[L], nlev2s[L], du3[L], dl3[L], t, sc, gi, gauss_iter2, mult_iter2, launches));
+      gi += gauss_iter3;
+      if (L + 1 == nlev3) {
+        gi -= gauss_iter3;
         break;
       }
-      k_tri_tb_residual_2d<<<grid(l), 256>>>(TB_LEVEL(l), dev[l][5], dev[l][6], dev[l][7]);
-      k_tri_tb_restrict_2d<<<grid(l + 1), 256>>>(nplane, n2s[l], n1s[l], dev[l][7], dev[l + 1][5]);
-      TCU(cudaMemsetAsync(dev[l + 1][6], 0, len[l + 1][6] * sizeof(double)));
+      const PlaneLevel& F = pl[L][0];
+      k_tri_tb_residual<<<grid(L), 256>>>(variant, n3s[L], n2s[L], n1s[L], F.a[0], F.a[1], F.a[2], F.a[3], F.a[4],
+                                          du3[L], dl3[L], F.b, F.x, F.res);
+      k_tri_tb_restrict_3d<<<grid(L + 1), 256>>>(n3s[L], n2s[L], n1s[L], F.res, pl[L + 1][0].b);
+      TCU(cudaMemsetAsync(pl[L + 1][0].x, 0, plane_vec_len(n3s[L + 1], n2s[L + 1], n1s[L + 1]) * sizeof(double)));
       launches += 2;
-      ++l;
+      ++L;
     }
-    for (;;) {  // and up (:471-493)
-      k_tri_tb_gs_2d<<<(nplane + 63) / 64, 64>>>(TB_LEVEL(l), dev[l][5], dev[l][6], gi, tb, wb);
-      ++launches;
-      gi -= gauss_iter2;
-      if (l == 0) break;
-      --l;
-      k_tri_tb_prolong_add_2d<<<grid(l), 256>>>(nplane, n2s[l], n1s[l], dev[l + 1][6], dev[l][6]);
+    for (;;) {  // and up (:915-937)
+      TCU(level_gs(variant, n3s[L], pl[L], nlev2s[L], du3[L], dl3[L], t, sc, gi, gauss_iter2, mult_iter2, launches));
+      gi -= gauss_iter3;
+      if (L == 0) break;
+      --L;
+      k_tri_tb_prolong_add<<<grid(L), 256>>>(1, n3s[L], n2s[L], n1s[L], pl[L + 1][0].x, pl[L][0].x);
       ++launches;
     }
     TCU(cudaGetLastError());
   }
-#undef TB_LEVEL
   asam::count_launches(launches);
-  TCU(cudaMemcpy(x, dev[0][6], len[0][6] * sizeof(double), cudaMemcpyDefault));
+  TCU(cudaMemcpy(x, pl[0][0].x, nv0 * sizeof(double), cudaMemcpyDefault));
   return ASAM_OK;
 }
 

@@ -663,6 +663,27 @@ int asam_tri_tb_multigrid_2d(int variant, int nplane, int nlev, const int *n2s, 
                              const double *const *d, const double *const *u1, const double *const *l1,
                              const double *const *u2, const double *const *l2, const double *b, double *x,
                              int gauss_iter2, int mult_iter);
+/* Solve_3D of TriDiagTB (variant 0, MULTI/TriDiagTB_Mod.f90:818-952) or
+ * TriDiagTR (variant 1, TriDiagTR_Mod.f90:902-1041): mult_iter3 (MultIter3)
+ * V-cycles of Multigrid_3D over nlev3 levels, finest first.  Level L has
+ * n3s[L] planes of n2s[L] lines of n1s[L] levels (each size halved, rounding
+ * up, on the next level), its couplings between planes u3[L], l3[L] as
+ * asam_tri_tb_compute_3d writes them (unused when n3s[L] is 1) and its
+ * planes' hierarchy of nlev2s[L] plane levels, all planes of plane level m
+ * at d[o+m], u1[o+m], l1[o+m], u2[o+m], l2[o+m] with o the sum of
+ * nlev2s[0..L-1] (the layout of asam_tri_tb_multigrid_2d's levels; plane
+ * level 0 is the level's own planes).  Down: GaussSeidel_3D with GaussIter 1,
+ * raised by gauss_iter3 per level -- plane sweeps forward and backward, each
+ * plane solved by Solve_2D (gauss_iter2, mult_iter2) from the current guess,
+ * then planes 1 and n3 once more -- the residual restricted by RestrictTB_3D,
+ * a zero coarse guess; up: GaussSeidel_3D again, the prolonged guess added.
+ * b, x [((k*n2 + j)*n1 + i)*2 + r] on the finest level; x in: the initial
+ * guess, out: the result.  nlev3 and every nlev2s[L] <= 32. */
+int asam_tri_tb_multigrid_3d(int variant, int nlev3, const int *n3s, const int *n2s, const int *n1s, const int *nlev2s,
+                             const double *const *u3, const double *const *l3, const double *const *d,
+                             const double *const *u1, const double *const *l1, const double *const *u2,
+                             const double *const *l2, const double *b, double *x, int gauss_iter2, int mult_iter2,
+                             int gauss_iter3, int mult_iter3);
 
 /* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141),
  * the same as MatVecTR_1D (MULTI/TriDiagTR_Mod.f90:133-153). */

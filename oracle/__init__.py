@@ -70,6 +70,10 @@ def load() -> C.CDLL:
             "ora_tri_tb_restrict_2d": (None, [I, I, I, V, V]),
             "ora_tri_tb_prolong_2d": (None, [I, I, I, V, V]),
             "ora_tri_tb_multigrid_2d": (None, [I, I, I, V, V] + [V] * 7 + [I, I]),
+            "ora_tri_tb_gauss_seidel_3d": (None, [I, I, I, V, V] + [V] * 9 + [I, I, I]),
+            "ora_tri_tb_restrict_3d": (None, [I, I, I, V, V]),
+            "ora_tri_tb_prolong_3d": (None, [I, I, I, V, V]),
+            "ora_tri_tb_multigrid_3d": (None, [I, I, V, V, V, V] + [V] * 9 + [I, I, I, I]),
             "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
         }
         sig.update({
@@ -540,6 +544,77 @@ def tri_tb_multigrid_2d(levels, b, x0, gauss_iter2=1, mult_iter=1, tr=False):
     lib.ora_tri_tb_multigrid_2d(int(tr), nplane, nlev, C.cast(n2s, C.c_void_p), C.cast(n1s, C.c_void_p),
                                 *[C.cast(a, C.c_void_p) for a in arrs], _p(bb), _p(x), int(gauss_iter2),
                                 int(mult_iter))
+    return x
+
+
+def _ptrs(arrs):
+    return C.cast((C.c_void_p * len(arrs))(*[a.ctypes.data if a is not None and a.size else None for a in arrs]),
+                  C.c_void_p)
+
+
+def _ints(vals):
+    return C.cast((C.c_int * len(vals))(*vals), C.c_void_p)
+
+
+def _level3(level):
+    """(plane_levels, u3, l3) with contiguous float64 arrays: plane_levels =
+    [(d, u1, l1, u2, l2), ...] of all the level's planes, finest first."""
+    planes, u3, l3 = level
+    keep = [_tb_plane_blocks(lv) for lv in planes]
+    return keep, np.ascontiguousarray(u3, dtype=np.float64), np.ascontiguousarray(l3, dtype=np.float64)
+
+
+def tri_tb_gauss_seidel_3d(level, b, x0, iters, gauss_iter2=1, mult_iter2=1, tr=False):
+    """GaussSeidel_3D (MULTI/TriDiagTB_Mod.f90:818-874; TriDiagTR with tr) of
+    one level: level = (plane_levels, u3, l3) -- plane_levels the hierarchy of
+    its n3 planes as tri_tb_multigrid_2d takes it, u3, l3 (n3-1, n2, n1, 4);
+    b, x0 (n3, n2, n1, 2); each plane solved by Solve_2D."""
+    lib = load()
+    keep, u3, l3 = _level3(level)
+    n3, n2, n1 = keep[0][0].shape[:3]
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.ascontiguousarray(x0, dtype=np.float64).copy()
+    lib.ora_tri_tb_gauss_seidel_3d(int(tr), n3, len(keep), _ints([k[0].shape[1] for k in keep]),
+                                   _ints([k[0].shape[2] for k in keep]), *[_ptrs([k[j] for k in keep]) for j in range(5)],
+                                   _p(u3) if u3.size else None, _p(l3) if l3.size else None, _p(bb), _p(x),
+                                   int(iters), int(gauss_iter2), int(mult_iter2))
+    return x
+
+
+def tri_tb_restrict_3d(res):
+    """RestrictTB_3D of a level res (n3, n2, n1, 2) -> halved sizes."""
+    lib = load()
+    r = np.ascontiguousarray(res, dtype=np.float64)
+    n3, n2, n1 = r.shape[:3]
+    out = np.empty(((n3 + 1) // 2, (n2 + 1) // 2, (n1 + 1) // 2, 2))
+    lib.ora_tri_tb_restrict_3d(n3, n2, n1, _p(r), _p(out))
+    return out
+
+
+def tri_tb_prolong_3d(xc, n3, n2, n1):
+    """ProlongateTB_3D of a coarse level onto n3 x n2 x n1."""
+    lib = load()
+    c = np.ascontiguousarray(xc, dtype=np.float64)
+    out = np.empty((n3, n2, n1, 2))
+    lib.ora_tri_tb_prolong_3d(n3, n2, n1, _p(c), _p(out))
+    return out
+
+
+def tri_tb_multigrid_3d(levels, b, x0, gauss_iter2=1, mult_iter2=1, gauss_iter3=1, mult_iter3=1, tr=False):
+    """Solve_3D (MULTI/TriDiagTB_Mod.f90:876-952; TriDiagTR with tr):
+    mult_iter3 V-cycles of Multigrid_3D over levels = [(plane_levels, u3,
+    l3), ...] finest first, each level's sizes halved (rounding up) from the
+    last; b, x0 (n3, n2, n1, 2) on the finest level."""
+    lib = load()
+    lv = [_level3(L) for L in levels]
+    flat = [k for keep, _, _ in lv for k in keep]
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.ascontiguousarray(x0, dtype=np.float64).copy()
+    lib.ora_tri_tb_multigrid_3d(int(tr), len(lv), _ints([k[0][0].shape[0] for k, _, _ in lv]),
+                                _ints([k[0][0].shape[1] for k, _, _ in lv]), _ints([k[0][0].shape[2] for k, _, _ in lv]),
+                                _ints([len(k) for k, _, _ in lv]), _ptrs([u for _, u, _ in lv]),
+                                _ptrs([l for _, _, l in lv]), *[_ptrs([k[j] for k in flat]) for j in range(5)], _p(bb),
+                                _p(x), int(gauss_iter2), int(mult_iter2), int(gauss_iter3), int(mult_iter3))
     return x
 
 

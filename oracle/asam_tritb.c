@@ -617,3 +617,193 @@ void ora_tri_tb_multigrid_2d(int variant, int nplane, int nlev, const int *n2s, 
     }
   }
 }
+
+/* The plane solve Solve(A%d(k)%P, t, x(:,:,:,k)) of GaussSeidel_3D: Solve_2D on
+ * plane k of a level whose planes carry nlev2 plane levels (the 2D level m
+ * of all n3 planes at d[m] .. l2[m], n2 x n1 halved m times). */
+static void solve_plane(int variant, int k, int nlev2, const int *n2s, const int *n1s, const double *const *d,
+                        const double *const *u1, const double *const *l1, const double *const *u2,
+                        const double *const *l2, const double *t, double *x, int gauss_iter2, int mult_iter2) {
+  const double *pd[32], *pu1[32], *pl1[32], *pu2[32], *pl2[32];
+  for (int m = 0; m < nlev2; ++m) {
+    const size_t n2 = (size_t)n2s[m], n1 = (size_t)n1s[m];
+    pd[m] = d[m] + k * n2 * n1 * 4;
+    pu1[m] = u1[m] + k * n2 * (n1 - 1) * 4;
+    pl1[m] = l1[m] + k * n2 * (n1 - 1) * 4;
+    pu2[m] = u2[m] + k * (n2 - 1) * n1 * 4;
+    pl2[m] = l2[m] + k * (n2 - 1) * n1 * 4;
+  }
+  ora_tri_tb_multigrid_2d(variant, 1, nlev2, n2s, n1s, pd, pu1, pl1, pu2, pl2, t, x, gauss_iter2, mult_iter2);
+}
+
+/* GaussSeidel_3D (MULTI/TriDiagTB_Mod.f90:818-874, TriDiagTR_Mod.f90:902-961) of
+ * one level of n3 planes: per iteration the planes 1..n3-1 forward and n3..2
+ * backward, each plane's right-hand side minus its couplings to the planes
+ * either side (u3, l3 as ora_tri_tb_compute_3d writes them), each plane
+ * solved by Solve_2D from the current guess; then plane 1 and, additionally,
+ * plane n3 once more.  n2s, n1s: the plane levels' sizes, n2s[0] = n2. */
+void ora_tri_tb_gauss_seidel_3d(int variant, int n3, int nlev2, const int *n2s, const int *n1s,
+                                const double *const *d, const double *const *u1, const double *const *l1,
+                                const double *const *u2, const double *const *l2, const double *u3, const double *l3,
+                                const double *b, double *x, int gauss_iter, int gauss_iter2, int mult_iter2) {
+  const int tr = variant == 1;
+  const size_t npl = (size_t)n2s[0] * n1s[0];
+  double *t = (double *)malloc(sizeof(double) * npl * 2);
+#define SOLVE(k, rhs) \
+  solve_plane(variant, k, nlev2, n2s, n1s, d, u1, l1, u2, l2, rhs, x + (size_t)(k)*npl * 2, gauss_iter2, mult_iter2)
+#define XP(a, r, k) (a + ((size_t)(k)*npl + (r)) * 2)
+#define CP(a, r, k) (a + ((size_t)(k)*npl + (r)) * 4)
+  if (n3 > 1) {
+    for (int it = 0; it < gauss_iter; ++it) {
+      memcpy(t, b, sizeof(double) * npl * 2);
+      for (int k = 0; k < n3 - 1; ++k) {
+        for (size_t r = 0; r < npl; ++r) couple_sub(tr, t + r * 2, CP(u3, r, k), XP(x, r, k + 1), t + r * 2);
+        SOLVE(k, t);
+        for (size_t r = 0; r < npl; ++r) {
+          couple_sub(tr, XP(b, r, k + 1), CP(l3, r, k), XP(x, r, k), t + r * 2);
+        }
+      }
+      SOLVE(n3 - 1, t);
+      for (size_t r = 0; r < npl; ++r) {
+        couple_sub(tr, XP(b, r, n3 - 2), CP(u3, r, n3 - 2), XP(x, r, n3 - 1), t + r * 2);
+      }
+      for (int k = n3 - 2; k >= 1; --k) {
+        for (size_t r = 0; r < npl; ++r) couple_sub(tr, t + r * 2, CP(l3, r, k - 1), XP(x, r, k - 1), t + r * 2);
+        SOLVE(k, t);
+        for (size_t r = 0; r < npl; ++r) {
+          couple_sub(tr, XP(b, r, k - 1), CP(u3, r, k - 1), XP(x, r, k), t + r * 2);
+        }
+      }
+    }
+    SOLVE(0, t);
+    for (size_t r = 0; r < npl; ++r) {
+      couple_sub(tr, XP(b, r, n3 - 1), CP(l3, r, n3 - 2), XP(x, r, n3 - 2), t + r * 2);
+    }
+    SOLVE(n3 - 1, t);
+  } else {
+    SOLVE(0, b);
+  }
+#undef SOLVE
+#undef XP
+#undef CP
+  free(t);
+}
+
+/* RestrictTB_3D (MULTI/TriDiagTB_Mod.f90:954-1026): the value the reference's
+ * overwriting loops leave in each coarse entry -- its fine cells summed along
+ * the axes where it has two (the last cell of an odd axis alone), in the
+ * order (i,j,k), (i+1,j,k), (i,j+1,k), (i,j,k+1), (i+1,j+1,k), (i+1,j,k+1),
+ * (i,j+1,k+1), (i+1,j+1,k+1) of the cells that exist; with two paired axes
+ * a, b: (a,b), (a+1,b), (a,b+1), (a+1,b+1). */
+void ora_tri_tb_restrict_3d(int n3, int n2, int n1, const double *res, double *resc) {
+  const int n1c = (n1 + 1) / 2, n2c = (n2 + 1) / 2, n3c = (n3 + 1) / 2;
+  static const int ord[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1},
+                                {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+  for (int kc = 0; kc < n3c; ++kc)
+    for (int jc = 0; jc < n2c; ++jc)
+      for (int ic = 0; ic < n1c; ++ic) {
+        const int pi = ic < n1 / 2, pj = jc < n2 / 2, pk = kc < n3 / 2;
+        const int i0 = pi ? 2 * ic : n1 - 1, j0 = pj ? 2 * jc : n2 - 1, k0 = pk ? 2 * kc : n3 - 1;
+        double s0 = 0.0, s1 = 0.0;
+        int first = 1;
+        for (int q = 0; q < 8; ++q) {
+          if ((ord[q][0] && !pi) || (ord[q][1] && !pj) || (ord[q][2] && !pk)) continue;
+          const double *v = res + ((((size_t)(k0 + ord[q][2]) * n2 + j0 + ord[q][1]) * n1) + i0 + ord[q][0]) * 2;
+          if (first) {
+            s0 = v[0];
+            s1 = v[1];
+            first = 0;
+          } else {
+            s0 = s0 + v[0];
+            s1 = s1 + v[1];
+          }
+        }
+        double *o = resc + (((size_t)kc * n2c + jc) * n1c + ic) * 2;
+        o[0] = s0;
+        o[1] = s1;
+      }
+}
+
+/* ProlongateTB_3D (MULTI/TriDiagTB_Mod.f90:1028-1100): each fine entry its
+ * coarse cell's value. */
+void ora_tri_tb_prolong_3d(int n3, int n2, int n1, const double *xc, double *x) {
+  const int n1c = (n1 + 1) / 2, n2c = (n2 + 1) / 2;
+  for (int k = 0; k < n3; ++k)
+    for (int j = 0; j < n2; ++j)
+      for (int i = 0; i < n1; ++i) {
+        const double *c = xc + (((size_t)(k / 2) * n2c + j / 2) * n1c + i / 2) * 2;
+        double *o = x + (((size_t)k * n2 + j) * n1 + i) * 2;
+        o[0] = c[0];
+        o[1] = c[1];
+      }
+}
+
+/* Solve_3D (MULTI/TriDiagTB_Mod.f90:940-952, TriDiagTR_Mod.f90:1028-1041):
+ * mult_iter3 V-cycles of Multigrid_3D (TriDiagTB_Mod.f90:876-938) over nlev3
+ * levels, level L of n3s[L] planes of n2s[L] x n1s[L] (each halved, rounding
+ * up, on the next level), its couplings between planes u3[L], l3[L] and its
+ * planes' nlev2s[L] plane levels at d[o + m] .. l2[o + m], o = the sum of
+ * nlev2s[0..L-1].  Down: GaussSeidel_3D with GaussIter 1, raised by
+ * gauss_iter3 per level, the residual b - A x restricted, a zero coarse
+ * guess; up: GaussSeidel_3D again, the prolonged guess added.  Each plane
+ * solve is Solve_2D with gauss_iter2, mult_iter2. */
+void ora_tri_tb_multigrid_3d(int variant, int nlev3, const int *n3s, const int *n2s, const int *n1s, const int *nlev2s,
+                             const double *const *u3, const double *const *l3, const double *const *d,
+                             const double *const *u1, const double *const *l1, const double *const *u2,
+                             const double *const *l2, const double *b, double *x, int gauss_iter2, int mult_iter2,
+                             int gauss_iter3, int mult_iter3) {
+  double *bl[32], *xl[32], *res[32];
+  int off[32], p2[32][32], p1[32][32];
+  for (int L = 0, o = 0; L < nlev3; ++L) {
+    const size_t n = (size_t)n3s[L] * n2s[L] * n1s[L] * 2;
+    res[L] = (double *)malloc(sizeof(double) * n);
+    bl[L] = L ? (double *)malloc(sizeof(double) * n) : (double *)b;
+    xl[L] = L ? (double *)malloc(sizeof(double) * n) : x;
+    off[L] = o;
+    o += nlev2s[L];
+    p2[L][0] = n2s[L];
+    p1[L][0] = n1s[L];
+    for (int m = 1; m < nlev2s[L]; ++m) {
+      p2[L][m] = (p2[L][m - 1] + 1) / 2;
+      p1[L][m] = (p1[L][m - 1] + 1) / 2;
+    }
+  }
+#define GS3(L, gi)                                                                                                 \
+  ora_tri_tb_gauss_seidel_3d(variant, n3s[L], nlev2s[L], p2[L], p1[L], d + off[L], u1 + off[L], l1 + off[L],    \
+                             u2 + off[L], l2 + off[L], u3[L], l3[L], bl[L], xl[L], gi, gauss_iter2, mult_iter2)
+  for (int it = 0; it < mult_iter3; ++it) {
+    int gi = 1, L = 0;
+    for (;;) {
+      GS3(L, gi);
+      gi += gauss_iter3;
+      if (L + 1 == nlev3) {
+        gi -= gauss_iter3;
+        break;
+      }
+      const size_t n = (size_t)n3s[L] * n2s[L] * n1s[L] * 2;
+      ora_tri_tb_matvec_3d(variant, n3s[L], n2s[L], n1s[L], d[off[L]], u1[off[L]], l1[off[L]], u2[off[L]],
+                           l2[off[L]], u3[L], l3[L], xl[L], res[L]);
+      for (size_t q = 0; q < n; ++q) res[L][q] = bl[L][q] - res[L][q];
+      ora_tri_tb_restrict_3d(n3s[L], n2s[L], n1s[L], res[L], bl[L + 1]);
+      memset(xl[L + 1], 0, sizeof(double) * (size_t)n3s[L + 1] * n2s[L + 1] * n1s[L + 1] * 2);
+      ++L;
+    }
+    for (;;) {
+      GS3(L, gi);
+      gi -= gauss_iter3;
+      if (L == 0) break;
+      --L;
+      const size_t n = (size_t)n3s[L] * n2s[L] * n1s[L] * 2;
+      ora_tri_tb_prolong_3d(n3s[L], n2s[L], n1s[L], xl[L + 1], res[L]);
+      for (size_t q = 0; q < n; ++q) xl[L][q] = xl[L][q] + res[L][q];
+    }
+  }
+#undef GS3
+  for (int L = 0; L < nlev3; ++L) {
+    free(res[L]);
+    if (L) {
+      free(bl[L]);
+      free(xl[L]);
+    }
+  }
+}

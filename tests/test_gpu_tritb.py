@@ -172,3 +172,59 @@ def test_tri_tb_multigrid_2d_bad_args(built_lib):
         asam.SolveTB_2D([levels[0], levels[0]], b, b, 1, 1)
     with pytest.raises(AsamError):
         asam.SolveTB_2D(levels, b, b, -1, 1)
+
+
+def random_levels_3d(n3, n2, n1, seed):
+    """Independent diagonally dominant levels and plane levels (bits only)."""
+    from tests.test_tritb import plane_case
+
+    levels, b0 = [], None
+    while True:
+        r = np.random.default_rng(seed + len(levels))
+        planes, p2, p1 = [], n2, n1
+        while True:
+            blocks, b = plane_case(n3, p2, p1, seed=seed + 100 * len(levels) + len(planes))
+            if b0 is None:
+                b0 = b
+            planes.append(blocks)
+            if p2 == 1 and p1 == 1:
+                break
+            p2, p1 = (p2 + 1) // 2, (p1 + 1) // 2
+        levels.append((planes, r.uniform(-1, 1, (n3 - 1, n2, n1, 4)), r.uniform(-1, 1, (n3 - 1, n2, n1, 4))))
+        if (n3, n2, n1) == (1, 1, 1):
+            return levels, b0
+        n3, n2, n1 = (n3 + 1) // 2, (n2 + 1) // 2, (n1 + 1) // 2
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("n3,n2,n1,gi3,cycles", [(4, 4, 4, 1, 2), (3, 5, 2, 2, 1), (1, 1, 1, 1, 2), (5, 1, 3, 0, 2),
+                                                  (12, 24, 20, 1, 1)])
+def test_tri_tb_multigrid_3d_bitwise(built_lib, variant, n3, n2, n1, gi3, cycles):
+    """Solve_3D / Multigrid_3D on the GPU (the plane sweeps of GaussSeidel_3D,
+    each plane's Solve_2D, the residual, RestrictTB_3D and the correction as
+    kernels on one stream) equals the oracle bit for bit, on Galerkin
+    hierarchies and on a 12x24x20 level with five levels."""
+    from tests.test_tritb import level_hierarchy_3d
+
+    tr = variant == "TR"
+    if n3 * n2 * n1 <= 64:
+        levels, b = level_hierarchy_3d(n3, n2, n1, seed=n3 + 5 * n2 + 11 * n1, tr=tr)
+    else:
+        levels, b = random_levels_3d(n3, n2, n1, seed=21)
+    x0 = np.random.default_rng(4).standard_normal(b.shape)
+    for gi2, mi2 in ((1, 1), (2, 2)):
+        assert np.array_equal(asam.SolveTB_3D(levels, b, x0, gi2, mi2, gi3, cycles, tr),
+                              oracle.tri_tb_multigrid_3d(levels, b, x0, gi2, mi2, gi3, cycles, tr))
+
+
+def test_tri_tb_multigrid_3d_bad_args(built_lib):
+    from asam_gb300._lib import AsamError
+
+    levels, b = random_levels_3d(3, 4, 4, seed=2)
+    with pytest.raises(AsamError):  # a level of the wrong size
+        asam.SolveTB_3D([levels[0], levels[0]], b, b)
+    planes, u3, l3 = levels[0]
+    with pytest.raises(ValueError):  # a plane level of the wrong size
+        asam.SolveTB_3D([(planes[:1] + planes[:1], u3, l3)] + levels[1:], b, b)
+    with pytest.raises(AsamError):
+        asam.SolveTB_3D(levels, b, b, mult_iter3=-1)

@@ -566,3 +566,231 @@ def test_oracle_multigrid_2d_converges(built_oracle, variant):
         errs.append(np.max(np.abs(x - ref)) / np.max(np.abs(ref)))
     assert errs[-1] <= 1e-10, errs
     assert all(e1 < e0 for e0, e1 in zip(errs, errs[1:]) if e0 > 1e-14), errs
+
+
+def restrict_3d_loops(res):
+    """RestrictTB_3D (MULTI/TriDiagTB_Mod.f90:954-1026) as the reference's
+    overwriting loops, statement by statement (0-based)."""
+    n3, n2, n1 = res.shape[:3]
+    n1c, n2c, n3c = (n1 + 1) // 2, (n2 + 1) // 2, (n3 + 1) // 2
+    R = lambda i, j, k: res[k, j, i]  # noqa: E731
+    out = np.zeros((n3c, n2c, n1c, 2))
+    out[n3c - 1, n2c - 1, n1c - 1] = R(n1 - 1, n2 - 1, n3 - 1)
+    for ic in range(n1 // 2):
+        out[n3c - 1, n2c - 1, ic] = R(2 * ic, n2 - 1, n3 - 1) + R(2 * ic + 1, n2 - 1, n3 - 1)
+    for jc in range(n2 // 2):
+        j = 2 * jc
+        out[n3c - 1, jc, n1c - 1] = R(n1 - 1, j, n3 - 1) + R(n1 - 1, j + 1, n3 - 1)
+        for ic in range(n1 // 2):
+            i = 2 * ic
+            out[n3c - 1, jc, ic] = R(i, j, n3 - 1) + R(i + 1, j, n3 - 1) + R(i, j + 1, n3 - 1) + R(i + 1, j + 1, n3 - 1)
+    for kc in range(n3 // 2):
+        k = 2 * kc
+        out[kc, n2c - 1, n1c - 1] = R(n1 - 1, n2 - 1, k) + R(n1 - 1, n2 - 1, k + 1)
+        for ic in range(n1 // 2):
+            i = 2 * ic
+            out[kc, n2c - 1, ic] = R(i, n2 - 1, k) + R(i + 1, n2 - 1, k) + R(i, n2 - 1, k + 1) + R(i + 1, n2 - 1, k + 1)
+        for jc in range(n2 // 2):
+            j = 2 * jc
+            out[kc, jc, n1c - 1] = R(n1 - 1, j, k) + R(n1 - 1, j + 1, k) + R(n1 - 1, j, k + 1) + R(n1 - 1, j + 1, k + 1)
+            for ic in range(n1 // 2):
+                i = 2 * ic
+                out[kc, jc, ic] = (R(i, j, k) + R(i + 1, j, k) + R(i, j + 1, k) + R(i, j, k + 1) + R(i + 1, j + 1, k)
+                                   + R(i + 1, j, k + 1) + R(i, j + 1, k + 1) + R(i + 1, j + 1, k + 1))
+    return out
+
+
+@pytest.mark.parametrize("n3,n2,n1", [(1, 1, 1), (2, 2, 2), (3, 5, 4), (4, 7, 6), (5, 3, 9), (2, 1, 3)])
+def test_oracle_restrict_prolong_3d(built_oracle, n3, n2, n1):
+    """RestrictTB_3D / ProlongateTB_3D (MULTI/TriDiagTB_Mod.f90:954-1100) bit
+    for bit against the reference's overwriting loops; the prolongation
+    copies each coarse entry to its fine cells."""
+    res = np.random.default_rng(n3 + n2 + n1).standard_normal((n3, n2, n1, 2))
+    got = oracle.tri_tb_restrict_3d(res)
+    assert np.array_equal(got, restrict_3d_loops(res))
+    back = oracle.tri_tb_prolong_3d(got, n3, n2, n1)
+    k, j, i = np.meshgrid(np.arange(n3), np.arange(n2), np.arange(n1), indexing="ij")
+    assert np.array_equal(back, got[k // 2, j // 2, i // 2])
+
+
+def couple_sub_np(t, c, x, tr):
+    """t - (coupling) x as the oracle forms it: TriDiagTB's vector times the
+    neighbour's first component, TriDiagTR's Mult_2 (CG/Matrix_Mod.f90)."""
+    if tr:
+        v0 = c[..., 0] * x[..., 0] + c[..., 2] * x[..., 1]
+        v1 = c[..., 1] * x[..., 0] + c[..., 3] * x[..., 1]
+        return np.stack([t[..., 0] - v0, t[..., 1] - v1], axis=-1)
+    return np.stack([t[..., 0] - c[..., 0] * x[..., 0], t[..., 1] - c[..., 1] * x[..., 0]], axis=-1)
+
+
+def plane_levels_of(blocks, tr):
+    levels = [tuple(blocks)]
+    while levels[-1][0].shape[1] > 1 or levels[-1][0].shape[2] > 1:
+        levels.append(galerkin_coarse(levels[-1], tr))
+    return levels
+
+
+def galerkin_coarse_3d(blocks7, tr):
+    """R A P of a level (7 blocks), 2x2x2 cells to one: again 7 blocks."""
+    n3, n2, n1 = blocks7[0].shape[:3]
+    c3, c2, c1 = (n3 + 1) // 2, (n2 + 1) // 2, (n1 + 1) // 2
+    idx = lambda i, j, k, a, b: ((k * a + j) * b + i) * 2  # noqa: E731
+    P = np.zeros((n3 * n2 * n1 * 2, c3 * c2 * c1 * 2))
+    for k in range(n3):
+        for j in range(n2):
+            for i in range(n1):
+                f, c = idx(i, j, k, n2, n1), idx(i // 2, j // 2, k // 2, c2, c1)
+                P[f:f + 2, c:c + 2] = np.eye(2)
+    Ac = P.T @ dense_level(blocks7, tr) @ P
+    blk = lambda a, c: Ac[a:a + 2, c:c + 2].reshape(-1, order="F")  # noqa: E731
+    out = [np.zeros((c3, c2, c1, 4)), np.zeros((c3, c2, max(c1 - 1, 0), 4)), np.zeros((c3, c2, max(c1 - 1, 0), 4)),
+           np.zeros((c3, max(c2 - 1, 0), c1, 4)), np.zeros((c3, max(c2 - 1, 0), c1, 4)),
+           np.zeros((max(c3 - 1, 0), c2, c1, 4)), np.zeros((max(c3 - 1, 0), c2, c1, 4))]
+    for k in range(c3):
+        for j in range(c2):
+            for i in range(c1):
+                a = idx(i, j, k, c2, c1)
+                out[0][k, j, i] = blk(a, a)
+                for ax, (di, dj, dk) in ((1, (1, 0, 0)), (3, (0, 1, 0)), (5, (0, 0, 1))):
+                    if i + di < c1 and j + dj < c2 and k + dk < c3:
+                        b_ = idx(i + di, j + dj, k + dk, c2, c1)
+                        out[ax][k, j, i] = blk(a, b_)
+                        out[ax + 1][k, j, i] = blk(b_, a)
+    assert np.allclose(dense_level(out, tr), Ac, atol=1e-12)
+    return out
+
+
+def level_hierarchy_3d(n3, n2, n1, seed, tr, dominance=8.0):
+    """A random diagonally dominant level and its Galerkin levels down to one
+    cell, each as (plane_levels, u3, l3) with Galerkin plane hierarchies."""
+    r = np.random.default_rng(seed)
+    blocks, _ = plane_case(n3, n2, n1, seed, dominance)
+    u3 = r.uniform(-1, 1, (n3 - 1, n2, n1, 4))
+    l3 = r.uniform(-1, 1, (n3 - 1, n2, n1, 4))
+    b = r.standard_normal((n3, n2, n1, 2))
+    b7 = list(blocks) + [u3, l3]
+    levels = []
+    while True:
+        levels.append((plane_levels_of(b7[:5], tr), b7[5], b7[6]))
+        if b7[0].shape[:3] == (1, 1, 1):
+            return levels, b
+        b7 = galerkin_coarse_3d(b7, tr)
+
+
+def compose_gauss_seidel_3d(level, b, x, iters, gi2, mi2, tr):
+    """GaussSeidel_3D (MULTI/TriDiagTB_Mod.f90:818-874) statement by
+    statement, each plane solved by the oracle's Solve_2D."""
+    planes, u3, l3 = level
+    n3 = planes[0][0].shape[0]
+    x = x.copy()
+
+    def solve(k, t):
+        lv = [tuple(a[k:k + 1] for a in p) for p in planes]
+        x[k] = oracle.tri_tb_multigrid_2d(lv, t[None], x[k:k + 1], gi2, mi2, tr)[0]
+
+    if n3 == 1:
+        solve(0, b[0])
+        return x
+    for _ in range(iters):
+        t = b[0].copy()
+        for k in range(n3 - 1):
+            t = couple_sub_np(t, u3[k], x[k + 1], tr)
+            solve(k, t)
+            t = couple_sub_np(b[k + 1], l3[k], x[k], tr)
+        solve(n3 - 1, t)
+        t = couple_sub_np(b[n3 - 2], u3[n3 - 2], x[n3 - 1], tr)
+        for k in range(n3 - 2, 0, -1):
+            t = couple_sub_np(t, l3[k - 1], x[k - 1], tr)
+            solve(k, t)
+            t = couple_sub_np(b[k - 1], u3[k - 1], x[k], tr)
+    solve(0, t)
+    t = couple_sub_np(b[n3 - 1], l3[n3 - 2], x[n3 - 2], tr)
+    solve(n3 - 1, t)
+    return x
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("n3,n2,n1,iters", [(1, 3, 4, 1), (2, 2, 3, 1), (4, 3, 5, 2), (3, 1, 1, 3)])
+def test_oracle_gauss_seidel_3d_composes(built_oracle, variant, n3, n2, n1, iters):
+    """GaussSeidel_3D in the oracle (MULTI/TriDiagTB_Mod.f90:818-874,
+    TriDiagTR_Mod.f90:902-961) equals its statement-by-statement composition
+    from the pinned Solve_2D bit for bit: the forward and backward plane
+    sweeps, then plane 1 and plane n3 once more."""
+    tr = variant == "TR"
+    levels, b = level_hierarchy_3d(n3, n2, n1, seed=n3 * 13 + n2 + n1, tr=tr)
+    x0 = np.random.default_rng(2).standard_normal(b.shape)
+    got = oracle.tri_tb_gauss_seidel_3d(levels[0], b, x0, iters, 1, 2, tr)
+    assert np.array_equal(got, compose_gauss_seidel_3d(levels[0], b, x0, iters, 1, 2, tr))
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+def test_oracle_gauss_seidel_3d_converges(built_oracle, variant):
+    """Plane sweeps with near-exact plane solves reach the dense solution of
+    a diagonally dominant level."""
+    tr = variant == "TR"
+    levels, b = level_hierarchy_3d(4, 4, 5, seed=5, tr=tr)
+    planes, u3, l3 = levels[0]
+    ref = np.linalg.solve(dense_level(tuple(planes[0]) + (u3, l3), tr), b.reshape(-1)).reshape(b.shape)
+    x = oracle.tri_tb_gauss_seidel_3d(levels[0], b, np.zeros_like(b), 30, 1, 30, tr)
+    assert np.max(np.abs(x - ref)) <= 1e-11 * np.max(np.abs(ref))
+
+
+def compose_multigrid_3d(levels, b, x, gi2, mi2, gi3, mi3, tr):
+    """Multigrid_3D (MULTI/TriDiagTB_Mod.f90:876-938) from the oracle's pinned
+    smoother, level product and transfers."""
+    nlev = len(levels)
+    x = x.copy()
+    for _ in range(mi3):
+        bl, xl = [b] + [None] * (nlev - 1), [x] + [None] * (nlev - 1)
+        gi, L = 1, 0
+        while True:
+            xl[L] = oracle.tri_tb_gauss_seidel_3d(levels[L], bl[L], xl[L], gi, gi2, mi2, tr)
+            gi += gi3
+            if L + 1 == nlev:
+                gi -= gi3
+                break
+            planes, u3, l3 = levels[L]
+            ax = oracle.tri_tb_matvec_3d(tuple(planes[0]) + (u3, l3), xl[L], tr)
+            bl[L + 1] = oracle.tri_tb_restrict_3d(bl[L] - ax)
+            xl[L + 1] = np.zeros_like(bl[L + 1])
+            L += 1
+        while True:
+            xl[L] = oracle.tri_tb_gauss_seidel_3d(levels[L], bl[L], xl[L], gi, gi2, mi2, tr)
+            gi -= gi3
+            if L == 0:
+                break
+            L -= 1
+            xl[L] = xl[L] + oracle.tri_tb_prolong_3d(xl[L + 1], *xl[L].shape[:3])
+        x = xl[0]
+    return x
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("n3,n2,n1,gi3,cycles", [(4, 4, 4, 1, 2), (3, 5, 2, 2, 1), (1, 1, 1, 1, 2), (5, 1, 3, 0, 2)])
+def test_oracle_multigrid_3d_composes(built_oracle, variant, n3, n2, n1, gi3, cycles):
+    """Solve_3D / Multigrid_3D (MULTI/TriDiagTB_Mod.f90:876-952,
+    TriDiagTR_Mod.f90:963-1041) in the oracle equal their composition from
+    the pinned pieces bit for bit."""
+    tr = variant == "TR"
+    levels, b = level_hierarchy_3d(n3, n2, n1, seed=n3 + 5 * n2 + 11 * n1, tr=tr)
+    x0 = np.random.default_rng(4).standard_normal(b.shape)
+    got = oracle.tri_tb_multigrid_3d(levels, b, x0, 1, 1, gi3, cycles, tr)
+    assert np.array_equal(got, compose_multigrid_3d(levels, b, x0, 1, 1, gi3, cycles, tr))
+    assert np.array_equal(oracle.tri_tb_multigrid_3d(levels, b, x0, 1, 1, gi3, 0, tr), x0)
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+def test_oracle_multigrid_3d_converges(built_oracle, variant):
+    """V-cycles over a Galerkin hierarchy of a weakly dominant 8x8x8 level
+    reach the dense solution, the error falling every cycle."""
+    tr = variant == "TR"
+    levels, b = level_hierarchy_3d(8, 8, 8, seed=9, tr=tr, dominance=4.0)
+    planes, u3, l3 = levels[0]
+    ref = np.linalg.solve(dense_level(tuple(planes[0]) + (u3, l3), tr), b.reshape(-1)).reshape(b.shape)
+    x = np.zeros_like(b)
+    errs = []
+    for _ in range(8):
+        x = oracle.tri_tb_multigrid_3d(levels, b, x, 1, 1, 1, 1, tr)
+        errs.append(np.max(np.abs(x - ref)) / np.max(np.abs(ref)))
+    assert errs[-1] <= 1e-9, errs
+    assert all(e1 < e0 for e0, e1 in zip(errs, errs[1:]) if e0 > 1e-14), errs
