@@ -804,6 +804,78 @@ def SolveTB_3D(levels, b, x0, gauss_iter2: int = 1, mult_iter2: int = 1, gauss_i
     return x
 
 
+class TriTBHierarchy:
+    """The TriDiagTB (TriDiagTR with dur) preconditioner resident on the
+    device: LaplTBCompute / LaplTRCompute (MULTI/JacAccGrav_Mod.f90:1312-1667)
+    of ref_level levels from the finest fields -- z_faces (F1, F1G, DTU1,
+    DUU1) (n3, n2, n1+1), x_faces (n3, n2+1, n1), y_faces (n3+1, n2, n1),
+    vol, dut, dur (n3, n2, n1) in the reversed index order -- and its
+    V-cycles (VCycleCG, :4502-4515)."""
+
+    def __init__(self, z_faces, x_faces, y_faces, vol, dut, dur=None, ref_level: int = 1, **coefs):
+        self.lib = _lib.load()
+        fs = [_f64(a) for a in list(z_faces) + list(x_faces) + list(y_faces)]
+        cells = [_f64(a) for a in (vol, dut) + ((dur,) if dur is not None else ())]
+        n3, n2, n1 = cells[0].shape
+        if (any(a.shape != (n3, n2, n1 + 1) for a in fs[:4]) or any(a.shape != (n3, n2 + 1, n1) for a in fs[4:8])
+                or any(a.shape != (n3 + 1, n2, n1) for a in fs[8:]) or any(a.shape != (n3, n2, n1) for a in cells)):
+            raise ValueError("z (n3,n2,n1+1), x (n3,n2+1,n1), y faces (n3+1,n2,n1), cells (n3,n2,n1)")
+        self.tr = dur is not None
+        self.ref_level = int(ref_level)
+        self.shape = (n3, n2, n1)
+        co = _lib.AsamTriTbCoefs(**{k: float(v) for k, v in coefs.items()})
+        h = C.c_void_p()
+        check(self.lib.asam_tri_tb_hier_create(int(self.tr), self.ref_level, n3, n2, n1, C.byref(co),
+                                               (C.c_void_p * 12)(*[a.ctypes.data for a in fs]), ptr(cells[0]),
+                                               ptr(cells[1]), ptr(cells[2]) if self.tr else None, C.byref(h)),
+              "asam_tri_tb_hier_create")
+        self.h = h
+
+    def level(self, level3: int, level2: int):
+        """(d, u1, l1, u2, l2) of plane level level2 of level level3, with u3,
+        l3 appended when level2 == level3."""
+        n3 = -(-self.shape[0] // 2 ** level3)
+        n2, n1 = (-(-n // 2 ** level2) for n in self.shape[1:])
+        shapes = [(n3, n2, n1, 4), (n3, n2, n1 - 1, 4), (n3, n2, n1 - 1, 4), (n3, n2 - 1, n1, 4), (n3, n2 - 1, n1, 4)]
+        if level2 == level3:
+            shapes += [(n3 - 1, n2, n1, 4)] * 2
+        out = []
+        for w, shp in enumerate(shapes):
+            a = np.empty(shp)
+            check(self.lib.asam_tri_tb_hier_get(self.h, int(level3), int(level2), w, ptr(a) if a.size else
+                                                C.cast(C.pointer(C.c_double(0.0)), C.c_void_p)),
+                  "asam_tri_tb_hier_get")
+            out.append(a)
+        return tuple(out)
+
+    def vcycle(self, b, x0=None, gauss_iter2: int = 1, mult_iter2: int = 1, gauss_iter3: int = 1,
+               mult_iter3: int = 1) -> np.ndarray:
+        bb = _f64(b)
+        x = np.zeros_like(bb) if x0 is None else _f64(x0).copy()
+        if bb.shape != self.shape + (2,) or x.shape != bb.shape:
+            raise ValueError(f"b, x0 of shape {self.shape + (2,)}")
+        check(self.lib.asam_tri_tb_hier_vcycle(self.h, ptr(bb), ptr(x), int(gauss_iter2), int(mult_iter2),
+                                               int(gauss_iter3), int(mult_iter3)), "asam_tri_tb_hier_vcycle")
+        return x
+
+    def close(self):
+        if self.h:
+            self.lib.asam_tri_tb_hier_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def MatVecTB_1D(d: np.ndarray, u: np.ndarray, l: np.ndarray, x: np.ndarray) -> np.ndarray:
     lib = _lib.load()
     d, u, l, xx = _f64(d), _f64(u), _f64(l), _f64(x)

@@ -11,6 +11,8 @@
 //   b, x, y[(col*n1 + i)*2 + r]        = b(r+1,i+1)
 // One thread per column; the elimination factors w go to a scratch array
 // laid out level-major ([i][e][col]) so that a warp's stores are coalesced.
+#include <memory>
+
 #include "context.h"
 
 namespace {
@@ -657,6 +659,96 @@ __global__ void k_tri_tb_couple_sub(int tr, int n, const double* t, const double
   st_v(o + (size_t)e * 2, couple_sub(tr, ld_v(t + (size_t)e * 2), c + (size_t)e * 4, ld_v(x + (size_t)e * 2)));
 }
 
+// The finest fields of LaplTBCompute / LaplTRCompute (MULTI/JacAccGrav_Mod.f90:
+// 1312-1667) and one coarsening of them: faces f[4a + q] of direction a
+// (q: F, FG, DTU, DUU; layouts of asam_tri_tb_compute_3d), cells vol, dut,
+// dur (dur null for TriDiagTB)
+struct TbFields {
+  const double* f[12];
+  const double *vol, *dut, *dur;
+};
+struct TbCoarse {
+  double* f[12];
+  double *vol, *dut, *dur;
+};
+
+__device__ __forceinline__ int tb_lo(int c, int s) { return (c - 1) * (s + 1) + 1; }
+__device__ __forceinline__ int tb_hi(int c, int s, int n) { return min(c * (s + 1), n); }
+
+// FaceCoarse of F and FG, CFaceCoarse of DTU (weighted by F) and DUU (by FG)
+// (JacAccGrav_Mod.f90:784-891), one thread per coarse face: the face
+// direction's fine face min((shift+1)*c, n), the other two directions'
+// cells summed with direction 1 slowest (the reference's loop order), then
+// the weighted sums divided by the coarse weight + Eps
+__global__ void k_tb_coarse_faces(int n3, int n2, int n1, TbFields g, int c3, int c2, int c1, TbCoarse c, int s12,
+                                  int s3) {
+  const size_t nz = (size_t)c3 * c2 * (c1 + 1), nx = (size_t)c3 * (c2 + 1) * c1, ny = (size_t)(c3 + 1) * c2 * c1;
+  const size_t e0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e0 >= nz + nx + ny) return;
+  int a, ic, jc, kc;
+  size_t e = e0;
+  if (e < nz) {
+    a = 0;
+    ic = (int)(e % (c1 + 1));
+    jc = (int)((e / (c1 + 1)) % c2) + 1;
+    kc = (int)(e / ((size_t)(c1 + 1) * c2)) + 1;
+  } else if ((e -= nz) < nx) {
+    a = 1;
+    ic = (int)(e % c1) + 1;
+    jc = (int)((e / c1) % (c2 + 1));
+    kc = (int)(e / ((size_t)c1 * (c2 + 1))) + 1;
+  } else {
+    e -= nx;
+    a = 2;
+    ic = (int)(e % c1) + 1;
+    jc = (int)((e / c1) % c2) + 1;
+    kc = (int)(e / ((size_t)c1 * c2));
+  }
+  const int e1 = a == 0, e2 = a == 1, e3 = a == 2;
+  const int ilo = e1 ? min((s12 + 1) * ic, n1) : tb_lo(ic, s12), ihi = e1 ? ilo : tb_hi(ic, s12, n1);
+  const int jlo = e2 ? min((s12 + 1) * jc, n2) : tb_lo(jc, s12), jhi = e2 ? jlo : tb_hi(jc, s12, n2);
+  const int klo = e3 ? min((s3 + 1) * kc, n3) : tb_lo(kc, s3), khi = e3 ? klo : tb_hi(kc, s3, n3);
+  const double *F = g.f[4 * a], *FG = g.f[4 * a + 1], *DT = g.f[4 * a + 2], *DU = g.f[4 * a + 3];
+  double f = 0.0, fg = 0.0, tf = 0.0, ug = 0.0;
+  for (int i = ilo; i <= ihi; ++i)
+    for (int j = jlo; j <= jhi; ++j)
+      for (int k = klo; k <= khi; ++k) {
+        const size_t q = ((size_t)(e3 ? k : k - 1) * (n2 + e2) + (e2 ? j : j - 1)) * (n1 + e1) + (e1 ? i : i - 1);
+        const double fq = F[q], gq = FG[q];
+        f = __dadd_rn(f, fq);
+        fg = __dadd_rn(fg, gq);
+        tf = __dadd_rn(tf, __dmul_rn(DT[q], fq));
+        ug = __dadd_rn(ug, __dmul_rn(DU[q], gq));
+      }
+  const size_t qc = ((size_t)(e3 ? kc : kc - 1) * (c2 + e2) + (e2 ? jc : jc - 1)) * (c1 + e1) + (e1 ? ic : ic - 1);
+  c.f[4 * a][qc] = f;
+  c.f[4 * a + 1][qc] = fg;
+  c.f[4 * a + 2][qc] = __ddiv_rn(tf, __dadd_rn(f, asam::kEps));
+  c.f[4 * a + 3][qc] = __ddiv_rn(ug, __dadd_rn(fg, asam::kEps));
+}
+
+// VolCoarse of Vol, CVolCoarse of DUT and DUR weighted by Vol
+// (JacAccGrav_Mod.f90:685-782), one thread per coarse cell
+__global__ void k_tb_coarse_cells(int n3, int n2, int n1, TbFields g, int c3, int c2, int c1, TbCoarse c, int s12,
+                                  int s3) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)c3 * c2 * c1) return;
+  const int ic = (int)(e % c1) + 1, jc = (int)((e / c1) % c2) + 1, kc = (int)(e / ((size_t)c1 * c2)) + 1;
+  double v = 0.0, tv = 0.0, rv = 0.0;
+  for (int i = tb_lo(ic, s12); i <= tb_hi(ic, s12, n1); ++i)
+    for (int j = tb_lo(jc, s12); j <= tb_hi(jc, s12, n2); ++j)
+      for (int k = tb_lo(kc, s3); k <= tb_hi(kc, s3, n3); ++k) {
+        const size_t q = ((size_t)(k - 1) * n2 + (j - 1)) * n1 + (i - 1);
+        const double vq = g.vol[q];
+        v = __dadd_rn(v, vq);
+        tv = __dadd_rn(tv, __dmul_rn(g.dut[q], vq));
+        if (g.dur) rv = __dadd_rn(rv, __dmul_rn(g.dur[q], vq));
+      }
+  c.vol[e] = v;
+  c.dut[e] = __ddiv_rn(tv, __dadd_rn(v, asam::kEps));
+  c.dur[e] = __ddiv_rn(rv, __dadd_rn(v, asam::kEps));
+}
+
 struct DevBufs {
   double* p[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   ~DevBufs() {
@@ -708,8 +800,9 @@ bool plane_levels_ok(int nlev, const int* n2s, const int* n1s, const double* con
   return true;
 }
 
-// copy a level's five block arrays (host or device) into cur and carve its
-// b, x and residual after them; cur advances past all of it
+// copy a level's five block arrays (host or device; src null: carve only)
+// into cur and carve its b, x and residual after them; cur advances past all
+// of it
 cudaError_t stage_plane_level(PlaneLevel& L, int nplane, int n2, int n1, const double* const src[5], double*& cur) {
   L.n2 = n2;
   L.n1 = n1;
@@ -718,7 +811,7 @@ cudaError_t stage_plane_level(PlaneLevel& L, int nplane, int n2, int n1, const d
                          (size_t)nplane * (n2 - 1) * n1 * 4};
   for (int q = 0; q < 5; ++q) {
     L.a[q] = cur;
-    if (len[q]) {
+    if (len[q] && src) {
       cudaError_t e = cudaMemcpy(cur, src[q], len[q] * sizeof(double), cudaMemcpyDefault);
       if (e != cudaSuccess) return e;
     }
@@ -834,7 +927,65 @@ cudaError_t level_gs(int variant, int n3, const PlaneLevel* pl, int nlev2, const
   return cudaGetLastError();
 }
 
+// Solve_3D: mult_iter3 V-cycles of Multigrid_3D (MULTI/TriDiagTB_Mod.f90:876-952)
+// over levels pl[L] (plane hierarchies of all planes, pl[L][0] the level's b,
+// x, residual) with couplings du3[L], dl3[L], from pl[0][0].b and the guess
+// pl[0][0].x
+cudaError_t level_cycles(int variant, int nlev3, const int* n3s, const int* n2s, const int* n1s, const int* nlev2s,
+                         PlaneLevel (*pl)[32], double* const* du3, double* const* dl3, double* t, const Scratch& sc,
+                         int gauss_iter2, int mult_iter2, int gauss_iter3, int mult_iter3, long& launches) {
+  auto grid = [&](int L) { return (unsigned)(((size_t)n3s[L] * n2s[L] * n1s[L] + 255) / 256); };
+  cudaError_t e;
+  for (int it = 0; it < mult_iter3; ++it) {
+    int gi = 1, L = 0;
+    for (;;) {  // the way down (:891-914)
+      e = level_gs(variant, n3s[L], pl[L], nlev2s[L], du3[L], dl3[L], t, sc, gi, gauss_iter2, mult_iter2, launches);
+      if (e != cudaSuccess) return e;
+      gi += gauss_iter3;
+      if (L + 1 == nlev3) {
+        gi -= gauss_iter3;
+        break;
+      }
+      const PlaneLevel& F = pl[L][0];
+      k_tri_tb_residual<<<grid(L), 256>>>(variant, n3s[L], n2s[L], n1s[L], F.a[0], F.a[1], F.a[2], F.a[3], F.a[4],
+                                          du3[L], dl3[L], F.b, F.x, F.res);
+      k_tri_tb_restrict_3d<<<grid(L + 1), 256>>>(n3s[L], n2s[L], n1s[L], F.res, pl[L + 1][0].b);
+      e = cudaMemsetAsync(pl[L + 1][0].x, 0, plane_vec_len(n3s[L + 1], n2s[L + 1], n1s[L + 1]) * sizeof(double));
+      if (e != cudaSuccess) return e;
+      launches += 2;
+      ++L;
+    }
+    for (;;) {  // and up (:915-937)
+      e = level_gs(variant, n3s[L], pl[L], nlev2s[L], du3[L], dl3[L], t, sc, gi, gauss_iter2, mult_iter2, launches);
+      if (e != cudaSuccess) return e;
+      gi -= gauss_iter3;
+      if (L == 0) break;
+      --L;
+      k_tri_tb_prolong_add<<<grid(L), 256>>>(1, n3s[L], n2s[L], n1s[L], pl[L + 1][0].x, pl[L][0].x);
+      ++launches;
+    }
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+// The device-resident hierarchy of LaplTBCompute / LaplTRCompute: per level its
+// plane hierarchy (all planes; plane level 0 carries the level's b, x and
+// residual) and its couplings between planes, one allocation.
+struct asam_tri_tb_hier {
+  int variant = 0, nlev3 = 0;
+  int n3s[32] = {}, n2s[32] = {}, n1s[32] = {}, nlev2s[32] = {};
+  PlaneLevel pl[32][32];
+  double* du3[32] = {};
+  double* dl3[32] = {};
+  double* mem = nullptr;
+  double* t = nullptr;
+  Scratch sc{nullptr, nullptr};
+  ~asam_tri_tb_hier() {
+    if (mem) cudaFree(mem);
+  }
+};
 
 extern "C" {
 
@@ -1128,38 +1279,154 @@ int asam_tri_tb_multigrid_3d(int variant, int nlev3, const int* n3s, const int* 
   TCU(cudaMemcpy(pl[0][0].b, b, nv0 * sizeof(double), cudaMemcpyDefault));
   TCU(cudaMemcpy(pl[0][0].x, x, nv0 * sizeof(double), cudaMemcpyDefault));
   long launches = 0;
-  auto grid = [&](int L) { return (unsigned)(((size_t)n3s[L] * n2s[L] * n1s[L] + 255) / 256); };
-  for (int it = 0; it < mult_iter3; ++it) {
-    int gi = 1, L = 0;
-    for (;;) {  // Multigrid_3D's way down (MULTI/TriDiagTB_Mod.f90:891-914)
-      TCU(level_gs(variant, n3s[L], pl[L], nlev2s[L], du3[L], dl3[L], t, sc, gi, gauss_iter2, mult_iter2, launches));
-      gi += gauss_iter3;
-      if (L + 1 == nlev3) {
-        gi -= gauss_iter3;
-        break;
-      }
-      const PlaneLevel& F = pl[L][0];
-      k_tri_tb_residual<<<grid(L), 256>>>(variant, n3s[L], n2s[L], n1s[L], F.a[0], F.a[1], F.a[2], F.a[3], F.a[4],
-                                          du3[L], dl3[L], F.b, F.x, F.res);
-      k_tri_tb_restrict_3d<<<grid(L + 1), 256>>>(n3s[L], n2s[L], n1s[L], F.res, pl[L + 1][0].b);
-      TCU(cudaMemsetAsync(pl[L + 1][0].x, 0, plane_vec_len(n3s[L + 1], n2s[L + 1], n1s[L + 1]) * sizeof(double)));
-      launches += 2;
-      ++L;
-    }
-    for (;;) {  // and up (:915-937)
-      TCU(level_gs(variant, n3s[L], pl[L], nlev2s[L], du3[L], dl3[L], t, sc, gi, gauss_iter2, mult_iter2, launches));
-      gi -= gauss_iter3;
-      if (L == 0) break;
-      --L;
-      k_tri_tb_prolong_add<<<grid(L), 256>>>(1, n3s[L], n2s[L], n1s[L], pl[L + 1][0].x, pl[L][0].x);
-      ++launches;
-    }
-    TCU(cudaGetLastError());
-  }
+  TCU(level_cycles(variant, nlev3, n3s, n2s, n1s, nlev2s, pl, du3, dl3, t, sc, gauss_iter2, mult_iter2, gauss_iter3,
+                   mult_iter3, launches));
   asam::count_launches(launches);
   TCU(cudaMemcpy(x, pl[0][0].x, nv0 * sizeof(double), cudaMemcpyDefault));
   return ASAM_OK;
 }
+
+int asam_tri_tb_hier_create(int variant, int ref_level, int n3, int n2, int n1, const asam_tri_tb_coefs* coefs,
+                            const double* const* faces, const double* vol, const double* dut, const double* dur,
+                            asam_tri_tb_hier** out) {
+  bool ok = (variant == 0 || variant == 1) && ref_level >= 1 && ref_level <= 32 && n3 >= 1 && n2 >= 1 && n1 >= 1 &&
+            coefs && faces && vol && dut && (variant == 0 || dur) && out;
+  for (int q = 0; ok && q < 12; ++q) ok = faces[q] != nullptr;
+  if (!ok) {
+    asam::set_last_error("asam_tri_tb_hier_create: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  *out = nullptr;
+  std::unique_ptr<asam_tri_tb_hier> h(new asam_tri_tb_hier);
+  h->variant = variant;
+  h->nlev3 = ref_level;
+  // level L3: n3 halved L3 times (rounding up); its plane level m: n2, n1
+  // halved L3 + m times (LaplTBCompute's (n + Shift)/(Shift + 1))
+  auto cdiv = [](int n, int L) { return (int)(((long long)n + (1LL << L) - 1) >> L); };
+  size_t tot = 0;
+  for (int L = 0; L < ref_level; ++L) {
+    h->n3s[L] = cdiv(n3, L);
+    h->n2s[L] = cdiv(n2, L);
+    h->n1s[L] = cdiv(n1, L);
+    h->nlev2s[L] = ref_level - L;
+    for (int m = 0; m < h->nlev2s[L]; ++m)
+      tot += plane_block_len(h->n3s[L], cdiv(n2, L + m), cdiv(n1, L + m)) +
+             3 * plane_vec_len(h->n3s[L], cdiv(n2, L + m), cdiv(n1, L + m));
+    tot += 2 * (size_t)(h->n3s[L] - 1) * h->n2s[L] * h->n1s[L] * 4;
+  }
+  const size_t npl = (size_t)n2 * n1, nc = (size_t)n3 * npl;
+  const size_t nz = (size_t)n3 * n2 * (n1 + 1), nx = (size_t)n3 * (n2 + 1) * n1, ny = (size_t)(n3 + 1) * npl;
+  const size_t nt = (size_t)n1 * 2, nw = (size_t)(n1 > 1 ? n1 - 1 : 1) * 4;
+  const size_t fields = 4 * (nz + nx + ny) + 3 * nc;  // the finest fields, and room for one coarsening of them
+  TCU(cudaMalloc((void**)&h->mem, (tot + npl * 2 + nt + nw) * sizeof(double)));
+  DevBufs work;
+  TCU(cudaMalloc((void**)&work.p[0], 2 * fields * sizeof(double)));
+  double* cur = h->mem;
+  for (int L = 0; L < ref_level; ++L) {
+    for (int m = 0; m < h->nlev2s[L]; ++m)
+      TCU(stage_plane_level(h->pl[L][m], h->n3s[L], cdiv(n2, L + m), cdiv(n1, L + m), nullptr, cur));
+    const size_t ncp = (size_t)(h->n3s[L] - 1) * h->n2s[L] * h->n1s[L] * 4;
+    h->du3[L] = ncp ? cur : nullptr;
+    h->dl3[L] = ncp ? cur + ncp : nullptr;
+    cur += 2 * ncp;
+  }
+  h->t = cur;
+  h->sc = Scratch{cur + npl * 2, cur + npl * 2 + nt};
+  // the finest fields on the device
+  TbFields g;
+  double* fp = work.p[0];
+  const size_t flen[3] = {nz, nx, ny};
+  for (int q = 0; q < 12; ++q) {
+    TCU(cudaMemcpy(fp, faces[q], flen[q / 4] * sizeof(double), cudaMemcpyDefault));
+    g.f[q] = fp;
+    fp += flen[q / 4];
+  }
+  const double* cells[3] = {vol, dut, variant == 1 ? dur : nullptr};
+  const double* gc[3];
+  for (int q = 0; q < 3; ++q) {
+    if (cells[q]) TCU(cudaMemcpy(fp, cells[q], nc * sizeof(double), cudaMemcpyDefault));
+    gc[q] = cells[q] ? fp : nullptr;
+    fp += nc;
+  }
+  g.vol = gc[0];
+  g.dut = gc[1];
+  g.dur = gc[2];
+  long launches = 0;
+  for (int L3 = 0; L3 < ref_level; ++L3)
+    for (int L2 = L3; L2 < ref_level; ++L2) {
+      const int s12 = (1 << L2) - 1, s3 = (1 << L3) - 1;
+      const int c3 = cdiv(n3, L3), c2 = cdiv(n2, L2), c1 = cdiv(n1, L2);
+      const size_t cz = (size_t)c3 * c2 * (c1 + 1), cx = (size_t)c3 * (c2 + 1) * c1, cy = (size_t)(c3 + 1) * c2 * c1;
+      const size_t ccl = (size_t)c3 * c2 * c1;
+      TbCoarse c;
+      double* cp = work.p[0] + fields;
+      const size_t clen[3] = {cz, cx, cy};
+      for (int q = 0; q < 12; ++q) {
+        c.f[q] = cp;
+        cp += clen[q / 4];
+      }
+      c.vol = cp;
+      c.dut = cp + ccl;
+      c.dur = cp + 2 * ccl;
+      k_tb_coarse_faces<<<(unsigned)((cz + cx + cy + 255) / 256), 256>>>(n3, n2, n1, g, c3, c2, c1, c, s12, s3);
+      k_tb_coarse_cells<<<(unsigned)((ccl + 255) / 256), 256>>>(n3, n2, n1, g, c3, c2, c1, c, s12, s3);
+      PlaneLevel& P = h->pl[L3][L2 - L3];
+      const Plane2D P2{c.f[0], c.f[1], c.f[2], c.f[3], c.f[4], c.f[5], c.f[6], c.f[7], c.vol, c.dut, c.dur,
+                       const_cast<double*>(P.a[1]), const_cast<double*>(P.a[2]), const_cast<double*>(P.a[3]),
+                       const_cast<double*>(P.a[4])};
+      const bool couple = L2 == L3;
+      k_tri_tb_compute_3d<<<(unsigned)((ccl + 255) / 256), 256>>>(variant, couple ? 1 : 0, c3, c2, c1, *coefs, P2,
+                                                                   c.f[8], c.f[9], c.f[10], c.f[11],
+                                                                   const_cast<double*>(P.a[0]),
+                                                                   couple ? h->du3[L3] : nullptr,
+                                                                   couple ? h->dl3[L3] : nullptr);
+      launches += 3;
+      TCU(cudaGetLastError());
+    }
+  TCU(cudaDeviceSynchronize());
+  asam::count_launches(launches);
+  *out = h.release();
+  return ASAM_OK;
+}
+
+int asam_tri_tb_hier_get(const asam_tri_tb_hier* h, int level3, int level2, int which, double* dst) {
+  if (!h || level3 < 0 || level3 >= h->nlev3 || level2 < level3 || level2 - level3 >= h->nlev2s[level3] || which < 0 ||
+      which > 6 || !dst) {
+    asam::set_last_error("asam_tri_tb_hier_get: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  const PlaneLevel& P = h->pl[level3][level2 - level3];
+  const size_t n3 = h->n3s[level3], n2 = P.n2, n1 = P.n1;
+  const size_t len[7] = {n3 * n2 * n1 * 4,      n3 * n2 * (n1 - 1) * 4, n3 * n2 * (n1 - 1) * 4, n3 * (n2 - 1) * n1 * 4,
+                         n3 * (n2 - 1) * n1 * 4, (n3 - 1) * n2 * n1 * 4, (n3 - 1) * n2 * n1 * 4};
+  const double* src = which < 5 ? P.a[which] : (level2 == level3 ? (which == 5 ? h->du3[level3] : h->dl3[level3]) : nullptr);
+  if (which >= 5 && level2 != level3) {
+    asam::set_last_error("asam_tri_tb_hier_get: couplings between planes exist on a level's own planes only", __FILE__,
+                         __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  if (len[which]) TCU(cudaMemcpy(dst, src, len[which] * sizeof(double), cudaMemcpyDefault));
+  return ASAM_OK;
+}
+
+int asam_tri_tb_hier_vcycle(asam_tri_tb_hier* h, const double* b, double* x, int gauss_iter2, int mult_iter2,
+                            int gauss_iter3, int mult_iter3) {
+  if (!h || !b || !x || gauss_iter2 < 0 || mult_iter2 < 0 || gauss_iter3 < 0 || mult_iter3 < 0) {
+    asam::set_last_error("asam_tri_tb_hier_vcycle: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  const size_t nv0 = plane_vec_len(h->n3s[0], h->n2s[0], h->n1s[0]);
+  TCU(cudaMemcpy(h->pl[0][0].b, b, nv0 * sizeof(double), cudaMemcpyDefault));
+  TCU(cudaMemcpy(h->pl[0][0].x, x, nv0 * sizeof(double), cudaMemcpyDefault));
+  long launches = 0;
+  TCU(level_cycles(h->variant, h->nlev3, h->n3s, h->n2s, h->n1s, h->nlev2s, h->pl, h->du3, h->dl3, h->t, h->sc,
+                   gauss_iter2, mult_iter2, gauss_iter3, mult_iter3, launches));
+  asam::count_launches(launches);
+  TCU(cudaMemcpy(x, h->pl[0][0].x, nv0 * sizeof(double), cudaMemcpyDefault));
+  return ASAM_OK;
+}
+
+void asam_tri_tb_hier_destroy(asam_tri_tb_hier* h) { delete h; }
 
 int asam_tri_tb_restrict_2d(int nplane, int n2, int n1, const double* res, double* resc) {
   if (nplane < 1 || n2 < 1 || n1 < 1 || !res || !resc) {

@@ -685,6 +685,35 @@ int asam_tri_tb_multigrid_3d(int variant, int nlev3, const int *n3s, const int *
                              const double *const *l2, const double *b, double *x, int gauss_iter2, int mult_iter2,
                              int gauss_iter3, int mult_iter3);
 
+/* The TriDiagTB / TriDiagTR preconditioner of the projection, resident on the
+ * device: LaplTBCompute (variant 0) or LaplTRCompute (variant 1,
+ * MULTI/JacAccGrav_Mod.f90:1312-1667) builds ref_level levels (RefLevel),
+ * level L3 of ceil(n3/2^L3) planes with the plane levels L2 = L3 ..
+ * ref_level-1 of ceil(n2/2^L2) x ceil(n1/2^L2), every one from the finest
+ * fields coarsened by FaceCoarse, CFaceCoarse, VolCoarse and CVolCoarse
+ * (:685-891; shift 0 on level 0 too) and assembled by Compute_3D (with the
+ * couplings between planes on the level itself, without them on its plane
+ * levels).  Inputs in the reversed index order (n1 the column direction,
+ * as ReverseWeight / Reverse leave them): faces[0..3] = F1, F1G, DTU1, DUU1
+ * [(k*n2 + j)*(n1+1) + i], faces[4..7] = F2, F2G, DTU2, DUU2
+ * [(k*(n2+1) + j)*n1 + i], faces[8..11] = F3, F3G, DTU3, DUU3
+ * [(k*n2 + j)*n1 + i] (k to n3), vol = VolG, dut = DUTG, dur = DURG
+ * (variant 1 only) [(k*n2 + j)*n1 + i]; coefs as asam_tri_tb_compute_3d.
+ * ref_level <= 32. */
+typedef struct asam_tri_tb_hier asam_tri_tb_hier;
+int asam_tri_tb_hier_create(int variant, int ref_level, int n3, int n2, int n1, const asam_tri_tb_coefs *coefs,
+                            const double *const *faces, const double *vol, const double *dut, const double *dur,
+                            asam_tri_tb_hier **out);
+/* one assembled array of the hierarchy (tests): which 0..6 = d, u1, l1, u2,
+ * l2, u3, l3 of plane level level2 of level level3 (u3, l3 only for
+ * level2 == level3), in the layouts of asam_tri_tb_compute_3d */
+int asam_tri_tb_hier_get(const asam_tri_tb_hier *h, int level3, int level2, int which, double *dst);
+/* mult_iter3 V-cycles of Multigrid_3D over the hierarchy (asam_tri_tb_multigrid_3d);
+ * VCycleCG (JacAccGrav_Mod.f90:4502-4515) runs one from x = 0. */
+int asam_tri_tb_hier_vcycle(asam_tri_tb_hier *h, const double *b, double *x, int gauss_iter2, int mult_iter2,
+                            int gauss_iter3, int mult_iter3);
+void asam_tri_tb_hier_destroy(asam_tri_tb_hier *h);
+
 /* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141),
  * the same as MatVecTR_1D (MULTI/TriDiagTR_Mod.f90:133-153). */
 int asam_tri_tb_matvec(int ncol, int n1, const double *d, const double *u, const double *l, const double *x,

@@ -74,6 +74,7 @@ def load() -> C.CDLL:
             "ora_tri_tb_restrict_3d": (None, [I, I, I, V, V]),
             "ora_tri_tb_prolong_3d": (None, [I, I, I, V, V]),
             "ora_tri_tb_multigrid_3d": (None, [I, I, V, V, V, V] + [V] * 9 + [I, I, I, I]),
+            "ora_tri_tb_lapl_level": (None, [I, I, I, I, V, V, V, V, V, I, I] + [V] * 7),
             "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
         }
         sig.update({
@@ -616,6 +617,53 @@ def tri_tb_multigrid_3d(levels, b, x0, gauss_iter2=1, mult_iter2=1, gauss_iter3=
                                 _ptrs([l for _, _, l in lv]), *[_ptrs([k[j] for k in flat]) for j in range(5)], _p(bb),
                                 _p(x), int(gauss_iter2), int(mult_iter2), int(gauss_iter3), int(mult_iter3))
     return x
+
+
+def tri_tb_lapl_level(z_faces, x_faces, y_faces, vol, dut, dur, level3, level2, coefs):
+    """One level of LaplTBCompute (dur None; LaplTRCompute with dur,
+    MULTI/JacAccGrav_Mod.f90:1312-1667): the finest faces z (F1, F1G, DTU1,
+    DUU1) (n3, n2, n1+1), x (n3, n2+1, n1), y (n3+1, n2, n1) and cells
+    coarsened with the shifts 2^level2-1 (directions 1, 2) and 2^level3-1
+    (direction 3), then Compute_3D, with the couplings between planes when
+    level2 == level3.  Returns d, u1, l1, u2, l2, u3, l3 as tri_tb_compute_3d."""
+    lib = load()
+    fs = [np.ascontiguousarray(a, dtype=np.float64) for a in list(z_faces) + list(x_faces) + list(y_faces)]
+    vol, dut = (np.ascontiguousarray(a, dtype=np.float64) for a in (vol, dut))
+    tr = dur is not None
+    durr = np.ascontiguousarray(dur, dtype=np.float64) if tr else None
+    n3, n2, n1 = vol.shape
+    c3 = -(-n3 // 2 ** level3)
+    c2, c1 = -(-n2 // 2 ** level2), -(-n1 // 2 ** level2)
+    keys = ("beta0_dtp", "fac1_l", "fac1_r", "grav_comp", "fac_anela", "fac2_l", "fac2_r", "fac3_l", "fac3_r")
+    sv = np.array([float(coefs.get(k, 1.0 if k == "beta0_dtp" else 0.0)) for k in keys])
+    d = np.empty((c3, c2, c1, 4))
+    u1 = np.empty((c3, c2, max(c1 - 1, 1), 4))
+    l1 = np.empty_like(u1)
+    u2 = np.empty((c3, max(c2 - 1, 1), c1, 4))
+    l2 = np.empty_like(u2)
+    u3 = np.zeros((max(c3 - 1, 1), c2, c1, 4))
+    l3 = np.zeros_like(u3)
+    lib.ora_tri_tb_lapl_level(int(tr), n3, n2, n1, _p(sv), _ptrs(fs), _p(vol), _p(dut),
+                              _p(durr) if tr else None, int(level3), int(level2), _p(d), _p(u1), _p(l1), _p(u2),
+                              _p(l2), _p(u3), _p(l3))
+    return (d, u1[:, :, :c1 - 1], l1[:, :, :c1 - 1], u2[:, :c2 - 1], l2[:, :c2 - 1], u3[:c3 - 1], l3[:c3 - 1])
+
+
+def tri_tb_lapl_compute(z_faces, x_faces, y_faces, vol, dut, dur=None, ref_level=1, **coefs):
+    """LaplTBCompute / LaplTRCompute (MULTI/JacAccGrav_Mod.f90:1312-1667): the
+    hierarchy of ref_level levels, level L3 with the plane levels L2 = L3 ..
+    ref_level-1, each built from the finest fields (tri_tb_lapl_level), as
+    tri_tb_multigrid_3d takes it: [(plane_levels, u3, l3), ...]."""
+    levels = []
+    for L3 in range(ref_level):
+        planes, u3, l3 = [], None, None
+        for L2 in range(L3, ref_level):
+            blk = tri_tb_lapl_level(z_faces, x_faces, y_faces, vol, dut, dur, L3, L2, coefs)
+            planes.append(blk[:5])
+            if L2 == L3:
+                u3, l3 = blk[5], blk[6]
+        levels.append((planes, u3, l3))
+    return levels
 
 
 class OracleProj:

@@ -5,6 +5,10 @@
  * reference's per-column arrays back to back, 2x2 blocks column-major
  * (index r + 2c), vectors (index r) per level. */
 #include <stddef.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define EPS_TB 1.0e-30 /* CG/Kind_Mod_gf.f90 Eps */
 
 static void mult_2(const double *b, const double *c, double *o) {
   double t1 = b[0] * c[0] + b[2] * c[1];
@@ -806,4 +810,92 @@ void ora_tri_tb_multigrid_3d(int variant, int nlev3, const int *n3s, const int *
       free(xl[L]);
     }
   }
+}
+
+/* One level of LaplTBCompute / LaplTRCompute (MULTI/JacAccGrav_Mod.f90:1312-1482,
+ * 1485-1667): the finest fields coarsened with the shifts 2^level2-1 along
+ * directions 1 and 2 and 2^level3-1 along direction 3 (level2 >= level3) --
+ * FaceCoarse of F and FG, CFaceCoarse of DTU weighted by F and of DUU
+ * weighted by FG, VolCoarse of Vol, CVolCoarse of DUT and DUR weighted by Vol
+ * (:685-891; every coarse value sums its fine values with direction 1
+ * slowest, then direction 2, then 3, the weighted ones then divided by the
+ * coarse weight + Eps) -- and assembled by Compute_3D: with the couplings
+ * between planes (the level itself, level2 == level3) or without (the
+ * level2-level3'th plane level of its planes).  Face and cell layouts as
+ * ora_tri_tb_compute_3d; level 0 too is the coarsening with shift 0. */
+static size_t tb_blo(int c, int s) { return (size_t)(c - 1) * (s + 1) + 1; }
+static size_t tb_bhi(int c, int s, int n) { return (size_t)c * (s + 1) < (size_t)n ? (size_t)c * (s + 1) : (size_t)n; }
+
+void ora_tri_tb_lapl_level(int variant, int n3, int n2, int n1, const double *s, const double *const *faces,
+                           const double *vol, const double *dut, const double *dur, int level3, int level2, double *d,
+                           double *u1, double *l1, double *u2, double *l2, double *u3, double *l3) {
+  const int s3 = (1 << level3) - 1, s12 = (1 << level2) - 1;
+  const int c1 = (n1 + s12) / (s12 + 1), c2 = (n2 + s12) / (s12 + 1), c3 = (n3 + s3) / (s3 + 1);
+  const size_t cz = (size_t)c3 * c2 * (c1 + 1), cx = (size_t)c3 * (c2 + 1) * c1, cy = (size_t)(c3 + 1) * c2 * c1;
+  const size_t cc = (size_t)c3 * c2 * c1;
+  double *buf = (double *)malloc(sizeof(double) * (4 * (cz + cx + cy) + 3 * cc));
+  double *cf[12];
+  const size_t clen[3] = {cz, cx, cy};
+  double *p = buf;
+  for (int q = 0; q < 12; ++q) {
+    cf[q] = p;
+    p += clen[q / 4];
+  }
+  double *vc = p, *dutc = p + cc, *durc = p + 2 * cc;
+  /* faces: direction a's index on the coarse face fixed (the fine face at
+   * min((shift+1)*c, n)), the other two summed over their cells */
+  for (int a = 0; a < 3; ++a) {
+    const double *F = faces[4 * a], *FG = faces[4 * a + 1], *DT = faces[4 * a + 2], *DU = faces[4 * a + 3];
+    const int e1 = a == 0, e2 = a == 1, e3 = a == 2; /* the face direction has one more entry */
+    for (int kc = 1 - e3; kc <= c3; ++kc)
+      for (int jc = 1 - e2; jc <= c2; ++jc)
+        for (int ic = 1 - e1; ic <= c1; ++ic) {
+          size_t ilo, ihi, jlo, jhi, klo, khi;
+          if (e1) ilo = ihi = (size_t)(s12 + 1) * ic < (size_t)n1 ? (size_t)(s12 + 1) * ic : (size_t)n1;
+          else { ilo = tb_blo(ic, s12); ihi = tb_bhi(ic, s12, n1); }
+          if (e2) jlo = jhi = (size_t)(s12 + 1) * jc < (size_t)n2 ? (size_t)(s12 + 1) * jc : (size_t)n2;
+          else { jlo = tb_blo(jc, s12); jhi = tb_bhi(jc, s12, n2); }
+          if (e3) klo = khi = (size_t)(s3 + 1) * kc < (size_t)n3 ? (size_t)(s3 + 1) * kc : (size_t)n3;
+          else { klo = tb_blo(kc, s3); khi = tb_bhi(kc, s3, n3); }
+          double f = 0.0, fg = 0.0, tf = 0.0, ug = 0.0;
+          for (size_t i = ilo; i <= ihi; ++i)
+            for (size_t j = jlo; j <= jhi; ++j)
+              for (size_t k = klo; k <= khi; ++k) {
+                /* fine index: 0-based on the face direction, 1-based cells */
+                const size_t ii = e1 ? i : i - 1, jj = e2 ? j : j - 1, kk = e3 ? k : k - 1;
+                const size_t q = ((kk * (size_t)(n2 + e2) + jj) * (size_t)(n1 + e1)) + ii;
+                f = f + F[q];
+                fg = fg + FG[q];
+                tf = tf + DT[q] * F[q];
+                ug = ug + DU[q] * FG[q];
+              }
+          const size_t ici = e1 ? (size_t)ic : (size_t)ic - 1, jci = e2 ? (size_t)jc : (size_t)jc - 1,
+                       kci = e3 ? (size_t)kc : (size_t)kc - 1;
+          const size_t qc = ((kci * (size_t)(c2 + e2) + jci) * (size_t)(c1 + e1)) + ici;
+          cf[4 * a][qc] = f;
+          cf[4 * a + 1][qc] = fg;
+          cf[4 * a + 2][qc] = tf / (f + EPS_TB);
+          cf[4 * a + 3][qc] = ug / (fg + EPS_TB);
+        }
+  }
+  for (int kc = 1; kc <= c3; ++kc)
+    for (int jc = 1; jc <= c2; ++jc)
+      for (int ic = 1; ic <= c1; ++ic) {
+        double v = 0.0, tv = 0.0, rv = 0.0;
+        for (size_t i = tb_blo(ic, s12); i <= tb_bhi(ic, s12, n1); ++i)
+          for (size_t j = tb_blo(jc, s12); j <= tb_bhi(jc, s12, n2); ++j)
+            for (size_t k = tb_blo(kc, s3); k <= tb_bhi(kc, s3, n3); ++k) {
+              const size_t q = ((k - 1) * n2 + (j - 1)) * n1 + (i - 1);
+              v = v + vol[q];
+              tv = tv + dut[q] * vol[q];
+              if (dur) rv = rv + dur[q] * vol[q];
+            }
+        const size_t qc = ((size_t)(kc - 1) * c2 + (jc - 1)) * c1 + (ic - 1);
+        vc[qc] = v;
+        dutc[qc] = tv / (v + EPS_TB);
+        durc[qc] = rv / (v + EPS_TB);
+      }
+  ora_tri_tb_compute_3d(variant, level2 == level3, c3, c2, c1, s, cf[0], cf[1], cf[2], cf[3], cf[4], cf[5], cf[6],
+                        cf[7], cf[8], cf[9], cf[10], cf[11], vc, dutc, durc, d, u1, l1, u2, l2, u3, l3);
+  free(buf);
 }

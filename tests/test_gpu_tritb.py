@@ -228,3 +228,31 @@ def test_tri_tb_multigrid_3d_bad_args(built_lib):
         asam.SolveTB_3D([(planes[:1] + planes[:1], u3, l3)] + levels[1:], b, b)
     with pytest.raises(AsamError):
         asam.SolveTB_3D(levels, b, b, mult_iter3=-1)
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("n3,n2,n1,ref_level", [(5, 6, 7, 3), (8, 8, 8, 4), (3, 1, 9, 2), (16, 48, 40, 5)])
+def test_tri_tb_hierarchy_bitwise(built_lib, variant, n3, n2, n1, ref_level):
+    """LaplTBCompute / LaplTRCompute on the GPU (the coarsening of the finest
+    fields and Compute_3D of every level and plane level, resident on the
+    device) equal the oracle's arrays bit for bit, and a V-cycle over the
+    resident hierarchy from x = 0 (VCycleCG) equals the oracle's Solve_3D
+    over the oracle's hierarchy."""
+    from tests.test_tritb import LAPL_COEFS, compute_inputs_3d
+
+    tr = variant == "TR"
+    zf, xf, yf, vol, dut, dur, _ = compute_inputs_3d(n3, n2, n1, seed=n3 * n2 + n1)
+    dd = dur if tr else None
+    with asam.TriTBHierarchy(zf, xf, yf, vol, dut, dd, ref_level=ref_level, **LAPL_COEFS) as h:
+        for L3 in range(ref_level):
+            for L2 in range(L3, ref_level):
+                got = h.level(L3, L2)
+                ref = oracle.tri_tb_lapl_level(zf, xf, yf, vol, dut, dd, L3, L2, LAPL_COEFS)
+                for g, r in zip(got, ref[:len(got)]):
+                    assert np.array_equal(g, r), (L3, L2)
+        b = np.random.default_rng(n1).standard_normal((n3, n2, n1, 2))
+        levels = oracle.tri_tb_lapl_compute(zf, xf, yf, vol, dut, dd, ref_level=ref_level, **LAPL_COEFS)
+        assert np.array_equal(h.vcycle(b), oracle.tri_tb_multigrid_3d(levels, b, np.zeros_like(b), 1, 1, 1, 1, tr))
+        x0 = np.random.default_rng(2).standard_normal(b.shape)
+        assert np.array_equal(h.vcycle(b, x0, 2, 2, 1, 2),
+                              oracle.tri_tb_multigrid_3d(levels, b, x0, 2, 2, 1, 2, tr))

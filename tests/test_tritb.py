@@ -794,3 +794,88 @@ def test_oracle_multigrid_3d_converges(built_oracle, variant):
         errs.append(np.max(np.abs(x - ref)) / np.max(np.abs(ref)))
     assert errs[-1] <= 1e-9, errs
     assert all(e1 < e0 for e0, e1 in zip(errs, errs[1:]) if e0 > 1e-14), errs
+
+
+LAPL_COEFS = dict(beta0_dtp=0.5, fac1_l=1.0, fac1_r=1.0, grav_comp=1.0, fac_anela=0.25, fac2_l=1.0, fac2_r=1.0,
+                  fac3_l=1.0, fac3_r=1.0)
+
+
+def coarsen_loops(zf, xf, yf, vol, dut, dur, s1, s2, s3):
+    """FaceCoarse, CFaceCoarse, VolCoarse, CVolCoarse (MULTI/JacAccGrav_Mod.f90:
+    685-891) as the reference's loops over the fine cells, accumulating into
+    the coarse arrays (0-based; direction 1 = the arrays' last axis)."""
+    eps = 1.0e-30
+    n3, n2, n1 = vol.shape
+    c1, c2, c3 = (n1 + s1) // (s1 + 1), (n2 + s2) // (s2 + 1), (n3 + s3) // (s3 + 1)
+    cc = lambda i, s: (i + 1 + s) // (s + 1) - 1  # noqa: E731  (1-based (i+s)/(s+1), back to 0-based)
+    out = []
+    for a, (F, FG, DT, DU) in enumerate((zf, xf, yf)):
+        shape = [(c3, c2, c1 + 1), (c3, c2 + 1, c1), (c3 + 1, c2, c1)][a]
+        Fc, FGc, Tc, Uc = (np.zeros(shape) for _ in range(4))
+        if a == 0:
+            it = ((ic, min((s1 + 1) * ic, n1), j, k) for ic in range(c1 + 1) for j in range(n2) for k in range(n3))
+            for ic, i, j, k in it:
+                q, r = (k, j, i), (cc(k, s3), cc(j, s2), ic)
+                Fc[r] += F[q]; FGc[r] += FG[q]; Tc[r] += DT[q] * F[q]; Uc[r] += DU[q] * FG[q]  # noqa: E702
+        elif a == 1:
+            it = ((i, jc, min((s2 + 1) * jc, n2), k) for i in range(n1) for jc in range(c2 + 1) for k in range(n3))
+            for i, jc, j, k in it:
+                q, r = (k, j, i), (cc(k, s3), jc, cc(i, s1))
+                Fc[r] += F[q]; FGc[r] += FG[q]; Tc[r] += DT[q] * F[q]; Uc[r] += DU[q] * FG[q]  # noqa: E702
+        else:
+            it = ((i, j, kc, min((s3 + 1) * kc, n3)) for i in range(n1) for j in range(n2) for kc in range(c3 + 1))
+            for i, j, kc, k in it:
+                q, r = (k, j, i), (kc, cc(j, s2), cc(i, s1))
+                Fc[r] += F[q]; FGc[r] += FG[q]; Tc[r] += DT[q] * F[q]; Uc[r] += DU[q] * FG[q]  # noqa: E702
+        out.append((Fc, FGc, Tc / (Fc + eps), Uc / (FGc + eps)))
+    V, TV, RV = np.zeros((c3, c2, c1)), np.zeros((c3, c2, c1)), np.zeros((c3, c2, c1))
+    for i in range(n1):
+        for j in range(n2):
+            for k in range(n3):
+                r = (cc(k, s3), cc(j, s2), cc(i, s1))
+                V[r] += vol[k, j, i]
+                TV[r] += dut[k, j, i] * vol[k, j, i]
+                if dur is not None:
+                    RV[r] += dur[k, j, i] * vol[k, j, i]
+    return out[0], out[1], out[2], V, TV / (V + eps), (RV / (V + eps) if dur is not None else None)
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("n3,n2,n1,level3,level2", [(5, 6, 7, 0, 0), (5, 6, 7, 1, 1), (5, 6, 7, 1, 2), (4, 3, 9, 0, 2),
+                                                     (3, 3, 3, 2, 2)])
+def test_oracle_lapl_level_matches_reference_loops(built_oracle, variant, n3, n2, n1, level3, level2):
+    """A level of LaplTBCompute / LaplTRCompute (MULTI/JacAccGrav_Mod.f90:
+    1312-1667) is Compute_3D of the finest fields coarsened by the
+    reference's loops with shifts 2^level2-1, 2^level2-1, 2^level3-1 -- level
+    0 too (shift 0 turns DTU into DTU*F/(F+Eps)) -- bit for bit, with the
+    couplings between planes on the level itself and without them on its
+    plane levels."""
+    tr = variant == "TR"
+    zf, xf, yf, vol, dut, dur, coefs = compute_inputs_3d(n3, n2, n1, seed=n3 + n2 + n1 + level2)
+    s12, s3 = 2 ** level2 - 1, 2 ** level3 - 1
+    z, x, y, V, T, R = coarsen_loops(zf, xf, yf, vol, dut, dur if tr else None, s12, s12, s3)
+    got = oracle.tri_tb_lapl_level(zf, xf, yf, vol, dut, dur if tr else None, level3, level2, coefs)
+    ref = oracle.tri_tb_compute_3d(z, x, y, V, T, R, couple=level2 == level3, **coefs)
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+def test_oracle_lapl_hierarchy_vcycle_converges(built_oracle, variant):
+    """The V-cycle over the hierarchy LaplTBCompute builds (four levels, the
+    plane levels of each) reaches the dense solution of the finest level,
+    each cycle faster than a plane sweep of GaussSeidel_3D on that level."""
+    tr = variant == "TR"
+    zf, xf, yf, vol, dut, dur, _ = compute_inputs_3d(8, 8, 8, seed=1)
+    levels = oracle.tri_tb_lapl_compute(zf, xf, yf, vol, dut, dur if tr else None, ref_level=4, **LAPL_COEFS)
+    assert [(p[0][0].shape[:3], len(p)) for p, _, _ in levels] == [((8, 8, 8), 4), ((4, 4, 4), 3), ((2, 2, 2), 2),
+                                                                  ((1, 1, 1), 1)]
+    planes, u3, l3 = levels[0]
+    b = np.random.default_rng(0).standard_normal((8, 8, 8, 2))
+    ref = np.linalg.solve(dense_level(tuple(planes[0]) + (u3, l3), tr), b.reshape(-1)).reshape(b.shape)
+    x, xg = np.zeros_like(b), np.zeros_like(b)
+    for _ in range(6):
+        x = oracle.tri_tb_multigrid_3d(levels, b, x, 1, 1, 1, 1, tr)
+        xg = oracle.tri_tb_gauss_seidel_3d(levels[0], b, xg, 1, 1, 1, tr)
+    err = lambda v: np.max(np.abs(v - ref)) / np.max(np.abs(ref))  # noqa: E731
+    assert err(x) <= 1e-8 and err(x) < 1e-3 * err(xg), (err(x), err(xg))
