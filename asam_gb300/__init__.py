@@ -848,6 +848,12 @@ class TriTBHierarchy:
             out.append(a)
         return tuple(out)
 
+    def set_zebra(self, on: bool = True) -> None:
+        """Zebra order of the smoothers (lines and planes of one parity at
+        once, the GPU's parallel order) for later V-cycles; off: the
+        reference's sequential order."""
+        check(self.lib.asam_tri_tb_hier_set_zebra(self.h, int(bool(on))), "asam_tri_tb_hier_set_zebra")
+
     def vcycle(self, b, x0=None, gauss_iter2: int = 1, mult_iter2: int = 1, gauss_iter3: int = 1,
                mult_iter3: int = 1) -> np.ndarray:
         bb = _f64(b)

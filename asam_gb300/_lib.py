@@ -139,6 +139,7 @@ SIGNATURES = [
     ("asam_tri_tb_hier_create", C.c_int, [C.c_int] * 5 + [C.POINTER(AsamTriTbCoefs), _V, _V, _V, _V, C.POINTER(_V)]),
     ("asam_tri_tb_hier_get", C.c_int, [_V, C.c_int, C.c_int, C.c_int, _V]),
     ("asam_tri_tb_hier_vcycle", C.c_int, [_V, _V, _V] + [C.c_int] * 4),
+    ("asam_tri_tb_hier_set_zebra", C.c_int, [_V, C.c_int]),
     ("asam_tri_tb_hier_destroy", None, [_V]),
     ("asam_tri_tb_solve", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V]),
     ("asam_tri_tb_matvec", C.c_int, [C.c_int, C.c_int, _V, _V, _V, _V, _V]),

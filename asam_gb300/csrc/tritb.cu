@@ -749,6 +749,62 @@ __global__ void k_tb_coarse_cells(int n3, int n2, int n1, TbFields g, int c3, in
   c.dur[e] = __ddiv_rn(rv, __dadd_rn(v, asam::kEps));
 }
 
+// Zebra half-sweep of GaussSeidel_2D (the GPU's parallel order): one thread per
+// line j = j0 + m*jstep (m < jcount) of every plane, its right-hand side with
+// the forward ((b - l x(j-1)) - u x(j+1)) or backward ((b - u x(j+1)) -
+// l x(j-1)) operation order written over x(j), then Solve_1D in place; the
+// lines of one parity read only lines of the other
+__global__ void k_tri_tb_gs_2d_lines(int tr, int nplane, int n2, int n1, const double* __restrict__ d,
+                                     const double* __restrict__ u1, const double* __restrict__ l1,
+                                     const double* __restrict__ u2, const double* __restrict__ l2,
+                                     const double* __restrict__ b, double* __restrict__ x, int j0, int jstep,
+                                     int jcount, int bwd, double* __restrict__ w) {
+  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x, nth = (size_t)nplane * jcount;
+  if (tid >= nth) return;
+  const size_t p = tid / jcount;
+  const int j = j0 + (int)(tid % jcount) * jstep;
+  const size_t line = p * n2 + j;
+  double* xl = x + line * n1 * 2;
+  const double* bl = b + line * n1 * 2;
+  for (int i = 0; i < n1; ++i) {
+    V2 v = ld_v(bl + 2 * i);
+    const double* cl = j > 0 ? l2 + ((p * (n2 - 1) + j - 1) * n1 + i) * 4 : nullptr;
+    const double* cu = j < n2 - 1 ? u2 + ((p * (n2 - 1) + j) * n1 + i) * 4 : nullptr;
+    if (!bwd) {
+      if (cl) v = couple_sub(tr, v, cl, ld_v(xl - (size_t)n1 * 2 + 2 * i));
+      if (cu) v = couple_sub(tr, v, cu, ld_v(xl + (size_t)n1 * 2 + 2 * i));
+    } else {
+      if (cu) v = couple_sub(tr, v, cu, ld_v(xl + (size_t)n1 * 2 + 2 * i));
+      if (cl) v = couple_sub(tr, v, cl, ld_v(xl - (size_t)n1 * 2 + 2 * i));
+    }
+    st_v(xl + 2 * i, v);
+  }
+  solve_col(n1, d + line * n1 * 4, u1 + line * (n1 - 1) * 4, l1 + line * (n1 - 1) * 4, xl, w + tid, nth);
+}
+
+// the right-hand sides of every plane of a level at once (zebra order of
+// GaussSeidel_3D): b(k) minus its couplings to planes k-1 and k+1 in the
+// forward or backward operation order
+__global__ void k_tri_tb_rhs3(int tr, int n3, size_t npl, const double* __restrict__ b,
+                              const double* __restrict__ u3, const double* __restrict__ l3,
+                              const double* __restrict__ x, int bwd, double* __restrict__ t) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)n3 * npl) return;
+  const int k = (int)(e / npl);
+  const size_t r = e % npl;
+  V2 v = ld_v(b + e * 2);
+  const double* cl = k > 0 ? l3 + ((size_t)(k - 1) * npl + r) * 4 : nullptr;
+  const double* cu = k < n3 - 1 ? u3 + ((size_t)k * npl + r) * 4 : nullptr;
+  if (!bwd) {
+    if (cl) v = couple_sub(tr, v, cl, ld_v(x + (e - npl) * 2));
+    if (cu) v = couple_sub(tr, v, cu, ld_v(x + (e + npl) * 2));
+  } else {
+    if (cu) v = couple_sub(tr, v, cu, ld_v(x + (e + npl) * 2));
+    if (cl) v = couple_sub(tr, v, cl, ld_v(x + (e - npl) * 2));
+  }
+  st_v(t + e * 2, v);
+}
+
 struct DevBufs {
   double* p[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   ~DevBufs() {
@@ -779,6 +835,9 @@ struct PlaneLevel {
 // the smoother's per-plane scratch, sized for the finest plane
 struct Scratch {
   double *t, *w;
+  // zebra order: the line solves' factors (nplane x ceil(n2/2) lines of the
+  // finest plane level), every plane's right-hand side and a copy of x
+  double *wz = nullptr, *tall = nullptr, *xtmp = nullptr;
 };
 
 size_t plane_block_len(int nplane, int n2, int n1) {
@@ -830,14 +889,36 @@ cudaError_t stage_plane_level(PlaneLevel& L, int nplane, int n2, int n1, const d
 // coarse levels' b, x and every residual are work space.  Kernels on the
 // legacy stream, the level loop here.
 cudaError_t plane_cycles(int variant, int nplane, int nlev, PlaneLevel* lv, const Scratch& sc, int gauss_iter2,
-                         int mult_iter, long& launches) {
+                         int mult_iter, long& launches, int zebra = 0) {
   auto grid = [&](const PlaneLevel& L) { return (unsigned)(((size_t)nplane * L.n2 * L.n1 + 255) / 256); };
+  // GaussSeidel_2D of one level in zebra order: four half-sweeps per
+  // iteration, then line 1 with the backward right-hand side
+  auto gs_zebra = [&](const PlaneLevel& L, int gi) {
+    auto lines = [&](int j0, int jstep, int jcount, int bwd) {
+      const size_t nth = (size_t)nplane * jcount;
+      k_tri_tb_gs_2d_lines<<<(unsigned)((nth + 127) / 128), 128>>>(variant, nplane, L.n2, L.n1, L.a[0], L.a[1], L.a[2],
+                                                                   L.a[3], L.a[4], L.b, L.x, j0, jstep, jcount, bwd,
+                                                                   sc.wz);
+      ++launches;
+    };
+    if (L.n2 > 1)
+      for (int it = 0; it < gi; ++it)
+        for (int half = 0; half < 4; ++half) {
+          const int par = half == 1 || half == 2;
+          lines(par, 2, (L.n2 - par + 1) / 2, half >= 2);
+        }
+    lines(0, 1, 1, 1);
+  };
 #define TB_LEVEL(L) variant, nplane, (L).n2, (L).n1, (L).a[0], (L).a[1], (L).a[2], (L).a[3], (L).a[4]
   for (int it = 0; it < mult_iter; ++it) {
     int gi = 1, l = 0;
     for (;;) {  // the way down (:449-470)
-      k_tri_tb_gs_2d<<<(nplane + 63) / 64, 64>>>(TB_LEVEL(lv[l]), lv[l].b, lv[l].x, gi, sc.t, sc.w);
-      ++launches;
+      if (zebra) {
+        gs_zebra(lv[l], gi);
+      } else {
+        k_tri_tb_gs_2d<<<(nplane + 63) / 64, 64>>>(TB_LEVEL(lv[l]), lv[l].b, lv[l].x, gi, sc.t, sc.w);
+        ++launches;
+      }
       gi += gauss_iter2;
       if (l + 1 == nlev) {
         gi -= gauss_iter2;
@@ -851,8 +932,12 @@ cudaError_t plane_cycles(int variant, int nplane, int nlev, PlaneLevel* lv, cons
       ++l;
     }
     for (;;) {  // and up (:471-493)
-      k_tri_tb_gs_2d<<<(nplane + 63) / 64, 64>>>(TB_LEVEL(lv[l]), lv[l].b, lv[l].x, gi, sc.t, sc.w);
-      ++launches;
+      if (zebra) {
+        gs_zebra(lv[l], gi);
+      } else {
+        k_tri_tb_gs_2d<<<(nplane + 63) / 64, 64>>>(TB_LEVEL(lv[l]), lv[l].b, lv[l].x, gi, sc.t, sc.w);
+        ++launches;
+      }
       gi -= gauss_iter2;
       if (l == 0) break;
       --l;
@@ -871,7 +956,8 @@ cudaError_t plane_cycles(int variant, int nplane, int nlev, PlaneLevel* lv, cons
 // forward and backward plane sweeps, each plane solved by Solve_2D from the
 // current guess, then plane 1 and plane n3 once more.  t: one plane.
 cudaError_t level_gs(int variant, int n3, const PlaneLevel* pl, int nlev2, const double* u3, const double* l3,
-                     double* t, const Scratch& sc, int gauss_iter, int gauss_iter2, int mult_iter2, long& launches) {
+                     double* t, const Scratch& sc, int gauss_iter, int gauss_iter2, int mult_iter2, long& launches,
+                     int zebra = 0) {
   const size_t npl = (size_t)pl[0].n2 * pl[0].n1;
   const double* b = pl[0].b;
   double* x = pl[0].x;
@@ -885,7 +971,7 @@ cudaError_t level_gs(int variant, int n3, const PlaneLevel* pl, int nlev2, const
     }
     one[0].b = const_cast<double*>(rhs);
     one[0].x = x + (size_t)k * npl * 2;
-    return plane_cycles(variant, 1, nlev2, one, sc, gauss_iter2, mult_iter2, launches);
+    return plane_cycles(variant, 1, nlev2, one, sc, gauss_iter2, mult_iter2, launches, zebra);
   };
   const unsigned g = (unsigned)((npl + 255) / 256);
   auto couple = [&](const double* tin, const double* c, const double* xn) {
@@ -901,7 +987,31 @@ cudaError_t level_gs(int variant, int n3, const PlaneLevel* pl, int nlev2, const
   auto B = [&](int k) { return b + (size_t)k * npl * 2; };
   auto U = [&](int k) { return u3 + (size_t)k * npl * 4; };
   auto Lo = [&](int k) { return l3 + (size_t)k * npl * 4; };
-  if (n3 > 1) {
+  if (n3 > 1 && zebra) {
+    // the planes of one parity at once: every plane's right-hand side, the 2D
+    // V-cycles of all planes on a copy of x, the parity's planes copied back
+    const size_t nv = (size_t)n3 * npl * 2;
+    const unsigned g3 = (unsigned)((n3 * npl + 255) / 256);
+    PlaneLevel all[32];
+    for (int m = 0; m < nlev2; ++m) all[m] = pl[m];
+    all[0].b = sc.tall;
+    all[0].x = sc.xtmp;
+    for (int it = 0; it < gauss_iter; ++it)
+      for (int half = 0; half < 4; ++half) {
+        const int par = half == 1 || half == 2;
+        k_tri_tb_rhs3<<<g3, 256>>>(variant, n3, npl, b, u3, l3, x, half >= 2, sc.tall);
+        ++launches;
+        TB_CHECK(cudaMemcpyAsync(sc.xtmp, x, nv * sizeof(double), cudaMemcpyDeviceToDevice));
+        TB_CHECK(plane_cycles(variant, n3, nlev2, all, sc, gauss_iter2, mult_iter2, launches, 1));
+        TB_CHECK(cudaMemcpy2DAsync(x + par * npl * 2, 2 * npl * 2 * sizeof(double), sc.xtmp + par * npl * 2,
+                                   2 * npl * 2 * sizeof(double), npl * 2 * sizeof(double), (n3 - par + 1) / 2,
+                                   cudaMemcpyDeviceToDevice));
+      }
+    couple(B(0), U(0), X(1));
+    TB_CHECK(solve(0, t));
+    couple(B(n3 - 1), Lo(n3 - 2), X(n3 - 2));
+    TB_CHECK(solve(n3 - 1, t));
+  } else if (n3 > 1) {
     for (int it = 0; it < gauss_iter; ++it) {
       TB_CHECK(cudaMemcpyAsync(t, b, npl * 2 * sizeof(double), cudaMemcpyDeviceToDevice));
       for (int k = 0; k < n3 - 1; ++k) {
@@ -933,13 +1043,15 @@ cudaError_t level_gs(int variant, int n3, const PlaneLevel* pl, int nlev2, const
 // pl[0][0].x
 cudaError_t level_cycles(int variant, int nlev3, const int* n3s, const int* n2s, const int* n1s, const int* nlev2s,
                          PlaneLevel (*pl)[32], double* const* du3, double* const* dl3, double* t, const Scratch& sc,
-                         int gauss_iter2, int mult_iter2, int gauss_iter3, int mult_iter3, long& launches) {
+                         int gauss_iter2, int mult_iter2, int gauss_iter3, int mult_iter3, long& launches,
+                         int zebra = 0) {
   auto grid = [&](int L) { return (unsigned)(((size_t)n3s[L] * n2s[L] * n1s[L] + 255) / 256); };
   cudaError_t e;
   for (int it = 0; it < mult_iter3; ++it) {
     int gi = 1, L = 0;
     for (;;) {  // the way down (:891-914)
-      e = level_gs(variant, n3s[L], pl[L], nlev2s[L], du3[L], dl3[L], t, sc, gi, gauss_iter2, mult_iter2, launches);
+      e = level_gs(variant, n3s[L], pl[L], nlev2s[L], du3[L], dl3[L], t, sc, gi, gauss_iter2, mult_iter2, launches,
+                   zebra);
       if (e != cudaSuccess) return e;
       gi += gauss_iter3;
       if (L + 1 == nlev3) {
@@ -956,7 +1068,8 @@ cudaError_t level_cycles(int variant, int nlev3, const int* n3s, const int* n2s,
       ++L;
     }
     for (;;) {  // and up (:915-937)
-      e = level_gs(variant, n3s[L], pl[L], nlev2s[L], du3[L], dl3[L], t, sc, gi, gauss_iter2, mult_iter2, launches);
+      e = level_gs(variant, n3s[L], pl[L], nlev2s[L], du3[L], dl3[L], t, sc, gi, gauss_iter2, mult_iter2, launches,
+                   zebra);
       if (e != cudaSuccess) return e;
       gi -= gauss_iter3;
       if (L == 0) break;
@@ -974,7 +1087,7 @@ cudaError_t level_cycles(int variant, int nlev3, const int* n3s, const int* n2s,
 // plane hierarchy (all planes; plane level 0 carries the level's b, x and
 // residual) and its couplings between planes, one allocation.
 struct asam_tri_tb_hier {
-  int variant = 0, nlev3 = 0;
+  int variant = 0, nlev3 = 0, zebra = 0;
   int n3s[32] = {}, n2s[32] = {}, n1s[32] = {}, nlev2s[32] = {};
   PlaneLevel pl[32][32];
   double* du3[32] = {};
@@ -1318,7 +1431,8 @@ int asam_tri_tb_hier_create(int variant, int ref_level, int n3, int n2, int n1, 
   const size_t nz = (size_t)n3 * n2 * (n1 + 1), nx = (size_t)n3 * (n2 + 1) * n1, ny = (size_t)(n3 + 1) * npl;
   const size_t nt = (size_t)n1 * 2, nw = (size_t)(n1 > 1 ? n1 - 1 : 1) * 4;
   const size_t fields = 4 * (nz + nx + ny) + 3 * nc;  // the finest fields, and room for one coarsening of them
-  TCU(cudaMalloc((void**)&h->mem, (tot + npl * 2 + nt + nw) * sizeof(double)));
+  const size_t nwz = (size_t)n3 * ((n2 + 1) / 2) * (n1 > 1 ? n1 - 1 : 1) * 4;
+  TCU(cudaMalloc((void**)&h->mem, (tot + npl * 2 + nt + nw + nwz + 2 * nc * 2) * sizeof(double)));
   DevBufs work;
   TCU(cudaMalloc((void**)&work.p[0], 2 * fields * sizeof(double)));
   double* cur = h->mem;
@@ -1332,6 +1446,9 @@ int asam_tri_tb_hier_create(int variant, int ref_level, int n3, int n2, int n1, 
   }
   h->t = cur;
   h->sc = Scratch{cur + npl * 2, cur + npl * 2 + nt};
+  h->sc.wz = cur + npl * 2 + nt + nw;
+  h->sc.tall = h->sc.wz + nwz;
+  h->sc.xtmp = h->sc.tall + nc * 2;
   // the finest fields on the device
   TbFields g;
   double* fp = work.p[0];
@@ -1420,9 +1537,18 @@ int asam_tri_tb_hier_vcycle(asam_tri_tb_hier* h, const double* b, double* x, int
   TCU(cudaMemcpy(h->pl[0][0].x, x, nv0 * sizeof(double), cudaMemcpyDefault));
   long launches = 0;
   TCU(level_cycles(h->variant, h->nlev3, h->n3s, h->n2s, h->n1s, h->nlev2s, h->pl, h->du3, h->dl3, h->t, h->sc,
-                   gauss_iter2, mult_iter2, gauss_iter3, mult_iter3, launches));
+                   gauss_iter2, mult_iter2, gauss_iter3, mult_iter3, launches, h->zebra));
   asam::count_launches(launches);
   TCU(cudaMemcpy(x, h->pl[0][0].x, nv0 * sizeof(double), cudaMemcpyDefault));
+  return ASAM_OK;
+}
+
+int asam_tri_tb_hier_set_zebra(asam_tri_tb_hier* h, int on) {
+  if (!h) {
+    asam::set_last_error("asam_tri_tb_hier_set_zebra: bad argument", __FILE__, __LINE__);
+    return ASAM_BAD_ARG;
+  }
+  h->zebra = on != 0;
   return ASAM_OK;
 }
 

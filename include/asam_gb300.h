@@ -712,6 +712,14 @@ int asam_tri_tb_hier_get(const asam_tri_tb_hier *h, int level3, int level2, int 
  * VCycleCG (JacAccGrav_Mod.f90:4502-4515) runs one from x = 0. */
 int asam_tri_tb_hier_vcycle(asam_tri_tb_hier *h, const double *b, double *x, int gauss_iter2, int mult_iter2,
                             int gauss_iter3, int mult_iter3);
+/* on != 0: the smoothers of later V-cycles in zebra order, the GPU's parallel
+ * order -- per Gauss-Seidel iteration the lines (planes) of parity 0 with
+ * the forward right-hand side, parity 1 forward, parity 1 backward, parity 0
+ * backward, all lines (planes) of one parity at once, then the reference's
+ * closing solves; every relaxation is the reference's arithmetic, only the
+ * order of the lines and planes differs.  0 (the default): the reference's
+ * sequential order. */
+int asam_tri_tb_hier_set_zebra(asam_tri_tb_hier *h, int on);
 void asam_tri_tb_hier_destroy(asam_tri_tb_hier *h);
 
 /* y = A x for the same blocks: MatVecTB_1D (MULTI/TriDiagTB_Mod.f90:121-141),

@@ -75,6 +75,7 @@ def load() -> C.CDLL:
             "ora_tri_tb_prolong_3d": (None, [I, I, I, V, V]),
             "ora_tri_tb_multigrid_3d": (None, [I, I, V, V, V, V] + [V] * 9 + [I, I, I, I]),
             "ora_tri_tb_lapl_level": (None, [I, I, I, I, V, V, V, V, V, I, I] + [V] * 7),
+            "ora_tri_tb_set_zebra": (None, [I]),
             "ora_tri_matvec": (None, [I, I, V, V, V, V, V]),
         }
         sig.update({
@@ -617,6 +618,12 @@ def tri_tb_multigrid_3d(levels, b, x0, gauss_iter2=1, mult_iter2=1, gauss_iter3=
                                 _ptrs([l for _, _, l in lv]), *[_ptrs([k[j] for k in flat]) for j in range(5)], _p(bb),
                                 _p(x), int(gauss_iter2), int(mult_iter2), int(gauss_iter3), int(mult_iter3))
     return x
+
+
+def tri_tb_set_zebra(on):
+    """The zebra order of the TriDiagTB/TR smoothers in the oracle (the GPU's
+    parallel order) for all later calls; off: the reference's order."""
+    load().ora_tri_tb_set_zebra(int(bool(on)))
 
 
 def tri_tb_lapl_level(z_faces, x_faces, y_faces, vol, dut, dur, level3, level2, coefs):

@@ -471,12 +471,71 @@ static void couple_sub(int tr, const double *t, const double *c, const double *x
   o[0] = t[0] - v[0];
   o[1] = t[1] - v[1];
 }
+/* Zebra order of the plane and level smoothers (the GPU's parallel order, not
+ * the reference's): per Gauss-Seidel iteration the lines (planes) of parity
+ * 0 with the forward right-hand side (b - l x(j-1)) - u x(j+1), parity 1
+ * forward, parity 1 backward ((b - u x(j+1)) - l x(j-1)), parity 0
+ * backward; then the reference's closing solves (line 1; planes 1 and n3)
+ * with its right-hand sides.  Every single relaxation is the reference's
+ * arithmetic, only the order of the lines (planes) differs. */
+static int g_tb_zebra = 0;
+void ora_tri_tb_set_zebra(int on) { g_tb_zebra = on != 0; }
+
+static void gs2d_zebra(int tr, int nplane, int n2, int n1, const double *d, const double *u1, const double *l1,
+                       const double *u2, const double *l2, const double *b, double *x, int gauss_iter, double *w) {
+  for (int p = 0; p < nplane; ++p) {
+    const size_t L0 = (size_t)p * n2;
+#define XL(j) (x + (L0 + (j)) * n1 * 2)
+#define BL(j) (b + (L0 + (j)) * n1 * 2)
+#define C2(a, i, j) (a + (((size_t)p * (n2 - 1) + (j)) * n1 + (i)) * 4)
+#define SOLVE(j)                                                                                                \
+  ora_tri_tb_solve(1, n1, d + (L0 + (j)) * n1 * 4, u1 + (L0 + (j)) * (n1 - 1) * 4, l1 + (L0 + (j)) * (n1 - 1) * 4, \
+                   XL(j), w)
+    if (n2 > 1) {
+      for (int it = 0; it < gauss_iter; ++it)
+        for (int half = 0; half < 4; ++half) {
+          const int par = half == 1 || half == 2, bwd = half >= 2;
+          for (int j = par; j < n2; j += 2) {
+            for (int i = 0; i < n1; ++i) {
+              double *o = XL(j) + 2 * i;
+              o[0] = BL(j)[2 * i];
+              o[1] = BL(j)[2 * i + 1];
+              if (!bwd) {
+                if (j > 0) couple_sub(tr, o, C2(l2, i, j - 1), XL(j - 1) + 2 * i, o);
+                if (j < n2 - 1) couple_sub(tr, o, C2(u2, i, j), XL(j + 1) + 2 * i, o);
+              } else {
+                if (j < n2 - 1) couple_sub(tr, o, C2(u2, i, j), XL(j + 1) + 2 * i, o);
+                if (j > 0) couple_sub(tr, o, C2(l2, i, j - 1), XL(j - 1) + 2 * i, o);
+              }
+            }
+            SOLVE(j);
+          }
+        }
+      for (int i = 0; i < n1; ++i) couple_sub(tr, BL(0) + 2 * i, C2(u2, i, 0), XL(1) + 2 * i, XL(0) + 2 * i);
+      SOLVE(0);
+    } else {
+      memcpy(XL(0), BL(0), sizeof(double) * 2 * (size_t)n1);
+      SOLVE(0);
+    }
+#undef XL
+#undef BL
+#undef C2
+#undef SOLVE
+  }
+}
+
 void ora_tri_tb_gauss_seidel_2d(int variant, int nplane, int n2, int n1, const double *d, const double *u1,
                                 const double *l1, const double *u2, const double *l2, const double *b, double *x,
                                 int gauss_iter) {
   const int tr = variant == 1;
   double *t = (double *)malloc(sizeof(double) * 2 * (size_t)n1);
   double *w = (double *)malloc(sizeof(double) * 4 * (size_t)(n1 > 1 ? n1 - 1 : 1));
+  if (g_tb_zebra) {
+    gs2d_zebra(tr, nplane, n2, n1, d, u1, l1, u2, l2, b, x, gauss_iter, w);
+    free(t);
+    free(w);
+    return;
+  }
   for (int p = 0; p < nplane; ++p) {
     const size_t L0 = (size_t)p * n2;
 #define XL(j) (x + (L0 + (j)) * n1 * 2)
@@ -657,7 +716,31 @@ void ora_tri_tb_gauss_seidel_3d(int variant, int n3, int nlev2, const int *n2s, 
   solve_plane(variant, k, nlev2, n2s, n1s, d, u1, l1, u2, l2, rhs, x + (size_t)(k)*npl * 2, gauss_iter2, mult_iter2)
 #define XP(a, r, k) (a + ((size_t)(k)*npl + (r)) * 2)
 #define CP(a, r, k) (a + ((size_t)(k)*npl + (r)) * 4)
-  if (n3 > 1) {
+  if (n3 > 1 && g_tb_zebra) {
+    for (int it = 0; it < gauss_iter; ++it)
+      for (int half = 0; half < 4; ++half) {
+        const int par = half == 1 || half == 2, bwd = half >= 2;
+        for (int k = par; k < n3; k += 2) {
+          for (size_t r = 0; r < npl; ++r) {
+            double *o = t + r * 2;
+            o[0] = XP(b, r, k)[0];
+            o[1] = XP(b, r, k)[1];
+            if (!bwd) {
+              if (k > 0) couple_sub(tr, o, CP(l3, r, k - 1), XP(x, r, k - 1), o);
+              if (k < n3 - 1) couple_sub(tr, o, CP(u3, r, k), XP(x, r, k + 1), o);
+            } else {
+              if (k < n3 - 1) couple_sub(tr, o, CP(u3, r, k), XP(x, r, k + 1), o);
+              if (k > 0) couple_sub(tr, o, CP(l3, r, k - 1), XP(x, r, k - 1), o);
+            }
+          }
+          SOLVE(k, t);
+        }
+      }
+    for (size_t r = 0; r < npl; ++r) couple_sub(tr, XP(b, r, 0), CP(u3, r, 0), XP(x, r, 1), t + r * 2);
+    SOLVE(0, t);
+    for (size_t r = 0; r < npl; ++r) couple_sub(tr, XP(b, r, n3 - 1), CP(l3, r, n3 - 2), XP(x, r, n3 - 2), t + r * 2);
+    SOLVE(n3 - 1, t);
+  } else if (n3 > 1) {
     for (int it = 0; it < gauss_iter; ++it) {
       memcpy(t, b, sizeof(double) * npl * 2);
       for (int k = 0; k < n3 - 1; ++k) {

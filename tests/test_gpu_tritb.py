@@ -256,3 +256,31 @@ def test_tri_tb_hierarchy_bitwise(built_lib, variant, n3, n2, n1, ref_level):
         x0 = np.random.default_rng(2).standard_normal(b.shape)
         assert np.array_equal(h.vcycle(b, x0, 2, 2, 1, 2),
                               oracle.tri_tb_multigrid_3d(levels, b, x0, 2, 2, 1, 2, tr))
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+@pytest.mark.parametrize("n3,n2,n1,ref_level", [(5, 6, 7, 3), (8, 8, 8, 4), (3, 1, 9, 2), (16, 48, 40, 5)])
+def test_tri_tb_hierarchy_zebra_bitwise(built_lib, variant, n3, n2, n1, ref_level):
+    """The zebra order on the GPU (every line of a parity in parallel, the
+    2D V-cycles of every plane of a parity at once) equals the oracle's zebra
+    order bit for bit."""
+    from tests.test_tritb import LAPL_COEFS, compute_inputs_3d
+
+    tr = variant == "TR"
+    zf, xf, yf, vol, dut, dur, _ = compute_inputs_3d(n3, n2, n1, seed=n3 * n2 + n1)
+    dd = dur if tr else None
+    levels = oracle.tri_tb_lapl_compute(zf, xf, yf, vol, dut, dd, ref_level=ref_level, **LAPL_COEFS)
+    b = np.random.default_rng(n1).standard_normal((n3, n2, n1, 2))
+    x0 = np.random.default_rng(2).standard_normal(b.shape)
+    with asam.TriTBHierarchy(zf, xf, yf, vol, dut, dd, ref_level=ref_level, **LAPL_COEFS) as h:
+        h.set_zebra(True)
+        try:
+            oracle.tri_tb_set_zebra(1)
+            ref1 = oracle.tri_tb_multigrid_3d(levels, b, np.zeros_like(b), 1, 1, 1, 1, tr)
+            ref2 = oracle.tri_tb_multigrid_3d(levels, b, x0, 2, 2, 1, 2, tr)
+        finally:
+            oracle.tri_tb_set_zebra(0)
+        assert np.array_equal(h.vcycle(b), ref1)
+        assert np.array_equal(h.vcycle(b, x0, 2, 2, 1, 2), ref2)
+        h.set_zebra(False)
+        assert np.array_equal(h.vcycle(b), oracle.tri_tb_multigrid_3d(levels, b, np.zeros_like(b), 1, 1, 1, 1, tr))

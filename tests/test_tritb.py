@@ -879,3 +879,42 @@ def test_oracle_lapl_hierarchy_vcycle_converges(built_oracle, variant):
         xg = oracle.tri_tb_gauss_seidel_3d(levels[0], b, xg, 1, 1, 1, tr)
     err = lambda v: np.max(np.abs(v - ref)) / np.max(np.abs(ref))  # noqa: E731
     assert err(x) <= 1e-8 and err(x) < 1e-3 * err(xg), (err(x), err(xg))
+
+
+@pytest.mark.parametrize("variant", ["TB", "TR"])
+def test_oracle_zebra_order_converges_like_the_reference(built_oracle, variant):
+    """The zebra order of the smoothers (lines and planes of one parity at
+    once, the GPU's parallel order) solves the same systems: V-cycles over
+    the built hierarchy reach the dense solution (about 17 times per cycle
+    where the reference order gains 45), and a plane of one line is the
+    reference's relaxation bit for bit."""
+    tr = variant == "TR"
+    zf, xf, yf, vol, dut, dur, _ = compute_inputs_3d(8, 8, 8, seed=1)
+    levels = oracle.tri_tb_lapl_compute(zf, xf, yf, vol, dut, dur if tr else None, ref_level=4, **LAPL_COEFS)
+    planes, u3, l3 = levels[0]
+    b = np.random.default_rng(0).standard_normal((8, 8, 8, 2))
+    ref = np.linalg.solve(dense_level(tuple(planes[0]) + (u3, l3), tr), b.reshape(-1)).reshape(b.shape)
+    err = lambda v: np.max(np.abs(v - ref)) / np.max(np.abs(ref))  # noqa: E731
+    out = {}
+    try:
+        for z in (0, 1):
+            oracle.tri_tb_set_zebra(z)
+            x = np.zeros_like(b)
+            errs = []
+            for _ in range(6):
+                x = oracle.tri_tb_multigrid_3d(levels, b, x, 1, 1, 1, 1, tr)
+                errs.append(err(x))
+            out[z] = (errs, x)
+        line = (planes[0][0][:1, :1],) + tuple(a[:1, :1] for a in planes[0][1:3]) + (planes[0][3][:1, :0],
+                                                                                      planes[0][4][:1, :0])
+        oracle.tri_tb_set_zebra(1)
+        y1 = oracle.tri_tb_gauss_seidel_2d(line, b[:1, :1], np.zeros_like(b[:1, :1]), 2, tr)
+        oracle.tri_tb_set_zebra(0)
+        y0 = oracle.tri_tb_gauss_seidel_2d(line, b[:1, :1], np.zeros_like(b[:1, :1]), 2, tr)
+    finally:
+        oracle.tri_tb_set_zebra(0)
+    (e0, _), (e1, xz) = out[0], out[1]
+    assert e1[-1] <= 2e-8 and e1[-1] <= 100 * e0[-1], (e0, e1)  # about 17x per cycle against 45x
+    assert all(b_ < a_ for a_, b_ in zip(e1, e1[1:])), e1
+    assert not np.array_equal(xz, out[0][1])  # the order differs
+    assert np.array_equal(y1, y0)  # one line: no order to change
