@@ -1402,7 +1402,9 @@ int asam_tri_tb_multigrid_3d(int variant, int nlev3, const int* n3s, const int* 
 int asam_tri_tb_hier_create(int variant, int ref_level, int n3, int n2, int n1, const asam_tri_tb_coefs* coefs,
                             const double* const* faces, const double* vol, const double* dut, const double* dur,
                             asam_tri_tb_hier** out) {
-  bool ok = (variant == 0 || variant == 1) && ref_level >= 1 && ref_level <= 32 && n3 >= 1 && n2 >= 1 && n1 >= 1 &&
+  // ref_level <= 24: the shifts 2^L - 1 stay within int, and 2^23 cells per
+  // direction already coarsen to one
+  bool ok = (variant == 0 || variant == 1) && ref_level >= 1 && ref_level <= 24 && n3 >= 1 && n2 >= 1 && n1 >= 1 &&
             coefs && faces && vol && dut && (variant == 0 || dur) && out;
   for (int q = 0; ok && q < 12; ++q) ok = faces[q] != nullptr;
   if (!ok) {

@@ -699,7 +699,7 @@ int asam_tri_tb_multigrid_3d(int variant, int nlev3, const int *n3s, const int *
  * [(k*(n2+1) + j)*n1 + i], faces[8..11] = F3, F3G, DTU3, DUU3
  * [(k*n2 + j)*n1 + i] (k to n3), vol = VolG, dut = DUTG, dur = DURG
  * (variant 1 only) [(k*n2 + j)*n1 + i]; coefs as asam_tri_tb_compute_3d.
- * ref_level <= 32. */
+ * 1 <= ref_level <= 24. */
 typedef struct asam_tri_tb_hier asam_tri_tb_hier;
 int asam_tri_tb_hier_create(int variant, int ref_level, int n3, int n2, int n1, const asam_tri_tb_coefs *coefs,
                             const double *const *faces, const double *vol, const double *dut, const double *dur,

@@ -284,3 +284,20 @@ def test_tri_tb_hierarchy_zebra_bitwise(built_lib, variant, n3, n2, n1, ref_leve
         assert np.array_equal(h.vcycle(b, x0, 2, 2, 1, 2), ref2)
         h.set_zebra(False)
         assert np.array_equal(h.vcycle(b), oracle.tri_tb_multigrid_3d(levels, b, np.zeros_like(b), 1, 1, 1, 1, tr))
+
+
+def test_tri_tb_hierarchy_bad_args(built_lib):
+    from asam_gb300._lib import AsamError
+    from tests.test_tritb import LAPL_COEFS, compute_inputs_3d
+
+    zf, xf, yf, vol, dut, dur, _ = compute_inputs_3d(3, 4, 5, seed=1)
+    for ref_level in (0, 25):
+        with pytest.raises(AsamError):
+            asam.TriTBHierarchy(zf, xf, yf, vol, dut, None, ref_level=ref_level, **LAPL_COEFS)
+    with pytest.raises(ValueError):  # faces of the wrong shape
+        asam.TriTBHierarchy(zf, xf[::-1][:3] + [xf[3][:, :-1]], yf, vol, dut, None, ref_level=2, **LAPL_COEFS)
+    with asam.TriTBHierarchy(zf, xf, yf, vol, dut, None, ref_level=2, **LAPL_COEFS) as h:
+        with pytest.raises(AsamError):
+            h.level(1, 0)  # plane levels start at the level itself
+        with pytest.raises(ValueError):
+            h.vcycle(np.zeros((3, 4, 4, 2)))
