@@ -167,11 +167,9 @@ __global__ void k_tri_tb_gs_2d(int tr, int nplane, int n2, int n1, const double*
 
 // RestrictTB_2D (TriDiagTB_Mod.f90:495-525) per coarse entry: the value the
 // reference's overwriting loops leave there
-__global__ void k_tri_tb_restrict_2d(int nplane, int n2, int n1, const double* __restrict__ res,
-                                     double* __restrict__ resc) {
+__device__ __forceinline__ void restrict_2d_entry(int n2, int n1, const double* __restrict__ res,
+                                                  double* __restrict__ resc, size_t e) {
   const int n1c = (n1 + 1) / 2, n2c = (n2 + 1) / 2;
-  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)nplane * n2c * n1c) return;
   const int ic = (int)(e % n1c);
   const int jc = (int)((e / n1c) % n2c);
   const size_t p = e / ((size_t)n1c * n2c);
@@ -190,6 +188,13 @@ __global__ void k_tri_tb_restrict_2d(int nplane, int n2, int n1, const double* _
     v = ic < n1 / 2 ? add_v(rf(2 * ic, n2 - 1), rf(2 * ic + 1, n2 - 1)) : rf(n1 - 1, n2 - 1);
   }
   st_v(resc + e * 2, v);
+}
+
+__global__ void k_tri_tb_restrict_2d(int nplane, int n2, int n1, const double* __restrict__ res,
+                                     double* __restrict__ resc) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)nplane * ((n2 + 1) / 2) * ((n1 + 1) / 2)) return;
+  restrict_2d_entry(n2, n1, res, resc, e);
 }
 
 // ProlongateTB_2D (TriDiagTB_Mod.f90:527-560): each fine entry its coarse cell's value
@@ -754,15 +759,11 @@ __global__ void k_tb_coarse_cells(int n3, int n2, int n1, TbFields g, int c3, in
 // the forward ((b - l x(j-1)) - u x(j+1)) or backward ((b - u x(j+1)) -
 // l x(j-1)) operation order written over x(j), then Solve_1D in place; the
 // lines of one parity read only lines of the other
-__global__ void k_tri_tb_gs_2d_lines(int tr, int nplane, int n2, int n1, const double* __restrict__ d,
-                                     const double* __restrict__ u1, const double* __restrict__ l1,
-                                     const double* __restrict__ u2, const double* __restrict__ l2,
-                                     const double* __restrict__ b, double* __restrict__ x, int j0, int jstep,
-                                     int jcount, int bwd, double* __restrict__ w) {
-  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x, nth = (size_t)nplane * jcount;
-  if (tid >= nth) return;
-  const size_t p = tid / jcount;
-  const int j = j0 + (int)(tid % jcount) * jstep;
+__device__ __forceinline__ void relax_line(int tr, int n2, int n1, const double* __restrict__ d,
+                                           const double* __restrict__ u1, const double* __restrict__ l1,
+                                           const double* __restrict__ u2, const double* __restrict__ l2,
+                                           const double* __restrict__ b, double* __restrict__ x, size_t p, int j,
+                                           int bwd, double* __restrict__ w, size_t ws) {
   const size_t line = p * n2 + j;
   double* xl = x + line * n1 * 2;
   const double* bl = b + line * n1 * 2;
@@ -779,7 +780,91 @@ __global__ void k_tri_tb_gs_2d_lines(int tr, int nplane, int n2, int n1, const d
     }
     st_v(xl + 2 * i, v);
   }
-  solve_col(n1, d + line * n1 * 4, u1 + line * (n1 - 1) * 4, l1 + line * (n1 - 1) * 4, xl, w + tid, nth);
+  solve_col(n1, d + line * n1 * 4, u1 + line * (n1 - 1) * 4, l1 + line * (n1 - 1) * 4, xl, w, ws);
+}
+
+__global__ void k_tri_tb_gs_2d_lines(int tr, int nplane, int n2, int n1, const double* __restrict__ d,
+                                     const double* __restrict__ u1, const double* __restrict__ l1,
+                                     const double* __restrict__ u2, const double* __restrict__ l2,
+                                     const double* __restrict__ b, double* __restrict__ x, int j0, int jstep,
+                                     int jcount, int bwd, double* __restrict__ w) {
+  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x, nth = (size_t)nplane * jcount;
+  if (tid >= nth) return;
+  relax_line(tr, n2, n1, d, u1, l1, u2, l2, b, x, tid / jcount, j0 + (int)(tid % jcount) * jstep, bwd, w + tid, nth);
+}
+
+// Solve_2D on nplane planes in zebra order as one launch: one CTA per plane
+// runs all mult_iter V-cycles of its plane hierarchy, its threads taking the
+// lines of one parity (or the entries of a residual, restriction or
+// correction) between block barriers; every relaxation, residual and
+// transfer is the multi-launch path's arithmetic, so the bits are the same.
+constexpr int kPlaneHierMax = 12;
+struct PlaneHierDev {
+  int nlev;
+  int n2[kPlaneHierMax], n1[kPlaneHierMax];
+  const double* a[kPlaneHierMax][5];
+  double *b[kPlaneHierMax], *x[kPlaneHierMax], *res[kPlaneHierMax];
+};
+
+__global__ void __launch_bounds__(128) k_tb_plane_vcycles(int tr, int nplane, PlaneHierDev H, int gauss_iter2,
+                                                          int mult_iter, double* __restrict__ w) {
+  const size_t p = blockIdx.x;
+  if (p >= (size_t)nplane) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const size_t ws = (size_t)nplane * H.n2[0];  // one factor slot per line of the finest level
+  auto gs = [&](int l, int gi) {
+    const int n2 = H.n2[l], n1 = H.n1[l];
+    const double *d = H.a[l][0], *u1 = H.a[l][1], *l1 = H.a[l][2], *u2 = H.a[l][3], *l2 = H.a[l][4];
+    if (n2 > 1)
+      for (int it = 0; it < gi; ++it)
+        for (int half = 0; half < 4; ++half) {
+          const int par = half == 1 || half == 2;
+          for (int j = par + 2 * tid; j < n2; j += 2 * nt)
+            relax_line(tr, n2, n1, d, u1, l1, u2, l2, H.b[l], H.x[l], p, j, half >= 2, w + p * H.n2[0] + j, ws);
+          __syncthreads();
+        }
+    if (tid == 0) relax_line(tr, n2, n1, d, u1, l1, u2, l2, H.b[l], H.x[l], p, 0, 1, w + p * H.n2[0], ws);
+    __syncthreads();
+  };
+  for (int it = 0; it < mult_iter; ++it) {
+    int gi = 1, l = 0;
+    for (;;) {  // the way down (MULTI/TriDiagTB_Mod.f90:449-470)
+      gs(l, gi);
+      gi += gauss_iter2;
+      if (l + 1 == H.nlev) {
+        gi -= gauss_iter2;
+        break;
+      }
+      const int n2 = H.n2[l], n1 = H.n1[l];
+      const size_t np = (size_t)n2 * n1, base = p * np;
+      for (size_t e = tid; e < np; e += nt)
+        st_v(H.res[l] + (base + e) * 2,
+             sub_v(ld_v(H.b[l] + (base + e) * 2), level_entry(tr, nplane, n2, n1, H.a[l][0], H.a[l][1], H.a[l][2],
+                                                              H.a[l][3], H.a[l][4], nullptr, nullptr, H.x[l], base + e)));
+      __syncthreads();
+      const size_t npc = (size_t)H.n2[l + 1] * H.n1[l + 1], basec = p * npc;
+      for (size_t e = tid; e < npc; e += nt) {
+        restrict_2d_entry(n2, n1, H.res[l], H.b[l + 1], basec + e);
+        st_v(H.x[l + 1] + (basec + e) * 2, V2{0.0, 0.0});
+      }
+      __syncthreads();
+      ++l;
+    }
+    for (;;) {  // and up (:471-493)
+      gs(l, gi);
+      gi -= gauss_iter2;
+      if (l == 0) break;
+      --l;
+      const int n2 = H.n2[l], n1 = H.n1[l], n1c = (n1 + 1) / 2, n2c = (n2 + 1) / 2;
+      const size_t np = (size_t)n2 * n1;
+      for (size_t e = tid; e < np; e += nt) {
+        const int i = (int)(e % n1), j = (int)(e / n1);
+        const size_t q = (p * np + e) * 2;
+        st_v(H.x[l] + q, add_v(ld_v(H.x[l] + q), ld_v(H.x[l + 1] + ((p * n2c + j / 2) * n1c + i / 2) * 2)));
+      }
+      __syncthreads();
+    }
+  }
 }
 
 // the right-hand sides of every plane of a level at once (zebra order of
@@ -838,6 +923,9 @@ struct Scratch {
   // zebra order: the line solves' factors (nplane x ceil(n2/2) lines of the
   // finest plane level), every plane's right-hand side and a copy of x
   double *wz = nullptr, *tall = nullptr, *xtmp = nullptr;
+  // the one-launch plane V-cycle's factors: a slot per line of the finest
+  // plane level of every plane
+  double* wl = nullptr;
 };
 
 size_t plane_block_len(int nplane, int n2, int n1) {
@@ -890,6 +978,21 @@ cudaError_t stage_plane_level(PlaneLevel& L, int nplane, int n2, int n1, const d
 // legacy stream, the level loop here.
 cudaError_t plane_cycles(int variant, int nplane, int nlev, PlaneLevel* lv, const Scratch& sc, int gauss_iter2,
                          int mult_iter, long& launches, int zebra = 0) {
+  if (zebra && sc.wl && nlev <= kPlaneHierMax) {  // the whole Solve_2D as one launch, a CTA per plane
+    PlaneHierDev H;
+    H.nlev = nlev;
+    for (int l = 0; l < nlev; ++l) {
+      H.n2[l] = lv[l].n2;
+      H.n1[l] = lv[l].n1;
+      for (int q = 0; q < 5; ++q) H.a[l][q] = lv[l].a[q];
+      H.b[l] = lv[l].b;
+      H.x[l] = lv[l].x;
+      H.res[l] = lv[l].res;
+    }
+    k_tb_plane_vcycles<<<nplane, 128>>>(variant, nplane, H, gauss_iter2, mult_iter, sc.wl);
+    ++launches;
+    return cudaGetLastError();
+  }
   auto grid = [&](const PlaneLevel& L) { return (unsigned)(((size_t)nplane * L.n2 * L.n1 + 255) / 256); };
   // GaussSeidel_2D of one level in zebra order: four half-sweeps per
   // iteration, then line 1 with the backward right-hand side
@@ -1434,7 +1537,8 @@ int asam_tri_tb_hier_create(int variant, int ref_level, int n3, int n2, int n1, 
   const size_t nt = (size_t)n1 * 2, nw = (size_t)(n1 > 1 ? n1 - 1 : 1) * 4;
   const size_t fields = 4 * (nz + nx + ny) + 3 * nc;  // the finest fields, and room for one coarsening of them
   const size_t nwz = (size_t)n3 * ((n2 + 1) / 2) * (n1 > 1 ? n1 - 1 : 1) * 4;
-  TCU(cudaMalloc((void**)&h->mem, (tot + npl * 2 + nt + nw + nwz + 2 * nc * 2) * sizeof(double)));
+  const size_t nwl = (size_t)n3 * n2 * (n1 > 1 ? n1 - 1 : 1) * 4;
+  TCU(cudaMalloc((void**)&h->mem, (tot + npl * 2 + nt + nw + nwz + 2 * nc * 2 + nwl) * sizeof(double)));
   DevBufs work;
   TCU(cudaMalloc((void**)&work.p[0], 2 * fields * sizeof(double)));
   double* cur = h->mem;
@@ -1451,6 +1555,7 @@ int asam_tri_tb_hier_create(int variant, int ref_level, int n3, int n2, int n1, 
   h->sc.wz = cur + npl * 2 + nt + nw;
   h->sc.tall = h->sc.wz + nwz;
   h->sc.xtmp = h->sc.tall + nc * 2;
+  h->sc.wl = h->sc.xtmp + nc * 2;
   // the finest fields on the device
   TbFields g;
   double* fp = work.p[0];
