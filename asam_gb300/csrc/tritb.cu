@@ -78,26 +78,48 @@ __device__ __forceinline__ V2 add_v(const V2& a, const V2& b) {
 // level i at w[(i*4 + e)*ws] (ws the stride between the columns' slots)
 __device__ void solve_col(int n1, const double* __restrict__ dc, const double* __restrict__ uc,
                           const double* __restrict__ lc, double* __restrict__ bc, double* __restrict__ w, size_t ws) {
+  // the next row's inputs are loaded before this row's arithmetic, so their
+  // latency overlaps the recurrence (the operations and their order are the
+  // same as a row-by-row evaluation)
   M2 t = ld_m(dc);
   V2 bp = div_2(ld_v(bc), t);
   st_v(bc, bp);
-  for (int i = 1; i < n1; ++i) {
-    const M2 li = ld_m(lc + (size_t)(i - 1) * 4);
-    const M2 wi = div_22(ld_m(uc + (size_t)(i - 1) * 4), t);
-    double* wp = w + (size_t)(i - 1) * 4 * ws;
-    wp[0] = wi.a11;
-    wp[ws] = wi.a21;
-    wp[2 * ws] = wi.a12;
-    wp[3 * ws] = wi.a22;
-    t = sub_m(ld_m(dc + (size_t)i * 4), mult_22(li, wi));
-    bp = div_2(sub_v(ld_v(bc + (size_t)i * 2), mult_2(li, bp)), t);
-    st_v(bc + (size_t)i * 2, bp);
-  }
-  for (int i = n1 - 2; i >= 0; --i) {
-    const double* wp = w + (size_t)i * 4 * ws;
-    const M2 wi{wp[0], wp[ws], wp[2 * ws], wp[3 * ws]};
-    bp = sub_v(ld_v(bc + (size_t)i * 2), mult_2(wi, bp));
-    st_v(bc + (size_t)i * 2, bp);
+  if (n1 > 1) {
+    M2 ln = ld_m(lc), un = ld_m(uc), dn = ld_m(dc + 4);
+    V2 bn = ld_v(bc + 2);
+    for (int i = 1; i < n1; ++i) {
+      const M2 li = ln, ui = un, di = dn;
+      const V2 bi = bn;
+      if (i + 1 < n1) {
+        ln = ld_m(lc + (size_t)i * 4);
+        un = ld_m(uc + (size_t)i * 4);
+        dn = ld_m(dc + (size_t)(i + 1) * 4);
+        bn = ld_v(bc + (size_t)(i + 1) * 2);
+      }
+      const M2 wi = div_22(ui, t);
+      double* wp = w + (size_t)(i - 1) * 4 * ws;
+      wp[0] = wi.a11;
+      wp[ws] = wi.a21;
+      wp[2 * ws] = wi.a12;
+      wp[3 * ws] = wi.a22;
+      t = sub_m(di, mult_22(li, wi));
+      bp = div_2(sub_v(bi, mult_2(li, bp)), t);
+      st_v(bc + (size_t)i * 2, bp);
+    }
+    const double* wp0 = w + (size_t)(n1 - 2) * 4 * ws;
+    M2 wn{wp0[0], wp0[ws], wp0[2 * ws], wp0[3 * ws]};
+    V2 cn = ld_v(bc + (size_t)(n1 - 2) * 2);
+    for (int i = n1 - 2; i >= 0; --i) {
+      const M2 wi = wn;
+      const V2 ci = cn;
+      if (i > 0) {
+        const double* wp = w + (size_t)(i - 1) * 4 * ws;
+        wn = M2{wp[0], wp[ws], wp[2 * ws], wp[3 * ws]};
+        cn = ld_v(bc + (size_t)(i - 1) * 2);
+      }
+      bp = sub_v(ci, mult_2(wi, bp));
+      st_v(bc + (size_t)i * 2, bp);
+    }
   }
 }
 
