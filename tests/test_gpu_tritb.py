@@ -4,9 +4,11 @@ the columns' assembly Compute_1D of both variants (TriDiagTB_Mod.f90:32-93,
 TriDiagTR_Mod.f90:32-105) with the oracle: bit-exact on every shape,
 including one- and two-level columns and a batch of 32768 columns of 128
 levels (the columns of a 256x128 plane stack of the 512x512x128 grid); the
-planes' and levels' assembly, product, smoother, transfers and V-cycle
-(Compute_2D/3D, MatVecTB_2D/3D, GaussSeidel_2D, RestrictTB_2D,
-ProlongateTB_2D, Multigrid_2D) bit for bit as well."""
+planes' and levels' assembly, product, smoothers, transfers and V-cycles
+(Compute_2D/3D, MatVecTB_2D/3D, GaussSeidel_2D/3D, RestrictTB_2D/3D,
+ProlongateTB_2D/3D, Multigrid_2D/3D), the resident hierarchy of
+LaplTBCompute / LaplTRCompute (MULTI/JacAccGrav_Mod.f90:1312-1667) and its
+V-cycle in the reference's order and in zebra order bit for bit as well."""
 import numpy as np
 import pytest
 
